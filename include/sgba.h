@@ -1,0 +1,186 @@
+/*
+ * sgba.h -- C ABI of the GB300 Schur-complement Levenberg-Marquardt bundle
+ * adjustment path (libsgba.so).
+ *
+ * This is the drop-in boundary for sophus-rs's
+ *   optimize_nlls(variables, cost_fns, eq_fns, params)
+ *     (crates/sophus_opt/src/nlls.rs:73-83)
+ * and the stateful
+ *   Optimizer::new / Optimizer::step / Optimizer::build_solution
+ *     (crates/sophus_opt/src/nlls/optimizer.rs:71-120, 345-376, 609-646)
+ * when the problem is the bundle-adjustment specialisation:
+ *   - one CostFn of PinholeCameraReprojectionCostTerm
+ *     (crates/sophus_opt/src/nlls/functor_library/costs/pinhole_reprojection.rs:28-95),
+ *     optionally with RobustKernel::Huber (crates/sophus_opt/src/robust_kernel.rs);
+ *   - families: intrinsics Conditioned, poses (Isometry3F64) Free with
+ *     constant ids, points (VecF64<3>) Marginalized with constant ids;
+ *   - params.solver = SchurBlockSparseLdlt (crates/sophus_solver/src/lib.rs:313).
+ *
+ * All pointers are plain host pointers; the library copies what it needs to
+ * device memory.  Every function returns an sgba_status (0 = OK, negative =
+ * error class mirroring NllsError, crates/sophus_opt/src/nlls/optimizer_types.rs:422-504);
+ * sgba_last_error() returns the message of the calling thread's last error.
+ * A problem handle is not thread-safe; it owns one CUDA stream.
+ */
+#ifndef SGBA_H
+#define SGBA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGBA_ABI_VERSION 1
+
+typedef enum {
+  SGBA_OK = 0,
+  SGBA_ERR_INVALID_ARGUMENT = -1,     /* bad pointer, size, index or non-finite input */
+  SGBA_ERR_INVALID_PARAMS = -2,       /* pose quaternion fails | |q| - 1 | <= 1e-6 (from_params) */
+  SGBA_ERR_SCHUR_MISSING_FREE_OR_MARG = -3, /* NllsError::SchurMissingFreeOrMarg */
+  SGBA_ERR_UNSUPPORTED = -4,          /* configuration outside this path */
+  SGBA_ERR_CUDA = -5,                 /* CUDA runtime failure (message has the CUDA error) */
+  SGBA_ERR_OUT_OF_MEMORY = -6,
+  SGBA_ERR_STATE = -7,                /* call out of order (e.g. step before init) */
+  SGBA_ERR_DEVICE_TIMEOUT = -8,       /* a bounded device wait gave up */
+} sgba_status;
+
+/* Problem description (host SoA; the caller keeps ownership, the library copies).
+ * Mirrors the VarBuilder families "cams" (Conditioned intrinsics), "poses"
+ * (Free Isometry3F64 with const ids) and "points" (Marginalized VecF64<3>
+ * with const ids) plus the CostTerms of PinholeCameraReprojectionCostTerm. */
+typedef struct {
+  int32_t n_cam;              /* number of poses */
+  const double *poses;        /* n_cam*7: world_from_camera params (qw qx qy qz tx ty tz) */
+  const uint8_t *pose_const;  /* n_cam flags (1 = constant id), or NULL */
+  int32_t n_pt;
+  const double *points;       /* n_pt*3 world points */
+  const uint8_t *point_const; /* n_pt flags, or NULL */
+  double intrinsics[4];       /* fx fy cx cy (PinholeCameraF64 params, Conditioned) */
+  int64_t n_obs;
+  const int32_t *obs_cam;     /* pose index per observation (entity_indices[1]) */
+  const int32_t *obs_pt;      /* point index per observation (entity_indices[2]) */
+  const double *obs_uv;       /* n_obs*2 pixel measurements (uv_in_image) */
+  double huber_delta;         /* > 0: RobustKernel::Huber(delta); <= 0: no kernel */
+} sgba_problem_desc;
+
+/* OptParams fields used on this path (crates/sophus_opt/src/nlls/optimizer_types.rs:161-240).
+ * Tolerances <= 0 disable the test, as 0.0 does in the reference. */
+typedef struct {
+  int32_t num_iterations;
+  double initial_lm_damping;
+  double function_tolerance;
+  double gradient_tolerance;
+  double parameter_tolerance;
+  int64_t max_consecutive_rejects;
+  int32_t skip_final_hessian;
+} sgba_opt_params;
+
+/* TerminationReason (crates/sophus_opt/src/nlls/optimizer_types.rs:93-122). */
+typedef enum {
+  SGBA_TERM_NONE = 0,
+  SGBA_TERM_FUNCTION_TOLERANCE = 1,
+  SGBA_TERM_GRADIENT_TOLERANCE = 2,
+  SGBA_TERM_PARAMETER_TOLERANCE = 3,
+  SGBA_TERM_MAX_ITERATIONS = 4,
+  SGBA_TERM_MAX_CONSECUTIVE_REJECTS = 5,
+} sgba_termination;
+
+/* One record per Optimizer::step, mirroring StepInfo
+ * (crates/sophus_opt/src/nlls/optimizer_types.rs:67-83) plus step diagnostics. */
+typedef struct {
+  double merit;        /* merit after the step */
+  double new_merit;    /* cost at the trial point (NaN when no trial point was formed) */
+  double lm_damping;   /* LM damping after the step */
+  double gain_ratio;   /* NaN when not computed */
+  double max_step;     /* max |delta| (NaN when no step) */
+  double max_grad;     /* max |neg_gradient| at the linearisation point */
+  int32_t accepted;
+  int32_t termination; /* sgba_termination */
+} sgba_iter_record;
+
+typedef struct sgba_problem sgba_problem;
+
+/* Version of this ABI (SGBA_ABI_VERSION). */
+int32_t sgba_abi_version(void);
+
+/* Copies the last error message of this thread into buf (NUL-terminated). */
+size_t sgba_last_error(char *buf, size_t cap);
+
+/* Validates and uploads a problem: sorts the cost terms as CostFn::sort does
+ * (crates/sophus_opt/src/nlls/cost/cost_fn.rs:354-393), assigns free/marg
+ * block indices (crates/sophus_opt/src/variables/var_families.rs:60-113) and
+ * builds the Hessian and reduced-camera-system sparsity
+ * (crates/sophus_opt/src/nlls/cost/cost_fn.rs:435-518,
+ *  crates/sophus_opt/src/nlls/damped_hessian.rs:261-325).  device < 0 keeps
+ * the current CUDA device. */
+int sgba_problem_create(const sgba_problem_desc *desc, int32_t device, sgba_problem **out);
+int sgba_problem_destroy(sgba_problem *p);
+
+/* Optimizer::new: validates the solver configuration
+ * (crates/sophus_opt/src/nlls/optimizer.rs:649-717), evaluates the initial
+ * merit and resets damping / reject counters. */
+int sgba_optimizer_init(sgba_problem *p, const sgba_opt_params *params);
+
+/* Optimizer::step: one LM iteration; fills *record. */
+int sgba_optimizer_step(sgba_problem *p, sgba_iter_record *record);
+
+/* optimize_nlls: init, step until a termination reason, then build_solution.
+ * Up to cap records are written; *n_records receives the number of steps. */
+int sgba_optimize(sgba_problem *p, const sgba_opt_params *params, sgba_iter_record *records,
+                  int32_t cap, int32_t *n_records, int32_t *termination);
+
+/* Current variables (OptimizationSolution.variables). NULL skips a family. */
+int sgba_get_variables(sgba_problem *p, double *poses, double *points);
+/* Current merit (OptimizationSolution.final_cost after sgba_optimize). */
+int sgba_get_cost(sgba_problem *p, double *cost);
+/* Overwrite the variables of an existing problem (same structure). */
+int sgba_set_variables(sgba_problem *p, const double *poses, const double *points);
+
+/* Sizes of the problem as laid out on the device. */
+typedef struct {
+  int32_t n_free_poses;     /* free pose blocks (6 dof) */
+  int32_t n_marg_points;    /* marginalized point blocks (3 dof) */
+  int64_t n_terms;          /* reduced cost terms (distinct (point, pose) pairs) */
+  int64_t n_h_blocks;       /* lower blocks of H: pose diag + point diag + point x pose */
+  int64_t n_s_blocks;       /* lower 6x6 blocks of the reduced camera system S */
+  int64_t n_schur_pairs;    /* observation pairs summed into S (sum over points of L(L+1)/2) */
+} sgba_layout;
+int sgba_get_layout(sgba_problem *p, sgba_layout *out);
+
+/* Block sparsity of H (lower: row block, col block in the global block order
+ * free poses then marginalized points) and of S (free pose blocks).  Arrays
+ * of length n_h_blocks / n_s_blocks (see sgba_get_layout); NULL skips one. */
+int sgba_export_pattern(sgba_problem *p, int32_t *h_rows, int32_t *h_cols, int32_t *s_rows,
+                        int32_t *s_cols);
+
+/* Linear system of the most recent step: S (dense 6nf x 6nf, row-major,
+ * lower triangle valid), reduced rhs (6nf) and the step delta (6nf + 3nm).
+ * NULL skips an output.  Used to compare each LM step with an FP64 LDLT. */
+int sgba_debug_last_system(sgba_problem *p, double *s_dense, double *rhs, double *delta);
+
+/* Opaque optimizer state (variables, damping, reject count, step count) for
+ * resume: *size receives the byte size when buf is NULL. */
+int sgba_state_save(sgba_problem *p, void *buf, size_t *size);
+int sgba_state_load(sgba_problem *p, const void *buf, size_t size);
+
+/* Per-kernel launch count and device time of the last sgba_optimize call
+ * (instrumentation for benchmarks; times are CUDA-event based). */
+typedef struct {
+  int64_t kernel_launches;   /* launches of this library's kernels */
+  double ms_total;           /* device time of the whole optimize call */
+  double ms_linearize;       /* landmark + camera passes (per call, summed) */
+  double ms_schur;           /* reduced camera system assembly */
+  double ms_factor;          /* factorization + solves + refinement */
+  double ms_update;          /* back-substitution, gauge projection, update */
+  double ms_cost;            /* trial cost + decision */
+} sgba_profile;
+int sgba_get_profile(sgba_problem *p, sgba_profile *out);
+/* Enable per-phase event timing (adds events between phases; off by default). */
+int sgba_set_profiling(sgba_problem *p, int32_t enabled);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SGBA_H */

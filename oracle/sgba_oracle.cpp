@@ -1,0 +1,1079 @@
+// sgba_oracle.cpp -- CPU FP64 restatement of sophus-rs's Schur-complement
+// LM bundle-adjustment inner loop.
+//
+// TEST INFRASTRUCTURE ONLY: the checker and the timed CPU baseline.  The
+// product never links or calls this file.  See sgba_oracle.h.
+//
+// Reference files restated (paths relative to the sophus-rs workspace):
+//   crates/sophus_opt/src/nlls/optimizer_step.rs:366-437      step_nlls_inner
+//   crates/sophus_opt/src/nlls/optimizer.rs:345-376,463-520   step/accept/reject/tolerances
+//   crates/sophus_opt/src/nlls/optimizer_helpers.rs:159-185,309-321
+//   crates/sophus_opt/src/nlls/linear_system/cost_system.rs:74-273
+//   crates/sophus_opt/src/nlls/cost/cost_fn.rs:173-433         eval/sort/calc_total_cost
+//   crates/sophus_opt/src/nlls/cost/compare_idx.rs:38-125
+//   crates/sophus_opt/src/nlls/cost/evaluated_term.rs:52-57,286-327
+//   crates/sophus_opt/src/robust_kernel.rs:13-35
+//   crates/sophus_opt/src/nlls/functor_library/costs/pinhole_reprojection.rs:42-95
+//   crates/sophus_lie/src/groups/rotation3.rs:176-182,363-387,449-492,575-577,761-778
+//   crates/sophus_lie/src/groups/affine_group_template.rs:354-410,505-510
+//   crates/sophus_lie/src/quaternion.rs:212-225
+//   crates/sophus_lie/src/lie_group/lie_group_manifold.rs:33-35,57-64
+//   crates/sophus_sensor/src/projections/perspective.rs:30-72
+//   crates/sophus_sensor/src/distortions/affine.rs:50-108
+//   crates/sophus_solver/src/ldlt/schur_ldlt.rs:82-278,536-812
+//   crates/sophus_solver/src/ldlt/block_sparse_ldlt.rs:99-190,479-747
+//   crates/sophus_solver/src/ldlt/dense_ldlt.rs:164-308
+//   crates/sophus_solver/src/ldlt/block_diag_ldlt.rs:80-160
+//   crates/sophus_solver/src/kernel.rs:84-106
+//
+// Deviations (documented; they change only rounding, never the algorithm):
+//   * S is factored in natural block order; the reference orders blocks with
+//     faer's AMD (third-party, not available here).  For the dense reduced
+//     camera systems of the BA configurations the fill is identical.
+//   * The 3x3 H_mm inverse is the cofactor/adjugate formula with the same
+//     "determinant exactly zero => failure" rule as nalgebra's try_inverse.
+//   * Bunch-Kaufman fallback for indefinite ill-conditioned pivot blocks is
+//     not restated; such a block is reported as a solve failure (a reject).
+#include "sgba_oracle.h"
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <thread>
+#include <vector>
+
+namespace {
+
+constexpr double kEps = 1e-6;            // sophus_autodiff EPS_F64 (linalg.rs:75)
+constexpr double kLdltTolRel = 1e-12;    // BlockSparseLdlt::default tol_rel
+constexpr double kMinPositive = DBL_MIN; // f64::MIN_POSITIVE
+
+// ---------------------------------------------------------------------------
+// Scalar abstraction: double, float, and a forward-mode dual number.
+// ---------------------------------------------------------------------------
+template <int N>
+struct Dual {
+  double v;
+  double d[N];
+  Dual() : v(0) { for (int i = 0; i < N; ++i) d[i] = 0; }
+  Dual(double x) : v(x) { for (int i = 0; i < N; ++i) d[i] = 0; }  // NOLINT
+};
+template <int N> Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v + b.v); for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i]; return r; }
+template <int N> Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v - b.v); for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i]; return r; }
+template <int N> Dual<N> operator-(const Dual<N>& a) {
+  Dual<N> r(-a.v); for (int i = 0; i < N; ++i) r.d[i] = -a.d[i]; return r; }
+template <int N> Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v * b.v); for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i]; return r; }
+template <int N> Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v / b.v);
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] * b.v - a.v * b.d[i]) / (b.v * b.v);
+  return r; }
+template <int N> Dual<N> dsqrt(const Dual<N>& a) {
+  double s = std::sqrt(a.v);
+  Dual<N> r(s);
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] / (2.0 * s);
+  return r;
+}
+template <int N> Dual<N> dsin(const Dual<N>& a) {
+  Dual<N> r(std::sin(a.v));
+  double c = std::cos(a.v);
+  for (int i = 0; i < N; ++i) r.d[i] = c * a.d[i];
+  return r;
+}
+template <int N> Dual<N> dcos(const Dual<N>& a) {
+  Dual<N> r(std::cos(a.v));
+  double s = -std::sin(a.v);
+  for (int i = 0; i < N; ++i) r.d[i] = s * a.d[i];
+  return r;
+}
+template <int N> double val(const Dual<N>& a) { return a.v; }
+
+inline double dsqrt(double a) { return std::sqrt(a); }
+inline double dsin(double a) { return std::sin(a); }
+inline double dcos(double a) { return std::cos(a); }
+inline double val(double a) { return a; }
+inline float dsqrt(float a) { return std::sqrt(a); }
+inline float val(float a) { return a; }
+
+// ---------------------------------------------------------------------------
+// SO(3) / SE(3) restated from sophus_lie.
+// Params layout: [qw, qx, qy, qz, tx, ty, tz]; tangent layout [omega; nu].
+// ---------------------------------------------------------------------------
+
+// QuaternionImpl::mult (quaternion.rs:212-225)
+template <class S>
+void quat_mult(const S* a, const S* b, S* o) {
+  S re = a[0] * b[0] - (a[1] * b[1] + a[2] * b[2] + a[3] * b[3]);
+  // ivec = rhs_ivec*lhs_re + lhs_ivec*rhs_re + cross(lhs_ivec, rhs_ivec)
+  S c0 = a[2] * b[3] - a[3] * b[2];
+  S c1 = a[3] * b[1] - a[1] * b[3];
+  S c2 = a[1] * b[2] - a[2] * b[1];
+  S i0 = b[1] * a[0] + a[1] * b[0] + c0;
+  S i1 = b[2] * a[0] + a[2] * b[0] + c1;
+  S i2 = b[3] * a[0] + a[3] * b[0] + c2;
+  o[0] = re; o[1] = i0; o[2] = i1; o[3] = i2;
+}
+
+// Rotation3Impl::matrix (rotation3.rs:449-492), row-major 3x3.
+template <class S>
+void rot_matrix(const S* q, S* m) {
+  const S r = q[0], x = q[1], y = q[2], z = q[3];
+  const S one(1.0), two(2.0);
+  S two_x = two * x, two_y = two * y, two_z = two * z, two_r = two * r;
+  S two_xx = two_x * x, two_yy = two_y * y, two_zz = two_z * z;
+  S two_xy = two_x * y, two_xz = two_x * z, two_yz = two_y * z;
+  S two_rx = two_r * x, two_ry = two_r * y, two_rz = two_r * z;
+  m[0] = one - (two_yy + two_zz); m[1] = two_xy - two_rz; m[2] = two_xz + two_ry;
+  m[3] = two_xy + two_rz; m[4] = one - (two_xx + two_zz); m[5] = two_yz - two_rx;
+  m[6] = two_xz - two_ry; m[7] = two_yz + two_rx; m[8] = one - (two_xx + two_yy);
+}
+
+// Rotation3Impl::exp (rotation3.rs:363-387)
+template <class S>
+void so3_exp(const S* w, S* q) {
+  S theta_sq = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  S theta_po4 = theta_sq * theta_sq;
+  S imag, real;
+  if (val(theta_sq) <= kEps * kEps) {
+    imag = S(0.5) - S(1.0 / 48.0) * theta_sq + S(1.0 / 3840.0) * theta_po4;
+    real = S(1.0) - S(1.0 / 8.0) * theta_sq + S(1.0 / 384.0) * theta_po4;
+  } else {
+    S theta = dsqrt(theta_sq);
+    S half = S(0.5) * theta;
+    imag = dsin(half) / theta;
+    real = dcos(half);
+  }
+  q[0] = real; q[1] = imag * w[0]; q[2] = imag * w[1]; q[3] = imag * w[2];
+}
+
+// Rotation3Impl::mat_v (rotation3.rs:761-778).  Note the Taylor branch test is
+// theta_sq <= EPS (not EPS^2), exactly as in the reference.
+template <class S>
+void so3_mat_v(const S* w, S* v) {
+  S theta_sq = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  // hat(omega)
+  S h[9] = {S(0.0), -w[2], w[1], w[2], S(0.0), -w[0], -w[1], w[0], S(0.0)};
+  S h2[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      S acc = h[i * 3 + 0] * h[0 * 3 + j];
+      acc = acc + h[i * 3 + 1] * h[1 * 3 + j];
+      acc = acc + h[i * 3 + 2] * h[2 * 3 + j];
+      h2[i * 3 + j] = acc;
+    }
+  if (val(theta_sq) <= kEps) {
+    for (int i = 0; i < 9; ++i) v[i] = S(0.5) * h[i];
+  } else {
+    S theta = dsqrt(theta_sq);
+    S a = (S(1.0) - dcos(theta)) / theta_sq;
+    S b = (theta - dsin(theta)) / (theta_sq * theta);
+    for (int i = 0; i < 9; ++i) v[i] = a * h[i] + b * h2[i];
+  }
+  v[0] = v[0] + S(1.0); v[4] = v[4] + S(1.0); v[8] = v[8] + S(1.0);
+}
+
+// HasDisambiguate for Rotation3 (rotation3.rs:176-182): keep w >= 0.
+template <class S>
+void disambiguate(S* q) {
+  if (!(0.0 <= val(q[0]))) { for (int i = 0; i < 4; ++i) q[i] = -q[i]; }
+}
+
+// Rotation3 are_params_valid (rotation3.rs:314-319): | |q| - 1 | <= EPS.
+template <class S>
+bool quat_valid(const S* q) {
+  double n = std::sqrt(val(q[0]) * val(q[0]) + val(q[1]) * val(q[1]) +
+                       val(q[2]) * val(q[2]) + val(q[3]) * val(q[3]));
+  return std::fabs(n - 1.0) <= kEps;
+}
+
+// AffineGroupTemplateImpl::exp (affine_group_template.rs:354-360)
+template <class S>
+void se3_exp(const S* xi, S* out) {
+  so3_exp(xi, out);
+  S v[9];
+  so3_mat_v(xi, v);
+  for (int i = 0; i < 3; ++i)
+    out[4 + i] = v[i * 3 + 0] * xi[3] + v[i * 3 + 1] * xi[4] + v[i * 3 + 2] * xi[5];
+  disambiguate(out);
+}
+
+// AffineGroupTemplateImpl::group_mul (affine_group_template.rs:387-396)
+template <class S>
+void se3_mul(const S* a, const S* b, S* out) {
+  S q[4];
+  quat_mult(a, b, q);
+  S r[9];
+  rot_matrix(a, r);
+  for (int i = 0; i < 3; ++i)
+    out[4 + i] = (r[i * 3 + 0] * b[4] + r[i * 3 + 1] * b[5] + r[i * 3 + 2] * b[6]) + a[4 + i];
+  for (int i = 0; i < 4; ++i) out[i] = q[i];
+  disambiguate(out);
+}
+
+// AffineGroupTemplateImpl::inverse (affine_group_template.rs:398-404)
+template <class S>
+void se3_inverse(const S* a, S* out) {
+  S q[4] = {a[0], -a[1], -a[2], -a[3]};
+  S r[9];
+  rot_matrix(q, r);
+  for (int i = 0; i < 3; ++i)
+    out[4 + i] = -(r[i * 3 + 0] * a[4] + r[i * 3 + 1] * a[5] + r[i * 3 + 2] * a[6]);
+  for (int i = 0; i < 4; ++i) out[i] = q[i];
+  disambiguate(out);
+}
+
+// Residual g = z - pi(T_wc^-1 * p_w)
+// (pinhole_reprojection.rs:42-50; camera.rs:94-99; perspective.rs:30-39;
+//  affine.rs:50-62)
+template <class S>
+void residual_generic(const S* pose, const S* p, const double* intr,
+                      const double* uv, S* r, S* x_cam_out = nullptr) {
+  S cw[7];
+  se3_inverse(pose, cw);
+  S rm[9];
+  rot_matrix(cw, rm);
+  S xc[3];
+  for (int i = 0; i < 3; ++i)
+    xc[i] = (rm[i * 3 + 0] * p[0] + rm[i * 3 + 1] * p[1] + rm[i * 3 + 2] * p[2]) + cw[4 + i];
+  S u = xc[0] / xc[2];
+  S v = xc[1] / xc[2];
+  S pu = u * S(intr[0]) + S(intr[2]);
+  S pv = v * S(intr[1]) + S(intr[3]);
+  r[0] = S(uv[0]) - pu;
+  r[1] = S(uv[1]) - pv;
+  if (x_cam_out) for (int i = 0; i < 3; ++i) x_cam_out[i] = xc[i];
+}
+
+// HuberKernel::apply / IsRobustKernel::weight (robust_kernel.rs:13-18,29-35)
+inline double huber_apply(double delta, double x) {
+  if (std::fabs(x) <= delta) return x * x;
+  return 2.0 * delta * std::fabs(x) - delta * delta;
+}
+inline double huber_weight(double delta, double nrm) {
+  if (nrm == 0.0) return 0.0;
+  return std::sqrt(huber_apply(delta, nrm)) / nrm;
+}
+
+// One evaluated term (evaluated_term.rs:286-327 for (C, F, M) kinds):
+// residual weighted by w; H blocks unweighted; cost = r~ . r~.
+template <class R>
+struct Term {
+  R hpp[36];   // J_pose^T J_pose (6x6)
+  R hmm[9];    // J_pt^T J_pt (3x3)
+  R hmp[18];   // J_pt^T J_pose (3x6)  -- the stored lower block (point row, pose col)
+  R gp[6];     // J_pose^T r~
+  R gm[3];     // J_pt^T r~
+  double cost;
+};
+
+// PinholeCameraReprojectionCostTerm::eval (pinhole_reprojection.rs:60-95)
+// in f64: residual, d_pi*R_cw, J_pose = d_pi_r_cw * [hat(-p), I], J_pt = -d_pi_r_cw.
+void eval_term_f64(const double* pose, const double* p, const double* intr,
+                   const double* uv, double huber, double* r, double* jp,
+                   double* jm, double* w_out, double* cost_out) {
+  double cw[7];
+  se3_inverse(pose, cw);
+  double rm[9];
+  rot_matrix(cw, rm);
+  double xc[3];
+  for (int i = 0; i < 3; ++i)
+    xc[i] = (rm[i * 3 + 0] * p[0] + rm[i * 3 + 1] * p[1] + rm[i * 3 + 2] * p[2]) + cw[4 + i];
+  double u = xc[0] / xc[2], v = xc[1] / xc[2];
+  r[0] = uv[0] - (u * intr[0] + intr[2]);
+  r[1] = uv[1] - (v * intr[1] + intr[3]);
+  // dx_distort_x * dx_proj_x (2x3)
+  double z = xc[2];
+  double dpi[6] = {intr[0] * (1.0 / z), 0.0, intr[0] * (-xc[0] / (z * z)),
+                   0.0, intr[1] * (1.0 / z), intr[1] * (-xc[1] / (z * z))};
+  double d[6];  // d_pi * R_cw (2x3)
+  for (int i = 0; i < 2; ++i)
+    for (int j = 0; j < 3; ++j)
+      d[i * 3 + j] = dpi[i * 3 + 0] * rm[0 * 3 + j] + dpi[i * 3 + 1] * rm[1 * 3 + j] +
+                     dpi[i * 3 + 2] * rm[2 * 3 + j];
+  // hat(-p) = [[0, p2, -p1], [-p2, 0, p0], [p1, -p0, 0]]
+  const double hm[9] = {0.0, p[2], -p[1], -p[2], 0.0, p[0], p[1], -p[0], 0.0};
+  for (int i = 0; i < 2; ++i) {
+    for (int j = 0; j < 3; ++j)
+      jp[i * 6 + j] = d[i * 3 + 0] * hm[0 * 3 + j] + d[i * 3 + 1] * hm[1 * 3 + j] +
+                      d[i * 3 + 2] * hm[2 * 3 + j];
+    for (int j = 0; j < 3; ++j) jp[i * 6 + 3 + j] = d[i * 3 + j];
+    for (int j = 0; j < 3; ++j) jm[i * 3 + j] = -d[i * 3 + j];
+  }
+  double w = 1.0;
+  double cost;
+  if (huber > 0.0) {
+    double nrm = std::sqrt(r[0] * r[0] + r[1] * r[1]);
+    w = huber_weight(huber, nrm);
+    double rw0 = w * r[0], rw1 = w * r[1];
+    cost = rw0 * rw0 + rw1 * rw1;
+  } else {
+    cost = r[0] * r[0] + r[1] * r[1];
+  }
+  if (w_out) *w_out = w;
+  if (cost_out) *cost_out = cost;
+}
+
+// Cost only (calc_total_cost treats every variable as Conditioned).
+double eval_cost_f64(const double* pose, const double* p, const double* intr,
+                     const double* uv, double huber) {
+  double r[2];
+  residual_generic<double>(pose, p, intr, uv, r);
+  if (huber > 0.0) {
+    double nrm = std::sqrt(r[0] * r[0] + r[1] * r[1]);
+    double w = huber_weight(huber, nrm);
+    double rw0 = w * r[0], rw1 = w * r[1];
+    return rw0 * rw0 + rw1 * rw1;
+  }
+  return r[0] * r[0] + r[1] * r[1];
+}
+
+template <class R>
+void make_term(const double* pose, const double* p, const double* intr,
+               const double* uv, double huber, Term<R>* t) {
+  double r[2], jp[12], jm[6], w, cost;
+  eval_term_f64(pose, p, intr, uv, huber, r, jp, jm, &w, &cost);
+  R Jp[12], Jm[6], rw[2];
+  for (int i = 0; i < 12; ++i) Jp[i] = static_cast<R>(jp[i]);
+  for (int i = 0; i < 6; ++i) Jm[i] = static_cast<R>(jm[i]);
+  rw[0] = static_cast<R>(w * r[0]);
+  rw[1] = static_cast<R>(w * r[1]);
+  for (int a = 0; a < 6; ++a) {
+    for (int b = 0; b < 6; ++b) t->hpp[a * 6 + b] = Jp[a] * Jp[b] + Jp[6 + a] * Jp[6 + b];
+    t->gp[a] = Jp[a] * rw[0] + Jp[6 + a] * rw[1];
+  }
+  for (int a = 0; a < 3; ++a) {
+    for (int b = 0; b < 3; ++b) t->hmm[a * 3 + b] = Jm[a] * Jm[b] + Jm[3 + a] * Jm[3 + b];
+    for (int b = 0; b < 6; ++b) t->hmp[a * 6 + b] = Jm[a] * Jp[b] + Jm[3 + a] * Jp[6 + b];
+    t->gm[a] = Jm[a] * rw[0] + Jm[3 + a] * rw[1];
+  }
+  t->cost = cost;
+}
+
+template <class R>
+void term_reduce(Term<R>* a, const Term<R>& b) {  // EvaluatedCostTerm::reduce
+  for (int i = 0; i < 36; ++i) a->hpp[i] += b.hpp[i];
+  for (int i = 0; i < 9; ++i) a->hmm[i] += b.hmm[i];
+  for (int i = 0; i < 18; ++i) a->hmp[i] += b.hmp[i];
+  for (int i = 0; i < 6; ++i) a->gp[i] += b.gp[i];
+  for (int i = 0; i < 3; ++i) a->gm[i] += b.gm[i];
+  a->cost += b.cost;
+}
+
+// nalgebra-style 3x3 try_inverse: cofactor/adjugate, fails iff det == 0.
+template <class R>
+bool inverse3(const R* m, R* o) {
+  R m11 = m[0], m12 = m[1], m13 = m[2];
+  R m21 = m[3], m22 = m[4], m23 = m[5];
+  R m31 = m[6], m32 = m[7], m33 = m[8];
+  R minor_m12_m23 = m22 * m33 - m32 * m23;
+  R minor_m11_m23 = m21 * m33 - m31 * m23;
+  R minor_m11_m22 = m21 * m32 - m31 * m22;
+  R det = m11 * minor_m12_m23 - m12 * minor_m11_m23 + m13 * minor_m11_m22;
+  if (det == R(0)) return false;
+  o[0] = minor_m12_m23 / det;
+  o[1] = (m13 * m32 - m33 * m12) / det;
+  o[2] = (m12 * m23 - m22 * m13) / det;
+  o[3] = -minor_m11_m23 / det;
+  o[4] = (m11 * m33 - m31 * m13) / det;
+  o[5] = (m13 * m21 - m23 * m11) / det;
+  o[6] = minor_m11_m22 / det;
+  o[7] = (m12 * m31 - m32 * m11) / det;
+  o[8] = (m11 * m22 - m21 * m12) / det;
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Dense LDLT of one diagonal block, PSD-aware (dense_ldlt.rs:164-270).
+// a: n x n row-major (lower used); on return unit-lower L in a, d in d.
+// Returns 0, -1 on a non-finite pivot, -2 if the block is indefinite with a
+// pivot condition below the Bunch-Kaufman threshold (not restated).
+// ---------------------------------------------------------------------------
+int ldlt_decompose_inplace(int n, double* a, double* d, double rel_tol) {
+  double max_abs_pivot = 1.0;
+  double min_abs_pivot = DBL_MAX;
+  int rank = 0;
+  bool has_negative = false;
+  for (int j = 0; j < n; ++j) {
+    for (int k = 0; k < j; ++k) {
+      double s = a[j * n + k];
+      for (int p = 0; p < k; ++p) s -= a[j * n + p] * d[p] * a[k * n + p];
+      double zero_tol = std::max(max_abs_pivot, 1.0) * rel_tol;
+      a[j * n + k] = (std::fabs(d[k]) <= zero_tol) ? 0.0 : s / d[k];
+    }
+    double djj = a[j * n + j];
+    for (int p = 0; p < j; ++p) {
+      double ljp = a[j * n + p];
+      djj -= d[p] * ljp * ljp;
+    }
+    if (!std::isfinite(djj)) return -1;
+    double zero_tol = std::max(max_abs_pivot, 1.0) * rel_tol;
+    if (std::fabs(djj) <= zero_tol) {
+      d[j] = 0.0;
+    } else {
+      if (djj < 0.0) has_negative = true;
+      d[j] = djj;
+      double ad = std::fabs(djj);
+      max_abs_pivot = std::max(max_abs_pivot, ad);
+      min_abs_pivot = std::min(min_abs_pivot, ad);
+      rank += 1;
+    }
+    a[j * n + j] = 1.0;
+  }
+  for (int r = 0; r < n; ++r)
+    for (int c = r + 1; c < n; ++c) a[r * n + c] = 0.0;
+  double pivot_condition = rank == 0 ? 0.0 : min_abs_pivot / max_abs_pivot;
+  if (has_negative && pivot_condition < 1e-10) return -2;  // BK fallback (ldlt.rs:44)
+  return 0;
+}
+
+// X <- X * (L D L^T)^-1 for an m x n block X (ldlt_right_matsolve_inplace,
+// dense_ldlt.rs:300-308): X L^-T, then X D^-1 (PSD-aware), then X L^-1.
+void ldlt_right_matsolve(int n, const double* l, const double* d, int m, double* x) {
+  // X <- X L^{-T}: solve Y L^T = X row by row: y_j = x_j - sum_{k<j} y_k L[j,k]
+  for (int r = 0; r < m; ++r) {
+    double* row = x + r * n;
+    for (int j = 0; j < n; ++j) {
+      double s = row[j];
+      for (int k = 0; k < j; ++k) s -= row[k] * l[j * n + k];
+      row[j] = s;
+    }
+    for (int j = 0; j < n; ++j) row[j] = (d[j] == 0.0) ? 0.0 : row[j] / d[j];
+    // X <- X L^{-1}: solve Y L = X: y_j = x_j - sum_{k>j} y_k L[k,j]
+    for (int j = n - 1; j >= 0; --j) {
+      double s = row[j];
+      for (int k = j + 1; k < n; ++k) s -= row[k] * l[k * n + j];
+      row[j] = s;
+    }
+  }
+}
+
+// y <- (L D L^T)^-1 y for one diagonal block (block_diag_ldlt.rs:118-133).
+void ldlt_block_solve_vec(int n, const double* l, const double* d, double* y) {
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < i; ++k) y[i] -= l[i * n + k] * y[k];
+  for (int i = 0; i < n; ++i) y[i] = (d[i] == 0.0) ? 0.0 : y[i] / d[i];
+  for (int i = n - 1; i >= 0; --i)
+    for (int k = i + 1; k < n; ++k) y[i] -= l[k * n + i] * y[k];
+}
+
+// Left-looking dense block LDLT in natural order (block_sparse_ldlt.rs:479-747
+// without AMD): A (N x N row-major, lower used) with nb blocks of size bs.
+struct BlockLdlt {
+  int n = 0, bs = 0, nb = 0;
+  std::vector<double> lblk;   // off-diagonal L blocks, dense nb x nb of bs x bs
+  std::vector<double> ldiag;  // per diag block: unit lower L_jj (bs x bs)
+  std::vector<double> d;      // n pivots
+
+  int factorize(int n_, int bs_, const double* a) {
+    n = n_; bs = bs_; nb = n / bs;
+    lblk.assign(static_cast<size_t>(nb) * nb * bs * bs, 0.0);
+    ldiag.assign(static_cast<size_t>(nb) * bs * bs, 0.0);
+    d.assign(n, 0.0);
+    std::vector<double> ccol(static_cast<size_t>(nb) * bs * bs);
+    std::vector<double> qjk(bs * bs), qik(bs * bs);
+    for (int j = 0; j < nb; ++j) {
+      // load column j (blocks i >= j)
+      for (int i = j; i < nb; ++i)
+        for (int r = 0; r < bs; ++r)
+          for (int c = 0; c < bs; ++c)
+            ccol[(static_cast<size_t>(i) * bs + r) * bs + c] = a[(static_cast<size_t>(i) * bs + r) * n + j * bs + c];
+      for (int k = 0; k < j; ++k) {
+        const double* ljk = &lblk[((static_cast<size_t>(j) * nb + k) * bs) * bs];
+        bool nz = false;
+        for (int t = 0; t < bs * bs; ++t) if (ljk[t] != 0.0) { nz = true; break; }
+        if (!nz) continue;  // L[j,k] absent: k not in the etree reach of j
+        const double* lkk = &ldiag[static_cast<size_t>(k) * bs * bs];
+        const double* dk = &d[static_cast<size_t>(k) * bs];
+        // Q[j,k] = L[j,k] * L[k,k]
+        for (int r = 0; r < bs; ++r)
+          for (int c = 0; c < bs; ++c) {
+            double s = 0.0;
+            for (int t = 0; t < bs; ++t) s += ljk[r * bs + t] * lkk[t * bs + c];
+            qjk[r * bs + c] = s;
+          }
+        for (int i = j; i < nb; ++i) {
+          const double* qi;
+          if (i == j) {
+            qi = qjk.data();
+          } else {
+            const double* lik = &lblk[((static_cast<size_t>(i) * nb + k) * bs) * bs];
+            bool nzi = false;
+            for (int t = 0; t < bs * bs; ++t) if (lik[t] != 0.0) { nzi = true; break; }
+            if (!nzi) continue;
+            for (int r = 0; r < bs; ++r)
+              for (int c = 0; c < bs; ++c) {
+                double s = 0.0;
+                for (int t = 0; t < bs; ++t) s += lik[r * bs + t] * lkk[t * bs + c];
+                qik[r * bs + c] = s;
+              }
+            qi = qik.data();
+          }
+          // C(i,j) -= Q[i,k] diag(d_k) Q[j,k]^T
+          double* cij = &ccol[static_cast<size_t>(i) * bs * bs];
+          for (int r = 0; r < bs; ++r)
+            for (int c = 0; c < bs; ++c) {
+              double s = 0.0;
+              for (int t = 0; t < bs; ++t) s += qi[r * bs + t] * dk[t] * qjk[c * bs + t];
+              cij[r * bs + c] -= s;
+            }
+        }
+      }
+      // factor the diagonal block
+      double* ljj = &ldiag[static_cast<size_t>(j) * bs * bs];
+      std::memcpy(ljj, &ccol[static_cast<size_t>(j) * bs * bs], sizeof(double) * bs * bs);
+      int st = ldlt_decompose_inplace(bs, ljj, &d[static_cast<size_t>(j) * bs], kLdltTolRel);
+      if (st != 0) return st;
+      for (int i = j + 1; i < nb; ++i) {
+        double* cij = &ccol[static_cast<size_t>(i) * bs * bs];
+        bool nz = false;
+        for (int t = 0; t < bs * bs; ++t) if (cij[t] != 0.0) { nz = true; break; }
+        if (!nz) continue;
+        ldlt_right_matsolve(bs, ljj, &d[static_cast<size_t>(j) * bs], bs, cij);
+        std::memcpy(&lblk[((static_cast<size_t>(i) * nb + j) * bs) * bs], cij, sizeof(double) * bs * bs);
+      }
+    }
+    return 0;
+  }
+
+  // BlockSparseLdltFactor::solve_inplace (block_sparse_ldlt.rs:99-190)
+  void solve(double* x) const {
+    for (int j = 0; j < nb; ++j)
+      for (int i = j + 1; i < nb; ++i) {
+        const double* lij = &lblk[((static_cast<size_t>(i) * nb + j) * bs) * bs];
+        for (int r = 0; r < bs; ++r) {
+          double s = 0.0;
+          for (int c = 0; c < bs; ++c) s += lij[r * bs + c] * x[j * bs + c];
+          x[i * bs + r] -= s;
+        }
+      }
+    for (int j = 0; j < nb; ++j)
+      ldlt_block_solve_vec(bs, &ldiag[static_cast<size_t>(j) * bs * bs], &d[static_cast<size_t>(j) * bs], x + j * bs);
+    for (int j = nb - 1; j >= 0; --j)
+      for (int i = j + 1; i < nb; ++i) {
+        const double* lij = &lblk[((static_cast<size_t>(i) * nb + j) * bs) * bs];
+        for (int c = 0; c < bs; ++c) {
+          double s = 0.0;
+          for (int r = 0; r < bs; ++r) s += lij[r * bs + c] * x[i * bs + r];
+          x[j * bs + c] -= s;
+        }
+      }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Problem structure: sorted terms, reduction ranges, active index maps.
+// ---------------------------------------------------------------------------
+struct Structure {
+  int nc = 0, np = 0;
+  int64_t no = 0;
+  std::vector<int64_t> order;        // sorted term -> original obs index
+  std::vector<int64_t> range_begin;  // reduction ranges over sorted terms
+  std::vector<int> pose_block;       // pose -> free block idx or -1
+  std::vector<int> point_block;      // point -> marg block idx or -1
+  int nf = 0, nm = 0;
+  // per reduction range: pose, point
+  std::vector<int> rng_pose, rng_pt;
+  // marg block -> list of reduction ranges (in order) -> used by Schur
+  std::vector<int64_t> pt_rng_begin;  // ranges are sorted by point, so contiguous
+};
+
+void build_structure(const ora_problem* p, Structure* s) {
+  s->nc = p->n_cam; s->np = p->n_pt; s->no = p->n_obs;
+  s->order.resize(p->n_obs);
+  std::iota(s->order.begin(), s->order.end(), 0);
+  // CostFn::sort (cost_fn.rs:354-393) with CompareIdx for kinds (c, f, m):
+  // permuted key = (point, pose, intrinsics); stable sort.
+  std::stable_sort(s->order.begin(), s->order.end(), [&](int64_t a, int64_t b) {
+    if (p->obs_pt[a] != p->obs_pt[b]) return p->obs_pt[a] < p->obs_pt[b];
+    return p->obs_cam[a] < p->obs_cam[b];
+  });
+  s->range_begin.clear(); s->rng_pose.clear(); s->rng_pt.clear();
+  int64_t i = 0;
+  while (i < p->n_obs) {
+    int64_t o = s->order[i];
+    int pt = p->obs_pt[o], ps = p->obs_cam[o];
+    s->range_begin.push_back(i);
+    s->rng_pose.push_back(ps); s->rng_pt.push_back(pt);
+    while (i < p->n_obs && p->obs_pt[s->order[i]] == pt && p->obs_cam[s->order[i]] == ps) ++i;
+  }
+  s->range_begin.push_back(p->n_obs);
+  s->pose_block.assign(p->n_cam, -1);
+  s->nf = 0;
+  for (int c = 0; c < p->n_cam; ++c)
+    if (!(p->pose_const && p->pose_const[c])) s->pose_block[c] = s->nf++;
+  s->point_block.assign(p->n_pt, -1);
+  s->nm = 0;
+  for (int q = 0; q < p->n_pt; ++q)
+    if (!(p->point_const && p->point_const[q])) s->point_block[q] = s->nm++;
+  // ranges grouped by point (sorted), index of first range per point
+  s->pt_rng_begin.assign(p->n_pt + 1, 0);
+  int64_t nr = static_cast<int64_t>(s->rng_pt.size());
+  int64_t r = 0;
+  for (int q = 0; q < p->n_pt; ++q) {
+    s->pt_rng_begin[q] = r;
+    while (r < nr && s->rng_pt[r] == q) ++r;
+  }
+  s->pt_rng_begin[p->n_pt] = nr;
+}
+
+template <class F>
+void parallel_for(int64_t n, int n_threads, F&& f) {  // f(begin, end, thread_id)
+  if (n_threads <= 1 || n < 1024) { f(int64_t(0), n, 0); return; }
+  std::vector<std::thread> th;
+  int64_t chunk = (n + n_threads - 1) / n_threads;
+  for (int t = 0; t < n_threads; ++t) {
+    int64_t b = t * chunk, e = std::min(n, b + chunk);
+    if (b >= e) break;
+    th.emplace_back([&f, b, e, t]() { f(b, e, t); });
+  }
+  for (auto& x : th) x.join();
+}
+
+double total_cost(const ora_problem* p, const double* poses, const double* points, int n_threads) {
+  // calc_total_cost (cost_fn.rs:403-433): sequential sum in sorted-term order
+  // when not parallel; per-thread partial sums otherwise.
+  int nt = std::max(1, n_threads);
+  std::vector<double> part(nt, 0.0);
+  parallel_for(p->n_obs, nt, [&](int64_t b, int64_t e, int t) {
+    double acc = 0.0;
+    for (int64_t i = b; i < e; ++i)
+      acc += eval_cost_f64(poses + 7 * p->obs_cam[i], points + 3 * p->obs_pt[i],
+                           p->intrinsics, p->obs_uv + 2 * i, p->huber_delta);
+    part[t] = acc;
+  });
+  double c = 0.0;
+  for (double v : part) c += v;
+  return c;
+}
+
+// Linear system in Schur-ready form: per free pose U (6x6) + neg_grad,
+// per marg point V (3x3) + neg_grad, per reduction range W^T (3x6).
+template <class R>
+struct System {
+  std::vector<R> U, bp;    // nf*36, nf*6
+  std::vector<R> V, bm;    // nm*9,  nm*3
+  std::vector<R> Wr;       // per reduction range: 3x6 (point row, pose col) -- valid when both active
+  double max_grad = 0.0;
+};
+
+// evaluate + populate_upper_triangular_normal_equation (cost_system.rs:74-273)
+template <class R>
+void build_system(const ora_problem* p, const Structure& s, const double* poses,
+                  const double* points, double nu, int n_threads, System<R>* sys) {
+  sys->U.assign(static_cast<size_t>(s.nf) * 36, R(0));
+  sys->bp.assign(static_cast<size_t>(s.nf) * 6, R(0));
+  sys->V.assign(static_cast<size_t>(s.nm) * 9, R(0));
+  sys->bm.assign(static_cast<size_t>(s.nm) * 3, R(0));
+  int64_t nr = static_cast<int64_t>(s.rng_pt.size());
+  sys->Wr.assign(static_cast<size_t>(nr) * 18, R(0));
+  int nt = std::max(1, n_threads);
+  // Parallel over points (disjoint V/bm and W); pose sums per thread.
+  std::vector<std::vector<R>> Ut(nt), bpt(nt);
+  parallel_for(p->n_pt, nt, [&](int64_t pb, int64_t pe, int t) {
+    Ut[t].assign(static_cast<size_t>(s.nf) * 36, R(0));
+    bpt[t].assign(static_cast<size_t>(s.nf) * 6, R(0));
+    for (int64_t q = pb; q < pe; ++q) {
+      for (int64_t r = s.pt_rng_begin[q]; r < s.pt_rng_begin[q + 1]; ++r) {
+        Term<R> term;
+        bool first = true;
+        for (int64_t k = s.range_begin[r]; k < s.range_begin[r + 1]; ++k) {
+          int64_t o = s.order[k];
+          Term<R> tk;
+          make_term<R>(poses + 7 * p->obs_cam[o], points + 3 * p->obs_pt[o],
+                       p->intrinsics, p->obs_uv + 2 * o, p->huber_delta, &tk);
+          if (first) { term = tk; first = false; } else { term_reduce(&term, tk); }
+        }
+        int pb_ = s.pose_block[s.rng_pose[r]];
+        int mb = s.point_block[s.rng_pt[r]];
+        if (pb_ >= 0) {
+          R* u = &Ut[t][static_cast<size_t>(pb_) * 36];
+          for (int i = 0; i < 36; ++i) u[i] += term.hpp[i];
+          if (nu != 0.0) for (int i = 0; i < 6; ++i) u[i * 7] += static_cast<R>(nu);
+          for (int i = 0; i < 6; ++i) bpt[t][pb_ * 6 + i] -= term.gp[i];
+        }
+        if (mb >= 0) {
+          R* v = &sys->V[static_cast<size_t>(mb) * 9];
+          for (int i = 0; i < 9; ++i) v[i] += term.hmm[i];
+          if (nu != 0.0) for (int i = 0; i < 3; ++i) v[i * 4] += static_cast<R>(nu);
+          for (int i = 0; i < 3; ++i) sys->bm[static_cast<size_t>(mb) * 3 + i] -= term.gm[i];
+          if (pb_ >= 0)
+            for (int i = 0; i < 18; ++i) sys->Wr[static_cast<size_t>(r) * 18 + i] = term.hmp[i];
+        }
+      }
+    }
+  });
+  for (int t = 0; t < nt; ++t) {
+    if (Ut[t].empty()) continue;
+    for (size_t i = 0; i < sys->U.size(); ++i) sys->U[i] += Ut[t][i];
+    for (size_t i = 0; i < sys->bp.size(); ++i) sys->bp[i] += bpt[t][i];
+  }
+  double mg = 0.0;
+  for (auto v : sys->bp) mg = std::max(mg, std::fabs(static_cast<double>(v)));
+  for (auto v : sys->bm) mg = std::max(mg, std::fabs(static_cast<double>(v)));
+  sys->max_grad = mg;
+}
+
+// SchurFactor::factorize + solve (schur_ldlt.rs:536-812) with the sequential
+// forward pass (schur_ldlt.rs:241-278).  delta = [dx_f; dx_m].
+template <class R>
+int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
+                int n_threads, std::vector<double>* delta, std::vector<double>* s_out,
+                std::vector<double>* rhs_out) {
+  const int nf = s.nf;
+  const int n6 = nf * 6;
+  const int nt = std::max(1, n_threads);
+  // S_ff = H_ff (diagonal blocks only for BA)
+  std::vector<std::vector<R>> St(nt);
+  std::vector<std::vector<R>> rt(nt);
+  std::vector<R> hinv(static_cast<size_t>(s.nm) * 9);
+  std::vector<int> fail(nt, 0);
+  parallel_for(p->n_pt, nt, [&](int64_t qb, int64_t qe, int t) {
+    St[t].assign(static_cast<size_t>(n6) * n6, R(0));
+    rt[t].assign(n6, R(0));
+    std::vector<int> fidx;
+    std::vector<const R*> hmf;
+    std::vector<R> inv_hmf;
+    for (int64_t q = qb; q < qe; ++q) {
+      int mb = s.point_block[q];
+      if (mb < 0) continue;
+      R inv[9];
+      if (!inverse3<R>(&sys.V[static_cast<size_t>(mb) * 9], inv)) { fail[t] = 1; return; }
+      for (int i = 0; i < 9; ++i) hinv[static_cast<size_t>(mb) * 9 + i] = inv[i];
+      const R* g = &sys.bm[static_cast<size_t>(mb) * 3];
+      R ig[3];
+      for (int i = 0; i < 3; ++i) ig[i] = inv[i * 3 + 0] * g[0] + inv[i * 3 + 1] * g[1] + inv[i * 3 + 2] * g[2];
+      // non-zero free blocks for this marg block, in free-block order
+      fidx.clear(); hmf.clear();
+      for (int64_t r = s.pt_rng_begin[q]; r < s.pt_rng_begin[q + 1]; ++r) {
+        int fb = s.pose_block[s.rng_pose[r]];
+        if (fb < 0) continue;
+        fidx.push_back(fb);
+        hmf.push_back(&sys.Wr[static_cast<size_t>(r) * 18]);
+      }
+      size_t L = fidx.size();
+      inv_hmf.assign(L * 18, R(0));
+      for (size_t a = 0; a < L; ++a)
+        for (int i = 0; i < 3; ++i)
+          for (int c = 0; c < 6; ++c)
+            inv_hmf[a * 18 + i * 6 + c] = inv[i * 3 + 0] * hmf[a][0 * 6 + c] +
+                                          inv[i * 3 + 1] * hmf[a][1 * 6 + c] +
+                                          inv[i * 3 + 2] * hmf[a][2 * 6 + c];
+      for (size_t i = 0; i < L; ++i) {
+        int fi = fidx[i];
+        // rhs_bar[f_i] -= H_mf_i^T * (H_mm^-1 g_m)
+        for (int c = 0; c < 6; ++c)
+          rt[t][fi * 6 + c] -= hmf[i][0 * 6 + c] * ig[0] + hmf[i][1 * 6 + c] * ig[1] + hmf[i][2 * 6 + c] * ig[2];
+        for (size_t j = 0; j <= i; ++j) {
+          int fj = fidx[j];
+          size_t ii = i, jj = j;
+          int row = fi, col = fj;
+          if (fi < fj) { row = fj; col = fi; ii = j; jj = i; }
+          // S[row, col] -= H_mf[ii]^T * (H_mm^-1 H_mf[jj])
+          R* sb = &St[t][0];
+          for (int r2 = 0; r2 < 6; ++r2)
+            for (int c2 = 0; c2 < 6; ++c2) {
+              R acc = hmf[ii][0 * 6 + r2] * inv_hmf[jj * 18 + 0 * 6 + c2] +
+                      hmf[ii][1 * 6 + r2] * inv_hmf[jj * 18 + 1 * 6 + c2] +
+                      hmf[ii][2 * 6 + r2] * inv_hmf[jj * 18 + 2 * 6 + c2];
+              sb[static_cast<size_t>(row * 6 + r2) * n6 + col * 6 + c2] -= acc;
+            }
+        }
+      }
+    }
+  });
+  for (int t = 0; t < nt; ++t) if (fail[t]) return -1;
+  std::vector<double> S(static_cast<size_t>(n6) * n6, 0.0);
+  std::vector<double> rhs(n6, 0.0);
+  {
+    // merge fold accumulators in thread order (the reduce step)
+    std::vector<R> Sacc(static_cast<size_t>(n6) * n6, R(0)), racc(n6, R(0));
+    for (int i = 0; i < nf; ++i)
+      for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c)
+          Sacc[static_cast<size_t>(i * 6 + r) * n6 + i * 6 + c] = sys.U[static_cast<size_t>(i) * 36 + r * 6 + c];
+    for (int i = 0; i < n6; ++i) racc[i] = sys.bp[i];
+    for (int t = 0; t < nt; ++t) {
+      if (St[t].empty()) continue;
+      for (size_t i = 0; i < Sacc.size(); ++i) Sacc[i] += St[t][i];
+      for (int i = 0; i < n6; ++i) racc[i] += rt[t][i];
+    }
+    for (size_t i = 0; i < Sacc.size(); ++i) S[i] = static_cast<double>(Sacc[i]);
+    for (int i = 0; i < n6; ++i) rhs[i] = static_cast<double>(racc[i]);
+  }
+  // symmetrize from the lower triangle for the dense factor
+  for (int r = 0; r < n6; ++r)
+    for (int c = r + 1; c < n6; ++c) S[static_cast<size_t>(r) * n6 + c] = S[static_cast<size_t>(c) * n6 + r];
+  if (s_out) *s_out = S;
+  if (rhs_out) *rhs_out = rhs;
+  BlockLdlt f;
+  if (f.factorize(n6, 6, S.data()) != 0) return -1;
+  std::vector<double> dxf(rhs);
+  f.solve(dxf.data());
+  delta->assign(static_cast<size_t>(n6) + static_cast<size_t>(s.nm) * 3, 0.0);
+  for (int i = 0; i < n6; ++i) (*delta)[i] = dxf[i];
+  // back-substitution: dx_m[b] = H_mm^-1 (g_m[b] - sum H_mf[b,f] dx_f[f])
+  for (int q = 0; q < p->n_pt; ++q) {
+    int mb = s.point_block[q];
+    if (mb < 0) continue;
+    double m[3];
+    for (int i = 0; i < 3; ++i) m[i] = static_cast<double>(sys.bm[static_cast<size_t>(mb) * 3 + i]);
+    for (int64_t r = s.pt_rng_begin[q]; r < s.pt_rng_begin[q + 1]; ++r) {
+      int fb = s.pose_block[s.rng_pose[r]];
+      if (fb < 0) continue;
+      const R* w = &sys.Wr[static_cast<size_t>(r) * 18];
+      for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int c = 0; c < 6; ++c) acc += static_cast<double>(w[i * 6 + c]) * dxf[fb * 6 + c];
+        m[i] -= acc;
+      }
+    }
+    const R* inv = &hinv[static_cast<size_t>(mb) * 9];
+    for (int i = 0; i < 3; ++i)
+      (*delta)[n6 + mb * 3 + i] = static_cast<double>(inv[i * 3 + 0]) * m[0] +
+                                  static_cast<double>(inv[i * 3 + 1]) * m[1] +
+                                  static_cast<double>(inv[i * 3 + 2]) * m[2];
+  }
+  return 0;
+}
+
+// VarFamilies::update (var_families.rs:203-209; var_family.rs:101-114;
+// lie_group_manifold.rs:57-64): T <- exp(delta) * T, p <- p + delta.
+// Returns false if a pose fails the params-validity assertion of from_params.
+bool apply_update(const ora_problem* p, const Structure& s, const std::vector<double>& delta,
+                  const double* poses, const double* points, double* npose, double* npts) {
+  bool ok = true;
+  std::memcpy(npose, poses, sizeof(double) * 7 * p->n_cam);
+  std::memcpy(npts, points, sizeof(double) * 3 * p->n_pt);
+  for (int c = 0; c < p->n_cam; ++c) {
+    int fb = s.pose_block[c];
+    if (fb < 0) continue;
+    double e[7];
+    se3_exp<double>(&delta[fb * 6], e);
+    if (!quat_valid(e)) ok = false;
+    double out[7];
+    se3_mul<double>(e, poses + 7 * c, out);
+    if (!quat_valid(out)) ok = false;
+    std::memcpy(npose + 7 * c, out, sizeof(out));
+  }
+  const int64_t off = static_cast<int64_t>(s.nf) * 6;
+  for (int q = 0; q < p->n_pt; ++q) {
+    int mb = s.point_block[q];
+    if (mb < 0) continue;
+    for (int i = 0; i < 3; ++i) npts[3 * q + i] = points[3 * q + i] + delta[off + mb * 3 + i];
+  }
+  return ok;
+}
+
+template <class R>
+int schur_step_impl(const ora_problem* p, const Structure& s, const double* poses,
+                    const double* points, double nu, int n_threads, std::vector<double>* delta,
+                    double* max_grad, std::vector<double>* neg_grad, std::vector<double>* S,
+                    std::vector<double>* rhs, double gradient_tolerance = -1.0) {
+  System<R> sys;
+  build_system<R>(p, s, poses, points, nu, n_threads, &sys);
+  if (max_grad) *max_grad = sys.max_grad;
+  if (neg_grad) {
+    neg_grad->clear();
+    for (auto v : sys.bp) neg_grad->push_back(static_cast<double>(v));
+    for (auto v : sys.bm) neg_grad->push_back(static_cast<double>(v));
+  }
+  // check_gradient_tolerance happens before the solve (optimizer_step.rs:382-384)
+  if (sys.max_grad < gradient_tolerance) return 1;
+  return schur_solve<R>(p, s, sys, n_threads, delta, S, rhs);
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+void ora_se3_exp(const double tangent[6], double out[7]) { se3_exp<double>(tangent, out); }
+void ora_se3_mul(const double a[7], const double b[7], double out[7]) { se3_mul<double>(a, b, out); }
+void ora_se3_inverse(const double a[7], double out[7]) { se3_inverse<double>(a, out); }
+
+void ora_eval_term(const double pose[7], const double point[3], const double intr[4],
+                   const double uv[2], double huber, double r[2], double j_pose[12],
+                   double j_point[6], double* weight, double* cost) {
+  eval_term_f64(pose, point, intr, uv, huber, r, j_pose, j_point, weight, cost);
+}
+
+void ora_eval_term_dual(const double pose[7], const double point[3], const double intr[4],
+                        const double uv[2], double j_pose[12], double j_point[6]) {
+  // r(delta, dp) = uv - pi((exp(delta) * T_wc)^-1 (p + dp)), derivatives at 0
+  // (the reference's DualScalar check, real_lie_group.rs:340-390).
+  using D = Dual<9>;
+  D xi[6], tw[7], T[7], pt[3], r[2];
+  for (int i = 0; i < 6; ++i) { xi[i] = D(0.0); xi[i].d[i] = 1.0; }
+  for (int i = 0; i < 7; ++i) T[i] = D(pose[i]);
+  for (int i = 0; i < 3; ++i) { pt[i] = D(point[i]); pt[i].d[6 + i] = 1.0; }
+  D e[7];
+  se3_exp<D>(xi, e);
+  se3_mul<D>(e, T, tw);
+  residual_generic<D>(tw, pt, intr, uv, r);
+  for (int i = 0; i < 2; ++i) {
+    for (int j = 0; j < 6; ++j) j_pose[i * 6 + j] = r[i].d[j];
+    for (int j = 0; j < 3; ++j) j_point[i * 3 + j] = r[i].d[6 + j];
+  }
+}
+
+int ora_block_ldlt_solve(int n, int bs, const double* a, const double* b, double* x) {
+  BlockLdlt f;
+  int st = f.factorize(n, bs, a);
+  if (st != 0) return st;
+  std::memcpy(x, b, sizeof(double) * n);
+  f.solve(x);
+  return 0;
+}
+
+double ora_total_cost(const ora_problem* p, int n_threads) {
+  return total_cost(p, p->poses, p->points, n_threads);
+}
+
+int64_t ora_dense_system(const ora_problem* p, double nu, double* h, double* neg_grad) {
+  Structure s;
+  build_structure(p, &s);
+  int64_t n = static_cast<int64_t>(s.nf) * 6 + static_cast<int64_t>(s.nm) * 3;
+  if (!h || !neg_grad) return n;
+  System<double> sys;
+  build_system<double>(p, s, p->poses, p->points, nu, 1, &sys);
+  std::fill(h, h + n * n, 0.0);
+  const int64_t off = static_cast<int64_t>(s.nf) * 6;
+  for (int f = 0; f < s.nf; ++f)
+    for (int r = 0; r < 6; ++r) {
+      for (int c = 0; c < 6; ++c) h[(f * 6 + r) * n + f * 6 + c] = sys.U[f * 36 + r * 6 + c];
+      neg_grad[f * 6 + r] = sys.bp[f * 6 + r];
+    }
+  for (int m = 0; m < s.nm; ++m)
+    for (int r = 0; r < 3; ++r) {
+      for (int c = 0; c < 3; ++c) h[(off + m * 3 + r) * n + off + m * 3 + c] = sys.V[m * 9 + r * 3 + c];
+      neg_grad[off + m * 3 + r] = sys.bm[m * 3 + r];
+    }
+  for (size_t r = 0; r + 1 < s.range_begin.size(); ++r) {
+    int fb = s.pose_block[s.rng_pose[r]], mb = s.point_block[s.rng_pt[r]];
+    if (fb < 0 || mb < 0) continue;
+    for (int i = 0; i < 3; ++i)
+      for (int c = 0; c < 6; ++c) {
+        double w = sys.Wr[r * 18 + i * 6 + c];
+        h[(off + mb * 3 + i) * n + fb * 6 + c] += w;
+        h[(fb * 6 + c) * n + off + mb * 3 + i] += w;
+      }
+  }
+  return n;
+}
+
+int ora_schur_step(const ora_problem* p, double nu, int n_threads, int emulate_fp32,
+                   double* delta, double* s_out, double* rhs_bar_out) {
+  Structure s;
+  build_structure(p, &s);
+  std::vector<double> d, S, rhs;
+  int st = emulate_fp32
+               ? schur_step_impl<float>(p, s, p->poses, p->points, nu, n_threads, &d, nullptr,
+                                        nullptr, s_out ? &S : nullptr, rhs_bar_out ? &rhs : nullptr)
+               : schur_step_impl<double>(p, s, p->poses, p->points, nu, n_threads, &d, nullptr,
+                                         nullptr, s_out ? &S : nullptr, rhs_bar_out ? &rhs : nullptr);
+  if (st != 0) return st;
+  std::memcpy(delta, d.data(), sizeof(double) * d.size());
+  if (s_out) std::memcpy(s_out, S.data(), sizeof(double) * S.size());
+  if (rhs_bar_out) std::memcpy(rhs_bar_out, rhs.data(), sizeof(double) * rhs.size());
+  return 0;
+}
+
+int ora_optimize(const ora_problem* p, const ora_params* prm, int n_threads,
+                 ora_record* records, int cap, int* n_records, double* poses_out,
+                 double* points_out) {
+  Structure s;
+  build_structure(p, &s);
+  if (s.nf == 0 || s.nm == 0) return -10;  // SchurMissingFreeOrMarg
+  std::vector<double> poses(p->poses, p->poses + 7 * p->n_cam);
+  std::vector<double> points(p->points, p->points + 3 * p->n_pt);
+  std::vector<double> npose(poses.size()), npts(points.size());
+  double merit = total_cost(p, poses.data(), points.data(), n_threads);
+  double nu = prm->initial_lm_damping;
+  int64_t rejects = 0;
+  int64_t steps = 0;
+  int nrec = 0;
+  int rc = 0;
+  for (;;) {
+    ora_record rec;
+    rec.new_merit = NAN;
+    rec.gain_ratio = NAN;
+    rec.max_step = NAN;
+    rec.accepted = 0;
+    int reason = ORA_TERM_NONE;
+    std::vector<double> delta, neg_grad;
+    double max_grad = 0.0;
+    int st = prm->emulate_fp32
+                 ? schur_step_impl<float>(p, s, poses.data(), points.data(), nu, n_threads, &delta,
+                                          &max_grad, &neg_grad, nullptr, nullptr,
+                                          prm->gradient_tolerance)
+                 : schur_step_impl<double>(p, s, poses.data(), points.data(), nu, n_threads, &delta,
+                                           &max_grad, &neg_grad, nullptr, nullptr,
+                                           prm->gradient_tolerance);
+    rec.max_grad = max_grad;
+    if (st == 1) {
+      reason = ORA_TERM_GRADIENT_TOL;
+    } else if (st != 0) {
+      // handle_solve_failure -> reject_step (optimizer.rs:470-485)
+      nu *= 2.0;
+      rejects += 1;
+      if (rejects >= prm->max_consecutive_rejects) reason = ORA_TERM_MAX_REJECTS;
+    } else {
+      bool valid = apply_update(p, s, delta, poses.data(), points.data(), npose.data(), npts.data());
+      if (!valid) { rc = -3; }  // the reference panics in from_params
+      double new_merit = total_cost(p, npose.data(), npts.data(), n_threads);
+      rec.new_merit = new_merit;
+      double max_step = 0.0;
+      for (double v : delta) max_step = std::max(max_step, std::fabs(v));
+      rec.max_step = max_step;
+      if (max_step < prm->parameter_tolerance) {
+        if (new_merit < merit) {
+          poses.swap(npose); points.swap(npts); merit = new_merit; rec.accepted = 1;
+        }
+        reason = ORA_TERM_PARAMETER_TOL;
+      } else {
+        // compute_gain_ratio (optimizer_helpers.rs:159-173)
+        double dd = 0.0, dg = 0.0;
+        for (size_t i = 0; i < delta.size(); ++i) { dd += delta[i] * delta[i]; dg += delta[i] * neg_grad[i]; }
+        double predicted = nu * dd + dg;
+        double actual = merit - new_merit;
+        double rho = (std::fabs(predicted) > kMinPositive) ? actual / predicted
+                                                            : (actual > 0.0 ? 1.0 : 0.0);
+        rec.gain_ratio = rho;
+        if (rho > 0.0 && new_merit < merit) {
+          double x = 2.0 * rho - 1.0;
+          double f = 1.0 - x * x * x;
+          nu *= std::max(f, 1.0 / 3.0);
+          rejects = 0;
+          double rel = (merit - new_merit) / (std::fabs(merit) + kMinPositive);
+          if (rel < prm->function_tolerance) reason = ORA_TERM_FUNCTION_TOL;
+          poses.swap(npose); points.swap(npts); merit = new_merit; rec.accepted = 1;
+        } else {
+          nu *= 2.0;
+          rejects += 1;
+          if (rejects >= prm->max_consecutive_rejects) reason = ORA_TERM_MAX_REJECTS;
+        }
+      }
+    }
+    steps += 1;
+    if (steps >= prm->num_iterations && reason == ORA_TERM_NONE) reason = ORA_TERM_MAX_ITERATIONS;
+    rec.merit = merit;
+    rec.lm_damping = nu;
+    rec.termination = reason;
+    if (nrec < cap && records) records[nrec] = rec;
+    ++nrec;
+    if (reason != ORA_TERM_NONE) break;
+  }
+  if (n_records) *n_records = nrec;
+  if (poses_out) std::memcpy(poses_out, poses.data(), sizeof(double) * poses.size());
+  if (points_out) std::memcpy(points_out, points.data(), sizeof(double) * points.size());
+  return rc;
+}
+
+}  // extern "C"

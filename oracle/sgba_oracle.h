@@ -1,0 +1,124 @@
+/*
+ * sgba_oracle.h -- CPU FP64 restatement of sophus-rs's Schur-complement
+ * Levenberg-Marquardt bundle-adjustment inner loop.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the correctness oracle for the
+ * GB300 path: only the test suite, the smoke check and the CPU-baseline leg
+ * of bench.py load it, and only as the checker / the timed CPU reference.
+ * The product (libsgba) never links, loads or calls it.
+ *
+ * Every routine cites the reference function it restates (paths relative to
+ * the sophus-rs workspace root).  The reference itself is Rust and cannot be
+ * built in this environment (no cargo/rustc, crates not vendored), so this is
+ * a restatement, not a wrapper.  Bit-level parity with the reference is
+ * unpinned where it depends on third-party arithmetic (nalgebra's 3x3
+ * inverse, faer's AMD ordering, rayon's summation order); the restated
+ * reference tolerance tests pin it at the reference's own tolerances.
+ */
+#ifndef SGBA_ORACLE_H
+#define SGBA_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* OptParams fields used on the BA path
+ * (crates/sophus_opt/src/nlls/optimizer_types.rs:161-240). */
+typedef struct {
+  int32_t num_iterations;
+  double initial_lm_damping;
+  double function_tolerance;
+  double gradient_tolerance;
+  double parameter_tolerance;
+  int64_t max_consecutive_rejects;
+  int32_t emulate_fp32; /* 1: per-term blocks, H and S assembled in float
+                           (studies the GPU's FP32 assembly); 0: all f64 */
+} ora_params;
+
+/* One StepInfo-like record per Optimizer::step
+ * (crates/sophus_opt/src/nlls/optimizer_types.rs:67-83). */
+typedef struct {
+  double merit;       /* merit after the step */
+  double new_merit;   /* cost at the trial point (NaN if no trial) */
+  double lm_damping;  /* damping after the step's update */
+  double gain_ratio;
+  double max_step;    /* max |delta| */
+  double max_grad;    /* max |neg_grad| */
+  int32_t accepted;
+  int32_t termination; /* ORA_TERM_* */
+} ora_record;
+
+enum {
+  ORA_TERM_NONE = 0,
+  ORA_TERM_FUNCTION_TOL = 1,
+  ORA_TERM_GRADIENT_TOL = 2,
+  ORA_TERM_PARAMETER_TOL = 3,
+  ORA_TERM_MAX_ITERATIONS = 4,
+  ORA_TERM_MAX_REJECTS = 5,
+};
+
+/* ---- geometry / per-term math (unit-level checks) ---------------------- */
+void ora_se3_exp(const double tangent[6], double out_params[7]);
+void ora_se3_mul(const double a[7], const double b[7], double out[7]);
+void ora_se3_inverse(const double a[7], double out[7]);
+/* Residual, analytic Jacobians (row-major 2x6 pose, 2x3 point), Huber
+ * weight and cost of one PinholeCameraReprojectionCostTerm. */
+void ora_eval_term(const double pose[7], const double point[3],
+                   const double intr[4], const double uv[2], double huber,
+                   double r[2], double j_pose[12], double j_point[6],
+                   double *weight, double *cost);
+/* Same Jacobians via forward-mode dual numbers (DualScalar restatement). */
+void ora_eval_term_dual(const double pose[7], const double point[3],
+                        const double intr[4], const double uv[2],
+                        double j_pose[12], double j_point[6]);
+
+/* ---- linear algebra ----------------------------------------------------- */
+/* Block LDLT (6x6 blocks when bs=6) of a dense SPD/PSD matrix, solve A x = b.
+ * Returns 0 on success, -1 on a non-finite pivot. */
+int ora_block_ldlt_solve(int n, int bs, const double *a_rowmajor,
+                         const double *b, double *x);
+
+/* ---- whole problem ------------------------------------------------------ */
+typedef struct {
+  int32_t n_cam;
+  const double *poses;         /* n_cam*7, world_from_camera (qw qx qy qz tx ty tz) */
+  const uint8_t *pose_const;   /* n_cam or NULL */
+  int32_t n_pt;
+  const double *points;        /* n_pt*3 */
+  const uint8_t *point_const;  /* n_pt or NULL */
+  double intrinsics[4];        /* fx fy cx cy */
+  int64_t n_obs;
+  const int32_t *obs_cam;
+  const int32_t *obs_pt;
+  const double *obs_uv;        /* n_obs*2 */
+  double huber_delta;          /* <= 0: no robust kernel */
+} ora_problem;
+
+/* Total cost at the given variables (calc_total_cost). */
+double ora_total_cost(const ora_problem *p, int n_threads);
+
+/* Dense damped normal equations over active scalars (free poses then
+ * marginalized points): H (n x n, row-major) and neg_grad (n). Returns n,
+ * or the required n when the buffers are NULL. */
+int64_t ora_dense_system(const ora_problem *p, double nu, double *h,
+                         double *neg_grad);
+
+/* One Schur solve (forward pass, block LDLT of S, back-substitution) at the
+ * given variables with damping nu.  delta has n active scalars.  Optionally
+ * returns S (nf x nf row-major) and rhs_bar.  Returns 0, or -1 on failure. */
+int ora_schur_step(const ora_problem *p, double nu, int n_threads,
+                   int emulate_fp32, double *delta, double *s_out,
+                   double *rhs_bar_out);
+
+/* optimize_nlls on this path.  poses_out/points_out receive the final
+ * variables.  Returns 0 or a negative error code. */
+int ora_optimize(const ora_problem *p, const ora_params *params,
+                 int n_threads, ora_record *records, int cap, int *n_records,
+                 double *poses_out, double *points_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

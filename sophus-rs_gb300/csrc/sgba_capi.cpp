@@ -1,0 +1,804 @@
+// sgba_capi.cpp -- host driver and C ABI of libsgba (include/sgba.h).
+//
+// Planning (once per problem): sort the cost terms as CostFn::sort does,
+// reduce equal (point, pose) terms, assign free / marginalized block indices,
+// build per-camera term lists, the reduced-camera-system block list and the
+// observation pairs summed into each block.  Per LM iteration the whole step
+// (linearize, Schur complement, factor + refine, back-substitute, update,
+// trial cost, accept/reject) is one CUDA graph; termination is decided on the
+// device, so optimize() enqueues num_iterations graph launches and
+// synchronizes once.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstddef>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/sgba.h"
+#include "sgba_internal.h"
+
+using sgba::Ctrl;
+using sgba::Dev;
+using sgba::Plan;
+using sgba::Record;
+using sgba::Sizes;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int set_error(int status, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return status;
+}
+
+#define SGBA_CK(expr)                                                                           \
+  do {                                                                                          \
+    cudaError_t e_ = (expr);                                                                    \
+    if (e_ != cudaSuccess) {                                                                    \
+      return set_error(e_ == cudaErrorMemoryAllocation ? SGBA_ERR_OUT_OF_MEMORY : SGBA_ERR_CUDA, \
+                       "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__);   \
+    }                                                                                           \
+  } while (0)
+
+constexpr int kTile = 256;           // terms per camera tile (one CTA)
+constexpr int32_t kMaxDenseFree = 1536;  // dense reduced-camera-system limit (6 * 1536 rows)
+
+}  // namespace
+
+struct sgba_problem {
+  Plan plan;
+  Sizes sz{};
+  Dev d;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  sgba_opt_params params{};
+  bool inited = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int iter_launches = 0;
+  // profile
+  bool profiling = false;
+  sgba_profile prof{};
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+template <class T>
+int dev_alloc(sgba_problem* p, T** ptr, size_t count) {
+  *ptr = nullptr;
+  if (count == 0) count = 1;
+  void* v = nullptr;
+  SGBA_CK(cudaMalloc(&v, sizeof(T) * count));
+  p->allocs.push_back(v);
+  *ptr = static_cast<T*>(v);
+  return SGBA_OK;
+}
+
+template <class T>
+int dev_upload(sgba_problem* p, T** ptr, const std::vector<T>& h) {
+  int st = dev_alloc(p, ptr, h.size());
+  if (st) return st;
+  if (!h.empty()) SGBA_CK(cudaMemcpy(*ptr, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+  return SGBA_OK;
+}
+
+bool finite_all(const double* v, int64_t n) {
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+// Rotation3 are_params_valid (crates/sophus_lie/src/groups/rotation3.rs:314-319).
+bool quat_valid(const double* q) {
+  double n = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  return std::fabs(n - 1.0) <= 1e-6;
+}
+
+int build_plan(const sgba_problem_desc* d, Plan* P) {
+  if (d->n_cam < 1) return set_error(SGBA_ERR_INVALID_ARGUMENT, "n_cam must be >= 1 (got %d)", d->n_cam);
+  if (d->n_pt < 0 || d->n_obs < 0) return set_error(SGBA_ERR_INVALID_ARGUMENT, "negative n_pt or n_obs");
+  if (!d->poses) return set_error(SGBA_ERR_INVALID_ARGUMENT, "poses is NULL");
+  if (d->n_pt > 0 && !d->points) return set_error(SGBA_ERR_INVALID_ARGUMENT, "points is NULL");
+  if (d->n_obs > 0 && (!d->obs_cam || !d->obs_pt || !d->obs_uv))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation arrays are NULL");
+  if (d->n_obs >= (int64_t(1) << 31))
+    return set_error(SGBA_ERR_UNSUPPORTED, "n_obs %lld exceeds the 2^31 term limit", (long long)d->n_obs);
+  if (!finite_all(d->poses, 7ll * d->n_cam) || !finite_all(d->points, 3ll * d->n_pt) ||
+      !finite_all(d->obs_uv, 2 * d->n_obs) || !finite_all(d->intrinsics, 4))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "non-finite input value");
+  for (int j = 0; j < d->n_cam; ++j)
+    if (!quat_valid(d->poses + 7 * j))
+      return set_error(SGBA_ERR_INVALID_PARAMS, "pose %d: quaternion norm differs from 1 by more than 1e-6", j);
+  const int nc = d->n_cam, np = d->n_pt;
+  const int64_t no = d->n_obs;
+  for (int64_t o = 0; o < no; ++o) {
+    if (d->obs_cam[o] < 0 || d->obs_cam[o] >= nc)
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation %lld: pose index %d out of range", (long long)o, d->obs_cam[o]);
+    if (d->obs_pt[o] < 0 || d->obs_pt[o] >= np)
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation %lld: point index %d out of range", (long long)o, d->obs_pt[o]);
+  }
+  P->nc = nc;
+  P->np = np;
+  P->no = no;
+  // Stable LSD counting sort: by pose, then by point => order (point, pose, original).
+  std::vector<int64_t> tmp(no), ord(no);
+  {
+    std::vector<int64_t> cnt(nc + 1, 0);
+    for (int64_t o = 0; o < no; ++o) cnt[d->obs_cam[o] + 1]++;
+    for (int j = 0; j < nc; ++j) cnt[j + 1] += cnt[j];
+    for (int64_t o = 0; o < no; ++o) tmp[cnt[d->obs_cam[o]]++] = o;
+    std::vector<int64_t> cp(np + 1, 0);
+    for (int64_t o = 0; o < no; ++o) cp[d->obs_pt[o] + 1]++;
+    for (int i = 0; i < np; ++i) cp[i + 1] += cp[i];
+    for (int64_t k = 0; k < no; ++k) {
+      int64_t o = tmp[k];
+      ord[cp[d->obs_pt[o]]++] = o;
+    }
+  }
+  P->ord = ord;
+  P->obs_pose.resize(no);
+  P->obs_pt.resize(no);
+  for (int64_t k = 0; k < no; ++k) {
+    P->obs_pose[k] = d->obs_cam[ord[k]];
+    P->obs_pt[k] = d->obs_pt[ord[k]];
+  }
+  // groups (reduction ranges: equal non-conditioned arguments, cost_fn.rs:374-390)
+  P->g_begin.clear();
+  P->g_pose.clear();
+  P->g_pt.clear();
+  for (int64_t k = 0; k < no; ++k) {
+    if (k == 0 || P->obs_pose[k] != P->obs_pose[k - 1] || P->obs_pt[k] != P->obs_pt[k - 1]) {
+      P->g_begin.push_back(k);
+      P->g_pose.push_back(P->obs_pose[k]);
+      P->g_pt.push_back(P->obs_pt[k]);
+    }
+  }
+  P->ng = static_cast<int64_t>(P->g_pose.size());
+  P->g_begin.push_back(no);
+  P->pt_g_begin.assign(np + 1, 0);
+  for (int64_t g = 0; g < P->ng; ++g) P->pt_g_begin[P->g_pt[g] + 1]++;
+  for (int i = 0; i < np; ++i) P->pt_g_begin[i + 1] += P->pt_g_begin[i];
+  // free / marginalized blocks (var_families.rs:60-113, var_family.rs:156-237)
+  P->pose_fb.assign(nc, -1);
+  P->fb_pose.clear();
+  for (int j = 0; j < nc; ++j)
+    if (!(d->pose_const && d->pose_const[j])) {
+      P->pose_fb[j] = static_cast<int32_t>(P->fb_pose.size());
+      P->fb_pose.push_back(j);
+    }
+  P->nf = static_cast<int32_t>(P->fb_pose.size());
+  P->pt_mb.assign(np, -1);
+  P->mb_pt.clear();
+  for (int i = 0; i < np; ++i)
+    if (!(d->point_const && d->point_const[i])) {
+      P->pt_mb[i] = static_cast<int32_t>(P->mb_pt.size());
+      P->mb_pt.push_back(i);
+    }
+  P->nm = static_cast<int32_t>(P->mb_pt.size());
+  P->cnt_f.assign(P->nf, 0.0);
+  P->cnt_m.assign(P->nm, 0.0);
+  int64_t h_off = 0;
+  for (int64_t g = 0; g < P->ng; ++g) {
+    int fb = P->pose_fb[P->g_pose[g]], mb = P->pt_mb[P->g_pt[g]];
+    if (fb >= 0) P->cnt_f[fb] += 1.0;
+    if (mb >= 0) P->cnt_m[mb] += 1.0;
+    if (fb >= 0 && mb >= 0) ++h_off;
+  }
+  int64_t h_diag = 0;
+  for (double c : P->cnt_f) h_diag += (c > 0);
+  for (double c : P->cnt_m) h_diag += (c > 0);
+  P->n_h_blocks = h_diag + h_off;
+  // camera term lists and tiles
+  P->cam_g_begin.assign(P->nf + 1, 0);
+  for (int64_t g = 0; g < P->ng; ++g) {
+    int fb = P->pose_fb[P->g_pose[g]];
+    if (fb >= 0) P->cam_g_begin[fb + 1]++;
+  }
+  for (int f = 0; f < P->nf; ++f) P->cam_g_begin[f + 1] += P->cam_g_begin[f];
+  P->cam_g.assign(P->cam_g_begin[P->nf], 0);
+  {
+    std::vector<int64_t> fill(P->cam_g_begin.begin(), P->cam_g_begin.end() - 1);
+    for (int64_t g = 0; g < P->ng; ++g) {
+      int fb = P->pose_fb[P->g_pose[g]];
+      if (fb >= 0) P->cam_g[fill[fb]++] = g;
+    }
+  }
+  P->tile_fb.clear();
+  P->tile_begin.clear();
+  P->tile_end.clear();
+  P->fb_tile_begin.assign(P->nf + 1, 0);
+  for (int f = 0; f < P->nf; ++f) {
+    P->fb_tile_begin[f] = static_cast<int64_t>(P->tile_fb.size());
+    for (int64_t e = P->cam_g_begin[f]; e < P->cam_g_begin[f + 1]; e += kTile) {
+      P->tile_fb.push_back(f);
+      P->tile_begin.push_back(e);
+      P->tile_end.push_back(std::min<int64_t>(e + kTile, P->cam_g_begin[f + 1]));
+    }
+  }
+  P->fb_tile_begin[P->nf] = static_cast<int64_t>(P->tile_fb.size());
+  // Reduced camera system: lower blocks (row >= col) of the Schur fill
+  // (crates/sophus_opt/src/nlls/damped_hessian.rs:261-325) and the
+  // observation pairs summed into each.
+  const int nf = P->nf;
+  P->sb_row.clear();
+  P->sb_col.clear();
+  P->sb_pair_begin.clear();
+  P->pair_a.clear();
+  P->pair_b.clear();
+  if (nf > 0 && nf <= kMaxDenseFree) {
+    const int64_t nlow = static_cast<int64_t>(nf) * (nf + 1) / 2;
+    std::vector<int64_t> cnt(nlow, 0);
+    std::vector<uint8_t> present(nlow, 0);
+    auto lid = [](int64_t r, int64_t c) { return r * (r + 1) / 2 + c; };
+    for (int f = 0; f < nf; ++f)
+      if (P->cnt_f[f] > 0) present[lid(f, f)] = 1;
+    std::vector<int64_t> fg;
+    for (int i = 0; i < np; ++i) {
+      if (P->pt_mb[i] < 0) continue;
+      fg.clear();
+      for (int64_t g = P->pt_g_begin[i]; g < P->pt_g_begin[i + 1]; ++g)
+        if (P->pose_fb[P->g_pose[g]] >= 0) fg.push_back(g);
+      for (size_t b = 0; b < fg.size(); ++b)
+        for (size_t a = 0; a <= b; ++a) {
+          int64_t r = P->pose_fb[P->g_pose[fg[b]]], c = P->pose_fb[P->g_pose[fg[a]]];
+          cnt[lid(r, c)]++;
+          present[lid(r, c)] = 1;
+        }
+    }
+    std::vector<int64_t> bid(nlow, -1);
+    int64_t nb = 0;
+    for (int r = 0; r < nf; ++r)
+      for (int c = 0; c <= r; ++c)
+        if (present[lid(r, c)]) {
+          bid[lid(r, c)] = nb++;
+          P->sb_row.push_back(r);
+          P->sb_col.push_back(c);
+        }
+    P->sb_pair_begin.assign(nb + 1, 0);
+    for (int r = 0; r < nf; ++r)
+      for (int c = 0; c <= r; ++c)
+        if (bid[lid(r, c)] >= 0) P->sb_pair_begin[bid[lid(r, c)] + 1] = cnt[lid(r, c)];
+    for (int64_t b = 0; b < nb; ++b) P->sb_pair_begin[b + 1] += P->sb_pair_begin[b];
+    const int64_t npairs = P->sb_pair_begin[nb];
+    P->pair_a.assign(npairs, 0);
+    P->pair_b.assign(npairs, 0);
+    std::vector<int64_t> fill(P->sb_pair_begin.begin(), P->sb_pair_begin.end() - 1);
+    for (int i = 0; i < np; ++i) {
+      if (P->pt_mb[i] < 0) continue;
+      fg.clear();
+      for (int64_t g = P->pt_g_begin[i]; g < P->pt_g_begin[i + 1]; ++g)
+        if (P->pose_fb[P->g_pose[g]] >= 0) fg.push_back(g);
+      for (size_t b = 0; b < fg.size(); ++b)
+        for (size_t a = 0; a <= b; ++a) {
+          int64_t r = P->pose_fb[P->g_pose[fg[b]]], c = P->pose_fb[P->g_pose[fg[a]]];
+          int64_t k = fill[bid[lid(r, c)]]++;
+          P->pair_a[k] = fg[b];
+          P->pair_b[k] = fg[a];
+        }
+    }
+  }
+  // Gauge: scale about the common center of the constant poses, when no point
+  // is constant and at least one pose is constant.
+  P->gauge_kind = 0;
+  bool any_const_pt = false;
+  for (int i = 0; i < np; ++i) any_const_pt |= (d->point_const && d->point_const[i]);
+  if (!any_const_pt && P->nf < nc && P->nm > 0) {
+    const double* c0 = nullptr;
+    bool same = true;
+    for (int j = 0; j < nc; ++j) {
+      if (P->pose_fb[j] >= 0) continue;
+      const double* t = d->poses + 7 * j + 4;
+      if (!c0) c0 = t;
+      else same = same && t[0] == c0[0] && t[1] == c0[1] && t[2] == c0[2];
+    }
+    if (c0 && same) {
+      P->gauge_kind = 1;
+      P->gauge_center[0] = c0[0];
+      P->gauge_center[1] = c0[1];
+      P->gauge_center[2] = c0[2];
+    }
+  }
+  return SGBA_OK;
+}
+
+int upload(sgba_problem* p, const sgba_problem_desc* desc) {
+  Plan& P = p->plan;
+  Dev& d = p->d;
+  Sizes& s = p->sz;
+  s.nc = P.nc;
+  s.np = P.np;
+  s.nf = P.nf;
+  s.nm = P.nm;
+  s.no = P.no;
+  s.ng = P.ng;
+  s.nsb = static_cast<int64_t>(P.sb_row.size());
+  s.ntiles = static_cast<int64_t>(P.tile_fb.size());
+  s.n6 = 6 * P.nf;
+  for (int k = 0; k < 4; ++k) s.intr[k] = desc->intrinsics[k];
+  s.huber = desc->huber_delta;
+  s.gauge_kind = P.gauge_kind;
+  for (int k = 0; k < 3; ++k) s.gauge_center[k] = P.gauge_center[k];
+  int st;
+  {
+    std::vector<double2> uv(P.no);
+    for (int64_t k = 0; k < P.no; ++k) uv[k] = make_double2(desc->obs_uv[2 * P.ord[k]], desc->obs_uv[2 * P.ord[k] + 1]);
+    if ((st = dev_upload(p, &d.obs_uv, uv))) return st;
+  }
+  if ((st = dev_upload(p, &d.obs_pose, P.obs_pose))) return st;
+  if ((st = dev_upload(p, &d.obs_pt, P.obs_pt))) return st;
+  if ((st = dev_upload(p, &d.g_begin, P.g_begin))) return st;
+  if ((st = dev_upload(p, &d.g_pose, P.g_pose))) return st;
+  if ((st = dev_upload(p, &d.g_pt, P.g_pt))) return st;
+  if ((st = dev_upload(p, &d.pt_g_begin, P.pt_g_begin))) return st;
+  if ((st = dev_upload(p, &d.pose_fb, P.pose_fb))) return st;
+  if ((st = dev_upload(p, &d.pt_mb, P.pt_mb))) return st;
+  if ((st = dev_upload(p, &d.fb_pose, P.fb_pose))) return st;
+  if ((st = dev_upload(p, &d.mb_pt, P.mb_pt))) return st;
+  if ((st = dev_upload(p, &d.cnt_f, P.cnt_f))) return st;
+  if ((st = dev_upload(p, &d.cnt_m, P.cnt_m))) return st;
+  if ((st = dev_upload(p, &d.cam_g, P.cam_g))) return st;
+  if ((st = dev_upload(p, &d.tile_fb, P.tile_fb))) return st;
+  if ((st = dev_upload(p, &d.tile_begin, P.tile_begin))) return st;
+  if ((st = dev_upload(p, &d.tile_end, P.tile_end))) return st;
+  if ((st = dev_upload(p, &d.fb_tile_begin, P.fb_tile_begin))) return st;
+  if ((st = dev_upload(p, &d.sb_row, P.sb_row))) return st;
+  if ((st = dev_upload(p, &d.sb_col, P.sb_col))) return st;
+  if ((st = dev_upload(p, &d.sb_pair_begin, P.sb_pair_begin))) return st;
+  {
+    std::vector<int2> pr(P.pair_a.size());
+    for (size_t k = 0; k < pr.size(); ++k) pr[k] = make_int2(static_cast<int>(P.pair_a[k]), static_cast<int>(P.pair_b[k]));
+    if ((st = dev_upload(p, &d.pairs, pr))) return st;
+    // the pair list is device-only from here on
+    std::vector<int64_t>().swap(P.pair_a);
+    std::vector<int64_t>().swap(P.pair_b);
+  }
+  // state (quaternions disambiguated to w >= 0 as from_params does)
+  {
+    std::vector<double> poses(desc->poses, desc->poses + 7 * P.nc);
+    for (int j = 0; j < P.nc; ++j)
+      if (!(0.0 <= poses[7 * j]))
+        for (int k = 0; k < 4; ++k) poses[7 * j + k] = -poses[7 * j + k];
+    if ((st = dev_upload(p, &d.poses, poses))) return st;
+    std::vector<double> pts(desc->points, desc->points + 3 * P.np);
+    if ((st = dev_upload(p, &d.points, pts))) return st;
+  }
+  if ((st = dev_alloc(p, &d.poses_t, 7 * static_cast<size_t>(P.nc)))) return st;
+  if ((st = dev_alloc(p, &d.points_t, 3 * static_cast<size_t>(P.np)))) return st;
+  if ((st = dev_alloc(p, &d.res, P.no))) return st;
+  if ((st = dev_alloc(p, &d.res_t, P.no))) return st;
+  if ((st = dev_alloc(p, &d.pose_f, 12 * static_cast<size_t>(P.nc)))) return st;
+  if ((st = dev_alloc(p, &d.pose_dd, 24 * static_cast<size_t>(P.nc)))) return st;
+  if ((st = dev_alloc(p, &d.zmat, 18 * static_cast<size_t>(P.ng)))) return st;
+  if ((st = dev_alloc(p, &d.cinv, 6 * static_cast<size_t>(P.nm)))) return st;
+  if ((st = dev_alloc(p, &d.cvec, 3 * static_cast<size_t>(P.nm)))) return st;
+  if ((st = dev_alloc(p, &d.bm, 3 * static_cast<size_t>(P.nm)))) return st;
+  if ((st = dev_alloc(p, &d.dm, 3 * static_cast<size_t>(P.nm)))) return st;
+  if ((st = dev_alloc(p, &d.bf, 6 * static_cast<size_t>(P.nf)))) return st;
+  if ((st = dev_alloc(p, &d.rb, 6 * static_cast<size_t>(P.nf)))) return st;
+  if ((st = dev_alloc(p, &d.ufull, 36 * static_cast<size_t>(P.nf)))) return st;
+  if ((st = dev_alloc(p, &d.tile_part, 33 * static_cast<size_t>(s.ntiles)))) return st;
+  const size_t n6 = static_cast<size_t>(s.n6);
+  if ((st = dev_alloc(p, &d.S, n6 * n6))) return st;
+  SGBA_CK(cudaMemset(d.S, 0, sizeof(double) * std::max<size_t>(n6 * n6, 1)));
+  if ((st = dev_alloc(p, &d.A, n6 * n6))) return st;
+  if ((st = dev_alloc(p, &d.dpiv, n6))) return st;
+  if ((st = dev_alloc(p, &d.wpanel, n6 * 48))) return st;
+  if ((st = dev_alloc(p, &d.x, n6))) return st;
+  if ((st = dev_alloc(p, &d.r, n6))) return st;
+  SGBA_CK(cudaMemset(d.x, 0, sizeof(double) * std::max<size_t>(n6, 1)));
+  SGBA_CK(cudaMemset(d.dm, 0, sizeof(double) * std::max<size_t>(3 * P.nm, 1)));
+  d.part_cap = sgba::cost_partials_needed(s);
+  if ((st = dev_alloc(p, &d.part, static_cast<size_t>(d.part_cap)))) return st;
+  if ((st = dev_alloc(p, &d.ctrl, 1))) return st;
+  SGBA_CK(cudaMemset(d.ctrl, 0, sizeof(Ctrl)));
+  if ((st = dev_alloc(p, &d.last_rec, 1))) return st;
+  return SGBA_OK;
+}
+
+// One LM iteration (Optimizer::step for the NLLS strategy).
+int enqueue_iteration(sgba_problem* p, cudaStream_t st) {
+  int n = 0;
+  n += sgba::launch_iteration_begin(p->sz, p->d, st);
+  n += sgba::launch_linearize(p->sz, p->d, 0.0, false, st);
+  n += sgba::launch_schur(p->sz, p->d, st);
+  n += sgba::launch_factor_solve(p->sz, p->d, st);
+  n += sgba::launch_update(p->sz, p->d, st);
+  n += sgba::launch_decide(p->sz, p->d, st);
+  return n;
+}
+
+int ensure_graph(sgba_problem* p) {
+  if (p->graph_exec) return SGBA_OK;
+  SGBA_CK(cudaStreamBeginCapture(p->stream, cudaStreamCaptureModeThreadLocal));
+  int n = enqueue_iteration(p, p->stream);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(p->stream, &g);
+  if (e != cudaSuccess)
+    return set_error(SGBA_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+  p->graph = g;
+  SGBA_CK(cudaGraphInstantiate(&p->graph_exec, g, 0));
+  p->iter_launches = n;
+  return SGBA_OK;
+}
+
+int check_launch() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(SGBA_ERR_CUDA, "kernel launch failed: %s", cudaGetErrorString(e));
+  return SGBA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t sgba_abi_version(void) { return SGBA_ABI_VERSION; }
+
+size_t sgba_last_error(char* buf, size_t cap) {
+  if (buf && cap > 0) {
+    size_t n = std::min(cap - 1, g_last_error.size());
+    std::memcpy(buf, g_last_error.data(), n);
+    buf[n] = '\0';
+  }
+  return g_last_error.size();
+}
+
+int sgba_problem_create(const sgba_problem_desc* desc, int32_t device, sgba_problem** out) {
+  if (!out) return set_error(SGBA_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  if (!desc) return set_error(SGBA_ERR_INVALID_ARGUMENT, "desc is NULL");
+  sgba_problem* p = new (std::nothrow) sgba_problem();
+  if (!p) return set_error(SGBA_ERR_OUT_OF_MEMORY, "host allocation failed");
+  int st = build_plan(desc, &p->plan);
+  if (st) { delete p; return st; }
+  if (p->plan.nf > kMaxDenseFree) {
+    const int nf = p->plan.nf;
+    delete p;
+    return set_error(SGBA_ERR_UNSUPPORTED, "%d free poses exceed the dense reduced-camera-system limit (%d)",
+                     nf, kMaxDenseFree);
+  }
+  int dev = device;
+  if (dev < 0) {
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) { delete p; return set_error(SGBA_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e)); }
+  }
+  p->device = dev;
+  cudaError_t e = cudaSetDevice(dev);
+  if (e != cudaSuccess) { delete p; return set_error(SGBA_ERR_CUDA, "cudaSetDevice(%d): %s", dev, cudaGetErrorString(e)); }
+  e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete p; return set_error(SGBA_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
+  st = upload(p, desc);
+  if (st) { sgba_problem_destroy(p); return st; }
+  *out = p;
+  return SGBA_OK;
+}
+
+int sgba_problem_destroy(sgba_problem* p) {
+  if (!p) return SGBA_OK;
+  cudaSetDevice(p->device);
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  for (void* v : p->allocs) cudaFree(v);
+  if (p->d.records) cudaFree(p->d.records);
+  if (p->stream) cudaStreamDestroy(p->stream);
+  delete p;
+  return SGBA_OK;
+}
+
+int sgba_optimizer_init(sgba_problem* p, const sgba_opt_params* prm) {
+  if (!p || !prm) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  SGBA_CK(cudaSetDevice(p->device));
+  // validate_solver_config (crates/sophus_opt/src/nlls/optimizer.rs:649-717)
+  if (p->plan.nf == 0 || p->plan.nm == 0)
+    return set_error(SGBA_ERR_SCHUR_MISSING_FREE_OR_MARG,
+                     "Schur solver needs free and marginalized variables (free scalars %d, marg scalars %d)",
+                     6 * p->plan.nf, 3 * p->plan.nm);
+  if (!std::isfinite(prm->initial_lm_damping))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "initial_lm_damping is not finite");
+  p->params = *prm;
+  const int cap = std::max(1, prm->num_iterations);
+  if (p->d.record_cap < cap) {
+    if (p->d.records) cudaFree(p->d.records);
+    p->d.records = nullptr;
+    SGBA_CK(cudaMalloc(&p->d.records, sizeof(Record) * cap));
+    p->d.record_cap = cap;
+    if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+  }
+  int gst = ensure_graph(p);  // capture before any work is queued on the stream
+  if (gst) return gst;
+  Ctrl c;
+  std::memset(&c, 0, sizeof(c));
+  c.nu = prm->initial_lm_damping;
+  c.ftol = prm->function_tolerance;
+  c.gtol = prm->gradient_tolerance;
+  c.ptol = prm->parameter_tolerance;
+  c.rejects = 0;
+  c.max_rejects = prm->max_consecutive_rejects;
+  c.step = 0;
+  c.num_iterations = prm->num_iterations;
+  c.record_cap = cap;
+  SGBA_CK(cudaMemcpyAsync(p->d.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice, p->stream));
+  sgba::launch_init_merit(p->sz, p->d, p->stream);
+  int st = check_launch();
+  if (st) return st;
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  p->inited = true;
+  return SGBA_OK;
+}
+
+int sgba_optimizer_step(sgba_problem* p, sgba_iter_record* rec) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  if (!p->inited) return set_error(SGBA_ERR_STATE, "sgba_optimizer_step before sgba_optimizer_init");
+  SGBA_CK(cudaSetDevice(p->device));
+  // Optimizer::step always performs a step; the done flag only stops the
+  // device-side loop of sgba_optimize.
+  const int zero = 0;
+  SGBA_CK(cudaMemcpyAsync(reinterpret_cast<char*>(p->d.ctrl) + offsetof(Ctrl, done), &zero, sizeof(int),
+                          cudaMemcpyHostToDevice, p->stream));
+  SGBA_CK(cudaGraphLaunch(p->graph_exec, p->stream));
+  Record r;
+  SGBA_CK(cudaMemcpyAsync(&r, p->d.last_rec, sizeof(Record), cudaMemcpyDeviceToHost, p->stream));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  if (rec) std::memcpy(rec, &r, sizeof(Record));
+  return SGBA_OK;
+}
+
+int sgba_optimize(sgba_problem* p, const sgba_opt_params* prm, sgba_iter_record* records, int32_t cap,
+                  int32_t* n_records, int32_t* termination) {
+  if (!p || !prm) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  SGBA_CK(cudaSetDevice(p->device));
+  SGBA_CK(cudaEventCreate(&e0));
+  SGBA_CK(cudaEventCreate(&e1));
+  int st = sgba_optimizer_init(p, prm);
+  if (st) { cudaEventDestroy(e0); cudaEventDestroy(e1); return st; }
+  SGBA_CK(cudaEventRecord(e0, p->stream));
+  const int iters = std::max(1, prm->num_iterations);
+  double ph[5] = {0, 0, 0, 0, 0};
+  if (!p->profiling) {
+    for (int it = 0; it < iters; ++it) SGBA_CK(cudaGraphLaunch(p->graph_exec, p->stream));
+  } else {
+    // Same kernels launched directly, with events between the phases.
+    cudaEvent_t ev[6];
+    for (auto& x : ev) SGBA_CK(cudaEventCreate(&x));
+    for (int it = 0; it < iters; ++it) {
+      SGBA_CK(cudaEventRecord(ev[0], p->stream));
+      sgba::launch_iteration_begin(p->sz, p->d, p->stream);
+      sgba::launch_linearize(p->sz, p->d, 0.0, false, p->stream);
+      SGBA_CK(cudaEventRecord(ev[1], p->stream));
+      sgba::launch_schur(p->sz, p->d, p->stream);
+      SGBA_CK(cudaEventRecord(ev[2], p->stream));
+      sgba::launch_factor_solve(p->sz, p->d, p->stream);
+      SGBA_CK(cudaEventRecord(ev[3], p->stream));
+      sgba::launch_update(p->sz, p->d, p->stream);
+      SGBA_CK(cudaEventRecord(ev[4], p->stream));
+      sgba::launch_decide(p->sz, p->d, p->stream);
+      SGBA_CK(cudaEventRecord(ev[5], p->stream));
+      SGBA_CK(cudaEventSynchronize(ev[5]));
+      for (int k = 0; k < 5; ++k) {
+        float m = 0.f;
+        cudaEventElapsedTime(&m, ev[k], ev[k + 1]);
+        ph[k] += m;
+      }
+    }
+    for (auto& x : ev) cudaEventDestroy(x);
+  }
+  // build_solution (optimizer.rs:609-646): final linearisation with zero
+  // damping (or the current damping when skip_final_hessian is set).
+  Ctrl c;
+  SGBA_CK(cudaMemcpyAsync(&c, p->d.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, p->stream));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  int final_launches = sgba::launch_linearize(p->sz, p->d, prm->skip_final_hessian ? c.nu : 0.0, true, p->stream);
+  SGBA_CK(cudaEventRecord(e1, p->stream));
+  st = check_launch();
+  if (st) { cudaEventDestroy(e0); cudaEventDestroy(e1); return st; }
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const int nrec = std::min(c.step, p->d.record_cap);
+  if (records && cap > 0) {
+    std::vector<Record> h(nrec);
+    if (nrec > 0) SGBA_CK(cudaMemcpy(h.data(), p->d.records, sizeof(Record) * nrec, cudaMemcpyDeviceToHost));
+    std::memcpy(records, h.data(), sizeof(Record) * std::min(nrec, cap));
+  }
+  if (n_records) *n_records = c.step;
+  if (termination) *termination = c.termination;
+  p->prof.kernel_launches = 3 + static_cast<int64_t>(iters) * p->iter_launches + final_launches;
+  p->prof.ms_total = ms;
+  p->prof.ms_linearize = ph[0];
+  p->prof.ms_schur = ph[1];
+  p->prof.ms_factor = ph[2];
+  p->prof.ms_update = ph[3];
+  p->prof.ms_cost = ph[4];
+  return SGBA_OK;
+}
+
+int sgba_get_variables(sgba_problem* p, double* poses, double* points) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  SGBA_CK(cudaSetDevice(p->device));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  if (poses) SGBA_CK(cudaMemcpy(poses, p->d.poses, sizeof(double) * 7 * p->plan.nc, cudaMemcpyDeviceToHost));
+  if (points && p->plan.np > 0)
+    SGBA_CK(cudaMemcpy(points, p->d.points, sizeof(double) * 3 * p->plan.np, cudaMemcpyDeviceToHost));
+  return SGBA_OK;
+}
+
+int sgba_set_variables(sgba_problem* p, const double* poses, const double* points) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  SGBA_CK(cudaSetDevice(p->device));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  if (poses) {
+    std::vector<double> h(poses, poses + 7 * p->plan.nc);
+    if (!finite_all(h.data(), static_cast<int64_t>(h.size())))
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "non-finite pose");
+    for (int j = 0; j < p->plan.nc; ++j) {
+      if (!quat_valid(&h[7 * j])) return set_error(SGBA_ERR_INVALID_PARAMS, "pose %d: invalid quaternion", j);
+      if (!(0.0 <= h[7 * j]))
+        for (int k = 0; k < 4; ++k) h[7 * j + k] = -h[7 * j + k];
+    }
+    SGBA_CK(cudaMemcpy(p->d.poses, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+  }
+  if (points && p->plan.np > 0) {
+    if (!finite_all(points, 3ll * p->plan.np)) return set_error(SGBA_ERR_INVALID_ARGUMENT, "non-finite point");
+    SGBA_CK(cudaMemcpy(p->d.points, points, sizeof(double) * 3 * p->plan.np, cudaMemcpyHostToDevice));
+  }
+  p->inited = false;
+  return SGBA_OK;
+}
+
+int sgba_get_cost(sgba_problem* p, double* cost) {
+  if (!p || !cost) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!p->inited) return set_error(SGBA_ERR_STATE, "no optimizer state (call sgba_optimizer_init)");
+  SGBA_CK(cudaSetDevice(p->device));
+  Ctrl c;
+  SGBA_CK(cudaMemcpyAsync(&c, p->d.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, p->stream));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  *cost = c.merit;
+  return SGBA_OK;
+}
+
+int sgba_get_layout(sgba_problem* p, sgba_layout* out) {
+  if (!p || !out) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  out->n_free_poses = p->plan.nf;
+  out->n_marg_points = p->plan.nm;
+  out->n_terms = p->plan.ng;
+  out->n_h_blocks = p->plan.n_h_blocks;
+  out->n_s_blocks = p->sz.nsb;
+  int64_t np = 0;
+  if (!p->plan.sb_pair_begin.empty()) np = p->plan.sb_pair_begin.back();
+  out->n_schur_pairs = np;
+  return SGBA_OK;
+}
+
+int sgba_export_pattern(sgba_problem* p, int32_t* h_rows, int32_t* h_cols, int32_t* s_rows, int32_t* s_cols) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  const Plan& P = p->plan;
+  if (h_rows && h_cols) {
+    int64_t k = 0;
+    for (int f = 0; f < P.nf; ++f)
+      if (P.cnt_f[f] > 0) { h_rows[k] = f; h_cols[k] = f; ++k; }
+    for (int m = 0; m < P.nm; ++m)
+      if (P.cnt_m[m] > 0) { h_rows[k] = P.nf + m; h_cols[k] = P.nf + m; ++k; }
+    for (int64_t g = 0; g < P.ng; ++g) {
+      int fb = P.pose_fb[P.g_pose[g]], mb = P.pt_mb[P.g_pt[g]];
+      if (fb >= 0 && mb >= 0) { h_rows[k] = P.nf + mb; h_cols[k] = fb; ++k; }
+    }
+  }
+  if (s_rows && s_cols) {
+    for (size_t b = 0; b < P.sb_row.size(); ++b) {
+      s_rows[b] = P.sb_row[b];
+      s_cols[b] = P.sb_col[b];
+    }
+  }
+  return SGBA_OK;
+}
+
+int sgba_debug_last_system(sgba_problem* p, double* s_dense, double* rhs, double* delta) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  SGBA_CK(cudaSetDevice(p->device));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  const size_t n6 = static_cast<size_t>(p->sz.n6);
+  if (s_dense) SGBA_CK(cudaMemcpy(s_dense, p->d.S, sizeof(double) * n6 * n6, cudaMemcpyDeviceToHost));
+  if (rhs) SGBA_CK(cudaMemcpy(rhs, p->d.rb, sizeof(double) * n6, cudaMemcpyDeviceToHost));
+  if (delta) {
+    SGBA_CK(cudaMemcpy(delta, p->d.x, sizeof(double) * n6, cudaMemcpyDeviceToHost));
+    if (p->plan.nm > 0)
+      SGBA_CK(cudaMemcpy(delta + n6, p->d.dm, sizeof(double) * 3 * p->plan.nm, cudaMemcpyDeviceToHost));
+  }
+  return SGBA_OK;
+}
+
+// State blob: magic, sizes, LM scalars, poses, points.
+int sgba_state_save(sgba_problem* p, void* buf, size_t* size) {
+  if (!p || !size) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np));
+  if (!buf) { *size = need; return SGBA_OK; }
+  if (*size < need) return set_error(SGBA_ERR_INVALID_ARGUMENT, "state buffer too small (%zu < %zu)", *size, need);
+  if (!p->inited) return set_error(SGBA_ERR_STATE, "no optimizer state to save");
+  SGBA_CK(cudaSetDevice(p->device));
+  Ctrl c;
+  SGBA_CK(cudaMemcpyAsync(&c, p->d.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, p->stream));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  char* b = static_cast<char*>(buf);
+  std::memset(b, 0, 64);
+  const uint64_t magic = 0x5347424153544131ull;  // "SGBASTA1"
+  std::memcpy(b, &magic, 8);
+  int32_t nc = p->plan.nc, np = p->plan.np;
+  std::memcpy(b + 8, &nc, 4);
+  std::memcpy(b + 12, &np, 4);
+  std::memcpy(b + 16, &c.nu, 8);
+  std::memcpy(b + 24, &c.merit, 8);
+  int64_t rej = c.rejects, stp = c.step;
+  std::memcpy(b + 32, &rej, 8);
+  std::memcpy(b + 40, &stp, 8);
+  SGBA_CK(cudaMemcpy(b + 64, p->d.poses, sizeof(double) * 7 * nc, cudaMemcpyDeviceToHost));
+  if (np > 0) SGBA_CK(cudaMemcpy(b + 64 + sizeof(double) * 7 * nc, p->d.points, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost));
+  *size = need;
+  return SGBA_OK;
+}
+
+int sgba_state_load(sgba_problem* p, const void* buf, size_t size) {
+  if (!p || !buf) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!p->inited) return set_error(SGBA_ERR_STATE, "call sgba_optimizer_init before sgba_state_load");
+  const char* b = static_cast<const char*>(buf);
+  const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np));
+  uint64_t magic;
+  int32_t nc, np;
+  if (size < need) return set_error(SGBA_ERR_INVALID_ARGUMENT, "state blob too small");
+  std::memcpy(&magic, b, 8);
+  std::memcpy(&nc, b + 8, 4);
+  std::memcpy(&np, b + 12, 4);
+  if (magic != 0x5347424153544131ull || nc != p->plan.nc || np != p->plan.np)
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "state blob does not match this problem");
+  SGBA_CK(cudaSetDevice(p->device));
+  Ctrl c;
+  SGBA_CK(cudaMemcpyAsync(&c, p->d.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, p->stream));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  int64_t rej, stp;
+  std::memcpy(&c.nu, b + 16, 8);
+  std::memcpy(&c.merit, b + 24, 8);
+  std::memcpy(&rej, b + 32, 8);
+  std::memcpy(&stp, b + 40, 8);
+  c.rejects = rej;
+  c.step = static_cast<int>(stp);
+  c.done = 0;
+  SGBA_CK(cudaMemcpy(p->d.poses, b + 64, sizeof(double) * 7 * nc, cudaMemcpyHostToDevice));
+  if (np > 0) SGBA_CK(cudaMemcpy(p->d.points, b + 64 + sizeof(double) * 7 * nc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice));
+  SGBA_CK(cudaMemcpy(p->d.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice));
+  // residuals of the loaded state
+  sgba::launch_init_merit(p->sz, p->d, p->stream);
+  SGBA_CK(cudaMemcpyAsync(reinterpret_cast<char*>(p->d.ctrl) + offsetof(Ctrl, merit), b + 24, 8,
+                          cudaMemcpyHostToDevice, p->stream));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  return check_launch();
+}
+
+int sgba_get_profile(sgba_problem* p, sgba_profile* out) {
+  if (!p || !out) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = p->prof;
+  return SGBA_OK;
+}
+
+int sgba_set_profiling(sgba_problem* p, int32_t enabled) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  p->profiling = enabled != 0;
+  return SGBA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,165 @@
+// sgba_internal.h -- structures shared by the host driver (sgba_capi.cpp) and
+// the CUDA translation units.  Plain C++ (no CUDA types beyond cudaStream_t).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace sgba {
+
+// Device-resident LM control block (one per problem).  Written only by the
+// single-CTA control kernels, read by every kernel of an iteration.
+struct Ctrl {
+  // LM state (crates/sophus_opt/src/nlls/optimizer.rs:40-58)
+  double nu;            // lm_damping
+  double merit;         // current merit
+  double new_merit;     // trial merit of the current step
+  double gain_ratio;
+  double max_step;
+  double max_grad;
+  double alpha;         // gauge projection coefficient of the current step
+  double dd_sum;        // delta . delta
+  double dg_sum;        // delta . neg_grad
+  double ftol, gtol, ptol;
+  long long rejects;
+  long long max_rejects;
+  int step;             // total_step_count
+  int num_iterations;
+  int done;             // termination reached: every kernel returns at once
+  int skip;             // 0 normal, 1 gradient tolerance, 2 solve failure
+  int accept;
+  int termination;
+  int record_cap;
+  int fail;             // a point block failed its Cholesky this iteration
+  unsigned long long max_grad_bits;  // atomicMax over non-negative doubles
+  unsigned long long max_step_bits;
+};
+
+// Per-step record, layout-identical to sgba_iter_record.
+struct Record {
+  double merit, new_merit, lm_damping, gain_ratio, max_step, max_grad;
+  int32_t accepted, termination;
+};
+
+// Host-side plan: everything derived from the problem structure once.
+struct Plan {
+  int32_t nc = 0, np = 0, nf = 0, nm = 0;
+  int64_t no = 0, ng = 0;
+  // sorted observations (by point, then pose; stable)
+  std::vector<int64_t> ord;          // sorted -> original index
+  std::vector<int32_t> obs_pose, obs_pt;
+  // groups = reduced cost terms = distinct (point, pose) pairs, sorted
+  std::vector<int64_t> g_begin;      // ng+1, into sorted obs
+  std::vector<int32_t> g_pose, g_pt;
+  std::vector<int64_t> pt_g_begin;   // np+1
+  std::vector<int32_t> pose_fb;      // nc: free block or -1
+  std::vector<int32_t> pt_mb;        // np: marg block or -1
+  std::vector<int32_t> fb_pose;      // nf: pose index of a free block
+  std::vector<int32_t> mb_pt;        // nm: point index of a marg block
+  std::vector<double> cnt_f, cnt_m;  // reduced terms per free pose / marg point
+  // camera lists (all groups of each free pose), split into tiles
+  std::vector<int64_t> cam_g_begin;  // nf+1
+  std::vector<int64_t> cam_g;        // group ids
+  std::vector<int32_t> tile_fb;      // tile -> free block
+  std::vector<int64_t> tile_begin;   // tile -> first entry in cam_g
+  std::vector<int64_t> tile_end;
+  std::vector<int64_t> fb_tile_begin;  // nf+1
+  // reduced camera system blocks (lower, row >= col) and Schur pairs
+  std::vector<int32_t> sb_row, sb_col;
+  std::vector<int64_t> sb_pair_begin;  // nsb+1
+  std::vector<int64_t> pair_a, pair_b; // groups (row camera, col camera)
+  int64_t n_h_blocks = 0;
+  // gauge: 0 none, 1 scale about gauge_center
+  int gauge_kind = 0;
+  double gauge_center[3] = {0, 0, 0};
+};
+
+// Device buffers of one problem.
+struct Dev {
+  // static structure
+  double2* obs_uv = nullptr;       // sorted
+  int32_t* obs_pose = nullptr;     // sorted
+  int32_t* obs_pt = nullptr;       // sorted
+  int64_t* g_begin = nullptr;
+  int32_t* g_pose = nullptr;
+  int32_t* g_pt = nullptr;
+  int64_t* pt_g_begin = nullptr;
+  int32_t* pose_fb = nullptr;
+  int32_t* pt_mb = nullptr;
+  int32_t* fb_pose = nullptr;
+  int32_t* mb_pt = nullptr;
+  double* cnt_f = nullptr;
+  double* cnt_m = nullptr;
+  int64_t* cam_g = nullptr;
+  int32_t* tile_fb = nullptr;
+  int64_t* tile_begin = nullptr;
+  int64_t* tile_end = nullptr;
+  int64_t* fb_tile_begin = nullptr;
+  int32_t* sb_row = nullptr;
+  int32_t* sb_col = nullptr;
+  int64_t* sb_pair_begin = nullptr;
+  int2* pairs = nullptr;           // (group a, group b); int32 group ids
+  // state
+  double* poses = nullptr;         // nc*7
+  double* points = nullptr;        // np*3
+  double* poses_t = nullptr;       // trial
+  double* points_t = nullptr;
+  float2* res = nullptr;           // residual at current state (sorted obs)
+  float2* res_t = nullptr;         // residual at trial state
+  // per iteration
+  float* pose_f = nullptr;         // nc*12: R_cw (row-major) + t_cw, float
+  float* pose_dd = nullptr;        // nc*24: R_cw + t_cw as (hi,lo) pairs
+  float* zmat = nullptr;           // ng*18: Z = W C^-T (6x3 row-major)
+  double* cinv = nullptr;          // nm*6: C^-1 lower (00,10,11,20,21,22)
+  double* cvec = nullptr;          // nm*3: C^-1 b_m
+  double* bm = nullptr;            // nm*3: neg_grad of points
+  double* bf = nullptr;            // nf*6: neg_grad of poses
+  double* ufull = nullptr;         // nf*36: U_j (undamped J^T J) full 6x6
+  double* rb = nullptr;            // nf*6: reduced rhs
+  double* tile_part = nullptr;     // ntiles*33 partial sums
+  double* S = nullptr;             // n6*n6 FP64 (lower valid)
+  float* A = nullptr;              // n6*n6 FP32 factor (lower: unit L)
+  float* dpiv = nullptr;           // n6 pivots
+  float* wpanel = nullptr;         // n6*64 panel scratch (A_ip L^-T)
+  double* x = nullptr;             // n6 solution / refinement
+  double* r = nullptr;             // n6 residual
+  double* dm = nullptr;            // nm*3 point steps
+  double* part = nullptr;          // reduction partials
+  int part_cap = 0;
+  Ctrl* ctrl = nullptr;
+  Record* records = nullptr;
+  int record_cap = 0;
+  Record* last_rec = nullptr;      // record of the latest step
+};
+
+struct Sizes {
+  int32_t nc, np, nf, nm;
+  int64_t no, ng, nsb, ntiles;
+  int n6;
+  double intr[4];
+  double huber;
+  int gauge_kind;
+  double gauge_center[3];
+};
+
+// ---- launchers (sgba_kernels.cu / sgba_solver.cu) -------------------------
+// Each returns the number of kernel launches it enqueued.
+int launch_pose_tables(const Sizes& s, const Dev& d, const double* poses, cudaStream_t st);
+int launch_cost(const Sizes& s, const Dev& d, const double* poses, const double* points,
+                float2* res_out, double* partials, cudaStream_t st);
+int launch_init_merit(const Sizes& s, const Dev& d, cudaStream_t st);
+int launch_iteration_begin(const Sizes& s, const Dev& d, cudaStream_t st);
+int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_override,
+                     cudaStream_t st);
+int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st);
+int launch_factor_solve(const Sizes& s, const Dev& d, cudaStream_t st);
+int launch_update(const Sizes& s, const Dev& d, cudaStream_t st);
+int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st);
+
+int cost_partials_needed(const Sizes& s);  // reduction partial slots
+int solver_launch_count(const Sizes& s);
+
+}  // namespace sgba

@@ -1,0 +1,1174 @@
+// sgba_kernels.cu -- per-iteration kernels of the GB300 Schur-LM bundle
+// adjustment (everything except the reduced-camera-system factorization,
+// which lives in sgba_solver.cu).
+//
+// Precision plan (GB300 runs FP32 at ~64x its FP64 rate):
+//   * Jacobians and all block products in FP32 on the CUDA cores;
+//   * every sum that the reference forms in f64 (Hessian blocks, gradients,
+//     Schur complement, cost, step statistics) is carried in float-float
+//     (sgba_dd.cuh) and stored as f64;
+//   * f64 proper only for the SE(3) update of the poses and tiny scalars.
+// Reductions use fixed partitions and fixed trees: results are
+// bit-reproducible from run to run.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sgba_dd.cuh"
+#include "sgba_internal.h"
+
+namespace sgba {
+
+namespace {
+
+constexpr int kCostThreads = 256;
+constexpr int kCostMaxBlocks = 1216;  // 8 x 152 SMs
+constexpr double kEps = 1e-6;         // EPS_F64 (crates/sophus_autodiff/src/linalg.rs:75)
+
+__device__ __forceinline__ bool halted(const Ctrl* c) { return c->done != 0; }
+__device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0; }
+
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
+  // Non-negative doubles order like their bit patterns.
+  if (!(v >= 0.0)) v = (v != v) ? __longlong_as_double(0x7ff8000000000000ll) : 0.0;
+  atomicMax(addr, static_cast<unsigned long long>(__double_as_longlong(v)));
+}
+
+// --- SE(3) in f64 (restated from sophus_lie, see the oracle for citations) --
+// Rotation3Impl::matrix (crates/sophus_lie/src/groups/rotation3.rs:449-492)
+__device__ void rot_matrix(const double* q, double* m) {
+  double r = q[0], x = q[1], y = q[2], z = q[3];
+  double tx = 2.0 * x, ty = 2.0 * y, tz = 2.0 * z, tr = 2.0 * r;
+  double txx = tx * x, tyy = ty * y, tzz = tz * z;
+  double txy = tx * y, txz = tx * z, tyz = ty * z;
+  double trx = tr * x, try_ = tr * y, trz = tr * z;
+  m[0] = 1.0 - (tyy + tzz); m[1] = txy - trz; m[2] = txz + try_;
+  m[3] = txy + trz; m[4] = 1.0 - (txx + tzz); m[5] = tyz - trx;
+  m[6] = txz - try_; m[7] = tyz + trx; m[8] = 1.0 - (txx + tyy);
+}
+
+// Left-perturbation update T <- exp(xi) * T
+// (crates/sophus_lie/src/lie_group/lie_group_manifold.rs:33-35,57-64;
+//  exp: crates/sophus_lie/src/groups/affine_group_template.rs:354-360,
+//       crates/sophus_lie/src/groups/rotation3.rs:363-387 and mat_v :761-778;
+//  group_mul: affine_group_template.rs:387-396, quaternion.rs:212-225;
+//  disambiguate: rotation3.rs:176-182).
+__device__ void se3_left_update(const double* xi, const double* T, double* out) {
+  const double w0 = xi[0], w1 = xi[1], w2 = xi[2];
+  double th2 = w0 * w0 + w1 * w1 + w2 * w2;
+  double eq[4];
+  if (th2 <= kEps * kEps) {
+    double th4 = th2 * th2;
+    double im = 0.5 - (1.0 / 48.0) * th2 + (1.0 / 3840.0) * th4;
+    eq[0] = 1.0 - (1.0 / 8.0) * th2 + (1.0 / 384.0) * th4;
+    eq[1] = im * w0; eq[2] = im * w1; eq[3] = im * w2;
+  } else {
+    double th = sqrt(th2);
+    double s, c;
+    sincos(0.5 * th, &s, &c);
+    double im = s / th;
+    eq[0] = c; eq[1] = im * w0; eq[2] = im * w1; eq[3] = im * w2;
+  }
+  // mat_v * nu
+  double h[9] = {0.0, -w2, w1, w2, 0.0, -w0, -w1, w0, 0.0};
+  double v[9];
+  if (th2 <= kEps) {
+    for (int i = 0; i < 9; ++i) v[i] = 0.5 * h[i];
+  } else {
+    double h2[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        h2[i * 3 + j] = h[i * 3 + 0] * h[0 * 3 + j] + h[i * 3 + 1] * h[1 * 3 + j] + h[i * 3 + 2] * h[2 * 3 + j];
+    double th = sqrt(th2);
+    double a = (1.0 - cos(th)) / th2;
+    double b = (th - sin(th)) / (th2 * th);
+    for (int i = 0; i < 9; ++i) v[i] = a * h[i] + b * h2[i];
+  }
+  v[0] += 1.0; v[4] += 1.0; v[8] += 1.0;
+  double et[3];
+  for (int i = 0; i < 3; ++i) et[i] = v[i * 3 + 0] * xi[3] + v[i * 3 + 1] * xi[4] + v[i * 3 + 2] * xi[5];
+  if (!(0.0 <= eq[0])) { for (int i = 0; i < 4; ++i) eq[i] = -eq[i]; }
+  // exp(xi) * T
+  const double* b = T;
+  double q[4];
+  q[0] = eq[0] * b[0] - (eq[1] * b[1] + eq[2] * b[2] + eq[3] * b[3]);
+  q[1] = b[1] * eq[0] + eq[1] * b[0] + (eq[2] * b[3] - eq[3] * b[2]);
+  q[2] = b[2] * eq[0] + eq[2] * b[0] + (eq[3] * b[1] - eq[1] * b[3]);
+  q[3] = b[3] * eq[0] + eq[3] * b[0] + (eq[1] * b[2] - eq[2] * b[1]);
+  double r[9];
+  rot_matrix(eq, r);
+  for (int i = 0; i < 3; ++i)
+    out[4 + i] = (r[i * 3 + 0] * b[4] + r[i * 3 + 1] * b[5] + r[i * 3 + 2] * b[6]) + et[i];
+  if (!(0.0 <= q[0])) { for (int i = 0; i < 4; ++i) q[i] = -q[i]; }
+  for (int i = 0; i < 4; ++i) out[i] = q[i];
+}
+
+// HuberKernel (crates/sophus_opt/src/robust_kernel.rs:13-35): weight applied to
+// the residual; H stays J^T J.
+__device__ __forceinline__ float huber_weight_f(float huber, float r0, float r1) {
+  if (!(huber > 0.0f)) return 1.0f;
+  float nrm = sqrtf(r0 * r0 + r1 * r1);
+  if (nrm == 0.0f) return 0.0f;
+  if (nrm <= huber) return 1.0f;
+  return sqrtf(2.0f * huber * nrm - huber * huber) / nrm;
+}
+
+// Jacobians of r = z - pi(T_cw p) w.r.t. the left pose perturbation (2x6,
+// tangent [omega; nu]) and the point (2x3), in FP32
+// (crates/sophus_opt/src/nlls/functor_library/costs/pinhole_reprojection.rs:60-95).
+struct JacF {
+  float jp[12];  // row-major 2x6
+  float jm[6];   // row-major 2x3
+};
+__device__ __forceinline__ void jacobians_f(const float* pt /*R_cw 9 + t_cw 3*/, float px, float py,
+                                            float pz, float fx, float fy, JacF* J) {
+  float xc = pt[0] * px + pt[1] * py + pt[2] * pz + pt[9];
+  float yc = pt[3] * px + pt[4] * py + pt[5] * pz + pt[10];
+  float zc = pt[6] * px + pt[7] * py + pt[8] * pz + pt[11];
+  float iz = 1.0f / zc;
+  float a0 = fx * iz, a2 = -fx * xc * iz * iz;
+  float b1 = fy * iz, b2 = -fy * yc * iz * iz;
+  // D = dpi * R_cw (2x3)
+  float D[6];
+  for (int k = 0; k < 3; ++k) {
+    D[k] = a0 * pt[0 * 3 + k] + a2 * pt[2 * 3 + k];
+    D[3 + k] = b1 * pt[1 * 3 + k] + b2 * pt[2 * 3 + k];
+  }
+  for (int r = 0; r < 2; ++r) {
+    const float* d = D + 3 * r;
+    // D * hat(-p)
+    J->jp[r * 6 + 0] = -d[1] * pz + d[2] * py;
+    J->jp[r * 6 + 1] = d[0] * pz - d[2] * px;
+    J->jp[r * 6 + 2] = -d[0] * py + d[1] * px;
+    J->jp[r * 6 + 3] = d[0];
+    J->jp[r * 6 + 4] = d[1];
+    J->jp[r * 6 + 5] = d[2];
+    J->jm[r * 3 + 0] = -d[0];
+    J->jm[r * 3 + 1] = -d[1];
+    J->jm[r * 3 + 2] = -d[2];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pose tables: T_cw = T_wc^-1 in f64, published as float and float-float.
+// ---------------------------------------------------------------------------
+__global__ void k_pose_tables(int nc, const double* __restrict__ poses, float* __restrict__ pose_f,
+                              float* __restrict__ pose_dd, const Ctrl* ctrl, int respect_skip) {
+  if (respect_skip ? skipping(ctrl) : halted(ctrl)) return;
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nc) return;
+  const double* T = poses + 7 * j;
+  double qc[4] = {T[0], -T[1], -T[2], -T[3]};
+  double R[9];
+  rot_matrix(qc, R);
+  double t[3];
+  for (int i = 0; i < 3; ++i) t[i] = -(R[i * 3 + 0] * T[4] + R[i * 3 + 1] * T[5] + R[i * 3 + 2] * T[6]);
+  float* pf = pose_f + 12 * j;
+  float* pd = pose_dd + 24 * j;
+  for (int i = 0; i < 9; ++i) {
+    pf[i] = __double2float_rn(R[i]);
+    dd v = dd_from_double(R[i]);
+    pd[2 * i] = v.hi;
+    pd[2 * i + 1] = v.lo;
+  }
+  for (int i = 0; i < 3; ++i) {
+    pf[9 + i] = __double2float_rn(t[i]);
+    dd v = dd_from_double(t[i]);
+    pd[18 + 2 * i] = v.hi;
+    pd[18 + 2 * i + 1] = v.lo;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Cost: calc_total_cost (crates/sophus_opt/src/nlls/cost/cost_fn.rs:403-433)
+// in float-float; also publishes the FP32 residual for the next linearisation.
+// ---------------------------------------------------------------------------
+struct CostArgs {
+  int64_t no;
+  const double2* uv;
+  const int32_t* opose;
+  const int32_t* opt;
+  const float* pose_dd;
+  const double* points;
+  float2* res_out;
+  double* partials;
+  dd fx, fy, cx, cy;
+  float huber;
+  dd huber_dd;
+  int respect_skip;
+};
+
+__global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* ctrl) {
+  if (a.respect_skip ? skipping(ctrl) : halted(ctrl)) return;
+  dd acc = dd_make(0.0f, 0.0f);
+  for (int64_t o = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; o < a.no;
+       o += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const float* P = a.pose_dd + 24 * a.opose[o];
+    const double* pw = a.points + 3 * a.opt[o];
+    dd p0 = dd_from_double(pw[0]), p1 = dd_from_double(pw[1]), p2 = dd_from_double(pw[2]);
+    dd xc[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      dd r0 = dd_make(P[2 * (i * 3 + 0)], P[2 * (i * 3 + 0) + 1]);
+      dd r1 = dd_make(P[2 * (i * 3 + 1)], P[2 * (i * 3 + 1) + 1]);
+      dd r2 = dd_make(P[2 * (i * 3 + 2)], P[2 * (i * 3 + 2) + 1]);
+      dd tt = dd_make(P[18 + 2 * i], P[18 + 2 * i + 1]);
+      xc[i] = dd_add(dd_add(dd_add(dd_mul(r0, p0), dd_mul(r1, p1)), dd_mul(r2, p2)), tt);
+    }
+    dd u = dd_div(xc[0], xc[2]);
+    dd v = dd_div(xc[1], xc[2]);
+    double2 z = a.uv[o];
+    dd ru = dd_sub(dd_from_double(z.x), dd_add(dd_mul(u, a.fx), a.cx));
+    dd rv = dd_sub(dd_from_double(z.y), dd_add(dd_mul(v, a.fy), a.cy));
+    dd n2 = dd_add(dd_mul(ru, ru), dd_mul(rv, rv));
+    dd c = n2;
+    if (a.huber > 0.0f) {
+      dd nrm = dd_sqrt(n2);
+      if (!(nrm.hi <= a.huber || (nrm.hi == a.huber_dd.hi && nrm.lo <= a.huber_dd.lo))) {
+        // 2 delta |r| - delta^2
+        c = dd_sub(dd_mul(dd_add(a.huber_dd, a.huber_dd), nrm), dd_mul(a.huber_dd, a.huber_dd));
+      }
+    }
+    acc = dd_add(acc, c);
+    a.res_out[o] = make_float2(ru.hi + ru.lo, rv.hi + rv.lo);
+  }
+  // block reduction (fixed tree)
+  __shared__ float sh_hi[kCostThreads / 32], sh_lo[kCostThreads / 32];
+  acc = dd_warp_sum(acc);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { sh_hi[w] = acc.hi; sh_lo[w] = acc.lo; }
+  __syncthreads();
+  if (w == 0) {
+    dd v = (lane < (int)(blockDim.x >> 5)) ? dd_make(sh_hi[lane], sh_lo[lane]) : dd_make(0.0f, 0.0f);
+    v = dd_warp_sum(v);
+    if (lane == 0) a.partials[blockIdx.x] = dd_to_double(v);
+  }
+}
+
+// Sum n double partials with one CTA (fixed tree, float-float).
+__device__ double block_sum_partials(const double* part, int n) {
+  __shared__ float sh_hi[32], sh_lo[32];
+  dd acc = dd_make(0.0f, 0.0f);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc = dd_add(acc, dd_from_double(part[i]));
+  acc = dd_warp_sum(acc);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { sh_hi[w] = acc.hi; sh_lo[w] = acc.lo; }
+  __syncthreads();
+  double out = 0.0;
+  if (w == 0) {
+    dd v = (lane < (int)(blockDim.x >> 5)) ? dd_make(sh_hi[lane], sh_lo[lane]) : dd_make(0.0f, 0.0f);
+    v = dd_warp_sum(v);
+    out = dd_to_double(v);
+  }
+  __syncthreads();
+  return out;  // valid in warp 0
+}
+
+__global__ void k_init_merit(const double* part, int n, Ctrl* ctrl) {
+  double s = block_sum_partials(part, n);
+  if (threadIdx.x == 0) {
+    ctrl->merit = s;
+    ctrl->new_merit = s;
+  }
+}
+
+__global__ void k_iter_begin(Ctrl* ctrl) {
+  if (halted(ctrl)) return;
+  ctrl->skip = 0;
+  ctrl->accept = 0;
+  ctrl->max_grad_bits = 0ull;
+  ctrl->max_step_bits = 0ull;
+  ctrl->alpha = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Landmark pass: one warp per marginalized point.  Builds the point block
+// V_i = sum J_pt^T J_pt (+ nu * n_terms I), its gradient, the 3x3 Cholesky
+// factor C and Z_g = W_g C^-T for every term g of the point, where
+// W_g = J_pose^T J_pt.  Then the Schur complement contribution of the point
+// is sum_{a,b} Z_a Z_b^T and its rhs contribution Z_a (C^-1 b_m)
+// (compute_marg_block_contrib, crates/sophus_solver/src/ldlt/schur_ldlt.rs:82-135).
+// ---------------------------------------------------------------------------
+struct LinArgs {
+  int32_t np;
+  const int64_t* pt_g_begin;
+  const int64_t* g_begin;
+  const int32_t* g_pose;
+  const int32_t* pose_fb;
+  const int32_t* pt_mb;
+  const double* cnt_m;
+  const float* pose_f;
+  const double* points;
+  const float2* res;
+  float fx, fy, huber;
+  float* zmat;
+  double* cinv;
+  double* cvec;
+  double* bm;
+  double nu_override;
+  int use_override;
+  int* fail;
+};
+
+__global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
+  if (halted(ctrl)) return;
+  const int lane = threadIdx.x & 31;
+  const int warps_per_block = blockDim.x >> 5;
+  const double nu = a.use_override ? a.nu_override : ctrl->nu;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * warps_per_block + (threadIdx.x >> 5); i < a.np;
+       i += static_cast<int64_t>(gridDim.x) * warps_per_block) {
+    const int mb = a.pt_mb[i];
+    if (mb < 0) continue;  // constant point: no H_mm block
+    const float px = __double2float_rn(a.points[3 * i + 0]);
+    const float py = __double2float_rn(a.points[3 * i + 1]);
+    const float pz = __double2float_rn(a.points[3 * i + 2]);
+    const int64_t g0 = a.pt_g_begin[i], g1 = a.pt_g_begin[i + 1];
+    dd V[6], G[3];
+    for (int k = 0; k < 6; ++k) V[k] = dd_make(0.f, 0.f);
+    for (int k = 0; k < 3; ++k) G[k] = dd_make(0.f, 0.f);
+    // pass 1: V and g_m
+    for (int64_t g = g0 + lane; g < g1; g += 32) {
+      const float* P = a.pose_f + 12 * a.g_pose[g];
+      float v[6] = {0, 0, 0, 0, 0, 0}, gm[3] = {0, 0, 0};
+      for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+        JacF J;
+        jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+        float2 r = a.res[o];
+        float w = huber_weight_f(a.huber, r.x, r.y);
+        float r0 = w * r.x, r1 = w * r.y;
+        const float* m = J.jm;
+        v[0] += m[0] * m[0] + m[3] * m[3];
+        v[1] += m[0] * m[1] + m[3] * m[4];
+        v[2] += m[0] * m[2] + m[3] * m[5];
+        v[3] += m[1] * m[1] + m[4] * m[4];
+        v[4] += m[1] * m[2] + m[4] * m[5];
+        v[5] += m[2] * m[2] + m[5] * m[5];
+        gm[0] += m[0] * r0 + m[3] * r1;
+        gm[1] += m[1] * r0 + m[4] * r1;
+        gm[2] += m[2] * r0 + m[5] * r1;
+      }
+      for (int k = 0; k < 6; ++k) V[k] = dd_add_f(V[k], v[k]);
+      for (int k = 0; k < 3; ++k) G[k] = dd_add_f(G[k], gm[k]);
+    }
+    for (int k = 0; k < 6; ++k) V[k] = dd_warp_sum(V[k]);
+    for (int k = 0; k < 3; ++k) G[k] = dd_warp_sum(G[k]);
+    // damping nu * (number of reduced terms) on the diagonal
+    dd damp = dd_from_double(nu * a.cnt_m[mb]);
+    V[0] = dd_add(V[0], damp);
+    V[3] = dd_add(V[3], damp);
+    V[5] = dd_add(V[5], damp);
+    dd b[3] = {dd_neg(G[0]), dd_neg(G[1]), dd_neg(G[2])};  // neg_grad
+    // Cholesky V' = C C^T  (V layout: 00 01 02 11 12 22)
+    bool ok = V[0].hi > 0.0f;
+    dd c00 = dd_sqrt(V[0]);
+    dd c10 = dd_div(V[1], c00), c20 = dd_div(V[2], c00);
+    dd t11 = dd_sub(V[3], dd_mul(c10, c10));
+    ok = ok && t11.hi > 0.0f;
+    dd c11 = dd_sqrt(t11);
+    dd c21 = dd_div(dd_sub(V[4], dd_mul(c20, c10)), c11);
+    dd t22 = dd_sub(dd_sub(V[5], dd_mul(c20, c20)), dd_mul(c21, c21));
+    ok = ok && t22.hi > 0.0f;
+    dd c22 = dd_sqrt(t22);
+    ok = ok && isfinite(c00.hi) && isfinite(c11.hi) && isfinite(c22.hi) && isfinite(c10.hi) &&
+         isfinite(c20.hi) && isfinite(c21.hi);
+    if (!ok) {
+      if (lane == 0 && !a.use_override) atomicExch(a.fail, 1);
+      continue;
+    }
+    // C^-1 (lower)
+    dd one = dd_make(1.0f, 0.0f);
+    dd i00 = dd_div(one, c00), i11 = dd_div(one, c11), i22 = dd_div(one, c22);
+    dd i10 = dd_neg(dd_div(dd_mul(c10, i00), c11));
+    dd i21 = dd_neg(dd_div(dd_mul(c21, i11), c22));
+    dd i20 = dd_neg(dd_div(dd_add(dd_mul(c20, i00), dd_mul(c21, i10)), c22));
+    // c = C^-1 b
+    dd cv0 = dd_mul(i00, b[0]);
+    dd cv1 = dd_add(dd_mul(i10, b[0]), dd_mul(i11, b[1]));
+    dd cv2 = dd_add(dd_add(dd_mul(i20, b[0]), dd_mul(i21, b[1])), dd_mul(i22, b[2]));
+    if (lane == 0) {
+      double* ci = a.cinv + 6 * mb;
+      ci[0] = dd_to_double(i00); ci[1] = dd_to_double(i10); ci[2] = dd_to_double(i11);
+      ci[3] = dd_to_double(i20); ci[4] = dd_to_double(i21); ci[5] = dd_to_double(i22);
+      double* cvp = a.cvec + 3 * mb;
+      cvp[0] = dd_to_double(cv0); cvp[1] = dd_to_double(cv1); cvp[2] = dd_to_double(cv2);
+      double* bp = a.bm + 3 * mb;
+      bp[0] = dd_to_double(b[0]); bp[1] = dd_to_double(b[1]); bp[2] = dd_to_double(b[2]);
+      double mg = fmax(fabs(bp[0]), fmax(fabs(bp[1]), fabs(bp[2])));
+      atomic_max_nonneg(&ctrl->max_grad_bits, mg);
+    }
+    if (a.use_override) continue;  // final Hessian pass: no Schur data
+    // pass 2: Z_g = W_g C^-T for terms with a free pose
+    for (int64_t g = g0 + lane; g < g1; g += 32) {
+      const int pj = a.g_pose[g];
+      if (a.pose_fb[pj] < 0) continue;
+      const float* P = a.pose_f + 12 * pj;
+      float W[18];
+      for (int k = 0; k < 18; ++k) W[k] = 0.f;
+      for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+        JacF J;
+        jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+        for (int r = 0; r < 6; ++r)
+          for (int s = 0; s < 3; ++s) W[r * 3 + s] += J.jp[r] * J.jm[s] + J.jp[6 + r] * J.jm[3 + s];
+      }
+      // Z[r][t] = sum_{s<=t} W[r][s] * Cinv[t][s]
+      float* Z = a.zmat + 18 * g;
+      for (int r = 0; r < 6; ++r) {
+        dd z0 = dd_mul_f(i00, W[r * 3 + 0]);
+        dd z1 = dd_add(dd_mul_f(i10, W[r * 3 + 0]), dd_mul_f(i11, W[r * 3 + 1]));
+        dd z2 = dd_add(dd_add(dd_mul_f(i20, W[r * 3 + 0]), dd_mul_f(i21, W[r * 3 + 1])),
+                       dd_mul_f(i22, W[r * 3 + 2]));
+        Z[r * 3 + 0] = z0.hi + z0.lo;
+        Z[r * 3 + 1] = z1.hi + z1.lo;
+        Z[r * 3 + 2] = z2.hi + z2.lo;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Camera pass: one CTA per tile of terms of one free pose.  Accumulates
+// U_j = sum J_pose^T J_pose (21 upper entries), g_j = sum J_pose^T r~ and the
+// reduced-rhs term sum Z_g (C^-1 b_m).
+// ---------------------------------------------------------------------------
+constexpr int kTileThreads = 256;
+constexpr int kTileVals = 33;
+
+struct CamArgs {
+  const int32_t* tile_fb;
+  const int64_t* tile_begin;
+  const int64_t* tile_end;
+  const int64_t* cam_g;
+  const int64_t* g_begin;
+  const int32_t* g_pt;
+  const int32_t* fb_pose;
+  const int32_t* pt_mb;
+  const float* pose_f;
+  const double* points;
+  const float2* res;
+  const float* zmat;
+  const double* cvec;
+  float fx, fy, huber;
+  double* tile_part;
+  int with_schur;
+};
+
+__global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const Ctrl* ctrl) {
+  if (halted(ctrl)) return;
+  const int tile = blockIdx.x;
+  const int fb = a.tile_fb[tile];
+  const float* P = a.pose_f + 12 * a.fb_pose[fb];
+  float u[21], gp[6];
+  for (int k = 0; k < 21; ++k) u[k] = 0.f;
+  for (int k = 0; k < 6; ++k) gp[k] = 0.f;
+  dd zcd[6];
+  for (int k = 0; k < 6; ++k) zcd[k] = dd_make(0.f, 0.f);
+  const int64_t e = a.tile_begin[tile] + threadIdx.x;
+  if (e < a.tile_end[tile]) {
+    const int64_t g = a.cam_g[e];
+    const int pi = a.g_pt[g];
+    const float px = __double2float_rn(a.points[3 * pi + 0]);
+    const float py = __double2float_rn(a.points[3 * pi + 1]);
+    const float pz = __double2float_rn(a.points[3 * pi + 2]);
+    for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+      JacF J;
+      jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+      float2 r = a.res[o];
+      float w = huber_weight_f(a.huber, r.x, r.y);
+      float r0 = w * r.x, r1 = w * r.y;
+      int k = 0;
+      for (int p = 0; p < 6; ++p) {
+        for (int q = p; q < 6; ++q) u[k++] += J.jp[p] * J.jp[q] + J.jp[6 + p] * J.jp[6 + q];
+        gp[p] += J.jp[p] * r0 + J.jp[6 + p] * r1;
+      }
+    }
+    const int mb = a.pt_mb[pi];
+    if (a.with_schur && mb >= 0) {
+      const float* Z = a.zmat + 18 * g;
+      dd c0 = dd_from_double(a.cvec[3 * mb + 0]);
+      dd c1 = dd_from_double(a.cvec[3 * mb + 1]);
+      dd c2 = dd_from_double(a.cvec[3 * mb + 2]);
+      for (int r = 0; r < 6; ++r)
+        zcd[r] = dd_add(dd_add(dd_mul_f(c0, Z[r * 3 + 0]), dd_mul_f(c1, Z[r * 3 + 1])),
+                        dd_mul_f(c2, Z[r * 3 + 2]));
+    }
+  }
+  __shared__ float sh_hi[kTileVals][kTileThreads / 32];
+  __shared__ float sh_lo[kTileVals][kTileThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int k = 0; k < kTileVals; ++k) {
+    dd v = (k < 21) ? dd_from_float(u[k]) : (k < 27 ? dd_from_float(gp[k - 21]) : zcd[k - 27]);
+    v = dd_warp_sum(v);
+    if (lane == 0) { sh_hi[k][w] = v.hi; sh_lo[k][w] = v.lo; }
+  }
+  __syncthreads();
+  if (threadIdx.x < kTileVals) {
+    const int k = threadIdx.x;
+    dd v = dd_make(0.f, 0.f);
+    for (int q = 0; q < kTileThreads / 32; ++q) v = dd_add(v, dd_make(sh_hi[k][q], sh_lo[k][q]));
+    a.tile_part[static_cast<int64_t>(tile) * kTileVals + k] = dd_to_double(v);
+  }
+}
+
+__global__ void k_camera_finalize(int nf, const int64_t* fb_tile_begin, const double* tile_part,
+                                  double* ufull, double* bf, double* rb, Ctrl* ctrl, int with_schur) {
+  if (halted(ctrl)) return;
+  const int fb = blockIdx.x * blockDim.x + threadIdx.x;
+  if (fb >= nf) return;
+  dd acc[kTileVals];
+  for (int k = 0; k < kTileVals; ++k) acc[k] = dd_make(0.f, 0.f);
+  for (int64_t t = fb_tile_begin[fb]; t < fb_tile_begin[fb + 1]; ++t)
+    for (int k = 0; k < kTileVals; ++k) acc[k] = dd_add(acc[k], dd_from_double(tile_part[t * kTileVals + k]));
+  double* U = ufull + 36 * fb;
+  int k = 0;
+  for (int p = 0; p < 6; ++p)
+    for (int q = p; q < 6; ++q) {
+      double v = dd_to_double(acc[k++]);
+      U[p * 6 + q] = v;
+      U[q * 6 + p] = v;
+    }
+  double mg = 0.0;
+  for (int p = 0; p < 6; ++p) {
+    dd b = dd_neg(acc[21 + p]);
+    bf[6 * fb + p] = dd_to_double(b);
+    mg = fmax(mg, fabs(bf[6 * fb + p]));
+    if (with_schur) rb[6 * fb + p] = dd_to_double(dd_sub(b, acc[27 + p]));
+  }
+  atomic_max_nonneg(&ctrl->max_grad_bits, mg);
+}
+
+// Gradient-tolerance check before the solve (optimizer_step.rs:382-384) and
+// singular-point-block detection (SingularMargBlock -> reject).
+__global__ void k_gradcheck(Ctrl* ctrl, int* fail) {
+  if (halted(ctrl)) return;
+  double mg = __longlong_as_double(static_cast<long long>(ctrl->max_grad_bits));
+  ctrl->max_grad = mg;
+  if (mg < ctrl->gtol) {
+    ctrl->skip = 1;
+  } else if (*fail) {
+    ctrl->skip = 2;
+  }
+  *fail = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Reduced camera system: one warp per lower 6x6 block (row j >= col k).
+//   S_jk = [j == k] (U_j + nu n_j I) - sum_{pairs} Z_a Z_b^T
+// FP32 products, float-float accumulation, f64 store (both triangles).
+// ---------------------------------------------------------------------------
+struct SchurArgs {
+  int64_t nsb;
+  const int32_t* sb_row;
+  const int32_t* sb_col;
+  const int64_t* sb_pair_begin;
+  const int2* pairs;
+  const float* zmat;
+  const double* ufull;
+  const double* cnt_f;
+  double* S;
+  int n6;
+};
+
+__global__ void __launch_bounds__(256) k_schur(SchurArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  const double nu = ctrl->nu;
+  for (int64_t blk = static_cast<int64_t>(blockIdx.x) * wpb + (threadIdx.x >> 5); blk < a.nsb;
+       blk += static_cast<int64_t>(gridDim.x) * wpb) {
+    const int j = a.sb_row[blk], k = a.sb_col[blk];
+    dd acc[36];
+#pragma unroll
+    for (int e = 0; e < 36; ++e) acc[e] = dd_make(0.f, 0.f);
+    for (int64_t q = a.sb_pair_begin[blk] + lane; q < a.sb_pair_begin[blk + 1]; q += 32) {
+      const int2 pr = a.pairs[q];
+      const float* Za = a.zmat + 18 * static_cast<int64_t>(pr.x);
+      const float* Zb = a.zmat + 18 * static_cast<int64_t>(pr.y);
+      float za[18], zb[18];
+#pragma unroll
+      for (int e = 0; e < 18; e += 2) {
+        float2 x = *reinterpret_cast<const float2*>(Za + e);
+        float2 y = *reinterpret_cast<const float2*>(Zb + e);
+        za[e] = x.x; za[e + 1] = x.y;
+        zb[e] = y.x; zb[e + 1] = y.y;
+      }
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+          float p = za[r * 3 + 0] * zb[c * 3 + 0];
+          p = fmaf(za[r * 3 + 1], zb[c * 3 + 1], p);
+          p = fmaf(za[r * 3 + 2], zb[c * 3 + 2], p);
+          acc[r * 6 + c] = dd_add_f(acc[r * 6 + c], p);
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < 36; ++e) acc[e] = dd_warp_sum(acc[e]);
+    {
+      // every lane holds the 36 totals; lane e writes entries e and e + 32
+      for (int e = lane; e < 36; e += 32) {
+        const int r = e / 6, c = e % 6;
+        double v = -dd_to_double(acc[e]);
+        if (j == k) {
+          dd base = dd_from_double(a.ufull[36 * j + r * 6 + c]);
+          if (r == c) base = dd_add(base, dd_from_double(nu * a.cnt_f[j]));
+          v = dd_to_double(dd_sub(base, acc[e]));
+        }
+        const int64_t row = 6 * j + r, col = 6 * k + c;
+        a.S[row * a.n6 + col] = v;
+        a.S[col * a.n6 + row] = v;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Back-substitution (SchurFactor::solve, schur_ldlt.rs:782-803):
+//   dx_m = V'^-1 (b_m - sum W_g^T dx_f) = C^-T (c - sum Z_g^T dx_f)
+// ---------------------------------------------------------------------------
+struct BackArgs {
+  int32_t np;
+  const int64_t* pt_g_begin;
+  const int32_t* g_pose;
+  const int32_t* pose_fb;
+  const int32_t* pt_mb;
+  const float* zmat;
+  const double* cinv;
+  const double* cvec;
+  const double* xf;
+  double* dm;
+};
+
+__global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * wpb + (threadIdx.x >> 5); i < a.np;
+       i += static_cast<int64_t>(gridDim.x) * wpb) {
+    const int mb = a.pt_mb[i];
+    if (mb < 0) continue;
+    dd t[3] = {dd_make(0.f, 0.f), dd_make(0.f, 0.f), dd_make(0.f, 0.f)};
+    for (int64_t g = a.pt_g_begin[i] + lane; g < a.pt_g_begin[i + 1]; g += 32) {
+      const int fb = a.pose_fb[a.g_pose[g]];
+      if (fb < 0) continue;
+      const float* Z = a.zmat + 18 * g;
+      for (int r = 0; r < 6; ++r) {
+        dd x = dd_from_double(a.xf[6 * fb + r]);
+        for (int s = 0; s < 3; ++s) t[s] = dd_add(t[s], dd_mul_f(x, Z[r * 3 + s]));
+      }
+    }
+    for (int s = 0; s < 3; ++s) t[s] = dd_warp_sum(t[s]);
+    if (lane == 0) {
+      dd c0 = dd_sub(dd_from_double(a.cvec[3 * mb + 0]), t[0]);
+      dd c1 = dd_sub(dd_from_double(a.cvec[3 * mb + 1]), t[1]);
+      dd c2 = dd_sub(dd_from_double(a.cvec[3 * mb + 2]), t[2]);
+      const double* ci = a.cinv + 6 * mb;  // 00 10 11 20 21 22
+      dd i00 = dd_from_double(ci[0]), i10 = dd_from_double(ci[1]), i11 = dd_from_double(ci[2]);
+      dd i20 = dd_from_double(ci[3]), i21 = dd_from_double(ci[4]), i22 = dd_from_double(ci[5]);
+      // C^-T * c : (C^-T)[a][b] = Cinv[b][a]
+      dd d0 = dd_add(dd_add(dd_mul(i00, c0), dd_mul(i10, c1)), dd_mul(i20, c2));
+      dd d1 = dd_add(dd_mul(i11, c1), dd_mul(i21, c2));
+      dd d2 = dd_mul(i22, c2);
+      a.dm[3 * mb + 0] = dd_to_double(d0);
+      a.dm[3 * mb + 1] = dd_to_double(d1);
+      a.dm[3 * mb + 2] = dd_to_double(d2);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Gauge projection.  With a single constant camera (center c) and no constant
+// points, s -> scale about c is an exact symmetry of the cost, so H v = 0 for
+// v = ([0; t_j - c] per free pose, p_i - c per point) and b . v = 0.  The exact
+// damped step therefore satisfies v^T D delta = 0, D = diag(n_terms).  The
+// FP32 assembly leaves a spurious component along v amplified by 1/(nu n);
+// removing the D-projection restores the exact-arithmetic step.
+// ---------------------------------------------------------------------------
+struct GaugeArgs {
+  int nf, nm;
+  const int32_t* fb_pose;
+  const int32_t* mb_pt;
+  const double* poses;
+  const double* points;
+  const double* cnt_f;
+  const double* cnt_m;
+  const double* xf;
+  const double* dm;
+  double cx, cy, cz;
+  double* part;  // 2 * gridDim
+};
+
+__global__ void __launch_bounds__(256) k_gauge_partials(GaugeArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  dd num = dd_make(0.f, 0.f), den = dd_make(0.f, 0.f);
+  const int64_t n = static_cast<int64_t>(a.nf) + a.nm;
+  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double v[3], d[3], w;
+    if (t < a.nf) {
+      const double* T = a.poses + 7 * a.fb_pose[t];
+      v[0] = T[4] - a.cx; v[1] = T[5] - a.cy; v[2] = T[6] - a.cz;
+      d[0] = a.xf[6 * t + 3]; d[1] = a.xf[6 * t + 4]; d[2] = a.xf[6 * t + 5];
+      w = a.cnt_f[t];
+    } else {
+      const int mb = static_cast<int>(t - a.nf);
+      const double* p = a.points + 3 * a.mb_pt[mb];
+      v[0] = p[0] - a.cx; v[1] = p[1] - a.cy; v[2] = p[2] - a.cz;
+      d[0] = a.dm[3 * mb]; d[1] = a.dm[3 * mb + 1]; d[2] = a.dm[3 * mb + 2];
+      w = a.cnt_m[mb];
+    }
+    dd wd = dd_from_double(w);
+    for (int k = 0; k < 3; ++k) {
+      dd vk = dd_from_double(v[k]);
+      num = dd_add(num, dd_mul(dd_mul(wd, vk), dd_from_double(d[k])));
+      den = dd_add(den, dd_mul(dd_mul(wd, vk), vk));
+    }
+  }
+  __shared__ float sh[4][8];
+  num = dd_warp_sum(num);
+  den = dd_warp_sum(den);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { sh[0][w] = num.hi; sh[1][w] = num.lo; sh[2][w] = den.hi; sh[3][w] = den.lo; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    dd s0 = dd_make(0.f, 0.f), s1 = dd_make(0.f, 0.f);
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+      s0 = dd_add(s0, dd_make(sh[0][q], sh[1][q]));
+      s1 = dd_add(s1, dd_make(sh[2][q], sh[3][q]));
+    }
+    a.part[2 * blockIdx.x] = dd_to_double(s0);
+    a.part[2 * blockIdx.x + 1] = dd_to_double(s1);
+  }
+}
+
+__global__ void k_gauge_alpha(const double* part, int nblocks, Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  __shared__ double sn, sd;
+  if (threadIdx.x == 0) {
+    dd n = dd_make(0.f, 0.f), d = dd_make(0.f, 0.f);
+    for (int q = 0; q < nblocks; ++q) {
+      n = dd_add(n, dd_from_double(part[2 * q]));
+      d = dd_add(d, dd_from_double(part[2 * q + 1]));
+    }
+    sn = dd_to_double(n);
+    sd = dd_to_double(d);
+    ctrl->alpha = (sd > 0.0) ? sn / sd : 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Apply the (projected) step: trial poses exp(delta) * T, trial points p + d
+// (VarFamilies::update, crates/sophus_opt/src/variables/var_families.rs:203-209);
+// partial sums of delta.delta and delta.neg_grad for the gain ratio and max |delta|.
+// ---------------------------------------------------------------------------
+struct UpdArgs {
+  int nc, np, nf, nm;
+  const int32_t* pose_fb;
+  const int32_t* pt_mb;
+  const double* poses;
+  const double* points;
+  double* poses_t;
+  double* points_t;
+  double* xf;   // projected in place
+  double* dm;   // projected in place
+  const double* bf;
+  const double* bm;
+  int gauge_kind;
+  double cx, cy, cz;
+  double* part;  // 2 * gridDim
+};
+
+__global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  const double alpha = (a.gauge_kind == 1) ? ctrl->alpha : 0.0;
+  dd sdd = dd_make(0.f, 0.f), sdg = dd_make(0.f, 0.f);
+  double mx = 0.0;
+  const int64_t n = static_cast<int64_t>(a.nc) + a.np;
+  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (t < a.nc) {
+      const int j = static_cast<int>(t);
+      const double* T = a.poses + 7 * j;
+      double* O = a.poses_t + 7 * j;
+      const int fb = a.pose_fb[j];
+      if (fb < 0) {
+        for (int k = 0; k < 7; ++k) O[k] = T[k];
+        continue;
+      }
+      double xi[6];
+      for (int k = 0; k < 6; ++k) xi[k] = a.xf[6 * fb + k];
+      xi[3] -= alpha * (T[4] - a.cx);
+      xi[4] -= alpha * (T[5] - a.cy);
+      xi[5] -= alpha * (T[6] - a.cz);
+      for (int k = 0; k < 6; ++k) {
+        a.xf[6 * fb + k] = xi[k];
+        dd x = dd_from_double(xi[k]);
+        sdd = dd_add(sdd, dd_mul(x, x));
+        sdg = dd_add(sdg, dd_mul(x, dd_from_double(a.bf[6 * fb + k])));
+        mx = fmax(mx, fabs(xi[k]));
+      }
+      se3_left_update(xi, T, O);
+    } else {
+      const int i = static_cast<int>(t - a.nc);
+      const double* p = a.points + 3 * i;
+      double* O = a.points_t + 3 * i;
+      const int mb = a.pt_mb[i];
+      if (mb < 0) {
+        O[0] = p[0]; O[1] = p[1]; O[2] = p[2];
+        continue;
+      }
+      double d[3] = {a.dm[3 * mb] - alpha * (p[0] - a.cx), a.dm[3 * mb + 1] - alpha * (p[1] - a.cy),
+                     a.dm[3 * mb + 2] - alpha * (p[2] - a.cz)};
+      for (int k = 0; k < 3; ++k) {
+        a.dm[3 * mb + k] = d[k];
+        dd x = dd_from_double(d[k]);
+        sdd = dd_add(sdd, dd_mul(x, x));
+        sdg = dd_add(sdg, dd_mul(x, dd_from_double(a.bm[3 * mb + k])));
+        mx = fmax(mx, fabs(d[k]));
+        O[k] = p[k] + d[k];
+      }
+    }
+  }
+  atomic_max_nonneg(&ctrl->max_step_bits, mx);
+  __shared__ float sh[4][8];
+  sdd = dd_warp_sum(sdd);
+  sdg = dd_warp_sum(sdg);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { sh[0][w] = sdd.hi; sh[1][w] = sdd.lo; sh[2][w] = sdg.hi; sh[3][w] = sdg.lo; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    dd s0 = dd_make(0.f, 0.f), s1 = dd_make(0.f, 0.f);
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+      s0 = dd_add(s0, dd_make(sh[0][q], sh[1][q]));
+      s1 = dd_add(s1, dd_make(sh[2][q], sh[3][q]));
+    }
+    a.part[2 * blockIdx.x] = dd_to_double(s0);
+    a.part[2 * blockIdx.x + 1] = dd_to_double(s1);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// LM decision (step_nlls_inner, crates/sophus_opt/src/nlls/optimizer_step.rs:366-437;
+// accept/reject optimizer.rs:463-480; gain ratio optimizer_helpers.rs:159-173).
+// ---------------------------------------------------------------------------
+__global__ void k_decide(const double* cost_part, int n_cost, const double* upd_part, int n_upd,
+                         Ctrl* ctrl, Record* recs, Record* last) {
+  if (halted(ctrl)) return;
+  const int skip = ctrl->skip;
+  double new_merit = 0.0;
+  if (skip == 0) new_merit = block_sum_partials(cost_part, n_cost);
+  __shared__ double s_dd, s_dg;
+  if (skip == 0 && threadIdx.x == 0) {
+    dd a = dd_make(0.f, 0.f), b = dd_make(0.f, 0.f);
+    for (int q = 0; q < n_upd; ++q) {
+      a = dd_add(a, dd_from_double(upd_part[2 * q]));
+      b = dd_add(b, dd_from_double(upd_part[2 * q + 1]));
+    }
+    s_dd = dd_to_double(a);
+    s_dg = dd_to_double(b);
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const double nan = __longlong_as_double(0x7ff8000000000000ll);
+  Record rec;
+  rec.new_merit = nan;
+  rec.gain_ratio = nan;
+  rec.max_step = nan;
+  rec.accepted = 0;
+  rec.max_grad = ctrl->max_grad;
+  int reason = 0;
+  ctrl->accept = 0;
+  if (skip == 1) {
+    reason = 1 + 1;  // GradientTolerance
+  } else if (skip == 2) {
+    ctrl->nu *= 2.0;  // handle_solve_failure -> reject_step
+    ctrl->rejects += 1;
+    if (ctrl->rejects >= ctrl->max_rejects) reason = 5;
+  } else {
+    const double merit = ctrl->merit;
+    const double max_step = __longlong_as_double(static_cast<long long>(ctrl->max_step_bits));
+    rec.new_merit = new_merit;
+    rec.max_step = max_step;
+    ctrl->new_merit = new_merit;
+    ctrl->max_step = max_step;
+    ctrl->dd_sum = s_dd;
+    ctrl->dg_sum = s_dg;
+    if (max_step < ctrl->ptol) {
+      if (new_merit < merit) {
+        ctrl->accept = 1;
+        ctrl->merit = new_merit;
+        rec.accepted = 1;
+      }
+      reason = 3;  // ParameterTolerance
+    } else {
+      const double predicted = ctrl->nu * s_dd + s_dg;
+      const double actual = merit - new_merit;
+      const double min_pos = 2.2250738585072014e-308;
+      double rho = (fabs(predicted) > min_pos) ? actual / predicted : (actual > 0.0 ? 1.0 : 0.0);
+      rec.gain_ratio = rho;
+      ctrl->gain_ratio = rho;
+      if (rho > 0.0 && new_merit < merit) {
+        double x = 2.0 * rho - 1.0;
+        double f = 1.0 - x * x * x;
+        ctrl->nu *= fmax(f, 1.0 / 3.0);
+        ctrl->rejects = 0;
+        double rel = (merit - new_merit) / (fabs(merit) + min_pos);
+        if (rel < ctrl->ftol) reason = 1;  // FunctionTolerance
+        ctrl->accept = 1;
+        ctrl->merit = new_merit;
+        rec.accepted = 1;
+      } else {
+        ctrl->nu *= 2.0;
+        ctrl->rejects += 1;
+        if (ctrl->rejects >= ctrl->max_rejects) reason = 5;
+      }
+    }
+  }
+  ctrl->step += 1;
+  if (ctrl->step >= ctrl->num_iterations && reason == 0) reason = 4;  // MaxIterations
+  rec.merit = ctrl->merit;
+  rec.lm_damping = ctrl->nu;
+  rec.termination = reason;
+  ctrl->termination = reason;
+  if (ctrl->step - 1 < ctrl->record_cap) recs[ctrl->step - 1] = rec;
+  *last = rec;
+  if (reason != 0) ctrl->done = 1;
+}
+
+// Accepted step: trial state becomes the current state.
+__global__ void k_commit(int nc, int np, int64_t no, const double* poses_t, double* poses,
+                         const double* points_t, double* points, const float2* res_t, float2* res,
+                         const Ctrl* ctrl) {
+  if (!ctrl->accept) return;
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  const int64_t t0 = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  for (int64_t t = t0; t < no; t += stride) res[t] = res_t[t];
+  for (int64_t t = t0; t < 7 * static_cast<int64_t>(nc); t += stride) poses[t] = poses_t[t];
+  for (int64_t t = t0; t < 3 * static_cast<int64_t>(np); t += stride) points[t] = points_t[t];
+}
+
+int cost_grid(int64_t no) {
+  int64_t b = (no + kCostThreads - 1) / kCostThreads;
+  if (b < 1) b = 1;
+  if (b > kCostMaxBlocks) b = kCostMaxBlocks;
+  return static_cast<int>(b);
+}
+
+int warp_grid(int64_t items, int warps_per_block, int cap) {
+  int64_t b = (items + warps_per_block - 1) / warps_per_block;
+  if (b < 1) b = 1;
+  if (b > cap) b = cap;
+  return static_cast<int>(b);
+}
+
+constexpr int kUpdBlocks = 152;
+
+}  // namespace
+
+int cost_partials_needed(const Sizes& s) { return 4 * kUpdBlocks + cost_grid(s.no); }
+
+int launch_pose_tables(const Sizes& s, const Dev& d, const double* poses, cudaStream_t st) {
+  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, poses, d.pose_f, d.pose_dd, d.ctrl, 0);
+  return 1;
+}
+
+static CostArgs make_cost_args(const Sizes& s, const Dev& d, const double* points, float2* res_out,
+                               double* partials, int respect_skip) {
+  CostArgs a;
+  a.no = s.no;
+  a.uv = d.obs_uv;
+  a.opose = d.obs_pose;
+  a.opt = d.obs_pt;
+  a.pose_dd = d.pose_dd;
+  a.points = points;
+  a.res_out = res_out;
+  a.partials = partials;
+  a.fx = dd_make(static_cast<float>(s.intr[0]), static_cast<float>(s.intr[0] - static_cast<float>(s.intr[0])));
+  a.fy = dd_make(static_cast<float>(s.intr[1]), static_cast<float>(s.intr[1] - static_cast<float>(s.intr[1])));
+  a.cx = dd_make(static_cast<float>(s.intr[2]), static_cast<float>(s.intr[2] - static_cast<float>(s.intr[2])));
+  a.cy = dd_make(static_cast<float>(s.intr[3]), static_cast<float>(s.intr[3] - static_cast<float>(s.intr[3])));
+  a.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
+  a.huber_dd = dd_make(static_cast<float>(s.huber), static_cast<float>(s.huber - static_cast<float>(s.huber)));
+  a.respect_skip = respect_skip;
+  return a;
+}
+
+int launch_cost(const Sizes& s, const Dev& d, const double* poses, const double* points,
+                float2* res_out, double* partials, cudaStream_t st) {
+  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, poses, d.pose_f, d.pose_dd, d.ctrl, 1);
+  CostArgs a = make_cost_args(s, d, points, res_out, partials, 1);
+  k_cost<<<cost_grid(s.no), kCostThreads, 0, st>>>(a, d.ctrl);
+  return 2;
+}
+
+int launch_init_merit(const Sizes& s, const Dev& d, cudaStream_t st) {
+  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses, d.pose_f, d.pose_dd, d.ctrl, 0);
+  CostArgs a = make_cost_args(s, d, d.points, d.res, d.part, 0);
+  const int nb = cost_grid(s.no);
+  k_cost<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
+  k_init_merit<<<1, 256, 0, st>>>(d.part, nb, d.ctrl);
+  return 3;
+}
+
+int launch_iteration_begin(const Sizes& s, const Dev& d, cudaStream_t st) {
+  (void)s;
+  k_iter_begin<<<1, 1, 0, st>>>(d.ctrl);
+  return 1;
+}
+
+int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_override,
+                     cudaStream_t st) {
+  int n = 0;
+  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses, d.pose_f, d.pose_dd, d.ctrl, 0);
+  ++n;
+  LinArgs la;
+  la.np = s.np;
+  la.pt_g_begin = d.pt_g_begin;
+  la.g_begin = d.g_begin;
+  la.g_pose = d.g_pose;
+  la.pose_fb = d.pose_fb;
+  la.pt_mb = d.pt_mb;
+  la.cnt_m = d.cnt_m;
+  la.pose_f = d.pose_f;
+  la.points = d.points;
+  la.res = d.res;
+  la.fx = static_cast<float>(s.intr[0]);
+  la.fy = static_cast<float>(s.intr[1]);
+  la.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
+  la.zmat = d.zmat;
+  la.cinv = d.cinv;
+  la.cvec = d.cvec;
+  la.bm = d.bm;
+  la.nu_override = nu_override;
+  la.use_override = use_override ? 1 : 0;
+  la.fail = &d.ctrl->fail;
+  k_landmark<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(la, d.ctrl);
+  ++n;
+  if (s.ntiles > 0) {
+    CamArgs ca;
+    ca.tile_fb = d.tile_fb;
+    ca.tile_begin = d.tile_begin;
+    ca.tile_end = d.tile_end;
+    ca.cam_g = d.cam_g;
+    ca.g_begin = d.g_begin;
+    ca.g_pt = d.g_pt;
+    ca.fb_pose = d.fb_pose;
+    ca.pt_mb = d.pt_mb;
+    ca.pose_f = d.pose_f;
+    ca.points = d.points;
+    ca.res = d.res;
+    ca.zmat = d.zmat;
+    ca.cvec = d.cvec;
+    ca.fx = la.fx;
+    ca.fy = la.fy;
+    ca.huber = la.huber;
+    ca.tile_part = d.tile_part;
+    ca.with_schur = use_override ? 0 : 1;
+    k_camera_tiles<<<static_cast<unsigned>(s.ntiles), kTileThreads, 0, st>>>(ca, d.ctrl);
+    ++n;
+  }
+  k_camera_finalize<<<(s.nf + 63) / 64, 64, 0, st>>>(s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf,
+                                                     d.rb, d.ctrl, use_override ? 0 : 1);
+  ++n;
+  if (!use_override) {
+    k_gradcheck<<<1, 1, 0, st>>>(d.ctrl, &d.ctrl->fail);
+    ++n;
+  }
+  return n;
+}
+
+int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
+  SchurArgs a;
+  a.nsb = s.nsb;
+  a.sb_row = d.sb_row;
+  a.sb_col = d.sb_col;
+  a.sb_pair_begin = d.sb_pair_begin;
+  a.pairs = d.pairs;
+  a.zmat = d.zmat;
+  a.ufull = d.ufull;
+  a.cnt_f = d.cnt_f;
+  a.S = d.S;
+  a.n6 = s.n6;
+  k_schur<<<warp_grid(s.nsb, 8, 8192), 256, 0, st>>>(a, d.ctrl);
+  return 1;
+}
+
+int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
+  int n = 0;
+  BackArgs b;
+  b.np = s.np;
+  b.pt_g_begin = d.pt_g_begin;
+  b.g_pose = d.g_pose;
+  b.pose_fb = d.pose_fb;
+  b.pt_mb = d.pt_mb;
+  b.zmat = d.zmat;
+  b.cinv = d.cinv;
+  b.cvec = d.cvec;
+  b.xf = d.x;
+  b.dm = d.dm;
+  k_backsub<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(b, d.ctrl);
+  ++n;
+  if (s.gauge_kind == 1) {
+    GaugeArgs g;
+    g.nf = s.nf;
+    g.nm = s.nm;
+    g.fb_pose = d.fb_pose;
+    g.mb_pt = d.mb_pt;
+    g.poses = d.poses;
+    g.points = d.points;
+    g.cnt_f = d.cnt_f;
+    g.cnt_m = d.cnt_m;
+    g.xf = d.x;
+    g.dm = d.dm;
+    g.cx = s.gauge_center[0];
+    g.cy = s.gauge_center[1];
+    g.cz = s.gauge_center[2];
+    g.part = d.part;
+    k_gauge_partials<<<kUpdBlocks, 256, 0, st>>>(g, d.ctrl);
+    k_gauge_alpha<<<1, 32, 0, st>>>(d.part, kUpdBlocks, d.ctrl);
+    n += 2;
+  }
+  UpdArgs u;
+  u.nc = s.nc;
+  u.np = s.np;
+  u.nf = s.nf;
+  u.nm = s.nm;
+  u.pose_fb = d.pose_fb;
+  u.pt_mb = d.pt_mb;
+  u.poses = d.poses;
+  u.points = d.points;
+  u.poses_t = d.poses_t;
+  u.points_t = d.points_t;
+  u.xf = d.x;
+  u.dm = d.dm;
+  u.bf = d.bf;
+  u.bm = d.bm;
+  u.gauge_kind = s.gauge_kind;
+  u.cx = s.gauge_center[0];
+  u.cy = s.gauge_center[1];
+  u.cz = s.gauge_center[2];
+  u.part = d.part + 2 * kUpdBlocks;
+  k_apply_update<<<kUpdBlocks, 256, 0, st>>>(u, d.ctrl);
+  ++n;
+  return n;
+}
+
+int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
+  // trial cost (partials after the update partials)
+  double* cost_part = d.part + 4 * kUpdBlocks;
+  const int nb = cost_grid(s.no);
+  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses_t, d.pose_f, d.pose_dd, d.ctrl, 1);
+  CostArgs a = make_cost_args(s, d, d.points_t, d.res_t, cost_part, 1);
+  k_cost<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
+  k_decide<<<1, 256, 0, st>>>(cost_part, nb, d.part + 2 * kUpdBlocks, kUpdBlocks, d.ctrl, d.records,
+                              d.last_rec);
+  const int64_t big = s.no > 7 * (int64_t)s.nc ? s.no : 7 * (int64_t)s.nc;
+  const int64_t items = big > 3 * (int64_t)s.np ? big : 3 * (int64_t)s.np;
+  int cb = static_cast<int>((items + 255) / 256);
+  if (cb > 1216) cb = 1216;
+  if (cb < 1) cb = 1;
+  k_commit<<<cb, 256, 0, st>>>(s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res,
+                               d.ctrl);
+  return 4;
+}
+
+}  // namespace sgba

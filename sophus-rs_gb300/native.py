@@ -1,0 +1,318 @@
+"""ctypes binding of the C ABI in include/sgba.h (libsgba.so).
+
+The library is the product: there is no CPU fallback.  If libsgba.so is
+missing or cannot reach a CUDA device, every entry point raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "libsgba.so")
+_lib = None
+
+# sgba_status
+OK = 0
+ERR_INVALID_ARGUMENT = -1
+ERR_INVALID_PARAMS = -2
+ERR_SCHUR_MISSING_FREE_OR_MARG = -3
+ERR_UNSUPPORTED = -4
+ERR_CUDA = -5
+ERR_OUT_OF_MEMORY = -6
+ERR_STATE = -7
+ERR_DEVICE_TIMEOUT = -8
+
+# sgba_termination
+TERM_NONE = 0
+TERM_FUNCTION_TOLERANCE = 1
+TERM_GRADIENT_TOLERANCE = 2
+TERM_PARAMETER_TOLERANCE = 3
+TERM_MAX_ITERATIONS = 4
+TERM_MAX_CONSECUTIVE_REJECTS = 5
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [
+        ("n_cam", C.c_int32),
+        ("poses", C.POINTER(C.c_double)),
+        ("pose_const", C.POINTER(C.c_uint8)),
+        ("n_pt", C.c_int32),
+        ("points", C.POINTER(C.c_double)),
+        ("point_const", C.POINTER(C.c_uint8)),
+        ("intrinsics", C.c_double * 4),
+        ("n_obs", C.c_int64),
+        ("obs_cam", C.POINTER(C.c_int32)),
+        ("obs_pt", C.POINTER(C.c_int32)),
+        ("obs_uv", C.POINTER(C.c_double)),
+        ("huber_delta", C.c_double),
+    ]
+
+
+class OptParamsC(C.Structure):
+    _fields_ = [
+        ("num_iterations", C.c_int32),
+        ("initial_lm_damping", C.c_double),
+        ("function_tolerance", C.c_double),
+        ("gradient_tolerance", C.c_double),
+        ("parameter_tolerance", C.c_double),
+        ("max_consecutive_rejects", C.c_int64),
+        ("skip_final_hessian", C.c_int32),
+    ]
+
+
+class IterRecord(C.Structure):
+    _fields_ = [
+        ("merit", C.c_double),
+        ("new_merit", C.c_double),
+        ("lm_damping", C.c_double),
+        ("gain_ratio", C.c_double),
+        ("max_step", C.c_double),
+        ("max_grad", C.c_double),
+        ("accepted", C.c_int32),
+        ("termination", C.c_int32),
+    ]
+
+
+class Layout(C.Structure):
+    _fields_ = [
+        ("n_free_poses", C.c_int32),
+        ("n_marg_points", C.c_int32),
+        ("n_terms", C.c_int64),
+        ("n_h_blocks", C.c_int64),
+        ("n_s_blocks", C.c_int64),
+        ("n_schur_pairs", C.c_int64),
+    ]
+
+
+class Profile(C.Structure):
+    _fields_ = [
+        ("kernel_launches", C.c_int64),
+        ("ms_total", C.c_double),
+        ("ms_linearize", C.c_double),
+        ("ms_schur", C.c_double),
+        ("ms_factor", C.c_double),
+        ("ms_update", C.c_double),
+        ("ms_cost", C.c_double),
+    ]
+
+
+EXPORTED = [
+    "sgba_abi_version", "sgba_last_error", "sgba_problem_create", "sgba_problem_destroy",
+    "sgba_optimizer_init", "sgba_optimizer_step", "sgba_optimize", "sgba_get_variables",
+    "sgba_get_cost", "sgba_set_variables", "sgba_get_layout", "sgba_export_pattern",
+    "sgba_debug_last_system", "sgba_state_save", "sgba_state_load", "sgba_get_profile",
+    "sgba_set_profiling", "sgba_synth_generate", "sgba_synth_free",
+]
+
+
+class SgbaError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("sgba status %d: %s" % (status, message))
+        self.status = status
+        self.message = message
+
+
+def lib_path():
+    return _LIB_PATH
+
+
+def lib():
+    """Load libsgba.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise RuntimeError("libsgba.so is not built (%s); run `python __graft_entry__.py` first" % _LIB_PATH)
+    L = C.CDLL(_LIB_PATH)
+    dp = C.POINTER(C.c_double)
+    L.sgba_abi_version.restype = C.c_int32
+    L.sgba_last_error.argtypes = [C.c_char_p, C.c_size_t]
+    L.sgba_last_error.restype = C.c_size_t
+    L.sgba_problem_create.argtypes = [C.POINTER(ProblemDesc), C.c_int32, C.POINTER(C.c_void_p)]
+    L.sgba_problem_destroy.argtypes = [C.c_void_p]
+    L.sgba_optimizer_init.argtypes = [C.c_void_p, C.POINTER(OptParamsC)]
+    L.sgba_optimizer_step.argtypes = [C.c_void_p, C.POINTER(IterRecord)]
+    L.sgba_optimize.argtypes = [C.c_void_p, C.POINTER(OptParamsC), C.POINTER(IterRecord), C.c_int32,
+                                C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.sgba_get_variables.argtypes = [C.c_void_p, dp, dp]
+    L.sgba_set_variables.argtypes = [C.c_void_p, dp, dp]
+    L.sgba_get_cost.argtypes = [C.c_void_p, dp]
+    L.sgba_get_layout.argtypes = [C.c_void_p, C.POINTER(Layout)]
+    ip = C.POINTER(C.c_int32)
+    L.sgba_export_pattern.argtypes = [C.c_void_p, ip, ip, ip, ip]
+    L.sgba_debug_last_system.argtypes = [C.c_void_p, dp, dp, dp]
+    L.sgba_state_save.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_size_t)]
+    L.sgba_state_load.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+    L.sgba_get_profile.argtypes = [C.c_void_p, C.POINTER(Profile)]
+    L.sgba_set_profiling.argtypes = [C.c_void_p, C.c_int32]
+    _lib = L
+    return L
+
+
+def last_error():
+    L = lib()
+    buf = C.create_string_buffer(1024)
+    L.sgba_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(status):
+    if status != OK:
+        raise SgbaError(status, last_error())
+    return status
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ipt(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def _u8p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_uint8))
+
+
+def opt_params_c(p):
+    """Convert an OptParams-like object into the C struct."""
+    mr = p.max_consecutive_rejects
+    if mr is None or mr > (1 << 62):
+        mr = 1 << 62
+    return OptParamsC(int(p.num_iterations), float(p.initial_lm_damping), float(p.function_tolerance),
+                      float(p.gradient_tolerance), float(p.parameter_tolerance), int(mr),
+                      int(bool(getattr(p, "skip_final_hessian", False))))
+
+
+class Problem:
+    """One device-resident BA problem (sgba_problem handle).
+
+    `data` needs poses (n,7), points (m,3), intrinsics (4,), obs_cam, obs_pt,
+    obs_uv (k,2), huber_delta and optionally pose_const / point_const.
+    """
+
+    def __init__(self, data, device=-1):
+        L = lib()
+        self._keep = []
+        poses = np.ascontiguousarray(data.poses, dtype=np.float64).reshape(-1, 7)
+        points = np.ascontiguousarray(data.points, dtype=np.float64).reshape(-1, 3)
+        self.n_cam = poses.shape[0]
+        self.n_pt = points.shape[0]
+        obs_cam = np.ascontiguousarray(data.obs_cam, dtype=np.int32)
+        obs_pt = np.ascontiguousarray(data.obs_pt, dtype=np.int32)
+        obs_uv = np.ascontiguousarray(data.obs_uv, dtype=np.float64).reshape(-1, 2)
+        pc = getattr(data, "pose_const", None)
+        qc = getattr(data, "point_const", None)
+        pc = None if pc is None else np.ascontiguousarray(pc, dtype=np.uint8)
+        qc = None if qc is None else np.ascontiguousarray(qc, dtype=np.uint8)
+        self._keep += [poses, points, obs_cam, obs_pt, obs_uv, pc, qc]
+        d = ProblemDesc()
+        d.n_cam = self.n_cam
+        d.poses = _dptr(poses)
+        d.pose_const = _u8p(pc) if pc is not None else None
+        d.n_pt = self.n_pt
+        d.points = _dptr(points)
+        d.point_const = _u8p(qc) if qc is not None else None
+        for k in range(4):
+            d.intrinsics[k] = float(data.intrinsics[k])
+        d.n_obs = obs_cam.shape[0]
+        d.obs_cam = _ipt(obs_cam)
+        d.obs_pt = _ipt(obs_pt)
+        d.obs_uv = _dptr(obs_uv)
+        d.huber_delta = float(data.huber_delta) if data.huber_delta is not None else 0.0
+        h = C.c_void_p()
+        check(L.sgba_problem_create(C.byref(d), int(device), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sgba_problem_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self, params):
+        check(lib().sgba_optimizer_init(self._h, C.byref(opt_params_c(params))))
+
+    def step(self):
+        r = IterRecord()
+        check(lib().sgba_optimizer_step(self._h, C.byref(r)))
+        return r
+
+    def optimize(self, params):
+        cap = max(1, int(params.num_iterations))
+        recs = (IterRecord * cap)()
+        n = C.c_int32()
+        term = C.c_int32()
+        check(lib().sgba_optimize(self._h, C.byref(opt_params_c(params)), recs, cap, C.byref(n), C.byref(term)))
+        return [recs[i] for i in range(min(n.value, cap))], term.value
+
+    def variables(self):
+        poses = np.empty((self.n_cam, 7))
+        points = np.empty((self.n_pt, 3))
+        check(lib().sgba_get_variables(self._h, _dptr(poses), _dptr(points)))
+        return poses, points
+
+    def set_variables(self, poses=None, points=None):
+        pp = None if poses is None else np.ascontiguousarray(poses, dtype=np.float64)
+        qq = None if points is None else np.ascontiguousarray(points, dtype=np.float64)
+        check(lib().sgba_set_variables(self._h, _dptr(pp) if pp is not None else None,
+                                       _dptr(qq) if qq is not None else None))
+
+    def cost(self):
+        c = C.c_double()
+        check(lib().sgba_get_cost(self._h, C.byref(c)))
+        return c.value
+
+    def layout(self):
+        lay = Layout()
+        check(lib().sgba_get_layout(self._h, C.byref(lay)))
+        return lay
+
+    def export_pattern(self):
+        lay = self.layout()
+        hr = np.empty(lay.n_h_blocks, dtype=np.int32)
+        hc = np.empty(lay.n_h_blocks, dtype=np.int32)
+        sr = np.empty(lay.n_s_blocks, dtype=np.int32)
+        sc = np.empty(lay.n_s_blocks, dtype=np.int32)
+        check(lib().sgba_export_pattern(self._h, _ipt(hr), _ipt(hc), _ipt(sr), _ipt(sc)))
+        return (hr, hc), (sr, sc)
+
+    def last_system(self):
+        lay = self.layout()
+        n6 = 6 * lay.n_free_poses
+        S = np.empty((n6, n6))
+        rhs = np.empty(n6)
+        delta = np.empty(n6 + 3 * lay.n_marg_points)
+        check(lib().sgba_debug_last_system(self._h, _dptr(S), _dptr(rhs), _dptr(delta)))
+        return S, rhs, delta
+
+    def state_save(self):
+        size = C.c_size_t(0)
+        check(lib().sgba_state_save(self._h, None, C.byref(size)))
+        buf = C.create_string_buffer(size.value)
+        check(lib().sgba_state_save(self._h, buf, C.byref(size)))
+        return bytes(buf.raw[: size.value])
+
+    def state_load(self, blob):
+        buf = C.create_string_buffer(blob, len(blob))
+        check(lib().sgba_state_load(self._h, buf, len(blob)))
+
+    def set_profiling(self, on):
+        check(lib().sgba_set_profiling(self._h, 1 if on else 0))
+
+    def profile(self):
+        p = Profile()
+        check(lib().sgba_get_profile(self._h, C.byref(p)))
+        return p

@@ -1,0 +1,216 @@
+"""ctypes bindings of the CPU oracle (oracle/sgba_oracle.h).
+
+Test infrastructure only: used by the tests, smoke() and the CPU-baseline
+leg of bench.py as the checker / timed CPU restatement of the reference.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB = os.path.join(ROOT, "oracle", "_build", "libsgba_oracle.so")
+_lib = None
+
+
+class OraParams(C.Structure):
+    _fields_ = [
+        ("num_iterations", C.c_int32),
+        ("initial_lm_damping", C.c_double),
+        ("function_tolerance", C.c_double),
+        ("gradient_tolerance", C.c_double),
+        ("parameter_tolerance", C.c_double),
+        ("max_consecutive_rejects", C.c_int64),
+        ("emulate_fp32", C.c_int32),
+    ]
+
+
+class OraRecord(C.Structure):
+    _fields_ = [
+        ("merit", C.c_double),
+        ("new_merit", C.c_double),
+        ("lm_damping", C.c_double),
+        ("gain_ratio", C.c_double),
+        ("max_step", C.c_double),
+        ("max_grad", C.c_double),
+        ("accepted", C.c_int32),
+        ("termination", C.c_int32),
+    ]
+
+
+class OraProblem(C.Structure):
+    _fields_ = [
+        ("n_cam", C.c_int32),
+        ("poses", C.POINTER(C.c_double)),
+        ("pose_const", C.POINTER(C.c_uint8)),
+        ("n_pt", C.c_int32),
+        ("points", C.POINTER(C.c_double)),
+        ("point_const", C.POINTER(C.c_uint8)),
+        ("intrinsics", C.c_double * 4),
+        ("n_obs", C.c_int64),
+        ("obs_cam", C.POINTER(C.c_int32)),
+        ("obs_pt", C.POINTER(C.c_int32)),
+        ("obs_uv", C.POINTER(C.c_double)),
+        ("huber_delta", C.c_double),
+    ]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise RuntimeError("oracle library not built: %s" % LIB)
+        L = C.CDLL(LIB)
+        dp = C.POINTER(C.c_double)
+        L.ora_se3_exp.argtypes = [dp, dp]
+        L.ora_se3_mul.argtypes = [dp, dp, dp]
+        L.ora_se3_inverse.argtypes = [dp, dp]
+        L.ora_eval_term.argtypes = [dp, dp, dp, dp, C.c_double, dp, dp, dp, dp, dp]
+        L.ora_eval_term_dual.argtypes = [dp, dp, dp, dp, dp, dp]
+        L.ora_block_ldlt_solve.argtypes = [C.c_int, C.c_int, dp, dp, dp]
+        L.ora_total_cost.argtypes = [C.POINTER(OraProblem), C.c_int]
+        L.ora_total_cost.restype = C.c_double
+        L.ora_dense_system.argtypes = [C.POINTER(OraProblem), C.c_double, dp, dp]
+        L.ora_dense_system.restype = C.c_int64
+        L.ora_schur_step.argtypes = [C.POINTER(OraProblem), C.c_double, C.c_int, C.c_int, dp, dp, dp]
+        L.ora_optimize.argtypes = [C.POINTER(OraProblem), C.POINTER(OraParams), C.c_int,
+                                   C.POINTER(OraRecord), C.c_int, C.POINTER(C.c_int), dp, dp]
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class _Keep:
+    pass
+
+
+def problem_struct(prob):
+    k = _Keep()
+    k.poses = np.ascontiguousarray(prob.poses, dtype=np.float64)
+    k.points = np.ascontiguousarray(prob.points, dtype=np.float64)
+    k.obs_cam = np.ascontiguousarray(prob.obs_cam, dtype=np.int32)
+    k.obs_pt = np.ascontiguousarray(prob.obs_pt, dtype=np.int32)
+    k.obs_uv = np.ascontiguousarray(prob.obs_uv, dtype=np.float64)
+    pc = getattr(prob, "pose_const", None)
+    qc = getattr(prob, "point_const", None)
+    k.pc = None if pc is None else np.ascontiguousarray(pc, dtype=np.uint8)
+    k.qc = None if qc is None else np.ascontiguousarray(qc, dtype=np.uint8)
+    s = OraProblem()
+    s.n_cam = k.poses.shape[0]
+    s.poses = _d(k.poses)
+    s.pose_const = k.pc.ctypes.data_as(C.POINTER(C.c_uint8)) if k.pc is not None else None
+    s.n_pt = k.points.shape[0]
+    s.points = _d(k.points)
+    s.point_const = k.qc.ctypes.data_as(C.POINTER(C.c_uint8)) if k.qc is not None else None
+    for i in range(4):
+        s.intrinsics[i] = float(prob.intrinsics[i])
+    s.n_obs = k.obs_cam.shape[0]
+    s.obs_cam = k.obs_cam.ctypes.data_as(C.POINTER(C.c_int32))
+    s.obs_pt = k.obs_pt.ctypes.data_as(C.POINTER(C.c_int32))
+    s.obs_uv = _d(k.obs_uv)
+    s.huber_delta = float(prob.huber_delta or 0.0)
+    s._keep = k
+    return s
+
+
+def optimize(prob, params, n_threads=1, emulate_fp32=False):
+    L = lib()
+    s = problem_struct(prob)
+    mr = params.max_consecutive_rejects
+    if mr is None or mr > (1 << 62):
+        mr = 1 << 62
+    p = OraParams(int(params.num_iterations), float(params.initial_lm_damping), float(params.function_tolerance),
+                  float(params.gradient_tolerance), float(params.parameter_tolerance), int(mr),
+                  1 if emulate_fp32 else 0)
+    cap = max(1, int(params.num_iterations)) + 1
+    recs = (OraRecord * cap)()
+    n = C.c_int()
+    poses = np.empty((s.n_cam, 7))
+    points = np.empty((s.n_pt, 3))
+    rc = L.ora_optimize(C.byref(s), C.byref(p), int(n_threads), recs, cap, C.byref(n), _d(poses), _d(points))
+    if rc != 0:
+        raise RuntimeError("oracle optimize failed with %d" % rc)
+    return [recs[i] for i in range(min(n.value, cap))], poses, points
+
+
+def total_cost(prob, n_threads=1):
+    s = problem_struct(prob)
+    return lib().ora_total_cost(C.byref(s), int(n_threads))
+
+
+def dense_system(prob, nu):
+    L = lib()
+    s = problem_struct(prob)
+    n = L.ora_dense_system(C.byref(s), float(nu), None, None)
+    H = np.zeros((n, n))
+    b = np.zeros(n)
+    L.ora_dense_system(C.byref(s), float(nu), _d(H), _d(b))
+    return H, b
+
+
+def schur_step(prob, nu, n_threads=1):
+    """One Schur solve: returns (delta, S, rhs_bar); raises on failure."""
+    L = lib()
+    s = problem_struct(prob)
+    n = L.ora_dense_system(C.byref(s), float(nu), None, None)
+    nf6 = 6 * int(np.sum(1 - (np.asarray(prob.pose_const) if getattr(prob, "pose_const", None) is not None
+                              else np.zeros(prob.poses.shape[0], np.uint8))))
+    delta = np.zeros(n)
+    S = np.zeros((nf6, nf6))
+    rhs = np.zeros(nf6)
+    rc = L.ora_schur_step(C.byref(s), float(nu), int(n_threads), 0, _d(delta), _d(S), _d(rhs))
+    if rc != 0:
+        raise RuntimeError("oracle Schur step failed with %d" % rc)
+    return delta, S, rhs
+
+
+def se3_exp(xi):
+    out = np.zeros(7)
+    lib().ora_se3_exp(_d(np.ascontiguousarray(xi, dtype=np.float64)), _d(out))
+    return out
+
+
+def se3_mul(a, b):
+    out = np.zeros(7)
+    lib().ora_se3_mul(_d(np.ascontiguousarray(a, float)), _d(np.ascontiguousarray(b, float)), _d(out))
+    return out
+
+
+def se3_inverse(a):
+    out = np.zeros(7)
+    lib().ora_se3_inverse(_d(np.ascontiguousarray(a, float)), _d(out))
+    return out
+
+
+def eval_term(pose, point, intr, uv, huber):
+    r = np.zeros(2)
+    jp = np.zeros(12)
+    jm = np.zeros(6)
+    w = C.c_double()
+    c = C.c_double()
+    lib().ora_eval_term(_d(np.ascontiguousarray(pose, float)), _d(np.ascontiguousarray(point, float)),
+                        _d(np.ascontiguousarray(intr, float)), _d(np.ascontiguousarray(uv, float)),
+                        float(huber), _d(r), _d(jp), _d(jm), C.byref(w), C.byref(c))
+    return r, jp.reshape(2, 6), jm.reshape(2, 3), w.value, c.value
+
+
+def eval_term_dual(pose, point, intr, uv):
+    jp = np.zeros(12)
+    jm = np.zeros(6)
+    lib().ora_eval_term_dual(_d(np.ascontiguousarray(pose, float)), _d(np.ascontiguousarray(point, float)),
+                             _d(np.ascontiguousarray(intr, float)), _d(np.ascontiguousarray(uv, float)),
+                             _d(jp), _d(jm))
+    return jp.reshape(2, 6), jm.reshape(2, 3)
+
+
+def block_ldlt_solve(A, b, bs=6):
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    x = np.zeros_like(b)
+    rc = lib().ora_block_ldlt_solve(A.shape[0], bs, _d(A), _d(b), _d(x))
+    if rc != 0:
+        raise RuntimeError("block LDLT failed with %d" % rc)
+    return x
