@@ -1,0 +1,359 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Schur-LM bundle-adjustment path.
+
+Workload (the configuration the headline metric is quoted on): 100 SE(3)
+cameras on a radius-6 m Fibonacci sphere looking at the origin, 20,000 points
+uniform in [-2, 2]^3, each seen by 10..40 of the cameras that see it
+(~499k observations), pinhole fx=fy=500, Huber 1 px, camera 0 fixed,
+initial damping 1e-4.  Synthetic, seeded (seed 20261204).
+
+A "step" is one LM iteration over the whole problem (linearize, Schur
+complement, factor + solve, back-substitute, update, trial cost, decision).
+`value` is LM iterations/s with the problem resident in HBM (device time from
+CUDA events, L2 flushed before every step).  `e2e` is the same metric through
+the C ABI (sgba_optimize, the optimize_nlls drop-in) starting from host
+buffers: every step uploads the problem, runs the 20-iteration optimization
+and reads the variables back.
+
+--impl reference times the CPU restatement of the reference algorithm on the
+host cores on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "BA LM iters/sec + Jacobian obs/sec; learned-PCG vs exact LDLt at equal cost"
+UNIT = "LM iters/s"
+SEED = 20261203 + 1
+N_ITER_WORKLOAD = 20
+WORKLOAD = ("sphere BA: 100 SE(3) cams (99 free) on a r=6 m Fibonacci sphere, 20000 points in [-2,2]^3, "
+            "each seen by U{10..40} of its visible cams (~499k obs), pinhole 500/500/320/240, Huber 1 px, "
+            "nu0=1e-4, Schur LM with dense FP32-factor + f64-refined reduced camera system")
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier_and_max(value, ws):
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64)
+    if dist.get_backend() == "nccl":
+        t = t.cuda()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "", 1).isdigit())
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "", 1).isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _profile_traffic():
+    """dram bytes per launch of the roofline kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def _kernel_bytes(name, lay, prob):
+    """Algorithmic (compulsory) HBM bytes per launch of each kernel."""
+    n_obs = prob.n_obs
+    n_pt = prob.n_pt
+    n_cam = prob.n_cam
+    nf = lay.n_free_poses
+    nz = lay.n_h_blocks - nf - lay.n_marg_points  # terms with a free pose and a marginalized point
+    if name == "schur":
+        # read Z (18 f32) of every term once, U and the damping counts of each pose,
+        # write every lower S block once in f64
+        return 72 * nz + (288 + 8) * nf + 288 * lay.n_s_blocks
+    if name == "landmark":
+        # per observation: residual (8) + pose index (4) + term bounds (8); per term: Z (72);
+        # per point: position (24) + C^-1 (48) + C^-1 b (24) + neg gradient (24)
+        return 20 * n_obs + 72 * nz + 120 * n_pt + 48 * n_cam
+    if name == "cost":
+        # per observation: uv f64 (16) + indices (8) + residual out (8); points (24); poses (96)
+        return 32 * n_obs + 24 * n_pt + 96 * n_cam
+    if name == "camera":
+        # per term: residual (8) + point (24) + Z (72) + C^-1 b (24); per tile partial out
+        return (8 + 24) * n_obs + (72 + 24) * nz + 33 * 8 * ((lay.n_terms + 255) // 256)
+    if name == "backsub":
+        return 72 * nz + (48 + 24 + 24) * lay.n_marg_points + 48 * nf
+    return None
+
+
+def run_gpu(args, ws, rank, local):
+    import numpy as np
+
+    import __graft_entry__ as graft
+
+    if not os.path.exists(os.path.join(graft.PKG_DIR, "libsgba.so")):
+        graft.build_native()
+    pkg = graft.load_package()
+    native = pkg.native
+    prob = pkg.synth.generate(pkg.synth.SPHERE, seed=SEED + rank)
+    K, W = args.steps, args.warmup
+    params = pkg.OptParams(num_iterations=W + K + 1000, initial_lm_damping=prob.initial_lm_damping,
+                           function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
+                           max_consecutive_rejects=1 << 40, solver=pkg.LinearSolverEnum.SchurBlockSparseLdlt)
+    device = local
+    out = {}
+    with native.Problem(prob, device=device) as gp:
+        lay = gp.layout()
+        gp.init(params)
+        gp.bench_iterations(W, flush_l2=True)
+        _barrier(ws)
+        clocks = ClockSampler(device)
+        clocks.start()
+        ms, launches = gp.bench_iterations(K, flush_l2=True)
+        clk = clocks.stop()
+        ms_max = _barrier_and_max(ms, ws)
+        # per-kernel live timing (same stream, CUDA events, L2 flushed)
+        kernels = {"schur": native.KERNEL_SCHUR, "landmark": native.KERNEL_LANDMARK,
+                   "camera": native.KERNEL_CAMERA, "cost": native.KERNEL_COST,
+                   "factor": native.KERNEL_FACTOR, "backsub": native.KERNEL_BACKSUB}
+        kt = {k: gp.bench_kernel(v, reps=max(5, K), flush_l2=True) for k, v in kernels.items()}
+        # phase breakdown of a few iterations (events between phases; not the headline number)
+        gp.set_profiling(True)
+        n_prof = 5
+        gp.optimize(pkg.OptParams(num_iterations=n_prof, initial_lm_damping=prob.initial_lm_damping,
+                                  function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
+                                  max_consecutive_rejects=1 << 40, solver=pkg.LinearSolverEnum.SchurBlockSparseLdlt))
+        pr = gp.profile()
+        out["phase_ms"] = {"linearize": pr.ms_linearize / n_prof, "schur": pr.ms_schur / n_prof,
+                           "factor_solve": pr.ms_factor / n_prof, "update": pr.ms_update / n_prof,
+                           "cost_decide": pr.ms_cost / n_prof}
+        out["lay"] = lay
+    # end-to-end through the C ABI from (pinned) host buffers
+    e2e_steps = max(1, min(3, K))
+    host = prob
+    try:
+        import torch
+
+        def pin(a):
+            t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            return t.numpy()
+
+        host = prob.copy()
+        for f in ("poses", "points", "obs_cam", "obs_pt", "obs_uv", "pose_const"):
+            setattr(host, f, pin(getattr(prob, f)))
+        pinned = True
+    except Exception:
+        pinned = False
+    e2e_params = pkg.OptParams(num_iterations=N_ITER_WORKLOAD, initial_lm_damping=prob.initial_lm_damping,
+                               function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
+                               max_consecutive_rejects=1 << 40, solver=pkg.LinearSolverEnum.SchurBlockSparseLdlt)
+    # one untimed warm-up of the path (context, module load)
+    with native.Problem(host, device=device) as gp:
+        gp.optimize(e2e_params)
+        gp.variables()
+    _barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        with native.Problem(host, device=device) as gp:
+            gp.optimize(e2e_params)
+            poses, points = gp.variables()
+    e2e_s = _barrier_and_max(time.perf_counter() - t0, ws)
+    h2d = (host.poses.nbytes + host.points.nbytes + host.obs_cam.nbytes + host.obs_pt.nbytes +
+           host.obs_uv.nbytes + host.pose_const.nbytes)
+    d2h = poses.nbytes + points.nbytes
+    out.update(dict(ms=ms_max, launches=launches, kt=kt, clk=clk, e2e_s=e2e_s, e2e_steps=e2e_steps, h2d=h2d,
+                    d2h=d2h, pinned=pinned, prob=prob))
+    return out
+
+
+def cpu_baseline(prob, pkg, n_iter, threads):
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bindings as ob  # the oracle: CPU restatement of the reference
+
+    import __graft_entry__ as graft
+
+    graft.build_oracle()
+    params = pkg.OptParams(num_iterations=n_iter, initial_lm_damping=prob.initial_lm_damping,
+                           function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
+                           max_consecutive_rejects=1 << 40)
+    t0 = time.perf_counter()
+    recs, _, _ = ob.optimize(prob, params, n_threads=threads)
+    dt = time.perf_counter() - t0
+    return len(recs) / dt, dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-iters", type=int, default=0,
+                    help="profiling mode: only set up the workload and run this many LM iterations")
+    args = ap.parse_args()
+    if args.profile_iters > 0:
+        import __graft_entry__ as graft
+
+        pkg = graft.load_package()
+        prob = pkg.synth.generate(pkg.synth.SPHERE, seed=SEED)
+        params = pkg.OptParams(num_iterations=args.profile_iters, initial_lm_damping=prob.initial_lm_damping,
+                               function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
+                               max_consecutive_rejects=1 << 40, solver=pkg.LinearSolverEnum.SchurBlockSparseLdlt)
+        with pkg.native.Problem(prob, device=0) as gp:
+            recs, _ = gp.optimize(params)
+        print(json.dumps({"profile_iters": len(recs), "final_merit": recs[-1].merit}))
+        return
+    ws, rank, local = _dist()
+    if ws > 1:
+        import torch.distributed as dist
+
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        dist.init_process_group(backend=backend)
+
+    import __graft_entry__ as graft
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        if not os.path.exists(os.path.join(graft.PKG_DIR, "libsgba.so")):
+            graft.build_native()
+        pkg = graft.load_package()
+        prob = pkg.synth.generate(pkg.synth.SPHERE, seed=SEED)
+        threads = os.cpu_count() or 1
+        cpu_baseline(prob, pkg, max(1, args.warmup // 5), threads)  # warm caches / page in
+        v, dt = cpu_baseline(prob, pkg, args.steps, threads)
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic",
+                "config": {"workload": WORKLOAD, "n_obs": int(prob.n_obs)},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": "%d LM iterations of the workload on %d threads (setup included)"
+                                           % (args.steps, threads)},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    out = run_gpu(args, ws, rank, local)
+    if rank != 0:
+        return
+    pkg = graft.load_package()
+    prob, lay, kt = out["prob"], out["lay"], out["kt"]
+    K = args.steps
+    value = K * ws / (out["ms"] / 1000.0)
+    ms_per_step = out["ms"] / K
+    dominant = max(kt, key=kt.get)
+    hbm_peak, peak_src = _peaks()
+    traffic = _profile_traffic()
+    rl_kernel = dominant if _kernel_bytes(dominant, lay, prob) is not None else max(
+        (k for k in kt if _kernel_bytes(k, lay, prob) is not None), key=kt.get)
+    alg = _kernel_bytes(rl_kernel, lay, prob)
+    achieved = alg / (kt[rl_kernel] / 1000.0) / 1e9
+    roofline = {"bound": "hbm", "kernel": rl_kernel, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes": alg, "ms_per_launch": kt[rl_kernel],
+                "traffic": traffic.get(rl_kernel)}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak" if ws > 1 else "weak",
+        "vs_baseline": None, "dtype": "fp32 (Jacobians/products) + float-float sums + f64 update",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_obs": int(prob.n_obs), "n_terms": int(lay.n_terms),
+                   "n_schur_pairs": int(lay.n_schur_pairs), "l2": "flushed (256 MiB write) before every step",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "jacobian_obs_per_s": value * prob.n_obs,
+        "kernel_ms": kt,
+        "phase_ms_per_iteration": out.get("phase_ms"),
+        "roofline": roofline,
+        "gpu_launches": int(out["launches"]),
+        "e2e": {"value": N_ITER_WORKLOAD * out["e2e_steps"] * ws / out["e2e_s"], "unit": UNIT,
+                "h2d_bytes_per_step": int(out["h2d"]), "d2h_bytes_per_step": int(out["d2h"]),
+                "step": "create+upload, optimize (%d LM iterations), read back" % N_ITER_WORKLOAD,
+                "pinned_host": out["pinned"]},
+        "clocks": out["clk"],
+    }
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, dt = cpu_baseline(prob, pkg, 2, threads)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "2 LM iterations of the workload on %d threads (%.1f s, setup included)"
+                                          % (threads, dt)}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

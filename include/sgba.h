@@ -180,6 +180,28 @@ int sgba_get_profile(sgba_problem *p, sgba_profile *out);
 /* Enable per-phase event timing (adds events between phases; off by default). */
 int sgba_set_profiling(sgba_problem *p, int32_t enabled);
 
+/* ---- benchmark instrumentation (no counterpart in the reference) ---------
+ * Require sgba_optimizer_init.  Times come from CUDA events on the problem's
+ * stream.  With flush_l2 != 0 a 256 MiB buffer is written before every timed
+ * unit so each starts with a cold L2. */
+typedef enum {
+  SGBA_KERNEL_ITERATION = 0,   /* one whole LM iteration (the graph) */
+  SGBA_KERNEL_SCHUR = 1,       /* reduced camera system assembly (k_schur) */
+  SGBA_KERNEL_LANDMARK = 2,    /* landmark pass: point blocks, Cholesky, Z */
+  SGBA_KERNEL_CAMERA = 3,      /* camera pass: pose blocks and reduced rhs */
+  SGBA_KERNEL_COST = 4,        /* trial cost (float-float) */
+  SGBA_KERNEL_FACTOR = 5,      /* factorization + solves + refinement (several kernels) */
+  SGBA_KERNEL_BACKSUB = 6,     /* back-substitution */
+} sgba_kernel_id;
+
+/* Runs `iters` LM iterations (each its own graph launch); *ms_sum is the sum
+ * of their device times, *launches the number of kernel launches. */
+int sgba_bench_iterations(sgba_problem *p, int32_t iters, int32_t flush_l2, double *ms_sum,
+                          int64_t *launches);
+/* Re-launches one kernel (or kernel group) `reps` times on the current data;
+ * *ms_avg is the mean device time per launch. */
+int sgba_bench_kernel(sgba_problem *p, int32_t kernel, int32_t reps, int32_t flush_l2, double *ms_avg);
+
 #ifdef __cplusplus
 }
 #endif

@@ -71,6 +71,7 @@ struct sgba_problem {
   // profile
   bool profiling = false;
   sgba_profile prof{};
+  void* flush_buf = nullptr;  // L2 flush target for benchmark hooks
   std::vector<void*> allocs;
 };
 
@@ -381,9 +382,9 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_alloc(p, &d.res_t, P.no))) return st;
   if ((st = dev_alloc(p, &d.pose_f, 12 * static_cast<size_t>(P.nc)))) return st;
   if ((st = dev_alloc(p, &d.pose_dd, 24 * static_cast<size_t>(P.nc)))) return st;
-  if ((st = dev_alloc(p, &d.zmat, 18 * static_cast<size_t>(P.ng)))) return st;
+  if ((st = dev_alloc(p, &d.zmat, 20 * static_cast<size_t>(P.ng)))) return st;
   if ((st = dev_alloc(p, &d.cinv, 6 * static_cast<size_t>(P.nm)))) return st;
-  if ((st = dev_alloc(p, &d.cvec, 3 * static_cast<size_t>(P.nm)))) return st;
+  if ((st = dev_alloc(p, &d.cvec, 6 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.bm, 3 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.dm, 3 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.bf, 6 * static_cast<size_t>(P.nf)))) return st;
@@ -397,6 +398,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_alloc(p, &d.dpiv, n6))) return st;
   if ((st = dev_alloc(p, &d.wpanel, n6 * 48))) return st;
   if ((st = dev_alloc(p, &d.x, n6))) return st;
+  if ((st = dev_alloc(p, &d.xdd, 2 * n6))) return st;
   if ((st = dev_alloc(p, &d.r, n6))) return st;
   SGBA_CK(cudaMemset(d.x, 0, sizeof(double) * std::max<size_t>(n6, 1)));
   SGBA_CK(cudaMemset(d.dm, 0, sizeof(double) * std::max<size_t>(3 * P.nm, 1)));
@@ -492,6 +494,7 @@ int sgba_problem_destroy(sgba_problem* p) {
   if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
   if (p->graph) cudaGraphDestroy(p->graph);
   for (void* v : p->allocs) cudaFree(v);
+  if (p->flush_buf) cudaFree(p->flush_buf);
   if (p->d.records) cudaFree(p->d.records);
   if (p->stream) cudaStreamDestroy(p->stream);
   delete p;
@@ -787,6 +790,69 @@ int sgba_state_load(sgba_problem* p, const void* buf, size_t size) {
                           cudaMemcpyHostToDevice, p->stream));
   SGBA_CK(cudaStreamSynchronize(p->stream));
   return check_launch();
+}
+
+static int bench_prepare(sgba_problem* p, bool flush) {
+  if (!p->inited) return set_error(SGBA_ERR_STATE, "benchmark hooks need sgba_optimizer_init");
+  SGBA_CK(cudaSetDevice(p->device));
+  if (flush && !p->flush_buf) SGBA_CK(cudaMalloc(&p->flush_buf, size_t(256) << 20));
+  // clear done / skip so the kernels do their work
+  const int zero[2] = {0, 0};
+  SGBA_CK(cudaMemcpyAsync(reinterpret_cast<char*>(p->d.ctrl) + offsetof(Ctrl, done), zero, 2 * sizeof(int),
+                          cudaMemcpyHostToDevice, p->stream));
+  return SGBA_OK;
+}
+
+int sgba_bench_iterations(sgba_problem* p, int32_t iters, int32_t flush_l2, double* ms_sum, int64_t* launches) {
+  if (!p || !ms_sum) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  int st = bench_prepare(p, flush_l2 != 0);
+  if (st) return st;
+  cudaEvent_t a, b;
+  SGBA_CK(cudaEventCreate(&a));
+  SGBA_CK(cudaEventCreate(&b));
+  double total = 0.0;
+  for (int i = 0; i < iters; ++i) {
+    if (flush_l2) SGBA_CK(cudaMemsetAsync(p->flush_buf, i & 0xff, size_t(256) << 20, p->stream));
+    SGBA_CK(cudaEventRecord(a, p->stream));
+    SGBA_CK(cudaGraphLaunch(p->graph_exec, p->stream));
+    SGBA_CK(cudaEventRecord(b, p->stream));
+    SGBA_CK(cudaEventSynchronize(b));
+    float ms = 0.f;
+    SGBA_CK(cudaEventElapsedTime(&ms, a, b));
+    total += ms;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  *ms_sum = total;
+  if (launches) *launches = static_cast<int64_t>(iters) * p->iter_launches;
+  return SGBA_OK;
+}
+
+int sgba_bench_kernel(sgba_problem* p, int32_t kernel, int32_t reps, int32_t flush_l2, double* ms_avg) {
+  if (!p || !ms_avg || reps < 1) return set_error(SGBA_ERR_INVALID_ARGUMENT, "bad argument");
+  int st = bench_prepare(p, flush_l2 != 0);
+  if (st) return st;
+  cudaEvent_t a, b;
+  SGBA_CK(cudaEventCreate(&a));
+  SGBA_CK(cudaEventCreate(&b));
+  double total = 0.0;
+  for (int i = 0; i < reps; ++i) {
+    if (flush_l2) SGBA_CK(cudaMemsetAsync(p->flush_buf, i & 0xff, size_t(256) << 20, p->stream));
+    SGBA_CK(cudaEventRecord(a, p->stream));
+    if (kernel == SGBA_KERNEL_ITERATION) SGBA_CK(cudaGraphLaunch(p->graph_exec, p->stream));
+    else sgba::launch_single(p->sz, p->d, kernel, p->stream);
+    SGBA_CK(cudaEventRecord(b, p->stream));
+    SGBA_CK(cudaEventSynchronize(b));
+    float ms = 0.f;
+    SGBA_CK(cudaEventElapsedTime(&ms, a, b));
+    total += ms;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  st = check_launch();
+  if (st) return st;
+  *ms_avg = total / reps;
+  return SGBA_OK;
 }
 
 int sgba_get_profile(sgba_problem* p, sgba_profile* out) {

@@ -112,9 +112,9 @@ struct Dev {
   // per iteration
   float* pose_f = nullptr;         // nc*12: R_cw (row-major) + t_cw, float
   float* pose_dd = nullptr;        // nc*24: R_cw + t_cw as (hi,lo) pairs
-  float* zmat = nullptr;           // ng*18: Z = W C^-T (6x3 row-major)
-  double* cinv = nullptr;          // nm*6: C^-1 lower (00,10,11,20,21,22)
-  double* cvec = nullptr;          // nm*3: C^-1 b_m
+  float* zmat = nullptr;           // ng*20: Z = W C^-T (6x3 row-major, padded to 20 floats)
+  float* cinv = nullptr;           // nm*6: C^-1 lower (00,10,11,20,21,22), FP32
+  float* cvec = nullptr;           // nm*6: C^-1 b_m as float-float pairs
   double* bm = nullptr;            // nm*3: neg_grad of points
   double* bf = nullptr;            // nf*6: neg_grad of poses
   double* ufull = nullptr;         // nf*36: U_j (undamped J^T J) full 6x6
@@ -125,6 +125,7 @@ struct Dev {
   float* dpiv = nullptr;           // n6 pivots
   float* wpanel = nullptr;         // n6*64 panel scratch (A_ip L^-T)
   double* x = nullptr;             // n6 solution / refinement
+  float* xdd = nullptr;            // n6*2: solution as float-float pairs
   double* r = nullptr;             // n6 residual
   double* dm = nullptr;            // nm*3 point steps
   double* part = nullptr;          // reduction partials
@@ -159,6 +160,7 @@ int launch_factor_solve(const Sizes& s, const Dev& d, cudaStream_t st);
 int launch_update(const Sizes& s, const Dev& d, cudaStream_t st);
 int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st);
 
+int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st);
 int cost_partials_needed(const Sizes& s);  // reduction partial slots
 int solver_launch_count(const Sizes& s);
 

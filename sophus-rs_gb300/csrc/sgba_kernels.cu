@@ -149,6 +149,35 @@ __device__ __forceinline__ void jacobians_f(const float* pt /*R_cw 9 + t_cw 3*/,
   }
 }
 
+
+constexpr int kZS = 20;  // floats per Z row block (18 used; padded for float4 loads)
+
+// Sum over the 32 lanes of a warp of `nv` float values per lane, in
+// float-float: values are transposed through shared memory (red[nv][33]) and
+// lane v < nv adds the 32 entries of value v.  Returns the total of value
+// `lane` (valid for lane < nv).  Deterministic (fixed order).
+template <int NV>
+__device__ __forceinline__ dd warp_transpose_sum(const float* vals, float (*red)[33]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int v = 0; v < NV; ++v) red[v][lane] = vals[v];
+  __syncwarp();
+  dd acc = dd_make(0.f, 0.f);
+  if (lane < NV) {
+#pragma unroll 8
+    for (int l = 0; l < 32; ++l) acc = dd_add_f(acc, red[lane][l]);
+  }
+  __syncwarp();
+  return acc;
+}
+
+__device__ __forceinline__ dd shfl_dd(dd v, int src) {
+  dd o;
+  o.hi = __shfl_sync(0xffffffffu, v.hi, src);
+  o.lo = __shfl_sync(0xffffffffu, v.lo, src);
+  return o;
+}
+
 // ---------------------------------------------------------------------------
 // Pose tables: T_cw = T_wc^-1 in f64, published as float and float-float.
 // ---------------------------------------------------------------------------
@@ -288,6 +317,7 @@ __global__ void k_iter_begin(Ctrl* ctrl) {
 // W_g = J_pose^T J_pt.  Then the Schur complement contribution of the point
 // is sum_{a,b} Z_a Z_b^T and its rhs contribution Z_a (C^-1 b_m)
 // (compute_marg_block_contrib, crates/sophus_solver/src/ldlt/schur_ldlt.rs:82-135).
+// FP32 per-lane sums, float-float across lanes, FP32 3x3 factor.
 // ---------------------------------------------------------------------------
 struct LinArgs {
   int32_t np;
@@ -302,8 +332,8 @@ struct LinArgs {
   const float2* res;
   float fx, fy, huber;
   float* zmat;
-  double* cinv;
-  double* cvec;
+  float* cinv;   // 6 floats per point: C^-1 (00 10 11 20 21 22)
+  float* cvec;   // 3 float-float per point: C^-1 b_m
   double* bm;
   double nu_override;
   int use_override;
@@ -312,10 +342,13 @@ struct LinArgs {
 
 __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
   if (halted(ctrl)) return;
+  __shared__ float red[8][9][33];
   const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
   const int warps_per_block = blockDim.x >> 5;
   const double nu = a.use_override ? a.nu_override : ctrl->nu;
-  for (int64_t i = static_cast<int64_t>(blockIdx.x) * warps_per_block + (threadIdx.x >> 5); i < a.np;
+  double warp_max = 0.0;  // max |neg_grad| of this warp's points
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * warps_per_block + wib; i < a.np;
        i += static_cast<int64_t>(gridDim.x) * warps_per_block) {
     const int mb = a.pt_mb[i];
     if (mb < 0) continue;  // constant point: no H_mm block
@@ -323,13 +356,9 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
     const float py = __double2float_rn(a.points[3 * i + 1]);
     const float pz = __double2float_rn(a.points[3 * i + 2]);
     const int64_t g0 = a.pt_g_begin[i], g1 = a.pt_g_begin[i + 1];
-    dd V[6], G[3];
-    for (int k = 0; k < 6; ++k) V[k] = dd_make(0.f, 0.f);
-    for (int k = 0; k < 3; ++k) G[k] = dd_make(0.f, 0.f);
-    // pass 1: V and g_m
+    float v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // V00 V01 V02 V11 V12 V22, g0 g1 g2
     for (int64_t g = g0 + lane; g < g1; g += 32) {
       const float* P = a.pose_f + 12 * a.g_pose[g];
-      float v[6] = {0, 0, 0, 0, 0, 0}, gm[3] = {0, 0, 0};
       for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
         JacF J;
         jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
@@ -343,58 +372,60 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
         v[3] += m[1] * m[1] + m[4] * m[4];
         v[4] += m[1] * m[2] + m[4] * m[5];
         v[5] += m[2] * m[2] + m[5] * m[5];
-        gm[0] += m[0] * r0 + m[3] * r1;
-        gm[1] += m[1] * r0 + m[4] * r1;
-        gm[2] += m[2] * r0 + m[5] * r1;
+        v[6] += m[0] * r0 + m[3] * r1;
+        v[7] += m[1] * r0 + m[4] * r1;
+        v[8] += m[2] * r0 + m[5] * r1;
       }
-      for (int k = 0; k < 6; ++k) V[k] = dd_add_f(V[k], v[k]);
-      for (int k = 0; k < 3; ++k) G[k] = dd_add_f(G[k], gm[k]);
     }
-    for (int k = 0; k < 6; ++k) V[k] = dd_warp_sum(V[k]);
-    for (int k = 0; k < 3; ++k) G[k] = dd_warp_sum(G[k]);
-    // damping nu * (number of reduced terms) on the diagonal
-    dd damp = dd_from_double(nu * a.cnt_m[mb]);
-    V[0] = dd_add(V[0], damp);
-    V[3] = dd_add(V[3], damp);
-    V[5] = dd_add(V[5], damp);
-    dd b[3] = {dd_neg(G[0]), dd_neg(G[1]), dd_neg(G[2])};  // neg_grad
-    // Cholesky V' = C C^T  (V layout: 00 01 02 11 12 22)
-    bool ok = V[0].hi > 0.0f;
-    dd c00 = dd_sqrt(V[0]);
-    dd c10 = dd_div(V[1], c00), c20 = dd_div(V[2], c00);
-    dd t11 = dd_sub(V[3], dd_mul(c10, c10));
-    ok = ok && t11.hi > 0.0f;
-    dd c11 = dd_sqrt(t11);
-    dd c21 = dd_div(dd_sub(V[4], dd_mul(c20, c10)), c11);
-    dd t22 = dd_sub(dd_sub(V[5], dd_mul(c20, c20)), dd_mul(c21, c21));
-    ok = ok && t22.hi > 0.0f;
-    dd c22 = dd_sqrt(t22);
-    ok = ok && isfinite(c00.hi) && isfinite(c11.hi) && isfinite(c22.hi) && isfinite(c10.hi) &&
-         isfinite(c20.hi) && isfinite(c21.hi);
+    dd tot = warp_transpose_sum<9>(v, red[wib]);
+    // damping nu * (number of reduced terms) on the diagonal (entries 0, 3, 5)
+    if (lane == 0 || lane == 3 || lane == 5) tot = dd_add(tot, dd_from_double(nu * a.cnt_m[mb]));
+    if (lane >= 6) tot = dd_neg(tot);  // neg_grad b_m = -sum J^T r~
+    // broadcast: V as floats, b as float-float
+    float V[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      dd t = shfl_dd(tot, k);
+      V[k] = t.hi + t.lo;
+    }
+    dd b[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) b[k] = shfl_dd(tot, 6 + k);
+    if (lane == 0) {
+      double* bp = a.bm + 3 * mb;
+      bp[0] = dd_to_double(b[0]);
+      bp[1] = dd_to_double(b[1]);
+      bp[2] = dd_to_double(b[2]);
+      warp_max = fmax(warp_max, fmax(fabs(bp[0]), fmax(fabs(bp[1]), fabs(bp[2]))));
+    }
+    // Cholesky V' = C C^T in FP32  (V layout: 00 01 02 11 12 22)
+    const float c00 = sqrtf(V[0]);
+    const float c10 = V[1] / c00, c20 = V[2] / c00;
+    const float t11 = V[3] - c10 * c10;
+    const float c11 = sqrtf(t11);
+    const float c21 = (V[4] - c20 * c10) / c11;
+    const float t22 = V[5] - c20 * c20 - c21 * c21;
+    const float c22 = sqrtf(t22);
+    const bool ok = V[0] > 0.f && t11 > 0.f && t22 > 0.f && isfinite(c00) && isfinite(c11) && isfinite(c22) &&
+                    isfinite(c10) && isfinite(c20) && isfinite(c21);
     if (!ok) {
       if (lane == 0 && !a.use_override) atomicExch(a.fail, 1);
       continue;
     }
     // C^-1 (lower)
-    dd one = dd_make(1.0f, 0.0f);
-    dd i00 = dd_div(one, c00), i11 = dd_div(one, c11), i22 = dd_div(one, c22);
-    dd i10 = dd_neg(dd_div(dd_mul(c10, i00), c11));
-    dd i21 = dd_neg(dd_div(dd_mul(c21, i11), c22));
-    dd i20 = dd_neg(dd_div(dd_add(dd_mul(c20, i00), dd_mul(c21, i10)), c22));
-    // c = C^-1 b
-    dd cv0 = dd_mul(i00, b[0]);
-    dd cv1 = dd_add(dd_mul(i10, b[0]), dd_mul(i11, b[1]));
-    dd cv2 = dd_add(dd_add(dd_mul(i20, b[0]), dd_mul(i21, b[1])), dd_mul(i22, b[2]));
+    const float i00 = 1.f / c00, i11 = 1.f / c11, i22 = 1.f / c22;
+    const float i10 = -c10 * i00 * i11;
+    const float i21 = -c21 * i11 * i22;
+    const float i20 = -(c20 * i00 + c21 * i10) * i22;
     if (lane == 0) {
-      double* ci = a.cinv + 6 * mb;
-      ci[0] = dd_to_double(i00); ci[1] = dd_to_double(i10); ci[2] = dd_to_double(i11);
-      ci[3] = dd_to_double(i20); ci[4] = dd_to_double(i21); ci[5] = dd_to_double(i22);
-      double* cvp = a.cvec + 3 * mb;
-      cvp[0] = dd_to_double(cv0); cvp[1] = dd_to_double(cv1); cvp[2] = dd_to_double(cv2);
-      double* bp = a.bm + 3 * mb;
-      bp[0] = dd_to_double(b[0]); bp[1] = dd_to_double(b[1]); bp[2] = dd_to_double(b[2]);
-      double mg = fmax(fabs(bp[0]), fmax(fabs(bp[1]), fabs(bp[2])));
-      atomic_max_nonneg(&ctrl->max_grad_bits, mg);
+      float* ci = a.cinv + 6 * mb;
+      ci[0] = i00; ci[1] = i10; ci[2] = i11; ci[3] = i20; ci[4] = i21; ci[5] = i22;
+      // c = C^-1 b in float-float
+      dd cv0 = dd_mul_f(b[0], i00);
+      dd cv1 = dd_add(dd_mul_f(b[0], i10), dd_mul_f(b[1], i11));
+      dd cv2 = dd_add(dd_add(dd_mul_f(b[0], i20), dd_mul_f(b[1], i21)), dd_mul_f(b[2], i22));
+      float* cvp = a.cvec + 6 * mb;
+      cvp[0] = cv0.hi; cvp[1] = cv0.lo; cvp[2] = cv1.hi; cvp[3] = cv1.lo; cvp[4] = cv2.hi; cvp[5] = cv2.lo;
     }
     if (a.use_override) continue;  // final Hessian pass: no Schur data
     // pass 2: Z_g = W_g C^-T for terms with a free pose
@@ -403,32 +434,46 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
       if (a.pose_fb[pj] < 0) continue;
       const float* P = a.pose_f + 12 * pj;
       float W[18];
+#pragma unroll
       for (int k = 0; k < 18; ++k) W[k] = 0.f;
       for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
         JacF J;
         jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+#pragma unroll
         for (int r = 0; r < 6; ++r)
-          for (int s = 0; s < 3; ++s) W[r * 3 + s] += J.jp[r] * J.jm[s] + J.jp[6 + r] * J.jm[3 + s];
+#pragma unroll
+          for (int q = 0; q < 3; ++q) W[r * 3 + q] += J.jp[r] * J.jm[q] + J.jp[6 + r] * J.jm[3 + q];
       }
       // Z[r][t] = sum_{s<=t} W[r][s] * Cinv[t][s]
-      float* Z = a.zmat + 18 * g;
+      float Z[20];
+#pragma unroll
       for (int r = 0; r < 6; ++r) {
-        dd z0 = dd_mul_f(i00, W[r * 3 + 0]);
-        dd z1 = dd_add(dd_mul_f(i10, W[r * 3 + 0]), dd_mul_f(i11, W[r * 3 + 1]));
-        dd z2 = dd_add(dd_add(dd_mul_f(i20, W[r * 3 + 0]), dd_mul_f(i21, W[r * 3 + 1])),
-                       dd_mul_f(i22, W[r * 3 + 2]));
-        Z[r * 3 + 0] = z0.hi + z0.lo;
-        Z[r * 3 + 1] = z1.hi + z1.lo;
-        Z[r * 3 + 2] = z2.hi + z2.lo;
+        Z[r * 3 + 0] = W[r * 3 + 0] * i00;
+        Z[r * 3 + 1] = W[r * 3 + 0] * i10 + W[r * 3 + 1] * i11;
+        Z[r * 3 + 2] = W[r * 3 + 0] * i20 + W[r * 3 + 1] * i21 + W[r * 3 + 2] * i22;
       }
+      Z[18] = 0.f;
+      Z[19] = 0.f;
+      float4* dst = reinterpret_cast<float4*>(a.zmat + kZS * g);
+#pragma unroll
+      for (int q = 0; q < 5; ++q) dst[q] = make_float4(Z[4 * q], Z[4 * q + 1], Z[4 * q + 2], Z[4 * q + 3]);
     }
+  }
+  __shared__ double s_max[8];
+  if (lane == 0) s_max[wib] = warp_max;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int q = 0; q < warps_per_block; ++q) m = fmax(m, s_max[q]);
+    atomic_max_nonneg(&ctrl->max_grad_bits, m);
   }
 }
 
 // ---------------------------------------------------------------------------
 // Camera pass: one CTA per tile of terms of one free pose.  Accumulates
 // U_j = sum J_pose^T J_pose (21 upper entries), g_j = sum J_pose^T r~ and the
-// reduced-rhs term sum Z_g (C^-1 b_m).
+// reduced-rhs term sum Z_g (C^-1 b_m).  FP32 warp sums, float-float across
+// warps; the Z c products in float-float.
 // ---------------------------------------------------------------------------
 constexpr int kTileThreads = 256;
 constexpr int kTileVals = 33;
@@ -446,7 +491,7 @@ struct CamArgs {
   const double* points;
   const float2* res;
   const float* zmat;
-  const double* cvec;
+  const float* cvec;
   float fx, fy, huber;
   double* tile_part;
   int with_schur;
@@ -457,11 +502,12 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
   const int tile = blockIdx.x;
   const int fb = a.tile_fb[tile];
   const float* P = a.pose_f + 12 * a.fb_pose[fb];
-  float u[21], gp[6];
-  for (int k = 0; k < 21; ++k) u[k] = 0.f;
-  for (int k = 0; k < 6; ++k) gp[k] = 0.f;
-  dd zcd[6];
-  for (int k = 0; k < 6; ++k) zcd[k] = dd_make(0.f, 0.f);
+  float u[27];
+#pragma unroll
+  for (int k = 0; k < 27; ++k) u[k] = 0.f;
+  float zc[12];  // 6 float-float values as (hi, lo)
+#pragma unroll
+  for (int k = 0; k < 12; ++k) zc[k] = 0.f;
   const int64_t e = a.tile_begin[tile] + threadIdx.x;
   if (e < a.tile_end[tile]) {
     const int64_t g = a.cam_g[e];
@@ -476,29 +522,53 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
       float w = huber_weight_f(a.huber, r.x, r.y);
       float r0 = w * r.x, r1 = w * r.y;
       int k = 0;
+#pragma unroll
       for (int p = 0; p < 6; ++p) {
+#pragma unroll
         for (int q = p; q < 6; ++q) u[k++] += J.jp[p] * J.jp[q] + J.jp[6 + p] * J.jp[6 + q];
-        gp[p] += J.jp[p] * r0 + J.jp[6 + p] * r1;
+        u[21 + p] += J.jp[p] * r0 + J.jp[6 + p] * r1;
       }
     }
     const int mb = a.pt_mb[pi];
     if (a.with_schur && mb >= 0) {
-      const float* Z = a.zmat + 18 * g;
-      dd c0 = dd_from_double(a.cvec[3 * mb + 0]);
-      dd c1 = dd_from_double(a.cvec[3 * mb + 1]);
-      dd c2 = dd_from_double(a.cvec[3 * mb + 2]);
-      for (int r = 0; r < 6; ++r)
-        zcd[r] = dd_add(dd_add(dd_mul_f(c0, Z[r * 3 + 0]), dd_mul_f(c1, Z[r * 3 + 1])),
-                        dd_mul_f(c2, Z[r * 3 + 2]));
+      const float4* Z4 = reinterpret_cast<const float4*>(a.zmat + kZS * g);
+      float Z[20];
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        float4 z = Z4[q];
+        Z[4 * q] = z.x; Z[4 * q + 1] = z.y; Z[4 * q + 2] = z.z; Z[4 * q + 3] = z.w;
+      }
+      const float* cv = a.cvec + 6 * mb;
+      dd c0 = dd_make(cv[0], cv[1]), c1 = dd_make(cv[2], cv[3]), c2 = dd_make(cv[4], cv[5]);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        dd t = dd_add(dd_add(dd_mul_f(c0, Z[r * 3 + 0]), dd_mul_f(c1, Z[r * 3 + 1])), dd_mul_f(c2, Z[r * 3 + 2]));
+        zc[2 * r] = t.hi;
+        zc[2 * r + 1] = t.lo;
+      }
     }
   }
   __shared__ float sh_hi[kTileVals][kTileThreads / 32];
   __shared__ float sh_lo[kTileVals][kTileThreads / 32];
+  __shared__ float zred[kTileThreads / 32][12][33];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int k = 0; k < kTileVals; ++k) {
-    dd v = (k < 21) ? dd_from_float(u[k]) : (k < 27 ? dd_from_float(gp[k - 21]) : zcd[k - 27]);
-    v = dd_warp_sum(v);
-    if (lane == 0) { sh_hi[k][w] = v.hi; sh_lo[k][w] = v.lo; }
+  // U and g: FP32 butterfly inside the warp
+#pragma unroll
+  for (int k = 0; k < 27; ++k) {
+    float v = u[k];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) { sh_hi[k][w] = v; sh_lo[k][w] = 0.f; }
+  }
+  // Z c: float-float across the warp (values 2r = hi, 2r+1 = lo)
+#pragma unroll
+  for (int k = 0; k < 12; ++k) zred[w][k][lane] = zc[k];
+  __syncwarp();
+  if (lane < 6) {
+    dd acc = dd_make(0.f, 0.f);
+    for (int l = 0; l < 32; ++l) acc = dd_add(acc, dd_make(zred[w][2 * lane][l], zred[w][2 * lane + 1][l]));
+    sh_hi[27 + lane][w] = acc.hi;
+    sh_lo[27 + lane][w] = acc.lo;
   }
   __syncthreads();
   if (threadIdx.x < kTileVals) {
@@ -509,31 +579,45 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
   }
 }
 
-__global__ void k_camera_finalize(int nf, const int64_t* fb_tile_begin, const double* tile_part,
-                                  double* ufull, double* bf, double* rb, Ctrl* ctrl, int with_schur) {
+__global__ void __launch_bounds__(64) k_camera_finalize(int nf, const int64_t* fb_tile_begin,
+                                                        const double* tile_part, double* ufull, double* bf,
+                                                        double* rb, Ctrl* ctrl, int with_schur) {
   if (halted(ctrl)) return;
-  const int fb = blockIdx.x * blockDim.x + threadIdx.x;
-  if (fb >= nf) return;
-  dd acc[kTileVals];
-  for (int k = 0; k < kTileVals; ++k) acc[k] = dd_make(0.f, 0.f);
-  for (int64_t t = fb_tile_begin[fb]; t < fb_tile_begin[fb + 1]; ++t)
-    for (int k = 0; k < kTileVals; ++k) acc[k] = dd_add(acc[k], dd_from_double(tile_part[t * kTileVals + k]));
-  double* U = ufull + 36 * fb;
-  int k = 0;
-  for (int p = 0; p < 6; ++p)
-    for (int q = p; q < 6; ++q) {
-      double v = dd_to_double(acc[k++]);
-      U[p * 6 + q] = v;
-      U[q * 6 + p] = v;
+  const int fb = blockIdx.x;
+  const int k = threadIdx.x;
+  __shared__ double vals[kTileVals];
+  if (k < kTileVals) {
+    dd acc = dd_make(0.f, 0.f);
+    for (int64_t t = fb_tile_begin[fb]; t < fb_tile_begin[fb + 1]; ++t)
+      acc = dd_add(acc, dd_from_double(tile_part[t * kTileVals + k]));
+    if (k >= 21 && k < 27) {
+      acc = dd_neg(acc);  // neg_grad = -sum J^T r~
+    } else if (k >= 27) {
+      // reduced rhs: b_f - sum Z c  (b_f = -g)
+      dd g = dd_make(0.f, 0.f);
+      for (int64_t t = fb_tile_begin[fb]; t < fb_tile_begin[fb + 1]; ++t)
+        g = dd_add(g, dd_from_double(tile_part[t * kTileVals + k - 6]));
+      acc = dd_sub(dd_neg(g), acc);
     }
-  double mg = 0.0;
-  for (int p = 0; p < 6; ++p) {
-    dd b = dd_neg(acc[21 + p]);
-    bf[6 * fb + p] = dd_to_double(b);
-    mg = fmax(mg, fabs(bf[6 * fb + p]));
-    if (with_schur) rb[6 * fb + p] = dd_to_double(dd_sub(b, acc[27 + p]));
+    vals[k] = dd_to_double(acc);
   }
-  atomic_max_nonneg(&ctrl->max_grad_bits, mg);
+  __syncthreads();
+  if (k < 36) {
+    // full 6x6 U from the 21 upper entries
+    const int p = k / 6, q = k % 6;
+    const int a = p < q ? p : q, b = p < q ? q : p;
+    const int idx = a * 6 - a * (a - 1) / 2 + (b - a);
+    ufull[36 * fb + k] = vals[idx];
+  }
+  if (k < 6) {
+    bf[6 * fb + k] = vals[21 + k];
+    if (with_schur) rb[6 * fb + k] = vals[27 + k];
+  }
+  if (k == 0) {
+    double mg = 0.0;
+    for (int p = 0; p < 6; ++p) mg = fmax(mg, fabs(vals[21 + p]));
+    atomic_max_nonneg(&ctrl->max_grad_bits, mg);
+  }
 }
 
 // Gradient-tolerance check before the solve (optimizer_step.rs:382-384) and
@@ -553,7 +637,8 @@ __global__ void k_gradcheck(Ctrl* ctrl, int* fail) {
 // ---------------------------------------------------------------------------
 // Reduced camera system: one warp per lower 6x6 block (row j >= col k).
 //   S_jk = [j == k] (U_j + nu n_j I) - sum_{pairs} Z_a Z_b^T
-// FP32 products, float-float accumulation, f64 store (both triangles).
+// FP32 products and per-lane FP32 partial sums; float-float across lanes;
+// f64 store (both triangles).
 // ---------------------------------------------------------------------------
 struct SchurArgs {
   int64_t nsb;
@@ -568,56 +653,67 @@ struct SchurArgs {
   int n6;
 };
 
-__global__ void __launch_bounds__(256) k_schur(SchurArgs a, const Ctrl* ctrl) {
+__device__ __forceinline__ void load_z(const float* zmat, int g, float* z) {
+  const float4* p = reinterpret_cast<const float4*>(zmat + kZS * static_cast<int64_t>(g));
+#pragma unroll
+  for (int q = 0; q < 5; ++q) {
+    float4 v = __ldg(p + q);
+    z[4 * q] = v.x; z[4 * q + 1] = v.y; z[4 * q + 2] = v.z; z[4 * q + 3] = v.w;
+  }
+}
+
+__global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
+  __shared__ float red[8][36][33];
   const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const double nu = ctrl->nu;
-  for (int64_t blk = static_cast<int64_t>(blockIdx.x) * wpb + (threadIdx.x >> 5); blk < a.nsb;
+  for (int64_t blk = static_cast<int64_t>(blockIdx.x) * wpb + wib; blk < a.nsb;
        blk += static_cast<int64_t>(gridDim.x) * wpb) {
     const int j = a.sb_row[blk], k = a.sb_col[blk];
-    dd acc[36];
+    float acc[36];
 #pragma unroll
-    for (int e = 0; e < 36; ++e) acc[e] = dd_make(0.f, 0.f);
-    for (int64_t q = a.sb_pair_begin[blk] + lane; q < a.sb_pair_begin[blk + 1]; q += 32) {
+    for (int e = 0; e < 36; ++e) acc[e] = 0.f;
+    const int64_t q0 = a.sb_pair_begin[blk], q1 = a.sb_pair_begin[blk + 1];
+    for (int64_t q = q0 + lane; q < q1; q += 32) {
       const int2 pr = a.pairs[q];
-      const float* Za = a.zmat + 18 * static_cast<int64_t>(pr.x);
-      const float* Zb = a.zmat + 18 * static_cast<int64_t>(pr.y);
-      float za[18], zb[18];
-#pragma unroll
-      for (int e = 0; e < 18; e += 2) {
-        float2 x = *reinterpret_cast<const float2*>(Za + e);
-        float2 y = *reinterpret_cast<const float2*>(Zb + e);
-        za[e] = x.x; za[e + 1] = x.y;
-        zb[e] = y.x; zb[e + 1] = y.y;
-      }
+      float za[20], zb[20];
+      load_z(a.zmat, pr.x, za);
+      load_z(a.zmat, pr.y, zb);
 #pragma unroll
       for (int r = 0; r < 6; ++r)
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-          float p = za[r * 3 + 0] * zb[c * 3 + 0];
+          float p = acc[r * 6 + c];
+          p = fmaf(za[r * 3 + 0], zb[c * 3 + 0], p);
           p = fmaf(za[r * 3 + 1], zb[c * 3 + 1], p);
           p = fmaf(za[r * 3 + 2], zb[c * 3 + 2], p);
-          acc[r * 6 + c] = dd_add_f(acc[r * 6 + c], p);
+          acc[r * 6 + c] = p;
         }
     }
+    // transpose through shared memory; lane e (< 36) sums entry e in float-float
 #pragma unroll
-    for (int e = 0; e < 36; ++e) acc[e] = dd_warp_sum(acc[e]);
-    {
-      // every lane holds the 36 totals; lane e writes entries e and e + 32
-      for (int e = lane; e < 36; e += 32) {
-        const int r = e / 6, c = e % 6;
-        double v = -dd_to_double(acc[e]);
-        if (j == k) {
-          dd base = dd_from_double(a.ufull[36 * j + r * 6 + c]);
-          if (r == c) base = dd_add(base, dd_from_double(nu * a.cnt_f[j]));
-          v = dd_to_double(dd_sub(base, acc[e]));
-        }
-        const int64_t row = 6 * j + r, col = 6 * k + c;
-        a.S[row * a.n6 + col] = v;
-        a.S[col * a.n6 + row] = v;
+    for (int e = 0; e < 36; ++e) red[wib][e][lane] = acc[e];
+    __syncwarp();
+    for (int e = lane; e < 36; e += 32) {
+      dd t = dd_make(0.f, 0.f);
+#pragma unroll 8
+      for (int l = 0; l < 32; ++l) t = dd_add_f(t, red[wib][e][l]);
+      const int r = e / 6, c = e % 6;
+      double v;
+      if (j == k) {
+        dd base = dd_from_double(a.ufull[36 * j + r * 6 + c]);
+        if (r == c) base = dd_add(base, dd_from_double(nu * a.cnt_f[j]));
+        v = dd_to_double(dd_sub(base, t));
+      } else {
+        v = -dd_to_double(t);
       }
+      const int64_t row = 6 * j + r, col = 6 * k + c;
+      a.S[row * a.n6 + col] = v;
+      a.S[col * a.n6 + row] = v;
     }
+    __syncwarp();
   }
 }
 
@@ -632,17 +728,19 @@ struct BackArgs {
   const int32_t* pose_fb;
   const int32_t* pt_mb;
   const float* zmat;
-  const double* cinv;
-  const double* cvec;
-  const double* xf;
+  const float* cinv;
+  const float* cvec;
+  const float* xdd;  // dx_f as float-float pairs
   double* dm;
 };
 
 __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
+  __shared__ float red[8][6][33];
   const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
-  for (int64_t i = static_cast<int64_t>(blockIdx.x) * wpb + (threadIdx.x >> 5); i < a.np;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * wpb + wib; i < a.np;
        i += static_cast<int64_t>(gridDim.x) * wpb) {
     const int mb = a.pt_mb[i];
     if (mb < 0) continue;
@@ -650,28 +748,41 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
     for (int64_t g = a.pt_g_begin[i] + lane; g < a.pt_g_begin[i + 1]; g += 32) {
       const int fb = a.pose_fb[a.g_pose[g]];
       if (fb < 0) continue;
-      const float* Z = a.zmat + 18 * g;
+      float Z[20];
+      load_z(a.zmat, static_cast<int>(g), Z);
+      const float2* xp = reinterpret_cast<const float2*>(a.xdd) + 6 * fb;
+#pragma unroll
       for (int r = 0; r < 6; ++r) {
-        dd x = dd_from_double(a.xf[6 * fb + r]);
-        for (int s = 0; s < 3; ++s) t[s] = dd_add(t[s], dd_mul_f(x, Z[r * 3 + s]));
+        const float2 xv = xp[r];
+        const dd x = dd_make(xv.x, xv.y);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) t[q] = dd_add(t[q], dd_mul_f(x, Z[r * 3 + q]));
       }
     }
-    for (int s = 0; s < 3; ++s) t[s] = dd_warp_sum(t[s]);
+    float vals[6] = {t[0].hi, t[0].lo, t[1].hi, t[1].lo, t[2].hi, t[2].lo};
+#pragma unroll
+    for (int v = 0; v < 6; ++v) red[wib][v][lane] = vals[v];
+    __syncwarp();
     if (lane == 0) {
-      dd c0 = dd_sub(dd_from_double(a.cvec[3 * mb + 0]), t[0]);
-      dd c1 = dd_sub(dd_from_double(a.cvec[3 * mb + 1]), t[1]);
-      dd c2 = dd_sub(dd_from_double(a.cvec[3 * mb + 2]), t[2]);
-      const double* ci = a.cinv + 6 * mb;  // 00 10 11 20 21 22
-      dd i00 = dd_from_double(ci[0]), i10 = dd_from_double(ci[1]), i11 = dd_from_double(ci[2]);
-      dd i20 = dd_from_double(ci[3]), i21 = dd_from_double(ci[4]), i22 = dd_from_double(ci[5]);
+      dd s[3];
+      for (int q = 0; q < 3; ++q) {
+        s[q] = dd_make(0.f, 0.f);
+        for (int l = 0; l < 32; ++l) s[q] = dd_add(s[q], dd_make(red[wib][2 * q][l], red[wib][2 * q + 1][l]));
+      }
+      const float* cv = a.cvec + 6 * mb;
+      dd c0 = dd_sub(dd_make(cv[0], cv[1]), s[0]);
+      dd c1 = dd_sub(dd_make(cv[2], cv[3]), s[1]);
+      dd c2 = dd_sub(dd_make(cv[4], cv[5]), s[2]);
+      const float* ci = a.cinv + 6 * mb;  // 00 10 11 20 21 22
       // C^-T * c : (C^-T)[a][b] = Cinv[b][a]
-      dd d0 = dd_add(dd_add(dd_mul(i00, c0), dd_mul(i10, c1)), dd_mul(i20, c2));
-      dd d1 = dd_add(dd_mul(i11, c1), dd_mul(i21, c2));
-      dd d2 = dd_mul(i22, c2);
+      dd d0 = dd_add(dd_add(dd_mul_f(c0, ci[0]), dd_mul_f(c1, ci[1])), dd_mul_f(c2, ci[3]));
+      dd d1 = dd_add(dd_mul_f(c1, ci[2]), dd_mul_f(c2, ci[4]));
+      dd d2 = dd_mul_f(c2, ci[5]);
       a.dm[3 * mb + 0] = dd_to_double(d0);
       a.dm[3 * mb + 1] = dd_to_double(d1);
       a.dm[3 * mb + 2] = dd_to_double(d2);
     }
+    __syncwarp();
   }
 }
 
@@ -742,15 +853,15 @@ __global__ void __launch_bounds__(256) k_gauge_partials(GaugeArgs a, const Ctrl*
 
 __global__ void k_gauge_alpha(const double* part, int nblocks, Ctrl* ctrl) {
   if (skipping(ctrl)) return;
-  __shared__ double sn, sd;
+  dd n = dd_make(0.f, 0.f), d = dd_make(0.f, 0.f);
+  for (int q = threadIdx.x; q < nblocks; q += 32) {
+    n = dd_add(n, dd_from_double(part[2 * q]));
+    d = dd_add(d, dd_from_double(part[2 * q + 1]));
+  }
+  n = dd_warp_sum(n);
+  d = dd_warp_sum(d);
   if (threadIdx.x == 0) {
-    dd n = dd_make(0.f, 0.f), d = dd_make(0.f, 0.f);
-    for (int q = 0; q < nblocks; ++q) {
-      n = dd_add(n, dd_from_double(part[2 * q]));
-      d = dd_add(d, dd_from_double(part[2 * q + 1]));
-    }
-    sn = dd_to_double(n);
-    sd = dd_to_double(d);
+    const double sn = dd_to_double(n), sd = dd_to_double(d);
     ctrl->alpha = (sd > 0.0) ? sn / sd : 0.0;
   }
 }
@@ -828,21 +939,29 @@ __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
       }
     }
   }
-  atomic_max_nonneg(&ctrl->max_step_bits, mx);
   __shared__ float sh[4][8];
+  __shared__ double shm[8];
   sdd = dd_warp_sum(sdd);
   sdg = dd_warp_sum(sdg);
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, off));
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) { sh[0][w] = sdd.hi; sh[1][w] = sdd.lo; sh[2][w] = sdg.hi; sh[3][w] = sdg.lo; }
+  if (lane == 0) {
+    sh[0][w] = sdd.hi; sh[1][w] = sdd.lo; sh[2][w] = sdg.hi; sh[3][w] = sdg.lo;
+    shm[w] = mx;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     dd s0 = dd_make(0.f, 0.f), s1 = dd_make(0.f, 0.f);
+    double m = 0.0;
     for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
       s0 = dd_add(s0, dd_make(sh[0][q], sh[1][q]));
       s1 = dd_add(s1, dd_make(sh[2][q], sh[3][q]));
+      m = fmax(m, shm[q]);
     }
     a.part[2 * blockIdx.x] = dd_to_double(s0);
     a.part[2 * blockIdx.x + 1] = dd_to_double(s1);
+    atomic_max_nonneg(&ctrl->max_step_bits, m);
   }
 }
 
@@ -857,14 +976,18 @@ __global__ void k_decide(const double* cost_part, int n_cost, const double* upd_
   double new_merit = 0.0;
   if (skip == 0) new_merit = block_sum_partials(cost_part, n_cost);
   __shared__ double s_dd, s_dg;
-  if (skip == 0 && threadIdx.x == 0) {
+  if (skip == 0 && threadIdx.x < 32) {
     dd a = dd_make(0.f, 0.f), b = dd_make(0.f, 0.f);
-    for (int q = 0; q < n_upd; ++q) {
+    for (int q = threadIdx.x; q < n_upd; q += 32) {
       a = dd_add(a, dd_from_double(upd_part[2 * q]));
       b = dd_add(b, dd_from_double(upd_part[2 * q + 1]));
     }
-    s_dd = dd_to_double(a);
-    s_dg = dd_to_double(b);
+    a = dd_warp_sum(a);
+    b = dd_warp_sum(b);
+    if (threadIdx.x == 0) {
+      s_dd = dd_to_double(a);
+      s_dg = dd_to_double(b);
+    }
   }
   __syncthreads();
   if (threadIdx.x != 0) return;
@@ -1066,8 +1189,8 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
     k_camera_tiles<<<static_cast<unsigned>(s.ntiles), kTileThreads, 0, st>>>(ca, d.ctrl);
     ++n;
   }
-  k_camera_finalize<<<(s.nf + 63) / 64, 64, 0, st>>>(s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf,
-                                                     d.rb, d.ctrl, use_override ? 0 : 1);
+  k_camera_finalize<<<s.nf, 64, 0, st>>>(s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf, d.rb, d.ctrl,
+                                         use_override ? 0 : 1);
   ++n;
   if (!use_override) {
     k_gradcheck<<<1, 1, 0, st>>>(d.ctrl, &d.ctrl->fail);
@@ -1103,7 +1226,7 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
   b.zmat = d.zmat;
   b.cinv = d.cinv;
   b.cvec = d.cvec;
-  b.xf = d.x;
+  b.xdd = d.xdd;
   b.dm = d.dm;
   k_backsub<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(b, d.ctrl);
   ++n;
@@ -1150,6 +1273,86 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
   k_apply_update<<<kUpdBlocks, 256, 0, st>>>(u, d.ctrl);
   ++n;
   return n;
+}
+
+int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) {
+  switch (kernel_id) {
+    case 1:
+      return launch_schur(s, d, st);
+    case 2: {
+      LinArgs la;
+      la.np = s.np;
+      la.pt_g_begin = d.pt_g_begin;
+      la.g_begin = d.g_begin;
+      la.g_pose = d.g_pose;
+      la.pose_fb = d.pose_fb;
+      la.pt_mb = d.pt_mb;
+      la.cnt_m = d.cnt_m;
+      la.pose_f = d.pose_f;
+      la.points = d.points;
+      la.res = d.res;
+      la.fx = static_cast<float>(s.intr[0]);
+      la.fy = static_cast<float>(s.intr[1]);
+      la.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
+      la.zmat = d.zmat;
+      la.cinv = d.cinv;
+      la.cvec = d.cvec;
+      la.bm = d.bm;
+      la.nu_override = 0.0;
+      la.use_override = 0;
+      la.fail = &d.ctrl->fail;
+      k_landmark<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(la, d.ctrl);
+      return 1;
+    }
+    case 3: {
+      if (s.ntiles == 0) return 0;
+      CamArgs ca;
+      ca.tile_fb = d.tile_fb;
+      ca.tile_begin = d.tile_begin;
+      ca.tile_end = d.tile_end;
+      ca.cam_g = d.cam_g;
+      ca.g_begin = d.g_begin;
+      ca.g_pt = d.g_pt;
+      ca.fb_pose = d.fb_pose;
+      ca.pt_mb = d.pt_mb;
+      ca.pose_f = d.pose_f;
+      ca.points = d.points;
+      ca.res = d.res;
+      ca.zmat = d.zmat;
+      ca.cvec = d.cvec;
+      ca.fx = static_cast<float>(s.intr[0]);
+      ca.fy = static_cast<float>(s.intr[1]);
+      ca.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
+      ca.tile_part = d.tile_part;
+      ca.with_schur = 1;
+      k_camera_tiles<<<static_cast<unsigned>(s.ntiles), kTileThreads, 0, st>>>(ca, d.ctrl);
+      return 1;
+    }
+    case 4: {
+      CostArgs a = make_cost_args(s, d, d.points_t, d.res_t, d.part + 4 * kUpdBlocks, 1);
+      k_cost<<<cost_grid(s.no), kCostThreads, 0, st>>>(a, d.ctrl);
+      return 1;
+    }
+    case 5:
+      return launch_factor_solve(s, d, st);
+    case 6: {
+      BackArgs b;
+      b.np = s.np;
+      b.pt_g_begin = d.pt_g_begin;
+      b.g_pose = d.g_pose;
+      b.pose_fb = d.pose_fb;
+      b.pt_mb = d.pt_mb;
+      b.zmat = d.zmat;
+      b.cinv = d.cinv;
+      b.cvec = d.cvec;
+      b.xdd = d.xdd;
+      b.dm = d.dm;
+      k_backsub<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(b, d.ctrl);
+      return 1;
+    }
+    default:
+      return 0;
+  }
 }
 
 int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {

@@ -102,8 +102,18 @@ EXPORTED = [
     "sgba_optimizer_init", "sgba_optimizer_step", "sgba_optimize", "sgba_get_variables",
     "sgba_get_cost", "sgba_set_variables", "sgba_get_layout", "sgba_export_pattern",
     "sgba_debug_last_system", "sgba_state_save", "sgba_state_load", "sgba_get_profile",
-    "sgba_set_profiling", "sgba_synth_generate", "sgba_synth_free",
+    "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_synth_generate",
+    "sgba_synth_free",
 ]
+
+# sgba_kernel_id
+KERNEL_ITERATION = 0
+KERNEL_SCHUR = 1
+KERNEL_LANDMARK = 2
+KERNEL_CAMERA = 3
+KERNEL_COST = 4
+KERNEL_FACTOR = 5
+KERNEL_BACKSUB = 6
 
 
 class SgbaError(RuntimeError):
@@ -146,6 +156,8 @@ def lib():
     L.sgba_state_load.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
     L.sgba_get_profile.argtypes = [C.c_void_p, C.POINTER(Profile)]
     L.sgba_set_profiling.argtypes = [C.c_void_p, C.c_int32]
+    L.sgba_bench_iterations.argtypes = [C.c_void_p, C.c_int32, C.c_int32, dp, C.POINTER(C.c_int64)]
+    L.sgba_bench_kernel.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, dp]
     _lib = L
     return L
 
@@ -316,3 +328,16 @@ class Problem:
         p = Profile()
         check(lib().sgba_get_profile(self._h, C.byref(p)))
         return p
+
+    def bench_iterations(self, iters, flush_l2=True):
+        """Device ms summed over `iters` LM iterations, and the kernel launch count."""
+        ms = C.c_double()
+        n = C.c_int64()
+        check(lib().sgba_bench_iterations(self._h, int(iters), 1 if flush_l2 else 0, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def bench_kernel(self, kernel, reps, flush_l2=True):
+        """Mean device ms of one launch of `kernel` (sgba_kernel_id) on the current data."""
+        ms = C.c_double()
+        check(lib().sgba_bench_kernel(self._h, int(kernel), int(reps), 1 if flush_l2 else 0, C.byref(ms)))
+        return ms.value
