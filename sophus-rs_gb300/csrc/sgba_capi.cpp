@@ -383,7 +383,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_alloc(p, &d.pose_f, 12 * static_cast<size_t>(P.nc)))) return st;
   if ((st = dev_alloc(p, &d.pose_dd, 24 * static_cast<size_t>(P.nc)))) return st;
   if ((st = dev_alloc(p, &d.zmat, 20 * static_cast<size_t>(P.ng)))) return st;
-  if ((st = dev_alloc(p, &d.cinv, 6 * static_cast<size_t>(P.nm)))) return st;
+  if ((st = dev_alloc(p, &d.cinv, 12 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.cvec, 6 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.bm, 3 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.dm, 3 * static_cast<size_t>(P.nm)))) return st;

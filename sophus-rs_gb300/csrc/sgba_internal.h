@@ -113,7 +113,7 @@ struct Dev {
   float* pose_f = nullptr;         // nc*12: R_cw (row-major) + t_cw, float
   float* pose_dd = nullptr;        // nc*24: R_cw + t_cw as (hi,lo) pairs
   float* zmat = nullptr;           // ng*20: Z = W C^-T (6x3 row-major, padded to 20 floats)
-  float* cinv = nullptr;           // nm*6: C^-1 lower (00,10,11,20,21,22), FP32
+  float* cinv = nullptr;           // nm*12: C^-1 lower (00,10,11,20,21,22) as float-float pairs
   float* cvec = nullptr;           // nm*6: C^-1 b_m as float-float pairs
   double* bm = nullptr;            // nm*3: neg_grad of points
   double* bf = nullptr;            // nf*6: neg_grad of poses

@@ -178,6 +178,42 @@ __device__ __forceinline__ dd shfl_dd(dd v, int src) {
   return o;
 }
 
+// The same Jacobians in float-float, for ill-conditioned point blocks.
+struct JacD {
+  dd jp[12];
+  dd jm[6];
+};
+__device__ void jacobians_dd(const float* Pd /*R_cw 9 + t_cw 3, (hi, lo) pairs*/, dd px, dd py, dd pz, dd fx, dd fy,
+                             JacD* J) {
+  dd R[9], t[3];
+  for (int i = 0; i < 9; ++i) R[i] = dd_make(Pd[2 * i], Pd[2 * i + 1]);
+  for (int i = 0; i < 3; ++i) t[i] = dd_make(Pd[18 + 2 * i], Pd[18 + 2 * i + 1]);
+  dd xc = dd_add(dd_add(dd_add(dd_mul(R[0], px), dd_mul(R[1], py)), dd_mul(R[2], pz)), t[0]);
+  dd yc = dd_add(dd_add(dd_add(dd_mul(R[3], px), dd_mul(R[4], py)), dd_mul(R[5], pz)), t[1]);
+  dd zc = dd_add(dd_add(dd_add(dd_mul(R[6], px), dd_mul(R[7], py)), dd_mul(R[8], pz)), t[2]);
+  dd iz = dd_div(dd_make(1.0f, 0.0f), zc);
+  dd iz2 = dd_mul(iz, iz);
+  dd a0 = dd_mul(fx, iz), a2 = dd_neg(dd_mul(dd_mul(fx, xc), iz2));
+  dd b1 = dd_mul(fy, iz), b2 = dd_neg(dd_mul(dd_mul(fy, yc), iz2));
+  dd D[6];
+  for (int k = 0; k < 3; ++k) {
+    D[k] = dd_add(dd_mul(a0, R[0 * 3 + k]), dd_mul(a2, R[2 * 3 + k]));
+    D[3 + k] = dd_add(dd_mul(b1, R[1 * 3 + k]), dd_mul(b2, R[2 * 3 + k]));
+  }
+  for (int r = 0; r < 2; ++r) {
+    const dd* d = D + 3 * r;
+    J->jp[r * 6 + 0] = dd_add(dd_neg(dd_mul(d[1], pz)), dd_mul(d[2], py));
+    J->jp[r * 6 + 1] = dd_sub(dd_mul(d[0], pz), dd_mul(d[2], px));
+    J->jp[r * 6 + 2] = dd_add(dd_neg(dd_mul(d[0], py)), dd_mul(d[1], px));
+    J->jp[r * 6 + 3] = d[0];
+    J->jp[r * 6 + 4] = d[1];
+    J->jp[r * 6 + 5] = d[2];
+    J->jm[r * 3 + 0] = dd_neg(d[0]);
+    J->jm[r * 3 + 1] = dd_neg(d[1]);
+    J->jm[r * 3 + 2] = dd_neg(d[2]);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Pose tables: T_cw = T_wc^-1 in f64, published as float and float-float.
 // ---------------------------------------------------------------------------
@@ -328,11 +364,13 @@ struct LinArgs {
   const int32_t* pt_mb;
   const double* cnt_m;
   const float* pose_f;
+  const float* pose_dd;
   const double* points;
   const float2* res;
   float fx, fy, huber;
+  dd fxd, fyd;
   float* zmat;
-  float* cinv;   // 6 floats per point: C^-1 (00 10 11 20 21 22)
+  float* cinv;   // 6 float-float per point: C^-1 (00 10 11 20 21 22)
   float* cvec;   // 3 float-float per point: C^-1 b_m
   double* bm;
   double nu_override;
@@ -381,14 +419,9 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
     // damping nu * (number of reduced terms) on the diagonal (entries 0, 3, 5)
     if (lane == 0 || lane == 3 || lane == 5) tot = dd_add(tot, dd_from_double(nu * a.cnt_m[mb]));
     if (lane >= 6) tot = dd_neg(tot);  // neg_grad b_m = -sum J^T r~
-    // broadcast: V as floats, b as float-float
-    float V[6];
+    dd Vd[6], b[3];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      dd t = shfl_dd(tot, k);
-      V[k] = t.hi + t.lo;
-    }
-    dd b[3];
+    for (int k = 0; k < 6; ++k) Vd[k] = shfl_dd(tot, k);
 #pragma unroll
     for (int k = 0; k < 3; ++k) b[k] = shfl_dd(tot, 6 + k);
     if (lane == 0) {
@@ -398,35 +431,110 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
       bp[2] = dd_to_double(b[2]);
       warp_max = fmax(warp_max, fmax(fabs(bp[0]), fmax(fabs(bp[1]), fabs(bp[2]))));
     }
-    // Cholesky V' = C C^T in FP32  (V layout: 00 01 02 11 12 22)
-    const float c00 = sqrtf(V[0]);
-    const float c10 = V[1] / c00, c20 = V[2] / c00;
-    const float t11 = V[3] - c10 * c10;
-    const float c11 = sqrtf(t11);
-    const float c21 = (V[4] - c20 * c10) / c11;
-    const float t22 = V[5] - c20 * c20 - c21 * c21;
-    const float c22 = sqrtf(t22);
-    const bool ok = V[0] > 0.f && t11 > 0.f && t22 > 0.f && isfinite(c00) && isfinite(c11) && isfinite(c22) &&
-                    isfinite(c10) && isfinite(c20) && isfinite(c21);
+    // Cholesky V' = C C^T (V layout: 00 01 02 11 12 22).  FP32 when the point
+    // block is well conditioned; float-float when a pivot lost more than three
+    // digits to cancellation (e.g. a point seen once: its depth is held only by
+    // the damping).  The branch is uniform across the warp.
+    float V[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) V[k] = Vd[k].hi + Vd[k].lo;
+    float c00 = sqrtf(V[0]);
+    float c10 = V[1] / c00, c20 = V[2] / c00;
+    float t11 = V[3] - c10 * c10;
+    float c11 = sqrtf(t11);
+    float c21 = (V[4] - c20 * c10) / c11;
+    float t22 = V[5] - c20 * c20 - c21 * c21;
+    const bool well = V[0] > 0.f && t11 > 1e-3f * V[3] && t22 > 1e-3f * V[5];
+    const dd pxd = dd_from_double(a.points[3 * i + 0]);
+    const dd pyd = dd_from_double(a.points[3 * i + 1]);
+    const dd pzd = dd_from_double(a.points[3 * i + 2]);
+    if (!well) {
+      // The FP32 Jacobians leave a rounding-level component of the gradient and
+      // of W along the weakly constrained direction, which 1/(nu n) would
+      // amplify: rebuild the whole point block in float-float.
+      dd acc[9];
+      for (int k = 0; k < 9; ++k) acc[k] = dd_make(0.f, 0.f);
+      for (int64_t g = g0 + lane; g < g1; g += 32) {
+        const float* Pd = a.pose_dd + 24 * a.g_pose[g];
+        for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+          JacD J;
+          jacobians_dd(Pd, pxd, pyd, pzd, a.fxd, a.fyd, &J);
+          float2 r = a.res[o];
+          float w = huber_weight_f(a.huber, r.x, r.y);
+          const float r0 = w * r.x, r1 = w * r.y;
+          const dd* m = J.jm;
+          acc[0] = dd_add(acc[0], dd_add(dd_mul(m[0], m[0]), dd_mul(m[3], m[3])));
+          acc[1] = dd_add(acc[1], dd_add(dd_mul(m[0], m[1]), dd_mul(m[3], m[4])));
+          acc[2] = dd_add(acc[2], dd_add(dd_mul(m[0], m[2]), dd_mul(m[3], m[5])));
+          acc[3] = dd_add(acc[3], dd_add(dd_mul(m[1], m[1]), dd_mul(m[4], m[4])));
+          acc[4] = dd_add(acc[4], dd_add(dd_mul(m[1], m[2]), dd_mul(m[4], m[5])));
+          acc[5] = dd_add(acc[5], dd_add(dd_mul(m[2], m[2]), dd_mul(m[5], m[5])));
+          acc[6] = dd_add(acc[6], dd_add(dd_mul_f(m[0], r0), dd_mul_f(m[3], r1)));
+          acc[7] = dd_add(acc[7], dd_add(dd_mul_f(m[1], r0), dd_mul_f(m[4], r1)));
+          acc[8] = dd_add(acc[8], dd_add(dd_mul_f(m[2], r0), dd_mul_f(m[5], r1)));
+        }
+      }
+      for (int k = 0; k < 9; ++k) acc[k] = dd_warp_sum(acc[k]);
+      const dd damp = dd_from_double(nu * a.cnt_m[mb]);
+      for (int k = 0; k < 6; ++k) Vd[k] = acc[k];
+      Vd[0] = dd_add(Vd[0], damp);
+      Vd[3] = dd_add(Vd[3], damp);
+      Vd[5] = dd_add(Vd[5], damp);
+      for (int k = 0; k < 3; ++k) b[k] = dd_neg(acc[6 + k]);
+      if (lane == 0) {
+        double* bp = a.bm + 3 * mb;
+        bp[0] = dd_to_double(b[0]);
+        bp[1] = dd_to_double(b[1]);
+        bp[2] = dd_to_double(b[2]);
+      }
+    }
+    dd I[6];  // C^-1 (00 10 11 20 21 22)
+    bool ok;
+    if (well) {
+      const float c22 = sqrtf(t22);
+      const float i00 = 1.f / c00, i11 = 1.f / c11, i22 = 1.f / c22;
+      const float i10 = -c10 * i00 * i11;
+      const float i21 = -c21 * i11 * i22;
+      const float i20 = -(c20 * i00 + c21 * i10) * i22;
+      ok = isfinite(i00) && isfinite(i11) && isfinite(i22) && isfinite(i10) && isfinite(i20) && isfinite(i21);
+      I[0] = dd_from_float(i00); I[1] = dd_from_float(i10); I[2] = dd_from_float(i11);
+      I[3] = dd_from_float(i20); I[4] = dd_from_float(i21); I[5] = dd_from_float(i22);
+    } else {
+      ok = Vd[0].hi > 0.0f;
+      dd e00 = dd_sqrt(Vd[0]);
+      dd e10 = dd_div(Vd[1], e00), e20 = dd_div(Vd[2], e00);
+      dd u11 = dd_sub(Vd[3], dd_mul(e10, e10));
+      ok = ok && u11.hi > 0.0f;
+      dd e11 = dd_sqrt(u11);
+      dd e21 = dd_div(dd_sub(Vd[4], dd_mul(e20, e10)), e11);
+      dd u22 = dd_sub(dd_sub(Vd[5], dd_mul(e20, e20)), dd_mul(e21, e21));
+      ok = ok && u22.hi > 0.0f;
+      dd e22 = dd_sqrt(u22);
+      const dd one = dd_make(1.0f, 0.0f);
+      I[0] = dd_div(one, e00);
+      I[2] = dd_div(one, e11);
+      I[5] = dd_div(one, e22);
+      I[1] = dd_neg(dd_div(dd_mul(e10, I[0]), e11));
+      I[4] = dd_neg(dd_div(dd_mul(e21, I[2]), e22));
+      I[3] = dd_neg(dd_div(dd_add(dd_mul(e20, I[0]), dd_mul(e21, I[1])), e22));
+      for (int k = 0; k < 6; ++k) ok = ok && isfinite(I[k].hi);
+    }
     if (!ok) {
       if (lane == 0 && !a.use_override) atomicExch(a.fail, 1);
       continue;
     }
-    // C^-1 (lower)
-    const float i00 = 1.f / c00, i11 = 1.f / c11, i22 = 1.f / c22;
-    const float i10 = -c10 * i00 * i11;
-    const float i21 = -c21 * i11 * i22;
-    const float i20 = -(c20 * i00 + c21 * i10) * i22;
     if (lane == 0) {
-      float* ci = a.cinv + 6 * mb;
-      ci[0] = i00; ci[1] = i10; ci[2] = i11; ci[3] = i20; ci[4] = i21; ci[5] = i22;
+      float* ci = a.cinv + 12 * mb;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) { ci[2 * k] = I[k].hi; ci[2 * k + 1] = I[k].lo; }
       // c = C^-1 b in float-float
-      dd cv0 = dd_mul_f(b[0], i00);
-      dd cv1 = dd_add(dd_mul_f(b[0], i10), dd_mul_f(b[1], i11));
-      dd cv2 = dd_add(dd_add(dd_mul_f(b[0], i20), dd_mul_f(b[1], i21)), dd_mul_f(b[2], i22));
+      dd cv0 = dd_mul(b[0], I[0]);
+      dd cv1 = dd_add(dd_mul(b[0], I[1]), dd_mul(b[1], I[2]));
+      dd cv2 = dd_add(dd_add(dd_mul(b[0], I[3]), dd_mul(b[1], I[4])), dd_mul(b[2], I[5]));
       float* cvp = a.cvec + 6 * mb;
       cvp[0] = cv0.hi; cvp[1] = cv0.lo; cvp[2] = cv1.hi; cvp[3] = cv1.lo; cvp[4] = cv2.hi; cvp[5] = cv2.lo;
     }
+    const float i00 = I[0].hi, i10 = I[1].hi, i11 = I[2].hi, i20 = I[3].hi, i21 = I[4].hi, i22 = I[5].hi;
     if (a.use_override) continue;  // final Hessian pass: no Schur data
     // pass 2: Z_g = W_g C^-T for terms with a free pose
     for (int64_t g = g0 + lane; g < g1; g += 32) {
@@ -434,23 +542,45 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
       if (a.pose_fb[pj] < 0) continue;
       const float* P = a.pose_f + 12 * pj;
       float W[18];
-#pragma unroll
-      for (int k = 0; k < 18; ++k) W[k] = 0.f;
-      for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
-        JacF J;
-        jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
-#pragma unroll
-        for (int r = 0; r < 6; ++r)
-#pragma unroll
-          for (int q = 0; q < 3; ++q) W[r * 3 + q] += J.jp[r] * J.jm[q] + J.jp[6 + r] * J.jm[3 + q];
-      }
-      // Z[r][t] = sum_{s<=t} W[r][s] * Cinv[t][s]
       float Z[20];
+      if (well) {
 #pragma unroll
-      for (int r = 0; r < 6; ++r) {
-        Z[r * 3 + 0] = W[r * 3 + 0] * i00;
-        Z[r * 3 + 1] = W[r * 3 + 0] * i10 + W[r * 3 + 1] * i11;
-        Z[r * 3 + 2] = W[r * 3 + 0] * i20 + W[r * 3 + 1] * i21 + W[r * 3 + 2] * i22;
+        for (int k = 0; k < 18; ++k) W[k] = 0.f;
+        for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+          JacF J;
+          jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+#pragma unroll
+          for (int r = 0; r < 6; ++r)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) W[r * 3 + q] += J.jp[r] * J.jm[q] + J.jp[6 + r] * J.jm[3 + q];
+        }
+        // Z[r][t] = sum_{s<=t} W[r][s] * Cinv[t][s]
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+          Z[r * 3 + 0] = W[r * 3 + 0] * i00;
+          Z[r * 3 + 1] = W[r * 3 + 0] * i10 + W[r * 3 + 1] * i11;
+          Z[r * 3 + 2] = W[r * 3 + 0] * i20 + W[r * 3 + 1] * i21 + W[r * 3 + 2] * i22;
+        }
+      } else {
+        // W and Z in float-float: the large entries of C^-1 cancel against W
+        dd Wd[18];
+        for (int k = 0; k < 18; ++k) Wd[k] = dd_make(0.f, 0.f);
+        const float* Pd = a.pose_dd + 24 * pj;
+        for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+          JacD J;
+          jacobians_dd(Pd, pxd, pyd, pzd, a.fxd, a.fyd, &J);
+          for (int r = 0; r < 6; ++r)
+            for (int q = 0; q < 3; ++q)
+              Wd[r * 3 + q] = dd_add(Wd[r * 3 + q], dd_add(dd_mul(J.jp[r], J.jm[q]), dd_mul(J.jp[6 + r], J.jm[3 + q])));
+        }
+        for (int r = 0; r < 6; ++r) {
+          dd z0 = dd_mul(I[0], Wd[r * 3 + 0]);
+          dd z1 = dd_add(dd_mul(I[1], Wd[r * 3 + 0]), dd_mul(I[2], Wd[r * 3 + 1]));
+          dd z2 = dd_add(dd_add(dd_mul(I[3], Wd[r * 3 + 0]), dd_mul(I[4], Wd[r * 3 + 1])), dd_mul(I[5], Wd[r * 3 + 2]));
+          Z[r * 3 + 0] = z0.hi + z0.lo;
+          Z[r * 3 + 1] = z1.hi + z1.lo;
+          Z[r * 3 + 2] = z2.hi + z2.lo;
+        }
       }
       Z[18] = 0.f;
       Z[19] = 0.f;
@@ -773,11 +903,13 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
       dd c0 = dd_sub(dd_make(cv[0], cv[1]), s[0]);
       dd c1 = dd_sub(dd_make(cv[2], cv[3]), s[1]);
       dd c2 = dd_sub(dd_make(cv[4], cv[5]), s[2]);
-      const float* ci = a.cinv + 6 * mb;  // 00 10 11 20 21 22
+      const float* cp = a.cinv + 12 * mb;  // 00 10 11 20 21 22 as (hi, lo)
+      dd ci[6];
+      for (int k = 0; k < 6; ++k) ci[k] = dd_make(cp[2 * k], cp[2 * k + 1]);
       // C^-T * c : (C^-T)[a][b] = Cinv[b][a]
-      dd d0 = dd_add(dd_add(dd_mul_f(c0, ci[0]), dd_mul_f(c1, ci[1])), dd_mul_f(c2, ci[3]));
-      dd d1 = dd_add(dd_mul_f(c1, ci[2]), dd_mul_f(c2, ci[4]));
-      dd d2 = dd_mul_f(c2, ci[5]);
+      dd d0 = dd_add(dd_add(dd_mul(c0, ci[0]), dd_mul(c1, ci[1])), dd_mul(c2, ci[3]));
+      dd d1 = dd_add(dd_mul(c1, ci[2]), dd_mul(c2, ci[4]));
+      dd d2 = dd_mul(c2, ci[5]);
       a.dm[3 * mb + 0] = dd_to_double(d0);
       a.dm[3 * mb + 1] = dd_to_double(d1);
       a.dm[3 * mb + 2] = dd_to_double(d2);
@@ -1153,6 +1285,9 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
   la.cnt_m = d.cnt_m;
   la.pose_f = d.pose_f;
   la.points = d.points;
+  la.pose_dd = d.pose_dd;
+  la.fxd = dd_make(static_cast<float>(s.intr[0]), static_cast<float>(s.intr[0] - static_cast<float>(s.intr[0])));
+  la.fyd = dd_make(static_cast<float>(s.intr[1]), static_cast<float>(s.intr[1] - static_cast<float>(s.intr[1])));
   la.res = d.res;
   la.fx = static_cast<float>(s.intr[0]);
   la.fy = static_cast<float>(s.intr[1]);
@@ -1290,6 +1425,9 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) 
       la.cnt_m = d.cnt_m;
       la.pose_f = d.pose_f;
       la.points = d.points;
+      la.pose_dd = d.pose_dd;
+      la.fxd = dd_make(static_cast<float>(s.intr[0]), static_cast<float>(s.intr[0] - static_cast<float>(s.intr[0])));
+      la.fyd = dd_make(static_cast<float>(s.intr[1]), static_cast<float>(s.intr[1] - static_cast<float>(s.intr[1])));
       la.res = d.res;
       la.fx = static_cast<float>(s.intr[0]);
       la.fy = static_cast<float>(s.intr[1]);

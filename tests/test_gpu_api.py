@@ -1,0 +1,172 @@
+"""GPU tests of the public API: the sophus_opt mirrors (Python and C++),
+stepping and resume, input validation, termination reasons and the LM step
+against an f64 LDLT of the same reduced camera system."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import fixed_iter_params
+
+pytestmark = pytest.mark.gpu
+
+COST_RTOL = 1e-6
+
+
+def _circle(pkg, n_cam=8, n_pt=300, seed=11):
+    return pkg.synth.generate(pkg.synth.CIRCLE, n_cam=n_cam, n_pt=n_pt, seed=seed)
+
+
+def test_cpp_mirror_restated_reference_tests(pkg):
+    import __graft_entry__ as graft
+
+    exe = graft.build_host_tests()
+    res = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    print(res.stdout)
+    assert res.returncode == 0, res.stdout + res.stderr
+
+
+def test_python_mirror_optimize_nlls_matches_oracle(pkg, oracle):
+    prob = _circle(pkg)
+    K = pkg.VarKind
+    variables = (pkg.VarBuilder.new()
+                 .add_family("cams", pkg.VarFamily.new(K.Conditioned, [pkg.PinholeCameraF64(prob.intrinsics)]))
+                 .add_family("poses", pkg.VarFamily.new_with_const_ids(
+                     K.Free, [pkg.Isometry3F64(p) for p in prob.poses], [0]))
+                 .add_family("points", pkg.VarFamily.new(K.Marginalized, prob.points))
+                 .build())
+    idx = np.stack([np.zeros(prob.n_obs, np.int64), prob.obs_cam, prob.obs_pt], axis=1)
+    terms = pkg.CostTerms.new(["cams", "poses", "points"], pkg.PinholeReprojectionTerms(prob.obs_uv, idx))
+    cost = pkg.CostFn.new_boxed_robust((), terms, pkg.RobustKernel.Huber(pkg.HuberKernel.new(1.0)))
+    params = fixed_iter_params(pkg, 8, 1e-4)
+    sol = pkg.optimize_nlls(variables, [cost], [], params)
+    orecs, oposes, opoints = oracle.optimize(prob, params)
+    g = np.array([s.merit for s in sol.steps])
+    o = np.array([r.merit for r in orecs])
+    assert np.max(np.abs(g - o) / o) < COST_RTOL
+    assert sol.steps[-1].termination == pkg.TerminationReason.MaxIterations
+    np.testing.assert_allclose(sol.variables.get_members("points"), opoints, atol=1e-4)
+
+
+def test_stepper_and_state_resume(pkg):
+    prob = _circle(pkg, seed=12)
+    params = fixed_iter_params(pkg, 50, 1e-4)
+    with pkg.native.Problem(prob, device=0) as gp:
+        gp.init(params)
+        first = [gp.step().merit for _ in range(3)]
+        blob = gp.state_save()
+        tail_a = [gp.step().merit for _ in range(3)]
+        gp.state_load(blob)
+        tail_b = [gp.step().merit for _ in range(3)]
+    assert tail_a == tail_b
+    assert first[-1] >= tail_a[0]
+
+
+def test_invalid_inputs_are_rejected(pkg):
+    E = pkg.native.SgbaError
+    base = _circle(pkg, n_cam=4, n_pt=30, seed=13)
+    bad = base.copy()
+    bad.obs_pt[5] = base.n_pt  # out of range
+    with pytest.raises(E) as e:
+        pkg.native.Problem(bad, device=0)
+    assert e.value.status == pkg.native.ERR_INVALID_ARGUMENT
+    bad = base.copy()
+    bad.poses[1, :4] *= 1.01  # |q| != 1
+    with pytest.raises(E) as e:
+        pkg.native.Problem(bad, device=0)
+    assert e.value.status == pkg.native.ERR_INVALID_PARAMS
+    bad = base.copy()
+    bad.obs_uv[3, 1] = np.nan
+    with pytest.raises(E) as e:
+        pkg.native.Problem(bad, device=0)
+    assert e.value.status == pkg.native.ERR_INVALID_ARGUMENT
+    bad = base.copy()
+    bad.point_const = np.ones(base.n_pt, np.uint8)  # nothing marginalized
+    with pkg.native.Problem(bad, device=0) as gp:
+        with pytest.raises(E) as e:
+            gp.init(fixed_iter_params(pkg, 2, 1e-4))
+        assert e.value.status == pkg.native.ERR_SCHUR_MISSING_FREE_OR_MARG
+
+
+def test_empty_and_degenerate_points(pkg, oracle):
+    """A point with one observation (rank-2 H_mm, made PD only by the damping)
+    and a point with no observation at all (zero H_mm: every solve fails, every
+    step is rejected, as SingularMargBlock makes the reference reject).
+
+    The single-view point's depth is held by nu = 1e-4 alone (condition number
+    ~1e8); its block is rebuilt in float-float, but the FP32 pose-side products
+    of its observation still perturb the reduced system at the 1e-4 level, so
+    this case is held to 1e-3 per iteration and 1e-5 at the end instead of the
+    1e-6 bar of well-posed problems (every point seen at least twice)."""
+    prob = _circle(pkg, n_cam=6, n_pt=80, seed=14)
+    keep = np.ones(prob.n_obs, bool)
+    first = np.where(prob.obs_pt == 3)[0]
+    keep[first[1:]] = False  # point 3 keeps a single observation
+    prob.obs_cam, prob.obs_pt, prob.obs_uv = prob.obs_cam[keep], prob.obs_pt[keep], prob.obs_uv[keep]
+    params = fixed_iter_params(pkg, 6, 1e-4)
+    with pkg.native.Problem(prob, device=0) as gp:
+        grecs, _ = gp.optimize(params)
+    orecs, _, _ = oracle.optimize(prob, params)
+    g, o = np.array([r.merit for r in grecs]), np.array([r.merit for r in orecs])
+    assert np.all(np.isfinite(g)) and all(r.accepted for r in grecs[:4])
+    assert np.max(np.abs(g - o) / o) < 1e-3
+    assert abs(g[-1] - o[-1]) / o[-1] < 1e-5
+    # orphan point: no term touches it
+    empty = prob.copy()
+    empty.obs_cam = empty.obs_cam[empty.obs_pt != 5]
+    empty.obs_uv = empty.obs_uv[empty.obs_pt != 5]
+    empty.obs_pt = empty.obs_pt[empty.obs_pt != 5]
+    with pkg.native.Problem(empty, device=0) as gp:
+        recs, term = gp.optimize(fixed_iter_params(pkg, 4, 1e-4))
+    assert all(not r.accepted for r in recs)
+    assert [r.lm_damping for r in recs] == [2e-4, 4e-4, 8e-4, 1.6e-3]
+
+
+@pytest.mark.parametrize("which", ["function", "gradient", "rejects"])
+def test_termination_reasons_match_oracle(pkg, oracle, which):
+    prob = _circle(pkg, n_cam=5, n_pt=60, seed=4)
+    if which == "function":
+        p = pkg.OptParams(num_iterations=100, initial_lm_damping=1e-4, function_tolerance=1e-3)
+    elif which == "gradient":
+        p = pkg.OptParams(num_iterations=100, initial_lm_damping=1e-4, gradient_tolerance=1e30)
+    else:
+        p = pkg.OptParams(num_iterations=1000, initial_lm_damping=1e-4, function_tolerance=0.0,
+                          gradient_tolerance=0.0, parameter_tolerance=0.0, max_consecutive_rejects=3)
+    with pkg.native.Problem(prob, device=0) as gp:
+        grecs, gterm = gp.optimize(p)
+    orecs, _, _ = oracle.optimize(prob, p)
+    assert gterm == orecs[-1].termination
+    if which != "rejects":
+        assert len(grecs) == len(orecs)
+    g, o = np.array([r.merit for r in grecs]), np.array([r.merit for r in orecs])
+    n = min(len(g), len(o))
+    assert np.max(np.abs(g[:n] - o[:n]) / o[:n]) < COST_RTOL
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_step_vs_f64_ldlt(pkg, kind):
+    """The GPU step (FP32 factor + f64 refinement + gauge projection) against an
+    f64 LDLT solve of the same reduced camera system; the relative error is
+    reported outside the scale-gauge direction."""
+    prob = pkg.synth.generate(kind, seed=pkg.synth.BASE_SEED + kind)
+    params = fixed_iter_params(pkg, 5, prob.initial_lm_damping)
+    errs = []
+    with pkg.native.Problem(prob, device=0) as gp:
+        gp.init(params)
+        for _ in range(3):
+            poses, _ = gp.variables()
+            gp.step()
+            S, rhs, delta = gp.last_system()
+            x64 = np.linalg.solve(S, rhs)
+            free = np.where(prob.pose_const == 0)[0]
+            c = poses[np.where(prob.pose_const == 1)[0][0], 4:]
+            v = np.zeros(S.shape[0])
+            for k, j in enumerate(free):
+                v[6 * k + 3:6 * k + 6] = poses[j, 4:] - c
+            v /= np.linalg.norm(v)
+            proj = lambda x: x - v * (v @ x)  # noqa: E731
+            xf = delta[:S.shape[0]]
+            errs.append(np.linalg.norm(proj(xf) - proj(x64)) / np.linalg.norm(proj(x64)))
+    print("config %d: step error vs f64 LDLT (outside the gauge):" % kind, errs)
+    assert max(errs) < 1e-5
