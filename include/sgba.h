@@ -202,6 +202,34 @@ int sgba_bench_iterations(sgba_problem *p, int32_t iters, int32_t flush_l2, doub
  * *ms_avg is the mean device time per launch. */
 int sgba_bench_kernel(sgba_problem *p, int32_t kernel, int32_t reps, int32_t flush_l2, double *ms_avg);
 
+/* ---- allocation-free total cost (no counterpart in the reference) --------
+ * calc_total_cost of the reprojection cost (the value sgba_get_cost reports,
+ * float-float on the GPU) over observations that the caller already holds in
+ * device memory, for callers that must not allocate while they run: code
+ * inside a pre-sized memory pool or a real-time loop, where a cudaMalloc
+ * would synchronize the device, fragment the pool or fail under a fixed
+ * budget.  It allocates nothing (no cudaMalloc, no library allocator): its
+ * scratch is one static device array of 599,808 bytes sized for at most 4096
+ * cameras, and n_cam above that is rejected with SGBA_ERR_INVALID_ARGUMENT.
+ *
+ * poses (7 doubles per camera, world-from-camera as in sgba_problem_desc),
+ * points (3 per point), obs_cam, obs_pt, obs_uv (2 per observation) and cost
+ * (1 double, written) are device pointers on the current device; intrinsics
+ * (fx, fy, cx, cy) is a host array; huber_delta <= 0 means no robust kernel.
+ * The call is asynchronous on `stream` (a cudaStream_t; NULL is the legacy
+ * default stream).  Nothing needs to be zeroed by the caller.  An observation
+ * index out of range makes *cost NaN.
+ *
+ * The first call on each device does the set-up with that device current
+ * (the scratch address and the loading of the kernels): make it before any
+ * stream capture begins.  Calls that overlap on one device (other streams,
+ * other threads) share the scratch and race: order them on one stream or
+ * with events. */
+int sgba_total_cost_noalloc(int32_t n_cam, const double *poses, int32_t n_pt, const double *points,
+                            int64_t n_obs, const int32_t *obs_cam, const int32_t *obs_pt,
+                            const double *obs_uv, const double *intrinsics, double huber_delta,
+                            double *cost, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -867,4 +867,28 @@ int sgba_set_profiling(sgba_problem* p, int32_t enabled) {
   return SGBA_OK;
 }
 
+int sgba_total_cost_noalloc(int32_t n_cam, const double* poses, int32_t n_pt, const double* points, int64_t n_obs,
+                            const int32_t* obs_cam, const int32_t* obs_pt, const double* obs_uv,
+                            const double* intrinsics, double huber_delta, double* cost, void* stream) {
+  // Host-side checks only: no CUDA call before the arguments are known good.
+  const int max_cams = sgba::noalloc_max_cams();
+  if (n_cam < 1 || n_cam > max_cams)
+    return set_error(SGBA_ERR_INVALID_ARGUMENT,
+                     "sgba_total_cost_noalloc: n_cam %d outside [1, %d] (the static scratch holds %d cameras)",
+                     n_cam, max_cams, max_cams);
+  if (n_pt < 0 || n_obs < 0) return set_error(SGBA_ERR_INVALID_ARGUMENT, "sgba_total_cost_noalloc: negative n_pt or n_obs");
+  if (!poses || !cost || !intrinsics || (n_pt > 0 && !points) || (n_obs > 0 && (!obs_cam || !obs_pt || !obs_uv)))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "sgba_total_cost_noalloc: NULL argument");
+  for (int i = 0; i < 4; ++i)
+    if (!std::isfinite(intrinsics[i]))
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "sgba_total_cost_noalloc: non-finite intrinsics");
+  if (!std::isfinite(huber_delta))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "sgba_total_cost_noalloc: non-finite huber_delta");
+  cudaError_t e = sgba::launch_total_cost_noalloc(n_cam, poses, n_pt, points, n_obs, obs_cam, obs_pt, obs_uv,
+                                                  intrinsics, huber_delta, cost, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess)
+    return set_error(SGBA_ERR_CUDA, "sgba_total_cost_noalloc: %s", cudaGetErrorString(e));
+  return SGBA_OK;
+}
+
 }  // extern "C"

@@ -164,4 +164,13 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st);
 int cost_partials_needed(const Sizes& s);  // reduction partial slots
 int solver_launch_count(const Sizes& s);
 
+// Allocation-free total cost over caller-owned device arrays; the scratch is a
+// static __device__ array (sgba_kernels.cu).  Arguments are validated by the
+// caller except the observation indices, which the kernel checks.
+int noalloc_max_cams();
+cudaError_t launch_total_cost_noalloc(int32_t nc, const double* poses, int32_t np, const double* points,
+                                      int64_t no, const int32_t* obs_cam, const int32_t* obs_pt,
+                                      const double* obs_uv, const double* intr, double huber,
+                                      double* cost, cudaStream_t st);
+
 }  // namespace sgba

@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "sgba_dd.cuh"
 #include "sgba_internal.h"
@@ -1510,6 +1511,154 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
   k_commit<<<cb, 256, 0, st>>>(s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res,
                                d.ctrl);
   return 4;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free total cost (sgba_total_cost_noalloc).
+//
+// The same float-float calc_total_cost as k_cost, for callers that hold the
+// observations in their own device memory and may not allocate: the scratch
+// (pose tables, per-CTA partial sums and a zero Ctrl) is one file-scope
+// __device__ array, sized for kNoAllocMaxCams cameras.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocMaxCams = 4096;
+constexpr size_t kNoAllocCtrlBytes = (sizeof(Ctrl) + 255) / 256 * 256;
+constexpr size_t kNoAllocPoseFOff = kNoAllocCtrlBytes;
+constexpr size_t kNoAllocPoseDDOff = kNoAllocPoseFOff + sizeof(float) * 12 * kNoAllocMaxCams;
+constexpr size_t kNoAllocPartOff = kNoAllocPoseDDOff + sizeof(float) * 24 * kNoAllocMaxCams;
+constexpr size_t kNoAllocBytes = kNoAllocPartOff + sizeof(double) * kCostMaxBlocks;
+static_assert(kNoAllocBytes == 599808, "the scratch size is stated in sgba.h");
+
+// [0, kNoAllocCtrlBytes): a Ctrl whose done and skip fields must read 0 (the
+// zero fill of module load; nothing writes it); then the float and
+// float-float pose tables; then the partial sums.  The tables and partials
+// are fully rewritten by every call before they are read.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_base[kNoAllocMaxDevices] = {};
+
+// k_cost without the residual output and with index checks: an observation
+// whose pose or point index is out of range contributes NaN (and is never
+// dereferenced), so the returned cost is NaN.
+__global__ void __launch_bounds__(kCostThreads) k_cost_noalloc(CostArgs a, int32_t nc, int32_t np) {
+  dd acc = dd_make(0.0f, 0.0f);
+  bool bad = false;
+  for (int64_t o = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; o < a.no;
+       o += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int32_t jc = a.opose[o], ip = a.opt[o];
+    if (jc < 0 || jc >= nc || ip < 0 || ip >= np) {
+      bad = true;
+      continue;
+    }
+    const float* P = a.pose_dd + 24 * jc;
+    const double* pw = a.points + 3 * ip;
+    dd p0 = dd_from_double(pw[0]), p1 = dd_from_double(pw[1]), p2 = dd_from_double(pw[2]);
+    dd xc[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      dd r0 = dd_make(P[2 * (i * 3 + 0)], P[2 * (i * 3 + 0) + 1]);
+      dd r1 = dd_make(P[2 * (i * 3 + 1)], P[2 * (i * 3 + 1) + 1]);
+      dd r2 = dd_make(P[2 * (i * 3 + 2)], P[2 * (i * 3 + 2) + 1]);
+      dd tt = dd_make(P[18 + 2 * i], P[18 + 2 * i + 1]);
+      xc[i] = dd_add(dd_add(dd_add(dd_mul(r0, p0), dd_mul(r1, p1)), dd_mul(r2, p2)), tt);
+    }
+    dd u = dd_div(xc[0], xc[2]);
+    dd v = dd_div(xc[1], xc[2]);
+    double2 z = a.uv[o];
+    dd ru = dd_sub(dd_from_double(z.x), dd_add(dd_mul(u, a.fx), a.cx));
+    dd rv = dd_sub(dd_from_double(z.y), dd_add(dd_mul(v, a.fy), a.cy));
+    dd n2 = dd_add(dd_mul(ru, ru), dd_mul(rv, rv));
+    dd c = n2;
+    if (a.huber > 0.0f) {
+      dd nrm = dd_sqrt(n2);
+      if (!(nrm.hi <= a.huber || (nrm.hi == a.huber_dd.hi && nrm.lo <= a.huber_dd.lo))) {
+        c = dd_sub(dd_mul(dd_add(a.huber_dd, a.huber_dd), nrm), dd_mul(a.huber_dd, a.huber_dd));
+      }
+    }
+    acc = dd_add(acc, c);
+  }
+  if (bad) acc = dd_make(__int_as_float(0x7fc00000), 0.0f);
+  __shared__ float sh_hi[kCostThreads / 32], sh_lo[kCostThreads / 32];
+  acc = dd_warp_sum(acc);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) { sh_hi[w] = acc.hi; sh_lo[w] = acc.lo; }
+  __syncthreads();
+  if (w == 0) {
+    dd v = (lane < (int)(blockDim.x >> 5)) ? dd_make(sh_hi[lane], sh_lo[lane]) : dd_make(0.0f, 0.0f);
+    v = dd_warp_sum(v);
+    if (lane == 0) a.partials[blockIdx.x] = dd_to_double(v);
+  }
+}
+
+__global__ void k_noalloc_finish(const double* part, int n, double* out) {
+  double s = block_sum_partials(part, n);
+  if (threadIdx.x == 0) out[0] = s;
+}
+
+// Per-device set-up, with the device current: the address of the scratch
+// array and the loading of the three kernels (CUDA's lazy module loading
+// would otherwise do that at the first launch).
+cudaError_t noalloc_base(unsigned char** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_base[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes fa;
+    if ((e = cudaFuncGetAttributes(&fa, k_pose_tables)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&fa, k_cost_noalloc)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&fa, k_noalloc_finish)) != cudaSuccess) return e;
+    g_noalloc_base[dev] = static_cast<unsigned char*>(p);
+  }
+  *out = g_noalloc_base[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+int noalloc_max_cams() { return kNoAllocMaxCams; }
+
+cudaError_t launch_total_cost_noalloc(int32_t nc, const double* poses, int32_t np, const double* points,
+                                      int64_t no, const int32_t* obs_cam, const int32_t* obs_pt,
+                                      const double* obs_uv, const double* intr, double huber,
+                                      double* cost, cudaStream_t st) {
+  unsigned char* base = nullptr;
+  cudaError_t e = noalloc_base(&base);
+  if (e != cudaSuccess) return e;
+  const Ctrl* zero_ctrl = reinterpret_cast<const Ctrl*>(base);
+  float* pose_f = reinterpret_cast<float*>(base + kNoAllocPoseFOff);
+  float* pose_dd = reinterpret_cast<float*>(base + kNoAllocPoseDDOff);
+  double* part = reinterpret_cast<double*>(base + kNoAllocPartOff);
+  k_pose_tables<<<(nc + 127) / 128, 128, 0, st>>>(nc, poses, pose_f, pose_dd, zero_ctrl, 0);
+  auto split = [](double x) { return dd_make(static_cast<float>(x), static_cast<float>(x - static_cast<float>(x))); };
+  CostArgs a;
+  a.no = no;
+  a.uv = reinterpret_cast<const double2*>(obs_uv);
+  a.opose = obs_cam;
+  a.opt = obs_pt;
+  a.pose_dd = pose_dd;
+  a.points = points;
+  a.res_out = nullptr;
+  a.partials = part;
+  a.fx = split(intr[0]);
+  a.fy = split(intr[1]);
+  a.cx = split(intr[2]);
+  a.cy = split(intr[3]);
+  a.huber = static_cast<float>(huber > 0 ? huber : 0.0);
+  a.huber_dd = split(huber);
+  a.respect_skip = 0;
+  const int nb = cost_grid(no);
+  k_cost_noalloc<<<nb, kCostThreads, 0, st>>>(a, nc, np);
+  k_noalloc_finish<<<1, 256, 0, st>>>(part, nb, cost);
+  return cudaGetLastError();
 }
 
 }  // namespace sgba
