@@ -394,6 +394,13 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   const size_t n6 = static_cast<size_t>(s.n6);
   if ((st = dev_alloc(p, &d.S, n6 * n6))) return st;
   SGBA_CK(cudaMemset(d.S, 0, sizeof(double) * std::max<size_t>(n6 * n6, 1)));
+  // single-launch cluster solver when the dense system fits one cluster's
+  // distributed shared memory; it reads the float-float copy of S
+  sgba::dense_cluster_setup(s.n6, &s.dense_c, &s.dense_smem);
+  if (s.dense_c > 0) {
+    if ((st = dev_alloc(p, &d.S2, n6 * n6))) return st;
+    SGBA_CK(cudaMemset(d.S2, 0, sizeof(float2) * std::max<size_t>(n6 * n6, 1)));
+  }
   if ((st = dev_alloc(p, &d.A, n6 * n6))) return st;
   if ((st = dev_alloc(p, &d.dpiv, n6))) return st;
   if ((st = dev_alloc(p, &d.wpanel, n6 * 48))) return st;

@@ -1,0 +1,794 @@
+// sgba_dense.cu -- factorization and solve of a dense reduced camera system
+// in ONE launch of one thread-block cluster, the matrix resident in the
+// cluster's distributed shared memory.
+//
+// Same arithmetic contract as sgba_solver.cu (the multi-launch path it
+// replaces for systems that fit): scalar LDL^T in natural order with the
+// PSD-aware pivot rule of the reference (crates/sophus_solver/src/ldlt/dense_ldlt.rs:164-270,
+// tol_rel = 1e-12, the relative threshold restarting at every 6x6 pose block;
+// a zero pivot zeroes its column of L and its solution entry), FP32 factor,
+// then one refinement step whose residual b - S x is formed in float-float
+// from the float-float copy of S written by k_schur.
+//
+// Layout: n is padded to P blocks of kNB = 24 rows (4 pose blocks; padding
+// rows are identity).  Row block r (rows 24r..24r+23, columns 0..24r+23) lives
+// in the shared memory of cluster rank r % C.  Per panel step p:
+//   owner(p), warp 0: LDL^T of the diagonal block, 1/d and the inverse of
+//      its unit lower factor;
+//   -- cluster barrier --
+//   every CTA copies that inverse and 1/d (DSMEM loads), then for its row
+//      blocks r > p: W_rp = A_rp L_pp^-T, L_rp = W_rp D^-1;
+//   -- cluster barrier --
+//   every CTA, row blocks r > p: A_rs -= W_rp L_sp^T for p < s <= r, L_sp
+//      read in place from its owner's shared memory.  The owner of p+1
+//      updates block p+1 first; its warp 0 then runs the diagonal step of
+//      p+1 while the other warps finish the update.
+// Triangular solves: one split cluster barrier per 24-row block; the owner
+// of the block does only the critical 24x24 work before arriving, every CTA
+// folds the older solution pieces into its accumulators while the barrier
+// completes.
+//
+// GB300 notes that shaped the code (measured): a cluster barrier costs ~400
+// cycles and a DSMEM load ~200, while warp shuffles in long chains and DSMEM
+// stores issued one after another by a single warp are far slower; so
+// reductions and broadcasts go through shared memory and data moves between
+// CTAs as loads by the consumer.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "sgba_dd.cuh"
+#include "sgba_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace sgba {
+
+namespace {
+
+constexpr int kNB = 24;
+constexpr int kLd = 28;              // row stride of the 24x24 inverses (float4 rows)
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxOwn = 24;          // row blocks per CTA
+constexpr int kMaxCluster = 16;
+constexpr float kTolRel = 1e-12f;
+constexpr size_t kSmemLimit = 232448;  // 227 KiB opt-in dynamic shared memory per CTA
+
+__host__ __device__ inline int row_ld(int r) { return kNB * (r + 1) + 4; }
+
+// Shared-memory carve-up of one CTA (floats), identical on host and device.
+struct Carve {
+  int nown;
+  int rowoff[kMaxOwn];
+  int wt, linv, dloc, rdloc, lpp, rdp, y, x, xs, bl, facc, accb, vdef, red, tmp, tmp2, flags, total;
+};
+
+__host__ __device__ inline void carve(int P, int C, int rank, Carve* c) {
+  int off = 0;
+  c->nown = 0;
+  for (int r = rank; r < P; r += C) {
+    if (c->nown < kMaxOwn) c->rowoff[c->nown] = off;
+    ++c->nown;
+    off += kNB * row_ld(r);
+  }
+  const int npad = kNB * P;
+  auto take = [&](int n) { int o = off; off += (n + 3) & ~3; return o; };
+  c->wt = take(c->nown * kNB * kNB);
+  c->linv = take(c->nown * kNB * kLd);
+  c->dloc = take(c->nown * kNB);
+  c->rdloc = take(c->nown * kNB);
+  c->lpp = take(kNB * kLd);
+  c->rdp = take(kNB);
+  c->y = take(npad);
+  c->x = take(npad);
+  c->xs = take(npad);
+  c->bl = take(npad);
+  c->facc = take(c->nown * kNB);
+  c->accb = take(npad);
+  c->vdef = take(npad);
+  c->red = take(2 * kThreads);
+  c->tmp = take(32);
+  c->tmp2 = take(32);
+  c->flags = take(4);
+  c->total = off;
+}
+
+struct DenseArgs {
+  int n;             // unpadded order (6 n_f)
+  int P;             // 24-row blocks
+  const float2* S2;  // n x n float-float (hi, lo), full symmetric
+  const double* b;   // n reduced rhs
+  double* x;         // n solution (f64)
+  float* xdd;        // n solution as float-float pairs
+  // scale gauge (one constant camera, no constant point): direction v of the
+  // free poses' translations about the constant camera's center
+  int gauge;
+  const double* poses;
+  const int32_t* fb_pose;
+  double center[3];
+};
+
+__device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0; }
+
+__device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release;\n" ::: "memory"); }
+__device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory"); }
+__device__ __forceinline__ void cl_sync() {
+  cl_arrive();
+  cl_wait();
+}
+
+// Offsets of every rank's regions (remote addressing), filled at kernel start.
+struct RankTab {
+  int rowoff[kMaxCluster][kMaxOwn];
+  int linv[kMaxCluster], rdloc[kMaxCluster], y[kMaxCluster], x[kMaxCluster], accb[kMaxCluster];
+};
+
+struct Ctx {
+  float* sm;
+  const Carve* cv;  // this CTA's carve-up, in shared memory
+  const RankTab* T;
+  int C, rank, P, n;
+  __device__ float* rowblk(int r) const { return sm + cv->rowoff[r / C]; }  // r owned by this CTA
+  __device__ int ld(int r) const { return row_ld(r); }
+  __device__ bool owns(int r) const { return r % C == rank; }
+};
+
+__device__ __forceinline__ float* remote(cg::cluster_group& cl, float* sm, int rank, int off) {
+  return cl.map_shared_rank(sm + off, rank);
+}
+
+// Diagonal step of block p (owner, warp 0): LDL^T of the 24x24 diagonal block
+// in place (lane i keeps row i in registers; columns are broadcast through
+// shared memory), 1/d, and the inverse of its unit lower factor.
+__device__ void diag_step(const Ctx& X, int p, int* bad_flag) {
+  const int lane = threadIdx.x & 31;
+  const int jp = p / X.C;
+  float* Ab = X.rowblk(p) + kNB * p;
+  const int ld = X.ld(p);
+  float* colbuf = X.sm + X.cv->tmp;
+  float a[kNB];
+#pragma unroll
+  for (int k = 0; k < kNB; ++k) a[k] = (lane < kNB && k <= lane) ? Ab[lane * ld + k] : 0.0f;
+  float maxp = 1.0f;
+  float* dl = X.sm + X.cv->dloc + kNB * jp;
+  float* rdl = X.sm + X.cv->rdloc + kNB * jp;
+#pragma unroll
+  for (int t = 0; t < kNB; ++t) {
+    if (t % 6 == 0) maxp = 1.0f;  // 24p is a multiple of 6: a new pose block starts here
+    colbuf[lane] = a[t];
+    __syncwarp();
+    float dt = colbuf[t];
+    const float tol = fmaxf(maxp, 1.0f) * kTolRel;
+    if (fabsf(dt) <= tol) dt = 0.0f;
+    else maxp = fmaxf(maxp, fabsf(dt));
+    const float rd = (dt == 0.0f) ? 0.0f : __frcp_rn(dt);
+    const float li = (lane > t) ? a[t] * rd : 0.0f;
+#pragma unroll
+    for (int k = t + 1; k < kNB; ++k) {
+      const float wk = colbuf[k];  // A[k][t], not yet scaled
+      if (k <= lane) a[k] = fmaf(-li, wk, a[k]);
+    }
+    __syncwarp();
+    if (lane > t) a[t] = li;
+    if (lane == 0) {
+      dl[t] = dt;
+      rdl[t] = rd;
+    }
+  }
+  if (lane < kNB) {
+#pragma unroll
+    for (int k = 0; k < kNB; ++k)
+      if (k < lane) Ab[lane * ld + k] = a[k];
+    Ab[lane * ld + lane] = 1.0f;
+  }
+  __syncwarp();
+  if (lane < kNB && !isfinite(dl[lane])) *bad_flag = 1;  // NonFinitePivot
+  // inverse of the unit lower factor: lane j computes column j
+  float xc[kNB];
+#pragma unroll
+  for (int i = 0; i < kNB; ++i) xc[i] = (i == lane) ? 1.0f : 0.0f;
+#pragma unroll
+  for (int i = 1; i < kNB; ++i) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < i; ++k) s = fmaf(Ab[i * ld + k], xc[k], s);
+    if (i > lane) xc[i] = -s;
+  }
+  float* Li = X.sm + X.cv->linv + kNB * kLd * jp;
+  if (lane < kNB) {
+#pragma unroll
+    for (int i = 0; i < kNB; ++i) Li[i * kLd + lane] = xc[i];
+  }
+}
+
+// Every CTA after the barrier of step p: copy Linv_pp and 1/d_p from the
+// owner of p (one float4 per thread).
+__device__ void pull_diag(const Ctx& X, cg::cluster_group& cl, int p) {
+  constexpr int kRowsF4 = kNB * (kLd / 4), kAllF4 = kRowsF4 + kNB / 4;
+  const int op = p % X.C, jp = p / X.C;
+  for (int q = threadIdx.x; q < kAllF4; q += kThreads) {
+    if (q < kRowsF4) {
+      const float4* src = reinterpret_cast<const float4*>(remote(cl, X.sm, op, X.T->linv[op] + kNB * kLd * jp));
+      reinterpret_cast<float4*>(X.sm + X.cv->lpp)[q] = src[q];
+    } else {
+      const float4* src = reinterpret_cast<const float4*>(remote(cl, X.sm, op, X.T->rdloc[op] + kNB * jp));
+      reinterpret_cast<float4*>(X.sm + X.cv->rdp)[q - kRowsF4] = src[q - kRowsF4];
+    }
+  }
+}
+
+// Panel step p, every CTA: for the owned row blocks r > p,
+// W_rp = A_rp Linv_pp^T (kept transposed for the update) and L_rp = W_rp D^-1
+// in place.  Linv_pp and 1/d were pushed by the owner of p.
+__device__ void panel_rows(const Ctx& X, int p) {
+  int j0 = 0;
+  while (j0 < X.cv->nown && X.rank + j0 * X.C <= p) ++j0;
+  const int total = (X.cv->nown - j0) * kNB * kNB;
+  const float* lpp = X.sm + X.cv->lpp;
+  const float* rdp = X.sm + X.cv->rdp;
+  for (int e = threadIdx.x; e < total; e += kThreads) {
+    const int jr = j0 + e / (kNB * kNB);
+    const int rem = e % (kNB * kNB), i = rem / kNB, t = rem % kNB;
+    const int r = X.rank + jr * X.C;
+    const float* arow = X.sm + X.cv->rowoff[jr] + i * X.ld(r) + kNB * p;
+    const float* lt = lpp + t * kLd;  // Linv[t][k], zero for k > t
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kNB; ++k) s = fmaf(arow[k], lt[k], s);
+    X.sm[X.cv->wt + kNB * kNB * jr + t * kNB + i] = s;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < total; e += kThreads) {
+    const int jr = j0 + e / (kNB * kNB);
+    const int rem = e % (kNB * kNB), i = rem / kNB, t = rem % kNB;
+    const int r = X.rank + jr * X.C;
+    X.sm[X.cv->rowoff[jr] + i * X.ld(r) + kNB * p + t] = X.sm[X.cv->wt + kNB * kNB * jr + t * kNB + i] * rdp[t];
+  }
+}
+
+// Row jj of L_sp (24 floats at column 24p of row block s), local or remote.
+__device__ __forceinline__ const float4* lrow(const Ctx& X, cg::cluster_group& cl, int s, int jj, int p) {
+  const int os = s % X.C;
+  const float* base = (os == X.rank) ? X.sm + X.cv->rowoff[s / X.C]
+                                     : remote(cl, X.sm, os, X.T->rowoff[os][s / X.C]);
+  return reinterpret_cast<const float4*>(base + jj * row_ld(s) + kNB * p);
+}
+
+// Update of panel p for the owned row blocks r in [r_lo, r_hi] by warps
+// [w0, w0 + nw): A_r[:, 24(p+1) + col] -= W_rp L_sp[jj]^T with
+// col = 24(s - p - 1) + jj.  A lane owns two output columns.
+__device__ void update_blocks(const Ctx& X, cg::cluster_group& cl, int p, int r_lo, int r_hi, int w0, int nw) {
+  const int warp = (threadIdx.x >> 5) - w0;
+  if (warp < 0 || warp >= nw) return;
+  const int lane = threadIdx.x & 31;
+  int task = 0;
+  for (int r = X.rank; r < X.P; r += X.C) {
+    if (r < r_lo || r > r_hi) continue;
+    const int ncol = kNB * (r - p);
+    const int nchunk = (ncol + 63) / 64;
+    const float4* wt = reinterpret_cast<const float4*>(X.sm + X.cv->wt + kNB * kNB * (r / X.C));
+    float* Ar = X.rowblk(r) + kNB * (p + 1);
+    const int ld = X.ld(r);
+    for (int ch = 0; ch < nchunk; ++ch, ++task) {
+      if (task % nw != warp) continue;
+      const int ca = ch * 64 + lane, cb = ca + 32;
+      const bool va = ca < ncol, vb = cb < ncol;
+      float la[kNB], lb[kNB];
+      {
+        const int c0 = va ? ca : 0, c1 = vb ? cb : 0;
+        const float4* pa = lrow(X, cl, p + 1 + c0 / kNB, c0 % kNB, p);
+        const float4* pb = lrow(X, cl, p + 1 + c1 / kNB, c1 % kNB, p);
+#pragma unroll
+        for (int q = 0; q < kNB / 4; ++q) {
+          const float4 u = pa[q], v = pb[q];
+          la[4 * q] = u.x; la[4 * q + 1] = u.y; la[4 * q + 2] = u.z; la[4 * q + 3] = u.w;
+          lb[4 * q] = v.x; lb[4 * q + 1] = v.y; lb[4 * q + 2] = v.z; lb[4 * q + 3] = v.w;
+        }
+      }
+      float acc0[kNB], acc1[kNB];
+#pragma unroll
+      for (int i = 0; i < kNB; ++i) { acc0[i] = 0.f; acc1[i] = 0.f; }
+#pragma unroll
+      for (int k = 0; k < kNB; ++k) {
+#pragma unroll
+        for (int q = 0; q < kNB / 4; ++q) {
+          const float4 w = wt[k * (kNB / 4) + q];
+          acc0[4 * q + 0] = fmaf(w.x, la[k], acc0[4 * q + 0]);
+          acc0[4 * q + 1] = fmaf(w.y, la[k], acc0[4 * q + 1]);
+          acc0[4 * q + 2] = fmaf(w.z, la[k], acc0[4 * q + 2]);
+          acc0[4 * q + 3] = fmaf(w.w, la[k], acc0[4 * q + 3]);
+          acc1[4 * q + 0] = fmaf(w.x, lb[k], acc1[4 * q + 0]);
+          acc1[4 * q + 1] = fmaf(w.y, lb[k], acc1[4 * q + 1]);
+          acc1[4 * q + 2] = fmaf(w.z, lb[k], acc1[4 * q + 2]);
+          acc1[4 * q + 3] = fmaf(w.w, lb[k], acc1[4 * q + 3]);
+        }
+      }
+      if (va) {
+#pragma unroll
+        for (int i = 0; i < kNB; ++i) Ar[i * ld + ca] -= acc0[i];
+      }
+      if (vb) {
+#pragma unroll
+        for (int i = 0; i < kNB; ++i) Ar[i * ld + cb] -= acc1[i];
+      }
+    }
+  }
+}
+
+// L y = bl over the 24-row blocks.  The owner of block p pulls y_{p-1} from
+// its owner, adds L_{p,p-1} y_{p-1} to its accumulator, forms y_p in its own
+// shared memory and arrives; meanwhile every CTA pulls y_{p-1} and folds it
+// into the accumulators of its other blocks.  Pieces of y stay with their
+// owners (the backward pass reads only its own).
+__device__ void solve_forward(const Ctx& X, cg::cluster_group& cl) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  float* y = X.sm + X.cv->y;
+  float* facc = X.sm + X.cv->facc;
+  float* tmp = X.sm + X.cv->tmp;
+  float* tmp2 = X.sm + X.cv->tmp2;
+  const float* bl = X.sm + X.cv->bl;
+  for (int e = tid; e < X.cv->nown * kNB; e += kThreads) facc[e] = 0.f;
+  __syncthreads();
+  cl_sync();
+  for (int p = 0; p < X.P; ++p) {
+    if (X.owns(p) && warp == 0) {
+      const int jp = p / X.C;
+      if (p > 0 && lane < kNB) {
+        const int oq = (p - 1) % X.C;
+        tmp2[lane] = remote(cl, X.sm, oq, X.T->y[oq])[kNB * (p - 1) + lane];
+      }
+      __syncwarp();
+      if (lane < kNB) {
+        float s = facc[kNB * jp + lane];
+        if (p > 0) {
+          const float* lr = X.rowblk(p) + lane * X.ld(p) + kNB * (p - 1);
+#pragma unroll
+          for (int k = 0; k < kNB; ++k) s = fmaf(lr[k], tmp2[k], s);
+        }
+        tmp[lane] = bl[kNB * p + lane] - s;
+      }
+      __syncwarp();
+      if (lane < kNB) {
+        const float* li = X.sm + X.cv->linv + kNB * kLd * jp + lane * kLd;
+        float v = 0.f;
+#pragma unroll
+        for (int j = 0; j < kNB; ++j) v = fmaf(li[j], tmp[j], v);
+        y[kNB * p + lane] = v;
+      }
+    }
+    __syncthreads();
+    cl_arrive();
+    if (p > 0) {
+      int j0 = 0;
+      while (j0 < X.cv->nown && X.rank + j0 * X.C <= p) ++j0;
+      if (j0 < X.cv->nown) {
+        const int oq = (p - 1) % X.C;
+        if (tid < kNB && oq != X.rank) y[kNB * (p - 1) + tid] = remote(cl, X.sm, oq, X.T->y[oq])[kNB * (p - 1) + tid];
+        __syncthreads();
+        const int rows = (X.cv->nown - j0) * kNB;
+        const float* yq = y + kNB * (p - 1);
+        for (int e = tid; e < rows; e += kThreads) {
+          const int jr = j0 + e / kNB, i = e % kNB;
+          const int r = X.rank + jr * X.C;
+          const float* lr = X.sm + X.cv->rowoff[jr] + i * X.ld(r) + kNB * (p - 1);
+          float s = 0.f;
+#pragma unroll
+          for (int k = 0; k < kNB; ++k) s = fmaf(lr[k], yq[k], s);
+          facc[kNB * jr + i] += s;
+        }
+      }
+    }
+    __syncthreads();
+    cl_wait();
+  }
+}
+
+// L^T x = D^-1 y over the blocks in reverse.  Each CTA accumulates the
+// contributions L_pq^T x_p of its own blocks p into accb; the owner of block
+// p sums the accumulators of all ranks in rank order.  It adds its own
+// contribution to block p-1 before arriving, the rest after.  Pieces of x
+// stay with their owners; gather_x collects the whole vector.
+__device__ void solve_backward(const Ctx& X, cg::cluster_group& cl) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int npad = kNB * X.P;
+  const float* y = X.sm + X.cv->y;
+  float* x = X.sm + X.cv->x;
+  float* accb = X.sm + X.cv->accb;
+  float* tmp = X.sm + X.cv->tmp;
+  float* tmp2 = X.sm + X.cv->tmp2;
+  for (int k = tid; k < npad; k += kThreads) accb[k] = 0.f;
+  __syncthreads();
+  cl_sync();
+  for (int p = X.P - 1; p >= 0; --p) {
+    const bool own = X.owns(p);
+    if (own && warp == 0) {
+      const int jp = p / X.C;
+      if (lane < kNB) {
+        float part[kMaxCluster];
+#pragma unroll
+        for (int c = 0; c < kMaxCluster; ++c)
+          part[c] = (c < X.C) ? remote(cl, X.sm, c, X.T->accb[c])[kNB * p + lane] : 0.f;
+        float s = 0.f;
+#pragma unroll
+        for (int c = 0; c < kMaxCluster; ++c) s += part[c];
+        const float z = y[kNB * p + lane] * X.sm[X.cv->rdloc + kNB * jp + lane];
+        tmp[lane] = z - s;
+      }
+      __syncwarp();
+      if (lane < kNB) {
+        const float* li = X.sm + X.cv->linv + kNB * kLd * jp;
+        float v = 0.f;
+#pragma unroll
+        for (int i = 0; i < kNB; ++i) v = fmaf(li[i * kLd + lane], tmp[i], v);
+        tmp2[lane] = v;
+        x[kNB * p + lane] = v;
+      }
+      __syncwarp();
+      if (p > 0 && lane < kNB) {
+        const float* ap = X.rowblk(p) + kNB * (p - 1) + lane;
+        const int ld = X.ld(p);
+        float s = 0.f;
+#pragma unroll
+        for (int i = 0; i < kNB; ++i) s = fmaf(ap[i * ld], tmp2[i], s);
+        accb[kNB * (p - 1) + lane] += s;
+      }
+    }
+    __syncthreads();
+    cl_arrive();
+    if (own && p > 1) {
+      const float* ap = X.rowblk(p);
+      const int ld = X.ld(p);
+      for (int k = tid; k < kNB * (p - 1); k += kThreads) {
+        float s = 0.f;
+#pragma unroll
+        for (int i = 0; i < kNB; ++i) s = fmaf(ap[i * ld + k], tmp2[i], s);
+        accb[k] += s;
+      }
+    }
+    __syncthreads();
+    cl_wait();
+  }
+}
+
+// Every CTA: copy the pieces of x owned by the other ranks (after a barrier).
+__device__ void gather_x(const Ctx& X, cg::cluster_group& cl) {
+  float* x = X.sm + X.cv->x;
+  for (int q = threadIdx.x; q < X.P * (kNB / 4); q += kThreads) {
+    const int blk = q / (kNB / 4), ob = blk % X.C;
+    if (ob == X.rank) continue;
+    reinterpret_cast<float4*>(x)[q] = reinterpret_cast<const float4*>(remote(cl, X.sm, ob, X.T->x[ob]))[q];
+  }
+  __syncthreads();
+}
+
+// Sum over one warp through shared memory (fixed tree, no shuffles).
+__device__ dd warp_sum_dd(dd v, float* wred, int lane) {
+  wred[2 * lane] = v.hi;
+  wred[2 * lane + 1] = v.lo;
+  __syncwarp();
+#pragma unroll
+  for (int s = 16; s > 0; s >>= 1) {
+    if (lane < s) {
+      const dd u = dd_add(dd_make(wred[2 * lane], wred[2 * lane + 1]),
+                          dd_make(wred[2 * (lane + s)], wred[2 * (lane + s) + 1]));
+      wred[2 * lane] = u.hi;
+      wred[2 * lane + 1] = u.lo;
+    }
+    __syncwarp();
+  }
+  const dd r = dd_make(wred[0], wred[1]);
+  __syncwarp();
+  return r;
+}
+
+// Sum over the CTA through shared memory (fixed tree); every thread gets it.
+__device__ dd block_sum_dd(dd v, float* red) {
+  const int tid = threadIdx.x;
+  red[2 * tid] = v.hi;
+  red[2 * tid + 1] = v.lo;
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if (tid < s) {
+      const dd u = dd_add(dd_make(red[2 * tid], red[2 * tid + 1]), dd_make(red[2 * (tid + s)], red[2 * (tid + s) + 1]));
+      red[2 * tid] = u.hi;
+      red[2 * tid + 1] = u.lo;
+    }
+    __syncthreads();
+  }
+  const dd r = dd_make(red[0], red[1]);
+  __syncthreads();
+  return r;
+}
+
+// bl = FP32(b - (S + alpha v v^T) x) on the owned rows, b and S in
+// float-float, x = FP32 x0, v the unit gauge direction (zero without gauge).
+__device__ void residual(const Ctx& X, const DenseArgs& a, float alpha) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const float* x = X.sm + X.cv->x;
+  const float* vd = X.sm + X.cv->vdef;
+  float* bl = X.sm + X.cv->bl;
+  float* red = X.sm + X.cv->red;
+  dd g = dd_make(0.f, 0.f);
+  for (int k = tid; k < a.n; k += kThreads) g = dd_add(g, dd_mul_f(dd_make(vd[k], 0.f), x[k]));
+  g = block_sum_dd(g, red);
+  const dd ag = dd_mul_f(g, alpha);
+  float* wred = red + 64 * warp;
+  for (int jr = 0; jr < X.cv->nown; ++jr) {
+    const int r = X.rank + jr * X.C;
+    for (int i = warp; i < kNB; i += kWarps) {
+      const int row = kNB * r + i;
+      if (row >= a.n) {
+        if (lane == 0) bl[row] = 0.f;
+        continue;
+      }
+      const float2* srow = a.S2 + static_cast<int64_t>(row) * a.n;
+      dd acc = dd_make(0.f, 0.f);
+      for (int k0 = lane; k0 < a.n; k0 += 32 * 8) {
+        float2 sv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int k = k0 + 32 * u;
+          sv[u] = (k < a.n) ? srow[k] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int k = k0 + 32 * u;
+          if (k < a.n) acc = dd_add(acc, dd_mul_f(dd_make(sv[u].x, sv[u].y), x[k]));
+        }
+      }
+      acc = warp_sum_dd(acc, wred, lane);
+      if (lane == 0) {
+        acc = dd_add(acc, dd_mul_f(ag, vd[row]));
+        const dd rr = dd_sub(dd_from_double(a.b[row]), acc);
+        bl[row] = rr.hi + rr.lo;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl* ctrl) {
+  // Every CTA reads the control block before the first cluster barrier and
+  // this kernel writes it only after the last one: the early return is
+  // uniform across the cluster.
+  if (skipping(ctrl)) return;
+  extern __shared__ __align__(16) float dsm[];
+  __shared__ RankTab T;
+  __shared__ Carve s_cv;
+  cg::cluster_group cl = cg::this_cluster();
+  Ctx X;
+  X.sm = dsm;
+  X.C = static_cast<int>(cl.num_blocks());
+  X.rank = static_cast<int>(cl.block_rank());
+  X.P = a.P;
+  X.n = a.n;
+  X.cv = &s_cv;
+  X.T = &T;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (tid == 0) carve(X.P, X.C, X.rank, &s_cv);
+  if (tid < X.C) {
+    Carve rc;
+    carve(X.P, X.C, tid, &rc);
+    for (int j = 0; j < kMaxOwn; ++j) T.rowoff[tid][j] = (j < rc.nown) ? rc.rowoff[j] : 0;
+    T.linv[tid] = rc.linv;
+    T.rdloc[tid] = rc.rdloc;
+    T.y[tid] = rc.y;
+    T.x[tid] = rc.x;
+    T.accb[tid] = rc.accb;
+  }
+  __syncthreads();
+  int* flags = reinterpret_cast<int*>(dsm + s_cv.flags);
+  if (tid == 0) flags[0] = 0;
+  // Gauge deflation.  With one constant camera and no constant point the
+  // reduced system has one eigenvalue of order nu (the scale direction v of
+  // the free poses' translations, rotation rows zero) against the rest of the
+  // spectrum; FP32 cannot factor that reliably.  The factor and the refinement
+  // use S + alpha v v^T (unit v, alpha = max diag S) instead: in exact
+  // arithmetic its solution differs from S^-1 b only along v, and the
+  // component along v is set afterwards by the gauge projection of the full
+  // step (an identity of the exact damped step).
+  const int npad = kNB * X.P;
+  float* vd = dsm + s_cv.vdef;
+  float* red = dsm + s_cv.red;
+  float alpha = 0.0f;
+  for (int k = tid; k < npad; k += kThreads) {
+    float v = 0.0f;
+    if (a.gauge && k < a.n && k % 6 >= 3) {
+      const double* tp = a.poses + 7 * a.fb_pose[k / 6];
+      v = static_cast<float>(tp[4 + k % 6 - 3] - a.center[k % 6 - 3]);
+    }
+    vd[k] = v;
+  }
+  if (a.gauge) {
+    __syncthreads();
+    float s2 = 0.0f, m = 0.0f;
+    for (int k = tid; k < a.n; k += kThreads) {
+      s2 = fmaf(vd[k], vd[k], s2);
+      m = fmaxf(m, a.S2[static_cast<int64_t>(k) * a.n + k].x);
+    }
+    red[tid] = s2;
+    red[kThreads + tid] = m;
+    __syncthreads();
+    for (int s = kThreads / 2; s > 0; s >>= 1) {
+      if (tid < s) {
+        red[tid] += red[tid + s];
+        red[kThreads + tid] = fmaxf(red[kThreads + tid], red[kThreads + tid + s]);
+      }
+      __syncthreads();
+    }
+    const float st = red[0], mt = red[kThreads];
+    const float inv = (st > 0.0f) ? 1.0f / sqrtf(st) : 0.0f;
+    alpha = (st > 0.0f) ? mt : 0.0f;
+    __syncthreads();
+    for (int k = tid; k < npad; k += kThreads) vd[k] *= inv;
+  }
+  __syncthreads();
+  // load the owned row blocks (FP32 high part of S + alpha v v^T; padding rows are identity)
+  for (int jr = 0; jr < s_cv.nown; ++jr) {
+    const int r = X.rank + jr * X.C;
+    const int w = kNB * (r + 1), ld = X.ld(r);
+    float* Ar = dsm + s_cv.rowoff[jr];
+    for (int e0 = tid; e0 < kNB * w; e0 += kThreads * 8) {
+      float hv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + kThreads * u;
+        const int i = e / w, col = e - i * w, row = kNB * r + i;
+        hv[u] = (e < kNB * w && row < a.n && col < a.n) ? a.S2[static_cast<int64_t>(row) * a.n + col].x : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + kThreads * u;
+        if (e >= kNB * w) break;
+        const int i = e / w, col = e - i * w, row = kNB * r + i;
+        Ar[i * ld + col] = (row < a.n && col < a.n) ? fmaf(alpha * vd[row], vd[col], hv[u])
+                                                    : (row == col ? 1.0f : 0.0f);
+      }
+    }
+    for (int i = tid; i < kNB; i += kThreads) {
+      const int row = kNB * r + i;
+      dsm[s_cv.bl + row] = (row < a.n) ? static_cast<float>(a.b[row]) : 0.0f;
+    }
+  }
+  __syncthreads();
+  cl_sync();  // every CTA is running before the first DSMEM access
+  if (X.rank == 0 && warp == 0) diag_step(X, 0, flags);
+  for (int p = 0; p < X.P; ++p) {
+    cl_sync();  // Linv_pp and 1/d_p final in the owner of p
+    pull_diag(X, cl, p);
+    __syncthreads();
+    panel_rows(X, p);
+    cl_sync();  // L_rp final for every r > p
+    if (p + 1 < X.P) {
+      if (X.owns(p + 1)) {
+        update_blocks(X, cl, p, p + 1, p + 1, 0, kWarps);
+        __syncthreads();
+        if (warp == 0) diag_step(X, p + 1, flags);
+        else update_blocks(X, cl, p, p + 2, X.P - 1, 1, kWarps - 1);
+      } else {
+        update_blocks(X, cl, p, p + 1, X.P - 1, 0, kWarps);
+      }
+    }
+  }
+  __syncthreads();
+  // x0 = (L D L^T)^-1 b in FP32
+  solve_forward(X, cl);
+  solve_backward(X, cl);
+  cl_sync();
+  gather_x(X, cl);
+  for (int k = tid; k < npad; k += kThreads) dsm[s_cv.xs + k] = dsm[s_cv.x + k];
+  residual(X, a, alpha);
+  __syncthreads();
+  // correction dx = (L D L^T)^-1 (b - S x0); x = x0 + dx in float-float
+  solve_forward(X, cl);
+  solve_backward(X, cl);
+  for (int jr = 0; jr < s_cv.nown; ++jr) {
+    const int r = X.rank + jr * X.C;
+    for (int i = tid; i < kNB; i += kThreads) {
+      const int row = kNB * r + i;
+      if (row >= a.n) continue;
+      const dd v = dd_add_f(dd_make(dsm[s_cv.xs + row], 0.0f), dsm[s_cv.x + row]);
+      a.x[row] = static_cast<double>(v.hi) + static_cast<double>(v.lo);
+      a.xdd[2 * row] = v.hi;
+      a.xdd[2 * row + 1] = v.lo;
+    }
+  }
+  if (tid == 0 && flags[0]) ctrl->skip = 2;  // NonFinitePivot -> solve failure -> reject
+  cl_sync();  // no CTA leaves while another may still read its shared memory
+}
+
+size_t dense_smem_bytes(int P, int C) {
+  size_t m = 0;
+  for (int r = 0; r < C; ++r) {
+    Carve c;
+    carve(P, C, r, &c);
+    if (c.nown > kMaxOwn) return SIZE_MAX;
+    const size_t b = sizeof(float) * static_cast<size_t>(c.total);
+    if (b > m) m = b;
+  }
+  return m;
+}
+
+}  // namespace
+
+int dense_cluster_setup(int n, int* cluster, size_t* smem) {
+  *cluster = 0;
+  *smem = 0;
+  if (n <= 0) return 0;
+  const int P = (n + kNB - 1) / kNB;
+  // one CTA per 24-row block up to 8; beyond, 16 (non-portable) or 8
+  int sizes[2] = {16, 8};
+  int ncand = 2;
+  if (P <= 8) {
+    sizes[0] = P;
+    ncand = 1;
+  }
+  for (int ci = 0; ci < ncand; ++ci) {
+    const int C = sizes[ci];
+    const size_t bytes = dense_smem_bytes(P, C);
+    if (bytes > kSmemLimit - sizeof(RankTab) - sizeof(Carve) - 1024) continue;
+    if (cudaFuncSetAttribute(k_dense_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(bytes)) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (C > 8 && cudaFuncSetAttribute(k_dense_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                     cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = bytes;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, k_dense_cluster, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (nclusters < 1) continue;
+    *cluster = C;
+    *smem = bytes;
+    return C;
+  }
+  return 0;
+}
+
+int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st) {
+  DenseArgs a;
+  a.n = s.n6;
+  a.P = (s.n6 + kNB - 1) / kNB;
+  a.S2 = d.S2;
+  a.b = d.rb;
+  a.x = d.x;
+  a.xdd = d.xdd;
+  a.gauge = (s.gauge_kind == 1) ? 1 : 0;
+  a.poses = d.poses;
+  a.fb_pose = d.fb_pose;
+  for (int k = 0; k < 3; ++k) a.center[k] = s.gauge_center[k];
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(s.dense_c);
+  cfg.blockDim = dim3(kThreads);
+  cfg.dynamicSmemBytes = s.dense_smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = s.dense_c;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, k_dense_cluster, a, d.ctrl);
+  return 1;
+}
+
+}  // namespace sgba

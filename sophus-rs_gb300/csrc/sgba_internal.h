@@ -121,6 +121,7 @@ struct Dev {
   double* rb = nullptr;            // nf*6: reduced rhs
   double* tile_part = nullptr;     // ntiles*33 partial sums
   double* S = nullptr;             // n6*n6 FP64 (lower valid)
+  float2* S2 = nullptr;            // n6*n6 float-float copy of S (cluster solver only)
   float* A = nullptr;              // n6*n6 FP32 factor (lower: unit L)
   float* dpiv = nullptr;           // n6 pivots
   float* wpanel = nullptr;         // n6*64 panel scratch (A_ip L^-T)
@@ -144,6 +145,8 @@ struct Sizes {
   double huber;
   int gauge_kind;
   double gauge_center[3];
+  int dense_c;        // cluster size of the single-launch dense solver, 0 = multi-launch path
+  size_t dense_smem;  // its dynamic shared memory per CTA
 };
 
 // ---- launchers (sgba_kernels.cu / sgba_solver.cu) -------------------------
@@ -163,6 +166,11 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st);
 int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st);
 int cost_partials_needed(const Sizes& s);  // reduction partial slots
 int solver_launch_count(const Sizes& s);
+
+// Single-launch cluster solver (sgba_dense.cu): chooses the cluster size for
+// order n (0 = does not fit) and enqueues the factorization + refined solve.
+int dense_cluster_setup(int n, int* cluster, size_t* smem);
+int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st);
 
 // Allocation-free total cost over caller-owned device arrays; the scratch is a
 // static __device__ array (sgba_kernels.cu).  Arguments are validated by the

@@ -781,6 +781,7 @@ struct SchurArgs {
   const double* ufull;
   const double* cnt_f;
   double* S;
+  float2* S2;  // float-float copy (may be null)
   int n6;
 };
 
@@ -832,17 +833,22 @@ __global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl)
 #pragma unroll 8
       for (int l = 0; l < 32; ++l) t = dd_add_f(t, red[wib][e][l]);
       const int r = e / 6, c = e % 6;
-      double v;
+      dd vd;
       if (j == k) {
         dd base = dd_from_double(a.ufull[36 * j + r * 6 + c]);
         if (r == c) base = dd_add(base, dd_from_double(nu * a.cnt_f[j]));
-        v = dd_to_double(dd_sub(base, t));
+        vd = dd_sub(base, t);
       } else {
-        v = -dd_to_double(t);
+        vd = dd_neg(t);
       }
+      const double v = dd_to_double(vd);
       const int64_t row = 6 * j + r, col = 6 * k + c;
       a.S[row * a.n6 + col] = v;
       a.S[col * a.n6 + row] = v;
+      if (a.S2) {
+        a.S2[row * a.n6 + col] = make_float2(vd.hi, vd.lo);
+        a.S2[col * a.n6 + row] = make_float2(vd.hi, vd.lo);
+      }
     }
     __syncwarp();
   }
@@ -1346,6 +1352,7 @@ int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
   a.ufull = d.ufull;
   a.cnt_f = d.cnt_f;
   a.S = d.S;
+  a.S2 = d.S2;
   a.n6 = s.n6;
   k_schur<<<warp_grid(s.nsb, 8, 8192), 256, 0, st>>>(a, d.ctrl);
   return 1;

@@ -267,11 +267,13 @@ __global__ void __launch_bounds__(256) k_residual(int n, const double* __restric
 }  // namespace
 
 int solver_launch_count(const Sizes& s) {
+  if (s.dense_c > 0) return 1;
   const int panels = (s.n6 + kPW - 1) / kPW;
   return 1 + 2 * panels + 1 + 2 * kRefineSteps;
 }
 
 int launch_factor_solve(const Sizes& s, const Dev& d, cudaStream_t st) {
+  if (s.dense_c > 0) return launch_dense_cluster(s, d, st);
   const int n = s.n6;
   int launches = 0;
   {
