@@ -156,6 +156,11 @@ def _kernel_bytes(name, lay, prob):
         return (8 + 24) * n_obs + (72 + 24) * nz + 33 * 8 * ((lay.n_terms + 255) // 256)
     if name == "backsub":
         return 72 * nz + (48 + 24 + 24) * lay.n_marg_points + 48 * nf
+    if name == "factor":
+        # single-launch cluster solver: read S once as float-float (8 B per entry) and the
+        # reduced rhs (f64); write the step as f64 and as float-float pairs
+        n6 = 6 * nf
+        return 8 * n6 * n6 + 8 * n6 + 16 * n6
     return None
 
 
@@ -327,6 +332,10 @@ def main():
                 "frac": achieved / hbm_peak, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes": alg, "ms_per_launch": kt[rl_kernel],
                 "traffic": traffic.get(rl_kernel)}
+    if rl_kernel == "factor":
+        n6 = 6 * lay.n_free_poses
+        roofline["note"] = ("latency-bound dependency chain (one cluster of 16 CTAs: %d panel steps + 3 "
+                            "triangular sweeps); FP32 work %.0f MFLOP per launch" % ((n6 + 23) // 24, n6 ** 3 / 3e6))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak" if ws > 1 else "weak",
