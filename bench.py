@@ -357,10 +357,12 @@ def main():
     }
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        v, dt = cpu_baseline(prob, pkg, 2, threads)
+        v0, _ = cpu_baseline(prob, pkg, 2, threads)  # rate estimate; sample ~10 s of CPU work
+        n_cpu = int(min(max(2, round(10.0 * v0)), 400))
+        v, dt = cpu_baseline(prob, pkg, n_cpu, threads)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "2 LM iterations of the workload on %d threads (%.1f s, setup included)"
-                                          % (threads, dt)}
+                                "sample": "%d LM iterations of the workload on %d threads (%.1f s, setup included)"
+                                          % (n_cpu, threads, dt)}
     print(json.dumps(line))
 
 
