@@ -53,6 +53,7 @@ int set_error(int status, const char* fmt, ...) {
   } while (0)
 
 constexpr int kTile = 256;           // terms per camera tile (one CTA)
+constexpr int64_t kSchurChunk = 256;  // observation pairs per warp in the Schur assembly
 constexpr int32_t kMaxDenseFree = 1536;  // dense reduced-camera-system limit (6 * 1536 rows)
 
 }  // namespace
@@ -290,6 +291,20 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
           P->pair_b[k] = fg[a];
         }
     }
+    // chunks of at most kSchurChunk pairs within one block (at least one per block)
+    P->chunk_begin.clear();
+    P->block_chunk_begin.assign(nb + 1, 0);
+    for (int64_t b = 0; b < nb; ++b) {
+      P->block_chunk_begin[b] = static_cast<int32_t>(P->chunk_begin.size());
+      const int64_t q0 = P->sb_pair_begin[b], q1 = P->sb_pair_begin[b + 1];
+      int64_t q = q0;
+      do {
+        P->chunk_begin.push_back(q);
+        q += kSchurChunk;
+      } while (q < q1);
+    }
+    P->block_chunk_begin[nb] = static_cast<int32_t>(P->chunk_begin.size());
+    P->chunk_begin.push_back(npairs);
   }
   // Gauge: scale about the common center of the constant poses, when no point
   // is constant and at least one pose is constant.
@@ -326,6 +341,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   s.no = P.no;
   s.ng = P.ng;
   s.nsb = static_cast<int64_t>(P.sb_row.size());
+  s.nchunk = P.chunk_begin.empty() ? 0 : static_cast<int64_t>(P.chunk_begin.size()) - 1;
   s.ntiles = static_cast<int64_t>(P.tile_fb.size());
   s.n6 = 6 * P.nf;
   for (int k = 0; k < 4; ++k) s.intr[k] = desc->intrinsics[k];
@@ -358,6 +374,11 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_upload(p, &d.sb_row, P.sb_row))) return st;
   if ((st = dev_upload(p, &d.sb_col, P.sb_col))) return st;
   if ((st = dev_upload(p, &d.sb_pair_begin, P.sb_pair_begin))) return st;
+  if (s.nchunk > 0) {
+    if ((st = dev_upload(p, &d.chunk_begin, P.chunk_begin))) return st;
+    if ((st = dev_upload(p, &d.block_chunk_begin, P.block_chunk_begin))) return st;
+    if ((st = dev_alloc(p, &d.schur_part, 36 * static_cast<size_t>(s.nchunk)))) return st;
+  }
   {
     std::vector<int2> pr(P.pair_a.size());
     for (size_t k = 0; k < pr.size(); ++k) pr[k] = make_int2(static_cast<int>(P.pair_a[k]), static_cast<int>(P.pair_b[k]));

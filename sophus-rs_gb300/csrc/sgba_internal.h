@@ -71,6 +71,8 @@ struct Plan {
   std::vector<int32_t> sb_row, sb_col;
   std::vector<int64_t> sb_pair_begin;  // nsb+1
   std::vector<int64_t> pair_a, pair_b; // groups (row camera, col camera)
+  std::vector<int64_t> chunk_begin;   // pair chunks of at most kSchurChunk pairs, within one block
+  std::vector<int32_t> block_chunk_begin;
   int64_t n_h_blocks = 0;
   // gauge: 0 none, 1 scale about gauge_center
   int gauge_kind = 0;
@@ -102,6 +104,9 @@ struct Dev {
   int32_t* sb_col = nullptr;
   int64_t* sb_pair_begin = nullptr;
   int2* pairs = nullptr;           // (group a, group b); int32 group ids
+  int64_t* chunk_begin = nullptr;  // Schur pair chunks: nchunk + 1, into pairs
+  int32_t* block_chunk_begin = nullptr;  // nsb + 1, into chunks
+  float2* schur_part = nullptr;    // 36 float-float partials per chunk
   // state
   double* poses = nullptr;         // nc*7
   double* points = nullptr;        // np*3
@@ -139,7 +144,7 @@ struct Dev {
 
 struct Sizes {
   int32_t nc, np, nf, nm;
-  int64_t no, ng, nsb, ntiles;
+  int64_t no, ng, nsb, ntiles, nchunk;
   int n6;
   double intr[4];
   double huber;

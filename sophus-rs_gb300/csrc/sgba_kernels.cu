@@ -777,6 +777,10 @@ struct SchurArgs {
   const int32_t* sb_col;
   const int64_t* sb_pair_begin;
   const int2* pairs;
+  int64_t nchunk;                 // pair chunks (each within one block)
+  const int64_t* chunk_begin;     // nchunk + 1, into pairs
+  const int32_t* block_chunk_begin;  // nsb + 1, into chunks
+  float2* part;                   // 36 float-float partials per chunk
   const float* zmat;
   const double* ufull;
   const double* cnt_f;
@@ -794,22 +798,26 @@ __device__ __forceinline__ void load_z(const float* zmat, int g, float* z) {
   }
 }
 
+// Pass 1, one warp per chunk of at most kSchurChunk observation pairs of one
+// block (heavy blocks are split so no warp walks thousands of pairs): FP32
+// products and per-lane FP32 sums, float-float across lanes, one partial
+// (36 float-float entries) per chunk.
 __global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   __shared__ float red[8][36][33];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
-  const double nu = ctrl->nu;
-  for (int64_t blk = static_cast<int64_t>(blockIdx.x) * wpb + wib; blk < a.nsb;
-       blk += static_cast<int64_t>(gridDim.x) * wpb) {
-    const int j = a.sb_row[blk], k = a.sb_col[blk];
+  for (int64_t ch = static_cast<int64_t>(blockIdx.x) * wpb + wib; ch < a.nchunk;
+       ch += static_cast<int64_t>(gridDim.x) * wpb) {
     float acc[36];
 #pragma unroll
     for (int e = 0; e < 36; ++e) acc[e] = 0.f;
-    const int64_t q0 = a.sb_pair_begin[blk], q1 = a.sb_pair_begin[blk + 1];
-    for (int64_t q = q0 + lane; q < q1; q += 32) {
-      const int2 pr = a.pairs[q];
+    const int64_t q1 = a.chunk_begin[ch + 1];
+    int64_t q = a.chunk_begin[ch] + lane;
+    int2 pr = (q < q1) ? a.pairs[q] : make_int2(0, 0);
+    while (q < q1) {
+      const int2 nx = (q + 32 < q1) ? a.pairs[q + 32] : make_int2(0, 0);  // next pair, prefetched
       float za[20], zb[20];
       load_z(a.zmat, pr.x, za);
       load_z(a.zmat, pr.y, zb);
@@ -817,12 +825,14 @@ __global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl)
       for (int r = 0; r < 6; ++r)
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
-          float p = acc[r * 6 + c];
-          p = fmaf(za[r * 3 + 0], zb[c * 3 + 0], p);
-          p = fmaf(za[r * 3 + 1], zb[c * 3 + 1], p);
-          p = fmaf(za[r * 3 + 2], zb[c * 3 + 2], p);
-          acc[r * 6 + c] = p;
+          float v = acc[r * 6 + c];
+          v = fmaf(za[r * 3 + 0], zb[c * 3 + 0], v);
+          v = fmaf(za[r * 3 + 1], zb[c * 3 + 1], v);
+          v = fmaf(za[r * 3 + 2], zb[c * 3 + 2], v);
+          acc[r * 6 + c] = v;
         }
+      pr = nx;
+      q += 32;
     }
     // transpose through shared memory; lane e (< 36) sums entry e in float-float
 #pragma unroll
@@ -832,17 +842,42 @@ __global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl)
       dd t = dd_make(0.f, 0.f);
 #pragma unroll 8
       for (int l = 0; l < 32; ++l) t = dd_add_f(t, red[wib][e][l]);
-      const int r = e / 6, c = e % 6;
+      a.part[36 * ch + e] = make_float2(t.hi, t.lo);
+    }
+    __syncwarp();
+  }
+}
+
+// Pass 2, one warp per lower block of S: the block's chunk partials summed in
+// chunk order (float-float), the diagonal U + nu n I added on diagonal
+// blocks; f64 store of both triangles (and the float-float copy).
+__global__ void __launch_bounds__(256) k_schur_reduce(SchurArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const double nu = ctrl->nu;
+  for (int64_t blk = static_cast<int64_t>(blockIdx.x) * wpb + wib; blk < a.nsb;
+       blk += static_cast<int64_t>(gridDim.x) * wpb) {
+    const int j = a.sb_row[blk], k = a.sb_col[blk];
+    const int c0 = a.block_chunk_begin[blk], c1 = a.block_chunk_begin[blk + 1];
+    for (int e = lane; e < 36; e += 32) {
+      dd t = dd_make(0.f, 0.f);
+      for (int c = c0; c < c1; ++c) {
+        const float2 v = a.part[36 * static_cast<int64_t>(c) + e];
+        t = dd_add(t, dd_make(v.x, v.y));
+      }
+      const int r = e / 6, cc = e % 6;
       dd vd;
       if (j == k) {
-        dd base = dd_from_double(a.ufull[36 * j + r * 6 + c]);
-        if (r == c) base = dd_add(base, dd_from_double(nu * a.cnt_f[j]));
+        dd base = dd_from_double(a.ufull[36 * j + r * 6 + cc]);
+        if (r == cc) base = dd_add(base, dd_from_double(nu * a.cnt_f[j]));
         vd = dd_sub(base, t);
       } else {
         vd = dd_neg(t);
       }
       const double v = dd_to_double(vd);
-      const int64_t row = 6 * j + r, col = 6 * k + c;
+      const int64_t row = 6 * j + r, col = 6 * k + cc;
       a.S[row * a.n6 + col] = v;
       a.S[col * a.n6 + row] = v;
       if (a.S2) {
@@ -850,7 +885,6 @@ __global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl)
         a.S2[col * a.n6 + row] = make_float2(vd.hi, vd.lo);
       }
     }
-    __syncwarp();
   }
 }
 
@@ -1354,8 +1388,13 @@ int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
   a.S = d.S;
   a.S2 = d.S2;
   a.n6 = s.n6;
-  k_schur<<<warp_grid(s.nsb, 8, 8192), 256, 0, st>>>(a, d.ctrl);
-  return 1;
+  a.nchunk = s.nchunk;
+  a.chunk_begin = d.chunk_begin;
+  a.block_chunk_begin = d.block_chunk_begin;
+  a.part = d.schur_part;
+  k_schur<<<warp_grid(s.nchunk, 8, 65536), 256, 0, st>>>(a, d.ctrl);
+  k_schur_reduce<<<warp_grid(s.nsb, 8, 8192), 256, 0, st>>>(a, d.ctrl);
+  return 2;
 }
 
 int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
