@@ -231,81 +231,13 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
     }
   }
   P->fb_tile_begin[P->nf] = static_cast<int64_t>(P->tile_fb.size());
-  // Reduced camera system: lower blocks (row >= col) of the Schur fill
-  // (crates/sophus_opt/src/nlls/damped_hessian.rs:261-325) and the
-  // observation pairs summed into each.
-  const int nf = P->nf;
+  // The reduced camera system pattern and its observation pairs are built on
+  // the device in upload() (build_schur_pattern).
   P->sb_row.clear();
   P->sb_col.clear();
   P->sb_pair_begin.clear();
-  P->pair_a.clear();
-  P->pair_b.clear();
-  if (nf > 0 && nf <= kMaxDenseFree) {
-    const int64_t nlow = static_cast<int64_t>(nf) * (nf + 1) / 2;
-    std::vector<int64_t> cnt(nlow, 0);
-    std::vector<uint8_t> present(nlow, 0);
-    auto lid = [](int64_t r, int64_t c) { return r * (r + 1) / 2 + c; };
-    for (int f = 0; f < nf; ++f)
-      if (P->cnt_f[f] > 0) present[lid(f, f)] = 1;
-    std::vector<int64_t> fg;
-    for (int i = 0; i < np; ++i) {
-      if (P->pt_mb[i] < 0) continue;
-      fg.clear();
-      for (int64_t g = P->pt_g_begin[i]; g < P->pt_g_begin[i + 1]; ++g)
-        if (P->pose_fb[P->g_pose[g]] >= 0) fg.push_back(g);
-      for (size_t b = 0; b < fg.size(); ++b)
-        for (size_t a = 0; a <= b; ++a) {
-          int64_t r = P->pose_fb[P->g_pose[fg[b]]], c = P->pose_fb[P->g_pose[fg[a]]];
-          cnt[lid(r, c)]++;
-          present[lid(r, c)] = 1;
-        }
-    }
-    std::vector<int64_t> bid(nlow, -1);
-    int64_t nb = 0;
-    for (int r = 0; r < nf; ++r)
-      for (int c = 0; c <= r; ++c)
-        if (present[lid(r, c)]) {
-          bid[lid(r, c)] = nb++;
-          P->sb_row.push_back(r);
-          P->sb_col.push_back(c);
-        }
-    P->sb_pair_begin.assign(nb + 1, 0);
-    for (int r = 0; r < nf; ++r)
-      for (int c = 0; c <= r; ++c)
-        if (bid[lid(r, c)] >= 0) P->sb_pair_begin[bid[lid(r, c)] + 1] = cnt[lid(r, c)];
-    for (int64_t b = 0; b < nb; ++b) P->sb_pair_begin[b + 1] += P->sb_pair_begin[b];
-    const int64_t npairs = P->sb_pair_begin[nb];
-    P->pair_a.assign(npairs, 0);
-    P->pair_b.assign(npairs, 0);
-    std::vector<int64_t> fill(P->sb_pair_begin.begin(), P->sb_pair_begin.end() - 1);
-    for (int i = 0; i < np; ++i) {
-      if (P->pt_mb[i] < 0) continue;
-      fg.clear();
-      for (int64_t g = P->pt_g_begin[i]; g < P->pt_g_begin[i + 1]; ++g)
-        if (P->pose_fb[P->g_pose[g]] >= 0) fg.push_back(g);
-      for (size_t b = 0; b < fg.size(); ++b)
-        for (size_t a = 0; a <= b; ++a) {
-          int64_t r = P->pose_fb[P->g_pose[fg[b]]], c = P->pose_fb[P->g_pose[fg[a]]];
-          int64_t k = fill[bid[lid(r, c)]]++;
-          P->pair_a[k] = fg[b];
-          P->pair_b[k] = fg[a];
-        }
-    }
-    // chunks of at most kSchurChunk pairs within one block (at least one per block)
-    P->chunk_begin.clear();
-    P->block_chunk_begin.assign(nb + 1, 0);
-    for (int64_t b = 0; b < nb; ++b) {
-      P->block_chunk_begin[b] = static_cast<int32_t>(P->chunk_begin.size());
-      const int64_t q0 = P->sb_pair_begin[b], q1 = P->sb_pair_begin[b + 1];
-      int64_t q = q0;
-      do {
-        P->chunk_begin.push_back(q);
-        q += kSchurChunk;
-      } while (q < q1);
-    }
-    P->block_chunk_begin[nb] = static_cast<int32_t>(P->chunk_begin.size());
-    P->chunk_begin.push_back(npairs);
-  }
+  P->chunk_begin.clear();
+  P->block_chunk_begin.clear();
   // Gauge: scale about the common center of the constant poses, when no point
   // is constant and at least one pose is constant.
   P->gauge_kind = 0;
@@ -330,6 +262,80 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
   return SGBA_OK;
 }
 
+// Reduced camera system: lower blocks (row >= col) of the Schur fill
+// (crates/sophus_opt/src/nlls/damped_hessian.rs:261-325) and the observation
+// pairs summed into each.  The pairs per block are counted on the device, the
+// block pattern and offsets are formed here, and the pair list itself is
+// written on the device in (block, point) order (sgba_plan.cu).
+int build_schur_pattern(sgba_problem* p) {
+  Plan& P = p->plan;
+  Dev& d = p->d;
+  const int nf = P.nf;
+  if (!(nf > 0 && nf <= kMaxDenseFree)) return SGBA_OK;
+  const int64_t nlow = static_cast<int64_t>(nf) * (nf + 1) / 2;
+  auto lid = [](int64_t r, int64_t c) { return r * (r + 1) / 2 + c; };
+  Sizes tmp_sizes = p->sz;
+  tmp_sizes.np = P.np;
+  int32_t* totals = nullptr;
+  SGBA_CK(cudaMalloc(&totals, sizeof(int32_t) * nlow));
+  std::vector<int32_t> cnt(nlow, 0);
+  cudaError_t e = cudaMemsetAsync(totals, 0, sizeof(int32_t) * nlow, p->stream);
+  if (e == cudaSuccess) e = sgba::pair_totals(tmp_sizes, d, totals, p->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cnt.data(), totals, sizeof(int32_t) * nlow, cudaMemcpyDeviceToHost, p->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+  cudaFree(totals);
+  if (e != cudaSuccess) return set_error(SGBA_ERR_CUDA, "Schur pattern (counts): %s", cudaGetErrorString(e));
+  std::vector<int32_t> bid(nlow, -1);
+  int64_t nb = 0;
+  for (int r = 0; r < nf; ++r)
+    for (int c = 0; c <= r; ++c)
+      if (cnt[lid(r, c)] > 0 || (r == c && P.cnt_f[r] > 0)) {
+        bid[lid(r, c)] = static_cast<int32_t>(nb++);
+        P.sb_row.push_back(r);
+        P.sb_col.push_back(c);
+      }
+  P.sb_pair_begin.assign(nb + 1, 0);
+  for (int64_t b = 0; b < nb; ++b) P.sb_pair_begin[b + 1] = P.sb_pair_begin[b] + cnt[lid(P.sb_row[b], P.sb_col[b])];
+  const int64_t npairs = P.sb_pair_begin[nb];
+  if (npairs >= (int64_t(1) << 31))
+    return set_error(SGBA_ERR_UNSUPPORTED, "%lld observation pairs exceed the 2^31 limit", (long long)npairs);
+  // chunks of at most kSchurChunk pairs within one block (at least one per block)
+  P.block_chunk_begin.assign(nb + 1, 0);
+  for (int64_t b = 0; b < nb; ++b) {
+    P.block_chunk_begin[b] = static_cast<int32_t>(P.chunk_begin.size());
+    int64_t q = P.sb_pair_begin[b];
+    do {
+      P.chunk_begin.push_back(q);
+      q += kSchurChunk;
+    } while (q < P.sb_pair_begin[b + 1]);
+  }
+  P.block_chunk_begin[nb] = static_cast<int32_t>(P.chunk_begin.size());
+  P.chunk_begin.push_back(npairs);
+  int st;
+  if ((st = dev_alloc(p, &d.pairs, static_cast<size_t>(npairs)))) return st;
+  if (npairs == 0) return SGBA_OK;
+  // point chunks: as many as keep the (chunk x block) table near 64 Mi entries
+  int64_t nch = (int64_t(64) << 20) / std::max<int64_t>(nb, 1);
+  nch = std::max<int64_t>(1, std::min<int64_t>({nch, 512, static_cast<int64_t>(P.np)}));
+  int32_t *bidmap = nullptr, *table = nullptr;
+  int64_t* bbeg = nullptr;
+  e = cudaMalloc(&bidmap, sizeof(int32_t) * nlow);
+  if (e == cudaSuccess) e = cudaMalloc(&table, sizeof(int32_t) * nch * nb);
+  if (e == cudaSuccess) e = cudaMalloc(&bbeg, sizeof(int64_t) * (nb + 1));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(bidmap, bid.data(), sizeof(int32_t) * nlow, cudaMemcpyHostToDevice, p->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(bbeg, P.sb_pair_begin.data(), sizeof(int64_t) * (nb + 1), cudaMemcpyHostToDevice, p->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(table, 0, sizeof(int32_t) * nch * nb, p->stream);
+  if (e == cudaSuccess) e = sgba::pair_fill(tmp_sizes, d, bidmap, nb, bbeg, static_cast<int32_t>(nch), table, p->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+  cudaFree(bidmap);
+  cudaFree(table);
+  cudaFree(bbeg);
+  if (e != cudaSuccess)
+    return set_error(e == cudaErrorMemoryAllocation ? SGBA_ERR_OUT_OF_MEMORY : SGBA_ERR_CUDA, "Schur pattern (pairs): %s",
+                     cudaGetErrorString(e));
+  return SGBA_OK;
+}
+
 int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   Plan& P = p->plan;
   Dev& d = p->d;
@@ -340,8 +346,6 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   s.nm = P.nm;
   s.no = P.no;
   s.ng = P.ng;
-  s.nsb = static_cast<int64_t>(P.sb_row.size());
-  s.nchunk = P.chunk_begin.empty() ? 0 : static_cast<int64_t>(P.chunk_begin.size()) - 1;
   s.ntiles = static_cast<int64_t>(P.tile_fb.size());
   s.n6 = 6 * P.nf;
   for (int k = 0; k < 4; ++k) s.intr[k] = desc->intrinsics[k];
@@ -371,6 +375,9 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_upload(p, &d.tile_begin, P.tile_begin))) return st;
   if ((st = dev_upload(p, &d.tile_end, P.tile_end))) return st;
   if ((st = dev_upload(p, &d.fb_tile_begin, P.fb_tile_begin))) return st;
+  if ((st = build_schur_pattern(p))) return st;
+  s.nsb = static_cast<int64_t>(P.sb_row.size());
+  s.nchunk = P.chunk_begin.empty() ? 0 : static_cast<int64_t>(P.chunk_begin.size()) - 1;
   if ((st = dev_upload(p, &d.sb_row, P.sb_row))) return st;
   if ((st = dev_upload(p, &d.sb_col, P.sb_col))) return st;
   if ((st = dev_upload(p, &d.sb_pair_begin, P.sb_pair_begin))) return st;
@@ -378,14 +385,6 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
     if ((st = dev_upload(p, &d.chunk_begin, P.chunk_begin))) return st;
     if ((st = dev_upload(p, &d.block_chunk_begin, P.block_chunk_begin))) return st;
     if ((st = dev_alloc(p, &d.schur_part, 36 * static_cast<size_t>(s.nchunk)))) return st;
-  }
-  {
-    std::vector<int2> pr(P.pair_a.size());
-    for (size_t k = 0; k < pr.size(); ++k) pr[k] = make_int2(static_cast<int>(P.pair_a[k]), static_cast<int>(P.pair_b[k]));
-    if ((st = dev_upload(p, &d.pairs, pr))) return st;
-    // the pair list is device-only from here on
-    std::vector<int64_t>().swap(P.pair_a);
-    std::vector<int64_t>().swap(P.pair_b);
   }
   // state (quaternions disambiguated to w >= 0 as from_params does)
   {

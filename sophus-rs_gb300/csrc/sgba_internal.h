@@ -70,7 +70,6 @@ struct Plan {
   // reduced camera system blocks (lower, row >= col) and Schur pairs
   std::vector<int32_t> sb_row, sb_col;
   std::vector<int64_t> sb_pair_begin;  // nsb+1
-  std::vector<int64_t> pair_a, pair_b; // groups (row camera, col camera)
   std::vector<int64_t> chunk_begin;   // pair chunks of at most kSchurChunk pairs, within one block
   std::vector<int32_t> block_chunk_begin;
   int64_t n_h_blocks = 0;
@@ -176,6 +175,14 @@ int solver_launch_count(const Sizes& s);
 // order n (0 = does not fit) and enqueues the factorization + refined solve.
 int dense_cluster_setup(int n, int* cluster, size_t* smem);
 int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st);
+
+// Schur observation-pair lists on the device (sgba_plan.cu): pairs per lower
+// block (atomic counts into totals[nf(nf+1)/2]); then the pair list d.pairs in
+// (block, point) order from the block map, block offsets and a zeroed
+// (chunk x block) table.
+cudaError_t pair_totals(const Sizes& s, const Dev& d, int32_t* totals, cudaStream_t st);
+cudaError_t pair_fill(const Sizes& s, const Dev& d, const int32_t* bidmap, int64_t nb, const int64_t* block_begin,
+                      int32_t nchunk, int32_t* table, cudaStream_t st);
 
 // Allocation-free total cost over caller-owned device arrays; the scratch is a
 // static __device__ array (sgba_kernels.cu).  Arguments are validated by the
