@@ -18,6 +18,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/sgba.h"
@@ -97,6 +98,24 @@ int dev_upload(sgba_problem* p, T** ptr, const std::vector<T>& h) {
   return SGBA_OK;
 }
 
+// Run f(begin, end) over [0, n) split across host threads (contiguous ranges,
+// so per-range work that is itself ordered stays deterministic).
+template <class F>
+void par_ranges(int64_t n, F f) {
+  const int64_t min_per = 32768;
+  int64_t t = static_cast<int64_t>(std::thread::hardware_concurrency());
+  t = std::max<int64_t>(1, std::min<int64_t>({t, 16, (n + min_per - 1) / min_per}));
+  if (t <= 1) {
+    f(int64_t(0), n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(t - 1);
+  for (int64_t k = 1; k < t; ++k) th.emplace_back(f, n * k / t, n * (k + 1) / t);
+  f(int64_t(0), n / t);
+  for (auto& x : th) x.join();
+}
+
 bool finite_all(const double* v, int64_t n) {
   for (int64_t i = 0; i < n; ++i)
     if (!std::isfinite(v[i])) return false;
@@ -127,52 +146,74 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
   const int nc = d->n_cam, np = d->n_pt;
   const int64_t no = d->n_obs;
   for (int64_t o = 0; o < no; ++o) {
-    if (d->obs_cam[o] < 0 || d->obs_cam[o] >= nc)
-      return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation %lld: pose index %d out of range", (long long)o, d->obs_cam[o]);
-    if (d->obs_pt[o] < 0 || d->obs_pt[o] >= np)
-      return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation %lld: point index %d out of range", (long long)o, d->obs_pt[o]);
+    const int32_t jc = d->obs_cam[o], ip = d->obs_pt[o];
+    if (static_cast<uint32_t>(jc) >= static_cast<uint32_t>(nc))
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation %lld: pose index %d out of range", (long long)o, jc);
+    if (static_cast<uint32_t>(ip) >= static_cast<uint32_t>(np))
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation %lld: point index %d out of range", (long long)o, ip);
   }
   P->nc = nc;
   P->np = np;
   P->no = no;
-  // Stable LSD counting sort: by pose, then by point => order (point, pose, original).
-  std::vector<int64_t> tmp(no), ord(no);
+  // Order (point, pose, original index): a stable counting sort by point, then
+  // a stable sort by pose inside each point (points have few observations).
+  std::vector<int64_t> ord(no);
+  std::vector<int64_t> cp(np + 1, 0);
+  for (int64_t o = 0; o < no; ++o) cp[d->obs_pt[o] + 1]++;
+  for (int i = 0; i < np; ++i) cp[i + 1] += cp[i];
   {
-    std::vector<int64_t> cnt(nc + 1, 0);
-    for (int64_t o = 0; o < no; ++o) cnt[d->obs_cam[o] + 1]++;
-    for (int j = 0; j < nc; ++j) cnt[j + 1] += cnt[j];
-    for (int64_t o = 0; o < no; ++o) tmp[cnt[d->obs_cam[o]]++] = o;
-    std::vector<int64_t> cp(np + 1, 0);
-    for (int64_t o = 0; o < no; ++o) cp[d->obs_pt[o] + 1]++;
-    for (int i = 0; i < np; ++i) cp[i + 1] += cp[i];
-    for (int64_t k = 0; k < no; ++k) {
-      int64_t o = tmp[k];
-      ord[cp[d->obs_pt[o]]++] = o;
-    }
+    std::vector<int64_t> fill(cp.begin(), cp.end() - 1);
+    for (int64_t o = 0; o < no; ++o) ord[fill[d->obs_pt[o]]++] = o;
   }
-  P->ord = ord;
+  // groups (reduction ranges: equal non-conditioned arguments, cost_fn.rs:374-390):
+  // runs of equal pose inside each point
+  std::vector<int64_t> gcount(np + 1, 0);
+  par_ranges(np, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i) {
+      int64_t* a = ord.data() + cp[i];
+      const int64_t n = cp[i + 1] - cp[i];
+      for (int64_t k = 1; k < n; ++k) {  // insertion sort by pose, stable
+        const int64_t v = a[k];
+        const int32_t key = d->obs_cam[v];
+        int64_t m = k;
+        while (m > 0 && d->obs_cam[a[m - 1]] > key) {
+          a[m] = a[m - 1];
+          --m;
+        }
+        a[m] = v;
+      }
+      int64_t runs = 0;
+      for (int64_t k = 0; k < n; ++k)
+        if (k == 0 || d->obs_cam[a[k]] != d->obs_cam[a[k - 1]]) ++runs;
+      gcount[i + 1] = runs;
+    }
+  });
+  for (int i = 0; i < np; ++i) gcount[i + 1] += gcount[i];
+  P->ng = gcount[np];
   P->obs_pose.resize(no);
   P->obs_pt.resize(no);
-  for (int64_t k = 0; k < no; ++k) {
-    P->obs_pose[k] = d->obs_cam[ord[k]];
-    P->obs_pt[k] = d->obs_pt[ord[k]];
-  }
-  // groups (reduction ranges: equal non-conditioned arguments, cost_fn.rs:374-390)
-  P->g_begin.clear();
-  P->g_pose.clear();
-  P->g_pt.clear();
-  for (int64_t k = 0; k < no; ++k) {
-    if (k == 0 || P->obs_pose[k] != P->obs_pose[k - 1] || P->obs_pt[k] != P->obs_pt[k - 1]) {
-      P->g_begin.push_back(k);
-      P->g_pose.push_back(P->obs_pose[k]);
-      P->g_pt.push_back(P->obs_pt[k]);
+  P->g_begin.resize(P->ng + 1);
+  P->g_pose.resize(P->ng);
+  P->g_pt.resize(P->ng);
+  par_ranges(np, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i) {
+      int64_t g = gcount[i];
+      for (int64_t k = cp[i]; k < cp[i + 1]; ++k) {
+        const int32_t jc = d->obs_cam[ord[k]];
+        P->obs_pose[k] = jc;
+        P->obs_pt[k] = static_cast<int32_t>(i);
+        if (k == cp[i] || jc != P->obs_pose[k - 1]) {
+          P->g_begin[g] = k;
+          P->g_pose[g] = jc;
+          P->g_pt[g] = static_cast<int32_t>(i);
+          ++g;
+        }
+      }
     }
-  }
-  P->ng = static_cast<int64_t>(P->g_pose.size());
-  P->g_begin.push_back(no);
-  P->pt_g_begin.assign(np + 1, 0);
-  for (int64_t g = 0; g < P->ng; ++g) P->pt_g_begin[P->g_pt[g] + 1]++;
-  for (int i = 0; i < np; ++i) P->pt_g_begin[i + 1] += P->pt_g_begin[i];
+  });
+  P->g_begin[P->ng] = no;
+  P->pt_g_begin.assign(gcount.begin(), gcount.end());
+  P->ord = std::move(ord);
   // free / marginalized blocks (var_families.rs:60-113, var_family.rs:156-237)
   P->pose_fb.assign(nc, -1);
   P->fb_pose.clear();
