@@ -420,11 +420,18 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
     // damping nu * (number of reduced terms) on the diagonal (entries 0, 3, 5)
     if (lane == 0 || lane == 3 || lane == 5) tot = dd_add(tot, dd_from_double(nu * a.cnt_m[mb]));
     if (lane >= 6) tot = dd_neg(tot);  // neg_grad b_m = -sum J^T r~
+    // broadcast the 9 sums through shared memory (cheaper than shuffles here)
+    if (lane < 9) {
+      red[wib][0][lane] = tot.hi;
+      red[wib][1][lane] = tot.lo;
+    }
+    __syncwarp();
     dd Vd[6], b[3];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) Vd[k] = shfl_dd(tot, k);
+    for (int k = 0; k < 6; ++k) Vd[k] = dd_make(red[wib][0][k], red[wib][1][k]);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) b[k] = shfl_dd(tot, 6 + k);
+    for (int k = 0; k < 3; ++k) b[k] = dd_make(red[wib][0][6 + k], red[wib][1][6 + k]);
+    __syncwarp();
     if (lane == 0) {
       double* bp = a.bm + 3 * mb;
       bp[0] = dd_to_double(b[0]);
@@ -681,16 +688,20 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
   }
   __shared__ float sh_hi[kTileVals][kTileThreads / 32];
   __shared__ float sh_lo[kTileVals][kTileThreads / 32];
-  __shared__ float zred[kTileThreads / 32][12][33];
+  __shared__ float zred[kTileThreads / 32][27][33];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  // U and g: FP32 butterfly inside the warp
+  // U and g: FP32 sums inside the warp, transposed through shared memory
 #pragma unroll
-  for (int k = 0; k < 27; ++k) {
-    float v = u[k];
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
-    if (lane == 0) { sh_hi[k][w] = v; sh_lo[k][w] = 0.f; }
+  for (int k = 0; k < 27; ++k) zred[w][k][lane] = u[k];
+  __syncwarp();
+  if (lane < 27) {
+    float v = 0.f;
+#pragma unroll 8
+    for (int l = 0; l < 32; ++l) v += zred[w][lane][l];
+    sh_hi[lane][w] = v;
+    sh_lo[lane][w] = 0.f;
   }
+  __syncwarp();
   // Z c: float-float across the warp (values 2r = hi, 2r+1 = lo)
 #pragma unroll
   for (int k = 0; k < 12; ++k) zred[w][k][lane] = zc[k];
@@ -930,16 +941,29 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
         for (int q = 0; q < 3; ++q) t[q] = dd_add(t[q], dd_mul_f(x, Z[r * 3 + q]));
       }
     }
-    float vals[6] = {t[0].hi, t[0].lo, t[1].hi, t[1].lo, t[2].hi, t[2].lo};
+    // float-float sum over the lanes: fixed tree through shared memory
 #pragma unroll
-    for (int v = 0; v < 6; ++v) red[wib][v][lane] = vals[v];
+    for (int q = 0; q < 3; ++q) {
+      red[wib][2 * q][lane] = t[q].hi;
+      red[wib][2 * q + 1][lane] = t[q].lo;
+    }
     __syncwarp();
+#pragma unroll
+    for (int h = 16; h > 0; h >>= 1) {
+      if (lane < h) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          const dd u = dd_add(dd_make(red[wib][2 * q][lane], red[wib][2 * q + 1][lane]),
+                              dd_make(red[wib][2 * q][lane + h], red[wib][2 * q + 1][lane + h]));
+          red[wib][2 * q][lane] = u.hi;
+          red[wib][2 * q + 1][lane] = u.lo;
+        }
+      }
+      __syncwarp();
+    }
     if (lane == 0) {
       dd s[3];
-      for (int q = 0; q < 3; ++q) {
-        s[q] = dd_make(0.f, 0.f);
-        for (int l = 0; l < 32; ++l) s[q] = dd_add(s[q], dd_make(red[wib][2 * q][l], red[wib][2 * q + 1][l]));
-      }
+      for (int q = 0; q < 3; ++q) s[q] = dd_make(red[wib][2 * q][0], red[wib][2 * q + 1][0]);
       const float* cv = a.cvec + 6 * mb;
       dd c0 = dd_sub(dd_make(cv[0], cv[1]), s[0]);
       dd c1 = dd_sub(dd_make(cv[2], cv[3]), s[1]);
