@@ -416,6 +416,31 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_upload(p, &d.tile_begin, P.tile_begin))) return st;
   if ((st = dev_upload(p, &d.tile_end, P.tile_end))) return st;
   if ((st = dev_upload(p, &d.fb_tile_begin, P.fb_tile_begin))) return st;
+  {
+    // landmark point chunks: consecutive points, at most 256 terms and 256 points
+    std::vector<int32_t> cpt(1, 0);
+    int64_t terms = 0, cap = 256;
+    int npts = 0;
+    for (int i = 0; i < P.np; ++i) {
+      const int64_t L = P.pt_g_begin[i + 1] - P.pt_g_begin[i];
+      cap = std::max(cap, L);
+      if (npts > 0 && (terms + L > 256 || npts == 256)) {
+        cpt.push_back(i);
+        terms = 0;
+        npts = 0;
+      }
+      terms += L;
+      ++npts;
+    }
+    if (cpt.back() != P.np) cpt.push_back(P.np);
+    s.nlchunk = static_cast<int32_t>(cpt.size()) - 1;
+    s.lmk_cap = static_cast<int32_t>(cap);
+    if (s.nlchunk > 0 && sgba::landmark_setup(s.lmk_cap) != 0) s.nlchunk = 0;  // fall back to the warp kernel
+    if ((st = dev_upload(p, &d.lmk_chunk_pt, cpt))) return st;
+    if ((st = dev_alloc(p, &d.slow_list, static_cast<size_t>(std::max(P.np, 1))))) return st;
+    if ((st = dev_alloc(p, &d.slow_count, 1))) return st;
+    SGBA_CK(cudaMemset(d.slow_count, 0, sizeof(int32_t)));
+  }
   if ((st = build_schur_pattern(p))) return st;
   s.nsb = static_cast<int64_t>(P.sb_row.size());
   s.nchunk = P.chunk_begin.empty() ? 0 : static_cast<int64_t>(P.chunk_begin.size()) - 1;

@@ -106,6 +106,9 @@ struct Dev {
   int64_t* chunk_begin = nullptr;  // Schur pair chunks: nchunk + 1, into pairs
   int32_t* block_chunk_begin = nullptr;  // nsb + 1, into chunks
   float2* schur_part = nullptr;    // 36 float-float partials per chunk
+  int32_t* lmk_chunk_pt = nullptr; // landmark pass: point chunks (<= 256 terms), nlchunk + 1
+  int32_t* slow_list = nullptr;    // points redone in float-float this iteration
+  int32_t* slow_count = nullptr;
   // state
   double* poses = nullptr;         // nc*7
   double* points = nullptr;        // np*3
@@ -144,6 +147,7 @@ struct Dev {
 struct Sizes {
   int32_t nc, np, nf, nm;
   int64_t no, ng, nsb, ntiles, nchunk;
+  int32_t nlchunk, lmk_cap;  // landmark point chunks and the most terms of one chunk
   int n6;
   double intr[4];
   double huber;
@@ -169,6 +173,7 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st);
 
 int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st);
 int cost_partials_needed(const Sizes& s);  // reduction partial slots
+int landmark_setup(int cap);  // dynamic shared memory of the chunked landmark pass (0 = ok)
 int solver_launch_count(const Sizes& s);
 
 // Single-launch cluster solver (sgba_dense.cu): chooses the cluster size for

@@ -377,6 +377,15 @@ struct LinArgs {
   double nu_override;
   int use_override;
   int* fail;
+  // chunked pass (k_landmark_chunks)
+  const int32_t* g_pt;
+  const int32_t* chunk_pt;   // point chunks: nchunk + 1
+  int32_t nchunk;
+  int32_t* slow_list;        // ill-conditioned points found by the chunked pass
+  int32_t* slow_count;
+  // list mode of k_landmark: only the listed points, float-float path forced
+  const int32_t* list;
+  const int32_t* list_count;
 };
 
 __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
@@ -387,8 +396,10 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
   const int warps_per_block = blockDim.x >> 5;
   const double nu = a.use_override ? a.nu_override : ctrl->nu;
   double warp_max = 0.0;  // max |neg_grad| of this warp's points
-  for (int64_t i = static_cast<int64_t>(blockIdx.x) * warps_per_block + wib; i < a.np;
-       i += static_cast<int64_t>(gridDim.x) * warps_per_block) {
+  const int64_t nitems = a.list ? static_cast<int64_t>(*a.list_count) : static_cast<int64_t>(a.np);
+  for (int64_t item = static_cast<int64_t>(blockIdx.x) * warps_per_block + wib; item < nitems;
+       item += static_cast<int64_t>(gridDim.x) * warps_per_block) {
+    const int64_t i = a.list ? static_cast<int64_t>(a.list[item]) : item;
     const int mb = a.pt_mb[i];
     if (mb < 0) continue;  // constant point: no H_mm block
     const float px = __double2float_rn(a.points[3 * i + 0]);
@@ -452,7 +463,7 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
     float c11 = sqrtf(t11);
     float c21 = (V[4] - c20 * c10) / c11;
     float t22 = V[5] - c20 * c20 - c21 * c21;
-    const bool well = V[0] > 0.f && t11 > 1e-3f * V[3] && t22 > 1e-3f * V[5];
+    const bool well = !a.list && V[0] > 0.f && t11 > 1e-3f * V[3] && t22 > 1e-3f * V[5];
     const dd pxd = dd_from_double(a.points[3 * i + 0]);
     const dd pyd = dd_from_double(a.points[3 * i + 1]);
     const dd pzd = dd_from_double(a.points[3 * i + 2]);
@@ -603,6 +614,171 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
   if (threadIdx.x == 0) {
     double m = 0.0;
     for (int q = 0; q < warps_per_block; ++q) m = fmax(m, s_max[q]);
+    atomic_max_nonneg(&ctrl->max_grad_bits, m);
+  }
+}
+
+// Landmark pass by chunks of consecutive points (<= kLmkTerms terms): one
+// thread per term for the Jacobian products, one thread per point for the
+// float-float sums, the damping and the 3x3 Cholesky, then one thread per
+// term for Z = W C^-T.  Same arithmetic as k_landmark's well-conditioned
+// path except that each term's FP32 contribution is summed in float-float
+// directly.  A point whose Cholesky loses more than three digits goes to
+// slow_list and is redone by k_landmark (list mode, float-float path).
+constexpr int kLmkTerms = 256;
+
+__global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) {
+  if (halted(ctrl)) return;
+  extern __shared__ float lsm[];        // [cap][9] term contributions
+  __shared__ float sci[kLmkTerms][6];   // C^-1 per point of the chunk (FP32)
+  __shared__ unsigned char sok[kLmkTerms];
+  __shared__ double smax[8];
+  const int tid = threadIdx.x;
+  const double nu = ctrl->nu;
+  double tmax = 0.0;
+  for (int c = blockIdx.x; c < a.nchunk; c += gridDim.x) {
+    const int p0 = a.chunk_pt[c], p1 = a.chunk_pt[c + 1];
+    const int64_t t0 = a.pt_g_begin[p0];
+    const int nt = static_cast<int>(a.pt_g_begin[p1] - t0);
+    // pass A: per-term V and J_m^T r~ contributions
+    for (int t = tid; t < nt; t += blockDim.x) {
+      const int64_t g = t0 + t;
+      const int i = a.g_pt[g];
+      const float px = __double2float_rn(a.points[3 * i + 0]);
+      const float py = __double2float_rn(a.points[3 * i + 1]);
+      const float pz = __double2float_rn(a.points[3 * i + 2]);
+      const float* P = a.pose_f + 12 * a.g_pose[g];
+      float v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+        JacF J;
+        jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+        const float2 r = a.res[o];
+        const float w = huber_weight_f(a.huber, r.x, r.y);
+        const float r0 = w * r.x, r1 = w * r.y;
+        const float* m = J.jm;
+        v[0] += m[0] * m[0] + m[3] * m[3];
+        v[1] += m[0] * m[1] + m[3] * m[4];
+        v[2] += m[0] * m[2] + m[3] * m[5];
+        v[3] += m[1] * m[1] + m[4] * m[4];
+        v[4] += m[1] * m[2] + m[4] * m[5];
+        v[5] += m[2] * m[2] + m[5] * m[5];
+        v[6] += m[0] * r0 + m[3] * r1;
+        v[7] += m[1] * r0 + m[4] * r1;
+        v[8] += m[2] * r0 + m[5] * r1;
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) lsm[9 * t + k] = v[k];
+    }
+    __syncthreads();
+    // pass B: per point
+    for (int q = tid; q < p1 - p0; q += blockDim.x) {
+      const int i = p0 + q;
+      const int mb = a.pt_mb[i];
+      sok[q] = 0;
+      if (mb < 0) continue;
+      const int tb = static_cast<int>(a.pt_g_begin[i] - t0), te = static_cast<int>(a.pt_g_begin[i + 1] - t0);
+      dd acc[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) acc[k] = dd_make(0.f, 0.f);
+      for (int t = tb; t < te; ++t)
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] = dd_add_f(acc[k], lsm[9 * t + k]);
+      const dd damp = dd_from_double(nu * a.cnt_m[mb]);
+      acc[0] = dd_add(acc[0], damp);
+      acc[3] = dd_add(acc[3], damp);
+      acc[5] = dd_add(acc[5], damp);
+      dd b[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) b[k] = dd_neg(acc[6 + k]);
+      double* bp = a.bm + 3 * mb;
+      bp[0] = dd_to_double(b[0]);
+      bp[1] = dd_to_double(b[1]);
+      bp[2] = dd_to_double(b[2]);
+      tmax = fmax(tmax, fmax(fabs(bp[0]), fmax(fabs(bp[1]), fabs(bp[2]))));
+      float V[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) V[k] = acc[k].hi + acc[k].lo;
+      const float c00 = sqrtf(V[0]);
+      const float c10 = V[1] / c00, c20 = V[2] / c00;
+      const float t11 = V[3] - c10 * c10;
+      const float c11 = sqrtf(t11);
+      const float c21 = (V[4] - c20 * c10) / c11;
+      const float t22 = V[5] - c20 * c20 - c21 * c21;
+      const bool well = V[0] > 0.f && t11 > 1e-3f * V[3] && t22 > 1e-3f * V[5];
+      if (!well) {
+        a.slow_list[atomicAdd(a.slow_count, 1)] = i;
+        continue;
+      }
+      const float c22 = sqrtf(t22);
+      const float i00 = 1.f / c00, i11 = 1.f / c11, i22 = 1.f / c22;
+      const float i10 = -c10 * i00 * i11;
+      const float i21 = -c21 * i11 * i22;
+      const float i20 = -(c20 * i00 + c21 * i10) * i22;
+      const bool ok = isfinite(i00) && isfinite(i11) && isfinite(i22) && isfinite(i10) && isfinite(i20) && isfinite(i21);
+      if (!ok) {
+        atomicExch(a.fail, 1);
+        continue;
+      }
+      const dd I[6] = {dd_from_float(i00), dd_from_float(i10), dd_from_float(i11),
+                       dd_from_float(i20), dd_from_float(i21), dd_from_float(i22)};
+      float* ci = a.cinv + 12 * mb;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) { ci[2 * k] = I[k].hi; ci[2 * k + 1] = I[k].lo; }
+      const dd cv0 = dd_mul(b[0], I[0]);
+      const dd cv1 = dd_add(dd_mul(b[0], I[1]), dd_mul(b[1], I[2]));
+      const dd cv2 = dd_add(dd_add(dd_mul(b[0], I[3]), dd_mul(b[1], I[4])), dd_mul(b[2], I[5]));
+      float* cvp = a.cvec + 6 * mb;
+      cvp[0] = cv0.hi; cvp[1] = cv0.lo; cvp[2] = cv1.hi; cvp[3] = cv1.lo; cvp[4] = cv2.hi; cvp[5] = cv2.lo;
+      sci[q][0] = i00; sci[q][1] = i10; sci[q][2] = i11; sci[q][3] = i20; sci[q][4] = i21; sci[q][5] = i22;
+      sok[q] = 1;
+    }
+    __syncthreads();
+    // pass C: Z_g = W_g C^-T for terms with a free pose
+    for (int t = tid; t < nt; t += blockDim.x) {
+      const int64_t g = t0 + t;
+      const int i = a.g_pt[g];
+      const int q = i - p0;
+      if (!sok[q]) continue;
+      const int pj = a.g_pose[g];
+      if (a.pose_fb[pj] < 0) continue;
+      const float px = __double2float_rn(a.points[3 * i + 0]);
+      const float py = __double2float_rn(a.points[3 * i + 1]);
+      const float pz = __double2float_rn(a.points[3 * i + 2]);
+      const float* P = a.pose_f + 12 * pj;
+      float W[18];
+#pragma unroll
+      for (int k = 0; k < 18; ++k) W[k] = 0.f;
+      for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+        JacF J;
+        jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+#pragma unroll
+          for (int u = 0; u < 3; ++u) W[r * 3 + u] += J.jp[r] * J.jm[u] + J.jp[6 + r] * J.jm[3 + u];
+      }
+      const float i00 = sci[q][0], i10 = sci[q][1], i11 = sci[q][2], i20 = sci[q][3], i21 = sci[q][4], i22 = sci[q][5];
+      float Z[20];
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        Z[r * 3 + 0] = W[r * 3 + 0] * i00;
+        Z[r * 3 + 1] = W[r * 3 + 0] * i10 + W[r * 3 + 1] * i11;
+        Z[r * 3 + 2] = W[r * 3 + 0] * i20 + W[r * 3 + 1] * i21 + W[r * 3 + 2] * i22;
+      }
+      Z[18] = 0.f;
+      Z[19] = 0.f;
+      float4* dst = reinterpret_cast<float4*>(a.zmat + kZS * g);
+#pragma unroll
+      for (int u = 0; u < 5; ++u) dst[u] = make_float4(Z[4 * u], Z[4 * u + 1], Z[4 * u + 2], Z[4 * u + 3]);
+    }
+    __syncthreads();
+  }
+  // max |neg_grad| over the block
+  for (int off = 16; off > 0; off >>= 1) tmax = fmax(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
+  if ((tid & 31) == 0) smax[tid >> 5] = tmax;
+  __syncthreads();
+  if (tid == 0) {
+    double m = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) m = fmax(m, smax[q]);
     atomic_max_nonneg(&ctrl->max_grad_bits, m);
   }
 }
@@ -1335,6 +1511,39 @@ int launch_iteration_begin(const Sizes& s, const Dev& d, cudaStream_t st) {
   return 1;
 }
 
+// Landmark pass: the chunked kernel plus the float-float redo of the points it
+// queued, or (final Hessian pass, or no chunk table) the warp-per-point kernel.
+static int launch_landmark(const Sizes& s, const Dev& d, LinArgs la, cudaStream_t st) {
+  la.g_pt = d.g_pt;
+  la.list = nullptr;
+  la.list_count = nullptr;
+  la.chunk_pt = d.lmk_chunk_pt;
+  la.nchunk = s.nlchunk;
+  la.slow_list = d.slow_list;
+  la.slow_count = d.slow_count;
+  if (!la.use_override && s.nlchunk > 0) {
+    cudaMemsetAsync(d.slow_count, 0, sizeof(int32_t), st);
+    const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
+    k_landmark_chunks<<<grid, 256, sizeof(float) * 9 * static_cast<size_t>(s.lmk_cap), st>>>(la, d.ctrl);
+    LinArgs lb = la;
+    lb.list = d.slow_list;
+    lb.list_count = d.slow_count;
+    k_landmark<<<64, 256, 0, st>>>(lb, d.ctrl);
+    return 2;
+  }
+  k_landmark<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(la, d.ctrl);
+  return 1;
+}
+
+int landmark_setup(int cap) {
+  const size_t bytes = sizeof(float) * 9 * static_cast<size_t>(cap);
+  if (bytes <= 48 * 1024) return 0;
+  return cudaFuncSetAttribute(k_landmark_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)) ==
+                 cudaSuccess
+             ? 0
+             : -1;
+}
+
 int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_override,
                      cudaStream_t st) {
   int n = 0;
@@ -1364,8 +1573,7 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
   la.nu_override = nu_override;
   la.use_override = use_override ? 1 : 0;
   la.fail = &d.ctrl->fail;
-  k_landmark<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(la, d.ctrl);
-  ++n;
+  n += launch_landmark(s, d, la, st);
   if (s.ntiles > 0) {
     CamArgs ca;
     ca.tile_fb = d.tile_fb;
@@ -1510,8 +1718,7 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) 
       la.nu_override = 0.0;
       la.use_override = 0;
       la.fail = &d.ctrl->fail;
-      k_landmark<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(la, d.ctrl);
-      return 1;
+      return launch_landmark(s, d, la, st);
     }
     case 3: {
       if (s.ntiles == 0) return 0;
