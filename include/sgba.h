@@ -131,6 +131,24 @@ int sgba_optimizer_step(sgba_problem *p, sgba_iter_record *record);
 int sgba_optimize(sgba_problem *p, const sgba_opt_params *params, sgba_iter_record *records,
                   int32_t cap, int32_t *n_records, int32_t *termination);
 
+/* Batched optimize_nlls over independent problems (local windows, configs[3]
+ * of the scope table): every window is an sgba_problem created as usual; the
+ * windows' LM iterations are enqueued on their own streams and run
+ * concurrently, with one host synchronisation at the end.  Per window the
+ * result is exactly what sgba_optimize would return for it.
+ * records: NULL, or n * cap records (window w at records + w * cap);
+ * results: n entries.  Returns SGBA_OK when the call itself is well formed;
+ * per-window failures are reported in results[w].status. */
+typedef struct {
+  int32_t status;       /* sgba_status of this window */
+  int32_t termination;  /* sgba_termination */
+  int32_t n_records;    /* steps taken */
+  float ms;             /* device time of the window (first iteration to final linearisation) */
+  double final_cost;    /* merit after the last step */
+} sgba_window_result;
+int sgba_batch_optimize(sgba_problem *const *problems, int32_t n, const sgba_opt_params *params,
+                        sgba_iter_record *records, int32_t cap, sgba_window_result *results);
+
 /* Current variables (OptimizationSolution.variables). NULL skips a family. */
 int sgba_get_variables(sgba_problem *p, double *poses, double *points);
 /* Current merit (OptimizationSolution.final_cost after sgba_optimize). */

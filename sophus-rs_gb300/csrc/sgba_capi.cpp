@@ -67,6 +67,7 @@ struct sgba_problem {
   cudaStream_t stream = nullptr;
   sgba_opt_params params{};
   bool inited = false;
+  bool defer_sync = false;  // batch: init without a host synchronisation
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
   int iter_launches = 0;
@@ -631,7 +632,7 @@ int sgba_optimizer_init(sgba_problem* p, const sgba_opt_params* prm) {
   sgba::launch_init_merit(p->sz, p->d, p->stream);
   int st = check_launch();
   if (st) return st;
-  SGBA_CK(cudaStreamSynchronize(p->stream));
+  if (!p->defer_sync) SGBA_CK(cudaStreamSynchronize(p->stream));
   p->inited = true;
   return SGBA_OK;
 }
@@ -981,6 +982,85 @@ int sgba_total_cost_noalloc(int32_t n_cam, const double* poses, int32_t n_pt, co
                                                   intrinsics, huber_delta, cost, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess)
     return set_error(SGBA_ERR_CUDA, "sgba_total_cost_noalloc: %s", cudaGetErrorString(e));
+  return SGBA_OK;
+}
+
+int sgba_batch_optimize(sgba_problem* const* problems, int32_t n, const sgba_opt_params* prm,
+                        sgba_iter_record* records, int32_t cap, sgba_window_result* results) {
+  if (!prm || (n > 0 && (!problems || !results))) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (n < 0) return set_error(SGBA_ERR_INVALID_ARGUMENT, "negative window count");
+  const int iters = std::max(1, prm->num_iterations);
+  std::vector<cudaEvent_t> e0(n, nullptr), e1(n, nullptr);
+  std::vector<int> live(n, 0);
+  // 1. init and all iterations, every window on its own stream
+  for (int w = 0; w < n; ++w) {
+    sgba_window_result& r = results[w];
+    std::memset(&r, 0, sizeof(r));
+    sgba_problem* p = problems[w];
+    if (!p) { r.status = set_error(SGBA_ERR_INVALID_ARGUMENT, "window %d: NULL problem", w); continue; }
+    if (cudaSetDevice(p->device) != cudaSuccess || cudaEventCreate(&e0[w]) != cudaSuccess ||
+        cudaEventCreate(&e1[w]) != cudaSuccess) {
+      r.status = set_error(SGBA_ERR_CUDA, "window %d: event creation failed", w);
+      continue;
+    }
+    p->defer_sync = true;
+    const int st = sgba_optimizer_init(p, prm);
+    p->defer_sync = false;
+    if (st) { r.status = st; continue; }
+    cudaError_t e = cudaEventRecord(e0[w], p->stream);
+    for (int it = 0; it < iters && e == cudaSuccess; ++it) e = cudaGraphLaunch(p->graph_exec, p->stream);
+    if (e != cudaSuccess) { r.status = set_error(SGBA_ERR_CUDA, "window %d: %s", w, cudaGetErrorString(e)); continue; }
+    live[w] = 1;
+  }
+  // 2. per window: the final linearisation of build_solution
+  for (int w = 0; w < n; ++w) {
+    if (!live[w]) continue;
+    sgba_problem* p = problems[w];
+    cudaSetDevice(p->device);
+    double nu = 0.0;
+    if (prm->skip_final_hessian) {
+      Ctrl c;
+      if (cudaMemcpyAsync(&c, p->d.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, p->stream) != cudaSuccess ||
+          cudaStreamSynchronize(p->stream) != cudaSuccess) {
+        results[w].status = set_error(SGBA_ERR_CUDA, "window %d: state readback failed", w);
+        live[w] = 0;
+        continue;
+      }
+      nu = c.nu;
+    }
+    sgba::launch_linearize(p->sz, p->d, nu, true, p->stream);
+    cudaEventRecord(e1[w], p->stream);
+  }
+  // 3. collect
+  for (int w = 0; w < n; ++w) {
+    sgba_window_result& r = results[w];
+    if (live[w]) {
+      sgba_problem* p = problems[w];
+      cudaSetDevice(p->device);
+      Ctrl c;
+      cudaError_t e = cudaMemcpyAsync(&c, p->d.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, p->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+      if (e != cudaSuccess) {
+        r.status = set_error(SGBA_ERR_CUDA, "window %d: %s", w, cudaGetErrorString(e));
+      } else {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0[w], e1[w]);
+        r.status = SGBA_OK;
+        r.termination = c.termination;
+        r.n_records = c.step;
+        r.ms = ms;
+        r.final_cost = c.merit;
+        if (records && cap > 0) {
+          const int nrec = std::min(std::min(c.step, p->d.record_cap), cap);
+          if (nrec > 0 && cudaMemcpy(records + static_cast<int64_t>(w) * cap, p->d.records, sizeof(Record) * nrec,
+                                     cudaMemcpyDeviceToHost) != cudaSuccess)
+            r.status = set_error(SGBA_ERR_CUDA, "window %d: record readback failed", w);
+        }
+      }
+    }
+    if (e0[w]) cudaEventDestroy(e0[w]);
+    if (e1[w]) cudaEventDestroy(e1[w]);
+  }
   return SGBA_OK;
 }
 

@@ -97,13 +97,23 @@ class Profile(C.Structure):
     ]
 
 
+class WindowResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int32),
+        ("termination", C.c_int32),
+        ("n_records", C.c_int32),
+        ("ms", C.c_float),
+        ("final_cost", C.c_double),
+    ]
+
+
 EXPORTED = [
     "sgba_abi_version", "sgba_last_error", "sgba_problem_create", "sgba_problem_destroy",
     "sgba_optimizer_init", "sgba_optimizer_step", "sgba_optimize", "sgba_get_variables",
     "sgba_get_cost", "sgba_set_variables", "sgba_get_layout", "sgba_export_pattern",
     "sgba_debug_last_system", "sgba_state_save", "sgba_state_load", "sgba_get_profile",
     "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_synth_generate",
-    "sgba_synth_free",
+    "sgba_synth_free", "sgba_batch_optimize",
 ]
 
 # sgba_kernel_id
@@ -158,6 +168,8 @@ def lib():
     L.sgba_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     L.sgba_bench_iterations.argtypes = [C.c_void_p, C.c_int32, C.c_int32, dp, C.POINTER(C.c_int64)]
     L.sgba_bench_kernel.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, dp]
+    L.sgba_batch_optimize.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(OptParamsC),
+                                      C.POINTER(IterRecord), C.c_int32, C.POINTER(WindowResult)]
     _lib = L
     return L
 
@@ -341,3 +353,22 @@ class Problem:
         ms = C.c_double()
         check(lib().sgba_bench_kernel(self._h, int(kernel), int(reps), 1 if flush_l2 else 0, C.byref(ms)))
         return ms.value
+
+
+def batch_optimize(problems, params):
+    """sgba_batch_optimize over Problem handles (independent windows).
+
+    Returns one (records, termination, device_ms, final_cost, status) tuple per
+    window; the windows run concurrently, one stream each."""
+    n = len(problems)
+    cap = max(1, int(params.num_iterations))
+    handles = (C.c_void_p * n)(*[p._h for p in problems])
+    recs = (IterRecord * (n * cap))()
+    res = (WindowResult * n)()
+    check(lib().sgba_batch_optimize(handles, n, C.byref(opt_params_c(params)), recs, cap, res))
+    out = []
+    for w in range(n):
+        r = res[w]
+        k = min(r.n_records, cap)
+        out.append(([recs[w * cap + i] for i in range(k)], r.termination, r.ms, r.final_cost, r.status))
+    return out

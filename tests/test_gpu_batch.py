@@ -1,0 +1,56 @@
+"""Batched optimisation of independent local windows (configs[3] of the scope
+table: 5-40 cameras, 200-4000 points per window) through sgba_batch_optimize.
+
+Every window must come out exactly as sgba_optimize computes it alone (the
+same kernels on the same data, run concurrently on separate streams), and
+match the oracle per iteration within the parity tolerance."""
+import numpy as np
+import pytest
+
+from conftest import fixed_iter_params
+
+pytestmark = pytest.mark.gpu
+
+COST_RTOL = 1e-6
+
+
+def _windows(pkg, n):
+    return [pkg.synth.generate(pkg.synth.WINDOW, seed=pkg.synth.BASE_SEED + 3 + w) for w in range(n)]
+
+
+def test_batch_equals_single_and_oracle(pkg, oracle):
+    wins = _windows(pkg, 6)
+    params = fixed_iter_params(pkg, 10, wins[0].initial_lm_damping)
+    probs = [pkg.native.Problem(w, device=0) for w in wins]
+    try:
+        out = pkg.native.batch_optimize(probs, params)
+        batch_vars = [p.variables() for p in probs]
+    finally:
+        for p in probs:
+            p.close()
+    for w, (recs, term, ms, final_cost, status) in enumerate(out):
+        assert status == pkg.native.OK
+        assert term == pkg.native.TERM_MAX_ITERATIONS and len(recs) == 10
+        assert ms > 0.0 and np.isfinite(final_cost)
+        with pkg.native.Problem(wins[w], device=0) as gp:
+            srecs, sterm = gp.optimize(params)
+            sposes, spoints = gp.variables()
+        assert [r.merit for r in recs] == [r.merit for r in srecs]
+        assert np.array_equal(batch_vars[w][0], sposes) and np.array_equal(batch_vars[w][1], spoints)
+        assert final_cost == srecs[-1].merit
+    for w in (0, 3):
+        orecs, _, _ = oracle.optimize(wins[w], params, n_threads=8)
+        g = np.array([r.merit for r in out[w][0]])
+        o = np.array([r.merit for r in orecs])
+        assert np.max(np.abs(g - o) / o) < COST_RTOL
+
+
+def test_batch_reports_per_window_errors(pkg):
+    good = _windows(pkg, 1)[0]
+    bad = good.copy()
+    bad.point_const = np.ones(bad.n_pt, np.uint8)  # nothing marginalized: the Schur solver refuses it
+    params = fixed_iter_params(pkg, 3, good.initial_lm_damping)
+    with pkg.native.Problem(good, device=0) as p0, pkg.native.Problem(bad, device=0) as p1:
+        out = pkg.native.batch_optimize([p0, p1], params)
+    assert out[0][4] == pkg.native.OK and len(out[0][0]) == 3
+    assert out[1][4] == pkg.native.ERR_SCHUR_MISSING_FREE_OR_MARG
