@@ -7,8 +7,9 @@
 // PSD-aware pivot rule of the reference (crates/sophus_solver/src/ldlt/dense_ldlt.rs:164-270,
 // tol_rel = 1e-12, the relative threshold restarting at every 6x6 pose block;
 // a zero pivot zeroes its column of L and its solution entry), FP32 factor,
-// then one refinement step whose residual b - S x is formed in float-float
-// from the float-float copy of S written by k_schur.
+// of the diagonally scaled matrix, then refinement steps whose residual
+// b - S x is formed in float-float from the float-float copy of S written by
+// k_schur.
 //
 // Layout: n is padded to P blocks of kNB = 24 rows (4 pose blocks; padding
 // rows are identity).  Row block r (rows 24r..24r+23, columns 0..24r+23) lives
@@ -55,6 +56,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kMaxOwn = 24;          // row blocks per CTA
 constexpr int kMaxCluster = 16;
 constexpr float kTolRel = 1e-12f;
+constexpr int kRefine = 2;           // refinement steps against the float-float S
 constexpr size_t kSmemLimit = 232448;  // 227 KiB opt-in dynamic shared memory per CTA
 
 __host__ __device__ inline int row_ld(int r) { return kNB * (r + 1) + 4; }
@@ -63,7 +65,7 @@ __host__ __device__ inline int row_ld(int r) { return kNB * (r + 1) + 4; }
 struct Carve {
   int nown;
   int rowoff[kMaxOwn];
-  int wt, linv, dloc, rdloc, lpp, rdp, y, x, xs, bl, facc, accb, vdef, red, tmp, tmp2, flags, total;
+  int wt, linv, dloc, rdloc, lpp, rdp, y, x, xs, xlo, bl, facc, accb, vdef, udef, red, tmp, tmp2, flags, total;
 };
 
 __host__ __device__ inline void carve(int P, int C, int rank, Carve* c) {
@@ -85,10 +87,12 @@ __host__ __device__ inline void carve(int P, int C, int rank, Carve* c) {
   c->y = take(npad);
   c->x = take(npad);
   c->xs = take(npad);
+  c->xlo = take(npad);
   c->bl = take(npad);
   c->facc = take(c->nown * kNB);
   c->accb = take(npad);
   c->vdef = take(npad);
+  c->udef = take(npad);
   c->red = take(2 * kThreads);
   c->tmp = take(32);
   c->tmp2 = take(32);
@@ -123,7 +127,7 @@ __device__ __forceinline__ void cl_sync() {
 // Offsets of every rank's regions (remote addressing), filled at kernel start.
 struct RankTab {
   int rowoff[kMaxCluster][kMaxOwn];
-  int linv[kMaxCluster], rdloc[kMaxCluster], y[kMaxCluster], x[kMaxCluster], accb[kMaxCluster];
+  int linv[kMaxCluster], rdloc[kMaxCluster], y[kMaxCluster], x[kMaxCluster], accb[kMaxCluster], flags[kMaxCluster];
 };
 
 struct Ctx {
@@ -521,19 +525,23 @@ __device__ dd block_sum_dd(dd v, float* red) {
   return r;
 }
 
-// bl = FP32(b - (S + alpha v v^T) x) on the owned rows, b and S in
-// float-float, x = FP32 x0, v the unit gauge direction (zero without gauge).
+// bl = D^-1/2 (b - S x) on the owned rows (FP32 of the float-float
+// residual), b and S in float-float, x = (xs, xlo) the float-float solution.
 __device__ void residual(const Ctx& X, const DenseArgs& a, float alpha) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const float* x = X.sm + X.cv->x;
+  const float* xh = X.sm + X.cv->xs;
+  const float* xl = X.sm + X.cv->xlo;
   const float* vd = X.sm + X.cv->vdef;
+  const float* ud = X.sm + X.cv->udef;
   float* bl = X.sm + X.cv->bl;
-  float* red = X.sm + X.cv->red;
+  float* wred = X.sm + X.cv->red + 64 * warp;
+  // deflated operator (retry after a breakdown): subtract alpha u (u . x~), x~ = D^1/2 x
   dd g = dd_make(0.f, 0.f);
-  for (int k = tid; k < a.n; k += kThreads) g = dd_add(g, dd_mul_f(dd_make(vd[k], 0.f), x[k]));
-  g = block_sum_dd(g, red);
+  if (alpha != 0.0f) {
+    for (int k = tid; k < a.n; k += kThreads) g = dd_add(g, dd_mul_f(dd_make(xh[k], xl[k]), ud[k] / vd[k]));
+    g = block_sum_dd(g, X.sm + X.cv->red);
+  }
   const dd ag = dd_mul_f(g, alpha);
-  float* wred = red + 64 * warp;
   for (int jr = 0; jr < X.cv->nown; ++jr) {
     const int r = X.rank + jr * X.C;
     for (int i = warp; i < kNB; i += kWarps) {
@@ -554,17 +562,76 @@ __device__ void residual(const Ctx& X, const DenseArgs& a, float alpha) {
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
           const int k = k0 + 32 * u;
-          if (k < a.n) acc = dd_add(acc, dd_mul_f(dd_make(sv[u].x, sv[u].y), x[k]));
+          if (k < a.n) acc = dd_add(acc, dd_mul(dd_make(sv[u].x, sv[u].y), dd_make(xh[k], xl[k])));
         }
       }
       acc = warp_sum_dd(acc, wred, lane);
       if (lane == 0) {
-        acc = dd_add(acc, dd_mul_f(ag, vd[row]));
         const dd rr = dd_sub(dd_from_double(a.b[row]), acc);
-        bl[row] = rr.hi + rr.lo;
+        bl[row] = (rr.hi + rr.lo) * vd[row] - (ag.hi + ag.lo) * ud[row];
       }
     }
   }
+}
+
+__device__ __forceinline__ float* dsm_ptr(const Ctx& X) { return X.sm; }
+
+__device__ void load_rows(const Ctx& X, const DenseArgs& a, float alpha) {
+  const int tid = threadIdx.x;
+  const float* vd = dsm_ptr(X) + X.cv->vdef;
+  const float* ud = dsm_ptr(X) + X.cv->udef;
+  float* dsm = dsm_ptr(X);
+  // load the owned row blocks (FP32 high part of the scaled S; padding rows are identity)
+  for (int jr = 0; jr < X.cv->nown; ++jr) {
+    const int r = X.rank + jr * X.C;
+    const int w = kNB * (r + 1), ld = X.ld(r);
+    float* Ar = dsm + X.cv->rowoff[jr];
+    for (int e0 = tid; e0 < kNB * w; e0 += kThreads * 8) {
+      float hv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + kThreads * u;
+        const int i = e / w, col = e - i * w, row = kNB * r + i;
+        hv[u] = (e < kNB * w && row < a.n && col < a.n) ? a.S2[static_cast<int64_t>(row) * a.n + col].x : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + kThreads * u;
+        if (e >= kNB * w) break;
+        const int i = e / w, col = e - i * w, row = kNB * r + i;
+        Ar[i * ld + col] = (row < a.n && col < a.n) ? fmaf(alpha * ud[row], ud[col], hv[u] * vd[row] * vd[col])
+                                                    : (row == col ? 1.0f : 0.0f);
+      }
+    }
+    for (int i = tid; i < kNB; i += kThreads) {
+      const int row = kNB * r + i;
+      dsm[X.cv->bl + row] = (row < a.n) ? static_cast<float>(a.b[row]) * vd[row] : 0.0f;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ void factor(const Ctx& X, cg::cluster_group& cl, int* flags) {
+  const int warp = threadIdx.x >> 5;
+  if (X.rank == 0 && warp == 0) diag_step(X, 0, flags);
+  for (int p = 0; p < X.P; ++p) {
+    cl_sync();  // Linv_pp and 1/d_p final in the owner of p
+    pull_diag(X, cl, p);
+    __syncthreads();
+    panel_rows(X, p);
+    cl_sync();  // L_rp final for every r > p
+    if (p + 1 < X.P) {
+      if (X.owns(p + 1)) {
+        diag_update(X, p);
+        __syncthreads();
+        if (warp == 0) diag_step(X, p + 1, flags);
+        else update_blocks(X, cl, p, p + 2, X.P - 1, 1, kWarps - 1);
+      } else {
+        update_blocks(X, cl, p, p + 1, X.P - 1, 0, kWarps);
+      }
+    }
+  }
+  __syncthreads();
 }
 
 __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl* ctrl) {
@@ -595,122 +662,113 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
     T.y[tid] = rc.y;
     T.x[tid] = rc.x;
     T.accb[tid] = rc.accb;
+    T.flags[tid] = rc.flags;
   }
   __syncthreads();
   int* flags = reinterpret_cast<int*>(dsm + s_cv.flags);
   if (tid == 0) flags[0] = 0;
-  // Gauge deflation.  With one constant camera and no constant point the
-  // reduced system has one eigenvalue of order nu (the scale direction v of
-  // the free poses' translations, rotation rows zero) against the rest of the
-  // spectrum; FP32 cannot factor that reliably.  The factor and the refinement
-  // use S + alpha v v^T (unit v, alpha = max diag S) instead: in exact
-  // arithmetic its solution differs from S^-1 b only along v, and the
-  // component along v is set afterwards by the gauge projection of the full
-  // step (an identity of the exact damped step).
+  // Symmetric diagonal (Jacobi) scaling: the factor is of D^-1/2 S D^-1/2,
+  // D = diag S, an exact change of variables that removes the conditioning
+  // due to the mixed units of rotation and translation rows (measured: the
+  // reduced system of a 100-camera loop goes from 4e10 to 1.5e7).
   const int npad = kNB * X.P;
-  float* vd = dsm + s_cv.vdef;
-  float* red = dsm + s_cv.red;
-  float alpha = 0.0f;
+  float* vd = dsm + s_cv.vdef;  // D^-1/2 (1 on padding and non-positive diagonals)
   for (int k = tid; k < npad; k += kThreads) {
-    float v = 0.0f;
-    if (a.gauge && k < a.n && k % 6 >= 3) {
-      const double* tp = a.poses + 7 * a.fb_pose[k / 6];
-      v = static_cast<float>(tp[4 + k % 6 - 3] - a.center[k % 6 - 3]);
+    float v = 1.0f;
+    if (k < a.n) {
+      const float dk = a.S2[static_cast<int64_t>(k) * a.n + k].x;
+      if (dk > 0.0f && isfinite(dk)) v = 1.0f / sqrtf(dk);
     }
     vd[k] = v;
+    dsm[s_cv.udef + k] = 0.0f;  // no deflation unless the factor breaks down
   }
-  if (a.gauge) {
-    __syncthreads();
-    float s2 = 0.0f, m = 0.0f;
-    for (int k = tid; k < a.n; k += kThreads) {
-      s2 = fmaf(vd[k], vd[k], s2);
-      m = fmaxf(m, a.S2[static_cast<int64_t>(k) * a.n + k].x);
-    }
-    red[tid] = s2;
-    red[kThreads + tid] = m;
-    __syncthreads();
-    for (int s = kThreads / 2; s > 0; s >>= 1) {
-      if (tid < s) {
-        red[tid] += red[tid + s];
-        red[kThreads + tid] = fmaxf(red[kThreads + tid], red[kThreads + tid + s]);
+  __syncthreads();
+  load_rows(X, a, 0.0f);
+  cl_sync();  // every CTA is running before the first DSMEM access
+  factor(X, cl, flags);
+  // A negative (or non-finite) pivot of the scaled FP32 factor means the
+  // scale-gauge eigenvalue was lost to rounding (tiny problems): refactor the
+  // scaled system deflated along u = D^1/2 v, the gauge direction in scaled
+  // variables (its solution differs from the exact one essentially only along
+  // the gauge, which the gauge projection of the full step sets).
+  float alpha = 0.0f;
+  {
+    int bad = 0;
+    for (int jr = 0; jr < s_cv.nown; ++jr)
+      for (int t = 0; t < kNB; ++t) {
+        const float dv = dsm[s_cv.dloc + kNB * jr + t];
+        if (!(dv >= 0.0f)) bad = 1;
+      }
+    if (tid == 0) flags[1] = bad;
+    cl_sync();
+    int any = 0;
+    for (int c = 0; c < X.C; ++c) any |= reinterpret_cast<const int*>(remote(cl, dsm, c, T.flags[c]))[1];
+    cl_sync();  // every CTA has read the flags
+    if (any && a.gauge) {
+      float* ud = dsm + s_cv.udef;
+      float* red = dsm + s_cv.red;
+      for (int k = tid; k < npad; k += kThreads) {
+        float v = 0.0f;
+        if (k < a.n && k % 6 >= 3) {
+          const double* tp = a.poses + 7 * a.fb_pose[k / 6];
+          v = static_cast<float>(tp[4 + k % 6 - 3] - a.center[k % 6 - 3]) / vd[k];
+        }
+        ud[k] = v;
       }
       __syncthreads();
-    }
-    const float st = red[0], mt = red[kThreads];
-    const float inv = (st > 0.0f) ? 1.0f / sqrtf(st) : 0.0f;
-    alpha = (st > 0.0f) ? mt : 0.0f;
-    __syncthreads();
-    for (int k = tid; k < npad; k += kThreads) vd[k] *= inv;
-  }
-  __syncthreads();
-  // load the owned row blocks (FP32 high part of S + alpha v v^T; padding rows are identity)
-  for (int jr = 0; jr < s_cv.nown; ++jr) {
-    const int r = X.rank + jr * X.C;
-    const int w = kNB * (r + 1), ld = X.ld(r);
-    float* Ar = dsm + s_cv.rowoff[jr];
-    for (int e0 = tid; e0 < kNB * w; e0 += kThreads * 8) {
-      float hv[8];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = e0 + kThreads * u;
-        const int i = e / w, col = e - i * w, row = kNB * r + i;
-        hv[u] = (e < kNB * w && row < a.n && col < a.n) ? a.S2[static_cast<int64_t>(row) * a.n + col].x : 0.0f;
-      }
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = e0 + kThreads * u;
-        if (e >= kNB * w) break;
-        const int i = e / w, col = e - i * w, row = kNB * r + i;
-        Ar[i * ld + col] = (row < a.n && col < a.n) ? fmaf(alpha * vd[row], vd[col], hv[u])
-                                                    : (row == col ? 1.0f : 0.0f);
-      }
-    }
-    for (int i = tid; i < kNB; i += kThreads) {
-      const int row = kNB * r + i;
-      dsm[s_cv.bl + row] = (row < a.n) ? static_cast<float>(a.b[row]) : 0.0f;
-    }
-  }
-  __syncthreads();
-  cl_sync();  // every CTA is running before the first DSMEM access
-  if (X.rank == 0 && warp == 0) diag_step(X, 0, flags);
-  for (int p = 0; p < X.P; ++p) {
-    cl_sync();  // Linv_pp and 1/d_p final in the owner of p
-    pull_diag(X, cl, p);
-    __syncthreads();
-    panel_rows(X, p);
-    cl_sync();  // L_rp final for every r > p
-    if (p + 1 < X.P) {
-      if (X.owns(p + 1)) {
-        diag_update(X, p);
+      float s2 = 0.0f;
+      for (int k = tid; k < npad; k += kThreads) s2 = fmaf(ud[k], ud[k], s2);
+      red[tid] = s2;
+      __syncthreads();
+      for (int h = kThreads / 2; h > 0; h >>= 1) {
+        if (tid < h) red[tid] += red[tid + h];
         __syncthreads();
-        if (warp == 0) diag_step(X, p + 1, flags);
-        else update_blocks(X, cl, p, p + 2, X.P - 1, 1, kWarps - 1);
-      } else {
-        update_blocks(X, cl, p, p + 1, X.P - 1, 0, kWarps);
       }
+      const float inv = red[0] > 0.0f ? 1.0f / sqrtf(red[0]) : 0.0f;
+      __syncthreads();
+      for (int k = tid; k < npad; k += kThreads) ud[k] *= inv;
+      alpha = 1.0f;  // the scaled diagonal is 1
+      if (tid == 0) flags[0] = 0;
+      __syncthreads();
+      load_rows(X, a, alpha);
+      __syncthreads();
+      factor(X, cl, flags);
     }
   }
-  __syncthreads();
-  // x0 = (L D L^T)^-1 b in FP32
+  // x0 = D^-1/2 (LDL^T)^-1 D^-1/2 b in FP32, then kRefine corrections against
+  // the float-float S; the solution is kept as float-float (xs, xlo) in every CTA.
   solve_forward(X, cl);
   solve_backward(X, cl);
   cl_sync();
   gather_x(X, cl);
-  for (int k = tid; k < npad; k += kThreads) dsm[s_cv.xs + k] = dsm[s_cv.x + k];
-  residual(X, a, alpha);
+  for (int k = tid; k < npad; k += kThreads) {
+    dsm[s_cv.xs + k] = dsm[s_cv.x + k] * vd[k];
+    dsm[s_cv.xlo + k] = 0.0f;
+  }
   __syncthreads();
-  // correction dx = (L D L^T)^-1 (b - S x0); x = x0 + dx in float-float
-  solve_forward(X, cl);
-  solve_backward(X, cl);
+  for (int it = 0; it < kRefine; ++it) {
+    residual(X, a, alpha);
+    __syncthreads();
+    solve_forward(X, cl);
+    solve_backward(X, cl);
+    cl_sync();
+    gather_x(X, cl);
+    for (int k = tid; k < npad; k += kThreads) {
+      const dd v = dd_add_f(dd_make(dsm[s_cv.xs + k], dsm[s_cv.xlo + k]), dsm[s_cv.x + k] * vd[k]);
+      dsm[s_cv.xs + k] = v.hi;
+      dsm[s_cv.xlo + k] = v.lo;
+    }
+    __syncthreads();
+  }
   for (int jr = 0; jr < s_cv.nown; ++jr) {
     const int r = X.rank + jr * X.C;
     for (int i = tid; i < kNB; i += kThreads) {
       const int row = kNB * r + i;
       if (row >= a.n) continue;
-      const dd v = dd_add_f(dd_make(dsm[s_cv.xs + row], 0.0f), dsm[s_cv.x + row]);
-      a.x[row] = static_cast<double>(v.hi) + static_cast<double>(v.lo);
-      a.xdd[2 * row] = v.hi;
-      a.xdd[2 * row + 1] = v.lo;
+      const float hi = dsm[s_cv.xs + row], lo = dsm[s_cv.xlo + row];
+      a.x[row] = static_cast<double>(hi) + static_cast<double>(lo);
+      a.xdd[2 * row] = hi;
+      a.xdd[2 * row + 1] = lo;
     }
   }
   if (tid == 0 && flags[0]) ctrl->skip = 2;  // NonFinitePivot -> solve failure -> reject
