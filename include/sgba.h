@@ -131,8 +131,10 @@ int sgba_optimizer_step(sgba_problem *p, sgba_iter_record *record);
 int sgba_optimize(sgba_problem *p, const sgba_opt_params *params, sgba_iter_record *records,
                   int32_t cap, int32_t *n_records, int32_t *termination);
 
-/* Batched optimize_nlls over independent problems (local windows, configs[3]
- * of the scope table): every window is an sgba_problem created as usual; the
+/* Batched optimize_nlls over independent problems (the local windows of a
+ * local bundle adjustment, 5-40 cameras each; in the reference one
+ * optimize_nlls call per window, crates/sophus_opt/src/nlls.rs):
+ * every window is an sgba_problem created as usual; the
  * windows' LM iterations are enqueued on their own streams and run
  * concurrently, with one host synchronisation at the end.  Per window the
  * result is exactly what sgba_optimize would return for it.

@@ -1,5 +1,5 @@
-"""Batched optimisation of independent local windows (configs[3] of the scope
-table: 5-40 cameras, 200-4000 points per window) through sgba_batch_optimize.
+"""Batched optimisation of independent local windows (5-40 cameras, 200-4000
+points per window) through sgba_batch_optimize.
 
 Every window must come out exactly as sgba_optimize computes it alone (the
 same kernels on the same data, run concurrently on separate streams), and
