@@ -166,7 +166,18 @@ typedef struct {
   int64_t n_h_blocks;       /* lower blocks of H: pose diag + point diag + point x pose */
   int64_t n_s_blocks;       /* lower 6x6 blocks of the reduced camera system S */
   int64_t n_schur_pairs;    /* observation pairs summed into S (sum over points of L(L+1)/2) */
+  int32_t solver;           /* reduced-system solver: SGBA_SOLVER_* */
+  int32_t band_width;       /* banded solver: band width in scalars (row r holds columns r-w+1..r) */
+  int32_t border_rows;      /* banded solver: dense border rows at the end (loop closures) */
+  int32_t reserved;
 } sgba_layout;
+/* Reduced camera system solvers (chosen at sgba_problem_create from the size
+ * and the block pattern of S). */
+enum {
+  SGBA_SOLVER_DENSE_CLUSTER = 0, /* dense S in one thread-block cluster's shared memory */
+  SGBA_SOLVER_BAND = 1,          /* band + dense border, float-float (sequential / loop problems) */
+  SGBA_SOLVER_DENSE_PANELS = 2   /* dense S, panel launches (large dense systems) */
+};
 int sgba_get_layout(sgba_problem *p, sgba_layout *out);
 
 /* Block sparsity of H (lower: row block, col block in the global block order

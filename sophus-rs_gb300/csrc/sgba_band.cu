@@ -1,0 +1,970 @@
+// sgba_band.cu -- factorization and solve of a banded reduced camera system
+// with a dense border: the reduced system of sequential and loop-shaped bundle
+// adjustment (cameras along a path, each point seen by a run of consecutive
+// cameras, loop closures between the last and the first cameras).
+//
+// Reference: BlockSparseLdlt::factorize_impl / solve_inplace
+// (crates/sophus_solver/src/ldlt/block_sparse_ldlt.rs:99-190, 479-747) with
+// the PSD-aware pivot rule of dense_ldlt.rs:164-270 (tol_rel = 1e-12, the
+// running maximum restarting at every 6x6 pose block).  The reference orders
+// the blocks by AMD; here the natural order is kept, which for these systems
+// has the fill of a band plus dense border rows.  In exact arithmetic every
+// order gives the same solution; only rounding differs.
+//
+// Structure (n = 6 n_f scalars, split after nband rows):
+//     S = [ A  C^T ]   A (nband x nband): row r has columns [r - W + 1, r] only;
+//         [ C  E   ]   C, E: the last nbd rows, dense (loop closures).
+// The natural-order LDL^T factor keeps A's band (fill stays inside each row's
+// envelope) and fills the border rows:
+//     A = L_A D_A L_A^T,   L_C = C L_A^-T D_A^-1,   E - L_C D_A L_C^T = L_E D_E L_E^T.
+// All arithmetic is float-float (48-bit significand) on the Jacobi-scaled
+// system D^-1/2 S D^-1/2: the reduced system of a 1500-camera loop has
+// kappa 6e10, 7.5e7 after scaling, beyond FP32 (and far beyond TF32/BF16
+// factors with refinement) but well inside float-float.
+//
+// Kernels (one LM iteration):
+//   k_band_scale      D^-1/2 from diag S
+//   k_band_load       band of A, border rows C | E and the right-hand side, scaled, float-float
+//   k_band_factor     one thread-block cluster: right-looking LDL^T of the band, 24-column panels;
+//                     rows dealt round-robin over the CTAs; per panel every CTA factors the 24x24
+//                     diagonal block (and the inverse of its unit lower factor) redundantly, solves
+//                     its own rows of the panel, then updates its own rows of the trailing band
+//   k_band_fwd        one CTA per border row and one for the right-hand side: z = L_A^-1 c
+//   k_band_corner     E - Z D_A^-1 Z^T (one warp per entry; the right-hand side row gives y_C)
+//   k_band_corner_solve  LDL^T of the corner and its solve
+//   k_band_tvec       t = D_A^-1 y_A - L_C^T x_C
+//   k_band_bwd        x_A = L_A^-T t, unscale, write the step
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "sgba_dd.cuh"
+#include "sgba_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace sgba {
+
+namespace {
+
+constexpr int kBP = 24;          // panel width (4 pose blocks)
+constexpr int kBT = 256;         // threads per CTA
+constexpr int kMaxWBlocks = 32;  // widest band, in pose blocks
+constexpr int kMaxW = 6 * kMaxWBlocks;
+constexpr int kMaxBorderBlocks = 24;
+constexpr int kMaxBorder = 6 * kMaxBorderBlocks;
+constexpr int kMaxOwnRows = (kMaxW - 1 + 7) / 8;  // rows of one CTA in a window (cluster >= 8)
+constexpr int kFwdSeg = 10;      // dot-product segments per panel row in the sweeps
+constexpr float kTolRel = 1e-12f;
+constexpr size_t kSmemLimit = 227 * 1024;
+
+__device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0; }
+
+__device__ __forceinline__ dd f2dd(float2 v) { return dd_make(v.x, v.y); }
+__device__ __forceinline__ float2 dd2f(dd v) { return make_float2(v.hi, v.lo); }
+
+// Accumulator of a float-float dot product: hi carries the running sum through
+// an exact TwoSum, every rounding error (of the products and of the sums)
+// goes into the float lo.  ~11 FP32 operations per term.
+struct Acc {
+  float hi, lo;
+};
+__device__ __forceinline__ Acc acc_init(dd v) { return Acc{v.hi, v.lo}; }
+__device__ __forceinline__ void acc_madd(Acc& a, dd x, dd y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  const float s = __fadd_rn(a.hi, p);
+  const float bb = __fsub_rn(s, a.hi);
+  const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  a.hi = s;
+  a.lo = __fadd_rn(a.lo, __fadd_rn(err, e));
+}
+__device__ __forceinline__ void acc_add(Acc& a, dd y) {
+  const float s = __fadd_rn(a.hi, y.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(y.hi, bb));
+  a.hi = s;
+  a.lo = __fadd_rn(a.lo, __fadd_rn(err, y.lo));
+}
+__device__ __forceinline__ dd acc_get(const Acc& a) { return dd_fast_two_sum(a.hi, a.lo); }
+
+__device__ __forceinline__ dd dd_from_prod(double v) { return dd_from_double(v); }
+
+// 1/d in float-float by Newton's iteration x <- x + x (1 - d x): the
+// hardware approximate reciprocal, one FP32 step (~2^-44 squared error terms
+// aside, 24 bits), then one float-float step whose residual 1 - d x is formed
+// from an exact product (1 - p.hi is exact: p.hi is within a few ulps of 1).
+__device__ __forceinline__ dd dd_rcp(dd d) {
+  float r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(d.hi));
+  r0 = __fmaf_rn(r0, __fmaf_rn(-d.hi, r0, 1.0f), r0);
+  const dd p = dd_mul_f(d, r0);
+  const float e = __fsub_rn(__fsub_rn(1.0f, p.hi), p.lo);
+  return dd_fast_two_sum(r0, __fmul_rn(r0, e));
+}
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_but_one() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+struct BandArgs {
+  int n;      // order of S
+  int nband;  // rows of the band part A (multiple of 6)
+  int W;      // band width: row r of A holds columns [r - W + 1, r]
+  int npan;   // 24-column panels of A
+  int nbd;    // border rows (n - nband)
+  int ring;   // row slots per CTA in the factor kernel
+  const double* S;  // n x n, both triangles
+  const double* b;  // reduced right-hand side
+  float* scl;       // n: D^-1/2
+  float2* Lb;       // nband x W: scaled A, then L_A below the diagonal
+  float2* Xinv;     // npan x 24 x 24: inverse of the unit lower diagonal block of each panel
+  float2* dpiv;     // n: pivots
+  float2* rdpiv;    // n: 1 / pivot (0 for a zero pivot)
+  float2* Pbuf;     // (W - 1) x 24: L D of the current panel, rows below it
+  float2* Zc;       // (nbd + 1) x nband: border rows of C and the scaled right-hand side, then L_A^-1 of them
+  float2* Zd;       // (nbd + 1) x nband: D_A^-1 Zc
+  float2* Cn;       // (nbd + 1) x (nbd + 1): E and the border part of the right-hand side, then the corner
+  float2* xw;       // n: t (band part) and x_C (border part)
+  double* x;        // n: the step (unscaled)
+  float* xdd;       // 2n: the step as float-float pairs
+};
+
+
+// ---------------------------------------------------------------- set-up ---
+
+__global__ void __launch_bounds__(256) k_band_scale(BandArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.n; r += gridDim.x * blockDim.x) {
+    const double v = a.S[static_cast<int64_t>(r) * a.n + r];
+    a.scl[r] = (v > 0.0 && isfinite(v)) ? static_cast<float>(1.0 / sqrt(v)) : 1.0f;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_band_load(BandArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  const int64_t nb_entries = static_cast<int64_t>(a.nband) * a.W;
+  const int64_t nz_entries = static_cast<int64_t>(a.nbd + 1) * a.nband;
+  const int64_t nc_entries = static_cast<int64_t>(a.nbd + 1) * (a.nbd + 1);
+  const int64_t total = nb_entries + nz_entries + nc_entries;
+  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < total;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (e < nb_entries) {
+      const int r = static_cast<int>(e / a.W);
+      const int c = r - a.W + 1 + static_cast<int>(e % a.W);
+      float2 v = make_float2(0.0f, 0.0f);
+      if (c >= 0) {
+        const double s = a.S[static_cast<int64_t>(r) * a.n + c];
+        v = dd2f(dd_from_prod(s * static_cast<double>(a.scl[r]) * static_cast<double>(a.scl[c])));
+      }
+      a.Lb[e] = v;
+    } else if (e < nb_entries + nz_entries) {
+      const int64_t q = e - nb_entries;
+      const int i = static_cast<int>(q / a.nband), c = static_cast<int>(q % a.nband);
+      double v;
+      if (i < a.nbd) {
+        const int r = a.nband + i;
+        v = a.S[static_cast<int64_t>(r) * a.n + c] * static_cast<double>(a.scl[r]) * static_cast<double>(a.scl[c]);
+      } else {
+        v = a.b[c] * static_cast<double>(a.scl[c]);
+      }
+      a.Zc[q] = dd2f(dd_from_prod(v));
+    } else {
+      const int64_t q = e - nb_entries - nz_entries;
+      const int i = static_cast<int>(q / (a.nbd + 1)), j = static_cast<int>(q % (a.nbd + 1));
+      double v = 0.0;
+      if (j < a.nbd) {
+        const int cj = a.nband + j;
+        if (i < a.nbd) {
+          const int r = a.nband + i;
+          v = a.S[static_cast<int64_t>(r) * a.n + cj] * static_cast<double>(a.scl[r]) *
+              static_cast<double>(a.scl[cj]);
+        } else {
+          v = a.b[cj] * static_cast<double>(a.scl[cj]);
+        }
+      }
+      a.Cn[q] = dd2f(dd_from_prod(v));
+    }
+  }
+}
+
+// ------------------------------------------------------- band factor -------
+
+struct FactorShared {
+  float2 dg[kBP][kBP + 1];   // diagonal block; L below the diagonal after the factor
+  float2 xi[kBP][kBP + 1];   // inverse of the unit lower factor
+  float2 sd[kBP], srd[kBP];  // pivots and their reciprocals
+  float2 arow[kMaxOwnRows][kBP];
+  const float2* dsrc[kBP];   // diagonal-block rows: their slots in the owners' shared memory
+  const float4* psrc[kMaxW]; // L D rows of the panel in their owners' shared memory
+  int rofs[kMaxOwnRows];     // own window rows: offset of column 0 in `rows`
+  int pre[kMaxOwnRows + 1];  // update work prefix over the own rows
+  int bad;
+};
+
+// Rows of the band are dealt round-robin: row r belongs to CTA r mod C and
+// lives, while it is within reach of the current panel, in slot
+// (r / C) mod ring of that CTA's shared memory (ring a power of two).  Rows
+// are prefetched with cp.async two panels ahead (the group issued after panel
+// p is waited for at panel p + 2), so the live rows span at most W + 72 and
+// ring * C >= W + 72 + C keeps two of them out of one slot.  A row is written
+// back to global memory once its own panel is factored.
+// Per panel: every CTA gathers the 24x24 diagonal block from the owners
+// (DSMEM) and factors it redundantly; each CTA solves its own rows of the
+// panel and publishes L D of them; after a cluster barrier every CTA gathers
+// the panel's L D (DSMEM) and updates its own rows in place.
+template <int C>
+__global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) {
+  // Every CTA reads the control block before the first cluster barrier and
+  // only CTA 0 writes it, after the last one: the early return is uniform.
+  if (skipping(ctrl)) return;
+  __shared__ FactorShared sh;
+  extern __shared__ __align__(16) float2 dyn[];
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = static_cast<int>(cl.block_rank());
+  const int tid = threadIdx.x;
+  const int W = a.W, rmask = a.ring - 1;
+  float2* rows = dyn;                  // ring x W
+  float2* pld = rows + a.ring * W;     // ring x kBP: L D of the own rows of the current panel
+  float2* pb = pld + a.ring * kBP;     // (W - 1) x (kBP + 1): L D of the panel, all rows below it
+  auto slot = [&](int r) { return (r / C) & rmask; };
+  // element (r, c) of an own row r: rows[rbase(r) + c]
+  auto rbase = [&](int r) { return slot(r) * W + (W - 1 - r); };
+  int loaded = 0;  // own rows below this index are resident (or in flight)
+  auto prefetch = [&](int hi) {
+    hi = min(hi, a.nband);
+    if (hi > loaded) {
+      const int r0 = loaded + ((rank - loaded % C) + C) % C;
+      const int nr = (r0 < hi) ? (hi - r0 + C - 1) / C : 0;
+      for (int e = tid; e < nr * W; e += kBT) {
+        const int r = r0 + (e / W) * C, k = e % W;
+        cp_async8(rows + slot(r) * W + k, a.Lb + static_cast<int64_t>(r) * W + k);
+      }
+      loaded = hi;
+    }
+    cp_async_commit();
+  };
+  if (tid == 0) sh.bad = 0;
+  // the entries of the 24x24 block this thread updates
+  int fi[3], fq[3];
+#pragma unroll
+  for (int u3 = 0; u3 < 3; ++u3) {
+    const int e = tid + u3 * kBT;
+    fi[u3] = (e < kBP * kBP) ? e / kBP : kBP;  // kBP: no entry
+    fq[u3] = (e < kBP * kBP) ? e % kBP : 0;
+  }
+  prefetch(W + 3 * kBP);
+  for (int p = 0; p < a.npan; ++p) {
+    const int c0 = kBP * p;
+    const int w = min(kBP, a.nband - c0);
+    const int c1 = c0 + w;
+    const int rend = min(c1 + W - 1, a.nband);
+    const int rfirst = c1 + ((rank - c1 % C) + C) % C;
+    const int nown = (rfirst < rend) ? (rend - rfirst + C - 1) / C : 0;
+    // rows < c0 + W + 46 are needed now; the group issued two panels ago
+    // covered rows < c0 + W + 48, the newest one may stay in flight
+    if (p == 0) cp_async_wait_all();
+    else cp_async_wait_but_one();
+    __syncthreads();  // the previous panel's readers of the tables below are done
+    if (tid < w) {
+      const int r = c0 + tid;
+      sh.dsrc[tid] = cl.map_shared_rank(rows + slot(r) * W, r % C);  // slot base; column c at c - r + W - 1
+    }
+    if (tid >= 32 && tid - 32 < rend - c1) {
+      const int r = c1 + tid - 32;
+      sh.psrc[tid - 32] = reinterpret_cast<const float4*>(cl.map_shared_rank(pld + slot(r) * kBP, r % C));
+    }
+    if (tid == 64) {
+      int acc = 0;
+      for (int ri = 0; ri < nown; ++ri) {
+        const int r = rfirst + ri * C;
+        sh.pre[ri] = acc;
+        sh.rofs[ri] = rbase(r);
+        acc += r - max(c1, r - W + 1) + 1;
+      }
+      sh.pre[nown] = acc;
+    }
+    __syncthreads();
+    cl.sync();  // the previous panel's update of rows >= c0 is complete in every CTA
+    // (1) diagonal block from its owners, identity for its inverse
+    for (int e = tid; e < kBP * kBP; e += kBT) {
+      const int i = e / kBP, k = e % kBP;
+      float2 v = make_float2(0.0f, 0.0f);
+      if (i < w && k <= i && (k - i + W - 1) >= 0) v = sh.dsrc[i][k - i + W - 1];
+      sh.dg[i][k] = v;
+      sh.xi[i][k] = make_float2(i == k ? 1.0f : 0.0f, 0.0f);
+    }
+    __syncthreads();
+    // (2) LDL^T of the diagonal block, X <- L^-1 alongside (the elementary
+    // column eliminations applied to the identity).  Every thread evaluates
+    // the pivot itself (same inputs, same operations: the same value in every
+    // thread), so each pivot costs one barrier.  Column t is final after pivot
+    // t (later pivots touch columns > t only); it is scaled to L on output.
+    {
+      float maxp = 1.0f;
+      for (int t = 0; t < w; ++t) {
+        dd dt = f2dd(sh.dg[t][t]);
+        if ((c0 + t) % 6 == 0) maxp = 1.0f;
+        const float tol = fmaxf(maxp, 1.0f) * kTolRel;
+        if (!isfinite(dt.hi)) {
+          if (tid == 0) sh.bad = 1;
+          dt = dd_make(0.0f, 0.0f);
+        } else if (fabsf(dt.hi) <= tol) {
+          dt = dd_make(0.0f, 0.0f);
+        } else {
+          maxp = fmaxf(maxp, fabsf(dt.hi));
+        }
+        const dd rd = (dt.hi == 0.0f) ? dd_make(0.0f, 0.0f) : dd_rcp(dt);
+        if (tid == 0) {
+          sh.sd[t] = dd2f(dt);
+          sh.srd[t] = dd2f(rd);
+        }
+        // all loads of this thread's (up to) three entries first, then the
+        // arithmetic, then the stores: the three chains overlap
+        float2 va[3], vb[3], vc[3];
+        bool act[3];
+        float2* dst[3];
+#pragma unroll
+        for (int u3 = 0; u3 < 3; ++u3) {
+          const int i = fi[u3], q = fq[u3];
+          act[u3] = (i > t && i < w) && (q <= t || q <= i);
+          const int ii = act[u3] ? i : 0;
+          va[u3] = sh.dg[ii][t];
+          if (q > t) {  // trailing: a_iq -= l_it a_qt
+            dst[u3] = &sh.dg[ii][q];
+            vc[u3] = sh.dg[q < kBP ? q : 0][t];
+          } else {      // X_iq -= l_it X_tq, q <= t
+            dst[u3] = &sh.xi[ii][q];
+            vc[u3] = sh.xi[t][q];
+          }
+          vb[u3] = *dst[u3];
+        }
+        dd res[3];
+#pragma unroll
+        for (int u3 = 0; u3 < 3; ++u3) {
+          const dd li = dd_mul(f2dd(va[u3]), rd);
+          Acc acc = acc_init(f2dd(vb[u3]));
+          acc_madd(acc, dd_neg(li), f2dd(vc[u3]));
+          res[u3] = acc_get(acc);
+        }
+#pragma unroll
+        for (int u3 = 0; u3 < 3; ++u3)
+          if (act[u3]) *dst[u3] = dd2f(res[u3]);
+        __syncthreads();
+      }
+    }
+    // (3) outputs: X and pivots (spread over the CTAs); the own rows of this
+    // panel are final: write them back
+    for (int e = rank * kBT + tid; e < kBP * kBP; e += C * kBT)
+      a.Xinv[static_cast<int64_t>(p) * kBP * kBP + e] = sh.xi[e / kBP][e % kBP];
+    if (rank == C - 1 && tid < w) {
+      a.dpiv[c0 + tid] = sh.sd[tid];
+      a.rdpiv[c0 + tid] = sh.srd[tid];
+    }
+    {
+      const int d0 = c0 + ((rank - c0 % C) + C) % C;
+      const int nd = (d0 < c1) ? (c1 - d0 + C - 1) / C : 0;
+      for (int e = tid; e < nd * W; e += kBT) {
+        const int r = d0 + (e / W) * C, k = e % W;
+        const int c = r - W + 1 + k;
+        float2 v = make_float2(0.0f, 0.0f);
+        if (c >= 0 && c < c0) {
+          v = rows[slot(r) * W + k];
+        } else if (c >= c0 && c < r) {
+          v = dd2f(dd_mul(f2dd(sh.dg[r - c0][c - c0]), f2dd(sh.srd[c - c0])));
+        } else if (c == r) {
+          v = make_float2(1.0f, 0.0f);
+        }
+        a.Lb[static_cast<int64_t>(r) * W + k] = v;
+      }
+    }
+    // (4) own rows of the panel: L_rk = (sum_{j<=k} a_rj X_kj) / d_k
+    for (int e = tid; e < nown * kBP; e += kBT) {
+      const int ri = e / kBP, j = e % kBP;
+      const int r = rfirst + ri * C;
+      float2 v = make_float2(0.0f, 0.0f);
+      if (j < w && c0 + j >= r - W + 1) v = rows[sh.rofs[ri] + c0 + j];
+      sh.arow[ri][j] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < nown * kBP; e += kBT) {
+      const int ri = e / kBP, k = e % kBP;
+      const int r = rfirst + ri * C;
+      dd l = dd_make(0.0f, 0.0f);
+      if (k < w) {
+        Acc acc = acc_init(dd_make(0.0f, 0.0f));
+        for (int j = 0; j <= k; ++j) acc_madd(acc, f2dd(sh.arow[ri][j]), f2dd(sh.xi[k][j]));
+        l = dd_mul(acc_get(acc), f2dd(sh.srd[k]));
+        if (c0 + k >= r - W + 1) rows[sh.rofs[ri] + c0 + k] = dd2f(l);
+      }
+      pld[slot(r) * kBP + k] = dd2f(k < w ? dd_mul(l, f2dd(sh.sd[k])) : l);
+    }
+    cl.sync();  // L D of every row of the panel is published
+    // (5) the panel's L D, all rows below it, from their owners: 16-byte
+    // loads (a row is 12 float4), eight in flight per thread
+    const int nrows = rend - c1;
+    {
+      constexpr int kQ = kBP / 2;
+      const int nq = nrows * kQ;
+      for (int e0 = tid; e0 < nq; e0 += 8 * kBT) {
+        float4 v4[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int e = e0 + u * kBT;
+          if (e < nq) v4[u] = sh.psrc[e / kQ][e % kQ];
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int e = e0 + u * kBT;
+          if (e < nq) {
+            const int q = e / kQ, k2 = e % kQ;
+            pb[q * (kBP + 1) + 2 * k2] = make_float2(v4[u].x, v4[u].y);
+            pb[q * (kBP + 1) + 2 * k2 + 1] = make_float2(v4[u].z, v4[u].w);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // (6) trailing update of the own rows: a_rc -= sum_k L_rk d_k L_ck, c in [max(c1, r-W+1), r]
+    const int total = sh.pre[nown];
+    int ri = 0;  // e only grows: the row search carries over
+    for (int e = tid; e < total; e += kBT) {
+      while (ri + 1 < nown && sh.pre[ri + 1] <= e) ++ri;
+      const int r = rfirst + ri * C;
+      const int c = max(c1, r - W + 1) + (e - sh.pre[ri]);
+      float2* rowr = rows + sh.rofs[ri];
+      Acc acc0 = acc_init(f2dd(rowr[c]));
+      Acc acc1 = acc_init(dd_make(0.0f, 0.0f));
+      const float2* pr = pb + (c - c1) * (kBP + 1);
+      const int k0 = max(0, r - W + 1 - c0);  // L_rk is zero left of the band
+      int k = k0;
+      for (; k + 1 < w; k += 2) {
+        acc_madd(acc0, dd_neg(f2dd(rowr[c0 + k])), f2dd(pr[k]));
+        acc_madd(acc1, dd_neg(f2dd(rowr[c0 + k + 1])), f2dd(pr[k + 1]));
+      }
+      if (k < w) acc_madd(acc0, dd_neg(f2dd(rowr[c0 + k])), f2dd(pr[k]));
+      acc_add(acc0, acc_get(acc1));
+      rowr[c] = dd2f(acc_get(acc0));
+    }
+    // (7) rows that the panel after next reaches
+    prefetch(c0 + W + 4 * kBP);
+  }
+  cp_async_wait_all();
+  cl.sync();  // no CTA leaves while another may still read its shared memory
+  if (rank == 0 && tid == 0 && sh.bad) ctrl->skip = 2;  // NonFinitePivot -> solve failure -> reject
+}
+
+// ------------------------------------------------ forward substitution ----
+
+// Shared memory of the sweeps: the vector (nband), then two buffers of the
+// panel's L entries (kBP x (W - 1)) and two of its X (kBP x kBP).  Each panel's
+// entries are copied with cp.async while the previous panel is computed.
+__host__ __device__ inline size_t sweep_smem_floats2(int nband, int W) {
+  return static_cast<size_t>(nband) + 1 + 2 * static_cast<size_t>(kBP) * W + 2 * kBP * kBP;
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+// One CTA per row of Zc (border rows of C and the right-hand side):
+// z = L_A^-1 c, then Zd = D_A^-1 z.
+__global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  extern __shared__ __align__(16) float2 sw[];
+  const int W = a.W, span = W - 1;
+  float2* v = sw;
+  float2* blk = v + ((a.nband + 1) & ~1);  // 2 x kBP x W (16-byte aligned: W is even)
+  float2* xb = blk + 2 * kBP * W;          // 2 x kBP x kBP
+  __shared__ float2 part[kBP][kFwdSeg];
+  __shared__ float2 u[kBP];
+  const int tid = threadIdx.x;
+  const int row = blockIdx.x;
+  float2* zrow = a.Zc + static_cast<int64_t>(row) * a.nband;
+  // row c of panel p: slots [0, span) of Lb row c are the columns [c - W + 1, c);
+  // whole rows are copied (W float2, 16-byte pieces)
+  auto stage = [&](int p) {
+    const int c0 = kBP * p, w = min(kBP, a.nband - c0), buf = p & 1;
+    const int h = W / 2;
+    for (int e = tid; e < w * h; e += kBT) {
+      const int i = e / h, q = e % h;
+      cp_async16(blk + (buf * kBP + i) * W + 2 * q, a.Lb + static_cast<int64_t>(c0 + i) * W + 2 * q);
+    }
+    for (int e = tid; e < kBP * kBP / 2; e += kBT)
+      cp_async16(xb + buf * kBP * kBP + 2 * e, a.Xinv + static_cast<int64_t>(p) * kBP * kBP + 2 * e);
+    cp_async_commit();
+  };
+  for (int c = tid; c < a.nband; c += kBT) v[c] = zrow[c];
+  stage(0);
+  const int seg = (span + kFwdSeg - 1) / kFwdSeg;
+  for (int p = 0; p < a.npan; ++p) {
+    const int c0 = kBP * p;
+    const int w = min(kBP, a.nband - c0);
+    const int buf = p & 1;
+    if (p + 1 < a.npan) stage(p + 1);
+    else cp_async_commit();
+    cp_async_wait_but_one();
+    __syncthreads();
+    if (tid < kBP * kFwdSeg) {
+      const int cl = tid / kFwdSeg, sgi = tid % kFwdSeg;
+      Acc acc = acc_init(dd_make(0.0f, 0.0f));
+      if (cl < w) {
+        const int c = c0 + cl;
+        const int jlo = max(max(0, c - W + 1), c0 - span + sgi * seg);
+        const int jhi = min(c0, c0 - span + (sgi + 1) * seg);
+        const float2* lrow = blk + (buf * kBP + cl) * W + (W - 1 - c);
+        for (int j = jlo; j < jhi; ++j) acc_madd(acc, f2dd(lrow[j]), f2dd(v[j]));
+      }
+      part[cl][sgi] = dd2f(acc_get(acc));
+    }
+    __syncthreads();
+    if (tid < w) {
+      Acc acc = acc_init(f2dd(v[c0 + tid]));
+      for (int q = 0; q < kFwdSeg; ++q) acc_add(acc, dd_neg(f2dd(part[tid][q])));
+      u[tid] = dd2f(acc_get(acc));
+    }
+    __syncthreads();
+    if (tid < w) {
+      const float2* xr = xb + buf * kBP * kBP + tid * kBP;
+      Acc acc = acc_init(dd_make(0.0f, 0.0f));
+      for (int j = 0; j <= tid; ++j) acc_madd(acc, f2dd(xr[j]), f2dd(u[j]));
+      v[c0 + tid] = dd2f(acc_get(acc));
+    }
+    __syncthreads();
+  }
+  cp_async_wait_all();
+  float2* drow = a.Zd + static_cast<int64_t>(row) * a.nband;
+  for (int c = tid; c < a.nband; c += kBT) {
+    zrow[c] = v[c];
+    drow[c] = dd2f(dd_mul(f2dd(v[c]), f2dd(a.rdpiv[c])));
+  }
+}
+
+// ----------------------------------------------------------- corner -------
+
+// Lower entries (i, j), j <= i <= nbd, of the corner:
+// Cn_ij -= sum_c Zd_ic Zc_jc.  Row nbd (the right-hand side) becomes y_C.
+// One 128-thread CTA per 4x4 tile of entries; warp w takes row i = 4 ti + w
+// against the tile's four j (the Zc rows are shared through L1).
+constexpr int kCornerTile = 4;
+__global__ void __launch_bounds__(128) k_band_corner(BandArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t m = a.nbd + 1;
+  const int64_t nt = (m + kCornerTile - 1) / kCornerTile;
+  const int64_t ntiles = nt * (nt + 1) / 2;
+  __shared__ float2 red[kCornerTile][kCornerTile][32];
+  for (int64_t q = blockIdx.x; q < ntiles; q += gridDim.x) {
+    int ti = static_cast<int>((sqrt(8.0 * static_cast<double>(q) + 1.0) - 1.0) * 0.5);
+    while (static_cast<int64_t>(ti) * (ti + 1) / 2 > q) --ti;
+    while (static_cast<int64_t>(ti + 1) * (ti + 2) / 2 <= q) ++ti;
+    const int tj = static_cast<int>(q - static_cast<int64_t>(ti) * (ti + 1) / 2);
+    const int i = kCornerTile * ti + wib;
+    Acc acc[kCornerTile];
+#pragma unroll
+    for (int jj = 0; jj < kCornerTile; ++jj) acc[jj] = acc_init(dd_make(0.0f, 0.0f));
+    if (i < m) {
+      const float2* zi = a.Zd + static_cast<int64_t>(i) * a.nband;
+      const float2* zj = a.Zc + static_cast<int64_t>(kCornerTile * tj) * a.nband;
+      for (int c = lane; c < a.nband; c += 32) {
+        const dd x = f2dd(zi[c]);
+#pragma unroll
+        for (int jj = 0; jj < kCornerTile; ++jj)
+          if (kCornerTile * tj + jj < m) acc_madd(acc[jj], x, f2dd(zj[static_cast<int64_t>(jj) * a.nband + c]));
+      }
+    }
+#pragma unroll
+    for (int jj = 0; jj < kCornerTile; ++jj) red[wib][jj][lane] = dd2f(acc_get(acc[jj]));
+    __syncwarp();
+    if (lane < kCornerTile) {
+      const int j = kCornerTile * tj + lane;
+      if (i < m && j <= i) {
+        Acc t = acc_init(f2dd(a.Cn[static_cast<int64_t>(i) * m + j]));
+        for (int l = 0; l < 32; ++l) acc_add(t, dd_neg(f2dd(red[wib][lane][l])));
+        a.Cn[static_cast<int64_t>(i) * m + j] = dd2f(acc_get(t));
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// One CTA: LDL^T of the corner (PSD-aware pivots), then x_C.
+__global__ void __launch_bounds__(kBT) k_band_corner_solve(BandArgs a, Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  extern __shared__ __align__(16) float2 cm[];  // nbd x nbd (lower), then y (nbd)
+  __shared__ float2 sdv, srdv;
+  __shared__ float smax;
+  __shared__ int sbad;
+  const int m = a.nbd;
+  const int tid = threadIdx.x;
+  if (m == 0) return;
+  float2* y = cm + m * m;
+  const int64_t ld = m + 1;
+  for (int e = tid; e < m * m; e += kBT) {
+    const int i = e / m, j = e % m;
+    cm[e] = (j <= i) ? a.Cn[i * ld + j] : make_float2(0.0f, 0.0f);
+  }
+  for (int j = tid; j < m; j += kBT) y[j] = a.Cn[static_cast<int64_t>(m) * ld + j];
+  if (tid == 0) sbad = 0;
+  __syncthreads();
+  for (int t = 0; t < m; ++t) {
+    if (tid == 0) {
+      dd dt = f2dd(cm[t * m + t]);
+      if ((a.nband + t) % 6 == 0) smax = 1.0f;
+      const float tol = fmaxf(smax, 1.0f) * kTolRel;
+      if (!isfinite(dt.hi)) {
+        sbad = 1;
+        dt = dd_make(0.0f, 0.0f);
+      } else if (fabsf(dt.hi) <= tol) {
+        dt = dd_make(0.0f, 0.0f);
+      } else {
+        smax = fmaxf(smax, fabsf(dt.hi));
+      }
+      sdv = dd2f(dt);
+      srdv = dd2f(dt.hi == 0.0f ? dd_make(0.0f, 0.0f) : dd_rcp(dt));
+      a.dpiv[a.nband + t] = sdv;
+      a.rdpiv[a.nband + t] = srdv;
+    }
+    __syncthreads();
+    const dd rd = f2dd(srdv);
+    const int rem = m - t - 1;
+    for (int e = tid; e < rem * (rem + 1) / 2; e += kBT) {
+      int ii = static_cast<int>((__fsqrt_rn(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
+      while (ii * (ii + 1) / 2 > e) --ii;
+      while ((ii + 1) * (ii + 2) / 2 <= e) ++ii;
+      const int i = t + 1 + ii, k = t + 1 + (e - ii * (ii + 1) / 2);
+      const dd li = dd_mul(f2dd(cm[i * m + t]), rd);
+      Acc acc = acc_init(f2dd(cm[i * m + k]));
+      acc_madd(acc, dd_neg(li), f2dd(cm[k * m + t]));
+      cm[i * m + k] = dd2f(acc_get(acc));
+    }
+    __syncthreads();
+    for (int i = t + 1 + tid; i < m; i += kBT) cm[i * m + t] = dd2f(dd_mul(f2dd(cm[i * m + t]), rd));
+    __syncthreads();
+  }
+  // L_E D_E L_E^T x = y: forward, diagonal, backward (one warp per step)
+  __shared__ float2 red[32];
+  const int lane = tid & 31;
+  for (int i = 0; i < m; ++i) {
+    if (tid < 32) {
+      Acc acc = acc_init(dd_make(0.0f, 0.0f));
+      for (int k = lane; k < i; k += 32) acc_madd(acc, f2dd(cm[i * m + k]), f2dd(y[k]));
+      red[lane] = dd2f(acc_get(acc));
+      __syncwarp();
+      if (lane == 0) {
+        Acc t = acc_init(f2dd(y[i]));
+        for (int l = 0; l < 32; ++l) acc_add(t, dd_neg(f2dd(red[l])));
+        y[i] = dd2f(acc_get(t));
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < m; i += kBT) y[i] = dd2f(dd_mul(f2dd(y[i]), f2dd(a.rdpiv[a.nband + i])));
+  __syncthreads();
+  for (int i = m - 1; i >= 0; --i) {
+    if (tid < 32) {
+      Acc acc = acc_init(dd_make(0.0f, 0.0f));
+      for (int k = i + 1 + lane; k < m; k += 32) acc_madd(acc, f2dd(cm[k * m + i]), f2dd(y[k]));
+      red[lane] = dd2f(acc_get(acc));
+      __syncwarp();
+      if (lane == 0) {
+        Acc t = acc_init(f2dd(y[i]));
+        for (int l = 0; l < 32; ++l) acc_add(t, dd_neg(f2dd(red[l])));
+        y[i] = dd2f(acc_get(t));
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < m; i += kBT) a.xw[a.nband + i] = y[i];
+  if (tid == 0 && sbad) ctrl->skip = 2;
+}
+
+// t_c = Zd_{rhs,c} - sum_i Zd_ic x_Ci for the band columns.
+__global__ void __launch_bounds__(256) k_band_tvec(BandArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.nband; c += gridDim.x * blockDim.x) {
+    Acc acc = acc_init(f2dd(a.Zd[static_cast<int64_t>(a.nbd) * a.nband + c]));
+    for (int i = 0; i < a.nbd; ++i)
+      acc_madd(acc, dd_neg(f2dd(a.Zd[static_cast<int64_t>(i) * a.nband + c])), f2dd(a.xw[a.nband + i]));
+    a.xw[c] = dd2f(acc_get(acc));
+  }
+}
+
+// One CTA: x_A = L_A^-T t (panels from the last), unscale, write the step.
+__global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  extern __shared__ __align__(16) float2 sw[];
+  const int W = a.W, span = W - 1;
+  float2* xv = sw;
+  float2* blk = xv + ((a.nband + 1) & ~1);  // 2 x span x kBP: rows below the panel, the panel's columns
+  float2* xb = blk + 2 * kBP * W;           // 2 x kBP x kBP
+  __shared__ float2 part[kBP][kFwdSeg];
+  __shared__ float2 u[kBP];
+  const int tid = threadIdx.x;
+  auto stage = [&](int p) {
+    const int c0 = kBP * p, w = min(kBP, a.nband - c0), c1 = c0 + w, buf = p & 1;
+    const int nr = min(span, a.nband - c1);
+    for (int e = tid; e < nr * kBP; e += kBT) {
+      const int q = e / kBP, k = e % kBP;
+      const int r = c1 + q;
+      const int sl = c0 + k - r + W - 1;
+      float2* dst = blk + (buf * span + q) * kBP + k;
+      if (k < w && sl >= 0) cp_async8(dst, a.Lb + static_cast<int64_t>(r) * W + sl);
+      else *dst = make_float2(0.0f, 0.0f);
+    }
+    for (int e = tid; e < kBP * kBP / 2; e += kBT)
+      cp_async16(xb + buf * kBP * kBP + 2 * e, a.Xinv + static_cast<int64_t>(p) * kBP * kBP + 2 * e);
+    cp_async_commit();
+  };
+  for (int c = tid; c < a.nband; c += kBT) xv[c] = a.xw[c];
+  stage(a.npan - 1);
+  const int seg = (span + kFwdSeg - 1) / kFwdSeg;
+  for (int p = a.npan - 1; p >= 0; --p) {
+    const int c0 = kBP * p;
+    const int w = min(kBP, a.nband - c0);
+    const int c1 = c0 + w;
+    const int buf = p & 1;
+    if (p > 0) stage(p - 1);
+    else cp_async_commit();
+    cp_async_wait_but_one();
+    __syncthreads();
+    if (tid < kBP * kFwdSeg) {
+      const int cl = tid / kFwdSeg, sgi = tid % kFwdSeg;
+      Acc acc = acc_init(dd_make(0.0f, 0.0f));
+      if (cl < w) {
+        const int c = c0 + cl;
+        // rows r in [c1, min(c + W, nband)), split over the fixed window [c1, c1 + span)
+        const int rlo = c1 + sgi * seg;
+        const int rhi = min(min(c + W, a.nband), c1 + (sgi + 1) * seg);
+        for (int r = rlo; r < rhi; ++r)
+          acc_madd(acc, f2dd(blk[(buf * span + (r - c1)) * kBP + cl]), f2dd(xv[r]));
+      }
+      part[cl][sgi] = dd2f(acc_get(acc));
+    }
+    __syncthreads();
+    if (tid < w) {
+      Acc acc = acc_init(f2dd(xv[c0 + tid]));
+      for (int q = 0; q < kFwdSeg; ++q) acc_add(acc, dd_neg(f2dd(part[tid][q])));
+      u[tid] = dd2f(acc_get(acc));
+    }
+    __syncthreads();
+    if (tid < w) {
+      // x_{c0+k} = sum_{i >= k} X_ik u_i
+      const float2* x2 = xb + buf * kBP * kBP;
+      Acc acc = acc_init(dd_make(0.0f, 0.0f));
+      for (int i = tid; i < w; ++i) acc_madd(acc, f2dd(x2[i * kBP + tid]), f2dd(u[i]));
+      xv[c0 + tid] = dd2f(acc_get(acc));
+    }
+    __syncthreads();
+  }
+  cp_async_wait_all();
+  for (int r = tid; r < a.n; r += kBT) {
+    const dd v = (r < a.nband) ? f2dd(xv[r]) : f2dd(a.xw[r]);
+    const dd xs = dd_mul(v, dd_make(a.scl[r], 0.0f));
+    a.x[r] = dd_to_double(xs);
+    a.xdd[2 * r] = xs.hi;
+    a.xdd[2 * r + 1] = xs.lo;
+  }
+}
+
+BandArgs band_args(const Sizes& s, const Dev& d) {
+  BandArgs a;
+  a.n = s.n6;
+  a.nband = s.band_rows;
+  a.W = s.band_w;
+  a.npan = (s.band_rows + kBP - 1) / kBP;
+  a.nbd = s.n6 - s.band_rows;
+  a.ring = s.band_ring;
+  a.S = d.S;
+  a.b = d.rb;
+  a.scl = d.band_scl;
+  a.Lb = d.band_L;
+  a.Xinv = d.band_Xinv;
+  a.dpiv = d.band_d;
+  a.rdpiv = d.band_rd;
+  a.Pbuf = d.band_P;
+  a.Zc = d.band_Z;
+  a.Zd = d.band_Zd;
+  a.Cn = d.band_E;
+  a.xw = d.band_xw;
+  a.x = d.x;
+  a.xdd = d.xdd;
+  return a;
+}
+
+int band_ring(int W, int C) {
+  const int need = (W + 3 * kBP + C - 1) / C + 1;
+  int ring = 1;
+  while (ring < need) ring <<= 1;
+  return ring;
+}
+
+size_t factor_dyn_smem(int W, int C) {
+  const int ring = band_ring(W, C);
+  return sizeof(float2) * (static_cast<size_t>(ring) * W + static_cast<size_t>(ring) * kBP +
+                           static_cast<size_t>(W - 1) * (kBP + 1));
+}
+
+size_t band_sweep_smem(int nband, int W) { return sizeof(float2) * sweep_smem_floats2(nband, W); }
+
+}  // namespace
+
+int band_shape(int nf, const std::vector<int32_t>& sb_row, const std::vector<int32_t>& sb_col, int* band_rows,
+               int* band_w) {
+  *band_rows = 0;
+  *band_w = 0;
+  if (nf < 8) return 0;
+  std::vector<int32_t> first(nf);
+  for (int i = 0; i < nf; ++i) first[i] = i;
+  for (size_t q = 0; q < sb_row.size(); ++q) {
+    const int r = sb_row[q], c = sb_col[q];
+    if (r >= 0 && r < nf && c >= 0 && c <= r) first[r] = std::min(first[r], c);
+  }
+  std::vector<int32_t> prefw(nf);
+  int run = 0;
+  for (int i = 0; i < nf; ++i) {
+    run = std::max(run, i - first[i] + 1);
+    prefw[i] = run;
+  }
+  double best = -1.0;
+  int best_rb = 0, best_wb = 0;
+  for (int nbdb = 0; nbdb <= kMaxBorderBlocks && nbdb <= nf - 8; ++nbdb) {
+    const int rb = nf - nbdb;
+    const int wb = prefw[rb - 1];
+    if (wb > kMaxWBlocks) continue;
+    const double cost = static_cast<double>(rb) * wb * wb + 2.0 * nbdb * rb * wb + static_cast<double>(nbdb) * nbdb * rb;
+    if (best < 0.0 || cost < best) {
+      best = cost;
+      best_rb = rb;
+      best_wb = wb;
+    }
+  }
+  if (best < 0.0) return 0;
+  // worth it only where the band is much narrower than the system
+  if (4 * best_wb > nf) return 0;
+  *band_rows = 6 * best_rb;
+  *band_w = 6 * best_wb;
+  return 1;
+}
+
+int band_setup(int n, int nband, int W, int* cluster, int* ring) {
+  *cluster = 0;
+  *ring = 0;
+  if (nband <= 0 || W < 6 || W > kMaxW || n - nband > kMaxBorder) return 0;
+  const size_t sweep = band_sweep_smem(nband, W);
+  if (sweep > kSmemLimit - 4096) return 0;
+  const int m = n - nband;
+  const size_t corner = sizeof(float2) * static_cast<size_t>(m) * (m + 1);
+  if (corner > kSmemLimit - 4096) return 0;
+  const size_t fmax = factor_dyn_smem(W, 8);  // the larger of the two cluster sizes tried
+  if (cudaFuncSetAttribute(k_band_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sweep)) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_band_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sweep)) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_band_corner_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(std::max<size_t>(corner, 16))) != cudaSuccess ||
+      cudaFuncSetAttribute(k_band_factor<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(fmax)) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(k_band_factor<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(fmax)) !=
+          cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const int sizes[2] = {16, 8};
+  for (int ci = 0; ci < 2; ++ci) {
+    const int C = sizes[ci];
+    if (C > 8 && cudaFuncSetAttribute(k_band_factor<16>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                     cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(kBT);
+    cfg.dynamicSmemBytes = factor_dyn_smem(W, C);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    const cudaError_t oe = (C == 16) ? cudaOccupancyMaxActiveClusters(&nclusters, k_band_factor<16>, &cfg)
+                                     : cudaOccupancyMaxActiveClusters(&nclusters, k_band_factor<8>, &cfg);
+    if (oe != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    if (nclusters < 1) continue;
+    *cluster = C;
+    *ring = band_ring(W, C);
+    return C;
+  }
+  return 0;
+}
+
+int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
+  const BandArgs a = band_args(s, d);
+  int launches = 0;
+  k_band_scale<<<(a.n + 255) / 256, 256, 0, st>>>(a, d.ctrl);
+  ++launches;
+  {
+    const int64_t total = static_cast<int64_t>(a.nband) * a.W + static_cast<int64_t>(a.nbd + 1) * a.nband +
+                          static_cast<int64_t>(a.nbd + 1) * (a.nbd + 1);
+    int blocks = static_cast<int>(std::min<int64_t>((total + 255) / 256, 4096));
+    k_band_load<<<std::max(blocks, 1), 256, 0, st>>>(a, d.ctrl);
+    ++launches;
+  }
+  {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(s.band_c);
+    cfg.blockDim = dim3(kBT);
+    cfg.dynamicSmemBytes = factor_dyn_smem(a.W, s.band_c);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = s.band_c;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    if (s.band_c == 16) cudaLaunchKernelEx(&cfg, k_band_factor<16>, a, d.ctrl);
+    else cudaLaunchKernelEx(&cfg, k_band_factor<8>, a, d.ctrl);
+    ++launches;
+  }
+  k_band_fwd<<<a.nbd + 1, kBT, band_sweep_smem(a.nband, a.W), st>>>(a, d.ctrl);
+  ++launches;
+  {
+    const int64_t nt = (a.nbd + 1 + kCornerTile - 1) / kCornerTile;
+    const int blocks = static_cast<int>(std::min<int64_t>(nt * (nt + 1) / 2, 8192));
+    k_band_corner<<<std::max(blocks, 1), 128, 0, st>>>(a, d.ctrl);
+    ++launches;
+  }
+  {
+    const size_t corner = sizeof(float2) * static_cast<size_t>(a.nbd) * (a.nbd + 1);
+    k_band_corner_solve<<<1, kBT, std::max<size_t>(corner, 16), st>>>(a, d.ctrl);
+    ++launches;
+  }
+  k_band_tvec<<<std::max((a.nband + 255) / 256, 1), 256, 0, st>>>(a, d.ctrl);
+  ++launches;
+  k_band_bwd<<<1, kBT, band_sweep_smem(a.nband, a.W), st>>>(a, d.ctrl);
+  ++launches;
+  return launches;
+}
+
+int band_launch_count() { return 8; }
+
+}  // namespace sgba

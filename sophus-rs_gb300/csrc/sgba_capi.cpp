@@ -488,9 +488,39 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
     if ((st = dev_alloc(p, &d.S2, n6 * n6))) return st;
     SGBA_CK(cudaMemset(d.S2, 0, sizeof(float2) * std::max<size_t>(n6 * n6, 1)));
   }
-  if ((st = dev_alloc(p, &d.A, n6 * n6))) return st;
-  if ((st = dev_alloc(p, &d.dpiv, n6))) return st;
-  if ((st = dev_alloc(p, &d.wpanel, n6 * 48))) return st;
+  s.band_rows = s.band_w = s.band_c = s.band_ring = 0;
+  if (s.dense_c == 0) {
+    // banded reduced system (sequential / loop problems): band + dense border solver
+    int rows = 0, w = 0, c = 0, ring = 0;
+    if (sgba::band_shape(P.nf, P.sb_row, P.sb_col, &rows, &w) && sgba::band_setup(s.n6, rows, w, &c, &ring) > 0) {
+      s.band_rows = rows;
+      s.band_w = w;
+      s.band_c = c;
+      s.band_ring = ring;
+      const size_t nbd1 = n6 - static_cast<size_t>(rows) + 1;
+      const size_t npan = (static_cast<size_t>(rows) + 23) / 24;
+      if ((st = dev_alloc(p, &d.band_scl, n6))) return st;
+      if ((st = dev_alloc(p, &d.band_L, static_cast<size_t>(rows) * w))) return st;
+      if ((st = dev_alloc(p, &d.band_Xinv, npan * 24 * 24))) return st;
+      if ((st = dev_alloc(p, &d.band_d, n6))) return st;
+      if ((st = dev_alloc(p, &d.band_rd, n6))) return st;
+      if ((st = dev_alloc(p, &d.band_P, static_cast<size_t>(w) * 24))) return st;
+      if ((st = dev_alloc(p, &d.band_Z, nbd1 * rows))) return st;
+      if ((st = dev_alloc(p, &d.band_Zd, nbd1 * rows))) return st;
+      if ((st = dev_alloc(p, &d.band_E, nbd1 * nbd1))) return st;
+      if ((st = dev_alloc(p, &d.band_xw, n6))) return st;
+    }
+  }
+  // point blocks keep the FP32 Cholesky while no pivot loses more than three
+  // digits; the others are redone in float-float by a 64-CTA pass
+  s.lmk_well_tol = 1e-3f;
+  s.lmk_list_grid = 64;
+  if (s.dense_c == 0 && s.band_c == 0) {
+    // multi-launch dense solver
+    if ((st = dev_alloc(p, &d.A, n6 * n6))) return st;
+    if ((st = dev_alloc(p, &d.dpiv, n6))) return st;
+    if ((st = dev_alloc(p, &d.wpanel, n6 * 48))) return st;
+  }
   if ((st = dev_alloc(p, &d.x, n6))) return st;
   if ((st = dev_alloc(p, &d.xdd, 2 * n6))) return st;
   if ((st = dev_alloc(p, &d.r, n6))) return st;
@@ -780,6 +810,11 @@ int sgba_get_layout(sgba_problem* p, sgba_layout* out) {
   int64_t np = 0;
   if (!p->plan.sb_pair_begin.empty()) np = p->plan.sb_pair_begin.back();
   out->n_schur_pairs = np;
+  out->solver = p->sz.dense_c > 0 ? SGBA_SOLVER_DENSE_CLUSTER
+                                  : (p->sz.band_c > 0 ? SGBA_SOLVER_BAND : SGBA_SOLVER_DENSE_PANELS);
+  out->band_width = p->sz.band_c > 0 ? p->sz.band_w : 0;
+  out->border_rows = p->sz.band_c > 0 ? p->sz.n6 - p->sz.band_rows : 0;
+  out->reserved = 0;
   return SGBA_OK;
 }
 

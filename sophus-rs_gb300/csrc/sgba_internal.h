@@ -129,6 +129,17 @@ struct Dev {
   double* tile_part = nullptr;     // ntiles*33 partial sums
   double* S = nullptr;             // n6*n6 FP64 (lower valid)
   float2* S2 = nullptr;            // n6*n6 float-float copy of S (cluster solver only)
+  // banded solver (sgba_band.cu): band of the scaled S and its factor, border rows, corner
+  float* band_scl = nullptr;       // n6: D^-1/2
+  float2* band_L = nullptr;        // band_rows x band_w
+  float2* band_Xinv = nullptr;     // panels x 24 x 24
+  float2* band_d = nullptr;        // n6 pivots
+  float2* band_rd = nullptr;       // n6 reciprocal pivots
+  float2* band_P = nullptr;        // band_w x 24 panel exchange
+  float2* band_Z = nullptr;        // (border + 1) x band_rows
+  float2* band_Zd = nullptr;       // (border + 1) x band_rows
+  float2* band_E = nullptr;        // (border + 1)^2
+  float2* band_xw = nullptr;       // n6
   float* A = nullptr;              // n6*n6 FP32 factor (lower: unit L)
   float* dpiv = nullptr;           // n6 pivots
   float* wpanel = nullptr;         // n6*64 panel scratch (A_ip L^-T)
@@ -155,6 +166,12 @@ struct Sizes {
   double gauge_center[3];
   int dense_c;        // cluster size of the single-launch dense solver, 0 = multi-launch path
   size_t dense_smem;  // its dynamic shared memory per CTA
+  int band_rows;      // banded solver: rows of the band part (0 = not used)
+  int band_w;         // its band width
+  int band_c;         // its cluster size
+  int band_ring;      // its row slots per CTA
+  float lmk_well_tol;  // point blocks: FP32 Cholesky kept while every pivot keeps this fraction
+  int lmk_list_grid;   // CTAs of the float-float redo of the other points
 };
 
 // ---- launchers (sgba_kernels.cu / sgba_solver.cu) -------------------------
@@ -181,6 +198,15 @@ int solver_launch_count(const Sizes& s);
 int dense_cluster_setup(int n, int* cluster, size_t* smem);
 int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st);
 
+// Banded solver (sgba_band.cu) for reduced systems that are a band plus a few
+// dense border rows (sequential and loop-shaped problems).  band_shape picks
+// the split from the lower block pattern of S (0 = not banded enough);
+// band_setup checks the launch limits and returns the cluster size (0 = no).
+int band_shape(int nf, const std::vector<int32_t>& sb_row, const std::vector<int32_t>& sb_col, int* band_rows,
+               int* band_w);
+int band_setup(int n, int nband, int w, int* cluster, int* ring);
+int launch_band(const Sizes& s, const Dev& d, cudaStream_t st);
+int band_launch_count();
 // Schur observation-pair lists on the device (sgba_plan.cu): pairs per lower
 // block (atomic counts into totals[nf(nf+1)/2]); then the pair list d.pairs in
 // (block, point) order from the block map, block offsets and a zeroed

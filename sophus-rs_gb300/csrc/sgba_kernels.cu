@@ -383,6 +383,10 @@ struct LinArgs {
   int32_t nchunk;
   int32_t* slow_list;        // ill-conditioned points found by the chunked pass
   int32_t* slow_count;
+  // FP32 Cholesky of a point block is kept while each pivot keeps more than
+  // this fraction of its diagonal entry; otherwise the block is rebuilt in
+  // float-float
+  float well_tol;
   // list mode of k_landmark: only the listed points, float-float path forced
   const int32_t* list;
   const int32_t* list_count;
@@ -463,7 +467,7 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
     float c11 = sqrtf(t11);
     float c21 = (V[4] - c20 * c10) / c11;
     float t22 = V[5] - c20 * c20 - c21 * c21;
-    const bool well = !a.list && V[0] > 0.f && t11 > 1e-3f * V[3] && t22 > 1e-3f * V[5];
+    const bool well = !a.list && V[0] > 0.f && t11 > a.well_tol * V[3] && t22 > a.well_tol * V[5];
     const dd pxd = dd_from_double(a.points[3 * i + 0]);
     const dd pyd = dd_from_double(a.points[3 * i + 1]);
     const dd pzd = dd_from_double(a.points[3 * i + 2]);
@@ -704,7 +708,7 @@ __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) 
       const float c11 = sqrtf(t11);
       const float c21 = (V[4] - c20 * c10) / c11;
       const float t22 = V[5] - c20 * c20 - c21 * c21;
-      const bool well = V[0] > 0.f && t11 > 1e-3f * V[3] && t22 > 1e-3f * V[5];
+      const bool well = V[0] > 0.f && t11 > a.well_tol * V[3] && t22 > a.well_tol * V[5];
       if (!well) {
         a.slow_list[atomicAdd(a.slow_count, 1)] = i;
         continue;
@@ -1528,7 +1532,7 @@ static int launch_landmark(const Sizes& s, const Dev& d, LinArgs la, cudaStream_
     LinArgs lb = la;
     lb.list = d.slow_list;
     lb.list_count = d.slow_count;
-    k_landmark<<<64, 256, 0, st>>>(lb, d.ctrl);
+    k_landmark<<<s.lmk_list_grid, 256, 0, st>>>(lb, d.ctrl);
     return 2;
   }
   k_landmark<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(la, d.ctrl);
@@ -1550,6 +1554,7 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
   k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses, d.pose_f, d.pose_dd, d.ctrl, 0);
   ++n;
   LinArgs la;
+  la.well_tol = s.lmk_well_tol;
   la.np = s.np;
   la.pt_g_begin = d.pt_g_begin;
   la.g_begin = d.g_begin;
@@ -1695,6 +1700,7 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) 
       return launch_schur(s, d, st);
     case 2: {
       LinArgs la;
+      la.well_tol = s.lmk_well_tol;
       la.np = s.np;
       la.pt_g_begin = d.pt_g_begin;
       la.g_begin = d.g_begin;

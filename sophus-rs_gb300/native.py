@@ -31,6 +31,11 @@ TERM_PARAMETER_TOLERANCE = 3
 TERM_MAX_ITERATIONS = 4
 TERM_MAX_CONSECUTIVE_REJECTS = 5
 
+# sgba_layout.solver
+SOLVER_DENSE_CLUSTER = 0
+SOLVER_BAND = 1
+SOLVER_DENSE_PANELS = 2
+
 
 class ProblemDesc(C.Structure):
     _fields_ = [
@@ -82,6 +87,10 @@ class Layout(C.Structure):
         ("n_h_blocks", C.c_int64),
         ("n_s_blocks", C.c_int64),
         ("n_schur_pairs", C.c_int64),
+        ("solver", C.c_int32),
+        ("band_width", C.c_int32),
+        ("border_rows", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
