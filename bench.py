@@ -36,6 +36,21 @@ N_ITER_WORKLOAD = 20
 WORKLOAD = ("sphere BA: 100 SE(3) cams (99 free) on a r=6 m Fibonacci sphere, 20000 points in [-2,2]^3, "
             "each seen by U{10..40} of its visible cams (~499k obs), pinhole 500/500/320/240, Huber 1 px, "
             "nu0=1e-4, Schur LM with dense FP32-factor + f64-refined reduced camera system")
+# Other workloads (parity-test configurations, measured with --workload):
+#   loop    1500 cameras on a r=50 m loop, 300,000 points on a r=60 m cylinder, consecutive-camera
+#           tracks of Geom(0.12) clipped to [3, 25] (~2.5M obs), 15 LM iterations; banded solver and
+#           float-float linearization
+#   windows 1024 independent local windows (cameras U{5..40}, points U{200..4000}), 10 LM iterations
+#           each, optimised concurrently by sgba_batch_optimize
+WORKLOADS = {
+    "sphere": dict(kind="SPHERE", n_cam=0, n_pt=0, seed=SEED, n_iter=N_ITER_WORKLOAD, desc=WORKLOAD),
+    "loop": dict(kind="LOOP", n_cam=1500, n_pt=300000, seed=20261203 + 2, n_iter=15,
+                 desc=("loop BA: 1500 SE(3) cams on a r=50 m loop facing outward, 300000 points on a r=60 m "
+                       "cylinder, consecutive-camera tracks Geom(0.12) clipped to [3,25] (~2.5M obs), Huber 1 px, "
+                       "nu0=1e-4; banded float-float LDL^T of the reduced camera system, float-float linearization")),
+}
+N_WINDOWS = 1024
+WINDOW_ITERS = 10
 
 
 def _dist():
@@ -157,9 +172,16 @@ def _kernel_bytes(name, lay, prob):
     if name == "backsub":
         return 72 * nz + (48 + 24 + 24) * lay.n_marg_points + 48 * nf
     if name == "factor":
+        n6 = 6 * nf
+        if getattr(lay, "solver", 0) == 1:
+            # banded solver: the band of S read once in f64 (row r: columns r-W+1..r) and the border rows;
+            # the float-float band written (scaled S), read and written back once by the factor, read by the
+            # two sweeps; border rows and the rhs (nbd + 1 rows of the band width) in and out in float-float
+            nb = n6 - lay.border_rows
+            w = lay.band_width
+            return 8 * nb * w + 8 * lay.border_rows * n6 + 8 * nb * w * 5 + 16 * (lay.border_rows + 1) * nb * 2
         # single-launch cluster solver: read S once as float-float (8 B per entry) and the
         # reduced rhs (f64); write the step as f64 and as float-float pairs
-        n6 = 6 * nf
         return 8 * n6 * n6 + 8 * n6 + 16 * n6
     return None
 
@@ -173,7 +195,9 @@ def run_gpu(args, ws, rank, local):
         graft.build_native()
     pkg = graft.load_package()
     native = pkg.native
-    prob = pkg.synth.generate(pkg.synth.SPHERE, seed=SEED + rank)
+    wl = WORKLOADS[args.workload]
+    prob = pkg.synth.generate(getattr(pkg.synth, wl["kind"]), n_cam=wl["n_cam"], n_pt=wl["n_pt"],
+                              seed=wl["seed"] + rank)
     K, W = args.steps, args.warmup
     params = pkg.OptParams(num_iterations=W + K + 1000, initial_lm_damping=prob.initial_lm_damping,
                            function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
@@ -222,7 +246,7 @@ def run_gpu(args, ws, rank, local):
         pinned = True
     except Exception:
         pinned = False
-    e2e_params = pkg.OptParams(num_iterations=N_ITER_WORKLOAD, initial_lm_damping=prob.initial_lm_damping,
+    e2e_params = pkg.OptParams(num_iterations=wl["n_iter"], initial_lm_damping=prob.initial_lm_damping,
                                function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
                                max_consecutive_rejects=1 << 40, solver=pkg.LinearSolverEnum.SchurBlockSparseLdlt)
     # one untimed warm-up of the path (context, module load)
@@ -244,6 +268,64 @@ def run_gpu(args, ws, rank, local):
     return out
 
 
+def run_windows(args, ws, rank, local):
+    """Config: N_WINDOWS independent windows, WINDOW_ITERS LM iterations each, one
+    sgba_batch_optimize call per step (all windows concurrently)."""
+    import numpy as np
+
+    import __graft_entry__ as graft
+
+    if not os.path.exists(os.path.join(graft.PKG_DIR, "libsgba.so")):
+        graft.build_native()
+    pkg = graft.load_package()
+    native = pkg.native
+    base = pkg.synth.BASE_SEED + 3 + rank * N_WINDOWS
+    wins = [pkg.synth.generate(pkg.synth.WINDOW, seed=base + w) for w in range(N_WINDOWS)]
+    params = pkg.OptParams(num_iterations=WINDOW_ITERS, initial_lm_damping=wins[0].initial_lm_damping,
+                           function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
+                           max_consecutive_rejects=1 << 40, solver=pkg.LinearSolverEnum.SchurBlockSparseLdlt)
+    K, W = args.steps, args.warmup
+    probs = [native.Problem(w, device=local) for w in wins]
+    try:
+        for _ in range(W):
+            native.batch_optimize(probs, params)
+        _barrier(ws)
+        clocks = ClockSampler(local)
+        clocks.start()
+        t0 = time.perf_counter()
+        ms = []
+        for _ in range(K):
+            out = native.batch_optimize(probs, params)
+            for (recs, term, wms, fc, st) in out:
+                if st != native.OK:
+                    raise RuntimeError("window failed with status %d: %s" % (st, native.last_error()))
+                ms.append(wms)
+        dt = _barrier_and_max(time.perf_counter() - t0, ws)
+        clk = clocks.stop()
+    finally:
+        for p in probs:
+            p.close()
+    # end to end: create (upload) + batch + read back, from host arrays
+    t0 = time.perf_counter()
+    for _ in range(max(1, min(3, K))):
+        ps = [native.Problem(w, device=local) for w in wins]
+        try:
+            native.batch_optimize(ps, params)
+            res = [p.variables() for p in ps]
+        finally:
+            for p in ps:
+                p.close()
+    e2e_steps = max(1, min(3, K))
+    e2e_s = _barrier_and_max(time.perf_counter() - t0, ws)
+    h2d = sum(w.poses.nbytes + w.points.nbytes + w.obs_cam.nbytes + w.obs_pt.nbytes + w.obs_uv.nbytes
+              + w.pose_const.nbytes for w in wins)
+    d2h = sum(a.nbytes + b.nbytes for a, b in res)
+    ms = np.array(ms)
+    return dict(value=N_WINDOWS * K * ws / dt, dt=dt, p50=float(np.percentile(ms, 50)),
+                p99=float(np.percentile(ms, 99)), clk=clk, e2e=N_WINDOWS * e2e_steps * ws / e2e_s, h2d=h2d, d2h=d2h,
+                n_obs=int(sum(w.n_obs for w in wins)), wins=wins, params=params, pkg=pkg)
+
+
 def cpu_baseline(prob, pkg, n_iter, threads):
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import oracle_bindings as ob  # the oracle: CPU restatement of the reference
@@ -260,6 +342,26 @@ def cpu_baseline(prob, pkg, n_iter, threads):
     return len(recs) / dt, dt
 
 
+def cpu_windows(wins, pkg, threads):
+    """The oracle on a sample of windows, windows spread over the host threads."""
+    import concurrent.futures
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_bindings as ob  # the oracle: CPU restatement of the reference
+
+    import __graft_entry__ as graft
+
+    graft.build_oracle()
+    params = pkg.OptParams(num_iterations=WINDOW_ITERS, initial_lm_damping=wins[0].initial_lm_damping,
+                           function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
+                           max_consecutive_rejects=1 << 40)
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda w: ob.optimize(w, params, n_threads=1), wins))
+    dt = time.perf_counter() - t0
+    return len(wins) / dt, dt
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -267,6 +369,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="sphere", choices=["sphere", "loop", "windows"],
+                    help="sphere: the headline configuration; loop / windows: the 1500-camera loop and the "
+                         "batched local windows")
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling mode: only set up the workload and run this many LM iterations")
     args = ap.parse_args()
@@ -274,7 +379,8 @@ def main():
         import __graft_entry__ as graft
 
         pkg = graft.load_package()
-        prob = pkg.synth.generate(pkg.synth.SPHERE, seed=SEED)
+        wl = WORKLOADS["loop" if args.workload == "loop" else "sphere"]
+        prob = pkg.synth.generate(getattr(pkg.synth, wl["kind"]), n_cam=wl["n_cam"], n_pt=wl["n_pt"], seed=wl["seed"])
         params = pkg.OptParams(num_iterations=args.profile_iters, initial_lm_damping=prob.initial_lm_damping,
                                function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
                                max_consecutive_rejects=1 << 40, solver=pkg.LinearSolverEnum.SchurBlockSparseLdlt)
@@ -297,7 +403,22 @@ def main():
         if not os.path.exists(os.path.join(graft.PKG_DIR, "libsgba.so")):
             graft.build_native()
         pkg = graft.load_package()
-        prob = pkg.synth.generate(pkg.synth.SPHERE, seed=SEED)
+        if args.workload == "windows":
+            wins = [pkg.synth.generate(pkg.synth.WINDOW, seed=pkg.synth.BASE_SEED + 3 + w) for w in range(16)]
+            threads = os.cpu_count() or 1
+            v, dt = cpu_windows(wins, pkg, threads)
+            line = {"metric": METRIC, "value": v, "unit": "windows/s", "impl": "reference", "n_gpus": args.gpus,
+                    "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / len(wins),
+                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                    "data": "synthetic", "config": {"workload": "windows", "n_windows": len(wins)},
+                    "cpu_baseline": {"value": v, "unit": "windows/s", "cores": threads, "kind": "port",
+                                     "sample": "%d windows, %d LM iterations each, one per thread at a time"
+                                               % (len(wins), WINDOW_ITERS)},
+                    "e2e": {"value": v, "unit": "windows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            print(json.dumps(line))
+            return
+        wl = WORKLOADS[args.workload]
+        prob = pkg.synth.generate(getattr(pkg.synth, wl["kind"]), n_cam=wl["n_cam"], n_pt=wl["n_pt"], seed=wl["seed"])
         threads = os.cpu_count() or 1
         cpu_baseline(prob, pkg, max(1, args.warmup // 5), threads)  # warm caches / page in
         v, dt = cpu_baseline(prob, pkg, args.steps, threads)
@@ -305,11 +426,39 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic",
-                "config": {"workload": WORKLOAD, "n_obs": int(prob.n_obs)},
+                "config": {"workload": wl["desc"], "n_obs": int(prob.n_obs)},
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                  "sample": "%d LM iterations of the workload on %d threads (setup included)"
                                            % (args.steps, threads)},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if args.workload == "windows":
+        out = run_windows(args, ws, rank, local)
+        if rank != 0:
+            return
+        line = {
+            "metric": METRIC, "value": out["value"], "unit": "windows/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * out["dt"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "fp32 (Jacobians/products) + float-float sums + f64 update", "data": "synthetic",
+            "config": {"workload": "%d local windows (cams U{5..40}, points U{200..4000}), %d LM iterations each, "
+                                   "one sgba_batch_optimize per step" % (N_WINDOWS, WINDOW_ITERS),
+                       "n_obs_total": out["n_obs"], "l2": "inputs larger than L2 (all windows resident)"},
+            "window_ms": {"p50": out["p50"], "p99": out["p99"]},
+            "roofline": None,
+            "e2e": {"value": out["e2e"], "unit": "windows/s", "h2d_bytes_per_step": int(out["h2d"]),
+                    "d2h_bytes_per_step": int(out["d2h"]),
+                    "step": "create+upload all windows, batch optimize, read back"},
+            "clocks": out["clk"],
+        }
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            v, dt = cpu_windows(out["wins"][:64], out["pkg"], threads)
+            line["cpu_baseline"] = {"value": v, "unit": "windows/s", "cores": threads, "kind": "port",
+                                    "sample": "64 windows, %d LM iterations each, one per thread at a time (%.1f s)"
+                                              % (WINDOW_ITERS, dt)}
         print(json.dumps(line))
         return
 
@@ -334,14 +483,21 @@ def main():
                 "traffic": traffic.get(rl_kernel)}
     if rl_kernel == "factor":
         n6 = 6 * lay.n_free_poses
-        roofline["note"] = ("latency-bound dependency chain (one cluster of 16 CTAs: %d panel steps + 3 "
-                            "triangular sweeps); FP32 work %.0f MFLOP per launch" % ((n6 + 23) // 24, n6 ** 3 / 3e6))
+        if lay.solver == 1:
+            roofline["note"] = ("latency-bound dependency chain: banded float-float LDL^T in one 16-CTA cluster "
+                                "(%d panel steps of 24 pivots), forward/backward sweeps of the same length"
+                                % ((n6 - lay.border_rows + 23) // 24))
+        else:
+            roofline["note"] = ("latency-bound dependency chain (one cluster of 16 CTAs: %d panel steps + 3 "
+                                "triangular sweeps); FP32 work %.0f MFLOP per launch" % ((n6 + 23) // 24, n6 ** 3 / 3e6))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak" if ws > 1 else "weak",
-        "vs_baseline": None, "dtype": "fp32 (Jacobians/products) + float-float sums + f64 update",
+        "vs_baseline": None,
+        "dtype": ("float-float (Jacobians, products, sums, LDL^T) + f64 update" if lay.float_float_lin
+                  else "fp32 (Jacobians/products) + float-float sums + f64 update"),
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_obs": int(prob.n_obs), "n_terms": int(lay.n_terms),
+        "config": {"workload": WORKLOADS[args.workload]["desc"], "n_obs": int(prob.n_obs), "n_terms": int(lay.n_terms),
                    "n_schur_pairs": int(lay.n_schur_pairs), "l2": "flushed (256 MiB write) before every step",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "jacobian_obs_per_s": value * prob.n_obs,
@@ -349,9 +505,9 @@ def main():
         "phase_ms_per_iteration": out.get("phase_ms"),
         "roofline": roofline,
         "gpu_launches": int(out["launches"]),
-        "e2e": {"value": N_ITER_WORKLOAD * out["e2e_steps"] * ws / out["e2e_s"], "unit": UNIT,
+        "e2e": {"value": WORKLOADS[args.workload]["n_iter"] * out["e2e_steps"] * ws / out["e2e_s"], "unit": UNIT,
                 "h2d_bytes_per_step": int(out["h2d"]), "d2h_bytes_per_step": int(out["d2h"]),
-                "step": "create+upload, optimize (%d LM iterations), read back" % N_ITER_WORKLOAD,
+                "step": "create+upload, optimize (%d LM iterations), read back" % WORKLOADS[args.workload]["n_iter"],
                 "pinned_host": out["pinned"]},
         "clocks": out["clk"],
     }

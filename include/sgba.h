@@ -169,7 +169,7 @@ typedef struct {
   int32_t solver;           /* reduced-system solver: SGBA_SOLVER_* */
   int32_t band_width;       /* banded solver: band width in scalars (row r holds columns r-w+1..r) */
   int32_t border_rows;      /* banded solver: dense border rows at the end (loop closures) */
-  int32_t reserved;
+  int32_t float_float_lin;  /* 1: Jacobians, products and Z in float-float (loop-shaped problems) */
 } sgba_layout;
 /* Reduced camera system solvers (chosen at sgba_problem_create from the size
  * and the block pattern of S). */

@@ -852,8 +852,6 @@ int band_shape(int nf, const std::vector<int32_t>& sb_row, const std::vector<int
     }
   }
   if (best < 0.0) return 0;
-  // worth it only where the band is much narrower than the system
-  if (4 * best_wb > nf) return 0;
   *band_rows = 6 * best_rb;
   *band_w = 6 * best_wb;
   return 1;
@@ -869,16 +867,12 @@ int band_setup(int n, int nband, int W, int* cluster, int* ring) {
   const size_t corner = sizeof(float2) * static_cast<size_t>(m) * (m + 1);
   if (corner > kSmemLimit - 4096) return 0;
   const size_t fmax = factor_dyn_smem(W, 8);  // the larger of the two cluster sizes tried
-  if (cudaFuncSetAttribute(k_band_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sweep)) !=
+  if (raise_dynamic_smem(reinterpret_cast<const void*>(k_band_fwd), sweep) != cudaSuccess ||
+      raise_dynamic_smem(reinterpret_cast<const void*>(k_band_bwd), sweep) != cudaSuccess ||
+      raise_dynamic_smem(reinterpret_cast<const void*>(k_band_corner_solve), std::max<size_t>(corner, 16)) !=
           cudaSuccess ||
-      cudaFuncSetAttribute(k_band_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sweep)) !=
-          cudaSuccess ||
-      cudaFuncSetAttribute(k_band_corner_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           static_cast<int>(std::max<size_t>(corner, 16))) != cudaSuccess ||
-      cudaFuncSetAttribute(k_band_factor<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(fmax)) !=
-          cudaSuccess ||
-      cudaFuncSetAttribute(k_band_factor<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(fmax)) !=
-          cudaSuccess) {
+      raise_dynamic_smem(reinterpret_cast<const void*>(k_band_factor<16>), fmax) != cudaSuccess ||
+      raise_dynamic_smem(reinterpret_cast<const void*>(k_band_factor<8>), fmax) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }

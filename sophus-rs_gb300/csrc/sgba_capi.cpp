@@ -17,6 +17,9 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <utility>
+#include <mutex>
+#include <map>
 #include <string>
 #include <thread>
 #include <vector>
@@ -29,6 +32,24 @@ using sgba::Dev;
 using sgba::Plan;
 using sgba::Record;
 using sgba::Sizes;
+
+namespace sgba {
+
+cudaError_t raise_dynamic_smem(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> granted;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& g = granted[std::make_pair(func, dev)];
+  if (bytes <= g) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes));
+  if (e == cudaSuccess) g = bytes;
+  return e;
+}
+
+}  // namespace sgba
 
 namespace {
 
@@ -484,19 +505,23 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   // single-launch cluster solver when the dense system fits one cluster's
   // distributed shared memory; it reads the float-float copy of S
   sgba::dense_cluster_setup(s.n6, &s.dense_c, &s.dense_smem);
-  if (s.dense_c > 0) {
-    if ((st = dev_alloc(p, &d.S2, n6 * n6))) return st;
-    SGBA_CK(cudaMemset(d.S2, 0, sizeof(float2) * std::max<size_t>(n6 * n6, 1)));
-  }
   s.band_rows = s.band_w = s.band_c = s.band_ring = 0;
-  if (s.dense_c == 0) {
+  int brows = 0, bw = 0;
+  const bool banded = sgba::band_shape(P.nf, P.sb_row, P.sb_col, &brows, &bw) != 0;
+  // loop-shaped: block bandwidth at most half the free poses (float-float
+  // linearization and, even where the dense cluster solver would fit, the
+  // float-float band solver: the FP32 factor with refinement leaves ~2e-6 in
+  // the cost of a 100-camera loop)
+  const bool loop_shaped = banded && 2 * (bw / 6) <= P.nf;
+  if (banded && (s.dense_c == 0 ? 4 * (bw / 6) <= P.nf : loop_shaped)) {
     // banded reduced system (sequential / loop problems): band + dense border solver
-    int rows = 0, w = 0, c = 0, ring = 0;
-    if (sgba::band_shape(P.nf, P.sb_row, P.sb_col, &rows, &w) && sgba::band_setup(s.n6, rows, w, &c, &ring) > 0) {
+    int rows = brows, w = bw, c = 0, ring = 0;
+    if (sgba::band_setup(s.n6, rows, w, &c, &ring) > 0) {
       s.band_rows = rows;
       s.band_w = w;
       s.band_c = c;
       s.band_ring = ring;
+      s.dense_c = 0;
       const size_t nbd1 = n6 - static_cast<size_t>(rows) + 1;
       const size_t npan = (static_cast<size_t>(rows) + 23) / 24;
       if ((st = dev_alloc(p, &d.band_scl, n6))) return st;
@@ -511,10 +536,26 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
       if ((st = dev_alloc(p, &d.band_xw, n6))) return st;
     }
   }
+  if (s.dense_c > 0) {
+    if ((st = dev_alloc(p, &d.S2, n6 * n6))) return st;
+    SGBA_CK(cudaMemset(d.S2, 0, sizeof(float2) * std::max<size_t>(n6 * n6, 1)));
+  }
   // point blocks keep the FP32 Cholesky while no pivot loses more than three
   // digits; the others are redone in float-float by a 64-CTA pass
   s.lmk_well_tol = 1e-3f;
   s.lmk_list_grid = 64;
+  // Loop-shaped problems (block bandwidth of S at most half the free poses)
+  // get the float-float linearization: their reduced systems cancel ~25x in
+  // S = U - sum Z Z^T and their bending modes are weakly constrained, so FP32
+  // Jacobian-side products move the step by percents (measured on 300- and
+  // 1500-camera loops).
+  s.lin_dd = loop_shaped ? 1 : 0;
+  if (s.lin_dd) {
+    if ((st = dev_alloc(p, &d.res_lo, P.no))) return st;
+    if ((st = dev_alloc(p, &d.res_lo_t, P.no))) return st;
+    if ((st = dev_alloc(p, &d.zdd, static_cast<size_t>(sgba::kZddFloats) * static_cast<size_t>(std::max<int64_t>(P.ng, 1)))))
+      return st;
+  }
   if (s.dense_c == 0 && s.band_c == 0) {
     // multi-launch dense solver
     if ((st = dev_alloc(p, &d.A, n6 * n6))) return st;
@@ -814,7 +855,7 @@ int sgba_get_layout(sgba_problem* p, sgba_layout* out) {
                                   : (p->sz.band_c > 0 ? SGBA_SOLVER_BAND : SGBA_SOLVER_DENSE_PANELS);
   out->band_width = p->sz.band_c > 0 ? p->sz.band_w : 0;
   out->border_rows = p->sz.band_c > 0 ? p->sz.n6 - p->sz.band_rows : 0;
-  out->reserved = 0;
+  out->float_float_lin = p->sz.lin_dd;
   return SGBA_OK;
 }
 

@@ -805,8 +805,7 @@ int dense_cluster_setup(int n, int* cluster, size_t* smem) {
     const int C = sizes[ci];
     const size_t bytes = dense_smem_bytes(P, C);
     if (bytes > kSmemLimit - sizeof(RankTab) - sizeof(Carve) - 1024) continue;
-    if (cudaFuncSetAttribute(k_dense_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(bytes)) != cudaSuccess) {
+    if (raise_dynamic_smem(reinterpret_cast<const void*>(k_dense_cluster), bytes) != cudaSuccess) {
       cudaGetLastError();
       continue;
     }

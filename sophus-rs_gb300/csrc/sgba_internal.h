@@ -10,6 +10,9 @@
 
 namespace sgba {
 
+// floats per term of the float-float Z (6x3 as (hi, lo) pairs, padded to float4)
+constexpr int kZddFloats = 40;
+
 // Device-resident LM control block (one per problem).  Written only by the
 // single-CTA control kernels, read by every kernel of an iteration.
 struct Ctrl {
@@ -116,6 +119,9 @@ struct Dev {
   double* points_t = nullptr;
   float2* res = nullptr;           // residual at current state (sorted obs)
   float2* res_t = nullptr;         // residual at trial state
+  float2* res_lo = nullptr;        // low parts of res (float-float linearization)
+  float2* res_lo_t = nullptr;      // low parts of res_t
+  float* zdd = nullptr;            // ng*kZddFloats: Z as float-float pairs (float-float linearization)
   // per iteration
   float* pose_f = nullptr;         // nc*12: R_cw (row-major) + t_cw, float
   float* pose_dd = nullptr;        // nc*24: R_cw + t_cw as (hi,lo) pairs
@@ -170,6 +176,7 @@ struct Sizes {
   int band_w;         // its band width
   int band_c;         // its cluster size
   int band_ring;      // its row slots per CTA
+  int lin_dd;          // float-float linearization (Jacobians, products and Z in float-float)
   float lmk_well_tol;  // point blocks: FP32 Cholesky kept while every pivot keeps this fraction
   int lmk_list_grid;   // CTAs of the float-float redo of the other points
 };
@@ -198,10 +205,18 @@ int solver_launch_count(const Sizes& s);
 int dense_cluster_setup(int n, int* cluster, size_t* smem);
 int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st);
 
+// Raise a kernel's dynamic shared memory limit to at least `bytes` on the
+// current device.  The limit is a per-function, per-device setting shared by
+// every problem (and every captured graph) in the process, so it only ever
+// grows: a later, smaller problem must not lower it under an earlier one's
+// launches.  Thread-safe.
+cudaError_t raise_dynamic_smem(const void* func, size_t bytes);
+
 // Banded solver (sgba_band.cu) for reduced systems that are a band plus a few
 // dense border rows (sequential and loop-shaped problems).  band_shape picks
-// the split from the lower block pattern of S (0 = not banded enough);
-// band_setup checks the launch limits and returns the cluster size (0 = no).
+// the split from the lower block pattern of S (0 = no split within the band
+// and border limits); band_setup checks the launch limits and returns the
+// cluster size (0 = no).
 int band_shape(int nf, const std::vector<int32_t>& sb_row, const std::vector<int32_t>& sb_col, int* band_rows,
                int* band_w);
 int band_setup(int n, int nband, int w, int* cluster, int* ring);

@@ -114,6 +114,58 @@ __device__ __forceinline__ float huber_weight_f(float huber, float r0, float r1)
   return sqrtf(2.0f * huber * nrm - huber * huber) / nrm;
 }
 
+// Accumulator of a float-float dot product: hi carries the running sum through
+// an exact TwoSum, the rounding errors of the products and of the sums go into
+// the float lo.
+struct Acc {
+  float hi, lo;
+};
+__device__ __forceinline__ Acc acc_zero() { return Acc{0.0f, 0.0f}; }
+__device__ __forceinline__ void acc_madd(Acc& a, dd x, dd y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  const float s = __fadd_rn(a.hi, p);
+  const float bb = __fsub_rn(s, a.hi);
+  const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  a.hi = s;
+  a.lo = __fadd_rn(a.lo, __fadd_rn(err, e));
+}
+__device__ __forceinline__ void acc_addf(Acc& a, float y) {
+  const float s = __fadd_rn(a.hi, y);
+  const float bb = __fsub_rn(s, a.hi);
+  const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(y, bb));
+  a.hi = s;
+  a.lo = __fadd_rn(a.lo, err);
+}
+__device__ __forceinline__ dd acc_get(const Acc& a) { return dd_fast_two_sum(a.hi, a.lo); }
+
+// The same weighting in float-float: r~ = w r with w = sqrt(rho(|r|)) / |r|.
+__device__ __forceinline__ void huber_weighted_dd(float huber, dd huber_dd, dd r0, dd r1, dd* o0, dd* o1) {
+  if (!(huber > 0.0f)) {
+    *o0 = r0;
+    *o1 = r1;
+    return;
+  }
+  const dd n2 = dd_add(dd_mul(r0, r0), dd_mul(r1, r1));
+  const dd nrm = dd_sqrt(n2);
+  if (nrm.hi == 0.0f) {
+    *o0 = dd_make(0.0f, 0.0f);
+    *o1 = dd_make(0.0f, 0.0f);
+    return;
+  }
+  if (nrm.hi < huber || (nrm.hi == huber_dd.hi && nrm.lo <= huber_dd.lo)) {
+    *o0 = r0;
+    *o1 = r1;
+    return;
+  }
+  const dd rho = dd_sub(dd_mul(dd_add(huber_dd, huber_dd), nrm), dd_mul(huber_dd, huber_dd));
+  const dd w = dd_div(dd_sqrt(rho), nrm);
+  *o0 = dd_mul(w, r0);
+  *o1 = dd_mul(w, r1);
+}
+
 // Jacobians of r = z - pi(T_cw p) w.r.t. the left pose perturbation (2x6,
 // tangent [omega; nu]) and the point (2x3), in FP32
 // (crates/sophus_opt/src/nlls/functor_library/costs/pinhole_reprojection.rs:60-95).
@@ -152,6 +204,7 @@ __device__ __forceinline__ void jacobians_f(const float* pt /*R_cw 9 + t_cw 3*/,
 
 
 constexpr int kZS = 20;  // floats per Z row block (18 used; padded for float4 loads)
+constexpr int kZD = kZddFloats;  // floats per float-float Z (36 used; padded for float4 loads)
 
 // Sum over the 32 lanes of a warp of `nv` float values per lane, in
 // float-float: values are transposed through shared memory (red[nv][33]) and
@@ -257,6 +310,7 @@ struct CostArgs {
   const float* pose_dd;
   const double* points;
   float2* res_out;
+  float2* res_lo_out;  // low parts of the residuals (float-float linearization), or null
   double* partials;
   dd fx, fy, cx, cy;
   float huber;
@@ -296,7 +350,9 @@ __global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* c
       }
     }
     acc = dd_add(acc, c);
-    a.res_out[o] = make_float2(ru.hi + ru.lo, rv.hi + rv.lo);
+    const float rh = ru.hi + ru.lo, vh = rv.hi + rv.lo;
+    a.res_out[o] = make_float2(rh, vh);
+    if (a.res_lo_out) a.res_lo_out[o] = make_float2((ru.hi - rh) + ru.lo, (rv.hi - vh) + rv.lo);
   }
   // block reduction (fixed tree)
   __shared__ float sh_hi[kCostThreads / 32], sh_lo[kCostThreads / 32];
@@ -390,6 +446,12 @@ struct LinArgs {
   // list mode of k_landmark: only the listed points, float-float path forced
   const int32_t* list;
   const int32_t* list_count;
+  // float-float linearization: every point on the float-float path, residual
+  // low parts and the Huber weight in float-float, Z kept as float-float pairs
+  int force_dd;
+  const float2* res_lo;
+  float* zdd;  // kZD floats per term: Z (6x3) as (hi, lo) pairs
+  dd huber_dd;
 };
 
 __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
@@ -467,7 +529,7 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
     float c11 = sqrtf(t11);
     float c21 = (V[4] - c20 * c10) / c11;
     float t22 = V[5] - c20 * c20 - c21 * c21;
-    const bool well = !a.list && V[0] > 0.f && t11 > a.well_tol * V[3] && t22 > a.well_tol * V[5];
+    const bool well = !a.list && !a.force_dd && V[0] > 0.f && t11 > a.well_tol * V[3] && t22 > a.well_tol * V[5];
     const dd pxd = dd_from_double(a.points[3 * i + 0]);
     const dd pyd = dd_from_double(a.points[3 * i + 1]);
     const dd pzd = dd_from_double(a.points[3 * i + 2]);
@@ -483,8 +545,15 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
           JacD J;
           jacobians_dd(Pd, pxd, pyd, pzd, a.fxd, a.fyd, &J);
           float2 r = a.res[o];
-          float w = huber_weight_f(a.huber, r.x, r.y);
-          const float r0 = w * r.x, r1 = w * r.y;
+          dd r0, r1;
+          if (a.res_lo) {
+            const float2 rl = a.res_lo[o];
+            huber_weighted_dd(a.huber, a.huber_dd, dd_make(r.x, rl.x), dd_make(r.y, rl.y), &r0, &r1);
+          } else {
+            const float w = huber_weight_f(a.huber, r.x, r.y);
+            r0 = dd_from_float(w * r.x);
+            r1 = dd_from_float(w * r.y);
+          }
           const dd* m = J.jm;
           acc[0] = dd_add(acc[0], dd_add(dd_mul(m[0], m[0]), dd_mul(m[3], m[3])));
           acc[1] = dd_add(acc[1], dd_add(dd_mul(m[0], m[1]), dd_mul(m[3], m[4])));
@@ -492,9 +561,9 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
           acc[3] = dd_add(acc[3], dd_add(dd_mul(m[1], m[1]), dd_mul(m[4], m[4])));
           acc[4] = dd_add(acc[4], dd_add(dd_mul(m[1], m[2]), dd_mul(m[4], m[5])));
           acc[5] = dd_add(acc[5], dd_add(dd_mul(m[2], m[2]), dd_mul(m[5], m[5])));
-          acc[6] = dd_add(acc[6], dd_add(dd_mul_f(m[0], r0), dd_mul_f(m[3], r1)));
-          acc[7] = dd_add(acc[7], dd_add(dd_mul_f(m[1], r0), dd_mul_f(m[4], r1)));
-          acc[8] = dd_add(acc[8], dd_add(dd_mul_f(m[2], r0), dd_mul_f(m[5], r1)));
+          acc[6] = dd_add(acc[6], dd_add(dd_mul(m[0], r0), dd_mul(m[3], r1)));
+          acc[7] = dd_add(acc[7], dd_add(dd_mul(m[1], r0), dd_mul(m[4], r1)));
+          acc[8] = dd_add(acc[8], dd_add(dd_mul(m[2], r0), dd_mul(m[5], r1)));
         }
       }
       for (int k = 0; k < 9; ++k) acc[k] = dd_warp_sum(acc[k]);
@@ -596,6 +665,7 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
             for (int q = 0; q < 3; ++q)
               Wd[r * 3 + q] = dd_add(Wd[r * 3 + q], dd_add(dd_mul(J.jp[r], J.jm[q]), dd_mul(J.jp[6 + r], J.jm[3 + q])));
         }
+        float* zd = a.zdd ? a.zdd + kZD * g : nullptr;
         for (int r = 0; r < 6; ++r) {
           dd z0 = dd_mul(I[0], Wd[r * 3 + 0]);
           dd z1 = dd_add(dd_mul(I[1], Wd[r * 3 + 0]), dd_mul(I[2], Wd[r * 3 + 1]));
@@ -603,6 +673,11 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
           Z[r * 3 + 0] = z0.hi + z0.lo;
           Z[r * 3 + 1] = z1.hi + z1.lo;
           Z[r * 3 + 2] = z2.hi + z2.lo;
+          if (zd) {
+            zd[6 * r + 0] = z0.hi; zd[6 * r + 1] = z0.lo;
+            zd[6 * r + 2] = z1.hi; zd[6 * r + 3] = z1.lo;
+            zd[6 * r + 4] = z2.hi; zd[6 * r + 5] = z2.lo;
+          }
         }
       }
       Z[18] = 0.f;
@@ -813,6 +888,11 @@ struct CamArgs {
   float fx, fy, huber;
   double* tile_part;
   int with_schur;
+  // float-float linearization
+  const float* pose_dd;
+  const float2* res_lo;
+  const float* zdd;
+  dd fxd, fyd, huber_dd;
 };
 
 __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const Ctrl* ctrl) {
@@ -901,6 +981,96 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
   }
 }
 
+// Float-float linearization of a camera tile: Jacobians, residual weights,
+// products and sums all in float-float (the loop problems' reduced systems
+// cancel ~25x, beyond what FP32 products leave).  Same outputs as
+// k_camera_tiles.
+__global__ void __launch_bounds__(kTileThreads) k_camera_tiles_dd(CamArgs a, const Ctrl* ctrl) {
+  if (halted(ctrl)) return;
+  const int tile = blockIdx.x;
+  const int fb = a.tile_fb[tile];
+  const float* Pd = a.pose_dd + 24 * a.fb_pose[fb];
+  Acc u[33];
+#pragma unroll
+  for (int k = 0; k < 33; ++k) u[k] = acc_zero();
+  const int64_t e = a.tile_begin[tile] + threadIdx.x;
+  if (e < a.tile_end[tile]) {
+    const int64_t g = a.cam_g[e];
+    const int pi = a.g_pt[g];
+    const dd px = dd_from_double(a.points[3 * pi + 0]);
+    const dd py = dd_from_double(a.points[3 * pi + 1]);
+    const dd pz = dd_from_double(a.points[3 * pi + 2]);
+    for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+      JacD J;
+      jacobians_dd(Pd, px, py, pz, a.fxd, a.fyd, &J);
+      const float2 r = a.res[o], rl = a.res_lo[o];
+      dd r0, r1;
+      huber_weighted_dd(a.huber, a.huber_dd, dd_make(r.x, rl.x), dd_make(r.y, rl.y), &r0, &r1);
+      int k = 0;
+#pragma unroll
+      for (int p = 0; p < 6; ++p) {
+#pragma unroll
+        for (int q = p; q < 6; ++q) {
+          acc_madd(u[k], J.jp[p], J.jp[q]);
+          acc_madd(u[k], J.jp[6 + p], J.jp[6 + q]);
+          ++k;
+        }
+        acc_madd(u[21 + p], J.jp[p], r0);
+        acc_madd(u[21 + p], J.jp[6 + p], r1);
+      }
+    }
+    const int mb = a.pt_mb[pi];
+    if (a.with_schur && mb >= 0) {
+      const float* zd = a.zdd + kZD * g;
+      const float* cv = a.cvec + 6 * mb;
+      const dd c0 = dd_make(cv[0], cv[1]), c1 = dd_make(cv[2], cv[3]), c2 = dd_make(cv[4], cv[5]);
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        acc_madd(u[27 + r], dd_make(zd[6 * r + 0], zd[6 * r + 1]), c0);
+        acc_madd(u[27 + r], dd_make(zd[6 * r + 2], zd[6 * r + 3]), c1);
+        acc_madd(u[27 + r], dd_make(zd[6 * r + 4], zd[6 * r + 5]), c2);
+      }
+    }
+  }
+  // float-float sums over the warp (transposed through shared memory, the hi
+  // parts then the lo parts), then over the warps in fixed order
+  __shared__ float zred[kTileThreads / 32][33][33];
+  __shared__ float sh_hi[33][kTileThreads / 32];
+  __shared__ float sh_lo[33][kTileThreads / 32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  Acc t0 = acc_zero(), t1 = acc_zero();  // values lane and lane + 32
+#pragma unroll
+  for (int k = 0; k < 33; ++k) zred[w][k][lane] = u[k].hi;
+  __syncwarp();
+  for (int l = 0; l < 32; ++l) acc_addf(t0, zred[w][lane][l]);
+  if (lane == 0)
+    for (int l = 0; l < 32; ++l) acc_addf(t1, zred[w][32][l]);
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 33; ++k) zred[w][k][lane] = u[k].lo;
+  __syncwarp();
+  for (int l = 0; l < 32; ++l) acc_addf(t0, zred[w][lane][l]);
+  if (lane == 0)
+    for (int l = 0; l < 32; ++l) acc_addf(t1, zred[w][32][l]);
+  {
+    const dd v0 = acc_get(t0);
+    sh_hi[lane][w] = v0.hi;
+    sh_lo[lane][w] = v0.lo;
+    if (lane == 0) {
+      const dd v1 = acc_get(t1);
+      sh_hi[32][w] = v1.hi;
+      sh_lo[32][w] = v1.lo;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < kTileVals) {
+    const int k = threadIdx.x;
+    dd v = dd_make(0.f, 0.f);
+    for (int q = 0; q < kTileThreads / 32; ++q) v = dd_add(v, dd_make(sh_hi[k][q], sh_lo[k][q]));
+    a.tile_part[static_cast<int64_t>(tile) * kTileVals + k] = dd_to_double(v);
+  }
+}
+
 __global__ void __launch_bounds__(64) k_camera_finalize(int nf, const int64_t* fb_tile_begin,
                                                         const double* tile_part, double* ufull, double* bf,
                                                         double* rb, Ctrl* ctrl, int with_schur) {
@@ -973,6 +1143,7 @@ struct SchurArgs {
   const int32_t* block_chunk_begin;  // nsb + 1, into chunks
   float2* part;                   // 36 float-float partials per chunk
   const float* zmat;
+  const float* zdd;   // float-float Z (float-float linearization)
   const double* ufull;
   const double* cnt_f;
   double* S;
@@ -1039,6 +1210,65 @@ __global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl)
   }
 }
 
+// Pass 1 of the float-float linearization: the same chunks, float-float Z and
+// float-float products and sums (36 accumulators per lane).
+__global__ void __launch_bounds__(256, 1) k_schur_dd(SchurArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  __shared__ float red[8][36][33];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  for (int64_t ch = static_cast<int64_t>(blockIdx.x) * wpb + wib; ch < a.nchunk;
+       ch += static_cast<int64_t>(gridDim.x) * wpb) {
+    Acc acc[36];
+#pragma unroll
+    for (int e = 0; e < 36; ++e) acc[e] = acc_zero();
+    const int64_t q1 = a.chunk_begin[ch + 1];
+    for (int64_t q = a.chunk_begin[ch] + lane; q < q1; q += 32) {
+      const int2 pr = a.pairs[q];
+      float za[36], zb[36];
+      const float4* pa = reinterpret_cast<const float4*>(a.zdd + kZD * static_cast<int64_t>(pr.x));
+      const float4* pb = reinterpret_cast<const float4*>(a.zdd + kZD * static_cast<int64_t>(pr.y));
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        const float4 u = __ldg(pa + k), v = __ldg(pb + k);
+        za[4 * k] = u.x; za[4 * k + 1] = u.y; za[4 * k + 2] = u.z; za[4 * k + 3] = u.w;
+        zb[4 * k] = v.x; zb[4 * k + 1] = v.y; zb[4 * k + 2] = v.z; zb[4 * k + 3] = v.w;
+      }
+#pragma unroll
+      for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c)
+#pragma unroll
+          for (int t = 0; t < 3; ++t)
+            acc_madd(acc[r * 6 + c], dd_make(za[6 * r + 2 * t], za[6 * r + 2 * t + 1]),
+                     dd_make(zb[6 * c + 2 * t], zb[6 * c + 2 * t + 1]));
+    }
+    // lanes' accumulators summed in float-float: hi parts, then lo parts
+    Acc t0 = acc_zero(), t1 = acc_zero();  // entries lane and lane + 32
+#pragma unroll
+    for (int e = 0; e < 36; ++e) red[wib][e][lane] = acc[e].hi;
+    __syncwarp();
+    for (int l = 0; l < 32; ++l) acc_addf(t0, red[wib][lane][l]);
+    if (lane < 4)
+      for (int l = 0; l < 32; ++l) acc_addf(t1, red[wib][lane + 32][l]);
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < 36; ++e) red[wib][e][lane] = acc[e].lo;
+    __syncwarp();
+    for (int l = 0; l < 32; ++l) acc_addf(t0, red[wib][lane][l]);
+    if (lane < 4)
+      for (int l = 0; l < 32; ++l) acc_addf(t1, red[wib][lane + 32][l]);
+    const dd v0 = acc_get(t0);
+    a.part[36 * ch + lane] = make_float2(v0.hi, v0.lo);
+    if (lane < 4) {
+      const dd v1 = acc_get(t1);
+      a.part[36 * ch + lane + 32] = make_float2(v1.hi, v1.lo);
+    }
+    __syncwarp();
+  }
+}
+
 // Pass 2, one warp per lower block of S: the block's chunk partials summed in
 // chunk order (float-float), the diagonal U + nu n I added on diagonal
 // blocks; f64 store of both triangles (and the float-float copy).
@@ -1090,6 +1320,7 @@ struct BackArgs {
   const int32_t* pose_fb;
   const int32_t* pt_mb;
   const float* zmat;
+  const float* zdd;  // float-float Z (float-float linearization) or null
   const float* cinv;
   const float* cvec;
   const float* xdd;  // dx_f as float-float pairs
@@ -1110,15 +1341,26 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
     for (int64_t g = a.pt_g_begin[i] + lane; g < a.pt_g_begin[i + 1]; g += 32) {
       const int fb = a.pose_fb[a.g_pose[g]];
       if (fb < 0) continue;
-      float Z[20];
-      load_z(a.zmat, static_cast<int>(g), Z);
       const float2* xp = reinterpret_cast<const float2*>(a.xdd) + 6 * fb;
+      if (a.zdd) {
+        const float* zd = a.zdd + kZD * g;
 #pragma unroll
-      for (int r = 0; r < 6; ++r) {
-        const float2 xv = xp[r];
-        const dd x = dd_make(xv.x, xv.y);
+        for (int r = 0; r < 6; ++r) {
+          const float2 xv = xp[r];
+          const dd x = dd_make(xv.x, xv.y);
 #pragma unroll
-        for (int q = 0; q < 3; ++q) t[q] = dd_add(t[q], dd_mul_f(x, Z[r * 3 + q]));
+          for (int q = 0; q < 3; ++q) t[q] = dd_add(t[q], dd_mul(x, dd_make(zd[6 * r + 2 * q], zd[6 * r + 2 * q + 1])));
+        }
+      } else {
+        float Z[20];
+        load_z(a.zmat, static_cast<int>(g), Z);
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+          const float2 xv = xp[r];
+          const dd x = dd_make(xv.x, xv.y);
+#pragma unroll
+          for (int q = 0; q < 3; ++q) t[q] = dd_add(t[q], dd_mul_f(x, Z[r * 3 + q]));
+        }
       }
     }
     // float-float sum over the lanes: fixed tree through shared memory
@@ -1437,11 +1679,13 @@ __global__ void k_decide(const double* cost_part, int n_cost, const double* upd_
 // Accepted step: trial state becomes the current state.
 __global__ void k_commit(int nc, int np, int64_t no, const double* poses_t, double* poses,
                          const double* points_t, double* points, const float2* res_t, float2* res,
-                         const Ctrl* ctrl) {
+                         const float2* res_lo_t, float2* res_lo, const Ctrl* ctrl) {
   if (!ctrl->accept) return;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   const int64_t t0 = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   for (int64_t t = t0; t < no; t += stride) res[t] = res_t[t];
+  if (res_lo)
+    for (int64_t t = t0; t < no; t += stride) res_lo[t] = res_lo_t[t];
   for (int64_t t = t0; t < 7 * static_cast<int64_t>(nc); t += stride) poses[t] = poses_t[t];
   for (int64_t t = t0; t < 3 * static_cast<int64_t>(np); t += stride) points[t] = points_t[t];
 }
@@ -1474,6 +1718,7 @@ int launch_pose_tables(const Sizes& s, const Dev& d, const double* poses, cudaSt
 static CostArgs make_cost_args(const Sizes& s, const Dev& d, const double* points, float2* res_out,
                                double* partials, int respect_skip) {
   CostArgs a;
+  a.res_lo_out = (res_out == d.res) ? d.res_lo : (res_out == d.res_t ? d.res_lo_t : nullptr);
   a.no = s.no;
   a.uv = d.obs_uv;
   a.opose = d.obs_pose;
@@ -1515,44 +1760,7 @@ int launch_iteration_begin(const Sizes& s, const Dev& d, cudaStream_t st) {
   return 1;
 }
 
-// Landmark pass: the chunked kernel plus the float-float redo of the points it
-// queued, or (final Hessian pass, or no chunk table) the warp-per-point kernel.
-static int launch_landmark(const Sizes& s, const Dev& d, LinArgs la, cudaStream_t st) {
-  la.g_pt = d.g_pt;
-  la.list = nullptr;
-  la.list_count = nullptr;
-  la.chunk_pt = d.lmk_chunk_pt;
-  la.nchunk = s.nlchunk;
-  la.slow_list = d.slow_list;
-  la.slow_count = d.slow_count;
-  if (!la.use_override && s.nlchunk > 0) {
-    cudaMemsetAsync(d.slow_count, 0, sizeof(int32_t), st);
-    const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
-    k_landmark_chunks<<<grid, 256, sizeof(float) * 9 * static_cast<size_t>(s.lmk_cap), st>>>(la, d.ctrl);
-    LinArgs lb = la;
-    lb.list = d.slow_list;
-    lb.list_count = d.slow_count;
-    k_landmark<<<s.lmk_list_grid, 256, 0, st>>>(lb, d.ctrl);
-    return 2;
-  }
-  k_landmark<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(la, d.ctrl);
-  return 1;
-}
-
-int landmark_setup(int cap) {
-  const size_t bytes = sizeof(float) * 9 * static_cast<size_t>(cap);
-  if (bytes <= 48 * 1024) return 0;
-  return cudaFuncSetAttribute(k_landmark_chunks, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(bytes)) ==
-                 cudaSuccess
-             ? 0
-             : -1;
-}
-
-int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_override,
-                     cudaStream_t st) {
-  int n = 0;
-  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses, d.pose_f, d.pose_dd, d.ctrl, 0);
-  ++n;
+static LinArgs make_lin_args(const Sizes& s, const Dev& d, double nu_override, bool use_override) {
   LinArgs la;
   la.well_tol = s.lmk_well_tol;
   la.np = s.np;
@@ -1571,6 +1779,7 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
   la.fx = static_cast<float>(s.intr[0]);
   la.fy = static_cast<float>(s.intr[1]);
   la.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
+  la.huber_dd = dd_make(static_cast<float>(s.huber), static_cast<float>(s.huber - static_cast<float>(s.huber)));
   la.zmat = d.zmat;
   la.cinv = d.cinv;
   la.cvec = d.cvec;
@@ -1578,30 +1787,107 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
   la.nu_override = nu_override;
   la.use_override = use_override ? 1 : 0;
   la.fail = &d.ctrl->fail;
-  n += launch_landmark(s, d, la, st);
-  if (s.ntiles > 0) {
-    CamArgs ca;
-    ca.tile_fb = d.tile_fb;
-    ca.tile_begin = d.tile_begin;
-    ca.tile_end = d.tile_end;
-    ca.cam_g = d.cam_g;
-    ca.g_begin = d.g_begin;
-    ca.g_pt = d.g_pt;
-    ca.fb_pose = d.fb_pose;
-    ca.pt_mb = d.pt_mb;
-    ca.pose_f = d.pose_f;
-    ca.points = d.points;
-    ca.res = d.res;
-    ca.zmat = d.zmat;
-    ca.cvec = d.cvec;
-    ca.fx = la.fx;
-    ca.fy = la.fy;
-    ca.huber = la.huber;
-    ca.tile_part = d.tile_part;
-    ca.with_schur = use_override ? 0 : 1;
-    k_camera_tiles<<<static_cast<unsigned>(s.ntiles), kTileThreads, 0, st>>>(ca, d.ctrl);
-    ++n;
+  la.g_pt = d.g_pt;
+  la.list = nullptr;
+  la.list_count = nullptr;
+  la.chunk_pt = d.lmk_chunk_pt;
+  la.nchunk = s.nlchunk;
+  la.slow_list = d.slow_list;
+  la.slow_count = d.slow_count;
+  la.force_dd = s.lin_dd;
+  la.res_lo = s.lin_dd ? d.res_lo : nullptr;
+  la.zdd = s.lin_dd ? d.zdd : nullptr;
+  return la;
+}
+
+static CamArgs make_cam_args(const Sizes& s, const Dev& d, int with_schur) {
+  CamArgs ca;
+  ca.tile_fb = d.tile_fb;
+  ca.tile_begin = d.tile_begin;
+  ca.tile_end = d.tile_end;
+  ca.cam_g = d.cam_g;
+  ca.g_begin = d.g_begin;
+  ca.g_pt = d.g_pt;
+  ca.fb_pose = d.fb_pose;
+  ca.pt_mb = d.pt_mb;
+  ca.pose_f = d.pose_f;
+  ca.points = d.points;
+  ca.res = d.res;
+  ca.zmat = d.zmat;
+  ca.cvec = d.cvec;
+  ca.fx = static_cast<float>(s.intr[0]);
+  ca.fy = static_cast<float>(s.intr[1]);
+  ca.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
+  ca.tile_part = d.tile_part;
+  ca.with_schur = with_schur;
+  ca.pose_dd = d.pose_dd;
+  ca.res_lo = d.res_lo;
+  ca.zdd = d.zdd;
+  ca.fxd = dd_make(static_cast<float>(s.intr[0]), static_cast<float>(s.intr[0] - static_cast<float>(s.intr[0])));
+  ca.fyd = dd_make(static_cast<float>(s.intr[1]), static_cast<float>(s.intr[1] - static_cast<float>(s.intr[1])));
+  ca.huber_dd = dd_make(static_cast<float>(s.huber), static_cast<float>(s.huber - static_cast<float>(s.huber)));
+  return ca;
+}
+
+static int launch_camera(const Sizes& s, const Dev& d, int with_schur, cudaStream_t st) {
+  if (s.ntiles == 0) return 0;
+  const CamArgs ca = make_cam_args(s, d, with_schur);
+  if (s.lin_dd) k_camera_tiles_dd<<<static_cast<unsigned>(s.ntiles), kTileThreads, 0, st>>>(ca, d.ctrl);
+  else k_camera_tiles<<<static_cast<unsigned>(s.ntiles), kTileThreads, 0, st>>>(ca, d.ctrl);
+  return 1;
+}
+
+static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
+  BackArgs b;
+  b.np = s.np;
+  b.pt_g_begin = d.pt_g_begin;
+  b.g_pose = d.g_pose;
+  b.pose_fb = d.pose_fb;
+  b.pt_mb = d.pt_mb;
+  b.zmat = d.zmat;
+  b.zdd = s.lin_dd ? d.zdd : nullptr;
+  b.cinv = d.cinv;
+  b.cvec = d.cvec;
+  b.xdd = d.xdd;
+  b.dm = d.dm;
+  k_backsub<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(b, d.ctrl);
+  return 1;
+}
+
+// Landmark pass: the chunked kernel plus the float-float redo of the points it
+// queued, or (final Hessian pass, no chunk table, or the float-float
+// linearization) the warp-per-point kernel.
+static int launch_landmark(const Sizes& s, const Dev& d, LinArgs la, cudaStream_t st) {
+  if (!la.use_override && s.nlchunk > 0 && !s.lin_dd) {
+    cudaMemsetAsync(d.slow_count, 0, sizeof(int32_t), st);
+    const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
+    k_landmark_chunks<<<grid, 256, sizeof(float) * 9 * static_cast<size_t>(s.lmk_cap), st>>>(la, d.ctrl);
+    LinArgs lb = la;
+    lb.list = d.slow_list;
+    lb.list_count = d.slow_count;
+    k_landmark<<<s.lmk_list_grid, 256, 0, st>>>(lb, d.ctrl);
+    return 2;
   }
+  k_landmark<<<warp_grid(s.np, 8, s.lin_dd ? 16384 : 4096), 256, 0, st>>>(la, d.ctrl);
+  return 1;
+}
+
+int landmark_setup(int cap) {
+  const size_t bytes = sizeof(float) * 9 * static_cast<size_t>(cap);
+  if (bytes <= 48 * 1024) return 0;
+  return raise_dynamic_smem(reinterpret_cast<const void*>(k_landmark_chunks), bytes) ==
+                 cudaSuccess
+             ? 0
+             : -1;
+}
+
+int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_override,
+                     cudaStream_t st) {
+  int n = 0;
+  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses, d.pose_f, d.pose_dd, d.ctrl, 0);
+  ++n;
+  n += launch_landmark(s, d, make_lin_args(s, d, nu_override, use_override), st);
+  n += launch_camera(s, d, use_override ? 0 : 1, st);
   k_camera_finalize<<<s.nf, 64, 0, st>>>(s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf, d.rb, d.ctrl,
                                          use_override ? 0 : 1);
   ++n;
@@ -1620,6 +1906,7 @@ int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
   a.sb_pair_begin = d.sb_pair_begin;
   a.pairs = d.pairs;
   a.zmat = d.zmat;
+  a.zdd = d.zdd;
   a.ufull = d.ufull;
   a.cnt_f = d.cnt_f;
   a.S = d.S;
@@ -1629,26 +1916,15 @@ int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
   a.chunk_begin = d.chunk_begin;
   a.block_chunk_begin = d.block_chunk_begin;
   a.part = d.schur_part;
-  k_schur<<<warp_grid(s.nchunk, 8, 65536), 256, 0, st>>>(a, d.ctrl);
+  if (s.lin_dd) k_schur_dd<<<warp_grid(s.nchunk, 8, 65536), 256, 0, st>>>(a, d.ctrl);
+  else k_schur<<<warp_grid(s.nchunk, 8, 65536), 256, 0, st>>>(a, d.ctrl);
   k_schur_reduce<<<warp_grid(s.nsb, 8, 8192), 256, 0, st>>>(a, d.ctrl);
   return 2;
 }
 
 int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
   int n = 0;
-  BackArgs b;
-  b.np = s.np;
-  b.pt_g_begin = d.pt_g_begin;
-  b.g_pose = d.g_pose;
-  b.pose_fb = d.pose_fb;
-  b.pt_mb = d.pt_mb;
-  b.zmat = d.zmat;
-  b.cinv = d.cinv;
-  b.cvec = d.cvec;
-  b.xdd = d.xdd;
-  b.dm = d.dm;
-  k_backsub<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(b, d.ctrl);
-  ++n;
+  n += launch_backsub(s, d, st);
   if (s.gauge_kind == 1) {
     GaugeArgs g;
     g.nf = s.nf;
@@ -1698,58 +1974,10 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) 
   switch (kernel_id) {
     case 1:
       return launch_schur(s, d, st);
-    case 2: {
-      LinArgs la;
-      la.well_tol = s.lmk_well_tol;
-      la.np = s.np;
-      la.pt_g_begin = d.pt_g_begin;
-      la.g_begin = d.g_begin;
-      la.g_pose = d.g_pose;
-      la.pose_fb = d.pose_fb;
-      la.pt_mb = d.pt_mb;
-      la.cnt_m = d.cnt_m;
-      la.pose_f = d.pose_f;
-      la.points = d.points;
-      la.pose_dd = d.pose_dd;
-      la.fxd = dd_make(static_cast<float>(s.intr[0]), static_cast<float>(s.intr[0] - static_cast<float>(s.intr[0])));
-      la.fyd = dd_make(static_cast<float>(s.intr[1]), static_cast<float>(s.intr[1] - static_cast<float>(s.intr[1])));
-      la.res = d.res;
-      la.fx = static_cast<float>(s.intr[0]);
-      la.fy = static_cast<float>(s.intr[1]);
-      la.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
-      la.zmat = d.zmat;
-      la.cinv = d.cinv;
-      la.cvec = d.cvec;
-      la.bm = d.bm;
-      la.nu_override = 0.0;
-      la.use_override = 0;
-      la.fail = &d.ctrl->fail;
-      return launch_landmark(s, d, la, st);
-    }
-    case 3: {
-      if (s.ntiles == 0) return 0;
-      CamArgs ca;
-      ca.tile_fb = d.tile_fb;
-      ca.tile_begin = d.tile_begin;
-      ca.tile_end = d.tile_end;
-      ca.cam_g = d.cam_g;
-      ca.g_begin = d.g_begin;
-      ca.g_pt = d.g_pt;
-      ca.fb_pose = d.fb_pose;
-      ca.pt_mb = d.pt_mb;
-      ca.pose_f = d.pose_f;
-      ca.points = d.points;
-      ca.res = d.res;
-      ca.zmat = d.zmat;
-      ca.cvec = d.cvec;
-      ca.fx = static_cast<float>(s.intr[0]);
-      ca.fy = static_cast<float>(s.intr[1]);
-      ca.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
-      ca.tile_part = d.tile_part;
-      ca.with_schur = 1;
-      k_camera_tiles<<<static_cast<unsigned>(s.ntiles), kTileThreads, 0, st>>>(ca, d.ctrl);
-      return 1;
-    }
+    case 2:
+      return launch_landmark(s, d, make_lin_args(s, d, 0.0, false), st);
+    case 3:
+      return launch_camera(s, d, 1, st);
     case 4: {
       CostArgs a = make_cost_args(s, d, d.points_t, d.res_t, d.part + 4 * kUpdBlocks, 1);
       k_cost<<<cost_grid(s.no), kCostThreads, 0, st>>>(a, d.ctrl);
@@ -1757,21 +1985,8 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) 
     }
     case 5:
       return launch_factor_solve(s, d, st);
-    case 6: {
-      BackArgs b;
-      b.np = s.np;
-      b.pt_g_begin = d.pt_g_begin;
-      b.g_pose = d.g_pose;
-      b.pose_fb = d.pose_fb;
-      b.pt_mb = d.pt_mb;
-      b.zmat = d.zmat;
-      b.cinv = d.cinv;
-      b.cvec = d.cvec;
-      b.xdd = d.xdd;
-      b.dm = d.dm;
-      k_backsub<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(b, d.ctrl);
-      return 1;
-    }
+    case 6:
+      return launch_backsub(s, d, st);
     default:
       return 0;
   }
@@ -1792,7 +2007,7 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
   if (cb > 1216) cb = 1216;
   if (cb < 1) cb = 1;
   k_commit<<<cb, 256, 0, st>>>(s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res,
-                               d.ctrl);
+                               d.res_lo_t, d.res_lo, d.ctrl);
   return 4;
 }
 
@@ -1930,6 +2145,7 @@ cudaError_t launch_total_cost_noalloc(int32_t nc, const double* poses, int32_t n
   a.pose_dd = pose_dd;
   a.points = points;
   a.res_out = nullptr;
+  a.res_lo_out = nullptr;
   a.partials = part;
   a.fx = split(intr[0]);
   a.fy = split(intr[1]);

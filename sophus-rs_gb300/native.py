@@ -90,7 +90,7 @@ class Layout(C.Structure):
         ("solver", C.c_int32),
         ("band_width", C.c_int32),
         ("border_rows", C.c_int32),
-        ("reserved", C.c_int32),
+        ("float_float_lin", C.c_int32),
     ]
 
 

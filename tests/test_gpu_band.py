@@ -75,10 +75,11 @@ def test_band_step_vs_f64_solve(pkg, open_path):
     assert max(errs) < 1e-6
 
 
-def _trajectory(pkg, oracle, prob, n_iter):
+def _trajectory(pkg, oracle, prob, n_iter, band=True):
     params = fixed_iter_params(pkg, n_iter, prob.initial_lm_damping)
     with pkg.native.Problem(prob, device=0) as gp:
-        assert gp.layout().solver == pkg.native.SOLVER_BAND
+        if band:
+            assert gp.layout().solver == pkg.native.SOLVER_BAND
         grecs, _ = gp.optimize(params)
     orecs, _, _ = oracle.optimize(prob, params, n_threads=16)
     g = np.array([r.merit for r in grecs])
@@ -94,32 +95,39 @@ def _trajectory(pkg, oracle, prob, n_iter):
               % (k, gr.merit, gr.accepted, orr.merit, orr.accepted, change))
         if change > 1e-9:
             assert gr.accepted == orr.accepted, "decision differs at iteration %d" % k
-    return np.abs(g - o) / o
+    return np.abs(g - o) / o, o
 
 
 def test_band_trajectory_parity_loop1500(pkg, oracle):
-    """The 1500-camera loop (300,000 points, ~2.5M observations): per-iteration
-    cost within 1e-6 of the oracle over the first 9 LM iterations.  Beyond
-    them the FP32 Jacobian-side assembly of S (error ~1e-5 of its diagonal
-    scale by then) moves the step of the weakly constrained loop by 1-2% and
-    the trajectories separate."""
+    """The 1500-camera loop (300,000 points, ~2.5M observations), 15 LM
+    iterations.  From iteration 11 on this trajectory amplifies rounding: the
+    f64 oracle run with 16 and with 15 threads (only the summation order
+    differs) separates by ~1e-6 to 1e-5 by iteration 13-15.  The bar per
+    iteration is therefore 1e-6 relative or ten times the oracle's own
+    order sensitivity at that iteration, whichever is larger."""
     prob = _loop(pkg, 1500, 300000)
-    rel = _trajectory(pkg, oracle, prob, 9)
+    rel, o16 = _trajectory(pkg, oracle, prob, 15)
+    params = fixed_iter_params(pkg, 15, prob.initial_lm_damping)
+    o15 = np.array([r.merit for r in oracle.optimize(prob, params, n_threads=15)[0]])
+    self_dev = np.abs(o16 - o15) / o16
+    bar = np.maximum(COST_RTOL, 10.0 * self_dev)
     print("loop 1500 cams: per-iteration cost deviation", rel)
-    assert rel.max() < COST_RTOL
+    print("oracle 16 vs 15 threads:", self_dev)
+    assert np.all(rel[:10] < COST_RTOL)
+    assert np.all(rel < bar)
 
 
-@pytest.mark.parametrize("n_cam,n_pt", [(300, 3000), (600, 12000)])
-def test_band_small_loop_precision_limit(pkg, oracle, n_cam, n_pt):
-    """Loops with few points per camera (10-20): the Schur complement cancels
-    ~25x (S = U - sum Z Z^T), so the FP32 products of the Jacobian-side
-    assembly perturb S by ~1.6e-6 of its diagonal scale; the weakly
-    constrained bending modes of the loop then move the step by a few
-    percent and the cost by up to ~7e-6 of the oracle's.  This is a
-    measured precision limit of the FP32 assembly (the solver itself matches
-    an f64 solve of the same system to 1e-8, test_band_step_vs_f64_solve);
-    tolerance here: 2e-5."""
+@pytest.mark.parametrize("n_cam,n_pt", [(100, 3000), (300, 3000), (600, 12000)])
+def test_loop_trajectory_parity(pkg, oracle, n_cam, n_pt):
+    """Loops with few points per camera (10-30): the Schur complement cancels
+    ~25x (S = U - sum Z Z^T) and the loop's bending modes are weakly
+    constrained, so these problems run the float-float linearization (with
+    FP32 Jacobian-side products the cost deviated by up to 7e-6) and the
+    float-float band solver (the FP32 dense factor with refinement left 2e-6
+    on the 100-camera loop)."""
     prob = _loop(pkg, n_cam, n_pt)
-    rel = _trajectory(pkg, oracle, prob, 8)
+    with pkg.native.Problem(prob, device=0) as gp:
+        assert gp.layout().float_float_lin == 1
+    rel, _ = _trajectory(pkg, oracle, prob, 8)
     print("loop %d cams: per-iteration cost deviation" % n_cam, rel)
-    assert rel.max() < 2e-5
+    assert rel.max() < COST_RTOL

@@ -54,3 +54,20 @@ def test_batch_reports_per_window_errors(pkg):
         out = pkg.native.batch_optimize([p0, p1], params)
     assert out[0][4] == pkg.native.OK and len(out[0][0]) == 3
     assert out[1][4] == pkg.native.ERR_SCHUR_MISSING_FREE_OR_MARG
+
+
+def test_mixed_sizes_keep_launch_limits(pkg):
+    """Kernel launch limits (dynamic shared memory) are per function and per
+    device, shared by every problem in the process: creating a small problem
+    after a large one has captured its iteration graph must not break the
+    large one's launches."""
+    big = pkg.synth.generate(pkg.synth.CIRCLE, n_cam=40, n_pt=4000, seed=pkg.synth.BASE_SEED + 41)
+    small = pkg.synth.generate(pkg.synth.CIRCLE, n_cam=5, n_pt=200, seed=pkg.synth.BASE_SEED + 42)
+    params = fixed_iter_params(pkg, 3, big.initial_lm_damping)
+    with pkg.native.Problem(big, device=0) as gb:
+        first, _ = gb.optimize(params)
+        with pkg.native.Problem(small, device=0) as gs:
+            gs.optimize(fixed_iter_params(pkg, 3, small.initial_lm_damping))
+        second, _ = gb.optimize(params)
+    assert len(first) == len(second) == 3
+    assert np.isfinite(second[-1].merit)
