@@ -363,6 +363,10 @@ def cpu_windows(wins, pkg, threads):
 
 
 def main():
+    if "--workload" in sys.argv and "windows" in sys.argv:
+        # one CUDA stream per window: let the streams map onto more hardware
+        # queues than the default 8 (must be set before the CUDA context exists)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
