@@ -17,6 +17,10 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <pthread.h>
+#include <functional>
+#include <condition_variable>
+#include <atomic>
 #include <utility>
 #include <mutex>
 #include <map>
@@ -76,7 +80,7 @@ int set_error(int status, const char* fmt, ...) {
 
 constexpr int kTile = 256;           // terms per camera tile (one CTA)
 constexpr int64_t kSchurChunk = 256;  // observation pairs per warp in the Schur assembly
-constexpr int32_t kMaxDenseFree = 1536;  // dense reduced-camera-system limit (6 * 1536 rows)
+constexpr int32_t kMaxDenseFree = 4096;  // reduced-camera-system limit (6 * 4096 rows, stored dense in f64)
 
 }  // namespace
 
@@ -122,20 +126,114 @@ int dev_upload(sgba_problem* p, T** ptr, const std::vector<T>& h) {
 
 // Run f(begin, end) over [0, n) split across host threads (contiguous ranges,
 // so per-range work that is itself ordered stays deterministic).
+// Persistent host worker pool (the set-up loops of sgba_problem_create run on
+// it; threads are created once per process).  run(n, f) calls f(k) for every
+// k in [0, n) on the workers and the calling thread and returns when all have
+// finished; parallel regions from different host threads are serialised.
+class HostPool {
+ public:
+  static HostPool& get() {
+    static HostPool pool;
+    return pool;
+  }
+  int threads() const { return forked_child() ? 1 : nthreads_; }
+  void run(int n, const std::function<void(int)>& f) {
+    if (n <= 0) return;
+    if (n == 1 || nthreads_ <= 1 || forked_child()) {  // a forked child has no workers
+      for (int k = 0; k < n; ++k) f(k);
+      return;
+    }
+    std::lock_guard<std::mutex> region_lock(region_mu_);
+    Region r;
+    r.fn = &f;
+    r.n = n;
+    r.remaining = n;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      region_ = &r;
+      ++gen_;
+    }
+    cv_.notify_all();
+    drain(r);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return r.remaining == 0 && r.active == 0; });
+    region_ = nullptr;
+  }
+
+ private:
+  struct Region {
+    const std::function<void(int)>* fn = nullptr;
+    int n = 0;
+    std::atomic<int> next{0};
+    int remaining = 0;  // guarded by mu_
+    int active = 0;     // workers inside the region, guarded by mu_
+  };
+  static bool& forked_child() {
+    static bool forked = false;
+    return forked;
+  }
+  static void on_fork_child() { forked_child() = true; }
+  HostPool() {
+    pthread_atfork(nullptr, nullptr, &HostPool::on_fork_child);
+    int t = static_cast<int>(std::thread::hardware_concurrency());
+    nthreads_ = std::max(1, std::min(t, 16));
+    for (int k = 1; k < nthreads_; ++k) workers_.emplace_back([this] { loop(); });
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& w : workers_) w.join();
+  }
+  void drain(Region& r) {
+    for (;;) {
+      const int k = r.next.fetch_add(1);
+      if (k >= r.n) return;
+      (*r.fn)(k);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--r.remaining == 0) done_cv_.notify_all();
+    }
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      Region* r = nullptr;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return stop_ || (gen_ != seen && region_ != nullptr); });
+        if (stop_) return;
+        seen = gen_;
+        r = region_;
+        ++r->active;
+      }
+      drain(*r);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--r->active == 0 && r->remaining == 0) done_cv_.notify_all();
+    }
+  }
+  int nthreads_ = 1;
+  std::vector<std::thread> workers_;
+  std::mutex region_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  Region* region_ = nullptr;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
+// f(begin, end) over contiguous chunks of [0, n) on the host pool.
+template <class F>
+int par_chunks(int64_t n, int64_t min_per, F f) {
+  const int64_t t = std::max<int64_t>(
+      1, std::min<int64_t>(HostPool::get().threads(), (n + min_per - 1) / std::max<int64_t>(min_per, 1)));
+  HostPool::get().run(static_cast<int>(t), [&](int k) { f(k, n * k / t, n * (k + 1) / t); });
+  return static_cast<int>(t);
+}
+
 template <class F>
 void par_ranges(int64_t n, F f) {
-  const int64_t min_per = 32768;
-  int64_t t = static_cast<int64_t>(std::thread::hardware_concurrency());
-  t = std::max<int64_t>(1, std::min<int64_t>({t, 16, (n + min_per - 1) / min_per}));
-  if (t <= 1) {
-    f(int64_t(0), n);
-    return;
-  }
-  std::vector<std::thread> th;
-  th.reserve(t - 1);
-  for (int64_t k = 1; k < t; ++k) th.emplace_back(f, n * k / t, n * (k + 1) / t);
-  f(int64_t(0), n / t);
-  for (auto& x : th) x.join();
+  par_chunks(n, 32768, [&](int, int64_t b, int64_t e) { f(b, e); });
 }
 
 bool finite_all(const double* v, int64_t n) {
@@ -159,33 +257,81 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
     return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation arrays are NULL");
   if (d->n_obs >= (int64_t(1) << 31))
     return set_error(SGBA_ERR_UNSUPPORTED, "n_obs %lld exceeds the 2^31 term limit", (long long)d->n_obs);
-  if (!finite_all(d->poses, 7ll * d->n_cam) || !finite_all(d->points, 3ll * d->n_pt) ||
-      !finite_all(d->obs_uv, 2 * d->n_obs) || !finite_all(d->intrinsics, 4))
+  std::atomic<bool> finite_uv{true};
+  par_ranges(2 * d->n_obs, [&](int64_t b, int64_t e) {
+    if (!finite_all(d->obs_uv + b, e - b)) finite_uv = false;
+  });
+  if (!finite_all(d->poses, 7ll * d->n_cam) || !finite_all(d->points, 3ll * d->n_pt) || !finite_uv ||
+      !finite_all(d->intrinsics, 4))
     return set_error(SGBA_ERR_INVALID_ARGUMENT, "non-finite input value");
   for (int j = 0; j < d->n_cam; ++j)
     if (!quat_valid(d->poses + 7 * j))
       return set_error(SGBA_ERR_INVALID_PARAMS, "pose %d: quaternion norm differs from 1 by more than 1e-6", j);
   const int nc = d->n_cam, np = d->n_pt;
   const int64_t no = d->n_obs;
-  for (int64_t o = 0; o < no; ++o) {
-    const int32_t jc = d->obs_cam[o], ip = d->obs_pt[o];
-    if (static_cast<uint32_t>(jc) >= static_cast<uint32_t>(nc))
-      return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation %lld: pose index %d out of range", (long long)o, jc);
-    if (static_cast<uint32_t>(ip) >= static_cast<uint32_t>(np))
+  {
+    // the first out-of-range observation, as a sequential scan reports it
+    std::atomic<int64_t> first_bad{no};
+    par_ranges(no, [&](int64_t b, int64_t e) {
+      for (int64_t o = b; o < e; ++o) {
+        if (static_cast<uint32_t>(d->obs_cam[o]) >= static_cast<uint32_t>(nc) ||
+            static_cast<uint32_t>(d->obs_pt[o]) >= static_cast<uint32_t>(np)) {
+          int64_t cur = first_bad.load();
+          while (o < cur && !first_bad.compare_exchange_weak(cur, o)) {
+          }
+          return;
+        }
+      }
+    });
+    const int64_t o = first_bad.load();
+    if (o < no) {
+      const int32_t jc = d->obs_cam[o], ip = d->obs_pt[o];
+      if (static_cast<uint32_t>(jc) >= static_cast<uint32_t>(nc))
+        return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation %lld: pose index %d out of range", (long long)o, jc);
       return set_error(SGBA_ERR_INVALID_ARGUMENT, "observation %lld: point index %d out of range", (long long)o, ip);
+    }
   }
   P->nc = nc;
   P->np = np;
   P->no = no;
   // Order (point, pose, original index): a stable counting sort by point, then
   // a stable sort by pose inside each point (points have few observations).
+  // The counting sort runs on chunks of observations: per-chunk counts, then
+  // each chunk's slots follow the earlier chunks' inside every point, so the
+  // order is exactly the sequential stable one.
   std::vector<int64_t> ord(no);
   std::vector<int64_t> cp(np + 1, 0);
-  for (int64_t o = 0; o < no; ++o) cp[d->obs_pt[o] + 1]++;
-  for (int i = 0; i < np; ++i) cp[i + 1] += cp[i];
   {
-    std::vector<int64_t> fill(cp.begin(), cp.end() - 1);
-    for (int64_t o = 0; o < no; ++o) ord[fill[d->obs_pt[o]]++] = o;
+    const int64_t T = std::max<int64_t>(1, std::min<int64_t>(HostPool::get().threads(), (no + 65535) / 65536));
+    std::vector<std::vector<int32_t>> cnt(T);
+    HostPool::get().run(static_cast<int>(T), [&](int t) {
+      cnt[t].assign(np, 0);
+      for (int64_t o = no * t / T; o < no * (t + 1) / T; ++o) cnt[t][d->obs_pt[o]]++;
+    });
+    for (int i = 0; i < np; ++i) {
+      int64_t run = 0;
+      for (int64_t t = 0; t < T; ++t) run += cnt[t][i];
+      cp[i + 1] = run;
+    }
+    for (int i = 0; i < np; ++i) cp[i + 1] += cp[i];
+    std::vector<std::vector<int64_t>> base(T);
+    par_ranges(np, [&](int64_t i0, int64_t i1) {
+      for (int64_t i = i0; i < i1; ++i) {
+        int64_t run = cp[i];
+        for (int64_t t = 0; t < T; ++t) {
+          const int32_t c = cnt[t][i];
+          cnt[t][i] = static_cast<int32_t>(run - cp[i]);  // chunk t's first slot inside point i
+          run += c;
+        }
+      }
+    });
+    HostPool::get().run(static_cast<int>(T), [&](int t) {
+      std::vector<int32_t>& slot = cnt[t];
+      for (int64_t o = no * t / T; o < no * (t + 1) / T; ++o) {
+        const int32_t i = d->obs_pt[o];
+        ord[cp[i] + slot[i]++] = o;
+      }
+    });
   }
   // groups (reduction ranges: equal non-conditioned arguments, cost_fn.rs:374-390):
   // runs of equal pose inside each point
@@ -255,32 +401,57 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
   P->nm = static_cast<int32_t>(P->mb_pt.size());
   P->cnt_f.assign(P->nf, 0.0);
   P->cnt_m.assign(P->nm, 0.0);
+  // per marginalized point: its reduced terms; per free pose: its terms,
+  // counted on chunks of terms; the camera term lists fill stably the same way
+  par_ranges(np, [&](int64_t i0, int64_t i1) {
+    for (int64_t i = i0; i < i1; ++i)
+      if (P->pt_mb[i] >= 0) P->cnt_m[P->pt_mb[i]] = static_cast<double>(P->pt_g_begin[i + 1] - P->pt_g_begin[i]);
+  });
+  const int64_t TG = std::max<int64_t>(1, std::min<int64_t>(HostPool::get().threads(), (P->ng + 65535) / 65536));
+  std::vector<std::vector<int64_t>> fcnt(TG);
+  std::vector<int64_t> hoff_part(TG, 0);
+  HostPool::get().run(static_cast<int>(TG), [&](int t) {
+    fcnt[t].assign(P->nf, 0);
+    int64_t h = 0;
+    for (int64_t g = P->ng * t / TG; g < P->ng * (t + 1) / TG; ++g) {
+      const int fb = P->pose_fb[P->g_pose[g]];
+      if (fb < 0) continue;
+      fcnt[t][fb]++;
+      if (P->pt_mb[P->g_pt[g]] >= 0) ++h;
+    }
+    hoff_part[t] = h;
+  });
   int64_t h_off = 0;
-  for (int64_t g = 0; g < P->ng; ++g) {
-    int fb = P->pose_fb[P->g_pose[g]], mb = P->pt_mb[P->g_pt[g]];
-    if (fb >= 0) P->cnt_f[fb] += 1.0;
-    if (mb >= 0) P->cnt_m[mb] += 1.0;
-    if (fb >= 0 && mb >= 0) ++h_off;
-  }
+  for (int64_t t = 0; t < TG; ++t) h_off += hoff_part[t];
+  for (int f = 0; f < P->nf; ++f)
+    for (int64_t t = 0; t < TG; ++t) P->cnt_f[f] += static_cast<double>(fcnt[t][f]);
   int64_t h_diag = 0;
   for (double c : P->cnt_f) h_diag += (c > 0);
   for (double c : P->cnt_m) h_diag += (c > 0);
   P->n_h_blocks = h_diag + h_off;
   // camera term lists and tiles
   P->cam_g_begin.assign(P->nf + 1, 0);
-  for (int64_t g = 0; g < P->ng; ++g) {
-    int fb = P->pose_fb[P->g_pose[g]];
-    if (fb >= 0) P->cam_g_begin[fb + 1]++;
+  for (int f = 0; f < P->nf; ++f) {
+    int64_t run = 0;
+    for (int64_t t = 0; t < TG; ++t) run += fcnt[t][f];
+    P->cam_g_begin[f + 1] = P->cam_g_begin[f] + run;
   }
-  for (int f = 0; f < P->nf; ++f) P->cam_g_begin[f + 1] += P->cam_g_begin[f];
   P->cam_g.assign(P->cam_g_begin[P->nf], 0);
-  {
-    std::vector<int64_t> fill(P->cam_g_begin.begin(), P->cam_g_begin.end() - 1);
-    for (int64_t g = 0; g < P->ng; ++g) {
-      int fb = P->pose_fb[P->g_pose[g]];
-      if (fb >= 0) P->cam_g[fill[fb]++] = g;
+  for (int f = 0; f < P->nf; ++f) {
+    int64_t run = P->cam_g_begin[f];
+    for (int64_t t = 0; t < TG; ++t) {
+      const int64_t c = fcnt[t][f];
+      fcnt[t][f] = run;  // chunk t's first slot in camera f's list
+      run += c;
     }
   }
+  HostPool::get().run(static_cast<int>(TG), [&](int t) {
+    std::vector<int64_t>& slot = fcnt[t];
+    for (int64_t g = P->ng * t / TG; g < P->ng * (t + 1) / TG; ++g) {
+      const int fb = P->pose_fb[P->g_pose[g]];
+      if (fb >= 0) P->cam_g[slot[fb]++] = g;
+    }
+  });
   P->tile_fb.clear();
   P->tile_begin.clear();
   P->tile_end.clear();
@@ -418,7 +589,9 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   int st;
   {
     std::vector<double2> uv(P.no);
-    for (int64_t k = 0; k < P.no; ++k) uv[k] = make_double2(desc->obs_uv[2 * P.ord[k]], desc->obs_uv[2 * P.ord[k] + 1]);
+    par_ranges(P.no, [&](int64_t b, int64_t e) {
+      for (int64_t k = b; k < e; ++k) uv[k] = make_double2(desc->obs_uv[2 * P.ord[k]], desc->obs_uv[2 * P.ord[k] + 1]);
+    });
     if ((st = dev_upload(p, &d.obs_uv, uv))) return st;
   }
   if ((st = dev_upload(p, &d.obs_pose, P.obs_pose))) return st;
