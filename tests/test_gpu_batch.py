@@ -71,3 +71,31 @@ def test_mixed_sizes_keep_launch_limits(pkg):
         second, _ = gb.optimize(params)
     assert len(first) == len(second) == 3
     assert np.isfinite(second[-1].merit)
+
+
+def test_batch_graph_reuse_and_recapture(pkg):
+    """Repeated batches over the same windows reuse the batched graphs and give
+    bit-identical results; more iterations (larger record buffers, graphs
+    captured again) still match the windows optimised one by one."""
+    wins = _windows(pkg, 4)
+    p10 = fixed_iter_params(pkg, 10, wins[0].initial_lm_damping)
+    p12 = fixed_iter_params(pkg, 12, wins[0].initial_lm_damping)
+    probs = [pkg.native.Problem(w, device=0) for w in wins]
+    try:
+        first = pkg.native.batch_optimize(probs, p10)
+        for p, w in zip(probs, wins):
+            p.set_variables(w.poses, w.points)
+        again = pkg.native.batch_optimize(probs, p10)
+        for a, b in zip(first, again):
+            assert [r.merit for r in a[0]] == [r.merit for r in b[0]] and a[3] == b[3]
+        for p, w in zip(probs, wins):
+            p.set_variables(w.poses, w.points)
+        longer = pkg.native.batch_optimize(probs, p12)
+    finally:
+        for p in probs:
+            p.close()
+    for w, (recs, term, ms, final_cost, status) in enumerate(longer):
+        assert status == pkg.native.OK and len(recs) == 12
+        with pkg.native.Problem(wins[w], device=0) as gp:
+            srecs, _ = gp.optimize(p12)
+        assert [r.merit for r in recs] == [r.merit for r in srecs]
