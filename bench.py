@@ -138,12 +138,12 @@ def _peaks():
         return 6800.0, "fallback"
 
 
-def _profile_traffic():
-    """dram bytes per launch of the roofline kernel from the committed ncu summary."""
+def _profile_traffic(workload):
+    """DRAM bytes per launch of each kernel of a workload, from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "roofline_traffic.json")
     try:
         with open(path) as f:
-            return json.load(f)
+            return json.load(f).get(workload, {})
     except Exception:
         return {}
 
@@ -476,7 +476,7 @@ def main():
     ms_per_step = out["ms"] / K
     dominant = max(kt, key=kt.get)
     hbm_peak, peak_src = _peaks()
-    traffic = _profile_traffic()
+    traffic = _profile_traffic(args.workload)
     rl_kernel = dominant if _kernel_bytes(dominant, lay, prob) is not None else max(
         (k for k in kt if _kernel_bytes(k, lay, prob) is not None), key=kt.get)
     alg = _kernel_bytes(rl_kernel, lay, prob)
