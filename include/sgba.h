@@ -176,7 +176,8 @@ typedef struct {
 enum {
   SGBA_SOLVER_DENSE_CLUSTER = 0, /* dense S in one thread-block cluster's shared memory */
   SGBA_SOLVER_BAND = 1,          /* band + dense border, float-float (sequential / loop problems) */
-  SGBA_SOLVER_DENSE_PANELS = 2   /* dense S, panel launches (large dense systems) */
+  SGBA_SOLVER_DENSE_PANELS = 2,  /* dense S, panel launches (large dense systems) */
+  SGBA_SOLVER_DENSE_SMALL = 3    /* dense S of at most 144 rows: one CTA, float-float (local windows) */
 };
 int sgba_get_layout(sgba_problem *p, sgba_layout *out);
 

@@ -709,7 +709,13 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
       if ((st = dev_alloc(p, &d.band_xw, n6))) return st;
     }
   }
-  if (s.dense_c > 0) {
+  // small systems that are not loop-shaped: the one-CTA float-float solver
+  s.small_dense = 0;
+  if (s.band_c == 0 && !loop_shaped && sgba::small_dense_setup(s.n6)) {
+    s.small_dense = 1;
+    s.dense_c = 0;
+  }
+  if (s.dense_c > 0 || s.small_dense) {
     if ((st = dev_alloc(p, &d.S2, n6 * n6))) return st;
     SGBA_CK(cudaMemset(d.S2, 0, sizeof(float2) * std::max<size_t>(n6 * n6, 1)));
   }
@@ -1024,8 +1030,9 @@ int sgba_get_layout(sgba_problem* p, sgba_layout* out) {
   int64_t np = 0;
   if (!p->plan.sb_pair_begin.empty()) np = p->plan.sb_pair_begin.back();
   out->n_schur_pairs = np;
-  out->solver = p->sz.dense_c > 0 ? SGBA_SOLVER_DENSE_CLUSTER
-                                  : (p->sz.band_c > 0 ? SGBA_SOLVER_BAND : SGBA_SOLVER_DENSE_PANELS);
+  out->solver = p->sz.small_dense   ? SGBA_SOLVER_DENSE_SMALL
+                : p->sz.dense_c > 0 ? SGBA_SOLVER_DENSE_CLUSTER
+                                    : (p->sz.band_c > 0 ? SGBA_SOLVER_BAND : SGBA_SOLVER_DENSE_PANELS);
   out->band_width = p->sz.band_c > 0 ? p->sz.band_w : 0;
   out->border_rows = p->sz.band_c > 0 ? p->sz.n6 - p->sz.band_rows : 0;
   out->float_float_lin = p->sz.lin_dd;

@@ -775,6 +775,111 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
   cl_sync();  // no CTA leaves while another may still read its shared memory
 }
 
+// ---------------------------------------------------------------------------
+// Small reduced systems (n <= kSmallMax: local windows of up to 25 cameras):
+// one CTA, S in float-float in shared memory, LDL^T with the PSD-aware pivot
+// rule and the forward substitution of b fused into it (one barrier per pivot:
+// every thread evaluates the pivot itself), then the diagonal and the
+// backward sweep.  Float-float resolves these systems without refinement; the
+// cluster kernel's fixed costs (cluster barriers, a large code footprint that
+// starts cold on each SM) dominate at this size.
+// ---------------------------------------------------------------------------
+constexpr int kSmallMax = 144;
+
+__device__ __forceinline__ dd sd_f2dd(float2 v) { return dd_make(v.x, v.y); }
+__device__ __forceinline__ float2 sd_dd2f(dd v) { return make_float2(v.hi, v.lo); }
+
+// 1/d by Newton's iteration from the hardware approximate reciprocal (one
+// FP32 step, one float-float step with an exactly formed residual).
+__device__ __forceinline__ dd sd_rcp(dd d) {
+  float r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(d.hi));
+  r0 = __fmaf_rn(r0, __fmaf_rn(-d.hi, r0, 1.0f), r0);
+  const dd p = dd_mul_f(d, r0);
+  const float e = __fsub_rn(__fsub_rn(1.0f, p.hi), p.lo);
+  return dd_fast_two_sum(r0, __fmul_rn(r0, e));
+}
+
+__global__ void __launch_bounds__(256, 1) k_small_dense(DenseArgs a, Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  extern __shared__ __align__(16) float2 sm[];
+  const int m = a.n;
+  float2* A = sm;          // m x m, lower used
+  float2* y = sm + m * m;  // rhs -> z -> x
+  float2* rdv = y + m;     // reciprocal pivots
+  __shared__ int s_bad;
+  const int tid = threadIdx.x;
+  if (tid == 0) s_bad = 0;
+  for (int e = tid; e < m * m; e += 256) {
+    const int i = e / m, j = e % m;
+    A[e] = (j <= i) ? a.S2[static_cast<int64_t>(i) * m + j] : make_float2(0.0f, 0.0f);
+  }
+  for (int i = tid; i < m; i += 256) y[i] = sd_dd2f(dd_from_double(a.b[i]));
+  __syncthreads();
+  float maxp = 1.0f;
+  for (int t = 0; t < m; ++t) {
+    dd dt = sd_f2dd(A[t * m + t]);
+    if (t % 6 == 0) maxp = 1.0f;  // a new pose block
+    const float tol = fmaxf(maxp, 1.0f) * 1e-12f;
+    bool bad = false;
+    if (!isfinite(dt.hi)) {
+      bad = true;
+      dt = dd_make(0.0f, 0.0f);
+    } else if (fabsf(dt.hi) <= tol) {
+      dt = dd_make(0.0f, 0.0f);
+    } else {
+      maxp = fmaxf(maxp, fabsf(dt.hi));
+    }
+    const dd rd = (dt.hi == 0.0f) ? dd_make(0.0f, 0.0f) : sd_rcp(dt);
+    if (tid == 0) {
+      rdv[t] = sd_dd2f(rd);
+      if (bad) s_bad = 1;
+    }
+    const int rem = m - t - 1;
+    const dd yt = sd_f2dd(y[t]);
+    // trailing entries (i, q), t < q <= i: a_iq -= a_it rd a_qt; rhs y_i -= l_it y_t
+    const int ntri = rem * (rem + 1) / 2;
+    for (int e = tid; e < ntri + rem; e += 256) {
+      if (e < ntri) {
+        int ii = static_cast<int>((__fsqrt_rn(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
+        while (ii * (ii + 1) / 2 > e) --ii;
+        while ((ii + 1) * (ii + 2) / 2 <= e) ++ii;
+        const int i = t + 1 + ii, q = t + 1 + (e - ii * (ii + 1) / 2);
+        const dd li = dd_mul(sd_f2dd(A[i * m + t]), rd);
+        const dd v = dd_sub(sd_f2dd(A[i * m + q]), dd_mul(li, sd_f2dd(A[q * m + t])));
+        A[i * m + q] = sd_dd2f(v);
+      } else {
+        const int i = t + 1 + (e - ntri);
+        const dd li = dd_mul(sd_f2dd(A[i * m + t]), rd);
+        y[i] = sd_dd2f(dd_sub(sd_f2dd(y[i]), dd_mul(li, yt)));
+      }
+    }
+    __syncthreads();
+  }
+  // L columns (a_it rd_t), the diagonal solve
+  for (int e = tid; e < m * m; e += 256) {
+    const int i = e / m, t = e % m;
+    if (t < i) A[e] = sd_dd2f(dd_mul(sd_f2dd(A[e]), sd_f2dd(rdv[t])));
+  }
+  for (int i = tid; i < m; i += 256) y[i] = sd_dd2f(dd_mul(sd_f2dd(y[i]), sd_f2dd(rdv[i])));
+  __syncthreads();
+  // backward: x_t final, then x_i -= L_ti x_t for i < t
+  for (int t = m - 1; t > 0; --t) {
+    const dd xt = sd_f2dd(y[t]);
+    for (int i = tid; i < t; i += 256) y[i] = sd_dd2f(dd_sub(sd_f2dd(y[i]), dd_mul(sd_f2dd(A[t * m + i]), xt)));
+    __syncthreads();
+  }
+  for (int i = tid; i < m; i += 256) {
+    const dd v = sd_f2dd(y[i]);
+    a.x[i] = dd_to_double(v);
+    a.xdd[2 * i] = v.hi;
+    a.xdd[2 * i + 1] = v.lo;
+  }
+  if (tid == 0 && s_bad) ctrl->skip = 2;  // NonFinitePivot -> solve failure -> reject
+}
+
+size_t small_dense_smem(int n) { return sizeof(float2) * (static_cast<size_t>(n) * n + 2 * static_cast<size_t>(n)); }
+
 size_t dense_smem_bytes(int P, int C) {
   size_t m = 0;
   for (int r = 0; r < C; ++r) {
@@ -836,6 +941,27 @@ int dense_cluster_setup(int n, int* cluster, size_t* smem) {
     return C;
   }
   return 0;
+}
+
+int small_dense_setup(int n) {
+  if (n <= 0 || n > kSmallMax) return 0;
+  if (raise_dynamic_smem(reinterpret_cast<const void*>(k_small_dense), small_dense_smem(n)) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return 1;
+}
+
+int launch_small_dense(const Sizes& s, const Dev& d, cudaStream_t st) {
+  DenseArgs a{};
+  a.n = s.n6;
+  a.P = (s.n6 + kNB - 1) / kNB;
+  a.S2 = d.S2;
+  a.b = d.rb;
+  a.x = d.x;
+  a.xdd = d.xdd;
+  k_small_dense<<<1, 256, small_dense_smem(s.n6), st>>>(a, d.ctrl);
+  return 1;
 }
 
 int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st) {

@@ -170,6 +170,7 @@ struct Sizes {
   double huber;
   int gauge_kind;
   double gauge_center[3];
+  int small_dense;    // 1: one-CTA float-float solver (small systems)
   int dense_c;        // cluster size of the single-launch dense solver, 0 = multi-launch path
   size_t dense_smem;  // its dynamic shared memory per CTA
   int band_rows;      // banded solver: rows of the band part (0 = not used)
@@ -204,6 +205,9 @@ int solver_launch_count(const Sizes& s);
 // order n (0 = does not fit) and enqueues the factorization + refined solve.
 int dense_cluster_setup(int n, int* cluster, size_t* smem);
 int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st);
+// Small systems (local windows): one CTA, float-float LDL^T (1 = usable).
+int small_dense_setup(int n);
+int launch_small_dense(const Sizes& s, const Dev& d, cudaStream_t st);
 
 // Raise a kernel's dynamic shared memory limit to at least `bytes` on the
 // current device.  The limit is a per-function, per-device setting shared by

@@ -12,7 +12,7 @@
 //   k_pair_totals   pairs per lower block (atomic counts; order-free);
 //   (host)          the block pattern, block offsets;
 //   k_pair_count    pairs per (point chunk, block);
-//   k_pair_scan     exclusive scan over the chunks of each block;
+//   k_pair_scan     exclusive scan over the chunks of each block (one warp per block);
 //   k_pair_fill     one CTA per point chunk walks its points in order, each
 //                   point's pairs in parallel (they fall into distinct blocks).
 // The order is (block, point), exactly the order of a sequential build.
@@ -92,12 +92,25 @@ __global__ void __launch_bounds__(256) k_pair_count(PairArgs a) {
   }
 }
 
-// One thread per block: table[c][b] <- first pair slot of chunk c in block b.
+// One warp per block b: table[c][b] <- first pair slot of chunk c in block b
+// (an exclusive scan over the chunks: each lane sums a run of chunks, a warp
+// scan of the run totals, then each lane writes its run).
 __global__ void __launch_bounds__(256) k_pair_scan(PairArgs a, const int64_t* block_begin) {
-  for (int64_t b = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; b < a.nb;
-       b += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    int64_t run = block_begin[b];
-    for (int c = 0; c < a.nchunk; ++c) {
+  const int lane = threadIdx.x & 31;
+  const int per = (a.nchunk + 31) / 32;
+  const int c0 = min(a.nchunk, lane * per), c1 = min(a.nchunk, c0 + per);
+  for (int64_t b = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; b < a.nb;
+       b += (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5) {
+    int64_t own = 0;
+    for (int c = c0; c < c1; ++c) own += a.table[static_cast<int64_t>(c) * a.nb + b];
+    int64_t incl = own;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const int64_t v = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += v;
+    }
+    int64_t run = block_begin[b] + incl - own;
+    for (int c = c0; c < c1; ++c) {
       int32_t* e = a.table + static_cast<int64_t>(c) * a.nb + b;
       const int32_t v = *e;
       *e = static_cast<int32_t>(run);
@@ -166,7 +179,8 @@ cudaError_t pair_fill(const Sizes& s, const Dev& d, const int32_t* bidmap, int64
   if (blocks > 8192) blocks = 8192;
   if (blocks < 1) blocks = 1;
   k_pair_count<<<blocks, 256, 0, st>>>(a);
-  int sb = static_cast<int>((nb + 255) / 256);
+  int sb = static_cast<int>((nb * 32 + 255) / 256);
+  if (sb > 8192) sb = 8192;
   if (sb < 1) sb = 1;
   k_pair_scan<<<sb, 256, 0, st>>>(a, block_begin);
   k_pair_fill<<<nchunk, 256, 0, st>>>(a);

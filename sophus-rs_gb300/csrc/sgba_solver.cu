@@ -267,6 +267,7 @@ __global__ void __launch_bounds__(256) k_residual(int n, const double* __restric
 }  // namespace
 
 int solver_launch_count(const Sizes& s) {
+  if (s.small_dense) return 1;
   if (s.dense_c > 0) return 1;
   if (s.band_c > 0) return band_launch_count();
   const int panels = (s.n6 + kPW - 1) / kPW;
@@ -274,6 +275,7 @@ int solver_launch_count(const Sizes& s) {
 }
 
 int launch_factor_solve(const Sizes& s, const Dev& d, cudaStream_t st) {
+  if (s.small_dense) return launch_small_dense(s, d, st);
   if (s.dense_c > 0) return launch_dense_cluster(s, d, st);
   if (s.band_c > 0) return launch_band(s, d, st);
   const int n = s.n6;

@@ -35,6 +35,7 @@ TERM_MAX_CONSECUTIVE_REJECTS = 5
 SOLVER_DENSE_CLUSTER = 0
 SOLVER_BAND = 1
 SOLVER_DENSE_PANELS = 2
+SOLVER_DENSE_SMALL = 3
 
 
 class ProblemDesc(C.Structure):
