@@ -39,6 +39,8 @@ struct Ctrl {
   int fail;             // a point block failed its Cholesky this iteration
   unsigned long long max_grad_bits;  // atomicMax over non-negative doubles
   unsigned long long max_step_bits;
+  int fin_ticket;   // k_camera_finalize: blocks done (the last one runs the gradient check)
+  int cost_ticket;  // trial k_cost: blocks done (the last one runs the LM decision)
 };
 
 // Per-step record, layout-identical to sgba_iter_record.

@@ -271,19 +271,12 @@ __device__ void jacobians_dd(const float* Pd /*R_cw 9 + t_cw 3, (hi, lo) pairs*/
 // ---------------------------------------------------------------------------
 // Pose tables: T_cw = T_wc^-1 in f64, published as float and float-float.
 // ---------------------------------------------------------------------------
-__global__ void k_pose_tables(int nc, const double* __restrict__ poses, float* __restrict__ pose_f,
-                              float* __restrict__ pose_dd, const Ctrl* ctrl, int respect_skip) {
-  if (respect_skip ? skipping(ctrl) : halted(ctrl)) return;
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= nc) return;
-  const double* T = poses + 7 * j;
+__device__ __forceinline__ void pose_table(const double* T, float* pf, float* pd) {
   double qc[4] = {T[0], -T[1], -T[2], -T[3]};
   double R[9];
   rot_matrix(qc, R);
   double t[3];
   for (int i = 0; i < 3; ++i) t[i] = -(R[i * 3 + 0] * T[4] + R[i * 3 + 1] * T[5] + R[i * 3 + 2] * T[6]);
-  float* pf = pose_f + 12 * j;
-  float* pd = pose_dd + 24 * j;
   for (int i = 0; i < 9; ++i) {
     pf[i] = __double2float_rn(R[i]);
     dd v = dd_from_double(R[i]);
@@ -296,6 +289,26 @@ __global__ void k_pose_tables(int nc, const double* __restrict__ poses, float* _
     pd[18 + 2 * i] = v.hi;
     pd[18 + 2 * i + 1] = v.lo;
   }
+}
+
+// Pose tables of every camera.  With `begin` set (the first kernel of an LM
+// iteration) thread 0 also opens the iteration: clears the step flags and
+// maxima and the count of points queued for the float-float redo.
+__global__ void k_pose_tables(int nc, const double* __restrict__ poses, float* __restrict__ pose_f,
+                              float* __restrict__ pose_dd, const Ctrl* ctrl, int respect_skip, Ctrl* begin,
+                              int32_t* zero_count) {
+  if (respect_skip ? skipping(ctrl) : halted(ctrl)) return;
+  if (begin && blockIdx.x == 0 && threadIdx.x == 0) {
+    begin->skip = 0;
+    begin->accept = 0;
+    begin->max_grad_bits = 0ull;
+    begin->max_step_bits = 0ull;
+    begin->alpha = 0.0;
+    if (zero_count) *zero_count = 0;
+  }
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= nc) return;
+  pose_table(poses + 7 * j, pose_f + 12 * j, pose_dd + 24 * j);
 }
 
 // ---------------------------------------------------------------------------
@@ -316,9 +329,23 @@ struct CostArgs {
   float huber;
   dd huber_dd;
   int respect_skip;
+  // trial cost of an LM iteration: the last block to finish runs the decision
+  Ctrl* decide;  // null: no decision
+  const double* upd_part;
+  int n_upd;
+  Record* recs;
+  Record* last;
 };
 
+__device__ void decide_body(const double* cost_part, int n_cost, const double* upd_part, int n_upd, Ctrl* ctrl,
+                            Record* recs, Record* last);
+
 __global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* ctrl) {
+  if (a.decide && !halted(ctrl) && skipping(ctrl)) {
+    // no trial (gradient tolerance or a failed solve): decide at once
+    if (blockIdx.x == 0) decide_body(a.partials, 0, a.upd_part, a.n_upd, a.decide, a.recs, a.last);
+    return;
+  }
   if (a.respect_skip ? skipping(ctrl) : halted(ctrl)) return;
   dd acc = dd_make(0.0f, 0.0f);
   for (int64_t o = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; o < a.no;
@@ -365,6 +392,17 @@ __global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* c
     v = dd_warp_sum(v);
     if (lane == 0) a.partials[blockIdx.x] = dd_to_double(v);
   }
+  if (a.decide) {
+    __shared__ bool s_last;
+    __threadfence();
+    if (threadIdx.x == 0) s_last = (atomicAdd(&a.decide->cost_ticket, 1) == static_cast<int>(gridDim.x) - 1);
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      if (threadIdx.x == 0) a.decide->cost_ticket = 0;
+      decide_body(a.partials, static_cast<int>(gridDim.x), a.upd_part, a.n_upd, a.decide, a.recs, a.last);
+    }
+  }
 }
 
 // Sum n double partials with one CTA (fixed tree, float-float).
@@ -394,14 +432,6 @@ __global__ void k_init_merit(const double* part, int n, Ctrl* ctrl) {
   }
 }
 
-__global__ void k_iter_begin(Ctrl* ctrl) {
-  if (halted(ctrl)) return;
-  ctrl->skip = 0;
-  ctrl->accept = 0;
-  ctrl->max_grad_bits = 0ull;
-  ctrl->max_step_bits = 0ull;
-  ctrl->alpha = 0.0;
-}
 
 // ---------------------------------------------------------------------------
 // Landmark pass: one warp per marginalized point.  Builds the point block
@@ -1110,21 +1140,29 @@ __global__ void __launch_bounds__(64) k_camera_finalize(int nf, const int64_t* f
     for (int p = 0; p < 6; ++p) mg = fmax(mg, fabs(vals[21 + p]));
     atomic_max_nonneg(&ctrl->max_grad_bits, mg);
   }
+  if (with_schur) {
+    // the last block to finish: gradient-tolerance check before the solve
+    // (optimizer_step.rs:382-384) and singular point blocks (SingularMargBlock
+    // -> reject); every block's maximum is in by then
+    __shared__ bool s_last;
+    __threadfence();
+    if (k == 0) s_last = (atomicAdd(&ctrl->fin_ticket, 1) == static_cast<int>(gridDim.x) - 1);
+    __syncthreads();
+    if (s_last && k == 0) {
+      __threadfence();
+      const double mg = __longlong_as_double(static_cast<long long>(atomicAdd(&ctrl->max_grad_bits, 0ull)));
+      ctrl->max_grad = mg;
+      if (mg < ctrl->gtol) {
+        ctrl->skip = 1;
+      } else if (ctrl->fail) {
+        ctrl->skip = 2;
+      }
+      ctrl->fail = 0;
+      ctrl->fin_ticket = 0;
+    }
+  }
 }
 
-// Gradient-tolerance check before the solve (optimizer_step.rs:382-384) and
-// singular-point-block detection (SingularMargBlock -> reject).
-__global__ void k_gradcheck(Ctrl* ctrl, int* fail) {
-  if (halted(ctrl)) return;
-  double mg = __longlong_as_double(static_cast<long long>(ctrl->max_grad_bits));
-  ctrl->max_grad = mg;
-  if (mg < ctrl->gtol) {
-    ctrl->skip = 1;
-  } else if (*fail) {
-    ctrl->skip = 2;
-  }
-  *fail = 0;
-}
 
 // ---------------------------------------------------------------------------
 // Reduced camera system: one warp per lower 6x6 block (row j >= col k).
@@ -1470,20 +1508,6 @@ __global__ void __launch_bounds__(256) k_gauge_partials(GaugeArgs a, const Ctrl*
   }
 }
 
-__global__ void k_gauge_alpha(const double* part, int nblocks, Ctrl* ctrl) {
-  if (skipping(ctrl)) return;
-  dd n = dd_make(0.f, 0.f), d = dd_make(0.f, 0.f);
-  for (int q = threadIdx.x; q < nblocks; q += 32) {
-    n = dd_add(n, dd_from_double(part[2 * q]));
-    d = dd_add(d, dd_from_double(part[2 * q + 1]));
-  }
-  n = dd_warp_sum(n);
-  d = dd_warp_sum(d);
-  if (threadIdx.x == 0) {
-    const double sn = dd_to_double(n), sd = dd_to_double(d);
-    ctrl->alpha = (sd > 0.0) ? sn / sd : 0.0;
-  }
-}
 
 // ---------------------------------------------------------------------------
 // Apply the (projected) step: trial poses exp(delta) * T, trial points p + d
@@ -1505,11 +1529,36 @@ struct UpdArgs {
   int gauge_kind;
   double cx, cy, cz;
   double* part;  // 2 * gridDim
+  const double* gauge_part;  // 2 * gauge_blocks partial sums of the gauge projection
+  int gauge_blocks;
+  float* pose_f;   // trial pose tables, written here for the trial cost
+  float* pose_dd;
 };
 
 __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
   if (skipping(ctrl)) return;
-  const double alpha = (a.gauge_kind == 1) ? ctrl->alpha : 0.0;
+  // gauge coefficient alpha = sum num / sum den over the k_gauge_partials
+  // blocks, formed identically in every CTA (fixed order, warp 0)
+  __shared__ double s_alpha;
+  double alpha = 0.0;
+  if (a.gauge_kind == 1) {
+    if (threadIdx.x < 32) {
+      dd n = dd_make(0.f, 0.f), d = dd_make(0.f, 0.f);
+      for (int q = threadIdx.x; q < a.gauge_blocks; q += 32) {
+        n = dd_add(n, dd_from_double(a.gauge_part[2 * q]));
+        d = dd_add(d, dd_from_double(a.gauge_part[2 * q + 1]));
+      }
+      n = dd_warp_sum(n);
+      d = dd_warp_sum(d);
+      if (threadIdx.x == 0) {
+        const double sn = dd_to_double(n), sd = dd_to_double(d);
+        s_alpha = (sd > 0.0) ? sn / sd : 0.0;
+      }
+    }
+    __syncthreads();
+    alpha = s_alpha;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->alpha = alpha;
+  }
   dd sdd = dd_make(0.f, 0.f), sdg = dd_make(0.f, 0.f);
   double mx = 0.0;
   const int64_t n = static_cast<int64_t>(a.nc) + a.np;
@@ -1522,6 +1571,7 @@ __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
       const int fb = a.pose_fb[j];
       if (fb < 0) {
         for (int k = 0; k < 7; ++k) O[k] = T[k];
+        pose_table(O, a.pose_f + 12 * j, a.pose_dd + 24 * j);
         continue;
       }
       double xi[6];
@@ -1537,6 +1587,7 @@ __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
         mx = fmax(mx, fabs(xi[k]));
       }
       se3_left_update(xi, T, O);
+      pose_table(O, a.pose_f + 12 * j, a.pose_dd + 24 * j);
     } else {
       const int i = static_cast<int>(t - a.nc);
       const double* p = a.points + 3 * i;
@@ -1588,9 +1639,8 @@ __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
 // LM decision (step_nlls_inner, crates/sophus_opt/src/nlls/optimizer_step.rs:366-437;
 // accept/reject optimizer.rs:463-480; gain ratio optimizer_helpers.rs:159-173).
 // ---------------------------------------------------------------------------
-__global__ void k_decide(const double* cost_part, int n_cost, const double* upd_part, int n_upd,
-                         Ctrl* ctrl, Record* recs, Record* last) {
-  if (halted(ctrl)) return;
+__device__ void decide_body(const double* cost_part, int n_cost, const double* upd_part, int n_upd, Ctrl* ctrl,
+                            Record* recs, Record* last) {
   const int skip = ctrl->skip;
   double new_merit = 0.0;
   if (skip == 0) new_merit = block_sum_partials(cost_part, n_cost);
@@ -1711,7 +1761,7 @@ constexpr int kUpdBlocks = 152;
 int cost_partials_needed(const Sizes& s) { return 4 * kUpdBlocks + cost_grid(s.no); }
 
 int launch_pose_tables(const Sizes& s, const Dev& d, const double* poses, cudaStream_t st) {
-  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, poses, d.pose_f, d.pose_dd, d.ctrl, 0);
+  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, poses, d.pose_f, d.pose_dd, d.ctrl, 0, nullptr, nullptr);
   return 1;
 }
 
@@ -1734,19 +1784,24 @@ static CostArgs make_cost_args(const Sizes& s, const Dev& d, const double* point
   a.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
   a.huber_dd = dd_make(static_cast<float>(s.huber), static_cast<float>(s.huber - static_cast<float>(s.huber)));
   a.respect_skip = respect_skip;
+  a.decide = nullptr;
+  a.upd_part = nullptr;
+  a.n_upd = 0;
+  a.recs = nullptr;
+  a.last = nullptr;
   return a;
 }
 
 int launch_cost(const Sizes& s, const Dev& d, const double* poses, const double* points,
                 float2* res_out, double* partials, cudaStream_t st) {
-  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, poses, d.pose_f, d.pose_dd, d.ctrl, 1);
+  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, poses, d.pose_f, d.pose_dd, d.ctrl, 1, nullptr, nullptr);
   CostArgs a = make_cost_args(s, d, points, res_out, partials, 1);
   k_cost<<<cost_grid(s.no), kCostThreads, 0, st>>>(a, d.ctrl);
   return 2;
 }
 
 int launch_init_merit(const Sizes& s, const Dev& d, cudaStream_t st) {
-  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses, d.pose_f, d.pose_dd, d.ctrl, 0);
+  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses, d.pose_f, d.pose_dd, d.ctrl, 0, nullptr, nullptr);
   CostArgs a = make_cost_args(s, d, d.points, d.res, d.part, 0);
   const int nb = cost_grid(s.no);
   k_cost<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
@@ -1755,9 +1810,11 @@ int launch_init_merit(const Sizes& s, const Dev& d, cudaStream_t st) {
 }
 
 int launch_iteration_begin(const Sizes& s, const Dev& d, cudaStream_t st) {
+  // the iteration is opened by the first kernel of launch_linearize
   (void)s;
-  k_iter_begin<<<1, 1, 0, st>>>(d.ctrl);
-  return 1;
+  (void)d;
+  (void)st;
+  return 0;
 }
 
 static LinArgs make_lin_args(const Sizes& s, const Dev& d, double nu_override, bool use_override) {
@@ -1857,9 +1914,9 @@ static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
 // Landmark pass: the chunked kernel plus the float-float redo of the points it
 // queued, or (final Hessian pass, no chunk table, or the float-float
 // linearization) the warp-per-point kernel.
-static int launch_landmark(const Sizes& s, const Dev& d, LinArgs la, cudaStream_t st) {
+static int launch_landmark(const Sizes& s, const Dev& d, LinArgs la, cudaStream_t st, bool zero_slow = true) {
   if (!la.use_override && s.nlchunk > 0 && !s.lin_dd) {
-    cudaMemsetAsync(d.slow_count, 0, sizeof(int32_t), st);
+    if (zero_slow) cudaMemsetAsync(d.slow_count, 0, sizeof(int32_t), st);
     const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
     k_landmark_chunks<<<grid, 256, sizeof(float) * 9 * static_cast<size_t>(s.lmk_cap), st>>>(la, d.ctrl);
     LinArgs lb = la;
@@ -1884,17 +1941,17 @@ int landmark_setup(int cap) {
 int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_override,
                      cudaStream_t st) {
   int n = 0;
-  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses, d.pose_f, d.pose_dd, d.ctrl, 0);
+  // an LM iteration (not the final linearisation) is opened here
+  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses, d.pose_f, d.pose_dd, d.ctrl, 0,
+                                                    use_override ? nullptr : d.ctrl,
+                                                    use_override ? nullptr : d.slow_count);
   ++n;
-  n += launch_landmark(s, d, make_lin_args(s, d, nu_override, use_override), st);
+  n += launch_landmark(s, d, make_lin_args(s, d, nu_override, use_override), st, use_override);
   n += launch_camera(s, d, use_override ? 0 : 1, st);
+  // the last block of the finalisation runs the gradient check of an LM iteration
   k_camera_finalize<<<s.nf, 64, 0, st>>>(s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf, d.rb, d.ctrl,
                                          use_override ? 0 : 1);
   ++n;
-  if (!use_override) {
-    k_gradcheck<<<1, 1, 0, st>>>(d.ctrl, &d.ctrl->fail);
-    ++n;
-  }
   return n;
 }
 
@@ -1942,8 +1999,7 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
     g.cz = s.gauge_center[2];
     g.part = d.part;
     k_gauge_partials<<<kUpdBlocks, 256, 0, st>>>(g, d.ctrl);
-    k_gauge_alpha<<<1, 32, 0, st>>>(d.part, kUpdBlocks, d.ctrl);
-    n += 2;
+    n += 1;
   }
   UpdArgs u;
   u.nc = s.nc;
@@ -1965,6 +2021,10 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
   u.cy = s.gauge_center[1];
   u.cz = s.gauge_center[2];
   u.part = d.part + 2 * kUpdBlocks;
+  u.gauge_part = d.part;
+  u.gauge_blocks = kUpdBlocks;
+  u.pose_f = d.pose_f;
+  u.pose_dd = d.pose_dd;
   k_apply_update<<<kUpdBlocks, 256, 0, st>>>(u, d.ctrl);
   ++n;
   return n;
@@ -1993,14 +2053,17 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) 
 }
 
 int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
-  // trial cost (partials after the update partials)
+  // trial cost (partials after the update partials; the trial pose tables
+  // were written by k_apply_update); its last block runs the LM decision
   double* cost_part = d.part + 4 * kUpdBlocks;
   const int nb = cost_grid(s.no);
-  k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses_t, d.pose_f, d.pose_dd, d.ctrl, 1);
   CostArgs a = make_cost_args(s, d, d.points_t, d.res_t, cost_part, 1);
+  a.decide = d.ctrl;
+  a.upd_part = d.part + 2 * kUpdBlocks;
+  a.n_upd = kUpdBlocks;
+  a.recs = d.records;
+  a.last = d.last_rec;
   k_cost<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
-  k_decide<<<1, 256, 0, st>>>(cost_part, nb, d.part + 2 * kUpdBlocks, kUpdBlocks, d.ctrl, d.records,
-                              d.last_rec);
   const int64_t big = s.no > 7 * (int64_t)s.nc ? s.no : 7 * (int64_t)s.nc;
   const int64_t items = big > 3 * (int64_t)s.np ? big : 3 * (int64_t)s.np;
   int cb = static_cast<int>((items + 255) / 256);
@@ -2008,7 +2071,7 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
   if (cb < 1) cb = 1;
   k_commit<<<cb, 256, 0, st>>>(s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res,
                                d.res_lo_t, d.res_lo, d.ctrl);
-  return 4;
+  return 2;
 }
 
 // ---------------------------------------------------------------------------
@@ -2135,7 +2198,7 @@ cudaError_t launch_total_cost_noalloc(int32_t nc, const double* poses, int32_t n
   float* pose_f = reinterpret_cast<float*>(base + kNoAllocPoseFOff);
   float* pose_dd = reinterpret_cast<float*>(base + kNoAllocPoseDDOff);
   double* part = reinterpret_cast<double*>(base + kNoAllocPartOff);
-  k_pose_tables<<<(nc + 127) / 128, 128, 0, st>>>(nc, poses, pose_f, pose_dd, zero_ctrl, 0);
+  k_pose_tables<<<(nc + 127) / 128, 128, 0, st>>>(nc, poses, pose_f, pose_dd, zero_ctrl, 0, nullptr, nullptr);
   auto split = [](double x) { return dd_make(static_cast<float>(x), static_cast<float>(x - static_cast<float>(x))); };
   CostArgs a;
   a.no = no;
@@ -2146,6 +2209,7 @@ cudaError_t launch_total_cost_noalloc(int32_t nc, const double* poses, int32_t n
   a.points = points;
   a.res_out = nullptr;
   a.res_lo_out = nullptr;
+  a.decide = nullptr;
   a.partials = part;
   a.fx = split(intr[0]);
   a.fy = split(intr[1]);
