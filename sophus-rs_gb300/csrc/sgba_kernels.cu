@@ -502,6 +502,10 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
     const float py = __double2float_rn(a.points[3 * i + 1]);
     const float pz = __double2float_rn(a.points[3 * i + 2]);
     const int64_t g0 = a.pt_g_begin[i], g1 = a.pt_g_begin[i + 1];
+    dd Vd[6], b[3];
+    bool well = false;
+    float c00 = 0.f, c10 = 0.f, c20 = 0.f, c11 = 0.f, c21 = 0.f, t11 = 0.f, t22 = 0.f;  // FP32 Cholesky
+    if (!a.force_dd) {  // the float-float linearization skips the FP32 pass
     float v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // V00 V01 V02 V11 V12 V22, g0 g1 g2
     for (int64_t g = g0 + lane; g < g1; g += 32) {
       const float* P = a.pose_f + 12 * a.g_pose[g];
@@ -533,7 +537,6 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
       red[wib][1][lane] = tot.lo;
     }
     __syncwarp();
-    dd Vd[6], b[3];
 #pragma unroll
     for (int k = 0; k < 6; ++k) Vd[k] = dd_make(red[wib][0][k], red[wib][1][k]);
 #pragma unroll
@@ -553,13 +556,15 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
     float V[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) V[k] = Vd[k].hi + Vd[k].lo;
-    float c00 = sqrtf(V[0]);
-    float c10 = V[1] / c00, c20 = V[2] / c00;
-    float t11 = V[3] - c10 * c10;
-    float c11 = sqrtf(t11);
-    float c21 = (V[4] - c20 * c10) / c11;
-    float t22 = V[5] - c20 * c20 - c21 * c21;
-    const bool well = !a.list && !a.force_dd && V[0] > 0.f && t11 > a.well_tol * V[3] && t22 > a.well_tol * V[5];
+    c00 = sqrtf(V[0]);
+    c10 = V[1] / c00;
+    c20 = V[2] / c00;
+    t11 = V[3] - c10 * c10;
+    c11 = sqrtf(t11);
+    c21 = (V[4] - c20 * c10) / c11;
+    t22 = V[5] - c20 * c20 - c21 * c21;
+    well = !a.list && V[0] > 0.f && t11 > a.well_tol * V[3] && t22 > a.well_tol * V[5];
+    }
     const dd pxd = dd_from_double(a.points[3 * i + 0]);
     const dd pyd = dd_from_double(a.points[3 * i + 1]);
     const dd pzd = dd_from_double(a.points[3 * i + 2]);
@@ -608,6 +613,7 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
         bp[0] = dd_to_double(b[0]);
         bp[1] = dd_to_double(b[1]);
         bp[2] = dd_to_double(b[2]);
+        if (a.force_dd) warp_max = fmax(warp_max, fmax(fabs(bp[0]), fmax(fabs(bp[1]), fabs(bp[2]))));
       }
     }
     dd I[6];  // C^-1 (00 10 11 20 21 22)
