@@ -598,17 +598,20 @@ __global__ void __launch_bounds__(128) k_band_corner(BandArgs a, const Ctrl* ctr
   }
 }
 
-// One CTA: LDL^T of the corner (PSD-aware pivots), then x_C.
+// One CTA: LDL^T of the corner (PSD-aware pivots) with the forward
+// substitution of y_C fused into it, then the diagonal and the backward sweep.
+// Every thread evaluates each pivot itself (same inputs, same operations), so
+// a pivot costs one barrier; column t is scaled to L after the factorization
+// (later pivots do not touch it).
 __global__ void __launch_bounds__(kBT) k_band_corner_solve(BandArgs a, Ctrl* ctrl) {
   if (skipping(ctrl)) return;
-  extern __shared__ __align__(16) float2 cm[];  // nbd x nbd (lower), then y (nbd)
-  __shared__ float2 sdv, srdv;
-  __shared__ float smax;
+  extern __shared__ __align__(16) float2 cm[];  // nbd x nbd (lower), then y (nbd), then 1/d (nbd)
   __shared__ int sbad;
   const int m = a.nbd;
   const int tid = threadIdx.x;
   if (m == 0) return;
   float2* y = cm + m * m;
+  float2* rdv = y + m;
   const int64_t ld = m + 1;
   for (int e = tid; e < m * m; e += kBT) {
     const int i = e / m, j = e % m;
@@ -617,76 +620,65 @@ __global__ void __launch_bounds__(kBT) k_band_corner_solve(BandArgs a, Ctrl* ctr
   for (int j = tid; j < m; j += kBT) y[j] = a.Cn[static_cast<int64_t>(m) * ld + j];
   if (tid == 0) sbad = 0;
   __syncthreads();
+  float maxp = 1.0f;
   for (int t = 0; t < m; ++t) {
+    dd dt = f2dd(cm[t * m + t]);
+    if ((a.nband + t) % 6 == 0) maxp = 1.0f;
+    const float tol = fmaxf(maxp, 1.0f) * kTolRel;
+    bool bad = false;
+    if (!isfinite(dt.hi)) {
+      bad = true;
+      dt = dd_make(0.0f, 0.0f);
+    } else if (fabsf(dt.hi) <= tol) {
+      dt = dd_make(0.0f, 0.0f);
+    } else {
+      maxp = fmaxf(maxp, fabsf(dt.hi));
+    }
+    const dd rd = (dt.hi == 0.0f) ? dd_make(0.0f, 0.0f) : dd_rcp(dt);
     if (tid == 0) {
-      dd dt = f2dd(cm[t * m + t]);
-      if ((a.nband + t) % 6 == 0) smax = 1.0f;
-      const float tol = fmaxf(smax, 1.0f) * kTolRel;
-      if (!isfinite(dt.hi)) {
-        sbad = 1;
-        dt = dd_make(0.0f, 0.0f);
-      } else if (fabsf(dt.hi) <= tol) {
-        dt = dd_make(0.0f, 0.0f);
-      } else {
-        smax = fmaxf(smax, fabsf(dt.hi));
-      }
-      sdv = dd2f(dt);
-      srdv = dd2f(dt.hi == 0.0f ? dd_make(0.0f, 0.0f) : dd_rcp(dt));
-      a.dpiv[a.nband + t] = sdv;
-      a.rdpiv[a.nband + t] = srdv;
+      a.dpiv[a.nband + t] = dd2f(dt);
+      a.rdpiv[a.nband + t] = dd2f(rd);
+      rdv[t] = dd2f(rd);
+      if (bad) sbad = 1;
     }
-    __syncthreads();
-    const dd rd = f2dd(srdv);
     const int rem = m - t - 1;
-    for (int e = tid; e < rem * (rem + 1) / 2; e += kBT) {
-      int ii = static_cast<int>((__fsqrt_rn(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
-      while (ii * (ii + 1) / 2 > e) --ii;
-      while ((ii + 1) * (ii + 2) / 2 <= e) ++ii;
-      const int i = t + 1 + ii, k = t + 1 + (e - ii * (ii + 1) / 2);
-      const dd li = dd_mul(f2dd(cm[i * m + t]), rd);
-      Acc acc = acc_init(f2dd(cm[i * m + k]));
-      acc_madd(acc, dd_neg(li), f2dd(cm[k * m + t]));
-      cm[i * m + k] = dd2f(acc_get(acc));
+    const int ntri = rem * (rem + 1) / 2;
+    const dd yt = f2dd(y[t]);
+    for (int e = tid; e < ntri + rem; e += kBT) {
+      if (e < ntri) {  // trailing (i, k), t < k <= i: a_ik -= a_it rd a_kt
+        int ii = static_cast<int>((__fsqrt_rn(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
+        while (ii * (ii + 1) / 2 > e) --ii;
+        while ((ii + 1) * (ii + 2) / 2 <= e) ++ii;
+        const int i = t + 1 + ii, k = t + 1 + (e - ii * (ii + 1) / 2);
+        const dd li = dd_mul(f2dd(cm[i * m + t]), rd);
+        Acc acc = acc_init(f2dd(cm[i * m + k]));
+        acc_madd(acc, dd_neg(li), f2dd(cm[k * m + t]));
+        cm[i * m + k] = dd2f(acc_get(acc));
+      } else {         // forward substitution: y_i -= l_it y_t
+        const int i = t + 1 + (e - ntri);
+        const dd li = dd_mul(f2dd(cm[i * m + t]), rd);
+        Acc acc = acc_init(f2dd(y[i]));
+        acc_madd(acc, dd_neg(li), yt);
+        y[i] = dd2f(acc_get(acc));
+      }
     }
     __syncthreads();
-    for (int i = t + 1 + tid; i < m; i += kBT) cm[i * m + t] = dd2f(dd_mul(f2dd(cm[i * m + t]), rd));
+  }
+  for (int e = tid; e < m * m; e += kBT) {
+    const int i = e / m, t = e % m;
+    if (t < i) cm[e] = dd2f(dd_mul(f2dd(cm[e]), f2dd(rdv[t])));
+  }
+  for (int i = tid; i < m; i += kBT) y[i] = dd2f(dd_mul(f2dd(y[i]), f2dd(rdv[i])));
+  __syncthreads();
+  for (int t = m - 1; t > 0; --t) {  // x_t final: x_i -= L_ti x_t for i < t
+    const dd xt = f2dd(y[t]);
+    for (int i = tid; i < t; i += kBT) {
+      Acc acc = acc_init(f2dd(y[i]));
+      acc_madd(acc, dd_neg(f2dd(cm[t * m + i])), xt);
+      y[i] = dd2f(acc_get(acc));
+    }
     __syncthreads();
   }
-  // L_E D_E L_E^T x = y: forward, diagonal, backward (one warp per step)
-  __shared__ float2 red[32];
-  const int lane = tid & 31;
-  for (int i = 0; i < m; ++i) {
-    if (tid < 32) {
-      Acc acc = acc_init(dd_make(0.0f, 0.0f));
-      for (int k = lane; k < i; k += 32) acc_madd(acc, f2dd(cm[i * m + k]), f2dd(y[k]));
-      red[lane] = dd2f(acc_get(acc));
-      __syncwarp();
-      if (lane == 0) {
-        Acc t = acc_init(f2dd(y[i]));
-        for (int l = 0; l < 32; ++l) acc_add(t, dd_neg(f2dd(red[l])));
-        y[i] = dd2f(acc_get(t));
-      }
-      __syncwarp();
-    }
-  }
-  __syncthreads();
-  for (int i = tid; i < m; i += kBT) y[i] = dd2f(dd_mul(f2dd(y[i]), f2dd(a.rdpiv[a.nband + i])));
-  __syncthreads();
-  for (int i = m - 1; i >= 0; --i) {
-    if (tid < 32) {
-      Acc acc = acc_init(dd_make(0.0f, 0.0f));
-      for (int k = i + 1 + lane; k < m; k += 32) acc_madd(acc, f2dd(cm[k * m + i]), f2dd(y[k]));
-      red[lane] = dd2f(acc_get(acc));
-      __syncwarp();
-      if (lane == 0) {
-        Acc t = acc_init(f2dd(y[i]));
-        for (int l = 0; l < 32; ++l) acc_add(t, dd_neg(f2dd(red[l])));
-        y[i] = dd2f(acc_get(t));
-      }
-      __syncwarp();
-    }
-  }
-  __syncthreads();
   for (int i = tid; i < m; i += kBT) a.xw[a.nband + i] = y[i];
   if (tid == 0 && sbad) ctrl->skip = 2;
 }
@@ -864,7 +856,7 @@ int band_setup(int n, int nband, int W, int* cluster, int* ring) {
   const size_t sweep = band_sweep_smem(nband, W);
   if (sweep > kSmemLimit - 4096) return 0;
   const int m = n - nband;
-  const size_t corner = sizeof(float2) * static_cast<size_t>(m) * (m + 1);
+  const size_t corner = sizeof(float2) * static_cast<size_t>(m) * (m + 2);
   if (corner > kSmemLimit - 4096) return 0;
   const size_t fmax = factor_dyn_smem(W, 8);  // the larger of the two cluster sizes tried
   if (raise_dynamic_smem(reinterpret_cast<const void*>(k_band_fwd), sweep) != cudaSuccess ||
@@ -948,7 +940,7 @@ int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
     ++launches;
   }
   {
-    const size_t corner = sizeof(float2) * static_cast<size_t>(a.nbd) * (a.nbd + 1);
+    const size_t corner = sizeof(float2) * static_cast<size_t>(a.nbd) * (a.nbd + 2);
     k_band_corner_solve<<<1, kBT, std::max<size_t>(corner, 16), st>>>(a, d.ctrl);
     ++launches;
   }
