@@ -56,7 +56,8 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kMaxOwn = 24;          // row blocks per CTA
 constexpr int kMaxCluster = 16;
 constexpr float kTolRel = 1e-12f;
-constexpr int kRefine = 2;           // refinement steps against the float-float S
+constexpr int kRefine = 2;           // refinement steps against the float-float S (at most)
+constexpr float kRefineSkip = 1e-9f;  // predicted relative error below which the second one is skipped
 constexpr size_t kSmemLimit = 232448;  // 227 KiB opt-in dynamic shared memory per CTA
 
 __host__ __device__ inline int row_ld(int r) { return kNB * (r + 1) + 4; }
@@ -741,11 +742,30 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
   solve_backward(X, cl);
   cl_sync();
   gather_x(X, cl);
-  for (int k = tid; k < npad; k += kThreads) {
-    dsm[s_cv.xs + k] = dsm[s_cv.x + k] * vd[k];
-    dsm[s_cv.xlo + k] = 0.0f;
+  // max |.| over the whole vector (every CTA holds it after gather_x, so every
+  // CTA reaches the same value and the same decision below)
+  __shared__ float s_red[kThreads];
+  auto block_max = [&](float v) {
+    s_red[tid] = v;
+    __syncthreads();
+    for (int h = kThreads / 2; h > 0; h >>= 1) {
+      if (tid < h) s_red[tid] = fmaxf(s_red[tid], s_red[tid + h]);
+      __syncthreads();
+    }
+    const float r = s_red[0];
+    __syncthreads();
+    return r;
+  };
+  float dprev;  // max |correction| of the previous solve, scaled variables
+  {
+    float m = 0.0f;
+    for (int k = tid; k < npad; k += kThreads) {
+      dsm[s_cv.xs + k] = dsm[s_cv.x + k] * vd[k];
+      dsm[s_cv.xlo + k] = 0.0f;
+      m = fmaxf(m, fabsf(dsm[s_cv.x + k]));
+    }
+    dprev = block_max(m);
   }
-  __syncthreads();
   for (int it = 0; it < kRefine; ++it) {
     residual(X, a, alpha);
     __syncthreads();
@@ -753,12 +773,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
     solve_backward(X, cl);
     cl_sync();
     gather_x(X, cl);
+    float dm = 0.0f, xm = 0.0f;
     for (int k = tid; k < npad; k += kThreads) {
       const dd v = dd_add_f(dd_make(dsm[s_cv.xs + k], dsm[s_cv.xlo + k]), dsm[s_cv.x + k] * vd[k]);
       dsm[s_cv.xs + k] = v.hi;
       dsm[s_cv.xlo + k] = v.lo;
+      dm = fmaxf(dm, fabsf(dsm[s_cv.x + k]));
+      xm = fmaxf(xm, fabsf(v.hi / vd[k]));
     }
     __syncthreads();
+    if (it + 1 < kRefine) {
+      // the refinement contracts the error by about dm / dprev per step: when
+      // the error it predicts after this step, dm^2 / dprev, is below
+      // kRefineSkip of the solution (scaled variables), the next step is skipped
+      dm = block_max(dm);
+      xm = block_max(xm);
+      const bool done = dm * dm <= kRefineSkip * dprev * xm;  // NaN keeps refining
+      dprev = dm;
+      if (done) break;
+    }
   }
   for (int jr = 0; jr < s_cv.nown; ++jr) {
     const int r = X.rank + jr * X.C;
