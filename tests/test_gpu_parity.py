@@ -128,3 +128,20 @@ def test_deterministic(pkg):
             out.append((np.array([r.merit for r in recs]), gp.variables()))
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1][0], out[1][1][0]) and np.array_equal(out[0][1][1], out[1][1][1])
+
+
+def test_large_dense_system_uses_panel_solver(pkg, oracle):
+    """A dense reduced system too large for one thread-block cluster's shared
+    memory (160 cameras on the sphere: 954 rows) goes to the multi-launch panel
+    solver (FP32 blocked LDL^T, f64 refinement); per-iteration cost within the
+    parity tolerance of the oracle."""
+    prob = pkg.synth.generate(pkg.synth.SPHERE, n_cam=160, n_pt=8000, seed=pkg.synth.BASE_SEED + 51)
+    with pkg.native.Problem(prob, device=0) as gp:
+        lay = gp.layout()
+    assert lay.solver == pkg.native.SOLVER_DENSE_PANELS
+    (grecs, gterm, _, _), (orecs, _, _) = _run_both(pkg, oracle, prob, 6)
+    g, o = _merits(grecs), _merits(orecs)
+    assert len(g) == len(o) == 6
+    rel = np.abs(g - o) / np.abs(o)
+    print("160-camera sphere (panel solver): per-iteration cost deviation", rel)
+    assert rel.max() < COST_RTOL
