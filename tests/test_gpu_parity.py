@@ -132,16 +132,16 @@ def test_deterministic(pkg):
 
 def test_large_dense_system_uses_panel_solver(pkg, oracle):
     """A dense reduced system too large for one thread-block cluster's shared
-    memory (160 cameras on the sphere: 954 rows) goes to the multi-launch panel
-    solver (FP32 blocked LDL^T, f64 refinement); per-iteration cost within the
-    parity tolerance of the oracle."""
-    prob = pkg.synth.generate(pkg.synth.SPHERE, n_cam=160, n_pt=8000, seed=pkg.synth.BASE_SEED + 51)
+    memory (300 cameras on the sphere: 1794 rows, not banded) goes to the
+    multi-launch panel solver (FP32 blocked LDL^T, f64 refinement);
+    per-iteration cost within the parity tolerance of the oracle."""
+    prob = pkg.synth.generate(pkg.synth.SPHERE, n_cam=300, n_pt=6000, seed=pkg.synth.BASE_SEED + 51)
     with pkg.native.Problem(prob, device=0) as gp:
         lay = gp.layout()
     assert lay.solver == pkg.native.SOLVER_DENSE_PANELS
-    (grecs, gterm, _, _), (orecs, _, _) = _run_both(pkg, oracle, prob, 6)
+    (grecs, gterm, _, _), (orecs, _, _) = _run_both(pkg, oracle, prob, 4, threads=16)
     g, o = _merits(grecs), _merits(orecs)
-    assert len(g) == len(o) == 6
+    assert len(g) == len(o) == 4
     rel = np.abs(g - o) / np.abs(o)
-    print("160-camera sphere (panel solver): per-iteration cost deviation", rel)
+    print("300-camera sphere (panel solver): per-iteration cost deviation", rel)
     assert rel.max() < COST_RTOL
