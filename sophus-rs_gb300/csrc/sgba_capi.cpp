@@ -101,6 +101,11 @@ struct sgba_problem {
   sgba_profile prof{};
   void* flush_buf = nullptr;  // L2 flush target for benchmark hooks
   std::vector<void*> allocs;
+  // small device buffers are carved from chunks (fewer cudaMalloc / cudaFree
+  // calls at create and destroy); large ones get their own allocation
+  char* chunk_ptr = nullptr;
+  size_t chunk_left = 0;
+  size_t chunk_size = size_t(1) << 20;
 };
 
 namespace {
@@ -109,9 +114,23 @@ template <class T>
 int dev_alloc(sgba_problem* p, T** ptr, size_t count) {
   *ptr = nullptr;
   if (count == 0) count = 1;
+  const size_t bytes = (sizeof(T) * count + 255) & ~size_t(255);
   void* v = nullptr;
-  SGBA_CK(cudaMalloc(&v, sizeof(T) * count));
-  p->allocs.push_back(v);
+  if (bytes * 4 > p->chunk_size) {
+    SGBA_CK(cudaMalloc(&v, bytes));
+    p->allocs.push_back(v);
+  } else {
+    if (bytes > p->chunk_left) {
+      void* c = nullptr;
+      SGBA_CK(cudaMalloc(&c, p->chunk_size));
+      p->allocs.push_back(c);
+      p->chunk_ptr = static_cast<char*>(c);
+      p->chunk_left = p->chunk_size;
+    }
+    v = p->chunk_ptr;
+    p->chunk_ptr += bytes;
+    p->chunk_left -= bytes;
+  }
   *ptr = static_cast<T*>(v);
   return SGBA_OK;
 }
@@ -572,6 +591,8 @@ int build_schur_pattern(sgba_problem* p) {
 
 int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   Plan& P = p->plan;
+  // chunk size for the small buffers: about 48 bytes per observation, 1-16 MiB
+  p->chunk_size = std::min<size_t>(size_t(16) << 20, std::max<size_t>(size_t(1) << 20, 48 * static_cast<size_t>(P.no)));
   Dev& d = p->d;
   Sizes& s = p->sz;
   s.nc = P.nc;
