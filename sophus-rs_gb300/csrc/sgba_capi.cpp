@@ -135,8 +135,8 @@ int dev_alloc(sgba_problem* p, T** ptr, size_t count) {
   return SGBA_OK;
 }
 
-template <class T>
-int dev_upload(sgba_problem* p, T** ptr, const std::vector<T>& h) {
+template <class T, class A>
+int dev_upload(sgba_problem* p, T** ptr, const std::vector<T, A>& h) {
   int st = dev_alloc(p, ptr, h.size());
   if (st) return st;
   if (!h.empty()) SGBA_CK(cudaMemcpy(*ptr, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
@@ -318,7 +318,7 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
   // The counting sort runs on chunks of observations: per-chunk counts, then
   // each chunk's slots follow the earlier chunks' inside every point, so the
   // order is exactly the sequential stable one.
-  std::vector<int64_t> ord(no);
+  sgba::RawVec<int64_t> ord(no);
   std::vector<int64_t> cp(np + 1, 0);
   {
     const int64_t T = std::max<int64_t>(1, std::min<int64_t>(HostPool::get().threads(), (no + 65535) / 65536));
@@ -455,7 +455,7 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
     for (int64_t t = 0; t < TG; ++t) run += fcnt[t][f];
     P->cam_g_begin[f + 1] = P->cam_g_begin[f] + run;
   }
-  P->cam_g.assign(P->cam_g_begin[P->nf], 0);
+  P->cam_g.resize(P->cam_g_begin[P->nf]);
   for (int f = 0; f < P->nf; ++f) {
     int64_t run = P->cam_g_begin[f];
     for (int64_t t = 0; t < TG; ++t) {
@@ -609,7 +609,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   for (int k = 0; k < 3; ++k) s.gauge_center[k] = P.gauge_center[k];
   int st;
   {
-    std::vector<double2> uv(P.no);
+    sgba::RawVec<double2> uv(P.no);
     par_ranges(P.no, [&](int64_t b, int64_t e) {
       for (int64_t k = b; k < e; ++k) uv[k] = make_double2(desc->obs_uv[2 * P.ord[k]], desc->obs_uv[2 * P.ord[k] + 1]);
     });

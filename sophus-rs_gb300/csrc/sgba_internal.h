@@ -6,6 +6,8 @@
 
 #include <cstdint>
 #include <string>
+#include <memory>
+#include <utility>
 #include <vector>
 
 namespace sgba {
@@ -49,16 +51,40 @@ struct Record {
   int32_t accepted, termination;
 };
 
+// std::vector allocator that leaves new elements default-initialised (no
+// zero fill): the set-up overwrites its large arrays completely, in parallel,
+// so the pages are first touched by the threads that fill them.
+template <class T>
+struct NoInitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() = default;
+  template <class U>
+  NoInitAlloc(const NoInitAlloc<U>&) {}
+  template <class U>
+  void construct(U* ptr) {
+    ::new (static_cast<void*>(ptr)) U;
+  }
+  template <class U, class... Args>
+  void construct(U* ptr, Args&&... args) {
+    ::new (static_cast<void*>(ptr)) U(std::forward<Args>(args)...);
+  }
+};
+template <class T>
+using RawVec = std::vector<T, NoInitAlloc<T>>;
+
 // Host-side plan: everything derived from the problem structure once.
 struct Plan {
   int32_t nc = 0, np = 0, nf = 0, nm = 0;
   int64_t no = 0, ng = 0;
   // sorted observations (by point, then pose; stable)
-  std::vector<int64_t> ord;          // sorted -> original index
-  std::vector<int32_t> obs_pose, obs_pt;
+  RawVec<int64_t> ord;               // sorted -> original index
+  RawVec<int32_t> obs_pose, obs_pt;
   // groups = reduced cost terms = distinct (point, pose) pairs, sorted
-  std::vector<int64_t> g_begin;      // ng+1, into sorted obs
-  std::vector<int32_t> g_pose, g_pt;
+  RawVec<int64_t> g_begin;           // ng+1, into sorted obs
+  RawVec<int32_t> g_pose, g_pt;
   std::vector<int64_t> pt_g_begin;   // np+1
   std::vector<int32_t> pose_fb;      // nc: free block or -1
   std::vector<int32_t> pt_mb;        // np: marg block or -1
@@ -67,7 +93,7 @@ struct Plan {
   std::vector<double> cnt_f, cnt_m;  // reduced terms per free pose / marg point
   // camera lists (all groups of each free pose), split into tiles
   std::vector<int64_t> cam_g_begin;  // nf+1
-  std::vector<int64_t> cam_g;        // group ids
+  RawVec<int64_t> cam_g;             // group ids
   std::vector<int32_t> tile_fb;      // tile -> free block
   std::vector<int64_t> tile_begin;   // tile -> first entry in cam_g
   std::vector<int64_t> tile_end;
