@@ -12,7 +12,7 @@
 //   k_pair_totals   pairs per lower block (atomic counts; order-free);
 //   (host)          the block pattern, block offsets;
 //   k_pair_count    pairs per (point chunk, block);
-//   k_pair_scan     exclusive scan over the chunks of each block (one warp per block);
+//   k_pair_scan     exclusive scan over the chunks of each block (one thread per block);
 //   k_pair_fill     one CTA per point chunk walks its points in order, each
 //                   point's pairs in parallel (they fall into distinct blocks).
 // The order is (block, point), exactly the order of a sequential build.
@@ -28,10 +28,13 @@ namespace {
 
 __device__ __forceinline__ int64_t lower_id(int64_t r, int64_t c) { return r * (r + 1) / 2 + c; }
 
-// Pair index t of an L-term point -> (b, a), a <= b.
+// Pair index t of an L-term point -> (b, a), a <= b: row b is the one with
+// b(b+1)/2 <= t < (b+1)(b+2)/2. A float estimate of the row (FP64 runs at a
+// small fraction of the FP32 rate), then exact integer corrections.
 __device__ __forceinline__ void decode_pair(int64_t t, int* b, int* a) {
-  int bb = static_cast<int>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
-  while (static_cast<int64_t>(bb) * (bb + 1) / 2 > t) --bb;
+  int bb = static_cast<int>((sqrtf(8.0f * static_cast<float>(t) + 1.0f) - 1.0f) * 0.5f);
+  if (bb < 0) bb = 0;
+  while (bb > 0 && static_cast<int64_t>(bb) * (bb + 1) / 2 > t) --bb;
   while (static_cast<int64_t>(bb + 1) * (bb + 2) / 2 <= t) ++bb;
   *b = bb;
   *a = static_cast<int>(t - static_cast<int64_t>(bb) * (bb + 1) / 2);
@@ -92,28 +95,28 @@ __global__ void __launch_bounds__(256) k_pair_count(PairArgs a) {
   }
 }
 
-// One warp per block b: table[c][b] <- first pair slot of chunk c in block b
-// (an exclusive scan over the chunks: each lane sums a run of chunks, a warp
-// scan of the run totals, then each lane writes its run).
-__global__ void __launch_bounds__(256) k_pair_scan(PairArgs a, const int64_t* block_begin) {
-  const int lane = threadIdx.x & 31;
-  const int per = (a.nchunk + 31) / 32;
-  const int c0 = min(a.nchunk, lane * per), c1 = min(a.nchunk, c0 + per);
-  for (int64_t b = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; b < a.nb;
-       b += (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5) {
-    int64_t own = 0;
-    for (int c = c0; c < c1; ++c) own += a.table[static_cast<int64_t>(c) * a.nb + b];
-    int64_t incl = own;
+// One thread per block b: table[c][b] <- first pair slot of chunk c in block b
+// (an exclusive scan over the chunks; neighbouring threads take neighbouring
+// blocks, so every step reads and writes one contiguous row of the table).
+__global__ void __launch_bounds__(128) k_pair_scan(PairArgs a, const int64_t* block_begin) {
+  for (int64_t b = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; b < a.nb;
+       b += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int64_t run = block_begin[b];
+    int32_t* e = a.table + b;
+    int c = 0;
+    for (; c + 16 <= a.nchunk; c += 16) {
+      int32_t v[16];
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const int64_t v = __shfl_up_sync(0xffffffffu, incl, off);
-      if (lane >= off) incl += v;
+      for (int k = 0; k < 16; ++k) v[k] = e[static_cast<int64_t>(c + k) * a.nb];
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        e[static_cast<int64_t>(c + k) * a.nb] = static_cast<int32_t>(run);
+        run += v[k];
+      }
     }
-    int64_t run = block_begin[b] + incl - own;
-    for (int c = c0; c < c1; ++c) {
-      int32_t* e = a.table + static_cast<int64_t>(c) * a.nb + b;
-      const int32_t v = *e;
-      *e = static_cast<int32_t>(run);
+    for (; c < a.nchunk; ++c) {
+      const int32_t v = e[static_cast<int64_t>(c) * a.nb];
+      e[static_cast<int64_t>(c) * a.nb] = static_cast<int32_t>(run);
       run += v;
     }
   }
@@ -179,10 +182,10 @@ cudaError_t pair_fill(const Sizes& s, const Dev& d, const int32_t* bidmap, int64
   if (blocks > 8192) blocks = 8192;
   if (blocks < 1) blocks = 1;
   k_pair_count<<<blocks, 256, 0, st>>>(a);
-  int sb = static_cast<int>((nb * 32 + 255) / 256);
+  int sb = static_cast<int>((nb + 127) / 128);
   if (sb > 8192) sb = 8192;
   if (sb < 1) sb = 1;
-  k_pair_scan<<<sb, 256, 0, st>>>(a, block_begin);
+  k_pair_scan<<<sb, 128, 0, st>>>(a, block_begin);
   k_pair_fill<<<nchunk, 256, 0, st>>>(a);
   return cudaGetLastError();
 }
