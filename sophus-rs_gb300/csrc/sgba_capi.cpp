@@ -21,6 +21,7 @@
 #include <functional>
 #include <condition_variable>
 #include <atomic>
+#include <chrono>
 #include <utility>
 #include <mutex>
 #include <map>
@@ -149,6 +150,16 @@ int dev_upload(sgba_problem* p, T** ptr, const std::vector<T, A>& h) {
 // it; threads are created once per process).  run(n, f) calls f(k) for every
 // k in [0, n) on the workers and the calling thread and returns when all have
 // finished; parallel regions from different host threads are serialised.
+// The set-up runs about a dozen short regions back to back, so a worker that
+// finished a region watches for the next one for a while (kSpinNs) before it
+// sleeps on the condition variable, and regions are entered and retired
+// through atomics: a wake-up through the condition variable, or a convoy on
+// one mutex, costs tens of microseconds per region.
+//
+// Retiring a region: the caller clears region_ once every item ran, then
+// waits until no worker is inside_. A worker counts itself inside_ before it
+// reads region_, so one that arrives after the caller saw inside_ == 0 reads
+// the cleared pointer (sequentially consistent atomics).
 class HostPool {
  public:
   static HostPool& get() {
@@ -166,26 +177,34 @@ class HostPool {
     Region r;
     r.fn = &f;
     r.n = n;
-    r.remaining = n;
+    r.remaining.store(n);
     {
-      std::lock_guard<std::mutex> lk(mu_);
-      region_ = &r;
-      ++gen_;
+      std::lock_guard<std::mutex> lk(mu_);  // sleepers test gen_ under mu_
+      region_.store(&r);
+      gen_.fetch_add(1);
     }
     cv_.notify_all();
     drain(r);
-    std::unique_lock<std::mutex> lk(mu_);
-    done_cv_.wait(lk, [&] { return r.remaining == 0 && r.active == 0; });
-    region_ = nullptr;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int it = 0; r.remaining.load() != 0; ++it) {
+      if ((it & 63) == 63 && std::chrono::steady_clock::now() - t0 > std::chrono::nanoseconds(kSpinNs)) {
+        std::unique_lock<std::mutex> lk(mu_);
+        done_cv_.wait(lk, [&] { return r.remaining.load() == 0; });
+        break;
+      }
+    }
+    region_.store(nullptr);
+    for (int it = 0; inside_.load() != 0; ++it)
+      if ((it & 63) == 63) std::this_thread::yield();
   }
 
  private:
+  static constexpr int64_t kSpinNs = 200000;
   struct Region {
     const std::function<void(int)>* fn = nullptr;
     int n = 0;
     std::atomic<int> next{0};
-    int remaining = 0;  // guarded by mu_
-    int active = 0;     // workers inside the region, guarded by mu_
+    std::atomic<int> remaining{0};
   };
   static bool& forked_child() {
     static bool forked = false;
@@ -211,33 +230,38 @@ class HostPool {
       const int k = r.next.fetch_add(1);
       if (k >= r.n) return;
       (*r.fn)(k);
-      std::lock_guard<std::mutex> lk(mu_);
-      if (--r.remaining == 0) done_cv_.notify_all();
+      if (r.remaining.fetch_sub(1) == 1) {
+        std::lock_guard<std::mutex> lk(mu_);
+        done_cv_.notify_all();
+      }
     }
   }
   void loop() {
     uint64_t seen = 0;
     for (;;) {
-      Region* r = nullptr;
-      {
+      // watch for the next region before sleeping
+      const auto t0 = std::chrono::steady_clock::now();
+      for (int it = 0; gen_.load() == seen; ++it)
+        if ((it & 63) == 63 && std::chrono::steady_clock::now() - t0 > std::chrono::nanoseconds(kSpinNs)) break;
+      if (gen_.load() == seen) {
         std::unique_lock<std::mutex> lk(mu_);
-        cv_.wait(lk, [&] { return stop_ || (gen_ != seen && region_ != nullptr); });
+        cv_.wait(lk, [&] { return stop_ || gen_.load() != seen; });
         if (stop_) return;
-        seen = gen_;
-        r = region_;
-        ++r->active;
       }
-      drain(*r);
-      std::lock_guard<std::mutex> lk(mu_);
-      if (--r->active == 0 && r->remaining == 0) done_cv_.notify_all();
+      seen = gen_.load();
+      inside_.fetch_add(1);
+      Region* r = region_.load();
+      if (r) drain(*r);
+      inside_.fetch_sub(1);
     }
   }
   int nthreads_ = 1;
   std::vector<std::thread> workers_;
   std::mutex region_mu_, mu_;
   std::condition_variable cv_, done_cv_;
-  Region* region_ = nullptr;
-  uint64_t gen_ = 0;
+  std::atomic<Region*> region_{nullptr};
+  std::atomic<uint64_t> gen_{0};
+  std::atomic<int> inside_{0};
   bool stop_ = false;
 };
 
@@ -253,6 +277,13 @@ int par_chunks(int64_t n, int64_t min_per, F f) {
 template <class F>
 void par_ranges(int64_t n, F f) {
   par_chunks(n, 32768, [&](int, int64_t b, int64_t e) { f(b, e); });
+}
+
+// f(begin, end) over ranges of points, whose work is their observations:
+// chunks of at least 512 points.
+template <class F>
+void par_points(int64_t np, F f) {
+  par_chunks(np, 512, [&](int, int64_t b, int64_t e) { f(b, e); });
 }
 
 bool finite_all(const double* v, int64_t n) {
@@ -319,6 +350,8 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
   // each chunk's slots follow the earlier chunks' inside every point, so the
   // order is exactly the sequential stable one.
   sgba::RawVec<int64_t> ord(no);
+  P->obs_pose.resize(no);  // the pose of every sorted observation, filled with ord
+  int32_t* const opose = P->obs_pose.data();
   std::vector<int64_t> cp(np + 1, 0);
   {
     const int64_t T = std::max<int64_t>(1, std::min<int64_t>(HostPool::get().threads(), (no + 65535) / 65536));
@@ -327,14 +360,16 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
       cnt[t].assign(np, 0);
       for (int64_t o = no * t / T; o < no * (t + 1) / T; ++o) cnt[t][d->obs_pt[o]]++;
     });
-    for (int i = 0; i < np; ++i) {
-      int64_t run = 0;
-      for (int64_t t = 0; t < T; ++t) run += cnt[t][i];
-      cp[i + 1] = run;
-    }
+    par_points(np, [&](int64_t i0, int64_t i1) {
+      for (int64_t i = i0; i < i1; ++i) {
+        int64_t run = 0;
+        for (int64_t t = 0; t < T; ++t) run += cnt[t][i];
+        cp[i + 1] = run;
+      }
+    });
     for (int i = 0; i < np; ++i) cp[i + 1] += cp[i];
     std::vector<std::vector<int64_t>> base(T);
-    par_ranges(np, [&](int64_t i0, int64_t i1) {
+    par_points(np, [&](int64_t i0, int64_t i1) {
       for (int64_t i = i0; i < i1; ++i) {
         int64_t run = cp[i];
         for (int64_t t = 0; t < T; ++t) {
@@ -348,48 +383,51 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
       std::vector<int32_t>& slot = cnt[t];
       for (int64_t o = no * t / T; o < no * (t + 1) / T; ++o) {
         const int32_t i = d->obs_pt[o];
-        ord[cp[i] + slot[i]++] = o;
+        const int64_t k = cp[i] + slot[i]++;
+        ord[k] = o;
+        opose[k] = d->obs_cam[o];
       }
     });
   }
   // groups (reduction ranges: equal non-conditioned arguments, cost_fn.rs:374-390):
   // runs of equal pose inside each point
   std::vector<int64_t> gcount(np + 1, 0);
-  par_ranges(np, [&](int64_t i0, int64_t i1) {
+  par_points(np, [&](int64_t i0, int64_t i1) {
     for (int64_t i = i0; i < i1; ++i) {
       int64_t* a = ord.data() + cp[i];
+      int32_t* kp = opose + cp[i];
       const int64_t n = cp[i + 1] - cp[i];
       for (int64_t k = 1; k < n; ++k) {  // insertion sort by pose, stable
         const int64_t v = a[k];
-        const int32_t key = d->obs_cam[v];
+        const int32_t key = kp[k];
         int64_t m = k;
-        while (m > 0 && d->obs_cam[a[m - 1]] > key) {
+        while (m > 0 && kp[m - 1] > key) {
           a[m] = a[m - 1];
+          kp[m] = kp[m - 1];
           --m;
         }
         a[m] = v;
+        kp[m] = key;
       }
       int64_t runs = 0;
       for (int64_t k = 0; k < n; ++k)
-        if (k == 0 || d->obs_cam[a[k]] != d->obs_cam[a[k - 1]]) ++runs;
+        if (k == 0 || kp[k] != kp[k - 1]) ++runs;
       gcount[i + 1] = runs;
     }
   });
   for (int i = 0; i < np; ++i) gcount[i + 1] += gcount[i];
   P->ng = gcount[np];
-  P->obs_pose.resize(no);
   P->obs_pt.resize(no);
   P->g_begin.resize(P->ng + 1);
   P->g_pose.resize(P->ng);
   P->g_pt.resize(P->ng);
-  par_ranges(np, [&](int64_t i0, int64_t i1) {
+  par_points(np, [&](int64_t i0, int64_t i1) {
     for (int64_t i = i0; i < i1; ++i) {
       int64_t g = gcount[i];
       for (int64_t k = cp[i]; k < cp[i + 1]; ++k) {
-        const int32_t jc = d->obs_cam[ord[k]];
-        P->obs_pose[k] = jc;
+        const int32_t jc = opose[k];
         P->obs_pt[k] = static_cast<int32_t>(i);
-        if (k == cp[i] || jc != P->obs_pose[k - 1]) {
+        if (k == cp[i] || jc != opose[k - 1]) {
           P->g_begin[g] = k;
           P->g_pose[g] = jc;
           P->g_pt[g] = static_cast<int32_t>(i);
@@ -422,7 +460,7 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
   P->cnt_m.assign(P->nm, 0.0);
   // per marginalized point: its reduced terms; per free pose: its terms,
   // counted on chunks of terms; the camera term lists fill stably the same way
-  par_ranges(np, [&](int64_t i0, int64_t i1) {
+  par_points(np, [&](int64_t i0, int64_t i1) {
     for (int64_t i = i0; i < i1; ++i)
       if (P->pt_mb[i] >= 0) P->cnt_m[P->pt_mb[i]] = static_cast<double>(P->pt_g_begin[i + 1] - P->pt_g_begin[i]);
   });
