@@ -66,7 +66,7 @@ __host__ __device__ inline int row_ld(int r) { return kNB * (r + 1) + 4; }
 struct Carve {
   int nown;
   int rowoff[kMaxOwn];
-  int wt, linv, dloc, rdloc, lpp, rdp, y, x, xs, xlo, bl, facc, accb, vdef, udef, red, tmp, tmp2, flags, total;
+  int wt, linv, dloc, rdloc, lpp, rdp, y, x, xs, xlo, bl, facc, accb, vdef, udef, red, tmp, tmp2, colbuf, flags, total;
 };
 
 __host__ __device__ inline void carve(int P, int C, int rank, Carve* c) {
@@ -97,6 +97,7 @@ __host__ __device__ inline void carve(int P, int C, int rank, Carve* c) {
   c->red = take(2 * kThreads);
   c->tmp = take(32);
   c->tmp2 = take(32);
+  c->colbuf = take(64);
   c->flags = take(4);
   c->total = off;
 }
@@ -146,14 +147,15 @@ __device__ __forceinline__ float* remote(cg::cluster_group& cl, float* sm, int r
 }
 
 // Diagonal step of block p (owner, warp 0): LDL^T of the 24x24 diagonal block
-// in place (lane i keeps row i in registers; columns are broadcast through
-// shared memory), 1/d, and the inverse of its unit lower factor.
+// in place (lane i keeps row i in registers; each column is broadcast through
+// shared memory, read back as float4s; two buffers, one warp barrier per
+// pivot), 1/d, and the inverse of its unit lower factor.
 __device__ void diag_step(const Ctx& X, int p, int* bad_flag) {
   const int lane = threadIdx.x & 31;
   const int jp = p / X.C;
   float* Ab = X.rowblk(p) + kNB * p;
   const int ld = X.ld(p);
-  float* colbuf = X.sm + X.cv->tmp;
+  float* colbuf = X.sm + X.cv->colbuf;  // two 32-float column buffers
   float a[kNB];
 #pragma unroll
   for (int k = 0; k < kNB; ++k) a[k] = (lane < kNB && k <= lane) ? Ab[lane * ld + k] : 0.0f;
@@ -163,26 +165,31 @@ __device__ void diag_step(const Ctx& X, int p, int* bad_flag) {
 #pragma unroll
   for (int t = 0; t < kNB; ++t) {
     if (t % 6 == 0) maxp = 1.0f;  // 24p is a multiple of 6: a new pose block starts here
-    colbuf[lane] = a[t];
+    float* cb = colbuf + 32 * (t & 1);  // two buffers: one warp barrier per pivot
+    cb[lane] = a[t];
     __syncwarp();
-    float dt = colbuf[t];
+    float col[kNB];
+#pragma unroll
+    for (int q = 0; q < kNB / 4; ++q) {
+      const float4 v = reinterpret_cast<const float4*>(cb)[q];
+      col[4 * q] = v.x; col[4 * q + 1] = v.y; col[4 * q + 2] = v.z; col[4 * q + 3] = v.w;
+    }
+    float dt = col[t];
     const float tol = fmaxf(maxp, 1.0f) * kTolRel;
     if (fabsf(dt) <= tol) dt = 0.0f;
     else maxp = fmaxf(maxp, fabsf(dt));
     const float rd = (dt == 0.0f) ? 0.0f : __frcp_rn(dt);
     const float li = (lane > t) ? a[t] * rd : 0.0f;
+    // entries above this lane's diagonal take junk here; they are never read or stored
 #pragma unroll
-    for (int k = t + 1; k < kNB; ++k) {
-      const float wk = colbuf[k];  // A[k][t], not yet scaled
-      if (k <= lane) a[k] = fmaf(-li, wk, a[k]);
-    }
-    __syncwarp();
+    for (int k = t + 1; k < kNB; ++k) a[k] = fmaf(-li, col[k], a[k]);
     if (lane > t) a[t] = li;
     if (lane == 0) {
       dl[t] = dt;
       rdl[t] = rd;
     }
   }
+  __syncwarp();
   if (lane < kNB) {
 #pragma unroll
     for (int k = 0; k < kNB; ++k)
@@ -197,10 +204,21 @@ __device__ void diag_step(const Ctx& X, int p, int* bad_flag) {
   for (int i = 0; i < kNB; ++i) xc[i] = (i == lane) ? 1.0f : 0.0f;
 #pragma unroll
   for (int i = 1; i < kNB; ++i) {
-    float s = 0.f;
+    float row[kNB];
 #pragma unroll
-    for (int k = 0; k < i; ++k) s = fmaf(Ab[i * ld + k], xc[k], s);
-    if (i > lane) xc[i] = -s;
+    for (int q = 0; q < (i + 3) / 4; ++q) {
+      const float4 v = reinterpret_cast<const float4*>(Ab + i * ld)[q];
+      row[4 * q] = v.x; row[4 * q + 1] = v.y; row[4 * q + 2] = v.z; row[4 * q + 3] = v.w;
+    }
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+    for (int k = 0; k < i; ++k) {
+      if (k % 4 == 0) s0 = fmaf(row[k], xc[k], s0);
+      else if (k % 4 == 1) s1 = fmaf(row[k], xc[k], s1);
+      else if (k % 4 == 2) s2 = fmaf(row[k], xc[k], s2);
+      else s3 = fmaf(row[k], xc[k], s3);
+    }
+    if (i > lane) xc[i] = -((s0 + s1) + (s2 + s3));
   }
   float* Li = X.sm + X.cv->linv + kNB * kLd * jp;
   if (lane < kNB) {
@@ -227,48 +245,108 @@ __device__ void pull_diag(const Ctx& X, cg::cluster_group& cl, int p) {
 
 // Panel step p, every CTA: for the owned row blocks r > p,
 // W_rp = A_rp Linv_pp^T (kept transposed for the update) and L_rp = W_rp D^-1
-// in place.  Linv_pp and 1/d were pushed by the owner of p.
+// in place.  Linv_pp and 1/d were pulled from the owner of p.  4x4 register
+// tiles from float4 shared-memory reads; every entry is summed over k in order.
 __device__ void panel_rows(const Ctx& X, int p) {
   int j0 = 0;
   while (j0 < X.cv->nown && X.rank + j0 * X.C <= p) ++j0;
-  const int total = (X.cv->nown - j0) * kNB * kNB;
+  const int ntile = (X.cv->nown - j0) * 36;  // 4x4 tiles of each 24x24 block
   const float* lpp = X.sm + X.cv->lpp;
   const float* rdp = X.sm + X.cv->rdp;
-  for (int e = threadIdx.x; e < total; e += kThreads) {
-    const int jr = j0 + e / (kNB * kNB);
-    const int rem = e % (kNB * kNB), i = rem / kNB, t = rem % kNB;
-    const int r = X.rank + jr * X.C;
-    const float* arow = X.sm + X.cv->rowoff[jr] + i * X.ld(r) + kNB * p;
-    const float* lt = lpp + t * kLd;  // Linv[t][k], zero for k > t
-    float s = 0.f;
+  // W = A_rp Linv_pp^T, 4x4 tiles; each entry summed over k in order; stored transposed (wt)
+  for (int e = threadIdx.x; e < ntile; e += kThreads) {
+    const int jr = j0 + e / 36, rem = e % 36, i0 = 4 * (rem / 6), t0 = 4 * (rem % 6);
+    const int r = X.rank + jr * X.C, ld = X.ld(r);
+    const float* A0 = X.sm + X.cv->rowoff[jr] + kNB * p;
+    float w[4][4];
 #pragma unroll
-    for (int k = 0; k < kNB; ++k) s = fmaf(arow[k], lt[k], s);
-    X.sm[X.cv->wt + kNB * kNB * jr + t * kNB + i] = s;
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) w[u][v] = 0.f;
+#pragma unroll
+    for (int q = 0; q < kNB / 4; ++q) {
+      float4 av[4], lv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) av[u] = reinterpret_cast<const float4*>(A0 + (i0 + u) * ld)[q];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) lv[v] = reinterpret_cast<const float4*>(lpp + (t0 + v) * kLd)[q];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          float acc = w[u][v];
+          acc = fmaf(av[u].x, lv[v].x, acc);
+          acc = fmaf(av[u].y, lv[v].y, acc);
+          acc = fmaf(av[u].z, lv[v].z, acc);
+          acc = fmaf(av[u].w, lv[v].w, acc);
+          w[u][v] = acc;
+        }
+    }
+    float* wt = X.sm + X.cv->wt + kNB * kNB * jr;
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+      reinterpret_cast<float4*>(wt + (t0 + v) * kNB + i0)[0] = make_float4(w[0][v], w[1][v], w[2][v], w[3][v]);
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < total; e += kThreads) {
-    const int jr = j0 + e / (kNB * kNB);
-    const int rem = e % (kNB * kNB), i = rem / kNB, t = rem % kNB;
-    const int r = X.rank + jr * X.C;
-    X.sm[X.cv->rowoff[jr] + i * X.ld(r) + kNB * p + t] = X.sm[X.cv->wt + kNB * kNB * jr + t * kNB + i] * rdp[t];
+  // L_rp = W D^-1 in place
+  for (int e = threadIdx.x; e < ntile; e += kThreads) {
+    const int jr = j0 + e / 36, rem = e % 36, i0 = 4 * (rem / 6), t0 = 4 * (rem % 6);
+    const int r = X.rank + jr * X.C, ld = X.ld(r);
+    float* A0 = X.sm + X.cv->rowoff[jr] + kNB * p;
+    const float* wt = X.sm + X.cv->wt + kNB * kNB * jr;
+    float4 wv[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) wv[v] = reinterpret_cast<const float4*>(wt + (t0 + v) * kNB + i0)[0];
+    const float4 rv = reinterpret_cast<const float4*>(rdp)[t0 / 4];
+    reinterpret_cast<float4*>(A0 + (i0 + 0) * ld + t0)[0] = make_float4(wv[0].x * rv.x, wv[1].x * rv.y, wv[2].x * rv.z, wv[3].x * rv.w);
+    reinterpret_cast<float4*>(A0 + (i0 + 1) * ld + t0)[0] = make_float4(wv[0].y * rv.x, wv[1].y * rv.y, wv[2].y * rv.z, wv[3].y * rv.w);
+    reinterpret_cast<float4*>(A0 + (i0 + 2) * ld + t0)[0] = make_float4(wv[0].z * rv.x, wv[1].z * rv.y, wv[2].z * rv.z, wv[3].z * rv.w);
+    reinterpret_cast<float4*>(A0 + (i0 + 3) * ld + t0)[0] = make_float4(wv[0].w * rv.x, wv[1].w * rv.y, wv[2].w * rv.z, wv[3].w * rv.w);
   }
 }
 
-// Owner of p+1, all threads: the update of its diagonal block by panel p,
-// A_{p+1,p+1} -= W_{p+1,p} L_{p+1,p}^T (lower triangle; both factors local).
-// Measured 2.5x faster than leaving this block to one warp of update_blocks.
+// Owner of p+1: the update of its diagonal block by panel p,
+// A_{p+1,p+1} -= W_{p+1,p} L_{p+1,p}^T (lower triangle; both factors local),
+// in 4x4 register tiles (21 of them), each entry summed over t in order.
 __device__ void diag_update(const Ctx& X, int p) {
   const int r = p + 1, jr = r / X.C, ld = X.ld(r);
   float* Ar = X.rowblk(r);
   const float* wt = X.sm + X.cv->wt + kNB * kNB * jr;
-  for (int e = threadIdx.x; e < kNB * kNB; e += kThreads) {
-    const int i = e / kNB, k = e % kNB;
-    if (k > i) continue;
-    const float* lk = Ar + k * ld + kNB * p;
-    float acc = 0.f;
+  // 4x4 tiles (i0, k0) of the lower triangle, k0 <= i0: 21 tiles
+  for (int e = threadIdx.x; e < 21; e += kThreads) {
+    int ib = 0, rem = e;
+    while (rem > ib) { rem -= ib + 1; ++ib; }
+    const int i0 = 4 * ib, k0 = 4 * rem;
+    float acc[4][4];
 #pragma unroll
-    for (int t = 0; t < kNB; ++t) acc = fmaf(wt[t * kNB + i], lk[t], acc);
-    Ar[i * ld + kNB * r + k] -= acc;
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
+#pragma unroll
+    for (int q = 0; q < kNB / 4; ++q) {
+      float4 lk[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) lk[v] = reinterpret_cast<const float4*>(Ar + (k0 + v) * ld + kNB * p)[q];
+      float4 wv[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) wv[c] = reinterpret_cast<const float4*>(wt + (4 * q + c) * kNB + i0)[0];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const float lt[4] = {lk[v].x, lk[v].y, lk[v].z, lk[v].w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          acc[0][v] = fmaf(wv[c].x, lt[c], acc[0][v]);
+          acc[1][v] = fmaf(wv[c].y, lt[c], acc[1][v]);
+          acc[2][v] = fmaf(wv[c].z, lt[c], acc[2][v]);
+          acc[3][v] = fmaf(wv[c].w, lt[c], acc[3][v]);
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v)
+        if (k0 + v <= i0 + u) Ar[(i0 + u) * ld + kNB * r + k0 + v] -= acc[u][v];
   }
 }
 
