@@ -102,14 +102,48 @@ struct sgba_problem {
   sgba_profile prof{};
   void* flush_buf = nullptr;  // L2 flush target for benchmark hooks
   std::vector<void*> allocs;
-  // small device buffers are carved from chunks (fewer cudaMalloc / cudaFree
-  // calls at create and destroy); large ones get their own allocation
+  // Device memory comes from a stream-ordered pool (problem_pool) on the
+  // problem's stream. Small device buffers are carved from chunks (fewer
+  // allocations at create and destroy); large ones get their own allocation.
+  cudaMemPool_t pool = nullptr;
   char* chunk_ptr = nullptr;
   size_t chunk_left = 0;
   size_t chunk_size = size_t(1) << 20;
 };
 
 namespace {
+
+// One stream-ordered memory pool per device for all problems: allocations are
+// cudaMallocFromPoolAsync on the problem's stream and sgba_problem_destroy
+// frees with cudaFreeAsync, so creating and destroying many small problems
+// (local windows) costs no cudaMalloc / cudaFree (which synchronises the
+// device). Freed memory stays cached for the next problem up to 1/16 of the
+// device's memory; above that the pool returns it at synchronisation points.
+cudaMemPool_t problem_pool(int dev) {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = pools.find(dev);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps pr{};
+  pr.allocType = cudaMemAllocationTypePinned;
+  pr.location.type = cudaMemLocationTypeDevice;
+  pr.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  if (cudaMemPoolCreate(&pool, &pr) != cudaSuccess) return nullptr;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+    uint64_t keep = total_b / 16;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  pools[dev] = pool;
+  return pool;
+}
+
+template <class V>
+void release(V& v) {
+  V().swap(v);
+}
 
 template <class T>
 int dev_alloc(sgba_problem* p, T** ptr, size_t count) {
@@ -118,12 +152,12 @@ int dev_alloc(sgba_problem* p, T** ptr, size_t count) {
   const size_t bytes = (sizeof(T) * count + 255) & ~size_t(255);
   void* v = nullptr;
   if (bytes * 4 > p->chunk_size) {
-    SGBA_CK(cudaMalloc(&v, bytes));
+    SGBA_CK(cudaMallocFromPoolAsync(&v, bytes, p->pool, p->stream));
     p->allocs.push_back(v);
   } else {
     if (bytes > p->chunk_left) {
       void* c = nullptr;
-      SGBA_CK(cudaMalloc(&c, p->chunk_size));
+      SGBA_CK(cudaMallocFromPoolAsync(&c, p->chunk_size, p->pool, p->stream));
       p->allocs.push_back(c);
       p->chunk_ptr = static_cast<char*>(c);
       p->chunk_left = p->chunk_size;
@@ -136,11 +170,13 @@ int dev_alloc(sgba_problem* p, T** ptr, size_t count) {
   return SGBA_OK;
 }
 
+// Device copy of a host vector, ordered on the problem's stream: `h` must stay
+// alive until upload() synchronises the stream at its end.
 template <class T, class A>
 int dev_upload(sgba_problem* p, T** ptr, const std::vector<T, A>& h) {
   int st = dev_alloc(p, ptr, h.size());
   if (st) return st;
-  if (!h.empty()) SGBA_CK(cudaMemcpy(*ptr, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice));
+  if (!h.empty()) SGBA_CK(cudaMemcpyAsync(*ptr, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, p->stream));
   return SGBA_OK;
 }
 
@@ -274,9 +310,13 @@ int par_chunks(int64_t n, int64_t min_per, F f) {
   return static_cast<int>(t);
 }
 
+// Items per thread below which a loop is not split further (a fork-join of
+// the pool costs a few microseconds while its workers are awake).
+constexpr int64_t kMinPerThread = 8192;
+
 template <class F>
 void par_ranges(int64_t n, F f) {
-  par_chunks(n, 32768, [&](int, int64_t b, int64_t e) { f(b, e); });
+  par_chunks(n, kMinPerThread, [&](int, int64_t b, int64_t e) { f(b, e); });
 }
 
 // f(begin, end) over ranges of points, whose work is their observations:
@@ -354,7 +394,7 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
   int32_t* const opose = P->obs_pose.data();
   std::vector<int64_t> cp(np + 1, 0);
   {
-    const int64_t T = std::max<int64_t>(1, std::min<int64_t>(HostPool::get().threads(), (no + 65535) / 65536));
+    const int64_t T = std::max<int64_t>(1, std::min<int64_t>(HostPool::get().threads(), (no + kMinPerThread - 1) / kMinPerThread));
     std::vector<std::vector<int32_t>> cnt(T);
     HostPool::get().run(static_cast<int>(T), [&](int t) {
       cnt[t].assign(np, 0);
@@ -464,7 +504,7 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
     for (int64_t i = i0; i < i1; ++i)
       if (P->pt_mb[i] >= 0) P->cnt_m[P->pt_mb[i]] = static_cast<double>(P->pt_g_begin[i + 1] - P->pt_g_begin[i]);
   });
-  const int64_t TG = std::max<int64_t>(1, std::min<int64_t>(HostPool::get().threads(), (P->ng + 65535) / 65536));
+  const int64_t TG = std::max<int64_t>(1, std::min<int64_t>(HostPool::get().threads(), (P->ng + kMinPerThread - 1) / kMinPerThread));
   std::vector<std::vector<int64_t>> fcnt(TG);
   std::vector<int64_t> hoff_part(TG, 0);
   HostPool::get().run(static_cast<int>(TG), [&](int t) {
@@ -568,13 +608,13 @@ int build_schur_pattern(sgba_problem* p) {
   Sizes tmp_sizes = p->sz;
   tmp_sizes.np = P.np;
   int32_t* totals = nullptr;
-  SGBA_CK(cudaMalloc(&totals, sizeof(int32_t) * nlow));
+  SGBA_CK(cudaMallocFromPoolAsync(&totals, sizeof(int32_t) * nlow, p->pool, p->stream));
   std::vector<int32_t> cnt(nlow, 0);
   cudaError_t e = cudaMemsetAsync(totals, 0, sizeof(int32_t) * nlow, p->stream);
   if (e == cudaSuccess) e = sgba::pair_totals(tmp_sizes, d, totals, p->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(cnt.data(), totals, sizeof(int32_t) * nlow, cudaMemcpyDeviceToHost, p->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
-  cudaFree(totals);
+  cudaFreeAsync(totals, p->stream);
   if (e != cudaSuccess) return set_error(SGBA_ERR_CUDA, "Schur pattern (counts): %s", cudaGetErrorString(e));
   std::vector<int32_t> bid(nlow, -1);
   int64_t nb = 0;
@@ -610,17 +650,17 @@ int build_schur_pattern(sgba_problem* p) {
   nch = std::max<int64_t>(1, std::min<int64_t>({nch, 512, static_cast<int64_t>(P.np)}));
   int32_t *bidmap = nullptr, *table = nullptr;
   int64_t* bbeg = nullptr;
-  e = cudaMalloc(&bidmap, sizeof(int32_t) * nlow);
-  if (e == cudaSuccess) e = cudaMalloc(&table, sizeof(int32_t) * nch * nb);
-  if (e == cudaSuccess) e = cudaMalloc(&bbeg, sizeof(int64_t) * (nb + 1));
+  e = cudaMallocFromPoolAsync(&bidmap, sizeof(int32_t) * nlow, p->pool, p->stream);
+  if (e == cudaSuccess) e = cudaMallocFromPoolAsync(&table, sizeof(int32_t) * nch * nb, p->pool, p->stream);
+  if (e == cudaSuccess) e = cudaMallocFromPoolAsync(&bbeg, sizeof(int64_t) * (nb + 1), p->pool, p->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(bidmap, bid.data(), sizeof(int32_t) * nlow, cudaMemcpyHostToDevice, p->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(bbeg, P.sb_pair_begin.data(), sizeof(int64_t) * (nb + 1), cudaMemcpyHostToDevice, p->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(table, 0, sizeof(int32_t) * nch * nb, p->stream);
   if (e == cudaSuccess) e = sgba::pair_fill(tmp_sizes, d, bidmap, nb, bbeg, static_cast<int32_t>(nch), table, p->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
-  cudaFree(bidmap);
-  cudaFree(table);
-  cudaFree(bbeg);
+  if (bidmap) cudaFreeAsync(bidmap, p->stream);
+  if (table) cudaFreeAsync(table, p->stream);
+  if (bbeg) cudaFreeAsync(bbeg, p->stream);
   if (e != cudaSuccess)
     return set_error(e == cudaErrorMemoryAllocation ? SGBA_ERR_OUT_OF_MEMORY : SGBA_ERR_CUDA, "Schur pattern (pairs): %s",
                      cudaGetErrorString(e));
@@ -646,13 +686,15 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   s.gauge_kind = P.gauge_kind;
   for (int k = 0; k < 3; ++k) s.gauge_center[k] = P.gauge_center[k];
   int st;
-  {
-    sgba::RawVec<double2> uv(P.no);
-    par_ranges(P.no, [&](int64_t b, int64_t e) {
-      for (int64_t k = b; k < e; ++k) uv[k] = make_double2(desc->obs_uv[2 * P.ord[k]], desc->obs_uv[2 * P.ord[k] + 1]);
-    });
-    if ((st = dev_upload(p, &d.obs_uv, uv))) return st;
-  }
+  // host staging of the copies below: alive until the stream is synchronised
+  sgba::RawVec<double2> uv(P.no);
+  std::vector<int32_t> cpt(1, 0);
+  std::vector<double> poses(desc->poses, desc->poses + 7 * P.nc);
+  std::vector<double> pts(desc->points, desc->points + 3 * P.np);
+  par_ranges(P.no, [&](int64_t b, int64_t e) {
+    for (int64_t k = b; k < e; ++k) uv[k] = make_double2(desc->obs_uv[2 * P.ord[k]], desc->obs_uv[2 * P.ord[k] + 1]);
+  });
+  if ((st = dev_upload(p, &d.obs_uv, uv))) return st;
   if ((st = dev_upload(p, &d.obs_pose, P.obs_pose))) return st;
   if ((st = dev_upload(p, &d.obs_pt, P.obs_pt))) return st;
   if ((st = dev_upload(p, &d.g_begin, P.g_begin))) return st;
@@ -672,7 +714,6 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_upload(p, &d.fb_tile_begin, P.fb_tile_begin))) return st;
   {
     // landmark point chunks: consecutive points, at most 256 terms and 256 points
-    std::vector<int32_t> cpt(1, 0);
     int64_t terms = 0, cap = 256;
     int npts = 0;
     for (int i = 0; i < P.np; ++i) {
@@ -693,7 +734,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
     if ((st = dev_upload(p, &d.lmk_chunk_pt, cpt))) return st;
     if ((st = dev_alloc(p, &d.slow_list, static_cast<size_t>(std::max(P.np, 1))))) return st;
     if ((st = dev_alloc(p, &d.slow_count, 1))) return st;
-    SGBA_CK(cudaMemset(d.slow_count, 0, sizeof(int32_t)));
+    SGBA_CK(cudaMemsetAsync(d.slow_count, 0, sizeof(int32_t), p->stream));
   }
   if ((st = build_schur_pattern(p))) return st;
   s.nsb = static_cast<int64_t>(P.sb_row.size());
@@ -707,15 +748,11 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
     if ((st = dev_alloc(p, &d.schur_part, 36 * static_cast<size_t>(s.nchunk)))) return st;
   }
   // state (quaternions disambiguated to w >= 0 as from_params does)
-  {
-    std::vector<double> poses(desc->poses, desc->poses + 7 * P.nc);
-    for (int j = 0; j < P.nc; ++j)
-      if (!(0.0 <= poses[7 * j]))
-        for (int k = 0; k < 4; ++k) poses[7 * j + k] = -poses[7 * j + k];
-    if ((st = dev_upload(p, &d.poses, poses))) return st;
-    std::vector<double> pts(desc->points, desc->points + 3 * P.np);
-    if ((st = dev_upload(p, &d.points, pts))) return st;
-  }
+  for (int j = 0; j < P.nc; ++j)
+    if (!(0.0 <= poses[7 * j]))
+      for (int k = 0; k < 4; ++k) poses[7 * j + k] = -poses[7 * j + k];
+  if ((st = dev_upload(p, &d.poses, poses))) return st;
+  if ((st = dev_upload(p, &d.points, pts))) return st;
   if ((st = dev_alloc(p, &d.poses_t, 7 * static_cast<size_t>(P.nc)))) return st;
   if ((st = dev_alloc(p, &d.points_t, 3 * static_cast<size_t>(P.np)))) return st;
   if ((st = dev_alloc(p, &d.res, P.no))) return st;
@@ -733,7 +770,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_alloc(p, &d.tile_part, 33 * static_cast<size_t>(s.ntiles)))) return st;
   const size_t n6 = static_cast<size_t>(s.n6);
   if ((st = dev_alloc(p, &d.S, n6 * n6))) return st;
-  SGBA_CK(cudaMemset(d.S, 0, sizeof(double) * std::max<size_t>(n6 * n6, 1)));
+  SGBA_CK(cudaMemsetAsync(d.S, 0, sizeof(double) * std::max<size_t>(n6 * n6, 1), p->stream));
   // single-launch cluster solver when the dense system fits one cluster's
   // distributed shared memory; it reads the float-float copy of S
   sgba::dense_cluster_setup(s.n6, &s.dense_c, &s.dense_smem);
@@ -776,7 +813,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   }
   if (s.dense_c > 0 || s.small_dense) {
     if ((st = dev_alloc(p, &d.S2, n6 * n6))) return st;
-    SGBA_CK(cudaMemset(d.S2, 0, sizeof(float2) * std::max<size_t>(n6 * n6, 1)));
+    SGBA_CK(cudaMemsetAsync(d.S2, 0, sizeof(float2) * std::max<size_t>(n6 * n6, 1), p->stream));
   }
   // point blocks keep the FP32 Cholesky while no pivot loses more than three
   // digits; the others are redone in float-float by a 64-CTA pass
@@ -803,13 +840,35 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_alloc(p, &d.x, n6))) return st;
   if ((st = dev_alloc(p, &d.xdd, 2 * n6))) return st;
   if ((st = dev_alloc(p, &d.r, n6))) return st;
-  SGBA_CK(cudaMemset(d.x, 0, sizeof(double) * std::max<size_t>(n6, 1)));
-  SGBA_CK(cudaMemset(d.dm, 0, sizeof(double) * std::max<size_t>(3 * P.nm, 1)));
+  SGBA_CK(cudaMemsetAsync(d.x, 0, sizeof(double) * std::max<size_t>(n6, 1), p->stream));
+  SGBA_CK(cudaMemsetAsync(d.dm, 0, sizeof(double) * std::max<size_t>(3 * P.nm, 1), p->stream));
   d.part_cap = sgba::cost_partials_needed(s);
   if ((st = dev_alloc(p, &d.part, static_cast<size_t>(d.part_cap)))) return st;
   if ((st = dev_alloc(p, &d.ctrl, 1))) return st;
-  SGBA_CK(cudaMemset(d.ctrl, 0, sizeof(Ctrl)));
+  SGBA_CK(cudaMemsetAsync(d.ctrl, 0, sizeof(Ctrl), p->stream));
   if ((st = dev_alloc(p, &d.last_rec, 1))) return st;
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  // The per-observation host tables are on the device now; the host keeps
+  // only what the queries after creation read (counts, block maps, the S
+  // pattern). Releasing the rest lets the next problem's set-up reuse the
+  // memory instead of faulting in fresh pages.
+  release(P.ord);
+  release(P.obs_pose);
+  release(P.obs_pt);
+  release(P.g_begin);
+  release(P.g_pose);
+  release(P.g_pt);
+  release(P.pt_g_begin);
+  release(P.fb_pose);
+  release(P.mb_pt);
+  release(P.cam_g_begin);
+  release(P.cam_g);
+  release(P.tile_fb);
+  release(P.tile_begin);
+  release(P.tile_end);
+  release(P.fb_tile_begin);
+  release(P.chunk_begin);
+  release(P.block_chunk_begin);
   return SGBA_OK;
 }
 
@@ -884,6 +943,8 @@ int sgba_problem_create(const sgba_problem_desc* desc, int32_t device, sgba_prob
   if (e != cudaSuccess) { delete p; return set_error(SGBA_ERR_CUDA, "cudaSetDevice(%d): %s", dev, cudaGetErrorString(e)); }
   e = cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete p; return set_error(SGBA_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)); }
+  p->pool = problem_pool(dev);
+  if (!p->pool) { sgba_problem_destroy(p); return set_error(SGBA_ERR_CUDA, "device memory pool of device %d", dev); }
   st = upload(p, desc);
   if (st) { sgba_problem_destroy(p); return st; }
   *out = p;
@@ -896,7 +957,7 @@ int sgba_problem_destroy(sgba_problem* p) {
   if (p->stream) cudaStreamSynchronize(p->stream);
   if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
   if (p->graph) cudaGraphDestroy(p->graph);
-  for (void* v : p->allocs) cudaFree(v);
+  for (void* v : p->allocs) cudaFreeAsync(v, p->stream);  // back to the pool, in stream order
   if (p->flush_buf) cudaFree(p->flush_buf);
   if (p->d.records) cudaFree(p->d.records);
   if (p->stream) cudaStreamDestroy(p->stream);
@@ -1102,13 +1163,20 @@ int sgba_export_pattern(sgba_problem* p, int32_t* h_rows, int32_t* h_cols, int32
   if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
   const Plan& P = p->plan;
   if (h_rows && h_cols) {
+    // the pose and point of every reduced term, read back from the device
+    std::vector<int32_t> g_pose(P.ng), g_pt(P.ng);
+    SGBA_CK(cudaSetDevice(p->device));
+    if (P.ng > 0) {
+      SGBA_CK(cudaMemcpy(g_pose.data(), p->d.g_pose, sizeof(int32_t) * P.ng, cudaMemcpyDeviceToHost));
+      SGBA_CK(cudaMemcpy(g_pt.data(), p->d.g_pt, sizeof(int32_t) * P.ng, cudaMemcpyDeviceToHost));
+    }
     int64_t k = 0;
     for (int f = 0; f < P.nf; ++f)
       if (P.cnt_f[f] > 0) { h_rows[k] = f; h_cols[k] = f; ++k; }
     for (int m = 0; m < P.nm; ++m)
       if (P.cnt_m[m] > 0) { h_rows[k] = P.nf + m; h_cols[k] = P.nf + m; ++k; }
     for (int64_t g = 0; g < P.ng; ++g) {
-      int fb = P.pose_fb[P.g_pose[g]], mb = P.pt_mb[P.g_pt[g]];
+      int fb = P.pose_fb[g_pose[g]], mb = P.pt_mb[g_pt[g]];
       if (fb >= 0 && mb >= 0) { h_rows[k] = P.nf + mb; h_cols[k] = fb; ++k; }
     }
   }
