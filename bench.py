@@ -294,12 +294,14 @@ def run_windows(args, ws, rank, local):
         clocks.start()
         t0 = time.perf_counter()
         ms = []
+        launches = 0
         for _ in range(K):
             out = native.batch_optimize(probs, params)
             for (recs, term, wms, fc, st) in out:
                 if st != native.OK:
                     raise RuntimeError("window failed with status %d: %s" % (st, native.last_error()))
                 ms.append(wms)
+            launches += sum(int(p.profile().kernel_launches) for p in probs)
         dt = _barrier_and_max(time.perf_counter() - t0, ws)
         clk = clocks.stop()
     finally:
@@ -321,7 +323,7 @@ def run_windows(args, ws, rank, local):
               + w.pose_const.nbytes for w in wins)
     d2h = sum(a.nbytes + b.nbytes for a, b in res)
     ms = np.array(ms)
-    return dict(value=N_WINDOWS * K * ws / dt, dt=dt, p50=float(np.percentile(ms, 50)),
+    return dict(value=N_WINDOWS * K * ws / dt, dt=dt, launches=launches, p50=float(np.percentile(ms, 50)),
                 p99=float(np.percentile(ms, 99)), clk=clk, e2e=N_WINDOWS * e2e_steps * ws / e2e_s, h2d=h2d, d2h=d2h,
                 n_obs=int(sum(w.n_obs for w in wins)), wins=wins, params=params, pkg=pkg)
 
@@ -451,6 +453,7 @@ def main():
                                    "one sgba_batch_optimize per step" % (N_WINDOWS, WINDOW_ITERS),
                        "n_obs_total": out["n_obs"], "l2": "inputs larger than L2 (all windows resident)"},
             "window_ms": {"p50": out["p50"], "p99": out["p99"]},
+            "gpu_launches": int(out["launches"]),
             "roofline": None,
             "e2e": {"value": out["e2e"], "unit": "windows/s", "h2d_bytes_per_step": int(out["h2d"]),
                     "d2h_bytes_per_step": int(out["d2h"]),

@@ -1411,7 +1411,8 @@ int sgba_batch_optimize(sgba_problem* const* problems, int32_t n, const sgba_opt
       }
       nu = c.nu;
     }
-    sgba::launch_linearize(p->sz, p->d, nu, true, p->stream);
+    const int final_launches = sgba::launch_linearize(p->sz, p->d, nu, true, p->stream);
+    p->prof.kernel_launches = 3 + static_cast<int64_t>(iters) * p->iter_launches + final_launches;
     cudaEventRecord(e1[w], p->stream);
   }
   // 3. collect
