@@ -495,8 +495,9 @@ def main():
                                 "(%d panel steps of 24 pivots), forward/backward sweeps of the same length"
                                 % ((n6 - lay.border_rows + 23) // 24))
         else:
-            roofline["note"] = ("latency-bound dependency chain (one cluster of 16 CTAs: %d panel steps + 3 "
-                                "triangular sweeps); FP32 work %.0f MFLOP per launch" % ((n6 + 23) // 24, n6 ** 3 / 3e6))
+            roofline["note"] = ("latency-bound dependency chain (one cluster of 16 CTAs: %d panel steps, then a "
+                                "forward and a backward sweep per solve, one solve plus one or two refinement "
+                                "solves); FP32 work %.0f MFLOP per launch" % ((n6 + 23) // 24, n6 ** 3 / 3e6))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": K, "warmup": args.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak" if ws > 1 else "weak",
