@@ -484,9 +484,12 @@ struct LinArgs {
   dd huber_dd;
 };
 
-__global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
+__global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
   if (halted(ctrl)) return;
   __shared__ float red[8][9][33];
+  // float-float path: the Jacobians of each lane's first term (a term with
+  // one observation), kept from the sums for the Z pass; [value][lane]
+  __shared__ float jcache[8][36][32];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int warps_per_block = blockDim.x >> 5;
@@ -576,9 +579,16 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
       for (int k = 0; k < 9; ++k) acc[k] = dd_make(0.f, 0.f);
       for (int64_t g = g0 + lane; g < g1; g += 32) {
         const float* Pd = a.pose_dd + 24 * a.g_pose[g];
+        const bool keep = (g == g0 + lane) && (a.g_begin[g + 1] - a.g_begin[g] == 1);
         for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
           JacD J;
           jacobians_dd(Pd, pxd, pyd, pzd, a.fxd, a.fyd, &J);
+          if (keep) {
+#pragma unroll
+            for (int k = 0; k < 12; ++k) { jcache[wib][2 * k][lane] = J.jp[k].hi; jcache[wib][2 * k + 1][lane] = J.jp[k].lo; }
+#pragma unroll
+            for (int k = 0; k < 6; ++k) { jcache[wib][24 + 2 * k][lane] = J.jm[k].hi; jcache[wib][25 + 2 * k][lane] = J.jm[k].lo; }
+          }
           float2 r = a.res[o];
           dd r0, r1;
           if (a.res_lo) {
@@ -694,9 +704,17 @@ __global__ void __launch_bounds__(256) k_landmark(LinArgs a, Ctrl* ctrl) {
         dd Wd[18];
         for (int k = 0; k < 18; ++k) Wd[k] = dd_make(0.f, 0.f);
         const float* Pd = a.pose_dd + 24 * pj;
+        const bool kept = (g == g0 + lane) && (a.g_begin[g + 1] - a.g_begin[g] == 1);
         for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
           JacD J;
-          jacobians_dd(Pd, pxd, pyd, pzd, a.fxd, a.fyd, &J);
+          if (kept) {  // the same Jacobians as in the sums above
+#pragma unroll
+            for (int k = 0; k < 12; ++k) J.jp[k] = dd_make(jcache[wib][2 * k][lane], jcache[wib][2 * k + 1][lane]);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) J.jm[k] = dd_make(jcache[wib][24 + 2 * k][lane], jcache[wib][25 + 2 * k][lane]);
+          } else {
+            jacobians_dd(Pd, pxd, pyd, pzd, a.fxd, a.fyd, &J);
+          }
           for (int r = 0; r < 6; ++r)
             for (int q = 0; q < 3; ++q)
               Wd[r * 3 + q] = dd_add(Wd[r * 3 + q], dd_add(dd_mul(J.jp[r], J.jm[q]), dd_mul(J.jp[6 + r], J.jm[3 + q])));
