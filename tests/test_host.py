@@ -88,3 +88,39 @@ def test_huber_kernel_matches_reference_formula(pkg):
     k = pkg.HuberKernel.new(1.0)
     assert k.apply(0.5) == 0.25 and k.apply(3.0) == 5.0
     assert k.weight(0.0) == 0.0 and abs(k.weight(3.0) - np.sqrt(5.0) / 3.0) < 1e-15
+
+
+def test_concurrent_validation_reports_first_bad_observation(pkg):
+    """sgba_problem_create validates observations in parallel chunks on the
+    host worker pool; the error names the first bad observation, as a
+    sequential scan would, also with several host threads creating problems
+    at once (their parallel regions share the pool). No CUDA call is reached."""
+    import threading
+
+    base = pkg.synth.generate(pkg.synth.CIRCLE, n_cam=10, n_pt=6000, seed=pkg.synth.BASE_SEED + 7)
+    assert base.n_obs > 40000  # several chunks of the parallel scan
+    E = pkg.native.SgbaError
+    errors = []
+
+    def worker(t):
+        try:
+            for r in range(8):
+                first = 1000 + 5000 * t + 37 * r
+                bad = base.copy()
+                bad.obs_pt[base.n_obs - 3] = base.n_pt + 1  # a later bad one, in another chunk
+                bad.obs_pt[first] = base.n_pt
+                try:
+                    pkg.native.Problem(bad, device=0)
+                    errors.append("thread %d: no error" % t)
+                except E as e:
+                    if e.status != pkg.native.ERR_INVALID_ARGUMENT or "observation %d:" % first not in e.message:
+                        errors.append("thread %d: %s" % (t, e.message))
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append("thread %d: %r" % (t, e))
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
