@@ -730,7 +730,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
   X.n = a.n;
   X.cv = &s_cv;
   X.T = &T;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x;
   if (tid == 0) carve(X.P, X.C, X.rank, &s_cv);
   if (tid < X.C) {
     Carve rc;

@@ -225,13 +225,6 @@ __device__ __forceinline__ dd warp_transpose_sum(const float* vals, float (*red)
   return acc;
 }
 
-__device__ __forceinline__ dd shfl_dd(dd v, int src) {
-  dd o;
-  o.hi = __shfl_sync(0xffffffffu, v.hi, src);
-  o.lo = __shfl_sync(0xffffffffu, v.lo, src);
-  return o;
-}
-
 // The same Jacobians in float-float, for ill-conditioned point blocks.
 struct JacD {
   dd jp[12];
