@@ -15,19 +15,20 @@
 // rows are identity).  Row block r (rows 24r..24r+23, columns 0..24r+23) lives
 // in the shared memory of cluster rank r % C.  Per panel step p:
 //   owner(p), warp 0: LDL^T of the diagonal block, 1/d and the inverse of
-//      its unit lower factor;
+//      its unit lower factor; then all its threads store that inverse and
+//      1/d into every CTA (DSMEM stores);
 //   -- cluster barrier --
-//   every CTA copies that inverse and 1/d (DSMEM loads), then for its row
-//      blocks r > p: W_rp = A_rp L_pp^-T, L_rp = W_rp D^-1;
+//   every CTA, its row blocks r > p: W_rp = A_rp L_pp^-T, L_rp = W_rp D^-1;
 //   -- cluster barrier --
 //   every CTA, row blocks r > p: A_rs -= W_rp L_sp^T for p < s <= r, L_sp
 //      read in place from its owner's shared memory.  The owner of p+1
 //      updates block p+1 first; its warp 0 then runs the diagonal step of
 //      p+1 while the other warps finish the update.
 // Triangular solves: one split cluster barrier per 24-row block; the owner
-// of the block does only the critical 24x24 work before arriving, every CTA
-// folds the older solution pieces into its accumulators while the barrier
-// completes.
+// of the block does only the critical 24x24 work before arriving (in the
+// forward sweep it also stores its piece of y into the next block's owner),
+// every CTA folds the older solution pieces into its accumulators while the
+// barrier completes.
 //
 // GB300 notes that shaped the code (measured): a cluster barrier costs ~400
 // cycles and a DSMEM load ~200, while warp shuffles in long chains and DSMEM
@@ -66,7 +67,7 @@ __host__ __device__ inline int row_ld(int r) { return kNB * (r + 1) + 4; }
 struct Carve {
   int nown;
   int rowoff[kMaxOwn];
-  int wt, linv, dloc, rdloc, lpp, rdp, y, x, xs, xlo, bl, facc, accb, vdef, udef, red, tmp, tmp2, colbuf, flags, total;
+  int wt, linv, dloc, rdloc, lpp, rdp, y, x, xs, xlo, bl, facc, accb, vdef, udef, red, tmp, tmp2, colbuf, ynext, flags, total;
 };
 
 __host__ __device__ inline void carve(int P, int C, int rank, Carve* c) {
@@ -98,6 +99,7 @@ __host__ __device__ inline void carve(int P, int C, int rank, Carve* c) {
   c->tmp = take(32);
   c->tmp2 = take(32);
   c->colbuf = take(64);
+  c->ynext = take(32);
   c->flags = take(4);
   c->total = off;
 }
@@ -130,6 +132,7 @@ __device__ __forceinline__ void cl_sync() {
 struct RankTab {
   int rowoff[kMaxCluster][kMaxOwn];
   int linv[kMaxCluster], rdloc[kMaxCluster], y[kMaxCluster], x[kMaxCluster], accb[kMaxCluster], flags[kMaxCluster];
+  int lpp[kMaxCluster], rdp[kMaxCluster], ynext[kMaxCluster];
 };
 
 struct Ctx {
@@ -227,25 +230,28 @@ __device__ void diag_step(const Ctx& X, int p, int* bad_flag) {
   }
 }
 
-// Every CTA after the barrier of step p: copy Linv_pp and 1/d_p from the
-// owner of p (one float4 per thread).
-__device__ void pull_diag(const Ctx& X, cg::cluster_group& cl, int p) {
+// The owner of block b, all threads, after its diagonal step: Linv_bb and
+// 1/d_b into every CTA's lpp / rdp (DSMEM stores; the next cluster barrier
+// publishes them). Their previous contents were last read by panel_rows of
+// the step before, which every CTA finished before that step's second barrier.
+__device__ void push_diag(const Ctx& X, cg::cluster_group& cl, int b) {
   constexpr int kRowsF4 = kNB * (kLd / 4), kAllF4 = kRowsF4 + kNB / 4;
-  const int op = p % X.C, jp = p / X.C;
-  for (int q = threadIdx.x; q < kAllF4; q += kThreads) {
+  const int jb = b / X.C;
+  const float4* lsrc = reinterpret_cast<const float4*>(X.sm + X.cv->linv + kNB * kLd * jb);
+  const float4* rsrc = reinterpret_cast<const float4*>(X.sm + X.cv->rdloc + kNB * jb);
+  for (int e = threadIdx.x; e < kAllF4 * X.C; e += kThreads) {
+    const int c = e / kAllF4, q = e - c * kAllF4;
     if (q < kRowsF4) {
-      const float4* src = reinterpret_cast<const float4*>(remote(cl, X.sm, op, X.T->linv[op] + kNB * kLd * jp));
-      reinterpret_cast<float4*>(X.sm + X.cv->lpp)[q] = src[q];
+      reinterpret_cast<float4*>(remote(cl, X.sm, c, X.T->lpp[c]))[q] = lsrc[q];
     } else {
-      const float4* src = reinterpret_cast<const float4*>(remote(cl, X.sm, op, X.T->rdloc[op] + kNB * jp));
-      reinterpret_cast<float4*>(X.sm + X.cv->rdp)[q - kRowsF4] = src[q - kRowsF4];
+      reinterpret_cast<float4*>(remote(cl, X.sm, c, X.T->rdp[c]))[q - kRowsF4] = rsrc[q - kRowsF4];
     }
   }
 }
 
 // Panel step p, every CTA: for the owned row blocks r > p,
 // W_rp = A_rp Linv_pp^T (kept transposed for the update) and L_rp = W_rp D^-1
-// in place.  Linv_pp and 1/d were pulled from the owner of p.  4x4 register
+// in place.  Linv_pp and 1/d were pushed by the owner of p.  4x4 register
 // tiles from float4 shared-memory reads; every entry is summed over k in order.
 __device__ void panel_rows(const Ctx& X, int p) {
   int j0 = 0;
@@ -419,17 +425,20 @@ __device__ void update_blocks(const Ctx& X, cg::cluster_group& cl, int p, int r_
   }
 }
 
-// L y = bl over the 24-row blocks.  The owner of block p pulls y_{p-1} from
-// its owner, adds L_{p,p-1} y_{p-1} to its accumulator, forms y_p in its own
-// shared memory and arrives; meanwhile every CTA pulls y_{p-1} and folds it
-// into the accumulators of its other blocks.  Pieces of y stay with their
-// owners (the backward pass reads only its own).
+// L y = bl over the 24-row blocks.  The owner of block p finds y_{p-1} in its
+// own ynext (stored there by the owner of p-1 before the previous barrier),
+// adds L_{p,p-1} y_{p-1} to its accumulator, forms y_p in its own shared
+// memory, stores a copy into the ynext of the owner of p+1 and arrives;
+// meanwhile every CTA pulls y_{p-1} and folds it into the accumulators of its
+// other blocks.  Pieces of y stay with their owners (the backward pass reads
+// only its own).  The next store into a CTA's ynext follows its read: at
+// least one cluster barrier later when C > 1, after the warp barrier of the
+// same step when C = 1.
 __device__ void solve_forward(const Ctx& X, cg::cluster_group& cl) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   float* y = X.sm + X.cv->y;
   float* facc = X.sm + X.cv->facc;
   float* tmp = X.sm + X.cv->tmp;
-  float* tmp2 = X.sm + X.cv->tmp2;
   const float* bl = X.sm + X.cv->bl;
   for (int e = tid; e < X.cv->nown * kNB; e += kThreads) facc[e] = 0.f;
   __syncthreads();
@@ -437,27 +446,36 @@ __device__ void solve_forward(const Ctx& X, cg::cluster_group& cl) {
   for (int p = 0; p < X.P; ++p) {
     if (X.owns(p) && warp == 0) {
       const int jp = p / X.C;
-      if (p > 0 && lane < kNB) {
-        const int oq = (p - 1) % X.C;
-        tmp2[lane] = remote(cl, X.sm, oq, X.T->y[oq])[kNB * (p - 1) + lane];
-      }
-      __syncwarp();
+      const float* yprev = X.sm + X.cv->ynext;  // y_{p-1}, stored here by its owner
       if (lane < kNB) {
-        float s = facc[kNB * jp + lane];
+        float s0 = facc[kNB * jp + lane], s1 = 0.f, s2 = 0.f, s3 = 0.f;
         if (p > 0) {
-          const float* lr = X.rowblk(p) + lane * X.ld(p) + kNB * (p - 1);
+          const float4* lr = reinterpret_cast<const float4*>(X.rowblk(p) + lane * X.ld(p) + kNB * (p - 1));
+          const float4* yq = reinterpret_cast<const float4*>(yprev);
 #pragma unroll
-          for (int k = 0; k < kNB; ++k) s = fmaf(lr[k], tmp2[k], s);
+          for (int q = 0; q < kNB / 4; ++q) {
+            const float4 a4 = lr[q], b4 = yq[q];
+            s0 = fmaf(a4.x, b4.x, s0); s1 = fmaf(a4.y, b4.y, s1); s2 = fmaf(a4.z, b4.z, s2); s3 = fmaf(a4.w, b4.w, s3);
+          }
         }
-        tmp[lane] = bl[kNB * p + lane] - s;
+        tmp[lane] = bl[kNB * p + lane] - ((s0 + s1) + (s2 + s3));
       }
       __syncwarp();
       if (lane < kNB) {
-        const float* li = X.sm + X.cv->linv + kNB * kLd * jp + lane * kLd;
-        float v = 0.f;
+        const float4* li = reinterpret_cast<const float4*>(X.sm + X.cv->linv + kNB * kLd * jp + lane * kLd);
+        const float4* t4 = reinterpret_cast<const float4*>(tmp);
+        float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
 #pragma unroll
-        for (int j = 0; j < kNB; ++j) v = fmaf(li[j], tmp[j], v);
+        for (int q = 0; q < kNB / 4; ++q) {
+          const float4 a4 = li[q], b4 = t4[q];
+          v0 = fmaf(a4.x, b4.x, v0); v1 = fmaf(a4.y, b4.y, v1); v2 = fmaf(a4.z, b4.z, v2); v3 = fmaf(a4.w, b4.w, v3);
+        }
+        const float v = (v0 + v1) + (v2 + v3);
         y[kNB * p + lane] = v;
+        if (p + 1 < X.P) {  // to the owner of the next block, before this block's barrier
+          const int on = (p + 1) % X.C;
+          remote(cl, X.sm, on, X.T->ynext[on])[lane] = v;
+        }
       }
     }
     __syncthreads();
@@ -693,10 +711,12 @@ __device__ void load_rows(const Ctx& X, const DenseArgs& a, float alpha) {
 __device__ void factor(const Ctx& X, cg::cluster_group& cl, int* flags) {
   const int warp = threadIdx.x >> 5;
   if (X.rank == 0 && warp == 0) diag_step(X, 0, flags);
-  for (int p = 0; p < X.P; ++p) {
-    cl_sync();  // Linv_pp and 1/d_p final in the owner of p
-    pull_diag(X, cl, p);
+  if (X.rank == 0) {
     __syncthreads();
+    push_diag(X, cl, 0);
+  }
+  for (int p = 0; p < X.P; ++p) {
+    cl_sync();  // Linv_pp and 1/d_p pushed into every CTA
     panel_rows(X, p);
     cl_sync();  // L_rp final for every r > p
     if (p + 1 < X.P) {
@@ -708,6 +728,10 @@ __device__ void factor(const Ctx& X, cg::cluster_group& cl, int* flags) {
       } else {
         update_blocks(X, cl, p, p + 1, X.P - 1, 0, kWarps);
       }
+    }
+    if (p + 1 < X.P && X.owns(p + 1)) {
+      __syncthreads();  // the diagonal step of p + 1 is done
+      push_diag(X, cl, p + 1);
     }
   }
   __syncthreads();
@@ -742,6 +766,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
     T.x[tid] = rc.x;
     T.accb[tid] = rc.accb;
     T.flags[tid] = rc.flags;
+    T.lpp[tid] = rc.lpp;
+    T.rdp[tid] = rc.rdp;
+    T.ynext[tid] = rc.ynext;
   }
   __syncthreads();
   int* flags = reinterpret_cast<int*>(dsm + s_cv.flags);
