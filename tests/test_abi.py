@@ -47,3 +47,41 @@ def test_null_arguments_fail_cleanly_without_gpu(pkg):
     desc.n_cam = 0
     assert L.sgba_problem_create(ctypes.byref(desc), 0, ctypes.byref(h)) == pkg.native.ERR_INVALID_ARGUMENT
     assert L.sgba_optimizer_init(None, None) == pkg.native.ERR_INVALID_ARGUMENT
+
+
+def _c_structs(text):
+    """typedef struct { ... } name; -> [field names in order] (comments removed)."""
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"typedef\s+struct\s*\{(.*?)\}\s*(\w+)\s*;", text, flags=re.S):
+        fields = []
+        for decl in m.group(1).split(";"):
+            decl = decl.strip()
+            if decl:
+                fields.append(re.match(r".*?(\w+)\s*(\[[^\]]*\])?$", decl, flags=re.S).group(1))
+        out[m.group(2)] = fields
+    return out
+
+
+def _rust_structs(text):
+    out = {}
+    for m in re.finditer(r"pub struct (\w+)\s*\{(.*?)\n\}", text, flags=re.S):
+        out[m.group(1)] = re.findall(r"^\s*pub (\w+)\s*:", m.group(2), flags=re.M)
+    return out
+
+
+def test_rust_ffi_declarations_match_the_header():
+    """rust/sgba-sys/src/ffi.rs declares every function of include/sgba.h and
+    its structs with the same fields in the same order (the crate is not
+    compiled here; this keeps the declarations in step with the header)."""
+    header = open(os.path.join(ROOT, "include", "sgba.h")).read()
+    ffi = open(os.path.join(ROOT, "rust", "sgba-sys", "src", "ffi.rs")).read()
+    c_fns = set(re.findall(r"^\s*(?:int|int32_t|size_t)\s+\**\s*(sgba_\w+)\s*\(",
+                           re.sub(r"/\*.*?\*/", "", header, flags=re.S), flags=re.M))
+    rust_fns = set(re.findall(r"pub fn (sgba_\w+)\s*\(", ffi))
+    assert c_fns and c_fns == rust_fns, (sorted(c_fns - rust_fns), sorted(rust_fns - c_fns))
+    c_structs = _c_structs(header)
+    rust_structs = _rust_structs(ffi)
+    for name, fields in c_structs.items():
+        assert name in rust_structs, name
+        assert rust_structs[name] == fields, (name, fields, rust_structs[name])
