@@ -249,10 +249,12 @@ def run_gpu(args, ws, rank, local):
     e2e_params = pkg.OptParams(num_iterations=wl["n_iter"], initial_lm_damping=prob.initial_lm_damping,
                                function_tolerance=0.0, gradient_tolerance=0.0, parameter_tolerance=0.0,
                                max_consecutive_rejects=1 << 40, solver=pkg.LinearSolverEnum.SchurBlockSparseLdlt)
-    # one untimed warm-up of the path (context, module load)
+    # one untimed warm-up of the path (context, module load); its per-iteration
+    # merits are compared with the oracle's below
     with native.Problem(host, device=device) as gp:
-        gp.optimize(e2e_params)
+        warm_recs, _ = gp.optimize(e2e_params)
         gp.variables()
+    gpu_merits = [r.merit for r in warm_recs]
     _barrier(ws)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -264,7 +266,7 @@ def run_gpu(args, ws, rank, local):
            host.obs_uv.nbytes + host.pose_const.nbytes)
     d2h = poses.nbytes + points.nbytes
     out.update(dict(ms=ms_max, launches=launches, kt=kt, clk=clk, e2e_s=e2e_s, e2e_steps=e2e_steps, h2d=h2d,
-                    d2h=d2h, pinned=pinned, prob=prob))
+                    d2h=d2h, pinned=pinned, prob=prob, gpu_merits=gpu_merits))
     return out
 
 
@@ -341,6 +343,7 @@ def cpu_baseline(prob, pkg, n_iter, threads):
     t0 = time.perf_counter()
     recs, _, _ = ob.optimize(prob, params, n_threads=threads)
     dt = time.perf_counter() - t0
+    cpu_baseline.last_merits = [r.merit for r in recs]
     return len(recs) / dt, dt
 
 
@@ -527,6 +530,16 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": "%d LM iterations of the workload on %d threads (%.1f s, setup included)"
                                           % (n_cpu, threads, dt)}
+        # the same optimisation from the same start: per-iteration merit of the
+        # e2e run against the oracle's (FP64 restatement of the reference)
+        ora = getattr(cpu_baseline, "last_merits", [])
+        gpu = out.get("gpu_merits", [])
+        k = min(len(ora), len(gpu))
+        if k > 0:
+            dev = max(abs(g - o) / abs(o) for g, o in zip(gpu[:k], ora[:k]) if o != 0.0)
+            line["parity"] = {"per_iteration_cost_max_rel_dev": dev, "iterations_compared": k,
+                              "final_cost_rel_gap": abs(gpu[k - 1] - ora[k - 1]) / abs(ora[k - 1]),
+                              "reference": "oracle (FP64 CPU restatement of the reference)"}
     print(json.dumps(line))
 
 
