@@ -491,6 +491,15 @@ def main():
                 "frac": achieved / hbm_peak, "peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes": alg, "ms_per_launch": kt[rl_kernel],
                 "traffic": traffic.get(rl_kernel)}
+    # every timed kernel against the same peak: algorithmic bytes per launch
+    # over its live time, with its DRAM traffic per launch from ncu
+    kernel_roofline = {}
+    for k, ms in kt.items():
+        b = _kernel_bytes(k, lay, prob)
+        if b is not None and ms > 0:
+            a = b / (ms / 1000.0) / 1e9
+            kernel_roofline[k] = {"achieved_gbs": a, "frac": a / hbm_peak, "algorithmic_bytes": b,
+                                  "ms_per_launch": ms, "traffic": traffic.get(k)}
     if rl_kernel == "factor":
         n6 = 6 * lay.n_free_poses
         if lay.solver == 1:
@@ -515,6 +524,7 @@ def main():
         "kernel_ms": kt,
         "phase_ms_per_iteration": out.get("phase_ms"),
         "roofline": roofline,
+        "kernel_roofline": kernel_roofline,
         "gpu_launches": int(out["launches"]),
         "e2e": {"value": WORKLOADS[args.workload]["n_iter"] * out["e2e_steps"] * ws / out["e2e_s"], "unit": UNIT,
                 "h2d_bytes_per_step": int(out["h2d"]), "d2h_bytes_per_step": int(out["d2h"]),
