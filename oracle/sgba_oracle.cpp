@@ -275,7 +275,7 @@ struct Term {
 // in f64: residual, d_pi*R_cw, J_pose = d_pi_r_cw * [hat(-p), I], J_pt = -d_pi_r_cw.
 void eval_term_f64(const double* pose, const double* p, const double* intr,
                    const double* uv, double huber, double* r, double* jp,
-                   double* jm, double* w_out, double* cost_out) {
+                   double* jm, double* w_out, double* cost_out, double* jc = nullptr) {
   double cw[7];
   se3_inverse(pose, cw);
   double rm[9];
@@ -286,6 +286,12 @@ void eval_term_f64(const double* pose, const double* p, const double* intr,
   double u = xc[0] / xc[2], v = xc[1] / xc[2];
   r[0] = uv[0] - (u * intr[0] + intr[2]);
   r[1] = uv[1] - (v * intr[1] + intr[3]);
+  if (jc) {
+    // J_cam = -dx_distort_params(proj) (pinhole_reprojection.rs:85;
+    // affine.rs:77-108): params (fx, fy, cx, cy), 2x4 row-major
+    const double j[8] = {-u, 0.0, -1.0, 0.0, 0.0, -v, 0.0, -1.0};
+    for (int i = 0; i < 8; ++i) jc[i] = j[i];
+  }
   // dx_distort_x * dx_proj_x (2x3)
   double z = xc[2];
   double dpi[6] = {intr[0] * (1.0 / z), 0.0, intr[0] * (-xc[0] / (z * z)),
@@ -352,6 +358,57 @@ void make_term(const double* pose, const double* p, const double* intr,
     t->gm[a] = Jm[a] * rw[0] + Jm[3 + a] * rw[1];
   }
   t->cost = cost;
+}
+
+// The blocks of a term that involve Free intrinsics (kinds (F, F, M)):
+// J_cam^T J_cam, J_pose^T J_cam (pose row, intrinsics column), J_pt^T J_cam
+// (point row, intrinsics column) and J_cam^T r~.
+template <class R>
+struct CamTerm {
+  R hcc[16];
+  R hpc[24];
+  R hmc[12];
+  R gc[4];
+};
+
+// make_term plus the intrinsics blocks (same arithmetic for the Term part).
+template <class R>
+void make_term_cam(const double* pose, const double* p, const double* intr,
+                   const double* uv, double huber, Term<R>* t, CamTerm<R>* ct) {
+  double r[2], jp[12], jm[6], jc[8], w, cost;
+  eval_term_f64(pose, p, intr, uv, huber, r, jp, jm, &w, &cost, jc);
+  R Jp[12], Jm[6], Jc[8], rw[2];
+  for (int i = 0; i < 12; ++i) Jp[i] = static_cast<R>(jp[i]);
+  for (int i = 0; i < 6; ++i) Jm[i] = static_cast<R>(jm[i]);
+  for (int i = 0; i < 8; ++i) Jc[i] = static_cast<R>(jc[i]);
+  rw[0] = static_cast<R>(w * r[0]);
+  rw[1] = static_cast<R>(w * r[1]);
+  for (int a = 0; a < 6; ++a) {
+    for (int b = 0; b < 6; ++b) t->hpp[a * 6 + b] = Jp[a] * Jp[b] + Jp[6 + a] * Jp[6 + b];
+    t->gp[a] = Jp[a] * rw[0] + Jp[6 + a] * rw[1];
+  }
+  for (int a = 0; a < 3; ++a) {
+    for (int b = 0; b < 3; ++b) t->hmm[a * 3 + b] = Jm[a] * Jm[b] + Jm[3 + a] * Jm[3 + b];
+    for (int b = 0; b < 6; ++b) t->hmp[a * 6 + b] = Jm[a] * Jp[b] + Jm[3 + a] * Jp[6 + b];
+    t->gm[a] = Jm[a] * rw[0] + Jm[3 + a] * rw[1];
+  }
+  t->cost = cost;
+  for (int a = 0; a < 4; ++a) {
+    for (int b = 0; b < 4; ++b) ct->hcc[a * 4 + b] = Jc[a] * Jc[b] + Jc[4 + a] * Jc[4 + b];
+    ct->gc[a] = Jc[a] * rw[0] + Jc[4 + a] * rw[1];
+  }
+  for (int a = 0; a < 6; ++a)
+    for (int b = 0; b < 4; ++b) ct->hpc[a * 4 + b] = Jp[a] * Jc[b] + Jp[6 + a] * Jc[4 + b];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 4; ++b) ct->hmc[a * 4 + b] = Jm[a] * Jc[b] + Jm[3 + a] * Jc[4 + b];
+}
+
+template <class R>
+void cam_term_reduce(CamTerm<R>* a, const CamTerm<R>& b) {
+  for (int i = 0; i < 16; ++i) a->hcc[i] += b.hcc[i];
+  for (int i = 0; i < 24; ++i) a->hpc[i] += b.hpc[i];
+  for (int i = 0; i < 12; ++i) a->hmc[i] += b.hmc[i];
+  for (int i = 0; i < 4; ++i) a->gc[i] += b.gc[i];
 }
 
 template <class R>
@@ -634,7 +691,8 @@ void parallel_for(int64_t n, int n_threads, F&& f) {  // f(begin, end, thread_id
   for (auto& x : th) x.join();
 }
 
-double total_cost(const ora_problem* p, const double* poses, const double* points, int n_threads) {
+double total_cost(const ora_problem* p, const double* intr, const double* poses, const double* points,
+                  int n_threads) {
   // calc_total_cost (cost_fn.rs:403-433): sequential sum in sorted-term order
   // when not parallel; per-thread partial sums otherwise.
   int nt = std::max(1, n_threads);
@@ -643,7 +701,7 @@ double total_cost(const ora_problem* p, const double* poses, const double* point
     double acc = 0.0;
     for (int64_t i = b; i < e; ++i)
       acc += eval_cost_f64(poses + 7 * p->obs_cam[i], points + 3 * p->obs_pt[i],
-                           p->intrinsics, p->obs_uv + 2 * i, p->huber_delta);
+                           intr, p->obs_uv + 2 * i, p->huber_delta);
     part[t] = acc;
   });
   double c = 0.0;
@@ -658,38 +716,67 @@ struct System {
   std::vector<R> U, bp;    // nf*36, nf*6
   std::vector<R> V, bm;    // nm*9,  nm*3
   std::vector<R> Wr;       // per reduction range: 3x6 (point row, pose col) -- valid when both active
+  // Free intrinsics only (empty otherwise): their 4x4 block and neg_grad, and
+  // the blocks coupling them to each free pose (6x4) and marg point (3x4)
+  std::vector<R> Ucc, bc, Hpc, Hmc;
   double max_grad = 0.0;
 };
 
 // evaluate + populate_upper_triangular_normal_equation (cost_system.rs:74-273)
 template <class R>
-void build_system(const ora_problem* p, const Structure& s, const double* poses,
+void build_system(const ora_problem* p, const Structure& s, const double* intr, const double* poses,
                   const double* points, double nu, int n_threads, System<R>* sys) {
+  const bool fc = p->intrinsics_free != 0;
   sys->U.assign(static_cast<size_t>(s.nf) * 36, R(0));
   sys->bp.assign(static_cast<size_t>(s.nf) * 6, R(0));
   sys->V.assign(static_cast<size_t>(s.nm) * 9, R(0));
   sys->bm.assign(static_cast<size_t>(s.nm) * 3, R(0));
   int64_t nr = static_cast<int64_t>(s.rng_pt.size());
   sys->Wr.assign(static_cast<size_t>(nr) * 18, R(0));
+  if (fc) sys->Hmc.assign(static_cast<size_t>(s.nm) * 12, R(0));
   int nt = std::max(1, n_threads);
-  // Parallel over points (disjoint V/bm and W); pose sums per thread.
-  std::vector<std::vector<R>> Ut(nt), bpt(nt);
+  // Parallel over points (disjoint V/bm and W); pose (and intrinsics) sums per thread.
+  std::vector<std::vector<R>> Ut(nt), bpt(nt), Uct(nt), bct(nt), Hpct(nt);
   parallel_for(p->n_pt, nt, [&](int64_t pb, int64_t pe, int t) {
     Ut[t].assign(static_cast<size_t>(s.nf) * 36, R(0));
     bpt[t].assign(static_cast<size_t>(s.nf) * 6, R(0));
+    if (fc) {
+      Uct[t].assign(16, R(0));
+      bct[t].assign(4, R(0));
+      Hpct[t].assign(static_cast<size_t>(s.nf) * 24, R(0));
+    }
     for (int64_t q = pb; q < pe; ++q) {
       for (int64_t r = s.pt_rng_begin[q]; r < s.pt_rng_begin[q + 1]; ++r) {
         Term<R> term;
+        CamTerm<R> cterm;
         bool first = true;
         for (int64_t k = s.range_begin[r]; k < s.range_begin[r + 1]; ++k) {
           int64_t o = s.order[k];
           Term<R> tk;
-          make_term<R>(poses + 7 * p->obs_cam[o], points + 3 * p->obs_pt[o],
-                       p->intrinsics, p->obs_uv + 2 * o, p->huber_delta, &tk);
+          if (fc) {
+            CamTerm<R> ck;
+            make_term_cam<R>(poses + 7 * p->obs_cam[o], points + 3 * p->obs_pt[o], intr,
+                             p->obs_uv + 2 * o, p->huber_delta, &tk, &ck);
+            if (first) cterm = ck; else cam_term_reduce(&cterm, ck);
+          } else {
+            make_term<R>(poses + 7 * p->obs_cam[o], points + 3 * p->obs_pt[o],
+                         intr, p->obs_uv + 2 * o, p->huber_delta, &tk);
+          }
           if (first) { term = tk; first = false; } else { term_reduce(&term, tk); }
         }
         int pb_ = s.pose_block[s.rng_pose[r]];
         int mb = s.point_block[s.rng_pt[r]];
+        if (fc) {
+          // the intrinsics are touched by every term: nu I per evaluated term
+          R* uc = Uct[t].data();
+          for (int i = 0; i < 16; ++i) uc[i] += cterm.hcc[i];
+          if (nu != 0.0) for (int i = 0; i < 4; ++i) uc[i * 5] += static_cast<R>(nu);
+          for (int i = 0; i < 4; ++i) bct[t][i] -= cterm.gc[i];
+          if (pb_ >= 0)
+            for (int i = 0; i < 24; ++i) Hpct[t][static_cast<size_t>(pb_) * 24 + i] += cterm.hpc[i];
+          if (mb >= 0)
+            for (int i = 0; i < 12; ++i) sys->Hmc[static_cast<size_t>(mb) * 12 + i] += cterm.hmc[i];
+        }
         if (pb_ >= 0) {
           R* u = &Ut[t][static_cast<size_t>(pb_) * 36];
           for (int i = 0; i < 36; ++i) u[i] += term.hpp[i];
@@ -712,20 +799,40 @@ void build_system(const ora_problem* p, const Structure& s, const double* poses,
     for (size_t i = 0; i < sys->U.size(); ++i) sys->U[i] += Ut[t][i];
     for (size_t i = 0; i < sys->bp.size(); ++i) sys->bp[i] += bpt[t][i];
   }
+  if (fc) {
+    sys->Ucc.assign(16, R(0));
+    sys->bc.assign(4, R(0));
+    sys->Hpc.assign(static_cast<size_t>(s.nf) * 24, R(0));
+    for (int t = 0; t < nt; ++t) {
+      if (Uct[t].empty()) continue;
+      for (int i = 0; i < 16; ++i) sys->Ucc[i] += Uct[t][i];
+      for (int i = 0; i < 4; ++i) sys->bc[i] += bct[t][i];
+      for (size_t i = 0; i < sys->Hpc.size(); ++i) sys->Hpc[i] += Hpct[t][i];
+    }
+  }
   double mg = 0.0;
+  for (auto v : sys->bc) mg = std::max(mg, std::fabs(static_cast<double>(v)));
   for (auto v : sys->bp) mg = std::max(mg, std::fabs(static_cast<double>(v)));
   for (auto v : sys->bm) mg = std::max(mg, std::fabs(static_cast<double>(v)));
   sys->max_grad = mg;
 }
 
 // SchurFactor::factorize + solve (schur_ldlt.rs:536-812) with the sequential
-// forward pass (schur_ldlt.rs:241-278).  delta = [dx_f; dx_m].
+// forward pass (schur_ldlt.rs:241-278).  delta = [dx_c; dx_f; dx_m], dx_c the
+// 4 intrinsics when they are free (empty otherwise).  In S the intrinsics
+// come first (their family's partition precedes the poses'), padded to one
+// 6-row block with an identity so the factor keeps 6x6 blocks; the pivot rule
+// restarts at that block as at every partition block.
 template <class R>
 int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
                 int n_threads, std::vector<double>* delta, std::vector<double>* s_out,
                 std::vector<double>* rhs_out) {
+  const bool fc = p->intrinsics_free != 0;
   const int nf = s.nf;
   const int n6 = nf * 6;
+  const int nci = fc ? 6 : 0;  // rows of the (padded) intrinsics block in S
+  const int nc4 = fc ? 4 : 0;  // intrinsics scalars in delta
+  const int n = nci + n6;
   const int nt = std::max(1, n_threads);
   // S_ff = H_ff (diagonal blocks only for BA)
   std::vector<std::vector<R>> St(nt);
@@ -733,8 +840,8 @@ int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
   std::vector<R> hinv(static_cast<size_t>(s.nm) * 9);
   std::vector<int> fail(nt, 0);
   parallel_for(p->n_pt, nt, [&](int64_t qb, int64_t qe, int t) {
-    St[t].assign(static_cast<size_t>(n6) * n6, R(0));
-    rt[t].assign(n6, R(0));
+    St[t].assign(static_cast<size_t>(n) * n, R(0));
+    rt[t].assign(n, R(0));
     std::vector<int> fidx;
     std::vector<const R*> hmf;
     std::vector<R> inv_hmf;
@@ -767,7 +874,7 @@ int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
         int fi = fidx[i];
         // rhs_bar[f_i] -= H_mf_i^T * (H_mm^-1 g_m)
         for (int c = 0; c < 6; ++c)
-          rt[t][fi * 6 + c] -= hmf[i][0 * 6 + c] * ig[0] + hmf[i][1 * 6 + c] * ig[1] + hmf[i][2 * 6 + c] * ig[2];
+          rt[t][nci + fi * 6 + c] -= hmf[i][0 * 6 + c] * ig[0] + hmf[i][1 * 6 + c] * ig[1] + hmf[i][2 * 6 + c] * ig[2];
         for (size_t j = 0; j <= i; ++j) {
           int fj = fidx[j];
           size_t ii = i, jj = j;
@@ -780,43 +887,78 @@ int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
               R acc = hmf[ii][0 * 6 + r2] * inv_hmf[jj * 18 + 0 * 6 + c2] +
                       hmf[ii][1 * 6 + r2] * inv_hmf[jj * 18 + 1 * 6 + c2] +
                       hmf[ii][2 * 6 + r2] * inv_hmf[jj * 18 + 2 * 6 + c2];
-              sb[static_cast<size_t>(row * 6 + r2) * n6 + col * 6 + c2] -= acc;
+              sb[static_cast<size_t>(nci + row * 6 + r2) * n + nci + col * 6 + c2] -= acc;
             }
+        }
+      }
+      if (fc) {
+        // the intrinsics column: Y = H_mc (3x4), H_mm^-1 Y
+        const R* y = &sys.Hmc[static_cast<size_t>(mb) * 12];
+        R iy[12];
+        for (int i = 0; i < 3; ++i)
+          for (int c = 0; c < 4; ++c)
+            iy[i * 4 + c] = inv[i * 3 + 0] * y[0 * 4 + c] + inv[i * 3 + 1] * y[1 * 4 + c] + inv[i * 3 + 2] * y[2 * 4 + c];
+        R* sb = &St[t][0];
+        for (int c = 0; c < 4; ++c)
+          rt[t][c] -= y[0 * 4 + c] * ig[0] + y[1 * 4 + c] * ig[1] + y[2 * 4 + c] * ig[2];
+        for (int r2 = 0; r2 < 4; ++r2)
+          for (int c2 = 0; c2 < 4; ++c2)
+            sb[static_cast<size_t>(r2) * n + c2] -=
+                y[0 * 4 + r2] * iy[0 * 4 + c2] + y[1 * 4 + r2] * iy[1 * 4 + c2] + y[2 * 4 + r2] * iy[2 * 4 + c2];
+        for (size_t i = 0; i < L; ++i) {
+          // S[pose f_i, intrinsics] -= H_mf_i^T (H_mm^-1 Y)
+          for (int r2 = 0; r2 < 6; ++r2)
+            for (int c2 = 0; c2 < 4; ++c2)
+              sb[static_cast<size_t>(nci + fidx[i] * 6 + r2) * n + c2] -=
+                  hmf[i][0 * 6 + r2] * iy[0 * 4 + c2] + hmf[i][1 * 6 + r2] * iy[1 * 4 + c2] +
+                  hmf[i][2 * 6 + r2] * iy[2 * 4 + c2];
         }
       }
     }
   });
   for (int t = 0; t < nt; ++t) if (fail[t]) return -1;
-  std::vector<double> S(static_cast<size_t>(n6) * n6, 0.0);
-  std::vector<double> rhs(n6, 0.0);
+  std::vector<double> S(static_cast<size_t>(n) * n, 0.0);
+  std::vector<double> rhs(n, 0.0);
   {
     // merge fold accumulators in thread order (the reduce step)
-    std::vector<R> Sacc(static_cast<size_t>(n6) * n6, R(0)), racc(n6, R(0));
+    std::vector<R> Sacc(static_cast<size_t>(n) * n, R(0)), racc(n, R(0));
     for (int i = 0; i < nf; ++i)
       for (int r = 0; r < 6; ++r)
         for (int c = 0; c < 6; ++c)
-          Sacc[static_cast<size_t>(i * 6 + r) * n6 + i * 6 + c] = sys.U[static_cast<size_t>(i) * 36 + r * 6 + c];
-    for (int i = 0; i < n6; ++i) racc[i] = sys.bp[i];
+          Sacc[static_cast<size_t>(nci + i * 6 + r) * n + nci + i * 6 + c] = sys.U[static_cast<size_t>(i) * 36 + r * 6 + c];
+    for (int i = 0; i < n6; ++i) racc[nci + i] = sys.bp[i];
+    if (fc) {
+      for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) Sacc[static_cast<size_t>(r) * n + c] = sys.Ucc[r * 4 + c];
+      Sacc[static_cast<size_t>(4) * n + 4] = R(1);  // padding rows: identity, zero rhs
+      Sacc[static_cast<size_t>(5) * n + 5] = R(1);
+      for (int i = 0; i < nf; ++i)
+        for (int r = 0; r < 6; ++r)
+          for (int c = 0; c < 4; ++c)
+            Sacc[static_cast<size_t>(nci + i * 6 + r) * n + c] = sys.Hpc[static_cast<size_t>(i) * 24 + r * 4 + c];
+      for (int c = 0; c < 4; ++c) racc[c] = sys.bc[c];
+    }
     for (int t = 0; t < nt; ++t) {
       if (St[t].empty()) continue;
       for (size_t i = 0; i < Sacc.size(); ++i) Sacc[i] += St[t][i];
-      for (int i = 0; i < n6; ++i) racc[i] += rt[t][i];
+      for (int i = 0; i < n; ++i) racc[i] += rt[t][i];
     }
     for (size_t i = 0; i < Sacc.size(); ++i) S[i] = static_cast<double>(Sacc[i]);
-    for (int i = 0; i < n6; ++i) rhs[i] = static_cast<double>(racc[i]);
+    for (int i = 0; i < n; ++i) rhs[i] = static_cast<double>(racc[i]);
   }
   // symmetrize from the lower triangle for the dense factor
-  for (int r = 0; r < n6; ++r)
-    for (int c = r + 1; c < n6; ++c) S[static_cast<size_t>(r) * n6 + c] = S[static_cast<size_t>(c) * n6 + r];
+  for (int r = 0; r < n; ++r)
+    for (int c = r + 1; c < n; ++c) S[static_cast<size_t>(r) * n + c] = S[static_cast<size_t>(c) * n + r];
   if (s_out) *s_out = S;
   if (rhs_out) *rhs_out = rhs;
   BlockLdlt f;
-  if (f.factorize(n6, 6, S.data()) != 0) return -1;
+  if (f.factorize(n, 6, S.data()) != 0) return -1;
   std::vector<double> dxf(rhs);
   f.solve(dxf.data());
-  delta->assign(static_cast<size_t>(n6) + static_cast<size_t>(s.nm) * 3, 0.0);
-  for (int i = 0; i < n6; ++i) (*delta)[i] = dxf[i];
-  // back-substitution: dx_m[b] = H_mm^-1 (g_m[b] - sum H_mf[b,f] dx_f[f])
+  delta->assign(static_cast<size_t>(nc4) + static_cast<size_t>(n6) + static_cast<size_t>(s.nm) * 3, 0.0);
+  for (int i = 0; i < nc4; ++i) (*delta)[i] = dxf[i];
+  for (int i = 0; i < n6; ++i) (*delta)[nc4 + i] = dxf[nci + i];
+  // back-substitution: dx_m[b] = H_mm^-1 (g_m[b] - sum H_mf[b,f] dx_f[f] - H_mc[b] dx_c)
   for (int q = 0; q < p->n_pt; ++q) {
     int mb = s.point_block[q];
     if (mb < 0) continue;
@@ -828,39 +970,51 @@ int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
       const R* w = &sys.Wr[static_cast<size_t>(r) * 18];
       for (int i = 0; i < 3; ++i) {
         double acc = 0.0;
-        for (int c = 0; c < 6; ++c) acc += static_cast<double>(w[i * 6 + c]) * dxf[fb * 6 + c];
+        for (int c = 0; c < 6; ++c) acc += static_cast<double>(w[i * 6 + c]) * dxf[nci + fb * 6 + c];
+        m[i] -= acc;
+      }
+    }
+    if (fc) {
+      const R* y = &sys.Hmc[static_cast<size_t>(mb) * 12];
+      for (int i = 0; i < 3; ++i) {
+        double acc = 0.0;
+        for (int c = 0; c < 4; ++c) acc += static_cast<double>(y[i * 4 + c]) * dxf[c];
         m[i] -= acc;
       }
     }
     const R* inv = &hinv[static_cast<size_t>(mb) * 9];
     for (int i = 0; i < 3; ++i)
-      (*delta)[n6 + mb * 3 + i] = static_cast<double>(inv[i * 3 + 0]) * m[0] +
-                                  static_cast<double>(inv[i * 3 + 1]) * m[1] +
-                                  static_cast<double>(inv[i * 3 + 2]) * m[2];
+      (*delta)[nc4 + n6 + mb * 3 + i] = static_cast<double>(inv[i * 3 + 0]) * m[0] +
+                                        static_cast<double>(inv[i * 3 + 1]) * m[1] +
+                                        static_cast<double>(inv[i * 3 + 2]) * m[2];
   }
   return 0;
 }
 
 // VarFamilies::update (var_families.rs:203-209; var_family.rs:101-114;
-// lie_group_manifold.rs:57-64): T <- exp(delta) * T, p <- p + delta.
+// lie_group_manifold.rs:57-64): T <- exp(delta) * T, p <- p + delta, and
+// free pinhole intrinsics (a vector space) params <- params + delta.
 // Returns false if a pose fails the params-validity assertion of from_params.
 bool apply_update(const ora_problem* p, const Structure& s, const std::vector<double>& delta,
-                  const double* poses, const double* points, double* npose, double* npts) {
+                  const double* intr, const double* poses, const double* points, double* nintr,
+                  double* npose, double* npts) {
   bool ok = true;
+  const int nc4 = p->intrinsics_free ? 4 : 0;
+  for (int i = 0; i < 4; ++i) nintr[i] = intr[i] + (nc4 ? delta[i] : 0.0);
   std::memcpy(npose, poses, sizeof(double) * 7 * p->n_cam);
   std::memcpy(npts, points, sizeof(double) * 3 * p->n_pt);
   for (int c = 0; c < p->n_cam; ++c) {
     int fb = s.pose_block[c];
     if (fb < 0) continue;
     double e[7];
-    se3_exp<double>(&delta[fb * 6], e);
+    se3_exp<double>(&delta[nc4 + fb * 6], e);
     if (!quat_valid(e)) ok = false;
     double out[7];
     se3_mul<double>(e, poses + 7 * c, out);
     if (!quat_valid(out)) ok = false;
     std::memcpy(npose + 7 * c, out, sizeof(out));
   }
-  const int64_t off = static_cast<int64_t>(s.nf) * 6;
+  const int64_t off = nc4 + static_cast<int64_t>(s.nf) * 6;
   for (int q = 0; q < p->n_pt; ++q) {
     int mb = s.point_block[q];
     if (mb < 0) continue;
@@ -870,15 +1024,16 @@ bool apply_update(const ora_problem* p, const Structure& s, const std::vector<do
 }
 
 template <class R>
-int schur_step_impl(const ora_problem* p, const Structure& s, const double* poses,
+int schur_step_impl(const ora_problem* p, const Structure& s, const double* intr, const double* poses,
                     const double* points, double nu, int n_threads, std::vector<double>* delta,
                     double* max_grad, std::vector<double>* neg_grad, std::vector<double>* S,
                     std::vector<double>* rhs, double gradient_tolerance = -1.0) {
   System<R> sys;
-  build_system<R>(p, s, poses, points, nu, n_threads, &sys);
+  build_system<R>(p, s, intr, poses, points, nu, n_threads, &sys);
   if (max_grad) *max_grad = sys.max_grad;
   if (neg_grad) {
     neg_grad->clear();
+    for (auto v : sys.bc) neg_grad->push_back(static_cast<double>(v));
     for (auto v : sys.bp) neg_grad->push_back(static_cast<double>(v));
     for (auto v : sys.bm) neg_grad->push_back(static_cast<double>(v));
   }
@@ -933,22 +1088,30 @@ int ora_block_ldlt_solve(int n, int bs, const double* a, const double* b, double
 }
 
 double ora_total_cost(const ora_problem* p, int n_threads) {
-  return total_cost(p, p->poses, p->points, n_threads);
+  return total_cost(p, p->intrinsics, p->poses, p->points, n_threads);
+}
+
+void ora_eval_term_intrinsics(const double pose[7], const double point[3], const double intr[4],
+                              double j_cam[8]) {
+  const double uv[2] = {0.0, 0.0};
+  double r[2], jp[12], jm[6], w, cost;
+  eval_term_f64(pose, point, intr, uv, 0.0, r, jp, jm, &w, &cost, j_cam);
 }
 
 int64_t ora_dense_system(const ora_problem* p, double nu, double* h, double* neg_grad) {
   Structure s;
   build_structure(p, &s);
-  int64_t n = static_cast<int64_t>(s.nf) * 6 + static_cast<int64_t>(s.nm) * 3;
+  const int64_t c0 = p->intrinsics_free ? 4 : 0;  // scalars of the free intrinsics, first
+  int64_t n = c0 + static_cast<int64_t>(s.nf) * 6 + static_cast<int64_t>(s.nm) * 3;
   if (!h || !neg_grad) return n;
   System<double> sys;
-  build_system<double>(p, s, p->poses, p->points, nu, 1, &sys);
+  build_system<double>(p, s, p->intrinsics, p->poses, p->points, nu, 1, &sys);
   std::fill(h, h + n * n, 0.0);
-  const int64_t off = static_cast<int64_t>(s.nf) * 6;
+  const int64_t off = c0 + static_cast<int64_t>(s.nf) * 6;
   for (int f = 0; f < s.nf; ++f)
     for (int r = 0; r < 6; ++r) {
-      for (int c = 0; c < 6; ++c) h[(f * 6 + r) * n + f * 6 + c] = sys.U[f * 36 + r * 6 + c];
-      neg_grad[f * 6 + r] = sys.bp[f * 6 + r];
+      for (int c = 0; c < 6; ++c) h[(c0 + f * 6 + r) * n + c0 + f * 6 + c] = sys.U[f * 36 + r * 6 + c];
+      neg_grad[c0 + f * 6 + r] = sys.bp[f * 6 + r];
     }
   for (int m = 0; m < s.nm; ++m)
     for (int r = 0; r < 3; ++r) {
@@ -961,9 +1124,29 @@ int64_t ora_dense_system(const ora_problem* p, double nu, double* h, double* neg
     for (int i = 0; i < 3; ++i)
       for (int c = 0; c < 6; ++c) {
         double w = sys.Wr[r * 18 + i * 6 + c];
-        h[(off + mb * 3 + i) * n + fb * 6 + c] += w;
-        h[(fb * 6 + c) * n + off + mb * 3 + i] += w;
+        h[(off + mb * 3 + i) * n + c0 + fb * 6 + c] += w;
+        h[(c0 + fb * 6 + c) * n + off + mb * 3 + i] += w;
       }
+  }
+  if (c0) {
+    for (int r = 0; r < 4; ++r) {
+      for (int c = 0; c < 4; ++c) h[r * n + c] = sys.Ucc[r * 4 + c];
+      neg_grad[r] = sys.bc[r];
+    }
+    for (int f = 0; f < s.nf; ++f)
+      for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 4; ++c) {
+          const double v = sys.Hpc[f * 24 + r * 4 + c];
+          h[(c0 + f * 6 + r) * n + c] = v;
+          h[c * n + c0 + f * 6 + r] = v;
+        }
+    for (int m = 0; m < s.nm; ++m)
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) {
+          const double v = sys.Hmc[m * 12 + r * 4 + c];
+          h[(off + m * 3 + r) * n + c] = v;
+          h[c * n + off + m * 3 + r] = v;
+        }
   }
   return n;
 }
@@ -974,9 +1157,9 @@ int ora_schur_step(const ora_problem* p, double nu, int n_threads, int emulate_f
   build_structure(p, &s);
   std::vector<double> d, S, rhs;
   int st = emulate_fp32
-               ? schur_step_impl<float>(p, s, p->poses, p->points, nu, n_threads, &d, nullptr,
+               ? schur_step_impl<float>(p, s, p->intrinsics, p->poses, p->points, nu, n_threads, &d, nullptr,
                                         nullptr, s_out ? &S : nullptr, rhs_bar_out ? &rhs : nullptr)
-               : schur_step_impl<double>(p, s, p->poses, p->points, nu, n_threads, &d, nullptr,
+               : schur_step_impl<double>(p, s, p->intrinsics, p->poses, p->points, nu, n_threads, &d, nullptr,
                                          nullptr, s_out ? &S : nullptr, rhs_bar_out ? &rhs : nullptr);
   if (st != 0) return st;
   std::memcpy(delta, d.data(), sizeof(double) * d.size());
@@ -988,13 +1171,21 @@ int ora_schur_step(const ora_problem* p, double nu, int n_threads, int emulate_f
 int ora_optimize(const ora_problem* p, const ora_params* prm, int n_threads,
                  ora_record* records, int cap, int* n_records, double* poses_out,
                  double* points_out) {
+  return ora_optimize_ex(p, prm, n_threads, records, cap, n_records, poses_out, points_out, nullptr);
+}
+
+int ora_optimize_ex(const ora_problem* p, const ora_params* prm, int n_threads,
+                    ora_record* records, int cap, int* n_records, double* poses_out,
+                    double* points_out, double* intrinsics_out) {
   Structure s;
   build_structure(p, &s);
-  if (s.nf == 0 || s.nm == 0) return -10;  // SchurMissingFreeOrMarg
+  // SchurMissingFreeOrMarg: no free or no marginalized scalars
+  if ((s.nf == 0 && !p->intrinsics_free) || s.nm == 0) return -10;
+  std::vector<double> intr(p->intrinsics, p->intrinsics + 4), nintr(4);
   std::vector<double> poses(p->poses, p->poses + 7 * p->n_cam);
   std::vector<double> points(p->points, p->points + 3 * p->n_pt);
   std::vector<double> npose(poses.size()), npts(points.size());
-  double merit = total_cost(p, poses.data(), points.data(), n_threads);
+  double merit = total_cost(p, intr.data(), poses.data(), points.data(), n_threads);
   double nu = prm->initial_lm_damping;
   int64_t rejects = 0;
   int64_t steps = 0;
@@ -1010,10 +1201,10 @@ int ora_optimize(const ora_problem* p, const ora_params* prm, int n_threads,
     std::vector<double> delta, neg_grad;
     double max_grad = 0.0;
     int st = prm->emulate_fp32
-                 ? schur_step_impl<float>(p, s, poses.data(), points.data(), nu, n_threads, &delta,
+                 ? schur_step_impl<float>(p, s, intr.data(), poses.data(), points.data(), nu, n_threads, &delta,
                                           &max_grad, &neg_grad, nullptr, nullptr,
                                           prm->gradient_tolerance)
-                 : schur_step_impl<double>(p, s, poses.data(), points.data(), nu, n_threads, &delta,
+                 : schur_step_impl<double>(p, s, intr.data(), poses.data(), points.data(), nu, n_threads, &delta,
                                            &max_grad, &neg_grad, nullptr, nullptr,
                                            prm->gradient_tolerance);
     rec.max_grad = max_grad;
@@ -1025,16 +1216,17 @@ int ora_optimize(const ora_problem* p, const ora_params* prm, int n_threads,
       rejects += 1;
       if (rejects >= prm->max_consecutive_rejects) reason = ORA_TERM_MAX_REJECTS;
     } else {
-      bool valid = apply_update(p, s, delta, poses.data(), points.data(), npose.data(), npts.data());
+      bool valid = apply_update(p, s, delta, intr.data(), poses.data(), points.data(), nintr.data(),
+                                npose.data(), npts.data());
       if (!valid) { rc = -3; }  // the reference panics in from_params
-      double new_merit = total_cost(p, npose.data(), npts.data(), n_threads);
+      double new_merit = total_cost(p, nintr.data(), npose.data(), npts.data(), n_threads);
       rec.new_merit = new_merit;
       double max_step = 0.0;
       for (double v : delta) max_step = std::max(max_step, std::fabs(v));
       rec.max_step = max_step;
       if (max_step < prm->parameter_tolerance) {
         if (new_merit < merit) {
-          poses.swap(npose); points.swap(npts); merit = new_merit; rec.accepted = 1;
+          intr.swap(nintr); poses.swap(npose); points.swap(npts); merit = new_merit; rec.accepted = 1;
         }
         reason = ORA_TERM_PARAMETER_TOL;
       } else {
@@ -1053,7 +1245,7 @@ int ora_optimize(const ora_problem* p, const ora_params* prm, int n_threads,
           rejects = 0;
           double rel = (merit - new_merit) / (std::fabs(merit) + kMinPositive);
           if (rel < prm->function_tolerance) reason = ORA_TERM_FUNCTION_TOL;
-          poses.swap(npose); points.swap(npts); merit = new_merit; rec.accepted = 1;
+          intr.swap(nintr); poses.swap(npose); points.swap(npts); merit = new_merit; rec.accepted = 1;
         } else {
           nu *= 2.0;
           rejects += 1;
@@ -1073,6 +1265,7 @@ int ora_optimize(const ora_problem* p, const ora_params* prm, int n_threads,
   if (n_records) *n_records = nrec;
   if (poses_out) std::memcpy(poses_out, poses.data(), sizeof(double) * poses.size());
   if (points_out) std::memcpy(points_out, points.data(), sizeof(double) * points.size());
+  if (intrinsics_out) std::memcpy(intrinsics_out, intr.data(), sizeof(double) * 4);
   return rc;
 }
 

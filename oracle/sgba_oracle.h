@@ -94,20 +94,25 @@ typedef struct {
   const int32_t *obs_pt;
   const double *obs_uv;        /* n_obs*2 */
   double huber_delta;          /* <= 0: no robust kernel */
+  int32_t intrinsics_free;     /* 1: the intrinsics are one Free variable (family kinds
+                                  (F, F, M) instead of (C, F, M)); 0: Conditioned */
 } ora_problem;
 
 /* Total cost at the given variables (calc_total_cost). */
 double ora_total_cost(const ora_problem *p, int n_threads);
 
-/* Dense damped normal equations over active scalars (free poses then
- * marginalized points): H (n x n, row-major) and neg_grad (n). Returns n,
- * or the required n when the buffers are NULL. */
+/* Dense damped normal equations over active scalars (the 4 intrinsics when
+ * they are free, then free poses, then marginalized points): H (n x n,
+ * row-major) and neg_grad (n). Returns n, or the required n when the buffers
+ * are NULL. */
 int64_t ora_dense_system(const ora_problem *p, double nu, double *h,
                          double *neg_grad);
 
 /* One Schur solve (forward pass, block LDLT of S, back-substitution) at the
- * given variables with damping nu.  delta has n active scalars.  Optionally
- * returns S (nf x nf row-major) and rhs_bar.  Returns 0, or -1 on failure. */
+ * given variables with damping nu.  delta has n active scalars (layout of
+ * ora_dense_system).  Optionally returns S (ns x ns row-major) and rhs_bar,
+ * ns = 6 nf, plus 6 when the intrinsics are free: their block comes first,
+ * padded to 6 rows with an identity.  Returns 0, or -1 on failure. */
 int ora_schur_step(const ora_problem *p, double nu, int n_threads,
                    int emulate_fp32, double *delta, double *s_out,
                    double *rhs_bar_out);
@@ -117,6 +122,18 @@ int ora_schur_step(const ora_problem *p, double nu, int n_threads,
 int ora_optimize(const ora_problem *p, const ora_params *params,
                  int n_threads, ora_record *records, int cap, int *n_records,
                  double *poses_out, double *points_out);
+
+/* ora_optimize that also returns the final intrinsics (4 doubles; they
+ * change only when p->intrinsics_free). */
+int ora_optimize_ex(const ora_problem *p, const ora_params *params,
+                    int n_threads, ora_record *records, int cap, int *n_records,
+                    double *poses_out, double *points_out, double *intrinsics_out);
+
+/* Jacobian of one term's residual with respect to the pinhole intrinsics
+ * (fx, fy, cx, cy), row-major 2x4 (pinhole_reprojection.rs:85:
+ * -dx_distort_params of the projected point, affine.rs:77-108). */
+void ora_eval_term_intrinsics(const double pose[7], const double point[3],
+                              const double intr[4], double j_cam[8]);
 
 #ifdef __cplusplus
 }

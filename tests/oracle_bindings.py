@@ -52,6 +52,7 @@ class OraProblem(C.Structure):
         ("obs_pt", C.POINTER(C.c_int32)),
         ("obs_uv", C.POINTER(C.c_double)),
         ("huber_delta", C.c_double),
+        ("intrinsics_free", C.c_int32),
     ]
 
 
@@ -75,6 +76,9 @@ def lib():
         L.ora_schur_step.argtypes = [C.POINTER(OraProblem), C.c_double, C.c_int, C.c_int, dp, dp, dp]
         L.ora_optimize.argtypes = [C.POINTER(OraProblem), C.POINTER(OraParams), C.c_int,
                                    C.POINTER(OraRecord), C.c_int, C.POINTER(C.c_int), dp, dp]
+        L.ora_optimize_ex.argtypes = [C.POINTER(OraProblem), C.POINTER(OraParams), C.c_int,
+                                      C.POINTER(OraRecord), C.c_int, C.POINTER(C.c_int), dp, dp, dp]
+        L.ora_eval_term_intrinsics.argtypes = [dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -112,11 +116,14 @@ def problem_struct(prob):
     s.obs_pt = k.obs_pt.ctypes.data_as(C.POINTER(C.c_int32))
     s.obs_uv = _d(k.obs_uv)
     s.huber_delta = float(prob.huber_delta or 0.0)
+    s.intrinsics_free = 1 if getattr(prob, "intrinsics_free", False) else 0
     s._keep = k
     return s
 
 
-def optimize(prob, params, n_threads=1, emulate_fp32=False):
+def optimize(prob, params, n_threads=1, emulate_fp32=False, with_intrinsics=False):
+    """Records, final poses and points (and the final intrinsics when
+    with_intrinsics; they change only when prob.intrinsics_free)."""
     L = lib()
     s = problem_struct(prob)
     mr = params.max_consecutive_rejects
@@ -130,10 +137,13 @@ def optimize(prob, params, n_threads=1, emulate_fp32=False):
     n = C.c_int()
     poses = np.empty((s.n_cam, 7))
     points = np.empty((s.n_pt, 3))
-    rc = L.ora_optimize(C.byref(s), C.byref(p), int(n_threads), recs, cap, C.byref(n), _d(poses), _d(points))
+    intr = np.empty(4)
+    rc = L.ora_optimize_ex(C.byref(s), C.byref(p), int(n_threads), recs, cap, C.byref(n), _d(poses), _d(points),
+                           _d(intr))
     if rc != 0:
         raise RuntimeError("oracle optimize failed with %d" % rc)
-    return [recs[i] for i in range(min(n.value, cap))], poses, points
+    out = [recs[i] for i in range(min(n.value, cap))], poses, points
+    return out + (intr,) if with_intrinsics else out
 
 
 def total_cost(prob, n_threads=1):
@@ -152,12 +162,14 @@ def dense_system(prob, nu):
 
 
 def schur_step(prob, nu, n_threads=1):
-    """One Schur solve: returns (delta, S, rhs_bar); raises on failure."""
+    """One Schur solve: returns (delta, S, rhs_bar); raises on failure.
+    With free intrinsics S and rhs_bar start with their block, padded to 6."""
     L = lib()
     s = problem_struct(prob)
     n = L.ora_dense_system(C.byref(s), float(nu), None, None)
     nf6 = 6 * int(np.sum(1 - (np.asarray(prob.pose_const) if getattr(prob, "pose_const", None) is not None
                               else np.zeros(prob.poses.shape[0], np.uint8))))
+    nf6 += 6 if getattr(prob, "intrinsics_free", False) else 0
     delta = np.zeros(n)
     S = np.zeros((nf6, nf6))
     rhs = np.zeros(nf6)
@@ -214,3 +226,11 @@ def block_ldlt_solve(A, b, bs=6):
     if rc != 0:
         raise RuntimeError("block LDLT failed with %d" % rc)
     return x
+
+
+def eval_term_intrinsics(pose, point, intr):
+    """d residual / d (fx, fy, cx, cy), 2x4."""
+    j = np.zeros(8)
+    lib().ora_eval_term_intrinsics(_d(np.ascontiguousarray(pose, float)), _d(np.ascontiguousarray(point, float)),
+                                   _d(np.ascontiguousarray(intr, float)), _d(j))
+    return j.reshape(2, 4)
