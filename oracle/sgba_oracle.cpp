@@ -232,7 +232,7 @@ void se3_inverse(const S* a, S* out) {
 //  affine.rs:50-62)
 template <class S>
 void residual_generic(const S* pose, const S* p, const double* intr,
-                      const double* uv, S* r, S* x_cam_out = nullptr) {
+                      const double* uv, S* r, S* x_cam_out = nullptr, int model = ORA_CAMERA_PINHOLE) {
   S cw[7];
   se3_inverse(pose, cw);
   S rm[9];
@@ -242,6 +242,12 @@ void residual_generic(const S* pose, const S* p, const double* intr,
     xc[i] = (rm[i * 3 + 0] * p[0] + rm[i * 3 + 1] * p[1] + rm[i * 3 + 2] * p[2]) + cw[4 + i];
   S u = xc[0] / xc[2];
   S v = xc[1] / xc[2];
+  if (model == ORA_CAMERA_EUCM) {  // enhanced_unified.rs:59-88
+    S rho = dsqrt(S(intr[5]) * (u * u + v * v) + S(1.0));
+    S norm = S(intr[4]) * rho + S(1.0 - intr[4]);
+    u = u / norm;
+    v = v / norm;
+  }
   S pu = u * S(intr[0]) + S(intr[2]);
   S pv = v * S(intr[1]) + S(intr[3]);
   r[0] = S(uv[0]) - pu;
@@ -275,7 +281,8 @@ struct Term {
 // in f64: residual, d_pi*R_cw, J_pose = d_pi_r_cw * [hat(-p), I], J_pt = -d_pi_r_cw.
 void eval_term_f64(const double* pose, const double* p, const double* intr,
                    const double* uv, double huber, double* r, double* jp,
-                   double* jm, double* w_out, double* cost_out, double* jc = nullptr) {
+                   double* jm, double* w_out, double* cost_out, double* jc = nullptr,
+                   int model = ORA_CAMERA_PINHOLE) {
   double cw[7];
   se3_inverse(pose, cw);
   double rm[9];
@@ -283,19 +290,53 @@ void eval_term_f64(const double* pose, const double* p, const double* intr,
   double xc[3];
   for (int i = 0; i < 3; ++i)
     xc[i] = (rm[i * 3 + 0] * p[0] + rm[i * 3 + 1] * p[1] + rm[i * 3 + 2] * p[2]) + cw[4 + i];
-  double u = xc[0] / xc[2], v = xc[1] / xc[2];
-  r[0] = uv[0] - (u * intr[0] + intr[2]);
-  r[1] = uv[1] - (v * intr[1] + intr[3]);
-  if (jc) {
-    // J_cam = -dx_distort_params(proj) (pinhole_reprojection.rs:85;
-    // affine.rs:77-108): params (fx, fy, cx, cy), 2x4 row-major
-    const double j[8] = {-u, 0.0, -1.0, 0.0, 0.0, -v, 0.0, -1.0};
-    for (int i = 0; i < 8; ++i) jc[i] = j[i];
+  double dpi[6];  // dx_distort_x * dx_proj_x (2x3)
+  if (model == ORA_CAMERA_EUCM) {
+    // EnhancedUnifiedDistortionImpl::distort / dx_distort_x /
+    // dx_distort_params (enhanced_unified.rs:59-88,117-156,158-215), on the
+    // z = 1 projection (perspective.rs:30-39); J_cam is 2x6
+    const double z = xc[2];
+    const double x = xc[0] / z, y = xc[1] / z;
+    const double fx = intr[0], fy = intr[1], alpha = intr[4], beta = intr[5];
+    const double r2 = x * x + y * y;
+    const double rho2 = beta * r2 + 1.0;
+    const double rho = std::sqrt(rho2);
+    const double norm = alpha * rho + (1.0 - alpha);
+    const double mx = x / norm, my = y / norm;
+    r[0] = uv[0] - (fx * mx + intr[2]);
+    r[1] = uv[1] - (fy * my + intr[3]);
+    const double drho_dx = (2.0 * beta * x) / (2.0 * rho);
+    const double drho_dy = (2.0 * beta * y) / (2.0 * rho);
+    const double dnorm_dx = alpha * drho_dx, dnorm_dy = alpha * drho_dy;
+    const double n2 = norm * norm;
+    const double dd[4] = {fx * ((norm - x * dnorm_dx) / n2), fx * (-x * dnorm_dy / n2),
+                          fy * (-y * dnorm_dx / n2), fy * ((norm - y * dnorm_dy) / n2)};
+    // dx_proj_x = [[1/z, 0, -x_c/z^2], [0, 1/z, -y_c/z^2]]
+    const double pz[6] = {1.0 / z, 0.0, -xc[0] / (z * z), 0.0, 1.0 / z, -xc[1] / (z * z)};
+    for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 3; ++j) dpi[i * 3 + j] = dd[i * 2 + 0] * pz[0 * 3 + j] + dd[i * 2 + 1] * pz[1 * 3 + j];
+    if (jc) {
+      const double drho_dbeta = r2 / (2.0 * rho);
+      const double dnorm_dalpha = rho - 1.0, dnorm_dbeta = alpha * drho_dbeta;
+      const double j[12] = {-mx, 0.0, -1.0, 0.0, -fx * (-x * dnorm_dalpha / n2), -fx * (-x * dnorm_dbeta / n2),
+                            0.0, -my, 0.0, -1.0, -fy * (-y * dnorm_dalpha / n2), -fy * (-y * dnorm_dbeta / n2)};
+      for (int i = 0; i < 12; ++i) jc[i] = j[i];
+    }
+  } else {
+    double u = xc[0] / xc[2], v = xc[1] / xc[2];
+    r[0] = uv[0] - (u * intr[0] + intr[2]);
+    r[1] = uv[1] - (v * intr[1] + intr[3]);
+    if (jc) {
+      // J_cam = -dx_distort_params(proj) (pinhole_reprojection.rs:85;
+      // affine.rs:77-108): params (fx, fy, cx, cy), 2x4 row-major
+      const double j[8] = {-u, 0.0, -1.0, 0.0, 0.0, -v, 0.0, -1.0};
+      for (int i = 0; i < 8; ++i) jc[i] = j[i];
+    }
+    double z = xc[2];
+    const double dp[6] = {intr[0] * (1.0 / z), 0.0, intr[0] * (-xc[0] / (z * z)),
+                          0.0, intr[1] * (1.0 / z), intr[1] * (-xc[1] / (z * z))};
+    for (int i = 0; i < 6; ++i) dpi[i] = dp[i];
   }
-  // dx_distort_x * dx_proj_x (2x3)
-  double z = xc[2];
-  double dpi[6] = {intr[0] * (1.0 / z), 0.0, intr[0] * (-xc[0] / (z * z)),
-                   0.0, intr[1] * (1.0 / z), intr[1] * (-xc[1] / (z * z))};
   double d[6];  // d_pi * R_cw (2x3)
   for (int i = 0; i < 2; ++i)
     for (int j = 0; j < 3; ++j)
@@ -326,9 +367,9 @@ void eval_term_f64(const double* pose, const double* p, const double* intr,
 
 // Cost only (calc_total_cost treats every variable as Conditioned).
 double eval_cost_f64(const double* pose, const double* p, const double* intr,
-                     const double* uv, double huber) {
+                     const double* uv, double huber, int model = ORA_CAMERA_PINHOLE) {
   double r[2];
-  residual_generic<double>(pose, p, intr, uv, r);
+  residual_generic<double>(pose, p, intr, uv, r, nullptr, model);
   if (huber > 0.0) {
     double nrm = std::sqrt(r[0] * r[0] + r[1] * r[1]);
     double w = huber_weight(huber, nrm);
@@ -340,9 +381,9 @@ double eval_cost_f64(const double* pose, const double* p, const double* intr,
 
 template <class R>
 void make_term(const double* pose, const double* p, const double* intr,
-               const double* uv, double huber, Term<R>* t) {
+               const double* uv, double huber, Term<R>* t, int model = ORA_CAMERA_PINHOLE) {
   double r[2], jp[12], jm[6], w, cost;
-  eval_term_f64(pose, p, intr, uv, huber, r, jp, jm, &w, &cost);
+  eval_term_f64(pose, p, intr, uv, huber, r, jp, jm, &w, &cost, nullptr, model);
   R Jp[12], Jm[6], rw[2];
   for (int i = 0; i < 12; ++i) Jp[i] = static_cast<R>(jp[i]);
   for (int i = 0; i < 6; ++i) Jm[i] = static_cast<R>(jm[i]);
@@ -360,27 +401,28 @@ void make_term(const double* pose, const double* p, const double* intr,
   t->cost = cost;
 }
 
-// The blocks of a term that involve Free intrinsics (kinds (F, F, M)):
-// J_cam^T J_cam, J_pose^T J_cam (pose row, intrinsics column), J_pt^T J_cam
-// (point row, intrinsics column) and J_cam^T r~.
+// The blocks of a term that involve Free intrinsics (kinds (F, F, M)), for
+// nc = 4 (pinhole) or 6 (EUCM) params: J_cam^T J_cam (nc x nc), J_pose^T J_cam
+// (pose row, intrinsics column, 6 x nc), J_pt^T J_cam (point row, 3 x nc)
+// and J_cam^T r~, each row-major with row stride nc.
 template <class R>
 struct CamTerm {
-  R hcc[16];
-  R hpc[24];
-  R hmc[12];
-  R gc[4];
+  R hcc[36];
+  R hpc[36];
+  R hmc[18];
+  R gc[6];
 };
 
 // make_term plus the intrinsics blocks (same arithmetic for the Term part).
 template <class R>
 void make_term_cam(const double* pose, const double* p, const double* intr,
-                   const double* uv, double huber, Term<R>* t, CamTerm<R>* ct) {
-  double r[2], jp[12], jm[6], jc[8], w, cost;
-  eval_term_f64(pose, p, intr, uv, huber, r, jp, jm, &w, &cost, jc);
-  R Jp[12], Jm[6], Jc[8], rw[2];
+                   const double* uv, double huber, Term<R>* t, CamTerm<R>* ct, int model, int nc) {
+  double r[2], jp[12], jm[6], jc[12], w, cost;
+  eval_term_f64(pose, p, intr, uv, huber, r, jp, jm, &w, &cost, jc, model);
+  R Jp[12], Jm[6], Jc[12], rw[2];
   for (int i = 0; i < 12; ++i) Jp[i] = static_cast<R>(jp[i]);
   for (int i = 0; i < 6; ++i) Jm[i] = static_cast<R>(jm[i]);
-  for (int i = 0; i < 8; ++i) Jc[i] = static_cast<R>(jc[i]);
+  for (int i = 0; i < 2 * nc; ++i) Jc[i] = static_cast<R>(jc[i]);
   rw[0] = static_cast<R>(w * r[0]);
   rw[1] = static_cast<R>(w * r[1]);
   for (int a = 0; a < 6; ++a) {
@@ -393,22 +435,23 @@ void make_term_cam(const double* pose, const double* p, const double* intr,
     t->gm[a] = Jm[a] * rw[0] + Jm[3 + a] * rw[1];
   }
   t->cost = cost;
-  for (int a = 0; a < 4; ++a) {
-    for (int b = 0; b < 4; ++b) ct->hcc[a * 4 + b] = Jc[a] * Jc[b] + Jc[4 + a] * Jc[4 + b];
-    ct->gc[a] = Jc[a] * rw[0] + Jc[4 + a] * rw[1];
+  *ct = CamTerm<R>{};
+  for (int a = 0; a < nc; ++a) {
+    for (int b = 0; b < nc; ++b) ct->hcc[a * nc + b] = Jc[a] * Jc[b] + Jc[nc + a] * Jc[nc + b];
+    ct->gc[a] = Jc[a] * rw[0] + Jc[nc + a] * rw[1];
   }
   for (int a = 0; a < 6; ++a)
-    for (int b = 0; b < 4; ++b) ct->hpc[a * 4 + b] = Jp[a] * Jc[b] + Jp[6 + a] * Jc[4 + b];
+    for (int b = 0; b < nc; ++b) ct->hpc[a * nc + b] = Jp[a] * Jc[b] + Jp[6 + a] * Jc[nc + b];
   for (int a = 0; a < 3; ++a)
-    for (int b = 0; b < 4; ++b) ct->hmc[a * 4 + b] = Jm[a] * Jc[b] + Jm[3 + a] * Jc[4 + b];
+    for (int b = 0; b < nc; ++b) ct->hmc[a * nc + b] = Jm[a] * Jc[b] + Jm[3 + a] * Jc[nc + b];
 }
 
 template <class R>
 void cam_term_reduce(CamTerm<R>* a, const CamTerm<R>& b) {
-  for (int i = 0; i < 16; ++i) a->hcc[i] += b.hcc[i];
-  for (int i = 0; i < 24; ++i) a->hpc[i] += b.hpc[i];
-  for (int i = 0; i < 12; ++i) a->hmc[i] += b.hmc[i];
-  for (int i = 0; i < 4; ++i) a->gc[i] += b.gc[i];
+  for (int i = 0; i < 36; ++i) a->hcc[i] += b.hcc[i];
+  for (int i = 0; i < 36; ++i) a->hpc[i] += b.hpc[i];
+  for (int i = 0; i < 18; ++i) a->hmc[i] += b.hmc[i];
+  for (int i = 0; i < 6; ++i) a->gc[i] += b.gc[i];
 }
 
 template <class R>
@@ -639,6 +682,14 @@ struct Structure {
   std::vector<int64_t> pt_rng_begin;  // ranges are sorted by point, so contiguous
 };
 
+// Params of the camera model: fx fy cx cy, then alpha beta for EUCM.
+inline int cam_params(const ora_problem* p) { return p->camera_model == ORA_CAMERA_EUCM ? 6 : 4; }
+inline void problem_intrinsics(const ora_problem* p, double* intr6) {
+  for (int i = 0; i < 4; ++i) intr6[i] = p->intrinsics[i];
+  intr6[4] = p->camera_model == ORA_CAMERA_EUCM ? p->eucm_alpha_beta[0] : 0.0;
+  intr6[5] = p->camera_model == ORA_CAMERA_EUCM ? p->eucm_alpha_beta[1] : 0.0;
+}
+
 void build_structure(const ora_problem* p, Structure* s) {
   s->nc = p->n_cam; s->np = p->n_pt; s->no = p->n_obs;
   s->order.resize(p->n_obs);
@@ -701,7 +752,7 @@ double total_cost(const ora_problem* p, const double* intr, const double* poses,
     double acc = 0.0;
     for (int64_t i = b; i < e; ++i)
       acc += eval_cost_f64(poses + 7 * p->obs_cam[i], points + 3 * p->obs_pt[i],
-                           intr, p->obs_uv + 2 * i, p->huber_delta);
+                           intr, p->obs_uv + 2 * i, p->huber_delta, p->camera_model);
     part[t] = acc;
   });
   double c = 0.0;
@@ -716,8 +767,9 @@ struct System {
   std::vector<R> U, bp;    // nf*36, nf*6
   std::vector<R> V, bm;    // nm*9,  nm*3
   std::vector<R> Wr;       // per reduction range: 3x6 (point row, pose col) -- valid when both active
-  // Free intrinsics only (empty otherwise): their 4x4 block and neg_grad, and
-  // the blocks coupling them to each free pose (6x4) and marg point (3x4)
+  // Free intrinsics only (empty otherwise), nc = 4 or 6 params: their nc x nc
+  // block and neg_grad, and the blocks coupling them to each free pose
+  // (6 x nc) and marg point (3 x nc)
   std::vector<R> Ucc, bc, Hpc, Hmc;
   double max_grad = 0.0;
 };
@@ -727,13 +779,15 @@ template <class R>
 void build_system(const ora_problem* p, const Structure& s, const double* intr, const double* poses,
                   const double* points, double nu, int n_threads, System<R>* sys) {
   const bool fc = p->intrinsics_free != 0;
+  const int nc = cam_params(p);
+  const int model = p->camera_model;
   sys->U.assign(static_cast<size_t>(s.nf) * 36, R(0));
   sys->bp.assign(static_cast<size_t>(s.nf) * 6, R(0));
   sys->V.assign(static_cast<size_t>(s.nm) * 9, R(0));
   sys->bm.assign(static_cast<size_t>(s.nm) * 3, R(0));
   int64_t nr = static_cast<int64_t>(s.rng_pt.size());
   sys->Wr.assign(static_cast<size_t>(nr) * 18, R(0));
-  if (fc) sys->Hmc.assign(static_cast<size_t>(s.nm) * 12, R(0));
+  if (fc) sys->Hmc.assign(static_cast<size_t>(s.nm) * 3 * nc, R(0));
   int nt = std::max(1, n_threads);
   // Parallel over points (disjoint V/bm and W); pose (and intrinsics) sums per thread.
   std::vector<std::vector<R>> Ut(nt), bpt(nt), Uct(nt), bct(nt), Hpct(nt);
@@ -741,9 +795,9 @@ void build_system(const ora_problem* p, const Structure& s, const double* intr, 
     Ut[t].assign(static_cast<size_t>(s.nf) * 36, R(0));
     bpt[t].assign(static_cast<size_t>(s.nf) * 6, R(0));
     if (fc) {
-      Uct[t].assign(16, R(0));
-      bct[t].assign(4, R(0));
-      Hpct[t].assign(static_cast<size_t>(s.nf) * 24, R(0));
+      Uct[t].assign(static_cast<size_t>(nc) * nc, R(0));
+      bct[t].assign(nc, R(0));
+      Hpct[t].assign(static_cast<size_t>(s.nf) * 6 * nc, R(0));
     }
     for (int64_t q = pb; q < pe; ++q) {
       for (int64_t r = s.pt_rng_begin[q]; r < s.pt_rng_begin[q + 1]; ++r) {
@@ -756,11 +810,11 @@ void build_system(const ora_problem* p, const Structure& s, const double* intr, 
           if (fc) {
             CamTerm<R> ck;
             make_term_cam<R>(poses + 7 * p->obs_cam[o], points + 3 * p->obs_pt[o], intr,
-                             p->obs_uv + 2 * o, p->huber_delta, &tk, &ck);
+                             p->obs_uv + 2 * o, p->huber_delta, &tk, &ck, model, nc);
             if (first) cterm = ck; else cam_term_reduce(&cterm, ck);
           } else {
             make_term<R>(poses + 7 * p->obs_cam[o], points + 3 * p->obs_pt[o],
-                         intr, p->obs_uv + 2 * o, p->huber_delta, &tk);
+                         intr, p->obs_uv + 2 * o, p->huber_delta, &tk, model);
           }
           if (first) { term = tk; first = false; } else { term_reduce(&term, tk); }
         }
@@ -769,13 +823,13 @@ void build_system(const ora_problem* p, const Structure& s, const double* intr, 
         if (fc) {
           // the intrinsics are touched by every term: nu I per evaluated term
           R* uc = Uct[t].data();
-          for (int i = 0; i < 16; ++i) uc[i] += cterm.hcc[i];
-          if (nu != 0.0) for (int i = 0; i < 4; ++i) uc[i * 5] += static_cast<R>(nu);
-          for (int i = 0; i < 4; ++i) bct[t][i] -= cterm.gc[i];
+          for (int i = 0; i < nc * nc; ++i) uc[i] += cterm.hcc[i];
+          if (nu != 0.0) for (int i = 0; i < nc; ++i) uc[i * (nc + 1)] += static_cast<R>(nu);
+          for (int i = 0; i < nc; ++i) bct[t][i] -= cterm.gc[i];
           if (pb_ >= 0)
-            for (int i = 0; i < 24; ++i) Hpct[t][static_cast<size_t>(pb_) * 24 + i] += cterm.hpc[i];
+            for (int i = 0; i < 6 * nc; ++i) Hpct[t][static_cast<size_t>(pb_) * 6 * nc + i] += cterm.hpc[i];
           if (mb >= 0)
-            for (int i = 0; i < 12; ++i) sys->Hmc[static_cast<size_t>(mb) * 12 + i] += cterm.hmc[i];
+            for (int i = 0; i < 3 * nc; ++i) sys->Hmc[static_cast<size_t>(mb) * 3 * nc + i] += cterm.hmc[i];
         }
         if (pb_ >= 0) {
           R* u = &Ut[t][static_cast<size_t>(pb_) * 36];
@@ -800,13 +854,13 @@ void build_system(const ora_problem* p, const Structure& s, const double* intr, 
     for (size_t i = 0; i < sys->bp.size(); ++i) sys->bp[i] += bpt[t][i];
   }
   if (fc) {
-    sys->Ucc.assign(16, R(0));
-    sys->bc.assign(4, R(0));
-    sys->Hpc.assign(static_cast<size_t>(s.nf) * 24, R(0));
+    sys->Ucc.assign(static_cast<size_t>(nc) * nc, R(0));
+    sys->bc.assign(nc, R(0));
+    sys->Hpc.assign(static_cast<size_t>(s.nf) * 6 * nc, R(0));
     for (int t = 0; t < nt; ++t) {
       if (Uct[t].empty()) continue;
-      for (int i = 0; i < 16; ++i) sys->Ucc[i] += Uct[t][i];
-      for (int i = 0; i < 4; ++i) sys->bc[i] += bct[t][i];
+      for (int i = 0; i < nc * nc; ++i) sys->Ucc[i] += Uct[t][i];
+      for (int i = 0; i < nc; ++i) sys->bc[i] += bct[t][i];
       for (size_t i = 0; i < sys->Hpc.size(); ++i) sys->Hpc[i] += Hpct[t][i];
     }
   }
@@ -819,19 +873,21 @@ void build_system(const ora_problem* p, const Structure& s, const double* intr, 
 
 // SchurFactor::factorize + solve (schur_ldlt.rs:536-812) with the sequential
 // forward pass (schur_ldlt.rs:241-278).  delta = [dx_c; dx_f; dx_m], dx_c the
-// 4 intrinsics when they are free (empty otherwise).  In S the intrinsics
-// come first (their family's partition precedes the poses'), padded to one
-// 6-row block with an identity so the factor keeps 6x6 blocks; the pivot rule
-// restarts at that block as at every partition block.
+// nc = 4 (pinhole) or 6 (EUCM) intrinsics when they are free (empty
+// otherwise).  In S the intrinsics come first (their family's partition
+// precedes the poses'), padded to one 6-row block with an identity so the
+// factor keeps 6x6 blocks; the pivot rule restarts at that block as at every
+// partition block.
 template <class R>
 int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
                 int n_threads, std::vector<double>* delta, std::vector<double>* s_out,
                 std::vector<double>* rhs_out) {
   const bool fc = p->intrinsics_free != 0;
+  const int nc = cam_params(p);
   const int nf = s.nf;
   const int n6 = nf * 6;
-  const int nci = fc ? 6 : 0;  // rows of the (padded) intrinsics block in S
-  const int nc4 = fc ? 4 : 0;  // intrinsics scalars in delta
+  const int nci = fc ? 6 : 0;   // rows of the (padded) intrinsics block in S
+  const int nc4 = fc ? nc : 0;  // intrinsics scalars in delta
   const int n = nci + n6;
   const int nt = std::max(1, n_threads);
   // S_ff = H_ff (diagonal blocks only for BA)
@@ -892,26 +948,26 @@ int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
         }
       }
       if (fc) {
-        // the intrinsics column: Y = H_mc (3x4), H_mm^-1 Y
-        const R* y = &sys.Hmc[static_cast<size_t>(mb) * 12];
-        R iy[12];
+        // the intrinsics column: Y = H_mc (3 x nc), H_mm^-1 Y
+        const R* y = &sys.Hmc[static_cast<size_t>(mb) * 3 * nc];
+        R iy[18];
         for (int i = 0; i < 3; ++i)
-          for (int c = 0; c < 4; ++c)
-            iy[i * 4 + c] = inv[i * 3 + 0] * y[0 * 4 + c] + inv[i * 3 + 1] * y[1 * 4 + c] + inv[i * 3 + 2] * y[2 * 4 + c];
+          for (int c = 0; c < nc; ++c)
+            iy[i * nc + c] = inv[i * 3 + 0] * y[0 * nc + c] + inv[i * 3 + 1] * y[1 * nc + c] + inv[i * 3 + 2] * y[2 * nc + c];
         R* sb = &St[t][0];
-        for (int c = 0; c < 4; ++c)
-          rt[t][c] -= y[0 * 4 + c] * ig[0] + y[1 * 4 + c] * ig[1] + y[2 * 4 + c] * ig[2];
-        for (int r2 = 0; r2 < 4; ++r2)
-          for (int c2 = 0; c2 < 4; ++c2)
+        for (int c = 0; c < nc; ++c)
+          rt[t][c] -= y[0 * nc + c] * ig[0] + y[1 * nc + c] * ig[1] + y[2 * nc + c] * ig[2];
+        for (int r2 = 0; r2 < nc; ++r2)
+          for (int c2 = 0; c2 < nc; ++c2)
             sb[static_cast<size_t>(r2) * n + c2] -=
-                y[0 * 4 + r2] * iy[0 * 4 + c2] + y[1 * 4 + r2] * iy[1 * 4 + c2] + y[2 * 4 + r2] * iy[2 * 4 + c2];
+                y[0 * nc + r2] * iy[0 * nc + c2] + y[1 * nc + r2] * iy[1 * nc + c2] + y[2 * nc + r2] * iy[2 * nc + c2];
         for (size_t i = 0; i < L; ++i) {
           // S[pose f_i, intrinsics] -= H_mf_i^T (H_mm^-1 Y)
           for (int r2 = 0; r2 < 6; ++r2)
-            for (int c2 = 0; c2 < 4; ++c2)
+            for (int c2 = 0; c2 < nc; ++c2)
               sb[static_cast<size_t>(nci + fidx[i] * 6 + r2) * n + c2] -=
-                  hmf[i][0 * 6 + r2] * iy[0 * 4 + c2] + hmf[i][1 * 6 + r2] * iy[1 * 4 + c2] +
-                  hmf[i][2 * 6 + r2] * iy[2 * 4 + c2];
+                  hmf[i][0 * 6 + r2] * iy[0 * nc + c2] + hmf[i][1 * 6 + r2] * iy[1 * nc + c2] +
+                  hmf[i][2 * 6 + r2] * iy[2 * nc + c2];
         }
       }
     }
@@ -928,15 +984,14 @@ int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
           Sacc[static_cast<size_t>(nci + i * 6 + r) * n + nci + i * 6 + c] = sys.U[static_cast<size_t>(i) * 36 + r * 6 + c];
     for (int i = 0; i < n6; ++i) racc[nci + i] = sys.bp[i];
     if (fc) {
-      for (int r = 0; r < 4; ++r)
-        for (int c = 0; c < 4; ++c) Sacc[static_cast<size_t>(r) * n + c] = sys.Ucc[r * 4 + c];
-      Sacc[static_cast<size_t>(4) * n + 4] = R(1);  // padding rows: identity, zero rhs
-      Sacc[static_cast<size_t>(5) * n + 5] = R(1);
+      for (int r = 0; r < nc; ++r)
+        for (int c = 0; c < nc; ++c) Sacc[static_cast<size_t>(r) * n + c] = sys.Ucc[r * nc + c];
+      for (int k = nc; k < 6; ++k) Sacc[static_cast<size_t>(k) * n + k] = R(1);  // padding: identity, zero rhs
       for (int i = 0; i < nf; ++i)
         for (int r = 0; r < 6; ++r)
-          for (int c = 0; c < 4; ++c)
-            Sacc[static_cast<size_t>(nci + i * 6 + r) * n + c] = sys.Hpc[static_cast<size_t>(i) * 24 + r * 4 + c];
-      for (int c = 0; c < 4; ++c) racc[c] = sys.bc[c];
+          for (int c = 0; c < nc; ++c)
+            Sacc[static_cast<size_t>(nci + i * 6 + r) * n + c] = sys.Hpc[static_cast<size_t>(i) * 6 * nc + r * nc + c];
+      for (int c = 0; c < nc; ++c) racc[c] = sys.bc[c];
     }
     for (int t = 0; t < nt; ++t) {
       if (St[t].empty()) continue;
@@ -975,10 +1030,10 @@ int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
       }
     }
     if (fc) {
-      const R* y = &sys.Hmc[static_cast<size_t>(mb) * 12];
+      const R* y = &sys.Hmc[static_cast<size_t>(mb) * 3 * nc];
       for (int i = 0; i < 3; ++i) {
         double acc = 0.0;
-        for (int c = 0; c < 4; ++c) acc += static_cast<double>(y[i * 4 + c]) * dxf[c];
+        for (int c = 0; c < nc; ++c) acc += static_cast<double>(y[i * nc + c]) * dxf[c];
         m[i] -= acc;
       }
     }
@@ -999,8 +1054,8 @@ bool apply_update(const ora_problem* p, const Structure& s, const std::vector<do
                   const double* intr, const double* poses, const double* points, double* nintr,
                   double* npose, double* npts) {
   bool ok = true;
-  const int nc4 = p->intrinsics_free ? 4 : 0;
-  for (int i = 0; i < 4; ++i) nintr[i] = intr[i] + (nc4 ? delta[i] : 0.0);
+  const int nc4 = p->intrinsics_free ? cam_params(p) : 0;
+  for (int i = 0; i < 6; ++i) nintr[i] = intr[i] + (i < nc4 ? delta[i] : 0.0);
   std::memcpy(npose, poses, sizeof(double) * 7 * p->n_cam);
   std::memcpy(npts, points, sizeof(double) * 3 * p->n_pt);
   for (int c = 0; c < p->n_cam; ++c) {
@@ -1088,7 +1143,16 @@ int ora_block_ldlt_solve(int n, int bs, const double* a, const double* b, double
 }
 
 double ora_total_cost(const ora_problem* p, int n_threads) {
-  return total_cost(p, p->intrinsics, p->poses, p->points, n_threads);
+  double intr[6];
+  problem_intrinsics(p, intr);
+  return total_cost(p, intr, p->poses, p->points, n_threads);
+}
+
+void ora_eval_term_ex(const double pose[7], const double point[3], const double intr[6],
+                      int32_t camera_model, const double uv[2], double r[2], double j_pose[12],
+                      double j_point[6], double j_cam[12]) {
+  double w, cost;
+  eval_term_f64(pose, point, intr, uv, 0.0, r, j_pose, j_point, &w, &cost, j_cam, camera_model);
 }
 
 void ora_eval_term_intrinsics(const double pose[7], const double point[3], const double intr[4],
@@ -1101,11 +1165,14 @@ void ora_eval_term_intrinsics(const double pose[7], const double point[3], const
 int64_t ora_dense_system(const ora_problem* p, double nu, double* h, double* neg_grad) {
   Structure s;
   build_structure(p, &s);
-  const int64_t c0 = p->intrinsics_free ? 4 : 0;  // scalars of the free intrinsics, first
+  const int nc = cam_params(p);
+  const int64_t c0 = p->intrinsics_free ? nc : 0;  // scalars of the free intrinsics, first
   int64_t n = c0 + static_cast<int64_t>(s.nf) * 6 + static_cast<int64_t>(s.nm) * 3;
   if (!h || !neg_grad) return n;
+  double intr[6];
+  problem_intrinsics(p, intr);
   System<double> sys;
-  build_system<double>(p, s, p->intrinsics, p->poses, p->points, nu, 1, &sys);
+  build_system<double>(p, s, intr, p->poses, p->points, nu, 1, &sys);
   std::fill(h, h + n * n, 0.0);
   const int64_t off = c0 + static_cast<int64_t>(s.nf) * 6;
   for (int f = 0; f < s.nf; ++f)
@@ -1129,21 +1196,21 @@ int64_t ora_dense_system(const ora_problem* p, double nu, double* h, double* neg
       }
   }
   if (c0) {
-    for (int r = 0; r < 4; ++r) {
-      for (int c = 0; c < 4; ++c) h[r * n + c] = sys.Ucc[r * 4 + c];
+    for (int r = 0; r < nc; ++r) {
+      for (int c = 0; c < nc; ++c) h[r * n + c] = sys.Ucc[r * nc + c];
       neg_grad[r] = sys.bc[r];
     }
     for (int f = 0; f < s.nf; ++f)
       for (int r = 0; r < 6; ++r)
-        for (int c = 0; c < 4; ++c) {
-          const double v = sys.Hpc[f * 24 + r * 4 + c];
+        for (int c = 0; c < nc; ++c) {
+          const double v = sys.Hpc[f * 6 * nc + r * nc + c];
           h[(c0 + f * 6 + r) * n + c] = v;
           h[c * n + c0 + f * 6 + r] = v;
         }
     for (int m = 0; m < s.nm; ++m)
       for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 4; ++c) {
-          const double v = sys.Hmc[m * 12 + r * 4 + c];
+        for (int c = 0; c < nc; ++c) {
+          const double v = sys.Hmc[m * 3 * nc + r * nc + c];
           h[(off + m * 3 + r) * n + c] = v;
           h[c * n + off + m * 3 + r] = v;
         }
@@ -1155,11 +1222,13 @@ int ora_schur_step(const ora_problem* p, double nu, int n_threads, int emulate_f
                    double* delta, double* s_out, double* rhs_bar_out) {
   Structure s;
   build_structure(p, &s);
+  double intr[6];
+  problem_intrinsics(p, intr);
   std::vector<double> d, S, rhs;
   int st = emulate_fp32
-               ? schur_step_impl<float>(p, s, p->intrinsics, p->poses, p->points, nu, n_threads, &d, nullptr,
+               ? schur_step_impl<float>(p, s, intr, p->poses, p->points, nu, n_threads, &d, nullptr,
                                         nullptr, s_out ? &S : nullptr, rhs_bar_out ? &rhs : nullptr)
-               : schur_step_impl<double>(p, s, p->intrinsics, p->poses, p->points, nu, n_threads, &d, nullptr,
+               : schur_step_impl<double>(p, s, intr, p->poses, p->points, nu, n_threads, &d, nullptr,
                                          nullptr, s_out ? &S : nullptr, rhs_bar_out ? &rhs : nullptr);
   if (st != 0) return st;
   std::memcpy(delta, d.data(), sizeof(double) * d.size());
@@ -1181,7 +1250,8 @@ int ora_optimize_ex(const ora_problem* p, const ora_params* prm, int n_threads,
   build_structure(p, &s);
   // SchurMissingFreeOrMarg: no free or no marginalized scalars
   if ((s.nf == 0 && !p->intrinsics_free) || s.nm == 0) return -10;
-  std::vector<double> intr(p->intrinsics, p->intrinsics + 4), nintr(4);
+  std::vector<double> intr(6), nintr(6);
+  problem_intrinsics(p, intr.data());
   std::vector<double> poses(p->poses, p->poses + 7 * p->n_cam);
   std::vector<double> points(p->points, p->points + 3 * p->n_pt);
   std::vector<double> npose(poses.size()), npts(points.size());
@@ -1265,7 +1335,7 @@ int ora_optimize_ex(const ora_problem* p, const ora_params* prm, int n_threads,
   if (n_records) *n_records = nrec;
   if (poses_out) std::memcpy(poses_out, poses.data(), sizeof(double) * poses.size());
   if (points_out) std::memcpy(points_out, points.data(), sizeof(double) * points.size());
-  if (intrinsics_out) std::memcpy(intrinsics_out, intr.data(), sizeof(double) * 4);
+  if (intrinsics_out) std::memcpy(intrinsics_out, intr.data(), sizeof(double) * 6);
   return rc;
 }
 

@@ -96,7 +96,15 @@ typedef struct {
   double huber_delta;          /* <= 0: no robust kernel */
   int32_t intrinsics_free;     /* 1: the intrinsics are one Free variable (family kinds
                                   (F, F, M) instead of (C, F, M)); 0: Conditioned */
+  int32_t camera_model;        /* ORA_CAMERA_PINHOLE (params fx fy cx cy) or
+                                  ORA_CAMERA_EUCM (fx fy cx cy alpha beta) */
+  double eucm_alpha_beta[2];   /* alpha, beta of the EUCM model */
 } ora_problem;
+
+enum {
+  ORA_CAMERA_PINHOLE = 0, /* PinholeCamera: affine distortion (affine.rs:50-108) */
+  ORA_CAMERA_EUCM = 1,    /* EnhancedUnifiedCamera (enhanced_unified.rs:55-215) */
+};
 
 /* Total cost at the given variables (calc_total_cost). */
 double ora_total_cost(const ora_problem *p, int n_threads);
@@ -123,8 +131,9 @@ int ora_optimize(const ora_problem *p, const ora_params *params,
                  int n_threads, ora_record *records, int cap, int *n_records,
                  double *poses_out, double *points_out);
 
-/* ora_optimize that also returns the final intrinsics (4 doubles; they
- * change only when p->intrinsics_free). */
+/* ora_optimize that also returns the final intrinsics (6 doubles: fx fy cx
+ * cy, then alpha beta of the EUCM model, zero for a pinhole; they change
+ * only when p->intrinsics_free). */
 int ora_optimize_ex(const ora_problem *p, const ora_params *params,
                     int n_threads, ora_record *records, int cap, int *n_records,
                     double *poses_out, double *points_out, double *intrinsics_out);
@@ -134,6 +143,14 @@ int ora_optimize_ex(const ora_problem *p, const ora_params *params,
  * -dx_distort_params of the projected point, affine.rs:77-108). */
 void ora_eval_term_intrinsics(const double pose[7], const double point[3],
                               const double intr[4], double j_cam[8]);
+
+/* One term for either camera model: residual, J_pose (2x6), J_point (2x3)
+ * and J_cam (2 x n_params, n_params = 4 or 6), row-major; intr holds the
+ * model's params (pinhole_reprojection.rs:60-95, ba_problem.rs:69-110). */
+void ora_eval_term_ex(const double pose[7], const double point[3],
+                      const double intr[6], int32_t camera_model, const double uv[2],
+                      double r[2], double j_pose[12], double j_point[6],
+                      double j_cam[12]);
 
 #ifdef __cplusplus
 }

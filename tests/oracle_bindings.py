@@ -53,7 +53,13 @@ class OraProblem(C.Structure):
         ("obs_uv", C.POINTER(C.c_double)),
         ("huber_delta", C.c_double),
         ("intrinsics_free", C.c_int32),
+        ("camera_model", C.c_int32),
+        ("eucm_alpha_beta", C.c_double * 2),
     ]
+
+
+CAMERA_PINHOLE = 0
+CAMERA_EUCM = 1
 
 
 def lib():
@@ -79,6 +85,7 @@ def lib():
         L.ora_optimize_ex.argtypes = [C.POINTER(OraProblem), C.POINTER(OraParams), C.c_int,
                                       C.POINTER(OraRecord), C.c_int, C.POINTER(C.c_int), dp, dp, dp]
         L.ora_eval_term_intrinsics.argtypes = [dp, dp, dp, dp]
+        L.ora_eval_term_ex.argtypes = [dp, dp, dp, C.c_int32, dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -117,13 +124,18 @@ def problem_struct(prob):
     s.obs_uv = _d(k.obs_uv)
     s.huber_delta = float(prob.huber_delta or 0.0)
     s.intrinsics_free = 1 if getattr(prob, "intrinsics_free", False) else 0
+    s.camera_model = int(getattr(prob, "camera_model", CAMERA_PINHOLE))
+    ab = getattr(prob, "eucm_alpha_beta", (0.0, 0.0))
+    s.eucm_alpha_beta[0] = float(ab[0])
+    s.eucm_alpha_beta[1] = float(ab[1])
     s._keep = k
     return s
 
 
 def optimize(prob, params, n_threads=1, emulate_fp32=False, with_intrinsics=False):
     """Records, final poses and points (and the final intrinsics when
-    with_intrinsics; they change only when prob.intrinsics_free)."""
+    with_intrinsics: fx fy cx cy alpha beta, alpha and beta zero for a
+    pinhole; they change only when prob.intrinsics_free)."""
     L = lib()
     s = problem_struct(prob)
     mr = params.max_consecutive_rejects
@@ -137,7 +149,7 @@ def optimize(prob, params, n_threads=1, emulate_fp32=False, with_intrinsics=Fals
     n = C.c_int()
     poses = np.empty((s.n_cam, 7))
     points = np.empty((s.n_pt, 3))
-    intr = np.empty(4)
+    intr = np.empty(6)
     rc = L.ora_optimize_ex(C.byref(s), C.byref(p), int(n_threads), recs, cap, C.byref(n), _d(poses), _d(points),
                            _d(intr))
     if rc != 0:
@@ -234,3 +246,16 @@ def eval_term_intrinsics(pose, point, intr):
     lib().ora_eval_term_intrinsics(_d(np.ascontiguousarray(pose, float)), _d(np.ascontiguousarray(point, float)),
                                    _d(np.ascontiguousarray(intr, float)), _d(j))
     return j.reshape(2, 4)
+
+
+def eval_term_ex(pose, point, intr6, camera_model, uv):
+    """Residual, J_pose (2x6), J_point (2x3), J_cam (2 x 4 or 6) of one term."""
+    r = np.zeros(2)
+    jp = np.zeros(12)
+    jm = np.zeros(6)
+    jc = np.zeros(12)
+    lib().ora_eval_term_ex(_d(np.ascontiguousarray(pose, float)), _d(np.ascontiguousarray(point, float)),
+                           _d(np.ascontiguousarray(intr6, float)), int(camera_model),
+                           _d(np.ascontiguousarray(uv, float)), _d(r), _d(jp), _d(jm), _d(jc))
+    nc = 6 if camera_model == CAMERA_EUCM else 4
+    return r, jp.reshape(2, 6), jm.reshape(2, 3), jc[:2 * nc].reshape(2, nc)

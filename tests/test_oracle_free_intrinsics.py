@@ -67,7 +67,7 @@ def test_free_intrinsics_ba_converges(pkg, oracle):
         # than with them held Conditioned at the perturbed start
         assert abs(intr[0] - truth[0]) < 0.25 * abs(prob.intrinsics[0] - truth[0])
         rc, _, _, intr_c = oracle.optimize(cond, params, with_intrinsics=True)
-        np.testing.assert_array_equal(intr_c, cond.intrinsics)
+        np.testing.assert_array_equal(intr_c, list(cond.intrinsics) + [0.0, 0.0])
         assert recs[-1].merit < 0.2 * rc[-1].merit
 
 
@@ -81,4 +81,112 @@ def test_conditioned_intrinsics_stay_fixed(pkg, oracle):
     b, pb, qb = oracle.optimize(cond, params)
     assert [r.merit for r in a] == [r.merit for r in b]
     np.testing.assert_array_equal(pa, pb)
-    np.testing.assert_array_equal(ia, prob.intrinsics)
+    np.testing.assert_array_equal(ia, list(prob.intrinsics) + [0.0, 0.0])
+
+
+# ---- EUCM (the camera of the reference's BA example problem) -------------
+# enhanced_unified.rs:55-215; EucmCameraReprojectionCostTerm, ba_problem.rs:69-110;
+# the reference's true / initial params, ba_problem.rs:162-166,294-304.
+EUCM_TRUE = np.array([300.0, 300.0, 320.0, 240.0, 0.5, 1.0])
+EUCM_INIT = np.array([297.0, 297.0, 321.0, 241.0, 0.495, 1.0])
+
+
+def _rot(q):
+    w, x, y, z = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                     [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                     [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+
+
+def _eucm_project(params, x_cam):
+    fx, fy, cx, cy, alpha, beta = params
+    x, y = x_cam[0] / x_cam[2], x_cam[1] / x_cam[2]
+    rho = np.sqrt(beta * (x * x + y * y) + 1.0)
+    norm = alpha * rho + (1.0 - alpha)
+    return np.array([fx * x / norm + cx, fy * y / norm + cy])
+
+
+def _eucm_problem(pkg, seed, free=True):
+    prob = pkg.synth.generate(pkg.synth.CIRCLE, n_cam=4, n_pt=20, seed=seed)
+    uv = np.zeros((prob.n_obs, 2))
+    for o in range(prob.n_obs):
+        T = prob.poses_true[prob.obs_cam[o]]
+        uv[o] = _eucm_project(EUCM_TRUE, _rot(T[:4]).T @ (prob.points_true[prob.obs_pt[o]] - T[4:]))
+    prob.obs_uv = uv + 0.15 * (np.random.default_rng(2).random(uv.shape) - 0.5)
+    prob.poses[:2] = prob.poses_true[:2]
+    prob.pose_const[:2] = 1
+    prob.intrinsics = EUCM_INIT[:4].copy()
+    cond = prob.copy()
+    for pr in (prob, cond):
+        pr.camera_model = 1
+        pr.eucm_alpha_beta = EUCM_INIT[4:].copy()
+    prob.intrinsics_free = free
+    return prob, cond
+
+
+def test_eucm_jacobians_vs_central_differences(pkg, oracle):
+    prob = pkg.synth.generate(pkg.synth.CIRCLE, n_cam=5, n_pt=40, seed=3)
+    intr = EUCM_TRUE.copy()
+    for o in range(0, prob.n_obs, max(1, prob.n_obs // 20)):
+        pose, pt, uv = prob.poses[prob.obs_cam[o]], prob.points[prob.obs_pt[o]], prob.obs_uv[o]
+        r0, Jp, Jm, Jc = oracle.eval_term_ex(pose, pt, intr, 1, uv)
+
+        def res(ps=pose, p=pt, k=intr):
+            return oracle.eval_term_ex(ps, p, k, 1, uv)[0]
+        h = 1e-6
+        for k in range(6):  # left perturbation exp(delta) * T_wc
+            d = np.zeros(6)
+            d[k] = h
+            rp = res(ps=oracle.se3_mul(oracle.se3_exp(d), pose))
+            rm = res(ps=oracle.se3_mul(oracle.se3_exp(-d), pose))
+            np.testing.assert_allclose(Jp[:, k], (rp - rm) / (2 * h), rtol=1e-5, atol=1e-5)
+        for k in range(3):
+            e = np.zeros(3)
+            e[k] = h
+            np.testing.assert_allclose(Jm[:, k], (res(p=pt + e) - res(p=pt - e)) / (2 * h), rtol=1e-5, atol=1e-5)
+        for k in range(6):
+            hk = 1e-6 * max(1.0, abs(intr[k]))
+            ip, im = intr.copy(), intr.copy()
+            ip[k] += hk
+            im[k] -= hk
+            np.testing.assert_allclose(Jc[:, k], (res(k=ip) - res(k=im)) / (2 * hk), rtol=1e-5, atol=1e-6)
+
+
+def test_eucm_with_alpha_zero_is_the_pinhole(pkg, oracle):
+    prob = pkg.synth.generate(pkg.synth.CIRCLE, n_cam=5, n_pt=40, seed=4)
+    intr = np.array(list(prob.intrinsics) + [0.0, 0.7])
+    for o in range(0, prob.n_obs, 37):
+        pose, pt, uv = prob.poses[prob.obs_cam[o]], prob.points[prob.obs_pt[o]], prob.obs_uv[o]
+        r_e, jp_e, jm_e, jc_e = oracle.eval_term_ex(pose, pt, intr, 1, uv)
+        r_p, jp_p, jm_p, jc_p = oracle.eval_term_ex(pose, pt, intr, 0, uv)
+        np.testing.assert_allclose(r_e, r_p, rtol=1e-12, atol=1e-9)
+        np.testing.assert_allclose(jp_e, jp_p, rtol=1e-12, atol=1e-9)
+        np.testing.assert_allclose(jm_e, jm_p, rtol=1e-12, atol=1e-9)
+        np.testing.assert_allclose(jc_e[:, :4], jc_p, rtol=1e-12, atol=1e-12)
+
+
+def test_eucm_free_intrinsics_schur_vs_dense(pkg, oracle):
+    prob, _ = _eucm_problem(pkg, seed=3)
+    for nu in (1e-2, 1.0):
+        H, b = oracle.dense_system(prob, nu)
+        nf = int(np.sum(prob.pose_const == 0))
+        assert H.shape[0] == 6 + 6 * nf + 3 * prob.n_pt
+        dense = np.linalg.solve(H, b)
+        delta, S, rhs = oracle.schur_step(prob, nu)
+        np.testing.assert_allclose(delta, dense, rtol=1e-9, atol=1e-9 * np.abs(dense).max())
+
+
+def test_eucm_ba_converges(pkg, oracle):
+    """ba_problem.rs:517-547 with its EUCM camera free: pose RMS < 0.01,
+    point RMS < 0.1 after 20 iterations from the reference's initial params."""
+    params = pkg.OptParams(num_iterations=20, initial_lm_damping=1.0, function_tolerance=0.0, gradient_tolerance=0.0,
+                           parameter_tolerance=0.0, max_consecutive_rejects=1 << 40)
+    for seed in (pkg.synth.BASE_SEED, 5):
+        prob, cond = _eucm_problem(pkg, seed)
+        recs, poses, points, intr = oracle.optimize(prob, params, with_intrinsics=True)
+        pose_rms = np.sqrt(np.mean(np.sum((poses[:, 4:] - prob.poses_true[:, 4:]) ** 2, axis=1)))
+        pt_rms = np.sqrt(np.mean(np.sum((points - prob.points_true) ** 2, axis=1)))
+        assert pose_rms < 0.01 and pt_rms < 0.1, (seed, pose_rms, pt_rms)
+        rc, _, _ = oracle.optimize(cond, params)
+        assert recs[-1].merit < rc[-1].merit
+        assert abs(intr[0] - EUCM_TRUE[0]) < abs(EUCM_INIT[0] - EUCM_TRUE[0])
