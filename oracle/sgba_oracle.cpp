@@ -20,6 +20,8 @@
 //   crates/sophus_lie/src/lie_group/lie_group_manifold.rs:33-35,57-64
 //   crates/sophus_sensor/src/projections/perspective.rs:30-72
 //   crates/sophus_sensor/src/distortions/affine.rs:50-108
+//   crates/sophus_sensor/src/distortions/enhanced_unified.rs:55-215  EUCM camera
+//   crates/sophus_opt/src/example_problems/ba_problem.rs:69-110     EUCM cost term (free intrinsics)
 //   crates/sophus_solver/src/ldlt/schur_ldlt.rs:82-278,536-812
 //   crates/sophus_solver/src/ldlt/block_sparse_ldlt.rs:99-190,479-747
 //   crates/sophus_solver/src/ldlt/dense_ldlt.rs:164-308
