@@ -1099,6 +1099,86 @@ int schur_step_impl(const ora_problem* p, const Structure& s, const double* intr
   return schur_solve<R>(p, s, sys, n_threads, delta, S, rhs);
 }
 
+// Covariance queries (SchurFactor::inverse_block, schur_ldlt.rs:815-957) at
+// the given variables with zero damping: S^-1 densely (the block LDLT of S
+// applied to unit vectors), H_mm^-1 and the rows H_mf per marg block.
+struct CovCtx {
+  Structure s;
+  System<double> sys;
+  int n = 0, nci = 0, nc = 0;
+  std::vector<double> Sinv;  // n x n
+};
+
+int cov_build(const ora_problem* p, CovCtx* c) {
+  build_structure(p, &c->s);
+  double intr[6];
+  problem_intrinsics(p, intr);
+  build_system<double>(p, c->s, intr, p->poses, p->points, 0.0, 1, &c->sys);
+  std::vector<double> delta, S, rhs;
+  if (schur_solve<double>(p, c->s, c->sys, 1, &delta, &S, &rhs) != 0) return -2;
+  c->nc = cam_params(p);
+  c->nci = p->intrinsics_free ? 6 : 0;
+  c->n = c->nci + 6 * c->s.nf;
+  const int n = c->n;
+  BlockLdlt f;
+  if (f.factorize(n, 6, S.data()) != 0) return -2;
+  c->Sinv.assign(static_cast<size_t>(n) * n, 0.0);
+  std::vector<double> e(n);
+  for (int j = 0; j < n; ++j) {
+    std::fill(e.begin(), e.end(), 0.0);
+    e[j] = 1.0;
+    f.solve(e.data());
+    for (int i = 0; i < n; ++i) c->Sinv[static_cast<size_t>(i) * n + j] = e[i];
+  }
+  return 0;
+}
+
+// Offset and size in S of a free variable, or -1.
+int cov_free_offset(const ora_problem* p, const CovCtx& c, int kind, int index, int* dim) {
+  if (kind == ORA_VAR_INTRINSICS) {
+    *dim = c.nc;
+    return p->intrinsics_free ? 0 : -1;
+  }
+  if (kind == ORA_VAR_POSE) {
+    *dim = 6;
+    if (index < 0 || index >= p->n_cam || c.s.pose_block[index] < 0) return -1;
+    return c.nci + 6 * c.s.pose_block[index];
+  }
+  return -1;
+}
+
+// H_mf of point q as a dense 3 x n row block (S's column layout).
+std::vector<double> cov_hmf(const ora_problem* p, const CovCtx& c, int q) {
+  const int n = c.n, mb = c.s.point_block[q];
+  std::vector<double> h(static_cast<size_t>(3) * n, 0.0);
+  for (int64_t r = c.s.pt_rng_begin[q]; r < c.s.pt_rng_begin[q + 1]; ++r) {
+    int fb = c.s.pose_block[c.s.rng_pose[r]];
+    if (fb < 0) continue;
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < 6; ++k) h[static_cast<size_t>(i) * n + c.nci + fb * 6 + k] = c.sys.Wr[r * 18 + i * 6 + k];
+  }
+  if (p->intrinsics_free)
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < c.nc; ++k) h[static_cast<size_t>(i) * n + k] = c.sys.Hmc[static_cast<size_t>(mb) * 3 * c.nc + i * c.nc + k];
+  return h;
+}
+
+bool cov_hmm_inv(const CovCtx& c, int q, double* inv) {
+  return inverse3<double>(&c.sys.V[static_cast<size_t>(c.s.point_block[q]) * 9], inv);
+}
+
+// -(S^-1[free rows, :] H_mf_q^T) H_mm[q]^-1  (dim x 3)
+void cov_free_marg(const CovCtx& c, int off, int dim, const std::vector<double>& hmf, const double* hinv,
+                   double* out) {
+  const int n = c.n;
+  for (int a = 0; a < dim; ++a) {
+    double t[3] = {0.0, 0.0, 0.0};
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < n; ++k) t[i] += c.Sinv[static_cast<size_t>(off + a) * n + k] * hmf[static_cast<size_t>(i) * n + k];
+    for (int j = 0; j < 3; ++j) out[a * 3 + j] = -(t[0] * hinv[0 * 3 + j] + t[1] * hinv[1 * 3 + j] + t[2] * hinv[2 * 3 + j]);
+  }
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -1341,4 +1421,63 @@ int ora_optimize_ex(const ora_problem* p, const ora_params* prm, int n_threads,
   return rc;
 }
 
-}  // extern "C"
+int ora_covariance_block(const ora_problem* p, int32_t row_kind, int32_t row_index, int32_t col_kind,
+                         int32_t col_index, double* out, int32_t* rows, int32_t* cols) {
+  CovCtx c;
+  const int st = cov_build(p, &c);
+  if (st != 0) return st;
+  auto point_ok = [&](int q) { return q >= 0 && q < p->n_pt && c.s.point_block[q] >= 0; };
+  const bool rf = row_kind != ORA_VAR_POINT, cf = col_kind != ORA_VAR_POINT;
+  int rd = 3, cd = 3;
+  const int ro = rf ? cov_free_offset(p, c, row_kind, row_index, &rd) : (point_ok(row_index) ? 0 : -1);
+  const int co = cf ? cov_free_offset(p, c, col_kind, col_index, &cd) : (point_ok(col_index) ? 0 : -1);
+  if (ro < 0 || co < 0) return -1;
+  if (rows) *rows = rd;
+  if (cols) *cols = cd;
+  const int n = c.n;
+  if (rf && cf) {
+    for (int a = 0; a < rd; ++a)
+      for (int b = 0; b < cd; ++b) out[a * cd + b] = c.Sinv[static_cast<size_t>(ro + a) * n + co + b];
+    return 0;
+  }
+  if (rf || cf) {  // free x marg, or its transpose
+    const int q = rf ? col_index : row_index;
+    const int off = rf ? ro : co, dim = rf ? rd : cd;
+    double hinv[9];
+    if (!cov_hmm_inv(c, q, hinv)) return -2;
+    std::vector<double> fm(static_cast<size_t>(dim) * 3);
+    cov_free_marg(c, off, dim, cov_hmf(p, c, q), hinv, fm.data());
+    for (int a = 0; a < dim; ++a)
+      for (int j = 0; j < 3; ++j) {
+        if (rf) out[a * 3 + j] = fm[a * 3 + j];
+        else out[j * dim + a] = fm[a * 3 + j];
+      }
+    return 0;
+  }
+  // marg x marg: H_mm[i]^-1 H_mf_i S^-1 H_mf_j^T H_mm[j]^-1 (+ H_mm[i]^-1 on the diagonal)
+  double hi[9], hj[9];
+  if (!cov_hmm_inv(c, row_index, hi) || !cov_hmm_inv(c, col_index, hj)) return -2;
+  const std::vector<double> fi = cov_hmf(p, c, row_index), fj = cov_hmf(p, c, col_index);
+  double core[9];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      double acc = 0.0;
+      for (int k = 0; k < n; ++k) {
+        double sk = 0.0;
+        for (int l = 0; l < n; ++l) sk += c.Sinv[static_cast<size_t>(k) * n + l] * fj[static_cast<size_t>(b) * n + l];
+        acc += fi[static_cast<size_t>(a) * n + k] * sk;
+      }
+      core[a * 3 + b] = acc;
+    }
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      double v = 0.0;
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) v += hi[a * 3 + k] * core[k * 3 + l] * hj[l * 3 + b];
+      if (row_index == col_index) v += hi[a * 3 + b];
+      out[a * 3 + b] = v;
+    }
+  return 0;
+}
+
+}  // extern "C\"

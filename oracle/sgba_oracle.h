@@ -152,6 +152,28 @@ void ora_eval_term_ex(const double pose[7], const double point[3],
                       double r[2], double j_pose[12], double j_point[6],
                       double j_cam[12]);
 
+/* Covariance block between two variables: a block of the inverse of the
+ * undamped H at the given variables, through the Schur complement as
+ * SchurFactor::inverse_block computes it (crates/sophus_solver/src/ldlt/schur_ldlt.rs:815-957):
+ *   free x free  S^-1[row, col]
+ *   free x marg  -(S^-1 H_fm H_mm^-1)[row, col]
+ *   marg x marg  H_mm^-1 delta_ij + H_mm[i]^-1 H_mf_i S^-1 H_mf_j^T H_mm[j]^-1
+ * Kinds: ORA_VAR_INTRINSICS (index ignored; only when they are free),
+ * ORA_VAR_POSE (pose index), ORA_VAR_POINT (point index).  out receives the
+ * rows x cols block row-major (4 or 6 intrinsics, 6 per pose, 3 per point).
+ * Returns 0; -1 for a variable without a block (constant or Conditioned, where
+ * the reference returns None); -2 when S cannot be factored.  Full-rank H
+ * only: the reference's min-norm pseudo-inverse for a gauge-deficient S is
+ * not restated. */
+enum {
+  ORA_VAR_INTRINSICS = 0,
+  ORA_VAR_POSE = 1,
+  ORA_VAR_POINT = 2,
+};
+int ora_covariance_block(const ora_problem *p, int32_t row_kind, int32_t row_index,
+                         int32_t col_kind, int32_t col_index, double *out,
+                         int32_t *rows, int32_t *cols);
+
 #ifdef __cplusplus
 }
 #endif

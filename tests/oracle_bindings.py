@@ -86,6 +86,8 @@ def lib():
                                       C.POINTER(OraRecord), C.c_int, C.POINTER(C.c_int), dp, dp, dp]
         L.ora_eval_term_intrinsics.argtypes = [dp, dp, dp, dp]
         L.ora_eval_term_ex.argtypes = [dp, dp, dp, C.c_int32, dp, dp, dp, dp, dp]
+        L.ora_covariance_block.argtypes = [C.POINTER(OraProblem), C.c_int32, C.c_int32, C.c_int32, C.c_int32, dp,
+                                           C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         _lib = L
     return _lib
 
@@ -259,3 +261,21 @@ def eval_term_ex(pose, point, intr6, camera_model, uv):
                            _d(np.ascontiguousarray(uv, float)), _d(r), _d(jp), _d(jm), _d(jc))
     nc = 6 if camera_model == CAMERA_EUCM else 4
     return r, jp.reshape(2, 6), jm.reshape(2, 3), jc[:2 * nc].reshape(2, nc)
+
+
+VAR_INTRINSICS, VAR_POSE, VAR_POINT = 0, 1, 2
+
+
+def covariance_block(prob, row, col):
+    """Covariance block between row = (kind, index) and col = (kind, index)
+    (SchurFactor::inverse_block), or None for a variable without a block."""
+    s = problem_struct(prob)
+    out = np.zeros(36)
+    nr, nc = C.c_int32(), C.c_int32()
+    rc = lib().ora_covariance_block(C.byref(s), int(row[0]), int(row[1]), int(col[0]), int(col[1]), _d(out),
+                                    C.byref(nr), C.byref(nc))
+    if rc == -1:
+        return None
+    if rc != 0:
+        raise RuntimeError("oracle covariance failed with %d" % rc)
+    return out[:nr.value * nc.value].reshape(nr.value, nc.value)

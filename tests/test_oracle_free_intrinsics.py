@@ -190,3 +190,42 @@ def test_eucm_ba_converges(pkg, oracle):
         rc, _, _ = oracle.optimize(cond, params)
         assert recs[-1].merit < rc[-1].merit
         assert abs(intr[0] - EUCM_TRUE[0]) < abs(EUCM_INIT[0] - EUCM_TRUE[0])
+
+
+# ---- covariance queries (SchurFactor::inverse_block, schur_ldlt.rs:815-957) ----
+
+
+def _dense_offsets(prob, c0):
+    nf_idx = np.cumsum(prob.pose_const == 0) - 1
+    nf = int(np.sum(prob.pose_const == 0))
+    return (lambda j: c0 + 6 * int(nf_idx[j])), (lambda q: c0 + 6 * nf + 3 * q)
+
+
+def test_covariance_blocks_vs_dense_inverse(pkg, oracle):
+    """Every kind of block against the inverse of the dense undamped H."""
+    cases = []
+    prob, _, _ = _problem(pkg, seed=3, free=False)  # pinhole, intrinsics Conditioned
+    cases.append((prob, 0))
+    prob, _ = _eucm_problem(pkg, seed=3)  # EUCM, intrinsics free (6 params first)
+    cases.append((prob, 6))
+    for prob, c0 in cases:
+        H, _ = oracle.dense_system(prob, 0.0)
+        cov = np.linalg.inv(H)
+        pose_off, pt_off = _dense_offsets(prob, c0)
+        scale = np.abs(cov).max()
+        free_poses = [j for j in range(prob.n_cam) if not prob.pose_const[j]]
+        pairs = [((1, free_poses[0]), (1, free_poses[-1])), ((1, free_poses[-1]), (2, 5)), ((2, 5), (1, free_poses[0])),
+                 ((2, 3), (2, 3)), ((2, 3), (2, 11))]
+        if c0:
+            pairs += [((0, 0), (0, 0)), ((0, 0), (1, free_poses[0])), ((2, 7), (0, 0))]
+        for row, col in pairs:
+            blk = oracle.covariance_block(prob, row, col)
+            def rng(v):
+                kind, idx = v
+                return (slice(0, c0) if kind == 0 else slice(pose_off(idx), pose_off(idx) + 6) if kind == 1
+                        else slice(pt_off(idx), pt_off(idx) + 3))
+            np.testing.assert_allclose(blk, cov[rng(row), rng(col)], rtol=1e-7, atol=1e-9 * scale)
+        # constant poses and Conditioned intrinsics have no block (the reference returns None)
+        assert oracle.covariance_block(prob, (1, 0), (1, 0)) is None
+        if not c0:
+            assert oracle.covariance_block(prob, (0, 0), (0, 0)) is None
