@@ -1,12 +1,13 @@
-"""The oracle with Free pinhole intrinsics (family kinds (F, F, M)): the first
-step of the scope table's next row (free intrinsics), checked on the CPU
-before any GPU kernel exists for it.
+"""The oracle beyond the GPU path: Free intrinsics (family kinds (F, F, M)),
+the EUCM camera and covariance queries, checked on the CPU before any GPU
+kernel exists for them.
 
-  J_cam         pinhole_reprojection.rs:85 (-dx_distort_params, affine.rs:77-108)
-                against central differences of the residual
+  J_cam            pinhole_reprojection.rs:85 (-dx_distort_params, affine.rs:77-108),
+                   enhanced_unified.rs:55-215; against central differences
   schur_vs_dense   schur_ldlt.rs:1083-1127 (1e-9), with the intrinsics block
-  ba_converges  ba_problem.rs:517-547: free intrinsics started 1 % off, poses
-                0 and 1 fixed; pose RMS < 0.01, point RMS < 0.1
+  ba_converges     ba_problem.rs:517-547: free intrinsics started off the truth,
+                   poses 0 and 1 fixed; pose RMS < 0.01, point RMS < 0.1
+  inverse_block    schur_ldlt.rs:815-957 against the dense inverse of H
 """
 import numpy as np
 
