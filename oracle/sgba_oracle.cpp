@@ -22,7 +22,10 @@
 //   crates/sophus_sensor/src/distortions/affine.rs:50-108
 //   crates/sophus_sensor/src/distortions/enhanced_unified.rs:55-215  EUCM camera
 //   crates/sophus_opt/src/example_problems/ba_problem.rs:69-110     EUCM cost term (free intrinsics)
-//   crates/sophus_solver/src/ldlt/schur_ldlt.rs:82-278,536-812
+//   crates/sophus_solver/src/ldlt/schur_ldlt.rs:82-278,450-490,536-812  (range-space KKT)
+//   crates/sophus_opt/src/nlls/linear_system/eq_system.rs:149-258  G^T lambda, -c, update_lambdas
+//   crates/sophus_opt/src/example_problems/ba_scale_constraint.rs:57-100  TranslationNormConstraint
+//   crates/sophus_opt/src/nlls/optimizer.rs:527-535             no gradient test with constraints
 //   crates/sophus_solver/src/ldlt/block_sparse_ldlt.rs:99-190,479-747
 //   crates/sophus_solver/src/ldlt/dense_ldlt.rs:164-308
 //   crates/sophus_solver/src/ldlt/block_diag_ldlt.rs:80-160
@@ -36,6 +39,8 @@
 //     "determinant exactly zero => failure" rule as nalgebra's try_inverse.
 //   * Bunch-Kaufman fallback for indefinite ill-conditioned pivot blocks is
 //     not restated; such a block is reported as a solve failure (a reject).
+//   * The small dense inverse of G S^-1 G^T is Gauss-Jordan with partial
+//     pivoting where nalgebra's try_inverse uses closed forms up to 3x3.
 #include "sgba_oracle.h"
 
 #include <algorithm>
@@ -880,10 +885,67 @@ void build_system(const ora_problem* p, const Structure& s, const double* intr, 
 // precedes the poses'), padded to one 6-row block with an identity so the
 // factor keeps 6x6 blocks; the pivot rule restarts at that block as at every
 // partition block.
+// Equality constraints TranslationNormConstraint (ba_scale_constraint.rs:44-100):
+// c(T) = |t(T)| - r.  Its Jacobian is taken, as the reference's dual numbers
+// take it, under the left perturbation exp(x) * T at x = 0.  The tangent is
+// (w, v), rotation first (affine_group_template.rs:162-169); the translation
+// moves by w x t + v, so dc/dv = t^T / |t| and dc/dw = t^T [e_k]x t / |t| = 0,
+// exactly zero in floating point as well.
+struct EqTerms {
+  int n = 0;
+  std::vector<double> c;    // n residuals
+  std::vector<double> jac;  // n x 6, row-major
+  std::vector<int> fb;      // free block of each term's pose, -1 when the pose is constant
+};
+
+void eq_eval(const ora_problem* p, const Structure* s, const double* poses, EqTerms* e) {
+  e->n = p->n_eq;
+  e->c.assign(e->n, 0.0);
+  e->jac.assign(static_cast<size_t>(e->n) * 6, 0.0);
+  e->fb.assign(e->n, -1);
+  for (int k = 0; k < e->n; ++k) {
+    if (p->eq_pose[k] < 0 || p->eq_pose[k] >= p->n_cam) { e->c[k] = NAN; continue; }
+    const double* t = poses + 7 * p->eq_pose[k] + 4;
+    double nrm = std::sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+    e->c[k] = nrm - p->eq_radius[k];
+    for (int i = 0; i < 3; ++i) e->jac[k * 6 + 3 + i] = t[i] / nrm;
+    if (s) e->fb[k] = s->pose_block[p->eq_pose[k]];
+  }
+}
+
+// Inverse of the small dense m x m matrix G S^-1 G^T (nalgebra try_inverse in
+// schur_ldlt.rs:723-728): Gauss-Jordan with partial pivoting.  False when a
+// pivot is zero or not finite.
+bool small_inverse(int m, std::vector<double> a, std::vector<double>* inv) {
+  inv->assign(static_cast<size_t>(m) * m, 0.0);
+  for (int i = 0; i < m; ++i) (*inv)[i * m + i] = 1.0;
+  for (int col = 0; col < m; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < m; ++r)
+      if (std::fabs(a[r * m + col]) > std::fabs(a[piv * m + col])) piv = r;
+    double d = a[piv * m + col];
+    if (!(std::fabs(d) > 0.0) || !std::isfinite(d)) return false;
+    if (piv != col)
+      for (int c = 0; c < m; ++c) {
+        std::swap(a[piv * m + c], a[col * m + c]);
+        std::swap((*inv)[piv * m + c], (*inv)[col * m + c]);
+      }
+    for (int c = 0; c < m; ++c) { a[col * m + c] /= d; (*inv)[col * m + c] /= d; }
+    for (int r = 0; r < m; ++r) {
+      if (r == col) continue;
+      double f = a[r * m + col];
+      if (f == 0.0) continue;
+      for (int c = 0; c < m; ++c) { a[r * m + c] -= f * a[col * m + c]; (*inv)[r * m + c] -= f * (*inv)[col * m + c]; }
+    }
+  }
+  return true;
+}
+
 template <class R>
 int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
                 int n_threads, std::vector<double>* delta, std::vector<double>* s_out,
-                std::vector<double>* rhs_out) {
+                std::vector<double>* rhs_out, const EqTerms* eq = nullptr,
+                const double* lambda = nullptr) {
   const bool fc = p->intrinsics_free != 0;
   const int nc = cam_params(p);
   const int nf = s.nf;
@@ -985,6 +1047,14 @@ int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
         for (int c = 0; c < 6; ++c)
           Sacc[static_cast<size_t>(nci + i * 6 + r) * n + nci + i * 6 + c] = sys.U[static_cast<size_t>(i) * 36 + r * 6 + c];
     for (int i = 0; i < n6; ++i) racc[nci + i] = sys.bp[i];
+    if (eq && lambda) {
+      // the constraint rows add G^T lambda to the free gradient when the KKT
+      // system is populated (eq_system.rs, populate_lower_triangular_kkt_mat)
+      for (int k = 0; k < eq->n; ++k) {
+        if (eq->fb[k] < 0) continue;
+        for (int c = 0; c < 6; ++c) racc[nci + eq->fb[k] * 6 + c] += static_cast<R>(eq->jac[k * 6 + c] * lambda[k]);
+      }
+    }
     if (fc) {
       for (int r = 0; r < nc; ++r)
         for (int c = 0; c < nc; ++c) Sacc[static_cast<size_t>(r) * n + c] = sys.Ucc[r * nc + c];
@@ -1012,7 +1082,47 @@ int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
   if (f.factorize(n, 6, S.data()) != 0) return -1;
   std::vector<double> dxf(rhs);
   f.solve(dxf.data());
-  delta->assign(static_cast<size_t>(nc4) + static_cast<size_t>(n6) + static_cast<size_t>(s.nm) * 3, 0.0);
+  const int m = eq ? eq->n : 0;
+  std::vector<double> dlam(m, 0.0);
+  if (m > 0) {
+    // Range-space KKT solve (SchurFactor::factorize / solve, schur_ldlt.rs:674-772):
+    // Y = S^-1 G^T, M = G Y, dlam = M^-1 (G u - rhs_c) with rhs_c = -c,
+    // dx_f = S^-1 (rhs_bar - G^T dlam).
+    std::vector<double> G(static_cast<size_t>(m) * n, 0.0);
+    for (int k = 0; k < m; ++k)
+      if (eq->fb[k] >= 0)
+        for (int c = 0; c < 6; ++c) G[static_cast<size_t>(k) * n + nci + eq->fb[k] * 6 + c] = eq->jac[k * 6 + c];
+    std::vector<double> Y(static_cast<size_t>(m) * n);  // column k of Y stored as row k
+    for (int k = 0; k < m; ++k) {
+      std::copy(&G[static_cast<size_t>(k) * n], &G[static_cast<size_t>(k + 1) * n], &Y[static_cast<size_t>(k) * n]);
+      f.solve(&Y[static_cast<size_t>(k) * n]);
+    }
+    std::vector<double> M(static_cast<size_t>(m) * m), Minv;
+    for (int a = 0; a < m; ++a)
+      for (int b = 0; b < m; ++b) {
+        double acc = 0.0;
+        for (int i = 0; i < n; ++i) acc += G[static_cast<size_t>(a) * n + i] * Y[static_cast<size_t>(b) * n + i];
+        M[a * m + b] = acc;
+      }
+    if (!small_inverse(m, M, &Minv)) return -2;
+    std::vector<double> w(m);
+    for (int k = 0; k < m; ++k) {
+      double acc = 0.0;
+      for (int i = 0; i < n; ++i) acc += G[static_cast<size_t>(k) * n + i] * dxf[i];
+      w[k] = acc + eq->c[k];
+    }
+    for (int a = 0; a < m; ++a) {
+      double acc = 0.0;
+      for (int b = 0; b < m; ++b) acc += Minv[a * m + b] * w[b];
+      dlam[a] = acc;
+    }
+    dxf = rhs;
+    for (int k = 0; k < m; ++k)
+      for (int i = 0; i < n; ++i) dxf[i] -= G[static_cast<size_t>(k) * n + i] * dlam[k];
+    f.solve(dxf.data());
+  }
+  delta->assign(static_cast<size_t>(nc4) + static_cast<size_t>(n6) + static_cast<size_t>(s.nm) * 3 + m, 0.0);
+  for (int k = 0; k < m; ++k) (*delta)[nc4 + n6 + static_cast<size_t>(s.nm) * 3 + k] = dlam[k];
   for (int i = 0; i < nc4; ++i) (*delta)[i] = dxf[i];
   for (int i = 0; i < n6; ++i) (*delta)[nc4 + i] = dxf[nci + i];
   // back-substitution: dx_m[b] = H_mm^-1 (g_m[b] - sum H_mf[b,f] dx_f[f] - H_mc[b] dx_c)
@@ -1080,11 +1190,19 @@ bool apply_update(const ora_problem* p, const Structure& s, const std::vector<do
   return ok;
 }
 
+// EqSystem::update_lambdas (eq_system.rs): lambda <- lambda - dlam, dlam the
+// last n_eq entries of the step.
+void update_lambdas(int n_eq, const std::vector<double>& delta, std::vector<double>* lambda) {
+  const size_t off = delta.size() - static_cast<size_t>(n_eq);
+  for (int k = 0; k < n_eq; ++k) (*lambda)[k] -= delta[off + k];
+}
+
 template <class R>
 int schur_step_impl(const ora_problem* p, const Structure& s, const double* intr, const double* poses,
                     const double* points, double nu, int n_threads, std::vector<double>* delta,
                     double* max_grad, std::vector<double>* neg_grad, std::vector<double>* S,
-                    std::vector<double>* rhs, double gradient_tolerance = -1.0) {
+                    std::vector<double>* rhs, double gradient_tolerance = -1.0,
+                    const EqTerms* eq = nullptr, const double* lambda = nullptr) {
   System<R> sys;
   build_system<R>(p, s, intr, poses, points, nu, n_threads, &sys);
   if (max_grad) *max_grad = sys.max_grad;
@@ -1093,10 +1211,22 @@ int schur_step_impl(const ora_problem* p, const Structure& s, const double* intr
     for (auto v : sys.bc) neg_grad->push_back(static_cast<double>(v));
     for (auto v : sys.bp) neg_grad->push_back(static_cast<double>(v));
     for (auto v : sys.bm) neg_grad->push_back(static_cast<double>(v));
+    if (eq) {
+      // the KKT right-hand side: + G^T lambda on the free rows, -c on the
+      // constraint rows (eq_system.rs, populate_lower_triangular_kkt_mat)
+      const size_t nc4 = sys.bc.size();
+      for (int k = 0; k < eq->n; ++k) {
+        if (eq->fb[k] < 0) continue;
+        for (int c = 0; c < 6; ++c)
+          (*neg_grad)[nc4 + static_cast<size_t>(eq->fb[k]) * 6 + c] += eq->jac[k * 6 + c] * lambda[k];
+      }
+      for (int k = 0; k < eq->n; ++k) neg_grad->push_back(-eq->c[k]);
+    }
   }
-  // check_gradient_tolerance happens before the solve (optimizer_step.rs:382-384)
-  if (sys.max_grad < gradient_tolerance) return 1;
-  return schur_solve<R>(p, s, sys, n_threads, delta, S, rhs);
+  // check_gradient_tolerance happens before the solve (optimizer_step.rs:382-384);
+  // it is skipped when there are equality constraints (optimizer.rs:527-535)
+  if (!(eq && eq->n > 0) && sys.max_grad < gradient_tolerance) return 1;
+  return schur_solve<R>(p, s, sys, n_threads, delta, S, rhs, eq, lambda);
 }
 
 // Covariance queries (SchurFactor::inverse_block, schur_ldlt.rs:815-957) at
@@ -1337,6 +1467,10 @@ int ora_optimize_ex(const ora_problem* p, const ora_params* prm, int n_threads,
   std::vector<double> poses(p->poses, p->poses + 7 * p->n_cam);
   std::vector<double> points(p->points, p->points + 3 * p->n_pt);
   std::vector<double> npose(poses.size()), npts(points.size());
+  for (int k = 0; k < p->n_eq; ++k)
+    if (p->eq_pose[k] < 0 || p->eq_pose[k] >= p->n_cam) return -11;
+  EqTerms eq;
+  std::vector<double> lambda(p->n_eq, 0.0);  // EqSystem::new: zero multipliers
   double merit = total_cost(p, intr.data(), poses.data(), points.data(), n_threads);
   double nu = prm->initial_lm_damping;
   int64_t rejects = 0;
@@ -1352,13 +1486,18 @@ int ora_optimize_ex(const ora_problem* p, const ora_params* prm, int n_threads,
     int reason = ORA_TERM_NONE;
     std::vector<double> delta, neg_grad;
     double max_grad = 0.0;
+    const EqTerms* eqp = nullptr;
+    if (p->n_eq > 0) {  // eq_system.eval before the cost system (optimizer_helpers.rs:277-283)
+      eq_eval(p, &s, poses.data(), &eq);
+      eqp = &eq;
+    }
     int st = prm->emulate_fp32
                  ? schur_step_impl<float>(p, s, intr.data(), poses.data(), points.data(), nu, n_threads, &delta,
                                           &max_grad, &neg_grad, nullptr, nullptr,
-                                          prm->gradient_tolerance)
+                                          prm->gradient_tolerance, eqp, lambda.data())
                  : schur_step_impl<double>(p, s, intr.data(), poses.data(), points.data(), nu, n_threads, &delta,
                                            &max_grad, &neg_grad, nullptr, nullptr,
-                                           prm->gradient_tolerance);
+                                           prm->gradient_tolerance, eqp, lambda.data());
     rec.max_grad = max_grad;
     if (st == 1) {
       reason = ORA_TERM_GRADIENT_TOL;
@@ -1379,6 +1518,7 @@ int ora_optimize_ex(const ora_problem* p, const ora_params* prm, int n_threads,
       if (max_step < prm->parameter_tolerance) {
         if (new_merit < merit) {
           intr.swap(nintr); poses.swap(npose); points.swap(npts); merit = new_merit; rec.accepted = 1;
+          update_lambdas(p->n_eq, delta, &lambda);
         }
         reason = ORA_TERM_PARAMETER_TOL;
       } else {
@@ -1398,6 +1538,7 @@ int ora_optimize_ex(const ora_problem* p, const ora_params* prm, int n_threads,
           double rel = (merit - new_merit) / (std::fabs(merit) + kMinPositive);
           if (rel < prm->function_tolerance) reason = ORA_TERM_FUNCTION_TOL;
           intr.swap(nintr); poses.swap(npose); points.swap(npts); merit = new_merit; rec.accepted = 1;
+          update_lambdas(p->n_eq, delta, &lambda);
         } else {
           nu *= 2.0;
           rejects += 1;
@@ -1480,4 +1621,28 @@ int ora_covariance_block(const ora_problem* p, int32_t row_kind, int32_t row_ind
   return 0;
 }
 
-}  // extern "C\"
+void ora_eq_eval(const ora_problem* p, const double* poses, double* c, double* jac) {
+  EqTerms e;
+  eq_eval(p, nullptr, poses, &e);
+  if (c) std::memcpy(c, e.c.data(), sizeof(double) * e.c.size());
+  if (jac) std::memcpy(jac, e.jac.data(), sizeof(double) * e.jac.size());
+}
+
+int ora_schur_kkt_step(const ora_problem* p, double nu, const double* lambda, int n_threads, double* delta) {
+  for (int k = 0; k < p->n_eq; ++k)
+    if (p->eq_pose[k] < 0 || p->eq_pose[k] >= p->n_cam) return -11;
+  Structure s;
+  build_structure(p, &s);
+  double intr[6];
+  problem_intrinsics(p, intr);
+  EqTerms eq;
+  eq_eval(p, &s, p->poses, &eq);
+  std::vector<double> d;
+  int st = schur_step_impl<double>(p, s, intr, p->poses, p->points, nu, n_threads, &d, nullptr, nullptr,
+                                   nullptr, nullptr, -1.0, &eq, lambda);
+  if (st != 0) return st;
+  std::memcpy(delta, d.data(), sizeof(double) * d.size());
+  return 0;
+}
+
+}  // extern "C"

@@ -99,6 +99,11 @@ typedef struct {
   int32_t camera_model;        /* ORA_CAMERA_PINHOLE (params fx fy cx cy) or
                                   ORA_CAMERA_EUCM (fx fy cx cy alpha beta) */
   double eucm_alpha_beta[2];   /* alpha, beta of the EUCM model */
+  int32_t n_eq;                /* equality constraints |t(pose)| = radius
+                                  (TranslationNormConstraint, ba_scale_constraint.rs:44-100);
+                                  0: unconstrained */
+  const int32_t *eq_pose;      /* n_eq pose indices (each a Free pose) */
+  const double *eq_radius;     /* n_eq target translation norms */
 } ora_problem;
 
 enum {
@@ -126,7 +131,12 @@ int ora_schur_step(const ora_problem *p, double nu, int n_threads,
                    double *rhs_bar_out);
 
 /* optimize_nlls on this path.  poses_out/points_out receive the final
- * variables.  Returns 0 or a negative error code. */
+ * variables.  With equality constraints (n_eq > 0) each step is the KKT step
+ * of ora_schur_kkt_step from multipliers that start at zero, the gain ratio
+ * and the parameter test run over [dx; dlam] against [neg_grad + G^T lambda;
+ * -c], the merit stays the cost alone, and the gradient test is skipped
+ * (optimizer_step.rs:365-430, optimizer.rs:527-535).  Returns 0 or a
+ * negative error code. */
 int ora_optimize(const ora_problem *p, const ora_params *params,
                  int n_threads, ora_record *records, int cap, int *n_records,
                  double *poses_out, double *points_out);
@@ -173,6 +183,27 @@ enum {
 int ora_covariance_block(const ora_problem *p, int32_t row_kind, int32_t row_index,
                          int32_t col_kind, int32_t col_index, double *out,
                          int32_t *rows, int32_t *cols);
+
+/* ---- equality constraints (Schur path, range-space KKT) ------------------ */
+/* Residuals c_k = |t(T_k)| - r_k of the problem's TranslationNormConstraint
+ * terms at the given poses (n_cam x 7), and their Jacobians under the left
+ * perturbation exp(x) * T at x = 0, row-major n_eq x 6
+ * (ba_scale_constraint.rs:64-100). */
+void ora_eq_eval(const ora_problem *p, const double *poses, double *c, double *jac);
+
+/* One damped step with the equality constraints, at the problem's variables
+ * and the multipliers lambda (n_eq): the KKT system
+ *   [H   G^T] [dx  ]   [neg_grad + G^T lambda]
+ *   [G   0  ] [dlam] = [-c                   ]
+ * solved as SchurFactor::solve does it (schur_ldlt.rs:756-812): points
+ * eliminated, then u = S^-1 rhs_bar, dlam = (G S^-1 G^T)^-1 (G u + c),
+ * dx_f = S^-1 (rhs_bar - G^T dlam), points back-substituted.  delta receives
+ * n + n_eq entries: dx in the layout of ora_dense_system, then dlam.  The
+ * multipliers then move as lambda <- lambda - dlam (EqSystem::update_lambdas).
+ * Returns 0; -1 when S cannot be factored; -2 for a singular G S^-1 G^T
+ * (SingularKktConstraint). */
+int ora_schur_kkt_step(const ora_problem *p, double nu, const double *lambda, int n_threads,
+                       double *delta);
 
 #ifdef __cplusplus
 }

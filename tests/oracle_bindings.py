@@ -55,6 +55,9 @@ class OraProblem(C.Structure):
         ("intrinsics_free", C.c_int32),
         ("camera_model", C.c_int32),
         ("eucm_alpha_beta", C.c_double * 2),
+        ("n_eq", C.c_int32),
+        ("eq_pose", C.POINTER(C.c_int32)),
+        ("eq_radius", C.POINTER(C.c_double)),
     ]
 
 
@@ -88,6 +91,8 @@ def lib():
         L.ora_eval_term_ex.argtypes = [dp, dp, dp, C.c_int32, dp, dp, dp, dp, dp]
         L.ora_covariance_block.argtypes = [C.POINTER(OraProblem), C.c_int32, C.c_int32, C.c_int32, C.c_int32, dp,
                                            C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+        L.ora_eq_eval.argtypes = [C.POINTER(OraProblem), dp, dp, dp]
+        L.ora_schur_kkt_step.argtypes = [C.POINTER(OraProblem), C.c_double, dp, C.c_int, dp]
         _lib = L
     return _lib
 
@@ -130,6 +135,14 @@ def problem_struct(prob):
     ab = getattr(prob, "eucm_alpha_beta", (0.0, 0.0))
     s.eucm_alpha_beta[0] = float(ab[0])
     s.eucm_alpha_beta[1] = float(ab[1])
+    # TranslationNormConstraint terms: prob.eq_pose (indices), prob.eq_radius
+    ep = getattr(prob, "eq_pose", None)
+    k.eq_pose = np.ascontiguousarray(ep if ep is not None else [], dtype=np.int32)
+    k.eq_radius = np.ascontiguousarray(getattr(prob, "eq_radius", None) if ep is not None else [], dtype=np.float64)
+    assert k.eq_pose.shape == k.eq_radius.shape
+    s.n_eq = k.eq_pose.shape[0]
+    s.eq_pose = k.eq_pose.ctypes.data_as(C.POINTER(C.c_int32)) if s.n_eq else None
+    s.eq_radius = _d(k.eq_radius) if s.n_eq else None
     s._keep = k
     return s
 
@@ -279,3 +292,30 @@ def covariance_block(prob, row, col):
     if rc != 0:
         raise RuntimeError("oracle covariance failed with %d" % rc)
     return out[:nr.value * nc.value].reshape(nr.value, nc.value)
+
+
+def eq_eval(prob, poses=None):
+    """Residuals c_k = |t(T_k)| - r_k of the problem's TranslationNormConstraint
+    terms and their 1x6 Jacobians (left perturbation), at poses (default: the
+    problem's)."""
+    s = problem_struct(prob)
+    P = np.ascontiguousarray(prob.poses if poses is None else poses, dtype=np.float64)
+    c = np.zeros(s.n_eq)
+    J = np.zeros((s.n_eq, 6))
+    lib().ora_eq_eval(C.byref(s), _d(P), _d(c), _d(J))
+    return c, J
+
+
+def schur_kkt_step(prob, nu, lam, n_threads=1):
+    """One damped step with the equality constraints: [dx; dlam] (dx in the
+    layout of dense_system); raises on failure."""
+    L = lib()
+    s = problem_struct(prob)
+    n = L.ora_dense_system(C.byref(s), float(nu), None, None)
+    lam = np.ascontiguousarray(lam, dtype=np.float64)
+    assert lam.shape == (s.n_eq,)
+    delta = np.zeros(n + s.n_eq)
+    rc = L.ora_schur_kkt_step(C.byref(s), float(nu), _d(lam), int(n_threads), _d(delta))
+    if rc != 0:
+        raise RuntimeError("oracle KKT step failed with %d" % rc)
+    return delta
