@@ -26,6 +26,10 @@
 //   crates/sophus_opt/src/nlls/linear_system/eq_system.rs:149-258  G^T lambda, -c, update_lambdas
 //   crates/sophus_opt/src/example_problems/ba_scale_constraint.rs:57-100  TranslationNormConstraint
 //   crates/sophus_opt/src/nlls/optimizer.rs:527-535             no gradient test with constraints
+//   crates/sophus_opt/src/nlls/functor_library/costs/isometry3_prior.rs  Isometry3PriorCostTerm
+//   crates/sophus_lie/src/groups/rotation3.rs:389-410,778-800, affine_group_template.rs:362-370  SE(3) log
+//   crates/sophus_autodiff/src/dual/dual_scalar.rs:400-420      dual atan2
+//   crates/sophus_opt/src/nlls/cost/evaluated_term.rs:286-327   precision-weighted terms
 //   crates/sophus_solver/src/ldlt/block_sparse_ldlt.rs:99-190,479-747
 //   crates/sophus_solver/src/ldlt/dense_ldlt.rs:164-308
 //   crates/sophus_solver/src/ldlt/block_diag_ldlt.rs:80-160
@@ -98,12 +102,21 @@ template <int N> Dual<N> dcos(const Dual<N>& a) {
   for (int i = 0; i < N; ++i) r.d[i] = s * a.d[i];
   return r;
 }
+// atan2(y, x): d/dy = x / (x^2 + y^2), d/dx = -y / (x^2 + y^2)
+// (dual_scalar.rs:400-420).
+template <int N> Dual<N> datan2(const Dual<N>& y, const Dual<N>& x) {
+  Dual<N> r(std::atan2(y.v, x.v));
+  const double inv = 1.0 / (y.v * y.v + x.v * x.v);
+  for (int i = 0; i < N; ++i) r.d[i] = (x.v * y.d[i] - y.v * x.d[i]) * inv;
+  return r;
+}
 template <int N> double val(const Dual<N>& a) { return a.v; }
 
 inline double dsqrt(double a) { return std::sqrt(a); }
 inline double dsin(double a) { return std::sin(a); }
 inline double dcos(double a) { return std::cos(a); }
 inline double val(double a) { return a; }
+inline double datan2(double y, double x) { return std::atan2(y, x); }
 inline float dsqrt(float a) { return std::sqrt(a); }
 inline float val(float a) { return a; }
 
@@ -232,6 +245,61 @@ void se3_inverse(const S* a, S* out) {
     out[4 + i] = -(r[i * 3 + 0] * a[4] + r[i * 3 + 1] * a[5] + r[i * 3 + 2] * a[6]);
   for (int i = 0; i < 4; ++i) out[i] = q[i];
   disambiguate(out);
+}
+
+// Rotation3Impl::log (rotation3.rs:389-410): 2 atan(|v| / w) v / |v| with
+// the sign of w folded in, and its series 2 / w - (2/3) |v|^2 / w^3 when
+// |v|^2 <= EPS^2.
+template <class S>
+void so3_log(const S* q, S* w) {
+  const S* iv = q + 1;
+  S sq = iv[0] * iv[0] + iv[1] * iv[1] + iv[2] * iv[2];
+  S qw = q[0];
+  S f;
+  if (val(sq) <= kEps * kEps) {
+    S wsq = qw * qw;
+    f = S(2.0) / qw - S(2.0 / 3.0) * sq / (wsq * qw);
+  } else {
+    S n = dsqrt(sq);
+    S sign = val(qw) <= 0.0 ? S(-1.0) : S(1.0);
+    S at = sign * datan2(n, sign * qw);
+    f = S(2.0) * at / n;
+  }
+  for (int i = 0; i < 3; ++i) w[i] = iv[i] * f;
+}
+
+// Rotation3Impl::mat_v_inverse (rotation3.rs:778-800): I - W/2 + c W^2 with
+// c = (1 - (theta/2) cos(theta/2) / sin(theta/2)) / theta^2, and c = 1/12 when
+// theta^2 <= EPS.  m row-major.
+template <class S>
+void so3_mat_v_inverse(const S* w, S* m) {
+  S th_sq = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  const S zero(0.0);
+  const S hat[9] = {zero, -w[2], w[1], w[2], zero, -w[0], -w[1], w[0], zero};
+  S hat_sq[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      hat_sq[i * 3 + j] = hat[i * 3 + 0] * hat[0 * 3 + j] + hat[i * 3 + 1] * hat[1 * 3 + j] +
+                          hat[i * 3 + 2] * hat[2 * 3 + j];
+  S c;
+  if (val(th_sq) <= kEps) {
+    c = S(1.0 / 12.0);
+  } else {
+    S theta = dsqrt(th_sq);
+    S half = S(0.5) * theta;
+    c = (S(1.0) - (S(0.5) * theta * dcos(half)) / dsin(half)) / (theta * theta);
+  }
+  for (int i = 0; i < 9; ++i) m[i] = ((i % 4 == 0) ? S(1.0) : zero) - hat[i] * S(0.5) + hat_sq[i] * c;
+}
+
+// AffineGroupTemplateImpl::log (affine_group_template.rs:362-370): the
+// rotation's log, then V^-1 t; tangent (w, v).
+template <class S>
+void se3_log(const S* a, S* xi) {
+  so3_log<S>(a, xi);
+  S m[9];
+  so3_mat_v_inverse<S>(xi, m);
+  for (int i = 0; i < 3; ++i) xi[3 + i] = m[i * 3 + 0] * a[4] + m[i * 3 + 1] * a[5] + m[i * 3 + 2] * a[6];
 }
 
 // Residual g = z - pi(T_wc^-1 * p_w)
@@ -749,6 +817,79 @@ void parallel_for(int64_t n, int n_threads, F&& f) {  // f(begin, end, thread_id
   for (auto& x : th) x.join();
 }
 
+// Isometry3PriorCostTerm::eval (isometry3_prior.rs): g = log(T E^-1), J the
+// dual-number derivative of log(exp(x) T E^-1) at x = 0, then
+// EvaluatedCostTerm::make with the precision W (evaluated_term.rs:286-327):
+// lambda_res = W g, gradient J^T W g, Hessian J^T (W J), cost g^T W g.
+void prior_term(const double* pose, const double* mean, const double* W, double* g, double* J,
+                double* hpp, double* gp, double* cost) {
+  double einv[7], te[7];
+  se3_inverse<double>(mean, einv);
+  se3_mul<double>(pose, einv, te);
+  se3_log<double>(te, g);
+  using D = Dual<6>;
+  D x[6], e[7], td[7], ed[7], a[7], b[7], gd[6];
+  for (int i = 0; i < 6; ++i) x[i].d[i] = 1.0;
+  se3_exp<D>(x, e);
+  for (int i = 0; i < 7; ++i) { td[i] = D(pose[i]); ed[i] = D(einv[i]); }
+  se3_mul<D>(e, td, a);
+  se3_mul<D>(a, ed, b);
+  se3_log<D>(b, gd);
+  for (int r = 0; r < 6; ++r)
+    for (int c = 0; c < 6; ++c) J[r * 6 + c] = gd[r].d[c];
+  double lr[6], wj[36];
+  for (int r = 0; r < 6; ++r) {
+    double acc = 0.0;
+    for (int c = 0; c < 6; ++c) acc += W[r * 6 + c] * g[c];
+    lr[r] = acc;
+    for (int c = 0; c < 6; ++c) {
+      double s = 0.0;
+      for (int k = 0; k < 6; ++k) s += W[r * 6 + k] * J[k * 6 + c];
+      wj[r * 6 + c] = s;
+    }
+  }
+  for (int r = 0; r < 6; ++r) {
+    double acc = 0.0;
+    for (int k = 0; k < 6; ++k) acc += J[k * 6 + r] * lr[k];
+    gp[r] = acc;
+    for (int c = 0; c < 6; ++c) {
+      double s = 0.0;
+      for (int k = 0; k < 6; ++k) s += J[k * 6 + r] * wj[k * 6 + c];
+      hpp[r * 6 + c] = s;
+    }
+  }
+  double cst = 0.0;
+  for (int r = 0; r < 6; ++r) cst += g[r] * lr[r];
+  *cost = cst;
+}
+
+// The prior terms sorted by pose (stable), as CostFn::sort orders them; a term
+// whose pose index is out of range is left out (ora_optimize rejects it).
+std::vector<int> prior_order(const ora_problem* p) {
+  std::vector<int> ord;
+  for (int k = 0; k < p->n_prior; ++k)
+    if (p->prior_pose[k] >= 0 && p->prior_pose[k] < p->n_cam) ord.push_back(k);
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return p->prior_pose[a] < p->prior_pose[b]; });
+  return ord;
+}
+
+bool priors_valid(const ora_problem* p) {
+  for (int k = 0; k < p->n_prior; ++k)
+    if (p->prior_pose[k] < 0 || p->prior_pose[k] >= p->n_cam) return false;
+  return true;
+}
+
+double prior_total_cost(const ora_problem* p, const double* poses) {
+  double c = 0.0;
+  for (int k : prior_order(p)) {
+    double g[6], J[36], h[36], gp[6], cost;
+    prior_term(poses + 7 * p->prior_pose[k], p->prior_mean + 7 * k, p->prior_precision + 36 * k, g, J, h, gp,
+               &cost);
+    c += cost;
+  }
+  return c;
+}
+
 double total_cost(const ora_problem* p, const double* intr, const double* poses, const double* points,
                   int n_threads) {
   // calc_total_cost (cost_fn.rs:403-433): sequential sum in sorted-term order
@@ -762,7 +903,7 @@ double total_cost(const ora_problem* p, const double* intr, const double* poses,
                            intr, p->obs_uv + 2 * i, p->huber_delta, p->camera_model);
     part[t] = acc;
   });
-  double c = 0.0;
+  double c = p->n_prior > 0 ? prior_total_cost(p, poses) : 0.0;  // the cost functions in list order
   for (double v : part) c += v;
   return c;
 }
@@ -855,6 +996,31 @@ void build_system(const ora_problem* p, const Structure& s, const double* intr, 
       }
     }
   });
+  if (p->n_prior > 0) {
+    // the prior cost function comes first: its terms reduced per pose
+    // (EvaluatedCostTerm::reduce), nu I once per reduced term (cost_system.rs:229-236)
+    std::vector<int> ord = prior_order(p);
+    for (size_t k = 0; k < ord.size();) {
+      const int pose = p->prior_pose[ord[k]];
+      double h[36] = {0.0}, gsum[6] = {0.0};
+      size_t k2 = k;
+      for (; k2 < ord.size() && p->prior_pose[ord[k2]] == pose; ++k2) {
+        double g[6], J[36], hp[36], gp[6], cost;
+        prior_term(poses + 7 * pose, p->prior_mean + 7 * ord[k2], p->prior_precision + 36 * ord[k2], g, J, hp,
+                   gp, &cost);
+        for (int i = 0; i < 36; ++i) h[i] += hp[i];
+        for (int i = 0; i < 6; ++i) gsum[i] += gp[i];
+      }
+      const int fb = s.pose_block[pose];
+      if (fb >= 0) {
+        R* u = &sys->U[static_cast<size_t>(fb) * 36];
+        for (int i = 0; i < 36; ++i) u[i] += static_cast<R>(h[i]);
+        if (nu != 0.0) for (int i = 0; i < 6; ++i) u[i * 7] += static_cast<R>(nu);
+        for (int i = 0; i < 6; ++i) sys->bp[static_cast<size_t>(fb) * 6 + i] -= static_cast<R>(gsum[i]);
+      }
+      k = k2;
+    }
+  }
   for (int t = 0; t < nt; ++t) {
     if (Ut[t].empty()) continue;
     for (size_t i = 0; i < sys->U.size(); ++i) sys->U[i] += Ut[t][i];
@@ -878,13 +1044,6 @@ void build_system(const ora_problem* p, const Structure& s, const double* intr, 
   sys->max_grad = mg;
 }
 
-// SchurFactor::factorize + solve (schur_ldlt.rs:536-812) with the sequential
-// forward pass (schur_ldlt.rs:241-278).  delta = [dx_c; dx_f; dx_m], dx_c the
-// nc = 4 (pinhole) or 6 (EUCM) intrinsics when they are free (empty
-// otherwise).  In S the intrinsics come first (their family's partition
-// precedes the poses'), padded to one 6-row block with an identity so the
-// factor keeps 6x6 blocks; the pivot rule restarts at that block as at every
-// partition block.
 // Equality constraints TranslationNormConstraint (ba_scale_constraint.rs:44-100):
 // c(T) = |t(T)| - r.  Its Jacobian is taken, as the reference's dual numbers
 // take it, under the left perturbation exp(x) * T at x = 0.  The tangent is
@@ -941,6 +1100,13 @@ bool small_inverse(int m, std::vector<double> a, std::vector<double>* inv) {
   return true;
 }
 
+// SchurFactor::factorize + solve (schur_ldlt.rs:536-812) with the sequential
+// forward pass (schur_ldlt.rs:241-278).  delta = [dx_c; dx_f; dx_m], dx_c the
+// nc = 4 (pinhole) or 6 (EUCM) intrinsics when they are free (empty
+// otherwise).  In S the intrinsics come first (their family's partition
+// precedes the poses'), padded to one 6-row block with an identity so the
+// factor keeps 6x6 blocks; the pivot rule restarts at that block as at every
+// partition block.
 template <class R>
 int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
                 int n_threads, std::vector<double>* delta, std::vector<double>* s_out,
@@ -1469,6 +1635,7 @@ int ora_optimize_ex(const ora_problem* p, const ora_params* prm, int n_threads,
   std::vector<double> npose(poses.size()), npts(points.size());
   for (int k = 0; k < p->n_eq; ++k)
     if (p->eq_pose[k] < 0 || p->eq_pose[k] >= p->n_cam) return -11;
+  if (!priors_valid(p)) return -12;
   EqTerms eq;
   std::vector<double> lambda(p->n_eq, 0.0);  // EqSystem::new: zero multipliers
   double merit = total_cost(p, intr.data(), poses.data(), points.data(), n_threads);
@@ -1620,6 +1787,14 @@ int ora_covariance_block(const ora_problem* p, int32_t row_kind, int32_t row_ind
     }
   return 0;
 }
+
+void ora_eval_prior(const double pose[7], const double mean[7], const double precision[36], double r[6],
+                    double j_pose[36], double* cost) {
+  double h[36], gp[6];
+  prior_term(pose, mean, precision, r, j_pose, h, gp, cost);
+}
+
+void ora_se3_log(const double params[7], double out[6]) { se3_log<double>(params, out); }
 
 void ora_eq_eval(const ora_problem* p, const double* poses, double* c, double* jac) {
   EqTerms e;

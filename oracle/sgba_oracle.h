@@ -74,6 +74,14 @@ void ora_eval_term_dual(const double pose[7], const double point[3],
                         const double intr[4], const double uv[2],
                         double j_pose[12], double j_point[6]);
 
+/* One Isometry3PriorCostTerm: residual g = log(T E^-1) (tangent rotation
+ * first), J (6x6 row-major) its derivative under exp(x) * T at x = 0 by dual
+ * numbers, and cost g^T W g (isometry3_prior.rs; evaluated_term.rs:286-327). */
+void ora_eval_prior(const double pose[7], const double mean[7], const double precision[36],
+                    double r[6], double j_pose[36], double *cost);
+/* SE(3) log (affine_group_template.rs:362-370), tangent (rotation, translation). */
+void ora_se3_log(const double params[7], double out_tangent[6]);
+
 /* ---- linear algebra ----------------------------------------------------- */
 /* Block LDLT (6x6 blocks when bs=6) of a dense SPD/PSD matrix, solve A x = b.
  * Returns 0 on success, -1 on a non-finite pivot. */
@@ -104,6 +112,12 @@ typedef struct {
                                   0: unconstrained */
   const int32_t *eq_pose;      /* n_eq pose indices (each a Free pose) */
   const double *eq_radius;     /* n_eq target translation norms */
+  int32_t n_prior;             /* Isometry3PriorCostTerm terms (isometry3_prior.rs): a second
+                                  cost function, ahead of the reprojection one in the cost
+                                  list as in cam_calib.rs:318-325; 0: none */
+  const int32_t *prior_pose;   /* n_prior pose indices */
+  const double *prior_mean;    /* n_prior x 7 prior means E (qw qx qy qz tx ty tz) */
+  const double *prior_precision; /* n_prior x 36 precision matrices W, row-major */
 } ora_problem;
 
 enum {

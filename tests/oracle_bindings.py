@@ -58,6 +58,10 @@ class OraProblem(C.Structure):
         ("n_eq", C.c_int32),
         ("eq_pose", C.POINTER(C.c_int32)),
         ("eq_radius", C.POINTER(C.c_double)),
+        ("n_prior", C.c_int32),
+        ("prior_pose", C.POINTER(C.c_int32)),
+        ("prior_mean", C.POINTER(C.c_double)),
+        ("prior_precision", C.POINTER(C.c_double)),
     ]
 
 
@@ -92,6 +96,8 @@ def lib():
         L.ora_covariance_block.argtypes = [C.POINTER(OraProblem), C.c_int32, C.c_int32, C.c_int32, C.c_int32, dp,
                                            C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
         L.ora_eq_eval.argtypes = [C.POINTER(OraProblem), dp, dp, dp]
+        L.ora_eval_prior.argtypes = [dp, dp, dp, dp, dp, dp]
+        L.ora_se3_log.argtypes = [dp, dp]
         L.ora_schur_kkt_step.argtypes = [C.POINTER(OraProblem), C.c_double, dp, C.c_int, dp]
         _lib = L
     return _lib
@@ -143,6 +149,18 @@ def problem_struct(prob):
     s.n_eq = k.eq_pose.shape[0]
     s.eq_pose = k.eq_pose.ctypes.data_as(C.POINTER(C.c_int32)) if s.n_eq else None
     s.eq_radius = _d(k.eq_radius) if s.n_eq else None
+    # Isometry3PriorCostTerm terms: prob.prior_pose, prob.prior_mean (n x 7), prob.prior_precision (n x 6 x 6)
+    pp = getattr(prob, "prior_pose", None)
+    k.prior_pose = np.ascontiguousarray(pp if pp is not None else [], dtype=np.int32)
+    k.prior_mean = np.ascontiguousarray(prob.prior_mean if pp is not None else np.zeros((0, 7)), dtype=np.float64)
+    k.prior_precision = np.ascontiguousarray(prob.prior_precision if pp is not None else np.zeros((0, 6, 6)),
+                                             dtype=np.float64)
+    assert k.prior_mean.shape == (k.prior_pose.shape[0], 7)
+    assert k.prior_precision.shape == (k.prior_pose.shape[0], 6, 6)
+    s.n_prior = k.prior_pose.shape[0]
+    s.prior_pose = k.prior_pose.ctypes.data_as(C.POINTER(C.c_int32)) if s.n_prior else None
+    s.prior_mean = _d(k.prior_mean) if s.n_prior else None
+    s.prior_precision = _d(k.prior_precision) if s.n_prior else None
     s._keep = k
     return s
 
@@ -319,3 +337,20 @@ def schur_kkt_step(prob, nu, lam, n_threads=1):
     if rc != 0:
         raise RuntimeError("oracle KKT step failed with %d" % rc)
     return delta
+
+
+def eval_prior(pose, mean, precision):
+    """One Isometry3PriorCostTerm: residual (6), Jacobian (6x6), cost."""
+    r = np.zeros(6)
+    J = np.zeros((6, 6))
+    cost = C.c_double()
+    lib().ora_eval_prior(_d(np.ascontiguousarray(pose, dtype=np.float64)),
+                         _d(np.ascontiguousarray(mean, dtype=np.float64)),
+                         _d(np.ascontiguousarray(precision, dtype=np.float64)), _d(r), _d(J), C.byref(cost))
+    return r, J, cost.value
+
+
+def se3_log(params):
+    out = np.zeros(6)
+    lib().ora_se3_log(_d(np.ascontiguousarray(params, dtype=np.float64)), _d(out))
+    return out
