@@ -27,6 +27,7 @@
 //   crates/sophus_opt/src/example_problems/ba_scale_constraint.rs:57-100  TranslationNormConstraint
 //   crates/sophus_opt/src/nlls/optimizer.rs:527-535             no gradient test with constraints
 //   crates/sophus_opt/src/nlls/functor_library/costs/isometry3_prior.rs  Isometry3PriorCostTerm
+//   crates/sophus_opt/src/nlls/functor_library/costs/pose_graph3.rs      PoseGraph3CostTerm
 //   crates/sophus_lie/src/groups/rotation3.rs:389-410,778-800, affine_group_template.rs:362-370  SE(3) log
 //   crates/sophus_autodiff/src/dual/dual_scalar.rs:400-420      dual atan2
 //   crates/sophus_opt/src/nlls/cost/evaluated_term.rs:286-327   precision-weighted terms
@@ -890,6 +891,62 @@ double prior_total_cost(const ora_problem* p, const double* poses) {
   return c;
 }
 
+// PoseGraph3CostTerm::eval (pose_graph3.rs): g = log(T_m^-1 T_n M^-1) and
+// the Jacobians -/+ Isometry3::dx_log_a_exp_x_b_at_0(T_m^-1, T_n M^-1), taken
+// here by dual numbers through log(a exp(x) b) at x = 0; no precision, no
+// robust kernel: cost g^T g, gradients J^T g, blocks J_m^T J_m, J_n^T J_n, J_m^T J_n.
+void edge_term(const double* tm, const double* tn, const double* mn, double* g, double* Jm, double* Jn,
+               double* cost) {
+  double a[7], mninv[7], b[7], ab[7];
+  se3_inverse<double>(tm, a);
+  se3_inverse<double>(mn, mninv);
+  se3_mul<double>(tn, mninv, b);
+  se3_mul<double>(a, b, ab);
+  se3_log<double>(ab, g);
+  using D = Dual<6>;
+  D x[6], e[7], ad[7], bd[7], t1[7], t2[7], gd[6];
+  for (int i = 0; i < 6; ++i) x[i].d[i] = 1.0;
+  se3_exp<D>(x, e);
+  for (int i = 0; i < 7; ++i) { ad[i] = D(a[i]); bd[i] = D(b[i]); }
+  se3_mul<D>(ad, e, t1);
+  se3_mul<D>(t1, bd, t2);
+  se3_log<D>(t2, gd);
+  for (int r = 0; r < 6; ++r)
+    for (int c = 0; c < 6; ++c) { Jn[r * 6 + c] = gd[r].d[c]; Jm[r * 6 + c] = -gd[r].d[c]; }
+  double cst = 0.0;
+  for (int r = 0; r < 6; ++r) cst += g[r] * g[r];
+  *cost = cst;
+}
+
+// The edge terms sorted by (m, n) (stable), as CostFn::sort orders them;
+// terms with an out-of-range or repeated pose are left out (ora_optimize
+// rejects them).
+std::vector<int> edge_order(const ora_problem* p) {
+  std::vector<int> ord;
+  for (int k = 0; k < p->n_edge; ++k) {
+    const int m = p->edge_pose[2 * k], n = p->edge_pose[2 * k + 1];
+    if (m >= 0 && m < p->n_cam && n >= 0 && n < p->n_cam && m != n) ord.push_back(k);
+  }
+  std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+    if (p->edge_pose[2 * a] != p->edge_pose[2 * b]) return p->edge_pose[2 * a] < p->edge_pose[2 * b];
+    return p->edge_pose[2 * a + 1] < p->edge_pose[2 * b + 1];
+  });
+  return ord;
+}
+
+bool edges_valid(const ora_problem* p) { return static_cast<int>(edge_order(p).size()) == std::max(0, p->n_edge); }
+
+double edge_total_cost(const ora_problem* p, const double* poses) {
+  double c = 0.0;
+  for (int k : edge_order(p)) {
+    double g[6], Jm[36], Jn[36], cost;
+    edge_term(poses + 7 * p->edge_pose[2 * k], poses + 7 * p->edge_pose[2 * k + 1], p->edge_mn + 7 * k, g, Jm, Jn,
+              &cost);
+    c += cost;
+  }
+  return c;
+}
+
 double total_cost(const ora_problem* p, const double* intr, const double* poses, const double* points,
                   int n_threads) {
   // calc_total_cost (cost_fn.rs:403-433): sequential sum in sorted-term order
@@ -903,7 +960,9 @@ double total_cost(const ora_problem* p, const double* intr, const double* poses,
                            intr, p->obs_uv + 2 * i, p->huber_delta, p->camera_model);
     part[t] = acc;
   });
-  double c = p->n_prior > 0 ? prior_total_cost(p, poses) : 0.0;  // the cost functions in list order
+  // the cost functions in list order: priors, pose-graph edges, reprojection
+  double c = p->n_prior > 0 ? prior_total_cost(p, poses) : 0.0;
+  if (p->n_edge > 0) c += edge_total_cost(p, poses);
   for (double v : part) c += v;
   return c;
 }
@@ -919,6 +978,9 @@ struct System {
   // block and neg_grad, and the blocks coupling them to each free pose
   // (6 x nc) and marg point (3 x nc)
   std::vector<R> Ucc, bc, Hpc, Hmc;
+  // pose-pose blocks from the edge terms, lower triangle: block (row fi, col fj), fi > fj
+  std::vector<int> off_row, off_col;
+  std::vector<R> off_blk;  // 36 per block, row-major
   double max_grad = 0.0;
 };
 
@@ -1017,6 +1079,58 @@ void build_system(const ora_problem* p, const Structure& s, const double* intr, 
         for (int i = 0; i < 36; ++i) u[i] += static_cast<R>(h[i]);
         if (nu != 0.0) for (int i = 0; i < 6; ++i) u[i * 7] += static_cast<R>(nu);
         for (int i = 0; i < 6; ++i) sys->bp[static_cast<size_t>(fb) * 6 + i] -= static_cast<R>(gsum[i]);
+      }
+      k = k2;
+    }
+  }
+  if (p->n_edge > 0) {
+    // the pose-graph cost function: terms reduced per (m, n); nu I once per
+    // reduced term on each free argument (cost_system.rs:190-273)
+    std::vector<int> ord = edge_order(p);
+    for (size_t k = 0; k < ord.size();) {
+      const int m = p->edge_pose[2 * ord[k]], n = p->edge_pose[2 * ord[k] + 1];
+      double hmm[36] = {0.0}, hnn[36] = {0.0}, hmn[36] = {0.0}, gm[6] = {0.0}, gn[6] = {0.0};
+      size_t k2 = k;
+      for (; k2 < ord.size() && p->edge_pose[2 * ord[k2]] == m && p->edge_pose[2 * ord[k2] + 1] == n; ++k2) {
+        double g[6], Jm[36], Jn[36], cost;
+        edge_term(poses + 7 * m, poses + 7 * n, p->edge_mn + 7 * ord[k2], g, Jm, Jn, &cost);
+        for (int r = 0; r < 6; ++r) {
+          for (int c = 0; c < 6; ++c) {
+            double sm = 0.0, sn = 0.0, so = 0.0;
+            for (int q = 0; q < 6; ++q) {
+              sm += Jm[q * 6 + r] * Jm[q * 6 + c];
+              sn += Jn[q * 6 + r] * Jn[q * 6 + c];
+              so += Jm[q * 6 + r] * Jn[q * 6 + c];
+            }
+            hmm[r * 6 + c] += sm;
+            hnn[r * 6 + c] += sn;
+            hmn[r * 6 + c] += so;
+          }
+          double am = 0.0, an = 0.0;
+          for (int q = 0; q < 6; ++q) { am += Jm[q * 6 + r] * g[q]; an += Jn[q * 6 + r] * g[q]; }
+          gm[r] += am;
+          gn[r] += an;
+        }
+      }
+      const int fm = s.pose_block[m], fn = s.pose_block[n];
+      const int fbs[2] = {fm, fn};
+      const double* hs[2] = {hmm, hnn};
+      const double* gs[2] = {gm, gn};
+      for (int a = 0; a < 2; ++a) {
+        if (fbs[a] < 0) continue;
+        R* u = &sys->U[static_cast<size_t>(fbs[a]) * 36];
+        for (int i = 0; i < 36; ++i) u[i] += static_cast<R>(hs[a][i]);
+        if (nu != 0.0) for (int i = 0; i < 6; ++i) u[i * 7] += static_cast<R>(nu);
+        for (int i = 0; i < 6; ++i) sys->bp[static_cast<size_t>(fbs[a]) * 6 + i] -= static_cast<R>(gs[a][i]);
+      }
+      if (fm >= 0 && fn >= 0) {
+        // lower-triangle block: rows of the later free block
+        const bool m_lower = fm > fn;
+        sys->off_row.push_back(m_lower ? fm : fn);
+        sys->off_col.push_back(m_lower ? fn : fm);
+        for (int r = 0; r < 6; ++r)
+          for (int c = 0; c < 6; ++c)
+            sys->off_blk.push_back(static_cast<R>(m_lower ? hmn[r * 6 + c] : hmn[c * 6 + r]));
       }
       k = k2;
     }
@@ -1213,6 +1327,11 @@ int schur_solve(const ora_problem* p, const Structure& s, const System<R>& sys,
         for (int c = 0; c < 6; ++c)
           Sacc[static_cast<size_t>(nci + i * 6 + r) * n + nci + i * 6 + c] = sys.U[static_cast<size_t>(i) * 36 + r * 6 + c];
     for (int i = 0; i < n6; ++i) racc[nci + i] = sys.bp[i];
+    for (size_t e = 0; e < sys.off_row.size(); ++e)
+      for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c)
+          Sacc[static_cast<size_t>(nci + sys.off_row[e] * 6 + r) * n + nci + sys.off_col[e] * 6 + c] +=
+              sys.off_blk[e * 36 + r * 6 + c];
     if (eq && lambda) {
       // the constraint rows add G^T lambda to the free gradient when the KKT
       // system is populated (eq_system.rs, populate_lower_triangular_kkt_mat)
@@ -1563,6 +1682,13 @@ int64_t ora_dense_system(const ora_problem* p, double nu, double* h, double* neg
       for (int c = 0; c < 3; ++c) h[(off + m * 3 + r) * n + off + m * 3 + c] = sys.V[m * 9 + r * 3 + c];
       neg_grad[off + m * 3 + r] = sys.bm[m * 3 + r];
     }
+  for (size_t e = 0; e < sys.off_row.size(); ++e)
+    for (int r = 0; r < 6; ++r)
+      for (int c = 0; c < 6; ++c) {
+        const double v = sys.off_blk[e * 36 + r * 6 + c];
+        h[(c0 + sys.off_row[e] * 6 + r) * n + c0 + sys.off_col[e] * 6 + c] += v;
+        h[(c0 + sys.off_col[e] * 6 + c) * n + c0 + sys.off_row[e] * 6 + r] += v;
+      }
   for (size_t r = 0; r + 1 < s.range_begin.size(); ++r) {
     int fb = s.pose_block[s.rng_pose[r]], mb = s.point_block[s.rng_pt[r]];
     if (fb < 0 || mb < 0) continue;
@@ -1636,6 +1762,7 @@ int ora_optimize_ex(const ora_problem* p, const ora_params* prm, int n_threads,
   for (int k = 0; k < p->n_eq; ++k)
     if (p->eq_pose[k] < 0 || p->eq_pose[k] >= p->n_cam) return -11;
   if (!priors_valid(p)) return -12;
+  if (!edges_valid(p)) return -13;
   EqTerms eq;
   std::vector<double> lambda(p->n_eq, 0.0);  // EqSystem::new: zero multipliers
   double merit = total_cost(p, intr.data(), poses.data(), points.data(), n_threads);
@@ -1795,6 +1922,11 @@ void ora_eval_prior(const double pose[7], const double mean[7], const double pre
 }
 
 void ora_se3_log(const double params[7], double out[6]) { se3_log<double>(params, out); }
+
+void ora_eval_edge(const double pose_m[7], const double pose_n[7], const double m_from_n[7], double r[6],
+                   double j_m[36], double j_n[36], double* cost) {
+  edge_term(pose_m, pose_n, m_from_n, r, j_m, j_n, cost);
+}
 
 void ora_eq_eval(const ora_problem* p, const double* poses, double* c, double* jac) {
   EqTerms e;

@@ -79,6 +79,11 @@ void ora_eval_term_dual(const double pose[7], const double point[3],
  * numbers, and cost g^T W g (isometry3_prior.rs; evaluated_term.rs:286-327). */
 void ora_eval_prior(const double pose[7], const double mean[7], const double precision[36],
                     double r[6], double j_pose[36], double *cost);
+/* One PoseGraph3CostTerm: g = log(T_m^-1 T_n M^-1), J_n the derivative of
+ * log(a exp(x) b) at x = 0 with a = T_m^-1, b = T_n M^-1 (by dual numbers), J_m
+ * = -J_n (6x6 row-major each), cost g^T g (pose_graph3.rs). */
+void ora_eval_edge(const double pose_m[7], const double pose_n[7], const double m_from_n[7],
+                   double r[6], double j_m[36], double j_n[36], double *cost);
 /* SE(3) log (affine_group_template.rs:362-370), tangent (rotation, translation). */
 void ora_se3_log(const double params[7], double out_tangent[6]);
 
@@ -118,6 +123,10 @@ typedef struct {
   const int32_t *prior_pose;   /* n_prior pose indices */
   const double *prior_mean;    /* n_prior x 7 prior means E (qw qx qy qz tx ty tz) */
   const double *prior_precision; /* n_prior x 36 precision matrices W, row-major */
+  int32_t n_edge;              /* PoseGraph3CostTerm terms (pose_graph3.rs): a cost function
+                                  between the priors and the reprojection one; 0: none */
+  const int32_t *edge_pose;    /* n_edge x 2 pose indices (m, n), m != n */
+  const double *edge_mn;       /* n_edge x 7 measured pose_m_from_pose_n */
 } ora_problem;
 
 enum {

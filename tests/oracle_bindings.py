@@ -62,6 +62,9 @@ class OraProblem(C.Structure):
         ("prior_pose", C.POINTER(C.c_int32)),
         ("prior_mean", C.POINTER(C.c_double)),
         ("prior_precision", C.POINTER(C.c_double)),
+        ("n_edge", C.c_int32),
+        ("edge_pose", C.POINTER(C.c_int32)),
+        ("edge_mn", C.POINTER(C.c_double)),
     ]
 
 
@@ -98,6 +101,7 @@ def lib():
         L.ora_eq_eval.argtypes = [C.POINTER(OraProblem), dp, dp, dp]
         L.ora_eval_prior.argtypes = [dp, dp, dp, dp, dp, dp]
         L.ora_se3_log.argtypes = [dp, dp]
+        L.ora_eval_edge.argtypes = [dp, dp, dp, dp, dp, dp, dp]
         L.ora_schur_kkt_step.argtypes = [C.POINTER(OraProblem), C.c_double, dp, C.c_int, dp]
         _lib = L
     return _lib
@@ -161,6 +165,14 @@ def problem_struct(prob):
     s.prior_pose = k.prior_pose.ctypes.data_as(C.POINTER(C.c_int32)) if s.n_prior else None
     s.prior_mean = _d(k.prior_mean) if s.n_prior else None
     s.prior_precision = _d(k.prior_precision) if s.n_prior else None
+    # PoseGraph3CostTerm terms: prob.edge_pose (n x 2), prob.edge_mn (n x 7)
+    ee = getattr(prob, "edge_pose", None)
+    k.edge_pose = np.ascontiguousarray(ee if ee is not None else np.zeros((0, 2)), dtype=np.int32)
+    k.edge_mn = np.ascontiguousarray(prob.edge_mn if ee is not None else np.zeros((0, 7)), dtype=np.float64)
+    assert k.edge_pose.shape == (k.edge_pose.shape[0], 2) and k.edge_mn.shape == (k.edge_pose.shape[0], 7)
+    s.n_edge = k.edge_pose.shape[0]
+    s.edge_pose = k.edge_pose.ctypes.data_as(C.POINTER(C.c_int32)) if s.n_edge else None
+    s.edge_mn = _d(k.edge_mn) if s.n_edge else None
     s._keep = k
     return s
 
@@ -354,3 +366,14 @@ def se3_log(params):
     out = np.zeros(6)
     lib().ora_se3_log(_d(np.ascontiguousarray(params, dtype=np.float64)), _d(out))
     return out
+
+
+def eval_edge(pose_m, pose_n, m_from_n):
+    """One PoseGraph3CostTerm: residual (6), J_m, J_n (6x6 each), cost."""
+    r = np.zeros(6)
+    Jm = np.zeros((6, 6))
+    Jn = np.zeros((6, 6))
+    cost = C.c_double()
+    f = lambda a: _d(np.ascontiguousarray(a, dtype=np.float64))  # noqa: E731
+    lib().ora_eval_edge(f(pose_m), f(pose_n), f(m_from_n), _d(r), _d(Jm), _d(Jn), C.byref(cost))
+    return r, Jm, Jn, cost.value
