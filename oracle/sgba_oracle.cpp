@@ -1520,9 +1520,61 @@ int schur_step_impl(const ora_problem* p, const Structure& s, const double* intr
 struct CovCtx {
   Structure s;
   System<double> sys;
-  int n = 0, nci = 0, nc = 0;
-  std::vector<double> Sinv;  // n x n
+  int n = 0, nci = 0, nc = 0, rank = 0;
+  std::vector<double> Sinv;  // n x n: S^-1, or the min-norm pseudo-inverse S+ when S is rank-deficient
 };
+
+// MinNormLdlt::pseudo_inverse (min_norm_ldlt.rs:55-140) with the block-sparse
+// backend's columns (block_sparse_min_norm_ldlt.rs:98-160): with A = L D L^T,
+// L the block factor times the unit-lower factors of the diagonal blocks, E the
+// columns of L at the positive pivots J and G = E^T E,
+//   A+ = E G^-1 diag(d_J)^-1 G^-1 E^T.
+// out: n x n row-major.  Returns 0, or -2 when G cannot be factored.
+int pseudo_inverse(const BlockLdlt& f, std::vector<double>* out) {
+  const int n = f.n, bs = f.bs, nb = f.nb;
+  std::vector<int> J;
+  for (int j = 0; j < n; ++j)
+    if (f.d[j] > 0.0) J.push_back(j);
+  const int r = static_cast<int>(J.size());
+  out->assign(static_cast<size_t>(n) * n, 0.0);
+  if (r == 0) return 0;
+  std::vector<double> E(static_cast<size_t>(n) * r, 0.0);  // n x r row-major
+  for (int c = 0; c < r; ++c) {
+    const int bj = J[c] / bs, co = J[c] % bs;
+    const double* ljj = &f.ldiag[static_cast<size_t>(bj) * bs * bs];
+    for (int q = 0; q < bs; ++q) E[static_cast<size_t>(bj * bs + q) * r + c] = ljj[q * bs + co];
+    for (int bi = bj + 1; bi < nb; ++bi) {
+      const double* lij = &f.lblk[((static_cast<size_t>(bi) * nb + bj) * bs) * bs];
+      for (int q = 0; q < bs; ++q) {
+        double acc = 0.0;
+        for (int t = 0; t < bs; ++t) acc += lij[q * bs + t] * ljj[t * bs + co];
+        E[static_cast<size_t>(bi * bs + q) * r + c] = acc;
+      }
+    }
+  }
+  std::vector<double> G(static_cast<size_t>(r) * r), gd(r);
+  for (int a = 0; a < r; ++a)
+    for (int b = 0; b < r; ++b) {
+      double acc = 0.0;
+      for (int i = 0; i < n; ++i) acc += E[static_cast<size_t>(i) * r + a] * E[static_cast<size_t>(i) * r + b];
+      G[static_cast<size_t>(a) * r + b] = acc;
+    }
+  if (ldlt_decompose_inplace(r, G.data(), gd.data(), kLdltTolRel) != 0) return -2;
+  for (int a = 0; a < r; ++a)
+    if (!(gd[a] > 0.0)) return -2;  // G is positive definite on the positive-pivot subspace
+  std::vector<double> W(E);  // W = E G^-1 diag(d_J)^-1 G^-1
+  ldlt_right_matsolve(r, G.data(), gd.data(), n, W.data());
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < r; ++c) W[static_cast<size_t>(i) * r + c] /= f.d[J[c]];
+  ldlt_right_matsolve(r, G.data(), gd.data(), n, W.data());
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double acc = 0.0;
+      for (int c = 0; c < r; ++c) acc += W[static_cast<size_t>(i) * r + c] * E[static_cast<size_t>(j) * r + c];
+      (*out)[static_cast<size_t>(i) * n + j] = acc;
+    }
+  return 0;
+}
 
 int cov_build(const ora_problem* p, CovCtx* c) {
   build_structure(p, &c->s);
@@ -1537,6 +1589,12 @@ int cov_build(const ora_problem* p, CovCtx* c) {
   const int n = c->n;
   BlockLdlt f;
   if (f.factorize(n, 6, S.data()) != 0) return -2;
+  int rank = 0;
+  for (int j = 0; j < n; ++j) rank += f.d[j] > 0.0 ? 1 : 0;
+  c->rank = rank;
+  // a gauge-deficient S: the min-norm pseudo-inverse (SchurFactor::ensure_s_inv,
+  // schur_ldlt.rs:847-866); full rank: S^-1 by solves (try_inverse)
+  if (rank < n) return pseudo_inverse(f, &c->Sinv);
   c->Sinv.assign(static_cast<size_t>(n) * n, 0.0);
   std::vector<double> e(n);
   for (int j = 0; j < n; ++j) {
@@ -1926,6 +1984,18 @@ void ora_se3_log(const double params[7], double out[6]) { se3_log<double>(params
 void ora_eval_edge(const double pose_m[7], const double pose_n[7], const double m_from_n[7], double r[6],
                    double j_m[36], double j_n[36], double* cost) {
   edge_term(pose_m, pose_n, m_from_n, r, j_m, j_n, cost);
+}
+
+int ora_min_norm_pinv(int n, int bs, const double* a, double* out) {
+  if (n <= 0 || bs <= 0 || n % bs != 0) return -1;
+  BlockLdlt f;
+  if (f.factorize(n, bs, a) != 0) return -2;
+  std::vector<double> pinv;
+  int rank = 0;
+  for (int j = 0; j < n; ++j) rank += f.d[j] > 0.0 ? 1 : 0;
+  if (pseudo_inverse(f, &pinv) != 0) return -2;
+  std::memcpy(out, pinv.data(), sizeof(double) * pinv.size());
+  return rank;
 }
 
 void ora_eq_eval(const ora_problem* p, const double* poses, double* c, double* jac) {

@@ -93,6 +93,11 @@ void ora_se3_log(const double params[7], double out_tangent[6]);
 int ora_block_ldlt_solve(int n, int bs, const double *a_rowmajor,
                          const double *b, double *x);
 
+/* Min-norm pseudo-inverse of a dense symmetric PSD matrix through its block
+ * LDL^T (bs x bs blocks): E G^-1 diag(d_J)^-1 G^-1 E^T as above.  Returns the
+ * rank (the positive pivots), or a negative error. */
+int ora_min_norm_pinv(int n, int bs, const double *a_rowmajor, double *out);
+
 /* ---- whole problem ------------------------------------------------------ */
 typedef struct {
   int32_t n_cam;
@@ -194,10 +199,11 @@ void ora_eval_term_ex(const double pose[7], const double point[3],
  * Kinds: ORA_VAR_INTRINSICS (index ignored; only when they are free),
  * ORA_VAR_POSE (pose index), ORA_VAR_POINT (point index).  out receives the
  * rows x cols block row-major (4 or 6 intrinsics, 6 per pose, 3 per point).
+ * When S is rank-deficient (a free gauge: no pose held), S^-1 above is the
+ * min-norm pseudo-inverse E G^-1 diag(d_J)^-1 G^-1 E^T of its LDL^T factor
+ * (min_norm_ldlt.rs:55-140, block_sparse_min_norm_ldlt.rs:98-160).
  * Returns 0; -1 for a variable without a block (constant or Conditioned, where
- * the reference returns None); -2 when S cannot be factored.  Full-rank H
- * only: the reference's min-norm pseudo-inverse for a gauge-deficient S is
- * not restated. */
+ * the reference returns None); -2 when S cannot be factored. */
 enum {
   ORA_VAR_INTRINSICS = 0,
   ORA_VAR_POSE = 1,

@@ -102,6 +102,7 @@ def lib():
         L.ora_eval_prior.argtypes = [dp, dp, dp, dp, dp, dp]
         L.ora_se3_log.argtypes = [dp, dp]
         L.ora_eval_edge.argtypes = [dp, dp, dp, dp, dp, dp, dp]
+        L.ora_min_norm_pinv.argtypes = [C.c_int, C.c_int, dp, dp]
         L.ora_schur_kkt_step.argtypes = [C.POINTER(OraProblem), C.c_double, dp, C.c_int, dp]
         _lib = L
     return _lib
@@ -377,3 +378,13 @@ def eval_edge(pose_m, pose_n, m_from_n):
     f = lambda a: _d(np.ascontiguousarray(a, dtype=np.float64))  # noqa: E731
     lib().ora_eval_edge(f(pose_m), f(pose_n), f(m_from_n), _d(r), _d(Jm), _d(Jn), C.byref(cost))
     return r, Jm, Jn, cost.value
+
+
+def min_norm_pinv(A, bs=6):
+    """(pseudo-inverse, rank) of a symmetric PSD matrix by the min-norm LDL^T."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    out = np.zeros_like(A)
+    r = lib().ora_min_norm_pinv(A.shape[0], int(bs), _d(A), _d(out))
+    if r < 0:
+        raise RuntimeError("oracle pseudo-inverse failed with %d" % r)
+    return out, r

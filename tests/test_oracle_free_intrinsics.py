@@ -230,3 +230,42 @@ def test_covariance_blocks_vs_dense_inverse(pkg, oracle):
         assert oracle.covariance_block(prob, (1, 0), (1, 0)) is None
         if not c0:
             assert oracle.covariance_block(prob, (0, 0), (0, 0)) is None
+
+
+# ---- min-norm pseudo-inverse for a rank-deficient S (min_norm_ldlt.rs:55-140) ----
+
+
+def test_min_norm_pseudo_inverse_vs_svd(oracle):
+    """E G^-1 diag(d_J)^-1 G^-1 E^T of the block LDL^T against the SVD
+    pseudo-inverse. The factor zeroes a pivot below 1e-12 x max(1, the running
+    largest pivot of its block); matrices of norm ~1e-2 keep their roundoff
+    pivots (~1e-18) far below that floor and their true pivots far above it."""
+    rng = np.random.default_rng(0)
+    for n, r in ((24, 24), (24, 19), (24, 13), (36, 30)):
+        B = rng.standard_normal((n, r))
+        A = 1e-2 * (B @ B.T) / r
+        P, rank = oracle.min_norm_pinv(A)
+        assert rank == r
+        ref = np.linalg.pinv(A, rcond=1e-10, hermitian=True)
+        np.testing.assert_allclose(P, ref, rtol=0, atol=1e-9 * np.abs(ref).max())
+
+
+def test_covariance_with_an_unobserved_free_pose(pkg, oracle):
+    """A free pose with no observations leaves six exact zero pivots in S: the
+    free x free blocks are those of the pseudo-inverse, zero for that pose."""
+    prob = pkg.synth.generate(pkg.synth.CIRCLE, n_cam=6, n_pt=60, seed=3)
+    keep = prob.obs_cam != 2
+    prob.obs_cam, prob.obs_pt, prob.obs_uv = prob.obs_cam[keep], prob.obs_pt[keep], prob.obs_uv[keep]
+    prob.pose_const = np.zeros(6, np.uint8)
+    prob.pose_const[0] = 1
+    H, _ = oracle.dense_system(prob, 0.0)
+    nf = 30
+    S_dense = H[:nf, :nf] - H[:nf, nf:] @ np.linalg.solve(H[nf:, nf:], H[:nf, nf:].T)
+    assert np.all(S_dense[6:12] == 0.0)  # pose 2 is free block 1 (pose 0 is constant)
+    ref = np.linalg.pinv(S_dense, rcond=1e-12, hermitian=True)
+    for a in range(1, 6):
+        for b in range(1, 6):
+            blk = oracle.covariance_block(prob, (1, a), (1, b))
+            np.testing.assert_allclose(blk, ref[6 * (a - 1):6 * a, 6 * (b - 1):6 * b], rtol=0,
+                                       atol=1e-7 * np.abs(ref).max())
+    assert np.all(oracle.covariance_block(prob, (1, 2), (1, 2)) == 0.0)
