@@ -62,7 +62,9 @@ typedef struct {
   const int32_t *obs_cam;     /* pose index per observation (entity_indices[1]) */
   const int32_t *obs_pt;      /* point index per observation (entity_indices[2]) */
   const double *obs_uv;       /* n_obs*2 pixel measurements (uv_in_image) */
-  double huber_delta;         /* > 0: RobustKernel::Huber(delta); <= 0: no kernel */
+  double huber_delta;         /* > 0: RobustKernel::Huber(delta); <= 0: no kernel.  A positive
+                               * delta must be a normal float (1.2e-38 .. 3.4e38): the kernels
+                               * compare residual norms with it in float */
 } sgba_problem_desc;
 
 /* OptParams fields used on this path (crates/sophus_opt/src/nlls/optimizer_types.rs:161-240).
@@ -192,6 +194,19 @@ int sgba_export_pattern(sgba_problem *p, int32_t *h_rows, int32_t *h_cols, int32
  * NULL skips an output.  Used to compare each LM step with an FP64 LDLT. */
 int sgba_debug_last_system(sgba_problem *p, double *s_dense, double *rhs, double *delta);
 
+/* Per-term Jacobians at the current variables, evaluated by the same device
+ * code as the linearization: J_pose (2x6 row-major per term, left perturbation
+ * exp(delta) * world_from_camera, delta = [omega; nu]) and J_point (2x3) of the
+ * residual uv - proj(camera_from_world * point) of
+ * PinholeCameraReprojectionCostTerm::eval
+ * (crates/sophus_opt/src/nlls/functor_library/costs/pinhole_reprojection.rs:60-95),
+ * which the reference evaluates with DualScalar forward mode.  One term per
+ * (cam[i], pt[i]); precision 0 = FP32 (the linearization of well-conditioned
+ * problems), 1 = float-float (loop-shaped problems and point blocks rebuilt in
+ * float-float).  j_pose: n*12 doubles, j_point: n*6.  Synchronous. */
+int sgba_debug_jacobians(sgba_problem *p, int64_t n, const int32_t *cam, const int32_t *pt, int32_t precision,
+                         double *j_pose, double *j_point);
+
 /* Opaque optimizer state (variables, damping, reject count, step count) for
  * resume: *size receives the byte size when buf is NULL. */
 int sgba_state_save(sgba_problem *p, void *buf, size_t *size);
@@ -247,7 +262,11 @@ int sgba_bench_kernel(sgba_problem *p, int32_t kernel, int32_t reps, int32_t flu
  * poses (7 doubles per camera, world-from-camera as in sgba_problem_desc),
  * points (3 per point), obs_cam, obs_pt, obs_uv (2 per observation) and cost
  * (1 double, written) are device pointers on the current device; intrinsics
- * (fx, fy, cx, cy) is a host array; huber_delta <= 0 means no robust kernel.
+ * (fx, fy, cx, cy) is a host array; huber_delta <= 0 means no robust kernel
+ * (a positive delta must be a normal float, as in sgba_problem_desc).  The
+ * device arrays must be aligned to their element: obs_uv to 16 bytes (its
+ * (u, v) pairs are loaded together), the double arrays to 8 and the index
+ * arrays to 4; a misaligned pointer is rejected with SGBA_ERR_INVALID_ARGUMENT.
  * The call is asynchronous on `stream` (a cudaStream_t; NULL is the legacy
  * default stream).  Nothing needs to be zeroed by the caller.  An observation
  * index out of range makes *cost NaN.

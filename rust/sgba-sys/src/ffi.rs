@@ -184,6 +184,15 @@ extern "C" {
         s_cols: *mut i32,
     ) -> c_int;
     pub fn sgba_debug_last_system(p: *mut sgba_problem, s_dense: *mut f64, rhs: *mut f64, delta: *mut f64) -> c_int;
+    pub fn sgba_debug_jacobians(
+        p: *mut sgba_problem,
+        n: i64,
+        cam: *const i32,
+        pt: *const i32,
+        precision: i32,
+        j_pose: *mut f64,
+        j_point: *mut f64,
+    ) -> c_int;
     pub fn sgba_state_save(p: *mut sgba_problem, buf: *mut c_void, size: *mut usize) -> c_int;
     pub fn sgba_state_load(p: *mut sgba_problem, buf: *const c_void, size: usize) -> c_int;
     pub fn sgba_get_profile(p: *mut sgba_problem, out: *mut sgba_profile) -> c_int;

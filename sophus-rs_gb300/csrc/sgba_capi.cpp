@@ -79,6 +79,29 @@ int set_error(int status, const char* fmt, ...) {
     }                                                                                           \
   } while (0)
 
+// The kernels compare residual norms with the Huber threshold in float: a
+// positive threshold must be a normal float (a smaller one would round to 0
+// and silently drop the robust kernel).
+bool huber_in_float_range(double h) { return !(h > 0.0) || (h >= 1.17549435e-38 && h <= 3.40282347e38); }
+
+// CUDA events owned by one call: destroyed when the call returns, on every path.
+struct EventSet {
+  std::vector<cudaEvent_t> ev;
+  EventSet() = default;
+  EventSet(const EventSet&) = delete;
+  EventSet& operator=(const EventSet&) = delete;
+  ~EventSet() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
+  cudaError_t create(cudaEvent_t* out) {
+    cudaEvent_t e = nullptr;
+    const cudaError_t r = cudaEventCreate(&e);
+    if (r == cudaSuccess) ev.push_back(e);
+    *out = e;
+    return r;
+  }
+};
+
 constexpr int kTile = 256;           // terms per camera tile (one CTA)
 constexpr int64_t kSchurChunk = 256;  // observation pairs per warp in the Schur assembly
 constexpr int32_t kMaxDenseFree = 4096;  // reduced-camera-system limit (6 * 4096 rows, stored dense in f64)
@@ -354,6 +377,10 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
   if (!finite_all(d->poses, 7ll * d->n_cam) || !finite_all(d->points, 3ll * d->n_pt) || !finite_uv ||
       !finite_all(d->intrinsics, 4))
     return set_error(SGBA_ERR_INVALID_ARGUMENT, "non-finite input value");
+  if (std::isnan(d->huber_delta) || !huber_in_float_range(d->huber_delta))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT,
+                     "huber_delta %g: a positive threshold must lie in the normal float range [1.2e-38, 3.4e38]",
+                     d->huber_delta);
   for (int j = 0; j < d->n_cam; ++j)
     if (!quat_valid(d->poses + 7 * j))
       return set_error(SGBA_ERR_INVALID_PARAMS, "pose %d: quaternion norm differs from 1 by more than 1e-6", j);
@@ -828,9 +855,12 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if (s.lin_dd) {
     if ((st = dev_alloc(p, &d.res_lo, P.no))) return st;
     if ((st = dev_alloc(p, &d.res_lo_t, P.no))) return st;
-    if ((st = dev_alloc(p, &d.zdd, static_cast<size_t>(sgba::kZddFloats) * static_cast<size_t>(std::max<int64_t>(P.ng, 1)))))
-      return st;
   }
+  // float-float Z: every term under the float-float linearization; otherwise
+  // the terms of the points whose blocks are rebuilt in float-float (flagged
+  // in zmat's padding)
+  if ((st = dev_alloc(p, &d.zdd, static_cast<size_t>(sgba::kZddFloats) * static_cast<size_t>(std::max<int64_t>(P.ng, 1)))))
+    return st;
   if (s.dense_c == 0 && s.band_c == 0) {
     // multi-launch dense solver
     if ((st = dev_alloc(p, &d.A, n6 * n6))) return st;
@@ -1027,12 +1057,13 @@ int sgba_optimizer_step(sgba_problem* p, sgba_iter_record* rec) {
 int sgba_optimize(sgba_problem* p, const sgba_opt_params* prm, sgba_iter_record* records, int32_t cap,
                   int32_t* n_records, int32_t* termination) {
   if (!p || !prm) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  EventSet events;  // every event below is destroyed on every return path
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   SGBA_CK(cudaSetDevice(p->device));
-  SGBA_CK(cudaEventCreate(&e0));
-  SGBA_CK(cudaEventCreate(&e1));
+  SGBA_CK(events.create(&e0));
+  SGBA_CK(events.create(&e1));
   int st = sgba_optimizer_init(p, prm);
-  if (st) { cudaEventDestroy(e0); cudaEventDestroy(e1); return st; }
+  if (st) return st;
   SGBA_CK(cudaEventRecord(e0, p->stream));
   const int iters = std::max(1, prm->num_iterations);
   double ph[5] = {0, 0, 0, 0, 0};
@@ -1041,7 +1072,7 @@ int sgba_optimize(sgba_problem* p, const sgba_opt_params* prm, sgba_iter_record*
   } else {
     // Same kernels launched directly, with events between the phases.
     cudaEvent_t ev[6];
-    for (auto& x : ev) SGBA_CK(cudaEventCreate(&x));
+    for (auto& x : ev) SGBA_CK(events.create(&x));
     for (int it = 0; it < iters; ++it) {
       SGBA_CK(cudaEventRecord(ev[0], p->stream));
       sgba::launch_iteration_begin(p->sz, p->d, p->stream);
@@ -1062,7 +1093,6 @@ int sgba_optimize(sgba_problem* p, const sgba_opt_params* prm, sgba_iter_record*
         ph[k] += m;
       }
     }
-    for (auto& x : ev) cudaEventDestroy(x);
   }
   // build_solution (optimizer.rs:609-646): final linearisation with zero
   // damping (or the current damping when skip_final_hessian is set).
@@ -1072,12 +1102,10 @@ int sgba_optimize(sgba_problem* p, const sgba_opt_params* prm, sgba_iter_record*
   int final_launches = sgba::launch_linearize(p->sz, p->d, prm->skip_final_hessian ? c.nu : 0.0, true, p->stream);
   SGBA_CK(cudaEventRecord(e1, p->stream));
   st = check_launch();
-  if (st) { cudaEventDestroy(e0); cudaEventDestroy(e1); return st; }
+  if (st) return st;
   SGBA_CK(cudaStreamSynchronize(p->stream));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   const int nrec = std::min(c.step, p->d.record_cap);
   if (records && cap > 0) {
     std::vector<Record> h(nrec);
@@ -1201,6 +1229,42 @@ int sgba_debug_last_system(sgba_problem* p, double* s_dense, double* rhs, double
     if (p->plan.nm > 0)
       SGBA_CK(cudaMemcpy(delta + n6, p->d.dm, sizeof(double) * 3 * p->plan.nm, cudaMemcpyDeviceToHost));
   }
+  return SGBA_OK;
+}
+
+int sgba_debug_jacobians(sgba_problem* p, int64_t n, const int32_t* cam, const int32_t* pt, int32_t precision,
+                         double* j_pose, double* j_point) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  if (n < 0) return set_error(SGBA_ERR_INVALID_ARGUMENT, "negative term count");
+  if (n > 0 && (!cam || !pt || !j_pose || !j_point)) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (precision != 0 && precision != 1) return set_error(SGBA_ERR_INVALID_ARGUMENT, "precision must be 0 or 1");
+  for (int64_t i = 0; i < n; ++i) {
+    if (cam[i] < 0 || cam[i] >= p->plan.nc || pt[i] < 0 || pt[i] >= p->plan.np)
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "term %lld: camera %d / point %d out of range",
+                       static_cast<long long>(i), cam[i], pt[i]);
+  }
+  if (n == 0) return SGBA_OK;
+  SGBA_CK(cudaSetDevice(p->device));
+  // one pool allocation: cam, pt (int32) then J_pose, J_point (f64)
+  const size_t idx_bytes = (sizeof(int32_t) * 2 * static_cast<size_t>(n) + 255) & ~size_t(255);
+  const size_t bytes = idx_bytes + sizeof(double) * 18 * static_cast<size_t>(n);
+  void* buf = nullptr;
+  SGBA_CK(cudaMallocFromPoolAsync(&buf, bytes, p->pool, p->stream));
+  int32_t* dcam = static_cast<int32_t*>(buf);
+  int32_t* dpt = dcam + n;
+  double* djp = reinterpret_cast<double*>(static_cast<char*>(buf) + idx_bytes);
+  double* djm = djp + 12 * n;
+  cudaError_t e = cudaMemcpyAsync(dcam, cam, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dpt, pt, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream);
+  if (e == cudaSuccess) e = sgba::launch_debug_jacobians(p->sz, p->d, n, dcam, dpt, precision, djp, djm, p->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(j_pose, djp, sizeof(double) * 12 * n, cudaMemcpyDeviceToHost, p->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(j_point, djm, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, p->stream);
+  cudaFreeAsync(buf, p->stream);
+  const cudaError_t es = cudaStreamSynchronize(p->stream);
+  if (e == cudaSuccess) e = es;
+  if (e != cudaSuccess) return set_error(SGBA_ERR_CUDA, "sgba_debug_jacobians: %s", cudaGetErrorString(e));
   return SGBA_OK;
 }
 
@@ -1361,6 +1425,15 @@ int sgba_total_cost_noalloc(int32_t n_cam, const double* poses, int32_t n_pt, co
       return set_error(SGBA_ERR_INVALID_ARGUMENT, "sgba_total_cost_noalloc: non-finite intrinsics");
   if (!std::isfinite(huber_delta))
     return set_error(SGBA_ERR_INVALID_ARGUMENT, "sgba_total_cost_noalloc: non-finite huber_delta");
+  if (!huber_in_float_range(huber_delta))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT,
+                     "sgba_total_cost_noalloc: huber_delta %g outside the float range the kernels compare in", huber_delta);
+  // the kernels load obs_uv as 16-byte pairs and the other arrays as whole elements
+  auto misaligned = [](const void* q, uintptr_t a) { return q && (reinterpret_cast<uintptr_t>(q) % a) != 0; };
+  if (misaligned(obs_uv, 16) || misaligned(poses, 8) || misaligned(points, 8) || misaligned(cost, 8) ||
+      misaligned(obs_cam, 4) || misaligned(obs_pt, 4))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT,
+                     "sgba_total_cost_noalloc: misaligned device pointer (obs_uv needs 16 bytes, doubles 8, indices 4)");
   cudaError_t e = sgba::launch_total_cost_noalloc(n_cam, poses, n_pt, points, n_obs, obs_cam, obs_pt, obs_uv,
                                                   intrinsics, huber_delta, cost, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess)

@@ -262,6 +262,12 @@ cudaError_t pair_totals(const Sizes& s, const Dev& d, int32_t* totals, cudaStrea
 cudaError_t pair_fill(const Sizes& s, const Dev& d, const int32_t* bidmap, int64_t nb, const int64_t* block_begin,
                       int32_t nchunk, int32_t* table, cudaStream_t st);
 
+// Per-term Jacobians (2x6 pose, 2x3 point) of the given (camera, point) pairs
+// at the current variables, as the linearization kernels evaluate them:
+// precision 0 FP32, 1 float-float (sgba_debug_jacobians).
+cudaError_t launch_debug_jacobians(const Sizes& s, const Dev& d, int64_t n, const int32_t* cam, const int32_t* pt,
+                                   int precision, double* jp, double* jm, cudaStream_t st);
+
 // Allocation-free total cost over caller-owned device arrays; the scratch is a
 // static __device__ array (sgba_kernels.cu).  Arguments are validated by the
 // caller except the observation indices, which the kernel checks.

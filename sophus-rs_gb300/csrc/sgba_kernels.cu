@@ -727,7 +727,9 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
           }
         }
       }
-      Z[18] = 0.f;
+      // padding entry 18 flags a term whose float-float Z is in zdd (the
+      // back-substitution and the reduced rhs of such a point read it there)
+      Z[18] = (!well && a.zdd) ? 1.f : 0.f;
       Z[19] = 0.f;
       float4* dst = reinterpret_cast<float4*>(a.zmat + kZS * g);
 #pragma unroll
@@ -985,11 +987,24 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
       }
       const float* cv = a.cvec + 6 * mb;
       dd c0 = dd_make(cv[0], cv[1]), c1 = dd_make(cv[2], cv[3]), c2 = dd_make(cv[4], cv[5]);
+      if (Z[18] != 0.f && a.zdd) {
+        // a point rebuilt in float-float: its float-float Z
+        const float* zd = a.zdd + kZD * g;
 #pragma unroll
-      for (int r = 0; r < 6; ++r) {
-        dd t = dd_add(dd_add(dd_mul_f(c0, Z[r * 3 + 0]), dd_mul_f(c1, Z[r * 3 + 1])), dd_mul_f(c2, Z[r * 3 + 2]));
-        zc[2 * r] = t.hi;
-        zc[2 * r + 1] = t.lo;
+        for (int r = 0; r < 6; ++r) {
+          dd t = dd_add(dd_add(dd_mul(c0, dd_make(zd[6 * r + 0], zd[6 * r + 1])),
+                               dd_mul(c1, dd_make(zd[6 * r + 2], zd[6 * r + 3]))),
+                        dd_mul(c2, dd_make(zd[6 * r + 4], zd[6 * r + 5])));
+          zc[2 * r] = t.hi;
+          zc[2 * r + 1] = t.lo;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+          dd t = dd_add(dd_add(dd_mul_f(c0, Z[r * 3 + 0]), dd_mul_f(c1, Z[r * 3 + 1])), dd_mul_f(c2, Z[r * 3 + 2]));
+          zc[2 * r] = t.hi;
+          zc[2 * r + 1] = t.lo;
+        }
       }
     }
   }
@@ -1376,6 +1391,7 @@ struct BackArgs {
   const int32_t* pt_mb;
   const float* zmat;
   const float* zdd;  // float-float Z (float-float linearization) or null
+  const float* zdd_flagged;  // float-float Z of the terms flagged in zmat (other problems)
   const float* cinv;
   const float* cvec;
   const float* xdd;  // dx_f as float-float pairs
@@ -1409,12 +1425,27 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
       } else {
         float Z[20];
         load_z(a.zmat, static_cast<int>(g), Z);
+        if (Z[18] != 0.f && a.zdd_flagged) {
+          // a point rebuilt in float-float: C^-T amplifies the rounding of Z
+          // along its weakly held direction, so Z^T dx_f is summed from the
+          // float-float Z
+          const float* zd = a.zdd_flagged + kZD * g;
 #pragma unroll
-        for (int r = 0; r < 6; ++r) {
-          const float2 xv = xp[r];
-          const dd x = dd_make(xv.x, xv.y);
+          for (int r = 0; r < 6; ++r) {
+            const float2 xv = xp[r];
+            const dd x = dd_make(xv.x, xv.y);
 #pragma unroll
-          for (int q = 0; q < 3; ++q) t[q] = dd_add(t[q], dd_mul_f(x, Z[r * 3 + q]));
+            for (int q = 0; q < 3; ++q)
+              t[q] = dd_add(t[q], dd_mul(x, dd_make(zd[6 * r + 2 * q], zd[6 * r + 2 * q + 1])));
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < 6; ++r) {
+            const float2 xv = xp[r];
+            const dd x = dd_make(xv.x, xv.y);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) t[q] = dd_add(t[q], dd_mul_f(x, Z[r * 3 + q]));
+          }
         }
       }
     }
@@ -1870,7 +1901,7 @@ static LinArgs make_lin_args(const Sizes& s, const Dev& d, double nu_override, b
   la.slow_count = d.slow_count;
   la.force_dd = s.lin_dd;
   la.res_lo = s.lin_dd ? d.res_lo : nullptr;
-  la.zdd = s.lin_dd ? d.zdd : nullptr;
+  la.zdd = d.zdd;
   return la;
 }
 
@@ -1920,6 +1951,7 @@ static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
   b.pt_mb = d.pt_mb;
   b.zmat = d.zmat;
   b.zdd = s.lin_dd ? d.zdd : nullptr;
+  b.zdd_flagged = d.zdd;
   b.cinv = d.cinv;
   b.cvec = d.cvec;
   b.xdd = d.xdd;
@@ -2089,6 +2121,47 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
   k_commit<<<cb, 256, 0, st>>>(s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res,
                                d.res_lo_t, d.res_lo, d.ctrl);
   return 2;
+}
+
+// ---------------------------------------------------------------------------
+// Per-term Jacobians as the linearization evaluates them (sgba_debug_jacobians):
+// the pose table of the observing camera and jacobians_f (FP32 linearization)
+// or jacobians_dd (float-float linearization and rebuilt point blocks), with
+// the same rounding of the inputs as k_landmark / k_camera_tiles.
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void k_debug_jacobians(int64_t n, const int32_t* __restrict__ cam, const int32_t* __restrict__ pt,
+                                  const double* __restrict__ poses, const double* __restrict__ points, double fx,
+                                  double fy, int precision, double* __restrict__ jp, double* __restrict__ jm) {
+  const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  float pf[12], pd[24];
+  pose_table(poses + 7 * static_cast<int64_t>(cam[i]), pf, pd);
+  const double* pw = points + 3 * static_cast<int64_t>(pt[i]);
+  if (precision == 0) {
+    JacF J;
+    jacobians_f(pf, __double2float_rn(pw[0]), __double2float_rn(pw[1]), __double2float_rn(pw[2]),
+                static_cast<float>(fx), static_cast<float>(fy), &J);
+    for (int k = 0; k < 12; ++k) jp[12 * i + k] = J.jp[k];
+    for (int k = 0; k < 6; ++k) jm[6 * i + k] = J.jm[k];
+  } else {
+    JacD J;
+    const dd fxd = dd_make(static_cast<float>(fx), static_cast<float>(fx - static_cast<float>(fx)));
+    const dd fyd = dd_make(static_cast<float>(fy), static_cast<float>(fy - static_cast<float>(fy)));
+    jacobians_dd(pd, dd_from_double(pw[0]), dd_from_double(pw[1]), dd_from_double(pw[2]), fxd, fyd, &J);
+    for (int k = 0; k < 12; ++k) jp[12 * i + k] = dd_to_double(J.jp[k]);
+    for (int k = 0; k < 6; ++k) jm[6 * i + k] = dd_to_double(J.jm[k]);
+  }
+}
+}  // namespace
+
+cudaError_t launch_debug_jacobians(const Sizes& s, const Dev& d, int64_t n, const int32_t* cam, const int32_t* pt,
+                                   int precision, double* jp, double* jm, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const int64_t blocks = (n + 127) / 128;
+  k_debug_jacobians<<<static_cast<unsigned>(blocks), 128, 0, st>>>(n, cam, pt, d.poses, d.points, s.intr[0],
+                                                                   s.intr[1], precision, jp, jm);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

@@ -121,9 +121,8 @@ EXPORTED = [
     "sgba_abi_version", "sgba_last_error", "sgba_problem_create", "sgba_problem_destroy",
     "sgba_optimizer_init", "sgba_optimizer_step", "sgba_optimize", "sgba_get_variables",
     "sgba_get_cost", "sgba_set_variables", "sgba_get_layout", "sgba_export_pattern",
-    "sgba_debug_last_system", "sgba_state_save", "sgba_state_load", "sgba_get_profile",
-    "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_synth_generate",
-    "sgba_synth_free", "sgba_batch_optimize",
+    "sgba_debug_last_system", "sgba_debug_jacobians", "sgba_state_save", "sgba_state_load", "sgba_get_profile",
+    "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_batch_optimize",
 ]
 
 # sgba_kernel_id
@@ -172,6 +171,7 @@ def lib():
     ip = C.POINTER(C.c_int32)
     L.sgba_export_pattern.argtypes = [C.c_void_p, ip, ip, ip, ip]
     L.sgba_debug_last_system.argtypes = [C.c_void_p, dp, dp, dp]
+    L.sgba_debug_jacobians.argtypes = [C.c_void_p, C.c_int64, ip, ip, C.c_int32, dp, dp]
     L.sgba_state_save.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(C.c_size_t)]
     L.sgba_state_load.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
     L.sgba_get_profile.argtypes = [C.c_void_p, C.POINTER(Profile)]
@@ -331,6 +331,20 @@ class Problem:
         delta = np.empty(n6 + 3 * lay.n_marg_points)
         check(lib().sgba_debug_last_system(self._h, _dptr(S), _dptr(rhs), _dptr(delta)))
         return S, rhs, delta
+
+    def jacobians(self, cam, pt, precision=0):
+        """Per-term J_pose (n, 2, 6) and J_point (n, 2, 3) at the current
+        variables, as the linearization kernels evaluate them (precision 0:
+        FP32, 1: float-float)."""
+        cam = np.ascontiguousarray(cam, dtype=np.int32)
+        pt = np.ascontiguousarray(pt, dtype=np.int32)
+        n = cam.shape[0]
+        jp = np.empty((n, 2, 6))
+        jm = np.empty((n, 2, 3))
+        ip = C.POINTER(C.c_int32)
+        check(lib().sgba_debug_jacobians(self._h, n, cam.ctypes.data_as(ip), pt.ctypes.data_as(ip),
+                                         int(precision), _dptr(jp), _dptr(jm)))
+        return jp, jm
 
     def state_save(self):
         size = C.c_size_t(0)

@@ -1,10 +1,30 @@
-"""Seeded synthetic BA scenes (sgba_synth_generate in libsgba.so, host code)."""
+"""Seeded synthetic BA scenes (sgba_synth_generate in libsgba_synth.so, host
+code; include/sgba_synth.h).  The generator is a separate small library, not
+part of libsgba.so."""
 import ctypes as C
+import os
 from dataclasses import dataclass
 
 import numpy as np
 
-from . import native
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsgba_synth.so")
+_libs = {}
+
+
+def _lib(path=None):
+    path = path or LIB_PATH
+    L = _libs.get(path)
+    if L is None:
+        if not os.path.exists(path):
+            raise RuntimeError("scene generator library not built: %s" % path)
+        L = C.CDLL(path)
+        L.sgba_synth_generate.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
+                                          C.POINTER(C.POINTER(_SynthC))]
+        L.sgba_synth_generate.restype = C.c_int
+        L.sgba_synth_free.argtypes = [C.POINTER(_SynthC)]
+        _libs[path] = L
+    return L
 
 CIRCLE = 0
 SPHERE = 1
@@ -68,11 +88,10 @@ class BAProblem:
         return BAProblem(**{k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in self.__dict__.items()})
 
 
-def generate(kind, n_cam=0, n_pt=0, seed=BASE_SEED):
-    L = native.lib()
-    L.sgba_synth_generate.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(C.POINTER(_SynthC))]
-    L.sgba_synth_generate.restype = C.c_int
-    L.sgba_synth_free.argtypes = [C.POINTER(_SynthC)]
+def generate(kind, n_cam=0, n_pt=0, seed=BASE_SEED, lib_path=None):
+    """One seeded scene.  lib_path selects another library that exports the
+    same generator (the CPU reference arm of the benchmark uses the oracle's)."""
+    L = _lib(lib_path)
     ptr = C.POINTER(_SynthC)()
     st = L.sgba_synth_generate(int(kind), int(n_cam), int(n_pt), C.c_uint64(seed), C.byref(ptr))
     if st != 0:

@@ -7,26 +7,32 @@ import re
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _declared_functions():
+def _declared_functions(header):
     names = set()
-    inc = os.path.join(ROOT, "include")
-    for f in os.listdir(inc):
-        if not f.endswith(".h"):
-            continue
-        text = open(os.path.join(inc, f)).read()
-        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        for m in re.finditer(r"^\s*(?:int|int32_t|size_t|void)\s+\**\s*(sgba_\w+)\s*\(", text, flags=re.M):
-            names.add(m.group(1))
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    for m in re.finditer(r"^\s*(?:int|int32_t|size_t|void)\s+\**\s*(sgba_\w+)\s*\(", text, flags=re.M):
+        names.add(m.group(1))
     return names
 
 
 def test_library_exports_every_declared_symbol(pkg):
+    """include/sgba.h is libsgba.so's ABI, include/sgba_synth.h the scene
+    generator's (libsgba_synth.so); every header in include/ is one of them."""
+    assert sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")) == \
+        ["sgba.h", "sgba_synth.h"]
     lib = ctypes.CDLL(pkg.native.lib_path())
-    declared = _declared_functions()
+    declared = _declared_functions("sgba.h")
     assert "sgba_optimize" in declared and "sgba_problem_create" in declared
     missing = [n for n in sorted(declared) if not hasattr(lib, n)]
     assert not missing, missing
     assert set(pkg.native.EXPORTED) <= declared
+    gen = ctypes.CDLL(pkg.synth.LIB_PATH)
+    gen_declared = _declared_functions("sgba_synth.h")
+    assert gen_declared == {"sgba_synth_generate", "sgba_synth_free"}
+    assert all(hasattr(gen, n) for n in gen_declared)
+    # the generator is not part of the product library
+    assert not hasattr(lib, "sgba_synth_generate")
 
 
 def test_abi_version_and_error_buffer(pkg):

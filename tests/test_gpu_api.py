@@ -95,10 +95,10 @@ def test_empty_and_degenerate_points(pkg, oracle):
     step is rejected, as SingularMargBlock makes the reference reject).
 
     The single-view point's depth is held by nu = 1e-4 alone (condition number
-    ~1e8); its block is rebuilt in float-float, but the FP32 pose-side products
-    of its observation still perturb the reduced system at the 1e-4 level, so
-    this case is held to 1e-3 per iteration and 1e-5 at the end instead of the
-    1e-6 bar of well-posed problems (every point seen at least twice)."""
+    ~1e8): its block, its Z = W C^-T and the back-substitution through C^-T are
+    carried in float-float, so it meets the same 1e-6 per-iteration bar as
+    well-posed problems (the reference keeps such points:
+    compute_marg_block_contrib, crates/sophus_solver/src/ldlt/schur_ldlt.rs:82-135)."""
     prob = _circle(pkg, n_cam=6, n_pt=80, seed=14)
     keep = np.ones(prob.n_obs, bool)
     first = np.where(prob.obs_pt == 3)[0]
@@ -110,8 +110,8 @@ def test_empty_and_degenerate_points(pkg, oracle):
     orecs, _, _ = oracle.optimize(prob, params)
     g, o = np.array([r.merit for r in grecs]), np.array([r.merit for r in orecs])
     assert np.all(np.isfinite(g)) and all(r.accepted for r in grecs[:4])
-    assert np.max(np.abs(g - o) / o) < 1e-3
-    assert abs(g[-1] - o[-1]) / o[-1] < 1e-5
+    assert np.max(np.abs(g - o) / o) < COST_RTOL
+    assert abs(g[-1] - o[-1]) / o[-1] < COST_RTOL
     # orphan point: no term touches it
     empty = prob.copy()
     empty.obs_cam = empty.obs_cam[empty.obs_pt != 5]

@@ -1,4 +1,6 @@
-"""sgba_total_cost_noalloc: the allocation-free total cost against the cost
+"""sgba_total_cost_noalloc: the allocation-free total cost against the
+oracle's calc_total_cost (the FP64 CPU restatement of the reference,
+crates/sophus_opt/src/nlls/cost/cost_fn.rs:403-433) and against the cost
 that sgba_get_cost reports for the same variables.
 
 The file name sorts last so that the GPU test also runs after every other
@@ -34,6 +36,26 @@ def test_rejects_more_cameras_than_the_scratch_holds(pkg):
     assert st == pkg.native.ERR_INVALID_ARGUMENT and "NULL" in pkg.native.last_error()
 
 
+def test_rejects_misaligned_pointers_and_unrepresentable_huber(pkg):
+    """Also host-side checks, before any CUDA call: the kernels load obs_uv as
+    16-byte pairs, and compare with the Huber threshold in float."""
+    f = _bind(pkg)
+    intr = (C.c_double * 4)(500.0, 500.0, 320.0, 240.0)
+    base = 1 << 20  # never dereferenced: the checks reject first
+    args = dict(poses=base, points=base + 256, cam=base + 512, pt=base + 768, uv=base + 1024, out=base + 1280)
+
+    def call(huber=1.0, **kw):
+        a = dict(args, **kw)
+        return f(2, a["poses"], 1, a["points"], 1, a["cam"], a["pt"], a["uv"], intr, huber, a["out"], None)
+
+    assert call(uv=base + 1024 + 8) == pkg.native.ERR_INVALID_ARGUMENT  # 8 but not 16 bytes
+    assert "misaligned" in pkg.native.last_error()
+    assert call(poses=base + 4) == pkg.native.ERR_INVALID_ARGUMENT
+    assert call(cam=base + 514) == pkg.native.ERR_INVALID_ARGUMENT
+    assert call(huber=1e-40) == pkg.native.ERR_INVALID_ARGUMENT  # positive, below the normal floats
+    assert "huber" in pkg.native.last_error()
+
+
 def _expected_cost(pkg, prob):
     with pkg.native.Problem(prob, device=0) as gp:
         gp.init(fixed_iter_params(pkg, 1, prob.initial_lm_damping))
@@ -59,22 +81,25 @@ def _call(pkg, f, torch, prob, a):
 
 
 @pytest.mark.gpu
-def test_noalloc_cost_matches_get_cost(pkg):
+def test_noalloc_cost_matches_oracle_and_get_cost(pkg, oracle):
     torch = pytest.importorskip("torch")
     torch.cuda.init()
     f = _bind(pkg)
     first = pkg.synth.generate(pkg.synth.CIRCLE, seed=pkg.synth.BASE_SEED + 11)
     second = pkg.synth.generate(pkg.synth.LOOP, n_cam=300, n_pt=3000, seed=pkg.synth.BASE_SEED + 12)
     second.huber_delta = 0.0  # no robust kernel on the second problem
-    expected = [_expected_cost(pkg, p) for p in (first, second)]
-    arrays = [_device_arrays(torch, p) for p in (first, second)]
+    probs = (first, second)
+    expected = [_expected_cost(pkg, p) for p in probs]
+    ora = [oracle.total_cost(p) for p in probs]  # f64 calc_total_cost, Huber and no kernel
+    arrays = [_device_arrays(torch, p) for p in probs]
     # two calls in a row on one stream, different sizes, then read both
     _call(pkg, f, torch, first, arrays[0])
     _call(pkg, f, torch, second, arrays[1])
     torch.cuda.synchronize()
     got = [float(a["out"].cpu()[0]) for a in arrays]
-    for g, e in zip(got, expected):
+    for g, e, o in zip(got, expected, ora):
         assert np.isfinite(g) and abs(g - e) <= RTOL * abs(e), (g, e)
+        assert abs(g - o) <= RTOL * abs(o), (g, o)
     # the same inputs again: bit-identical (fixed reduction order)
     _call(pkg, f, torch, first, arrays[0])
     torch.cuda.synchronize()
