@@ -249,6 +249,55 @@ int sgba_bench_iterations(sgba_problem *p, int32_t iters, int32_t flush_l2, doub
  * *ms_avg is the mean device time per launch. */
 int sgba_bench_kernel(sgba_problem *p, int32_t kernel, int32_t reps, int32_t flush_l2, double *ms_avg);
 
+/* ---- iterative solve of the reduced camera system ------------------------
+ * The reference solves S dx_f = b only exactly (block LDL^T, selected through
+ * the closed LinearSolverEnum, crates/sophus_solver/src/lib.rs:295-318; the
+ * Schur factor crates/sophus_solver/src/ldlt/schur_ldlt.rs:536-812).  These
+ * entry points add preconditioned conjugate gradients (FP64, Jacobi-scaled
+ * system, one cooperative launch) in front of the exact factorization: when
+ * PCG reaches |b - S x| <= tolerance |b| (scaled system) within
+ * max_iterations, its x is the step and the factorization is skipped;
+ * otherwise the factorization runs as usual (the fallback), in the same LM
+ * iteration.  The preconditioner is block-Jacobi per free pose (mode 1), or
+ * block-Jacobi corrected by a learned 6x6 block per pose (mode 2):
+ * P_j = C_j^-T (I + L_j L_j^T) C_j^-1, C_j C_j^T the pose's scaled diagonal
+ * block, L_j from a message-passing network over the camera covisibility
+ * graph (3 layers, hidden width 64, BF16 weights, FP32 accumulation).
+ * Default: mode 0, the exact factorization alone. */
+typedef enum {
+  SGBA_LINSOLVE_EXACT = 0,
+  SGBA_LINSOLVE_PCG_BLOCK_JACOBI = 1,
+  SGBA_LINSOLVE_PCG_LEARNED = 2,
+} sgba_linsolve_mode;
+typedef struct {
+  int32_t mode;            /* sgba_linsolve_mode */
+  int32_t max_iterations;  /* PCG iteration cap (e.g. 50) */
+  double tolerance;        /* relative residual (e.g. 1e-8) */
+} sgba_linear_solver;
+typedef struct sgba_pcg_model sgba_pcg_model;
+/* Selects the reduced-system solver of a problem (the iteration graph is
+ * captured again).  model: required for mode 2, on the problem's device; it
+ * must stay alive while the problem uses it. */
+int sgba_set_linear_solver(sgba_problem *p, const sgba_linear_solver *cfg, const sgba_pcg_model *model);
+/* PCG counters since sgba_optimizer_init. */
+typedef struct {
+  int64_t solves;                 /* PCG solves */
+  int64_t fallbacks;              /* of which fell back to the exact factorization */
+  int64_t iterations;             /* PCG iterations in total */
+  int32_t last_iterations;
+  int32_t last_status;            /* 0 converged, 1 iteration cap, 2 breakdown, 3 barrier wait gave up */
+  double last_relative_residual;
+} sgba_pcg_stats;
+int sgba_get_pcg_stats(sgba_problem *p, sgba_pcg_stats *out);
+/* The network's parameters (FP32 master copy; the kernels read a BF16 copy). */
+int32_t sgba_pcg_num_params(void);
+/* A model on `device` (< 0: current) with seeded initial weights: Glorot
+ * uniform hidden layers, output head at L_j = 0.1 I. */
+int sgba_pcg_model_create(int32_t device, uint64_t seed, sgba_pcg_model **out);
+int sgba_pcg_model_destroy(sgba_pcg_model *m);
+int sgba_pcg_model_set_params(sgba_pcg_model *m, const float *params, int32_t n);
+int sgba_pcg_model_get_params(const sgba_pcg_model *m, float *params, int32_t n);
+
 /* ---- allocation-free total cost (no counterpart in the reference) --------
  * calc_total_cost of the reprojection cost (the value sgba_get_cost reports,
  * float-float on the GPU) over observations that the caller already holds in

@@ -149,6 +149,35 @@ pub struct sgba_profile {
     pub ms_cost: f64,
 }
 
+#[repr(C)]
+#[derive(Debug, Clone, Copy, Default)]
+pub struct sgba_linear_solver {
+    pub mode: i32,
+    pub max_iterations: i32,
+    pub tolerance: f64,
+}
+
+#[repr(C)]
+#[derive(Debug, Clone, Copy, Default)]
+pub struct sgba_pcg_stats {
+    pub solves: i64,
+    pub fallbacks: i64,
+    pub iterations: i64,
+    pub last_iterations: i32,
+    pub last_status: i32,
+    pub last_relative_residual: f64,
+}
+
+pub const SGBA_LINSOLVE_EXACT: i32 = 0;
+pub const SGBA_LINSOLVE_PCG_BLOCK_JACOBI: i32 = 1;
+pub const SGBA_LINSOLVE_PCG_LEARNED: i32 = 2;
+
+/// Opaque parameters of the learned block preconditioner.
+#[repr(C)]
+pub struct sgba_pcg_model {
+    _private: [u8; 0],
+}
+
 extern "C" {
     pub fn sgba_abi_version() -> i32;
     pub fn sgba_last_error(buf: *mut c_char, cap: usize) -> usize;
@@ -205,6 +234,17 @@ extern "C" {
         launches: *mut i64,
     ) -> c_int;
     pub fn sgba_bench_kernel(p: *mut sgba_problem, kernel: i32, reps: i32, flush_l2: i32, ms_avg: *mut f64) -> c_int;
+    pub fn sgba_set_linear_solver(
+        p: *mut sgba_problem,
+        cfg: *const sgba_linear_solver,
+        model: *const sgba_pcg_model,
+    ) -> c_int;
+    pub fn sgba_get_pcg_stats(p: *mut sgba_problem, out: *mut sgba_pcg_stats) -> c_int;
+    pub fn sgba_pcg_num_params() -> i32;
+    pub fn sgba_pcg_model_create(device: i32, seed: u64, out: *mut *mut sgba_pcg_model) -> c_int;
+    pub fn sgba_pcg_model_destroy(m: *mut sgba_pcg_model) -> c_int;
+    pub fn sgba_pcg_model_set_params(m: *mut sgba_pcg_model, params: *const f32, n: i32) -> c_int;
+    pub fn sgba_pcg_model_get_params(m: *const sgba_pcg_model, params: *mut f32, n: i32) -> c_int;
     pub fn sgba_total_cost_noalloc(
         n_cam: i32,
         poses: *const f64,

@@ -61,7 +61,8 @@ constexpr int kFwdSeg = 10;      // dot-product segments per panel row in the sw
 constexpr float kTolRel = 1e-12f;
 constexpr size_t kSmemLimit = 227 * 1024;
 
-__device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0; }
+// the factorization is skipped on termination, on a skipped step and when PCG converged
+__device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0 || c->pcg_done != 0; }
 
 __device__ __forceinline__ dd f2dd(float2 v) { return dd_make(v.x, v.y); }
 __device__ __forceinline__ float2 dd2f(dd v) { return make_float2(v.hi, v.lo); }

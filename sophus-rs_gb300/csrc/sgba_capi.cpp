@@ -25,6 +25,7 @@
 #include <utility>
 #include <mutex>
 #include <map>
+#include <memory>
 #include <string>
 #include <thread>
 #include <vector>
@@ -791,6 +792,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_alloc(p, &d.cvec, 6 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.bm, 3 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.dm, 3 * static_cast<size_t>(P.nm)))) return st;
+  if ((st = dev_alloc(p, &d.gauge_um, 3 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.bf, 6 * static_cast<size_t>(P.nf)))) return st;
   if ((st = dev_alloc(p, &d.rb, 6 * static_cast<size_t>(P.nf)))) return st;
   if ((st = dev_alloc(p, &d.ufull, 36 * static_cast<size_t>(P.nf)))) return st;
@@ -1438,6 +1440,233 @@ int sgba_total_cost_noalloc(int32_t n_cam, const double* poses, int32_t n_pt, co
                                                   intrinsics, huber_delta, cost, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess)
     return set_error(SGBA_ERR_CUDA, "sgba_total_cost_noalloc: %s", cudaGetErrorString(e));
+  return SGBA_OK;
+}
+
+// ---- iterative solve of the reduced camera system ------------------------
+
+namespace {
+
+// Full block rows of S (both triangles) from the lower block list, columns
+// ascending in every row; diag[j] = lower block id of block (j, j).
+void pcg_structure(const Plan& P, std::vector<int32_t>* rowptr, std::vector<int32_t>* cols,
+                   std::vector<int32_t>* blks, std::vector<int32_t>* diag) {
+  const int nf = P.nf;
+  std::vector<std::vector<std::pair<int32_t, int32_t>>> rows(nf);
+  diag->assign(nf, -1);
+  for (size_t b = 0; b < P.sb_row.size(); ++b) {
+    const int j = P.sb_row[b], k = P.sb_col[b];
+    rows[j].push_back({k, static_cast<int32_t>(b)});
+    if (j != k) rows[k].push_back({j, static_cast<int32_t>(b) | static_cast<int32_t>(0x80000000u)});
+    else (*diag)[j] = static_cast<int32_t>(b);
+  }
+  rowptr->assign(nf + 1, 0);
+  cols->clear();
+  blks->clear();
+  for (int j = 0; j < nf; ++j) {
+    std::sort(rows[j].begin(), rows[j].end());
+    for (const auto& e : rows[j]) {
+      cols->push_back(e.first);
+      blks->push_back(e.second);
+    }
+    (*rowptr)[j + 1] = static_cast<int32_t>(cols->size());
+  }
+}
+
+int pcg_alloc(sgba_problem* p) {
+  Dev& d = p->d;
+  if (d.pcg_rowptr) return SGBA_OK;
+  Sizes& s = p->sz;
+  std::vector<int32_t> rowptr, cols, blks, diag;
+  pcg_structure(p->plan, &rowptr, &cols, &blks, &diag);
+  for (int j = 0; j < s.nf; ++j)
+    if (diag[j] < 0) return set_error(SGBA_ERR_STATE, "free pose block %d has no diagonal block in S", j);
+  int st;
+  const size_t nf = static_cast<size_t>(s.nf), n6 = static_cast<size_t>(s.n6);
+  if ((st = dev_upload(p, &d.pcg_rowptr, rowptr))) return st;
+  if ((st = dev_upload(p, &d.pcg_cols, cols))) return st;
+  if ((st = dev_upload(p, &d.pcg_blks, blks))) return st;
+  if ((st = dev_upload(p, &d.pcg_diag, diag))) return st;
+  if ((st = dev_alloc(p, &d.pcg_S, 36 * static_cast<size_t>(s.nsb)))) return st;
+  if ((st = dev_alloc(p, &d.pcg_scl, n6))) return st;
+  if ((st = dev_alloc(p, &d.pcg_P, 36 * nf))) return st;
+  if ((st = dev_alloc(p, &d.pcg_Cinv, 36 * nf))) return st;
+  if ((st = dev_alloc(p, &d.pcg_vec, 5 * n6))) return st;
+  if ((st = dev_alloc(p, &d.pcg_bar, 4))) return st;
+  if ((st = dev_alloc(p, &d.pcg_part, 4 * static_cast<size_t>(sgba::kPcgMaxGrid)))) return st;
+  if ((st = dev_alloc(p, &d.pcg_feat, nf * sgba::kPcgFeat))) return st;
+  if ((st = dev_alloc(p, &d.pcg_ew, cols.size()))) return st;
+  if ((st = dev_alloc(p, &d.pcg_h, 2 * nf * sgba::kPcgHidden))) return st;
+  if ((st = dev_alloc(p, &d.pcg_msg, nf * sgba::kPcgHidden))) return st;
+  if ((st = dev_alloc(p, &d.pcg_L, nf * sgba::kPcgOut))) return st;
+  s.pcg_nnzb = static_cast<int64_t>(cols.size());
+  SGBA_CK(cudaStreamSynchronize(p->stream));  // the host vectors above go out of scope
+  return SGBA_OK;
+}
+
+uint16_t f32_to_bf16(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  u += 0x7fffu + ((u >> 16) & 1u);  // round to nearest even
+  return static_cast<uint16_t>(u >> 16);
+}
+
+int model_upload(sgba::PcgModel& m, const std::vector<float>& w) {
+  std::vector<uint16_t> b(w.size());
+  for (size_t i = 0; i < w.size(); ++i) b[i] = f32_to_bf16(w[i]);
+  SGBA_CK(cudaSetDevice(m.device));
+  SGBA_CK(cudaMemcpy(m.w32, w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice));
+  SGBA_CK(cudaMemcpy(m.wbf, b.data(), sizeof(uint16_t) * b.size(), cudaMemcpyHostToDevice));
+  return SGBA_OK;
+}
+
+}  // namespace
+
+struct sgba_pcg_model {
+  sgba::PcgModel m;
+};
+
+int32_t sgba_pcg_num_params(void) { return sgba::kPcgParams; }
+
+int sgba_pcg_model_create(int32_t device, uint64_t seed, sgba_pcg_model** out) {
+  if (!out) return set_error(SGBA_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  int dev = device;
+  if (dev < 0) SGBA_CK(cudaGetDevice(&dev));
+  SGBA_CK(cudaSetDevice(dev));
+  std::unique_ptr<sgba_pcg_model> h(new (std::nothrow) sgba_pcg_model());
+  if (!h) return set_error(SGBA_ERR_OUT_OF_MEMORY, "host allocation failed");
+  sgba::PcgModel& m = h->m;
+  m.device = dev;
+  const size_t n = sgba::kPcgParams;
+  auto fail = [&](cudaError_t e) {
+    cudaFree(m.w32); cudaFree(m.wbf); cudaFree(m.m1); cudaFree(m.m2); cudaFree(m.grad);
+    return set_error(SGBA_ERR_OUT_OF_MEMORY, "model allocation: %s", cudaGetErrorString(e));
+  };
+  cudaError_t e;
+  if ((e = cudaMalloc(&m.w32, sizeof(float) * n)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&m.wbf, sizeof(uint16_t) * n)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&m.m1, sizeof(float) * n)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&m.m2, sizeof(float) * n)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&m.grad, sizeof(float) * n)) != cudaSuccess) return fail(e);
+  cudaMemset(m.m1, 0, sizeof(float) * n);
+  cudaMemset(m.m2, 0, sizeof(float) * n);
+  cudaMemset(m.grad, 0, sizeof(float) * n);
+  // Glorot-uniform hidden weights from a SplitMix64 stream; the output head
+  // starts at L = 0.1 I (P = 1.01 x block-Jacobi: the gradient of L L^T
+  // vanishes at L = 0) with small random weights
+  std::vector<float> w(n, 0.0f);
+  uint64_t st = seed;
+  auto uni = [&st]() {
+    uint64_t z = (st += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    z ^= z >> 31;
+    return static_cast<double>(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+  };
+  const int H = sgba::kPcgHidden, F = sgba::kPcgFeat;
+  const double a_in = std::sqrt(6.0 / (F + H)), a_h = 0.5 * std::sqrt(6.0 / (2.0 * H));
+  for (int i = 0; i < H * F; ++i) w[i] = static_cast<float>(a_in * uni());
+  size_t off = static_cast<size_t>(H) * F + H;
+  for (int l = 0; l < sgba::kPcgLayers; ++l) {
+    for (int i = 0; i < 2 * H * H; ++i) w[off + i] = static_cast<float>(a_h * uni());
+    off += 2 * static_cast<size_t>(H) * H + H;
+  }
+  for (int i = 0; i < sgba::kPcgOut * H; ++i) w[off + i] = static_cast<float>(0.01 * uni());
+  off += static_cast<size_t>(sgba::kPcgOut) * H;
+  for (int r = 0, t = 0; r < 6; ++r)
+    for (int c = 0; c <= r; ++c, ++t) w[off + t] = (r == c) ? 0.1f : 0.0f;
+  int rc = model_upload(m, w);
+  if (rc) { fail(cudaSuccess); return rc; }
+  *out = h.release();
+  return SGBA_OK;
+}
+
+int sgba_pcg_model_destroy(sgba_pcg_model* h) {
+  if (!h) return SGBA_OK;
+  cudaSetDevice(h->m.device);
+  cudaFree(h->m.w32);
+  cudaFree(h->m.wbf);
+  cudaFree(h->m.m1);
+  cudaFree(h->m.m2);
+  cudaFree(h->m.grad);
+  delete h;
+  return SGBA_OK;
+}
+
+int sgba_pcg_model_set_params(sgba_pcg_model* h, const float* params, int32_t n) {
+  if (!h || !params) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (n != sgba::kPcgParams) return set_error(SGBA_ERR_INVALID_ARGUMENT, "%d parameters (expected %d)", n, sgba::kPcgParams);
+  for (int i = 0; i < n; ++i)
+    if (!std::isfinite(params[i])) return set_error(SGBA_ERR_INVALID_ARGUMENT, "parameter %d is not finite", i);
+  std::vector<float> w(params, params + n);
+  int rc = model_upload(h->m, w);
+  if (rc) return rc;
+  SGBA_CK(cudaMemset(h->m.m1, 0, sizeof(float) * n));
+  SGBA_CK(cudaMemset(h->m.m2, 0, sizeof(float) * n));
+  h->m.step = 0;
+  return SGBA_OK;
+}
+
+int sgba_pcg_model_get_params(const sgba_pcg_model* h, float* params, int32_t n) {
+  if (!h || !params) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (n != sgba::kPcgParams) return set_error(SGBA_ERR_INVALID_ARGUMENT, "%d parameters (expected %d)", n, sgba::kPcgParams);
+  SGBA_CK(cudaSetDevice(h->m.device));
+  SGBA_CK(cudaMemcpy(params, h->m.w32, sizeof(float) * n, cudaMemcpyDeviceToHost));
+  return SGBA_OK;
+}
+
+int sgba_set_linear_solver(sgba_problem* p, const sgba_linear_solver* cfg, const sgba_pcg_model* model) {
+  if (!p || !cfg) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (cfg->mode < SGBA_LINSOLVE_EXACT || cfg->mode > SGBA_LINSOLVE_PCG_LEARNED)
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "unknown linear solver mode %d", cfg->mode);
+  if (cfg->mode == SGBA_LINSOLVE_PCG_LEARNED && !model)
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "the learned preconditioner needs a model");
+  if (cfg->mode != SGBA_LINSOLVE_EXACT) {
+    if (!(cfg->max_iterations >= 1) || !(cfg->tolerance > 0.0) || !std::isfinite(cfg->tolerance))
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "PCG needs max_iterations >= 1 and a finite tolerance > 0");
+    if (p->plan.nf < 1) return set_error(SGBA_ERR_SCHUR_MISSING_FREE_OR_MARG, "no free pose: nothing to solve");
+    if (model && model->m.device != p->device)
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "model on device %d, problem on device %d", model->m.device,
+                       p->device);
+  }
+  SGBA_CK(cudaSetDevice(p->device));
+  if (cfg->mode != SGBA_LINSOLVE_EXACT) {
+    int st = pcg_alloc(p);
+    if (st) return st;
+    int grid = 0;
+    if (sgba::pcg_setup(p->plan.nf, &grid) != 0 || grid < 1)
+      return set_error(SGBA_ERR_UNSUPPORTED, "cooperative launch of the PCG kernel is not available");
+    if (cfg->mode == SGBA_LINSOLVE_PCG_LEARNED && sgba::pcg_net_setup() != 0)
+      return set_error(SGBA_ERR_CUDA, "could not raise the shared memory limit of the network kernels");
+    p->sz.pcg_grid = grid;
+  }
+  p->sz.pcg_mode = cfg->mode;
+  p->sz.pcg_max_iters = cfg->max_iterations;
+  p->sz.pcg_tol = cfg->tolerance;
+  p->d.pcg_w = (cfg->mode == SGBA_LINSOLVE_PCG_LEARNED) ? model->m.wbf : nullptr;
+  // the iteration graph is captured again with the new solver chain
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }
+  if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+  const int zero = 0;
+  SGBA_CK(cudaMemcpy(reinterpret_cast<char*>(p->d.ctrl) + offsetof(Ctrl, pcg_done), &zero, sizeof(int),
+                     cudaMemcpyHostToDevice));
+  return SGBA_OK;
+}
+
+int sgba_get_pcg_stats(sgba_problem* p, sgba_pcg_stats* out) {
+  if (!p || !out) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  SGBA_CK(cudaSetDevice(p->device));
+  Ctrl c;
+  SGBA_CK(cudaMemcpyAsync(&c, p->d.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, p->stream));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  out->solves = c.pcg_solves;
+  out->fallbacks = c.pcg_fallbacks;
+  out->iterations = c.pcg_total_iters;
+  out->last_iterations = c.pcg_iters;
+  out->last_status = c.pcg_status;
+  out->last_relative_residual = c.pcg_relres;
   return SGBA_OK;
 }
 

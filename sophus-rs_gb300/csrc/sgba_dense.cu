@@ -119,7 +119,8 @@ struct DenseArgs {
   double center[3];
 };
 
-__device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0; }
+// the factorization is skipped on termination, on a skipped step and when PCG converged
+__device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0 || c->pcg_done != 0; }
 
 __device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release;\n" ::: "memory"); }
 __device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory"); }

@@ -43,6 +43,15 @@ struct Ctrl {
   unsigned long long max_step_bits;
   int fin_ticket;   // k_camera_finalize: blocks done (the last one runs the gradient check)
   int cost_ticket;  // trial k_cost: blocks done (the last one runs the LM decision)
+  // preconditioned conjugate gradients on the reduced system (sgba_pcg.cu)
+  int pcg_done;     // 1: PCG reached its tolerance this iteration, the exact factorization is skipped
+  int pcg_iters;    // PCG iterations of the latest solve
+  int pcg_status;   // 0 ok, 1 iteration cap reached, 2 breakdown, 3 a grid barrier timed out
+  int pcg_pad;
+  double pcg_relres;            // relative residual reached by the latest solve
+  long long pcg_solves;         // PCG solves so far
+  long long pcg_fallbacks;      // of which went to the exact factorization
+  long long pcg_total_iters;    // PCG iterations so far
 };
 
 // Per-step record, layout-identical to sgba_iter_record.
@@ -181,13 +190,57 @@ struct Dev {
   float* xdd = nullptr;            // n6*2: solution as float-float pairs
   double* r = nullptr;             // n6 residual
   double* dm = nullptr;            // nm*3 point steps
+  double* gauge_um = nullptr;      // nm*3 the free poses' gauge direction back-substituted into the points
   double* part = nullptr;          // reduction partials
   int part_cap = 0;
   Ctrl* ctrl = nullptr;
   Record* records = nullptr;
   int record_cap = 0;
   Record* last_rec = nullptr;      // record of the latest step
+  // PCG on the reduced system (sgba_pcg.cu); allocated when a PCG solver is selected
+  int32_t* pcg_rowptr = nullptr;   // nf + 1: full block rows of S (both triangles)
+  int32_t* pcg_cols = nullptr;     // column block of each entry
+  int32_t* pcg_blks = nullptr;     // lower block id of each entry; bit 31 set: use its transpose
+  int32_t* pcg_diag = nullptr;     // nf: lower block id of each diagonal block
+  double* pcg_S = nullptr;         // nsb * 36: Jacobi-scaled lower blocks
+  double* pcg_scl = nullptr;       // n6: D^-1/2
+  double* pcg_P = nullptr;         // nf * 36: preconditioner blocks
+  double* pcg_Cinv = nullptr;      // nf * 36: inverse Cholesky factor of each scaled diagonal block
+  double* pcg_vec = nullptr;       // 5 * n6: x r p q z (scaled)
+  double* pcg_part = nullptr;      // pcg_grid * 4 partial dot products
+  unsigned* pcg_bar = nullptr;     // grid barrier: arrival count, generation
+  float* pcg_feat = nullptr;       // nf * kPcgFeat node features (learned correction)
+  float* pcg_ew = nullptr;         // edge weight (block Frobenius norm) of every full-row entry
+  float* pcg_h = nullptr;          // 2 * nf * kPcgHidden hidden states
+  float* pcg_msg = nullptr;        // nf * kPcgHidden aggregated messages
+  float* pcg_L = nullptr;          // nf * 21: learned correction factor (lower 6x6)
+  const uint16_t* pcg_w = nullptr; // BF16 weights of the learned correction (owned by a model), or null
 };
+
+// Parameters of the learned block preconditioner on one device: the FP32
+// master copy, the BF16 copy the kernels read, Adam moments and a gradient
+// buffer (training).
+struct PcgModel {
+  int device = 0;
+  float* w32 = nullptr;
+  uint16_t* wbf = nullptr;
+  float* m1 = nullptr;
+  float* m2 = nullptr;
+  float* grad = nullptr;
+  long long step = 0;
+};
+
+// Learned block preconditioner: node features, hidden width, message-passing layers.
+constexpr int kPcgFeat = 32;
+constexpr int kPcgHidden = 64;
+constexpr int kPcgLayers = 3;
+constexpr int kPcgOut = 21;
+// Parameter layout (FP32 master copy; the forward reads a BF16 copy):
+//   W_in [kPcgHidden x kPcgFeat], b_in [kPcgHidden],
+//   per layer: W_self [H x H], W_msg [H x H], b [H],
+//   W_out [kPcgOut x H], b_out [kPcgOut]
+constexpr int kPcgParams = kPcgHidden * kPcgFeat + kPcgHidden +
+                           kPcgLayers * (2 * kPcgHidden * kPcgHidden + kPcgHidden) + kPcgOut * kPcgHidden + kPcgOut;
 
 struct Sizes {
   int32_t nc, np, nf, nm;
@@ -206,6 +259,11 @@ struct Sizes {
   int band_c;         // its cluster size
   int band_ring;      // its row slots per CTA
   int lin_dd;          // float-float linearization (Jacobians, products and Z in float-float)
+  int pcg_mode;        // 0 exact factorization; 1 PCG, block-Jacobi; 2 PCG, learned correction (fallback: exact)
+  int pcg_max_iters;
+  double pcg_tol;      // relative residual of the Jacobi-scaled system
+  int pcg_grid;        // CTAs of the cooperative PCG kernel
+  int64_t pcg_nnzb;    // entries of the full block rows
   float lmk_well_tol;  // point blocks: FP32 Cholesky kept while every pivot keeps this fraction
   int lmk_list_grid;   // CTAs of the float-float redo of the other points
 };
@@ -221,6 +279,7 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
                      cudaStream_t st);
 int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st);
 int launch_factor_solve(const Sizes& s, const Dev& d, cudaStream_t st);
+int launch_exact_solve(const Sizes& s, const Dev& d, cudaStream_t st);  // the factorization alone
 int launch_update(const Sizes& s, const Dev& d, cudaStream_t st);
 int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st);
 
@@ -261,6 +320,20 @@ int band_launch_count();
 cudaError_t pair_totals(const Sizes& s, const Dev& d, int32_t* totals, cudaStream_t st);
 cudaError_t pair_fill(const Sizes& s, const Dev& d, const int32_t* bidmap, int64_t nb, const int64_t* block_begin,
                       int32_t nchunk, int32_t* table, cudaStream_t st);
+
+// PCG on the reduced system (sgba_pcg.cu): grid size for the cooperative
+// kernel (0 = cannot launch), and the launch chain (structure arrays uploaded
+// by the host).  The exact factorization that follows is skipped when PCG
+// converged (Ctrl::pcg_done).
+constexpr int kPcgMaxGrid = 2048;  // CTAs of the cooperative PCG kernel at most (partial-sum slots)
+int pcg_setup(int nf, int* grid);
+int launch_pcg(const Sizes& s, const Dev& d, cudaStream_t st);
+int pcg_launch_count(const Sizes& s);
+// The learned correction's forward pass (sgba_pcg_net.cu): node features,
+// embedding, message-passing layers and the output head into Dev::pcg_L.
+int pcg_net_setup();
+int launch_pcg_net(const Sizes& s, const Dev& d, cudaStream_t st);
+int pcg_net_launch_count();
 
 // Per-term Jacobians (2x6 pose, 2x3 point) of the given (camera, point) pairs
 // at the current variables, as the linearization kernels evaluate them:

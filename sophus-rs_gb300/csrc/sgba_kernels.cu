@@ -297,6 +297,7 @@ __global__ void k_pose_tables(int nc, const double* __restrict__ poses, float* _
     begin->max_grad_bits = 0ull;
     begin->max_step_bits = 0ull;
     begin->alpha = 0.0;
+    begin->pcg_done = 0;
     if (zero_count) *zero_count = 0;
   }
   int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1396,22 +1397,52 @@ struct BackArgs {
   const float* cvec;
   const float* xdd;  // dx_f as float-float pairs
   double* dm;
+  // scale gauge: the free poses' gauge direction v_f = [0; t_j - c] carried
+  // through the same back-substitution, u_m = -C^-T sum Z_g^T v_f (the
+  // projection's direction for the points)
+  int gauge_kind;
+  const double* poses;
+  double cx, cy, cz;
+  double* um;
 };
 
 __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
-  __shared__ float red[8][6][33];
+  __shared__ float red[8][12][33];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
+  const bool gauge = a.gauge_kind == 1;
   for (int64_t i = static_cast<int64_t>(blockIdx.x) * wpb + wib; i < a.np;
        i += static_cast<int64_t>(gridDim.x) * wpb) {
     const int mb = a.pt_mb[i];
     if (mb < 0) continue;
     dd t[3] = {dd_make(0.f, 0.f), dd_make(0.f, 0.f), dd_make(0.f, 0.f)};
+    dd tg[3] = {dd_make(0.f, 0.f), dd_make(0.f, 0.f), dd_make(0.f, 0.f)};  // sum Z^T v_f
     for (int64_t g = a.pt_g_begin[i] + lane; g < a.pt_g_begin[i + 1]; g += 32) {
-      const int fb = a.pose_fb[a.g_pose[g]];
+      const int pj = a.g_pose[g];
+      const int fb = a.pose_fb[pj];
       if (fb < 0) continue;
+      if (gauge) {
+        const double* T = a.poses + 7 * static_cast<int64_t>(pj);
+        const dd v3 = dd_from_double(T[4] - a.cx), v4 = dd_from_double(T[5] - a.cy), v5 = dd_from_double(T[6] - a.cz);
+        const float* zd = (a.zdd || a.zdd_flagged) ? (a.zdd ? a.zdd : a.zdd_flagged) + kZD * g : nullptr;
+        float Zf[20];
+        load_z(a.zmat, static_cast<int>(g), Zf);
+        const bool use_dd = a.zdd || (Zf[18] != 0.f && a.zdd_flagged);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          if (use_dd) {
+            tg[q] = dd_add(tg[q], dd_mul(v3, dd_make(zd[6 * 3 + 2 * q], zd[6 * 3 + 2 * q + 1])));
+            tg[q] = dd_add(tg[q], dd_mul(v4, dd_make(zd[6 * 4 + 2 * q], zd[6 * 4 + 2 * q + 1])));
+            tg[q] = dd_add(tg[q], dd_mul(v5, dd_make(zd[6 * 5 + 2 * q], zd[6 * 5 + 2 * q + 1])));
+          } else {
+            tg[q] = dd_add(tg[q], dd_mul_f(v3, Zf[3 * 3 + q]));
+            tg[q] = dd_add(tg[q], dd_mul_f(v4, Zf[4 * 3 + q]));
+            tg[q] = dd_add(tg[q], dd_mul_f(v5, Zf[5 * 3 + q]));
+          }
+        }
+      }
       const float2* xp = reinterpret_cast<const float2*>(a.xdd) + 6 * fb;
       if (a.zdd) {
         const float* zd = a.zdd + kZD * g;
@@ -1454,13 +1485,15 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
     for (int q = 0; q < 3; ++q) {
       red[wib][2 * q][lane] = t[q].hi;
       red[wib][2 * q + 1][lane] = t[q].lo;
+      red[wib][6 + 2 * q][lane] = tg[q].hi;
+      red[wib][6 + 2 * q + 1][lane] = tg[q].lo;
     }
     __syncwarp();
+    const int nq = gauge ? 6 : 3;
 #pragma unroll
     for (int h = 16; h > 0; h >>= 1) {
       if (lane < h) {
-#pragma unroll
-        for (int q = 0; q < 3; ++q) {
+        for (int q = 0; q < nq; ++q) {
           const dd u = dd_add(dd_make(red[wib][2 * q][lane], red[wib][2 * q + 1][lane]),
                               dd_make(red[wib][2 * q][lane + h], red[wib][2 * q + 1][lane + h]));
           red[wib][2 * q][lane] = u.hi;
@@ -1468,6 +1501,21 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
         }
       }
       __syncwarp();
+    }
+    if (lane == 0 && gauge) {
+      // u_m = -C^-T sum Z^T v_f
+      const float* cp = a.cinv + 12 * mb;
+      dd ci[6];
+      for (int k = 0; k < 6; ++k) ci[k] = dd_make(cp[2 * k], cp[2 * k + 1]);
+      const dd g0 = dd_make(red[wib][6][0], red[wib][7][0]);
+      const dd g1 = dd_make(red[wib][8][0], red[wib][9][0]);
+      const dd g2 = dd_make(red[wib][10][0], red[wib][11][0]);
+      const dd u0 = dd_add(dd_add(dd_mul(g0, ci[0]), dd_mul(g1, ci[1])), dd_mul(g2, ci[3]));
+      const dd u1 = dd_add(dd_mul(g1, ci[2]), dd_mul(g2, ci[4]));
+      const dd u2 = dd_mul(g2, ci[5]);
+      a.um[3 * mb + 0] = -dd_to_double(u0);
+      a.um[3 * mb + 1] = -dd_to_double(u1);
+      a.um[3 * mb + 2] = -dd_to_double(u2);
     }
     if (lane == 0) {
       dd s[3];
@@ -1496,8 +1544,14 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
 // points, s -> scale about c is an exact symmetry of the cost, so H v = 0 for
 // v = ([0; t_j - c] per free pose, p_i - c per point) and b . v = 0.  The exact
 // damped step therefore satisfies v^T D delta = 0, D = diag(n_terms).  The
-// FP32 assembly leaves a spurious component along v amplified by 1/(nu n);
-// removing the D-projection restores the exact-arithmetic step.
+// FP32 assembly leaves a spurious component in the pose step along the weak
+// direction v_f of S, amplified by 1/(nu n); the back-substitution carries it
+// into the points as u_m = -V^-1 W^T v_f.  For a point determined by its views
+// u_m = v_m to O(nu); for a point seen only by the constant camera u_m = 0, and
+// for a point seen once u_m lacks its depth component (its damped block
+// forgets the gauge direction there).  So the spurious part is alpha u with
+// u = (v_f, u_m), and alpha = v^T D delta / v^T D u removes it while keeping
+// the exact identity v^T D delta = 0.
 // ---------------------------------------------------------------------------
 struct GaugeArgs {
   int nf, nm;
@@ -1509,6 +1563,7 @@ struct GaugeArgs {
   const double* cnt_m;
   const double* xf;
   const double* dm;
+  const double* um;  // back-substituted gauge direction of the points
   double cx, cy, cz;
   double* part;  // 2 * gridDim
 };
@@ -1519,16 +1574,18 @@ __global__ void __launch_bounds__(256) k_gauge_partials(GaugeArgs a, const Ctrl*
   const int64_t n = static_cast<int64_t>(a.nf) + a.nm;
   for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n;
        t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    double v[3], d[3], w;
+    double v[3], u[3], d[3], w;
     if (t < a.nf) {
       const double* T = a.poses + 7 * a.fb_pose[t];
       v[0] = T[4] - a.cx; v[1] = T[5] - a.cy; v[2] = T[6] - a.cz;
+      u[0] = v[0]; u[1] = v[1]; u[2] = v[2];
       d[0] = a.xf[6 * t + 3]; d[1] = a.xf[6 * t + 4]; d[2] = a.xf[6 * t + 5];
       w = a.cnt_f[t];
     } else {
       const int mb = static_cast<int>(t - a.nf);
       const double* p = a.points + 3 * a.mb_pt[mb];
       v[0] = p[0] - a.cx; v[1] = p[1] - a.cy; v[2] = p[2] - a.cz;
+      u[0] = a.um[3 * mb]; u[1] = a.um[3 * mb + 1]; u[2] = a.um[3 * mb + 2];
       d[0] = a.dm[3 * mb]; d[1] = a.dm[3 * mb + 1]; d[2] = a.dm[3 * mb + 2];
       w = a.cnt_m[mb];
     }
@@ -1536,7 +1593,7 @@ __global__ void __launch_bounds__(256) k_gauge_partials(GaugeArgs a, const Ctrl*
     for (int k = 0; k < 3; ++k) {
       dd vk = dd_from_double(v[k]);
       num = dd_add(num, dd_mul(dd_mul(wd, vk), dd_from_double(d[k])));
-      den = dd_add(den, dd_mul(dd_mul(wd, vk), vk));
+      den = dd_add(den, dd_mul(dd_mul(wd, vk), dd_from_double(u[k])));
     }
   }
   __shared__ float sh[4][8];
@@ -1579,6 +1636,7 @@ struct UpdArgs {
   double* part;  // 2 * gridDim
   const double* gauge_part;  // 2 * gauge_blocks partial sums of the gauge projection
   int gauge_blocks;
+  const double* um;          // the points' part of the projection direction
   float* pose_f;   // trial pose tables, written here for the trial cost
   float* pose_dd;
 };
@@ -1645,8 +1703,12 @@ __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
         O[0] = p[0]; O[1] = p[1]; O[2] = p[2];
         continue;
       }
-      double d[3] = {a.dm[3 * mb] - alpha * (p[0] - a.cx), a.dm[3 * mb + 1] - alpha * (p[1] - a.cy),
-                     a.dm[3 * mb + 2] - alpha * (p[2] - a.cz)};
+      double d[3] = {a.dm[3 * mb], a.dm[3 * mb + 1], a.dm[3 * mb + 2]};
+      if (a.gauge_kind == 1) {
+        d[0] -= alpha * a.um[3 * mb];
+        d[1] -= alpha * a.um[3 * mb + 1];
+        d[2] -= alpha * a.um[3 * mb + 2];
+      }
       for (int k = 0; k < 3; ++k) {
         a.dm[3 * mb + k] = d[k];
         dd x = dd_from_double(d[k]);
@@ -1956,6 +2018,12 @@ static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
   b.cvec = d.cvec;
   b.xdd = d.xdd;
   b.dm = d.dm;
+  b.gauge_kind = s.gauge_kind;
+  b.poses = d.poses;
+  b.cx = s.gauge_center[0];
+  b.cy = s.gauge_center[1];
+  b.cz = s.gauge_center[2];
+  b.um = d.gauge_um;
   k_backsub<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(b, d.ctrl);
   return 1;
 }
@@ -2043,6 +2111,7 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
     g.cnt_m = d.cnt_m;
     g.xf = d.x;
     g.dm = d.dm;
+    g.um = d.gauge_um;
     g.cx = s.gauge_center[0];
     g.cy = s.gauge_center[1];
     g.cz = s.gauge_center[2];
@@ -2072,6 +2141,7 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
   u.part = d.part + 2 * kUpdBlocks;
   u.gauge_part = d.part;
   u.gauge_blocks = kUpdBlocks;
+  u.um = d.gauge_um;
   u.pose_f = d.pose_f;
   u.pose_dd = d.pose_dd;
   k_apply_update<<<kUpdBlocks, 256, 0, st>>>(u, d.ctrl);

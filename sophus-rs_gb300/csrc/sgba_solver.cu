@@ -27,7 +27,8 @@ constexpr int kPW = 48;  // panel width (multiple of the 6-dof pose block)
 constexpr float kTolRel = 1e-12f;
 constexpr int kRefineSteps = 1;
 
-__device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0; }
+// the factorization is skipped on termination, on a skipped step and when PCG converged
+__device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0 || c->pcg_done != 0; }
 
 __global__ void k_s_to_f32(int n, const double* __restrict__ S, float* __restrict__ A, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
@@ -267,14 +268,22 @@ __global__ void __launch_bounds__(256) k_residual(int n, const double* __restric
 }  // namespace
 
 int solver_launch_count(const Sizes& s) {
-  if (s.small_dense) return 1;
-  if (s.dense_c > 0) return 1;
-  if (s.band_c > 0) return band_launch_count();
+  const int pcg = s.pcg_mode ? pcg_launch_count(s) : 0;
+  if (s.small_dense) return pcg + 1;
+  if (s.dense_c > 0) return pcg + 1;
+  if (s.band_c > 0) return pcg + band_launch_count();
   const int panels = (s.n6 + kPW - 1) / kPW;
-  return 1 + 2 * panels + 1 + 2 * kRefineSteps;
+  return pcg + 1 + 2 * panels + 1 + 2 * kRefineSteps;
 }
 
 int launch_factor_solve(const Sizes& s, const Dev& d, cudaStream_t st) {
+  // PCG first when selected; the exact factorization below skips itself when
+  // PCG converged (Ctrl::pcg_done) and is the fallback otherwise
+  const int pcg = s.pcg_mode ? launch_pcg(s, d, st) : 0;
+  return pcg + launch_exact_solve(s, d, st);
+}
+
+int launch_exact_solve(const Sizes& s, const Dev& d, cudaStream_t st) {
   if (s.small_dense) return launch_small_dense(s, d, st);
   if (s.dense_c > 0) return launch_dense_cluster(s, d, st);
   if (s.band_c > 0) return launch_band(s, d, st);

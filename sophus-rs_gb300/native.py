@@ -117,12 +117,34 @@ class WindowResult(C.Structure):
     ]
 
 
+class LinearSolverC(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("max_iterations", C.c_int32), ("tolerance", C.c_double)]
+
+
+class PcgStats(C.Structure):
+    _fields_ = [
+        ("solves", C.c_int64),
+        ("fallbacks", C.c_int64),
+        ("iterations", C.c_int64),
+        ("last_iterations", C.c_int32),
+        ("last_status", C.c_int32),
+        ("last_relative_residual", C.c_double),
+    ]
+
+
+# sgba_linsolve_mode
+LINSOLVE_EXACT = 0
+LINSOLVE_PCG_BLOCK_JACOBI = 1
+LINSOLVE_PCG_LEARNED = 2
+
 EXPORTED = [
     "sgba_abi_version", "sgba_last_error", "sgba_problem_create", "sgba_problem_destroy",
     "sgba_optimizer_init", "sgba_optimizer_step", "sgba_optimize", "sgba_get_variables",
     "sgba_get_cost", "sgba_set_variables", "sgba_get_layout", "sgba_export_pattern",
     "sgba_debug_last_system", "sgba_debug_jacobians", "sgba_state_save", "sgba_state_load", "sgba_get_profile",
     "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_batch_optimize",
+    "sgba_set_linear_solver", "sgba_get_pcg_stats", "sgba_pcg_num_params", "sgba_pcg_model_create",
+    "sgba_pcg_model_destroy", "sgba_pcg_model_set_params", "sgba_pcg_model_get_params",
 ]
 
 # sgba_kernel_id
@@ -180,6 +202,14 @@ def lib():
     L.sgba_bench_kernel.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, dp]
     L.sgba_batch_optimize.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(OptParamsC),
                                       C.POINTER(IterRecord), C.c_int32, C.POINTER(WindowResult)]
+    L.sgba_set_linear_solver.argtypes = [C.c_void_p, C.POINTER(LinearSolverC), C.c_void_p]
+    L.sgba_get_pcg_stats.argtypes = [C.c_void_p, C.POINTER(PcgStats)]
+    L.sgba_pcg_num_params.restype = C.c_int32
+    L.sgba_pcg_model_create.argtypes = [C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)]
+    L.sgba_pcg_model_destroy.argtypes = [C.c_void_p]
+    fp = C.POINTER(C.c_float)
+    L.sgba_pcg_model_set_params.argtypes = [C.c_void_p, fp, C.c_int32]
+    L.sgba_pcg_model_get_params.argtypes = [C.c_void_p, fp, C.c_int32]
     _lib = L
     return L
 
@@ -346,6 +376,19 @@ class Problem:
                                          int(precision), _dptr(jp), _dptr(jm)))
         return jp, jm
 
+    def set_linear_solver(self, mode, max_iterations=50, tolerance=1e-8, model=None):
+        """Reduced-system solver: LINSOLVE_EXACT, LINSOLVE_PCG_BLOCK_JACOBI or
+        LINSOLVE_PCG_LEARNED (needs a PcgModel); PCG falls back to the exact
+        factorization when it misses the tolerance within max_iterations."""
+        cfg = LinearSolverC(int(mode), int(max_iterations), float(tolerance))
+        self._model = model  # kept alive while the problem uses it
+        check(lib().sgba_set_linear_solver(self._h, C.byref(cfg), model._h if model is not None else None))
+
+    def pcg_stats(self):
+        st = PcgStats()
+        check(lib().sgba_get_pcg_stats(self._h, C.byref(st)))
+        return st
+
     def state_save(self):
         size = C.c_size_t(0)
         check(lib().sgba_state_save(self._h, None, C.byref(size)))
@@ -396,3 +439,44 @@ def batch_optimize(problems, params):
         k = min(r.n_records, cap)
         out.append(([recs[w * cap + i] for i in range(k)], r.termination, r.ms, r.final_cost, r.status))
     return out
+
+
+class PcgModel:
+    """Parameters of the learned block preconditioner (sgba_pcg_model)."""
+
+    def __init__(self, device=0, seed=20261203, params=None):
+        h = C.c_void_p()
+        check(lib().sgba_pcg_model_create(int(device), C.c_uint64(seed), C.byref(h)))
+        self._h = h
+        if params is not None:
+            self.set_params(params)
+
+    @staticmethod
+    def num_params():
+        return int(lib().sgba_pcg_num_params())
+
+    def set_params(self, params):
+        w = np.ascontiguousarray(params, dtype=np.float32).ravel()
+        check(lib().sgba_pcg_model_set_params(self._h, w.ctypes.data_as(C.POINTER(C.c_float)), w.shape[0]))
+
+    def params(self):
+        w = np.empty(self.num_params(), np.float32)
+        check(lib().sgba_pcg_model_get_params(self._h, w.ctypes.data_as(C.POINTER(C.c_float)), w.shape[0]))
+        return w
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sgba_pcg_model_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
