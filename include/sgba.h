@@ -298,6 +298,40 @@ int sgba_pcg_model_destroy(sgba_pcg_model *m);
 int sgba_pcg_model_set_params(sgba_pcg_model *m, const float *params, int32_t n);
 int sgba_pcg_model_get_params(const sgba_pcg_model *m, float *params, int32_t n);
 
+/* Training of the learned preconditioner on reduced systems with their exact
+ * solutions (no counterpart in the reference).  Loss of one system:
+ * e = x* - P b, loss = e^T S e / x*^T S x* (Jacobi-scaled system), minimised
+ * by Adam over the FP32 master weights; forward and backward are this
+ * library's kernels (the forward is the inference arithmetic). */
+typedef struct sgba_pcg_trainset sgba_pcg_trainset;
+typedef struct {
+  int32_t epochs;
+  int32_t batch;          /* systems per Adam step */
+  double learning_rate;
+  uint64_t seed;          /* order of the systems in each epoch */
+} sgba_pcg_train_params;
+int sgba_pcg_trainset_create(int32_t device, sgba_pcg_trainset **out);
+int sgba_pcg_trainset_destroy(sgba_pcg_trainset *t);
+int32_t sgba_pcg_trainset_size(const sgba_pcg_trainset *t);
+/* Appends a system given on the host: the lower blocks (s_rows[k] >= s_cols[k],
+ * n_blocks x 36 doubles, row-major) of a Jacobi-scaled SPD S, b and the
+ * solution x of S x = b (6 nf each). */
+int sgba_pcg_trainset_add(sgba_pcg_trainset *t, int32_t nf, int64_t n_blocks, const int32_t *s_rows,
+                          const int32_t *s_cols, const double *blocks, const double *b, const double *x);
+/* Appends the reduced system of the problem's latest LM step, scaled, with
+ * its solution by the exact factorization. */
+int sgba_pcg_collect(sgba_problem *p, sgba_pcg_trainset *t);
+/* Loss of one system and (grad != NULL) its gradient w.r.t. the parameters. */
+int sgba_pcg_loss_grad(sgba_pcg_model *m, sgba_pcg_trainset *t, int32_t index, double *loss, float *grad,
+                       int32_t n_grad);
+/* Adam over the set; epoch_loss (NULL or tp->epochs entries): mean loss of
+ * each epoch, evaluated before each system's update. */
+int sgba_pcg_train(sgba_pcg_model *m, sgba_pcg_trainset *t, const sgba_pcg_train_params *tp, double *epoch_loss);
+/* PCG on a stored system: mode 1 block-Jacobi, 2 learned (model). */
+int sgba_pcg_evaluate(const sgba_pcg_model *m, sgba_pcg_trainset *t, int32_t index, int32_t mode,
+                      int32_t max_iterations, double tolerance, int32_t *iterations, double *relative_residual,
+                      int32_t *status);
+
 /* ---- allocation-free total cost (no counterpart in the reference) --------
  * calc_total_cost of the reprojection cost (the value sgba_get_cost reports,
  * float-float on the GPU) over observations that the caller already holds in

@@ -172,6 +172,21 @@ pub const SGBA_LINSOLVE_EXACT: i32 = 0;
 pub const SGBA_LINSOLVE_PCG_BLOCK_JACOBI: i32 = 1;
 pub const SGBA_LINSOLVE_PCG_LEARNED: i32 = 2;
 
+#[repr(C)]
+#[derive(Debug, Clone, Copy, Default)]
+pub struct sgba_pcg_train_params {
+    pub epochs: i32,
+    pub batch: i32,
+    pub learning_rate: f64,
+    pub seed: u64,
+}
+
+/// Opaque training set of the learned block preconditioner.
+#[repr(C)]
+pub struct sgba_pcg_trainset {
+    _private: [u8; 0],
+}
+
 /// Opaque parameters of the learned block preconditioner.
 #[repr(C)]
 pub struct sgba_pcg_model {
@@ -245,6 +260,45 @@ extern "C" {
     pub fn sgba_pcg_model_destroy(m: *mut sgba_pcg_model) -> c_int;
     pub fn sgba_pcg_model_set_params(m: *mut sgba_pcg_model, params: *const f32, n: i32) -> c_int;
     pub fn sgba_pcg_model_get_params(m: *const sgba_pcg_model, params: *mut f32, n: i32) -> c_int;
+    pub fn sgba_pcg_trainset_create(device: i32, out: *mut *mut sgba_pcg_trainset) -> c_int;
+    pub fn sgba_pcg_trainset_destroy(t: *mut sgba_pcg_trainset) -> c_int;
+    pub fn sgba_pcg_trainset_size(t: *const sgba_pcg_trainset) -> i32;
+    pub fn sgba_pcg_trainset_add(
+        t: *mut sgba_pcg_trainset,
+        nf: i32,
+        n_blocks: i64,
+        s_rows: *const i32,
+        s_cols: *const i32,
+        blocks: *const f64,
+        b: *const f64,
+        x: *const f64,
+    ) -> c_int;
+    pub fn sgba_pcg_collect(p: *mut sgba_problem, t: *mut sgba_pcg_trainset) -> c_int;
+    pub fn sgba_pcg_loss_grad(
+        m: *mut sgba_pcg_model,
+        t: *mut sgba_pcg_trainset,
+        index: i32,
+        loss: *mut f64,
+        grad: *mut f32,
+        n_grad: i32,
+    ) -> c_int;
+    pub fn sgba_pcg_train(
+        m: *mut sgba_pcg_model,
+        t: *mut sgba_pcg_trainset,
+        tp: *const sgba_pcg_train_params,
+        epoch_loss: *mut f64,
+    ) -> c_int;
+    pub fn sgba_pcg_evaluate(
+        m: *const sgba_pcg_model,
+        t: *mut sgba_pcg_trainset,
+        index: i32,
+        mode: i32,
+        max_iterations: i32,
+        tolerance: f64,
+        iterations: *mut i32,
+        relative_residual: *mut f64,
+        status: *mut i32,
+    ) -> c_int;
     pub fn sgba_total_cost_noalloc(
         n_cam: i32,
         poses: *const f64,

@@ -1491,7 +1491,8 @@ int pcg_alloc(sgba_problem* p) {
   if ((st = dev_alloc(p, &d.pcg_scl, n6))) return st;
   if ((st = dev_alloc(p, &d.pcg_P, 36 * nf))) return st;
   if ((st = dev_alloc(p, &d.pcg_Cinv, 36 * nf))) return st;
-  if ((st = dev_alloc(p, &d.pcg_vec, 5 * n6))) return st;
+  if ((st = dev_alloc(p, &d.pcg_vec, 6 * n6))) return st;
+  if ((st = dev_alloc(p, &d.pcg_S2, 36 * static_cast<size_t>(s.nsb)))) return st;
   if ((st = dev_alloc(p, &d.pcg_bar, 4))) return st;
   if ((st = dev_alloc(p, &d.pcg_part, 4 * static_cast<size_t>(sgba::kPcgMaxGrid)))) return st;
   if ((st = dev_alloc(p, &d.pcg_feat, nf * sgba::kPcgFeat))) return st;
@@ -1667,6 +1668,246 @@ int sgba_get_pcg_stats(sgba_problem* p, sgba_pcg_stats* out) {
   out->last_iterations = c.pcg_iters;
   out->last_status = c.pcg_status;
   out->last_relative_residual = c.pcg_relres;
+  return SGBA_OK;
+}
+
+// ---- training the learned preconditioner ----------------------------------
+
+struct sgba_pcg_trainset {
+  sgba::PcgTrainSet t;
+  cudaStream_t stream = nullptr;
+};
+
+namespace {
+
+// Device copy of one system; blocks64 / b / xs are device or host pointers
+// (kind = the cudaMemcpy direction from them).
+int trainset_append(sgba_pcg_trainset* h, const Plan* plan, int nf, const std::vector<int32_t>& sb_row,
+                    const std::vector<int32_t>& sb_col, const double* blocks64, const double* b, const double* xs,
+                    cudaMemcpyKind kind) {
+  sgba::PcgSystem s;
+  s.nf = nf;
+  s.nsb = static_cast<int64_t>(sb_row.size());
+  Plan tmp;
+  tmp.nf = nf;
+  tmp.sb_row = sb_row;
+  tmp.sb_col = sb_col;
+  std::vector<int32_t> rowptr, cols, blks, diag;
+  pcg_structure(plan ? *plan : tmp, &rowptr, &cols, &blks, &diag);
+  for (int j = 0; j < nf; ++j)
+    if (diag[j] < 0) return set_error(SGBA_ERR_INVALID_ARGUMENT, "block row %d has no diagonal block", j);
+  s.nnzb = static_cast<int64_t>(cols.size());
+  const size_t n6 = 6 * static_cast<size_t>(nf), nb = 36 * static_cast<size_t>(s.nsb);
+  auto fail = [&](cudaError_t e) {
+    cudaFree(s.rowptr); cudaFree(s.cols); cudaFree(s.blks); cudaFree(s.diag);
+    cudaFree(s.Sb); cudaFree(s.Sb2); cudaFree(s.b); cudaFree(s.xs);
+    return set_error(e == cudaErrorMemoryAllocation ? SGBA_ERR_OUT_OF_MEMORY : SGBA_ERR_CUDA, "training set: %s",
+                     cudaGetErrorString(e));
+  };
+  cudaError_t e;
+  if ((e = cudaMalloc(&s.rowptr, sizeof(int32_t) * rowptr.size())) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&s.cols, sizeof(int32_t) * std::max<size_t>(cols.size(), 1))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&s.blks, sizeof(int32_t) * std::max<size_t>(blks.size(), 1))) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&s.diag, sizeof(int32_t) * diag.size())) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&s.Sb, sizeof(double) * nb)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&s.Sb2, sizeof(float2) * nb)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&s.b, sizeof(double) * n6)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&s.xs, sizeof(double) * n6)) != cudaSuccess) return fail(e);
+  e = cudaMemcpy(s.rowptr, rowptr.data(), sizeof(int32_t) * rowptr.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(s.cols, cols.data(), sizeof(int32_t) * cols.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(s.blks, blks.data(), sizeof(int32_t) * blks.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(s.diag, diag.data(), sizeof(int32_t) * diag.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(s.Sb, blocks64, sizeof(double) * nb, kind);
+  if (e == cudaSuccess) e = cudaMemcpy(s.b, b, sizeof(double) * n6, kind);
+  if (e == cudaSuccess) e = cudaMemcpy(s.xs, xs, sizeof(double) * n6, kind);
+  if (e != cudaSuccess) return fail(e);
+  // float-float copy of the blocks and den = x* . b on the host
+  std::vector<double> hb(nb), hbv(n6), hx(n6);
+  e = cudaMemcpy(hb.data(), s.Sb, sizeof(double) * nb, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(hbv.data(), s.b, sizeof(double) * n6, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(hx.data(), s.xs, sizeof(double) * n6, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail(e);
+  std::vector<float2> h2(nb);
+  for (size_t i = 0; i < nb; ++i) {
+    if (!std::isfinite(hb[i])) { fail(cudaSuccess); return set_error(SGBA_ERR_INVALID_ARGUMENT, "non-finite block entry"); }
+    const float hi = static_cast<float>(hb[i]);
+    h2[i] = make_float2(hi, static_cast<float>(hb[i] - static_cast<double>(hi)));
+  }
+  if ((e = cudaMemcpy(s.Sb2, h2.data(), sizeof(float2) * nb, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e);
+  double den = 0.0;
+  for (size_t i = 0; i < n6; ++i) den += hx[i] * hbv[i];
+  if (!(den > 0.0) || !std::isfinite(den)) {
+    fail(cudaSuccess);
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "x* . b = %g: not a positive definite system's solution", den);
+  }
+  s.den = den;
+  h->t.sys.push_back(s);
+  return SGBA_OK;
+}
+
+}  // namespace
+
+int sgba_pcg_trainset_create(int32_t device, sgba_pcg_trainset** out) {
+  if (!out) return set_error(SGBA_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  int dev = device;
+  if (dev < 0) SGBA_CK(cudaGetDevice(&dev));
+  SGBA_CK(cudaSetDevice(dev));
+  std::unique_ptr<sgba_pcg_trainset> h(new (std::nothrow) sgba_pcg_trainset());
+  if (!h) return set_error(SGBA_ERR_OUT_OF_MEMORY, "host allocation failed");
+  h->t.device = dev;
+  SGBA_CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  *out = h.release();
+  return SGBA_OK;
+}
+
+int sgba_pcg_trainset_destroy(sgba_pcg_trainset* h) {
+  if (!h) return SGBA_OK;
+  cudaSetDevice(h->t.device);
+  if (h->stream) {
+    cudaStreamSynchronize(h->stream);
+    cudaStreamDestroy(h->stream);
+  }
+  delete h;
+  return SGBA_OK;
+}
+
+int32_t sgba_pcg_trainset_size(const sgba_pcg_trainset* h) { return h ? static_cast<int32_t>(h->t.sys.size()) : 0; }
+
+int sgba_pcg_trainset_add(sgba_pcg_trainset* h, int32_t nf, int64_t n_blocks, const int32_t* s_rows,
+                          const int32_t* s_cols, const double* blocks, const double* b, const double* x) {
+  if (!h || !s_rows || !s_cols || !blocks || !b || !x) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (nf < 1 || n_blocks < nf) return set_error(SGBA_ERR_INVALID_ARGUMENT, "bad system size");
+  std::vector<int32_t> r(s_rows, s_rows + n_blocks), c(s_cols, s_cols + n_blocks);
+  for (int64_t k = 0; k < n_blocks; ++k)
+    if (r[k] < 0 || r[k] >= nf || c[k] < 0 || c[k] > r[k])
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "block %lld: (%d, %d) is not a lower block of a %d-row system",
+                       static_cast<long long>(k), r[k], c[k], nf);
+  SGBA_CK(cudaSetDevice(h->t.device));
+  return trainset_append(h, nullptr, nf, r, c, blocks, b, x, cudaMemcpyHostToDevice);
+}
+
+int sgba_pcg_collect(sgba_problem* p, sgba_pcg_trainset* h) {
+  if (!p || !h) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!p->inited) return set_error(SGBA_ERR_STATE, "sgba_pcg_collect before sgba_optimizer_init");
+  if (h->t.device != p->device) return set_error(SGBA_ERR_INVALID_ARGUMENT, "training set on another device");
+  SGBA_CK(cudaSetDevice(p->device));
+  int st = pcg_alloc(p);
+  if (st) return st;
+  // the reduced system of the latest linearisation: its scaled blocks and
+  // its exact solution (the factorization, not the gauge-projected step)
+  const Ctrl* cz = nullptr;
+  (void)cz;
+  Ctrl c;
+  SGBA_CK(cudaMemcpyAsync(&c, p->d.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, p->stream));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  if (c.step < 1) return set_error(SGBA_ERR_STATE, "sgba_pcg_collect needs a step first");
+  Ctrl saved = c;
+  c.done = 0;
+  c.skip = 0;
+  c.pcg_done = 0;
+  SGBA_CK(cudaMemcpyAsync(p->d.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice, p->stream));
+  sgba::Sizes z = p->sz;
+  z.pcg_mode = 0;
+  sgba::launch_pcg_blocks_only(z, p->d, p->stream);
+  sgba::launch_exact_solve(z, p->d, p->stream);
+  SGBA_CK(cudaGetLastError());
+  Ctrl after;
+  SGBA_CK(cudaMemcpyAsync(&after, p->d.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, p->stream));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  SGBA_CK(cudaMemcpy(p->d.ctrl, &saved, sizeof(Ctrl), cudaMemcpyHostToDevice));
+  if (after.skip != 0) return set_error(SGBA_ERR_STATE, "the exact factorization failed on this system");
+  const size_t n6 = static_cast<size_t>(p->sz.n6);
+  std::vector<double> scl(n6), rb(n6), x(n6);
+  SGBA_CK(cudaMemcpy(scl.data(), p->d.pcg_scl, sizeof(double) * n6, cudaMemcpyDeviceToHost));
+  SGBA_CK(cudaMemcpy(rb.data(), p->d.rb, sizeof(double) * n6, cudaMemcpyDeviceToHost));
+  SGBA_CK(cudaMemcpy(x.data(), p->d.x, sizeof(double) * n6, cudaMemcpyDeviceToHost));
+  for (size_t i = 0; i < n6; ++i) {
+    rb[i] *= scl[i];  // b~ = D^-1/2 b
+    x[i] /= scl[i];   // x~ = D^1/2 x
+  }
+  std::vector<double> blocks(36 * static_cast<size_t>(p->sz.nsb));
+  SGBA_CK(cudaMemcpy(blocks.data(), p->d.pcg_S, sizeof(double) * blocks.size(), cudaMemcpyDeviceToHost));
+  SGBA_CK(cudaSetDevice(h->t.device));
+  return trainset_append(h, &p->plan, p->plan.nf, p->plan.sb_row, p->plan.sb_col, blocks.data(), rb.data(), x.data(),
+                         cudaMemcpyHostToDevice);
+}
+
+int sgba_pcg_loss_grad(sgba_pcg_model* m, sgba_pcg_trainset* h, int32_t index, double* loss, float* grad,
+                       int32_t n_grad) {
+  if (!m || !h || !loss) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (index < 0 || index >= static_cast<int32_t>(h->t.sys.size()))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "system %d of %zu", index, h->t.sys.size());
+  if (grad && n_grad != sgba::kPcgParams)
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "%d gradient entries (expected %d)", n_grad, sgba::kPcgParams);
+  if (m->m.device != h->t.device) return set_error(SGBA_ERR_INVALID_ARGUMENT, "model and training set on different devices");
+  SGBA_CK(cudaSetDevice(h->t.device));
+  SGBA_CK(cudaMemsetAsync(m->m.grad, 0, sizeof(float) * sgba::kPcgParams, h->stream));
+  SGBA_CK(sgba::pcg_loss_grad(m->m, h->t, index, grad != nullptr, loss, h->stream));
+  if (grad) {
+    SGBA_CK(cudaMemcpyAsync(grad, m->m.grad, sizeof(float) * sgba::kPcgParams, cudaMemcpyDeviceToHost, h->stream));
+    SGBA_CK(cudaMemsetAsync(m->m.grad, 0, sizeof(float) * sgba::kPcgParams, h->stream));
+    SGBA_CK(cudaStreamSynchronize(h->stream));
+  }
+  return SGBA_OK;
+}
+
+int sgba_pcg_train(sgba_pcg_model* m, sgba_pcg_trainset* h, const sgba_pcg_train_params* tp, double* epoch_loss) {
+  if (!m || !h || !tp) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  const int n = static_cast<int>(h->t.sys.size());
+  if (n < 1) return set_error(SGBA_ERR_INVALID_ARGUMENT, "empty training set");
+  if (tp->epochs < 1 || tp->batch < 1 || !(tp->learning_rate > 0.0))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "epochs, batch and learning_rate must be positive");
+  if (m->m.device != h->t.device) return set_error(SGBA_ERR_INVALID_ARGUMENT, "model and training set on different devices");
+  SGBA_CK(cudaSetDevice(h->t.device));
+  SGBA_CK(cudaMemsetAsync(m->m.grad, 0, sizeof(float) * sgba::kPcgParams, h->stream));
+  std::vector<int> order(n);
+  uint64_t rng = tp->seed;
+  auto next = [&rng]() {
+    uint64_t z = (rng += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+  };
+  for (int ep = 0; ep < tp->epochs; ++ep) {
+    for (int i = 0; i < n; ++i) order[i] = i;
+    for (int i = n - 1; i > 0; --i) std::swap(order[i], order[static_cast<int>(next() % (uint64_t)(i + 1))]);
+    double tot = 0.0;
+    int in_batch = 0;
+    for (int i = 0; i < n; ++i) {
+      double l = 0.0;
+      SGBA_CK(sgba::pcg_loss_grad(m->m, h->t, order[i], true, &l, h->stream));
+      tot += l;
+      if (++in_batch == tp->batch || i == n - 1) {
+        SGBA_CK(sgba::pcg_adam(m->m, 1.0f / static_cast<float>(in_batch), static_cast<float>(tp->learning_rate),
+                               0.9f, 0.999f, 1e-8f, h->stream));
+        in_batch = 0;
+      }
+    }
+    if (epoch_loss) epoch_loss[ep] = tot / n;
+  }
+  SGBA_CK(cudaStreamSynchronize(h->stream));
+  return SGBA_OK;
+}
+
+int sgba_pcg_evaluate(const sgba_pcg_model* m, sgba_pcg_trainset* h, int32_t index, int32_t mode,
+                      int32_t max_iterations, double tolerance, int32_t* iterations, double* relative_residual,
+                      int32_t* status) {
+  if (!h || !iterations || !relative_residual || !status) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (index < 0 || index >= static_cast<int32_t>(h->t.sys.size()))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "system %d of %zu", index, h->t.sys.size());
+  if (mode != SGBA_LINSOLVE_PCG_BLOCK_JACOBI && mode != SGBA_LINSOLVE_PCG_LEARNED)
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "mode must be 1 or 2");
+  if (mode == SGBA_LINSOLVE_PCG_LEARNED && !m) return set_error(SGBA_ERR_INVALID_ARGUMENT, "mode 2 needs a model");
+  if (max_iterations < 1 || !(tolerance > 0.0)) return set_error(SGBA_ERR_INVALID_ARGUMENT, "bad iteration cap or tolerance");
+  SGBA_CK(cudaSetDevice(h->t.device));
+  int it = 0, stt = 0;
+  double rr = 0.0;
+  SGBA_CK(sgba::pcg_evaluate(m ? &m->m : nullptr, h->t, index, mode, max_iterations, tolerance, &it, &rr, &stt,
+                             h->stream));
+  *iterations = it;
+  *relative_residual = rr;
+  *status = stt;
   return SGBA_OK;
 }
 

@@ -203,10 +203,11 @@ struct Dev {
   int32_t* pcg_blks = nullptr;     // lower block id of each entry; bit 31 set: use its transpose
   int32_t* pcg_diag = nullptr;     // nf: lower block id of each diagonal block
   double* pcg_S = nullptr;         // nsb * 36: Jacobi-scaled lower blocks
+  float2* pcg_S2 = nullptr;        // nsb * 36: the same as float-float pairs (the PCG products)
   double* pcg_scl = nullptr;       // n6: D^-1/2
   double* pcg_P = nullptr;         // nf * 36: preconditioner blocks
   double* pcg_Cinv = nullptr;      // nf * 36: inverse Cholesky factor of each scaled diagonal block
-  double* pcg_vec = nullptr;       // 5 * n6: x r p q z (scaled)
+  double* pcg_vec = nullptr;       // 6 * n6: x r u p s w (scaled)
   double* pcg_part = nullptr;      // pcg_grid * 4 partial dot products
   unsigned* pcg_bar = nullptr;     // grid barrier: arrival count, generation
   float* pcg_feat = nullptr;       // nf * kPcgFeat node features (learned correction)
@@ -228,6 +229,48 @@ struct PcgModel {
   float* m2 = nullptr;
   float* grad = nullptr;
   long long step = 0;
+};
+
+// One reduced system of a training set (device arrays): the full block rows
+// of S~ (Jacobi-scaled), b~ and the exact solution x*; den = x*^T b~.
+struct PcgSystem {
+  int nf = 0;
+  int64_t nsb = 0, nnzb = 0;
+  int32_t* rowptr = nullptr;
+  int32_t* cols = nullptr;
+  int32_t* blks = nullptr;
+  int32_t* diag = nullptr;
+  double* Sb = nullptr;
+  float2* Sb2 = nullptr;
+  double* b = nullptr;
+  double* xs = nullptr;
+  double den = 0.0;
+};
+
+// Training set and the training / evaluation workspace (sized for the
+// largest system).
+struct PcgTrainSet {
+  int device = 0;
+  std::vector<PcgSystem> sys;
+  std::vector<void*> ws;
+  int cap_nf = 0;
+  int64_t cap_nnzb = 0;
+  float *feat = nullptr, *ew = nullptr, *wsum = nullptr, *Hs = nullptr, *Ms = nullptr, *Us = nullptr, *L = nullptr;
+  double *P = nullptr, *Ci = nullptr, *evec = nullptr, *Se = nullptr, *loss_part = nullptr, *loss = nullptr;
+  float *dL = nullptr, *dHa = nullptr, *dHb = nullptr, *dU = nullptr, *dM = nullptr, *dHp = nullptr;
+  float* hbuf = nullptr;
+  double* vec = nullptr;
+  double* part = nullptr;
+  unsigned* bar = nullptr;
+  Ctrl* ctrl = nullptr;
+  double* xout = nullptr;
+  float* xdd = nullptr;
+  PcgTrainSet() = default;
+  PcgTrainSet(const PcgTrainSet&) = delete;
+  PcgTrainSet& operator=(const PcgTrainSet&) = delete;
+  ~PcgTrainSet();
+  cudaError_t reserve(int nf, int64_t nnzb);
+  void free_workspace();
 };
 
 // Learned block preconditioner: node features, hidden width, message-passing layers.
@@ -328,12 +371,25 @@ cudaError_t pair_fill(const Sizes& s, const Dev& d, const int32_t* bidmap, int64
 constexpr int kPcgMaxGrid = 2048;  // CTAs of the cooperative PCG kernel at most (partial-sum slots)
 int pcg_setup(int nf, int* grid);
 int launch_pcg(const Sizes& s, const Dev& d, cudaStream_t st);
+// The same after the scaled blocks exist (pcg_S, pcg_S2; d.rb already scaled
+// when d.pcg_scl is null): network, preconditioner, solve.
+int launch_pcg_scaled(const Sizes& s, const Dev& d, cudaStream_t st);
+// Only the Jacobi-scaled blocks (pcg_S, pcg_S2, pcg_scl) from the dense S.
+int launch_pcg_blocks_only(const Sizes& s, const Dev& d, cudaStream_t st);
 int pcg_launch_count(const Sizes& s);
 // The learned correction's forward pass (sgba_pcg_net.cu): node features,
 // embedding, message-passing layers and the output head into Dev::pcg_L.
 int pcg_net_setup();
 int launch_pcg_net(const Sizes& s, const Dev& d, cudaStream_t st);
 int pcg_net_launch_count();
+// Training (sgba_pcg_net.cu): forward (and backward, accumulating into
+// m.grad) on system idx, *loss synchronously when non-null; one Adam step
+// (gradients scaled by `scale`, then zeroed); PCG on a stored system
+// (mode 1 block-Jacobi, 2 learned).
+cudaError_t pcg_loss_grad(PcgModel& m, PcgTrainSet& t, int idx, bool backward, double* loss, cudaStream_t st);
+cudaError_t pcg_adam(PcgModel& m, float scale, float lr, float b1, float b2, float eps, cudaStream_t st);
+cudaError_t pcg_evaluate(const PcgModel* m, PcgTrainSet& t, int idx, int mode, int max_iters, double tol,
+                         int* iters, double* relres, int* status, cudaStream_t st);
 
 // Per-term Jacobians (2x6 pose, 2x3 point) of the given (camera, point) pairs
 // at the current variables, as the linearization kernels evaluate them:

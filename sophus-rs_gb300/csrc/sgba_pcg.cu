@@ -9,7 +9,8 @@
 //   * a block preconditioner per free pose: P_j = C_j^-T (I + L_j L_j^T) C_j^-1
 //     with C_j the Cholesky factor of the 6x6 diagonal block of S~ (L_j = 0 is
 //     block-Jacobi; L_j comes from the learned network, sgba_pcg_net.cu);
-//   * CG in FP64 in one cooperative launch (grid barriers with bounded waits);
+//   * CG with FP64 vectors and a float-float matrix-vector product, in one
+//     cooperative launch (grid barriers with bounded waits);
 //     converged when |b~ - S~ x~| <= tol |b~|.  If it is not converged after
 //     max_iters iterations (or breaks down, or a barrier wait gives up), the
 //     exact factorization that follows in the same iteration runs as usual;
@@ -23,16 +24,35 @@
 
 #include "sgba_dd.cuh"
 #include "sgba_internal.h"
+#include "sgba_pcg_dev.cuh"
 
 namespace sgba {
 
 namespace {
 
-constexpr int kPT = 256;                  // threads per CTA
+constexpr int kPT = 512;                  // threads per CTA
 constexpr int kPW = kPT / 32;             // warps per CTA
 constexpr long long kBarSpins = 1ll << 22;  // x ~256 ns sleeps: a barrier wait gives up after ~1 s
 
 __device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0; }
+
+// Float-float dot-product accumulator: the running sum through an exact
+// TwoSum, the rounding errors of products and sums gathered in the lo part.
+struct Acc {
+  float hi, lo;
+};
+__device__ __forceinline__ void acc_madd(Acc& a, dd x, dd y) {
+  const float pr = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -pr);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  const float s = __fadd_rn(a.hi, pr);
+  const float bb = __fsub_rn(s, a.hi);
+  const float err = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(pr, bb));
+  a.hi = s;
+  a.lo = __fadd_rn(a.lo, __fadd_rn(err, e));
+}
+__device__ __forceinline__ dd acc_get(const Acc& a) { return dd_fast_two_sum(a.hi, a.lo); }
 
 struct PcgArgs {
   int nf, n6;
@@ -47,12 +67,13 @@ struct PcgArgs {
   const double* rb;    // reduced right-hand side (unscaled)
   double* scl;
   double* Sb;
+  float2* Sb2;         // the same blocks as float-float (hi, lo) pairs
   double* P;
   double* Cinv;
   const float* L;      // learned correction (nf * 21) or null
-  double* vec;         // x r p q z
+  double* vec;         // x r u p s w
   double* part;
-  unsigned* bar;       // [0] arrivals, [1] generation, [2] abort flag
+  unsigned* bar;       // [0] arrivals (monotonic within a launch), [2] abort flag
   double* xout;
   float* xdd;
   int max_iters;
@@ -73,89 +94,15 @@ __global__ void __launch_bounds__(kPT) k_pcg_blocks(PcgArgs a, const Ctrl* ctrl)
     const double dr = a.S[static_cast<int64_t>(r) * a.n6 + r], dc = a.S[static_cast<int64_t>(c) * a.n6 + c];
     const double sr = (dr > 0.0 && isfinite(dr)) ? 1.0 / sqrt(dr) : 1.0;
     const double sc = (dc > 0.0 && isfinite(dc)) ? 1.0 / sqrt(dc) : 1.0;
-    a.Sb[t] = a.S[static_cast<int64_t>(r) * a.n6 + c] * sr * sc;
+    const double v = a.S[static_cast<int64_t>(r) * a.n6 + c] * sr * sc;
+    a.Sb[t] = v;
+    const dd vd = dd_from_double(v);
+    a.Sb2[t] = make_float2(vd.hi, vd.lo);
     if (r == c) a.scl[r] = sr;
   }
 }
 
-// 6x6 Cholesky B = C C^T (lower, f64); false if a pivot is not positive.
-__device__ bool chol6(const double* B, double* C) {
-  for (int k = 0; k < 36; ++k) C[k] = 0.0;
-  for (int j = 0; j < 6; ++j) {
-    double d = B[j * 6 + j];
-    for (int k = 0; k < j; ++k) d -= C[j * 6 + k] * C[j * 6 + k];
-    if (!(d > 0.0) || !isfinite(d)) return false;
-    const double cjj = sqrt(d);
-    C[j * 6 + j] = cjj;
-    for (int i = j + 1; i < 6; ++i) {
-      double v = B[i * 6 + j];
-      for (int k = 0; k < j; ++k) v -= C[i * 6 + k] * C[j * 6 + k];
-      C[i * 6 + j] = v / cjj;
-    }
-  }
-  return true;
-}
-
-// Inverse of a lower-triangular 6x6 (lower).
-__device__ void trinv6(const double* C, double* X) {
-  for (int k = 0; k < 36; ++k) X[k] = 0.0;
-  for (int j = 0; j < 6; ++j) {
-    X[j * 6 + j] = 1.0 / C[j * 6 + j];
-    for (int i = j + 1; i < 6; ++i) {
-      double v = 0.0;
-      for (int k = j; k < i; ++k) v -= C[i * 6 + k] * X[k * 6 + j];
-      X[i * 6 + j] = v / C[i * 6 + i];
-    }
-  }
-}
-
 }  // namespace
-
-// P_j = Ci^T (I + L L^T) Ci with Ci = C^-1 (C C^T = diagonal block of S~).
-// Shared with the training code: the same arithmetic builds the training
-// preconditioner.
-__device__ void pcg_precond_block(const double* B, const float* Lrow, double* P, double* Ci) {
-  double C[36];
-  if (!chol6(B, C)) {
-    for (int k = 0; k < 36; ++k) {
-      P[k] = (k % 7 == 0) ? 1.0 : 0.0;
-      Ci[k] = P[k];
-    }
-    return;
-  }
-  trinv6(C, Ci);
-  double M[36];
-  for (int i = 0; i < 6; ++i)
-    for (int j = 0; j < 6; ++j) M[i * 6 + j] = (i == j) ? 1.0 : 0.0;
-  if (Lrow) {
-    // L lower 6x6 packed row-wise: (0,0) (1,0) (1,1) (2,0) ...
-    double Lf[36];
-    for (int k = 0; k < 36; ++k) Lf[k] = 0.0;
-    int t = 0;
-    for (int i = 0; i < 6; ++i)
-      for (int j = 0; j <= i; ++j) Lf[i * 6 + j] = static_cast<double>(Lrow[t++]);
-    for (int i = 0; i < 6; ++i)
-      for (int j = 0; j < 6; ++j) {
-        double v = 0.0;
-        for (int k = 0; k < 6; ++k) v += Lf[i * 6 + k] * Lf[j * 6 + k];
-        M[i * 6 + j] += v;
-      }
-  }
-  // P = Ci^T M Ci
-  double T[36];
-  for (int i = 0; i < 6; ++i)
-    for (int j = 0; j < 6; ++j) {
-      double v = 0.0;
-      for (int k = 0; k < 6; ++k) v += M[i * 6 + k] * Ci[k * 6 + j];
-      T[i * 6 + j] = v;
-    }
-  for (int i = 0; i < 6; ++i)
-    for (int j = 0; j < 6; ++j) {
-      double v = 0.0;
-      for (int k = 0; k < 6; ++k) v += Ci[k * 6 + i] * T[k * 6 + j];
-      P[i * 6 + j] = v;
-    }
-}
 
 namespace {
 
@@ -169,229 +116,247 @@ __global__ void __launch_bounds__(128) k_pcg_precond(PcgArgs a, const Ctrl* ctrl
 
 // ------------------------------------------------------------------ solve ---
 
-// Grid barrier for a cooperative launch.  Every wait is bounded: after
-// kBarSpins sleeps the CTA sets the abort flag and returns false; every CTA
-// also returns false once it sees the flag, so no CTA waits twice for a CTA
-// that has left.
-__device__ bool grid_barrier(unsigned* bar, unsigned nblocks) {
+// Grid barrier for a cooperative launch: a monotonic arrival counter; the
+// k-th barrier of a launch waits until k * gridDim CTAs have arrived (the
+// counter is zeroed before the launch).  Every wait is bounded: after
+// kBarSpins polls the CTA sets the abort flag and returns false; every CTA
+// also returns false once it sees the flag.
+__device__ bool grid_barrier(unsigned* bar, unsigned target) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned* vb = bar;
-    const unsigned gen = vb[1];
     __threadfence();
+    atomicAdd(bar, 1u);
     int ok = 1;
-    if (atomicAdd(bar, 1u) == nblocks - 1) {
-      bar[0] = 0u;
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      long long spins = 0;
-      while (vb[1] == gen) {
-        if (vb[2] != 0u) { ok = 0; break; }
-        if (++spins > kBarSpins) {
-          atomicExch(bar + 2, 1u);
-          ok = 0;
-          break;
-        }
-        __nanosleep(256);
+    long long spins = 0;
+    unsigned v;
+    for (;;) {
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+      if (v >= target) break;
+      unsigned ab;
+      asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(ab) : "l"(bar + 2) : "memory");
+      if (ab != 0u) { ok = 0; break; }
+      if (++spins > kBarSpins) {
+        atomicExch(bar + 2, 1u);
+        ok = 0;
+        break;
       }
+      if (spins > 64) __nanosleep(64);
     }
     __threadfence();
-    if (vb[2] != 0u) ok = 0;
     s_ok = ok;
   }
   __syncthreads();
   return s_ok != 0;
 }
 
-// Sum of one partial per CTA (slot k of 4), the same fixed order in every CTA.
-__device__ double sum_parts(const double* part, int k) {
-  __shared__ double s_sum;
+// Sum of one partial per CTA (slot k of kSlots), the same fixed order in
+// every CTA.
+constexpr int kSlots = 4;
+__device__ void sum_parts3(const double* part, double* out) {
+  __shared__ double s_sum[3];
   if (threadIdx.x < 32) {
-    double v = 0.0;
-    for (int g = threadIdx.x; g < static_cast<int>(gridDim.x); g += 32) v += __ldcg(part + 4 * g + k);
-    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-    if (threadIdx.x == 0) s_sum = v;
+    double v0 = 0.0, v1 = 0.0, v2 = 0.0;
+    for (int g = threadIdx.x; g < static_cast<int>(gridDim.x); g += 32) {
+      v0 += __ldcg(part + kSlots * g + 0);
+      v1 += __ldcg(part + kSlots * g + 1);
+      v2 += __ldcg(part + kSlots * g + 2);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      v0 += __shfl_down_sync(0xffffffffu, v0, off);
+      v1 += __shfl_down_sync(0xffffffffu, v1, off);
+      v2 += __shfl_down_sync(0xffffffffu, v2, off);
+    }
+    if (threadIdx.x == 0) {
+      s_sum[0] = v0;
+      s_sum[1] = v1;
+      s_sum[2] = v2;
+    }
   }
   __syncthreads();
-  const double r = s_sum;
+  out[0] = s_sum[0];
+  out[1] = s_sum[1];
+  out[2] = s_sum[2];
   __syncthreads();
-  return r;
 }
 
-// Per-CTA partials: warp sums (lane 0 of each warp holds them) combined in
-// warp order and written to part[4 * blockIdx + k].
-__device__ void write_parts(double* part, double v0, double v1, int k0, int k1) {
-  __shared__ double s0[kPW], s1[kPW];
+// Per-CTA partials of three dot products: warp sums combined in warp order.
+__device__ void write_parts3(double* part, double v0, double v1, double v2) {
+  __shared__ double s[3][kPW];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int off = 16; off > 0; off >>= 1) {
     v0 += __shfl_down_sync(0xffffffffu, v0, off);
     v1 += __shfl_down_sync(0xffffffffu, v1, off);
+    v2 += __shfl_down_sync(0xffffffffu, v2, off);
   }
   if (lane == 0) {
-    s0[w] = v0;
-    s1[w] = v1;
+    s[0][w] = v0;
+    s[1][w] = v1;
+    s[2][w] = v2;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    double t0 = 0.0, t1 = 0.0;
-    for (int q = 0; q < kPW; ++q) {
-      t0 += s0[q];
-      t1 += s1[q];
-    }
-    part[4 * blockIdx.x + k0] = t0;
-    if (k1 >= 0) part[4 * blockIdx.x + k1] = t1;
+  if (threadIdx.x < 3) {
+    double t = 0.0;
+    for (int q = 0; q < kPW; ++q) t += s[threadIdx.x][q];
+    part[kSlots * blockIdx.x + threadIdx.x] = t;
   }
 }
 
-// q_j = sum over the full block row j of S~_jk p_k: lanes take entries, each
-// lane forms all six rows of its block product, then a fixed shuffle tree.
-__device__ __forceinline__ void block_row_matvec(const PcgArgs& a, int j, const double* p, double* q6) {
+// w_j = sum over the full block row j of S~_jk u_k in float-float (the blocks
+// as (hi, lo) FP32 pairs: FP64 runs at 1/64 of the FP32 rate here): lanes
+// take entries, each lane forms the six rows of its block product, then a
+// fixed shuffle tree.  Returns the six sums in every lane.
+__device__ __forceinline__ void block_row_matvec(const PcgArgs& a, int j, const double* u, double* w6) {
   const int lane = threadIdx.x & 31;
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  Acc acc[6];
+#pragma unroll
+  for (int r = 0; r < 6; ++r) acc[r] = Acc{0.0f, 0.0f};
   for (int e = a.rowptr[j] + lane; e < a.rowptr[j + 1]; e += 32) {
     const int k = a.cols[e];
     const int bi = a.blks[e];
     const bool tr = bi < 0;
-    const double* B = a.Sb + 36 * static_cast<int64_t>(bi & 0x7fffffff);
-    double pk[6];
+    const float4* B4 = reinterpret_cast<const float4*>(a.Sb2 + 36 * static_cast<int64_t>(bi & 0x7fffffff));
+    dd uk[6];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) pk[c] = __ldcg(p + 6 * k + c);
-    if (!tr) {
+    for (int c = 0; c < 6; ++c) uk[c] = dd_from_double(__ldcg(u + 6 * k + c));
 #pragma unroll
-      for (int r = 0; r < 6; ++r)
+    for (int h = 0; h < 18; ++h) {
+      const float4 v = B4[h];  // entries 2h, 2h + 1 as (hi, lo)
 #pragma unroll
-        for (int c = 0; c < 6; ++c) acc[r] = fma(B[r * 6 + c], pk[c], acc[r]);
-    } else {
-#pragma unroll
-      for (int r = 0; r < 6; ++r)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) acc[r] = fma(B[c * 6 + r], pk[c], acc[r]);
+      for (int q = 0; q < 2; ++q) {
+        const int t = 2 * h + q;
+        const int rr = tr ? t % 6 : t / 6, cc = tr ? t / 6 : t % 6;
+        acc_madd(acc[rr], q ? dd_make(v.z, v.w) : dd_make(v.x, v.y), uk[cc]);
+      }
     }
   }
 #pragma unroll
-  for (int r = 0; r < 6; ++r)
-    for (int off = 16; off > 0; off >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], off);
-#pragma unroll
-  for (int r = 0; r < 6; ++r) q6[r] = acc[r];
+  for (int r = 0; r < 6; ++r) {
+    dd t = acc_get(acc[r]);
+    for (int off = 16; off > 0; off >>= 1)
+      t = dd_add(t, dd_make(__shfl_xor_sync(0xffffffffu, t.hi, off), __shfl_xor_sync(0xffffffffu, t.lo, off)));
+    w6[r] = dd_to_double(t);
+  }
 }
 
+// z = P_j r_j for the row's six entries (lane < 6 holds r_{6j+lane}).
+__device__ __forceinline__ double precond_row(const PcgArgs& a, int j, double rv) {
+  const int lane = threadIdx.x & 31;
+  double zv = 0.0;
+#pragma unroll
+  for (int c = 0; c < 6; ++c) {
+    const double rc = __shfl_sync(0xffffffffu, rv, c);
+    if (lane < 6) zv = fma(a.P[36 * static_cast<int64_t>(j) + lane * 6 + c], rc, zv);
+  }
+  return zv;
+}
+
+// PCG in the single-reduction form of Chronopoulos and Gear ("s-step
+// iterative methods for symmetric linear systems", 1989): one matrix-vector
+// product and one fused reduction of (r, u), (w, u), (r, r) per iteration,
+// two grid barriers.  x~ solves S~ x~ = b~ (Jacobi-scaled).
 __global__ void __launch_bounds__(kPT) k_pcg_solve(PcgArgs a, Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   const int lane = threadIdx.x & 31;
   const int gw = blockIdx.x * kPW + (threadIdx.x >> 5);
   const int nw = gridDim.x * kPW;
   const unsigned nb = gridDim.x;
+  unsigned nbar = 0;
   double* x = a.vec;
   double* r = a.vec + a.n6;
-  double* p = a.vec + 2 * a.n6;
-  double* q = a.vec + 3 * a.n6;
-  double* z = a.vec + 4 * a.n6;
-  // x = 0, r = b~, z = P r, p = z
-  double rz = 0.0, bb = 0.0;
+  double* u = a.vec + 2 * a.n6;
+  double* p = a.vec + 3 * a.n6;
+  double* sv = a.vec + 4 * a.n6;  // s = S~ p
+  double* w = a.vec + 5 * a.n6;   // w = S~ u
+  // x = 0, r = b~, u = P r
   for (int j = gw; j < a.nf; j += nw) {
     double rv = 0.0;
     if (lane < 6) {
       const int i = 6 * j + lane;
-      rv = a.scl[i] * a.rb[i];
+      rv = (a.scl ? a.scl[i] : 1.0) * a.rb[i];
       x[i] = 0.0;
       r[i] = rv;
+      p[i] = 0.0;
+      sv[i] = 0.0;
     }
-    double zv = 0.0;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      const double rc = __shfl_sync(0xffffffffu, rv, c);
-      if (lane < 6) zv = fma(a.P[36 * static_cast<int64_t>(j) + lane * 6 + c], rc, zv);
-    }
-    if (lane < 6) {
-      const int i = 6 * j + lane;
-      z[i] = zv;
-      p[i] = zv;
-      rz += rv * zv;
-      bb += rv * rv;
-    }
+    const double zv = precond_row(a, j, rv);
+    if (lane < 6) u[6 * j + lane] = zv;
   }
-  write_parts(a.part, rz, bb, 0, 1);
-  bool ok = grid_barrier(a.bar, nb);
-  double rho = ok ? sum_parts(a.part, 0) : 0.0;
-  const double bnorm2 = ok ? sum_parts(a.part, 1) : 0.0;
+  bool ok = grid_barrier(a.bar, (++nbar) * nb);
+  double gamma = 0.0, alpha = 0.0, bnorm2 = 0.0, rr = 0.0;
   int it = 0;
   int status = ok ? 1 : 3;
-  double rr = bnorm2;
-  if (ok && !(bnorm2 > 0.0)) status = 0;  // b = 0: x = 0 is exact
-  const double tol2 = a.tol * a.tol * bnorm2;
-  while (ok && status == 1 && it < a.max_iters) {
-    // q = S~ p, p.q
-    double pq = 0.0;
+  for (;;) {
+    if (!ok) { status = 3; break; }
+    // w = S~ u; dots (r, u), (w, u), (r, r)
+    double ru = 0.0, wu = 0.0, r2 = 0.0;
     for (int j = gw; j < a.nf; j += nw) {
-      double q6[6];
-      block_row_matvec(a, j, p, q6);
+      double w6[6];
+      block_row_matvec(a, j, u, w6);
       if (lane < 6) {
         const int i = 6 * j + lane;
-        const double qv = q6[lane];
-        q[i] = qv;
-        pq += __ldcg(p + i) * qv;
+        const double wv = w6[lane], uv = u[i], rv = r[i];
+        w[i] = wv;
+        ru += rv * uv;
+        wu += wv * uv;
+        r2 += rv * rv;
       }
     }
-    write_parts(a.part, pq, 0.0, 2, -1);
-    if (!(ok = grid_barrier(a.bar, nb))) { status = 3; break; }
-    const double pqs = sum_parts(a.part, 2);
-    if (!(pqs > 0.0) || !isfinite(pqs)) { status = 2; break; }
-    const double alpha = rho / pqs;
-    // x += alpha p, r -= alpha q, z = P r
-    double rzn = 0.0, rrn = 0.0;
+    write_parts3(a.part, ru, wu, r2);
+    if (!(ok = grid_barrier(a.bar, (++nbar) * nb))) { status = 3; break; }
+    double sums[3];
+    sum_parts3(a.part, sums);
+    const double gamma_n = sums[0], delta = sums[1];
+    rr = sums[2];
+    if (it == 0) bnorm2 = rr;
+    if (!(bnorm2 > 0.0)) { status = 0; break; }  // b = 0: x = 0 is exact
+    if (rr <= a.tol * a.tol * bnorm2) { status = 0; break; }
+    if (it >= a.max_iters) { status = 1; break; }
+    double beta;
+    if (it == 0) {
+      beta = 0.0;
+      alpha = gamma_n / delta;
+    } else {
+      beta = gamma_n / gamma;
+      alpha = gamma_n / (delta - beta * gamma_n / alpha);
+    }
+    gamma = gamma_n;
+    if (!(alpha > 0.0) || !isfinite(alpha) || !(gamma_n > 0.0)) { status = 2; break; }
+    // p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s, u = P r
     for (int j = gw; j < a.nf; j += nw) {
       double rv = 0.0;
       if (lane < 6) {
         const int i = 6 * j + lane;
-        x[i] = fma(alpha, p[i], x[i]);
-        rv = fma(-alpha, q[i], r[i]);
+        const double pv = fma(beta, p[i], u[i]);
+        const double sn = fma(beta, sv[i], w[i]);
+        p[i] = pv;
+        sv[i] = sn;
+        x[i] = fma(alpha, pv, x[i]);
+        rv = fma(-alpha, sn, r[i]);
         r[i] = rv;
       }
-      double zv = 0.0;
-#pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        const double rc = __shfl_sync(0xffffffffu, rv, c);
-        if (lane < 6) zv = fma(a.P[36 * static_cast<int64_t>(j) + lane * 6 + c], rc, zv);
-      }
-      if (lane < 6) {
-        z[6 * j + lane] = zv;
-        rzn += rv * zv;
-        rrn += rv * rv;
-      }
+      const double zv = precond_row(a, j, rv);
+      if (lane < 6) u[6 * j + lane] = zv;
     }
-    write_parts(a.part, rzn, rrn, 0, 1);
-    if (!(ok = grid_barrier(a.bar, nb))) { status = 3; break; }
-    const double rho_n = sum_parts(a.part, 0);
-    rr = sum_parts(a.part, 1);
     ++it;
-    if (rr <= tol2) { status = 0; break; }
-    if (!(rho_n > 0.0) || !isfinite(rho_n)) { status = 2; break; }
-    const double beta = rho_n / rho;
-    rho = rho_n;
-    for (int j = gw; j < a.nf; j += nw) {
-      if (lane < 6) {
-        const int i = 6 * j + lane;
-        p[i] = fma(beta, p[i], z[i]);
-      }
-    }
-    if (!(ok = grid_barrier(a.bar, nb))) { status = 3; break; }
+    if (!(ok = grid_barrier(a.bar, (++nbar) * nb))) { status = 3; break; }
   }
   const bool conv = ok && status == 0;
   if (conv) {
     for (int j = gw; j < a.nf; j += nw) {
       if (lane < 6) {
         const int i = 6 * j + lane;
-        const double v = a.scl[i] * x[i];
-        a.xout[i] = v;
-        const dd vd = dd_from_double(v);
-        a.xdd[2 * i] = vd.hi;
-        a.xdd[2 * i + 1] = vd.lo;
+        const double v = (a.scl ? a.scl[i] : 1.0) * x[i];
+        if (a.xout) a.xout[i] = v;
+        if (a.xdd) {
+          const dd vd = dd_from_double(v);
+          a.xdd[2 * i] = vd.hi;
+          a.xdd[2 * i + 1] = vd.lo;
+        }
       }
     }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && ctrl) {
     ctrl->pcg_done = conv ? 1 : 0;
     ctrl->pcg_iters = it;
     ctrl->pcg_status = status;
@@ -417,6 +382,7 @@ PcgArgs pcg_args(const Sizes& s, const Dev& d) {
   a.rb = d.rb;
   a.scl = d.pcg_scl;
   a.Sb = d.pcg_S;
+  a.Sb2 = d.pcg_S2;
   a.P = d.pcg_P;
   a.Cinv = d.pcg_Cinv;
   a.L = (s.pcg_mode == 2) ? d.pcg_L : nullptr;
@@ -449,15 +415,21 @@ int pcg_setup(int nf, int* grid) {
 
 int pcg_launch_count(const Sizes& s) { return 3 + (s.pcg_mode == 2 ? pcg_net_launch_count() : 0); }
 
+int launch_pcg_blocks_only(const Sizes& s, const Dev& d, cudaStream_t st) {
+  const PcgArgs a = pcg_args(s, d);
+  const int64_t total = s.nsb * 36;
+  const int blocks = static_cast<int>(std::min<int64_t>((total + kPT - 1) / kPT, 8192));
+  k_pcg_blocks<<<blocks > 0 ? blocks : 1, kPT, 0, st>>>(a, d.ctrl);
+  return 1;
+}
+
 int launch_pcg(const Sizes& s, const Dev& d, cudaStream_t st) {
+  return launch_pcg_blocks_only(s, d, st) + launch_pcg_scaled(s, d, st);
+}
+
+int launch_pcg_scaled(const Sizes& s, const Dev& d, cudaStream_t st) {
   const PcgArgs a = pcg_args(s, d);
   int n = 0;
-  {
-    const int64_t total = s.nsb * 36;
-    const int blocks = static_cast<int>(std::min<int64_t>((total + kPT - 1) / kPT, 8192));
-    k_pcg_blocks<<<blocks > 0 ? blocks : 1, kPT, 0, st>>>(a, d.ctrl);
-    ++n;
-  }
   if (s.pcg_mode == 2) n += launch_pcg_net(s, d, st);
   k_pcg_precond<<<(s.nf + 127) / 128, 128, 0, st>>>(a, d.ctrl);
   ++n;

@@ -14,9 +14,14 @@
 // With W_out = 0 and b_out = 0 the preconditioner is block-Jacobi.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
+#include <cstring>
+#include <vector>
 
 #include "sgba_internal.h"
+#include "sgba_pcg_dev.cuh"
 
 namespace sgba {
 
@@ -28,94 +33,8 @@ constexpr int H = kPcgHidden;
 constexpr int F = kPcgFeat;
 
 __device__ __forceinline__ bool skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0; }
-__device__ __forceinline__ float bf16f(uint16_t u) { return __uint_as_float(static_cast<unsigned>(u) << 16); }
 
 }  // namespace
-
-// Offsets of the parameter blocks (in elements).
-__host__ __device__ constexpr int pcg_off_win() { return 0; }
-__host__ __device__ constexpr int pcg_off_bin() { return H * F; }
-__host__ __device__ constexpr int pcg_off_ws(int l) { return H * F + H + l * (2 * H * H + H); }
-__host__ __device__ constexpr int pcg_off_wm(int l) { return pcg_off_ws(l) + H * H; }
-__host__ __device__ constexpr int pcg_off_b(int l) { return pcg_off_ws(l) + 2 * H * H; }
-__host__ __device__ constexpr int pcg_off_wout() { return pcg_off_ws(kPcgLayers); }
-__host__ __device__ constexpr int pcg_off_bout() { return pcg_off_wout() + kPcgOut * H; }
-static_assert(pcg_off_bout() + kPcgOut == kPcgParams, "parameter layout");
-
-// Node features of free pose j from the Jacobi-scaled blocks.  Also writes
-// the edge weight w_jk of every entry of block row j (0 on the diagonal).
-__device__ void pcg_node_features(int j, const int32_t* rowptr, const int32_t* cols, const int32_t* blks,
-                                  const int32_t* diag, const double* Sb, float* f, float* ew) {
-  // one warp: lanes over the row's entries
-  const int lane = threadIdx.x & 31;
-  double sw = 0.0, sw2 = 0.0, mw = 0.0;
-  int deg = 0;
-  for (int e = rowptr[j] + lane; e < rowptr[j + 1]; e += 32) {
-    const double* B = Sb + 36 * static_cast<int64_t>(blks[e] & 0x7fffffff);
-    double n2 = 0.0;
-    for (int t = 0; t < 36; ++t) n2 += B[t] * B[t];
-    const double w = sqrt(n2);
-    const bool off = cols[e] != j;
-    ew[e] = off ? static_cast<float>(w) : 0.0f;
-    if (off) {
-      sw += w;
-      sw2 += n2;
-      mw = fmax(mw, w);
-      ++deg;
-    }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    sw += __shfl_xor_sync(0xffffffffu, sw, o);
-    sw2 += __shfl_xor_sync(0xffffffffu, sw2, o);
-    mw = fmax(mw, __shfl_xor_sync(0xffffffffu, mw, o));
-    deg += __shfl_xor_sync(0xffffffffu, deg, o);
-  }
-  if (lane == 0) {
-    const double* B = Sb + 36 * static_cast<int64_t>(diag[j]);
-    int t = 0;
-    for (int r = 0; r < 6; ++r)
-      for (int c = r + 1; c < 6; ++c) f[t++] = static_cast<float>(B[r * 6 + c]);
-    // diagonal of B^-1 by the Cholesky factor (B^-1 = C^-T C^-1)
-    double C[36];
-    bool ok = true;
-    for (int a = 0; a < 36; ++a) C[a] = 0.0;
-    for (int c = 0; c < 6 && ok; ++c) {
-      double d = B[c * 6 + c];
-      for (int k = 0; k < c; ++k) d -= C[c * 6 + k] * C[c * 6 + k];
-      if (!(d > 0.0) || !isfinite(d)) { ok = false; break; }
-      C[c * 6 + c] = sqrt(d);
-      for (int i = c + 1; i < 6; ++i) {
-        double v = B[i * 6 + c];
-        for (int k = 0; k < c; ++k) v -= C[i * 6 + k] * C[c * 6 + k];
-        C[i * 6 + c] = v / C[c * 6 + c];
-      }
-    }
-    double X[36];  // C^-1
-    for (int a = 0; a < 36; ++a) X[a] = 0.0;
-    if (ok) {
-      for (int c = 0; c < 6; ++c) {
-        X[c * 6 + c] = 1.0 / C[c * 6 + c];
-        for (int i = c + 1; i < 6; ++i) {
-          double v = 0.0;
-          for (int k = c; k < i; ++k) v -= C[i * 6 + k] * X[k * 6 + c];
-          X[i * 6 + c] = v / C[i * 6 + i];
-        }
-      }
-    }
-    for (int r = 0; r < 6; ++r) {
-      double v = 0.0;
-      for (int k = r; k < 6; ++k) v += X[k * 6 + r] * X[k * 6 + r];
-      f[15 + r] = ok ? static_cast<float>(log(fmax(v, 1e-30))) : 0.0f;
-    }
-    f[21] = static_cast<float>(log1p(static_cast<double>(deg)));
-    f[22] = static_cast<float>(sw);
-    f[23] = static_cast<float>(mw);
-    f[24] = static_cast<float>(sqrt(sw2));
-    f[25] = static_cast<float>(deg > 0 ? sw / deg : 0.0);
-    for (int k = 26; k < F; ++k) f[k] = 0.0f;
-  }
-  __syncwarp();
-}
 
 namespace {
 
@@ -268,6 +187,521 @@ int launch_pcg_net(const Sizes& s, const Dev& d, cudaStream_t st) {
     hout = const_cast<float*>(t);
   }
   return 1 + kPcgLayers;
+}
+
+
+// ===========================================================================
+// Training: reduced systems S~ x* = b~ (Jacobi-scaled) with their exact
+// solutions, loss, gradients by hand-written backward kernels, Adam.
+//
+// Loss of one system (the energy-norm error of one preconditioned step):
+//   e = x* - P b~,   loss = e^T S~ e / x*^T S~ x*     (x*^T S~ x* = x*^T b~)
+// P = blockdiag(P_j), P_j = Ci_j^T (I + L_j L_j^T) Ci_j.  Backward:
+//   g = dloss/dy = -2 S~ e / den  (y = P b~),  dloss/dP_j = g_j b_j^T,
+//   dloss/dM_j = Ci_j G_j Ci_j^T,  dloss/dL_j = (Gm_j + Gm_j^T) L_j,
+// then through the head, the message-passing layers (relu, the weighted
+// mean of the neighbours) and the embedding.  The forward arithmetic is the
+// inference kernels' (same BF16 weights, same FP32 operation order); the
+// gradients are FP32 and update the FP32 master weights (Adam).  Every
+// reduction runs in a fixed order: training is bit-reproducible.
+// ===========================================================================
+
+namespace {
+
+constexpr int kTT = 256;
+
+struct TrainArgs {
+  int nf;
+  const int32_t* rowptr;
+  const int32_t* cols;
+  const int32_t* blks;
+  const int32_t* diag;
+  const double* Sb;
+  const double* b;
+  const double* xs;
+  const uint16_t* w;  // BF16 weights (forward and data gradients)
+  float* feat;        // nf x F
+  float* ew;          // nnzb
+  float* wsum;        // nf
+  float* Hs;          // (kPcgLayers + 1) x nf x H
+  float* Ms;          // kPcgLayers x nf x H
+  float* Us;          // kPcgLayers x nf x H (pre-activations)
+  float* L;           // nf x 21
+  double* P;          // nf x 36
+  double* Ci;         // nf x 36
+  double* e;          // n6
+  double* Se;         // n6
+  double* loss_part;  // per CTA
+  float* dL;          // nf x 21
+  float* dHa;         // nf x H
+  float* dHb;         // nf x H
+  float* dU;          // nf x H
+  float* dM;          // nf x H
+  float* grad;        // kPcgParams (accumulated)
+};
+
+__global__ void __launch_bounds__(kTT) k_tr_features(TrainArgs a) {
+  __shared__ float sf[kTT / 32][F];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j = blockIdx.x * (kTT / 32) + w; j < a.nf; j += gridDim.x * (kTT / 32)) {
+    pcg_node_features(j, a.rowptr, a.cols, a.blks, a.diag, a.Sb, sf[w], a.ew);
+    if (lane == 0) {
+      for (int k = 0; k < F; ++k) a.feat[static_cast<int64_t>(j) * F + k] = sf[w][k];
+      float ws = 0.f;  // the inference kernel's order
+      for (int e = a.rowptr[j]; e < a.rowptr[j + 1]; ++e)
+        if (a.ew[e] != 0.0f) ws += a.ew[e];
+      a.wsum[j] = ws;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void k_tr_embed(TrainArgs a) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(a.nf) * H) return;
+  const int64_t j = t / H;
+  const int o = static_cast<int>(t % H);
+  float v = bf16f(a.w[pcg_off_bin() + o]);
+  for (int k = 0; k < F; ++k) v = fmaf(bf16f(a.w[pcg_off_win() + o * F + k]), a.feat[j * F + k], v);
+  a.Hs[t] = fmaxf(v, 0.0f);
+}
+
+__global__ void k_tr_message(TrainArgs a, int l) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(a.nf) * H) return;
+  const int j = static_cast<int>(t / H);
+  const int o = static_cast<int>(t % H);
+  const float* Hl = a.Hs + static_cast<int64_t>(l) * a.nf * H;
+  float m = 0.f, ws = 0.f;
+  for (int e = a.rowptr[j]; e < a.rowptr[j + 1]; ++e) {
+    const float we = a.ew[e];
+    if (we == 0.0f) continue;
+    m = fmaf(we, Hl[static_cast<int64_t>(a.cols[e]) * H + o], m);
+    ws += we;
+  }
+  const float inv = ws > 0.f ? 1.0f / ws : 0.0f;
+  a.Ms[static_cast<int64_t>(l) * a.nf * H + t] = m * inv;
+}
+
+__global__ void k_tr_layer(TrainArgs a, int l) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(a.nf) * H) return;
+  const int64_t j = t / H;
+  const int o = static_cast<int>(t % H);
+  const float* Hl = a.Hs + static_cast<int64_t>(l) * a.nf * H;
+  const float* Ml = a.Ms + static_cast<int64_t>(l) * a.nf * H;
+  float v = bf16f(a.w[pcg_off_b(l) + o]);
+  for (int k = 0; k < H; ++k) v = fmaf(bf16f(a.w[pcg_off_ws(l) + o * H + k]), Hl[j * H + k], v);
+  for (int k = 0; k < H; ++k) v = fmaf(bf16f(a.w[pcg_off_wm(l) + o * H + k]), Ml[j * H + k], v);
+  a.Us[static_cast<int64_t>(l) * a.nf * H + t] = v;
+  a.Hs[static_cast<int64_t>(l + 1) * a.nf * H + t] = Hl[t] + fmaxf(v, 0.0f);
+}
+
+__global__ void k_tr_head(TrainArgs a) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(a.nf) * kPcgOut) return;
+  const int64_t j = t / kPcgOut;
+  const int o = static_cast<int>(t % kPcgOut);
+  const float* Hl = a.Hs + static_cast<int64_t>(kPcgLayers) * a.nf * H;
+  float v = bf16f(a.w[pcg_off_bout() + o]);
+  for (int k = 0; k < H; ++k) v = fmaf(bf16f(a.w[pcg_off_wout() + o * H + k]), Hl[j * H + k], v);
+  a.L[t] = v;
+}
+
+// P_j, Ci_j and e_j = x*_j - P_j b_j.
+__global__ void k_tr_precond(TrainArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.nf) return;
+  double* P = a.P + 36 * static_cast<int64_t>(j);
+  pcg_precond_block(a.Sb + 36 * static_cast<int64_t>(a.diag[j]), a.L + kPcgOut * static_cast<int64_t>(j), P,
+                    a.Ci + 36 * static_cast<int64_t>(j));
+  for (int r = 0; r < 6; ++r) {
+    double y = 0.0;
+    for (int c = 0; c < 6; ++c) y += P[r * 6 + c] * a.b[6 * j + c];
+    a.e[6 * j + r] = a.xs[6 * j + r] - y;
+  }
+}
+
+// Se = S~ e (FP64, warp per block row) and per-CTA partials of e . Se.
+__global__ void __launch_bounds__(kTT) k_tr_matvec(TrainArgs a) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double part = 0.0;
+  for (int j = blockIdx.x * (kTT / 32) + w; j < a.nf; j += gridDim.x * (kTT / 32)) {
+    double acc[6] = {0, 0, 0, 0, 0, 0};
+    for (int e = a.rowptr[j] + lane; e < a.rowptr[j + 1]; e += 32) {
+      const int k = a.cols[e];
+      const int bi = a.blks[e];
+      const double* B = a.Sb + 36 * static_cast<int64_t>(bi & 0x7fffffff);
+      for (int r = 0; r < 6; ++r)
+        for (int c = 0; c < 6; ++c) acc[r] += (bi < 0 ? B[c * 6 + r] : B[r * 6 + c]) * a.e[6 * k + c];
+    }
+    for (int r = 0; r < 6; ++r)
+      for (int off = 16; off > 0; off >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], off);
+    if (lane == 0)
+      for (int r = 0; r < 6; ++r) {
+        a.Se[6 * j + r] = acc[r];
+        part += a.e[6 * j + r] * acc[r];
+      }
+  }
+  __shared__ double sp[kTT / 32];
+  if (lane == 0) sp[w] = part;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < kTT / 32; ++q) t += sp[q];
+    a.loss_part[blockIdx.x] = t;
+  }
+}
+
+__global__ void k_tr_loss(const double* part, int n, double den, double* loss) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < n; ++i) t += part[i];
+    *loss = t / den;
+  }
+}
+
+// dloss/dL_j (lower-triangular entries).
+__global__ void k_tr_dL(TrainArgs a, double den) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.nf) return;
+  const double* Ci = a.Ci + 36 * static_cast<int64_t>(j);
+  double g[6], bj[6];
+  for (int r = 0; r < 6; ++r) {
+    g[r] = -2.0 * a.Se[6 * j + r] / den;
+    bj[r] = a.b[6 * j + r];
+  }
+  // Gm = Ci G Ci^T with G = g b^T: Gm = (Ci g)(Ci b)^T
+  double cg[6], cb[6];
+  for (int r = 0; r < 6; ++r) {
+    double u = 0.0, v = 0.0;
+    for (int k = 0; k < 6; ++k) {
+      u += Ci[r * 6 + k] * g[k];
+      v += Ci[r * 6 + k] * bj[k];
+    }
+    cg[r] = u;
+    cb[r] = v;
+  }
+  double Lf[36];
+  for (int k = 0; k < 36; ++k) Lf[k] = 0.0;
+  const float* Lr = a.L + kPcgOut * static_cast<int64_t>(j);
+  for (int r = 0, t = 0; r < 6; ++r)
+    for (int c = 0; c <= r; ++c, ++t) Lf[r * 6 + c] = Lr[t];
+  for (int r = 0, t = 0; r < 6; ++r)
+    for (int c = 0; c <= r; ++c, ++t) {
+      double v = 0.0;
+      for (int k = 0; k < 6; ++k) v += (cg[r] * cb[k] + cb[r] * cg[k]) * Lf[k * 6 + c];
+      a.dL[kPcgOut * static_cast<int64_t>(j) + t] = static_cast<float>(v);
+    }
+}
+
+// out[i, k] += sum_j A[j, i] B[j, k]; with bias: outb[i] += sum_j A[j, i].
+__global__ void k_tr_wgrad(int nf, const float* A, int m, const float* B, int n, float* out, float* outb) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m * n) return;
+  const int i = t / n, k = t % n;
+  float s = 0.f, sb = 0.f;
+  for (int j = 0; j < nf; ++j) {
+    const float av = A[static_cast<int64_t>(j) * m + i];
+    s = fmaf(av, B[static_cast<int64_t>(j) * n + k], s);
+    sb += av;
+  }
+  out[t] += s;
+  if (outb && k == 0) outb[i] += sb;
+}
+
+// dH (nf x H) = dL W_out
+__global__ void k_tr_head_back(TrainArgs a) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(a.nf) * H) return;
+  const int64_t j = t / H;
+  const int k = static_cast<int>(t % H);
+  float v = 0.f;
+  for (int o = 0; o < kPcgOut; ++o) v = fmaf(a.dL[j * kPcgOut + o], bf16f(a.w[pcg_off_wout() + o * H + k]), v);
+  a.dHa[t] = v;
+}
+
+// dU = dH_next * relu'(U)
+__global__ void k_tr_du(TrainArgs a, int l, const float* dHn) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(a.nf) * H) return;
+  a.dU[t] = a.Us[static_cast<int64_t>(l) * a.nf * H + t] > 0.0f ? dHn[t] : 0.0f;
+}
+
+// dM = dU W_msg;  dHp = dH_next + dU W_self
+__global__ void k_tr_dm(TrainArgs a, int l, const float* dHn, float* dHp) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(a.nf) * H) return;
+  const int64_t j = t / H;
+  const int k = static_cast<int>(t % H);
+  float vm = 0.f, vs = 0.f;
+  for (int o = 0; o < H; ++o) {
+    const float du = a.dU[j * H + o];
+    vm = fmaf(du, bf16f(a.w[pcg_off_wm(l) + o * H + k]), vm);
+    vs = fmaf(du, bf16f(a.w[pcg_off_ws(l) + o * H + k]), vs);
+  }
+  a.dM[t] = vm;
+  dHp[t] = dHn[t] + vs;
+}
+
+// dH_l[j] = dHp[j] + sum over neighbours i of (w_ij / wsum_i) dM[i]
+__global__ void k_tr_scatter(TrainArgs a, const float* dHp, float* dHl) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(a.nf) * H) return;
+  const int j = static_cast<int>(t / H);
+  const int k = static_cast<int>(t % H);
+  float v = dHp[t];
+  for (int e = a.rowptr[j]; e < a.rowptr[j + 1]; ++e) {
+    const float we = a.ew[e];
+    if (we == 0.0f) continue;
+    const int i = a.cols[e];
+    const float ws = a.wsum[i];
+    if (ws > 0.f) v = fmaf(we * (1.0f / ws), a.dM[static_cast<int64_t>(i) * H + k], v);
+  }
+  dHl[t] = v;
+}
+
+// dpre = dH0 * relu'(H0) (H0 = relu(pre): H0 > 0 <=> pre > 0), in place
+__global__ void k_tr_embed_back(TrainArgs a, float* dH0) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(a.nf) * H) return;
+  if (!(a.Hs[t] > 0.0f)) dH0[t] = 0.0f;
+}
+
+__device__ __forceinline__ uint16_t bf16_rn(float f) {
+  unsigned u = __float_as_uint(f);
+  u += 0x7fffu + ((u >> 16) & 1u);
+  return static_cast<uint16_t>(u >> 16);
+}
+
+__global__ void k_tr_adam(int n, float* w, uint16_t* wbf, float* m1, float* m2, float* grad, float scale, float lr,
+                          float b1, float b2, float eps, float c1, float c2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float g = grad[i] * scale;
+  const float m = b1 * m1[i] + (1.0f - b1) * g;
+  const float v = b2 * m2[i] + (1.0f - b2) * g * g;
+  m1[i] = m;
+  m2[i] = v;
+  const float wn = w[i] - lr * (m / c1) / (sqrtf(v / c2) + eps);
+  w[i] = wn;
+  wbf[i] = bf16_rn(wn);
+  grad[i] = 0.0f;
+}
+
+inline unsigned nblk(int64_t n, int t) { return static_cast<unsigned>((n + t - 1) / t); }
+
+}  // namespace
+
+// ---------------------------------------------------------------- host ----
+
+PcgTrainSet::~PcgTrainSet() {
+  cudaSetDevice(device);
+  for (auto& s : sys) {
+    cudaFree(s.rowptr);
+    cudaFree(s.cols);
+    cudaFree(s.blks);
+    cudaFree(s.diag);
+    cudaFree(s.Sb);
+    cudaFree(s.Sb2);
+    cudaFree(s.b);
+    cudaFree(s.xs);
+  }
+  free_workspace();
+}
+
+void PcgTrainSet::free_workspace() {
+  for (void* p : ws) cudaFree(p);
+  ws.clear();
+  cap_nf = 0;
+  cap_nnzb = 0;
+}
+
+template <class T>
+static cudaError_t ws_alloc(PcgTrainSet* t, T** p, size_t n) {
+  void* v = nullptr;
+  cudaError_t e = cudaMalloc(&v, sizeof(T) * std::max<size_t>(n, 1));
+  if (e == cudaSuccess) {
+    t->ws.push_back(v);
+    *p = static_cast<T*>(v);
+  }
+  return e;
+}
+
+cudaError_t PcgTrainSet::reserve(int nf, int64_t nnzb) {
+  if (nf <= cap_nf && nnzb <= cap_nnzb && !ws.empty()) return cudaSuccess;
+  free_workspace();
+  const size_t n = static_cast<size_t>(nf), nh = n * H;
+  cudaError_t e;
+  if ((e = ws_alloc(this, &feat, n * F)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &ew, static_cast<size_t>(nnzb))) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &wsum, n)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &Hs, (kPcgLayers + 1) * nh)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &Ms, kPcgLayers * nh)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &Us, kPcgLayers * nh)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &L, n * kPcgOut)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &P, n * 36)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &Ci, n * 36)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &evec, 6 * n)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &Se, 6 * n)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &loss_part, 4096)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &loss, 1)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &dL, n * kPcgOut)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &dHa, nh)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &dHb, nh)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &dU, nh)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &dM, nh)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &dHp, nh)) != cudaSuccess) return e;
+  // PCG evaluation of a stored system
+  if ((e = ws_alloc(this, &hbuf, 2 * nh)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &vec, 6 * 6 * n)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &part, 4 * static_cast<size_t>(kPcgMaxGrid))) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &bar, 4)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &ctrl, 1)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &xout, 6 * n)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &xdd, 12 * n)) != cudaSuccess) return e;
+  cap_nf = nf;
+  cap_nnzb = nnzb;
+  return cudaSuccess;
+}
+
+static TrainArgs train_args(PcgTrainSet& t, const PcgSystem& s, const PcgModel& m) {
+  TrainArgs a;
+  a.nf = s.nf;
+  a.rowptr = s.rowptr;
+  a.cols = s.cols;
+  a.blks = s.blks;
+  a.diag = s.diag;
+  a.Sb = s.Sb;
+  a.b = s.b;
+  a.xs = s.xs;
+  a.w = m.wbf;
+  a.feat = t.feat;
+  a.ew = t.ew;
+  a.wsum = t.wsum;
+  a.Hs = t.Hs;
+  a.Ms = t.Ms;
+  a.Us = t.Us;
+  a.L = t.L;
+  a.P = t.P;
+  a.Ci = t.Ci;
+  a.e = t.evec;
+  a.Se = t.Se;
+  a.loss_part = t.loss_part;
+  a.dL = t.dL;
+  a.dHa = t.dHa;
+  a.dHb = t.dHb;
+  a.dU = t.dU;
+  a.dM = t.dM;
+  a.grad = m.grad;
+  return a;
+}
+
+cudaError_t pcg_loss_grad(PcgModel& m, PcgTrainSet& t, int idx, bool backward, double* loss, cudaStream_t st) {
+  const PcgSystem& s = t.sys[idx];
+  cudaError_t e = t.reserve(s.nf, s.nnzb);
+  if (e != cudaSuccess) return e;
+  const TrainArgs a = train_args(t, s, m);
+  const int64_t nh = static_cast<int64_t>(s.nf) * H;
+  const unsigned gw = nblk(s.nf, kTT / 32);
+  k_tr_features<<<gw, kTT, 0, st>>>(a);
+  k_tr_embed<<<nblk(nh, kTT), kTT, 0, st>>>(a);
+  for (int l = 0; l < kPcgLayers; ++l) {
+    k_tr_message<<<nblk(nh, kTT), kTT, 0, st>>>(a, l);
+    k_tr_layer<<<nblk(nh, kTT), kTT, 0, st>>>(a, l);
+  }
+  k_tr_head<<<nblk(static_cast<int64_t>(s.nf) * kPcgOut, kTT), kTT, 0, st>>>(a);
+  k_tr_precond<<<nblk(s.nf, 128), 128, 0, st>>>(a);
+  const unsigned mvb = std::min<unsigned>(gw, 4096);
+  k_tr_matvec<<<mvb, kTT, 0, st>>>(a);
+  k_tr_loss<<<1, 32, 0, st>>>(t.loss_part, static_cast<int>(mvb), s.den, t.loss);
+  if (backward) {
+    float* g = m.grad;
+    k_tr_dL<<<nblk(s.nf, 128), 128, 0, st>>>(a, s.den);
+    k_tr_wgrad<<<nblk(kPcgOut * H, 128), 128, 0, st>>>(s.nf, t.dL, kPcgOut, t.Hs + kPcgLayers * nh, H,
+                                                       g + pcg_off_wout(), g + pcg_off_bout());
+    k_tr_head_back<<<nblk(nh, kTT), kTT, 0, st>>>(a);
+    float* dHn = t.dHa;  // gradient w.r.t. H_{l+1}
+    float* dHl = t.dHb;
+    for (int l = kPcgLayers - 1; l >= 0; --l) {
+      k_tr_du<<<nblk(nh, kTT), kTT, 0, st>>>(a, l, dHn);
+      k_tr_wgrad<<<nblk(H * H, 128), 128, 0, st>>>(s.nf, t.dU, H, t.Hs + l * nh, H, g + pcg_off_ws(l),
+                                                   g + pcg_off_b(l));
+      k_tr_wgrad<<<nblk(H * H, 128), 128, 0, st>>>(s.nf, t.dU, H, t.Ms + l * nh, H, g + pcg_off_wm(l), nullptr);
+      k_tr_dm<<<nblk(nh, kTT), kTT, 0, st>>>(a, l, dHn, t.dHp);
+      k_tr_scatter<<<nblk(nh, kTT), kTT, 0, st>>>(a, t.dHp, dHl);
+      std::swap(dHn, dHl);
+    }
+    k_tr_embed_back<<<nblk(nh, kTT), kTT, 0, st>>>(a, dHn);
+    k_tr_wgrad<<<nblk(H * F, 128), 128, 0, st>>>(s.nf, dHn, H, t.feat, F, g + pcg_off_win(), g + pcg_off_bin());
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (loss) {
+    if ((e = cudaMemcpyAsync(loss, t.loss, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t pcg_adam(PcgModel& m, float scale, float lr, float b1, float b2, float eps, cudaStream_t st) {
+  m.step += 1;
+  const float c1 = 1.0f - std::pow(b1, static_cast<float>(m.step));
+  const float c2 = 1.0f - std::pow(b2, static_cast<float>(m.step));
+  k_tr_adam<<<nblk(kPcgParams, 256), 256, 0, st>>>(kPcgParams, m.w32, m.wbf, m.m1, m.m2, m.grad, scale, lr, b1, b2,
+                                                   eps, c1, c2);
+  return cudaGetLastError();
+}
+
+cudaError_t pcg_evaluate(const PcgModel* m, PcgTrainSet& t, int idx, int mode, int max_iters, double tol,
+                         int* iters, double* relres, int* status, cudaStream_t st) {
+  const PcgSystem& s = t.sys[idx];
+  cudaError_t e = t.reserve(s.nf, s.nnzb);
+  if (e != cudaSuccess) return e;
+  int grid = 0;
+  if (pcg_setup(s.nf, &grid) != 0 || grid < 1) return cudaErrorNotSupported;
+  if (mode == 2 && pcg_net_setup() != 0) return cudaErrorInvalidValue;
+  Sizes z;
+  std::memset(&z, 0, sizeof(z));
+  z.nf = s.nf;
+  z.n6 = 6 * s.nf;
+  z.nsb = s.nsb;
+  z.pcg_mode = mode;
+  z.pcg_max_iters = max_iters;
+  z.pcg_tol = tol;
+  z.pcg_grid = grid;
+  z.pcg_nnzb = s.nnzb;
+  Dev d;
+  d.pcg_rowptr = s.rowptr;
+  d.pcg_cols = s.cols;
+  d.pcg_blks = s.blks;
+  d.pcg_diag = s.diag;
+  d.pcg_S = s.Sb;
+  d.pcg_S2 = s.Sb2;
+  d.pcg_scl = nullptr;  // the stored system is scaled already
+  d.rb = const_cast<double*>(s.b);
+  d.pcg_P = t.P;
+  d.pcg_Cinv = t.Ci;
+  d.pcg_vec = t.vec;
+  d.pcg_part = t.part;
+  d.pcg_bar = t.bar;
+  d.pcg_feat = t.feat;
+  d.pcg_ew = t.ew;
+  d.pcg_h = t.hbuf;
+  d.pcg_L = t.L;
+  d.pcg_w = m ? m->wbf : nullptr;
+  d.x = t.xout;
+  d.xdd = t.xdd;
+  d.ctrl = t.ctrl;
+  if ((e = cudaMemsetAsync(t.ctrl, 0, sizeof(Ctrl), st)) != cudaSuccess) return e;
+  launch_pcg_scaled(z, d, st);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  Ctrl c;
+  if ((e = cudaMemcpyAsync(&c, t.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return e;
+  *iters = c.pcg_iters;
+  *relres = c.pcg_relres;
+  *status = c.pcg_status;
+  return cudaSuccess;
 }
 
 }  // namespace sgba

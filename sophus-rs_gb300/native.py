@@ -145,7 +145,13 @@ EXPORTED = [
     "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_batch_optimize",
     "sgba_set_linear_solver", "sgba_get_pcg_stats", "sgba_pcg_num_params", "sgba_pcg_model_create",
     "sgba_pcg_model_destroy", "sgba_pcg_model_set_params", "sgba_pcg_model_get_params",
+    "sgba_pcg_trainset_create", "sgba_pcg_trainset_destroy", "sgba_pcg_trainset_size", "sgba_pcg_trainset_add",
+    "sgba_pcg_collect", "sgba_pcg_loss_grad", "sgba_pcg_train", "sgba_pcg_evaluate",
 ]
+
+
+class PcgTrainParams(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("learning_rate", C.c_double), ("seed", C.c_uint64)]
 
 # sgba_kernel_id
 KERNEL_ITERATION = 0
@@ -210,6 +216,16 @@ def lib():
     fp = C.POINTER(C.c_float)
     L.sgba_pcg_model_set_params.argtypes = [C.c_void_p, fp, C.c_int32]
     L.sgba_pcg_model_get_params.argtypes = [C.c_void_p, fp, C.c_int32]
+    L.sgba_pcg_trainset_create.argtypes = [C.c_int32, C.POINTER(C.c_void_p)]
+    L.sgba_pcg_trainset_destroy.argtypes = [C.c_void_p]
+    L.sgba_pcg_trainset_size.argtypes = [C.c_void_p]
+    L.sgba_pcg_trainset_size.restype = C.c_int32
+    L.sgba_pcg_trainset_add.argtypes = [C.c_void_p, C.c_int32, C.c_int64, ip, ip, dp, dp, dp]
+    L.sgba_pcg_collect.argtypes = [C.c_void_p, C.c_void_p]
+    L.sgba_pcg_loss_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, dp, fp, C.c_int32]
+    L.sgba_pcg_train.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(PcgTrainParams), dp]
+    L.sgba_pcg_evaluate.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double,
+                                    C.POINTER(C.c_int32), dp, C.POINTER(C.c_int32)]
     _lib = L
     return L
 
@@ -384,6 +400,11 @@ class Problem:
         self._model = model  # kept alive while the problem uses it
         check(lib().sgba_set_linear_solver(self._h, C.byref(cfg), model._h if model is not None else None))
 
+    def collect(self, trainset):
+        """Append the reduced system of the latest LM step (scaled, with its
+        exact solution) to a PcgTrainSet."""
+        check(lib().sgba_pcg_collect(self._h, trainset._h))
+
     def pcg_stats(self):
         st = PcgStats()
         check(lib().sgba_get_pcg_stats(self._h, C.byref(st)))
@@ -467,6 +488,71 @@ class PcgModel:
     def close(self):
         if getattr(self, "_h", None):
             lib().sgba_pcg_model_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PcgTrainSet:
+    """Reduced systems with exact solutions for training the preconditioner
+    (sgba_pcg_trainset)."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        check(lib().sgba_pcg_trainset_create(int(device), C.byref(h)))
+        self._h = h
+
+    def __len__(self):
+        return int(lib().sgba_pcg_trainset_size(self._h))
+
+    def add(self, nf, s_rows, s_cols, blocks, b, x):
+        """A Jacobi-scaled system from host arrays (lower blocks, n x 36)."""
+        r = np.ascontiguousarray(s_rows, dtype=np.int32)
+        c = np.ascontiguousarray(s_cols, dtype=np.int32)
+        bl = np.ascontiguousarray(blocks, dtype=np.float64).reshape(-1, 36)
+        bv = np.ascontiguousarray(b, dtype=np.float64)
+        xv = np.ascontiguousarray(x, dtype=np.float64)
+        check(lib().sgba_pcg_trainset_add(self._h, int(nf), r.shape[0], _ipt(r), _ipt(c), _dptr(bl), _dptr(bv),
+                                          _dptr(xv)))
+
+    def loss_grad(self, model, index, with_grad=True):
+        loss = C.c_double()
+        if with_grad:
+            g = np.empty(PcgModel.num_params(), np.float32)
+            check(lib().sgba_pcg_loss_grad(model._h, self._h, int(index), C.byref(loss),
+                                           g.ctypes.data_as(C.POINTER(C.c_float)), g.shape[0]))
+            return loss.value, g
+        check(lib().sgba_pcg_loss_grad(model._h, self._h, int(index), C.byref(loss), None, 0))
+        return loss.value
+
+    def train(self, model, epochs, batch=8, learning_rate=1e-3, seed=1):
+        losses = np.zeros(int(epochs))
+        tp = PcgTrainParams(int(epochs), int(batch), float(learning_rate), C.c_uint64(seed))
+        check(lib().sgba_pcg_train(model._h, self._h, C.byref(tp), _dptr(losses)))
+        return losses
+
+    def evaluate(self, index, mode, model=None, max_iterations=50, tolerance=1e-8):
+        """PCG on stored system `index`: (iterations, relative residual, status)."""
+        it = C.c_int32()
+        rr = C.c_double()
+        st = C.c_int32()
+        check(lib().sgba_pcg_evaluate(model._h if model is not None else None, self._h, int(index), int(mode),
+                                      int(max_iterations), float(tolerance), C.byref(it), C.byref(rr), C.byref(st)))
+        return it.value, rr.value, st.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().sgba_pcg_trainset_destroy(self._h)
             self._h = None
 
     def __enter__(self):
