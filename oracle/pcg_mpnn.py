@@ -13,7 +13,8 @@ This file restates, in numpy float64, what the library computes on the GPU:
   h0 = relu(W_in f + b_in);  m_j = sum_k w_jk h_k / sum_k w_jk;
   h' = h + relu(W_s h + W_m m + b)  (3 layers);  L_j = W_o h + b_o;
   P_j = Ci_j^T (I + L_j L_j^T) Ci_j,  Ci_j = chol(B_j)^-1;
-  e = x* - P b,  loss = e^T S~ e / x*^T b.
+  y = P b,  loss = min_a |x* - a y|^2_S~ / x*^T b = 1 - (y^T b)^2 / (x*^T b  y^T S~ y)
+  (the error left by one preconditioned step of optimal length from 0).
 
 gradient() is a hand-written backward pass of the same graph; it is itself
 checked against central differences in the tests.
@@ -131,11 +132,12 @@ def forward(params, nf, s_rows, s_cols, blocks, b, xs, bf16=True):
         Cis.append(Ci)
         Ls.append(L)
         y[6 * j:6 * j + 6] = P @ b[6 * j:6 * j + 6]
-    e = xs - y
-    Se = matvec(nf, R, blocks, e)
+    Sy = matvec(nf, R, blocks, y)
     den = float(xs @ b)
-    loss = float(e @ Se) / den
-    ctx = dict(p=p, R=R, W=W, f=f, h=h, Ms=Ms, Us=Us, Ls=Ls, Cis=Cis, Se=Se, den=den, b=b, nf=nf)
+    q = float(y @ Sy)
+    nn = float(y @ b)
+    loss = 1.0 - nn * nn / (den * q)
+    ctx = dict(p=p, R=R, W=W, f=f, h=h, Ms=Ms, Us=Us, Ls=Ls, Cis=Cis, Sy=Sy, den=den, q=q, nn=nn, b=b, nf=nf)
     return loss, ctx
 
 
@@ -155,9 +157,11 @@ def gradient(params, nf, s_rows, s_cols, blocks, b, xs, bf16=True):
     g = {k: np.zeros(s) for k, (o, s) in lay.items()}
     tril = np.tril_indices(6)
     dLv = np.zeros((nf, OUT))
+    cc = 2.0 * c["nn"] / (c["den"] * c["q"])
+    astar = c["nn"] / c["q"]
     for j in range(nf):
-        gj = -2.0 * c["Se"][6 * j:6 * j + 6] / c["den"]
         bj = b[6 * j:6 * j + 6]
+        gj = cc * (astar * c["Sy"][6 * j:6 * j + 6] - bj)
         Ci = c["Cis"][j]
         Gm = Ci @ np.outer(gj, bj) @ Ci.T
         D = (Gm + Gm.T) @ c["Ls"][j]

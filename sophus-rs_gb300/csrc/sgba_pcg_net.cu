@@ -194,11 +194,15 @@ int launch_pcg_net(const Sizes& s, const Dev& d, cudaStream_t st) {
 // Training: reduced systems S~ x* = b~ (Jacobi-scaled) with their exact
 // solutions, loss, gradients by hand-written backward kernels, Adam.
 //
-// Loss of one system (the energy-norm error of one preconditioned step):
-//   e = x* - P b~,   loss = e^T S~ e / x*^T S~ x*     (x*^T S~ x* = x*^T b~)
+// Loss of one system: the energy-norm error left by one preconditioned step
+// of optimal length from x = 0 (the first step of PCG; invariant to scaling P,
+// as PCG is):
+//   y = P b~,  N = y^T b~,  Q = y^T S~ y,  den = x*^T b~,
+//   loss = min_a |x* - a y|_S~^2 / den = 1 - N^2 / (den Q)
 // P = blockdiag(P_j), P_j = Ci_j^T (I + L_j L_j^T) Ci_j.  Backward:
-//   g = dloss/dy = -2 S~ e / den  (y = P b~),  dloss/dP_j = g_j b_j^T,
-//   dloss/dM_j = Ci_j G_j Ci_j^T,  dloss/dL_j = (Gm_j + Gm_j^T) L_j,
+//   g = dloss/dy = (2 N / (den Q)) (a* S~ y - b~),  a* = N / Q,
+//   dloss/dP_j = g_j b_j^T,  dloss/dM_j = Ci_j G_j Ci_j^T,
+//   dloss/dL_j = (Gm_j + Gm_j^T) L_j,
 // then through the head, the message-passing layers (relu, the weighted
 // mean of the neighbours) and the embedding.  The forward arithmetic is the
 // inference kernels' (same BF16 weights, same FP32 operation order); the
@@ -229,7 +233,7 @@ struct TrainArgs {
   float* L;           // nf x 21
   double* P;          // nf x 36
   double* Ci;         // nf x 36
-  double* e;          // n6
+  double* e;          // n6: y = P b~
   double* Se;         // n6
   double* loss_part;  // per CTA
   float* dL;          // nf x 21
@@ -308,7 +312,7 @@ __global__ void k_tr_head(TrainArgs a) {
   a.L[t] = v;
 }
 
-// P_j, Ci_j and e_j = x*_j - P_j b_j.
+// P_j, Ci_j and y_j = P_j b_j.
 __global__ void k_tr_precond(TrainArgs a) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= a.nf) return;
@@ -318,14 +322,15 @@ __global__ void k_tr_precond(TrainArgs a) {
   for (int r = 0; r < 6; ++r) {
     double y = 0.0;
     for (int c = 0; c < 6; ++c) y += P[r * 6 + c] * a.b[6 * j + c];
-    a.e[6 * j + r] = a.xs[6 * j + r] - y;
+    a.e[6 * j + r] = y;
   }
 }
 
-// Se = S~ e (FP64, warp per block row) and per-CTA partials of e . Se.
+// Se = S~ y (FP64, warp per block row) and per-CTA partials of y . S~ y and
+// y . b~ (slots 2 * block, 2 * block + 1).
 __global__ void __launch_bounds__(kTT) k_tr_matvec(TrainArgs a) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  double part = 0.0;
+  double part = 0.0, partn = 0.0;
   for (int j = blockIdx.x * (kTT / 32) + w; j < a.nf; j += gridDim.x * (kTT / 32)) {
     double acc[6] = {0, 0, 0, 0, 0, 0};
     for (int e = a.rowptr[j] + lane; e < a.rowptr[j + 1]; e += 32) {
@@ -341,35 +346,51 @@ __global__ void __launch_bounds__(kTT) k_tr_matvec(TrainArgs a) {
       for (int r = 0; r < 6; ++r) {
         a.Se[6 * j + r] = acc[r];
         part += a.e[6 * j + r] * acc[r];
+        partn += a.e[6 * j + r] * a.b[6 * j + r];
       }
   }
-  __shared__ double sp[kTT / 32];
-  if (lane == 0) sp[w] = part;
+  __shared__ double sp[2][kTT / 32];
+  if (lane == 0) {
+    sp[0][w] = part;
+    sp[1][w] = partn;
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int q = 0; q < kTT / 32; ++q) t += sp[q];
-    a.loss_part[blockIdx.x] = t;
+    double t = 0.0, tn = 0.0;
+    for (int q = 0; q < kTT / 32; ++q) {
+      t += sp[0][q];
+      tn += sp[1][q];
+    }
+    a.loss_part[2 * blockIdx.x] = t;
+    a.loss_part[2 * blockIdx.x + 1] = tn;
   }
 }
 
+// loss[0] = 1 - N^2 / (den Q); loss[1] = Q, loss[2] = N for the backward pass.
 __global__ void k_tr_loss(const double* part, int n, double den, double* loss) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double t = 0.0;
-    for (int i = 0; i < n; ++i) t += part[i];
-    *loss = t / den;
+    double q = 0.0, nn = 0.0;
+    for (int i = 0; i < n; ++i) {
+      q += part[2 * i];
+      nn += part[2 * i + 1];
+    }
+    loss[0] = (q > 0.0) ? 1.0 - nn * nn / (den * q) : 1.0;
+    loss[1] = q;
+    loss[2] = nn;
   }
 }
 
 // dloss/dL_j (lower-triangular entries).
-__global__ void k_tr_dL(TrainArgs a, double den) {
+__global__ void k_tr_dL(TrainArgs a, double den, const double* qn) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= a.nf) return;
   const double* Ci = a.Ci + 36 * static_cast<int64_t>(j);
+  const double q = qn[1], nn = qn[2];
+  const double c = (q > 0.0) ? 2.0 * nn / (den * q) : 0.0, astar = (q > 0.0) ? nn / q : 0.0;
   double g[6], bj[6];
   for (int r = 0; r < 6; ++r) {
-    g[r] = -2.0 * a.Se[6 * j + r] / den;
     bj[r] = a.b[6 * j + r];
+    g[r] = c * (astar * a.Se[6 * j + r] - bj[r]);
   }
   // Gm = Ci G Ci^T with G = g b^T: Gm = (Ci g)(Ci b)^T
   double cg[6], cb[6];
@@ -544,8 +565,8 @@ cudaError_t PcgTrainSet::reserve(int nf, int64_t nnzb) {
   if ((e = ws_alloc(this, &Ci, n * 36)) != cudaSuccess) return e;
   if ((e = ws_alloc(this, &evec, 6 * n)) != cudaSuccess) return e;
   if ((e = ws_alloc(this, &Se, 6 * n)) != cudaSuccess) return e;
-  if ((e = ws_alloc(this, &loss_part, 4096)) != cudaSuccess) return e;
-  if ((e = ws_alloc(this, &loss, 1)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &loss_part, 2 * 4096)) != cudaSuccess) return e;
+  if ((e = ws_alloc(this, &loss, 4)) != cudaSuccess) return e;
   if ((e = ws_alloc(this, &dL, n * kPcgOut)) != cudaSuccess) return e;
   if ((e = ws_alloc(this, &dHa, nh)) != cudaSuccess) return e;
   if ((e = ws_alloc(this, &dHb, nh)) != cudaSuccess) return e;
@@ -617,7 +638,7 @@ cudaError_t pcg_loss_grad(PcgModel& m, PcgTrainSet& t, int idx, bool backward, d
   k_tr_loss<<<1, 32, 0, st>>>(t.loss_part, static_cast<int>(mvb), s.den, t.loss);
   if (backward) {
     float* g = m.grad;
-    k_tr_dL<<<nblk(s.nf, 128), 128, 0, st>>>(a, s.den);
+    k_tr_dL<<<nblk(s.nf, 128), 128, 0, st>>>(a, s.den, t.loss);
     k_tr_wgrad<<<nblk(kPcgOut * H, 128), 128, 0, st>>>(s.nf, t.dL, kPcgOut, t.Hs + kPcgLayers * nh, H,
                                                        g + pcg_off_wout(), g + pcg_off_bout());
     k_tr_head_back<<<nblk(nh, kTT), kTT, 0, st>>>(a);

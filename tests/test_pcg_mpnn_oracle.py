@@ -42,7 +42,7 @@ def test_gradient_matches_central_differences():
 
 def test_block_jacobi_point_and_perfect_preconditioner():
     """L = 0 gives block-Jacobi; for a block-diagonal S block-Jacobi is exact
-    (loss 0)."""
+    (loss 0), and the loss does not change when P is scaled."""
     nf = 4
     rows, cols, blocks, b, x = random_system(nf, seed=11, band=0)
     keep = rows == cols  # drop the loop closure: block-diagonal
@@ -53,4 +53,13 @@ def test_block_jacobi_point_and_perfect_preconditioner():
     x = np.linalg.solve(A, b)
     p = np.zeros(M.layout()[1])
     loss, _ = M.forward(p, nf, rows, cols, blocks, b, x, bf16=False)
-    assert loss < 1e-24
+    assert abs(loss) < 1e-12
+    # L = t I for every pose: P = (1 + t^2) x block-Jacobi, same loss
+    rows2, cols2, blocks2, b2, x2 = random_system(nf, seed=12)
+    lay, _ = M.layout()
+    o, _ = lay["b_o"]
+    l0, _ = M.forward(p, nf, rows2, cols2, blocks2, b2, x2, bf16=False)
+    p2 = p.copy()
+    p2[o + np.array([0, 2, 5, 9, 14, 20])] = 0.7
+    l1, _ = M.forward(p2, nf, rows2, cols2, blocks2, b2, x2, bf16=False)
+    assert abs(l0 - l1) < 1e-12 and 0.0 < l0 < 1.0
