@@ -224,6 +224,30 @@ def _step_errors(gp, prob, n_steps):
     return step_errors(gp, prob, n_steps)
 
 
+def _learned_pcg(pkg, prob, device, K, W, n_iter):
+    native = pkg.native
+    if not os.path.exists(native.TRAINED_WEIGHTS):
+        return {"unavailable": "no trained weights (%s)" % os.path.relpath(native.TRAINED_WEIGHTS, ROOT)}
+    with native.PcgModel.load(device=device) as model:
+        with native.Problem(prob, device=device) as gp:
+            gp.set_linear_solver(native.LINSOLVE_PCG_LEARNED, 50, 1e-8, model)
+            gp.init(_fixed(pkg, W + K + 1000, prob.initial_lm_damping))
+            gp.bench_iterations(W, flush_l2=True)
+            ms, _ = gp.bench_iterations(K, flush_l2=True)
+            st = gp.pcg_stats()
+        with native.Problem(prob, device=device) as gp:
+            gp.set_linear_solver(native.LINSOLVE_PCG_LEARNED, 50, 1e-8, model)
+            recs, _ = gp.optimize(_fixed(pkg, n_iter, prob.initial_lm_damping))
+            st2 = gp.pcg_stats()
+    return {"value": K / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / K,
+            "pcg_solves": int(st.solves), "pcg_fallbacks": int(st.fallbacks),
+            "fallback_rate": st.fallbacks / max(1, st.solves),
+            "mean_pcg_iterations": st.iterations / max(1, st.solves),
+            "final_cost": recs[-1].merit, "solve_fallback_rate": st2.fallbacks / max(1, st2.solves),
+            "config": "PCG (learned block preconditioner, 3-layer message passing, hidden 64, BF16 weights), "
+                      "cap 50 iterations, tolerance 1e-8 relative residual, exact factorization as fallback"}
+
+
 def run_gpu(args, ws, rank, local):
     import numpy as np
 
@@ -259,6 +283,11 @@ def run_gpu(args, ws, rank, local):
                            "factor_solve": pr.ms_factor / n_prof, "update": pr.ms_update / n_prof,
                            "cost_decide": pr.ms_cost / n_prof}
         out["lay"] = lay
+    # the learned-PCG solver of the reduced system (PCG with the trained block
+    # preconditioner, 50 iterations to 1e-8, the exact factorization as its
+    # fallback) on the same workload: device-resident rate and the final cost
+    # of the same optimisation, against the plain path
+    out["learned_pcg"] = _learned_pcg(pkg, prob, device, K, W, wl["n_iter"]) if rank == 0 else None
     # the LM step against an FP64 LDL^T of the same reduced system, first steps
     # from the workload's start (not timed)
     if rank == 0 and not args.no_cpu_baseline:
@@ -602,6 +631,14 @@ def main():
                 "pinned_host": out["pinned"]},
         "clocks": out["clk"],
     }
+    lp = out.get("learned_pcg")
+    if lp:
+        if "value" in lp:
+            gm = out.get("gpu_merits", [])
+            lp["ratio_vs_plain"] = lp["value"] / value
+            if gm:
+                lp["final_cost_rel_gap_vs_plain"] = abs(lp["final_cost"] - gm[-1]) / abs(gm[-1])
+        line["learned_pcg"] = lp
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         n_iter = WORKLOADS[args.workload]["n_iter"]

@@ -854,6 +854,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   // Jacobian-side products move the step by percents (measured on 300- and
   // 1500-camera loops).
   s.lin_dd = loop_shaped ? 1 : 0;
+  s.lmk_dd_ok = (s.lin_dd && s.nlchunk > 0 && sgba::landmark_dd_setup(s.lmk_cap) == 0) ? 1 : 0;
   if (s.lin_dd) {
     if ((st = dev_alloc(p, &d.res_lo, P.no))) return st;
     if ((st = dev_alloc(p, &d.res_lo_t, P.no))) return st;

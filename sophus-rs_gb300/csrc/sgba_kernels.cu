@@ -912,6 +912,196 @@ __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) 
   }
 }
 
+// The float-float landmark pass of loop-shaped problems by chunks of
+// consecutive points (<= kLmkTerms terms): every lane busy on a term (a
+// point's track is ~8 terms there, so a warp per point left 3/4 of its lanes
+// idle).  Pass A, a thread per term: float-float Jacobians (kept in shared
+// memory), Huber-weighted residual, the term's V and J_m^T r~ contributions.
+// Pass B, a thread per point: the sums in term order, damping, float-float
+// Cholesky and C^-1, C^-1 b.  Pass C, a thread per term: W = sum J_p^T J_m
+// over the term's observations and Z = W C^-T in float-float.  The same
+// arithmetic as k_landmark's float-float path; only the order of the sums
+// over a point's terms differs (sequential here, a lane tree there).
+constexpr int kLmkDDTermFloats = 18 + 36;  // 9 float-float sums + the Jacobians (18 float-float)
+
+__global__ void __launch_bounds__(256) k_landmark_chunks_dd(LinArgs a, Ctrl* ctrl) {
+  if (halted(ctrl)) return;
+  extern __shared__ float lsd[];               // [cap][kLmkDDTermFloats]
+  __shared__ float sci[kLmkTerms][12];         // C^-1 of each point of the chunk (float-float)
+  __shared__ unsigned char sok[kLmkTerms];
+  __shared__ double smax[8];
+  const int tid = threadIdx.x;
+  const double nu = ctrl->nu;
+  double tmax = 0.0;
+  for (int c = blockIdx.x; c < a.nchunk; c += gridDim.x) {
+    const int p0 = a.chunk_pt[c], p1 = a.chunk_pt[c + 1];
+    const int64_t t0 = a.pt_g_begin[p0];
+    const int nt = static_cast<int>(a.pt_g_begin[p1] - t0);
+    // pass A
+    for (int t = tid; t < nt; t += blockDim.x) {
+      const int64_t g = t0 + t;
+      const int i = a.g_pt[g];
+      const dd px = dd_from_double(a.points[3 * i + 0]);
+      const dd py = dd_from_double(a.points[3 * i + 1]);
+      const dd pz = dd_from_double(a.points[3 * i + 2]);
+      JacD J;
+      jacobians_dd(a.pose_dd + 24 * a.g_pose[g], px, py, pz, a.fxd, a.fyd, &J);
+      float* ts = lsd + static_cast<int64_t>(t) * kLmkDDTermFloats;
+#pragma unroll
+      for (int k = 0; k < 12; ++k) { ts[18 + 2 * k] = J.jp[k].hi; ts[19 + 2 * k] = J.jp[k].lo; }
+#pragma unroll
+      for (int k = 0; k < 6; ++k) { ts[42 + 2 * k] = J.jm[k].hi; ts[43 + 2 * k] = J.jm[k].lo; }
+      dd acc[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) acc[k] = dd_make(0.f, 0.f);
+      const dd* m = J.jm;
+      for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+        const float2 r = a.res[o], rl = a.res_lo[o];
+        dd r0, r1;
+        huber_weighted_dd(a.huber, a.huber_dd, dd_make(r.x, rl.x), dd_make(r.y, rl.y), &r0, &r1);
+        acc[0] = dd_add(acc[0], dd_add(dd_mul(m[0], m[0]), dd_mul(m[3], m[3])));
+        acc[1] = dd_add(acc[1], dd_add(dd_mul(m[0], m[1]), dd_mul(m[3], m[4])));
+        acc[2] = dd_add(acc[2], dd_add(dd_mul(m[0], m[2]), dd_mul(m[3], m[5])));
+        acc[3] = dd_add(acc[3], dd_add(dd_mul(m[1], m[1]), dd_mul(m[4], m[4])));
+        acc[4] = dd_add(acc[4], dd_add(dd_mul(m[1], m[2]), dd_mul(m[4], m[5])));
+        acc[5] = dd_add(acc[5], dd_add(dd_mul(m[2], m[2]), dd_mul(m[5], m[5])));
+        acc[6] = dd_add(acc[6], dd_add(dd_mul(m[0], r0), dd_mul(m[3], r1)));
+        acc[7] = dd_add(acc[7], dd_add(dd_mul(m[1], r0), dd_mul(m[4], r1)));
+        acc[8] = dd_add(acc[8], dd_add(dd_mul(m[2], r0), dd_mul(m[5], r1)));
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) { ts[2 * k] = acc[k].hi; ts[2 * k + 1] = acc[k].lo; }
+    }
+    __syncthreads();
+    // pass B
+    for (int q = tid; q < p1 - p0; q += blockDim.x) {
+      const int i = p0 + q;
+      const int mb = a.pt_mb[i];
+      sok[q] = 0;
+      if (mb < 0) continue;
+      const int tb = static_cast<int>(a.pt_g_begin[i] - t0), te = static_cast<int>(a.pt_g_begin[i + 1] - t0);
+      dd acc[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) acc[k] = dd_make(0.f, 0.f);
+      for (int t = tb; t < te; ++t) {
+        const float* ts = lsd + static_cast<int64_t>(t) * kLmkDDTermFloats;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] = dd_add(acc[k], dd_make(ts[2 * k], ts[2 * k + 1]));
+      }
+      const dd damp = dd_from_double(nu * a.cnt_m[mb]);
+      dd Vd[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) Vd[k] = acc[k];
+      Vd[0] = dd_add(Vd[0], damp);
+      Vd[3] = dd_add(Vd[3], damp);
+      Vd[5] = dd_add(Vd[5], damp);
+      dd b[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) b[k] = dd_neg(acc[6 + k]);
+      double* bp = a.bm + 3 * mb;
+      bp[0] = dd_to_double(b[0]);
+      bp[1] = dd_to_double(b[1]);
+      bp[2] = dd_to_double(b[2]);
+      tmax = fmax(tmax, fmax(fabs(bp[0]), fmax(fabs(bp[1]), fabs(bp[2]))));
+      bool ok = Vd[0].hi > 0.0f;
+      const dd e00 = dd_sqrt(Vd[0]);
+      const dd e10 = dd_div(Vd[1], e00), e20 = dd_div(Vd[2], e00);
+      const dd u11 = dd_sub(Vd[3], dd_mul(e10, e10));
+      ok = ok && u11.hi > 0.0f;
+      const dd e11 = dd_sqrt(u11);
+      const dd e21 = dd_div(dd_sub(Vd[4], dd_mul(e20, e10)), e11);
+      const dd u22 = dd_sub(dd_sub(Vd[5], dd_mul(e20, e20)), dd_mul(e21, e21));
+      ok = ok && u22.hi > 0.0f;
+      const dd e22 = dd_sqrt(u22);
+      const dd one = dd_make(1.0f, 0.0f);
+      dd I[6];
+      I[0] = dd_div(one, e00);
+      I[2] = dd_div(one, e11);
+      I[5] = dd_div(one, e22);
+      I[1] = dd_neg(dd_div(dd_mul(e10, I[0]), e11));
+      I[4] = dd_neg(dd_div(dd_mul(e21, I[2]), e22));
+      I[3] = dd_neg(dd_div(dd_add(dd_mul(e20, I[0]), dd_mul(e21, I[1])), e22));
+#pragma unroll
+      for (int k = 0; k < 6; ++k) ok = ok && isfinite(I[k].hi);
+      if (!ok) {
+        atomicExch(a.fail, 1);
+        continue;
+      }
+      float* ci = a.cinv + 12 * mb;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        ci[2 * k] = I[k].hi;
+        ci[2 * k + 1] = I[k].lo;
+        sci[q][2 * k] = I[k].hi;
+        sci[q][2 * k + 1] = I[k].lo;
+      }
+      const dd cv0 = dd_mul(b[0], I[0]);
+      const dd cv1 = dd_add(dd_mul(b[0], I[1]), dd_mul(b[1], I[2]));
+      const dd cv2 = dd_add(dd_add(dd_mul(b[0], I[3]), dd_mul(b[1], I[4])), dd_mul(b[2], I[5]));
+      float* cvp = a.cvec + 6 * mb;
+      cvp[0] = cv0.hi; cvp[1] = cv0.lo; cvp[2] = cv1.hi; cvp[3] = cv1.lo; cvp[4] = cv2.hi; cvp[5] = cv2.lo;
+      sok[q] = 1;
+    }
+    __syncthreads();
+    // pass C
+    for (int t = tid; t < nt; t += blockDim.x) {
+      const int64_t g = t0 + t;
+      const int i = a.g_pt[g];
+      const int q = i - p0;
+      if (!sok[q]) continue;
+      const int pj = a.g_pose[g];
+      if (a.pose_fb[pj] < 0) continue;
+      const float* ts = lsd + static_cast<int64_t>(t) * kLmkDDTermFloats;
+      dd jp[12], jm[6];
+#pragma unroll
+      for (int k = 0; k < 12; ++k) jp[k] = dd_make(ts[18 + 2 * k], ts[19 + 2 * k]);
+#pragma unroll
+      for (int k = 0; k < 6; ++k) jm[k] = dd_make(ts[42 + 2 * k], ts[43 + 2 * k]);
+      dd Wd[18];
+#pragma unroll
+      for (int k = 0; k < 18; ++k) Wd[k] = dd_make(0.f, 0.f);
+      for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+#pragma unroll
+          for (int u = 0; u < 3; ++u)
+            Wd[r * 3 + u] = dd_add(Wd[r * 3 + u], dd_add(dd_mul(jp[r], jm[u]), dd_mul(jp[6 + r], jm[3 + u])));
+      }
+      dd I[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) I[k] = dd_make(sci[q][2 * k], sci[q][2 * k + 1]);
+      float Z[20];
+      float* zd = a.zdd + kZD * g;
+#pragma unroll
+      for (int r = 0; r < 6; ++r) {
+        const dd z0 = dd_mul(I[0], Wd[r * 3 + 0]);
+        const dd z1 = dd_add(dd_mul(I[1], Wd[r * 3 + 0]), dd_mul(I[2], Wd[r * 3 + 1]));
+        const dd z2 = dd_add(dd_add(dd_mul(I[3], Wd[r * 3 + 0]), dd_mul(I[4], Wd[r * 3 + 1])), dd_mul(I[5], Wd[r * 3 + 2]));
+        Z[r * 3 + 0] = z0.hi + z0.lo;
+        Z[r * 3 + 1] = z1.hi + z1.lo;
+        Z[r * 3 + 2] = z2.hi + z2.lo;
+        zd[6 * r + 0] = z0.hi; zd[6 * r + 1] = z0.lo;
+        zd[6 * r + 2] = z1.hi; zd[6 * r + 3] = z1.lo;
+        zd[6 * r + 4] = z2.hi; zd[6 * r + 5] = z2.lo;
+      }
+      Z[18] = 1.f;  // float-float Z in zdd
+      Z[19] = 0.f;
+      float4* dst = reinterpret_cast<float4*>(a.zmat + kZS * g);
+#pragma unroll
+      for (int u = 0; u < 5; ++u) dst[u] = make_float4(Z[4 * u], Z[4 * u + 1], Z[4 * u + 2], Z[4 * u + 3]);
+    }
+    __syncthreads();
+  }
+  for (int off = 16; off > 0; off >>= 1) tmax = fmax(tmax, __shfl_xor_sync(0xffffffffu, tmax, off));
+  if ((tid & 31) == 0) smax[tid >> 5] = tmax;
+  __syncthreads();
+  if (tid == 0) {
+    double m = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) m = fmax(m, smax[q]);
+    atomic_max_nonneg(&ctrl->max_grad_bits, m);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Camera pass: one CTA per tile of terms of one free pose.  Accumulates
 // U_j = sum J_pose^T J_pose (21 upper entries), g_j = sum J_pose^T r~ and the
@@ -2032,6 +2222,12 @@ static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
 // queued, or (final Hessian pass, no chunk table, or the float-float
 // linearization) the warp-per-point kernel.
 static int launch_landmark(const Sizes& s, const Dev& d, LinArgs la, cudaStream_t st, bool zero_slow = true) {
+  if (!la.use_override && s.nlchunk > 0 && s.lin_dd && s.lmk_dd_ok) {
+    const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
+    k_landmark_chunks_dd<<<grid, 256, sizeof(float) * kLmkDDTermFloats * static_cast<size_t>(s.lmk_cap), st>>>(
+        la, d.ctrl);
+    return 1;
+  }
   if (!la.use_override && s.nlchunk > 0 && !s.lin_dd) {
     if (zero_slow) cudaMemsetAsync(d.slow_count, 0, sizeof(int32_t), st);
     const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
@@ -2053,6 +2249,13 @@ int landmark_setup(int cap) {
                  cudaSuccess
              ? 0
              : -1;
+}
+
+int landmark_dd_setup(int cap) {
+  const size_t bytes = sizeof(float) * kLmkDDTermFloats * static_cast<size_t>(cap);
+  if (bytes > 200 * 1024) return -1;
+  if (bytes <= 48 * 1024) return 0;
+  return raise_dynamic_smem(reinterpret_cast<const void*>(k_landmark_chunks_dd), bytes) == cudaSuccess ? 0 : -1;
 }
 
 int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_override,

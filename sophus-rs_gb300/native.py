@@ -462,8 +462,19 @@ def batch_optimize(problems, params):
     return out
 
 
+TRAINED_WEIGHTS = os.path.join(_HERE, "weights", "pcg_mpnn_loop.npz")
+
+
 class PcgModel:
     """Parameters of the learned block preconditioner (sgba_pcg_model)."""
+
+    @classmethod
+    def load(cls, path=TRAINED_WEIGHTS, device=0):
+        """A model with the parameters saved by pcg_train.py (an .npz with
+        `params`, FP32)."""
+        with np.load(path) as z:
+            params = np.asarray(z["params"], dtype=np.float32)
+        return cls(device=device, params=params)
 
     def __init__(self, device=0, seed=20261203, params=None):
         h = C.c_void_p()
