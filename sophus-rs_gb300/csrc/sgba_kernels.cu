@@ -1613,61 +1613,49 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
       const int pj = a.g_pose[g];
       const int fb = a.pose_fb[pj];
       if (fb < 0) continue;
-      if (gauge) {
-        const double* T = a.poses + 7 * static_cast<int64_t>(pj);
-        const dd v3 = dd_from_double(T[4] - a.cx), v4 = dd_from_double(T[5] - a.cy), v5 = dd_from_double(T[6] - a.cz);
-        const float* zd = (a.zdd || a.zdd_flagged) ? (a.zdd ? a.zdd : a.zdd_flagged) + kZD * g : nullptr;
-        float Zf[20];
-        load_z(a.zmat, static_cast<int>(g), Zf);
-        const bool use_dd = a.zdd || (Zf[18] != 0.f && a.zdd_flagged);
+      // Z of the term, read once: float-float under the float-float
+      // linearization and for the points rebuilt in float-float (C^-T
+      // amplifies the rounding of Z along their weakly held direction), FP32
+      // otherwise
+      float zr[36];
+      bool use_dd = a.zdd != nullptr;
+      if (!use_dd) {
+        float Z[20];
+        load_z(a.zmat, static_cast<int>(g), Z);
+        use_dd = Z[18] != 0.f && a.zdd_flagged;
+        if (!use_dd) {
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-          if (use_dd) {
-            tg[q] = dd_add(tg[q], dd_mul(v3, dd_make(zd[6 * 3 + 2 * q], zd[6 * 3 + 2 * q + 1])));
-            tg[q] = dd_add(tg[q], dd_mul(v4, dd_make(zd[6 * 4 + 2 * q], zd[6 * 4 + 2 * q + 1])));
-            tg[q] = dd_add(tg[q], dd_mul(v5, dd_make(zd[6 * 5 + 2 * q], zd[6 * 5 + 2 * q + 1])));
-          } else {
-            tg[q] = dd_add(tg[q], dd_mul_f(v3, Zf[3 * 3 + q]));
-            tg[q] = dd_add(tg[q], dd_mul_f(v4, Zf[4 * 3 + q]));
-            tg[q] = dd_add(tg[q], dd_mul_f(v5, Zf[5 * 3 + q]));
+          for (int k = 0; k < 18; ++k) {
+            zr[2 * k] = Z[k];
+            zr[2 * k + 1] = 0.f;
           }
         }
       }
+      if (use_dd) {
+        const float4* zp = reinterpret_cast<const float4*>((a.zdd ? a.zdd : a.zdd_flagged) + kZD * g);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          const float4 v = __ldg(zp + k);
+          zr[4 * k] = v.x; zr[4 * k + 1] = v.y; zr[4 * k + 2] = v.z; zr[4 * k + 3] = v.w;
+        }
+      }
+      // entry (r, q) of Z: (zr[6 r + 2 q], zr[6 r + 2 q + 1]) as (hi, lo)
       const float2* xp = reinterpret_cast<const float2*>(a.xdd) + 6 * fb;
-      if (a.zdd) {
-        const float* zd = a.zdd + kZD * g;
 #pragma unroll
-        for (int r = 0; r < 6; ++r) {
-          const float2 xv = xp[r];
-          const dd x = dd_make(xv.x, xv.y);
+      for (int r = 0; r < 6; ++r) {
+        const float2 xv = xp[r];
+        const dd x = dd_make(xv.x, xv.y);
 #pragma unroll
-          for (int q = 0; q < 3; ++q) t[q] = dd_add(t[q], dd_mul(x, dd_make(zd[6 * r + 2 * q], zd[6 * r + 2 * q + 1])));
-        }
-      } else {
-        float Z[20];
-        load_z(a.zmat, static_cast<int>(g), Z);
-        if (Z[18] != 0.f && a.zdd_flagged) {
-          // a point rebuilt in float-float: C^-T amplifies the rounding of Z
-          // along its weakly held direction, so Z^T dx_f is summed from the
-          // float-float Z
-          const float* zd = a.zdd_flagged + kZD * g;
+        for (int q = 0; q < 3; ++q) t[q] = dd_add(t[q], dd_mul(x, dd_make(zr[6 * r + 2 * q], zr[6 * r + 2 * q + 1])));
+      }
+      if (gauge) {
+        const double* T = a.poses + 7 * static_cast<int64_t>(pj);
+        const dd v[3] = {dd_from_double(T[4] - a.cx), dd_from_double(T[5] - a.cy), dd_from_double(T[6] - a.cz)};
 #pragma unroll
-          for (int r = 0; r < 6; ++r) {
-            const float2 xv = xp[r];
-            const dd x = dd_make(xv.x, xv.y);
+        for (int r = 3; r < 6; ++r)
 #pragma unroll
-            for (int q = 0; q < 3; ++q)
-              t[q] = dd_add(t[q], dd_mul(x, dd_make(zd[6 * r + 2 * q], zd[6 * r + 2 * q + 1])));
-          }
-        } else {
-#pragma unroll
-          for (int r = 0; r < 6; ++r) {
-            const float2 xv = xp[r];
-            const dd x = dd_make(xv.x, xv.y);
-#pragma unroll
-            for (int q = 0; q < 3; ++q) t[q] = dd_add(t[q], dd_mul_f(x, Z[r * 3 + q]));
-          }
-        }
+          for (int q = 0; q < 3; ++q)
+            tg[q] = dd_add(tg[q], dd_mul(v[r - 3], dd_make(zr[6 * r + 2 * q], zr[6 * r + 2 * q + 1])));
       }
     }
     // float-float sum over the lanes: fixed tree through shared memory
