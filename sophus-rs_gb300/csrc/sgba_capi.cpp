@@ -855,6 +855,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   // 1500-camera loops).
   s.lin_dd = loop_shaped ? 1 : 0;
   s.lmk_dd_ok = (s.lin_dd && s.nlchunk > 0 && sgba::landmark_dd_setup(s.lmk_cap) == 0) ? 1 : 0;
+  s.bsub_chunks_ok = (s.nlchunk > 0 && sgba::backsub_chunks_setup(s.lmk_cap) == 0) ? 1 : 0;
   if (s.lin_dd) {
     if ((st = dev_alloc(p, &d.res_lo, P.no))) return st;
     if ((st = dev_alloc(p, &d.res_lo_t, P.no))) return st;

@@ -303,6 +303,7 @@ struct Sizes {
   int band_ring;      // its row slots per CTA
   int lin_dd;          // float-float linearization (Jacobians, products and Z in float-float)
   int lmk_dd_ok;       // the chunked float-float landmark pass fits (else the warp-per-point kernel)
+  int bsub_chunks_ok;  // the chunked back-substitution fits (else the warp-per-point kernel)
   int pcg_mode;        // 0 exact factorization; 1 PCG, block-Jacobi; 2 PCG, learned correction (fallback: exact)
   int pcg_max_iters;
   double pcg_tol;      // relative residual of the Jacobi-scaled system
@@ -331,6 +332,7 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st);
 int cost_partials_needed(const Sizes& s);  // reduction partial slots
 int landmark_setup(int cap);  // dynamic shared memory of the chunked landmark pass (0 = ok)
 int landmark_dd_setup(int cap);  // the same for its float-float variant (0 = ok)
+int backsub_chunks_setup(int cap);  // the chunked back-substitution (0 = ok)
 int solver_launch_count(const Sizes& s);
 
 // Single-launch cluster solver (sgba_dense.cu): chooses the cluster size for

@@ -1717,6 +1717,125 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
   }
 }
 
+// Back-substitution by chunks of consecutive points (the landmark pass's
+// chunks): a thread per term forms Z_g^T dx_f and Z_g^T v_f (float-float),
+// then a thread per point sums its terms in order and applies C^-T.  Same
+// arithmetic per term as k_backsub; every lane busy (the loops' tracks of
+// ~8 terms left 3/4 of a warp-per-point kernel idle).
+__global__ void __launch_bounds__(256) k_backsub_chunks(BackArgs a, const int32_t* chunk_pt, int nchunk,
+                                                        const int32_t* g_pt, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  extern __shared__ float bsm[];  // [cap][12]: Z^T dx_f, Z^T v_f as (hi, lo)
+  const bool gauge = a.gauge_kind == 1;
+  const int tid = threadIdx.x;
+  for (int c = blockIdx.x; c < nchunk; c += gridDim.x) {
+    const int p0 = chunk_pt[c], p1 = chunk_pt[c + 1];
+    const int64_t t0 = a.pt_g_begin[p0];
+    const int nt = static_cast<int>(a.pt_g_begin[p1] - t0);
+    for (int t = tid; t < nt; t += blockDim.x) {
+      const int64_t g = t0 + t;
+      const int pj = a.g_pose[g];
+      const int fb = a.pose_fb[pj];
+      dd tt[3] = {dd_make(0.f, 0.f), dd_make(0.f, 0.f), dd_make(0.f, 0.f)};
+      dd tg[3] = {dd_make(0.f, 0.f), dd_make(0.f, 0.f), dd_make(0.f, 0.f)};
+      if (fb >= 0 && a.pt_mb[g_pt[g]] >= 0) {
+        const float2* xp = reinterpret_cast<const float2*>(a.xdd) + 6 * fb;
+        dd v[3] = {dd_make(0.f, 0.f), dd_make(0.f, 0.f), dd_make(0.f, 0.f)};
+        if (gauge) {
+          const double* T = a.poses + 7 * static_cast<int64_t>(pj);
+          v[0] = dd_from_double(T[4] - a.cx);
+          v[1] = dd_from_double(T[5] - a.cy);
+          v[2] = dd_from_double(T[6] - a.cz);
+        }
+        bool use_dd = a.zdd != nullptr;
+        float Z[20];
+        if (!use_dd) {
+          load_z(a.zmat, static_cast<int>(g), Z);
+          use_dd = Z[18] != 0.f && a.zdd_flagged;
+        }
+        if (use_dd) {
+          const float4* zp = reinterpret_cast<const float4*>((a.zdd ? a.zdd : a.zdd_flagged) + kZD * g);
+          float zr[36];
+#pragma unroll
+          for (int k = 0; k < 9; ++k) {
+            const float4 w4 = __ldg(zp + k);
+            zr[4 * k] = w4.x; zr[4 * k + 1] = w4.y; zr[4 * k + 2] = w4.z; zr[4 * k + 3] = w4.w;
+          }
+#pragma unroll
+          for (int r = 0; r < 6; ++r) {
+            const float2 xv = xp[r];
+            const dd x = dd_make(xv.x, xv.y);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              const dd z = dd_make(zr[6 * r + 2 * q], zr[6 * r + 2 * q + 1]);
+              tt[q] = dd_add(tt[q], dd_mul(x, z));
+              if (gauge && r >= 3) tg[q] = dd_add(tg[q], dd_mul(v[r - 3], z));
+            }
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < 6; ++r) {
+            const float2 xv = xp[r];
+            const dd x = dd_make(xv.x, xv.y);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              tt[q] = dd_add(tt[q], dd_mul_f(x, Z[r * 3 + q]));
+              if (gauge && r >= 3) tg[q] = dd_add(tg[q], dd_mul_f(v[r - 3], Z[r * 3 + q]));
+            }
+          }
+        }
+      }
+      float* ts = bsm + static_cast<int64_t>(t) * 12;
+#pragma unroll
+      for (int q = 0; q < 3; ++q) {
+        ts[2 * q] = tt[q].hi;
+        ts[2 * q + 1] = tt[q].lo;
+        ts[6 + 2 * q] = tg[q].hi;
+        ts[7 + 2 * q] = tg[q].lo;
+      }
+    }
+    __syncthreads();
+    for (int q = tid; q < p1 - p0; q += blockDim.x) {
+      const int i = p0 + q;
+      const int mb = a.pt_mb[i];
+      if (mb < 0) continue;
+      const int tb = static_cast<int>(a.pt_g_begin[i] - t0), te = static_cast<int>(a.pt_g_begin[i + 1] - t0);
+      dd sm[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) sm[k] = dd_make(0.f, 0.f);
+      for (int t = tb; t < te; ++t) {
+        const float* ts = bsm + static_cast<int64_t>(t) * 12;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) sm[k] = dd_add(sm[k], dd_make(ts[2 * k], ts[2 * k + 1]));
+      }
+      const float* cp = a.cinv + 12 * mb;  // 00 10 11 20 21 22 as (hi, lo)
+      dd ci[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) ci[k] = dd_make(cp[2 * k], cp[2 * k + 1]);
+      const float* cv = a.cvec + 6 * mb;
+      const dd c0 = dd_sub(dd_make(cv[0], cv[1]), sm[0]);
+      const dd c1 = dd_sub(dd_make(cv[2], cv[3]), sm[1]);
+      const dd c2 = dd_sub(dd_make(cv[4], cv[5]), sm[2]);
+      // C^-T * c : (C^-T)[a][b] = Cinv[b][a]
+      const dd d0 = dd_add(dd_add(dd_mul(c0, ci[0]), dd_mul(c1, ci[1])), dd_mul(c2, ci[3]));
+      const dd d1 = dd_add(dd_mul(c1, ci[2]), dd_mul(c2, ci[4]));
+      const dd d2 = dd_mul(c2, ci[5]);
+      a.dm[3 * mb + 0] = dd_to_double(d0);
+      a.dm[3 * mb + 1] = dd_to_double(d1);
+      a.dm[3 * mb + 2] = dd_to_double(d2);
+      if (gauge) {
+        const dd u0 = dd_add(dd_add(dd_mul(sm[3], ci[0]), dd_mul(sm[4], ci[1])), dd_mul(sm[5], ci[3]));
+        const dd u1 = dd_add(dd_mul(sm[4], ci[2]), dd_mul(sm[5], ci[4]));
+        const dd u2 = dd_mul(sm[5], ci[5]);
+        a.um[3 * mb + 0] = -dd_to_double(u0);
+        a.um[3 * mb + 1] = -dd_to_double(u1);
+        a.um[3 * mb + 2] = -dd_to_double(u2);
+      }
+    }
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Gauge projection.  With a single constant camera (center c) and no constant
 // points, s -> scale about c is an exact symmetry of the cost, so H v = 0 for
@@ -2202,6 +2321,12 @@ static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
   b.cy = s.gauge_center[1];
   b.cz = s.gauge_center[2];
   b.um = d.gauge_um;
+  if (s.nlchunk > 0 && s.bsub_chunks_ok) {
+    const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
+    k_backsub_chunks<<<grid, 256, sizeof(float) * 12 * static_cast<size_t>(s.lmk_cap), st>>>(
+        b, d.lmk_chunk_pt, s.nlchunk, d.g_pt, d.ctrl);
+    return 1;
+  }
   k_backsub<<<warp_grid(s.np, 8, 4096), 256, 0, st>>>(b, d.ctrl);
   return 1;
 }
@@ -2237,6 +2362,13 @@ int landmark_setup(int cap) {
                  cudaSuccess
              ? 0
              : -1;
+}
+
+int backsub_chunks_setup(int cap) {
+  const size_t bytes = sizeof(float) * 12 * static_cast<size_t>(cap);
+  if (bytes > 200 * 1024) return -1;
+  if (bytes <= 48 * 1024) return 0;
+  return raise_dynamic_smem(reinterpret_cast<const void*>(k_backsub_chunks), bytes) == cudaSuccess ? 0 : -1;
 }
 
 int landmark_dd_setup(int cap) {
