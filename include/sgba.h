@@ -118,6 +118,25 @@ size_t sgba_last_error(char *buf, size_t cap);
  *  crates/sophus_opt/src/nlls/damped_hessian.rs:261-325).  device < 0 keeps
  * the current CUDA device. */
 int sgba_problem_create(const sgba_problem_desc *desc, int32_t device, sgba_problem **out);
+
+/* Options of sgba_problem_create_ex.  intrinsics_free = 1 makes the camera
+ * family Free (the reference's VarKind::Free for the "cams" family: kinds
+ * (F, F, M), pinhole_reprojection.rs:85 J_cam): the four pinhole parameters
+ * fx fy cx cy are optimised with the poses, nu I per reduced term on their
+ * block, as one more (padded) 6-row block of the reduced system.  The block
+ * comes first in the exported patterns and in sgba_debug_last_system (the
+ * reference's family order).  Only the pinhole camera (camera_model 0);
+ * loop-shaped problems (the banded solver) and PCG with free intrinsics are
+ * rejected with SGBA_ERR_UNSUPPORTED. */
+enum { SGBA_CAMERA_PINHOLE = 0 };
+typedef struct {
+  int32_t intrinsics_free;  /* 0 Conditioned (default), 1 Free */
+  int32_t camera_model;     /* SGBA_CAMERA_PINHOLE */
+  int32_t reserved[6];      /* zero */
+} sgba_problem_options;
+/* sgba_problem_create with options (NULL: the defaults). */
+int sgba_problem_create_ex(const sgba_problem_desc *desc, const sgba_problem_options *options, int32_t device,
+                           sgba_problem **out);
 int sgba_problem_destroy(sgba_problem *p);
 
 /* Optimizer::new: validates the solver configuration
@@ -155,6 +174,8 @@ int sgba_batch_optimize(sgba_problem *const *problems, int32_t n, const sgba_opt
 
 /* Current variables (OptimizationSolution.variables). NULL skips a family. */
 int sgba_get_variables(sgba_problem *p, double *poses, double *points);
+/* Current intrinsics fx fy cx cy (changed by the optimisation when free). */
+int sgba_get_intrinsics(sgba_problem *p, double *intrinsics);
 /* Current merit (OptimizationSolution.final_cost after sgba_optimize). */
 int sgba_get_cost(sgba_problem *p, double *cost);
 /* Overwrite the variables of an existing problem (same structure). */
@@ -172,6 +193,7 @@ typedef struct {
   int32_t band_width;       /* banded solver: band width in scalars (row r holds columns r-w+1..r) */
   int32_t border_rows;      /* banded solver: dense border rows at the end (loop closures) */
   int32_t float_float_lin;  /* 1: Jacobians, products and Z in float-float (loop-shaped problems) */
+  int32_t intrinsics_rows;  /* 6 when the intrinsics are free (their padded block in S), else 0 */
 } sgba_layout;
 /* Reduced camera system solvers (chosen at sgba_problem_create from the size
  * and the block pattern of S). */
@@ -189,8 +211,9 @@ int sgba_get_layout(sgba_problem *p, sgba_layout *out);
 int sgba_export_pattern(sgba_problem *p, int32_t *h_rows, int32_t *h_cols, int32_t *s_rows,
                         int32_t *s_cols);
 
-/* Linear system of the most recent step: S (dense 6nf x 6nf, row-major,
- * lower triangle valid), reduced rhs (6nf) and the step delta (6nf + 3nm).
+/* Linear system of the most recent step: S (dense n x n, row-major, lower
+ * triangle valid, n = intrinsics_rows + 6nf), reduced rhs (n) and the step
+ * delta (n + 3nm); with free intrinsics their (padded) block comes first.
  * NULL skips an output.  Used to compare each LM step with an FP64 LDLT. */
 int sgba_debug_last_system(sgba_problem *p, double *s_dense, double *rhs, double *delta);
 

@@ -134,6 +134,16 @@ pub struct sgba_layout {
     pub band_width: i32,
     pub border_rows: i32,
     pub float_float_lin: i32,
+    pub intrinsics_rows: i32,
+}
+
+/// Options of `sgba_problem_create_ex` (free pinhole intrinsics).
+#[repr(C)]
+#[derive(Debug, Clone, Copy, Default)]
+pub struct sgba_problem_options {
+    pub intrinsics_free: i32,
+    pub camera_model: i32,
+    pub reserved: [i32; 6],
 }
 
 /// Launch count and device times of the last `sgba_optimize`.
@@ -197,6 +207,13 @@ extern "C" {
     pub fn sgba_abi_version() -> i32;
     pub fn sgba_last_error(buf: *mut c_char, cap: usize) -> usize;
     pub fn sgba_problem_create(desc: *const sgba_problem_desc, device: i32, out: *mut *mut sgba_problem) -> c_int;
+    pub fn sgba_problem_create_ex(
+        desc: *const sgba_problem_desc,
+        options: *const sgba_problem_options,
+        device: i32,
+        out: *mut *mut sgba_problem,
+    ) -> c_int;
+    pub fn sgba_get_intrinsics(p: *mut sgba_problem, intrinsics: *mut f64) -> c_int;
     pub fn sgba_problem_destroy(p: *mut sgba_problem) -> c_int;
     pub fn sgba_optimizer_init(p: *mut sgba_problem, params: *const sgba_opt_params) -> c_int;
     pub fn sgba_optimizer_step(p: *mut sgba_problem, record: *mut sgba_iter_record) -> c_int;

@@ -111,6 +111,7 @@ constexpr int32_t kMaxDenseFree = 4096;  // reduced-camera-system limit (6 * 409
 
 struct sgba_problem {
   Plan plan;
+  int intr_free = 0;  // the pinhole intrinsics are a Free family (sgba_problem_create_ex)
   Sizes sz{};
   Dev d;
   int device = 0;
@@ -708,7 +709,8 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   s.no = P.no;
   s.ng = P.ng;
   s.ntiles = static_cast<int64_t>(P.tile_fb.size());
-  s.n6 = 6 * P.nf;
+  s.intr_free = p->intr_free;
+  s.n6 = 6 * P.nf + (p->intr_free ? 6 : 0);
   for (int k = 0; k < 4; ++k) s.intr[k] = desc->intrinsics[k];
   s.huber = desc->huber_delta;
   s.gauge_kind = P.gauge_kind;
@@ -779,6 +781,13 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   for (int j = 0; j < P.nc; ++j)
     if (!(0.0 <= poses[7 * j]))
       for (int k = 0; k < 4; ++k) poses[7 * j + k] = -poses[7 * j + k];
+  {
+    // intrinsics: current (4) and trial (4), both from the descriptor
+    std::vector<double> intr(8);
+    for (int k = 0; k < 4; ++k) intr[k] = intr[4 + k] = desc->intrinsics[k];
+    if ((st = dev_upload(p, &d.intr, intr))) return st;
+    d.intr_t = d.intr + 4;
+  }
   if ((st = dev_upload(p, &d.poses, poses))) return st;
   if ((st = dev_upload(p, &d.points, pts))) return st;
   if ((st = dev_alloc(p, &d.poses_t, 7 * static_cast<size_t>(P.nc)))) return st;
@@ -793,6 +802,13 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_alloc(p, &d.bm, 3 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.dm, 3 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.gauge_um, 3 * static_cast<size_t>(P.nm)))) return st;
+  if (p->intr_free) {
+    if ((st = dev_alloc(p, &d.intr_part, 18 * static_cast<size_t>(std::max(P.np, 1))))) return st;
+    if ((st = dev_alloc(p, &d.intr_zk, 24 * static_cast<size_t>(std::max(P.nm, 1))))) return st;
+    if ((st = dev_alloc(p, &d.intr_scj, 24 * static_cast<size_t>(std::max(P.nf, 1))))) return st;
+    if ((st = dev_alloc(p, &d.intr_sum, 22))) return st;
+    SGBA_CK(cudaMemsetAsync(d.intr_sum, 0, sizeof(double) * 22, p->stream));
+  }
   if ((st = dev_alloc(p, &d.bf, 6 * static_cast<size_t>(P.nf)))) return st;
   if ((st = dev_alloc(p, &d.rb, 6 * static_cast<size_t>(P.nf)))) return st;
   if ((st = dev_alloc(p, &d.ufull, 36 * static_cast<size_t>(P.nf)))) return st;
@@ -811,7 +827,10 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   // float-float band solver: the FP32 factor with refinement leaves ~2e-6 in
   // the cost of a 100-camera loop)
   const bool loop_shaped = banded && 2 * (bw / 6) <= P.nf;
-  if (banded && (s.dense_c == 0 ? 4 * (bw / 6) <= P.nf : loop_shaped)) {
+  if (loop_shaped && p->intr_free)
+    return set_error(SGBA_ERR_UNSUPPORTED,
+                     "free intrinsics on a loop-shaped problem (banded float-float solver) are not on this path");
+  if (banded && !p->intr_free && (s.dense_c == 0 ? 4 * (bw / 6) <= P.nf : loop_shaped)) {
     // banded reduced system (sequential / loop problems): band + dense border solver
     int rows = brows, w = bw, c = 0, ring = 0;
     if (sgba::band_setup(s.n6, rows, w, &c, &ring) > 0) {
@@ -954,11 +973,22 @@ size_t sgba_last_error(char* buf, size_t cap) {
 }
 
 int sgba_problem_create(const sgba_problem_desc* desc, int32_t device, sgba_problem** out) {
+  return sgba_problem_create_ex(desc, nullptr, device, out);
+}
+
+int sgba_problem_create_ex(const sgba_problem_desc* desc, const sgba_problem_options* opts, int32_t device,
+                           sgba_problem** out) {
   if (!out) return set_error(SGBA_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
   if (!desc) return set_error(SGBA_ERR_INVALID_ARGUMENT, "desc is NULL");
+  if (opts && opts->camera_model != SGBA_CAMERA_PINHOLE)
+    return set_error(SGBA_ERR_UNSUPPORTED, "camera model %d: only the pinhole camera runs on this path",
+                     opts->camera_model);
+  if (opts && opts->intrinsics_free != 0 && opts->intrinsics_free != 1)
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "intrinsics_free must be 0 or 1");
   sgba_problem* p = new (std::nothrow) sgba_problem();
   if (!p) return set_error(SGBA_ERR_OUT_OF_MEMORY, "host allocation failed");
+  p->intr_free = (opts && opts->intrinsics_free) ? 1 : 0;
   int st = build_plan(desc, &p->plan);
   if (st) { delete p; return st; }
   if (p->plan.nf > kMaxDenseFree) {
@@ -1003,10 +1033,10 @@ int sgba_optimizer_init(sgba_problem* p, const sgba_opt_params* prm) {
   if (!p || !prm) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
   SGBA_CK(cudaSetDevice(p->device));
   // validate_solver_config (crates/sophus_opt/src/nlls/optimizer.rs:649-717)
-  if (p->plan.nf == 0 || p->plan.nm == 0)
+  if ((p->plan.nf == 0 && !p->intr_free) || p->plan.nm == 0)
     return set_error(SGBA_ERR_SCHUR_MISSING_FREE_OR_MARG,
                      "Schur solver needs free and marginalized variables (free scalars %d, marg scalars %d)",
-                     6 * p->plan.nf, 3 * p->plan.nm);
+                     6 * p->plan.nf + (p->intr_free ? 4 : 0), 3 * p->plan.nm);
   if (!std::isfinite(prm->initial_lm_damping))
     return set_error(SGBA_ERR_INVALID_ARGUMENT, "initial_lm_damping is not finite");
   p->params = *prm;
@@ -1161,6 +1191,14 @@ int sgba_set_variables(sgba_problem* p, const double* poses, const double* point
   return SGBA_OK;
 }
 
+int sgba_get_intrinsics(sgba_problem* p, double* intrinsics) {
+  if (!p || !intrinsics) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  SGBA_CK(cudaSetDevice(p->device));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  SGBA_CK(cudaMemcpy(intrinsics, p->d.intr, sizeof(double) * 4, cudaMemcpyDeviceToHost));
+  return SGBA_OK;
+}
+
 int sgba_get_cost(sgba_problem* p, double* cost) {
   if (!p || !cost) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
   if (!p->inited) return set_error(SGBA_ERR_STATE, "no optimizer state (call sgba_optimizer_init)");
@@ -1179,6 +1217,15 @@ int sgba_get_layout(sgba_problem* p, sgba_layout* out) {
   out->n_terms = p->plan.ng;
   out->n_h_blocks = p->plan.n_h_blocks;
   out->n_s_blocks = p->sz.nsb;
+  out->intrinsics_rows = p->intr_free ? 6 : 0;
+  if (p->intr_free) {
+    // the intrinsics block, its coupling to every free pose and marg point with terms
+    int64_t fh = 0, mh = 0;
+    for (int f = 0; f < p->plan.nf; ++f) fh += p->plan.cnt_f[f] > 0;
+    for (int m = 0; m < p->plan.nm; ++m) mh += p->plan.cnt_m[m] > 0;
+    out->n_h_blocks += 1 + fh + mh;
+    out->n_s_blocks += 1 + fh;
+  }
   int64_t np = 0;
   if (!p->plan.sb_pair_begin.empty()) np = p->plan.sb_pair_begin.back();
   out->n_schur_pairs = np;
@@ -1202,21 +1249,36 @@ int sgba_export_pattern(sgba_problem* p, int32_t* h_rows, int32_t* h_cols, int32
       SGBA_CK(cudaMemcpy(g_pose.data(), p->d.g_pose, sizeof(int32_t) * P.ng, cudaMemcpyDeviceToHost));
       SGBA_CK(cudaMemcpy(g_pt.data(), p->d.g_pt, sizeof(int32_t) * P.ng, cudaMemcpyDeviceToHost));
     }
+    // global block order: the intrinsics (when free), free poses, marg points
+    const int o = p->intr_free ? 1 : 0;
     int64_t k = 0;
+    if (o) { h_rows[k] = 0; h_cols[k] = 0; ++k; }
     for (int f = 0; f < P.nf; ++f)
-      if (P.cnt_f[f] > 0) { h_rows[k] = f; h_cols[k] = f; ++k; }
+      if (P.cnt_f[f] > 0) { h_rows[k] = o + f; h_cols[k] = o + f; ++k; }
     for (int m = 0; m < P.nm; ++m)
-      if (P.cnt_m[m] > 0) { h_rows[k] = P.nf + m; h_cols[k] = P.nf + m; ++k; }
+      if (P.cnt_m[m] > 0) { h_rows[k] = o + P.nf + m; h_cols[k] = o + P.nf + m; ++k; }
     for (int64_t g = 0; g < P.ng; ++g) {
       int fb = P.pose_fb[g_pose[g]], mb = P.pt_mb[g_pt[g]];
-      if (fb >= 0 && mb >= 0) { h_rows[k] = P.nf + mb; h_cols[k] = fb; ++k; }
+      if (fb >= 0 && mb >= 0) { h_rows[k] = o + P.nf + mb; h_cols[k] = o + fb; ++k; }
+    }
+    if (o) {
+      for (int f = 0; f < P.nf; ++f)
+        if (P.cnt_f[f] > 0) { h_rows[k] = 1 + f; h_cols[k] = 0; ++k; }
+      for (int m = 0; m < P.nm; ++m)
+        if (P.cnt_m[m] > 0) { h_rows[k] = 1 + P.nf + m; h_cols[k] = 0; ++k; }
     }
   }
   if (s_rows && s_cols) {
-    for (size_t b = 0; b < P.sb_row.size(); ++b) {
-      s_rows[b] = P.sb_row[b];
-      s_cols[b] = P.sb_col[b];
+    const int o = p->intr_free ? 1 : 0;
+    size_t k = 0;
+    if (o) { s_rows[k] = 0; s_cols[k] = 0; ++k; }
+    for (size_t b = 0; b < P.sb_row.size(); ++b, ++k) {
+      s_rows[k] = o + P.sb_row[b];
+      s_cols[k] = o + P.sb_col[b];
     }
+    if (o)
+      for (int f = 0; f < P.nf; ++f)
+        if (P.cnt_f[f] > 0) { s_rows[k] = 1 + f; s_cols[k] = 0; ++k; }
   }
   return SGBA_OK;
 }
@@ -1232,6 +1294,24 @@ int sgba_debug_last_system(sgba_problem* p, double* s_dense, double* rhs, double
     SGBA_CK(cudaMemcpy(delta, p->d.x, sizeof(double) * n6, cudaMemcpyDeviceToHost));
     if (p->plan.nm > 0)
       SGBA_CK(cudaMemcpy(delta + n6, p->d.dm, sizeof(double) * 3 * p->plan.nm, cudaMemcpyDeviceToHost));
+  }
+  if (p->intr_free) {
+    // internally the intrinsics block is last; the reference's order puts it first
+    const size_t kp = n6 - 6;
+    auto perm = [kp](size_t i) { return i < 6 ? kp + i : i - 6; };  // exported index -> internal
+    if (s_dense) {
+      std::vector<double> t(s_dense, s_dense + n6 * n6);
+      for (size_t i = 0; i < n6; ++i)
+        for (size_t j = 0; j < n6; ++j) s_dense[i * n6 + j] = t[perm(i) * n6 + perm(j)];
+    }
+    if (rhs) {
+      std::vector<double> t(rhs, rhs + n6);
+      for (size_t i = 0; i < n6; ++i) rhs[i] = t[perm(i)];
+    }
+    if (delta) {
+      std::vector<double> t(delta, delta + n6);
+      for (size_t i = 0; i < n6; ++i) delta[i] = t[perm(i)];
+    }
   }
   return SGBA_OK;
 }
@@ -1275,7 +1355,7 @@ int sgba_debug_jacobians(sgba_problem* p, int64_t n, const int32_t* cam, const i
 // State blob: magic, sizes, LM scalars, poses, points.
 int sgba_state_save(sgba_problem* p, void* buf, size_t* size) {
   if (!p || !size) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
-  const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np));
+  const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np) + 4);
   if (!buf) { *size = need; return SGBA_OK; }
   if (*size < need) return set_error(SGBA_ERR_INVALID_ARGUMENT, "state buffer too small (%zu < %zu)", *size, need);
   if (!p->inited) return set_error(SGBA_ERR_STATE, "no optimizer state to save");
@@ -1297,6 +1377,7 @@ int sgba_state_save(sgba_problem* p, void* buf, size_t* size) {
   std::memcpy(b + 40, &stp, 8);
   SGBA_CK(cudaMemcpy(b + 64, p->d.poses, sizeof(double) * 7 * nc, cudaMemcpyDeviceToHost));
   if (np > 0) SGBA_CK(cudaMemcpy(b + 64 + sizeof(double) * 7 * nc, p->d.points, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost));
+  SGBA_CK(cudaMemcpy(b + need - 32, p->d.intr, sizeof(double) * 4, cudaMemcpyDeviceToHost));
   *size = need;
   return SGBA_OK;
 }
@@ -1305,7 +1386,7 @@ int sgba_state_load(sgba_problem* p, const void* buf, size_t size) {
   if (!p || !buf) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
   if (!p->inited) return set_error(SGBA_ERR_STATE, "call sgba_optimizer_init before sgba_state_load");
   const char* b = static_cast<const char*>(buf);
-  const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np));
+  const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np) + 4);
   uint64_t magic;
   int32_t nc, np;
   if (size < need) return set_error(SGBA_ERR_INVALID_ARGUMENT, "state blob too small");
@@ -1328,6 +1409,8 @@ int sgba_state_load(sgba_problem* p, const void* buf, size_t size) {
   c.done = 0;
   SGBA_CK(cudaMemcpy(p->d.poses, b + 64, sizeof(double) * 7 * nc, cudaMemcpyHostToDevice));
   if (np > 0) SGBA_CK(cudaMemcpy(p->d.points, b + 64 + sizeof(double) * 7 * nc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice));
+  SGBA_CK(cudaMemcpy(p->d.intr, b + need - 32, sizeof(double) * 4, cudaMemcpyHostToDevice));
+  SGBA_CK(cudaMemcpy(p->d.intr_t, b + need - 32, sizeof(double) * 4, cudaMemcpyHostToDevice));
   SGBA_CK(cudaMemcpy(p->d.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice));
   // residuals of the loaded state
   sgba::launch_init_merit(p->sz, p->d, p->stream);
@@ -1629,6 +1712,7 @@ int sgba_set_linear_solver(sgba_problem* p, const sgba_linear_solver* cfg, const
     if (!(cfg->max_iterations >= 1) || !(cfg->tolerance > 0.0) || !std::isfinite(cfg->tolerance))
       return set_error(SGBA_ERR_INVALID_ARGUMENT, "PCG needs max_iterations >= 1 and a finite tolerance > 0");
     if (p->plan.nf < 1) return set_error(SGBA_ERR_SCHUR_MISSING_FREE_OR_MARG, "no free pose: nothing to solve");
+    if (p->intr_free) return set_error(SGBA_ERR_UNSUPPORTED, "PCG with free intrinsics is not on this path");
     if (model && model->m.device != p->device)
       return set_error(SGBA_ERR_INVALID_ARGUMENT, "model on device %d, problem on device %d", model->m.device,
                        p->device);

@@ -117,6 +117,7 @@ struct DenseArgs {
   const double* poses;
   const int32_t* fb_pose;
   double center[3];
+  int npose;         // rows of the free poses (6 n_f; free intrinsics follow them)
 };
 
 // the factorization is skipped on termination, on a skipped step and when PCG converged
@@ -816,7 +817,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
       float* red = dsm + s_cv.red;
       for (int k = tid; k < npad; k += kThreads) {
         float v = 0.0f;
-        if (k < a.n && k % 6 >= 3) {
+        if (k < a.npose && k % 6 >= 3) {
           const double* tp = a.poses + 7 * a.fb_pose[k / 6];
           v = static_cast<float>(tp[4 + k % 6 - 3] - a.center[k % 6 - 3]) / vd[k];
         }
@@ -1115,6 +1116,7 @@ int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st) {
   a.poses = d.poses;
   a.fb_pose = d.fb_pose;
   for (int k = 0; k < 3; ++k) a.center[k] = s.gauge_center[k];
+  a.npose = 6 * s.nf;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(s.dense_c);
   cfg.blockDim = dim3(kThreads);

@@ -153,6 +153,8 @@ struct Dev {
   double* poses = nullptr;         // nc*7
   double* points = nullptr;        // np*3
   double* poses_t = nullptr;       // trial
+  double* intr = nullptr;          // 4: intrinsics fx fy cx cy (device copy; the kernels read them here)
+  double* intr_t = nullptr;        // 4: trial intrinsics (free intrinsics)
   double* points_t = nullptr;
   float2* res = nullptr;           // residual at current state (sorted obs)
   float2* res_t = nullptr;         // residual at trial state
@@ -191,6 +193,11 @@ struct Dev {
   double* r = nullptr;             // n6 residual
   double* dm = nullptr;            // nm*3 point steps
   double* gauge_um = nullptr;      // nm*3 the free poses' gauge direction back-substituted into the points
+  // free intrinsics (Sizes::intr_free)
+  double* intr_part = nullptr;     // np*18 per-point parts of S_kk, J_k^T r~, Zk c
+  float* intr_zk = nullptr;        // nm*24 Zk = Y C^-T (4x3) as (hi, lo) pairs
+  double* intr_scj = nullptr;      // nf*24 S_kj (4x6)
+  double* intr_sum = nullptr;      // 18 sums + 4 neg_grad of the intrinsics
   double* part = nullptr;          // reduction partials
   int part_cap = 0;
   Ctrl* ctrl = nullptr;
@@ -302,6 +309,7 @@ struct Sizes {
   int band_c;         // its cluster size
   int band_ring;      // its row slots per CTA
   int lin_dd;          // float-float linearization (Jacobians, products and Z in float-float)
+  int intr_free;       // the pinhole intrinsics are Free: one more (padded) 6-row block, last in S
   int lmk_dd_ok;       // the chunked float-float landmark pass fits (else the warp-per-point kernel)
   int bsub_chunks_ok;  // the chunked back-substitution fits (else the warp-per-point kernel)
   int pcg_mode;        // 0 exact factorization; 1 PCG, block-Jacobi; 2 PCG, learned correction (fallback: exact)

@@ -319,7 +319,8 @@ struct CostArgs {
   float2* res_out;
   float2* res_lo_out;  // low parts of the residuals (float-float linearization), or null
   double* partials;
-  dd fx, fy, cx, cy;
+  dd fx, fy, cx, cy;    // intrinsics when intr is null (the allocation-free entry point)
+  const double* intr;   // device intrinsics fx fy cx cy (current or trial), or null
   float huber;
   dd huber_dd;
   int respect_skip;
@@ -335,6 +336,8 @@ __device__ void decide_body(const double* cost_part, int n_cost, const double* u
                             Record* recs, Record* last);
 
 __global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* ctrl) {
+  const dd fx_ = a.intr ? dd_from_double(a.intr[0]) : a.fx, fy_ = a.intr ? dd_from_double(a.intr[1]) : a.fy;
+  const dd cx_ = a.intr ? dd_from_double(a.intr[2]) : a.cx, cy_ = a.intr ? dd_from_double(a.intr[3]) : a.cy;
   if (a.decide && !halted(ctrl) && skipping(ctrl)) {
     // no trial (gradient tolerance or a failed solve): decide at once
     if (blockIdx.x == 0) decide_body(a.partials, 0, a.upd_part, a.n_upd, a.decide, a.recs, a.last);
@@ -359,8 +362,8 @@ __global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* c
     dd u = dd_div(xc[0], xc[2]);
     dd v = dd_div(xc[1], xc[2]);
     double2 z = a.uv[o];
-    dd ru = dd_sub(dd_from_double(z.x), dd_add(dd_mul(u, a.fx), a.cx));
-    dd rv = dd_sub(dd_from_double(z.y), dd_add(dd_mul(v, a.fy), a.cy));
+    dd ru = dd_sub(dd_from_double(z.x), dd_add(dd_mul(u, fx_), cx_));
+    dd rv = dd_sub(dd_from_double(z.y), dd_add(dd_mul(v, fy_), cy_));
     dd n2 = dd_add(dd_mul(ru, ru), dd_mul(rv, rv));
     dd c = n2;
     if (a.huber > 0.0f) {
@@ -448,8 +451,8 @@ struct LinArgs {
   const float* pose_dd;
   const double* points;
   const float2* res;
-  float fx, fy, huber;
-  dd fxd, fyd;
+  const double* intr;  // device intrinsics fx fy cx cy
+  float huber;
   float* zmat;
   float* cinv;   // 6 float-float per point: C^-1 (00 10 11 20 21 22)
   float* cvec;   // 3 float-float per point: C^-1 b_m
@@ -479,6 +482,9 @@ struct LinArgs {
 };
 
 __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
+  const float fx_ = __double2float_rn(a.intr[0]), fy_ = __double2float_rn(a.intr[1]);
+  const dd fxd_ = dd_from_double(a.intr[0]), fyd_ = dd_from_double(a.intr[1]);
+  (void)fx_; (void)fy_; (void)fxd_; (void)fyd_;
   if (halted(ctrl)) return;
   __shared__ float red[8][9][33];
   // float-float path: the Jacobians of each lane's first term (a term with
@@ -508,7 +514,7 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
       const float* P = a.pose_f + 12 * a.g_pose[g];
       for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
         JacF J;
-        jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+        jacobians_f(P, px, py, pz, fx_, fy_, &J);
         float2 r = a.res[o];
         float w = huber_weight_f(a.huber, r.x, r.y);
         float r0 = w * r.x, r1 = w * r.y;
@@ -576,7 +582,7 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
         const bool keep = (g == g0 + lane) && (a.g_begin[g + 1] - a.g_begin[g] == 1);
         for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
           JacD J;
-          jacobians_dd(Pd, pxd, pyd, pzd, a.fxd, a.fyd, &J);
+          jacobians_dd(Pd, pxd, pyd, pzd, fxd_, fyd_, &J);
           if (keep) {
 #pragma unroll
             for (int k = 0; k < 12; ++k) { jcache[wib][2 * k][lane] = J.jp[k].hi; jcache[wib][2 * k + 1][lane] = J.jp[k].lo; }
@@ -680,7 +686,7 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
         for (int k = 0; k < 18; ++k) W[k] = 0.f;
         for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
           JacF J;
-          jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+          jacobians_f(P, px, py, pz, fx_, fy_, &J);
 #pragma unroll
           for (int r = 0; r < 6; ++r)
 #pragma unroll
@@ -707,7 +713,7 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
 #pragma unroll
             for (int k = 0; k < 6; ++k) J.jm[k] = dd_make(jcache[wib][24 + 2 * k][lane], jcache[wib][25 + 2 * k][lane]);
           } else {
-            jacobians_dd(Pd, pxd, pyd, pzd, a.fxd, a.fyd, &J);
+            jacobians_dd(Pd, pxd, pyd, pzd, fxd_, fyd_, &J);
           }
           for (int r = 0; r < 6; ++r)
             for (int q = 0; q < 3; ++q)
@@ -757,6 +763,9 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
 constexpr int kLmkTerms = 256;
 
 __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) {
+  const float fx_ = __double2float_rn(a.intr[0]), fy_ = __double2float_rn(a.intr[1]);
+  const dd fxd_ = dd_from_double(a.intr[0]), fyd_ = dd_from_double(a.intr[1]);
+  (void)fx_; (void)fy_; (void)fxd_; (void)fyd_;
   if (halted(ctrl)) return;
   extern __shared__ float lsm[];        // [cap][9] term contributions
   __shared__ float sci[kLmkTerms][6];   // C^-1 per point of the chunk (FP32)
@@ -780,7 +789,7 @@ __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) 
       float v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
       for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
         JacF J;
-        jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+        jacobians_f(P, px, py, pz, fx_, fy_, &J);
         const float2 r = a.res[o];
         const float w = huber_weight_f(a.huber, r.x, r.y);
         const float r0 = w * r.x, r1 = w * r.y;
@@ -879,7 +888,7 @@ __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) 
       for (int k = 0; k < 18; ++k) W[k] = 0.f;
       for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
         JacF J;
-        jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+        jacobians_f(P, px, py, pz, fx_, fy_, &J);
 #pragma unroll
         for (int r = 0; r < 6; ++r)
 #pragma unroll
@@ -925,6 +934,9 @@ __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) 
 constexpr int kLmkDDTermFloats = 18 + 36;  // 9 float-float sums + the Jacobians (18 float-float)
 
 __global__ void __launch_bounds__(256) k_landmark_chunks_dd(LinArgs a, Ctrl* ctrl) {
+  const float fx_ = __double2float_rn(a.intr[0]), fy_ = __double2float_rn(a.intr[1]);
+  const dd fxd_ = dd_from_double(a.intr[0]), fyd_ = dd_from_double(a.intr[1]);
+  (void)fx_; (void)fy_; (void)fxd_; (void)fyd_;
   if (halted(ctrl)) return;
   extern __shared__ float lsd[];               // [cap][kLmkDDTermFloats]
   __shared__ float sci[kLmkTerms][12];         // C^-1 of each point of the chunk (float-float)
@@ -945,7 +957,7 @@ __global__ void __launch_bounds__(256) k_landmark_chunks_dd(LinArgs a, Ctrl* ctr
       const dd py = dd_from_double(a.points[3 * i + 1]);
       const dd pz = dd_from_double(a.points[3 * i + 2]);
       JacD J;
-      jacobians_dd(a.pose_dd + 24 * a.g_pose[g], px, py, pz, a.fxd, a.fyd, &J);
+      jacobians_dd(a.pose_dd + 24 * a.g_pose[g], px, py, pz, fxd_, fyd_, &J);
       float* ts = lsd + static_cast<int64_t>(t) * kLmkDDTermFloats;
 #pragma unroll
       for (int k = 0; k < 12; ++k) { ts[18 + 2 * k] = J.jp[k].hi; ts[19 + 2 * k] = J.jp[k].lo; }
@@ -1125,17 +1137,21 @@ struct CamArgs {
   const float2* res;
   const float* zmat;
   const float* cvec;
-  float fx, fy, huber;
+  const double* intr;  // device intrinsics fx fy cx cy
+  float huber;
   double* tile_part;
   int with_schur;
   // float-float linearization
   const float* pose_dd;
   const float2* res_lo;
   const float* zdd;
-  dd fxd, fyd, huber_dd;
+  dd huber_dd;
 };
 
 __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const Ctrl* ctrl) {
+  const float fx_ = __double2float_rn(a.intr[0]), fy_ = __double2float_rn(a.intr[1]);
+  const dd fxd_ = dd_from_double(a.intr[0]), fyd_ = dd_from_double(a.intr[1]);
+  (void)fx_; (void)fy_; (void)fxd_; (void)fyd_;
   if (halted(ctrl)) return;
   const int tile = blockIdx.x;
   const int fb = a.tile_fb[tile];
@@ -1155,7 +1171,7 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
     const float pz = __double2float_rn(a.points[3 * pi + 2]);
     for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
       JacF J;
-      jacobians_f(P, px, py, pz, a.fx, a.fy, &J);
+      jacobians_f(P, px, py, pz, fx_, fy_, &J);
       float2 r = a.res[o];
       float w = huber_weight_f(a.huber, r.x, r.y);
       float r0 = w * r.x, r1 = w * r.y;
@@ -1239,6 +1255,9 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
 // cancel ~25x, beyond what FP32 products leave).  Same outputs as
 // k_camera_tiles.
 __global__ void __launch_bounds__(kTileThreads) k_camera_tiles_dd(CamArgs a, const Ctrl* ctrl) {
+  const float fx_ = __double2float_rn(a.intr[0]), fy_ = __double2float_rn(a.intr[1]);
+  const dd fxd_ = dd_from_double(a.intr[0]), fyd_ = dd_from_double(a.intr[1]);
+  (void)fx_; (void)fy_; (void)fxd_; (void)fyd_;
   if (halted(ctrl)) return;
   const int tile = blockIdx.x;
   const int fb = a.tile_fb[tile];
@@ -1255,7 +1274,7 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles_dd(CamArgs a, con
     const dd pz = dd_from_double(a.points[3 * pi + 2]);
     for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
       JacD J;
-      jacobians_dd(Pd, px, py, pz, a.fxd, a.fyd, &J);
+      jacobians_dd(Pd, px, py, pz, fxd_, fyd_, &J);
       const float2 r = a.res[o], rl = a.res_lo[o];
       dd r0, r1;
       huber_weighted_dd(a.huber, a.huber_dd, dd_make(r.x, rl.x), dd_make(r.y, rl.y), &r0, &r1);
@@ -1594,7 +1613,26 @@ struct BackArgs {
   const double* poses;
   double cx, cy, cz;
   double* um;
+  // free intrinsics: dx_m also loses C^-T Zk^T dx_k (dx_k at rows 6 nf .. 6 nf + 3)
+  const float* zk;  // nm x 24 or null
+  int k0;           // 6 nf
 };
+
+// s[q] += (Zk^T dx_k)_q for a point with terms (free intrinsics).
+__device__ __forceinline__ void intr_backsub_term(const BackArgs& a, int mb, dd* s) {
+  const float* zk = a.zk + 24 * static_cast<int64_t>(mb);
+  const float2* xk = reinterpret_cast<const float2*>(a.xdd) + a.k0;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    dd t = s[q];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float2 xv = xk[r];
+      t = dd_add(t, dd_mul(dd_make(xv.x, xv.y), dd_make(zk[2 * (r * 3 + q)], zk[2 * (r * 3 + q) + 1])));
+    }
+    s[q] = t;
+  }
+}
 
 __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
@@ -1698,6 +1736,7 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
     if (lane == 0) {
       dd s[3];
       for (int q = 0; q < 3; ++q) s[q] = dd_make(red[wib][2 * q][0], red[wib][2 * q + 1][0]);
+      if (a.zk && a.pt_g_begin[i + 1] > a.pt_g_begin[i]) intr_backsub_term(a, mb, s);
       const float* cv = a.cvec + 6 * mb;
       dd c0 = dd_sub(dd_make(cv[0], cv[1]), s[0]);
       dd c1 = dd_sub(dd_make(cv[2], cv[3]), s[1]);
@@ -1808,6 +1847,7 @@ __global__ void __launch_bounds__(256) k_backsub_chunks(BackArgs a, const int32_
 #pragma unroll
         for (int k = 0; k < 6; ++k) sm[k] = dd_add(sm[k], dd_make(ts[2 * k], ts[2 * k + 1]));
       }
+      if (a.zk && te > tb) intr_backsub_term(a, mb, sm);
       const float* cp = a.cinv + 12 * mb;  // 00 10 11 20 21 22 as (hi, lo)
       dd ci[6];
 #pragma unroll
@@ -1834,6 +1874,336 @@ __global__ void __launch_bounds__(256) k_backsub_chunks(BackArgs a, const int32_
     }
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// Free pinhole intrinsics (kinds F, F, M: the intrinsics family Free).  The
+// intrinsics k = (fx, fy, cx, cy) are one more free variable that every term
+// touches: J_k = d r / d k = -[[x/z, 0, 1, 0], [0, y/z, 0, 1]] per observation
+// (pinhole_reprojection.rs:85, the camera's dx_params), with the reference's
+// nu I per reduced term on its diagonal.  Internally the intrinsics are the
+// last block of S (rows 6 nf .. 6 nf + 5, padded from 4 to 6 rows with an
+// identity, as the oracle pads them); the step is the same in any order.
+//   per point i:  Y_i = sum J_k^T J_m,  Zk_i = Y_i C_i^-T,
+//   S_kk = sum J_k^T J_k - sum_i Zk_i Zk_i^T + nu n_terms I,
+//   S_kj = sum_{terms of pose j} (J_k^T J_p - Zk_i Z_g^T),
+//   rhs_k = -sum J_k^T r~ - sum_i Zk_i c_i,
+//   dx_m -= C^-T Zk_i^T dx_k in the back-substitution, k <- k + dx_k.
+// Everything in float-float (these problems are small: the dense solvers).
+// ---------------------------------------------------------------------------
+constexpr int kIntrPart = 18;  // per point: S_kk part (10), J_k^T r~ (4), Zk c (4)
+
+struct IntrArgs {
+  int np, nf, n6;
+  int64_t ng;
+  const int64_t* pt_g_begin;
+  const int64_t* g_begin;
+  const int32_t* g_pose;
+  const int32_t* g_pt;
+  const int32_t* pose_fb;
+  const int32_t* pt_mb;
+  const float* pose_dd;
+  const double* points;
+  const float2* res;
+  float huber;
+  dd huber_dd;
+  const double* intr;
+  const float* cinv;
+  const float* cvec;
+  const float* zmat;
+  const float* zdd;          // float-float Z of every term (float-float linearization) or null
+  const float* zdd_flagged;  // float-float Z of flagged terms
+  const int64_t* cam_g;
+  const int64_t* tile_begin;
+  const int64_t* tile_end;
+  const int64_t* fb_tile_begin;
+  double* ipart;  // np x kIntrPart
+  float* zk;      // nm x 24: Zk (4x3) as (hi, lo)
+  double* scj;    // nf x 24: S_kj (4x6)
+  double* isum;   // kIntrPart sums, then -sum J_k^T r~ (4)
+  double* S;
+  float2* S2;
+  double* rb;
+  int fail_check;
+};
+
+// The observation's camera-frame point (float-float) and the projection
+// Jacobians: J_p, J_m as jacobians_dd, J_k rows [-u, 0, -1, 0], [0, -v, 0, -1].
+__device__ void intr_term_jacobians(const float* Pd, dd px, dd py, dd pz, dd fxd, dd fyd, JacD* J, dd* u, dd* v) {
+  dd R[9], t[3];
+  for (int i = 0; i < 9; ++i) R[i] = dd_make(Pd[2 * i], Pd[2 * i + 1]);
+  for (int i = 0; i < 3; ++i) t[i] = dd_make(Pd[18 + 2 * i], Pd[18 + 2 * i + 1]);
+  const dd xc = dd_add(dd_add(dd_add(dd_mul(R[0], px), dd_mul(R[1], py)), dd_mul(R[2], pz)), t[0]);
+  const dd yc = dd_add(dd_add(dd_add(dd_mul(R[3], px), dd_mul(R[4], py)), dd_mul(R[5], pz)), t[1]);
+  const dd zc = dd_add(dd_add(dd_add(dd_mul(R[6], px), dd_mul(R[7], py)), dd_mul(R[8], pz)), t[2]);
+  *u = dd_div(xc, zc);
+  *v = dd_div(yc, zc);
+  jacobians_dd(Pd, px, py, pz, fxd, fyd, J);
+}
+
+// One thread per point: its terms' J_k^T J_k, J_k^T r~, Y = J_k^T J_m, then
+// with the point's C^-1 (landmark pass) Zk = Y C^-T and its parts of S_kk and
+// rhs_k.
+__global__ void __launch_bounds__(128) k_intr_points(IntrArgs a, const Ctrl* ctrl) {
+  if (halted(ctrl)) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.np) return;
+  const dd fxd = dd_from_double(a.intr[0]), fyd = dd_from_double(a.intr[1]);
+  const dd px = dd_from_double(a.points[3 * i]), py = dd_from_double(a.points[3 * i + 1]),
+           pz = dd_from_double(a.points[3 * i + 2]);
+  dd hkk[10], gk[4], Y[12];
+  for (int k = 0; k < 10; ++k) hkk[k] = dd_make(0.f, 0.f);
+  for (int k = 0; k < 4; ++k) gk[k] = dd_make(0.f, 0.f);
+  for (int k = 0; k < 12; ++k) Y[k] = dd_make(0.f, 0.f);
+  const dd one = dd_make(1.0f, 0.0f);
+  for (int64_t g = a.pt_g_begin[i]; g < a.pt_g_begin[i + 1]; ++g) {
+    JacD J;
+    dd u, v;
+    intr_term_jacobians(a.pose_dd + 24 * a.g_pose[g], px, py, pz, fxd, fyd, &J, &u, &v);
+    // J_k (2x4): row 0 = (-u, 0, -1, 0), row 1 = (0, -v, 0, -1)
+    const dd jk[8] = {dd_neg(u), dd_make(0.f, 0.f), dd_neg(one), dd_make(0.f, 0.f),
+                      dd_make(0.f, 0.f), dd_neg(v), dd_make(0.f, 0.f), dd_neg(one)};
+    for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
+      const float2 r = a.res[o];
+      dd r0, r1;
+      huber_weighted_dd(a.huber, a.huber_dd, dd_from_float(r.x), dd_from_float(r.y), &r0, &r1);
+      int k = 0;
+      for (int p = 0; p < 4; ++p) {
+        for (int q = p; q < 4; ++q) {
+          hkk[k] = dd_add(hkk[k], dd_add(dd_mul(jk[p], jk[q]), dd_mul(jk[4 + p], jk[4 + q])));
+          ++k;
+        }
+        gk[p] = dd_add(gk[p], dd_add(dd_mul(jk[p], r0), dd_mul(jk[4 + p], r1)));
+        for (int s2 = 0; s2 < 3; ++s2)
+          Y[p * 3 + s2] = dd_add(Y[p * 3 + s2], dd_add(dd_mul(jk[p], J.jm[s2]), dd_mul(jk[4 + p], J.jm[3 + s2])));
+      }
+    }
+  }
+  double* out = a.ipart + static_cast<int64_t>(i) * kIntrPart;
+  const int mb = a.pt_mb[i];
+  dd zz[10], zc4[4];
+  for (int k = 0; k < 10; ++k) zz[k] = dd_make(0.f, 0.f);
+  for (int k = 0; k < 4; ++k) zc4[k] = dd_make(0.f, 0.f);
+  if (mb >= 0 && a.pt_g_begin[i + 1] > a.pt_g_begin[i]) {
+    const float* cp = a.cinv + 12 * mb;
+    dd I[6];
+    for (int k = 0; k < 6; ++k) I[k] = dd_make(cp[2 * k], cp[2 * k + 1]);
+    const float* cv = a.cvec + 6 * mb;
+    const dd c[3] = {dd_make(cv[0], cv[1]), dd_make(cv[2], cv[3]), dd_make(cv[4], cv[5])};
+    dd Zk[12];
+    for (int r = 0; r < 4; ++r) {
+      Zk[r * 3 + 0] = dd_mul(I[0], Y[r * 3 + 0]);
+      Zk[r * 3 + 1] = dd_add(dd_mul(I[1], Y[r * 3 + 0]), dd_mul(I[2], Y[r * 3 + 1]));
+      Zk[r * 3 + 2] = dd_add(dd_add(dd_mul(I[3], Y[r * 3 + 0]), dd_mul(I[4], Y[r * 3 + 1])), dd_mul(I[5], Y[r * 3 + 2]));
+    }
+    int k = 0;
+    for (int p = 0; p < 4; ++p) {
+      for (int q = p; q < 4; ++q) {
+        dd t = dd_make(0.f, 0.f);
+        for (int s2 = 0; s2 < 3; ++s2) t = dd_add(t, dd_mul(Zk[p * 3 + s2], Zk[q * 3 + s2]));
+        zz[k++] = t;
+      }
+      dd t = dd_make(0.f, 0.f);
+      for (int s2 = 0; s2 < 3; ++s2) t = dd_add(t, dd_mul(Zk[p * 3 + s2], c[s2]));
+      zc4[p] = t;
+    }
+    float* zo = a.zk + 24 * static_cast<int64_t>(mb);
+    for (int k2 = 0; k2 < 12; ++k2) {
+      zo[2 * k2] = Zk[k2].hi;
+      zo[2 * k2 + 1] = Zk[k2].lo;
+    }
+  }
+  for (int k = 0; k < 10; ++k) out[k] = dd_to_double(dd_sub(hkk[k], zz[k]));
+  for (int k = 0; k < 4; ++k) out[10 + k] = dd_to_double(gk[k]);
+  for (int k = 0; k < 4; ++k) out[14 + k] = dd_to_double(zc4[k]);
+}
+
+// One CTA: the per-point parts summed in a fixed order; the intrinsics'
+// neg_grad -sum J_k^T r~ joins the gradient-tolerance maximum.
+__global__ void __launch_bounds__(256) k_intr_reduce(IntrArgs a, Ctrl* ctrl) {
+  if (halted(ctrl)) return;
+  __shared__ float sh_hi[256], sh_lo[256];
+  for (int k = 0; k < kIntrPart; ++k) {
+    dd acc = dd_make(0.f, 0.f);
+    for (int i = threadIdx.x; i < a.np; i += blockDim.x)
+      acc = dd_add(acc, dd_from_double(a.ipart[static_cast<int64_t>(i) * kIntrPart + k]));
+    sh_hi[threadIdx.x] = acc.hi;
+    sh_lo[threadIdx.x] = acc.lo;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+      if (threadIdx.x < h) {
+        const dd t = dd_add(dd_make(sh_hi[threadIdx.x], sh_lo[threadIdx.x]),
+                            dd_make(sh_hi[threadIdx.x + h], sh_lo[threadIdx.x + h]));
+        sh_hi[threadIdx.x] = t.hi;
+        sh_lo[threadIdx.x] = t.lo;
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) a.isum[k] = dd_to_double(dd_make(sh_hi[0], sh_lo[0]));
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double mg = 0.0;
+    for (int k = 0; k < 4; ++k) {
+      const double bk = -a.isum[10 + k];
+      a.isum[kIntrPart + k] = bk;
+      mg = fmax(mg, fabs(bk));
+    }
+    atomic_max_nonneg(&ctrl->max_grad_bits, mg);
+  }
+}
+
+// One CTA per free pose: S_kj = sum over its terms of J_k^T J_p - Zk_i Z_g^T.
+__global__ void __launch_bounds__(128) k_intr_cams(IntrArgs a, const Ctrl* ctrl) {
+  if (halted(ctrl)) return;
+  const int fb = blockIdx.x;
+  __shared__ float sh_hi[24][129], sh_lo[24][129];
+  dd acc[24];
+  for (int k = 0; k < 24; ++k) acc[k] = dd_make(0.f, 0.f);
+  const dd fxd = dd_from_double(a.intr[0]), fyd = dd_from_double(a.intr[1]);
+  const int64_t t0 = a.fb_tile_begin[fb], t1 = a.fb_tile_begin[fb + 1];
+  const int64_t e0 = (t1 > t0) ? a.tile_begin[t0] : 0, e1 = (t1 > t0) ? a.tile_end[t1 - 1] : 0;
+  const dd one = dd_make(1.0f, 0.0f);
+  for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    const int64_t g = a.cam_g[e];
+    const int i = a.g_pt[g];
+    const dd px = dd_from_double(a.points[3 * i]), py = dd_from_double(a.points[3 * i + 1]),
+             pz = dd_from_double(a.points[3 * i + 2]);
+    JacD J;
+    dd u, v;
+    intr_term_jacobians(a.pose_dd + 24 * a.g_pose[g], px, py, pz, fxd, fyd, &J, &u, &v);
+    const dd jk[8] = {dd_neg(u), dd_make(0.f, 0.f), dd_neg(one), dd_make(0.f, 0.f),
+                      dd_make(0.f, 0.f), dd_neg(v), dd_make(0.f, 0.f), dd_neg(one)};
+    for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o)
+      for (int p = 0; p < 4; ++p)
+        for (int q = 0; q < 6; ++q)
+          acc[p * 6 + q] = dd_add(acc[p * 6 + q], dd_add(dd_mul(jk[p], J.jp[q]), dd_mul(jk[4 + p], J.jp[6 + q])));
+    const int mb = a.pt_mb[i];
+    if (mb >= 0) {
+      // Z_g (6x3): float-float where the landmark pass kept it so, else FP32
+      dd Z[18];
+      const float4* z4 = reinterpret_cast<const float4*>(a.zmat + 20 * g);
+      float zf[20];
+      for (int k = 0; k < 5; ++k) {
+        const float4 w4 = z4[k];
+        zf[4 * k] = w4.x; zf[4 * k + 1] = w4.y; zf[4 * k + 2] = w4.z; zf[4 * k + 3] = w4.w;
+      }
+      const float* zd = a.zdd ? a.zdd + kZddFloats * g : ((zf[18] != 0.f && a.zdd_flagged) ? a.zdd_flagged + kZddFloats * g : nullptr);
+      for (int k = 0; k < 18; ++k) Z[k] = zd ? dd_make(zd[2 * k], zd[2 * k + 1]) : dd_from_float(zf[k]);
+      const float* zk = a.zk + 24 * static_cast<int64_t>(mb);
+      for (int p = 0; p < 4; ++p)
+        for (int q = 0; q < 6; ++q) {
+          dd t = dd_make(0.f, 0.f);
+          for (int s2 = 0; s2 < 3; ++s2)
+            t = dd_add(t, dd_mul(dd_make(zk[2 * (p * 3 + s2)], zk[2 * (p * 3 + s2) + 1]), Z[q * 3 + s2]));
+          acc[p * 6 + q] = dd_sub(acc[p * 6 + q], t);
+        }
+    }
+  }
+  for (int k = 0; k < 24; ++k) {
+    sh_hi[k][threadIdx.x] = acc[k].hi;
+    sh_lo[k][threadIdx.x] = acc[k].lo;
+  }
+  __syncthreads();
+  if (threadIdx.x < 24) {
+    const int k = threadIdx.x;
+    dd t = dd_make(0.f, 0.f);
+    for (int q = 0; q < static_cast<int>(blockDim.x); ++q) t = dd_add(t, dd_make(sh_hi[k][q], sh_lo[k][q]));
+    a.scj[24 * static_cast<int64_t>(fb) + k] = dd_to_double(t);
+  }
+}
+
+// The intrinsics rows of S (block nf, both triangles) and of the reduced rhs:
+// blocks 0..nf-1 write S_kj, block nf the damped S_kk (identity padding).
+__global__ void __launch_bounds__(64) k_intr_fill(IntrArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  const int b = blockIdx.x;
+  const int k0 = 6 * a.nf;
+  const int e = threadIdx.x;
+  if (e >= 36) return;
+  const int r = e / 6, c = e % 6;
+  if (b < a.nf) {
+    const double v = (r < 4) ? a.scj[24 * static_cast<int64_t>(b) + r * 6 + c] : 0.0;
+    const int64_t row = k0 + r, col = 6 * b + c;
+    a.S[row * a.n6 + col] = v;
+    a.S[col * a.n6 + row] = v;
+    if (a.S2) {
+      const dd vd = dd_from_double(v);
+      a.S2[row * a.n6 + col] = make_float2(vd.hi, vd.lo);
+      a.S2[col * a.n6 + row] = make_float2(vd.hi, vd.lo);
+    }
+  } else {
+    double v;
+    if (r < 4 && c < 4) {
+      const int p = r < c ? r : c, q = r < c ? c : r;
+      const int idx = p * 4 - p * (p - 1) / 2 + (q - p);
+      v = a.isum[idx];
+      if (r == c) v += ctrl->nu * static_cast<double>(a.ng);
+    } else {
+      v = (r == c) ? 1.0 : 0.0;
+    }
+    const int64_t row = k0 + r, col = k0 + c;
+    a.S[row * a.n6 + col] = v;
+    if (a.S2) {
+      const dd vd = dd_from_double(v);
+      a.S2[row * a.n6 + col] = make_float2(vd.hi, vd.lo);
+    }
+    if (c == 0) a.rb[k0 + r] = (r < 4) ? a.isum[kIntrPart + r] - a.isum[14 + r] : 0.0;
+  }
+}
+
+IntrArgs intr_args(const Sizes& s, const Dev& d) {
+  IntrArgs a;
+  a.np = s.np;
+  a.nf = s.nf;
+  a.n6 = s.n6;
+  a.ng = s.ng;
+  a.pt_g_begin = d.pt_g_begin;
+  a.g_begin = d.g_begin;
+  a.g_pose = d.g_pose;
+  a.g_pt = d.g_pt;
+  a.pose_fb = d.pose_fb;
+  a.pt_mb = d.pt_mb;
+  a.pose_dd = d.pose_dd;
+  a.points = d.points;
+  a.res = d.res;
+  a.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
+  a.huber_dd = dd_make(static_cast<float>(s.huber), static_cast<float>(s.huber - static_cast<float>(s.huber)));
+  a.intr = d.intr;
+  a.cinv = d.cinv;
+  a.cvec = d.cvec;
+  a.zmat = d.zmat;
+  a.zdd = s.lin_dd ? d.zdd : nullptr;
+  a.zdd_flagged = d.zdd;
+  a.cam_g = d.cam_g;
+  a.tile_begin = d.tile_begin;
+  a.tile_end = d.tile_end;
+  a.fb_tile_begin = d.fb_tile_begin;
+  a.ipart = d.intr_part;
+  a.zk = d.intr_zk;
+  a.scj = d.intr_scj;
+  a.isum = d.intr_sum;
+  a.S = d.S;
+  a.S2 = d.S2;
+  a.rb = d.rb;
+  a.fail_check = 0;
+  return a;
+}
+
+int launch_intr_linearize(const Sizes& s, const Dev& d, cudaStream_t st) {
+  if (!s.intr_free) return 0;
+  const IntrArgs a = intr_args(s, d);
+  k_intr_points<<<(s.np + 127) / 128 > 0 ? (s.np + 127) / 128 : 1, 128, 0, st>>>(a, d.ctrl);
+  k_intr_reduce<<<1, 256, 0, st>>>(a, d.ctrl);
+  if (s.nf > 0) k_intr_cams<<<s.nf, 128, 0, st>>>(a, d.ctrl);
+  return s.nf > 0 ? 3 : 2;
+}
+
+int launch_intr_fill(const Sizes& s, const Dev& d, cudaStream_t st) {
+  if (!s.intr_free) return 0;
+  const IntrArgs a = intr_args(s, d);
+  k_intr_fill<<<s.nf + 1, 64, 0, st>>>(a, d.ctrl);
+  return 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -1936,6 +2306,11 @@ struct UpdArgs {
   const double* um;          // the points' part of the projection direction
   float* pose_f;   // trial pose tables, written here for the trial cost
   float* pose_dd;
+  // free intrinsics: k_t = k + dx_k (dx_k at xf[6 nf .. 6 nf + 3]), neg_grad bk
+  int intr_free;
+  const double* intr;
+  double* intr_t;
+  const double* bk;
 };
 
 __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
@@ -1964,6 +2339,17 @@ __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
   }
   dd sdd = dd_make(0.f, 0.f), sdg = dd_make(0.f, 0.f);
   double mx = 0.0;
+  if (a.intr_free && blockIdx.x == 0 && threadIdx.x == 0) {
+    // the intrinsics are a vector space: k + dx_k (no gauge component)
+    for (int k = 0; k < 4; ++k) {
+      const double xk = a.xf[6 * a.nf + k];
+      a.intr_t[k] = a.intr[k] + xk;
+      const dd x = dd_from_double(xk);
+      sdd = dd_add(sdd, dd_mul(x, x));
+      sdg = dd_add(sdg, dd_mul(x, dd_from_double(a.bk[k])));
+      mx = fmax(mx, fabs(xk));
+    }
+  }
   const int64_t n = static_cast<int64_t>(a.nc) + a.np;
   for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n;
        t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -2136,10 +2522,12 @@ __device__ void decide_body(const double* cost_part, int n_cost, const double* u
 // Accepted step: trial state becomes the current state.
 __global__ void k_commit(int nc, int np, int64_t no, const double* poses_t, double* poses,
                          const double* points_t, double* points, const float2* res_t, float2* res,
-                         const float2* res_lo_t, float2* res_lo, const Ctrl* ctrl) {
+                         const float2* res_lo_t, float2* res_lo, const double* intr_t, double* intr,
+                         const Ctrl* ctrl) {
   if (!ctrl->accept) return;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   const int64_t t0 = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (intr && t0 < 4) intr[t0] = intr_t[t0];
   for (int64_t t = t0; t < no; t += stride) res[t] = res_t[t];
   if (res_lo)
     for (int64_t t = t0; t < no; t += stride) res_lo[t] = res_lo_t[t];
@@ -2184,10 +2572,8 @@ static CostArgs make_cost_args(const Sizes& s, const Dev& d, const double* point
   a.points = points;
   a.res_out = res_out;
   a.partials = partials;
-  a.fx = dd_make(static_cast<float>(s.intr[0]), static_cast<float>(s.intr[0] - static_cast<float>(s.intr[0])));
-  a.fy = dd_make(static_cast<float>(s.intr[1]), static_cast<float>(s.intr[1] - static_cast<float>(s.intr[1])));
-  a.cx = dd_make(static_cast<float>(s.intr[2]), static_cast<float>(s.intr[2] - static_cast<float>(s.intr[2])));
-  a.cy = dd_make(static_cast<float>(s.intr[3]), static_cast<float>(s.intr[3] - static_cast<float>(s.intr[3])));
+  a.fx = a.fy = a.cx = a.cy = dd_make(0.f, 0.f);
+  a.intr = (points == d.points_t) ? d.intr_t : d.intr;  // the trial point's intrinsics
   a.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
   a.huber_dd = dd_make(static_cast<float>(s.huber), static_cast<float>(s.huber - static_cast<float>(s.huber)));
   a.respect_skip = respect_skip;
@@ -2237,11 +2623,8 @@ static LinArgs make_lin_args(const Sizes& s, const Dev& d, double nu_override, b
   la.pose_f = d.pose_f;
   la.points = d.points;
   la.pose_dd = d.pose_dd;
-  la.fxd = dd_make(static_cast<float>(s.intr[0]), static_cast<float>(s.intr[0] - static_cast<float>(s.intr[0])));
-  la.fyd = dd_make(static_cast<float>(s.intr[1]), static_cast<float>(s.intr[1] - static_cast<float>(s.intr[1])));
   la.res = d.res;
-  la.fx = static_cast<float>(s.intr[0]);
-  la.fy = static_cast<float>(s.intr[1]);
+  la.intr = d.intr;
   la.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
   la.huber_dd = dd_make(static_cast<float>(s.huber), static_cast<float>(s.huber - static_cast<float>(s.huber)));
   la.zmat = d.zmat;
@@ -2279,16 +2662,13 @@ static CamArgs make_cam_args(const Sizes& s, const Dev& d, int with_schur) {
   ca.res = d.res;
   ca.zmat = d.zmat;
   ca.cvec = d.cvec;
-  ca.fx = static_cast<float>(s.intr[0]);
-  ca.fy = static_cast<float>(s.intr[1]);
+  ca.intr = d.intr;
   ca.huber = static_cast<float>(s.huber > 0 ? s.huber : 0.0);
   ca.tile_part = d.tile_part;
   ca.with_schur = with_schur;
   ca.pose_dd = d.pose_dd;
   ca.res_lo = d.res_lo;
   ca.zdd = d.zdd;
-  ca.fxd = dd_make(static_cast<float>(s.intr[0]), static_cast<float>(s.intr[0] - static_cast<float>(s.intr[0])));
-  ca.fyd = dd_make(static_cast<float>(s.intr[1]), static_cast<float>(s.intr[1] - static_cast<float>(s.intr[1])));
   ca.huber_dd = dd_make(static_cast<float>(s.huber), static_cast<float>(s.huber - static_cast<float>(s.huber)));
   return ca;
 }
@@ -2321,6 +2701,8 @@ static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
   b.cy = s.gauge_center[1];
   b.cz = s.gauge_center[2];
   b.um = d.gauge_um;
+  b.zk = s.intr_free ? d.intr_zk : nullptr;
+  b.k0 = 6 * s.nf;
   if (s.nlchunk > 0 && s.bsub_chunks_ok) {
     const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
     k_backsub_chunks<<<grid, 256, sizeof(float) * 12 * static_cast<size_t>(s.lmk_cap), st>>>(
@@ -2387,6 +2769,7 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
                                                     use_override ? nullptr : d.slow_count);
   ++n;
   n += launch_landmark(s, d, make_lin_args(s, d, nu_override, use_override), st, use_override);
+  n += launch_intr_linearize(s, d, st);
   n += launch_camera(s, d, use_override ? 0 : 1, st);
   // the last block of the finalisation runs the gradient check of an LM iteration
   k_camera_finalize<<<s.nf, 64, 0, st>>>(s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf, d.rb, d.ctrl,
@@ -2416,7 +2799,7 @@ int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
   if (s.lin_dd) k_schur_dd<<<warp_grid(s.nchunk, 8, 65536), 256, 0, st>>>(a, d.ctrl);
   else k_schur<<<warp_grid(s.nchunk, 8, 65536), 256, 0, st>>>(a, d.ctrl);
   k_schur_reduce<<<warp_grid(s.nsb, 8, 8192), 256, 0, st>>>(a, d.ctrl);
-  return 2;
+  return 2 + launch_intr_fill(s, d, st);
 }
 
 int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
@@ -2465,6 +2848,10 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
   u.gauge_part = d.part;
   u.gauge_blocks = kUpdBlocks;
   u.um = d.gauge_um;
+  u.intr_free = s.intr_free;
+  u.intr = d.intr;
+  u.intr_t = d.intr_t;
+  u.bk = d.intr_sum ? d.intr_sum + kIntrPart : nullptr;
   u.pose_f = d.pose_f;
   u.pose_dd = d.pose_dd;
   k_apply_update<<<kUpdBlocks, 256, 0, st>>>(u, d.ctrl);
@@ -2512,7 +2899,8 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
   if (cb > 1216) cb = 1216;
   if (cb < 1) cb = 1;
   k_commit<<<cb, 256, 0, st>>>(s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res,
-                               d.res_lo_t, d.res_lo, d.ctrl);
+                               d.res_lo_t, d.res_lo, s.intr_free ? d.intr_t : nullptr,
+                               s.intr_free ? d.intr : nullptr, d.ctrl);
   return 2;
 }
 
@@ -2524,10 +2912,12 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
 // ---------------------------------------------------------------------------
 namespace {
 __global__ void k_debug_jacobians(int64_t n, const int32_t* __restrict__ cam, const int32_t* __restrict__ pt,
-                                  const double* __restrict__ poses, const double* __restrict__ points, double fx,
-                                  double fy, int precision, double* __restrict__ jp, double* __restrict__ jm) {
+                                  const double* __restrict__ poses, const double* __restrict__ points,
+                                  const double* __restrict__ intr, int precision, double* __restrict__ jp,
+                                  double* __restrict__ jm) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (i >= n) return;
+  const double fx = intr[0], fy = intr[1];
   float pf[12], pd[24];
   pose_table(poses + 7 * static_cast<int64_t>(cam[i]), pf, pd);
   const double* pw = points + 3 * static_cast<int64_t>(pt[i]);
@@ -2552,8 +2942,8 @@ cudaError_t launch_debug_jacobians(const Sizes& s, const Dev& d, int64_t n, cons
                                    int precision, double* jp, double* jm, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   const int64_t blocks = (n + 127) / 128;
-  k_debug_jacobians<<<static_cast<unsigned>(blocks), 128, 0, st>>>(n, cam, pt, d.poses, d.points, s.intr[0],
-                                                                   s.intr[1], precision, jp, jm);
+  k_debug_jacobians<<<static_cast<unsigned>(blocks), 128, 0, st>>>(n, cam, pt, d.poses, d.points, d.intr,
+                                                                   precision, jp, jm);
   return cudaGetLastError();
 }
 
@@ -2698,6 +3088,7 @@ cudaError_t launch_total_cost_noalloc(int32_t nc, const double* poses, int32_t n
   a.fy = split(intr[1]);
   a.cx = split(intr[2]);
   a.cy = split(intr[3]);
+  a.intr = nullptr;
   a.huber = static_cast<float>(huber > 0 ? huber : 0.0);
   a.huber_dd = split(huber);
   a.respect_skip = 0;

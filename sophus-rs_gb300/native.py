@@ -92,7 +92,12 @@ class Layout(C.Structure):
         ("band_width", C.c_int32),
         ("border_rows", C.c_int32),
         ("float_float_lin", C.c_int32),
+        ("intrinsics_rows", C.c_int32),
     ]
+
+
+class ProblemOptions(C.Structure):
+    _fields_ = [("intrinsics_free", C.c_int32), ("camera_model", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class Profile(C.Structure):
@@ -138,7 +143,8 @@ LINSOLVE_PCG_BLOCK_JACOBI = 1
 LINSOLVE_PCG_LEARNED = 2
 
 EXPORTED = [
-    "sgba_abi_version", "sgba_last_error", "sgba_problem_create", "sgba_problem_destroy",
+    "sgba_abi_version", "sgba_last_error", "sgba_problem_create", "sgba_problem_create_ex",
+    "sgba_get_intrinsics", "sgba_problem_destroy",
     "sgba_optimizer_init", "sgba_optimizer_step", "sgba_optimize", "sgba_get_variables",
     "sgba_get_cost", "sgba_set_variables", "sgba_get_layout", "sgba_export_pattern",
     "sgba_debug_last_system", "sgba_debug_jacobians", "sgba_state_save", "sgba_state_load", "sgba_get_profile",
@@ -187,6 +193,9 @@ def lib():
     L.sgba_last_error.argtypes = [C.c_char_p, C.c_size_t]
     L.sgba_last_error.restype = C.c_size_t
     L.sgba_problem_create.argtypes = [C.POINTER(ProblemDesc), C.c_int32, C.POINTER(C.c_void_p)]
+    L.sgba_problem_create_ex.argtypes = [C.POINTER(ProblemDesc), C.POINTER(ProblemOptions), C.c_int32,
+                                         C.POINTER(C.c_void_p)]
+    L.sgba_get_intrinsics.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     L.sgba_problem_destroy.argtypes = [C.c_void_p]
     L.sgba_optimizer_init.argtypes = [C.c_void_p, C.POINTER(OptParamsC)]
     L.sgba_optimizer_step.argtypes = [C.c_void_p, C.POINTER(IterRecord)]
@@ -272,8 +281,12 @@ class Problem:
     obs_uv (k,2), huber_delta and optionally pose_const / point_const.
     """
 
-    def __init__(self, data, device=-1):
+    def __init__(self, data, device=-1, intrinsics_free=None):
+        """intrinsics_free (default: data.intrinsics_free, else False): the
+        pinhole intrinsics are a Free family, optimised with the poses."""
         L = lib()
+        if intrinsics_free is None:
+            intrinsics_free = bool(getattr(data, "intrinsics_free", False))
         self._keep = []
         poses = np.ascontiguousarray(data.poses, dtype=np.float64).reshape(-1, 7)
         points = np.ascontiguousarray(data.points, dtype=np.float64).reshape(-1, 3)
@@ -302,7 +315,12 @@ class Problem:
         d.obs_uv = _dptr(obs_uv)
         d.huber_delta = float(data.huber_delta) if data.huber_delta is not None else 0.0
         h = C.c_void_p()
-        check(L.sgba_problem_create(C.byref(d), int(device), C.byref(h)))
+        if intrinsics_free:
+            opts = ProblemOptions()
+            opts.intrinsics_free = 1
+            check(L.sgba_problem_create_ex(C.byref(d), C.byref(opts), int(device), C.byref(h)))
+        else:
+            check(L.sgba_problem_create(C.byref(d), int(device), C.byref(h)))
         self._h = h
 
     def close(self):
@@ -369,9 +387,15 @@ class Problem:
         check(lib().sgba_export_pattern(self._h, _ipt(hr), _ipt(hc), _ipt(sr), _ipt(sc)))
         return (hr, hc), (sr, sc)
 
+    def intrinsics(self):
+        """Current fx fy cx cy."""
+        out = np.empty(4)
+        check(lib().sgba_get_intrinsics(self._h, _dptr(out)))
+        return out
+
     def last_system(self):
         lay = self.layout()
-        n6 = 6 * lay.n_free_poses
+        n6 = 6 * lay.n_free_poses + lay.intrinsics_rows
         S = np.empty((n6, n6))
         rhs = np.empty(n6)
         delta = np.empty(n6 + 3 * lay.n_marg_points)

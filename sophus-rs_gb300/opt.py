@@ -379,8 +379,11 @@ def _extract_problem(variables, cost_fns):
         raise NotOnGpuPath("reprojection cost needs (intrinsics, pose, point) families")
     fam = [variables.collection[n] for n in names]
     kinds = tuple(f.kind for f in fam)
-    if kinds != (VarKind.Conditioned, VarKind.Free, VarKind.Marginalized):
-        raise NotOnGpuPath("GPU path needs kinds (Conditioned, Free, Marginalized), got %s" % (kinds,))
+    if kinds not in ((VarKind.Conditioned, VarKind.Free, VarKind.Marginalized),
+                     (VarKind.Free, VarKind.Free, VarKind.Marginalized)):
+        raise NotOnGpuPath("GPU path needs kinds (Conditioned or Free, Free, Marginalized), got %s" % (kinds,))
+    if kinds[0] == VarKind.Free and fam[0].constant_ids:
+        raise NotOnGpuPath("a constant id in a Free intrinsics family is not on this path")
     intr = fam[0].members
     if len(intr) != 1:
         raise NotOnGpuPath("GPU path supports one intrinsics member")
@@ -404,6 +407,7 @@ def _extract_problem(variables, cost_fns):
     prob = BAProblem(poses=poses, points=points, intrinsics=np.asarray(cparams, float),
                      obs_cam=idx[:, 1].astype(np.int32), obs_pt=idx[:, 2].astype(np.int32),
                      obs_uv=terms.uv_in_image, huber_delta=huber, pose_const=pc, point_const=qc)
+    prob.intrinsics_free = kinds[0] == VarKind.Free
     return prob, names
 
 
@@ -414,8 +418,14 @@ def _step_info(rec, k):
                     accepted=bool(rec.accepted))
 
 
-def _write_back(variables, names, poses, points):
+def _write_back(variables, names, poses, points, intrinsics=None):
     fams = dict(variables.collection)
+    if intrinsics is not None:
+        cf = fams[names[0]]
+        cam = cf.members[0]
+        new = PinholeCameraF64(np.asarray(intrinsics, float)) if isinstance(cam, PinholeCameraF64) else \
+            np.asarray(intrinsics, float)
+        fams[names[0]] = VarFamily(cf.kind, [new], sorted(cf.constant_ids))
     pf = fams[names[1]]
     if isinstance(pf.members, np.ndarray):
         pm = poses.copy()
@@ -455,14 +465,18 @@ class Optimizer:
         self._steps.append(info)
         return info
 
+    def _intrinsics(self):
+        return self._gpu.intrinsics() if self._variables.collection[self._names[0]].kind == VarKind.Free else None
+
     def variables(self):
         poses, points = self._gpu.variables()
-        return _write_back(self._variables, self._names, poses, points)
+        return _write_back(self._variables, self._names, poses, points, self._intrinsics())
 
     def build_solution(self):
         poses, points = self._gpu.variables()
         cost = self._gpu.cost()
-        sol = OptimizationSolution(_write_back(self._variables, self._names, poses, points), cost, self._steps)
+        sol = OptimizationSolution(_write_back(self._variables, self._names, poses, points, self._intrinsics()),
+                                   cost, self._steps)
         self._gpu.close()
         return sol
 
@@ -474,6 +488,7 @@ def optimize_nlls(variables, cost_fns, eq_fns, params, device=-1):
     with native.Problem(prob, device=device) as gp:
         recs, _ = gp.optimize(params)
         poses, points = gp.variables()
+        intr = gp.intrinsics() if prob.intrinsics_free else None
         cost = gp.cost()
     steps = [_step_info(r, k) for k, r in enumerate(recs)]
-    return OptimizationSolution(_write_back(variables, names, poses, points), cost, steps)
+    return OptimizationSolution(_write_back(variables, names, poses, points, intr), cost, steps)

@@ -71,6 +71,7 @@ class BAProblem:
     points_true: np.ndarray = None
     initial_lm_damping: float = 1e-4
     num_iterations: int = 10
+    intrinsics_free: bool = False  # the pinhole intrinsics are optimised too (a Free camera family)
 
     @property
     def n_cam(self):
