@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define SGBA_ABI_VERSION 1
+#define SGBA_ABI_VERSION 2
 
 typedef enum {
   SGBA_OK = 0,
@@ -119,20 +119,33 @@ size_t sgba_last_error(char *buf, size_t cap);
  * the current CUDA device. */
 int sgba_problem_create(const sgba_problem_desc *desc, int32_t device, sgba_problem **out);
 
-/* Options of sgba_problem_create_ex.  intrinsics_free = 1 makes the camera
- * family Free (the reference's VarKind::Free for the "cams" family: kinds
- * (F, F, M), pinhole_reprojection.rs:85 J_cam): the four pinhole parameters
- * fx fy cx cy are optimised with the poses, nu I per reduced term on their
- * block, as one more (padded) 6-row block of the reduced system.  The block
- * comes first in the exported patterns and in sgba_debug_last_system (the
- * reference's family order).  Only the pinhole camera (camera_model 0);
- * loop-shaped problems (the banded solver) and PCG with free intrinsics are
- * rejected with SGBA_ERR_UNSUPPORTED. */
-enum { SGBA_CAMERA_PINHOLE = 0 };
+/* Options of sgba_problem_create_ex.
+ *
+ * camera_model selects the camera of every observation:
+ *   SGBA_CAMERA_PINHOLE  params fx fy cx cy (PinholeCameraF64,
+ *                        crates/sophus_sensor/src/camera_enum/perspective_camera.rs)
+ *   SGBA_CAMERA_EUCM     the enhanced unified camera model, params fx fy cx cy
+ *                        alpha beta (EnhancedUnifiedCameraF64,
+ *                        crates/sophus_sensor/src/distortions/enhanced_unified.rs:55-215;
+ *                        the camera of the reference's BA example problem,
+ *                        crates/sophus_opt/src/example_problems/ba_problem.rs:69-110):
+ *                        desc->intrinsics holds fx fy cx cy, eucm_alpha_beta
+ *                        alpha beta.  For the pinhole eucm_alpha_beta is zero.
+ * intrinsics_free = 1 makes the camera family Free (the reference's
+ * VarKind::Free for the "cams" family: kinds (F, F, M), J_cam =
+ * -dx_distort_params, pinhole_reprojection.rs:85): the camera's params (4 or
+ * 6) are optimised with the poses, nu I per reduced term on their block, as
+ * one more 6-row block of the reduced system (the pinhole's 4 rows padded).
+ * The block comes first in the exported patterns and in
+ * sgba_debug_last_system (the reference's family order).  Loop-shaped problems
+ * (the banded solver) and PCG with free intrinsics are rejected with
+ * SGBA_ERR_UNSUPPORTED. */
+enum { SGBA_CAMERA_PINHOLE = 0, SGBA_CAMERA_EUCM = 1 };
 typedef struct {
-  int32_t intrinsics_free;  /* 0 Conditioned (default), 1 Free */
-  int32_t camera_model;     /* SGBA_CAMERA_PINHOLE */
-  int32_t reserved[6];      /* zero */
+  int32_t intrinsics_free;     /* 0 Conditioned (default), 1 Free */
+  int32_t camera_model;        /* SGBA_CAMERA_PINHOLE or SGBA_CAMERA_EUCM */
+  double eucm_alpha_beta[2];   /* EUCM alpha beta (finite); zero for the pinhole */
+  int32_t reserved[2];         /* zero */
 } sgba_problem_options;
 /* sgba_problem_create with options (NULL: the defaults). */
 int sgba_problem_create_ex(const sgba_problem_desc *desc, const sgba_problem_options *options, int32_t device,
@@ -174,7 +187,8 @@ int sgba_batch_optimize(sgba_problem *const *problems, int32_t n, const sgba_opt
 
 /* Current variables (OptimizationSolution.variables). NULL skips a family. */
 int sgba_get_variables(sgba_problem *p, double *poses, double *points);
-/* Current intrinsics fx fy cx cy (changed by the optimisation when free). */
+/* Current camera params (changed by the optimisation when free): fx fy cx cy,
+ * then alpha beta for the EUCM camera (4 or 6 doubles). */
 int sgba_get_intrinsics(sgba_problem *p, double *intrinsics);
 /* Current merit (OptimizationSolution.final_cost after sgba_optimize). */
 int sgba_get_cost(sgba_problem *p, double *cost);
@@ -193,7 +207,7 @@ typedef struct {
   int32_t band_width;       /* banded solver: band width in scalars (row r holds columns r-w+1..r) */
   int32_t border_rows;      /* banded solver: dense border rows at the end (loop closures) */
   int32_t float_float_lin;  /* 1: Jacobians, products and Z in float-float (loop-shaped problems) */
-  int32_t intrinsics_rows;  /* 6 when the intrinsics are free (their padded block in S), else 0 */
+  int32_t intrinsics_rows;  /* 6 when the intrinsics are free (their block in S), else 0 */
 } sgba_layout;
 /* Reduced camera system solvers (chosen at sgba_problem_create from the size
  * and the block pattern of S). */

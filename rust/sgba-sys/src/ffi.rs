@@ -9,7 +9,7 @@
 use core::ffi::{c_char, c_int, c_void};
 use core::marker::{PhantomData, PhantomPinned};
 
-pub const SGBA_ABI_VERSION: i32 = 1;
+pub const SGBA_ABI_VERSION: i32 = 2;
 
 // sgba_status
 pub const SGBA_OK: c_int = 0;
@@ -137,13 +137,18 @@ pub struct sgba_layout {
     pub intrinsics_rows: i32,
 }
 
-/// Options of `sgba_problem_create_ex` (free pinhole intrinsics).
+pub const SGBA_CAMERA_PINHOLE: i32 = 0;
+pub const SGBA_CAMERA_EUCM: i32 = 1;
+
+/// Options of `sgba_problem_create_ex`: the camera model (pinhole, or EUCM
+/// with its alpha beta) and whether its params are free.
 #[repr(C)]
 #[derive(Debug, Clone, Copy, Default)]
 pub struct sgba_problem_options {
     pub intrinsics_free: i32,
     pub camera_model: i32,
-    pub reserved: [i32; 6],
+    pub eucm_alpha_beta: [f64; 2],
+    pub reserved: [i32; 2],
 }
 
 /// Launch count and device times of the last `sgba_optimize`.

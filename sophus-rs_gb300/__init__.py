@@ -9,6 +9,9 @@ from . import native, synth  # noqa: F401
 from .opt import (  # noqa: F401
     CostFn,
     CostTerms,
+    EnhancedUnifiedCameraF64,
+    EucmCameraReprojectionCostTerm,
+    EucmReprojectionTerms,
     HuberKernel,
     Isometry3F64,
     LinearSolverEnum,

@@ -38,6 +38,11 @@ using sgba::Dev;
 using sgba::Plan;
 using sgba::Record;
 using sgba::Sizes;
+using sgba::kIntrMax;
+using sgba::kIntrPart;
+using sgba::kIntrScj;
+using sgba::kIntrSum;
+using sgba::kIntrZk;
 
 namespace sgba {
 
@@ -111,7 +116,9 @@ constexpr int32_t kMaxDenseFree = 4096;  // reduced-camera-system limit (6 * 409
 
 struct sgba_problem {
   Plan plan;
-  int intr_free = 0;  // the pinhole intrinsics are a Free family (sgba_problem_create_ex)
+  int intr_free = 0;  // the camera params are a Free family (sgba_problem_create_ex)
+  int camera_model = SGBA_CAMERA_PINHOLE;
+  double eucm_ab[2] = {0.0, 0.0};  // EUCM alpha beta
   Sizes sz{};
   Dev d;
   int device = 0;
@@ -710,8 +717,12 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   s.ng = P.ng;
   s.ntiles = static_cast<int64_t>(P.tile_fb.size());
   s.intr_free = p->intr_free;
+  s.eucm = p->camera_model == SGBA_CAMERA_EUCM ? 1 : 0;
+  s.intr_nk = s.eucm ? 6 : 4;
   s.n6 = 6 * P.nf + (p->intr_free ? 6 : 0);
   for (int k = 0; k < 4; ++k) s.intr[k] = desc->intrinsics[k];
+  s.intr[4] = p->eucm_ab[0];
+  s.intr[5] = p->eucm_ab[1];
   s.huber = desc->huber_delta;
   s.gauge_kind = P.gauge_kind;
   for (int k = 0; k < 3; ++k) s.gauge_center[k] = P.gauge_center[k];
@@ -782,11 +793,11 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
     if (!(0.0 <= poses[7 * j]))
       for (int k = 0; k < 4; ++k) poses[7 * j + k] = -poses[7 * j + k];
   {
-    // intrinsics: current (4) and trial (4), both from the descriptor
-    std::vector<double> intr(8);
-    for (int k = 0; k < 4; ++k) intr[k] = intr[4 + k] = desc->intrinsics[k];
+    // camera params: current and trial, both from the descriptor and options
+    std::vector<double> intr(2 * kIntrMax);
+    for (int k = 0; k < kIntrMax; ++k) intr[k] = intr[kIntrMax + k] = s.intr[k];
     if ((st = dev_upload(p, &d.intr, intr))) return st;
-    d.intr_t = d.intr + 4;
+    d.intr_t = d.intr + kIntrMax;
   }
   if ((st = dev_upload(p, &d.poses, poses))) return st;
   if ((st = dev_upload(p, &d.points, pts))) return st;
@@ -803,11 +814,11 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   if ((st = dev_alloc(p, &d.dm, 3 * static_cast<size_t>(P.nm)))) return st;
   if ((st = dev_alloc(p, &d.gauge_um, 3 * static_cast<size_t>(P.nm)))) return st;
   if (p->intr_free) {
-    if ((st = dev_alloc(p, &d.intr_part, 18 * static_cast<size_t>(std::max(P.np, 1))))) return st;
-    if ((st = dev_alloc(p, &d.intr_zk, 24 * static_cast<size_t>(std::max(P.nm, 1))))) return st;
-    if ((st = dev_alloc(p, &d.intr_scj, 24 * static_cast<size_t>(std::max(P.nf, 1))))) return st;
-    if ((st = dev_alloc(p, &d.intr_sum, 22))) return st;
-    SGBA_CK(cudaMemsetAsync(d.intr_sum, 0, sizeof(double) * 22, p->stream));
+    if ((st = dev_alloc(p, &d.intr_part, kIntrPart * static_cast<size_t>(std::max(P.np, 1))))) return st;
+    if ((st = dev_alloc(p, &d.intr_zk, kIntrZk * static_cast<size_t>(std::max(P.nm, 1))))) return st;
+    if ((st = dev_alloc(p, &d.intr_scj, kIntrScj * static_cast<size_t>(std::max(P.nf, 1))))) return st;
+    if ((st = dev_alloc(p, &d.intr_sum, kIntrSum))) return st;
+    SGBA_CK(cudaMemsetAsync(d.intr_sum, 0, sizeof(double) * kIntrSum, p->stream));
   }
   if ((st = dev_alloc(p, &d.bf, 6 * static_cast<size_t>(P.nf)))) return st;
   if ((st = dev_alloc(p, &d.rb, 6 * static_cast<size_t>(P.nf)))) return st;
@@ -871,8 +882,11 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   // get the float-float linearization: their reduced systems cancel ~25x in
   // S = U - sum Z Z^T and their bending modes are weakly constrained, so FP32
   // Jacobian-side products move the step by percents (measured on 300- and
-  // 1500-camera loops).
-  s.lin_dd = loop_shaped ? 1 : 0;
+  // 1500-camera loops).  Free EUCM params get it too: fx, alpha and beta
+  // nearly trade off over a camera's field of view, so their block of S is
+  // close to singular and FP32 Jacobian products move the step by ~1e-6
+  // relative (measured on the 10-camera circle and the 4-camera example).
+  s.lin_dd = (loop_shaped || (p->intr_free && s.eucm)) ? 1 : 0;
   s.lmk_dd_ok = (s.lin_dd && s.nlchunk > 0 && sgba::landmark_dd_setup(s.lmk_cap) == 0) ? 1 : 0;
   s.bsub_chunks_ok = (s.nlchunk > 0 && sgba::backsub_chunks_setup(s.lmk_cap) == 0) ? 1 : 0;
   if (s.lin_dd) {
@@ -981,14 +995,24 @@ int sgba_problem_create_ex(const sgba_problem_desc* desc, const sgba_problem_opt
   if (!out) return set_error(SGBA_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
   if (!desc) return set_error(SGBA_ERR_INVALID_ARGUMENT, "desc is NULL");
-  if (opts && opts->camera_model != SGBA_CAMERA_PINHOLE)
-    return set_error(SGBA_ERR_UNSUPPORTED, "camera model %d: only the pinhole camera runs on this path",
+  if (opts && opts->camera_model != SGBA_CAMERA_PINHOLE && opts->camera_model != SGBA_CAMERA_EUCM)
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "camera model %d: expected SGBA_CAMERA_PINHOLE or SGBA_CAMERA_EUCM",
                      opts->camera_model);
   if (opts && opts->intrinsics_free != 0 && opts->intrinsics_free != 1)
     return set_error(SGBA_ERR_INVALID_ARGUMENT, "intrinsics_free must be 0 or 1");
+  const bool eucm = opts && opts->camera_model == SGBA_CAMERA_EUCM;
+  if (eucm && !(std::isfinite(opts->eucm_alpha_beta[0]) && std::isfinite(opts->eucm_alpha_beta[1])))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "non-finite EUCM alpha / beta");
+  if (opts && !eucm && (opts->eucm_alpha_beta[0] != 0.0 || opts->eucm_alpha_beta[1] != 0.0))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "eucm_alpha_beta must be zero for the pinhole camera");
   sgba_problem* p = new (std::nothrow) sgba_problem();
   if (!p) return set_error(SGBA_ERR_OUT_OF_MEMORY, "host allocation failed");
   p->intr_free = (opts && opts->intrinsics_free) ? 1 : 0;
+  p->camera_model = eucm ? SGBA_CAMERA_EUCM : SGBA_CAMERA_PINHOLE;
+  if (eucm) {
+    p->eucm_ab[0] = opts->eucm_alpha_beta[0];
+    p->eucm_ab[1] = opts->eucm_alpha_beta[1];
+  }
   int st = build_plan(desc, &p->plan);
   if (st) { delete p; return st; }
   if (p->plan.nf > kMaxDenseFree) {
@@ -1036,7 +1060,7 @@ int sgba_optimizer_init(sgba_problem* p, const sgba_opt_params* prm) {
   if ((p->plan.nf == 0 && !p->intr_free) || p->plan.nm == 0)
     return set_error(SGBA_ERR_SCHUR_MISSING_FREE_OR_MARG,
                      "Schur solver needs free and marginalized variables (free scalars %d, marg scalars %d)",
-                     6 * p->plan.nf + (p->intr_free ? 4 : 0), 3 * p->plan.nm);
+                     6 * p->plan.nf + (p->intr_free ? p->sz.intr_nk : 0), 3 * p->plan.nm);
   if (!std::isfinite(prm->initial_lm_damping))
     return set_error(SGBA_ERR_INVALID_ARGUMENT, "initial_lm_damping is not finite");
   p->params = *prm;
@@ -1195,7 +1219,7 @@ int sgba_get_intrinsics(sgba_problem* p, double* intrinsics) {
   if (!p || !intrinsics) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
   SGBA_CK(cudaSetDevice(p->device));
   SGBA_CK(cudaStreamSynchronize(p->stream));
-  SGBA_CK(cudaMemcpy(intrinsics, p->d.intr, sizeof(double) * 4, cudaMemcpyDeviceToHost));
+  SGBA_CK(cudaMemcpy(intrinsics, p->d.intr, sizeof(double) * p->sz.intr_nk, cudaMemcpyDeviceToHost));
   return SGBA_OK;
 }
 
@@ -1355,7 +1379,7 @@ int sgba_debug_jacobians(sgba_problem* p, int64_t n, const int32_t* cam, const i
 // State blob: magic, sizes, LM scalars, poses, points.
 int sgba_state_save(sgba_problem* p, void* buf, size_t* size) {
   if (!p || !size) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
-  const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np) + 4);
+  const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np) + kIntrMax);
   if (!buf) { *size = need; return SGBA_OK; }
   if (*size < need) return set_error(SGBA_ERR_INVALID_ARGUMENT, "state buffer too small (%zu < %zu)", *size, need);
   if (!p->inited) return set_error(SGBA_ERR_STATE, "no optimizer state to save");
@@ -1377,7 +1401,8 @@ int sgba_state_save(sgba_problem* p, void* buf, size_t* size) {
   std::memcpy(b + 40, &stp, 8);
   SGBA_CK(cudaMemcpy(b + 64, p->d.poses, sizeof(double) * 7 * nc, cudaMemcpyDeviceToHost));
   if (np > 0) SGBA_CK(cudaMemcpy(b + 64 + sizeof(double) * 7 * nc, p->d.points, sizeof(double) * 3 * np, cudaMemcpyDeviceToHost));
-  SGBA_CK(cudaMemcpy(b + need - 32, p->d.intr, sizeof(double) * 4, cudaMemcpyDeviceToHost));
+  SGBA_CK(cudaMemcpy(b + need - sizeof(double) * kIntrMax, p->d.intr, sizeof(double) * kIntrMax,
+                     cudaMemcpyDeviceToHost));
   *size = need;
   return SGBA_OK;
 }
@@ -1386,7 +1411,7 @@ int sgba_state_load(sgba_problem* p, const void* buf, size_t size) {
   if (!p || !buf) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
   if (!p->inited) return set_error(SGBA_ERR_STATE, "call sgba_optimizer_init before sgba_state_load");
   const char* b = static_cast<const char*>(buf);
-  const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np) + 4);
+  const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np) + kIntrMax);
   uint64_t magic;
   int32_t nc, np;
   if (size < need) return set_error(SGBA_ERR_INVALID_ARGUMENT, "state blob too small");
@@ -1409,8 +1434,10 @@ int sgba_state_load(sgba_problem* p, const void* buf, size_t size) {
   c.done = 0;
   SGBA_CK(cudaMemcpy(p->d.poses, b + 64, sizeof(double) * 7 * nc, cudaMemcpyHostToDevice));
   if (np > 0) SGBA_CK(cudaMemcpy(p->d.points, b + 64 + sizeof(double) * 7 * nc, sizeof(double) * 3 * np, cudaMemcpyHostToDevice));
-  SGBA_CK(cudaMemcpy(p->d.intr, b + need - 32, sizeof(double) * 4, cudaMemcpyHostToDevice));
-  SGBA_CK(cudaMemcpy(p->d.intr_t, b + need - 32, sizeof(double) * 4, cudaMemcpyHostToDevice));
+  SGBA_CK(cudaMemcpy(p->d.intr, b + need - sizeof(double) * kIntrMax, sizeof(double) * kIntrMax,
+                     cudaMemcpyHostToDevice));
+  SGBA_CK(cudaMemcpy(p->d.intr_t, b + need - sizeof(double) * kIntrMax, sizeof(double) * kIntrMax,
+                     cudaMemcpyHostToDevice));
   SGBA_CK(cudaMemcpy(p->d.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice));
   // residuals of the loaded state
   sgba::launch_init_merit(p->sz, p->d, p->stream);

@@ -14,6 +14,15 @@ namespace sgba {
 
 // floats per term of the float-float Z (6x3 as (hi, lo) pairs, padded to float4)
 constexpr int kZddFloats = 40;
+// Camera params on the device: fx fy cx cy alpha beta (the enhanced unified
+// camera model; alpha = beta = 0 is the pinhole).  Free intrinsics: per point
+// the S_kk triangle (21), J_k^T r~ (6) and Zk c (6); per marg point Zk (6x3,
+// float-float); per free pose S_kj (6x6).
+constexpr int kIntrMax = 6;
+constexpr int kIntrPart = 33;
+constexpr int kIntrZk = 36;
+constexpr int kIntrScj = 36;
+constexpr int kIntrSum = kIntrPart + kIntrMax;
 
 // Device-resident LM control block (one per problem).  Written only by the
 // single-CTA control kernels, read by every kernel of an iteration.
@@ -153,8 +162,9 @@ struct Dev {
   double* poses = nullptr;         // nc*7
   double* points = nullptr;        // np*3
   double* poses_t = nullptr;       // trial
-  double* intr = nullptr;          // 4: intrinsics fx fy cx cy (device copy; the kernels read them here)
-  double* intr_t = nullptr;        // 4: trial intrinsics (free intrinsics)
+  double* intr = nullptr;          // kIntrMax: camera params fx fy cx cy alpha beta (device copy; the kernels
+                                   // read them here; alpha = beta = 0 for the pinhole)
+  double* intr_t = nullptr;        // kIntrMax: trial params (free intrinsics)
   double* points_t = nullptr;
   float2* res = nullptr;           // residual at current state (sorted obs)
   float2* res_t = nullptr;         // residual at trial state
@@ -194,10 +204,10 @@ struct Dev {
   double* dm = nullptr;            // nm*3 point steps
   double* gauge_um = nullptr;      // nm*3 the free poses' gauge direction back-substituted into the points
   // free intrinsics (Sizes::intr_free)
-  double* intr_part = nullptr;     // np*18 per-point parts of S_kk, J_k^T r~, Zk c
-  float* intr_zk = nullptr;        // nm*24 Zk = Y C^-T (4x3) as (hi, lo) pairs
-  double* intr_scj = nullptr;      // nf*24 S_kj (4x6)
-  double* intr_sum = nullptr;      // 18 sums + 4 neg_grad of the intrinsics
+  double* intr_part = nullptr;     // np*kIntrPart per-point parts of S_kk, J_k^T r~, Zk c
+  float* intr_zk = nullptr;        // nm*kIntrZk Zk = Y C^-T (6x3) as (hi, lo) pairs
+  double* intr_scj = nullptr;      // nf*kIntrScj S_kj (6x6)
+  double* intr_sum = nullptr;      // kIntrSum: kIntrPart sums + 6 neg_grad of the intrinsics
   double* part = nullptr;          // reduction partials
   int part_cap = 0;
   Ctrl* ctrl = nullptr;
@@ -297,7 +307,7 @@ struct Sizes {
   int64_t no, ng, nsb, ntiles, nchunk;
   int32_t nlchunk, lmk_cap;  // landmark point chunks and the most terms of one chunk
   int n6;
-  double intr[4];
+  double intr[kIntrMax];  // fx fy cx cy alpha beta
   double huber;
   int gauge_kind;
   double gauge_center[3];
@@ -309,7 +319,9 @@ struct Sizes {
   int band_c;         // its cluster size
   int band_ring;      // its row slots per CTA
   int lin_dd;          // float-float linearization (Jacobians, products and Z in float-float)
-  int intr_free;       // the pinhole intrinsics are Free: one more (padded) 6-row block, last in S
+  int intr_free;       // the camera params are Free: one more 6-row block, last in S
+  int intr_nk;         // free params: 4 (pinhole, padded to 6 rows) or 6 (EUCM)
+  int eucm;            // the camera is the enhanced unified camera model (else the pinhole)
   int lmk_dd_ok;       // the chunked float-float landmark pass fits (else the warp-per-point kernel)
   int bsub_chunks_ok;  // the chunked back-substitution fits (else the warp-per-point kernel)
   int pcg_mode;        // 0 exact factorization; 1 PCG, block-Jacobi; 2 PCG, learned correction (fallback: exact)

@@ -166,26 +166,81 @@ __device__ __forceinline__ void huber_weighted_dd(float huber, dd huber_dd, dd r
   *o1 = dd_mul(w, r1);
 }
 
+// The camera of the projection: fx fy (cx cy enter only the residual) and,
+// for the enhanced unified camera model, alpha beta
+// (crates/sophus_sensor/src/distortions/enhanced_unified.rs:59-88).  The
+// device intrinsics hold fx fy cx cy alpha beta (alpha = beta = 0 for the
+// pinhole).  The kernels that evaluate Jacobians are instantiated per camera
+// model (template flag E), so the pinhole path carries no EUCM code.
+struct CamF {
+  float fx, fy, alpha, beta;
+};
+struct CamD {
+  dd fx, fy, alpha, beta, one_m_alpha;
+};
+__device__ __forceinline__ CamF cam_f(const double* intr) {
+  return CamF{__double2float_rn(intr[0]), __double2float_rn(intr[1]), __double2float_rn(intr[4]),
+              __double2float_rn(intr[5])};
+}
+__device__ __forceinline__ CamD cam_dd(const double* intr) {
+  return CamD{dd_from_double(intr[0]), dd_from_double(intr[1]), dd_from_double(intr[4]), dd_from_double(intr[5]),
+              dd_from_double(1.0 - intr[4])};
+}
+
+// EUCM distortion of the z = 1 projection (x, y): the distorted point
+// (x / norm, y / norm) with rho = sqrt(beta (x^2 + y^2) + 1),
+// norm = alpha rho + (1 - alpha)  (enhanced_unified.rs:59-88), in float-float.
+__device__ __forceinline__ dd eucm_norm_dd(const CamD& c, dd x, dd y, dd* rho_out, dd* r2_out) {
+  const dd r2 = dd_add(dd_mul(x, x), dd_mul(y, y));
+  const dd rho = dd_sqrt(dd_add(dd_mul(c.beta, r2), dd_make(1.0f, 0.0f)));
+  if (rho_out) *rho_out = rho;
+  if (r2_out) *r2_out = r2;
+  return dd_add(dd_mul(c.alpha, rho), c.one_m_alpha);
+}
+
 // Jacobians of r = z - pi(T_cw p) w.r.t. the left pose perturbation (2x6,
 // tangent [omega; nu]) and the point (2x3), in FP32
 // (crates/sophus_opt/src/nlls/functor_library/costs/pinhole_reprojection.rs:60-95).
+// For the EUCM camera d pi = M d proj with M the 2x2 derivative of the
+// distortion, dx_distort_x (enhanced_unified.rs:117-156):
+//   M = [fx (norm - x n_x), -fx x n_y; -fy y n_x, fy (norm - y n_y)] / norm^2,
+//   n_x = alpha beta x / rho, n_y = alpha beta y / rho,
+// and d proj = [1, 0, -x; 0, 1, -y] / z (perspective.rs:30-39).
 struct JacF {
   float jp[12];  // row-major 2x6
   float jm[6];   // row-major 2x3
 };
+template <bool E>  // E: the EUCM camera, else the pinhole
 __device__ __forceinline__ void jacobians_f(const float* pt /*R_cw 9 + t_cw 3*/, float px, float py,
-                                            float pz, float fx, float fy, JacF* J) {
+                                            float pz, const CamF& c, JacF* J) {
   float xc = pt[0] * px + pt[1] * py + pt[2] * pz + pt[9];
   float yc = pt[3] * px + pt[4] * py + pt[5] * pz + pt[10];
   float zc = pt[6] * px + pt[7] * py + pt[8] * pz + pt[11];
   float iz = 1.0f / zc;
-  float a0 = fx * iz, a2 = -fx * xc * iz * iz;
-  float b1 = fy * iz, b2 = -fy * yc * iz * iz;
   // D = dpi * R_cw (2x3)
   float D[6];
-  for (int k = 0; k < 3; ++k) {
-    D[k] = a0 * pt[0 * 3 + k] + a2 * pt[2 * 3 + k];
-    D[3 + k] = b1 * pt[1 * 3 + k] + b2 * pt[2 * 3 + k];
+  if constexpr (!E) {
+    float a0 = c.fx * iz, a2 = -c.fx * xc * iz * iz;
+    float b1 = c.fy * iz, b2 = -c.fy * yc * iz * iz;
+    for (int k = 0; k < 3; ++k) {
+      D[k] = a0 * pt[0 * 3 + k] + a2 * pt[2 * 3 + k];
+      D[3 + k] = b1 * pt[1 * 3 + k] + b2 * pt[2 * 3 + k];
+    }
+  } else {
+    const float x = xc * iz, y = yc * iz;
+    const float rho = sqrtf(c.beta * (x * x + y * y) + 1.0f);
+    const float nrm = c.alpha * rho + (1.0f - c.alpha);
+    const float in2 = 1.0f / (nrm * nrm);
+    const float ab = c.alpha * c.beta / rho;
+    const float nx = ab * x, ny = ab * y;
+    const float m00 = c.fx * (nrm - x * nx) * in2, m01 = -c.fx * x * ny * in2;
+    const float m10 = -c.fy * y * nx * in2, m11 = c.fy * (nrm - y * ny) * in2;
+    const float a0 = m00 * iz, a1 = m01 * iz, a2 = -(m00 * x + m01 * y) * iz;
+    const float b0 = m10 * iz, b1 = m11 * iz, b2 = -(m10 * x + m11 * y) * iz;
+    for (int k = 0; k < 3; ++k) {
+      D[k] = a0 * pt[0 * 3 + k] + a1 * pt[1 * 3 + k] + a2 * pt[2 * 3 + k];
+      D[3 + k] = b0 * pt[0 * 3 + k] + b1 * pt[1 * 3 + k] + b2 * pt[2 * 3 + k];
+    }
   }
   for (int r = 0; r < 2; ++r) {
     const float* d = D + 3 * r;
@@ -230,7 +285,8 @@ struct JacD {
   dd jp[12];
   dd jm[6];
 };
-__device__ void jacobians_dd(const float* Pd /*R_cw 9 + t_cw 3, (hi, lo) pairs*/, dd px, dd py, dd pz, dd fx, dd fy,
+template <bool E>
+__device__ void jacobians_dd(const float* Pd /*R_cw 9 + t_cw 3, (hi, lo) pairs*/, dd px, dd py, dd pz, const CamD& c,
                              JacD* J) {
   dd R[9], t[3];
   for (int i = 0; i < 9; ++i) R[i] = dd_make(Pd[2 * i], Pd[2 * i + 1]);
@@ -239,13 +295,34 @@ __device__ void jacobians_dd(const float* Pd /*R_cw 9 + t_cw 3, (hi, lo) pairs*/
   dd yc = dd_add(dd_add(dd_add(dd_mul(R[3], px), dd_mul(R[4], py)), dd_mul(R[5], pz)), t[1]);
   dd zc = dd_add(dd_add(dd_add(dd_mul(R[6], px), dd_mul(R[7], py)), dd_mul(R[8], pz)), t[2]);
   dd iz = dd_div(dd_make(1.0f, 0.0f), zc);
-  dd iz2 = dd_mul(iz, iz);
-  dd a0 = dd_mul(fx, iz), a2 = dd_neg(dd_mul(dd_mul(fx, xc), iz2));
-  dd b1 = dd_mul(fy, iz), b2 = dd_neg(dd_mul(dd_mul(fy, yc), iz2));
   dd D[6];
-  for (int k = 0; k < 3; ++k) {
-    D[k] = dd_add(dd_mul(a0, R[0 * 3 + k]), dd_mul(a2, R[2 * 3 + k]));
-    D[3 + k] = dd_add(dd_mul(b1, R[1 * 3 + k]), dd_mul(b2, R[2 * 3 + k]));
+  if constexpr (!E) {
+    dd iz2 = dd_mul(iz, iz);
+    dd a0 = dd_mul(c.fx, iz), a2 = dd_neg(dd_mul(dd_mul(c.fx, xc), iz2));
+    dd b1 = dd_mul(c.fy, iz), b2 = dd_neg(dd_mul(dd_mul(c.fy, yc), iz2));
+    for (int k = 0; k < 3; ++k) {
+      D[k] = dd_add(dd_mul(a0, R[0 * 3 + k]), dd_mul(a2, R[2 * 3 + k]));
+      D[3 + k] = dd_add(dd_mul(b1, R[1 * 3 + k]), dd_mul(b2, R[2 * 3 + k]));
+    }
+  } else {
+    const dd x = dd_mul(xc, iz), y = dd_mul(yc, iz);
+    dd rho;
+    const dd nrm = eucm_norm_dd(c, x, y, &rho, nullptr);
+    const dd in2 = dd_div(dd_make(1.0f, 0.0f), dd_mul(nrm, nrm));
+    const dd ab = dd_div(dd_mul(c.alpha, c.beta), rho);
+    const dd nx = dd_mul(ab, x), ny = dd_mul(ab, y);
+    const dd m00 = dd_mul(dd_mul(c.fx, dd_sub(nrm, dd_mul(x, nx))), in2);
+    const dd m01 = dd_neg(dd_mul(dd_mul(c.fx, dd_mul(x, ny)), in2));
+    const dd m10 = dd_neg(dd_mul(dd_mul(c.fy, dd_mul(y, nx)), in2));
+    const dd m11 = dd_mul(dd_mul(c.fy, dd_sub(nrm, dd_mul(y, ny))), in2);
+    const dd a0 = dd_mul(m00, iz), a1 = dd_mul(m01, iz);
+    const dd a2 = dd_neg(dd_mul(dd_add(dd_mul(m00, x), dd_mul(m01, y)), iz));
+    const dd b0 = dd_mul(m10, iz), b1 = dd_mul(m11, iz);
+    const dd b2 = dd_neg(dd_mul(dd_add(dd_mul(m10, x), dd_mul(m11, y)), iz));
+    for (int k = 0; k < 3; ++k) {
+      D[k] = dd_add(dd_add(dd_mul(a0, R[0 * 3 + k]), dd_mul(a1, R[1 * 3 + k])), dd_mul(a2, R[2 * 3 + k]));
+      D[3 + k] = dd_add(dd_add(dd_mul(b0, R[0 * 3 + k]), dd_mul(b1, R[1 * 3 + k])), dd_mul(b2, R[2 * 3 + k]));
+    }
   }
   for (int r = 0; r < 2; ++r) {
     const dd* d = D + 3 * r;
@@ -335,9 +412,12 @@ struct CostArgs {
 __device__ void decide_body(const double* cost_part, int n_cost, const double* upd_part, int n_upd, Ctrl* ctrl,
                             Record* recs, Record* last);
 
+template <bool E>
 __global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* ctrl) {
   const dd fx_ = a.intr ? dd_from_double(a.intr[0]) : a.fx, fy_ = a.intr ? dd_from_double(a.intr[1]) : a.fy;
   const dd cx_ = a.intr ? dd_from_double(a.intr[2]) : a.cx, cy_ = a.intr ? dd_from_double(a.intr[3]) : a.cy;
+  // EUCM camera: the z = 1 projection is divided by norm
+  const CamD camd = E ? cam_dd(a.intr) : CamD{};
   if (a.decide && !halted(ctrl) && skipping(ctrl)) {
     // no trial (gradient tolerance or a failed solve): decide at once
     if (blockIdx.x == 0) decide_body(a.partials, 0, a.upd_part, a.n_upd, a.decide, a.recs, a.last);
@@ -361,6 +441,11 @@ __global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* c
     }
     dd u = dd_div(xc[0], xc[2]);
     dd v = dd_div(xc[1], xc[2]);
+    if (E) {
+      const dd nrm = eucm_norm_dd(camd, u, v, nullptr, nullptr);
+      u = dd_div(u, nrm);
+      v = dd_div(v, nrm);
+    }
     double2 z = a.uv[o];
     dd ru = dd_sub(dd_from_double(z.x), dd_add(dd_mul(u, fx_), cx_));
     dd rv = dd_sub(dd_from_double(z.y), dd_add(dd_mul(v, fy_), cy_));
@@ -481,10 +566,11 @@ struct LinArgs {
   dd huber_dd;
 };
 
+template <bool E>
 __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
-  const float fx_ = __double2float_rn(a.intr[0]), fy_ = __double2float_rn(a.intr[1]);
-  const dd fxd_ = dd_from_double(a.intr[0]), fyd_ = dd_from_double(a.intr[1]);
-  (void)fx_; (void)fy_; (void)fxd_; (void)fyd_;
+  const CamF cam_ = cam_f(a.intr);
+  const CamD camd_ = cam_dd(a.intr);
+  (void)cam_; (void)camd_;
   if (halted(ctrl)) return;
   __shared__ float red[8][9][33];
   // float-float path: the Jacobians of each lane's first term (a term with
@@ -514,7 +600,7 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
       const float* P = a.pose_f + 12 * a.g_pose[g];
       for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
         JacF J;
-        jacobians_f(P, px, py, pz, fx_, fy_, &J);
+        jacobians_f<E>(P, px, py, pz, cam_, &J);
         float2 r = a.res[o];
         float w = huber_weight_f(a.huber, r.x, r.y);
         float r0 = w * r.x, r1 = w * r.y;
@@ -582,7 +668,7 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
         const bool keep = (g == g0 + lane) && (a.g_begin[g + 1] - a.g_begin[g] == 1);
         for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
           JacD J;
-          jacobians_dd(Pd, pxd, pyd, pzd, fxd_, fyd_, &J);
+          jacobians_dd<E>(Pd, pxd, pyd, pzd, camd_, &J);
           if (keep) {
 #pragma unroll
             for (int k = 0; k < 12; ++k) { jcache[wib][2 * k][lane] = J.jp[k].hi; jcache[wib][2 * k + 1][lane] = J.jp[k].lo; }
@@ -686,7 +772,7 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
         for (int k = 0; k < 18; ++k) W[k] = 0.f;
         for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
           JacF J;
-          jacobians_f(P, px, py, pz, fx_, fy_, &J);
+          jacobians_f<E>(P, px, py, pz, cam_, &J);
 #pragma unroll
           for (int r = 0; r < 6; ++r)
 #pragma unroll
@@ -713,7 +799,7 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
 #pragma unroll
             for (int k = 0; k < 6; ++k) J.jm[k] = dd_make(jcache[wib][24 + 2 * k][lane], jcache[wib][25 + 2 * k][lane]);
           } else {
-            jacobians_dd(Pd, pxd, pyd, pzd, fxd_, fyd_, &J);
+            jacobians_dd<E>(Pd, pxd, pyd, pzd, camd_, &J);
           }
           for (int r = 0; r < 6; ++r)
             for (int q = 0; q < 3; ++q)
@@ -762,10 +848,11 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
 // slow_list and is redone by k_landmark (list mode, float-float path).
 constexpr int kLmkTerms = 256;
 
+template <bool E>
 __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) {
-  const float fx_ = __double2float_rn(a.intr[0]), fy_ = __double2float_rn(a.intr[1]);
-  const dd fxd_ = dd_from_double(a.intr[0]), fyd_ = dd_from_double(a.intr[1]);
-  (void)fx_; (void)fy_; (void)fxd_; (void)fyd_;
+  const CamF cam_ = cam_f(a.intr);
+  const CamD camd_ = cam_dd(a.intr);
+  (void)cam_; (void)camd_;
   if (halted(ctrl)) return;
   extern __shared__ float lsm[];        // [cap][9] term contributions
   __shared__ float sci[kLmkTerms][6];   // C^-1 per point of the chunk (FP32)
@@ -789,7 +876,7 @@ __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) 
       float v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
       for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
         JacF J;
-        jacobians_f(P, px, py, pz, fx_, fy_, &J);
+        jacobians_f<E>(P, px, py, pz, cam_, &J);
         const float2 r = a.res[o];
         const float w = huber_weight_f(a.huber, r.x, r.y);
         const float r0 = w * r.x, r1 = w * r.y;
@@ -888,7 +975,7 @@ __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) 
       for (int k = 0; k < 18; ++k) W[k] = 0.f;
       for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
         JacF J;
-        jacobians_f(P, px, py, pz, fx_, fy_, &J);
+        jacobians_f<E>(P, px, py, pz, cam_, &J);
 #pragma unroll
         for (int r = 0; r < 6; ++r)
 #pragma unroll
@@ -933,10 +1020,11 @@ __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) 
 // over a point's terms differs (sequential here, a lane tree there).
 constexpr int kLmkDDTermFloats = 18 + 36;  // 9 float-float sums + the Jacobians (18 float-float)
 
+template <bool E>
 __global__ void __launch_bounds__(256) k_landmark_chunks_dd(LinArgs a, Ctrl* ctrl) {
-  const float fx_ = __double2float_rn(a.intr[0]), fy_ = __double2float_rn(a.intr[1]);
-  const dd fxd_ = dd_from_double(a.intr[0]), fyd_ = dd_from_double(a.intr[1]);
-  (void)fx_; (void)fy_; (void)fxd_; (void)fyd_;
+  const CamF cam_ = cam_f(a.intr);
+  const CamD camd_ = cam_dd(a.intr);
+  (void)cam_; (void)camd_;
   if (halted(ctrl)) return;
   extern __shared__ float lsd[];               // [cap][kLmkDDTermFloats]
   __shared__ float sci[kLmkTerms][12];         // C^-1 of each point of the chunk (float-float)
@@ -957,7 +1045,7 @@ __global__ void __launch_bounds__(256) k_landmark_chunks_dd(LinArgs a, Ctrl* ctr
       const dd py = dd_from_double(a.points[3 * i + 1]);
       const dd pz = dd_from_double(a.points[3 * i + 2]);
       JacD J;
-      jacobians_dd(a.pose_dd + 24 * a.g_pose[g], px, py, pz, fxd_, fyd_, &J);
+      jacobians_dd<E>(a.pose_dd + 24 * a.g_pose[g], px, py, pz, camd_, &J);
       float* ts = lsd + static_cast<int64_t>(t) * kLmkDDTermFloats;
 #pragma unroll
       for (int k = 0; k < 12; ++k) { ts[18 + 2 * k] = J.jp[k].hi; ts[19 + 2 * k] = J.jp[k].lo; }
@@ -1148,10 +1236,11 @@ struct CamArgs {
   dd huber_dd;
 };
 
+template <bool E>
 __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const Ctrl* ctrl) {
-  const float fx_ = __double2float_rn(a.intr[0]), fy_ = __double2float_rn(a.intr[1]);
-  const dd fxd_ = dd_from_double(a.intr[0]), fyd_ = dd_from_double(a.intr[1]);
-  (void)fx_; (void)fy_; (void)fxd_; (void)fyd_;
+  const CamF cam_ = cam_f(a.intr);
+  const CamD camd_ = cam_dd(a.intr);
+  (void)cam_; (void)camd_;
   if (halted(ctrl)) return;
   const int tile = blockIdx.x;
   const int fb = a.tile_fb[tile];
@@ -1171,7 +1260,7 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
     const float pz = __double2float_rn(a.points[3 * pi + 2]);
     for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
       JacF J;
-      jacobians_f(P, px, py, pz, fx_, fy_, &J);
+      jacobians_f<E>(P, px, py, pz, cam_, &J);
       float2 r = a.res[o];
       float w = huber_weight_f(a.huber, r.x, r.y);
       float r0 = w * r.x, r1 = w * r.y;
@@ -1254,10 +1343,11 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
 // products and sums all in float-float (the loop problems' reduced systems
 // cancel ~25x, beyond what FP32 products leave).  Same outputs as
 // k_camera_tiles.
+template <bool E>
 __global__ void __launch_bounds__(kTileThreads) k_camera_tiles_dd(CamArgs a, const Ctrl* ctrl) {
-  const float fx_ = __double2float_rn(a.intr[0]), fy_ = __double2float_rn(a.intr[1]);
-  const dd fxd_ = dd_from_double(a.intr[0]), fyd_ = dd_from_double(a.intr[1]);
-  (void)fx_; (void)fy_; (void)fxd_; (void)fyd_;
+  const CamF cam_ = cam_f(a.intr);
+  const CamD camd_ = cam_dd(a.intr);
+  (void)cam_; (void)camd_;
   if (halted(ctrl)) return;
   const int tile = blockIdx.x;
   const int fb = a.tile_fb[tile];
@@ -1274,7 +1364,7 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles_dd(CamArgs a, con
     const dd pz = dd_from_double(a.points[3 * pi + 2]);
     for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
       JacD J;
-      jacobians_dd(Pd, px, py, pz, fxd_, fyd_, &J);
+      jacobians_dd<E>(Pd, px, py, pz, camd_, &J);
       const float2 r = a.res[o], rl = a.res_lo[o];
       dd r0, r1;
       huber_weighted_dd(a.huber, a.huber_dd, dd_make(r.x, rl.x), dd_make(r.y, rl.y), &r0, &r1);
@@ -1613,20 +1703,20 @@ struct BackArgs {
   const double* poses;
   double cx, cy, cz;
   double* um;
-  // free intrinsics: dx_m also loses C^-T Zk^T dx_k (dx_k at rows 6 nf .. 6 nf + 3)
-  const float* zk;  // nm x 24 or null
+  // free intrinsics: dx_m also loses C^-T Zk^T dx_k (dx_k at rows 6 nf .. 6 nf + 5)
+  const float* zk;  // nm x kIntrZk or null
   int k0;           // 6 nf
 };
 
 // s[q] += (Zk^T dx_k)_q for a point with terms (free intrinsics).
 __device__ __forceinline__ void intr_backsub_term(const BackArgs& a, int mb, dd* s) {
-  const float* zk = a.zk + 24 * static_cast<int64_t>(mb);
+  const float* zk = a.zk + kIntrZk * static_cast<int64_t>(mb);
   const float2* xk = reinterpret_cast<const float2*>(a.xdd) + a.k0;
 #pragma unroll
   for (int q = 0; q < 3; ++q) {
     dd t = s[q];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+    for (int r = 0; r < kIntrMax; ++r) {
       const float2 xv = xk[r];
       t = dd_add(t, dd_mul(dd_make(xv.x, xv.y), dd_make(zk[2 * (r * 3 + q)], zk[2 * (r * 3 + q) + 1])));
     }
@@ -1877,13 +1967,19 @@ __global__ void __launch_bounds__(256) k_backsub_chunks(BackArgs a, const int32_
 }
 
 // ---------------------------------------------------------------------------
-// Free pinhole intrinsics (kinds F, F, M: the intrinsics family Free).  The
-// intrinsics k = (fx, fy, cx, cy) are one more free variable that every term
-// touches: J_k = d r / d k = -[[x/z, 0, 1, 0], [0, y/z, 0, 1]] per observation
-// (pinhole_reprojection.rs:85, the camera's dx_params), with the reference's
-// nu I per reduced term on its diagonal.  Internally the intrinsics are the
-// last block of S (rows 6 nf .. 6 nf + 5, padded from 4 to 6 rows with an
-// identity, as the oracle pads them); the step is the same in any order.
+// Free intrinsics (kinds F, F, M: the intrinsics family Free).  The camera's
+// params k are one more free variable that every term touches: J_k = d r / d k
+// per observation, the camera's -dx_params (pinhole_reprojection.rs:85):
+//   pinhole, k = (fx, fy, cx, cy):  J_k = -[[x, 0, 1, 0], [0, y, 0, 1]]
+//   EUCM, k = (fx, fy, cx, cy, alpha, beta) (enhanced_unified.rs:158-215):
+//     J_k = -[[mx, 0, 1, 0, -fx x (rho - 1) / norm^2, -fx x alpha r2 / (2 rho norm^2)],
+//             [0, my, 0, 1, -fy y (rho - 1) / norm^2, -fy y alpha r2 / (2 rho norm^2)]]
+//   with (x, y) the z = 1 projection, r2 = x^2 + y^2, (mx, my) = (x, y) / norm;
+// with the reference's nu I per reduced term on its diagonal.  Internally the
+// intrinsics are the last block of S (rows 6 nf .. 6 nf + 5; the pinhole's 4
+// params padded to 6 rows with an identity, as the oracle pads them); the step
+// is the same in any order.  The kernels work on 6 params throughout, the
+// pinhole's J_k having zero columns 4 and 5.
 //   per point i:  Y_i = sum J_k^T J_m,  Zk_i = Y_i C_i^-T,
 //   S_kk = sum J_k^T J_k - sum_i Zk_i Zk_i^T + nu n_terms I,
 //   S_kj = sum_{terms of pose j} (J_k^T J_p - Zk_i Z_g^T),
@@ -1891,10 +1987,15 @@ __global__ void __launch_bounds__(256) k_backsub_chunks(BackArgs a, const int32_
 //   dx_m -= C^-T Zk_i^T dx_k in the back-substitution, k <- k + dx_k.
 // Everything in float-float (these problems are small: the dense solvers).
 // ---------------------------------------------------------------------------
-constexpr int kIntrPart = 18;  // per point: S_kk part (10), J_k^T r~ (4), Zk c (4)
+constexpr int kK = kIntrMax;           // 6 params per J_k row
+constexpr int kKT = kK * (kK + 1) / 2;  // 21 entries of the S_kk triangle
+constexpr int kIntrG = kKT;             // offset of J_k^T r~ in a point's part
+constexpr int kIntrZc = kKT + kK;       // offset of Zk c
+static_assert(kIntrZc + kK == kIntrPart, "per-point intrinsics part layout");
 
 struct IntrArgs {
   int np, nf, n6;
+  int nk;  // free params: 4 (pinhole) or 6 (EUCM)
   int64_t ng;
   const int64_t* pt_g_begin;
   const int64_t* g_begin;
@@ -1918,27 +2019,48 @@ struct IntrArgs {
   const int64_t* tile_end;
   const int64_t* fb_tile_begin;
   double* ipart;  // np x kIntrPart
-  float* zk;      // nm x 24: Zk (4x3) as (hi, lo)
-  double* scj;    // nf x 24: S_kj (4x6)
-  double* isum;   // kIntrPart sums, then -sum J_k^T r~ (4)
+  float* zk;      // nm x kIntrZk: Zk (6x3) as (hi, lo)
+  double* scj;    // nf x kIntrScj: S_kj (6x6)
+  double* isum;   // kIntrPart sums, then -sum J_k^T r~ (6)
   double* S;
   float2* S2;
   double* rb;
   int fail_check;
 };
 
-// The observation's camera-frame point (float-float) and the projection
-// Jacobians: J_p, J_m as jacobians_dd, J_k rows [-u, 0, -1, 0], [0, -v, 0, -1].
-__device__ void intr_term_jacobians(const float* Pd, dd px, dd py, dd pz, dd fxd, dd fyd, JacD* J, dd* u, dd* v) {
+// The observation's projection Jacobians: J_p, J_m as jacobians_dd and J_k
+// (2x6 row-major, columns nk..5 zero).
+__device__ void intr_term_jacobians(const float* Pd, dd px, dd py, dd pz, const CamD& c, int nk, JacD* J, dd* jk) {
   dd R[9], t[3];
   for (int i = 0; i < 9; ++i) R[i] = dd_make(Pd[2 * i], Pd[2 * i + 1]);
   for (int i = 0; i < 3; ++i) t[i] = dd_make(Pd[18 + 2 * i], Pd[18 + 2 * i + 1]);
   const dd xc = dd_add(dd_add(dd_add(dd_mul(R[0], px), dd_mul(R[1], py)), dd_mul(R[2], pz)), t[0]);
   const dd yc = dd_add(dd_add(dd_add(dd_mul(R[3], px), dd_mul(R[4], py)), dd_mul(R[5], pz)), t[1]);
   const dd zc = dd_add(dd_add(dd_add(dd_mul(R[6], px), dd_mul(R[7], py)), dd_mul(R[8], pz)), t[2]);
-  *u = dd_div(xc, zc);
-  *v = dd_div(yc, zc);
-  jacobians_dd(Pd, px, py, pz, fxd, fyd, J);
+  const dd x = dd_div(xc, zc), y = dd_div(yc, zc);
+  const dd zero = dd_make(0.f, 0.f), mone = dd_make(-1.0f, 0.0f);
+  for (int k = 0; k < 2 * kK; ++k) jk[k] = zero;
+  jk[2] = mone;
+  jk[kK + 3] = mone;
+  if (nk == 6) {
+    dd rho, r2;
+    const dd nrm = eucm_norm_dd(c, x, y, &rho, &r2);
+    const dd in2 = dd_div(dd_make(1.0f, 0.0f), dd_mul(nrm, nrm));
+    const dd da = dd_mul(dd_sub(rho, dd_make(1.0f, 0.0f)), in2);                        // (rho - 1) / norm^2
+    const dd db = dd_div(dd_mul(dd_mul(c.alpha, r2), in2), dd_add(rho, rho));        // alpha r2 / (2 rho norm^2)
+    jk[0] = dd_neg(dd_div(x, nrm));
+    jk[kK + 1] = dd_neg(dd_div(y, nrm));
+    const dd fxx = dd_mul(c.fx, x), fyy = dd_mul(c.fy, y);
+    jk[4] = dd_mul(fxx, da);
+    jk[5] = dd_mul(fxx, db);
+    jk[kK + 4] = dd_mul(fyy, da);
+    jk[kK + 5] = dd_mul(fyy, db);
+  } else {
+    jk[0] = dd_neg(x);
+    jk[kK + 1] = dd_neg(y);
+  }
+  if (nk == 6) jacobians_dd<true>(Pd, px, py, pz, c, J);
+  else jacobians_dd<false>(Pd, px, py, pz, c, J);
 }
 
 // One thread per point: its terms' J_k^T J_k, J_k^T r~, Y = J_k^T J_m, then
@@ -1948,74 +2070,70 @@ __global__ void __launch_bounds__(128) k_intr_points(IntrArgs a, const Ctrl* ctr
   if (halted(ctrl)) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.np) return;
-  const dd fxd = dd_from_double(a.intr[0]), fyd = dd_from_double(a.intr[1]);
+  const CamD cam = cam_dd(a.intr);
   const dd px = dd_from_double(a.points[3 * i]), py = dd_from_double(a.points[3 * i + 1]),
            pz = dd_from_double(a.points[3 * i + 2]);
-  dd hkk[10], gk[4], Y[12];
-  for (int k = 0; k < 10; ++k) hkk[k] = dd_make(0.f, 0.f);
-  for (int k = 0; k < 4; ++k) gk[k] = dd_make(0.f, 0.f);
-  for (int k = 0; k < 12; ++k) Y[k] = dd_make(0.f, 0.f);
-  const dd one = dd_make(1.0f, 0.0f);
+  dd hkk[kKT], gk[kK], Y[3 * kK];
+  for (int k = 0; k < kKT; ++k) hkk[k] = dd_make(0.f, 0.f);
+  for (int k = 0; k < kK; ++k) gk[k] = dd_make(0.f, 0.f);
+  for (int k = 0; k < 3 * kK; ++k) Y[k] = dd_make(0.f, 0.f);
   for (int64_t g = a.pt_g_begin[i]; g < a.pt_g_begin[i + 1]; ++g) {
     JacD J;
-    dd u, v;
-    intr_term_jacobians(a.pose_dd + 24 * a.g_pose[g], px, py, pz, fxd, fyd, &J, &u, &v);
-    // J_k (2x4): row 0 = (-u, 0, -1, 0), row 1 = (0, -v, 0, -1)
-    const dd jk[8] = {dd_neg(u), dd_make(0.f, 0.f), dd_neg(one), dd_make(0.f, 0.f),
-                      dd_make(0.f, 0.f), dd_neg(v), dd_make(0.f, 0.f), dd_neg(one)};
+    dd jk[2 * kK];
+    intr_term_jacobians(a.pose_dd + 24 * a.g_pose[g], px, py, pz, cam, a.nk, &J, jk);
     for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o) {
       const float2 r = a.res[o];
       dd r0, r1;
       huber_weighted_dd(a.huber, a.huber_dd, dd_from_float(r.x), dd_from_float(r.y), &r0, &r1);
       int k = 0;
-      for (int p = 0; p < 4; ++p) {
-        for (int q = p; q < 4; ++q) {
-          hkk[k] = dd_add(hkk[k], dd_add(dd_mul(jk[p], jk[q]), dd_mul(jk[4 + p], jk[4 + q])));
+      for (int p = 0; p < kK; ++p) {
+        for (int q = p; q < kK; ++q) {
+          hkk[k] = dd_add(hkk[k], dd_add(dd_mul(jk[p], jk[q]), dd_mul(jk[kK + p], jk[kK + q])));
           ++k;
         }
-        gk[p] = dd_add(gk[p], dd_add(dd_mul(jk[p], r0), dd_mul(jk[4 + p], r1)));
+        gk[p] = dd_add(gk[p], dd_add(dd_mul(jk[p], r0), dd_mul(jk[kK + p], r1)));
         for (int s2 = 0; s2 < 3; ++s2)
-          Y[p * 3 + s2] = dd_add(Y[p * 3 + s2], dd_add(dd_mul(jk[p], J.jm[s2]), dd_mul(jk[4 + p], J.jm[3 + s2])));
+          Y[p * 3 + s2] = dd_add(Y[p * 3 + s2], dd_add(dd_mul(jk[p], J.jm[s2]), dd_mul(jk[kK + p], J.jm[3 + s2])));
       }
     }
   }
   double* out = a.ipart + static_cast<int64_t>(i) * kIntrPart;
   const int mb = a.pt_mb[i];
-  dd zz[10], zc4[4];
-  for (int k = 0; k < 10; ++k) zz[k] = dd_make(0.f, 0.f);
-  for (int k = 0; k < 4; ++k) zc4[k] = dd_make(0.f, 0.f);
+  dd zz[kKT], zc[kK];
+  for (int k = 0; k < kKT; ++k) zz[k] = dd_make(0.f, 0.f);
+  for (int k = 0; k < kK; ++k) zc[k] = dd_make(0.f, 0.f);
   if (mb >= 0 && a.pt_g_begin[i + 1] > a.pt_g_begin[i]) {
     const float* cp = a.cinv + 12 * mb;
     dd I[6];
     for (int k = 0; k < 6; ++k) I[k] = dd_make(cp[2 * k], cp[2 * k + 1]);
     const float* cv = a.cvec + 6 * mb;
     const dd c[3] = {dd_make(cv[0], cv[1]), dd_make(cv[2], cv[3]), dd_make(cv[4], cv[5])};
-    dd Zk[12];
-    for (int r = 0; r < 4; ++r) {
+    dd Zk[3 * kK];
+    for (int r = 0; r < kK; ++r) {
       Zk[r * 3 + 0] = dd_mul(I[0], Y[r * 3 + 0]);
       Zk[r * 3 + 1] = dd_add(dd_mul(I[1], Y[r * 3 + 0]), dd_mul(I[2], Y[r * 3 + 1]));
       Zk[r * 3 + 2] = dd_add(dd_add(dd_mul(I[3], Y[r * 3 + 0]), dd_mul(I[4], Y[r * 3 + 1])), dd_mul(I[5], Y[r * 3 + 2]));
     }
     int k = 0;
-    for (int p = 0; p < 4; ++p) {
-      for (int q = p; q < 4; ++q) {
+    for (int p = 0; p < kK; ++p) {
+      for (int q = p; q < kK; ++q) {
         dd t = dd_make(0.f, 0.f);
         for (int s2 = 0; s2 < 3; ++s2) t = dd_add(t, dd_mul(Zk[p * 3 + s2], Zk[q * 3 + s2]));
         zz[k++] = t;
       }
       dd t = dd_make(0.f, 0.f);
       for (int s2 = 0; s2 < 3; ++s2) t = dd_add(t, dd_mul(Zk[p * 3 + s2], c[s2]));
-      zc4[p] = t;
+      zc[p] = t;
     }
-    float* zo = a.zk + 24 * static_cast<int64_t>(mb);
-    for (int k2 = 0; k2 < 12; ++k2) {
+    float* zo = a.zk + kIntrZk * static_cast<int64_t>(mb);
+    for (int k2 = 0; k2 < 3 * kK; ++k2) {
       zo[2 * k2] = Zk[k2].hi;
       zo[2 * k2 + 1] = Zk[k2].lo;
     }
   }
-  for (int k = 0; k < 10; ++k) out[k] = dd_to_double(dd_sub(hkk[k], zz[k]));
-  for (int k = 0; k < 4; ++k) out[10 + k] = dd_to_double(gk[k]);
-  for (int k = 0; k < 4; ++k) out[14 + k] = dd_to_double(zc4[k]);
+  for (int k = 0; k < kKT; ++k) out[k] = dd_to_double(dd_sub(hkk[k], zz[k]));
+  for (int k = 0; k < kK; ++k) out[kIntrG + k] = dd_to_double(gk[k]);
+  for (int k = 0; k < kK; ++k) out[kIntrZc + k] = dd_to_double(zc[k]);
 }
 
 // One CTA: the per-point parts summed in a fixed order; the intrinsics'
@@ -2044,8 +2162,8 @@ __global__ void __launch_bounds__(256) k_intr_reduce(IntrArgs a, Ctrl* ctrl) {
   }
   if (threadIdx.x == 0) {
     double mg = 0.0;
-    for (int k = 0; k < 4; ++k) {
-      const double bk = -a.isum[10 + k];
+    for (int k = 0; k < kK; ++k) {
+      const double bk = -a.isum[kIntrG + k];
       a.isum[kIntrPart + k] = bk;
       mg = fmax(mg, fabs(bk));
     }
@@ -2054,30 +2172,29 @@ __global__ void __launch_bounds__(256) k_intr_reduce(IntrArgs a, Ctrl* ctrl) {
 }
 
 // One CTA per free pose: S_kj = sum over its terms of J_k^T J_p - Zk_i Z_g^T.
+// Thread t < nk * 6 of the final sum owns entry t (row t / 6 of S_kj).
 __global__ void __launch_bounds__(128) k_intr_cams(IntrArgs a, const Ctrl* ctrl) {
   if (halted(ctrl)) return;
   const int fb = blockIdx.x;
-  __shared__ float sh_hi[24][129], sh_lo[24][129];
-  dd acc[24];
-  for (int k = 0; k < 24; ++k) acc[k] = dd_make(0.f, 0.f);
-  const dd fxd = dd_from_double(a.intr[0]), fyd = dd_from_double(a.intr[1]);
+  constexpr int kE = kK * 6;
+  __shared__ float sh_hi[kE][129], sh_lo[kE][129];
+  dd acc[kE];
+  for (int k = 0; k < kE; ++k) acc[k] = dd_make(0.f, 0.f);
+  const CamD cam = cam_dd(a.intr);
   const int64_t t0 = a.fb_tile_begin[fb], t1 = a.fb_tile_begin[fb + 1];
   const int64_t e0 = (t1 > t0) ? a.tile_begin[t0] : 0, e1 = (t1 > t0) ? a.tile_end[t1 - 1] : 0;
-  const dd one = dd_make(1.0f, 0.0f);
   for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
     const int64_t g = a.cam_g[e];
     const int i = a.g_pt[g];
     const dd px = dd_from_double(a.points[3 * i]), py = dd_from_double(a.points[3 * i + 1]),
              pz = dd_from_double(a.points[3 * i + 2]);
     JacD J;
-    dd u, v;
-    intr_term_jacobians(a.pose_dd + 24 * a.g_pose[g], px, py, pz, fxd, fyd, &J, &u, &v);
-    const dd jk[8] = {dd_neg(u), dd_make(0.f, 0.f), dd_neg(one), dd_make(0.f, 0.f),
-                      dd_make(0.f, 0.f), dd_neg(v), dd_make(0.f, 0.f), dd_neg(one)};
+    dd jk[2 * kK];
+    intr_term_jacobians(a.pose_dd + 24 * a.g_pose[g], px, py, pz, cam, a.nk, &J, jk);
     for (int64_t o = a.g_begin[g]; o < a.g_begin[g + 1]; ++o)
-      for (int p = 0; p < 4; ++p)
+      for (int p = 0; p < kK; ++p)
         for (int q = 0; q < 6; ++q)
-          acc[p * 6 + q] = dd_add(acc[p * 6 + q], dd_add(dd_mul(jk[p], J.jp[q]), dd_mul(jk[4 + p], J.jp[6 + q])));
+          acc[p * 6 + q] = dd_add(acc[p * 6 + q], dd_add(dd_mul(jk[p], J.jp[q]), dd_mul(jk[kK + p], J.jp[6 + q])));
     const int mb = a.pt_mb[i];
     if (mb >= 0) {
       // Z_g (6x3): float-float where the landmark pass kept it so, else FP32
@@ -2090,8 +2207,8 @@ __global__ void __launch_bounds__(128) k_intr_cams(IntrArgs a, const Ctrl* ctrl)
       }
       const float* zd = a.zdd ? a.zdd + kZddFloats * g : ((zf[18] != 0.f && a.zdd_flagged) ? a.zdd_flagged + kZddFloats * g : nullptr);
       for (int k = 0; k < 18; ++k) Z[k] = zd ? dd_make(zd[2 * k], zd[2 * k + 1]) : dd_from_float(zf[k]);
-      const float* zk = a.zk + 24 * static_cast<int64_t>(mb);
-      for (int p = 0; p < 4; ++p)
+      const float* zk = a.zk + kIntrZk * static_cast<int64_t>(mb);
+      for (int p = 0; p < kK; ++p)
         for (int q = 0; q < 6; ++q) {
           dd t = dd_make(0.f, 0.f);
           for (int s2 = 0; s2 < 3; ++s2)
@@ -2100,21 +2217,21 @@ __global__ void __launch_bounds__(128) k_intr_cams(IntrArgs a, const Ctrl* ctrl)
         }
     }
   }
-  for (int k = 0; k < 24; ++k) {
+  for (int k = 0; k < kE; ++k) {
     sh_hi[k][threadIdx.x] = acc[k].hi;
     sh_lo[k][threadIdx.x] = acc[k].lo;
   }
   __syncthreads();
-  if (threadIdx.x < 24) {
+  if (threadIdx.x < kE) {
     const int k = threadIdx.x;
     dd t = dd_make(0.f, 0.f);
     for (int q = 0; q < static_cast<int>(blockDim.x); ++q) t = dd_add(t, dd_make(sh_hi[k][q], sh_lo[k][q]));
-    a.scj[24 * static_cast<int64_t>(fb) + k] = dd_to_double(t);
+    a.scj[kIntrScj * static_cast<int64_t>(fb) + k] = dd_to_double(t);
   }
 }
 
 // The intrinsics rows of S (block nf, both triangles) and of the reduced rhs:
-// blocks 0..nf-1 write S_kj, block nf the damped S_kk (identity padding).
+// blocks 0..nf-1 write S_kj, block nf the damped S_kk (rows nk..5 an identity).
 __global__ void __launch_bounds__(64) k_intr_fill(IntrArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   const int b = blockIdx.x;
@@ -2123,7 +2240,7 @@ __global__ void __launch_bounds__(64) k_intr_fill(IntrArgs a, const Ctrl* ctrl) 
   if (e >= 36) return;
   const int r = e / 6, c = e % 6;
   if (b < a.nf) {
-    const double v = (r < 4) ? a.scj[24 * static_cast<int64_t>(b) + r * 6 + c] : 0.0;
+    const double v = (r < a.nk) ? a.scj[kIntrScj * static_cast<int64_t>(b) + r * 6 + c] : 0.0;
     const int64_t row = k0 + r, col = 6 * b + c;
     a.S[row * a.n6 + col] = v;
     a.S[col * a.n6 + row] = v;
@@ -2134,9 +2251,9 @@ __global__ void __launch_bounds__(64) k_intr_fill(IntrArgs a, const Ctrl* ctrl) 
     }
   } else {
     double v;
-    if (r < 4 && c < 4) {
+    if (r < a.nk && c < a.nk) {
       const int p = r < c ? r : c, q = r < c ? c : r;
-      const int idx = p * 4 - p * (p - 1) / 2 + (q - p);
+      const int idx = p * kK - p * (p - 1) / 2 + (q - p);
       v = a.isum[idx];
       if (r == c) v += ctrl->nu * static_cast<double>(a.ng);
     } else {
@@ -2148,7 +2265,7 @@ __global__ void __launch_bounds__(64) k_intr_fill(IntrArgs a, const Ctrl* ctrl) 
       const dd vd = dd_from_double(v);
       a.S2[row * a.n6 + col] = make_float2(vd.hi, vd.lo);
     }
-    if (c == 0) a.rb[k0 + r] = (r < 4) ? a.isum[kIntrPart + r] - a.isum[14 + r] : 0.0;
+    if (c == 0) a.rb[k0 + r] = (r < a.nk) ? a.isum[kIntrPart + r] - a.isum[kIntrZc + r] : 0.0;
   }
 }
 
@@ -2157,6 +2274,7 @@ IntrArgs intr_args(const Sizes& s, const Dev& d) {
   a.np = s.np;
   a.nf = s.nf;
   a.n6 = s.n6;
+  a.nk = s.intr_nk;
   a.ng = s.ng;
   a.pt_g_begin = d.pt_g_begin;
   a.g_begin = d.g_begin;
@@ -2306,8 +2424,9 @@ struct UpdArgs {
   const double* um;          // the points' part of the projection direction
   float* pose_f;   // trial pose tables, written here for the trial cost
   float* pose_dd;
-  // free intrinsics: k_t = k + dx_k (dx_k at xf[6 nf .. 6 nf + 3]), neg_grad bk
+  // free intrinsics: k_t = k + dx_k (dx_k at xf[6 nf .. 6 nf + nk - 1]), neg_grad bk
   int intr_free;
+  int intr_nk;
   const double* intr;
   double* intr_t;
   const double* bk;
@@ -2341,7 +2460,7 @@ __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
   double mx = 0.0;
   if (a.intr_free && blockIdx.x == 0 && threadIdx.x == 0) {
     // the intrinsics are a vector space: k + dx_k (no gauge component)
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < a.intr_nk; ++k) {
       const double xk = a.xf[6 * a.nf + k];
       a.intr_t[k] = a.intr[k] + xk;
       const dd x = dd_from_double(xk);
@@ -2527,7 +2646,7 @@ __global__ void k_commit(int nc, int np, int64_t no, const double* poses_t, doub
   if (!ctrl->accept) return;
   const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
   const int64_t t0 = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  if (intr && t0 < 4) intr[t0] = intr_t[t0];
+  if (intr && t0 < kIntrMax) intr[t0] = intr_t[t0];
   for (int64_t t = t0; t < no; t += stride) res[t] = res_t[t];
   if (res_lo)
     for (int64_t t = t0; t < no; t += stride) res_lo[t] = res_lo_t[t];
@@ -2589,7 +2708,7 @@ int launch_cost(const Sizes& s, const Dev& d, const double* poses, const double*
                 float2* res_out, double* partials, cudaStream_t st) {
   k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, poses, d.pose_f, d.pose_dd, d.ctrl, 1, nullptr, nullptr);
   CostArgs a = make_cost_args(s, d, points, res_out, partials, 1);
-  k_cost<<<cost_grid(s.no), kCostThreads, 0, st>>>(a, d.ctrl);
+  (s.eucm ? k_cost<true> : k_cost<false>)<<<cost_grid(s.no), kCostThreads, 0, st>>>(a, d.ctrl);
   return 2;
 }
 
@@ -2597,7 +2716,7 @@ int launch_init_merit(const Sizes& s, const Dev& d, cudaStream_t st) {
   k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, d.poses, d.pose_f, d.pose_dd, d.ctrl, 0, nullptr, nullptr);
   CostArgs a = make_cost_args(s, d, d.points, d.res, d.part, 0);
   const int nb = cost_grid(s.no);
-  k_cost<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
+  (s.eucm ? k_cost<true> : k_cost<false>)<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
   k_init_merit<<<1, 256, 0, st>>>(d.part, nb, d.ctrl);
   return 3;
 }
@@ -2676,8 +2795,9 @@ static CamArgs make_cam_args(const Sizes& s, const Dev& d, int with_schur) {
 static int launch_camera(const Sizes& s, const Dev& d, int with_schur, cudaStream_t st) {
   if (s.ntiles == 0) return 0;
   const CamArgs ca = make_cam_args(s, d, with_schur);
-  if (s.lin_dd) k_camera_tiles_dd<<<static_cast<unsigned>(s.ntiles), kTileThreads, 0, st>>>(ca, d.ctrl);
-  else k_camera_tiles<<<static_cast<unsigned>(s.ntiles), kTileThreads, 0, st>>>(ca, d.ctrl);
+  const unsigned nt = static_cast<unsigned>(s.ntiles);
+  if (s.lin_dd) (s.eucm ? k_camera_tiles_dd<true> : k_camera_tiles_dd<false>)<<<nt, kTileThreads, 0, st>>>(ca, d.ctrl);
+  else (s.eucm ? k_camera_tiles<true> : k_camera_tiles<false>)<<<nt, kTileThreads, 0, st>>>(ca, d.ctrl);
   return 1;
 }
 
@@ -2719,31 +2839,39 @@ static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
 static int launch_landmark(const Sizes& s, const Dev& d, LinArgs la, cudaStream_t st, bool zero_slow = true) {
   if (!la.use_override && s.nlchunk > 0 && s.lin_dd && s.lmk_dd_ok) {
     const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
-    k_landmark_chunks_dd<<<grid, 256, sizeof(float) * kLmkDDTermFloats * static_cast<size_t>(s.lmk_cap), st>>>(
-        la, d.ctrl);
+    const size_t smem = sizeof(float) * kLmkDDTermFloats * static_cast<size_t>(s.lmk_cap);
+    (s.eucm ? k_landmark_chunks_dd<true> : k_landmark_chunks_dd<false>)<<<grid, 256, smem, st>>>(la, d.ctrl);
     return 1;
   }
   if (!la.use_override && s.nlchunk > 0 && !s.lin_dd) {
     if (zero_slow) cudaMemsetAsync(d.slow_count, 0, sizeof(int32_t), st);
     const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
-    k_landmark_chunks<<<grid, 256, sizeof(float) * 9 * static_cast<size_t>(s.lmk_cap), st>>>(la, d.ctrl);
+    const size_t smem = sizeof(float) * 9 * static_cast<size_t>(s.lmk_cap);
+    (s.eucm ? k_landmark_chunks<true> : k_landmark_chunks<false>)<<<grid, 256, smem, st>>>(la, d.ctrl);
     LinArgs lb = la;
     lb.list = d.slow_list;
     lb.list_count = d.slow_count;
-    k_landmark<<<s.lmk_list_grid, 256, 0, st>>>(lb, d.ctrl);
+    (s.eucm ? k_landmark<true> : k_landmark<false>)<<<s.lmk_list_grid, 256, 0, st>>>(lb, d.ctrl);
     return 2;
   }
-  k_landmark<<<warp_grid(s.np, 8, s.lin_dd ? 16384 : 4096), 256, 0, st>>>(la, d.ctrl);
+  const int wg = warp_grid(s.np, 8, s.lin_dd ? 16384 : 4096);
+  (s.eucm ? k_landmark<true> : k_landmark<false>)<<<wg, 256, 0, st>>>(la, d.ctrl);
   return 1;
+}
+
+// Raises the dynamic shared memory limit of both camera-model instances.
+template <class K>
+static int raise_both(K pinhole, K eucm, size_t bytes) {
+  return (raise_dynamic_smem(reinterpret_cast<const void*>(pinhole), bytes) == cudaSuccess &&
+          raise_dynamic_smem(reinterpret_cast<const void*>(eucm), bytes) == cudaSuccess)
+             ? 0
+             : -1;
 }
 
 int landmark_setup(int cap) {
   const size_t bytes = sizeof(float) * 9 * static_cast<size_t>(cap);
   if (bytes <= 48 * 1024) return 0;
-  return raise_dynamic_smem(reinterpret_cast<const void*>(k_landmark_chunks), bytes) ==
-                 cudaSuccess
-             ? 0
-             : -1;
+  return raise_both(k_landmark_chunks<false>, k_landmark_chunks<true>, bytes);
 }
 
 int backsub_chunks_setup(int cap) {
@@ -2757,7 +2885,7 @@ int landmark_dd_setup(int cap) {
   const size_t bytes = sizeof(float) * kLmkDDTermFloats * static_cast<size_t>(cap);
   if (bytes > 200 * 1024) return -1;
   if (bytes <= 48 * 1024) return 0;
-  return raise_dynamic_smem(reinterpret_cast<const void*>(k_landmark_chunks_dd), bytes) == cudaSuccess ? 0 : -1;
+  return raise_both(k_landmark_chunks_dd<false>, k_landmark_chunks_dd<true>, bytes);
 }
 
 int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_override,
@@ -2849,6 +2977,7 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
   u.gauge_blocks = kUpdBlocks;
   u.um = d.gauge_um;
   u.intr_free = s.intr_free;
+  u.intr_nk = s.intr_nk;
   u.intr = d.intr;
   u.intr_t = d.intr_t;
   u.bk = d.intr_sum ? d.intr_sum + kIntrPart : nullptr;
@@ -2869,7 +2998,7 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) 
       return launch_camera(s, d, 1, st);
     case 4: {
       CostArgs a = make_cost_args(s, d, d.points_t, d.res_t, d.part + 4 * kUpdBlocks, 1);
-      k_cost<<<cost_grid(s.no), kCostThreads, 0, st>>>(a, d.ctrl);
+      (s.eucm ? k_cost<true> : k_cost<false>)<<<cost_grid(s.no), kCostThreads, 0, st>>>(a, d.ctrl);
       return 1;
     }
     case 5:
@@ -2892,7 +3021,7 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
   a.n_upd = kUpdBlocks;
   a.recs = d.records;
   a.last = d.last_rec;
-  k_cost<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
+  (s.eucm ? k_cost<true> : k_cost<false>)<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
   const int64_t big = s.no > 7 * (int64_t)s.nc ? s.no : 7 * (int64_t)s.nc;
   const int64_t items = big > 3 * (int64_t)s.np ? big : 3 * (int64_t)s.np;
   int cb = static_cast<int>((items + 255) / 256);
@@ -2913,25 +3042,25 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
 namespace {
 __global__ void k_debug_jacobians(int64_t n, const int32_t* __restrict__ cam, const int32_t* __restrict__ pt,
                                   const double* __restrict__ poses, const double* __restrict__ points,
-                                  const double* __restrict__ intr, int precision, double* __restrict__ jp,
+                                  const double* __restrict__ intr, int eucm, int precision, double* __restrict__ jp,
                                   double* __restrict__ jm) {
   const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (i >= n) return;
-  const double fx = intr[0], fy = intr[1];
   float pf[12], pd[24];
   pose_table(poses + 7 * static_cast<int64_t>(cam[i]), pf, pd);
   const double* pw = points + 3 * static_cast<int64_t>(pt[i]);
   if (precision == 0) {
     JacF J;
-    jacobians_f(pf, __double2float_rn(pw[0]), __double2float_rn(pw[1]), __double2float_rn(pw[2]),
-                static_cast<float>(fx), static_cast<float>(fy), &J);
+    const float qx = __double2float_rn(pw[0]), qy = __double2float_rn(pw[1]), qz = __double2float_rn(pw[2]);
+    if (eucm) jacobians_f<true>(pf, qx, qy, qz, cam_f(intr), &J);
+    else jacobians_f<false>(pf, qx, qy, qz, cam_f(intr), &J);
     for (int k = 0; k < 12; ++k) jp[12 * i + k] = J.jp[k];
     for (int k = 0; k < 6; ++k) jm[6 * i + k] = J.jm[k];
   } else {
     JacD J;
-    const dd fxd = dd_make(static_cast<float>(fx), static_cast<float>(fx - static_cast<float>(fx)));
-    const dd fyd = dd_make(static_cast<float>(fy), static_cast<float>(fy - static_cast<float>(fy)));
-    jacobians_dd(pd, dd_from_double(pw[0]), dd_from_double(pw[1]), dd_from_double(pw[2]), fxd, fyd, &J);
+    const dd qx = dd_from_double(pw[0]), qy = dd_from_double(pw[1]), qz = dd_from_double(pw[2]);
+    if (eucm) jacobians_dd<true>(pd, qx, qy, qz, cam_dd(intr), &J);
+    else jacobians_dd<false>(pd, qx, qy, qz, cam_dd(intr), &J);
     for (int k = 0; k < 12; ++k) jp[12 * i + k] = dd_to_double(J.jp[k]);
     for (int k = 0; k < 6; ++k) jm[6 * i + k] = dd_to_double(J.jm[k]);
   }
@@ -2943,7 +3072,7 @@ cudaError_t launch_debug_jacobians(const Sizes& s, const Dev& d, int64_t n, cons
   if (n <= 0) return cudaSuccess;
   const int64_t blocks = (n + 127) / 128;
   k_debug_jacobians<<<static_cast<unsigned>(blocks), 128, 0, st>>>(n, cam, pt, d.poses, d.points, d.intr,
-                                                                   precision, jp, jm);
+                                                                   s.eucm, precision, jp, jm);
   return cudaGetLastError();
 }
 

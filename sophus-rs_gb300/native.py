@@ -23,6 +23,9 @@ ERR_OUT_OF_MEMORY = -6
 ERR_STATE = -7
 ERR_DEVICE_TIMEOUT = -8
 
+CAMERA_PINHOLE = 0
+CAMERA_EUCM = 1
+
 # sgba_termination
 TERM_NONE = 0
 TERM_FUNCTION_TOLERANCE = 1
@@ -97,7 +100,8 @@ class Layout(C.Structure):
 
 
 class ProblemOptions(C.Structure):
-    _fields_ = [("intrinsics_free", C.c_int32), ("camera_model", C.c_int32), ("reserved", C.c_int32 * 6)]
+    _fields_ = [("intrinsics_free", C.c_int32), ("camera_model", C.c_int32),
+                ("eucm_alpha_beta", C.c_double * 2), ("reserved", C.c_int32 * 2)]
 
 
 class Profile(C.Structure):
@@ -283,10 +287,13 @@ class Problem:
 
     def __init__(self, data, device=-1, intrinsics_free=None):
         """intrinsics_free (default: data.intrinsics_free, else False): the
-        pinhole intrinsics are a Free family, optimised with the poses."""
+        camera params are a Free family, optimised with the poses.  The camera
+        is data.camera_model (CAMERA_PINHOLE when absent; CAMERA_EUCM with
+        data.eucm_alpha_beta)."""
         L = lib()
         if intrinsics_free is None:
             intrinsics_free = bool(getattr(data, "intrinsics_free", False))
+        self.camera_model = int(getattr(data, "camera_model", CAMERA_PINHOLE))
         self._keep = []
         poses = np.ascontiguousarray(data.poses, dtype=np.float64).reshape(-1, 7)
         points = np.ascontiguousarray(data.points, dtype=np.float64).reshape(-1, 3)
@@ -315,9 +322,14 @@ class Problem:
         d.obs_uv = _dptr(obs_uv)
         d.huber_delta = float(data.huber_delta) if data.huber_delta is not None else 0.0
         h = C.c_void_p()
-        if intrinsics_free:
+        if intrinsics_free or self.camera_model != CAMERA_PINHOLE:
             opts = ProblemOptions()
-            opts.intrinsics_free = 1
+            opts.intrinsics_free = 1 if intrinsics_free else 0
+            opts.camera_model = self.camera_model
+            if self.camera_model == CAMERA_EUCM:
+                ab = data.eucm_alpha_beta
+                opts.eucm_alpha_beta[0] = float(ab[0])
+                opts.eucm_alpha_beta[1] = float(ab[1])
             check(L.sgba_problem_create_ex(C.byref(d), C.byref(opts), int(device), C.byref(h)))
         else:
             check(L.sgba_problem_create(C.byref(d), int(device), C.byref(h)))
@@ -388,8 +400,8 @@ class Problem:
         return (hr, hc), (sr, sc)
 
     def intrinsics(self):
-        """Current fx fy cx cy."""
-        out = np.empty(4)
+        """Current fx fy cx cy (then alpha beta for the EUCM camera)."""
+        out = np.empty(6 if self.camera_model == CAMERA_EUCM else 4)
         check(lib().sgba_get_intrinsics(self._h, _dptr(out)))
         return out
 

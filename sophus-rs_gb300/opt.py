@@ -14,10 +14,14 @@ to the GB300 backend:
   HuberKernel              crates/sophus_opt/src/robust_kernel.rs
   PinholeCameraReprojectionCostTerm
                            crates/sophus_opt/src/nlls/functor_library/costs/pinhole_reprojection.rs:28-95
+  EucmCameraReprojectionCostTerm
+                           crates/sophus_opt/src/example_problems/ba_problem.rs:69-110
+  PinholeCameraF64 / EnhancedUnifiedCameraF64
+                           crates/sophus_sensor/src/camera_enum/perspective_camera.rs:53-71
 
-Only the bundle-adjustment specialisation runs here (pinhole reprojection,
-intrinsics Conditioned, poses Free, points Marginalized, a Schur solver);
-other configurations raise NotOnGpuPath.
+Only the bundle-adjustment specialisation runs here (pinhole or EUCM
+reprojection, intrinsics Conditioned or Free, poses Free, points
+Marginalized, a Schur solver); other configurations raise NotOnGpuPath.
 """
 import enum
 from collections import OrderedDict
@@ -106,6 +110,19 @@ class PinholeCameraF64:
         return PinholeCameraF64(params, image_size)
 
 
+class EnhancedUnifiedCameraF64:
+    """Enhanced unified camera with params [fx, fy, cx, cy, alpha, beta]
+    (sophus_sensor EnhancedUnifiedCameraF64)."""
+
+    def __init__(self, params, image_size=(640, 480)):
+        self.params = np.asarray(params, dtype=np.float64).reshape(6).copy()
+        self.image_size = tuple(image_size)
+
+    @staticmethod
+    def from_params_and_size(params, image_size):
+        return EnhancedUnifiedCameraF64(params, image_size)
+
+
 class VarFamily:
     """A family of variables of one type (var_family.rs)."""
 
@@ -139,6 +156,8 @@ class VarFamily:
             return 6
         if isinstance(first, PinholeCameraF64):
             return 4
+        if isinstance(first, EnhancedUnifiedCameraF64):
+            return 6
         return int(np.asarray(first).size)
 
     def num_active(self):
@@ -186,6 +205,14 @@ class PinholeCameraReprojectionCostTerm:
     entity_indices: Any
 
 
+@dataclass
+class EucmCameraReprojectionCostTerm:
+    """uv_in_image, entity_indices = [intrinsics, pose, point] (EUCM camera)."""
+
+    uv_in_image: Any
+    entity_indices: Any
+
+
 class PinholeReprojectionTerms:
     """Struct-of-arrays container of many PinholeCameraReprojectionCostTerm."""
 
@@ -199,6 +226,10 @@ class PinholeReprojectionTerms:
         return self.uv_in_image.shape[0]
 
 
+class EucmReprojectionTerms(PinholeReprojectionTerms):
+    """Struct-of-arrays container of many EucmCameraReprojectionCostTerm."""
+
+
 class CostTerms:
     def __init__(self, family_names, terms):
         self.family_names = list(family_names)
@@ -206,9 +237,12 @@ class CostTerms:
             self.terms = terms
         else:
             terms = list(terms)
-            if terms and not all(isinstance(t, PinholeCameraReprojectionCostTerm) for t in terms):
-                raise NotOnGpuPath("only PinholeCameraReprojectionCostTerm residuals run on this backend")
-            self.terms = PinholeReprojectionTerms(
+            kinds = {type(t) for t in terms}
+            if not kinds <= {PinholeCameraReprojectionCostTerm, EucmCameraReprojectionCostTerm} or len(kinds) > 1:
+                raise NotOnGpuPath("only PinholeCameraReprojectionCostTerm or EucmCameraReprojectionCostTerm "
+                                   "residuals (one kind per CostTerms) run on this backend")
+            soa = EucmReprojectionTerms if kinds == {EucmCameraReprojectionCostTerm} else PinholeReprojectionTerms
+            self.terms = soa(
                 np.array([t.uv_in_image for t in terms], dtype=np.float64).reshape(-1, 2),
                 np.array([t.entity_indices for t in terms], dtype=np.int64).reshape(-1, 3))
 
@@ -388,8 +422,13 @@ def _extract_problem(variables, cost_fns):
     if len(intr) != 1:
         raise NotOnGpuPath("GPU path supports one intrinsics member")
     cam = intr[0]
-    cparams = cam.params if isinstance(cam, PinholeCameraF64) else np.asarray(cam, float)
     terms = cf.cost_terms.terms
+    eucm = isinstance(terms, EucmReprojectionTerms)
+    if eucm != isinstance(cam, EnhancedUnifiedCameraF64) and not isinstance(cam, np.ndarray):
+        raise NotOnGpuPath("the camera type does not match the reprojection cost term")
+    cparams = cam.params if isinstance(cam, (PinholeCameraF64, EnhancedUnifiedCameraF64)) else np.asarray(cam, float)
+    if cparams.size != (6 if eucm else 4):
+        raise NotOnGpuPath("camera params: expected %d, got %d" % (6 if eucm else 4, cparams.size))
     idx = terms.entity_indices
     if idx.shape[0] and (idx[:, 0].min() < 0 or idx[:, 0].max() != 0):
         raise NotOnGpuPath("intrinsics index must be 0")
@@ -404,10 +443,13 @@ def _extract_problem(variables, cost_fns):
         for i in fam[2].constant_ids:
             qc[i] = 1
     huber = cf.robust_kernel.delta if cf.robust_kernel is not None else 0.0
-    prob = BAProblem(poses=poses, points=points, intrinsics=np.asarray(cparams, float),
+    prob = BAProblem(poses=poses, points=points, intrinsics=np.asarray(cparams[:4], float),
                      obs_cam=idx[:, 1].astype(np.int32), obs_pt=idx[:, 2].astype(np.int32),
                      obs_uv=terms.uv_in_image, huber_delta=huber, pose_const=pc, point_const=qc)
     prob.intrinsics_free = kinds[0] == VarKind.Free
+    if eucm:
+        prob.camera_model = native.CAMERA_EUCM
+        prob.eucm_alpha_beta = np.asarray(cparams[4:6], float).copy()
     return prob, names
 
 
@@ -423,8 +465,10 @@ def _write_back(variables, names, poses, points, intrinsics=None):
     if intrinsics is not None:
         cf = fams[names[0]]
         cam = cf.members[0]
-        new = PinholeCameraF64(np.asarray(intrinsics, float)) if isinstance(cam, PinholeCameraF64) else \
-            np.asarray(intrinsics, float)
+        if isinstance(cam, (PinholeCameraF64, EnhancedUnifiedCameraF64)):
+            new = type(cam)(np.asarray(intrinsics, float), cam.image_size)
+        else:
+            new = np.asarray(intrinsics, float)
         fams[names[0]] = VarFamily(cf.kind, [new], sorted(cf.constant_ids))
     pf = fams[names[1]]
     if isinstance(pf.members, np.ndarray):

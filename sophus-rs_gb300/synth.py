@@ -71,7 +71,9 @@ class BAProblem:
     points_true: np.ndarray = None
     initial_lm_damping: float = 1e-4
     num_iterations: int = 10
-    intrinsics_free: bool = False  # the pinhole intrinsics are optimised too (a Free camera family)
+    intrinsics_free: bool = False  # the camera params are optimised too (a Free camera family)
+    camera_model: int = 0          # 0 pinhole, 1 enhanced unified camera model (EUCM)
+    eucm_alpha_beta: np.ndarray = None  # (2,) EUCM alpha beta (camera_model 1)
 
     @property
     def n_cam(self):

@@ -143,7 +143,9 @@ def problem_struct(prob):
     s.huber_delta = float(prob.huber_delta or 0.0)
     s.intrinsics_free = 1 if getattr(prob, "intrinsics_free", False) else 0
     s.camera_model = int(getattr(prob, "camera_model", CAMERA_PINHOLE))
-    ab = getattr(prob, "eucm_alpha_beta", (0.0, 0.0))
+    ab = getattr(prob, "eucm_alpha_beta", None)
+    if ab is None:
+        ab = (0.0, 0.0)
     s.eucm_alpha_beta[0] = float(ab[0])
     s.eucm_alpha_beta[1] = float(ab[1])
     # TranslationNormConstraint terms: prob.eq_pose (indices), prob.eq_radius

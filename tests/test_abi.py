@@ -37,7 +37,7 @@ def test_library_exports_every_declared_symbol(pkg):
 
 def test_abi_version_and_error_buffer(pkg):
     L = pkg.native.lib()
-    assert L.sgba_abi_version() == 1
+    assert L.sgba_abi_version() == 2
     buf = ctypes.create_string_buffer(8)
     L.sgba_last_error(buf, 8)  # no error yet or a previous one; must not overflow
     assert len(buf.value) < 8
@@ -91,3 +91,54 @@ def test_rust_ffi_declarations_match_the_header():
     for name, fields in c_structs.items():
         assert name in rust_structs, name
         assert rust_structs[name] == fields, (name, fields, rust_structs[name])
+
+
+# ctypes mirrors in native.py of the header's structs
+_CTYPES_OF = {"sgba_problem_desc": "ProblemDesc", "sgba_opt_params": "OptParamsC", "sgba_iter_record": "IterRecord",
+              "sgba_layout": "Layout", "sgba_problem_options": "ProblemOptions", "sgba_profile": "Profile",
+              "sgba_window_result": "WindowResult", "sgba_linear_solver": "LinearSolverC",
+              "sgba_pcg_stats": "PcgStats", "sgba_pcg_train_params": "PcgTrainParams"}
+
+
+def test_python_struct_layouts_match_the_header(pkg, tmp_path):
+    """sizeof and every field offset of the header's structs, as gcc lays them
+    out, equal the ctypes mirrors'."""
+    import subprocess
+    fields = _c_structs(open(os.path.join(ROOT, "include", "sgba.h")).read())
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "sgba.h"', "int main(void) {"]
+    for cname in _CTYPES_OF:
+        lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f in fields[cname]:
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f, cname, f))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    c = dict(line.split() for line in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                      text=True).stdout.splitlines())
+    for cname, pyname in _CTYPES_OF.items():
+        S = getattr(pkg.native, pyname)
+        assert int(c[cname]) == ctypes.sizeof(S), cname
+        assert [f[0] for f in S._fields_] == fields[cname], cname
+        for f in fields[cname]:
+            assert int(c["%s.%s" % (cname, f)]) == getattr(S, f).offset, (cname, f)
+
+
+def test_camera_options_validated_without_gpu(pkg):
+    """sgba_problem_create_ex rejects bad camera options on the host."""
+    L = pkg.native.lib()
+    h = ctypes.c_void_p()
+    desc = pkg.native.ProblemDesc()
+    for model, ab in ((2, (0.0, 0.0)), (-1, (0.0, 0.0)), (pkg.native.CAMERA_PINHOLE, (0.5, 1.0)),
+                      (pkg.native.CAMERA_EUCM, (float("nan"), 1.0)), (pkg.native.CAMERA_EUCM, (0.5, float("inf")))):
+        o = pkg.native.ProblemOptions()
+        o.camera_model = model
+        o.eucm_alpha_beta[0], o.eucm_alpha_beta[1] = ab
+        assert L.sgba_problem_create_ex(ctypes.byref(desc), ctypes.byref(o), 0, ctypes.byref(h)) == \
+            pkg.native.ERR_INVALID_ARGUMENT, (model, ab)
+        assert not h.value
+    o = pkg.native.ProblemOptions()
+    o.intrinsics_free = 2
+    assert L.sgba_problem_create_ex(ctypes.byref(desc), ctypes.byref(o), 0, ctypes.byref(h)) == \
+        pkg.native.ERR_INVALID_ARGUMENT
