@@ -19,7 +19,9 @@ host buffers: every step uploads the problem, runs the 15-iteration
 optimization and reads the variables back.
 
 --workload sphere / windows measure the other benchmark configurations (the
-100-camera sphere and the 1024 batched local windows) with the same contract.
+100-camera sphere and the 1024 batched local windows) with the same contract;
+--workload eucm the problem of the reference's own BA benchmark (10 cameras
+around an open box, one EUCM camera whose six params are free).
 --impl reference times the CPU restatement of the reference algorithm (the
 oracle) on the host cores on the same workload; that arm maps only the
 oracle's library (which carries its own copy of the scene generator).
@@ -48,6 +50,12 @@ WORKLOADS = {
                          "[-2,2]^3, each seen by U{10..40} of its visible cams (~499k obs), pinhole "
                          "500/500/320/240, Huber 1 px, nu0=1e-4, 20 LM iterations; dense FP32-factor + "
                          "float-float-refined reduced camera system")),
+    "eucm": dict(gen="ring_box_eucm", n_cam=10, n_pt=500, seed=20261203 + 5, n_iter=20,
+                 desc=("the reference's BA benchmark problem (BaProblem::new(10, 500)): 10 SE(3) cams on a r=8 m "
+                       "ring looking at an open box of 500 points (5000 obs), one EUCM camera with its 6 params "
+                       "Free (300/300/320/240/0.5/1.0 true, 297/297/321/241/0.495/1.0 initial), poses 0 and 1 "
+                       "fixed, uniform +-0.075 px noise, no robust kernel, nu0=1.0, 20 LM iterations; one-CTA "
+                       "float-float solver, float-float linearization")),
 }
 DEFAULT_WORKLOAD = "loop"
 N_WINDOWS = 1024
@@ -197,6 +205,14 @@ def _kernel_bytes(name, lay, prob):
     return None
 
 
+def _make_problem(synth, wl, seed, lib_path=None):
+    """The workload's scene from the package's generators (`synth` is the
+    package's synth module or a copy loaded on its own)."""
+    if wl.get("gen") == "ring_box_eucm":
+        return synth.ring_box_eucm(n_cam=wl["n_cam"], n_pt=wl["n_pt"], seed=seed)
+    return synth.generate(wl["kind"], n_cam=wl["n_cam"], n_pt=wl["n_pt"], seed=seed, lib_path=lib_path)
+
+
 def _load_pkg():
     import __graft_entry__ as graft
 
@@ -254,7 +270,7 @@ def run_gpu(args, ws, rank, local):
     pkg = _load_pkg()
     native = pkg.native
     wl = WORKLOADS[args.workload]
-    prob = pkg.synth.generate(wl["kind"], n_cam=wl["n_cam"], n_pt=wl["n_pt"], seed=wl["seed"] + rank)
+    prob = _make_problem(pkg.synth, wl, wl["seed"] + rank)
     K, W = args.steps, args.warmup
     params = _fixed(pkg, W + K + 1000, prob.initial_lm_damping)
     device = local
@@ -287,7 +303,8 @@ def run_gpu(args, ws, rank, local):
     # preconditioner, 50 iterations to 1e-8, the exact factorization as its
     # fallback) on the same workload: device-resident rate and the final cost
     # of the same optimisation, against the plain path
-    out["learned_pcg"] = _learned_pcg(pkg, prob, device, K, W, wl["n_iter"]) if rank == 0 else None
+    out["learned_pcg"] = (_learned_pcg(pkg, prob, device, K, W, wl["n_iter"])
+                          if rank == 0 and not prob.intrinsics_free else None)
     # the LM step against an FP64 LDL^T of the same reduced system, first steps
     # from the workload's start (not timed)
     if rank == 0 and not args.no_cpu_baseline:
@@ -418,15 +435,18 @@ def _oracle():
     return ob
 
 
-def _oracle_generate(kind, n_cam=0, n_pt=0, seed=0):
+def _oracle_generate(kind, n_cam=0, n_pt=0, seed=0, wl=None):
     """A scene from the generator that the oracle library carries (the same
-    source as libsgba_synth.so), loaded without the package."""
+    source as libsgba_synth.so; ring_box_eucm is numpy), loaded without the
+    package."""
     import importlib.util
 
     ob = _oracle()
     spec = importlib.util.spec_from_file_location("sgba_scene_gen", os.path.join(ROOT, "sophus-rs_gb300", "synth.py"))
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
+    if wl is not None:
+        return _make_problem(mod, wl, seed, lib_path=ob.LIB), mod
     return mod.generate(kind, n_cam=n_cam, n_pt=n_pt, seed=seed, lib_path=ob.LIB), mod
 
 
@@ -471,7 +491,7 @@ def run_reference(args):
         print(json.dumps(line))
         return
     wl = WORKLOADS[args.workload]
-    prob, _ = _oracle_generate(wl["kind"], n_cam=wl["n_cam"], n_pt=wl["n_pt"], seed=wl["seed"])
+    prob, _ = _oracle_generate(None, seed=wl["seed"], wl=wl)
     cpu_baseline(prob, 1, threads)  # warm caches / page in
     v, dt = cpu_baseline(prob, args.steps, threads)
     line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
@@ -509,9 +529,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=["loop", "sphere", "windows"],
+    ap.add_argument("--workload", default=DEFAULT_WORKLOAD, choices=["loop", "sphere", "windows", "eucm"],
                     help="loop: the 1500-camera loop (the headline configuration); sphere / windows: the "
-                         "100-camera sphere and the batched local windows")
+                         "100-camera sphere and the batched local windows; eucm: the reference's own BA "
+                         "benchmark problem (EUCM camera, params free)")
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling mode: only set up the workload and run this many LM iterations")
     args = ap.parse_args()
@@ -600,6 +621,9 @@ def main():
             roofline["note"] = ("latency-bound dependency chain: banded float-float LDL^T in one 16-CTA cluster "
                                 "(%d panel steps of 24 pivots), forward/backward sweeps of the same length"
                                 % ((n6 - lay.border_rows + 23) // 24))
+        elif lay.solver == 3:
+            roofline["note"] = ("latency-bound dependency chain: float-float LDL^T of the %d-row reduced system "
+                                "in one CTA, one barrier per pivot" % (n6 + lay.intrinsics_rows))
         else:
             roofline["note"] = ("latency-bound dependency chain (one cluster of 16 CTAs: %d panel steps, then a "
                                 "forward and a backward sweep per solve, one solve plus one or two refinement "

@@ -216,12 +216,23 @@ pub struct Solution {
     pub final_cost: f64,
 }
 
+/// The camera of every observation (`sgba_problem_options::camera_model`):
+/// the pinhole (params fx fy cx cy, `BaProblem::intrinsics`) or the enhanced
+/// unified camera model (EnhancedUnifiedCameraF64, params fx fy cx cy from
+/// `BaProblem::intrinsics`, then alpha beta here).
+#[derive(Debug, Clone, Copy, PartialEq)]
+pub enum Camera {
+    Pinhole,
+    Eucm { alpha: f64, beta: f64 },
+}
+
 /// A device-resident problem (an `sgba_problem` handle); destroyed on drop.
 /// It may move to another thread but is not shared between threads.
 pub struct Problem {
     raw: *mut ffi::sgba_problem,
     n_cam: usize,
     n_pt: usize,
+    n_cam_params: usize,
 }
 
 // SAFETY: a handle is used by one thread at a time (no Sync); the library
@@ -232,6 +243,12 @@ impl Problem {
     /// `sgba_problem_create`: validates and uploads; `device` < 0 keeps the
     /// current CUDA device.
     pub fn new(p: &BaProblem<'_>, device: i32) -> Result<Self, Error> {
+        Self::new_with_camera(p, Camera::Pinhole, false, device)
+    }
+
+    /// `sgba_problem_create_ex`: the camera model, and whether its params
+    /// are a Free family (kinds F, F, M) optimised with the poses.
+    pub fn new_with_camera(p: &BaProblem<'_>, camera: Camera, intrinsics_free: bool, device: i32) -> Result<Self, Error> {
         let n_obs = p.obs_cam.len();
         if p.obs_pt.len() != n_obs || p.obs_uv.len() != n_obs {
             return Err(Error::invalid_argument("observation arrays differ in length"));
@@ -256,11 +273,22 @@ impl Problem {
             obs_uv: p.obs_uv.as_ptr().cast::<f64>(),
             huber_delta: p.huber_delta.unwrap_or(0.0),
         };
+        let (camera_model, eucm_alpha_beta, n_cam_params) = match camera {
+            Camera::Pinhole => (ffi::SGBA_CAMERA_PINHOLE, [0.0, 0.0], 4),
+            Camera::Eucm { alpha, beta } => (ffi::SGBA_CAMERA_EUCM, [alpha, beta], 6),
+        };
+        let opts = ffi::sgba_problem_options {
+            intrinsics_free: i32::from(intrinsics_free),
+            camera_model,
+            eucm_alpha_beta,
+            reserved: [0; 2],
+        };
         let mut raw = core::ptr::null_mut();
         // SAFETY: every pointer in `desc` covers the length it states and
-        // outlives the call (the library copies the data).
-        check(unsafe { ffi::sgba_problem_create(&desc, device, &mut raw) })?;
-        Ok(Self { raw, n_cam: p.poses.len(), n_pt: p.points.len() })
+        // outlives the call (the library copies the data); `opts` is a
+        // complete options struct.
+        check(unsafe { ffi::sgba_problem_create_ex(&desc, &opts, device, &mut raw) })?;
+        Ok(Self { raw, n_cam: p.poses.len(), n_pt: p.points.len(), n_cam_params })
     }
 
     /// `Optimizer::new`: validates the solver configuration, evaluates the
@@ -316,6 +344,15 @@ impl Problem {
         // SAFETY: `self.raw` is a live handle.
         check(unsafe { ffi::sgba_get_cost(self.raw, &mut c) })?;
         Ok(c)
+    }
+
+    /// Current camera params: fx fy cx cy, then alpha beta for the EUCM
+    /// camera (moved by the optimisation when they are free).
+    pub fn intrinsics(&self) -> Result<Vec<f64>, Error> {
+        let mut k = vec![0.0; self.n_cam_params];
+        // SAFETY: `k` holds the 4 or 6 params of this problem's camera model.
+        check(unsafe { ffi::sgba_get_intrinsics(self.raw, k.as_mut_ptr()) })?;
+        Ok(k)
     }
 
     /// Sizes and the solver chosen for the reduced camera system.

@@ -184,3 +184,33 @@ def test_python_mirror_eucm_camera_family(pkg, oracle):
     out = sol.variables.get_members("cams")[0]
     assert isinstance(out, pkg.EnhancedUnifiedCameraF64)
     np.testing.assert_allclose(out.params, ointr, rtol=1e-5)
+
+
+@pytest.mark.parametrize("free", [True, False])
+def test_eucm_reference_benchmark_scene(pkg, oracle, free):
+    """The scene of the reference's BA benchmark (BaProblem::new(10, 500):
+    ring of 10 cameras around an open box, EUCM camera, no robust kernel, 20
+    iterations at damping 1.0, poses 0 and 1 fixed), params Free (ba_bench's
+    "free" rows) or Conditioned at the truth ("conditioned" rows): the
+    per-iteration cost equals the oracle's, and the ba_converges bars hold."""
+    prob = pkg.synth.ring_box_eucm(intrinsics_free=free)
+    if not free:
+        prob.intrinsics = prob.intrinsics_true[:4].copy()
+        prob.eucm_alpha_beta = prob.intrinsics_true[4:].copy()
+    params = pkg.OptParams(num_iterations=20, initial_lm_damping=1.0, function_tolerance=0.0, gradient_tolerance=0.0,
+                           parameter_tolerance=0.0, max_consecutive_rejects=1 << 40)
+    with pkg.native.Problem(prob, device=0) as gp:
+        grecs, _ = gp.optimize(params)
+        poses, points = gp.variables()
+        gintr = gp.intrinsics()
+    orecs, _, _, ointr = oracle.optimize(prob, params, n_threads=8, with_intrinsics=True)
+    g = np.array([r.merit for r in grecs])
+    o = np.array([r.merit for r in orecs])
+    dev = np.abs(g - o) / o
+    pose_rms = np.sqrt(np.mean(np.sum((poses[:, 4:] - prob.poses_true[:, 4:]) ** 2, axis=1)))
+    pt_rms = np.sqrt(np.mean(np.sum((points - prob.points_true) ** 2, axis=1)))
+    print("ring-box EUCM free %d: cost deviation max %.2e, pose RMS %.2e, point RMS %.2e, params %s"
+          % (free, dev.max(), pose_rms, pt_rms, gintr))
+    assert len(g) == len(o) == 20 and dev.max() < COST_RTOL
+    assert pose_rms < 0.01 and pt_rms < 0.1
+    np.testing.assert_allclose(gintr, ointr, rtol=1e-5)

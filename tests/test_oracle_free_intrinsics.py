@@ -269,3 +269,27 @@ def test_covariance_with_an_unobserved_free_pose(pkg, oracle):
             np.testing.assert_allclose(blk, ref[6 * (a - 1):6 * a, 6 * (b - 1):6 * b], rtol=0,
                                        atol=1e-7 * np.abs(ref).max())
     assert np.all(oracle.covariance_block(prob, (1, 2), (1, 2)) == 0.0)
+
+
+def test_ring_box_eucm_scene_converges(pkg, oracle):
+    """The reference's BA benchmark scene (BaProblem::new(10, 500), restated by
+    synth.ring_box_eucm): every camera sees every point of the open box through
+    the wide EUCM camera; with the params free the oracle meets the bars of the
+    reference's ba_converges (pose RMS < 0.01, point RMS < 0.1) in its 20
+    iterations, and with them Conditioned at the truth (ba_bench's
+    "conditioned" rows) as well."""
+    params = pkg.OptParams(num_iterations=20, initial_lm_damping=1.0, function_tolerance=0.0, gradient_tolerance=0.0,
+                           parameter_tolerance=0.0, max_consecutive_rejects=1 << 40)
+    prob = pkg.synth.ring_box_eucm()
+    assert (prob.n_cam, prob.n_pt, prob.n_obs) == (10, 500, 5000)
+    assert prob.huber_delta == 0.0 and list(prob.pose_const[:3]) == [1, 1, 0]
+    cond = prob.copy()
+    cond.intrinsics_free = False
+    cond.intrinsics = prob.intrinsics_true[:4].copy()
+    cond.eucm_alpha_beta = prob.intrinsics_true[4:].copy()
+    for p in (prob, cond):
+        recs, poses, points, intr = oracle.optimize(p, params, with_intrinsics=True)
+        pose_rms = np.sqrt(np.mean(np.sum((poses[:, 4:] - p.poses_true[:, 4:]) ** 2, axis=1)))
+        pt_rms = np.sqrt(np.mean(np.sum((points - p.points_true) ** 2, axis=1)))
+        assert pose_rms < 0.01 and pt_rms < 0.1, (p.intrinsics_free, pose_rms, pt_rms)
+        assert recs[-1].merit < 0.05 * recs[0].merit
