@@ -538,8 +538,8 @@ def main():
     args = ap.parse_args()
     if args.profile_iters > 0:
         pkg = _load_pkg()
-        wl = WORKLOADS["sphere" if args.workload == "sphere" else "loop"]
-        prob = pkg.synth.generate(wl["kind"], n_cam=wl["n_cam"], n_pt=wl["n_pt"], seed=wl["seed"])
+        wl = WORKLOADS[args.workload if args.workload in WORKLOADS else DEFAULT_WORKLOAD]
+        prob = _make_problem(pkg.synth, wl, wl["seed"])
         with pkg.native.Problem(prob, device=0) as gp:
             recs, _ = gp.optimize(_fixed(pkg, args.profile_iters, prob.initial_lm_damping))
         print(json.dumps({"profile_iters": len(recs), "final_merit": recs[-1].merit}))
