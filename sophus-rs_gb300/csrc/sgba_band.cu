@@ -51,7 +51,8 @@ namespace sgba {
 namespace {
 
 constexpr int kBP = 24;          // panel width (4 pose blocks)
-constexpr int kBT = 256;         // threads per CTA
+constexpr int kBT = 256;         // threads per CTA (sweeps, corner)
+constexpr int kFT = 320;         // threads per CTA of the factor: one per position of the 24x24 lower triangle (300)
 constexpr int kMaxWBlocks = 32;  // widest band, in pose blocks
 constexpr int kMaxW = 6 * kMaxWBlocks;
 constexpr int kMaxBorderBlocks = 24;
@@ -204,6 +205,8 @@ struct FactorShared {
   float2 dg[kBP][kBP + 1];   // diagonal block; L below the diagonal after the factor
   float2 xi[kBP][kBP + 1];   // inverse of the unit lower factor
   float2 sd[kBP], srd[kBP];  // pivots and their reciprocals
+  float2 cols[kBP][kBP];     // cols[t][i]: column t of the diagonal block once final (before pivot t)
+  float2 xs[kBP][kBP];       // xs[t][q]: row t of X once final (q < t)
   float2 arow[kMaxOwnRows][kBP];
   const float2* dsrc[kBP];   // diagonal-block rows: their slots in the owners' shared memory
   const float4* psrc[kMaxW]; // L D rows of the panel in their owners' shared memory
@@ -224,7 +227,7 @@ struct FactorShared {
 // panel and publishes L D of them; after a cluster barrier every CTA gathers
 // the panel's L D (DSMEM) and updates its own rows in place.
 template <int C>
-__global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) {
+__global__ void __launch_bounds__(kFT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) {
   // Every CTA reads the control block before the first cluster barrier and
   // only CTA 0 writes it, after the last one: the early return is uniform.
   if (skipping(ctrl)) return;
@@ -246,7 +249,7 @@ __global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) 
     if (hi > loaded) {
       const int r0 = loaded + ((rank - loaded % C) + C) % C;
       const int nr = (r0 < hi) ? (hi - r0 + C - 1) / C : 0;
-      for (int e = tid; e < nr * W; e += kBT) {
+      for (int e = tid; e < nr * W; e += kFT) {
         const int r = r0 + (e / W) * C, k = e % W;
         cp_async8(rows + slot(r) * W + k, a.Lb + static_cast<int64_t>(r) * W + k);
       }
@@ -255,13 +258,15 @@ __global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) 
     cp_async_commit();
   };
   if (tid == 0) sh.bad = 0;
-  // the entries of the 24x24 block this thread updates
-  int fi[3], fq[3];
-#pragma unroll
-  for (int u3 = 0; u3 < 3; ++u3) {
-    const int e = tid + u3 * kBT;
-    fi[u3] = (e < kBP * kBP) ? e / kBP : kBP;  // kBP: no entry
-    fq[u3] = (e < kBP * kBP) ? e % kBP : 0;
+  // the position (i, q), q <= i, of the 24x24 diagonal block this thread
+  // owns through the factor: thread e < 300 takes entry e of the lower
+  // triangle (row-major); fi = kBP: no position
+  int fi = kBP, fq = 0;
+  if (tid < kBP * (kBP + 1) / 2) {
+    int i = 0;
+    while ((i + 1) * (i + 2) / 2 <= tid) ++i;
+    fi = i;
+    fq = tid - i * (i + 1) / 2;
   }
   prefetch(W + 3 * kBP);
   for (int p = 0; p < a.npan; ++p) {
@@ -297,7 +302,7 @@ __global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) 
     __syncthreads();
     cl.sync();  // the previous panel's update of rows >= c0 is complete in every CTA
     // (1) diagonal block from its owners, identity for its inverse
-    for (int e = tid; e < kBP * kBP; e += kBT) {
+    for (int e = tid; e < kBP * kBP; e += kFT) {
       const int i = e / kBP, k = e % kBP;
       float2 v = make_float2(0.0f, 0.0f);
       if (i < w && k <= i && (k - i + W - 1) >= 0) v = sh.dsrc[i][k - i + W - 1];
@@ -306,66 +311,67 @@ __global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) 
     }
     __syncthreads();
     // (2) LDL^T of the diagonal block, X <- L^-1 alongside (the elementary
-    // column eliminations applied to the identity).  Every thread evaluates
-    // the pivot itself (same inputs, same operations: the same value in every
-    // thread), so each pivot costs one barrier.  Column t is final after pivot
-    // t (later pivots touch columns > t only); it is scaled to L on output.
+    // column eliminations applied to the identity).  Each thread keeps the
+    // entry of its position in registers: a_iq while q > t (the trailing
+    // update a_iq -= l_it a_qt, l_it = a_it / d_t), then X_iq (X_iq -= l_it
+    // X_tq, q <= t), so every pivot is one update per thread.  An entry goes to
+    // shared memory once, when it becomes final: column t + 1 of A into
+    // cols[t + 1], row t + 1 of X into xs[t + 1]; pivot t reads only those.
+    // Every thread evaluates the pivot itself (same inputs, same operations:
+    // the same value in every thread), so each pivot costs one barrier; the
+    // update is branch-free (both operands loaded, one selected).
     {
-      float maxp = 1.0f;
+      dd areg = dd_make(0.0f, 0.0f), xreg = dd_make(0.0f, 0.0f);
+      const int ic = fi < kBP ? fi : 0;
+      if (fi < w) {
+        areg = f2dd(sh.dg[fi][fq]);
+        if (fq == 0) sh.cols[0][fi] = sh.dg[fi][0];
+      }
+      __syncthreads();
+      float maxp = 1.0f;  // running maximum pivot of the 6x6 pose block (>= 1)
       for (int t = 0; t < w; ++t) {
-        dd dt = f2dd(sh.dg[t][t]);
+        dd dt = f2dd(sh.cols[t][t]);
         if ((c0 + t) % 6 == 0) maxp = 1.0f;
-        const float tol = fmaxf(maxp, 1.0f) * kTolRel;
-        if (!isfinite(dt.hi)) {
-          if (tid == 0) sh.bad = 1;
-          dt = dd_make(0.0f, 0.0f);
-        } else if (fabsf(dt.hi) <= tol) {
-          dt = dd_make(0.0f, 0.0f);
-        } else {
-          maxp = fmaxf(maxp, fabsf(dt.hi));
-        }
-        const dd rd = (dt.hi == 0.0f) ? dd_make(0.0f, 0.0f) : dd_rcp(dt);
+        // the pivot rule: a pivot that is not finite, or not above 1e-12 of
+        // the running maximum (at least 1), is zero; branch-free
+        const float ad = fabsf(dt.hi);
+        const bool fin = ad <= 3.402823466e38f;
+        const bool zero = !fin || !(ad > maxp * kTolRel);
+        if (!fin && tid == 0) sh.bad = 1;
+        maxp = zero ? maxp : fmaxf(maxp, ad);
+        const dd r = dd_rcp(dt);
+        dt = zero ? dd_make(0.0f, 0.0f) : dt;
+        const dd rd = zero ? dd_make(0.0f, 0.0f) : r;
         if (tid == 0) {
           sh.sd[t] = dd2f(dt);
           sh.srd[t] = dd2f(rd);
         }
-        // all loads of this thread's (up to) three entries first, then the
-        // arithmetic, then the stores: the three chains overlap
-        float2 va[3], vb[3], vc[3];
-        bool act[3];
-        float2* dst[3];
-#pragma unroll
-        for (int u3 = 0; u3 < 3; ++u3) {
-          const int i = fi[u3], q = fq[u3];
-          act[u3] = (i > t && i < w) && (q <= t || q <= i);
-          const int ii = act[u3] ? i : 0;
-          va[u3] = sh.dg[ii][t];
-          if (q > t) {  // trailing: a_iq -= l_it a_qt
-            dst[u3] = &sh.dg[ii][q];
-            vc[u3] = sh.dg[q < kBP ? q : 0][t];
-          } else {      // X_iq -= l_it X_tq, q <= t
-            dst[u3] = &sh.xi[ii][q];
-            vc[u3] = sh.xi[t][q];
-          }
-          vb[u3] = *dst[u3];
-        }
-        dd res[3];
-#pragma unroll
-        for (int u3 = 0; u3 < 3; ++u3) {
-          const dd li = dd_mul(f2dd(va[u3]), rd);
-          Acc acc = acc_init(f2dd(vb[u3]));
-          acc_madd(acc, dd_neg(li), f2dd(vc[u3]));
-          res[u3] = acc_get(acc);
-        }
-#pragma unroll
-        for (int u3 = 0; u3 < 3; ++u3)
-          if (act[u3]) *dst[u3] = dd2f(res[u3]);
+        const bool act = (fi > t) && (fi < w);
+        const bool isA = fq > t;
+        const float2 va = sh.cols[t][ic];
+        const float2 ca = sh.cols[t][fq];
+        const float2 cx = (fq == t) ? make_float2(1.0f, 0.0f) : sh.xs[t][fq];
+        const dd li = dd_mul(f2dd(va), rd);
+        Acc acc = acc_init(isA ? areg : xreg);
+        acc_madd(acc, dd_neg(li), f2dd(isA ? ca : cx));
+        const dd nv = acc_get(acc);
+        if (act && isA) areg = nv;
+        if (act && !isA) xreg = nv;
+        if (act && isA && fq == t + 1) sh.cols[t + 1][fi] = dd2f(nv);
+        if (act && !isA && fi == t + 1) sh.xs[t + 1][fq] = dd2f(nv);
         __syncthreads();
       }
+      // the block's outputs: below the diagonal u = a_iq as of pivot q - 1
+      // (L = u / d on output) and X; the diagonal of xi keeps the identity
+      if (fi < w && fq < fi) {
+        sh.dg[fi][fq] = dd2f(areg);
+        sh.xi[fi][fq] = dd2f(xreg);
+      }
+      __syncthreads();
     }
     // (3) outputs: X and pivots (spread over the CTAs); the own rows of this
     // panel are final: write them back
-    for (int e = rank * kBT + tid; e < kBP * kBP; e += C * kBT)
+    for (int e = rank * kFT + tid; e < kBP * kBP; e += C * kFT)
       a.Xinv[static_cast<int64_t>(p) * kBP * kBP + e] = sh.xi[e / kBP][e % kBP];
     if (rank == C - 1 && tid < w) {
       a.dpiv[c0 + tid] = sh.sd[tid];
@@ -374,7 +380,7 @@ __global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) 
     {
       const int d0 = c0 + ((rank - c0 % C) + C) % C;
       const int nd = (d0 < c1) ? (c1 - d0 + C - 1) / C : 0;
-      for (int e = tid; e < nd * W; e += kBT) {
+      for (int e = tid; e < nd * W; e += kFT) {
         const int r = d0 + (e / W) * C, k = e % W;
         const int c = r - W + 1 + k;
         float2 v = make_float2(0.0f, 0.0f);
@@ -389,7 +395,7 @@ __global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) 
       }
     }
     // (4) own rows of the panel: L_rk = (sum_{j<=k} a_rj X_kj) / d_k
-    for (int e = tid; e < nown * kBP; e += kBT) {
+    for (int e = tid; e < nown * kBP; e += kFT) {
       const int ri = e / kBP, j = e % kBP;
       const int r = rfirst + ri * C;
       float2 v = make_float2(0.0f, 0.0f);
@@ -397,7 +403,7 @@ __global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) 
       sh.arow[ri][j] = v;
     }
     __syncthreads();
-    for (int e = tid; e < nown * kBP; e += kBT) {
+    for (int e = tid; e < nown * kBP; e += kFT) {
       const int ri = e / kBP, k = e % kBP;
       const int r = rfirst + ri * C;
       dd l = dd_make(0.0f, 0.0f);
@@ -416,16 +422,16 @@ __global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) 
     {
       constexpr int kQ = kBP / 2;
       const int nq = nrows * kQ;
-      for (int e0 = tid; e0 < nq; e0 += 8 * kBT) {
+      for (int e0 = tid; e0 < nq; e0 += 8 * kFT) {
         float4 v4[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          const int e = e0 + u * kBT;
+          const int e = e0 + u * kFT;
           if (e < nq) v4[u] = sh.psrc[e / kQ][e % kQ];
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          const int e = e0 + u * kBT;
+          const int e = e0 + u * kFT;
           if (e < nq) {
             const int q = e / kQ, k2 = e % kQ;
             pb[q * (kBP + 1) + 2 * k2] = make_float2(v4[u].x, v4[u].y);
@@ -438,7 +444,7 @@ __global__ void __launch_bounds__(kBT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) 
     // (6) trailing update of the own rows: a_rc -= sum_k L_rk d_k L_ck, c in [max(c1, r-W+1), r]
     const int total = sh.pre[nown];
     int ri = 0;  // e only grows: the row search carries over
-    for (int e = tid; e < total; e += kBT) {
+    for (int e = tid; e < total; e += kFT) {
       while (ri + 1 < nown && sh.pre[ri + 1] <= e) ++ri;
       const int r = rfirst + ri * C;
       const int c = max(c1, r - W + 1) + (e - sh.pre[ri]);
@@ -879,7 +885,7 @@ int band_setup(int n, int nband, int W, int* cluster, int* ring) {
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(C);
-    cfg.blockDim = dim3(kBT);
+    cfg.blockDim = dim3(kFT);
     cfg.dynamicSmemBytes = factor_dyn_smem(W, C);
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -918,7 +924,7 @@ int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
   {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(s.band_c);
-    cfg.blockDim = dim3(kBT);
+    cfg.blockDim = dim3(kFT);
     cfg.dynamicSmemBytes = factor_dyn_smem(a.W, s.band_c);
     cfg.stream = st;
     cudaLaunchAttribute at[1];
