@@ -52,13 +52,13 @@ namespace {
 
 constexpr int kBP = 24;          // panel width (4 pose blocks)
 constexpr int kBT = 256;         // threads per CTA (sweeps, corner)
+constexpr int kCT = 1024;        // threads of the corner solve (one CTA; more warps hide its per-pivot chains)
 constexpr int kFT = 320;         // threads per CTA of the factor: one per position of the 24x24 lower triangle (300)
 constexpr int kMaxWBlocks = 32;  // widest band, in pose blocks
 constexpr int kMaxW = 6 * kMaxWBlocks;
 constexpr int kMaxBorderBlocks = 24;
 constexpr int kMaxBorder = 6 * kMaxBorderBlocks;
 constexpr int kMaxOwnRows = (kMaxW - 1 + 7) / 8;  // rows of one CTA in a window (cluster >= 8)
-constexpr int kFwdSeg = 10;      // dot-product segments per panel row in the sweeps
 constexpr float kTolRel = 1e-12f;
 constexpr size_t kSmemLimit = 227 * 1024;
 
@@ -484,16 +484,31 @@ __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
 }
 
+// Sum of a float-float value over the kSweepG consecutive lanes of a group
+// (butterfly over the group; every lane of the warp takes part).  Lane g = 0
+// of the group holds the total; the order is fixed.
+constexpr int kSweepG = 8;  // threads per row of a panel in the sweeps (24 rows: 192 threads)
+__device__ __forceinline__ dd group_sum(dd s) {
+#pragma unroll
+  for (int o = kSweepG / 2; o >= 1; o >>= 1) {
+    const float h = __shfl_xor_sync(0xffffffffu, s.hi, o);
+    const float l = __shfl_xor_sync(0xffffffffu, s.lo, o);
+    Acc acc = acc_init(s);
+    acc_add(acc, dd_make(h, l));
+    s = acc_get(acc);
+  }
+  return s;
+}
+
 // One CTA per row of Zc (border rows of C and the right-hand side):
 // z = L_A^-1 c, then Zd = D_A^-1 z.
 __global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   extern __shared__ __align__(16) float2 sw[];
-  const int W = a.W, span = W - 1;
+  const int W = a.W;
   float2* v = sw;
   float2* blk = v + ((a.nband + 1) & ~1);  // 2 x kBP x W (16-byte aligned: W is even)
   float2* xb = blk + 2 * kBP * W;          // 2 x kBP x kBP
-  __shared__ float2 part[kBP][kFwdSeg];
   __shared__ float2 u[kBP];
   const int tid = threadIdx.x;
   const int row = blockIdx.x;
@@ -513,7 +528,8 @@ __global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a, const Ctrl* ctrl) 
   };
   for (int c = tid; c < a.nband; c += kBT) v[c] = zrow[c];
   stage(0);
-  const int seg = (span + kFwdSeg - 1) / kFwdSeg;
+  // a group of kSweepG threads per row of the panel (warps 0..5)
+  const int cl = tid / kSweepG, g = tid % kSweepG;
   for (int p = 0; p < a.npan; ++p) {
     const int c0 = kBP * p;
     const int w = min(kBP, a.nband - c0);
@@ -522,30 +538,38 @@ __global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a, const Ctrl* ctrl) 
     else cp_async_commit();
     cp_async_wait_but_one();
     __syncthreads();
-    if (tid < kBP * kFwdSeg) {
-      const int cl = tid / kFwdSeg, sgi = tid % kFwdSeg;
-      Acc acc = acc_init(dd_make(0.0f, 0.0f));
+    if (tid < kBP * kSweepG) {
+      // u_c = v_c - sum_{j < c0} L_cj v_j: the group's lanes take every
+      // kSweepG-th column, two accumulators each
+      Acc a0 = acc_init(dd_make(0.0f, 0.0f)), a1 = acc_init(dd_make(0.0f, 0.0f));
       if (cl < w) {
         const int c = c0 + cl;
-        const int jlo = max(max(0, c - W + 1), c0 - span + sgi * seg);
-        const int jhi = min(c0, c0 - span + (sgi + 1) * seg);
         const float2* lrow = blk + (buf * kBP + cl) * W + (W - 1 - c);
-        for (int j = jlo; j < jhi; ++j) acc_madd(acc, f2dd(lrow[j]), f2dd(v[j]));
+        int j = max(0, c - W + 1) + g;
+        for (; j + kSweepG < c0; j += 2 * kSweepG) {
+          acc_madd(a0, f2dd(lrow[j]), f2dd(v[j]));
+          acc_madd(a1, f2dd(lrow[j + kSweepG]), f2dd(v[j + kSweepG]));
+        }
+        if (j < c0) acc_madd(a0, f2dd(lrow[j]), f2dd(v[j]));
       }
-      part[cl][sgi] = dd2f(acc_get(acc));
+      acc_add(a0, acc_get(a1));
+      const dd sm = group_sum(acc_get(a0));
+      if (g == 0 && cl < w) {
+        Acc acc = acc_init(f2dd(v[c0 + cl]));
+        acc_add(acc, dd_neg(sm));
+        u[cl] = dd2f(acc_get(acc));
+      }
     }
     __syncthreads();
-    if (tid < w) {
-      Acc acc = acc_init(f2dd(v[c0 + tid]));
-      for (int q = 0; q < kFwdSeg; ++q) acc_add(acc, dd_neg(f2dd(part[tid][q])));
-      u[tid] = dd2f(acc_get(acc));
-    }
-    __syncthreads();
-    if (tid < w) {
-      const float2* xr = xb + buf * kBP * kBP + tid * kBP;
+    if (tid < kBP * kSweepG) {
+      // v_{c0+cl} = sum_{j <= cl} X_cl,j u_j (X = L_pp^-1, unit lower)
       Acc acc = acc_init(dd_make(0.0f, 0.0f));
-      for (int j = 0; j <= tid; ++j) acc_madd(acc, f2dd(xr[j]), f2dd(u[j]));
-      v[c0 + tid] = dd2f(acc_get(acc));
+      if (cl < w) {
+        const float2* xr = xb + buf * kBP * kBP + cl * kBP;
+        for (int j = g; j <= cl; j += kSweepG) acc_madd(acc, f2dd(xr[j]), f2dd(u[j]));
+      }
+      const dd sm = group_sum(acc_get(acc));
+      if (g == 0 && cl < w) v[c0 + cl] = dd2f(sm);
     }
     __syncthreads();
   }
@@ -610,7 +634,7 @@ __global__ void __launch_bounds__(128) k_band_corner(BandArgs a, const Ctrl* ctr
 // Every thread evaluates each pivot itself (same inputs, same operations), so
 // a pivot costs one barrier; column t is scaled to L after the factorization
 // (later pivots do not touch it).
-__global__ void __launch_bounds__(kBT) k_band_corner_solve(BandArgs a, Ctrl* ctrl) {
+__global__ void __launch_bounds__(kCT) k_band_corner_solve(BandArgs a, Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   extern __shared__ __align__(16) float2 cm[];  // nbd x nbd (lower), then y (nbd), then 1/d (nbd)
   __shared__ int sbad;
@@ -620,11 +644,11 @@ __global__ void __launch_bounds__(kBT) k_band_corner_solve(BandArgs a, Ctrl* ctr
   float2* y = cm + m * m;
   float2* rdv = y + m;
   const int64_t ld = m + 1;
-  for (int e = tid; e < m * m; e += kBT) {
+  for (int e = tid; e < m * m; e += kCT) {
     const int i = e / m, j = e % m;
     cm[e] = (j <= i) ? a.Cn[i * ld + j] : make_float2(0.0f, 0.0f);
   }
-  for (int j = tid; j < m; j += kBT) y[j] = a.Cn[static_cast<int64_t>(m) * ld + j];
+  for (int j = tid; j < m; j += kCT) y[j] = a.Cn[static_cast<int64_t>(m) * ld + j];
   if (tid == 0) sbad = 0;
   __syncthreads();
   float maxp = 1.0f;
@@ -651,7 +675,7 @@ __global__ void __launch_bounds__(kBT) k_band_corner_solve(BandArgs a, Ctrl* ctr
     const int rem = m - t - 1;
     const int ntri = rem * (rem + 1) / 2;
     const dd yt = f2dd(y[t]);
-    for (int e = tid; e < ntri + rem; e += kBT) {
+    for (int e = tid; e < ntri + rem; e += kCT) {
       if (e < ntri) {  // trailing (i, k), t < k <= i: a_ik -= a_it rd a_kt
         int ii = static_cast<int>((__fsqrt_rn(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
         while (ii * (ii + 1) / 2 > e) --ii;
@@ -671,22 +695,22 @@ __global__ void __launch_bounds__(kBT) k_band_corner_solve(BandArgs a, Ctrl* ctr
     }
     __syncthreads();
   }
-  for (int e = tid; e < m * m; e += kBT) {
+  for (int e = tid; e < m * m; e += kCT) {
     const int i = e / m, t = e % m;
     if (t < i) cm[e] = dd2f(dd_mul(f2dd(cm[e]), f2dd(rdv[t])));
   }
-  for (int i = tid; i < m; i += kBT) y[i] = dd2f(dd_mul(f2dd(y[i]), f2dd(rdv[i])));
+  for (int i = tid; i < m; i += kCT) y[i] = dd2f(dd_mul(f2dd(y[i]), f2dd(rdv[i])));
   __syncthreads();
   for (int t = m - 1; t > 0; --t) {  // x_t final: x_i -= L_ti x_t for i < t
     const dd xt = f2dd(y[t]);
-    for (int i = tid; i < t; i += kBT) {
+    for (int i = tid; i < t; i += kCT) {
       Acc acc = acc_init(f2dd(y[i]));
       acc_madd(acc, dd_neg(f2dd(cm[t * m + i])), xt);
       y[i] = dd2f(acc_get(acc));
     }
     __syncthreads();
   }
-  for (int i = tid; i < m; i += kBT) a.xw[a.nband + i] = y[i];
+  for (int i = tid; i < m; i += kCT) a.xw[a.nband + i] = y[i];
   if (tid == 0 && sbad) ctrl->skip = 2;
 }
 
@@ -709,7 +733,6 @@ __global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a, const Ctrl* ctrl) 
   float2* xv = sw;
   float2* blk = xv + ((a.nband + 1) & ~1);  // 2 x span x kBP: rows below the panel, the panel's columns
   float2* xb = blk + 2 * kBP * W;           // 2 x kBP x kBP
-  __shared__ float2 part[kBP][kFwdSeg];
   __shared__ float2 u[kBP];
   const int tid = threadIdx.x;
   auto stage = [&](int p) {
@@ -729,7 +752,8 @@ __global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a, const Ctrl* ctrl) 
   };
   for (int c = tid; c < a.nband; c += kBT) xv[c] = a.xw[c];
   stage(a.npan - 1);
-  const int seg = (span + kFwdSeg - 1) / kFwdSeg;
+  // a group of kSweepG threads per column of the panel (warps 0..5)
+  const int cl = tid / kSweepG, g = tid % kSweepG;
   for (int p = a.npan - 1; p >= 0; --p) {
     const int c0 = kBP * p;
     const int w = min(kBP, a.nband - c0);
@@ -739,32 +763,39 @@ __global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a, const Ctrl* ctrl) 
     else cp_async_commit();
     cp_async_wait_but_one();
     __syncthreads();
-    if (tid < kBP * kFwdSeg) {
-      const int cl = tid / kFwdSeg, sgi = tid % kFwdSeg;
-      Acc acc = acc_init(dd_make(0.0f, 0.0f));
+    if (tid < kBP * kSweepG) {
+      // u_c = x_c - sum_r L_rc x_r, rows r in [c1, min(c + W, nband)): the
+      // group's lanes take every kSweepG-th row, two accumulators each
+      Acc a0 = acc_init(dd_make(0.0f, 0.0f)), a1 = acc_init(dd_make(0.0f, 0.0f));
       if (cl < w) {
         const int c = c0 + cl;
-        // rows r in [c1, min(c + W, nband)), split over the fixed window [c1, c1 + span)
-        const int rlo = c1 + sgi * seg;
-        const int rhi = min(min(c + W, a.nband), c1 + (sgi + 1) * seg);
-        for (int r = rlo; r < rhi; ++r)
-          acc_madd(acc, f2dd(blk[(buf * span + (r - c1)) * kBP + cl]), f2dd(xv[r]));
+        const int rhi = min(c + W, a.nband);
+        const float2* col = blk + buf * span * kBP + cl;  // row r at col[(r - c1) * kBP]
+        int r = c1 + g;
+        for (; r + kSweepG < rhi; r += 2 * kSweepG) {
+          acc_madd(a0, f2dd(col[(r - c1) * kBP]), f2dd(xv[r]));
+          acc_madd(a1, f2dd(col[(r + kSweepG - c1) * kBP]), f2dd(xv[r + kSweepG]));
+        }
+        if (r < rhi) acc_madd(a0, f2dd(col[(r - c1) * kBP]), f2dd(xv[r]));
       }
-      part[cl][sgi] = dd2f(acc_get(acc));
+      acc_add(a0, acc_get(a1));
+      const dd sm = group_sum(acc_get(a0));
+      if (g == 0 && cl < w) {
+        Acc acc = acc_init(f2dd(xv[c0 + cl]));
+        acc_add(acc, dd_neg(sm));
+        u[cl] = dd2f(acc_get(acc));
+      }
     }
     __syncthreads();
-    if (tid < w) {
-      Acc acc = acc_init(f2dd(xv[c0 + tid]));
-      for (int q = 0; q < kFwdSeg; ++q) acc_add(acc, dd_neg(f2dd(part[tid][q])));
-      u[tid] = dd2f(acc_get(acc));
-    }
-    __syncthreads();
-    if (tid < w) {
+    if (tid < kBP * kSweepG) {
       // x_{c0+k} = sum_{i >= k} X_ik u_i
-      const float2* x2 = xb + buf * kBP * kBP;
       Acc acc = acc_init(dd_make(0.0f, 0.0f));
-      for (int i = tid; i < w; ++i) acc_madd(acc, f2dd(x2[i * kBP + tid]), f2dd(u[i]));
-      xv[c0 + tid] = dd2f(acc_get(acc));
+      if (cl < w) {
+        const float2* x2 = xb + buf * kBP * kBP;
+        for (int i = cl + g; i < w; i += kSweepG) acc_madd(acc, f2dd(x2[i * kBP + cl]), f2dd(u[i]));
+      }
+      const dd sm = group_sum(acc_get(acc));
+      if (g == 0 && cl < w) xv[c0 + cl] = dd2f(sm);
     }
     __syncthreads();
   }
@@ -948,7 +979,7 @@ int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
   }
   {
     const size_t corner = sizeof(float2) * static_cast<size_t>(a.nbd) * (a.nbd + 2);
-    k_band_corner_solve<<<1, kBT, std::max<size_t>(corner, 16), st>>>(a, d.ctrl);
+    k_band_corner_solve<<<1, kCT, std::max<size_t>(corner, 16), st>>>(a, d.ctrl);
     ++launches;
   }
   k_band_tvec<<<std::max((a.nband + 255) / 256, 1), 256, 0, st>>>(a, d.ctrl);
