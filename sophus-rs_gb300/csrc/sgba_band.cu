@@ -29,6 +29,7 @@
 //                     rows dealt round-robin over the CTAs; per panel every CTA factors the 24x24
 //                     diagonal block (and the inverse of its unit lower factor) redundantly, solves
 //                     its own rows of the panel, then updates its own rows of the trailing band
+//   k_band_sweepmat   per panel, the sweep matrices X_p L_p and X_p^T L_b^T (one CTA per panel)
 //   k_band_fwd        one CTA per border row and one for the right-hand side: z = L_A^-1 c
 //   k_band_corner     E - Z D_A^-1 Z^T (one warp per entry; the right-hand side row gives y_C)
 //   k_band_corner_solve  LDL^T of the corner and its solve
@@ -125,11 +126,14 @@ struct BandArgs {
   int npan;   // 24-column panels of A
   int nbd;    // border rows (n - nband)
   int ring;   // row slots per CTA in the factor kernel
+  int nbuf;   // panel buffers of the sweeps (2 or 3)
   const double* S;  // n x n, both triangles
   const double* b;  // reduced right-hand side
   float* scl;       // n: D^-1/2
   float2* Lb;       // nband x W: scaled A, then L_A below the diagonal
   float2* Xinv;     // npan x 24 x 24: inverse of the unit lower diagonal block of each panel
+  float2* Mf;       // npan x 24 x W: X_p L_p (the panel's rows, columns c0 - W + 1 .. c0 - 1), forward sweep
+  float2* Mb;       // npan x 24 x W: X_p^T L^T (rows c1 .. c1 + W - 2 below the panel), backward sweep
   float2* dpiv;     // n: pivots
   float2* rdpiv;    // n: 1 / pivot (0 for a zero pivot)
   float2* Pbuf;     // (W - 1) x 24: L D of the current panel, rows below it
@@ -472,11 +476,12 @@ __global__ void __launch_bounds__(kFT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) 
 
 // ------------------------------------------------ forward substitution ----
 
-// Shared memory of the sweeps: the vector (nband), then two buffers of the
-// panel's L entries (kBP x (W - 1)) and two of its X (kBP x kBP).  Each panel's
-// entries are copied with cp.async while the previous panel is computed.
-__host__ __device__ inline size_t sweep_smem_floats2(int nband, int W) {
-  return static_cast<size_t>(nband) + 1 + 2 * static_cast<size_t>(kBP) * W + 2 * kBP * kBP;
+// Shared memory of the sweeps: the vector (nband), then nbuf buffers of the
+// panel's M (kBP x W), nbuf of its X (kBP x kBP) and nbuf of its 24 input
+// values.  The entries of the next nbuf - 1 panels are copied with cp.async
+// while a panel is computed (three buffers where they fit, else two).
+__host__ __device__ inline size_t sweep_smem_floats2(int nband, int W, int nbuf) {
+  return static_cast<size_t>(nband) + 1 + static_cast<size_t>(nbuf) * (static_cast<size_t>(kBP) * W + kBP * kBP + kBP);
 }
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
@@ -500,80 +505,135 @@ __device__ __forceinline__ dd group_sum(dd s) {
   return s;
 }
 
+// The sweep matrices of every panel (one CTA per panel, after the factor):
+//   forward:  z_p = X_p (c_p - L_p z_prev) = X_p c_p - Mf_p z_prev,  Mf_p = X_p L_p
+//             (L_p the panel's rows over the W - 1 columns before it);
+//   backward: x_p = X_p^T (t_p - L_b^T x_below) = X_p^T t_p - Mb_p x_below,
+//             Mb_p = X_p^T L_b^T (L_b the W - 1 rows below the panel over its columns).
+// Each sweep step is then one dot product per row of the panel.
+__global__ void __launch_bounds__(kBT) k_band_sweepmat(BandArgs a, const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  extern __shared__ __align__(16) float2 smx[];
+  const int W = a.W, span = W - 1;
+  const int p = blockIdx.x;
+  const int c0 = kBP * p, w = min(kBP, a.nband - c0), c1 = c0 + w;
+  const int tid = threadIdx.x;
+  float2* Lp = smx;             // kBP x W: the panel's rows, slots as in Lb
+  float2* Lq = Lp + kBP * W;    // span x kBP: the rows below, the panel's columns
+  float2* X = Lq + span * kBP;  // kBP x kBP
+  for (int e = tid; e < kBP * W; e += kBT) {
+    const int i = e / W, sl = e % W;
+    Lp[e] = (i < w) ? a.Lb[static_cast<int64_t>(c0 + i) * W + sl] : make_float2(0.0f, 0.0f);
+  }
+  for (int e = tid; e < span * kBP; e += kBT) {
+    const int q = e / kBP, k = e % kBP;
+    const int r = c1 + q, sl = c0 + k - r + W - 1;
+    Lq[e] = (r < a.nband && k < w && sl >= 0) ? a.Lb[static_cast<int64_t>(r) * W + sl] : make_float2(0.0f, 0.0f);
+  }
+  for (int e = tid; e < kBP * kBP; e += kBT) X[e] = a.Xinv[static_cast<int64_t>(p) * kBP * kBP + e];
+  __syncthreads();
+  float2* mf = a.Mf + static_cast<int64_t>(p) * kBP * W;
+  float2* mb = a.Mb + static_cast<int64_t>(p) * kBP * W;
+  for (int e = tid; e < 2 * kBP * W; e += kBT) {
+    const int half = e / (kBP * W), e1 = e % (kBP * W);
+    const int k = e1 / W, s2 = e1 % W;
+    Acc acc = acc_init(dd_make(0.0f, 0.0f));
+    if (half == 0) {
+      // Mf[k][s] = sum_{k' <= min(k, s)} X[k][k'] L[c0 + k'][col], col = c0 - W + 1 + s (slot s - k')
+      if (k < w && s2 < span)
+        for (int kk = 0; kk <= k && kk <= s2; ++kk) acc_madd(acc, f2dd(X[k * kBP + kk]), f2dd(Lp[kk * W + s2 - kk]));
+      mf[e1] = dd2f(acc_get(acc));
+    } else {
+      // Mb[k][q] = sum_{i = k}^{w - 1} X[i][k] L[c1 + q][c0 + i]
+      if (k < w && s2 < span)
+        for (int i = k; i < w; ++i) acc_madd(acc, f2dd(X[i * kBP + k]), f2dd(Lq[s2 * kBP + i]));
+      mb[e1] = dd2f(acc_get(acc));
+    }
+  }
+}
+
 // One CTA per row of Zc (border rows of C and the right-hand side):
-// z = L_A^-1 c, then Zd = D_A^-1 z.
+// z = L_A^-1 c, then Zd = D_A^-1 z.  Per panel, one dot per row: for row k of
+// the panel z_k = sum_{k' <= k} X_kk' c_k' - sum_s Mf_ks z_(c0 - W + 1 + s),
+// a group of kSweepG threads per row (warps 0..5).  The panel's inputs c come
+// from the unchanged Zc row (staged with the panel), so the outputs can go
+// straight into the vector; one barrier per panel.
 __global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   extern __shared__ __align__(16) float2 sw[];
   const int W = a.W;
+  const int nb = a.nbuf;
   float2* v = sw;
-  float2* blk = v + ((a.nband + 1) & ~1);  // 2 x kBP x W (16-byte aligned: W is even)
-  float2* xb = blk + 2 * kBP * W;          // 2 x kBP x kBP
-  __shared__ float2 u[kBP];
+  float2* mbuf = v + ((a.nband + 1) & ~1);  // nb x kBP x W (16-byte aligned: W is even)
+  float2* xb = mbuf + nb * kBP * W;         // nb x kBP x kBP
+  float2* cb = xb + nb * kBP * kBP;         // nb x kBP
   const int tid = threadIdx.x;
   const int row = blockIdx.x;
   float2* zrow = a.Zc + static_cast<int64_t>(row) * a.nband;
-  // row c of panel p: slots [0, span) of Lb row c are the columns [c - W + 1, c);
-  // whole rows are copied (W float2, 16-byte pieces)
+  const int h = W / 2;
+  const int i0 = tid / h, q0 = tid % h, di = kBT / h, dq = kBT % h;
   auto stage = [&](int p) {
-    const int c0 = kBP * p, w = min(kBP, a.nband - c0), buf = p & 1;
-    const int h = W / 2;
-    for (int e = tid; e < w * h; e += kBT) {
-      const int i = e / h, q = e % h;
-      cp_async16(blk + (buf * kBP + i) * W + 2 * q, a.Lb + static_cast<int64_t>(c0 + i) * W + 2 * q);
+    const int c0 = kBP * p, w = min(kBP, a.nband - c0), buf = p % nb;
+    const float2* src = a.Mf + static_cast<int64_t>(p) * kBP * W;
+    int i = i0, q = q0;
+    while (i < w) {  // the thread's 16-byte pieces, advancing by kBT without a division
+      cp_async16(mbuf + (buf * kBP + i) * W + 2 * q, src + i * W + 2 * q);
+      q += dq;
+      i += di;
+      if (q >= h) {
+        q -= h;
+        ++i;
+      }
     }
     for (int e = tid; e < kBP * kBP / 2; e += kBT)
       cp_async16(xb + buf * kBP * kBP + 2 * e, a.Xinv + static_cast<int64_t>(p) * kBP * kBP + 2 * e);
+    if (tid < w / 2) cp_async16(cb + buf * kBP + 2 * tid, zrow + c0 + 2 * tid);
     cp_async_commit();
   };
   for (int c = tid; c < a.nband; c += kBT) v[c] = zrow[c];
-  stage(0);
-  // a group of kSweepG threads per row of the panel (warps 0..5)
-  const int cl = tid / kSweepG, g = tid % kSweepG;
+  for (int s0 = 0; s0 < nb - 1; ++s0) {
+    if (s0 < a.npan) stage(s0);
+    else cp_async_commit();
+  }
+  const int k = tid / kSweepG, g = tid % kSweepG;
   for (int p = 0; p < a.npan; ++p) {
     const int c0 = kBP * p;
     const int w = min(kBP, a.nband - c0);
-    const int buf = p & 1;
-    if (p + 1 < a.npan) stage(p + 1);
+    const int buf = p % nb;
+    if (nb == 3) cp_async_wait_but_one();
+    else cp_async_wait_all();
+    __syncthreads();  // panel p landed; every thread is done with panel p - 1
+    if (p + nb - 1 < a.npan) stage(p + nb - 1);
     else cp_async_commit();
-    cp_async_wait_but_one();
-    __syncthreads();
     if (tid < kBP * kSweepG) {
-      // u_c = v_c - sum_{j < c0} L_cj v_j: the group's lanes take every
-      // kSweepG-th column, two accumulators each
-      Acc a0 = acc_init(dd_make(0.0f, 0.0f)), a1 = acc_init(dd_make(0.0f, 0.0f));
-      if (cl < w) {
-        const int c = c0 + cl;
-        const float2* lrow = blk + (buf * kBP + cl) * W + (W - 1 - c);
-        int j = max(0, c - W + 1) + g;
-        for (; j + kSweepG < c0; j += 2 * kSweepG) {
-          acc_madd(a0, f2dd(lrow[j]), f2dd(v[j]));
-          acc_madd(a1, f2dd(lrow[j + kSweepG]), f2dd(v[j + kSweepG]));
+      Acc a0 = acc_init(dd_make(0.0f, 0.0f)), a1 = a0, a2 = a0, a3 = a0;
+      if (k < w) {
+        const float2* xr = xb + buf * kBP * kBP + k * kBP;
+        const float2* cp = cb + buf * kBP;
+        for (int kk = g; kk <= k; kk += kSweepG) acc_madd(a0, f2dd(xr[kk]), f2dd(cp[kk]));
+        const float2* mrow = mbuf + (buf * kBP + k) * W;
+        const int vb = c0 - W + 1;  // column of slot 0
+        int s2 = max(0, -vb) + g;
+        for (; s2 + 3 * kSweepG < W - 1; s2 += 4 * kSweepG) {
+          const float2 m0 = mrow[s2], m1 = mrow[s2 + kSweepG], m2 = mrow[s2 + 2 * kSweepG], m3 = mrow[s2 + 3 * kSweepG];
+          const float2 v0 = v[vb + s2], v1 = v[vb + s2 + kSweepG], v2 = v[vb + s2 + 2 * kSweepG],
+                       v3 = v[vb + s2 + 3 * kSweepG];
+          acc_madd(a1, dd_neg(f2dd(m0)), f2dd(v0));
+          acc_madd(a2, dd_neg(f2dd(m1)), f2dd(v1));
+          acc_madd(a3, dd_neg(f2dd(m2)), f2dd(v2));
+          acc_madd(a0, dd_neg(f2dd(m3)), f2dd(v3));
         }
-        if (j < c0) acc_madd(a0, f2dd(lrow[j]), f2dd(v[j]));
+        for (; s2 < W - 1; s2 += kSweepG) acc_madd(a1, dd_neg(f2dd(mrow[s2])), f2dd(v[vb + s2]));
       }
       acc_add(a0, acc_get(a1));
+      acc_add(a2, acc_get(a3));
+      acc_add(a0, acc_get(a2));
       const dd sm = group_sum(acc_get(a0));
-      if (g == 0 && cl < w) {
-        Acc acc = acc_init(f2dd(v[c0 + cl]));
-        acc_add(acc, dd_neg(sm));
-        u[cl] = dd2f(acc_get(acc));
-      }
+      if (g == 0 && k < w) v[c0 + k] = dd2f(sm);
     }
-    __syncthreads();
-    if (tid < kBP * kSweepG) {
-      // v_{c0+cl} = sum_{j <= cl} X_cl,j u_j (X = L_pp^-1, unit lower)
-      Acc acc = acc_init(dd_make(0.0f, 0.0f));
-      if (cl < w) {
-        const float2* xr = xb + buf * kBP * kBP + cl * kBP;
-        for (int j = g; j <= cl; j += kSweepG) acc_madd(acc, f2dd(xr[j]), f2dd(u[j]));
-      }
-      const dd sm = group_sum(acc_get(acc));
-      if (g == 0 && cl < w) v[c0 + cl] = dd2f(sm);
-    }
-    __syncthreads();
   }
   cp_async_wait_all();
+  __syncthreads();
   float2* drow = a.Zd + static_cast<int64_t>(row) * a.nband;
   for (int c = tid; c < a.nband; c += kBT) {
     zrow[c] = v[c];
@@ -726,79 +786,83 @@ __global__ void __launch_bounds__(256) k_band_tvec(BandArgs a, const Ctrl* ctrl)
 }
 
 // One CTA: x_A = L_A^-T t (panels from the last), unscale, write the step.
+// Per panel, one dot per row: x_k = sum_{i >= k} X_ik t_i - sum_q Mb_kq x_(c1 + q),
+// a group of kSweepG threads per row (warps 0..5); t comes from the unchanged
+// xw (staged with the panel); one barrier per panel.
 __global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   extern __shared__ __align__(16) float2 sw[];
   const int W = a.W, span = W - 1;
+  const int nb = a.nbuf;
   float2* xv = sw;
-  float2* blk = xv + ((a.nband + 1) & ~1);  // 2 x span x kBP: rows below the panel, the panel's columns
-  float2* xb = blk + 2 * kBP * W;           // 2 x kBP x kBP
-  __shared__ float2 u[kBP];
+  float2* mbuf = xv + ((a.nband + 1) & ~1);  // nb x kBP x W
+  float2* xb = mbuf + nb * kBP * W;          // nb x kBP x kBP
+  float2* tb = xb + nb * kBP * kBP;          // nb x kBP
   const int tid = threadIdx.x;
+  const int h = W / 2;
+  const int i0 = tid / h, q0 = tid % h, di = kBT / h, dq = kBT % h;
   auto stage = [&](int p) {
-    const int c0 = kBP * p, w = min(kBP, a.nband - c0), c1 = c0 + w, buf = p & 1;
-    const int nr = min(span, a.nband - c1);
-    for (int e = tid; e < nr * kBP; e += kBT) {
-      const int q = e / kBP, k = e % kBP;
-      const int r = c1 + q;
-      const int sl = c0 + k - r + W - 1;
-      float2* dst = blk + (buf * span + q) * kBP + k;
-      if (k < w && sl >= 0) cp_async8(dst, a.Lb + static_cast<int64_t>(r) * W + sl);
-      else *dst = make_float2(0.0f, 0.0f);
+    const int c0 = kBP * p, w = min(kBP, a.nband - c0), buf = p % nb;
+    const float2* src = a.Mb + static_cast<int64_t>(p) * kBP * W;
+    int i = i0, q = q0;
+    while (i < w) {
+      cp_async16(mbuf + (buf * kBP + i) * W + 2 * q, src + i * W + 2 * q);
+      q += dq;
+      i += di;
+      if (q >= h) {
+        q -= h;
+        ++i;
+      }
     }
     for (int e = tid; e < kBP * kBP / 2; e += kBT)
       cp_async16(xb + buf * kBP * kBP + 2 * e, a.Xinv + static_cast<int64_t>(p) * kBP * kBP + 2 * e);
+    if (tid < w / 2) cp_async16(tb + buf * kBP + 2 * tid, a.xw + c0 + 2 * tid);
     cp_async_commit();
   };
   for (int c = tid; c < a.nband; c += kBT) xv[c] = a.xw[c];
-  stage(a.npan - 1);
-  // a group of kSweepG threads per column of the panel (warps 0..5)
-  const int cl = tid / kSweepG, g = tid % kSweepG;
+  for (int s0 = 0; s0 < nb - 1; ++s0) {
+    if (a.npan - 1 - s0 >= 0) stage(a.npan - 1 - s0);
+    else cp_async_commit();
+  }
+  const int k = tid / kSweepG, g = tid % kSweepG;
   for (int p = a.npan - 1; p >= 0; --p) {
     const int c0 = kBP * p;
     const int w = min(kBP, a.nband - c0);
     const int c1 = c0 + w;
-    const int buf = p & 1;
-    if (p > 0) stage(p - 1);
+    const int buf = p % nb;
+    if (nb == 3) cp_async_wait_but_one();
+    else cp_async_wait_all();
+    __syncthreads();  // panel p landed; every thread is done with panel p + 1
+    if (p - (nb - 1) >= 0) stage(p - (nb - 1));
     else cp_async_commit();
-    cp_async_wait_but_one();
-    __syncthreads();
     if (tid < kBP * kSweepG) {
-      // u_c = x_c - sum_r L_rc x_r, rows r in [c1, min(c + W, nband)): the
-      // group's lanes take every kSweepG-th row, two accumulators each
-      Acc a0 = acc_init(dd_make(0.0f, 0.0f)), a1 = acc_init(dd_make(0.0f, 0.0f));
-      if (cl < w) {
-        const int c = c0 + cl;
-        const int rhi = min(c + W, a.nband);
-        const float2* col = blk + buf * span * kBP + cl;  // row r at col[(r - c1) * kBP]
-        int r = c1 + g;
-        for (; r + kSweepG < rhi; r += 2 * kSweepG) {
-          acc_madd(a0, f2dd(col[(r - c1) * kBP]), f2dd(xv[r]));
-          acc_madd(a1, f2dd(col[(r + kSweepG - c1) * kBP]), f2dd(xv[r + kSweepG]));
+      Acc a0 = acc_init(dd_make(0.0f, 0.0f)), a1 = a0, a2 = a0, a3 = a0;
+      if (k < w) {
+        const float2* x2 = xb + buf * kBP * kBP;
+        const float2* tp = tb + buf * kBP;
+        for (int i = k + g; i < w; i += kSweepG) acc_madd(a0, f2dd(x2[i * kBP + k]), f2dd(tp[i]));
+        const float2* mrow = mbuf + (buf * kBP + k) * W;
+        const int nq = min(span, a.nband - c1);
+        int q = g;
+        for (; q + 3 * kSweepG < nq; q += 4 * kSweepG) {
+          const float2 m0 = mrow[q], m1 = mrow[q + kSweepG], m2 = mrow[q + 2 * kSweepG], m3 = mrow[q + 3 * kSweepG];
+          const float2 x0 = xv[c1 + q], x1 = xv[c1 + q + kSweepG], x2v = xv[c1 + q + 2 * kSweepG],
+                       x3 = xv[c1 + q + 3 * kSweepG];
+          acc_madd(a1, dd_neg(f2dd(m0)), f2dd(x0));
+          acc_madd(a2, dd_neg(f2dd(m1)), f2dd(x1));
+          acc_madd(a3, dd_neg(f2dd(m2)), f2dd(x2v));
+          acc_madd(a0, dd_neg(f2dd(m3)), f2dd(x3));
         }
-        if (r < rhi) acc_madd(a0, f2dd(col[(r - c1) * kBP]), f2dd(xv[r]));
+        for (; q < nq; q += kSweepG) acc_madd(a1, dd_neg(f2dd(mrow[q])), f2dd(xv[c1 + q]));
       }
       acc_add(a0, acc_get(a1));
+      acc_add(a2, acc_get(a3));
+      acc_add(a0, acc_get(a2));
       const dd sm = group_sum(acc_get(a0));
-      if (g == 0 && cl < w) {
-        Acc acc = acc_init(f2dd(xv[c0 + cl]));
-        acc_add(acc, dd_neg(sm));
-        u[cl] = dd2f(acc_get(acc));
-      }
+      if (g == 0 && k < w) xv[c0 + k] = dd2f(sm);
     }
-    __syncthreads();
-    if (tid < kBP * kSweepG) {
-      // x_{c0+k} = sum_{i >= k} X_ik u_i
-      Acc acc = acc_init(dd_make(0.0f, 0.0f));
-      if (cl < w) {
-        const float2* x2 = xb + buf * kBP * kBP;
-        for (int i = cl + g; i < w; i += kSweepG) acc_madd(acc, f2dd(x2[i * kBP + cl]), f2dd(u[i]));
-      }
-      const dd sm = group_sum(acc_get(acc));
-      if (g == 0 && cl < w) xv[c0 + cl] = dd2f(sm);
-    }
-    __syncthreads();
   }
+  __syncthreads();
   cp_async_wait_all();
   for (int r = tid; r < a.n; r += kBT) {
     const dd v = (r < a.nband) ? f2dd(xv[r]) : f2dd(a.xw[r]);
@@ -809,6 +873,8 @@ __global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a, const Ctrl* ctrl) 
   }
 }
 
+int sweep_nbuf(int nband, int W);
+
 BandArgs band_args(const Sizes& s, const Dev& d) {
   BandArgs a;
   a.n = s.n6;
@@ -817,6 +883,7 @@ BandArgs band_args(const Sizes& s, const Dev& d) {
   a.npan = (s.band_rows + kBP - 1) / kBP;
   a.nbd = s.n6 - s.band_rows;
   a.ring = s.band_ring;
+  a.nbuf = sweep_nbuf(a.nband, a.W);
   a.S = d.S;
   a.b = d.rb;
   a.scl = d.band_scl;
@@ -827,6 +894,8 @@ BandArgs band_args(const Sizes& s, const Dev& d) {
   a.Pbuf = d.band_P;
   a.Zc = d.band_Z;
   a.Zd = d.band_Zd;
+  a.Mf = d.band_Mf;
+  a.Mb = d.band_Mb;
   a.Cn = d.band_E;
   a.xw = d.band_xw;
   a.x = d.x;
@@ -847,7 +916,18 @@ size_t factor_dyn_smem(int W, int C) {
                            static_cast<size_t>(W - 1) * (kBP + 1));
 }
 
-size_t band_sweep_smem(int nband, int W) { return sizeof(float2) * sweep_smem_floats2(nband, W); }
+// Three panel buffers in the sweeps where they fit in shared memory, else two.
+int sweep_nbuf(int nband, int W) {
+  return sizeof(float2) * sweep_smem_floats2(nband, W, 3) <= kSmemLimit - 4096 ? 3 : 2;
+}
+
+size_t sweepmat_smem(int W) {
+  return sizeof(float2) * (static_cast<size_t>(kBP) * W + static_cast<size_t>(W - 1) * kBP + kBP * kBP);
+}
+
+size_t band_sweep_smem(int nband, int W) {
+  return sizeof(float2) * sweep_smem_floats2(nband, W, sweep_nbuf(nband, W));
+}
 
 }  // namespace
 
@@ -898,6 +978,7 @@ int band_setup(int n, int nband, int W, int* cluster, int* ring) {
   if (corner > kSmemLimit - 4096) return 0;
   const size_t fmax = factor_dyn_smem(W, 8);  // the larger of the two cluster sizes tried
   if (raise_dynamic_smem(reinterpret_cast<const void*>(k_band_fwd), sweep) != cudaSuccess ||
+      raise_dynamic_smem(reinterpret_cast<const void*>(k_band_sweepmat), sweepmat_smem(W)) != cudaSuccess ||
       raise_dynamic_smem(reinterpret_cast<const void*>(k_band_bwd), sweep) != cudaSuccess ||
       raise_dynamic_smem(reinterpret_cast<const void*>(k_band_corner_solve), std::max<size_t>(corner, 16)) !=
           cudaSuccess ||
@@ -969,6 +1050,8 @@ int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
     else cudaLaunchKernelEx(&cfg, k_band_factor<8>, a, d.ctrl);
     ++launches;
   }
+  k_band_sweepmat<<<a.npan, kBT, sweepmat_smem(a.W), st>>>(a, d.ctrl);
+  ++launches;
   k_band_fwd<<<a.nbd + 1, kBT, band_sweep_smem(a.nband, a.W), st>>>(a, d.ctrl);
   ++launches;
   {
@@ -989,6 +1072,6 @@ int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
   return launches;
 }
 
-int band_launch_count() { return 8; }
+int band_launch_count() { return 9; }
 
 }  // namespace sgba

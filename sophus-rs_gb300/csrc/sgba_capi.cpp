@@ -855,6 +855,8 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
       if ((st = dev_alloc(p, &d.band_scl, n6))) return st;
       if ((st = dev_alloc(p, &d.band_L, static_cast<size_t>(rows) * w))) return st;
       if ((st = dev_alloc(p, &d.band_Xinv, npan * 24 * 24))) return st;
+      if ((st = dev_alloc(p, &d.band_Mf, npan * 24 * static_cast<size_t>(w)))) return st;
+      if ((st = dev_alloc(p, &d.band_Mb, npan * 24 * static_cast<size_t>(w)))) return st;
       if ((st = dev_alloc(p, &d.band_d, n6))) return st;
       if ((st = dev_alloc(p, &d.band_rd, n6))) return st;
       if ((st = dev_alloc(p, &d.band_P, static_cast<size_t>(w) * 24))) return st;

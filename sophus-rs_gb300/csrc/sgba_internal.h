@@ -188,6 +188,8 @@ struct Dev {
   float* band_scl = nullptr;       // n6: D^-1/2
   float2* band_L = nullptr;        // band_rows x band_w
   float2* band_Xinv = nullptr;     // panels x 24 x 24
+  float2* band_Mf = nullptr;       // panels x 24 x band_w: X_p L of the panel's rows (forward sweep)
+  float2* band_Mb = nullptr;       // panels x 24 x band_w: X_p^T L^T of the rows below (backward sweep)
   float2* band_d = nullptr;        // n6 pivots
   float2* band_rd = nullptr;       // n6 reciprocal pivots
   float2* band_P = nullptr;        // band_w x 24 panel exchange
