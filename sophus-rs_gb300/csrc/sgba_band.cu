@@ -55,10 +55,15 @@ constexpr int kBP = 24;          // panel width (4 pose blocks)
 constexpr int kBT = 256;         // threads per CTA (sweeps, corner)
 constexpr int kCT = 1024;        // threads of the corner solve (one CTA; more warps hide its per-pivot chains)
 constexpr int kFT = 320;         // threads per CTA of the factor: one per position of the 24x24 lower triangle (300)
-constexpr int kMaxWBlocks = 32;  // widest band, in pose blocks
-constexpr int kMaxW = 6 * kMaxWBlocks;
+static_assert(kFT - 32 >= 6 * 48, "the factor kernel's threads 32.. cover the rows below a panel of the widest band");
+constexpr int kMaxWBlocks = 32;  // widest band of the band part, in pose blocks
 constexpr int kMaxBorderBlocks = 24;
 constexpr int kMaxBorder = 6 * kMaxBorderBlocks;
+// A dissected loop's corner (separator + closure) is factored as a dense band
+// (W = its rows).  The factor kernel maps the W - 1 rows below a panel to
+// threads 32 .. W + 30 of a CTA, so W <= kFT - 32 (288 rows, 48 pose blocks).
+constexpr int kMaxCornerBlocks = 48;
+constexpr int kMaxW = 6 * kMaxCornerBlocks;  // widest band the factor kernel takes (the corner's)
 constexpr int kMaxOwnRows = (kMaxW - 1 + 7) / 8;  // rows of one CTA in a window (cluster >= 8)
 constexpr float kTolRel = 1e-12f;
 constexpr size_t kSmemLimit = 227 * 1024;
@@ -143,7 +148,38 @@ struct BandArgs {
   float2* xw;       // n: t (band part) and x_C (border part)
   double* x;        // n: the step (unscaled)
   float* xdd;       // 2n: the step as float-float pairs
+  // Nested dissection of a loop: the rows are permuted (perm[r] is the row
+  // of S behind row r of the solved system; null: the identity) so that the
+  // band part is two independent segments (the loop's two arcs, the second
+  // in reverse order), factored and swept concurrently, and the border holds
+  // the separator between them and the loop closure.
+  const int32_t* perm;
+  int nseg;         // 1 or 2
+  int seg_row0[2];  // first row of each segment
+  int seg_rows[2];  // rows of each segment (multiples of 6)
+  int seg_pan0[2];  // first panel of each segment
+  int32_t* zlo;     // (nbd + 1) x nseg: first nonzero column of each Zc row in each segment (segment-relative)
+  float2* out_scaled;  // backward sweep: the scaled solution goes here (the corner's solve) instead of x / xdd
 };
+
+__device__ __forceinline__ int seg_of_row(const BandArgs& a, int r) { return (a.nseg > 1 && r >= a.seg_row0[1]) ? 1 : 0; }
+__device__ __forceinline__ int seg_of_panel(const BandArgs& a, int P) {
+  return (a.nseg > 1 && P >= a.seg_pan0[1]) ? 1 : 0;
+}
+__device__ __forceinline__ int prow(const BandArgs& a, int r) { return a.perm ? a.perm[r] : r; }
+// One segment as a band of its own: rows, panels and their tables offset.
+__device__ __forceinline__ BandArgs seg_view(const BandArgs& a, int sg) {
+  BandArgs b = a;
+  b.nband = a.seg_rows[sg];
+  b.npan = (b.nband + kBP - 1) / kBP;
+  b.Lb = a.Lb + static_cast<int64_t>(a.seg_row0[sg]) * a.W;
+  b.Xinv = a.Xinv + static_cast<int64_t>(a.seg_pan0[sg]) * kBP * kBP;
+  b.Mf = a.Mf + static_cast<int64_t>(a.seg_pan0[sg]) * kBP * a.W;
+  b.Mb = a.Mb + static_cast<int64_t>(a.seg_pan0[sg]) * kBP * a.W;
+  b.dpiv = a.dpiv + a.seg_row0[sg];
+  b.rdpiv = a.rdpiv + a.seg_row0[sg];
+  return b;
+}
 
 
 // ---------------------------------------------------------------- set-up ---
@@ -151,7 +187,8 @@ struct BandArgs {
 __global__ void __launch_bounds__(256) k_band_scale(BandArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < a.n; r += gridDim.x * blockDim.x) {
-    const double v = a.S[static_cast<int64_t>(r) * a.n + r];
+    const int pr = prow(a, r);
+    const double v = a.S[static_cast<int64_t>(pr) * a.n + pr];
     a.scl[r] = (v > 0.0 && isfinite(v)) ? static_cast<float>(1.0 / sqrt(v)) : 1.0f;
   }
 }
@@ -168,8 +205,8 @@ __global__ void __launch_bounds__(256) k_band_load(BandArgs a, const Ctrl* ctrl)
       const int r = static_cast<int>(e / a.W);
       const int c = r - a.W + 1 + static_cast<int>(e % a.W);
       float2 v = make_float2(0.0f, 0.0f);
-      if (c >= 0) {
-        const double s = a.S[static_cast<int64_t>(r) * a.n + c];
+      if (c >= a.seg_row0[seg_of_row(a, r)]) {  // inside the row's segment
+        const double s = a.S[static_cast<int64_t>(prow(a, r)) * a.n + prow(a, c)];
         v = dd2f(dd_from_prod(s * static_cast<double>(a.scl[r]) * static_cast<double>(a.scl[c])));
       }
       a.Lb[e] = v;
@@ -179,9 +216,10 @@ __global__ void __launch_bounds__(256) k_band_load(BandArgs a, const Ctrl* ctrl)
       double v;
       if (i < a.nbd) {
         const int r = a.nband + i;
-        v = a.S[static_cast<int64_t>(r) * a.n + c] * static_cast<double>(a.scl[r]) * static_cast<double>(a.scl[c]);
+        v = a.S[static_cast<int64_t>(prow(a, r)) * a.n + prow(a, c)] * static_cast<double>(a.scl[r]) *
+            static_cast<double>(a.scl[c]);
       } else {
-        v = a.b[c] * static_cast<double>(a.scl[c]);
+        v = a.b[prow(a, c)] * static_cast<double>(a.scl[c]);
       }
       a.Zc[q] = dd2f(dd_from_prod(v));
     } else {
@@ -192,10 +230,10 @@ __global__ void __launch_bounds__(256) k_band_load(BandArgs a, const Ctrl* ctrl)
         const int cj = a.nband + j;
         if (i < a.nbd) {
           const int r = a.nband + i;
-          v = a.S[static_cast<int64_t>(r) * a.n + cj] * static_cast<double>(a.scl[r]) *
+          v = a.S[static_cast<int64_t>(prow(a, r)) * a.n + prow(a, cj)] * static_cast<double>(a.scl[r]) *
               static_cast<double>(a.scl[cj]);
         } else {
-          v = a.b[cj] * static_cast<double>(a.scl[cj]);
+          v = a.b[prow(a, cj)] * static_cast<double>(a.scl[cj]);
         }
       }
       a.Cn[q] = dd2f(dd_from_prod(v));
@@ -231,10 +269,13 @@ struct FactorShared {
 // panel and publishes L D of them; after a cluster barrier every CTA gathers
 // the panel's L D (DSMEM) and updates its own rows in place.
 template <int C>
-__global__ void __launch_bounds__(kFT, 1) k_band_factor(BandArgs a, Ctrl* ctrl) {
+__global__ void __launch_bounds__(kFT, 1) k_band_factor(BandArgs a0, Ctrl* ctrl) {
   // Every CTA reads the control block before the first cluster barrier and
   // only CTA 0 writes it, after the last one: the early return is uniform.
   if (skipping(ctrl)) return;
+  // cluster k factors segment k (the two arcs of a dissected loop run
+  // concurrently, each as a band of its own)
+  const BandArgs a = seg_view(a0, static_cast<int>(blockIdx.x) / C);
   __shared__ FactorShared sh;
   extern __shared__ __align__(16) float2 dyn[];
   cg::cluster_group cl = cg::this_cluster();
@@ -511,11 +552,13 @@ __device__ __forceinline__ dd group_sum(dd s) {
 //   backward: x_p = X_p^T (t_p - L_b^T x_below) = X_p^T t_p - Mb_p x_below,
 //             Mb_p = X_p^T L_b^T (L_b the W - 1 rows below the panel over its columns).
 // Each sweep step is then one dot product per row of the panel.
-__global__ void __launch_bounds__(kBT) k_band_sweepmat(BandArgs a, const Ctrl* ctrl) {
+__global__ void __launch_bounds__(kBT) k_band_sweepmat(BandArgs a0, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   extern __shared__ __align__(16) float2 smx[];
+  const int sg = seg_of_panel(a0, static_cast<int>(blockIdx.x));
+  const BandArgs a = seg_view(a0, sg);
   const int W = a.W, span = W - 1;
-  const int p = blockIdx.x;
+  const int p = static_cast<int>(blockIdx.x) - a0.seg_pan0[sg];
   const int c0 = kBP * p, w = min(kBP, a.nband - c0), c1 = c0 + w;
   const int tid = threadIdx.x;
   float2* Lp = smx;             // kBP x W: the panel's rows, slots as in Lb
@@ -558,9 +601,13 @@ __global__ void __launch_bounds__(kBT) k_band_sweepmat(BandArgs a, const Ctrl* c
 // a group of kSweepG threads per row (warps 0..5).  The panel's inputs c come
 // from the unchanged Zc row (staged with the panel), so the outputs can go
 // straight into the vector; one barrier per panel.
-__global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a, const Ctrl* ctrl) {
+__global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a0, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   extern __shared__ __align__(16) float2 sw[];
+  // CTA (row, segment): the row's part in one segment of the band
+  const int sg = static_cast<int>(blockIdx.x) % a0.nseg;
+  const int row = static_cast<int>(blockIdx.x) / a0.nseg;
+  const BandArgs a = seg_view(a0, sg);
   const int W = a.W;
   const int nb = a.nbuf;
   float2* v = sw;
@@ -568,8 +615,7 @@ __global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a, const Ctrl* ctrl) 
   float2* xb = mbuf + nb * kBP * W;         // nb x kBP x kBP
   float2* cb = xb + nb * kBP * kBP;         // nb x kBP
   const int tid = threadIdx.x;
-  const int row = blockIdx.x;
-  float2* zrow = a.Zc + static_cast<int64_t>(row) * a.nband;
+  float2* zrow = a0.Zc + static_cast<int64_t>(row) * a0.nband + a0.seg_row0[sg];
   const int h = W / 2;
   const int i0 = tid / h, q0 = tid % h, di = kBT / h, dq = kBT % h;
   auto stage = [&](int p) {
@@ -590,13 +636,26 @@ __global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a, const Ctrl* ctrl) 
     if (tid < w / 2) cp_async16(cb + buf * kBP + 2 * tid, zrow + c0 + 2 * tid);
     cp_async_commit();
   };
-  for (int c = tid; c < a.nband; c += kBT) v[c] = zrow[c];
+  // the row's first nonzero in the segment: the panels before it stay zero
+  __shared__ int s_first;
+  if (tid == 0) s_first = a.nband;
+  __syncthreads();
+  int myfirst = a.nband;
+  for (int c = tid; c < a.nband; c += kBT) {
+    const float2 z = zrow[c];
+    v[c] = z;
+    if ((z.x != 0.0f || z.y != 0.0f) && c < myfirst) myfirst = c;
+  }
+  atomicMin(&s_first, myfirst);
+  __syncthreads();
+  const int pstart = s_first / kBP;
+  if (tid == 0 && a0.zlo) a0.zlo[row * a0.nseg + sg] = s_first;
   for (int s0 = 0; s0 < nb - 1; ++s0) {
-    if (s0 < a.npan) stage(s0);
+    if (pstart + s0 < a.npan) stage(pstart + s0);
     else cp_async_commit();
   }
   const int k = tid / kSweepG, g = tid % kSweepG;
-  for (int p = 0; p < a.npan; ++p) {
+  for (int p = pstart; p < a.npan; ++p) {
     const int c0 = kBP * p;
     const int w = min(kBP, a.nband - c0);
     const int buf = p % nb;
@@ -634,7 +693,7 @@ __global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a, const Ctrl* ctrl) 
   }
   cp_async_wait_all();
   __syncthreads();
-  float2* drow = a.Zd + static_cast<int64_t>(row) * a.nband;
+  float2* drow = a0.Zd + static_cast<int64_t>(row) * a0.nband + a0.seg_row0[sg];
   for (int c = tid; c < a.nband; c += kBT) {
     zrow[c] = v[c];
     drow[c] = dd2f(dd_mul(f2dd(v[c]), f2dd(a.rdpiv[c])));
@@ -667,11 +726,26 @@ __global__ void __launch_bounds__(128) k_band_corner(BandArgs a, const Ctrl* ctr
     if (i < m) {
       const float2* zi = a.Zd + static_cast<int64_t>(i) * a.nband;
       const float2* zj = a.Zc + static_cast<int64_t>(kCornerTile * tj) * a.nband;
-      for (int c = lane; c < a.nband; c += 32) {
-        const dd x = f2dd(zi[c]);
+      for (int sg = 0; sg < a.nseg; ++sg) {
+        // the rows are zero before their first nonzero in the segment: the
+        // tile's products start at the later of its rows' and columns' first
+        int lo = 0;
+        if (a.zlo) {
+          int li = a.seg_rows[sg], lj = a.seg_rows[sg];
+          for (int t = 0; t < kCornerTile; ++t) {
+            const int ri = kCornerTile * ti + t, rj = kCornerTile * tj + t;
+            if (ri < m) li = min(li, a.zlo[ri * a.nseg + sg]);
+            if (rj < m) lj = min(lj, a.zlo[rj * a.nseg + sg]);
+          }
+          lo = max(li, lj);
+        }
+        const int cend = a.seg_row0[sg] + a.seg_rows[sg];
+        for (int c = a.seg_row0[sg] + lo + lane; c < cend; c += 32) {
+          const dd x = f2dd(zi[c]);
 #pragma unroll
-        for (int jj = 0; jj < kCornerTile; ++jj)
-          if (kCornerTile * tj + jj < m) acc_madd(acc[jj], x, f2dd(zj[static_cast<int64_t>(jj) * a.nband + c]));
+          for (int jj = 0; jj < kCornerTile; ++jj)
+            if (kCornerTile * tj + jj < m) acc_madd(acc[jj], x, f2dd(zj[static_cast<int64_t>(jj) * a.nband + c]));
+        }
       }
     }
 #pragma unroll
@@ -774,6 +848,25 @@ __global__ void __launch_bounds__(kCT) k_band_corner_solve(BandArgs a, Ctrl* ctr
   if (tid == 0 && sbad) ctrl->skip = 2;
 }
 
+// The corner of a dissected loop as a dense band of its own (W = m): its
+// lower rows from Cn, and its right-hand side row (y_C) for the sweeps.
+__global__ void __launch_bounds__(256) k_band_corner_load(BandArgs ac, const float2* __restrict__ cn,
+                                                          const Ctrl* ctrl) {
+  if (skipping(ctrl)) return;
+  const int m = ac.nband, ld = m + 1;
+  const int64_t total = static_cast<int64_t>(m) * m + m;
+  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < total;
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    if (e < static_cast<int64_t>(m) * m) {
+      const int r = static_cast<int>(e / m), c = r - m + 1 + static_cast<int>(e % m);
+      ac.Lb[e] = (c >= 0) ? cn[static_cast<int64_t>(r) * ld + c] : make_float2(0.0f, 0.0f);
+    } else {
+      const int j = static_cast<int>(e - static_cast<int64_t>(m) * m);
+      ac.Zc[j] = cn[static_cast<int64_t>(m) * ld + j];
+    }
+  }
+}
+
 // t_c = Zd_{rhs,c} - sum_i Zd_ic x_Ci for the band columns.
 __global__ void __launch_bounds__(256) k_band_tvec(BandArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
@@ -789,9 +882,13 @@ __global__ void __launch_bounds__(256) k_band_tvec(BandArgs a, const Ctrl* ctrl)
 // Per panel, one dot per row: x_k = sum_{i >= k} X_ik t_i - sum_q Mb_kq x_(c1 + q),
 // a group of kSweepG threads per row (warps 0..5); t comes from the unchanged
 // xw (staged with the panel); one barrier per panel.
-__global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a, const Ctrl* ctrl) {
+__global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a0, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   extern __shared__ __align__(16) float2 sw[];
+  // CTA k sweeps segment k
+  const int sg = static_cast<int>(blockIdx.x);
+  const BandArgs a = seg_view(a0, sg);
+  const float2* xw = a0.xw + a0.seg_row0[sg];
   const int W = a.W, span = W - 1;
   const int nb = a.nbuf;
   float2* xv = sw;
@@ -816,10 +913,10 @@ __global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a, const Ctrl* ctrl) 
     }
     for (int e = tid; e < kBP * kBP / 2; e += kBT)
       cp_async16(xb + buf * kBP * kBP + 2 * e, a.Xinv + static_cast<int64_t>(p) * kBP * kBP + 2 * e);
-    if (tid < w / 2) cp_async16(tb + buf * kBP + 2 * tid, a.xw + c0 + 2 * tid);
+    if (tid < w / 2) cp_async16(tb + buf * kBP + 2 * tid, xw + c0 + 2 * tid);
     cp_async_commit();
   };
-  for (int c = tid; c < a.nband; c += kBT) xv[c] = a.xw[c];
+  for (int c = tid; c < a.nband; c += kBT) xv[c] = xw[c];
   for (int s0 = 0; s0 < nb - 1; ++s0) {
     if (a.npan - 1 - s0 >= 0) stage(a.npan - 1 - s0);
     else cp_async_commit();
@@ -864,19 +961,28 @@ __global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a, const Ctrl* ctrl) 
   }
   __syncthreads();
   cp_async_wait_all();
-  for (int r = tid; r < a.n; r += kBT) {
-    const dd v = (r < a.nband) ? f2dd(xv[r]) : f2dd(a.xw[r]);
-    const dd xs = dd_mul(v, dd_make(a.scl[r], 0.0f));
-    a.x[r] = dd_to_double(xs);
-    a.xdd[2 * r] = xs.hi;
-    a.xdd[2 * r + 1] = xs.lo;
+  if (a0.out_scaled) {  // the corner's solve: the scaled solution
+    for (int r = tid; r < a.nband; r += kBT) a0.out_scaled[a0.seg_row0[sg] + r] = xv[r];
+    return;
   }
+  // unscale and write the step at the rows of S (the segment's rows; CTA 0
+  // also the border rows, solved with the corner)
+  auto put = [&](int r, dd v) {
+    const dd xs = dd_mul(v, dd_make(a0.scl[r], 0.0f));
+    const int pr = prow(a0, r);
+    a0.x[pr] = dd_to_double(xs);
+    a0.xdd[2 * pr] = xs.hi;
+    a0.xdd[2 * pr + 1] = xs.lo;
+  };
+  for (int r = tid; r < a.nband; r += kBT) put(a0.seg_row0[sg] + r, f2dd(xv[r]));
+  if (sg == 0)
+    for (int r = a0.nband + tid; r < a0.n; r += kBT) put(r, f2dd(a0.xw[r]));
 }
 
 int sweep_nbuf(int nband, int W);
 
 BandArgs band_args(const Sizes& s, const Dev& d) {
-  BandArgs a;
+  BandArgs a{};
   a.n = s.n6;
   a.nband = s.band_rows;
   a.W = s.band_w;
@@ -900,7 +1006,50 @@ BandArgs band_args(const Sizes& s, const Dev& d) {
   a.xw = d.band_xw;
   a.x = d.x;
   a.xdd = d.xdd;
+  a.perm = d.band_perm;
+  a.nseg = s.band_nseg > 1 ? 2 : 1;
+  a.seg_row0[0] = 0;
+  a.seg_rows[0] = a.nseg > 1 ? s.band_seg_rows : a.nband;
+  a.seg_row0[1] = a.seg_rows[0];
+  a.seg_rows[1] = a.nband - a.seg_rows[0];
+  a.seg_pan0[0] = 0;
+  a.seg_pan0[1] = (a.seg_rows[0] + kBP - 1) / kBP;
+  a.npan = a.seg_pan0[1] + (a.nseg > 1 ? (a.seg_rows[1] + kBP - 1) / kBP : 0);
+  a.nbuf = sweep_nbuf(a.seg_rows[0] > a.seg_rows[1] ? a.seg_rows[0] : a.seg_rows[1], a.W);
+  a.zlo = d.band_zlo;
+  a.out_scaled = nullptr;
   return a;
+}
+
+// The corner of a dissected loop as a band solve of its own.
+BandArgs corner_args(const Sizes& s, const Dev& d, const BandArgs& a) {
+  BandArgs c = a;
+  const int m = a.nbd;
+  c.n = m;
+  c.nband = m;
+  c.W = m;
+  c.npan = (m + kBP - 1) / kBP;
+  c.nbd = 0;
+  c.ring = s.band_ring_c;
+  c.nbuf = sweep_nbuf(m, m);
+  c.Lb = d.band_Lc;
+  c.Xinv = d.band_Xc;
+  c.Mf = d.band_Mfc;
+  c.Mb = d.band_Mbc;
+  c.dpiv = a.dpiv + a.nband;
+  c.rdpiv = a.rdpiv + a.nband;
+  c.Zc = d.band_Zcc;
+  c.Zd = d.band_Zdc;
+  c.xw = d.band_Zdc;
+  c.perm = nullptr;
+  c.nseg = 1;
+  c.seg_row0[0] = c.seg_row0[1] = 0;
+  c.seg_rows[0] = m;
+  c.seg_rows[1] = 0;
+  c.seg_pan0[0] = c.seg_pan0[1] = 0;
+  c.zlo = d.band_zloc;
+  c.out_scaled = a.xw + a.nband;
+  return c;
 }
 
 int band_ring(int W, int C) {
@@ -967,23 +1116,31 @@ int band_shape(int nf, const std::vector<int32_t>& sb_row, const std::vector<int
   return 1;
 }
 
-int band_setup(int n, int nband, int W, int* cluster, int* ring) {
+int band_setup(int n, int nband, int W, int nseg, int seg_rows_max, int* cluster, int* ring, int* ring_c) {
   *cluster = 0;
   *ring = 0;
-  if (nband <= 0 || W < 6 || W > kMaxW || n - nband > kMaxBorder) return 0;
-  const size_t sweep = band_sweep_smem(nband, W);
+  *ring_c = 0;
+  const int m = n - nband;  // border rows
+  if (nband <= 0 || W < 6 || W > 6 * kMaxWBlocks) return 0;
+  if (nseg > 1 ? (m > kMaxW || m % 6 != 0 || m < kBP) : m > kMaxBorder) return 0;
+  const int segmax = nseg > 1 ? seg_rows_max : nband;
+  size_t sweep = band_sweep_smem(segmax, W);
   if (sweep > kSmemLimit - 4096) return 0;
-  const int m = n - nband;
-  const size_t corner = sizeof(float2) * static_cast<size_t>(m) * (m + 2);
-  if (corner > kSmemLimit - 4096) return 0;
-  const size_t fmax = factor_dyn_smem(W, 8);  // the larger of the two cluster sizes tried
+  size_t smat = sweepmat_smem(W);
+  size_t corner = 16;
+  if (nseg > 1) {  // the corner is factored and swept as a dense band (W = m)
+    sweep = std::max(sweep, band_sweep_smem(m, m));
+    smat = std::max(smat, sweepmat_smem(m));
+    if (sweep > kSmemLimit - 4096 || smat > kSmemLimit - 4096) return 0;
+  } else {
+    corner = sizeof(float2) * static_cast<size_t>(m) * (m + 2);
+    if (corner > kSmemLimit - 4096) return 0;
+  }
   if (raise_dynamic_smem(reinterpret_cast<const void*>(k_band_fwd), sweep) != cudaSuccess ||
-      raise_dynamic_smem(reinterpret_cast<const void*>(k_band_sweepmat), sweepmat_smem(W)) != cudaSuccess ||
+      raise_dynamic_smem(reinterpret_cast<const void*>(k_band_sweepmat), smat) != cudaSuccess ||
       raise_dynamic_smem(reinterpret_cast<const void*>(k_band_bwd), sweep) != cudaSuccess ||
       raise_dynamic_smem(reinterpret_cast<const void*>(k_band_corner_solve), std::max<size_t>(corner, 16)) !=
-          cudaSuccess ||
-      raise_dynamic_smem(reinterpret_cast<const void*>(k_band_factor<16>), fmax) != cudaSuccess ||
-      raise_dynamic_smem(reinterpret_cast<const void*>(k_band_factor<8>), fmax) != cudaSuccess) {
+          cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
@@ -995,10 +1152,19 @@ int band_setup(int n, int nband, int W, int* cluster, int* ring) {
       cudaGetLastError();
       continue;
     }
+    // the factor's shared memory at this cluster size (the widest band it takes)
+    const size_t fs = factor_dyn_smem(nseg > 1 ? std::max(W, m) : W, C);
+    if (fs > kSmemLimit - 32 * 1024) continue;
+    const void* fk = (C == 16) ? reinterpret_cast<const void*>(k_band_factor<16>)
+                               : reinterpret_cast<const void*>(k_band_factor<8>);
+    if (raise_dynamic_smem(fk, fs) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(C);
     cfg.blockDim = dim3(kFT);
-    cfg.dynamicSmemBytes = factor_dyn_smem(W, C);
+    cfg.dynamicSmemBytes = fs;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
     at[0].val.clusterDim.x = C;
@@ -1013,13 +1179,33 @@ int band_setup(int n, int nband, int W, int* cluster, int* ring) {
       cudaGetLastError();
       continue;
     }
-    if (nclusters < 1) continue;
+    if (nclusters < nseg) continue;  // the segments' clusters must run at the same time
     *cluster = C;
     *ring = band_ring(W, C);
+    *ring_c = nseg > 1 ? band_ring(m, C) : 0;
     return C;
   }
   return 0;
 }
+
+namespace {
+cudaError_t launch_factor(const BandArgs& a, int C, int nclusters, cudaStream_t st, const Ctrl* ctrl) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(C * nclusters);
+  cfg.blockDim = dim3(kFT);
+  cfg.dynamicSmemBytes = factor_dyn_smem(a.W, C);
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = C;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  Ctrl* c = const_cast<Ctrl*>(ctrl);
+  return (C == 16) ? cudaLaunchKernelEx(&cfg, k_band_factor<16>, a, c) : cudaLaunchKernelEx(&cfg, k_band_factor<8>, a, c);
+}
+}  // namespace
 
 int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
   const BandArgs a = band_args(s, d);
@@ -1033,26 +1219,12 @@ int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
     k_band_load<<<std::max(blocks, 1), 256, 0, st>>>(a, d.ctrl);
     ++launches;
   }
-  {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(s.band_c);
-    cfg.blockDim = dim3(kFT);
-    cfg.dynamicSmemBytes = factor_dyn_smem(a.W, s.band_c);
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = s.band_c;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    if (s.band_c == 16) cudaLaunchKernelEx(&cfg, k_band_factor<16>, a, d.ctrl);
-    else cudaLaunchKernelEx(&cfg, k_band_factor<8>, a, d.ctrl);
-    ++launches;
-  }
+  launch_factor(a, s.band_c, a.nseg, st, d.ctrl);  // one cluster per segment
+  ++launches;
   k_band_sweepmat<<<a.npan, kBT, sweepmat_smem(a.W), st>>>(a, d.ctrl);
   ++launches;
-  k_band_fwd<<<a.nbd + 1, kBT, band_sweep_smem(a.nband, a.W), st>>>(a, d.ctrl);
+  const int segmax = std::max(a.seg_rows[0], a.seg_rows[1]);
+  k_band_fwd<<<(a.nbd + 1) * a.nseg, kBT, band_sweep_smem(segmax, a.W), st>>>(a, d.ctrl);
   ++launches;
   {
     const int64_t nt = (a.nbd + 1 + kCornerTile - 1) / kCornerTile;
@@ -1060,18 +1232,31 @@ int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
     k_band_corner<<<std::max(blocks, 1), 128, 0, st>>>(a, d.ctrl);
     ++launches;
   }
-  {
+  if (a.nseg > 1) {
+    // the corner (separator and loop closure) as a dense band: factor, sweep
+    // matrices, forward and backward sweeps of its right-hand side -> x_C
+    const BandArgs c = corner_args(s, d, a);
+    const int64_t total = static_cast<int64_t>(c.nband) * c.nband + c.nband;
+    k_band_corner_load<<<static_cast<int>(std::min<int64_t>((total + 255) / 256, 4096)), 256, 0, st>>>(c, a.Cn,
+                                                                                                   d.ctrl);
+    launch_factor(c, s.band_c, 1, st, d.ctrl);
+    k_band_sweepmat<<<c.npan, kBT, sweepmat_smem(c.W), st>>>(c, d.ctrl);
+    k_band_fwd<<<1, kBT, band_sweep_smem(c.nband, c.W), st>>>(c, d.ctrl);
+    k_band_bwd<<<1, kBT, band_sweep_smem(c.nband, c.W), st>>>(c, d.ctrl);
+    launches += 5;
+  } else {
     const size_t corner = sizeof(float2) * static_cast<size_t>(a.nbd) * (a.nbd + 2);
     k_band_corner_solve<<<1, kCT, std::max<size_t>(corner, 16), st>>>(a, d.ctrl);
     ++launches;
   }
   k_band_tvec<<<std::max((a.nband + 255) / 256, 1), 256, 0, st>>>(a, d.ctrl);
   ++launches;
-  k_band_bwd<<<1, kBT, band_sweep_smem(a.nband, a.W), st>>>(a, d.ctrl);
+  k_band_bwd<<<a.nseg, kBT, band_sweep_smem(segmax, a.W), st>>>(a, d.ctrl);
   ++launches;
   return launches;
 }
 
-int band_launch_count() { return 9; }
+int band_launch_count(const Sizes& s) { return s.band_nseg > 1 ? 13 : 9; }
+
 
 }  // namespace sgba

@@ -831,6 +831,9 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   // distributed shared memory; it reads the float-float copy of S
   sgba::dense_cluster_setup(s.n6, &s.dense_c, &s.dense_smem);
   s.band_rows = s.band_w = s.band_c = s.band_ring = 0;
+  s.band_nseg = 1;
+  s.band_seg_rows = s.band_ring_c = 0;
+  std::vector<int32_t> perm;  // staging of the dissection's permutation (alive until the set-up synchronises)
   int brows = 0, bw = 0;
   const bool banded = sgba::band_shape(P.nf, P.sb_row, P.sb_col, &brows, &bw) != 0;
   // loop-shaped: block bandwidth at most half the free poses (float-float
@@ -843,15 +846,35 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
                      "free intrinsics on a loop-shaped problem (banded float-float solver) are not on this path");
   if (banded && !p->intr_free && (s.dense_c == 0 ? 4 * (bw / 6) <= P.nf : loop_shaped)) {
     // banded reduced system (sequential / loop problems): band + dense border solver
-    int rows = brows, w = bw, c = 0, ring = 0;
-    if (sgba::band_setup(s.n6, rows, w, &c, &ring) > 0) {
+    int rows = brows, w = bw, c = 0, ring = 0, ring_c = 0;
+    // Nested dissection of a loop: the band part is split into two arcs
+    // around a separator one band width long; the arcs are independent bands
+    // (the second in reverse order, so that both meet the separator at their
+    // ends), factored and swept concurrently, and the separator joins the
+    // loop closure in the corner.  Used when both arcs have at least 48 pose
+    // blocks and the corner (at most 48 pose blocks) fits the factor kernel
+    // as a dense band.
+    const int rb = rows / 6, wb = w / 6, nbdb = P.nf - rb;
+    const int m1 = (rb - wb) / 2, m2 = rb - wb - m1;
+    int nseg = 1;
+    if (loop_shaped && m1 >= 48 && m2 >= 48 && wb + nbdb <= 48 &&
+        sgba::band_setup(s.n6, 6 * (rb - wb), w, 2, 6 * std::max(m1, m2), &c, &ring, &ring_c) > 0) {
+      nseg = 2;
+      rows = 6 * (rb - wb);
+    } else if (sgba::band_setup(s.n6, rows, w, 1, rows, &c, &ring, &ring_c) <= 0) {
+      c = 0;
+    }
+    if (c > 0) {
       s.band_rows = rows;
       s.band_w = w;
       s.band_c = c;
       s.band_ring = ring;
+      s.band_nseg = nseg;
+      s.band_seg_rows = nseg > 1 ? 6 * m1 : rows;
+      s.band_ring_c = ring_c;
       s.dense_c = 0;
       const size_t nbd1 = n6 - static_cast<size_t>(rows) + 1;
-      const size_t npan = (static_cast<size_t>(rows) + 23) / 24;
+      const size_t npan = (static_cast<size_t>(rows) + 23) / 24 + 1;  // panels of both segments
       if ((st = dev_alloc(p, &d.band_scl, n6))) return st;
       if ((st = dev_alloc(p, &d.band_L, static_cast<size_t>(rows) * w))) return st;
       if ((st = dev_alloc(p, &d.band_Xinv, npan * 24 * 24))) return st;
@@ -864,6 +887,28 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
       if ((st = dev_alloc(p, &d.band_Zd, nbd1 * rows))) return st;
       if ((st = dev_alloc(p, &d.band_E, nbd1 * nbd1))) return st;
       if ((st = dev_alloc(p, &d.band_xw, n6))) return st;
+      if ((st = dev_alloc(p, &d.band_zlo, nbd1 * 2))) return st;
+      if (nseg > 1) {
+        // the permutation: arc 1 in order, arc 2 reversed, separator, closure
+        std::vector<int32_t> blocks;
+        blocks.reserve(P.nf);
+        for (int b = 0; b < m1; ++b) blocks.push_back(b);
+        for (int b = rb - 1; b >= m1 + wb; --b) blocks.push_back(b);
+        for (int b = m1; b < m1 + wb; ++b) blocks.push_back(b);
+        for (int b = rb; b < P.nf; ++b) blocks.push_back(b);
+        perm.assign(n6, 0);
+        for (size_t nb = 0; nb < blocks.size(); ++nb)
+          for (int k = 0; k < 6; ++k) perm[6 * nb + k] = 6 * blocks[nb] + k;
+        if ((st = dev_upload(p, &d.band_perm, perm))) return st;
+        const size_t mc = nbd1 - 1, npc = (mc + 23) / 24;
+        if ((st = dev_alloc(p, &d.band_Lc, mc * mc))) return st;
+        if ((st = dev_alloc(p, &d.band_Xc, npc * 24 * 24))) return st;
+        if ((st = dev_alloc(p, &d.band_Mfc, npc * 24 * mc))) return st;
+        if ((st = dev_alloc(p, &d.band_Mbc, npc * 24 * mc))) return st;
+        if ((st = dev_alloc(p, &d.band_Zcc, mc))) return st;
+        if ((st = dev_alloc(p, &d.band_Zdc, mc))) return st;
+        if ((st = dev_alloc(p, &d.band_zloc, 1))) return st;
+      }
     }
   }
   // small systems that are not loop-shaped: the one-CTA float-float solver

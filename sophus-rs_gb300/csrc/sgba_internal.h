@@ -197,6 +197,16 @@ struct Dev {
   float2* band_Zd = nullptr;       // (border + 1) x band_rows
   float2* band_E = nullptr;        // (border + 1)^2
   float2* band_xw = nullptr;       // n6
+  // nested dissection of a loop (band_nseg = 2)
+  int32_t* band_perm = nullptr;    // n6: row of the solved system -> row of S (null: identity)
+  int32_t* band_zlo = nullptr;     // (border + 1) x 2: first nonzero column of each border row per segment
+  float2* band_Lc = nullptr;       // corner x corner: the corner as a dense band, then its factor
+  float2* band_Xc = nullptr;       // its panels x 24 x 24
+  float2* band_Mfc = nullptr;      // its sweep matrices
+  float2* band_Mbc = nullptr;
+  float2* band_Zcc = nullptr;      // its right-hand side row (corner)
+  float2* band_Zdc = nullptr;      // its D^-1 z (corner)
+  int32_t* band_zloc = nullptr;    // 1
   float* A = nullptr;              // n6*n6 FP32 factor (lower: unit L)
   float* dpiv = nullptr;           // n6 pivots
   float* wpanel = nullptr;         // n6*64 panel scratch (A_ip L^-T)
@@ -320,6 +330,9 @@ struct Sizes {
   int band_w;         // its band width
   int band_c;         // its cluster size
   int band_ring;      // its row slots per CTA
+  int band_nseg;      // 2: nested dissection (two band segments, the corner = separator + closure)
+  int band_seg_rows;  // rows of the first segment
+  int band_ring_c;    // row slots per CTA of the corner's factor
   int lin_dd;          // float-float linearization (Jacobians, products and Z in float-float)
   int intr_free;       // the camera params are Free: one more 6-row block, last in S
   int intr_nk;         // free params: 4 (pinhole, padded to 6 rows) or 6 (EUCM)
@@ -379,9 +392,9 @@ cudaError_t raise_dynamic_smem(const void* func, size_t bytes);
 // cluster size (0 = no).
 int band_shape(int nf, const std::vector<int32_t>& sb_row, const std::vector<int32_t>& sb_col, int* band_rows,
                int* band_w);
-int band_setup(int n, int nband, int w, int* cluster, int* ring);
+int band_setup(int n, int nband, int w, int nseg, int seg_rows_max, int* cluster, int* ring, int* ring_c);
 int launch_band(const Sizes& s, const Dev& d, cudaStream_t st);
-int band_launch_count();
+int band_launch_count(const Sizes& s);
 // Schur observation-pair lists on the device (sgba_plan.cu): pairs per lower
 // block (atomic counts into totals[nf(nf+1)/2]); then the pair list d.pairs in
 // (block, point) order from the block map, block offsets and a zeroed

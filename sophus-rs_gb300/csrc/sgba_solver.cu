@@ -271,7 +271,7 @@ int solver_launch_count(const Sizes& s) {
   const int pcg = s.pcg_mode ? pcg_launch_count(s) : 0;
   if (s.small_dense) return pcg + 1;
   if (s.dense_c > 0) return pcg + 1;
-  if (s.band_c > 0) return pcg + band_launch_count();
+  if (s.band_c > 0) return pcg + band_launch_count(s);
   const int panels = (s.n6 + kPW - 1) / kPW;
   return pcg + 1 + 2 * panels + 1 + 2 * kRefineSteps;
 }

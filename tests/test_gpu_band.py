@@ -42,10 +42,13 @@ def test_band_solver_is_chosen(pkg):
         lay = gp.layout()
     assert lay.solver == pkg.native.SOLVER_BAND
     assert 0 < lay.band_width <= 6 * 32 and lay.band_width % 6 == 0
-    assert 0 < lay.border_rows <= 6 * 24
+    # nested dissection: the border holds the separator between the two arcs
+    # (one band width) and the loop closure
+    assert lay.band_width < lay.border_rows <= 6 * 48 and lay.border_rows % 6 == 0
     with pkg.native.Problem(_open_path(prob), device=0) as gp:
         lay = gp.layout()
-    assert lay.solver == pkg.native.SOLVER_BAND and lay.border_rows == 0
+    # the cut loop has no closure: the border is the separator alone
+    assert lay.solver == pkg.native.SOLVER_BAND and 0 < lay.border_rows <= lay.band_width
 
 
 @pytest.mark.parametrize("open_path", [False, True])
