@@ -131,7 +131,8 @@ struct BandArgs {
   int npan;   // 24-column panels of A
   int nbd;    // border rows (n - nband)
   int ring;   // row slots per CTA in the factor kernel
-  int nbuf;   // panel buffers of the sweeps (2 or 3)
+  int nbuf;   // panel buffers of the backward sweep (2 or 3)
+  int nbuf_f; // panel buffers of the forward sweep (2 where two CTAs per SM keep its many rows in one wave)
   const double* S;  // n x n, both triangles
   const double* b;  // reduced right-hand side
   float* scl;       // n: D^-1/2
@@ -609,7 +610,7 @@ __global__ void __launch_bounds__(kBT) k_band_fwd(BandArgs a0, const Ctrl* ctrl)
   const int row = static_cast<int>(blockIdx.x) / a0.nseg;
   const BandArgs a = seg_view(a0, sg);
   const int W = a.W;
-  const int nb = a.nbuf;
+  const int nb = a.nbuf_f;
   float2* v = sw;
   float2* mbuf = v + ((a.nband + 1) & ~1);  // nb x kBP x W (16-byte aligned: W is even)
   float2* xb = mbuf + nb * kBP * W;         // nb x kBP x kBP
@@ -867,13 +868,30 @@ __global__ void __launch_bounds__(256) k_band_corner_load(BandArgs ac, const flo
   }
 }
 
-// t_c = Zd_{rhs,c} - sum_i Zd_ic x_Ci for the band columns.
+// t_c = Zd_{rhs,c} - sum_i Zd_ic x_Ci for the band columns.  A CTA takes 32
+// columns (a lane each); its 8 warps split the border rows (warp w the rows
+// i = w mod 8, two accumulators), and warp 0 adds the 8 partial sums in order.
 __global__ void __launch_bounds__(256) k_band_tvec(BandArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.nband; c += gridDim.x * blockDim.x) {
+  __shared__ float2 part[8][32];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int c = blockIdx.x * 32 + lane;
+  Acc a0 = acc_init(dd_make(0.0f, 0.0f)), a1 = a0;
+  if (c < a.nband) {
+    int i = wib;
+    for (; i + 8 < a.nbd; i += 16) {
+      const float2 z0 = a.Zd[static_cast<int64_t>(i) * a.nband + c], z1 = a.Zd[static_cast<int64_t>(i + 8) * a.nband + c];
+      acc_madd(a0, dd_neg(f2dd(z0)), f2dd(a.xw[a.nband + i]));
+      acc_madd(a1, dd_neg(f2dd(z1)), f2dd(a.xw[a.nband + i + 8]));
+    }
+    if (i < a.nbd) acc_madd(a0, dd_neg(f2dd(a.Zd[static_cast<int64_t>(i) * a.nband + c])), f2dd(a.xw[a.nband + i]));
+  }
+  acc_add(a0, acc_get(a1));
+  part[wib][lane] = dd2f(acc_get(a0));
+  __syncthreads();
+  if (wib == 0 && c < a.nband) {
     Acc acc = acc_init(f2dd(a.Zd[static_cast<int64_t>(a.nbd) * a.nband + c]));
-    for (int i = 0; i < a.nbd; ++i)
-      acc_madd(acc, dd_neg(f2dd(a.Zd[static_cast<int64_t>(i) * a.nband + c])), f2dd(a.xw[a.nband + i]));
+    for (int w = 0; w < 8; ++w) acc_add(acc, f2dd(part[w][lane]));
     a.xw[c] = dd2f(acc_get(acc));
   }
 }
@@ -980,6 +998,7 @@ __global__ void __launch_bounds__(kBT) k_band_bwd(BandArgs a0, const Ctrl* ctrl)
 }
 
 int sweep_nbuf(int nband, int W);
+int fwd_nbuf(int nband, int W, int nctas);
 
 BandArgs band_args(const Sizes& s, const Dev& d) {
   BandArgs a{};
@@ -989,7 +1008,6 @@ BandArgs band_args(const Sizes& s, const Dev& d) {
   a.npan = (s.band_rows + kBP - 1) / kBP;
   a.nbd = s.n6 - s.band_rows;
   a.ring = s.band_ring;
-  a.nbuf = sweep_nbuf(a.nband, a.W);
   a.S = d.S;
   a.b = d.rb;
   a.scl = d.band_scl;
@@ -1015,7 +1033,9 @@ BandArgs band_args(const Sizes& s, const Dev& d) {
   a.seg_pan0[0] = 0;
   a.seg_pan0[1] = (a.seg_rows[0] + kBP - 1) / kBP;
   a.npan = a.seg_pan0[1] + (a.nseg > 1 ? (a.seg_rows[1] + kBP - 1) / kBP : 0);
-  a.nbuf = sweep_nbuf(a.seg_rows[0] > a.seg_rows[1] ? a.seg_rows[0] : a.seg_rows[1], a.W);
+  const int segmax = a.seg_rows[0] > a.seg_rows[1] ? a.seg_rows[0] : a.seg_rows[1];
+  a.nbuf = sweep_nbuf(segmax, a.W);
+  a.nbuf_f = fwd_nbuf(segmax, a.W, (a.nbd + 1) * a.nseg);
   a.zlo = d.band_zlo;
   a.out_scaled = nullptr;
   return a;
@@ -1032,6 +1052,7 @@ BandArgs corner_args(const Sizes& s, const Dev& d, const BandArgs& a) {
   c.nbd = 0;
   c.ring = s.band_ring_c;
   c.nbuf = sweep_nbuf(m, m);
+  c.nbuf_f = c.nbuf;
   c.Lb = d.band_Lc;
   c.Xinv = d.band_Xc;
   c.Mf = d.band_Mfc;
@@ -1076,6 +1097,18 @@ size_t sweepmat_smem(int W) {
 
 size_t band_sweep_smem(int nband, int W) {
   return sizeof(float2) * sweep_smem_floats2(nband, W, sweep_nbuf(nband, W));
+}
+
+// The forward sweep runs one CTA per border row and segment: with more CTAs
+// than SMs, two buffers (two CTAs per SM where they fit) keep the rows in one
+// wave; otherwise the deeper prefetch of sweep_nbuf.
+int fwd_nbuf(int nband, int W, int nctas) {
+  if (nctas > 132 && 2 * (sizeof(float2) * sweep_smem_floats2(nband, W, 2) + 1024) <= kSmemLimit) return 2;
+  return sweep_nbuf(nband, W);
+}
+
+size_t fwd_sweep_smem(int nband, int W, int nctas) {
+  return sizeof(float2) * sweep_smem_floats2(nband, W, fwd_nbuf(nband, W, nctas));
 }
 
 }  // namespace
@@ -1224,7 +1257,7 @@ int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
   k_band_sweepmat<<<a.npan, kBT, sweepmat_smem(a.W), st>>>(a, d.ctrl);
   ++launches;
   const int segmax = std::max(a.seg_rows[0], a.seg_rows[1]);
-  k_band_fwd<<<(a.nbd + 1) * a.nseg, kBT, band_sweep_smem(segmax, a.W), st>>>(a, d.ctrl);
+  k_band_fwd<<<(a.nbd + 1) * a.nseg, kBT, fwd_sweep_smem(segmax, a.W, (a.nbd + 1) * a.nseg), st>>>(a, d.ctrl);
   ++launches;
   {
     const int64_t nt = (a.nbd + 1 + kCornerTile - 1) / kCornerTile;
@@ -1249,7 +1282,7 @@ int launch_band(const Sizes& s, const Dev& d, cudaStream_t st) {
     k_band_corner_solve<<<1, kCT, std::max<size_t>(corner, 16), st>>>(a, d.ctrl);
     ++launches;
   }
-  k_band_tvec<<<std::max((a.nband + 255) / 256, 1), 256, 0, st>>>(a, d.ctrl);
+  k_band_tvec<<<std::max((a.nband + 31) / 32, 1), 256, 0, st>>>(a, d.ctrl);
   ++launches;
   k_band_bwd<<<a.nseg, kBT, band_sweep_smem(segmax, a.W), st>>>(a, d.ctrl);
   ++launches;
