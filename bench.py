@@ -8,7 +8,8 @@ run of consecutive cameras of length Geom(0.12) clipped to [3, 25]
 (~2.5M observations), pinhole fx=fy=500, Huber 1 px, camera 0 fixed, initial
 damping 1e-4, 15 LM iterations.  Synthetic, seeded (seed 20261205).  The
 reduced camera system is a band plus the loop-closure border, factored in
-float-float by the banded solver.
+float-float by the banded solver (nested dissection: the loop's two arcs in
+parallel, the separator and the closure in a dense corner).
 
 A "step" is one LM iteration over the whole problem (linearize, Schur
 complement, factor + solve, back-substitute, update, trial cost, decision).
@@ -43,8 +44,8 @@ WORKLOADS = {
     "loop": dict(kind=2, n_cam=1500, n_pt=300000, seed=20261203 + 2, n_iter=15,
                  desc=("loop BA: 1500 SE(3) cams on a r=50 m loop facing outward, 300000 points on a r=60 m "
                        "cylinder, consecutive-camera tracks Geom(0.12) clipped to [3,25] (~2.5M obs), Huber 1 px, "
-                       "nu0=1e-4, 15 LM iterations; banded float-float LDL^T of the reduced camera system, "
-                       "float-float linearization")),
+                       "nu0=1e-4, 15 LM iterations; banded float-float LDL^T of the reduced camera system (nested "
+                       "dissection: two arcs in parallel), float-float linearization")),
     "sphere": dict(kind=1, n_cam=0, n_pt=0, seed=20261203 + 1, n_iter=20,
                    desc=("sphere BA: 100 SE(3) cams (99 free) on a r=6 m Fibonacci sphere, 20000 points in "
                          "[-2,2]^3, each seen by U{10..40} of its visible cams (~499k obs), pinhole "
@@ -194,11 +195,14 @@ def _kernel_bytes(name, lay, prob):
         n6 = 6 * nf
         if getattr(lay, "solver", 0) == 1:
             # banded solver: the band of S read once in f64 (row r: columns r-W+1..r) and the border rows;
-            # the float-float band written (scaled S), read and written back once by the factor, read by the
-            # two sweeps; border rows and the rhs (nbd + 1 rows of the band width) in and out in float-float
+            # the float-float band written (scaled S), read and written back once by the factor, read by
+            # the sweep-matrix kernel, which writes the two per-panel sweep matrices (the band's size each),
+            # read once by each sweep; border rows and the rhs (nbd + 1 rows of the band width) in and out
+            # in float-float; the corner (m x m) written, factored in place and read by its sweep matrices
             nb = n6 - lay.border_rows
             w = lay.band_width
-            return 8 * nb * w + 8 * lay.border_rows * n6 + 8 * nb * w * 5 + 16 * (lay.border_rows + 1) * nb * 2
+            m = lay.border_rows
+            return (8 * nb * w + 8 * m * n6 + 8 * nb * w * 8 + 16 * (m + 1) * nb * 2 + 8 * m * m * 4)
         # single-launch cluster solver: read S once as float-float (8 B per entry) and the
         # reduced rhs (f64); write the step as f64 and as float-float pairs
         return 8 * n6 * n6 + 8 * n6 + 16 * n6
@@ -535,10 +539,15 @@ def main():
                          "benchmark problem (EUCM camera, params free)")
     ap.add_argument("--profile-iters", type=int, default=0,
                     help="profiling mode: only set up the workload and run this many LM iterations")
+    ap.add_argument("--profile-cams", type=int, default=0,
+                    help="profiling mode: the loop workload at this many cameras (200 points per camera), a "
+                         "small case for multi-pass profiler captures")
     args = ap.parse_args()
     if args.profile_iters > 0:
         pkg = _load_pkg()
-        wl = WORKLOADS[args.workload if args.workload in WORKLOADS else DEFAULT_WORKLOAD]
+        wl = dict(WORKLOADS[args.workload if args.workload in WORKLOADS else DEFAULT_WORKLOAD])
+        if args.profile_cams > 0 and wl.get("kind") == 2:
+            wl["n_cam"], wl["n_pt"] = args.profile_cams, 200 * args.profile_cams
         prob = _make_problem(pkg.synth, wl, wl["seed"])
         with pkg.native.Problem(prob, device=0) as gp:
             recs, _ = gp.optimize(_fixed(pkg, args.profile_iters, prob.initial_lm_damping))
@@ -618,9 +627,16 @@ def main():
     if rl_kernel == "factor":
         n6 = 6 * lay.n_free_poses
         if lay.solver == 1:
-            roofline["note"] = ("latency-bound dependency chain: banded float-float LDL^T in one 16-CTA cluster "
-                                "(%d panel steps of 24 pivots), forward/backward sweeps of the same length"
-                                % ((n6 - lay.border_rows + 23) // 24))
+            nb = n6 - lay.border_rows
+            if lay.border_rows > lay.band_width:
+                roofline["note"] = ("latency-bound dependency chains: nested dissection of the loop, two arcs of "
+                                    "~%d panel steps of 24 pivots factored and swept concurrently (one 16-CTA "
+                                    "cluster each), then the %d-row corner as a dense band"
+                                    % ((nb // 2 + 23) // 24, lay.border_rows))
+            else:
+                roofline["note"] = ("latency-bound dependency chain: banded float-float LDL^T in one 16-CTA "
+                                    "cluster (%d panel steps of 24 pivots), forward/backward sweeps of the same "
+                                    "length" % ((nb + 23) // 24))
         elif lay.solver == 3:
             roofline["note"] = ("latency-bound dependency chain: float-float LDL^T of the %d-row reduced system "
                                 "in one CTA, one barrier per pivot" % (n6 + lay.intrinsics_rows))
