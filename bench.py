@@ -381,6 +381,8 @@ def run_windows(args, ws, rank, local):
                     raise RuntimeError("window failed with status %d: %s" % (st, native.last_error()))
                 ms.append(wms)
             launches += sum(int(p.profile().kernel_launches) for p in probs)
+            bstats = native.batch_last_stats()
+            launches += bstats["kernel_launches"]
         dt = _barrier_and_max(time.perf_counter() - t0, ws)
         clk = clocks.stop()
         # per-window solve time: each window optimised alone (one sgba_optimize,
@@ -410,7 +412,8 @@ def run_windows(args, ws, rank, local):
     d2h = sum(a.nbytes + b.nbytes for a, b in res)
     ms = np.array(ms)
     solo = np.array(solo)
-    return dict(value=N_WINDOWS * K * ws / dt, dt=dt, launches=launches, p50=float(np.percentile(solo, 50)),
+    return dict(value=N_WINDOWS * K * ws / dt, dt=dt, launches=launches, batch=bstats,
+                p50=float(np.percentile(solo, 50)),
                 p99=float(np.percentile(solo, 99)), batch_p50=float(np.percentile(ms, 50)),
                 batch_p99=float(np.percentile(ms, 99)), clk=clk, e2e=N_WINDOWS * e2e_steps * ws / e2e_s, h2d=h2d,
                 d2h=d2h, n_obs=int(sum(w.n_obs for w in wins)), wins=wins, params=params, pkg=pkg)
@@ -576,11 +579,18 @@ def main():
             "dtype": "fp32 (Jacobians/products) + float-float sums + f64 update", "data": "synthetic",
             "config": _windows_config(),
             "n_obs_total": out["n_obs"],
-            "window_ms": {"solo_p50": out["p50"], "solo_p99": out["p99"],
-                          "in_batch_finish_p50": out["batch_p50"], "in_batch_finish_p99": out["batch_p99"],
+            "window_ms": {"solo_p50": out["p50"], "solo_p99": out["p99"], "batch_ms": out["batch"]["ms"],
                           "note": "solo: one window optimised alone (10 LM iterations + final linearisation, "
-                                  "device time), 64 windows; in_batch_finish: time from the batch start to each "
-                                  "window's end while all windows share the GPU"},
+                                  "device time), 64 windows; batch_ms: device time of one batched call (all "
+                                  "windows, init to final linearisation)"},
+            "batch": {"batched_windows": out["batch"]["batched_windows"], "schedule": out["batch"]["schedule"],
+                      "groups": out["batch"]["groups"], "order_by_work": bool(out["batch"]["order"]),
+                      "autotuner_settled": out["batch"]["tuned"],
+                      "schedule_ms_per_lm_iteration": out["batch"]["schedule_ms"],
+                      "launches_per_call": out["batch"]["kernel_launches"],
+                      "note": "every kernel of an LM iteration launched once for all windows (one CUDA graph per "
+                              "iteration and window group); the autotuner times one LM iteration per candidate "
+                              "schedule (groups 1/2/4 ordered by work, 1 as given) and keeps the fastest"},
             "gpu_launches": int(out["launches"]),
             "roofline": None,
             "e2e": {"value": out["e2e"], "unit": "windows/s", "h2d_bytes_per_step": int(out["h2d"]),

@@ -167,14 +167,19 @@ int sgba_optimize(sgba_problem *p, const sgba_opt_params *params, sgba_iter_reco
 
 /* Batched optimize_nlls over independent problems (the local windows of a
  * local bundle adjustment, 5-40 cameras each; in the reference one
- * optimize_nlls call per window, crates/sophus_opt/src/nlls.rs):
- * every window is an sgba_problem created as usual; the
- * windows' LM iterations are enqueued on their own streams and run
- * concurrently, with one host synchronisation at the end.  Per window the
- * result is exactly what sgba_optimize would return for it.
+ * optimize_nlls call per window, crates/sophus_opt/src/nlls.rs:73-83):
+ * every window is an sgba_problem created as usual.  Windows on the FP32
+ * linearization with the dense reduced-system solver (pinhole camera, fixed
+ * intrinsics, no PCG) run batched: each kernel of an LM iteration is launched
+ * once for all of them (block b of a launch runs block b - off[w] of window
+ * w's own grid), one CUDA graph per LM iteration and window group; the other
+ * windows run on their own streams alongside.  Per window the result is
+ * exactly what sgba_optimize would return for it.  A batched window's
+ * results[w].ms is the device time of the whole batched run.
  * records: NULL, or n * cap records (window w at records + w * cap);
  * results: n entries.  Returns SGBA_OK when the call itself is well formed;
- * per-window failures are reported in results[w].status. */
+ * per-window failures are reported in results[w].status.
+ * Concurrent calls on one device are serialised. */
 typedef struct {
   int32_t status;       /* sgba_status of this window */
   int32_t termination;  /* sgba_termination */
@@ -184,6 +189,25 @@ typedef struct {
 } sgba_window_result;
 int sgba_batch_optimize(sgba_problem *const *problems, int32_t n, const sgba_opt_params *params,
                         sgba_iter_record *records, int32_t cap, sgba_window_result *results);
+
+/* What the last sgba_batch_optimize call of the process did on its batched
+ * path (no counterpart in the reference).  The schedule -- window groups run
+ * on separate streams, and whether windows are ordered by decreasing work --
+ * never changes a window's results; an online autotuner times one LM
+ * iteration per candidate on the first calls for a shape (window and
+ * observation counts rounded to powers of two) and keeps the fastest. */
+typedef struct {
+  int32_t batched_windows;  /* windows run by the batched launches */
+  int32_t schedule;         /* candidate used for the last iterations */
+  int32_t groups;           /* its window groups (one stream and one graph each) */
+  int32_t order;            /* 1: windows ordered by decreasing work, 0: as given */
+  int32_t tuned;            /* 1: the autotuner has settled on a candidate for this shape */
+  int32_t pad;
+  int64_t kernel_launches;  /* kernels the batched path launched in the call */
+  float ms;                 /* device time of the batched path (init to final linearisation) */
+  float schedule_ms[4];     /* mean time of one LM iteration per candidate (0: not measured) */
+} sgba_batch_stats;
+int sgba_batch_last_stats(sgba_batch_stats *out);
 
 /* Current variables (OptimizationSolution.variables). NULL skips a family. */
 int sgba_get_variables(sgba_problem *p, double *poses, double *points);

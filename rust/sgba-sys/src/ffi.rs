@@ -120,6 +120,21 @@ pub struct sgba_window_result {
     pub final_cost: f64,
 }
 
+/// What the last batched optimisation did on its batched path.
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct sgba_batch_stats {
+    pub batched_windows: i32,
+    pub schedule: i32,
+    pub groups: i32,
+    pub order: i32,
+    pub tuned: i32,
+    pub pad: i32,
+    pub kernel_launches: i64,
+    pub ms: f32,
+    pub schedule_ms: [f32; 4],
+}
+
 /// Sizes of a problem as laid out on the device.
 #[repr(C)]
 #[derive(Clone, Copy, Debug, Default)]
@@ -238,6 +253,7 @@ extern "C" {
         cap: i32,
         results: *mut sgba_window_result,
     ) -> c_int;
+    pub fn sgba_batch_last_stats(out: *mut sgba_batch_stats) -> c_int;
     pub fn sgba_get_variables(p: *mut sgba_problem, poses: *mut f64, points: *mut f64) -> c_int;
     pub fn sgba_get_cost(p: *mut sgba_problem, cost: *mut f64) -> c_int;
     pub fn sgba_set_variables(p: *mut sgba_problem, poses: *const f64, points: *const f64) -> c_int;

@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstddef>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <pthread.h>
@@ -839,8 +840,13 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   // loop-shaped: block bandwidth at most half the free poses (float-float
   // linearization and, even where the dense cluster solver would fit, the
   // float-float band solver: the FP32 factor with refinement leaves ~2e-6 in
-  // the cost of a 100-camera loop)
-  const bool loop_shaped = banded && 2 * (bw / 6) <= P.nf;
+  // the cost of a 100-camera loop).  A reduced system with (nearly) every
+  // block present is dense, whatever split the band search finds (its border
+  // can hold up to 24 pose blocks): local windows of 20-40 cameras that all
+  // see the same points.
+  const int64_t full_blocks = static_cast<int64_t>(P.nf) * (P.nf + 1) / 2;
+  const bool nearly_dense = 10 * static_cast<int64_t>(P.sb_row.size()) > 9 * full_blocks;
+  const bool loop_shaped = banded && 2 * (bw / 6) <= P.nf && !nearly_dense;
   if (loop_shaped && p->intr_free)
     return set_error(SGBA_ERR_UNSUPPORTED,
                      "free intrinsics on a loop-shaped problem (banded float-float solver) are not on this path");
@@ -1513,9 +1519,10 @@ int sgba_bench_iterations(sgba_problem* p, int32_t iters, int32_t flush_l2, doub
   if (!p || !ms_sum) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
   int st = bench_prepare(p, flush_l2 != 0);
   if (st) return st;
+  EventSet events;
   cudaEvent_t a, b;
-  SGBA_CK(cudaEventCreate(&a));
-  SGBA_CK(cudaEventCreate(&b));
+  SGBA_CK(events.create(&a));
+  SGBA_CK(events.create(&b));
   double total = 0.0;
   for (int i = 0; i < iters; ++i) {
     if (flush_l2) SGBA_CK(cudaMemsetAsync(p->flush_buf, i & 0xff, size_t(256) << 20, p->stream));
@@ -1527,8 +1534,6 @@ int sgba_bench_iterations(sgba_problem* p, int32_t iters, int32_t flush_l2, doub
     SGBA_CK(cudaEventElapsedTime(&ms, a, b));
     total += ms;
   }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
   *ms_sum = total;
   if (launches) *launches = static_cast<int64_t>(iters) * p->iter_launches;
   return SGBA_OK;
@@ -1538,9 +1543,10 @@ int sgba_bench_kernel(sgba_problem* p, int32_t kernel, int32_t reps, int32_t flu
   if (!p || !ms_avg || reps < 1) return set_error(SGBA_ERR_INVALID_ARGUMENT, "bad argument");
   int st = bench_prepare(p, flush_l2 != 0);
   if (st) return st;
+  EventSet events;
   cudaEvent_t a, b;
-  SGBA_CK(cudaEventCreate(&a));
-  SGBA_CK(cudaEventCreate(&b));
+  SGBA_CK(events.create(&a));
+  SGBA_CK(events.create(&b));
   double total = 0.0;
   for (int i = 0; i < reps; ++i) {
     if (flush_l2) SGBA_CK(cudaMemsetAsync(p->flush_buf, i & 0xff, size_t(256) << 20, p->stream));
@@ -1553,8 +1559,6 @@ int sgba_bench_kernel(sgba_problem* p, int32_t kernel, int32_t reps, int32_t flu
     SGBA_CK(cudaEventElapsedTime(&ms, a, b));
     total += ms;
   }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
   st = check_launch();
   if (st) return st;
   *ms_avg = total / reps;
@@ -2075,6 +2079,350 @@ int sgba_pcg_evaluate(const sgba_pcg_model* m, sgba_pcg_trainset* h, int32_t ind
   return SGBA_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Batched windows.  The eligible windows of a batch are split into groups;
+// each group's LM iteration is one CUDA graph of batched launches (every
+// kernel once for all windows of the group) on its own stream.  The schedule
+// -- how many groups, and whether windows are ordered by decreasing work --
+// changes only which CTAs run side by side, never what a window computes, so
+// the autotuner below may pick it from timings: on the first calls for a
+// shape (window count and observation count, rounded to powers of two) it
+// times one LM iteration with each candidate schedule (iterations are
+// identical work for every schedule), then keeps the fastest for that shape.
+// SGBA_BATCH_SCHEDULE=<index> forces a candidate.
+// ---------------------------------------------------------------------------
+struct BatchSched {
+  int groups;
+  int order;  // 1: decreasing work, 0: as given
+};
+constexpr BatchSched kSched[] = {{1, 1}, {2, 1}, {4, 1}, {1, 0}};
+constexpr int kNSched = 4;
+
+struct TuneState {
+  double ms[kNSched] = {0, 0, 0, 0};
+  int samples[kNSched] = {0, 0, 0, 0};
+  int best = -1;
+};
+std::mutex g_tune_mu;
+std::map<std::pair<int, int>, TuneState> g_tune;
+
+std::mutex g_batch_stats_mu;
+sgba_batch_stats g_batch_stats{};
+
+// Streams of the batched path on one device (created once, kept).
+struct BatchCtx {
+  std::mutex mu;  // one batched run at a time per device
+  cudaStream_t main = nullptr;
+  cudaStream_t side[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+BatchCtx* batch_ctx(int dev) {
+  static std::mutex mu;
+  static std::map<int, std::unique_ptr<BatchCtx>> ctxs;
+  std::lock_guard<std::mutex> lk(mu);
+  auto& c = ctxs[dev];
+  if (!c) {
+    std::unique_ptr<BatchCtx> b(new BatchCtx());
+    if (cudaStreamCreateWithFlags(&b->main, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    for (auto& x : b->side)
+      if (cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    c = std::move(b);
+  }
+  return c.get();
+}
+
+int ceil_log2(int64_t v) {
+  int k = 0;
+  while ((int64_t(1) << k) < v && k < 62) ++k;
+  return k;
+}
+
+// sgba_optimizer_init's checks and record buffers for a window that the
+// batched launches run (its control block is written by the batch).
+int batch_window_prepare(sgba_problem* p, const sgba_opt_params* prm) {
+  SGBA_CK(cudaSetDevice(p->device));
+  if ((p->plan.nf == 0 && !p->intr_free) || p->plan.nm == 0)
+    return set_error(SGBA_ERR_SCHUR_MISSING_FREE_OR_MARG,
+                     "Schur solver needs free and marginalized variables (free scalars %d, marg scalars %d)",
+                     6 * p->plan.nf + (p->intr_free ? p->sz.intr_nk : 0), 3 * p->plan.nm);
+  if (!std::isfinite(prm->initial_lm_damping))
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "initial_lm_damping is not finite");
+  p->params = *prm;
+  const int cap = std::max(1, prm->num_iterations);
+  if (p->d.record_cap < cap) {
+    if (p->d.records) cudaFree(p->d.records);
+    p->d.records = nullptr;
+    SGBA_CK(cudaMalloc(&p->d.records, sizeof(Record) * cap));
+    p->d.record_cap = cap;
+    if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }
+    if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+  }
+  // the batch reads and writes the window's buffers on its own streams
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  return SGBA_OK;
+}
+
+struct BatchRun {
+  std::vector<size_t> index;  // window -> row of ctrl / recs
+  std::vector<Ctrl> ctrl;
+  std::vector<Record> recs;   // rows x cap
+  float ms = 0.f;
+};
+
+// One schedule's groups: tables and the captured iteration graph of each.
+struct SchedGroups {
+  int sched = -1;
+  std::vector<std::vector<int>> wins;  // per group: windows (indices into the batch list)
+  std::vector<sgba::BatchTables*> tabs;
+  std::vector<cudaGraphExec_t> graphs;
+  std::vector<int> iter_launches;
+};
+
+void sched_destroy(SchedGroups& g, cudaStream_t st) {
+  for (auto x : g.graphs)
+    if (x) cudaGraphExecDestroy(x);
+  for (auto t : g.tabs) sgba::batch_tables_destroy(t, st);
+  g.graphs.clear();
+  g.tabs.clear();
+}
+
+int sched_build(sgba_problem* const* problems, const std::vector<int>& batched, const std::vector<int>& by_work,
+                int sc, int skip_final, BatchCtx* bc, SchedGroups* out) {
+  const BatchSched S = kSched[sc];
+  out->sched = sc;
+  out->wins.assign(S.groups, {});
+  const std::vector<int>& ord = by_work;
+  // decreasing work dealt round robin (similar mixes per group); or as given
+  for (size_t k = 0; k < ord.size(); ++k) {
+    const int item = S.order ? ord[k] : static_cast<int>(k);
+    out->wins[k % S.groups].push_back(item);
+  }
+  for (int g = 0; g < S.groups; ++g) {
+    cudaStream_t st = g == 0 ? bc->main : bc->side[g];
+    std::vector<sgba::BatchWin> bw;
+    for (int item : out->wins[g]) {
+      const sgba_problem* p = problems[batched[item]];
+      bw.push_back(sgba::BatchWin{&p->sz, &p->d});
+    }
+    cudaError_t e = cudaSuccess;
+    sgba::BatchTables* t = bw.empty() ? nullptr : sgba::batch_tables_create(bw, skip_final, st, &e);
+    out->tabs.push_back(t);
+    out->graphs.push_back(nullptr);
+    out->iter_launches.push_back(0);
+    if (!bw.empty() && !t)
+      return set_error(SGBA_ERR_CUDA, "batch tables: %s", cudaGetErrorString(e));
+    if (!t) continue;
+    cudaGraph_t graph = nullptr;
+    SGBA_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    const int nl = sgba::batch_launch_iteration(t, st);
+    cudaError_t ce = cudaStreamEndCapture(st, &graph);
+    if (ce != cudaSuccess) return set_error(SGBA_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&out->graphs[g], graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return set_error(SGBA_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(ce));
+    out->iter_launches[g] = nl;
+  }
+  return SGBA_OK;
+}
+
+int batch_run(sgba_problem* const* problems, const std::vector<int>& batched, const sgba_opt_params* prm, int iters,
+              int cap, BatchRun* run) {
+  const int nb = static_cast<int>(batched.size());
+  const int dev = problems[batched[0]]->device;
+  SGBA_CK(cudaSetDevice(dev));
+  BatchCtx* bc = batch_ctx(dev);
+  if (!bc) return set_error(SGBA_ERR_CUDA, "batch streams could not be created");
+  std::lock_guard<std::mutex> lk(bc->mu);
+  // shape key and the schedule of every iteration
+  int64_t obs = 0;
+  std::vector<int64_t> work(nb);
+  for (int k = 0; k < nb; ++k) {
+    const Sizes& s = problems[batched[k]]->sz;
+    obs += s.no;
+    work[k] = s.no + 128 * s.nchunk;
+  }
+  std::vector<int> by_work(nb);
+  for (int k = 0; k < nb; ++k) by_work[k] = k;
+  std::stable_sort(by_work.begin(), by_work.end(), [&](int a, int b) { return work[a] > work[b]; });
+  const std::pair<int, int> key(ceil_log2(nb), ceil_log2(std::max<int64_t>(obs, 1)));
+  int forced = -1;
+  if (const char* env = std::getenv("SGBA_BATCH_SCHEDULE")) {
+    forced = std::atoi(env);
+    if (forced < 0 || forced >= kNSched) forced = -1;
+  }
+  std::vector<int> plan(iters, 0);
+  std::vector<int> timed(iters, 0);
+  {
+    std::lock_guard<std::mutex> tl(g_tune_mu);
+    TuneState& ts = g_tune[key];
+    if (forced >= 0) {
+      std::fill(plan.begin(), plan.end(), forced);
+    } else if (ts.best >= 0) {
+      std::fill(plan.begin(), plan.end(), ts.best);
+    } else {
+      // iteration 0 untimed; then one timed iteration per unmeasured
+      // candidate; then the best candidate measured before this call
+      // (candidate 0 when none was)
+      std::vector<int> todo;
+      int best = 0;
+      double bm = 1e300;
+      for (int c = 0; c < kNSched; ++c) {
+        if (ts.samples[c] == 0) todo.push_back(c);
+        else if (ts.ms[c] / ts.samples[c] < bm) { bm = ts.ms[c] / ts.samples[c]; best = c; }
+      }
+      plan[0] = todo.empty() ? best : todo[0];
+      size_t t = 0;
+      for (int it = 1; it < iters; ++it) {
+        if (t < todo.size()) { plan[it] = todo[t++]; timed[it] = 1; }
+        else plan[it] = best;
+      }
+    }
+  }
+  // build the schedules this call uses; on every return path the main
+  // stream (which joins every group's stream) is drained before the graphs
+  // and tables go
+  struct Schedules {
+    SchedGroups g[kNSched];
+    cudaStream_t main;
+    ~Schedules() {
+      cudaStreamSynchronize(main);
+      for (auto& x : g) sched_destroy(x, main);
+    }
+  } schedules;
+  schedules.main = bc->main;
+  SchedGroups* sg = schedules.g;
+  int st = SGBA_OK;
+  for (int it = 0; it < iters && st == SGBA_OK; ++it)
+    if (sg[plan[it]].sched < 0)
+      st = sched_build(problems, batched, by_work, plan[it], prm->skip_final_hessian, bc, &sg[plan[it]]);
+  if (st) return st;
+  Ctrl init;
+  std::memset(&init, 0, sizeof(init));
+  init.nu = prm->initial_lm_damping;
+  init.ftol = prm->function_tolerance;
+  init.gtol = prm->gradient_tolerance;
+  init.ptol = prm->parameter_tolerance;
+  init.max_rejects = prm->max_consecutive_rejects;
+  init.num_iterations = prm->num_iterations;
+  init.record_cap = iters;
+  EventSet events;
+  cudaEvent_t ev0, ev1, fork;
+  cudaEvent_t join[4];
+  SGBA_CK(events.create(&ev0));
+  SGBA_CK(events.create(&ev1));
+  SGBA_CK(events.create(&fork));
+  for (auto& j : join) SGBA_CK(events.create(&j));
+  std::vector<cudaEvent_t> itev(iters + 1, nullptr);
+  for (int it = 0; it <= iters; ++it)
+    if ((it < iters && timed[it]) || (it > 0 && timed[it - 1])) SGBA_CK(events.create(&itev[it]));
+  int64_t launches = 0;
+  // fork the groups of schedule sc from the main stream, run fn per group, join
+  auto across = [&](SchedGroups& G, const std::function<int(sgba::BatchTables*, int, cudaStream_t)>& fn) -> cudaError_t {
+    const int ng = static_cast<int>(G.tabs.size());
+    cudaError_t e = cudaEventRecord(fork, bc->main);
+    for (int g = 1; g < ng && e == cudaSuccess; ++g) e = cudaStreamWaitEvent(bc->side[g], fork, 0);
+    for (int g = 0; g < ng && e == cudaSuccess; ++g) {
+      if (!G.tabs[g]) continue;
+      launches += fn(G.tabs[g], g, g == 0 ? bc->main : bc->side[g]);
+      e = cudaGetLastError();
+    }
+    for (int g = 1; g < ng && e == cudaSuccess; ++g) {
+      e = cudaEventRecord(join[g], bc->side[g]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(bc->main, join[g], 0);
+    }
+    return e;
+  };
+  cudaError_t e = cudaEventRecord(ev0, bc->main);
+  SchedGroups& first = sg[plan[0]];
+  if (e == cudaSuccess)
+    e = across(first, [&](sgba::BatchTables* t, int, cudaStream_t s) { return sgba::batch_launch_init(t, init, s); });
+  for (int it = 0; it < iters && e == cudaSuccess; ++it) {
+    if (itev[it]) e = cudaEventRecord(itev[it], bc->main);
+    SchedGroups& G = sg[plan[it]];
+    if (e == cudaSuccess)
+      e = across(G, [&](sgba::BatchTables*, int g, cudaStream_t s) {
+        return cudaGraphLaunch(G.graphs[g], s) == cudaSuccess ? G.iter_launches[g] : 0;
+      });
+    if (e == cudaSuccess && itev[it + 1] && (timed[it])) e = cudaEventRecord(itev[it + 1], bc->main);
+  }
+  SchedGroups& last = sg[plan[iters - 1]];
+  const size_t rows = static_cast<size_t>(nb);
+  const size_t rcap = static_cast<size_t>(std::max(1, cap));
+  Ctrl* d_ctrl = nullptr;
+  Record* d_rec = nullptr;
+  if (e == cudaSuccess)
+    e = across(last, [&](sgba::BatchTables* t, int, cudaStream_t s) { return sgba::batch_launch_final(t, s); });
+  if (e == cudaSuccess) e = cudaEventRecord(ev1, bc->main);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_ctrl, sizeof(Ctrl) * rows, bc->main);
+  if (e == cudaSuccess) e = cudaMallocAsync(&d_rec, sizeof(Record) * rows * rcap, bc->main);
+  // rows: the last schedule's groups in order
+  run->index.assign(static_cast<size_t>(*std::max_element(batched.begin(), batched.end())) + 1, 0);
+  size_t row0 = 0;
+  std::vector<size_t> grow(last.tabs.size(), 0);
+  for (size_t g = 0; g < last.tabs.size(); ++g) {
+    grow[g] = row0;
+    for (size_t k = 0; k < last.wins[g].size(); ++k) run->index[batched[last.wins[g][k]]] = row0 + k;
+    row0 += last.wins[g].size();
+  }
+  if (e == cudaSuccess)
+    e = across(last, [&](sgba::BatchTables* t, int g, cudaStream_t s) {
+      return sgba::batch_launch_collect(t, d_ctrl + grow[g], d_rec + grow[g] * rcap, static_cast<int>(rcap), s);
+    });
+  run->ctrl.resize(rows);
+  run->recs.resize(rows * rcap);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(run->ctrl.data(), d_ctrl, sizeof(Ctrl) * rows, cudaMemcpyDeviceToHost, bc->main);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(run->recs.data(), d_rec, sizeof(Record) * rows * rcap, cudaMemcpyDeviceToHost, bc->main);
+  if (d_ctrl) cudaFreeAsync(d_ctrl, bc->main);
+  if (d_rec) cudaFreeAsync(d_rec, bc->main);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(bc->main);
+  if (e != cudaSuccess) return set_error(SGBA_ERR_CUDA, "batched windows: %s", cudaGetErrorString(e));
+  cudaEventElapsedTime(&run->ms, ev0, ev1);
+  // autotuner: the timed iterations
+  sgba_batch_stats bs{};
+  {
+    std::lock_guard<std::mutex> tl(g_tune_mu);
+    TuneState& ts = g_tune[key];
+    for (int it = 0; it < iters; ++it) {
+      if (!timed[it]) continue;
+      float m = 0.f;
+      if (cudaEventElapsedTime(&m, itev[it], itev[it + 1]) == cudaSuccess) {
+        ts.ms[plan[it]] += m;
+        ts.samples[plan[it]] += 1;
+      }
+    }
+    bool all = true;
+    int best = -1;
+    double bm = 1e300;
+    for (int c = 0; c < kNSched; ++c) {
+      if (ts.samples[c] == 0) { all = false; continue; }
+      const double v = ts.ms[c] / ts.samples[c];
+      bs.schedule_ms[c] = static_cast<float>(v);
+      if (v < bm) { bm = v; best = c; }
+    }
+    if (all && ts.best < 0) ts.best = best;
+    bs.tuned = ts.best >= 0 ? 1 : 0;
+  }
+  bs.batched_windows = nb;
+  bs.schedule = plan[iters - 1];
+  bs.groups = kSched[plan[iters - 1]].groups;
+  bs.order = kSched[plan[iters - 1]].order;
+  bs.kernel_launches = launches;
+  bs.ms = run->ms;
+  {
+    std::lock_guard<std::mutex> sl(g_batch_stats_mu);
+    g_batch_stats = bs;
+  }
+  return SGBA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int sgba_batch_optimize(sgba_problem* const* problems, int32_t n, const sgba_opt_params* prm,
                         sgba_iter_record* records, int32_t cap, sgba_window_result* results) {
   if (!prm || (n > 0 && (!problems || !results))) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
@@ -2082,12 +2430,27 @@ int sgba_batch_optimize(sgba_problem* const* problems, int32_t n, const sgba_opt
   const int iters = std::max(1, prm->num_iterations);
   std::vector<cudaEvent_t> e0(n, nullptr), e1(n, nullptr);
   std::vector<int> live(n, 0);
-  // 1. init and all iterations, every window on its own stream
+  std::vector<int> batched;  // windows run by the batched launches
+  int dev0 = -1;
+  // 0. validation; the windows that the batched launches can run
   for (int w = 0; w < n; ++w) {
     sgba_window_result& r = results[w];
     std::memset(&r, 0, sizeof(r));
     sgba_problem* p = problems[w];
     if (!p) { r.status = set_error(SGBA_ERR_INVALID_ARGUMENT, "window %d: NULL problem", w); continue; }
+    if (dev0 < 0) dev0 = p->device;
+    if (p->device == dev0 && !p->profiling && sgba::batch_eligible(p->sz)) {
+      const int st = batch_window_prepare(p, prm);
+      if (st) { r.status = st; continue; }
+      batched.push_back(w);
+      live[w] = 2;
+    }
+  }
+  // 1. the other windows: init and all iterations, each on its own stream
+  for (int w = 0; w < n; ++w) {
+    sgba_window_result& r = results[w];
+    sgba_problem* p = problems[w];
+    if (!p || live[w] == 2 || r.status) continue;
     if (cudaSetDevice(p->device) != cudaSuccess || cudaEventCreate(&e0[w]) != cudaSuccess ||
         cudaEventCreate(&e1[w]) != cudaSuccess) {
       r.status = set_error(SGBA_ERR_CUDA, "window %d: event creation failed", w);
@@ -2102,9 +2465,17 @@ int sgba_batch_optimize(sgba_problem* const* problems, int32_t n, const sgba_opt
     if (e != cudaSuccess) { r.status = set_error(SGBA_ERR_CUDA, "window %d: %s", w, cudaGetErrorString(e)); continue; }
     live[w] = 1;
   }
-  // 2. per window: the final linearisation of build_solution
+  // 2. the batched windows: every kernel of an iteration once for all of them
+  BatchRun run;
+  if (!batched.empty()) {
+    const int st = batch_run(problems, batched, prm, iters, cap, &run);
+    for (int w : batched) {
+      if (st) { results[w].status = st; live[w] = 0; }
+    }
+  }
+  // 3. the other windows: the final linearisation of build_solution
   for (int w = 0; w < n; ++w) {
-    if (!live[w]) continue;
+    if (live[w] != 1) continue;
     sgba_problem* p = problems[w];
     cudaSetDevice(p->device);
     double nu = 0.0;
@@ -2122,10 +2493,10 @@ int sgba_batch_optimize(sgba_problem* const* problems, int32_t n, const sgba_opt
     p->prof.kernel_launches = 3 + static_cast<int64_t>(iters) * p->iter_launches + final_launches;
     cudaEventRecord(e1[w], p->stream);
   }
-  // 3. collect
+  // 4. collect
   for (int w = 0; w < n; ++w) {
     sgba_window_result& r = results[w];
-    if (live[w]) {
+    if (live[w] == 1) {
       sgba_problem* p = problems[w];
       cudaSetDevice(p->device);
       Ctrl c;
@@ -2148,10 +2519,34 @@ int sgba_batch_optimize(sgba_problem* const* problems, int32_t n, const sgba_opt
             r.status = set_error(SGBA_ERR_CUDA, "window %d: record readback failed", w);
         }
       }
+    } else if (live[w] == 2) {
+      const size_t k = run.index[w];
+      const Ctrl& c = run.ctrl[k];
+      sgba_problem* p = problems[w];
+      r.status = SGBA_OK;
+      r.termination = c.termination;
+      r.n_records = c.step;
+      r.ms = run.ms;
+      r.final_cost = c.merit;
+      if (records && cap > 0) {
+        const int nrec = std::min(std::min(c.step, p->d.record_cap), cap);
+        if (nrec > 0)
+          std::memcpy(records + static_cast<int64_t>(w) * cap, run.recs.data() + k * static_cast<size_t>(cap),
+                      sizeof(Record) * nrec);
+      }
+      p->prof.kernel_launches = 0;  // counted for the whole batch (sgba_batch_last_stats)
+      p->inited = true;
     }
     if (e0[w]) cudaEventDestroy(e0[w]);
     if (e1[w]) cudaEventDestroy(e1[w]);
   }
+  return SGBA_OK;
+}
+
+int sgba_batch_last_stats(sgba_batch_stats* out) {
+  if (!out) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  std::lock_guard<std::mutex> lk(g_batch_stats_mu);
+  *out = g_batch_stats;
   return SGBA_OK;
 }
 

@@ -38,8 +38,11 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
+#include <vector>
 
 #include "sgba_dd.cuh"
 #include "sgba_internal.h"
@@ -58,6 +61,11 @@ constexpr int kMaxOwn = 24;          // row blocks per CTA
 constexpr int kMaxCluster = 16;
 constexpr float kTolRel = 1e-12f;
 constexpr int kRefine = 2;           // refinement steps against the float-float S (at most)
+// Systems of at most kRefineSmallN rows (local windows) refine up to
+// kRefineSmall times: their sweeps are a few panel steps, and two steps left
+// 7.5e-6 of the step in a 34-camera window (relative, outside the gauge).
+constexpr int kRefineSmallN = 240;
+constexpr int kRefineSmall = 4;
 constexpr float kRefineSkip = 1e-9f;  // predicted relative error below which the second one is skipped
 constexpr size_t kSmemLimit = 232448;  // 227 KiB opt-in dynamic shared memory per CTA
 
@@ -118,6 +126,7 @@ struct DenseArgs {
   const int32_t* fb_pose;
   double center[3];
   int npose;         // rows of the free poses (6 n_f; free intrinsics follow them)
+  int refine;        // refinement steps at most (cluster solver)
 };
 
 // the factorization is skipped on termination, on a skipped step and when PCG converged
@@ -739,7 +748,7 @@ __device__ void factor(const Ctx& X, cg::cluster_group& cl, int* flags) {
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl* ctrl) {
+__device__ __forceinline__ void dense_cluster_body(DenseArgs a, Ctrl* ctrl, int bid_, int nblk_) {
   // Every CTA reads the control block before the first cluster barrier and
   // this kernel writes it only after the last one: the early return is
   // uniform across the cluster.
@@ -843,7 +852,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
       factor(X, cl, flags);
     }
   }
-  // x0 = D^-1/2 (LDL^T)^-1 D^-1/2 b in FP32, then kRefine corrections against
+  // x0 = D^-1/2 (LDL^T)^-1 D^-1/2 b in FP32, then up to a.refine corrections against
   // the float-float S; the solution is kept as float-float (xs, xlo) in every CTA.
   solve_forward(X, cl);
   solve_backward(X, cl);
@@ -873,7 +882,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
     }
     dprev = block_max(m);
   }
-  for (int it = 0; it < kRefine; ++it) {
+  for (int it = 0; it < a.refine; ++it) {
     residual(X, a, alpha);
     __syncthreads();
     solve_forward(X, cl);
@@ -889,7 +898,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
       xm = fmaxf(xm, fabsf(v.hi / vd[k]));
     }
     __syncthreads();
-    if (it + 1 < kRefine) {
+    if (it + 1 < a.refine) {
       // the refinement contracts the error by about dm / dprev per step: when
       // the error it predicts after this step, dm^2 / dprev, is below
       // kRefineSkip of the solution (scaled variables), the next step is skipped
@@ -913,6 +922,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
   }
   if (tid == 0 && flags[0]) ctrl->skip = 2;  // NonFinitePivot -> solve failure -> reject
   cl_sync();  // no CTA leaves while another may still read its shared memory
+}
+__global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl* ctrl) {
+  dense_cluster_body(a, ctrl, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -940,7 +952,7 @@ __device__ __forceinline__ dd sd_rcp(dd d) {
   return dd_fast_two_sum(r0, __fmul_rn(r0, e));
 }
 
-__global__ void __launch_bounds__(256, 1) k_small_dense(DenseArgs a, Ctrl* ctrl) {
+__device__ __forceinline__ void small_dense_body(DenseArgs a, Ctrl* ctrl, int bid_, int nblk_) {
   if (skipping(ctrl)) return;
   extern __shared__ __align__(16) float2 sm[];
   const int m = a.n;
@@ -1017,6 +1029,9 @@ __global__ void __launch_bounds__(256, 1) k_small_dense(DenseArgs a, Ctrl* ctrl)
   }
   if (tid == 0 && s_bad) ctrl->skip = 2;  // NonFinitePivot -> solve failure -> reject
 }
+__global__ void __launch_bounds__(256, 1) k_small_dense(DenseArgs a, Ctrl* ctrl) {
+  small_dense_body(a, ctrl, blockIdx.x, gridDim.x);
+}
 
 size_t small_dense_smem(int n) { return sizeof(float2) * (static_cast<size_t>(n) * n + 2 * static_cast<size_t>(n)); }
 
@@ -1092,7 +1107,9 @@ int small_dense_setup(int n) {
   return 1;
 }
 
-int launch_small_dense(const Sizes& s, const Dev& d, cudaStream_t st) {
+namespace {
+
+DenseArgs small_dense_args(const Sizes& s, const Dev& d) {
   DenseArgs a{};
   a.n = s.n6;
   a.P = (s.n6 + kNB - 1) / kNB;
@@ -1100,11 +1117,10 @@ int launch_small_dense(const Sizes& s, const Dev& d, cudaStream_t st) {
   a.b = d.rb;
   a.x = d.x;
   a.xdd = d.xdd;
-  k_small_dense<<<1, 256, small_dense_smem(s.n6), st>>>(a, d.ctrl);
-  return 1;
+  return a;
 }
 
-int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st) {
+DenseArgs dense_cluster_args(const Sizes& s, const Dev& d) {
   DenseArgs a;
   a.n = s.n6;
   a.P = (s.n6 + kNB - 1) / kNB;
@@ -1117,6 +1133,19 @@ int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st) {
   a.fb_pose = d.fb_pose;
   for (int k = 0; k < 3; ++k) a.center[k] = s.gauge_center[k];
   a.npose = 6 * s.nf;
+  a.refine = s.n6 <= kRefineSmallN ? kRefineSmall : kRefine;
+  return a;
+}
+
+}  // namespace
+
+int launch_small_dense(const Sizes& s, const Dev& d, cudaStream_t st) {
+  k_small_dense<<<1, 256, small_dense_smem(s.n6), st>>>(small_dense_args(s, d), d.ctrl);
+  return 1;
+}
+
+int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st) {
+  const DenseArgs a = dense_cluster_args(s, d);
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(s.dense_c);
   cfg.blockDim = dim3(kThreads);
@@ -1131,6 +1160,147 @@ int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st) {
   cfg.numAttrs = 1;
   cudaLaunchKernelEx(&cfg, k_dense_cluster, a, d.ctrl);
   return 1;
+}
+
+
+// ---------------------------------------------------------------------------
+// The dense solver of a batch of windows: the windows on the one-CTA solver
+// in one launch (one CTA each), the others in one cluster launch per cluster
+// size (one cluster each).  Every window runs the kernel body its own launch
+// runs, with its own arguments and control block.
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void __launch_bounds__(256, 1) k_small_dense_w(const DenseArgs* args, Ctrl* const* ctrl,
+                                                          const int32_t* win) {
+  small_dense_body(args[blockIdx.x], ctrl[win[blockIdx.x]], 0, 1);
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_dense_cluster_w(const DenseArgs* args, Ctrl* const* ctrl,
+                                                                 const int32_t* win) {
+  const int i = static_cast<int>(blockIdx.x / cg::this_cluster().num_blocks());
+  dense_cluster_body(args[i], ctrl[win[i]], 0, 1);
+}
+
+struct DenseGroup {
+  int cluster = 0;  // 0: one-CTA solver
+  int count = 0;
+  size_t smem = 0;
+  const DenseArgs* args = nullptr;
+  const int32_t* win = nullptr;
+};
+
+}  // namespace
+
+struct DenseBatch {
+  void* dbuf = nullptr;
+  Ctrl* const* ctrl = nullptr;
+  std::vector<DenseGroup> groups;
+};
+
+DenseBatch* dense_batch_create(const std::vector<BatchWin>& wins, Ctrl* const* ctrl_dev, cudaStream_t st,
+                               cudaError_t* err) {
+  *err = cudaSuccess;
+  // group 0: the one-CTA solver; then one group per cluster size
+  std::vector<int> sizes;
+  std::vector<std::vector<DenseArgs>> args;
+  std::vector<std::vector<int32_t>> win;
+  std::vector<size_t> smem;
+  auto group_of = [&](int c) {
+    for (size_t g = 0; g < sizes.size(); ++g)
+      if (sizes[g] == c) return static_cast<int>(g);
+    sizes.push_back(c);
+    args.emplace_back();
+    win.emplace_back();
+    smem.push_back(0);
+    return static_cast<int>(sizes.size()) - 1;
+  };
+  for (size_t w = 0; w < wins.size(); ++w) {
+    const Sizes& s = *wins[w].s;
+    const Dev& d = *wins[w].d;
+    if (s.small_dense) {
+      const int g = group_of(0);
+      args[g].push_back(small_dense_args(s, d));
+      win[g].push_back(static_cast<int32_t>(w));
+      smem[g] = std::max(smem[g], small_dense_smem(s.n6));
+    } else if (s.dense_c > 0) {
+      const int g = group_of(s.dense_c);
+      args[g].push_back(dense_cluster_args(s, d));
+      win[g].push_back(static_cast<int32_t>(w));
+      smem[g] = std::max(smem[g], s.dense_smem);
+    } else {
+      *err = cudaErrorInvalidValue;
+      return nullptr;
+    }
+  }
+  std::vector<unsigned char> img;
+  auto put = [&](const void* p, size_t n) {
+    const size_t at = (img.size() + 15) / 16 * 16;
+    img.resize(at + n);
+    if (n) std::memcpy(img.data() + at, p, n);
+    return at;
+  };
+  std::vector<size_t> a_at(sizes.size()), w_at(sizes.size());
+  for (size_t g = 0; g < sizes.size(); ++g) {
+    a_at[g] = put(args[g].data(), sizeof(DenseArgs) * args[g].size());
+    w_at[g] = put(win[g].data(), sizeof(int32_t) * win[g].size());
+  }
+  DenseBatch* b = new DenseBatch();
+  b->ctrl = ctrl_dev;
+  cudaError_t e = cudaMallocAsync(&b->dbuf, img.empty() ? 16 : img.size(), st);
+  if (e == cudaSuccess && !img.empty()) e = cudaMemcpyAsync(b->dbuf, img.data(), img.size(), cudaMemcpyHostToDevice, st);
+  for (size_t g = 0; e == cudaSuccess && g < sizes.size(); ++g) {
+    DenseGroup G;
+    G.cluster = sizes[g];
+    G.count = static_cast<int>(args[g].size());
+    G.smem = smem[g];
+    G.args = reinterpret_cast<const DenseArgs*>(static_cast<unsigned char*>(b->dbuf) + a_at[g]);
+    G.win = reinterpret_cast<const int32_t*>(static_cast<unsigned char*>(b->dbuf) + w_at[g]);
+    const void* fn = G.cluster ? reinterpret_cast<const void*>(k_dense_cluster_w)
+                               : reinterpret_cast<const void*>(k_small_dense_w);
+    e = raise_dynamic_smem(fn, G.smem);
+    if (e == cudaSuccess && G.cluster > 8)
+      e = cudaFuncSetAttribute(k_dense_cluster_w, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    b->groups.push_back(G);
+  }
+  if (e != cudaSuccess) {
+    *err = e;
+    dense_batch_destroy(b, st);
+    return nullptr;
+  }
+  return b;
+}
+
+void dense_batch_destroy(DenseBatch* b, cudaStream_t st) {
+  if (!b) return;
+  if (b->dbuf) cudaFreeAsync(b->dbuf, st);
+  delete b;
+}
+
+int launch_dense_batch(const DenseBatch* b, cudaStream_t st) {
+  int n = 0;
+  for (const DenseGroup& G : b->groups) {
+    if (G.count == 0) continue;
+    if (G.cluster == 0) {
+      k_small_dense_w<<<G.count, 256, G.smem, st>>>(G.args, b->ctrl, G.win);
+    } else {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(static_cast<unsigned>(G.cluster * G.count));
+      cfg.blockDim = dim3(kThreads);
+      cfg.dynamicSmemBytes = G.smem;
+      cfg.stream = st;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = G.cluster;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      cudaLaunchKernelEx(&cfg, k_dense_cluster_w, G.args, b->ctrl, G.win);
+    }
+    ++n;
+  }
+  return n;
 }
 
 }  // namespace sgba

@@ -430,6 +430,46 @@ cudaError_t pcg_adam(PcgModel& m, float scale, float lr, float b1, float b2, flo
 cudaError_t pcg_evaluate(const PcgModel* m, PcgTrainSet& t, int idx, int mode, int max_iters, double tol,
                          int* iters, double* relres, int* status, cudaStream_t st);
 
+// ---- batched local windows ----------------------------------------------
+// A batch launches every kernel of an LM iteration once for many independent
+// problems (local windows).  Block b of a batched launch runs block
+// b - off[w] of window w's own grid with window w's arguments and control
+// block (off: prefix sums of the per-window grid sizes), so every window
+// computes exactly what its own launches compute (sgba_kernels.cu,
+// sgba_dense.cu).
+struct BatchWin {
+  const Sizes* s;
+  const Dev* d;
+};
+// 1: the window's iteration runs in batched launches (FP32 linearization with
+// the chunked landmark pass and back-substitution, pinhole camera, fixed
+// intrinsics, the one-CTA or one-cluster dense solver, no PCG).
+int batch_eligible(const Sizes& s);
+// Per-window arguments and block offsets of every batched kernel, uploaded
+// to the device once per call (stream-ordered allocation on st).
+struct BatchTables;
+BatchTables* batch_tables_create(const std::vector<BatchWin>& wins, int skip_final_hessian, cudaStream_t st,
+                                 cudaError_t* err);
+void batch_tables_destroy(BatchTables* t, cudaStream_t st);
+// Initial control blocks (the same for every window), pose tables, cost and
+// merit (sgba_optimizer_init).
+int batch_launch_init(const BatchTables* t, const Ctrl& init, cudaStream_t st);
+// One LM iteration of every window.
+int batch_launch_iteration(const BatchTables* t, cudaStream_t st);
+// build_solution's final linearisation of every window.
+int batch_launch_final(const BatchTables* t, cudaStream_t st);
+// Control blocks and the first cap records of every window into packed
+// device arrays (n Ctrl, n x cap Record).
+int batch_launch_collect(const BatchTables* t, Ctrl* ctrl_out, Record* rec_out, int cap, cudaStream_t st);
+int batch_window_count(const BatchTables* t);
+// The dense solver of a batch (sgba_dense.cu): one launch for the windows on
+// the one-CTA solver, one cluster launch per cluster size.
+struct DenseBatch;
+DenseBatch* dense_batch_create(const std::vector<BatchWin>& wins, Ctrl* const* ctrl_dev, cudaStream_t st,
+                               cudaError_t* err);
+void dense_batch_destroy(DenseBatch* b, cudaStream_t st);
+int launch_dense_batch(const DenseBatch* b, cudaStream_t st);
+
 // Per-term Jacobians (2x6 pose, 2x3 point) of the given (camera, point) pairs
 // at the current variables, as the linearization kernels evaluate them:
 // precision 0 FP32, 1 float-float (sgba_debug_jacobians).

@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
+#include <vector>
 #include <mutex>
 
 #include "sgba_dd.cuh"
@@ -364,11 +366,11 @@ __device__ __forceinline__ void pose_table(const double* T, float* pf, float* pd
 // Pose tables of every camera.  With `begin` set (the first kernel of an LM
 // iteration) thread 0 also opens the iteration: clears the step flags and
 // maxima and the count of points queued for the float-float redo.
-__global__ void k_pose_tables(int nc, const double* __restrict__ poses, float* __restrict__ pose_f,
+__device__ __forceinline__ void pose_tables_body(int nc, const double* __restrict__ poses, float* __restrict__ pose_f,
                               float* __restrict__ pose_dd, const Ctrl* ctrl, int respect_skip, Ctrl* begin,
-                              int32_t* zero_count) {
+                              int32_t* zero_count, int bid_, int nblk_) {
   if (respect_skip ? skipping(ctrl) : halted(ctrl)) return;
-  if (begin && blockIdx.x == 0 && threadIdx.x == 0) {
+  if (begin && bid_ == 0 && threadIdx.x == 0) {
     begin->skip = 0;
     begin->accept = 0;
     begin->max_grad_bits = 0ull;
@@ -377,9 +379,14 @@ __global__ void k_pose_tables(int nc, const double* __restrict__ poses, float* _
     begin->pcg_done = 0;
     if (zero_count) *zero_count = 0;
   }
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int j = bid_ * blockDim.x + threadIdx.x;
   if (j >= nc) return;
   pose_table(poses + 7 * j, pose_f + 12 * j, pose_dd + 24 * j);
+}
+__global__ void k_pose_tables(int nc, const double* __restrict__ poses, float* __restrict__ pose_f,
+                              float* __restrict__ pose_dd, const Ctrl* ctrl, int respect_skip, Ctrl* begin,
+                              int32_t* zero_count) {
+  pose_tables_body(nc, poses, pose_f, pose_dd, ctrl, respect_skip, begin, zero_count, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -413,20 +420,20 @@ __device__ void decide_body(const double* cost_part, int n_cost, const double* u
                             Record* recs, Record* last);
 
 template <bool E>
-__global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* ctrl) {
+__device__ __forceinline__ void cost_body(CostArgs a, const Ctrl* ctrl, int bid_, int nblk_) {
   const dd fx_ = a.intr ? dd_from_double(a.intr[0]) : a.fx, fy_ = a.intr ? dd_from_double(a.intr[1]) : a.fy;
   const dd cx_ = a.intr ? dd_from_double(a.intr[2]) : a.cx, cy_ = a.intr ? dd_from_double(a.intr[3]) : a.cy;
   // EUCM camera: the z = 1 projection is divided by norm
   const CamD camd = E ? cam_dd(a.intr) : CamD{};
   if (a.decide && !halted(ctrl) && skipping(ctrl)) {
     // no trial (gradient tolerance or a failed solve): decide at once
-    if (blockIdx.x == 0) decide_body(a.partials, 0, a.upd_part, a.n_upd, a.decide, a.recs, a.last);
+    if (bid_ == 0) decide_body(a.partials, 0, a.upd_part, a.n_upd, a.decide, a.recs, a.last);
     return;
   }
   if (a.respect_skip ? skipping(ctrl) : halted(ctrl)) return;
   dd acc = dd_make(0.0f, 0.0f);
-  for (int64_t o = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; o < a.no;
-       o += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+  for (int64_t o = bid_ * static_cast<int64_t>(blockDim.x) + threadIdx.x; o < a.no;
+       o += static_cast<int64_t>(nblk_) * blockDim.x) {
     const float* P = a.pose_dd + 24 * a.opose[o];
     const double* pw = a.points + 3 * a.opt[o];
     dd p0 = dd_from_double(pw[0]), p1 = dd_from_double(pw[1]), p2 = dd_from_double(pw[2]);
@@ -472,19 +479,23 @@ __global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* c
   if (w == 0) {
     dd v = (lane < (int)(blockDim.x >> 5)) ? dd_make(sh_hi[lane], sh_lo[lane]) : dd_make(0.0f, 0.0f);
     v = dd_warp_sum(v);
-    if (lane == 0) a.partials[blockIdx.x] = dd_to_double(v);
+    if (lane == 0) a.partials[bid_] = dd_to_double(v);
   }
   if (a.decide) {
     __shared__ bool s_last;
     __threadfence();
-    if (threadIdx.x == 0) s_last = (atomicAdd(&a.decide->cost_ticket, 1) == static_cast<int>(gridDim.x) - 1);
+    if (threadIdx.x == 0) s_last = (atomicAdd(&a.decide->cost_ticket, 1) == static_cast<int>(nblk_) - 1);
     __syncthreads();
     if (s_last) {
       __threadfence();
       if (threadIdx.x == 0) a.decide->cost_ticket = 0;
-      decide_body(a.partials, static_cast<int>(gridDim.x), a.upd_part, a.n_upd, a.decide, a.recs, a.last);
+      decide_body(a.partials, static_cast<int>(nblk_), a.upd_part, a.n_upd, a.decide, a.recs, a.last);
     }
   }
+}
+template <bool E>
+__global__ void __launch_bounds__(kCostThreads) k_cost(CostArgs a, const Ctrl* ctrl) {
+  cost_body<E>(a, ctrl, blockIdx.x, gridDim.x);
 }
 
 // Sum n double partials with one CTA (fixed tree, float-float).
@@ -544,6 +555,7 @@ struct LinArgs {
   double* bm;
   double nu_override;
   int use_override;
+  int nu_ctrl;  // with use_override: take the damping from the control block (batched final pass)
   int* fail;
   // chunked pass (k_landmark_chunks)
   const int32_t* g_pt;
@@ -567,7 +579,7 @@ struct LinArgs {
 };
 
 template <bool E>
-__global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
+__device__ __forceinline__ void landmark_body(LinArgs a, Ctrl* ctrl, int bid_, int nblk_) {
   const CamF cam_ = cam_f(a.intr);
   const CamD camd_ = cam_dd(a.intr);
   (void)cam_; (void)camd_;
@@ -579,11 +591,11 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int warps_per_block = blockDim.x >> 5;
-  const double nu = a.use_override ? a.nu_override : ctrl->nu;
+  const double nu = (a.use_override && !a.nu_ctrl) ? a.nu_override : ctrl->nu;
   double warp_max = 0.0;  // max |neg_grad| of this warp's points
   const int64_t nitems = a.list ? static_cast<int64_t>(*a.list_count) : static_cast<int64_t>(a.np);
-  for (int64_t item = static_cast<int64_t>(blockIdx.x) * warps_per_block + wib; item < nitems;
-       item += static_cast<int64_t>(gridDim.x) * warps_per_block) {
+  for (int64_t item = static_cast<int64_t>(bid_) * warps_per_block + wib; item < nitems;
+       item += static_cast<int64_t>(nblk_) * warps_per_block) {
     const int64_t i = a.list ? static_cast<int64_t>(a.list[item]) : item;
     const int mb = a.pt_mb[i];
     if (mb < 0) continue;  // constant point: no H_mm block
@@ -838,6 +850,10 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
     atomic_max_nonneg(&ctrl->max_grad_bits, m);
   }
 }
+template <bool E>
+__global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
+  landmark_body<E>(a, ctrl, blockIdx.x, gridDim.x);
+}
 
 // Landmark pass by chunks of consecutive points (<= kLmkTerms terms): one
 // thread per term for the Jacobian products, one thread per point for the
@@ -849,7 +865,7 @@ __global__ void __launch_bounds__(256, 2) k_landmark(LinArgs a, Ctrl* ctrl) {
 constexpr int kLmkTerms = 256;
 
 template <bool E>
-__global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) {
+__device__ __forceinline__ void landmark_chunks_body(LinArgs a, Ctrl* ctrl, int bid_, int nblk_) {
   const CamF cam_ = cam_f(a.intr);
   const CamD camd_ = cam_dd(a.intr);
   (void)cam_; (void)camd_;
@@ -861,7 +877,7 @@ __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) 
   const int tid = threadIdx.x;
   const double nu = ctrl->nu;
   double tmax = 0.0;
-  for (int c = blockIdx.x; c < a.nchunk; c += gridDim.x) {
+  for (int c = bid_; c < a.nchunk; c += nblk_) {
     const int p0 = a.chunk_pt[c], p1 = a.chunk_pt[c + 1];
     const int64_t t0 = a.pt_g_begin[p0];
     const int nt = static_cast<int>(a.pt_g_begin[p1] - t0);
@@ -1006,6 +1022,10 @@ __global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) 
     for (int q = 0; q < (int)(blockDim.x >> 5); ++q) m = fmax(m, smax[q]);
     atomic_max_nonneg(&ctrl->max_grad_bits, m);
   }
+}
+template <bool E>
+__global__ void __launch_bounds__(256) k_landmark_chunks(LinArgs a, Ctrl* ctrl) {
+  landmark_chunks_body<E>(a, ctrl, blockIdx.x, gridDim.x);
 }
 
 // The float-float landmark pass of loop-shaped problems by chunks of
@@ -1237,12 +1257,12 @@ struct CamArgs {
 };
 
 template <bool E>
-__global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const Ctrl* ctrl) {
+__device__ __forceinline__ void camera_tiles_body(CamArgs a, const Ctrl* ctrl, int bid_, int nblk_) {
   const CamF cam_ = cam_f(a.intr);
   const CamD camd_ = cam_dd(a.intr);
   (void)cam_; (void)camd_;
   if (halted(ctrl)) return;
-  const int tile = blockIdx.x;
+  const int tile = bid_;
   const int fb = a.tile_fb[tile];
   const float* P = a.pose_f + 12 * a.fb_pose[fb];
   float u[27];
@@ -1337,6 +1357,10 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
     for (int q = 0; q < kTileThreads / 32; ++q) v = dd_add(v, dd_make(sh_hi[k][q], sh_lo[k][q]));
     a.tile_part[static_cast<int64_t>(tile) * kTileVals + k] = dd_to_double(v);
   }
+}
+template <bool E>
+__global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const Ctrl* ctrl) {
+  camera_tiles_body<E>(a, ctrl, blockIdx.x, gridDim.x);
 }
 
 // Float-float linearization of a camera tile: Jacobians, residual weights,
@@ -1433,11 +1457,11 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles_dd(CamArgs a, con
   }
 }
 
-__global__ void __launch_bounds__(64) k_camera_finalize(int nf, const int64_t* fb_tile_begin,
+__device__ __forceinline__ void camera_finalize_body(int nf, const int64_t* fb_tile_begin,
                                                         const double* tile_part, double* ufull, double* bf,
-                                                        double* rb, Ctrl* ctrl, int with_schur) {
+                                                        double* rb, Ctrl* ctrl, int with_schur, int bid_, int nblk_) {
   if (halted(ctrl)) return;
-  const int fb = blockIdx.x;
+  const int fb = bid_;
   const int k = threadIdx.x;
   __shared__ double vals[kTileVals];
   if (k < kTileVals) {
@@ -1478,7 +1502,7 @@ __global__ void __launch_bounds__(64) k_camera_finalize(int nf, const int64_t* f
     // -> reject); every block's maximum is in by then
     __shared__ bool s_last;
     __threadfence();
-    if (k == 0) s_last = (atomicAdd(&ctrl->fin_ticket, 1) == static_cast<int>(gridDim.x) - 1);
+    if (k == 0) s_last = (atomicAdd(&ctrl->fin_ticket, 1) == static_cast<int>(nblk_) - 1);
     __syncthreads();
     if (s_last && k == 0) {
       __threadfence();
@@ -1493,6 +1517,11 @@ __global__ void __launch_bounds__(64) k_camera_finalize(int nf, const int64_t* f
       ctrl->fin_ticket = 0;
     }
   }
+}
+__global__ void __launch_bounds__(64) k_camera_finalize(int nf, const int64_t* fb_tile_begin,
+                                                        const double* tile_part, double* ufull, double* bf,
+                                                        double* rb, Ctrl* ctrl, int with_schur) {
+  camera_finalize_body(nf, fb_tile_begin, tile_part, ufull, bf, rb, ctrl, with_schur, blockIdx.x, gridDim.x);
 }
 
 
@@ -1534,14 +1563,14 @@ __device__ __forceinline__ void load_z(const float* zmat, int g, float* z) {
 // block (heavy blocks are split so no warp walks thousands of pairs): FP32
 // products and per-lane FP32 sums, float-float across lanes, one partial
 // (36 float-float entries) per chunk.
-__global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl) {
+__device__ __forceinline__ void schur_body(SchurArgs a, const Ctrl* ctrl, int bid_, int nblk_) {
   if (skipping(ctrl)) return;
   __shared__ float red[8][36][33];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
-  for (int64_t ch = static_cast<int64_t>(blockIdx.x) * wpb + wib; ch < a.nchunk;
-       ch += static_cast<int64_t>(gridDim.x) * wpb) {
+  for (int64_t ch = static_cast<int64_t>(bid_) * wpb + wib; ch < a.nchunk;
+       ch += static_cast<int64_t>(nblk_) * wpb) {
     float acc[36];
 #pragma unroll
     for (int e = 0; e < 36; ++e) acc[e] = 0.f;
@@ -1578,6 +1607,9 @@ __global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl)
     }
     __syncwarp();
   }
+}
+__global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl) {
+  schur_body(a, ctrl, blockIdx.x, gridDim.x);
 }
 
 // Pass 1 of the float-float linearization: the same chunks, float-float Z and
@@ -1642,14 +1674,14 @@ __global__ void __launch_bounds__(256, 1) k_schur_dd(SchurArgs a, const Ctrl* ct
 // Pass 2, one warp per lower block of S: the block's chunk partials summed in
 // chunk order (float-float), the diagonal U + nu n I added on diagonal
 // blocks; f64 store of both triangles (and the float-float copy).
-__global__ void __launch_bounds__(256) k_schur_reduce(SchurArgs a, const Ctrl* ctrl) {
+__device__ __forceinline__ void schur_reduce_body(SchurArgs a, const Ctrl* ctrl, int bid_, int nblk_) {
   if (skipping(ctrl)) return;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const double nu = ctrl->nu;
-  for (int64_t blk = static_cast<int64_t>(blockIdx.x) * wpb + wib; blk < a.nsb;
-       blk += static_cast<int64_t>(gridDim.x) * wpb) {
+  for (int64_t blk = static_cast<int64_t>(bid_) * wpb + wib; blk < a.nsb;
+       blk += static_cast<int64_t>(nblk_) * wpb) {
     const int j = a.sb_row[blk], k = a.sb_col[blk];
     const int c0 = a.block_chunk_begin[blk], c1 = a.block_chunk_begin[blk + 1];
     for (int e = lane; e < 36; e += 32) {
@@ -1677,6 +1709,9 @@ __global__ void __launch_bounds__(256) k_schur_reduce(SchurArgs a, const Ctrl* c
       }
     }
   }
+}
+__global__ void __launch_bounds__(256) k_schur_reduce(SchurArgs a, const Ctrl* ctrl) {
+  schur_reduce_body(a, ctrl, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1724,15 +1759,15 @@ __device__ __forceinline__ void intr_backsub_term(const BackArgs& a, int mb, dd*
   }
 }
 
-__global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
+__device__ __forceinline__ void backsub_body(BackArgs a, const Ctrl* ctrl, int bid_, int nblk_) {
   if (skipping(ctrl)) return;
   __shared__ float red[8][12][33];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const bool gauge = a.gauge_kind == 1;
-  for (int64_t i = static_cast<int64_t>(blockIdx.x) * wpb + wib; i < a.np;
-       i += static_cast<int64_t>(gridDim.x) * wpb) {
+  for (int64_t i = static_cast<int64_t>(bid_) * wpb + wib; i < a.np;
+       i += static_cast<int64_t>(nblk_) * wpb) {
     const int mb = a.pt_mb[i];
     if (mb < 0) continue;
     dd t[3] = {dd_make(0.f, 0.f), dd_make(0.f, 0.f), dd_make(0.f, 0.f)};
@@ -1845,19 +1880,22 @@ __global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
     __syncwarp();
   }
 }
+__global__ void __launch_bounds__(256) k_backsub(BackArgs a, const Ctrl* ctrl) {
+  backsub_body(a, ctrl, blockIdx.x, gridDim.x);
+}
 
 // Back-substitution by chunks of consecutive points (the landmark pass's
 // chunks): a thread per term forms Z_g^T dx_f and Z_g^T v_f (float-float),
 // then a thread per point sums its terms in order and applies C^-T.  Same
 // arithmetic per term as k_backsub; every lane busy (the loops' tracks of
 // ~8 terms left 3/4 of a warp-per-point kernel idle).
-__global__ void __launch_bounds__(256) k_backsub_chunks(BackArgs a, const int32_t* chunk_pt, int nchunk,
-                                                        const int32_t* g_pt, const Ctrl* ctrl) {
+__device__ __forceinline__ void backsub_chunks_body(BackArgs a, const int32_t* chunk_pt, int nchunk,
+                                                        const int32_t* g_pt, const Ctrl* ctrl, int bid_, int nblk_) {
   if (skipping(ctrl)) return;
   extern __shared__ float bsm[];  // [cap][12]: Z^T dx_f, Z^T v_f as (hi, lo)
   const bool gauge = a.gauge_kind == 1;
   const int tid = threadIdx.x;
-  for (int c = blockIdx.x; c < nchunk; c += gridDim.x) {
+  for (int c = bid_; c < nchunk; c += nblk_) {
     const int p0 = chunk_pt[c], p1 = chunk_pt[c + 1];
     const int64_t t0 = a.pt_g_begin[p0];
     const int nt = static_cast<int>(a.pt_g_begin[p1] - t0);
@@ -1964,6 +2002,10 @@ __global__ void __launch_bounds__(256) k_backsub_chunks(BackArgs a, const int32_
     }
     __syncthreads();
   }
+}
+__global__ void __launch_bounds__(256) k_backsub_chunks(BackArgs a, const int32_t* chunk_pt, int nchunk,
+                                                        const int32_t* g_pt, const Ctrl* ctrl) {
+  backsub_chunks_body(a, chunk_pt, nchunk, g_pt, ctrl, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -2353,12 +2395,12 @@ struct GaugeArgs {
   double* part;  // 2 * gridDim
 };
 
-__global__ void __launch_bounds__(256) k_gauge_partials(GaugeArgs a, const Ctrl* ctrl) {
+__device__ __forceinline__ void gauge_partials_body(GaugeArgs a, const Ctrl* ctrl, int bid_, int nblk_) {
   if (skipping(ctrl)) return;
   dd num = dd_make(0.f, 0.f), den = dd_make(0.f, 0.f);
   const int64_t n = static_cast<int64_t>(a.nf) + a.nm;
-  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n;
-       t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+  for (int64_t t = bid_ * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<int64_t>(nblk_) * blockDim.x) {
     double v[3], u[3], d[3], w;
     if (t < a.nf) {
       const double* T = a.poses + 7 * a.fb_pose[t];
@@ -2393,9 +2435,12 @@ __global__ void __launch_bounds__(256) k_gauge_partials(GaugeArgs a, const Ctrl*
       s0 = dd_add(s0, dd_make(sh[0][q], sh[1][q]));
       s1 = dd_add(s1, dd_make(sh[2][q], sh[3][q]));
     }
-    a.part[2 * blockIdx.x] = dd_to_double(s0);
-    a.part[2 * blockIdx.x + 1] = dd_to_double(s1);
+    a.part[2 * bid_] = dd_to_double(s0);
+    a.part[2 * bid_ + 1] = dd_to_double(s1);
   }
+}
+__global__ void __launch_bounds__(256) k_gauge_partials(GaugeArgs a, const Ctrl* ctrl) {
+  gauge_partials_body(a, ctrl, blockIdx.x, gridDim.x);
 }
 
 
@@ -2432,7 +2477,7 @@ struct UpdArgs {
   const double* bk;
 };
 
-__global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
+__device__ __forceinline__ void apply_update_body(UpdArgs a, Ctrl* ctrl, int bid_, int nblk_) {
   if (skipping(ctrl)) return;
   // gauge coefficient alpha = sum num / sum den over the k_gauge_partials
   // blocks, formed identically in every CTA (fixed order, warp 0)
@@ -2454,11 +2499,11 @@ __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
     }
     __syncthreads();
     alpha = s_alpha;
-    if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->alpha = alpha;
+    if (bid_ == 0 && threadIdx.x == 0) ctrl->alpha = alpha;
   }
   dd sdd = dd_make(0.f, 0.f), sdg = dd_make(0.f, 0.f);
   double mx = 0.0;
-  if (a.intr_free && blockIdx.x == 0 && threadIdx.x == 0) {
+  if (a.intr_free && bid_ == 0 && threadIdx.x == 0) {
     // the intrinsics are a vector space: k + dx_k (no gauge component)
     for (int k = 0; k < a.intr_nk; ++k) {
       const double xk = a.xf[6 * a.nf + k];
@@ -2470,8 +2515,8 @@ __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
     }
   }
   const int64_t n = static_cast<int64_t>(a.nc) + a.np;
-  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n;
-       t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+  for (int64_t t = bid_ * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n;
+       t += static_cast<int64_t>(nblk_) * blockDim.x) {
     if (t < a.nc) {
       const int j = static_cast<int>(t);
       const double* T = a.poses + 7 * j;
@@ -2541,10 +2586,13 @@ __global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
       s1 = dd_add(s1, dd_make(sh[2][q], sh[3][q]));
       m = fmax(m, shm[q]);
     }
-    a.part[2 * blockIdx.x] = dd_to_double(s0);
-    a.part[2 * blockIdx.x + 1] = dd_to_double(s1);
+    a.part[2 * bid_] = dd_to_double(s0);
+    a.part[2 * bid_ + 1] = dd_to_double(s1);
     atomic_max_nonneg(&ctrl->max_step_bits, m);
   }
+}
+__global__ void __launch_bounds__(256) k_apply_update(UpdArgs a, Ctrl* ctrl) {
+  apply_update_body(a, ctrl, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -2639,19 +2687,25 @@ __device__ void decide_body(const double* cost_part, int n_cost, const double* u
 }
 
 // Accepted step: trial state becomes the current state.
-__global__ void k_commit(int nc, int np, int64_t no, const double* poses_t, double* poses,
+__device__ __forceinline__ void commit_body(int nc, int np, int64_t no, const double* poses_t, double* poses,
                          const double* points_t, double* points, const float2* res_t, float2* res,
                          const float2* res_lo_t, float2* res_lo, const double* intr_t, double* intr,
-                         const Ctrl* ctrl) {
+                         const Ctrl* ctrl, int bid_, int nblk_) {
   if (!ctrl->accept) return;
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  const int64_t t0 = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t stride = static_cast<int64_t>(nblk_) * blockDim.x;
+  const int64_t t0 = bid_ * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (intr && t0 < kIntrMax) intr[t0] = intr_t[t0];
   for (int64_t t = t0; t < no; t += stride) res[t] = res_t[t];
   if (res_lo)
     for (int64_t t = t0; t < no; t += stride) res_lo[t] = res_lo_t[t];
   for (int64_t t = t0; t < 7 * static_cast<int64_t>(nc); t += stride) poses[t] = poses_t[t];
   for (int64_t t = t0; t < 3 * static_cast<int64_t>(np); t += stride) points[t] = points_t[t];
+}
+__global__ void k_commit(int nc, int np, int64_t no, const double* poses_t, double* poses,
+                         const double* points_t, double* points, const float2* res_t, float2* res,
+                         const float2* res_lo_t, float2* res_lo, const double* intr_t, double* intr,
+                         const Ctrl* ctrl) {
+  commit_body(nc, np, no, poses_t, poses, points_t, points, res_t, res, res_lo_t, res_lo, intr_t, intr, ctrl, blockIdx.x, gridDim.x);
 }
 
 int cost_grid(int64_t no) {
@@ -2752,6 +2806,7 @@ static LinArgs make_lin_args(const Sizes& s, const Dev& d, double nu_override, b
   la.bm = d.bm;
   la.nu_override = nu_override;
   la.use_override = use_override ? 1 : 0;
+  la.nu_ctrl = 0;
   la.fail = &d.ctrl->fail;
   la.g_pt = d.g_pt;
   la.list = nullptr;
@@ -2801,7 +2856,7 @@ static int launch_camera(const Sizes& s, const Dev& d, int with_schur, cudaStrea
   return 1;
 }
 
-static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
+static BackArgs make_back_args(const Sizes& s, const Dev& d) {
   BackArgs b;
   b.np = s.np;
   b.pt_g_begin = d.pt_g_begin;
@@ -2823,6 +2878,11 @@ static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
   b.um = d.gauge_um;
   b.zk = s.intr_free ? d.intr_zk : nullptr;
   b.k0 = 6 * s.nf;
+  return b;
+}
+
+static int launch_backsub(const Sizes& s, const Dev& d, cudaStream_t st) {
+  const BackArgs b = make_back_args(s, d);
   if (s.nlchunk > 0 && s.bsub_chunks_ok) {
     const int grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
     k_backsub_chunks<<<grid, 256, sizeof(float) * 12 * static_cast<size_t>(s.lmk_cap), st>>>(
@@ -2906,7 +2966,7 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
   return n;
 }
 
-int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
+static SchurArgs make_schur_args(const Sizes& s, const Dev& d) {
   SchurArgs a;
   a.nsb = s.nsb;
   a.sb_row = d.sb_row;
@@ -2924,35 +2984,38 @@ int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
   a.chunk_begin = d.chunk_begin;
   a.block_chunk_begin = d.block_chunk_begin;
   a.part = d.schur_part;
+  return a;
+}
+
+int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
+  const SchurArgs a = make_schur_args(s, d);
   if (s.lin_dd) k_schur_dd<<<warp_grid(s.nchunk, 8, 65536), 256, 0, st>>>(a, d.ctrl);
   else k_schur<<<warp_grid(s.nchunk, 8, 65536), 256, 0, st>>>(a, d.ctrl);
   k_schur_reduce<<<warp_grid(s.nsb, 8, 8192), 256, 0, st>>>(a, d.ctrl);
   return 2 + launch_intr_fill(s, d, st);
 }
 
-int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
-  int n = 0;
-  n += launch_backsub(s, d, st);
-  if (s.gauge_kind == 1) {
-    GaugeArgs g;
-    g.nf = s.nf;
-    g.nm = s.nm;
-    g.fb_pose = d.fb_pose;
-    g.mb_pt = d.mb_pt;
-    g.poses = d.poses;
-    g.points = d.points;
-    g.cnt_f = d.cnt_f;
-    g.cnt_m = d.cnt_m;
-    g.xf = d.x;
-    g.dm = d.dm;
-    g.um = d.gauge_um;
-    g.cx = s.gauge_center[0];
-    g.cy = s.gauge_center[1];
-    g.cz = s.gauge_center[2];
-    g.part = d.part;
-    k_gauge_partials<<<kUpdBlocks, 256, 0, st>>>(g, d.ctrl);
-    n += 1;
-  }
+static GaugeArgs make_gauge_args(const Sizes& s, const Dev& d) {
+  GaugeArgs g;
+  g.nf = s.nf;
+  g.nm = s.nm;
+  g.fb_pose = d.fb_pose;
+  g.mb_pt = d.mb_pt;
+  g.poses = d.poses;
+  g.points = d.points;
+  g.cnt_f = d.cnt_f;
+  g.cnt_m = d.cnt_m;
+  g.xf = d.x;
+  g.dm = d.dm;
+  g.um = d.gauge_um;
+  g.cx = s.gauge_center[0];
+  g.cy = s.gauge_center[1];
+  g.cz = s.gauge_center[2];
+  g.part = d.part;
+  return g;
+}
+
+static UpdArgs make_upd_args(const Sizes& s, const Dev& d) {
   UpdArgs u;
   u.nc = s.nc;
   u.np = s.np;
@@ -2983,7 +3046,17 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
   u.bk = d.intr_sum ? d.intr_sum + kIntrPart : nullptr;
   u.pose_f = d.pose_f;
   u.pose_dd = d.pose_dd;
-  k_apply_update<<<kUpdBlocks, 256, 0, st>>>(u, d.ctrl);
+  return u;
+}
+
+int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
+  int n = 0;
+  n += launch_backsub(s, d, st);
+  if (s.gauge_kind == 1) {
+    k_gauge_partials<<<kUpdBlocks, 256, 0, st>>>(make_gauge_args(s, d), d.ctrl);
+    n += 1;
+  }
+  k_apply_update<<<kUpdBlocks, 256, 0, st>>>(make_upd_args(s, d), d.ctrl);
   ++n;
   return n;
 }
@@ -3010,23 +3083,33 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) 
   }
 }
 
-int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
-  // trial cost (partials after the update partials; the trial pose tables
-  // were written by k_apply_update); its last block runs the LM decision
+// trial cost (partials after the update partials; the trial pose tables
+// were written by k_apply_update); its last block runs the LM decision
+static CostArgs make_decide_args(const Sizes& s, const Dev& d) {
   double* cost_part = d.part + 4 * kUpdBlocks;
-  const int nb = cost_grid(s.no);
   CostArgs a = make_cost_args(s, d, d.points_t, d.res_t, cost_part, 1);
   a.decide = d.ctrl;
   a.upd_part = d.part + 2 * kUpdBlocks;
   a.n_upd = kUpdBlocks;
   a.recs = d.records;
   a.last = d.last_rec;
-  (s.eucm ? k_cost<true> : k_cost<false>)<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
+  return a;
+}
+
+static int commit_grid(const Sizes& s) {
   const int64_t big = s.no > 7 * (int64_t)s.nc ? s.no : 7 * (int64_t)s.nc;
   const int64_t items = big > 3 * (int64_t)s.np ? big : 3 * (int64_t)s.np;
   int cb = static_cast<int>((items + 255) / 256);
   if (cb > 1216) cb = 1216;
   if (cb < 1) cb = 1;
+  return cb;
+}
+
+int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
+  const int nb = cost_grid(s.no);
+  const CostArgs a = make_decide_args(s, d);
+  (s.eucm ? k_cost<true> : k_cost<false>)<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
+  const int cb = commit_grid(s);
   k_commit<<<cb, 256, 0, st>>>(s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res,
                                d.res_lo_t, d.res_lo, s.intr_free ? d.intr_t : nullptr,
                                s.intr_free ? d.intr : nullptr, d.ctrl);
@@ -3225,6 +3308,445 @@ cudaError_t launch_total_cost_noalloc(int32_t nc, const double* poses, int32_t n
   k_cost_noalloc<<<nb, kCostThreads, 0, st>>>(a, nc, np);
   k_noalloc_finish<<<1, 256, 0, st>>>(part, nb, cost);
   return cudaGetLastError();
+}
+
+
+// ---------------------------------------------------------------------------
+// Batched local windows: each kernel of an LM iteration launched once for all
+// windows of a batch.  Block b of a batched launch is block b - off[w] of
+// window w's own grid (off: prefix sums of the per-window grid sizes), run
+// with window w's arguments and control block by the same kernel body, so
+// each window computes bit for bit what its own launches compute.
+// ---------------------------------------------------------------------------
+namespace {
+
+template <class A>
+struct WinTab {
+  const A* args;       // per window
+  Ctrl* const* ctrl;   // per window
+  const int32_t* off;  // n + 1 prefix sums of the per-window grid sizes
+  int n;
+};
+
+// the window of batched block b: the largest w with off[w] <= b (windows
+// without blocks in this launch have off[w] == off[w + 1] and are skipped)
+__device__ __forceinline__ int win_of(const int32_t* off, int n, int b) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= b) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+struct WinPos {
+  int w, b, nb;
+};
+template <class A>
+__device__ __forceinline__ WinPos win_pos(const WinTab<A>& t) {
+  const int w = win_of(t.off, t.n, static_cast<int>(blockIdx.x));
+  const int o = __ldg(t.off + w);
+  return WinPos{w, static_cast<int>(blockIdx.x) - o, __ldg(t.off + w + 1) - o};
+}
+
+struct PoseTabArgs {
+  int nc;
+  const double* poses;
+  float* pose_f;
+  float* pose_dd;
+  int respect_skip;
+  int begin;  // open the iteration (the window's control block)
+  int32_t* zero_count;
+};
+struct FinArgs {
+  int nf;
+  const int64_t* fb_tile_begin;
+  const double* tile_part;
+  double* ufull;
+  double* bf;
+  double* rb;
+  int with_schur;
+};
+struct BsubArgs {
+  BackArgs b;
+  const int32_t* chunk_pt;
+  int nchunk;
+  const int32_t* g_pt;
+};
+struct MeritArgs {
+  const double* part;
+  int n;
+};
+struct CommitArgs {
+  int nc, np;
+  int64_t no;
+  const double* poses_t;
+  double* poses;
+  const double* points_t;
+  double* points;
+  const float2* res_t;
+  float2* res;
+  const float2* res_lo_t;
+  float2* res_lo;
+  const double* intr_t;
+  double* intr;
+};
+
+__global__ void __launch_bounds__(128) k_pose_tables_w(WinTab<PoseTabArgs> t) {
+  const WinPos q = win_pos(t);
+  const PoseTabArgs a = t.args[q.w];
+  Ctrl* c = t.ctrl[q.w];
+  pose_tables_body(a.nc, a.poses, a.pose_f, a.pose_dd, c, a.respect_skip, a.begin ? c : nullptr, a.zero_count, q.b,
+                   q.nb);
+}
+template <bool E>
+__global__ void __launch_bounds__(kCostThreads) k_cost_w(WinTab<CostArgs> t) {
+  const WinPos q = win_pos(t);
+  cost_body<E>(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
+}
+__global__ void k_init_merit_w(WinTab<MeritArgs> t) {
+  const WinPos q = win_pos(t);
+  const MeritArgs a = t.args[q.w];
+  const double v = block_sum_partials(a.part, a.n);
+  if (threadIdx.x == 0) {
+    Ctrl* c = t.ctrl[q.w];
+    c->merit = v;
+    c->new_merit = v;
+  }
+}
+template <bool E>
+__global__ void __launch_bounds__(256, 2) k_landmark_w(WinTab<LinArgs> t) {
+  const WinPos q = win_pos(t);
+  landmark_body<E>(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
+}
+template <bool E>
+__global__ void __launch_bounds__(256) k_landmark_chunks_w(WinTab<LinArgs> t) {
+  const WinPos q = win_pos(t);
+  landmark_chunks_body<E>(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
+}
+template <bool E>
+__global__ void __launch_bounds__(kTileThreads) k_camera_tiles_w(WinTab<CamArgs> t) {
+  const WinPos q = win_pos(t);
+  camera_tiles_body<E>(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
+}
+__global__ void __launch_bounds__(64) k_camera_finalize_w(WinTab<FinArgs> t) {
+  const WinPos q = win_pos(t);
+  const FinArgs a = t.args[q.w];
+  camera_finalize_body(a.nf, a.fb_tile_begin, a.tile_part, a.ufull, a.bf, a.rb, t.ctrl[q.w], a.with_schur, q.b,
+                       q.nb);
+}
+__global__ void __launch_bounds__(256, 2) k_schur_w(WinTab<SchurArgs> t) {
+  const WinPos q = win_pos(t);
+  schur_body(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
+}
+__global__ void __launch_bounds__(256) k_schur_reduce_w(WinTab<SchurArgs> t) {
+  const WinPos q = win_pos(t);
+  schur_reduce_body(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
+}
+__global__ void __launch_bounds__(256) k_backsub_chunks_w(WinTab<BsubArgs> t) {
+  const WinPos q = win_pos(t);
+  const BsubArgs& a = t.args[q.w];
+  backsub_chunks_body(a.b, a.chunk_pt, a.nchunk, a.g_pt, t.ctrl[q.w], q.b, q.nb);
+}
+__global__ void __launch_bounds__(256) k_gauge_partials_w(WinTab<GaugeArgs> t) {
+  const WinPos q = win_pos(t);
+  gauge_partials_body(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
+}
+__global__ void __launch_bounds__(256) k_apply_update_w(WinTab<UpdArgs> t) {
+  const WinPos q = win_pos(t);
+  apply_update_body(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
+}
+__global__ void k_commit_w(WinTab<CommitArgs> t) {
+  const WinPos q = win_pos(t);
+  const CommitArgs a = t.args[q.w];
+  commit_body(a.nc, a.np, a.no, a.poses_t, a.poses, a.points_t, a.points, a.res_t, a.res, a.res_lo_t, a.res_lo,
+              a.intr_t, a.intr, t.ctrl[q.w], q.b, q.nb);
+}
+// control blocks of every window from one template (the batch shares its params)
+__global__ void k_ctrl_init_w(Ctrl init, Ctrl* const* ctrl, int n) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < n) *ctrl[w] = init;
+}
+// control blocks and the first cap records of every window into packed arrays
+__global__ void k_collect_w(Ctrl* const* ctrl, Record* const* recs, const int* rec_cap, int n, Ctrl* out,
+                            Record* rout, int cap) {
+  const int w = blockIdx.x;
+  if (w >= n) return;
+  const Ctrl* c = ctrl[w];
+  if (threadIdx.x == 0) out[w] = *c;
+  int nr = c->step < rec_cap[w] ? c->step : rec_cap[w];
+  if (nr > cap) nr = cap;
+  for (int r = threadIdx.x; r < nr; r += blockDim.x) rout[static_cast<int64_t>(w) * cap + r] = recs[w][r];
+}
+
+// One batched kernel's device table and launch shape.
+struct KTab {
+  const void* args = nullptr;
+  const int32_t* off = nullptr;
+  int blocks = 0;
+  size_t smem = 0;
+};
+
+}  // namespace
+
+struct BatchTables {
+  int n = 0;
+  void* dbuf = nullptr;
+  Ctrl** ctrl = nullptr;     // device: n control blocks
+  Record** recs = nullptr;   // device: n record buffers
+  int* rec_cap = nullptr;    // device: n record capacities
+  KTab pose_it, lmk_chunks, lmk_slow, cam, fin, schur, schur_red, bsub, gauge, upd, cost, commit;
+  KTab pose_init, cost_init, merit;
+  KTab pose_fin, lmk_fin, cam_fin, fin_fin;
+  DenseBatch* dense = nullptr;
+};
+
+int batch_eligible(const Sizes& s) {
+  return (!s.lin_dd && !s.eucm && !s.intr_free && !s.pcg_mode && s.band_c == 0 && (s.small_dense || s.dense_c > 0) &&
+          s.nlchunk > 0 && s.bsub_chunks_ok && s.ntiles > 0 && s.nf > 0)
+             ? 1
+             : 0;
+}
+
+int batch_window_count(const BatchTables* t) { return t ? t->n : 0; }
+
+namespace {
+
+// Host staging of the tables: one byte image, uploaded at once.
+struct TabImage {
+  std::vector<unsigned char> bytes;
+  size_t put(const void* p, size_t n) {
+    const size_t at = (bytes.size() + 15) / 16 * 16;
+    bytes.resize(at + n);
+    if (n) std::memcpy(bytes.data() + at, p, n);
+    return at;
+  }
+};
+
+// Collects one kernel's per-window arguments and grid sizes.
+template <class A>
+struct TabBuild {
+  std::vector<A> args;
+  std::vector<int32_t> off{0};
+  size_t smem = 0;
+  void add(const A& a, int blocks, size_t sm = 0) {
+    args.push_back(a);
+    off.push_back(off.back() + (blocks > 0 ? blocks : 0));
+    if (blocks > 0 && sm > smem) smem = sm;
+  }
+  void stage(TabImage& im, size_t* a_at, size_t* o_at) const {
+    *a_at = im.put(args.data(), sizeof(A) * args.size());
+    *o_at = im.put(off.data(), sizeof(int32_t) * off.size());
+  }
+};
+
+}  // namespace
+
+BatchTables* batch_tables_create(const std::vector<BatchWin>& wins, int skip_final_hessian, cudaStream_t st,
+                                 cudaError_t* err) {
+  *err = cudaSuccess;
+  const int n = static_cast<int>(wins.size());
+  TabBuild<PoseTabArgs> t_pose_it, t_pose_init, t_pose_fin;
+  TabBuild<LinArgs> t_lmk_chunks, t_lmk_slow, t_lmk_fin;
+  TabBuild<CamArgs> t_cam, t_cam_fin;
+  TabBuild<FinArgs> t_fin, t_fin_fin;
+  TabBuild<SchurArgs> t_schur, t_schur_red;
+  TabBuild<BsubArgs> t_bsub;
+  TabBuild<GaugeArgs> t_gauge;
+  TabBuild<UpdArgs> t_upd;
+  TabBuild<CostArgs> t_cost, t_cost_init;
+  TabBuild<CommitArgs> t_commit;
+  TabBuild<MeritArgs> t_merit;
+  std::vector<Ctrl*> ctrl(n);
+  std::vector<Record*> recs(n);
+  std::vector<int> rec_cap(n);
+  for (int w = 0; w < n; ++w) {
+    const Sizes& s = *wins[w].s;
+    const Dev& d = *wins[w].d;
+    ctrl[w] = d.ctrl;
+    recs[w] = d.records;
+    rec_cap[w] = d.record_cap;
+    const int pose_grid = (s.nc + 127) / 128;
+    const int lmk_grid = s.nlchunk < 8192 ? s.nlchunk : 8192;
+    // iteration (enqueue_iteration: launch_linearize, launch_schur,
+    // launch_factor_solve, launch_update, launch_decide)
+    t_pose_it.add(PoseTabArgs{s.nc, d.poses, d.pose_f, d.pose_dd, 0, 1, d.slow_count}, pose_grid);
+    const LinArgs la = make_lin_args(s, d, 0.0, false);
+    t_lmk_chunks.add(la, lmk_grid, sizeof(float) * 9 * static_cast<size_t>(s.lmk_cap));
+    LinArgs lb = la;
+    lb.list = d.slow_list;
+    lb.list_count = d.slow_count;
+    t_lmk_slow.add(lb, s.lmk_list_grid);
+    t_cam.add(make_cam_args(s, d, 1), static_cast<int>(s.ntiles));
+    t_fin.add(FinArgs{s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf, d.rb, 1}, s.nf);
+    const SchurArgs sa = make_schur_args(s, d);
+    t_schur.add(sa, warp_grid(s.nchunk, 8, 65536));
+    t_schur_red.add(sa, warp_grid(s.nsb, 8, 8192));
+    t_bsub.add(BsubArgs{make_back_args(s, d), d.lmk_chunk_pt, s.nlchunk, d.g_pt}, lmk_grid,
+               sizeof(float) * 12 * static_cast<size_t>(s.lmk_cap));
+    t_gauge.add(make_gauge_args(s, d), s.gauge_kind == 1 ? kUpdBlocks : 0);
+    t_upd.add(make_upd_args(s, d), kUpdBlocks);
+    t_cost.add(make_decide_args(s, d), cost_grid(s.no));
+    t_commit.add(CommitArgs{s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res, d.res_lo_t,
+                            d.res_lo, nullptr, nullptr},
+                 commit_grid(s));
+    // init (launch_init_merit)
+    t_pose_init.add(PoseTabArgs{s.nc, d.poses, d.pose_f, d.pose_dd, 0, 0, nullptr}, pose_grid);
+    t_cost_init.add(make_cost_args(s, d, d.points, d.res, d.part, 0), cost_grid(s.no));
+    t_merit.add(MeritArgs{d.part, cost_grid(s.no)}, 1);
+    // final linearisation (launch_linearize with the damping override)
+    t_pose_fin.add(PoseTabArgs{s.nc, d.poses, d.pose_f, d.pose_dd, 0, 0, nullptr}, pose_grid);
+    LinArgs lf = make_lin_args(s, d, 0.0, true);
+    lf.nu_ctrl = skip_final_hessian ? 1 : 0;
+    t_lmk_fin.add(lf, warp_grid(s.np, 8, 4096));
+    t_cam_fin.add(make_cam_args(s, d, 0), static_cast<int>(s.ntiles));
+    t_fin_fin.add(FinArgs{s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf, d.rb, 0}, s.nf);
+  }
+  TabImage im;
+  const size_t ctrl_at = im.put(ctrl.data(), sizeof(Ctrl*) * n);
+  const size_t recs_at = im.put(recs.data(), sizeof(Record*) * n);
+  const size_t cap_at = im.put(rec_cap.data(), sizeof(int) * n);
+  struct Pending {
+    KTab* k;
+    size_t a_at, o_at;
+  };
+  BatchTables* T = new BatchTables();
+  std::vector<Pending> pend;
+  auto stage = [&](auto& tb, KTab* k) {
+    Pending p{k, 0, 0};
+    tb.stage(im, &p.a_at, &p.o_at);
+    k->blocks = tb.off.back();
+    k->smem = tb.smem;
+    pend.push_back(p);
+  };
+  stage(t_pose_it, &T->pose_it);
+  stage(t_lmk_chunks, &T->lmk_chunks);
+  stage(t_lmk_slow, &T->lmk_slow);
+  stage(t_cam, &T->cam);
+  stage(t_fin, &T->fin);
+  stage(t_schur, &T->schur);
+  stage(t_schur_red, &T->schur_red);
+  stage(t_bsub, &T->bsub);
+  stage(t_gauge, &T->gauge);
+  stage(t_upd, &T->upd);
+  stage(t_cost, &T->cost);
+  stage(t_commit, &T->commit);
+  stage(t_pose_init, &T->pose_init);
+  stage(t_cost_init, &T->cost_init);
+  stage(t_merit, &T->merit);
+  stage(t_pose_fin, &T->pose_fin);
+  stage(t_lmk_fin, &T->lmk_fin);
+  stage(t_cam_fin, &T->cam_fin);
+  stage(t_fin_fin, &T->fin_fin);
+  T->n = n;
+  cudaError_t e = cudaMallocAsync(&T->dbuf, im.bytes.size() > 0 ? im.bytes.size() : 16, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(T->dbuf, im.bytes.data(), im.bytes.size(), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) {
+    *err = e;
+    if (T->dbuf) cudaFreeAsync(T->dbuf, st);
+    delete T;
+    return nullptr;
+  }
+  unsigned char* base = static_cast<unsigned char*>(T->dbuf);
+  T->ctrl = reinterpret_cast<Ctrl**>(base + ctrl_at);
+  T->recs = reinterpret_cast<Record**>(base + recs_at);
+  T->rec_cap = reinterpret_cast<int*>(base + cap_at);
+  for (const Pending& p : pend) {
+    p.k->args = base + p.a_at;
+    p.k->off = reinterpret_cast<const int32_t*>(base + p.o_at);
+  }
+  // dynamic shared memory limits of the batched kernels (per function and
+  // device, only ever raised)
+  if ((T->lmk_chunks.smem > 48 * 1024 &&
+       raise_dynamic_smem(reinterpret_cast<const void*>(k_landmark_chunks_w<false>), T->lmk_chunks.smem) !=
+           cudaSuccess) ||
+      (T->bsub.smem > 48 * 1024 &&
+       raise_dynamic_smem(reinterpret_cast<const void*>(k_backsub_chunks_w), T->bsub.smem) != cudaSuccess)) {
+    *err = cudaErrorInvalidValue;
+    batch_tables_destroy(T, st);
+    return nullptr;
+  }
+  T->dense = dense_batch_create(wins, T->ctrl, st, &e);
+  if (!T->dense) {
+    *err = e != cudaSuccess ? e : cudaErrorInvalidValue;
+    batch_tables_destroy(T, st);
+    return nullptr;
+  }
+  return T;
+}
+
+void batch_tables_destroy(BatchTables* t, cudaStream_t st) {
+  if (!t) return;
+  if (t->dense) dense_batch_destroy(t->dense, st);
+  if (t->dbuf) cudaFreeAsync(t->dbuf, st);
+  delete t;
+}
+
+namespace {
+
+template <class A>
+WinTab<A> wtab(const BatchTables* t, const KTab& k) {
+  return WinTab<A>{static_cast<const A*>(k.args), t->ctrl, k.off, t->n};
+}
+
+}  // namespace
+
+int batch_launch_init(const BatchTables* t, const Ctrl& init, cudaStream_t st) {
+  int n = 0;
+  k_ctrl_init_w<<<(t->n + 127) / 128, 128, 0, st>>>(init, t->ctrl, t->n);
+  ++n;
+  if (t->pose_init.blocks) {
+    k_pose_tables_w<<<t->pose_init.blocks, 128, 0, st>>>(wtab<PoseTabArgs>(t, t->pose_init));
+    ++n;
+  }
+  if (t->cost_init.blocks) {
+    k_cost_w<false><<<t->cost_init.blocks, kCostThreads, 0, st>>>(wtab<CostArgs>(t, t->cost_init));
+    ++n;
+  }
+  if (t->merit.blocks) {
+    k_init_merit_w<<<t->merit.blocks, 256, 0, st>>>(wtab<MeritArgs>(t, t->merit));
+    ++n;
+  }
+  return n;
+}
+
+int batch_launch_iteration(const BatchTables* t, cudaStream_t st) {
+  int n = 0;
+  auto go = [&](const KTab& k) { return k.blocks > 0 ? (++n, true) : false; };
+  if (go(t->pose_it)) k_pose_tables_w<<<t->pose_it.blocks, 128, 0, st>>>(wtab<PoseTabArgs>(t, t->pose_it));
+  if (go(t->lmk_chunks))
+    k_landmark_chunks_w<false>
+        <<<t->lmk_chunks.blocks, 256, t->lmk_chunks.smem, st>>>(wtab<LinArgs>(t, t->lmk_chunks));
+  if (go(t->lmk_slow)) k_landmark_w<false><<<t->lmk_slow.blocks, 256, 0, st>>>(wtab<LinArgs>(t, t->lmk_slow));
+  if (go(t->cam)) k_camera_tiles_w<false><<<t->cam.blocks, kTileThreads, 0, st>>>(wtab<CamArgs>(t, t->cam));
+  if (go(t->fin)) k_camera_finalize_w<<<t->fin.blocks, 64, 0, st>>>(wtab<FinArgs>(t, t->fin));
+  if (go(t->schur)) k_schur_w<<<t->schur.blocks, 256, 0, st>>>(wtab<SchurArgs>(t, t->schur));
+  if (go(t->schur_red)) k_schur_reduce_w<<<t->schur_red.blocks, 256, 0, st>>>(wtab<SchurArgs>(t, t->schur_red));
+  n += launch_dense_batch(t->dense, st);
+  if (go(t->bsub)) k_backsub_chunks_w<<<t->bsub.blocks, 256, t->bsub.smem, st>>>(wtab<BsubArgs>(t, t->bsub));
+  if (go(t->gauge)) k_gauge_partials_w<<<t->gauge.blocks, 256, 0, st>>>(wtab<GaugeArgs>(t, t->gauge));
+  if (go(t->upd)) k_apply_update_w<<<t->upd.blocks, 256, 0, st>>>(wtab<UpdArgs>(t, t->upd));
+  if (go(t->cost)) k_cost_w<false><<<t->cost.blocks, kCostThreads, 0, st>>>(wtab<CostArgs>(t, t->cost));
+  if (go(t->commit)) k_commit_w<<<t->commit.blocks, 256, 0, st>>>(wtab<CommitArgs>(t, t->commit));
+  return n;
+}
+
+int batch_launch_final(const BatchTables* t, cudaStream_t st) {
+  int n = 0;
+  auto go = [&](const KTab& k) { return k.blocks > 0 ? (++n, true) : false; };
+  if (go(t->pose_fin)) k_pose_tables_w<<<t->pose_fin.blocks, 128, 0, st>>>(wtab<PoseTabArgs>(t, t->pose_fin));
+  if (go(t->lmk_fin)) k_landmark_w<false><<<t->lmk_fin.blocks, 256, 0, st>>>(wtab<LinArgs>(t, t->lmk_fin));
+  if (go(t->cam_fin))
+    k_camera_tiles_w<false><<<t->cam_fin.blocks, kTileThreads, 0, st>>>(wtab<CamArgs>(t, t->cam_fin));
+  if (go(t->fin_fin)) k_camera_finalize_w<<<t->fin_fin.blocks, 64, 0, st>>>(wtab<FinArgs>(t, t->fin_fin));
+  return n;
+}
+
+int batch_launch_collect(const BatchTables* t, Ctrl* ctrl_out, Record* rec_out, int cap, cudaStream_t st) {
+  if (t->n == 0) return 0;
+  k_collect_w<<<t->n, 128, 0, st>>>(t->ctrl, t->recs, t->rec_cap, t->n, ctrl_out, rec_out, cap);
+  return 1;
 }
 
 }  // namespace sgba

@@ -126,6 +126,20 @@ class WindowResult(C.Structure):
     ]
 
 
+class BatchStats(C.Structure):
+    _fields_ = [
+        ("batched_windows", C.c_int32),
+        ("schedule", C.c_int32),
+        ("groups", C.c_int32),
+        ("order", C.c_int32),
+        ("tuned", C.c_int32),
+        ("pad", C.c_int32),
+        ("kernel_launches", C.c_int64),
+        ("ms", C.c_float),
+        ("schedule_ms", C.c_float * 4),
+    ]
+
+
 class LinearSolverC(C.Structure):
     _fields_ = [("mode", C.c_int32), ("max_iterations", C.c_int32), ("tolerance", C.c_double)]
 
@@ -152,7 +166,7 @@ EXPORTED = [
     "sgba_optimizer_init", "sgba_optimizer_step", "sgba_optimize", "sgba_get_variables",
     "sgba_get_cost", "sgba_set_variables", "sgba_get_layout", "sgba_export_pattern",
     "sgba_debug_last_system", "sgba_debug_jacobians", "sgba_state_save", "sgba_state_load", "sgba_get_profile",
-    "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_batch_optimize",
+    "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_batch_optimize", "sgba_batch_last_stats",
     "sgba_set_linear_solver", "sgba_get_pcg_stats", "sgba_pcg_num_params", "sgba_pcg_model_create",
     "sgba_pcg_model_destroy", "sgba_pcg_model_set_params", "sgba_pcg_model_get_params",
     "sgba_pcg_trainset_create", "sgba_pcg_trainset_destroy", "sgba_pcg_trainset_size", "sgba_pcg_trainset_add",
@@ -221,6 +235,7 @@ def lib():
     L.sgba_bench_kernel.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, dp]
     L.sgba_batch_optimize.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(OptParamsC),
                                       C.POINTER(IterRecord), C.c_int32, C.POINTER(WindowResult)]
+    L.sgba_batch_last_stats.argtypes = [C.POINTER(BatchStats)]
     L.sgba_set_linear_solver.argtypes = [C.c_void_p, C.POINTER(LinearSolverC), C.c_void_p]
     L.sgba_get_pcg_stats.argtypes = [C.c_void_p, C.POINTER(PcgStats)]
     L.sgba_pcg_num_params.restype = C.c_int32
@@ -483,7 +498,8 @@ def batch_optimize(problems, params):
     """sgba_batch_optimize over Problem handles (independent windows).
 
     Returns one (records, termination, device_ms, final_cost, status) tuple per
-    window; the windows run concurrently, one stream each."""
+    window.  Eligible windows run batched (each kernel of an LM iteration
+    launched once for all of them); the others concurrently, one stream each."""
     n = len(problems)
     cap = max(1, int(params.num_iterations))
     handles = (C.c_void_p * n)(*[p._h for p in problems])
@@ -496,6 +512,16 @@ def batch_optimize(problems, params):
         k = min(r.n_records, cap)
         out.append(([recs[w * cap + i] for i in range(k)], r.termination, r.ms, r.final_cost, r.status))
     return out
+
+
+def batch_last_stats():
+    """sgba_batch_last_stats: the batched path of the last batch_optimize call
+    (windows, schedule, autotuner state, kernel launches, device time)."""
+    st = BatchStats()
+    check(lib().sgba_batch_last_stats(C.byref(st)))
+    return dict(batched_windows=st.batched_windows, schedule=st.schedule, groups=st.groups, order=st.order,
+                tuned=bool(st.tuned), kernel_launches=int(st.kernel_launches), ms=float(st.ms),
+                schedule_ms=[float(x) for x in st.schedule_ms])
 
 
 TRAINED_WEIGHTS = os.path.join(_HERE, "weights", "pcg_mpnn_loop.npz")

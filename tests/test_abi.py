@@ -97,7 +97,8 @@ def test_rust_ffi_declarations_match_the_header():
 _CTYPES_OF = {"sgba_problem_desc": "ProblemDesc", "sgba_opt_params": "OptParamsC", "sgba_iter_record": "IterRecord",
               "sgba_layout": "Layout", "sgba_problem_options": "ProblemOptions", "sgba_profile": "Profile",
               "sgba_window_result": "WindowResult", "sgba_linear_solver": "LinearSolverC",
-              "sgba_pcg_stats": "PcgStats", "sgba_pcg_train_params": "PcgTrainParams"}
+              "sgba_pcg_stats": "PcgStats", "sgba_pcg_train_params": "PcgTrainParams",
+              "sgba_batch_stats": "BatchStats"}
 
 
 def test_python_struct_layouts_match_the_header(pkg, tmp_path):

@@ -1,9 +1,12 @@
 """Batched optimisation of independent local windows (5-40 cameras, 200-4000
 points per window) through sgba_batch_optimize.
 
-Every window must come out exactly as sgba_optimize computes it alone (the
-same kernels on the same data, run concurrently on separate streams), and
-match the oracle per iteration within the parity tolerance."""
+Every window must come out exactly as sgba_optimize computes it alone: the
+batched launches run each window's blocks with the kernel bodies and grids of
+its own launches, so the results are bit-identical whatever the batch holds
+and whichever schedule the autotuner picks; and every window matches the
+oracle per iteration within the parity tolerance."""
+import os
 import numpy as np
 import pytest
 
@@ -24,10 +27,12 @@ def test_batch_equals_single_and_oracle(pkg, oracle):
     probs = [pkg.native.Problem(w, device=0) for w in wins]
     try:
         out = pkg.native.batch_optimize(probs, params)
+        stats = pkg.native.batch_last_stats()
         batch_vars = [p.variables() for p in probs]
     finally:
         for p in probs:
             p.close()
+    assert stats["batched_windows"] == len(wins) and stats["kernel_launches"] > 0
     for w, (recs, term, ms, final_cost, status) in enumerate(out):
         assert status == pkg.native.OK
         assert term == pkg.native.TERM_MAX_ITERATIONS and len(recs) == 10
@@ -38,7 +43,7 @@ def test_batch_equals_single_and_oracle(pkg, oracle):
         assert [r.merit for r in recs] == [r.merit for r in srecs]
         assert np.array_equal(batch_vars[w][0], sposes) and np.array_equal(batch_vars[w][1], spoints)
         assert final_cost == srecs[-1].merit
-    for w in (0, 3):
+    for w in (0, 2, 3):  # 9, 34 and 5 cameras
         orecs, _, _ = oracle.optimize(wins[w], params, n_threads=8)
         g = np.array([r.merit for r in out[w][0]])
         o = np.array([r.merit for r in orecs])
@@ -99,3 +104,65 @@ def test_batch_graph_reuse_and_recapture(pkg):
         with pkg.native.Problem(wins[w], device=0) as gp:
             srecs, _ = gp.optimize(p12)
         assert [r.merit for r in recs] == [r.merit for r in srecs]
+
+
+def _run_batch(pkg, wins, params, free=()):
+    probs = [pkg.native.Problem(w, device=0, intrinsics_free=(k in free)) for k, w in enumerate(wins)]
+    try:
+        out = pkg.native.batch_optimize(probs, params)
+        stats = pkg.native.batch_last_stats()
+        variables = [p.variables() for p in probs]
+    finally:
+        for p in probs:
+            p.close()
+    return out, stats, variables
+
+
+def test_every_schedule_gives_the_same_results(pkg, monkeypatch):
+    """The schedules the autotuner chooses from (window groups on separate
+    streams, windows ordered by work or as given) change only which CTAs run
+    side by side: each one reproduces the windows bit for bit."""
+    wins = _windows(pkg, 9)
+    params = fixed_iter_params(pkg, 5, wins[0].initial_lm_damping)
+    runs = []
+    for sc, groups in enumerate((1, 2, 4, 1)):
+        monkeypatch.setenv("SGBA_BATCH_SCHEDULE", str(sc))
+        out, stats, variables = _run_batch(pkg, wins, params)
+        assert stats["schedule"] == sc and stats["groups"] == groups and stats["batched_windows"] == 9
+        assert all(o[4] == pkg.native.OK for o in out)
+        runs.append((out, variables))
+    monkeypatch.delenv("SGBA_BATCH_SCHEDULE")
+    ref_out, ref_vars = runs[0]
+    for out, variables in runs[1:]:
+        for w in range(len(wins)):
+            assert [r.merit for r in out[w][0]] == [r.merit for r in ref_out[w][0]]
+            assert np.array_equal(variables[w][0], ref_vars[w][0]) and np.array_equal(variables[w][1], ref_vars[w][1])
+
+
+def test_mixed_batch_runs_batched_and_stream_windows(pkg):
+    """Windows the batched launches do not cover (free intrinsics here) run on
+    their own streams in the same call; both kinds equal their single runs."""
+    wins = _windows(pkg, 4)
+    params = fixed_iter_params(pkg, 6, wins[0].initial_lm_damping)
+    out, stats, variables = _run_batch(pkg, wins, params, free=(1, 3))
+    assert stats["batched_windows"] == 2
+    for w, win in enumerate(wins):
+        assert out[w][4] == pkg.native.OK and len(out[w][0]) == 6
+        with pkg.native.Problem(win, device=0, intrinsics_free=(w in (1, 3))) as gp:
+            srecs, _ = gp.optimize(params)
+            sposes, spoints = gp.variables()
+        assert [r.merit for r in out[w][0]] == [r.merit for r in srecs]
+        assert np.array_equal(variables[w][0], sposes) and np.array_equal(variables[w][1], spoints)
+
+
+def test_autotuner_settles_on_the_fastest_schedule(pkg):
+    """With no schedule forced, the first call for a shape times one LM
+    iteration per candidate; the next call runs the fastest of them."""
+    wins = _windows(pkg, 12)
+    params = fixed_iter_params(pkg, 6, wins[0].initial_lm_damping)
+    assert "SGBA_BATCH_SCHEDULE" not in os.environ
+    _, first, _ = _run_batch(pkg, wins, params)
+    _, second, _ = _run_batch(pkg, wins, params)
+    assert second["tuned"] and all(m > 0.0 for m in second["schedule_ms"])
+    assert second["schedule"] == int(np.argmin(second["schedule_ms"]))
+    assert first["batched_windows"] == second["batched_windows"] == 12
