@@ -930,7 +930,7 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   // point blocks keep the FP32 Cholesky while no pivot loses more than three
   // digits; the others are redone in float-float by a 64-CTA pass
   s.lmk_well_tol = 1e-3f;
-  s.lmk_list_grid = 64;
+  s.lmk_list_grid = std::min(64, std::max(4, P.np / 256));  // grid-stride over the queued points: any grid gives the same results
   // Loop-shaped problems (block bandwidth of S at most half the free poses)
   // get the float-float linearization: their reduced systems cancel ~25x in
   // S = U - sum Z Z^T and their bending modes are weakly constrained, so FP32
@@ -944,6 +944,17 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   // FP32 EUCM Jacobians left 7.6e-7 in the cost of the reference's
   // 10-camera benchmark scene.
   s.lin_dd = (loop_shaped || (s.eucm && (p->intr_free || s.small_dense))) ? 1 : 0;
+  // S by tiles of pose blocks when nearly every block of S is present and a
+  // point is seen by at least half the free poses on average (local windows):
+  // each point's Z is then streamed once per tile instead of once per pair
+  s.schur_dense = (!s.lin_dd && !p->intr_free && nearly_dense &&
+                   2 * P.ng >= static_cast<int64_t>(P.np) * static_cast<int64_t>(P.nf))
+                      ? 1
+                      : 0;
+  if (s.schur_dense) {
+    if ((st = dev_alloc(p, &d.zterm, static_cast<size_t>(P.np) * static_cast<size_t>(P.nf)))) return st;
+    SGBA_CK(sgba::zterm_fill(s, d, d.zterm, p->stream));
+  }
   s.lmk_dd_ok = (s.lin_dd && s.nlchunk > 0 && sgba::landmark_dd_setup(s.lmk_cap) == 0) ? 1 : 0;
   s.bsub_chunks_ok = (s.nlchunk > 0 && sgba::backsub_chunks_setup(s.lmk_cap) == 0) ? 1 : 0;
   if (s.lin_dd) {

@@ -928,18 +928,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_dense_cluster(DenseArgs a, Ctrl
 }
 
 // ---------------------------------------------------------------------------
-// Small reduced systems (n <= kSmallMax: local windows of up to 25 cameras):
-// one CTA, S in float-float in shared memory, LDL^T with the PSD-aware pivot
-// rule and the forward substitution of b fused into it (one barrier per pivot:
-// every thread evaluates the pivot itself), then the diagonal and the
-// backward sweep.  Float-float resolves these systems without refinement; the
-// cluster kernel's fixed costs (cluster barriers, a large code footprint that
-// starts cold on each SM) dominate at this size.
+// Small reduced systems (n <= kSmallMax: local windows of up to 40 cameras):
+// one CTA, the lower triangle of S in float-float in shared memory (packed
+// by rows), LDL^T with the PSD-aware pivot rule and the forward substitution
+// of b fused into it (one barrier per pivot: every thread evaluates the pivot
+// itself; the trailing rows are dealt to the warps, a row's entries to the
+// lanes), then the diagonal and the backward sweep.  Float-float resolves
+// these systems without refinement (their scale gauge is held only by the
+// damping, which an FP32 factor with refinement does not resolve for windows
+// of 26-40 cameras); the cluster kernel's fixed costs (cluster barriers, a
+// large code footprint that starts cold on each SM) dominate at this size.
 // ---------------------------------------------------------------------------
-constexpr int kSmallMax = 144;
+constexpr int kSmallMax = 234;
 
 __device__ __forceinline__ dd sd_f2dd(float2 v) { return dd_make(v.x, v.y); }
 __device__ __forceinline__ float2 sd_dd2f(dd v) { return make_float2(v.hi, v.lo); }
+// packed lower triangle: entry (i, q), q <= i
+__device__ __forceinline__ int sd_at(int i, int q) { return i * (i + 1) / 2 + q; }
 
 // 1/d by Newton's iteration from the hardware approximate reciprocal (one
 // FP32 step, one float-float step with an exactly formed residual).
@@ -953,24 +958,24 @@ __device__ __forceinline__ dd sd_rcp(dd d) {
 }
 
 __device__ __forceinline__ void small_dense_body(DenseArgs a, Ctrl* ctrl, int bid_, int nblk_) {
+  (void)bid_;
+  (void)nblk_;
   if (skipping(ctrl)) return;
   extern __shared__ __align__(16) float2 sm[];
   const int m = a.n;
-  float2* A = sm;          // m x m, lower used
-  float2* y = sm + m * m;  // rhs -> z -> x
-  float2* rdv = y + m;     // reciprocal pivots
+  float2* A = sm;                      // lower triangle, packed by rows
+  float2* y = sm + m * (m + 1) / 2;    // rhs -> z -> x
+  float2* rdv = y + m;                 // reciprocal pivots
   __shared__ int s_bad;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_bad = 0;
-  for (int e = tid; e < m * m; e += 256) {
-    const int i = e / m, j = e % m;
-    A[e] = (j <= i) ? a.S2[static_cast<int64_t>(i) * m + j] : make_float2(0.0f, 0.0f);
-  }
+  for (int i = warp; i < m; i += 8)
+    for (int j = lane; j <= i; j += 32) A[sd_at(i, j)] = a.S2[static_cast<int64_t>(i) * m + j];
   for (int i = tid; i < m; i += 256) y[i] = sd_dd2f(dd_from_double(a.b[i]));
   __syncthreads();
   float maxp = 1.0f;
   for (int t = 0; t < m; ++t) {
-    dd dt = sd_f2dd(A[t * m + t]);
+    dd dt = sd_f2dd(A[sd_at(t, t)]);
     if (t % 6 == 0) maxp = 1.0f;  // a new pose block
     const float tol = fmaxf(maxp, 1.0f) * 1e-12f;
     bool bad = false;
@@ -987,38 +992,32 @@ __device__ __forceinline__ void small_dense_body(DenseArgs a, Ctrl* ctrl, int bi
       rdv[t] = sd_dd2f(rd);
       if (bad) s_bad = 1;
     }
-    const int rem = m - t - 1;
     const dd yt = sd_f2dd(y[t]);
-    // trailing entries (i, q), t < q <= i: a_iq -= a_it rd a_qt; rhs y_i -= l_it y_t
-    const int ntri = rem * (rem + 1) / 2;
-    for (int e = tid; e < ntri + rem; e += 256) {
-      if (e < ntri) {
-        int ii = static_cast<int>((__fsqrt_rn(8.0f * static_cast<float>(e) + 1.0f) - 1.0f) * 0.5f);
-        while (ii * (ii + 1) / 2 > e) --ii;
-        while ((ii + 1) * (ii + 2) / 2 <= e) ++ii;
-        const int i = t + 1 + ii, q = t + 1 + (e - ii * (ii + 1) / 2);
-        const dd li = dd_mul(sd_f2dd(A[i * m + t]), rd);
-        const dd v = dd_sub(sd_f2dd(A[i * m + q]), dd_mul(li, sd_f2dd(A[q * m + t])));
-        A[i * m + q] = sd_dd2f(v);
-      } else {
-        const int i = t + 1 + (e - ntri);
-        const dd li = dd_mul(sd_f2dd(A[i * m + t]), rd);
-        y[i] = sd_dd2f(dd_sub(sd_f2dd(y[i]), dd_mul(li, yt)));
+    // trailing rows i > t: a_iq -= (a_it rd) a_qt for t < q <= i; y_i -= (a_it rd) y_t
+    for (int i = t + 1 + warp; i < m; i += 8) {
+      const dd li = dd_mul(sd_f2dd(A[sd_at(i, t)]), rd);
+      const int ri = sd_at(i, 0);
+      for (int q = t + 1 + lane; q <= i; q += 32) {
+        const dd v = dd_sub(sd_f2dd(A[ri + q]), dd_mul(li, sd_f2dd(A[sd_at(q, t)])));
+        A[ri + q] = sd_dd2f(v);
       }
+      if (lane == 0) y[i] = sd_dd2f(dd_sub(sd_f2dd(y[i]), dd_mul(li, yt)));
     }
     __syncthreads();
   }
   // L columns (a_it rd_t), the diagonal solve
-  for (int e = tid; e < m * m; e += 256) {
-    const int i = e / m, t = e % m;
-    if (t < i) A[e] = sd_dd2f(dd_mul(sd_f2dd(A[e]), sd_f2dd(rdv[t])));
-  }
+  for (int i = warp; i < m; i += 8)
+    for (int t = lane; t < i; t += 32) {
+      const int e = sd_at(i, t);
+      A[e] = sd_dd2f(dd_mul(sd_f2dd(A[e]), sd_f2dd(rdv[t])));
+    }
   for (int i = tid; i < m; i += 256) y[i] = sd_dd2f(dd_mul(sd_f2dd(y[i]), sd_f2dd(rdv[i])));
   __syncthreads();
   // backward: x_t final, then x_i -= L_ti x_t for i < t
   for (int t = m - 1; t > 0; --t) {
     const dd xt = sd_f2dd(y[t]);
-    for (int i = tid; i < t; i += 256) y[i] = sd_dd2f(dd_sub(sd_f2dd(y[i]), dd_mul(sd_f2dd(A[t * m + i]), xt)));
+    const int rt = sd_at(t, 0);
+    for (int i = tid; i < t; i += 256) y[i] = sd_dd2f(dd_sub(sd_f2dd(y[i]), dd_mul(sd_f2dd(A[rt + i]), xt)));
     __syncthreads();
   }
   for (int i = tid; i < m; i += 256) {
@@ -1033,7 +1032,9 @@ __global__ void __launch_bounds__(256, 1) k_small_dense(DenseArgs a, Ctrl* ctrl)
   small_dense_body(a, ctrl, blockIdx.x, gridDim.x);
 }
 
-size_t small_dense_smem(int n) { return sizeof(float2) * (static_cast<size_t>(n) * n + 2 * static_cast<size_t>(n)); }
+size_t small_dense_smem(int n) {
+  return sizeof(float2) * (static_cast<size_t>(n) * (n + 1) / 2 + 2 * static_cast<size_t>(n));
+}
 
 size_t dense_smem_bytes(int P, int C) {
   size_t m = 0;
@@ -1201,7 +1202,8 @@ struct DenseBatch {
 DenseBatch* dense_batch_create(const std::vector<BatchWin>& wins, Ctrl* const* ctrl_dev, cudaStream_t st,
                                cudaError_t* err) {
   *err = cudaSuccess;
-  // group 0: the one-CTA solver; then one group per cluster size
+  // groups keyed by cluster size (> 0), or by a shared-memory class of the
+  // one-CTA solver (<= 0)
   std::vector<int> sizes;
   std::vector<std::vector<DenseArgs>> args;
   std::vector<std::vector<int32_t>> win;
@@ -1219,7 +1221,10 @@ DenseBatch* dense_batch_create(const std::vector<BatchWin>& wins, Ctrl* const* c
     const Sizes& s = *wins[w].s;
     const Dev& d = *wins[w].d;
     if (s.small_dense) {
-      const int g = group_of(0);
+      // by shared memory, so that small windows share an SM: <= 56 KiB,
+      // <= 112 KiB, larger (keys 0, -1, -2)
+      const size_t b = small_dense_smem(s.n6);
+      const int g = group_of(b <= 56 * 1024 ? 0 : (b <= 112 * 1024 ? -1 : -2));
       args[g].push_back(small_dense_args(s, d));
       win[g].push_back(static_cast<int32_t>(w));
       smem[g] = std::max(smem[g], small_dense_smem(s.n6));
@@ -1251,7 +1256,7 @@ DenseBatch* dense_batch_create(const std::vector<BatchWin>& wins, Ctrl* const* c
   if (e == cudaSuccess && !img.empty()) e = cudaMemcpyAsync(b->dbuf, img.data(), img.size(), cudaMemcpyHostToDevice, st);
   for (size_t g = 0; e == cudaSuccess && g < sizes.size(); ++g) {
     DenseGroup G;
-    G.cluster = sizes[g];
+    G.cluster = sizes[g] > 0 ? sizes[g] : 0;
     G.count = static_cast<int>(args[g].size());
     G.smem = smem[g];
     G.args = reinterpret_cast<const DenseArgs*>(static_cast<unsigned char*>(b->dbuf) + a_at[g]);

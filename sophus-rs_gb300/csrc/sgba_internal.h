@@ -156,6 +156,7 @@ struct Dev {
   int32_t* block_chunk_begin = nullptr;  // nsb + 1, into chunks
   float2* schur_part = nullptr;    // 36 float-float partials per chunk
   int32_t* lmk_chunk_pt = nullptr; // landmark pass: point chunks (<= 256 terms), nlchunk + 1
+  int32_t* zterm = nullptr;        // np x nf: term of each (point, free block) or -1 (tiled Schur pass)
   int32_t* slow_list = nullptr;    // points redone in float-float this iteration
   int32_t* slow_count = nullptr;
   // state
@@ -334,6 +335,7 @@ struct Sizes {
   int band_seg_rows;  // rows of the first segment
   int band_ring_c;    // row slots per CTA of the corner's factor
   int lin_dd;          // float-float linearization (Jacobians, products and Z in float-float)
+  int schur_dense;     // S by tiles of pose blocks (nearly dense S and Z: local windows), not by pairs
   int intr_free;       // the camera params are Free: one more 6-row block, last in S
   int intr_nk;         // free params: 4 (pinhole, padded to 6 rows) or 6 (EUCM)
   int eucm;            // the camera is the enhanced unified camera model (else the pinhole)
@@ -402,6 +404,9 @@ int band_launch_count(const Sizes& s);
 cudaError_t pair_totals(const Sizes& s, const Dev& d, int32_t* totals, cudaStream_t st);
 cudaError_t pair_fill(const Sizes& s, const Dev& d, const int32_t* bidmap, int64_t nb, const int64_t* block_begin,
                       int32_t nchunk, int32_t* table, cudaStream_t st);
+// The term of every (marginalized point, free pose block), -1 where the point
+// has none: T[i * nf + fb] (the tiled Schur pass of nearly dense systems).
+cudaError_t zterm_fill(const Sizes& s, const Dev& d, int32_t* T, cudaStream_t st);
 
 // PCG on the reduced system (sgba_pcg.cu): grid size for the cooperative
 // kernel (0 = cannot launch), and the launch chain (structure arrays uploaded

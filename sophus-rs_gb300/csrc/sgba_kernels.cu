@@ -1715,6 +1715,148 @@ __global__ void __launch_bounds__(256) k_schur_reduce(SchurArgs a, const Ctrl* c
 }
 
 // ---------------------------------------------------------------------------
+// Dense reduced systems (local windows: every camera sees most points): S
+// formed by tiles of kSdB x kSdB pose blocks instead of observation pairs.
+// A CTA owns one tile of the lower triangle and streams every point once, in
+// rounds of kSdPts points: thread (point, slot) fetches the Z record of the
+// point's term with the slot's pose (the term table T; zeros where there is
+// none) into registers one round ahead, stores it into shared memory, and
+// every thread then accumulates a 3 x 3 piece of the tile (FP32 within a
+// round, float-float across rounds).  The entries are written as
+// S = U + nu n I - sum Z Z^T (the formula of k_schur_reduce), in f64 and
+// float-float.  Loads per point and tile: 2 kSdB Z records, against two per
+// observation pair.
+// ---------------------------------------------------------------------------
+constexpr int kSdB = 8;          // pose blocks per tile side
+constexpr int kSdT = 6 * kSdB;   // 48 rows / columns
+constexpr int kSdPts = 16;       // points per round: 16 points x 16 slots = one per thread
+
+struct SchurDenseArgs {
+  int np, nf, n6;
+  const int32_t* zterm;  // np x nf: term of (point, free block) or -1
+  const float* zmat;
+  const double* ufull;
+  const double* cnt_f;
+  double* S;
+  float2* S2;
+};
+
+// the Z record (6 x 3 row-major, 20 floats) of term g, or zeros
+__device__ __forceinline__ void sd_fetch(const float* zmat, int g, float4* v) {
+  if (g >= 0) {
+    const float4* src = reinterpret_cast<const float4*>(zmat + kZS * static_cast<int64_t>(g));
+#pragma unroll
+    for (int q = 0; q < 5; ++q) v[q] = __ldg(src + q);
+  } else {
+#pragma unroll
+    for (int q = 0; q < 5; ++q) v[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
+__device__ __forceinline__ void schur_dense_body(SchurDenseArgs a, const Ctrl* ctrl, int bid_, int nblk_) {
+  (void)nblk_;
+  if (skipping(ctrl)) return;
+  __shared__ __align__(16) float zr[kSdPts][kSdT][4];  // Z rows of the tile's row poses (k = 0..2, padded)
+  __shared__ __align__(16) float zc[kSdPts][kSdT][4];  // the same for its column poses
+  // tile (ti, tj), tj <= ti, of the lower triangle
+  int ti = static_cast<int>((sqrtf(8.0f * static_cast<float>(bid_) + 1.0f) - 1.0f) * 0.5f);
+  while (ti * (ti + 1) / 2 > bid_) --ti;
+  while ((ti + 1) * (ti + 2) / 2 <= bid_) ++ti;
+  const int tj = bid_ - ti * (ti + 1) / 2;
+  const int I0 = ti * kSdB, J0 = tj * kSdB;
+  const int tid = threadIdx.x;
+  const int r0 = 3 * (tid >> 4), c0 = 3 * (tid & 15);
+  // this thread's staging slot: point pp of each round, pose fb
+  const int pp = tid >> 4, slot = tid & 15;
+  const int fb = slot < kSdB ? I0 + slot : J0 + slot - kSdB;
+  float(*dst)[4] = slot < kSdB ? &zr[pp][6 * slot] : &zc[pp][6 * (slot - kSdB)];
+  auto term_of = [&](int p0) {
+    const int i = p0 + pp;
+    return (i < a.np && fb < a.nf) ? __ldg(a.zterm + static_cast<int64_t>(i) * a.nf + fb) : -1;
+  };
+  float acc[3][3];
+  Acc accd[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      acc[i][j] = 0.0f;
+      accd[i][j] = acc_zero();
+    }
+  // the term index runs two rounds ahead, the Z record one round ahead
+  float4 v[5];
+  sd_fetch(a.zmat, term_of(0), v);
+  int g_next = term_of(kSdPts);
+  for (int p0 = 0; p0 < a.np; p0 += kSdPts) {
+    __syncthreads();  // the previous round's reads are done
+    reinterpret_cast<float4*>(dst[0])[0] = make_float4(v[0].x, v[0].y, v[0].z, 0.f);
+    reinterpret_cast<float4*>(dst[1])[0] = make_float4(v[0].w, v[1].x, v[1].y, 0.f);
+    reinterpret_cast<float4*>(dst[2])[0] = make_float4(v[1].z, v[1].w, v[2].x, 0.f);
+    reinterpret_cast<float4*>(dst[3])[0] = make_float4(v[2].y, v[2].z, v[2].w, 0.f);
+    reinterpret_cast<float4*>(dst[4])[0] = make_float4(v[3].x, v[3].y, v[3].z, 0.f);
+    reinterpret_cast<float4*>(dst[5])[0] = make_float4(v[3].w, v[4].x, v[4].y, 0.f);
+    __syncthreads();
+    if (p0 + kSdPts < a.np) {  // next round, in flight during the products
+      sd_fetch(a.zmat, g_next, v);
+      g_next = term_of(p0 + 2 * kSdPts);
+    }
+    const int npt = a.np - p0 < kSdPts ? a.np - p0 : kSdPts;
+    for (int q = 0; q < npt; ++q) {
+      float4 ra[3], cb[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) ra[i] = reinterpret_cast<const float4*>(&zr[q][r0 + i][0])[0];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) cb[j] = reinterpret_cast<const float4*>(&zc[q][c0 + j][0])[0];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          float w = acc[i][j];
+          w = fmaf(ra[i].x, cb[j].x, w);
+          w = fmaf(ra[i].y, cb[j].y, w);
+          w = fmaf(ra[i].z, cb[j].z, w);
+          acc[i][j] = w;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        acc_addf(accd[i][j], acc[i][j]);
+        acc[i][j] = 0.0f;
+      }
+  }
+  const double nu = ctrl->nu;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int row = 6 * I0 + r0 + i, col = 6 * J0 + c0 + j;
+      if (row >= a.n6 || col >= a.n6 || col > row) continue;
+      const dd t = acc_get(accd[i][j]);
+      const int bj = row / 6, bk = col / 6, r = row % 6, cc = col % 6;
+      dd vd;
+      if (bj == bk) {
+        dd base = dd_from_double(a.ufull[36 * bj + r * 6 + cc]);
+        if (r == cc) base = dd_add(base, dd_from_double(nu * a.cnt_f[bj]));
+        vd = dd_sub(base, t);
+      } else {
+        vd = dd_neg(t);
+      }
+      const double w = dd_to_double(vd);
+      a.S[static_cast<int64_t>(row) * a.n6 + col] = w;
+      a.S[static_cast<int64_t>(col) * a.n6 + row] = w;
+      if (a.S2) {
+        a.S2[static_cast<int64_t>(row) * a.n6 + col] = make_float2(vd.hi, vd.lo);
+        a.S2[static_cast<int64_t>(col) * a.n6 + row] = make_float2(vd.hi, vd.lo);
+      }
+    }
+}
+__global__ void __launch_bounds__(256) k_schur_dense(SchurDenseArgs a, const Ctrl* ctrl) {
+  schur_dense_body(a, ctrl, blockIdx.x, gridDim.x);
+}
+
+// ---------------------------------------------------------------------------
 // Back-substitution (SchurFactor::solve, schur_ldlt.rs:782-803):
 //   dx_m = V'^-1 (b_m - sum W_g^T dx_f) = C^-T (c - sum Z_g^T dx_f)
 // ---------------------------------------------------------------------------
@@ -2724,6 +2866,16 @@ int warp_grid(int64_t items, int warps_per_block, int cap) {
 
 constexpr int kUpdBlocks = 152;
 
+// CTAs of the update and gauge kernels: kUpdBlocks, or one per 256 poses and
+// points for small problems (local windows), whose update is a few thousand
+// items spread over 152 nearly idle CTAs otherwise.
+int upd_blocks(const Sizes& s) {
+  const int64_t items = static_cast<int64_t>(s.nc) + s.np;
+  if (items > 16384) return kUpdBlocks;
+  const int64_t b = (items + 255) / 256;
+  return b < 1 ? 1 : static_cast<int>(b);
+}
+
 }  // namespace
 
 int cost_partials_needed(const Sizes& s) { return 4 * kUpdBlocks + cost_grid(s.no); }
@@ -2987,7 +3139,30 @@ static SchurArgs make_schur_args(const Sizes& s, const Dev& d) {
   return a;
 }
 
+static SchurDenseArgs make_schur_dense_args(const Sizes& s, const Dev& d) {
+  SchurDenseArgs a;
+  a.np = s.np;
+  a.nf = s.nf;
+  a.n6 = s.n6;
+  a.zterm = d.zterm;
+  a.zmat = d.zmat;
+  a.ufull = d.ufull;
+  a.cnt_f = d.cnt_f;
+  a.S = d.S;
+  a.S2 = d.S2;
+  return a;
+}
+
+static int schur_dense_grid(const Sizes& s) {
+  const int nb = (s.nf + kSdB - 1) / kSdB;
+  return nb * (nb + 1) / 2;
+}
+
 int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
+  if (s.schur_dense) {
+    k_schur_dense<<<schur_dense_grid(s), 256, 0, st>>>(make_schur_dense_args(s, d), d.ctrl);
+    return 1 + launch_intr_fill(s, d, st);
+  }
   const SchurArgs a = make_schur_args(s, d);
   if (s.lin_dd) k_schur_dd<<<warp_grid(s.nchunk, 8, 65536), 256, 0, st>>>(a, d.ctrl);
   else k_schur<<<warp_grid(s.nchunk, 8, 65536), 256, 0, st>>>(a, d.ctrl);
@@ -3037,7 +3212,7 @@ static UpdArgs make_upd_args(const Sizes& s, const Dev& d) {
   u.cz = s.gauge_center[2];
   u.part = d.part + 2 * kUpdBlocks;
   u.gauge_part = d.part;
-  u.gauge_blocks = kUpdBlocks;
+  u.gauge_blocks = upd_blocks(s);
   u.um = d.gauge_um;
   u.intr_free = s.intr_free;
   u.intr_nk = s.intr_nk;
@@ -3053,10 +3228,10 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
   int n = 0;
   n += launch_backsub(s, d, st);
   if (s.gauge_kind == 1) {
-    k_gauge_partials<<<kUpdBlocks, 256, 0, st>>>(make_gauge_args(s, d), d.ctrl);
+    k_gauge_partials<<<upd_blocks(s), 256, 0, st>>>(make_gauge_args(s, d), d.ctrl);
     n += 1;
   }
-  k_apply_update<<<kUpdBlocks, 256, 0, st>>>(make_upd_args(s, d), d.ctrl);
+  k_apply_update<<<upd_blocks(s), 256, 0, st>>>(make_upd_args(s, d), d.ctrl);
   ++n;
   return n;
 }
@@ -3090,7 +3265,7 @@ static CostArgs make_decide_args(const Sizes& s, const Dev& d) {
   CostArgs a = make_cost_args(s, d, d.points_t, d.res_t, cost_part, 1);
   a.decide = d.ctrl;
   a.upd_part = d.part + 2 * kUpdBlocks;
-  a.n_upd = kUpdBlocks;
+  a.n_upd = upd_blocks(s);
   a.recs = d.records;
   a.last = d.last_rec;
   return a;
@@ -3436,6 +3611,10 @@ __global__ void __launch_bounds__(64) k_camera_finalize_w(WinTab<FinArgs> t) {
   camera_finalize_body(a.nf, a.fb_tile_begin, a.tile_part, a.ufull, a.bf, a.rb, t.ctrl[q.w], a.with_schur, q.b,
                        q.nb);
 }
+__global__ void __launch_bounds__(256) k_schur_dense_w(WinTab<SchurDenseArgs> t) {
+  const WinPos q = win_pos(t);
+  schur_dense_body(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
+}
 __global__ void __launch_bounds__(256, 2) k_schur_w(WinTab<SchurArgs> t) {
   const WinPos q = win_pos(t);
   schur_body(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
@@ -3496,7 +3675,7 @@ struct BatchTables {
   Ctrl** ctrl = nullptr;     // device: n control blocks
   Record** recs = nullptr;   // device: n record buffers
   int* rec_cap = nullptr;    // device: n record capacities
-  KTab pose_it, lmk_chunks, lmk_slow, cam, fin, schur, schur_red, bsub, gauge, upd, cost, commit;
+  KTab pose_it, lmk_chunks, lmk_slow, cam, fin, schur, schur_red, schur_dense, bsub, gauge, upd, cost, commit;
   KTab pose_init, cost_init, merit;
   KTab pose_fin, lmk_fin, cam_fin, fin_fin;
   DenseBatch* dense = nullptr;
@@ -3552,6 +3731,7 @@ BatchTables* batch_tables_create(const std::vector<BatchWin>& wins, int skip_fin
   TabBuild<CamArgs> t_cam, t_cam_fin;
   TabBuild<FinArgs> t_fin, t_fin_fin;
   TabBuild<SchurArgs> t_schur, t_schur_red;
+  TabBuild<SchurDenseArgs> t_schur_dense;
   TabBuild<BsubArgs> t_bsub;
   TabBuild<GaugeArgs> t_gauge;
   TabBuild<UpdArgs> t_upd;
@@ -3581,12 +3761,13 @@ BatchTables* batch_tables_create(const std::vector<BatchWin>& wins, int skip_fin
     t_cam.add(make_cam_args(s, d, 1), static_cast<int>(s.ntiles));
     t_fin.add(FinArgs{s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf, d.rb, 1}, s.nf);
     const SchurArgs sa = make_schur_args(s, d);
-    t_schur.add(sa, warp_grid(s.nchunk, 8, 65536));
-    t_schur_red.add(sa, warp_grid(s.nsb, 8, 8192));
+    t_schur.add(sa, s.schur_dense ? 0 : warp_grid(s.nchunk, 8, 65536));
+    t_schur_red.add(sa, s.schur_dense ? 0 : warp_grid(s.nsb, 8, 8192));
+    t_schur_dense.add(make_schur_dense_args(s, d), s.schur_dense ? schur_dense_grid(s) : 0);
     t_bsub.add(BsubArgs{make_back_args(s, d), d.lmk_chunk_pt, s.nlchunk, d.g_pt}, lmk_grid,
                sizeof(float) * 12 * static_cast<size_t>(s.lmk_cap));
-    t_gauge.add(make_gauge_args(s, d), s.gauge_kind == 1 ? kUpdBlocks : 0);
-    t_upd.add(make_upd_args(s, d), kUpdBlocks);
+    t_gauge.add(make_gauge_args(s, d), s.gauge_kind == 1 ? upd_blocks(s) : 0);
+    t_upd.add(make_upd_args(s, d), upd_blocks(s));
     t_cost.add(make_decide_args(s, d), cost_grid(s.no));
     t_commit.add(CommitArgs{s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res, d.res_lo_t,
                             d.res_lo, nullptr, nullptr},
@@ -3627,6 +3808,7 @@ BatchTables* batch_tables_create(const std::vector<BatchWin>& wins, int skip_fin
   stage(t_fin, &T->fin);
   stage(t_schur, &T->schur);
   stage(t_schur_red, &T->schur_red);
+  stage(t_schur_dense, &T->schur_dense);
   stage(t_bsub, &T->bsub);
   stage(t_gauge, &T->gauge);
   stage(t_upd, &T->upd);
@@ -3723,6 +3905,8 @@ int batch_launch_iteration(const BatchTables* t, cudaStream_t st) {
   if (go(t->fin)) k_camera_finalize_w<<<t->fin.blocks, 64, 0, st>>>(wtab<FinArgs>(t, t->fin));
   if (go(t->schur)) k_schur_w<<<t->schur.blocks, 256, 0, st>>>(wtab<SchurArgs>(t, t->schur));
   if (go(t->schur_red)) k_schur_reduce_w<<<t->schur_red.blocks, 256, 0, st>>>(wtab<SchurArgs>(t, t->schur_red));
+  if (go(t->schur_dense))
+    k_schur_dense_w<<<t->schur_dense.blocks, 256, 0, st>>>(wtab<SchurDenseArgs>(t, t->schur_dense));
   n += launch_dense_batch(t->dense, st);
   if (go(t->bsub)) k_backsub_chunks_w<<<t->bsub.blocks, 256, t->bsub.smem, st>>>(wtab<BsubArgs>(t, t->bsub));
   if (go(t->gauge)) k_gauge_partials_w<<<t->gauge.blocks, 256, 0, st>>>(wtab<GaugeArgs>(t, t->gauge));

@@ -190,4 +190,28 @@ cudaError_t pair_fill(const Sizes& s, const Dev& d, const int32_t* bidmap, int64
   return cudaGetLastError();
 }
 
+namespace {
+
+// term of each (marginalized point, free pose block): T[i * nf + fb] = g
+__global__ void k_zterm(int64_t ng, const int32_t* __restrict__ g_pt, const int32_t* __restrict__ g_pose,
+                        const int32_t* __restrict__ pose_fb, const int32_t* __restrict__ pt_mb, int nf,
+                        int32_t* __restrict__ T) {
+  const int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (g >= ng) return;
+  const int fb = pose_fb[g_pose[g]];
+  const int i = g_pt[g];
+  if (fb < 0 || pt_mb[i] < 0) return;
+  T[static_cast<int64_t>(i) * nf + fb] = static_cast<int32_t>(g);
+}
+
+}  // namespace
+
+cudaError_t zterm_fill(const Sizes& s, const Dev& d, int32_t* T, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(T, 0xff, sizeof(int32_t) * static_cast<size_t>(s.np) * s.nf, st);
+  if (e != cudaSuccess || s.ng == 0) return e;
+  const int64_t blocks = (s.ng + 255) / 256;
+  k_zterm<<<static_cast<unsigned>(blocks), 256, 0, st>>>(s.ng, d.g_pt, d.g_pose, d.pose_fb, d.pt_mb, s.nf, T);
+  return cudaGetLastError();
+}
+
 }  // namespace sgba
