@@ -545,7 +545,24 @@ def main():
     ap.add_argument("--profile-cams", type=int, default=0,
                     help="profiling mode: the loop workload at this many cameras (200 points per camera), a "
                          "small case for multi-pass profiler captures")
+    ap.add_argument("--profile-windows", type=int, default=N_WINDOWS,
+                    help="profiling mode of the windows workload: this many windows, two batched calls (the "
+                         "first settles the schedule autotuner)")
     args = ap.parse_args()
+    if args.profile_iters > 0 and args.workload == "windows":
+        pkg = _load_pkg()
+        wins = [pkg.synth.generate(pkg.synth.WINDOW, seed=pkg.synth.BASE_SEED + 3 + w)
+                for w in range(args.profile_windows)]
+        probs = [pkg.native.Problem(w, device=0) for w in wins]
+        try:
+            for _ in range(2):
+                pkg.native.batch_optimize(probs, _fixed(pkg, args.profile_iters, wins[0].initial_lm_damping))
+            print(json.dumps({"profile_iters": args.profile_iters, "windows": len(wins),
+                              "batch": pkg.native.batch_last_stats()}))
+        finally:
+            for p in probs:
+                p.close()
+        return
     if args.profile_iters > 0:
         pkg = _load_pkg()
         wl = dict(WORKLOADS[args.workload if args.workload in WORKLOADS else DEFAULT_WORKLOAD])
