@@ -1368,7 +1368,7 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles(CamArgs a, const 
 // cancel ~25x, beyond what FP32 products leave).  Same outputs as
 // k_camera_tiles.
 template <bool E>
-__global__ void __launch_bounds__(kTileThreads) k_camera_tiles_dd(CamArgs a, const Ctrl* ctrl) {
+__global__ void __launch_bounds__(kTileThreads, 2) k_camera_tiles_dd(CamArgs a, const Ctrl* ctrl) {
   const CamF cam_ = cam_f(a.intr);
   const CamD camd_ = cam_dd(a.intr);
   (void)cam_; (void)camd_;
@@ -1613,8 +1613,11 @@ __global__ void __launch_bounds__(256, 2) k_schur(SchurArgs a, const Ctrl* ctrl)
 }
 
 // Pass 1 of the float-float linearization: the same chunks, float-float Z and
-// float-float products and sums (36 accumulators per lane).
-__global__ void __launch_bounds__(256, 1) k_schur_dd(SchurArgs a, const Ctrl* ctrl) {
+// float-float products and sums (36 accumulators per lane).  The products of
+// a pair go by the inner index t (column t of both Z, 24 floats live instead
+// of 72), which keeps two CTAs per SM; every accumulator still receives its
+// t = 0, 1, 2 terms in that order.
+__global__ void __launch_bounds__(256, 2) k_schur_dd(SchurArgs a, const Ctrl* ctrl) {
   if (skipping(ctrl)) return;
   __shared__ float red[8][36][33];
   const int lane = threadIdx.x & 31;
@@ -1628,23 +1631,22 @@ __global__ void __launch_bounds__(256, 1) k_schur_dd(SchurArgs a, const Ctrl* ct
     const int64_t q1 = a.chunk_begin[ch + 1];
     for (int64_t q = a.chunk_begin[ch] + lane; q < q1; q += 32) {
       const int2 pr = a.pairs[q];
-      float za[36], zb[36];
-      const float4* pa = reinterpret_cast<const float4*>(a.zdd + kZD * static_cast<int64_t>(pr.x));
-      const float4* pb = reinterpret_cast<const float4*>(a.zdd + kZD * static_cast<int64_t>(pr.y));
+      const float2* pa = reinterpret_cast<const float2*>(a.zdd + kZD * static_cast<int64_t>(pr.x));
+      const float2* pb = reinterpret_cast<const float2*>(a.zdd + kZD * static_cast<int64_t>(pr.y));
 #pragma unroll
-      for (int k = 0; k < 9; ++k) {
-        const float4 u = __ldg(pa + k), v = __ldg(pb + k);
-        za[4 * k] = u.x; za[4 * k + 1] = u.y; za[4 * k + 2] = u.z; za[4 * k + 3] = u.w;
-        zb[4 * k] = v.x; zb[4 * k + 1] = v.y; zb[4 * k + 2] = v.z; zb[4 * k + 3] = v.w;
+      for (int t = 0; t < 3; ++t) {
+        float2 za[6], zb[6];  // column t of each Z: (hi, lo) of rows 0..5
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+          za[r] = __ldg(pa + 3 * r + t);
+          zb[r] = __ldg(pb + 3 * r + t);
+        }
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+#pragma unroll
+          for (int c = 0; c < 6; ++c)
+            acc_madd(acc[r * 6 + c], dd_make(za[r].x, za[r].y), dd_make(zb[c].x, zb[c].y));
       }
-#pragma unroll
-      for (int r = 0; r < 6; ++r)
-#pragma unroll
-        for (int c = 0; c < 6; ++c)
-#pragma unroll
-          for (int t = 0; t < 3; ++t)
-            acc_madd(acc[r * 6 + c], dd_make(za[6 * r + 2 * t], za[6 * r + 2 * t + 1]),
-                     dd_make(zb[6 * c + 2 * t], zb[6 * c + 2 * t + 1]));
     }
     // lanes' accumulators summed in float-float: hi parts, then lo parts
     Acc t0 = acc_zero(), t1 = acc_zero();  // entries lane and lane + 32
