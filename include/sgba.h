@@ -219,6 +219,20 @@ int sgba_get_cost(sgba_problem *p, double *cost);
 /* Overwrite the variables of an existing problem (same structure). */
 int sgba_set_variables(sgba_problem *p, const double *poses, const double *points);
 
+/* Pose priors: a second cost function of Isometry3PriorCostTerm terms
+ * (crates/sophus_opt/src/nlls/functor_library/costs/isometry3_prior.rs,
+ * tested by crates/sophus_opt/src/example_problems/cam_calib.rs:249-342).
+ * Prior k on pose[k] has the mean pose mean + 7k (qw qx qy qz tx ty tz) and
+ * the 6x6 precision precision + 36k (row-major); residual log(T E^-1), cost
+ * g^T W g, no robust kernel.  A prior on a constant pose adds only its cost.
+ * Replaces any earlier set (n = 0 removes them); takes effect at the next
+ * sgba_optimizer_init / sgba_optimize.  With priors the scale gauge is held by
+ * them (no gauge projection).  Windows with priors are not batched by
+ * sgba_batch_optimize (they run on their own streams).  Not with free camera
+ * params (SGBA_ERR_UNSUPPORTED). */
+int sgba_set_pose_priors(sgba_problem *p, int32_t n, const int32_t *pose, const double *mean,
+                         const double *precision);
+
 /* Sizes of the problem as laid out on the device. */
 typedef struct {
   int32_t n_free_poses;     /* free pose blocks (6 dof) */

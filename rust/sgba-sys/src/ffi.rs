@@ -254,6 +254,13 @@ extern "C" {
         results: *mut sgba_window_result,
     ) -> c_int;
     pub fn sgba_batch_last_stats(out: *mut sgba_batch_stats) -> c_int;
+    pub fn sgba_set_pose_priors(
+        p: *mut sgba_problem,
+        n: i32,
+        pose: *const i32,
+        mean: *const f64,
+        precision: *const f64,
+    ) -> c_int;
     pub fn sgba_get_variables(p: *mut sgba_problem, poses: *mut f64, points: *mut f64) -> c_int;
     pub fn sgba_get_cost(p: *mut sgba_problem, cost: *mut f64) -> c_int;
     pub fn sgba_set_variables(p: *mut sgba_problem, poses: *const f64, points: *const f64) -> c_int;

@@ -117,6 +117,8 @@ constexpr int32_t kMaxDenseFree = 4096;  // reduced-camera-system limit (6 * 409
 
 struct sgba_problem {
   Plan plan;
+  std::vector<double> cnt_f_base;  // damping counts of the free poses without pose priors
+  int gauge_base = -1;             // gauge kind without pose priors (-1: not saved yet)
   int intr_free = 0;  // the camera params are a Free family (sgba_problem_create_ex)
   int camera_model = SGBA_CAMERA_PINHOLE;
   double eucm_ab[2] = {0.0, 0.0};  // EUCM alpha beta
@@ -1257,6 +1259,81 @@ int sgba_get_variables(sgba_problem* p, double* poses, double* points) {
   if (poses) SGBA_CK(cudaMemcpy(poses, p->d.poses, sizeof(double) * 7 * p->plan.nc, cudaMemcpyDeviceToHost));
   if (points && p->plan.np > 0)
     SGBA_CK(cudaMemcpy(points, p->d.points, sizeof(double) * 3 * p->plan.np, cudaMemcpyDeviceToHost));
+  return SGBA_OK;
+}
+
+int sgba_set_pose_priors(sgba_problem* p, int32_t n, const int32_t* pose, const double* mean,
+                         const double* precision) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  if (n < 0) return set_error(SGBA_ERR_INVALID_ARGUMENT, "negative prior count");
+  if (n > 0 && (!pose || !mean || !precision)) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (p->intr_free) return set_error(SGBA_ERR_UNSUPPORTED, "pose priors with free camera params are not on this path");
+  const Plan& P = p->plan;
+  for (int32_t k = 0; k < n; ++k) {
+    if (pose[k] < 0 || pose[k] >= P.nc)
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "prior %d: pose index %d out of range", k, pose[k]);
+    if (!finite_all(mean + 7 * k, 7) || !finite_all(precision + 36 * static_cast<int64_t>(k), 36))
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "prior %d: non-finite mean or precision", k);
+    if (!quat_valid(mean + 7 * k)) return set_error(SGBA_ERR_INVALID_PARAMS, "prior %d: invalid quaternion", k);
+  }
+  SGBA_CK(cudaSetDevice(p->device));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  Dev& d = p->d;
+  Sizes& s = p->sz;
+  // CostFn::sort order: by pose, stable
+  std::vector<int32_t> ord(n);
+  for (int32_t k = 0; k < n; ++k) ord[k] = k;
+  std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return pose[a] < pose[b]; });
+  std::vector<int32_t> hp(n), hfb(n), beg(P.nf + 1, 0);
+  std::vector<double> hm(7 * static_cast<size_t>(n)), hw(36 * static_cast<size_t>(n));
+  for (int32_t k = 0; k < n; ++k) {
+    const int32_t o = ord[k];
+    hp[k] = pose[o];
+    hfb[k] = P.pose_fb[pose[o]];
+    std::memcpy(&hm[7 * k], mean + 7 * o, sizeof(double) * 7);
+    if (!(0.0 <= hm[7 * k]))
+      for (int q = 0; q < 4; ++q) hm[7 * k + q] = -hm[7 * k + q];
+    std::memcpy(&hw[36 * static_cast<size_t>(k)], precision + 36 * static_cast<int64_t>(o), sizeof(double) * 36);
+    if (hfb[k] >= 0) ++beg[hfb[k] + 1];
+  }
+  for (int f = 0; f < P.nf; ++f) beg[f + 1] += beg[f];
+  // damping once per pose with a prior (one reduced term of the prior cost function)
+  if (p->gauge_base < 0) {
+    p->cnt_f_base = P.cnt_f;
+    p->gauge_base = s.gauge_kind;
+  }
+  std::vector<double> cnt = p->cnt_f_base;
+  for (int f = 0; f < P.nf; ++f)
+    if (beg[f + 1] > beg[f]) cnt[f] += 1.0;
+  int st;
+  if (n > d.prior_cap) {
+    if ((st = dev_alloc(p, &d.prior_pose, static_cast<size_t>(n)))) return st;
+    if ((st = dev_alloc(p, &d.prior_fb, static_cast<size_t>(n)))) return st;
+    if ((st = dev_alloc(p, &d.prior_mean, 7 * static_cast<size_t>(n)))) return st;
+    if ((st = dev_alloc(p, &d.prior_W, 36 * static_cast<size_t>(n)))) return st;
+    if ((st = dev_alloc(p, &d.prior_out, static_cast<size_t>(sgba::kPriorOut) * n))) return st;
+    d.prior_cap = n;
+  }
+  if (!d.prior_fb_begin && (st = dev_alloc(p, &d.prior_fb_begin, static_cast<size_t>(P.nf) + 1))) return st;
+  if (n > 0) {
+    SGBA_CK(cudaMemcpyAsync(d.prior_pose, hp.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+    SGBA_CK(cudaMemcpyAsync(d.prior_fb, hfb.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+    SGBA_CK(cudaMemcpyAsync(d.prior_mean, hm.data(), sizeof(double) * hm.size(), cudaMemcpyHostToDevice, p->stream));
+    SGBA_CK(cudaMemcpyAsync(d.prior_W, hw.data(), sizeof(double) * hw.size(), cudaMemcpyHostToDevice, p->stream));
+  }
+  SGBA_CK(cudaMemcpyAsync(d.prior_fb_begin, beg.data(), sizeof(int32_t) * beg.size(), cudaMemcpyHostToDevice,
+                          p->stream));
+  if (P.nf > 0)
+    SGBA_CK(cudaMemcpyAsync(d.cnt_f, cnt.data(), sizeof(double) * P.nf, cudaMemcpyHostToDevice, p->stream));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  p->plan.cnt_f = cnt;
+  s.n_prior = n;
+  // the priors hold the gauge: no projection along the scale direction
+  s.gauge_kind = n > 0 ? 0 : p->gauge_base;
+  // the iteration graph is captured again with the prior launches
+  if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }
+  if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+  p->inited = false;
   return SGBA_OK;
 }
 

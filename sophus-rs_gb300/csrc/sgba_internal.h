@@ -157,6 +157,16 @@ struct Dev {
   float2* schur_part = nullptr;    // 36 float-float partials per chunk
   int32_t* lmk_chunk_pt = nullptr; // landmark pass: point chunks (<= 256 terms), nlchunk + 1
   int32_t* zterm = nullptr;        // np x nf: term of each (point, free block) or -1 (tiled Schur pass)
+  // pose priors (sgba_prior.cu), sorted by pose: pose, its free block (-1:
+  // constant pose), mean (7), precision (36), and per prior J^T W J (36) and
+  // J^T W g (6); per free block the range of its priors (nf + 1)
+  int32_t* prior_pose = nullptr;
+  int32_t* prior_fb = nullptr;
+  double* prior_mean = nullptr;
+  double* prior_W = nullptr;
+  double* prior_out = nullptr;
+  int32_t* prior_fb_begin = nullptr;
+  int prior_cap = 0;
   int32_t* slow_list = nullptr;    // points redone in float-float this iteration
   int32_t* slow_count = nullptr;
   // state
@@ -336,6 +346,7 @@ struct Sizes {
   int band_ring_c;    // row slots per CTA of the corner's factor
   int lin_dd;          // float-float linearization (Jacobians, products and Z in float-float)
   int schur_dense;     // S by tiles of pose blocks (nearly dense S and Z: local windows), not by pairs
+  int n_prior;         // pose priors (a second cost function; 0: none)
   int intr_free;       // the camera params are Free: one more 6-row block, last in S
   int intr_nk;         // free params: 4 (pinhole, padded to 6 rows) or 6 (EUCM)
   int eucm;            // the camera is the enhanced unified camera model (else the pinhole)
@@ -434,6 +445,23 @@ cudaError_t pcg_loss_grad(PcgModel& m, PcgTrainSet& t, int idx, bool backward, d
 cudaError_t pcg_adam(PcgModel& m, float scale, float lr, float b1, float b2, float eps, cudaStream_t st);
 cudaError_t pcg_evaluate(const PcgModel* m, PcgTrainSet& t, int idx, int mode, int max_iters, double tol,
                          int* iters, double* relres, int* status, cudaStream_t st);
+
+// ---- pose priors (sgba_prior.cu) -----------------------------------------
+constexpr int kPriorOut = 42;  // per prior: J^T W J (36, row-major), J^T W g (6)
+struct PriorArgs {
+  int n;
+  const int32_t* pose;
+  const int32_t* fb;
+  const double* mean;
+  const double* W;
+  double* out;
+};
+// The priors at `poses`: with lin, their blocks into Dev::prior_out (priors
+// on free poses); their total cost into *cost_sum (float-float sum in prior
+// order).  gate: 0 always, 1 unless the LM loop is done, 2 unless done or the
+// step is skipped.  Returns the launches (0 without priors).
+int launch_prior_eval(const Sizes& s, const Dev& d, const double* poses, int lin, int gate, double* cost_sum,
+                      cudaStream_t st);
 
 // ---- batched local windows ----------------------------------------------
 // A batch launches every kernel of an LM iteration once for many independent

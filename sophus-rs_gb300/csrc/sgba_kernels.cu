@@ -414,6 +414,7 @@ struct CostArgs {
   int n_upd;
   Record* recs;
   Record* last;
+  int n_extra;  // partials after the blocks' own (the pose priors' cost) that the decision adds
 };
 
 __device__ void decide_body(const double* cost_part, int n_cost, const double* upd_part, int n_upd, Ctrl* ctrl,
@@ -489,7 +490,7 @@ __device__ __forceinline__ void cost_body(CostArgs a, const Ctrl* ctrl, int bid_
     if (s_last) {
       __threadfence();
       if (threadIdx.x == 0) a.decide->cost_ticket = 0;
-      decide_body(a.partials, static_cast<int>(nblk_), a.upd_part, a.n_upd, a.decide, a.recs, a.last);
+      decide_body(a.partials, static_cast<int>(nblk_) + a.n_extra, a.upd_part, a.n_upd, a.decide, a.recs, a.last);
     }
   }
 }
@@ -1459,7 +1460,9 @@ __global__ void __launch_bounds__(kTileThreads, 2) k_camera_tiles_dd(CamArgs a, 
 
 __device__ __forceinline__ void camera_finalize_body(int nf, const int64_t* fb_tile_begin,
                                                         const double* tile_part, double* ufull, double* bf,
-                                                        double* rb, Ctrl* ctrl, int with_schur, int bid_, int nblk_) {
+                                                        double* rb, Ctrl* ctrl, int with_schur,
+                                                        const int32_t* prior_beg, const double* prior_out,
+                                                        int bid_, int nblk_) {
   if (halted(ctrl)) return;
   const int fb = bid_;
   const int k = threadIdx.x;
@@ -1468,13 +1471,31 @@ __device__ __forceinline__ void camera_finalize_body(int nf, const int64_t* fb_t
     dd acc = dd_make(0.f, 0.f);
     for (int64_t t = fb_tile_begin[fb]; t < fb_tile_begin[fb + 1]; ++t)
       acc = dd_add(acc, dd_from_double(tile_part[t * kTileVals + k]));
-    if (k >= 21 && k < 27) {
-      acc = dd_neg(acc);  // neg_grad = -sum J^T r~
-    } else if (k >= 27) {
+    // pose priors on this pose (sgba_prior.cu): J^T W J into the 21 upper
+    // entries, J^T W g with the gradient sums, in prior order
+    dd pr = dd_make(0.f, 0.f);
+    if (prior_beg) {
+      int idx;
+      if (k < 21) {
+        int a = 0, rem = k;
+        while (rem >= 6 - a) { rem -= 6 - a; ++a; }
+        idx = 6 * a + (a + rem);
+      } else {
+        idx = 36 + (k < 27 ? k - 21 : k - 27);
+      }
+      for (int q = prior_beg[fb]; q < prior_beg[fb + 1]; ++q)
+        pr = dd_add(pr, dd_from_double(prior_out[static_cast<int64_t>(kPriorOut) * q + idx]));
+    }
+    if (k < 21) {
+      acc = dd_add(acc, pr);
+    } else if (k < 27) {
+      acc = dd_neg(dd_add(acc, pr));  // neg_grad = -sum J^T r~ - sum J^T W g
+    } else {
       // reduced rhs: b_f - sum Z c  (b_f = -g)
       dd g = dd_make(0.f, 0.f);
       for (int64_t t = fb_tile_begin[fb]; t < fb_tile_begin[fb + 1]; ++t)
         g = dd_add(g, dd_from_double(tile_part[t * kTileVals + k - 6]));
+      g = dd_add(g, pr);
       acc = dd_sub(dd_neg(g), acc);
     }
     vals[k] = dd_to_double(acc);
@@ -1520,8 +1541,10 @@ __device__ __forceinline__ void camera_finalize_body(int nf, const int64_t* fb_t
 }
 __global__ void __launch_bounds__(64) k_camera_finalize(int nf, const int64_t* fb_tile_begin,
                                                         const double* tile_part, double* ufull, double* bf,
-                                                        double* rb, Ctrl* ctrl, int with_schur) {
-  camera_finalize_body(nf, fb_tile_begin, tile_part, ufull, bf, rb, ctrl, with_schur, blockIdx.x, gridDim.x);
+                                                        double* rb, Ctrl* ctrl, int with_schur,
+                                                        const int32_t* prior_beg, const double* prior_out) {
+  camera_finalize_body(nf, fb_tile_begin, tile_part, ufull, bf, rb, ctrl, with_schur, prior_beg, prior_out,
+                       blockIdx.x, gridDim.x);
 }
 
 
@@ -2880,7 +2903,7 @@ int upd_blocks(const Sizes& s) {
 
 }  // namespace
 
-int cost_partials_needed(const Sizes& s) { return 4 * kUpdBlocks + cost_grid(s.no); }
+int cost_partials_needed(const Sizes& s) { return 4 * kUpdBlocks + cost_grid(s.no) + 1; }  // + the priors' cost
 
 int launch_pose_tables(const Sizes& s, const Dev& d, const double* poses, cudaStream_t st) {
   k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, poses, d.pose_f, d.pose_dd, d.ctrl, 0, nullptr, nullptr);
@@ -2909,6 +2932,7 @@ static CostArgs make_cost_args(const Sizes& s, const Dev& d, const double* point
   a.n_upd = 0;
   a.recs = nullptr;
   a.last = nullptr;
+  a.n_extra = 0;
   return a;
 }
 
@@ -2925,8 +2949,9 @@ int launch_init_merit(const Sizes& s, const Dev& d, cudaStream_t st) {
   CostArgs a = make_cost_args(s, d, d.points, d.res, d.part, 0);
   const int nb = cost_grid(s.no);
   (s.eucm ? k_cost<true> : k_cost<false>)<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
-  k_init_merit<<<1, 256, 0, st>>>(d.part, nb, d.ctrl);
-  return 3;
+  const int np = launch_prior_eval(s, d, d.poses, 0, 0, d.part + nb, st);
+  k_init_merit<<<1, 256, 0, st>>>(d.part, nb + np, d.ctrl);
+  return 3 + np;
 }
 
 int launch_iteration_begin(const Sizes& s, const Dev& d, cudaStream_t st) {
@@ -3113,9 +3138,11 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
   n += launch_landmark(s, d, make_lin_args(s, d, nu_override, use_override), st, use_override);
   n += launch_intr_linearize(s, d, st);
   n += launch_camera(s, d, use_override ? 0 : 1, st);
+  n += launch_prior_eval(s, d, d.poses, 1, 1, nullptr, st);
   // the last block of the finalisation runs the gradient check of an LM iteration
   k_camera_finalize<<<s.nf, 64, 0, st>>>(s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf, d.rb, d.ctrl,
-                                         use_override ? 0 : 1);
+                                         use_override ? 0 : 1, s.n_prior > 0 ? d.prior_fb_begin : nullptr,
+                                         d.prior_out);
   ++n;
   return n;
 }
@@ -3284,13 +3311,15 @@ static int commit_grid(const Sizes& s) {
 
 int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
   const int nb = cost_grid(s.no);
-  const CostArgs a = make_decide_args(s, d);
+  CostArgs a = make_decide_args(s, d);
+  // the priors' trial cost first: one more partial for the decision
+  a.n_extra = launch_prior_eval(s, d, d.poses_t, 0, 2, a.partials + nb, st);
   (s.eucm ? k_cost<true> : k_cost<false>)<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
   const int cb = commit_grid(s);
   k_commit<<<cb, 256, 0, st>>>(s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res,
                                d.res_lo_t, d.res_lo, s.intr_free ? d.intr_t : nullptr,
                                s.intr_free ? d.intr : nullptr, d.ctrl);
-  return 2;
+  return 2 + a.n_extra;
 }
 
 // ---------------------------------------------------------------------------
@@ -3481,6 +3510,7 @@ cudaError_t launch_total_cost_noalloc(int32_t nc, const double* poses, int32_t n
   a.huber = static_cast<float>(huber > 0 ? huber : 0.0);
   a.huber_dd = split(huber);
   a.respect_skip = 0;
+  a.n_extra = 0;
   const int nb = cost_grid(no);
   k_cost_noalloc<<<nb, kCostThreads, 0, st>>>(a, nc, np);
   k_noalloc_finish<<<1, 256, 0, st>>>(part, nb, cost);
@@ -3610,8 +3640,8 @@ __global__ void __launch_bounds__(kTileThreads) k_camera_tiles_w(WinTab<CamArgs>
 __global__ void __launch_bounds__(64) k_camera_finalize_w(WinTab<FinArgs> t) {
   const WinPos q = win_pos(t);
   const FinArgs a = t.args[q.w];
-  camera_finalize_body(a.nf, a.fb_tile_begin, a.tile_part, a.ufull, a.bf, a.rb, t.ctrl[q.w], a.with_schur, q.b,
-                       q.nb);
+  camera_finalize_body(a.nf, a.fb_tile_begin, a.tile_part, a.ufull, a.bf, a.rb, t.ctrl[q.w], a.with_schur, nullptr,
+                       nullptr, q.b, q.nb);
 }
 __global__ void __launch_bounds__(256) k_schur_dense_w(WinTab<SchurDenseArgs> t) {
   const WinPos q = win_pos(t);
@@ -3684,7 +3714,8 @@ struct BatchTables {
 };
 
 int batch_eligible(const Sizes& s) {
-  return (!s.lin_dd && !s.eucm && !s.intr_free && !s.pcg_mode && s.band_c == 0 && (s.small_dense || s.dense_c > 0) &&
+  return (!s.lin_dd && !s.eucm && !s.intr_free && !s.pcg_mode && s.n_prior == 0 && s.band_c == 0 &&
+          (s.small_dense || s.dense_c > 0) &&
           s.nlchunk > 0 && s.bsub_chunks_ok && s.ntiles > 0 && s.nf > 0)
              ? 1
              : 0;

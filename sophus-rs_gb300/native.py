@@ -166,7 +166,7 @@ EXPORTED = [
     "sgba_optimizer_init", "sgba_optimizer_step", "sgba_optimize", "sgba_get_variables",
     "sgba_get_cost", "sgba_set_variables", "sgba_get_layout", "sgba_export_pattern",
     "sgba_debug_last_system", "sgba_debug_jacobians", "sgba_state_save", "sgba_state_load", "sgba_get_profile",
-    "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_batch_optimize", "sgba_batch_last_stats",
+    "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_batch_optimize", "sgba_batch_last_stats", "sgba_set_pose_priors",
     "sgba_set_linear_solver", "sgba_get_pcg_stats", "sgba_pcg_num_params", "sgba_pcg_model_create",
     "sgba_pcg_model_destroy", "sgba_pcg_model_set_params", "sgba_pcg_model_get_params",
     "sgba_pcg_trainset_create", "sgba_pcg_trainset_destroy", "sgba_pcg_trainset_size", "sgba_pcg_trainset_add",
@@ -236,6 +236,7 @@ def lib():
     L.sgba_batch_optimize.argtypes = [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(OptParamsC),
                                       C.POINTER(IterRecord), C.c_int32, C.POINTER(WindowResult)]
     L.sgba_batch_last_stats.argtypes = [C.POINTER(BatchStats)]
+    L.sgba_set_pose_priors.argtypes = [C.c_void_p, C.c_int32, ip, dp, dp]
     L.sgba_set_linear_solver.argtypes = [C.c_void_p, C.POINTER(LinearSolverC), C.c_void_p]
     L.sgba_get_pcg_stats.argtypes = [C.c_void_p, C.POINTER(PcgStats)]
     L.sgba_pcg_num_params.restype = C.c_int32
@@ -394,6 +395,16 @@ class Problem:
         qq = None if points is None else np.ascontiguousarray(points, dtype=np.float64)
         check(lib().sgba_set_variables(self._h, _dptr(pp) if pp is not None else None,
                                        _dptr(qq) if qq is not None else None))
+
+    def set_pose_priors(self, pose, mean, precision):
+        """sgba_set_pose_priors: Isometry3 priors (pose indices, n x 7 means, n x 6 x 6
+        precisions); an empty set removes them."""
+        pose = np.ascontiguousarray(pose, dtype=np.int32).reshape(-1)
+        n = pose.shape[0]
+        mean = np.ascontiguousarray(mean, dtype=np.float64).reshape(n, 7)
+        precision = np.ascontiguousarray(precision, dtype=np.float64).reshape(n, 6, 6)
+        check(lib().sgba_set_pose_priors(self._h, n, pose.ctypes.data_as(C.POINTER(C.c_int32)) if n else None,
+                                         _dptr(mean) if n else None, _dptr(precision) if n else None))
 
     def cost(self):
         c = C.c_double()
