@@ -14,6 +14,7 @@ from .opt import (  # noqa: F401
     EucmReprojectionTerms,
     HuberKernel,
     Isometry3F64,
+    Isometry3PriorCostTerm,
     LinearSolverEnum,
     LinearSolverError,
     NllsError,
@@ -25,6 +26,7 @@ from .opt import (  # noqa: F401
     PinholeCameraF64,
     PinholeCameraReprojectionCostTerm,
     PinholeReprojectionTerms,
+    PriorTerms,
     RobustKernel,
     SchurCostConnectsTwoMargFamilies,
     SchurMissingFreeOrMarg,

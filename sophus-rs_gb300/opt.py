@@ -213,6 +213,30 @@ class EucmCameraReprojectionCostTerm:
     entity_indices: Any
 
 
+@dataclass
+class Isometry3PriorCostTerm:
+    """isometry_prior_mean (an Isometry3F64 or 7 params), isometry_prior_precision
+    (6x6), entity_indices = [pose] (isometry3_prior.rs)."""
+
+    isometry_prior_mean: Any
+    isometry_prior_precision: Any
+    entity_indices: Any
+
+
+class PriorTerms:
+    """Struct-of-arrays container of Isometry3PriorCostTerm terms."""
+
+    def __init__(self, pose, mean, precision):
+        self.pose = np.ascontiguousarray(pose, dtype=np.int32).reshape(-1)
+        self.mean = np.ascontiguousarray(mean, dtype=np.float64).reshape(-1, 7)
+        self.precision = np.ascontiguousarray(precision, dtype=np.float64).reshape(-1, 6, 6)
+        if not (self.pose.shape[0] == self.mean.shape[0] == self.precision.shape[0]):
+            raise ValueError("prior poses, means and precisions differ in length")
+
+    def __len__(self):
+        return self.pose.shape[0]
+
+
 class PinholeReprojectionTerms:
     """Struct-of-arrays container of many PinholeCameraReprojectionCostTerm."""
 
@@ -233,11 +257,18 @@ class EucmReprojectionTerms(PinholeReprojectionTerms):
 class CostTerms:
     def __init__(self, family_names, terms):
         self.family_names = list(family_names)
-        if isinstance(terms, PinholeReprojectionTerms):
+        if isinstance(terms, (PinholeReprojectionTerms, PriorTerms)):
             self.terms = terms
         else:
             terms = list(terms)
             kinds = {type(t) for t in terms}
+            if kinds == {Isometry3PriorCostTerm}:
+                self.terms = PriorTerms(
+                    [int(np.asarray(t.entity_indices).reshape(-1)[0]) for t in terms],
+                    [t.isometry_prior_mean.params() if isinstance(t.isometry_prior_mean, Isometry3F64)
+                     else np.asarray(t.isometry_prior_mean, float) for t in terms],
+                    [np.asarray(t.isometry_prior_precision, float) for t in terms])
+                return
             if not kinds <= {PinholeCameraReprojectionCostTerm, EucmCameraReprojectionCostTerm} or len(kinds) > 1:
                 raise NotOnGpuPath("only PinholeCameraReprojectionCostTerm or EucmCameraReprojectionCostTerm "
                                    "residuals (one kind per CostTerms) run on this backend")
@@ -404,10 +435,22 @@ def _point_array(members):
     return np.ascontiguousarray(np.asarray(members, dtype=np.float64).reshape(-1, 3))
 
 
-def _extract_problem(variables, cost_fns):
-    if len(cost_fns) != 1:
+def _split_costs(cost_fns):
+    """The reprojection CostFn and the optional pose-prior CostFn."""
+    reproj = [cf for cf in cost_fns if not isinstance(cf.cost_terms.terms, PriorTerms)]
+    priors = [cf for cf in cost_fns if isinstance(cf.cost_terms.terms, PriorTerms)]
+    if len(reproj) != 1:
         raise NotOnGpuPath("exactly one reprojection CostFn is supported on the GPU path")
-    cf = cost_fns[0]
+    if len(priors) > 1:
+        raise NotOnGpuPath("at most one Isometry3PriorCostTerm CostFn is supported on the GPU path")
+    for cf in priors:
+        if cf.robust_kernel is not None:
+            raise NotOnGpuPath("a robust kernel on the pose priors is not on this path")
+    return reproj[0], (priors[0] if priors else None)
+
+
+def _extract_problem(variables, cost_fns):
+    cf, prior_cf = _split_costs(cost_fns)
     names = cf.cost_family_names()
     if len(names) != 3:
         raise NotOnGpuPath("reprojection cost needs (intrinsics, pose, point) families")
@@ -450,7 +493,18 @@ def _extract_problem(variables, cost_fns):
     if eucm:
         prob.camera_model = native.CAMERA_EUCM
         prob.eucm_alpha_beta = np.asarray(cparams[4:6], float).copy()
+    prob.priors = None
+    if prior_cf is not None:
+        if prior_cf.cost_family_names() != [names[1]]:
+            raise NotOnGpuPath("the pose priors must act on the reprojection cost's pose family")
+        prob.priors = prior_cf.cost_terms.terms
     return prob, names
+
+
+def _set_priors(gp, prob):
+    if getattr(prob, "priors", None) is not None:
+        t = prob.priors
+        gp.set_pose_priors(t.pose, t.mean, t.precision)
 
 
 def _step_info(rec, k):
@@ -496,6 +550,7 @@ class Optimizer:
         self._names = names
         self._params = params
         self._gpu = native.Problem(prob, device=device)
+        _set_priors(self._gpu, prob)
         self._gpu.init(params)
         self._steps = []
 
@@ -530,6 +585,7 @@ def optimize_nlls(variables, cost_fns, eq_fns, params, device=-1):
     _validate_solver_config(variables, cost_fns, eq_fns, params)
     prob, names = _extract_problem(variables, cost_fns)
     with native.Problem(prob, device=device) as gp:
+        _set_priors(gp, prob)
         recs, _ = gp.optimize(params)
         poses, points = gp.variables()
         intr = gp.intrinsics() if prob.intrinsics_free else None

@@ -111,3 +111,32 @@ def test_prior_set_replaced_and_removed(pkg):
             gp.set_pose_priors([1], [bad], [np.eye(6)])
     assert [r.merit for r in removed] == [r.merit for r in plain]
     assert with_prior[0].merit > plain[0].merit
+
+
+def test_python_mirror_prior_cost_fn(pkg, oracle):
+    """optimize_nlls of the Python mirror with a reprojection CostFn and an
+    Isometry3PriorCostTerm CostFn on the pose family (cam_calib.rs:249-342's
+    shape: every pose free, priors on poses 0 and 1)."""
+    prob = pkg.synth.generate(pkg.synth.CIRCLE, n_cam=5, n_pt=60, seed=pkg.synth.BASE_SEED + 23)
+    prob.pose_const = np.zeros(prob.n_cam, np.uint8)
+    K = pkg.VarKind
+    variables = (pkg.VarBuilder.new()
+                 .add_family("cams", pkg.VarFamily.new(K.Conditioned, [pkg.PinholeCameraF64(prob.intrinsics)]))
+                 .add_family("poses", pkg.VarFamily.new(K.Free, [pkg.Isometry3F64(p) for p in prob.poses]))
+                 .add_family("points", pkg.VarFamily.new(K.Marginalized, prob.points))
+                 .build())
+    idx = np.stack([np.zeros(prob.n_obs, np.int64), prob.obs_cam, prob.obs_pt], axis=1)
+    reproj = pkg.CostFn.new_boxed_robust(
+        None, pkg.CostTerms.new(["cams", "poses", "points"], pkg.PinholeReprojectionTerms(prob.obs_uv, idx)),
+        pkg.RobustKernel.Huber(pkg.HuberKernel.new(prob.huber_delta)))
+    W = 1e4 * np.eye(6)
+    priors = pkg.CostFn.new_boxed(None, pkg.CostTerms.new(
+        ["poses"], [pkg.Isometry3PriorCostTerm(pkg.Isometry3F64(prob.poses_true[j]), W, [j]) for j in (0, 1)]))
+    params = fixed_iter_params(pkg, 8, prob.initial_lm_damping)
+    sol = pkg.optimize_nlls(variables, [reproj, priors], [], params)
+    pp = _with_priors(prob, [0, 1], prob.poses_true[:2], [W, W])
+    orecs, _, _ = oracle.optimize(pp, params, n_threads=8)
+    assert len(sol.steps) == len(orecs)
+    g = np.array([st.merit for st in sol.steps])
+    o = np.array([r.merit for r in orecs])
+    assert np.max(np.abs(g - o) / o) < COST_RTOL

@@ -124,3 +124,33 @@ def test_concurrent_validation_reports_first_bad_observation(pkg):
     for th in threads:
         th.join()
     assert not errors, errors
+
+
+def test_prior_cost_fn_checks_before_any_gpu_call(pkg):
+    """The mirror accepts one Isometry3PriorCostTerm CostFn on the reprojection
+    cost's pose family, without a robust kernel; other shapes raise
+    NotOnGpuPath before a problem is created."""
+    prob = pkg.synth.generate(pkg.synth.CIRCLE, n_cam=4, n_pt=20, seed=7)
+    K = pkg.VarKind
+    variables = (pkg.VarBuilder.new()
+                 .add_family("cams", pkg.VarFamily.new(K.Conditioned, [pkg.PinholeCameraF64(prob.intrinsics)]))
+                 .add_family("poses", pkg.VarFamily.new_with_const_ids(
+                     K.Free, [pkg.Isometry3F64(p) for p in prob.poses], [0]))
+                 .add_family("points", pkg.VarFamily.new(K.Marginalized, prob.points))
+                 .build())
+    idx = np.stack([np.zeros(prob.n_obs, np.int64), prob.obs_cam, prob.obs_pt], axis=1)
+    reproj = pkg.CostFn.new_boxed(
+        None, pkg.CostTerms.new(["cams", "poses", "points"], pkg.PinholeReprojectionTerms(prob.obs_uv, idx)))
+    term = pkg.Isometry3PriorCostTerm(prob.poses[1], np.eye(6), [1])
+    prior = pkg.CostFn.new_boxed(None, pkg.CostTerms.new(["poses"], [term]))
+    assert isinstance(prior.cost_terms.terms, pkg.PriorTerms) and len(prior.cost_terms.terms) == 1
+    params = pkg.OptParams(num_iterations=2, solver=pkg.LinearSolverEnum.SchurBlockSparseLdlt)
+    with pytest.raises(pkg.NotOnGpuPath):
+        pkg.optimize_nlls(variables, [reproj, prior, prior], [], params)
+    robust = pkg.CostFn.new_boxed_robust(None, pkg.CostTerms.new(["poses"], [term]),
+                                         pkg.RobustKernel.Huber(pkg.HuberKernel.new(1.0)))
+    with pytest.raises(pkg.NotOnGpuPath):
+        pkg.optimize_nlls(variables, [reproj, robust], [], params)
+    other = pkg.CostFn.new_boxed(None, pkg.CostTerms.new(["cams"], [term]))
+    with pytest.raises(pkg.NotOnGpuPath):
+        pkg.optimize_nlls(variables, [reproj, other], [], params)
