@@ -150,6 +150,25 @@ typedef struct {
 /* sgba_problem_create with options (NULL: the defaults). */
 int sgba_problem_create_ex(const sgba_problem_desc *desc, const sgba_problem_options *options, int32_t device,
                            sgba_problem **out);
+
+/* Pose-graph edges: a cost function of PoseGraph3CostTerm terms
+ * (crates/sophus_opt/src/nlls/functor_library/costs/pose_graph3.rs) beside
+ * the reprojection cost.  Edge k joins poses edge_pose[2k] = m and
+ * edge_pose[2k + 1] = n (m != n) with the measured pose_m_from_pose_n
+ * edge_m_from_n + 7k (qw qx qy qz tx ty tz); residual log(T_m^-1 T_n M^-1),
+ * cost g^T g.  Edges with equal (m, n) form one reduced term.  A term between
+ * two free poses adds their block to the reduced camera system; the edges
+ * fix the scale (no gauge projection).  Not with free camera params. */
+typedef struct {
+  int32_t n_edge;
+  const int32_t *edge_pose;      /* n_edge x 2 */
+  const double *edge_m_from_n;   /* n_edge x 7 */
+} sgba_pose_graph;
+/* sgba_problem_create_ex with pose-graph edges (graph NULL or n_edge 0:
+ * none).  Problems with edges run on their own streams in
+ * sgba_batch_optimize. */
+int sgba_problem_create_graph(const sgba_problem_desc *desc, const sgba_problem_options *options,
+                              const sgba_pose_graph *graph, int32_t device, sgba_problem **out);
 int sgba_problem_destroy(sgba_problem *p);
 
 /* Optimizer::new: validates the solver configuration

@@ -120,6 +120,15 @@ pub struct sgba_window_result {
     pub final_cost: f64,
 }
 
+/// Pose-graph edges of `sgba_problem_create_graph`.
+#[repr(C)]
+#[derive(Clone, Copy, Debug)]
+pub struct sgba_pose_graph {
+    pub n_edge: i32,
+    pub edge_pose: *const i32,
+    pub edge_m_from_n: *const f64,
+}
+
 /// What the last batched optimisation did on its batched path.
 #[repr(C)]
 #[derive(Clone, Copy, Debug, Default)]
@@ -230,6 +239,13 @@ extern "C" {
     pub fn sgba_problem_create_ex(
         desc: *const sgba_problem_desc,
         options: *const sgba_problem_options,
+        device: i32,
+        out: *mut *mut sgba_problem,
+    ) -> c_int;
+    pub fn sgba_problem_create_graph(
+        desc: *const sgba_problem_desc,
+        options: *const sgba_problem_options,
+        graph: *const sgba_pose_graph,
         device: i32,
         out: *mut *mut sgba_problem,
     ) -> c_int;

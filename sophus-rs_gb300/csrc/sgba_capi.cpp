@@ -632,6 +632,72 @@ int build_plan(const sgba_problem_desc* d, Plan* P) {
   return SGBA_OK;
 }
 
+// Pose-graph edges (PoseGraph3CostTerm): validated, sorted by (m, n) as
+// CostFn::sort orders them, reduced into terms of equal (m, n); each term
+// adds one damping count to each of its free poses (nu I once per reduced
+// term, cost_system.rs:190-273); the per-free-block list of (term, side)
+// records.  The edges fix the scale: no gauge projection.
+int build_edges(const sgba_pose_graph* g, Plan* P) {
+  if (!g || g->n_edge == 0) return SGBA_OK;
+  const int32_t n = g->n_edge;
+  if (n < 0) return set_error(SGBA_ERR_INVALID_ARGUMENT, "negative edge count");
+  if (!g->edge_pose || !g->edge_m_from_n) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL edge array");
+  for (int32_t k = 0; k < n; ++k) {
+    const int32_t m = g->edge_pose[2 * k], q = g->edge_pose[2 * k + 1];
+    if (m < 0 || m >= P->nc || q < 0 || q >= P->nc || m == q)
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "edge %d: poses (%d, %d) out of range or equal", k, m, q);
+    if (!finite_all(g->edge_m_from_n + 7 * k, 7))
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "edge %d: non-finite measurement", k);
+    if (!quat_valid(g->edge_m_from_n + 7 * k))
+      return set_error(SGBA_ERR_INVALID_PARAMS, "edge %d: invalid quaternion", k);
+  }
+  std::vector<int32_t> ord(n);
+  for (int32_t k = 0; k < n; ++k) ord[k] = k;
+  std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) {
+    if (g->edge_pose[2 * a] != g->edge_pose[2 * b]) return g->edge_pose[2 * a] < g->edge_pose[2 * b];
+    return g->edge_pose[2 * a + 1] < g->edge_pose[2 * b + 1];
+  });
+  P->edge_m.resize(n);
+  P->edge_n.resize(n);
+  P->edge_mn.resize(7 * static_cast<size_t>(n));
+  P->eterm_begin.clear();
+  P->eterm_fm.clear();
+  P->eterm_fn.clear();
+  for (int32_t k = 0; k < n; ++k) {
+    const int32_t o = ord[k];
+    P->edge_m[k] = g->edge_pose[2 * o];
+    P->edge_n[k] = g->edge_pose[2 * o + 1];
+    double* mn = &P->edge_mn[7 * static_cast<size_t>(k)];
+    std::memcpy(mn, g->edge_m_from_n + 7 * o, sizeof(double) * 7);
+    if (!(0.0 <= mn[0]))
+      for (int q = 0; q < 4; ++q) mn[q] = -mn[q];
+    if (k == 0 || P->edge_m[k] != P->edge_m[k - 1] || P->edge_n[k] != P->edge_n[k - 1]) {
+      P->eterm_begin.push_back(k);
+      P->eterm_fm.push_back(P->pose_fb[P->edge_m[k]]);
+      P->eterm_fn.push_back(P->pose_fb[P->edge_n[k]]);
+    }
+  }
+  const int32_t nt = static_cast<int32_t>(P->eterm_fm.size());
+  P->eterm_begin.push_back(n);
+  // per free block its records (term t side 0 -> slot 2t, side 1 -> 2t + 1), in term order
+  P->efb_begin.assign(P->nf + 1, 0);
+  for (int32_t t = 0; t < nt; ++t) {
+    if (P->eterm_fm[t] >= 0) ++P->efb_begin[P->eterm_fm[t] + 1];
+    if (P->eterm_fn[t] >= 0) ++P->efb_begin[P->eterm_fn[t] + 1];
+  }
+  for (int f = 0; f < P->nf; ++f) P->efb_begin[f + 1] += P->efb_begin[f];
+  P->efb_slot.assign(P->efb_begin[P->nf], 0);
+  std::vector<int32_t> fill(P->efb_begin.begin(), P->efb_begin.end() - 1);
+  for (int32_t t = 0; t < nt; ++t) {
+    if (P->eterm_fm[t] >= 0) P->efb_slot[fill[P->eterm_fm[t]]++] = 2 * t;
+    if (P->eterm_fn[t] >= 0) P->efb_slot[fill[P->eterm_fn[t]]++] = 2 * t + 1;
+    if (P->eterm_fm[t] >= 0) P->cnt_f[P->eterm_fm[t]] += 1.0;
+    if (P->eterm_fn[t] >= 0) P->cnt_f[P->eterm_fn[t]] += 1.0;
+  }
+  P->gauge_kind = 0;
+  return SGBA_OK;
+}
+
 // Reduced camera system: lower blocks (row >= col) of the Schur fill
 // (crates/sophus_opt/src/nlls/damped_hessian.rs:261-325) and the observation
 // pairs summed into each.  The pairs per block are counted on the device, the
@@ -657,13 +723,36 @@ int build_schur_pattern(sgba_problem* p) {
   if (e != cudaSuccess) return set_error(SGBA_ERR_CUDA, "Schur pattern (counts): %s", cudaGetErrorString(e));
   std::vector<int32_t> bid(nlow, -1);
   int64_t nb = 0;
+  // pose-graph terms between two free poses need their block even where no
+  // point joins the two
+  std::vector<char> eforce(P.eterm_fm.empty() ? 0 : nlow, 0);
+  for (size_t t = 0; t < P.eterm_fm.size(); ++t)
+    if (P.eterm_fm[t] >= 0 && P.eterm_fn[t] >= 0)
+      eforce[lid(std::max(P.eterm_fm[t], P.eterm_fn[t]), std::min(P.eterm_fm[t], P.eterm_fn[t]))] = 1;
   for (int r = 0; r < nf; ++r)
     for (int c = 0; c <= r; ++c)
-      if (cnt[lid(r, c)] > 0 || (r == c && P.cnt_f[r] > 0)) {
+      if (cnt[lid(r, c)] > 0 || (r == c && P.cnt_f[r] > 0) || (!eforce.empty() && eforce[lid(r, c)])) {
         bid[lid(r, c)] = static_cast<int32_t>(nb++);
         P.sb_row.push_back(r);
         P.sb_col.push_back(c);
       }
+  if (!P.eterm_fm.empty()) {
+    // per block the terms landing there, in term order (bit 31: the block's
+    // rows are pose n's, i.e. J_m^T J_n transposed)
+    std::vector<std::vector<int32_t>> lists(nb);
+    for (size_t t = 0; t < P.eterm_fm.size(); ++t) {
+      const int fm = P.eterm_fm[t], fn = P.eterm_fn[t];
+      if (fm < 0 || fn < 0) continue;
+      const int32_t b = bid[lid(std::max(fm, fn), std::min(fm, fn))];
+      lists[b].push_back(static_cast<int32_t>(t) | (fm > fn ? 0 : static_cast<int32_t>(0x80000000u)));
+    }
+    P.eblk_begin.assign(nb + 1, 0);
+    P.eblk_term.clear();
+    for (int64_t b = 0; b < nb; ++b) {
+      P.eblk_term.insert(P.eblk_term.end(), lists[b].begin(), lists[b].end());
+      P.eblk_begin[b + 1] = static_cast<int32_t>(P.eblk_term.size());
+    }
+  }
   P.sb_pair_begin.assign(nb + 1, 0);
   for (int64_t b = 0; b < nb; ++b) P.sb_pair_begin[b + 1] = P.sb_pair_begin[b] + cnt[lid(P.sb_row[b], P.sb_col[b])];
   const int64_t npairs = P.sb_pair_begin[nb];
@@ -781,6 +870,23 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
     SGBA_CK(cudaMemsetAsync(d.slow_count, 0, sizeof(int32_t), p->stream));
   }
   if ((st = build_schur_pattern(p))) return st;
+  s.n_edge = static_cast<int>(P.edge_m.size());
+  s.n_eterm = static_cast<int>(P.eterm_fm.size());
+  if (s.n_edge > 0) {
+    const size_t nt = static_cast<size_t>(s.n_eterm);
+    if ((st = dev_upload(p, &d.edge_m, P.edge_m))) return st;
+    if ((st = dev_upload(p, &d.edge_n, P.edge_n))) return st;
+    if ((st = dev_upload(p, &d.edge_mn, P.edge_mn))) return st;
+    if ((st = dev_upload(p, &d.eterm_begin, P.eterm_begin))) return st;
+    if ((st = dev_upload(p, &d.eterm_fm, P.eterm_fm))) return st;
+    if ((st = dev_upload(p, &d.eterm_fn, P.eterm_fn))) return st;
+    if ((st = dev_alloc(p, &d.edge_out, 2 * nt * sgba::kPriorOut))) return st;
+    if ((st = dev_alloc(p, &d.edge_hmn, 36 * nt))) return st;
+    if ((st = dev_upload(p, &d.efb_begin, P.efb_begin))) return st;
+    if ((st = dev_upload(p, &d.efb_slot, P.efb_slot))) return st;
+    if ((st = dev_upload(p, &d.eblk_begin, P.eblk_begin))) return st;
+    if ((st = dev_upload(p, &d.eblk_term, P.eblk_term))) return st;
+  }
   s.nsb = static_cast<int64_t>(P.sb_row.size());
   s.nchunk = P.chunk_begin.empty() ? 0 : static_cast<int64_t>(P.chunk_begin.size()) - 1;
   if ((st = dev_upload(p, &d.sb_row, P.sb_row))) return st;
@@ -945,11 +1051,16 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
   // by launch latency, where float-float costs nothing measurable), where the
   // FP32 EUCM Jacobians left 7.6e-7 in the cost of the reference's
   // 10-camera benchmark scene.
-  s.lin_dd = (loop_shaped || (s.eucm && (p->intr_free || s.small_dense))) ? 1 : 0;
+  // Problems with pose-graph edges get it too: an edge's weight (residual in
+  // radians and meters, unit weight) is ~1e-6 of a pixel term's, so the edges
+  // hold the scale only weakly, and FP32 products in S (relative error ~1e-7)
+  // moved the step along that direction by ~10 % (measured on an 8-camera
+  // circle with odometry edges).
+  s.lin_dd = (loop_shaped || (s.eucm && (p->intr_free || s.small_dense)) || s.n_edge > 0) ? 1 : 0;
   // S by tiles of pose blocks when nearly every block of S is present and a
   // point is seen by at least half the free poses on average (local windows):
   // each point's Z is then streamed once per tile instead of once per pair
-  s.schur_dense = (!s.lin_dd && !p->intr_free && nearly_dense &&
+  s.schur_dense = (!s.lin_dd && !p->intr_free && s.n_edge == 0 && nearly_dense &&
                    2 * P.ng >= static_cast<int64_t>(P.np) * static_cast<int64_t>(P.nf))
                       ? 1
                       : 0;
@@ -1062,6 +1173,11 @@ int sgba_problem_create(const sgba_problem_desc* desc, int32_t device, sgba_prob
 
 int sgba_problem_create_ex(const sgba_problem_desc* desc, const sgba_problem_options* opts, int32_t device,
                            sgba_problem** out) {
+  return sgba_problem_create_graph(desc, opts, nullptr, device, out);
+}
+
+int sgba_problem_create_graph(const sgba_problem_desc* desc, const sgba_problem_options* opts,
+                              const sgba_pose_graph* graph, int32_t device, sgba_problem** out) {
   if (!out) return set_error(SGBA_ERR_INVALID_ARGUMENT, "out is NULL");
   *out = nullptr;
   if (!desc) return set_error(SGBA_ERR_INVALID_ARGUMENT, "desc is NULL");
@@ -1084,6 +1200,12 @@ int sgba_problem_create_ex(const sgba_problem_desc* desc, const sgba_problem_opt
     p->eucm_ab[1] = opts->eucm_alpha_beta[1];
   }
   int st = build_plan(desc, &p->plan);
+  if (st) { delete p; return st; }
+  if (graph && graph->n_edge != 0 && p->intr_free) {
+    delete p;
+    return set_error(SGBA_ERR_UNSUPPORTED, "pose-graph edges with free camera params are not on this path");
+  }
+  st = build_edges(graph, &p->plan);
   if (st) { delete p; return st; }
   if (p->plan.nf > kMaxDenseFree) {
     const int nf = p->plan.nf;

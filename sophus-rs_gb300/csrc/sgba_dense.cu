@@ -1134,7 +1134,9 @@ DenseArgs dense_cluster_args(const Sizes& s, const Dev& d) {
   a.fb_pose = d.fb_pose;
   for (int k = 0; k < 3; ++k) a.center[k] = s.gauge_center[k];
   a.npose = 6 * s.nf;
-  a.refine = s.n6 <= kRefineSmallN ? kRefineSmall : kRefine;
+  // weakly held directions (pose-graph edges against pixel terms) need the
+  // refinement to run longer; it stops once converged
+  a.refine = (s.n6 <= kRefineSmallN || s.n_edge > 0) ? kRefineSmall : kRefine;
   return a;
 }
 

@@ -125,6 +125,15 @@ struct Plan {
   // gauge: 0 none, 1 scale about gauge_center
   int gauge_kind = 0;
   double gauge_center[3] = {0, 0, 0};
+  // pose-graph edges (PoseGraph3CostTerm), sorted by (m, n); reduced terms =
+  // distinct (m, n): their edge ranges and free blocks (-1: constant pose);
+  // per lower block of S the terms whose off-diagonal block lands there
+  // (term id, bit 31: transposed), per free block its (term, side) records
+  std::vector<int32_t> edge_m, edge_n;
+  std::vector<double> edge_mn;
+  std::vector<int32_t> eterm_begin, eterm_fm, eterm_fn;
+  std::vector<int32_t> eblk_begin, eblk_term;
+  std::vector<int32_t> efb_begin, efb_slot;
 };
 
 // Device buffers of one problem.
@@ -167,6 +176,21 @@ struct Dev {
   double* prior_out = nullptr;
   int32_t* prior_fb_begin = nullptr;
   int prior_cap = 0;
+  // pose-graph edges (sgba_prior.cu): sorted edges, reduced terms, their
+  // records (side 0: m, side 1: n; J^T J (36) and J^T g (6) each) and the
+  // off-diagonal J_m^T J_n (36) per term; the CSR lists of Plan
+  int32_t* edge_m = nullptr;
+  int32_t* edge_n = nullptr;
+  double* edge_mn = nullptr;
+  int32_t* eterm_begin = nullptr;
+  int32_t* eterm_fm = nullptr;
+  int32_t* eterm_fn = nullptr;
+  double* edge_out = nullptr;
+  double* edge_hmn = nullptr;
+  int32_t* eblk_begin = nullptr;
+  int32_t* eblk_term = nullptr;
+  int32_t* efb_begin = nullptr;
+  int32_t* efb_slot = nullptr;
   int32_t* slow_list = nullptr;    // points redone in float-float this iteration
   int32_t* slow_count = nullptr;
   // state
@@ -347,6 +371,8 @@ struct Sizes {
   int lin_dd;          // float-float linearization (Jacobians, products and Z in float-float)
   int schur_dense;     // S by tiles of pose blocks (nearly dense S and Z: local windows), not by pairs
   int n_prior;         // pose priors (a second cost function; 0: none)
+  int n_edge;          // pose-graph edges (0: none)
+  int n_eterm;         // their reduced terms (distinct (m, n))
   int intr_free;       // the camera params are Free: one more 6-row block, last in S
   int intr_nk;         // free params: 4 (pinhole, padded to 6 rows) or 6 (EUCM)
   int eucm;            // the camera is the enhanced unified camera model (else the pinhole)
@@ -462,6 +488,11 @@ struct PriorArgs {
 // step is skipped.  Returns the launches (0 without priors).
 int launch_prior_eval(const Sizes& s, const Dev& d, const double* poses, int lin, int gate, double* cost_sum,
                       cudaStream_t st);
+// The pose-graph edges at `poses` (PoseGraph3CostTerm): with lin, per reduced
+// term the records of both sides into Dev::edge_out and J_m^T J_n into
+// Dev::edge_hmn; their total cost into *cost_sum.  The same gates.
+int launch_edge_eval(const Sizes& s, const Dev& d, const double* poses, int lin, int gate, double* cost_sum,
+                     cudaStream_t st);
 
 // ---- batched local windows ----------------------------------------------
 // A batch launches every kernel of an LM iteration once for many independent

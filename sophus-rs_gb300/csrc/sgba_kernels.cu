@@ -1462,7 +1462,8 @@ __device__ __forceinline__ void camera_finalize_body(int nf, const int64_t* fb_t
                                                         const double* tile_part, double* ufull, double* bf,
                                                         double* rb, Ctrl* ctrl, int with_schur,
                                                         const int32_t* prior_beg, const double* prior_out,
-                                                        int bid_, int nblk_) {
+                                                        const int32_t* e_beg, const int32_t* e_slot,
+                                                        const double* e_out, int bid_, int nblk_) {
   if (halted(ctrl)) return;
   const int fb = bid_;
   const int k = threadIdx.x;
@@ -1471,10 +1472,11 @@ __device__ __forceinline__ void camera_finalize_body(int nf, const int64_t* fb_t
     dd acc = dd_make(0.f, 0.f);
     for (int64_t t = fb_tile_begin[fb]; t < fb_tile_begin[fb + 1]; ++t)
       acc = dd_add(acc, dd_from_double(tile_part[t * kTileVals + k]));
-    // pose priors on this pose (sgba_prior.cu): J^T W J into the 21 upper
-    // entries, J^T W g with the gradient sums, in prior order
+    // cost functions on the poses alone (sgba_prior.cu): the priors on this
+    // pose in prior order, then its pose-graph records in term order; J^T W J
+    // into the 21 upper entries, J^T W g with the gradient sums
     dd pr = dd_make(0.f, 0.f);
-    if (prior_beg) {
+    if (prior_beg || e_beg) {
       int idx;
       if (k < 21) {
         int a = 0, rem = k;
@@ -1483,8 +1485,12 @@ __device__ __forceinline__ void camera_finalize_body(int nf, const int64_t* fb_t
       } else {
         idx = 36 + (k < 27 ? k - 21 : k - 27);
       }
-      for (int q = prior_beg[fb]; q < prior_beg[fb + 1]; ++q)
-        pr = dd_add(pr, dd_from_double(prior_out[static_cast<int64_t>(kPriorOut) * q + idx]));
+      if (prior_beg)
+        for (int q = prior_beg[fb]; q < prior_beg[fb + 1]; ++q)
+          pr = dd_add(pr, dd_from_double(prior_out[static_cast<int64_t>(kPriorOut) * q + idx]));
+      if (e_beg)
+        for (int q = e_beg[fb]; q < e_beg[fb + 1]; ++q)
+          pr = dd_add(pr, dd_from_double(e_out[static_cast<int64_t>(kPriorOut) * e_slot[q] + idx]));
     }
     if (k < 21) {
       acc = dd_add(acc, pr);
@@ -1542,9 +1548,11 @@ __device__ __forceinline__ void camera_finalize_body(int nf, const int64_t* fb_t
 __global__ void __launch_bounds__(64) k_camera_finalize(int nf, const int64_t* fb_tile_begin,
                                                         const double* tile_part, double* ufull, double* bf,
                                                         double* rb, Ctrl* ctrl, int with_schur,
-                                                        const int32_t* prior_beg, const double* prior_out) {
-  camera_finalize_body(nf, fb_tile_begin, tile_part, ufull, bf, rb, ctrl, with_schur, prior_beg, prior_out,
-                       blockIdx.x, gridDim.x);
+                                                        const int32_t* prior_beg, const double* prior_out,
+                                                        const int32_t* e_beg, const int32_t* e_slot,
+                                                        const double* e_out) {
+  camera_finalize_body(nf, fb_tile_begin, tile_part, ufull, bf, rb, ctrl, with_schur, prior_beg, prior_out, e_beg,
+                       e_slot, e_out, blockIdx.x, gridDim.x);
 }
 
 
@@ -1571,6 +1579,11 @@ struct SchurArgs {
   double* S;
   float2* S2;  // float-float copy (may be null)
   int n6;
+  // pose-graph edges: per lower block the terms whose J_m^T J_n lands there
+  // (bit 31: transposed), or null
+  const int32_t* eblk_begin;
+  const int32_t* eblk_term;
+  const double* e_hmn;
 };
 
 __device__ __forceinline__ void load_z(const float* zmat, int g, float* z) {
@@ -1724,6 +1737,13 @@ __device__ __forceinline__ void schur_reduce_body(SchurArgs a, const Ctrl* ctrl,
       } else {
         vd = dd_neg(t);
       }
+      if (a.eblk_begin)
+        for (int q = a.eblk_begin[blk]; q < a.eblk_begin[blk + 1]; ++q) {
+          const int32_t tt = a.eblk_term[q];
+          const int64_t term = tt & 0x7fffffff;
+          const double h = (tt < 0) ? a.e_hmn[36 * term + cc * 6 + r] : a.e_hmn[36 * term + r * 6 + cc];
+          vd = dd_add(vd, dd_from_double(h));
+        }
       const double v = dd_to_double(vd);
       const int64_t row = 6 * j + r, col = 6 * k + cc;
       a.S[row * a.n6 + col] = v;
@@ -2903,7 +2923,7 @@ int upd_blocks(const Sizes& s) {
 
 }  // namespace
 
-int cost_partials_needed(const Sizes& s) { return 4 * kUpdBlocks + cost_grid(s.no) + 1; }  // + the priors' cost
+int cost_partials_needed(const Sizes& s) { return 4 * kUpdBlocks + cost_grid(s.no) + 2; }  // + priors', edges' cost
 
 int launch_pose_tables(const Sizes& s, const Dev& d, const double* poses, cudaStream_t st) {
   k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, poses, d.pose_f, d.pose_dd, d.ctrl, 0, nullptr, nullptr);
@@ -2950,8 +2970,9 @@ int launch_init_merit(const Sizes& s, const Dev& d, cudaStream_t st) {
   const int nb = cost_grid(s.no);
   (s.eucm ? k_cost<true> : k_cost<false>)<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
   const int np = launch_prior_eval(s, d, d.poses, 0, 0, d.part + nb, st);
-  k_init_merit<<<1, 256, 0, st>>>(d.part, nb + np, d.ctrl);
-  return 3 + np;
+  const int ne = launch_edge_eval(s, d, d.poses, 0, 0, d.part + nb + np, st);
+  k_init_merit<<<1, 256, 0, st>>>(d.part, nb + np + ne, d.ctrl);
+  return 3 + np + ne;
 }
 
 int launch_iteration_begin(const Sizes& s, const Dev& d, cudaStream_t st) {
@@ -3139,10 +3160,12 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
   n += launch_intr_linearize(s, d, st);
   n += launch_camera(s, d, use_override ? 0 : 1, st);
   n += launch_prior_eval(s, d, d.poses, 1, 1, nullptr, st);
+  n += launch_edge_eval(s, d, d.poses, 1, 1, nullptr, st);
   // the last block of the finalisation runs the gradient check of an LM iteration
   k_camera_finalize<<<s.nf, 64, 0, st>>>(s.nf, d.fb_tile_begin, d.tile_part, d.ufull, d.bf, d.rb, d.ctrl,
                                          use_override ? 0 : 1, s.n_prior > 0 ? d.prior_fb_begin : nullptr,
-                                         d.prior_out);
+                                         d.prior_out, s.n_edge > 0 ? d.efb_begin : nullptr, d.efb_slot,
+                                         d.edge_out);
   ++n;
   return n;
 }
@@ -3165,6 +3188,9 @@ static SchurArgs make_schur_args(const Sizes& s, const Dev& d) {
   a.chunk_begin = d.chunk_begin;
   a.block_chunk_begin = d.block_chunk_begin;
   a.part = d.schur_part;
+  a.eblk_begin = s.n_edge > 0 ? d.eblk_begin : nullptr;
+  a.eblk_term = d.eblk_term;
+  a.e_hmn = d.edge_hmn;
   return a;
 }
 
@@ -3314,6 +3340,7 @@ int launch_decide(const Sizes& s, const Dev& d, cudaStream_t st) {
   CostArgs a = make_decide_args(s, d);
   // the priors' trial cost first: one more partial for the decision
   a.n_extra = launch_prior_eval(s, d, d.poses_t, 0, 2, a.partials + nb, st);
+  a.n_extra += launch_edge_eval(s, d, d.poses_t, 0, 2, a.partials + nb + a.n_extra, st);
   (s.eucm ? k_cost<true> : k_cost<false>)<<<nb, kCostThreads, 0, st>>>(a, d.ctrl);
   const int cb = commit_grid(s);
   k_commit<<<cb, 256, 0, st>>>(s.nc, s.np, s.no, d.poses_t, d.poses, d.points_t, d.points, d.res_t, d.res,
@@ -3641,7 +3668,7 @@ __global__ void __launch_bounds__(64) k_camera_finalize_w(WinTab<FinArgs> t) {
   const WinPos q = win_pos(t);
   const FinArgs a = t.args[q.w];
   camera_finalize_body(a.nf, a.fb_tile_begin, a.tile_part, a.ufull, a.bf, a.rb, t.ctrl[q.w], a.with_schur, nullptr,
-                       nullptr, q.b, q.nb);
+                       nullptr, nullptr, nullptr, nullptr, q.b, q.nb);
 }
 __global__ void __launch_bounds__(256) k_schur_dense_w(WinTab<SchurDenseArgs> t) {
   const WinPos q = win_pos(t);
@@ -3714,7 +3741,7 @@ struct BatchTables {
 };
 
 int batch_eligible(const Sizes& s) {
-  return (!s.lin_dd && !s.eucm && !s.intr_free && !s.pcg_mode && s.n_prior == 0 && s.band_c == 0 &&
+  return (!s.lin_dd && !s.eucm && !s.intr_free && !s.pcg_mode && s.n_prior == 0 && s.n_edge == 0 && s.band_c == 0 &&
           (s.small_dense || s.dense_c > 0) &&
           s.nlchunk > 0 && s.bsub_chunks_ok && s.ntiles > 0 && s.nf > 0)
              ? 1

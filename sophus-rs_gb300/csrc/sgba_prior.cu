@@ -1,5 +1,7 @@
-// sgba_prior.cu -- the pose prior cost function on the GPU
-// (Isometry3PriorCostTerm, crates/sophus_opt/src/nlls/functor_library/costs/isometry3_prior.rs).
+// sgba_prior.cu -- cost functions on the poses alone, on the GPU: the pose
+// prior (Isometry3PriorCostTerm,
+// crates/sophus_opt/src/nlls/functor_library/costs/isometry3_prior.rs) and
+// the pose-graph edge (PoseGraph3CostTerm, .../costs/pose_graph3.rs).
 //
 // Each prior k on pose j has a mean E_k and a 6x6 precision W_k; its residual
 // is g = log(T_j E_k^-1) and its Jacobian J the derivative of
@@ -12,6 +14,14 @@
 // per pose with a prior: one reduced term of the prior cost function,
 // cost_system.rs:229-236), the costs into one extra partial of the merit and
 // of the trial cost.
+//
+// Each edge on poses (m, n) with the measured pose_m_from_pose_n M has the
+// residual g = log(T_m^-1 T_n M^-1), no precision and no robust kernel: cost
+// g^T g.  With D the derivative of log(T_m^-1 exp(x) T_n M^-1) at x = 0
+// (Isometry3::dx_log_a_exp_x_b_at_0), J_n = D and J_m = -D.  Edges with the
+// same (m, n) form one reduced term: J_m^T J_m and J_n^T J_n (+ nu I once per
+// term) go to the diagonal blocks, J_m^T J_n to the lower block of S between
+// them (k_schur_reduce), -J^T g to the gradients (cost_system.rs:190-273).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -25,6 +35,16 @@ namespace sgba {
 namespace {
 
 constexpr int kPriorThreads = 256;
+
+struct EdgeArgs {
+  int nt;              // reduced terms
+  const int32_t* tbeg; // nt + 1: edge ranges
+  const int32_t* m;    // per edge
+  const int32_t* n;
+  const double* mn;    // per edge: pose_m_from_pose_n
+  double* out;         // 2 nt records: J^T J (36), J^T g (6); side 0 pose m, side 1 pose n
+  double* hmn;         // nt x 36: J_m^T J_n
+};
 
 __device__ __forceinline__ bool prior_halted(const Ctrl* c) { return c->done != 0; }
 __device__ __forceinline__ bool prior_skipping(const Ctrl* c) { return c->done != 0 || c->skip != 0; }
@@ -104,7 +124,94 @@ __global__ void __launch_bounds__(kPriorThreads) k_prior_eval(PriorArgs a, const
   if (threadIdx.x == 0) *cost_sum = dd_to_double(dd_make(sh_hi[0], sh_lo[0]));
 }
 
+// Reduced edge terms at the given poses (one CTA; a thread per term, its
+// edges in order).  lin: the records of both sides and J_m^T J_n.  Costs
+// summed as in k_prior_eval.
+__global__ void __launch_bounds__(kPriorThreads) k_edge_eval(EdgeArgs a, const double* __restrict__ poses, int lin,
+                                                            int gate, double* cost_sum, const Ctrl* ctrl) {
+  if ((gate == 1 && prior_halted(ctrl)) || (gate == 2 && prior_skipping(ctrl))) return;
+  dd acc = dd_make(0.0f, 0.0f);
+  for (int t = threadIdx.x; t < a.nt; t += kPriorThreads) {
+    double hmm[36], hnn[36], hmn[36], gm[6], gn[6];
+    for (int i = 0; i < 36; ++i) hmm[i] = hnn[i] = hmn[i] = 0.0;
+    for (int i = 0; i < 6; ++i) gm[i] = gn[i] = 0.0;
+    for (int e = a.tbeg[t]; e < a.tbeg[t + 1]; ++e) {
+      const double* Tm = poses + 7 * a.m[e];
+      const double* Tn = poses + 7 * a.n[e];
+      double ai[7], mninv[7], b[7], ab[7], g[6];
+      lie::se3_inverse(Tm, ai);
+      lie::se3_inverse(a.mn + 7 * e, mninv);
+      lie::se3_mul(Tn, mninv, b);
+      lie::se3_mul(ai, b, ab);
+      lie::se3_log(ab, g);
+      double cst = 0.0;
+      for (int r = 0; r < 6; ++r) cst += g[r] * g[r];
+      acc = dd_add(acc, dd_from_double(cst));
+      if (!lin) continue;
+      lie::D6 ex[7], ad[7], bd[7], t1[7], t2[7], gd[6];
+      lie::se3_exp_at_zero(ex);
+      for (int i = 0; i < 7; ++i) {
+        ad[i] = lie::dc(ai[i]);
+        bd[i] = lie::dc(b[i]);
+      }
+      lie::se3_mul(ad, ex, t1);
+      lie::se3_mul(t1, bd, t2);
+      lie::se3_log(t2, gd);
+      // J_n = D, J_m = -D
+      for (int r = 0; r < 6; ++r) {
+        double sg = 0.0;
+        for (int q = 0; q < 6; ++q) sg += gd[q].d[r] * g[q];
+        gn[r] += sg;
+        gm[r] -= sg;
+        for (int c = 0; c < 6; ++c) {
+          double s2 = 0.0;
+          for (int q = 0; q < 6; ++q) s2 += gd[q].d[r] * gd[q].d[c];
+          hnn[6 * r + c] += s2;
+          hmm[6 * r + c] += s2;
+          hmn[6 * r + c] -= s2;
+        }
+      }
+    }
+    if (lin) {
+      double* o0 = a.out + static_cast<int64_t>(kPriorOut) * (2 * t);
+      double* o1 = o0 + kPriorOut;
+      for (int i = 0; i < 36; ++i) {
+        o0[i] = hmm[i];
+        o1[i] = hnn[i];
+        a.hmn[36 * static_cast<int64_t>(t) + i] = hmn[i];
+      }
+      for (int i = 0; i < 6; ++i) {
+        o0[36 + i] = gm[i];
+        o1[36 + i] = gn[i];
+      }
+    }
+  }
+  if (!cost_sum) return;
+  __shared__ float sh_hi[kPriorThreads], sh_lo[kPriorThreads];
+  sh_hi[threadIdx.x] = acc.hi;
+  sh_lo[threadIdx.x] = acc.lo;
+  __syncthreads();
+  for (int h = kPriorThreads / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) {
+      const dd v = dd_add(dd_make(sh_hi[threadIdx.x], sh_lo[threadIdx.x]),
+                          dd_make(sh_hi[threadIdx.x + h], sh_lo[threadIdx.x + h]));
+      sh_hi[threadIdx.x] = v.hi;
+      sh_lo[threadIdx.x] = v.lo;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *cost_sum = dd_to_double(dd_make(sh_hi[0], sh_lo[0]));
+}
+
 }  // namespace
+
+int launch_edge_eval(const Sizes& s, const Dev& d, const double* poses, int lin, int gate, double* cost_sum,
+                     cudaStream_t st) {
+  if (s.n_edge <= 0) return 0;
+  EdgeArgs a{s.n_eterm, d.eterm_begin, d.edge_m, d.edge_n, d.edge_mn, d.edge_out, d.edge_hmn};
+  k_edge_eval<<<1, kPriorThreads, 0, st>>>(a, poses, lin, gate, cost_sum, d.ctrl);
+  return 1;
+}
 
 int launch_prior_eval(const Sizes& s, const Dev& d, const double* poses, int lin, int gate, double* cost_sum,
                       cudaStream_t st) {

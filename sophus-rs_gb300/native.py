@@ -104,6 +104,10 @@ class ProblemOptions(C.Structure):
                 ("eucm_alpha_beta", C.c_double * 2), ("reserved", C.c_int32 * 2)]
 
 
+class PoseGraph(C.Structure):
+    _fields_ = [("n_edge", C.c_int32), ("edge_pose", C.POINTER(C.c_int32)), ("edge_m_from_n", C.POINTER(C.c_double))]
+
+
 class Profile(C.Structure):
     _fields_ = [
         ("kernel_launches", C.c_int64),
@@ -161,7 +165,7 @@ LINSOLVE_PCG_BLOCK_JACOBI = 1
 LINSOLVE_PCG_LEARNED = 2
 
 EXPORTED = [
-    "sgba_abi_version", "sgba_last_error", "sgba_problem_create", "sgba_problem_create_ex",
+    "sgba_abi_version", "sgba_last_error", "sgba_problem_create", "sgba_problem_create_ex", "sgba_problem_create_graph",
     "sgba_get_intrinsics", "sgba_problem_destroy",
     "sgba_optimizer_init", "sgba_optimizer_step", "sgba_optimize", "sgba_get_variables",
     "sgba_get_cost", "sgba_set_variables", "sgba_get_layout", "sgba_export_pattern",
@@ -211,6 +215,8 @@ def lib():
     L.sgba_last_error.argtypes = [C.c_char_p, C.c_size_t]
     L.sgba_last_error.restype = C.c_size_t
     L.sgba_problem_create.argtypes = [C.POINTER(ProblemDesc), C.c_int32, C.POINTER(C.c_void_p)]
+    L.sgba_problem_create_graph.argtypes = [C.POINTER(ProblemDesc), C.POINTER(ProblemOptions), C.POINTER(PoseGraph),
+                                            C.c_int32, C.POINTER(C.c_void_p)]
     L.sgba_problem_create_ex.argtypes = [C.POINTER(ProblemDesc), C.POINTER(ProblemOptions), C.c_int32,
                                          C.POINTER(C.c_void_p)]
     L.sgba_get_intrinsics.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
@@ -338,7 +344,23 @@ class Problem:
         d.obs_uv = _dptr(obs_uv)
         d.huber_delta = float(data.huber_delta) if data.huber_delta is not None else 0.0
         h = C.c_void_p()
-        if intrinsics_free or self.camera_model != CAMERA_PINHOLE:
+        edges = getattr(data, "edge_pose", None)
+        if edges is not None and len(edges):
+            ep = np.ascontiguousarray(edges, dtype=np.int32).reshape(-1, 2)
+            mn = np.ascontiguousarray(data.edge_mn, dtype=np.float64).reshape(ep.shape[0], 7)
+            self._keep += [ep, mn]
+            g = PoseGraph()
+            g.n_edge = ep.shape[0]
+            g.edge_pose = ep.ctypes.data_as(C.POINTER(C.c_int32))
+            g.edge_m_from_n = _dptr(mn)
+            opts = ProblemOptions()
+            opts.intrinsics_free = 1 if intrinsics_free else 0
+            opts.camera_model = self.camera_model
+            if self.camera_model == CAMERA_EUCM:
+                opts.eucm_alpha_beta[0] = float(data.eucm_alpha_beta[0])
+                opts.eucm_alpha_beta[1] = float(data.eucm_alpha_beta[1])
+            check(L.sgba_problem_create_graph(C.byref(d), C.byref(opts), C.byref(g), int(device), C.byref(h)))
+        elif intrinsics_free or self.camera_model != CAMERA_PINHOLE:
             opts = ProblemOptions()
             opts.intrinsics_free = 1 if intrinsics_free else 0
             opts.camera_model = self.camera_model

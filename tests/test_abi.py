@@ -98,7 +98,7 @@ _CTYPES_OF = {"sgba_problem_desc": "ProblemDesc", "sgba_opt_params": "OptParamsC
               "sgba_layout": "Layout", "sgba_problem_options": "ProblemOptions", "sgba_profile": "Profile",
               "sgba_window_result": "WindowResult", "sgba_linear_solver": "LinearSolverC",
               "sgba_pcg_stats": "PcgStats", "sgba_pcg_train_params": "PcgTrainParams",
-              "sgba_batch_stats": "BatchStats"}
+              "sgba_batch_stats": "BatchStats", "sgba_pose_graph": "PoseGraph"}
 
 
 def test_python_struct_layouts_match_the_header(pkg, tmp_path):
