@@ -873,6 +873,7 @@ __device__ __forceinline__ void landmark_chunks_body(LinArgs a, Ctrl* ctrl, int 
   if (halted(ctrl)) return;
   extern __shared__ float lsm[];        // [cap][9] term contributions
   __shared__ float sci[kLmkTerms][6];   // C^-1 per point of the chunk (FP32)
+  __shared__ float2 ssum[kLmkTerms][9]; // per point: the 9 sums over its terms (float-float)
   __shared__ unsigned char sok[kLmkTerms];
   __shared__ double smax[8];
   const int tid = threadIdx.x;
@@ -912,19 +913,26 @@ __device__ __forceinline__ void landmark_chunks_body(LinArgs a, Ctrl* ctrl, int 
       for (int k = 0; k < 9; ++k) lsm[9 * t + k] = v[k];
     }
     __syncthreads();
-    // pass B: per point
+    // pass B1: every sum of every point, a thread per (point, value), over the
+    // point's terms in order (points of long tracks no longer serialise a
+    // single thread over all nine sums)
+    for (int e = tid; e < 9 * (p1 - p0); e += blockDim.x) {
+      const int q = e / 9, k = e - 9 * q;
+      const int tb = static_cast<int>(a.pt_g_begin[p0 + q] - t0), te = static_cast<int>(a.pt_g_begin[p0 + q + 1] - t0);
+      dd sacc = dd_make(0.f, 0.f);
+      for (int t = tb; t < te; ++t) sacc = dd_add_f(sacc, lsm[9 * t + k]);
+      ssum[q][k] = make_float2(sacc.hi, sacc.lo);
+    }
+    __syncthreads();
+    // pass B2: per point
     for (int q = tid; q < p1 - p0; q += blockDim.x) {
       const int i = p0 + q;
       const int mb = a.pt_mb[i];
       sok[q] = 0;
       if (mb < 0) continue;
-      const int tb = static_cast<int>(a.pt_g_begin[i] - t0), te = static_cast<int>(a.pt_g_begin[i + 1] - t0);
       dd acc[9];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) acc[k] = dd_make(0.f, 0.f);
-      for (int t = tb; t < te; ++t)
-#pragma unroll
-        for (int k = 0; k < 9; ++k) acc[k] = dd_add_f(acc[k], lsm[9 * t + k]);
+      for (int k = 0; k < 9; ++k) acc[k] = dd_make(ssum[q][k].x, ssum[q][k].y);
       const dd damp = dd_from_double(nu * a.cnt_m[mb]);
       acc[0] = dd_add(acc[0], damp);
       acc[3] = dd_add(acc[3], damp);
@@ -1049,6 +1057,7 @@ __global__ void __launch_bounds__(256) k_landmark_chunks_dd(LinArgs a, Ctrl* ctr
   if (halted(ctrl)) return;
   extern __shared__ float lsd[];               // [cap][kLmkDDTermFloats]
   __shared__ float sci[kLmkTerms][12];         // C^-1 of each point of the chunk (float-float)
+  __shared__ float2 ssum[kLmkTerms][9];        // per point: the 9 sums over its terms
   __shared__ unsigned char sok[kLmkTerms];
   __shared__ double smax[8];
   const int tid = threadIdx.x;
@@ -1094,21 +1103,27 @@ __global__ void __launch_bounds__(256) k_landmark_chunks_dd(LinArgs a, Ctrl* ctr
       for (int k = 0; k < 9; ++k) { ts[2 * k] = acc[k].hi; ts[2 * k + 1] = acc[k].lo; }
     }
     __syncthreads();
-    // pass B
+    // pass B1: a thread per (point, sum), over the point's terms in order
+    for (int e = tid; e < 9 * (p1 - p0); e += blockDim.x) {
+      const int q = e / 9, k = e - 9 * q;
+      const int tb = static_cast<int>(a.pt_g_begin[p0 + q] - t0), te = static_cast<int>(a.pt_g_begin[p0 + q + 1] - t0);
+      dd sacc = dd_make(0.f, 0.f);
+      for (int t = tb; t < te; ++t) {
+        const float* ts = lsd + static_cast<int64_t>(t) * kLmkDDTermFloats;
+        sacc = dd_add(sacc, dd_make(ts[2 * k], ts[2 * k + 1]));
+      }
+      ssum[q][k] = make_float2(sacc.hi, sacc.lo);
+    }
+    __syncthreads();
+    // pass B2: per point
     for (int q = tid; q < p1 - p0; q += blockDim.x) {
       const int i = p0 + q;
       const int mb = a.pt_mb[i];
       sok[q] = 0;
       if (mb < 0) continue;
-      const int tb = static_cast<int>(a.pt_g_begin[i] - t0), te = static_cast<int>(a.pt_g_begin[i + 1] - t0);
       dd acc[9];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) acc[k] = dd_make(0.f, 0.f);
-      for (int t = tb; t < te; ++t) {
-        const float* ts = lsd + static_cast<int64_t>(t) * kLmkDDTermFloats;
-#pragma unroll
-        for (int k = 0; k < 9; ++k) acc[k] = dd_add(acc[k], dd_make(ts[2 * k], ts[2 * k + 1]));
-      }
+      for (int k = 0; k < 9; ++k) acc[k] = dd_make(ssum[q][k].x, ssum[q][k].y);
       const dd damp = dd_from_double(nu * a.cnt_m[mb]);
       dd Vd[6];
 #pragma unroll
@@ -2080,6 +2095,7 @@ __device__ __forceinline__ void backsub_chunks_body(BackArgs a, const int32_t* c
                                                         const int32_t* g_pt, const Ctrl* ctrl, int bid_, int nblk_) {
   if (skipping(ctrl)) return;
   extern __shared__ float bsm[];  // [cap][12]: Z^T dx_f, Z^T v_f as (hi, lo)
+  __shared__ float2 ssum[kLmkTerms][6];  // per point: the 6 sums over its terms
   const bool gauge = a.gauge_kind == 1;
   const int tid = threadIdx.x;
   for (int c = bid_; c < nchunk; c += nblk_) {
@@ -2149,6 +2165,18 @@ __device__ __forceinline__ void backsub_chunks_body(BackArgs a, const int32_t* c
       }
     }
     __syncthreads();
+    // the sums of every point, a thread per (point, value), in term order
+    for (int e = tid; e < 6 * (p1 - p0); e += blockDim.x) {
+      const int q = e / 6, k = e - 6 * q;
+      const int tb = static_cast<int>(a.pt_g_begin[p0 + q] - t0), te = static_cast<int>(a.pt_g_begin[p0 + q + 1] - t0);
+      dd sacc = dd_make(0.f, 0.f);
+      for (int t = tb; t < te; ++t) {
+        const float* ts = bsm + static_cast<int64_t>(t) * 12;
+        sacc = dd_add(sacc, dd_make(ts[2 * k], ts[2 * k + 1]));
+      }
+      ssum[q][k] = make_float2(sacc.hi, sacc.lo);
+    }
+    __syncthreads();
     for (int q = tid; q < p1 - p0; q += blockDim.x) {
       const int i = p0 + q;
       const int mb = a.pt_mb[i];
@@ -2156,12 +2184,7 @@ __device__ __forceinline__ void backsub_chunks_body(BackArgs a, const int32_t* c
       const int tb = static_cast<int>(a.pt_g_begin[i] - t0), te = static_cast<int>(a.pt_g_begin[i + 1] - t0);
       dd sm[6];
 #pragma unroll
-      for (int k = 0; k < 6; ++k) sm[k] = dd_make(0.f, 0.f);
-      for (int t = tb; t < te; ++t) {
-        const float* ts = bsm + static_cast<int64_t>(t) * 12;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) sm[k] = dd_add(sm[k], dd_make(ts[2 * k], ts[2 * k + 1]));
-      }
+      for (int k = 0; k < 6; ++k) sm[k] = dd_make(ssum[q][k].x, ssum[q][k].y);
       if (a.zk && te > tb) intr_backsub_term(a, mb, sm);
       const float* cp = a.cinv + 12 * mb;  // 00 10 11 20 21 22 as (hi, lo)
       dd ci[6];
