@@ -527,6 +527,36 @@ class Problem:
         return ms.value
 
 
+def create_problems(datas, device=0, threads=None, **kw):
+    """Problem for each of many inputs (local windows), created concurrently on
+    host threads: sgba_problem_create is thread-safe, and each problem's set-up
+    (host plan, uploads, the Schur pattern on its own stream) is independent.
+    The problems come back in input order; if one fails, the others are closed
+    and the first error is raised."""
+    import concurrent.futures as cf
+
+    datas = list(datas)
+    if threads is None:
+        threads = min(16, os.cpu_count() or 1)
+    if threads <= 1 or len(datas) < 2:
+        return [Problem(d, device=device, **kw) for d in datas]
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        futs = [ex.submit(Problem, d, device, **kw) for d in datas]
+        out, err = [], None
+        for f in futs:
+            try:
+                out.append(f.result())
+            except Exception as e:  # noqa: BLE001 (re-raised below)
+                out.append(None)
+                err = err or e
+    if err is not None:
+        for p in out:
+            if p is not None:
+                p.close()
+        raise err
+    return out
+
+
 def batch_optimize(problems, params):
     """sgba_batch_optimize over Problem handles (independent windows).
 

@@ -166,3 +166,21 @@ def test_autotuner_settles_on_the_fastest_schedule(pkg):
     assert second["tuned"] and all(m > 0.0 for m in second["schedule_ms"])
     assert second["schedule"] == int(np.argmin(second["schedule_ms"]))
     assert first["batched_windows"] == second["batched_windows"] == 12
+
+
+def test_concurrent_creation_equals_sequential(pkg):
+    """Windows created concurrently on host threads (create_problems) optimise
+    exactly as windows created one by one."""
+    wins = _windows(pkg, 8)
+    params = fixed_iter_params(pkg, 4, wins[0].initial_lm_damping)
+    seq = [pkg.native.Problem(w, device=0) for w in wins]
+    con = pkg.native.create_problems(wins, device=0, threads=4)
+    try:
+        a = pkg.native.batch_optimize(seq, params)
+        b = pkg.native.batch_optimize(con, params)
+        for w in range(len(wins)):
+            assert [r.merit for r in a[w][0]] == [r.merit for r in b[w][0]]
+            assert np.array_equal(seq[w].variables()[0], con[w].variables()[0])
+    finally:
+        for p in seq + con:
+            p.close()
