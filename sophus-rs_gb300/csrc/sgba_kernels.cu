@@ -1912,7 +1912,7 @@ __device__ __forceinline__ void schur_dense_body(SchurDenseArgs a, const Ctrl* c
       }
     }
 }
-__global__ void __launch_bounds__(256) k_schur_dense(SchurDenseArgs a, const Ctrl* ctrl) {
+__global__ void __launch_bounds__(256, 3) k_schur_dense(SchurDenseArgs a, const Ctrl* ctrl) {
   schur_dense_body(a, ctrl, blockIdx.x, gridDim.x);
 }
 
@@ -3693,7 +3693,7 @@ __global__ void __launch_bounds__(64) k_camera_finalize_w(WinTab<FinArgs> t) {
   camera_finalize_body(a.nf, a.fb_tile_begin, a.tile_part, a.ufull, a.bf, a.rb, t.ctrl[q.w], a.with_schur, nullptr,
                        nullptr, nullptr, nullptr, nullptr, q.b, q.nb);
 }
-__global__ void __launch_bounds__(256) k_schur_dense_w(WinTab<SchurDenseArgs> t) {
+__global__ void __launch_bounds__(256, 3) k_schur_dense_w(WinTab<SchurDenseArgs> t) {
   const WinPos q = win_pos(t);
   schur_dense_body(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
 }
