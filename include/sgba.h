@@ -252,6 +252,18 @@ int sgba_set_variables(sgba_problem *p, const double *poses, const double *point
 int sgba_set_pose_priors(sgba_problem *p, int32_t n, const int32_t *pose, const double *mean,
                          const double *precision);
 
+/* Equality constraints |t(pose[k])| = radius[k] (TranslationNormConstraint,
+ * crates/sophus_opt/src/example_problems/ba_scale_constraint.rs:57-100), at
+ * most 8, each on a Free pose, solved with the LM step by the range-space KKT
+ * method of the Schur solver (crates/sophus_solver/src/ldlt/schur_ldlt.rs:
+ * 674-772): Y = S^-1 G^T, M = G Y, dlam = M^-1 (G S^-1 r + c), dx = S^-1 r - Y
+ * dlam; the multipliers start at zero at sgba_optimizer_init and move by -dlam
+ * with every accepted step (EqSystem::update_lambdas).  Only for reduced
+ * systems on the one-CTA solver (at most 234 rows, not loop-shaped), exact
+ * factorization (SGBA_ERR_UNSUPPORTED otherwise).  Replaces any earlier set
+ * (n = 0 removes them); the scale gauge is then held by the constraints. */
+int sgba_set_eq_constraints(sgba_problem *p, int32_t n, const int32_t *pose, const double *radius);
+
 /* Sizes of the problem as laid out on the device. */
 typedef struct {
   int32_t n_free_poses;     /* free pose blocks (6 dof) */

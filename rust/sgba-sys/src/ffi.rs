@@ -270,6 +270,7 @@ extern "C" {
         results: *mut sgba_window_result,
     ) -> c_int;
     pub fn sgba_batch_last_stats(out: *mut sgba_batch_stats) -> c_int;
+    pub fn sgba_set_eq_constraints(p: *mut sgba_problem, n: i32, pose: *const i32, radius: *const f64) -> c_int;
     pub fn sgba_set_pose_priors(
         p: *mut sgba_problem,
         n: i32,

@@ -1278,6 +1278,11 @@ int sgba_optimizer_init(sgba_problem* p, const sgba_opt_params* prm) {
   c.step = 0;
   c.num_iterations = prm->num_iterations;
   c.record_cap = cap;
+  c.n_eq = p->sz.n_eq;
+  c.eq_lambda = p->d.eq_lambda;
+  c.eq_dlam = p->d.eq_dlam;
+  if (p->sz.n_eq > 0)  // EqSystem::new: zero multipliers
+    SGBA_CK(cudaMemsetAsync(p->d.eq_lambda, 0, sizeof(double) * p->sz.n_eq, p->stream));
   SGBA_CK(cudaMemcpyAsync(p->d.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice, p->stream));
   sgba::launch_init_merit(p->sz, p->d, p->stream);
   int st = check_launch();
@@ -1451,8 +1456,66 @@ int sgba_set_pose_priors(sgba_problem* p, int32_t n, const int32_t* pose, const 
   p->plan.cnt_f = cnt;
   s.n_prior = n;
   // the priors hold the gauge: no projection along the scale direction
-  s.gauge_kind = n > 0 ? 0 : p->gauge_base;
+  s.gauge_kind = (n > 0 || s.n_eq > 0) ? 0 : p->gauge_base;
   // the iteration graph is captured again with the prior launches
+  if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }
+  if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
+  p->inited = false;
+  return SGBA_OK;
+}
+
+int sgba_set_eq_constraints(sgba_problem* p, int32_t n, const int32_t* pose, const double* radius) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  if (n < 0 || n > sgba::kMaxEq)
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "%d constraints: expected 0 .. %d", n, sgba::kMaxEq);
+  if (n > 0 && (!pose || !radius)) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  const Plan& P = p->plan;
+  Sizes& s = p->sz;
+  for (int32_t k = 0; k < n; ++k) {
+    if (pose[k] < 0 || pose[k] >= P.nc)
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "constraint %d: pose index %d out of range", k, pose[k]);
+    if (P.pose_fb[pose[k]] < 0)
+      return set_error(SGBA_ERR_INVALID_ARGUMENT, "constraint %d: pose %d is constant", k, pose[k]);
+    if (!std::isfinite(radius[k])) return set_error(SGBA_ERR_INVALID_ARGUMENT, "constraint %d: radius", k);
+  }
+  if (n > 0 && s.pcg_mode)
+    return set_error(SGBA_ERR_UNSUPPORTED, "equality constraints with the PCG solver are not on this path");
+  if (n > 0 && !s.small_dense)
+    return set_error(SGBA_ERR_UNSUPPORTED,
+                     "equality constraints run on the one-CTA solver (reduced systems of at most 234 rows)");
+  SGBA_CK(cudaSetDevice(p->device));
+  if (n > 0 && !sgba::small_dense_setup_eq(s.n6, n))
+    return set_error(SGBA_ERR_UNSUPPORTED, "%d constraints on a %d-row reduced system exceed the shared memory", n,
+                     s.n6);
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  Dev& d = p->d;
+  int st;
+  if (n > d.eq_cap) {
+    if ((st = dev_alloc(p, &d.eq_pose, static_cast<size_t>(n)))) return st;
+    if ((st = dev_alloc(p, &d.eq_fb, static_cast<size_t>(n)))) return st;
+    if ((st = dev_alloc(p, &d.eq_radius, static_cast<size_t>(n)))) return st;
+    if ((st = dev_alloc(p, &d.eq_c, static_cast<size_t>(n)))) return st;
+    if ((st = dev_alloc(p, &d.eq_jac, 3 * static_cast<size_t>(n)))) return st;
+    if ((st = dev_alloc(p, &d.eq_lambda, static_cast<size_t>(n)))) return st;
+    if ((st = dev_alloc(p, &d.eq_dlam, static_cast<size_t>(n)))) return st;
+    d.eq_cap = n;
+  }
+  if (n > 0) {
+    std::vector<int32_t> fb(n);
+    for (int32_t k = 0; k < n; ++k) fb[k] = P.pose_fb[pose[k]];
+    SGBA_CK(cudaMemcpyAsync(d.eq_pose, pose, sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+    SGBA_CK(cudaMemcpyAsync(d.eq_fb, fb.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, p->stream));
+    SGBA_CK(cudaMemcpyAsync(d.eq_radius, radius, sizeof(double) * n, cudaMemcpyHostToDevice, p->stream));
+    SGBA_CK(cudaMemsetAsync(d.eq_dlam, 0, sizeof(double) * n, p->stream));
+    SGBA_CK(cudaStreamSynchronize(p->stream));
+  }
+  if (p->gauge_base < 0) {
+    p->cnt_f_base = P.cnt_f;
+    p->gauge_base = s.gauge_kind;
+  }
+  s.n_eq = n;
+  // the constraints fix the scale: no gauge projection
+  s.gauge_kind = (n > 0 || s.n_prior > 0) ? 0 : p->gauge_base;
   if (p->graph_exec) { cudaGraphExecDestroy(p->graph_exec); p->graph_exec = nullptr; }
   if (p->graph) { cudaGraphDestroy(p->graph); p->graph = nullptr; }
   p->inited = false;
@@ -2005,6 +2068,7 @@ int sgba_set_linear_solver(sgba_problem* p, const sgba_linear_solver* cfg, const
       return set_error(SGBA_ERR_INVALID_ARGUMENT, "PCG needs max_iterations >= 1 and a finite tolerance > 0");
     if (p->plan.nf < 1) return set_error(SGBA_ERR_SCHUR_MISSING_FREE_OR_MARG, "no free pose: nothing to solve");
     if (p->intr_free) return set_error(SGBA_ERR_UNSUPPORTED, "PCG with free intrinsics is not on this path");
+    if (p->sz.n_eq > 0) return set_error(SGBA_ERR_UNSUPPORTED, "PCG with equality constraints is not on this path");
     if (model && model->m.device != p->device)
       return set_error(SGBA_ERR_INVALID_ARGUMENT, "model on device %d, problem on device %d", model->m.device,
                        p->device);

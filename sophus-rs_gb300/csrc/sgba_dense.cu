@@ -127,6 +127,13 @@ struct DenseArgs {
   double center[3];
   int npose;         // rows of the free poses (6 n_f; free intrinsics follow them)
   int refine;        // refinement steps at most (cluster solver)
+  // equality constraints (one-CTA solver): G row k is jac + 3k at rows
+  // 6 fb_k + 3 .. 5; c; the multiplier step out
+  int n_eq;
+  const int32_t* eq_fb;
+  const double* eq_jac;
+  const double* eq_c;
+  double* eq_dlam;
 };
 
 // the factorization is skipped on termination, on a skipped step and when PCG converged
@@ -966,12 +973,20 @@ __device__ __forceinline__ void small_dense_body(DenseArgs a, Ctrl* ctrl, int bi
   float2* A = sm;                      // lower triangle, packed by rows
   float2* y = sm + m * (m + 1) / 2;    // rhs -> z -> x
   float2* rdv = y + m;                 // reciprocal pivots
+  // equality constraints: columns Y_k = S^-1 G_k^T solved beside the rhs
+  // (range-space KKT, schur_ldlt.rs:674-772)
+  const int ne = a.n_eq;
+  float2* yg = rdv + m;                // ne x m
   __shared__ int s_bad;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   if (tid == 0) s_bad = 0;
   for (int i = warp; i < m; i += 8)
     for (int j = lane; j <= i; j += 32) A[sd_at(i, j)] = a.S2[static_cast<int64_t>(i) * m + j];
   for (int i = tid; i < m; i += 256) y[i] = sd_dd2f(dd_from_double(a.b[i]));
+  for (int e = tid; e < ne * m; e += 256) yg[e] = make_float2(0.0f, 0.0f);
+  __syncthreads();
+  if (tid < ne && a.eq_fb[tid] >= 0)
+    for (int i = 0; i < 3; ++i) yg[tid * m + 6 * a.eq_fb[tid] + 3 + i] = sd_dd2f(dd_from_double(a.eq_jac[3 * tid + i]));
   __syncthreads();
   float maxp = 1.0f;
   for (int t = 0; t < m; ++t) {
@@ -1002,6 +1017,10 @@ __device__ __forceinline__ void small_dense_body(DenseArgs a, Ctrl* ctrl, int bi
         A[ri + q] = sd_dd2f(v);
       }
       if (lane == 0) y[i] = sd_dd2f(dd_sub(sd_f2dd(y[i]), dd_mul(li, yt)));
+      if (lane >= 1 && lane <= ne) {
+        float2* yk = yg + (lane - 1) * m;
+        yk[i] = sd_dd2f(dd_sub(sd_f2dd(yk[i]), dd_mul(li, sd_f2dd(yk[t]))));
+      }
     }
     __syncthreads();
   }
@@ -1012,12 +1031,74 @@ __device__ __forceinline__ void small_dense_body(DenseArgs a, Ctrl* ctrl, int bi
       A[e] = sd_dd2f(dd_mul(sd_f2dd(A[e]), sd_f2dd(rdv[t])));
     }
   for (int i = tid; i < m; i += 256) y[i] = sd_dd2f(dd_mul(sd_f2dd(y[i]), sd_f2dd(rdv[i])));
+  for (int e = tid; e < ne * m; e += 256) yg[e] = sd_dd2f(dd_mul(sd_f2dd(yg[e]), sd_f2dd(rdv[e % m])));
   __syncthreads();
-  // backward: x_t final, then x_i -= L_ti x_t for i < t
+  // backward: x_t final, then x_i -= L_ti x_t for i < t (the rhs and every Y column)
   for (int t = m - 1; t > 0; --t) {
     const dd xt = sd_f2dd(y[t]);
     const int rt = sd_at(t, 0);
-    for (int i = tid; i < t; i += 256) y[i] = sd_dd2f(dd_sub(sd_f2dd(y[i]), dd_mul(sd_f2dd(A[rt + i]), xt)));
+    for (int e = tid; e < (1 + ne) * t; e += 256) {
+      const int col = e / t, i = e - col * t;
+      float2* v = col == 0 ? y : yg + (col - 1) * m;
+      const dd vt = col == 0 ? xt : sd_f2dd(v[t]);
+      v[i] = sd_dd2f(dd_sub(sd_f2dd(v[i]), dd_mul(sd_f2dd(A[rt + i]), vt)));
+    }
+    __syncthreads();
+  }
+  if (ne > 0) {
+    // M = G Y, w = G x + c, dlam = M^-1 w (Gauss-Jordan with partial pivoting,
+    // as the small inverse of schur_ldlt.rs:723-728), x -= Y dlam
+    __shared__ double s_dlam[kMaxEq];
+    if (tid == 0) {
+      double M[kMaxEq * kMaxEq], Mi[kMaxEq * kMaxEq], w[kMaxEq];
+      for (int p = 0; p < ne; ++p) {
+        const int fp = a.eq_fb[p];
+        double acc = a.eq_c[p];
+        for (int q = 0; q < ne; ++q) M[p * ne + q] = 0.0;
+        if (fp >= 0)
+          for (int i = 0; i < 3; ++i) {
+            const int row = 6 * fp + 3 + i;
+            const double gi = a.eq_jac[3 * p + i];
+            acc += gi * dd_to_double(sd_f2dd(y[row]));
+            for (int q = 0; q < ne; ++q) M[p * ne + q] += gi * dd_to_double(sd_f2dd(yg[q * m + row]));
+          }
+        w[p] = acc;
+      }
+      for (int p = 0; p < ne * ne; ++p) Mi[p] = (p / ne == p % ne) ? 1.0 : 0.0;
+      bool ok = true;
+      for (int col = 0; col < ne && ok; ++col) {
+        int piv = col;
+        for (int r = col + 1; r < ne; ++r)
+          if (fabs(M[r * ne + col]) > fabs(M[piv * ne + col])) piv = r;
+        const double dv = M[piv * ne + col];
+        if (!(fabs(dv) > 0.0) || !isfinite(dv)) { ok = false; break; }
+        if (piv != col)
+          for (int c = 0; c < ne; ++c) {
+            double t1 = M[piv * ne + c]; M[piv * ne + c] = M[col * ne + c]; M[col * ne + c] = t1;
+            double t2 = Mi[piv * ne + c]; Mi[piv * ne + c] = Mi[col * ne + c]; Mi[col * ne + c] = t2;
+          }
+        for (int c = 0; c < ne; ++c) { M[col * ne + c] /= dv; Mi[col * ne + c] /= dv; }
+        for (int r = 0; r < ne; ++r) {
+          if (r == col) continue;
+          const double f = M[r * ne + col];
+          if (f == 0.0) continue;
+          for (int c = 0; c < ne; ++c) { M[r * ne + c] -= f * M[col * ne + c]; Mi[r * ne + c] -= f * Mi[col * ne + c]; }
+        }
+      }
+      if (!ok) s_bad = 1;  // a singular M: a failed solve (reject)
+      for (int p = 0; p < ne; ++p) {
+        double acc = 0.0;
+        for (int q = 0; q < ne; ++q) acc += Mi[p * ne + q] * w[q];
+        s_dlam[p] = ok ? acc : 0.0;
+        a.eq_dlam[p] = s_dlam[p];
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < m; i += 256) {
+      dd v = sd_f2dd(y[i]);
+      for (int p = 0; p < ne; ++p) v = dd_sub(v, dd_mul(sd_f2dd(yg[p * m + i]), dd_from_double(s_dlam[p])));
+      y[i] = sd_dd2f(v);
+    }
     __syncthreads();
   }
   for (int i = tid; i < m; i += 256) {
@@ -1032,8 +1113,8 @@ __global__ void __launch_bounds__(256, 1) k_small_dense(DenseArgs a, Ctrl* ctrl)
   small_dense_body(a, ctrl, blockIdx.x, gridDim.x);
 }
 
-size_t small_dense_smem(int n) {
-  return sizeof(float2) * (static_cast<size_t>(n) * (n + 1) / 2 + 2 * static_cast<size_t>(n));
+size_t small_dense_smem(int n, int n_eq = 0) {
+  return sizeof(float2) * (static_cast<size_t>(n) * (n + 1) / 2 + (2 + static_cast<size_t>(n_eq)) * n);
 }
 
 size_t dense_smem_bytes(int P, int C) {
@@ -1099,6 +1180,15 @@ int dense_cluster_setup(int n, int* cluster, size_t* smem) {
   return 0;
 }
 
+int small_dense_setup_eq(int n, int n_eq) {
+  if (n <= 0 || n > kSmallMax || n_eq < 0 || n_eq > kMaxEq) return 0;
+  if (raise_dynamic_smem(reinterpret_cast<const void*>(k_small_dense), small_dense_smem(n, n_eq)) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return 1;
+}
+
 int small_dense_setup(int n) {
   if (n <= 0 || n > kSmallMax) return 0;
   if (raise_dynamic_smem(reinterpret_cast<const void*>(k_small_dense), small_dense_smem(n)) != cudaSuccess) {
@@ -1118,11 +1208,16 @@ DenseArgs small_dense_args(const Sizes& s, const Dev& d) {
   a.b = d.rb;
   a.x = d.x;
   a.xdd = d.xdd;
+  a.n_eq = s.n_eq;
+  a.eq_fb = d.eq_fb;
+  a.eq_jac = d.eq_jac;
+  a.eq_c = d.eq_c;
+  a.eq_dlam = d.eq_dlam;
   return a;
 }
 
 DenseArgs dense_cluster_args(const Sizes& s, const Dev& d) {
-  DenseArgs a;
+  DenseArgs a{};
   a.n = s.n6;
   a.P = (s.n6 + kNB - 1) / kNB;
   a.S2 = d.S2;
@@ -1143,7 +1238,7 @@ DenseArgs dense_cluster_args(const Sizes& s, const Dev& d) {
 }  // namespace
 
 int launch_small_dense(const Sizes& s, const Dev& d, cudaStream_t st) {
-  k_small_dense<<<1, 256, small_dense_smem(s.n6), st>>>(small_dense_args(s, d), d.ctrl);
+  k_small_dense<<<1, 256, small_dense_smem(s.n6, s.n_eq), st>>>(small_dense_args(s, d), d.ctrl);
   return 1;
 }
 

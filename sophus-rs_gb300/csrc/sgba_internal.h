@@ -61,6 +61,12 @@ struct Ctrl {
   long long pcg_solves;         // PCG solves so far
   long long pcg_fallbacks;      // of which went to the exact factorization
   long long pcg_total_iters;    // PCG iterations so far
+  // equality constraints (range-space KKT on the one-CTA solver): their
+  // count, the multipliers and the latest step's multiplier change
+  int n_eq;
+  int eq_pad;
+  double* eq_lambda;
+  const double* eq_dlam;
 };
 
 // Per-step record, layout-identical to sgba_iter_record.
@@ -191,6 +197,17 @@ struct Dev {
   int32_t* eblk_term = nullptr;
   int32_t* efb_begin = nullptr;
   int32_t* efb_slot = nullptr;
+  // equality constraints |t(pose)| = r (sgba_prior.cu, sgba_dense.cu): pose,
+  // free block, radius; per iteration c, the translation part of each G row
+  // (3), the multipliers and the step's change of them
+  int32_t* eq_pose = nullptr;
+  int32_t* eq_fb = nullptr;
+  double* eq_radius = nullptr;
+  double* eq_c = nullptr;
+  double* eq_jac = nullptr;
+  double* eq_lambda = nullptr;
+  double* eq_dlam = nullptr;
+  int eq_cap = 0;
   int32_t* slow_list = nullptr;    // points redone in float-float this iteration
   int32_t* slow_count = nullptr;
   // state
@@ -372,6 +389,7 @@ struct Sizes {
   int schur_dense;     // S by tiles of pose blocks (nearly dense S and Z: local windows), not by pairs
   int n_prior;         // pose priors (a second cost function; 0: none)
   int n_edge;          // pose-graph edges (0: none)
+  int n_eq;            // equality constraints |t(pose)| = r (0: none; the one-CTA solver only)
   int n_eterm;         // their reduced terms (distinct (m, n))
   int intr_free;       // the camera params are Free: one more 6-row block, last in S
   int intr_nk;         // free params: 4 (pinhole, padded to 6 rows) or 6 (EUCM)
@@ -415,6 +433,8 @@ int dense_cluster_setup(int n, int* cluster, size_t* smem);
 int launch_dense_cluster(const Sizes& s, const Dev& d, cudaStream_t st);
 // Small systems (local windows): one CTA, float-float LDL^T (1 = usable).
 int small_dense_setup(int n);
+// The same with n_eq equality constraints (their columns beside the rhs).
+int small_dense_setup_eq(int n, int n_eq);
 int launch_small_dense(const Sizes& s, const Dev& d, cudaStream_t st);
 
 // Raise a kernel's dynamic shared memory limit to at least `bytes` on the
@@ -493,6 +513,14 @@ int launch_prior_eval(const Sizes& s, const Dev& d, const double* poses, int lin
 // Dev::edge_hmn; their total cost into *cost_sum.  The same gates.
 int launch_edge_eval(const Sizes& s, const Dev& d, const double* poses, int lin, int gate, double* cost_sum,
                      cudaStream_t st);
+// Equality constraints (TranslationNormConstraint) at the current poses: c and
+// G, and G^T lambda added to the free gradient and the reduced rhs (after the
+// camera finalisation, before the solve).  Returns the launches.
+constexpr int kMaxEq = 8;
+int launch_eq_eval(const Sizes& s, const Dev& d, cudaStream_t st);
+// After the update: the multiplier step's share of the gain-ratio sums (one
+// more update partial at upd_slot) and of the largest step entry.
+int launch_eq_post(const Sizes& s, const Dev& d, double* upd_slot, cudaStream_t st);
 
 // ---- batched local windows ----------------------------------------------
 // A batch launches every kernel of an LM iteration once for many independent

@@ -1550,7 +1550,8 @@ __device__ __forceinline__ void camera_finalize_body(int nf, const int64_t* fb_t
       __threadfence();
       const double mg = __longlong_as_double(static_cast<long long>(atomicAdd(&ctrl->max_grad_bits, 0ull)));
       ctrl->max_grad = mg;
-      if (mg < ctrl->gtol) {
+      // the gradient check is skipped with equality constraints (optimizer.rs:527-535)
+      if (mg < ctrl->gtol && ctrl->n_eq == 0) {
         ctrl->skip = 1;
       } else if (ctrl->fail) {
         ctrl->skip = 2;
@@ -2859,6 +2860,7 @@ __device__ void decide_body(const double* cost_part, int n_cost, const double* u
         ctrl->accept = 1;
         ctrl->merit = new_merit;
         rec.accepted = 1;
+        for (int k = 0; k < ctrl->n_eq; ++k) ctrl->eq_lambda[k] -= ctrl->eq_dlam[k];  // update_lambdas
       }
       reason = 3;  // ParameterTolerance
     } else {
@@ -2878,6 +2880,7 @@ __device__ void decide_body(const double* cost_part, int n_cost, const double* u
         ctrl->accept = 1;
         ctrl->merit = new_merit;
         rec.accepted = 1;
+        for (int k = 0; k < ctrl->n_eq; ++k) ctrl->eq_lambda[k] -= ctrl->eq_dlam[k];  // update_lambdas
       } else {
         ctrl->nu *= 2.0;
         ctrl->rejects += 1;
@@ -2946,7 +2949,10 @@ int upd_blocks(const Sizes& s) {
 
 }  // namespace
 
-int cost_partials_needed(const Sizes& s) { return 4 * kUpdBlocks + cost_grid(s.no) + 2; }  // + priors', edges' cost
+// partials: gauge (2 per block), update (2 per block, then the constraints'
+// slot), cost (one per block, then the priors' and the edges')
+constexpr int kCostPartOff = 4 * kUpdBlocks + 2;
+int cost_partials_needed(const Sizes& s) { return kCostPartOff + cost_grid(s.no) + 2; }
 
 int launch_pose_tables(const Sizes& s, const Dev& d, const double* poses, cudaStream_t st) {
   k_pose_tables<<<(s.nc + 127) / 128, 128, 0, st>>>(s.nc, poses, d.pose_f, d.pose_dd, d.ctrl, 0, nullptr, nullptr);
@@ -3190,6 +3196,7 @@ int launch_linearize(const Sizes& s, const Dev& d, double nu_override, bool use_
                                          d.prior_out, s.n_edge > 0 ? d.efb_begin : nullptr, d.efb_slot,
                                          d.edge_out);
   ++n;
+  if (!use_override) n += launch_eq_eval(s, d, st);
   return n;
 }
 
@@ -3311,6 +3318,7 @@ int launch_update(const Sizes& s, const Dev& d, cudaStream_t st) {
   }
   k_apply_update<<<upd_blocks(s), 256, 0, st>>>(make_upd_args(s, d), d.ctrl);
   ++n;
+  n += launch_eq_post(s, d, d.part + 2 * kUpdBlocks + 2 * upd_blocks(s), st);
   return n;
 }
 
@@ -3323,7 +3331,7 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) 
     case 3:
       return launch_camera(s, d, 1, st);
     case 4: {
-      CostArgs a = make_cost_args(s, d, d.points_t, d.res_t, d.part + 4 * kUpdBlocks, 1);
+      CostArgs a = make_cost_args(s, d, d.points_t, d.res_t, d.part + kCostPartOff, 1);
       (s.eucm ? k_cost<true> : k_cost<false>)<<<cost_grid(s.no), kCostThreads, 0, st>>>(a, d.ctrl);
       return 1;
     }
@@ -3339,11 +3347,11 @@ int launch_single(const Sizes& s, const Dev& d, int kernel_id, cudaStream_t st) 
 // trial cost (partials after the update partials; the trial pose tables
 // were written by k_apply_update); its last block runs the LM decision
 static CostArgs make_decide_args(const Sizes& s, const Dev& d) {
-  double* cost_part = d.part + 4 * kUpdBlocks;
+  double* cost_part = d.part + kCostPartOff;
   CostArgs a = make_cost_args(s, d, d.points_t, d.res_t, cost_part, 1);
   a.decide = d.ctrl;
   a.upd_part = d.part + 2 * kUpdBlocks;
-  a.n_upd = upd_blocks(s);
+  a.n_upd = upd_blocks(s) + (s.n_eq > 0 ? 1 : 0);  // the constraints' slot after the blocks'
   a.recs = d.records;
   a.last = d.last_rec;
   return a;
@@ -3764,7 +3772,8 @@ struct BatchTables {
 };
 
 int batch_eligible(const Sizes& s) {
-  return (!s.lin_dd && !s.eucm && !s.intr_free && !s.pcg_mode && s.n_prior == 0 && s.n_edge == 0 && s.band_c == 0 &&
+  return (!s.lin_dd && !s.eucm && !s.intr_free && !s.pcg_mode && s.n_prior == 0 && s.n_edge == 0 && s.n_eq == 0 &&
+          s.band_c == 0 &&
           (s.small_dense || s.dense_c > 0) &&
           s.nlchunk > 0 && s.bsub_chunks_ok && s.ntiles > 0 && s.nf > 0)
              ? 1

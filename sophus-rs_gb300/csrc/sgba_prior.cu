@@ -203,7 +203,63 @@ __global__ void __launch_bounds__(kPriorThreads) k_edge_eval(EdgeArgs a, const d
   if (threadIdx.x == 0) *cost_sum = dd_to_double(dd_make(sh_hi[0], sh_lo[0]));
 }
 
+// Equality constraints c_k = |t(T_k)| - r_k (TranslationNormConstraint,
+// ba_scale_constraint.rs:57-100) at the current poses; under exp(x) T the
+// translation moves by w x t + v, so the Jacobian is (0, t^T / |t|).  The
+// KKT right-hand side gains G^T lambda on the free rows
+// (eq_system.rs, populate_lower_triangular_kkt_mat): added here to the
+// gradient and the reduced rhs in constraint order (one thread).
+__global__ void k_eq_eval(int n, const int32_t* __restrict__ pose, const int32_t* __restrict__ fb,
+                          const double* __restrict__ radius, const double* __restrict__ poses, double* c,
+                          double* jac, const double* lambda, double* bf, double* rb, const Ctrl* ctrl) {
+  if (prior_skipping(ctrl) || threadIdx.x != 0) return;
+  for (int k = 0; k < n; ++k) {
+    const double* t = poses + 7 * pose[k] + 4;
+    const double nrm = sqrt(t[0] * t[0] + t[1] * t[1] + t[2] * t[2]);
+    c[k] = nrm - radius[k];
+    for (int i = 0; i < 3; ++i) jac[3 * k + i] = t[i] / nrm;
+    if (fb[k] >= 0)
+      for (int i = 0; i < 3; ++i) {
+        bf[6 * fb[k] + 3 + i] += jac[3 * k + i] * lambda[k];
+        rb[6 * fb[k] + 3 + i] += jac[3 * k + i] * lambda[k];
+      }
+  }
+}
+
+// The multiplier step's share of compute_gain_ratio's sums (its entries of
+// the step against -c) and of the largest step entry.
+__global__ void k_eq_post(int n, const double* __restrict__ dlam, const double* __restrict__ c, double* slot,
+                          Ctrl* ctrl) {
+  if (prior_skipping(ctrl) || threadIdx.x != 0) return;
+  dd sdd = dd_make(0.f, 0.f), sdg = dd_make(0.f, 0.f);
+  double mx = 0.0;
+  for (int k = 0; k < n; ++k) {
+    const dd x = dd_from_double(dlam[k]);
+    sdd = dd_add(sdd, dd_mul(x, x));
+    sdg = dd_add(sdg, dd_mul(x, dd_from_double(-c[k])));
+    mx = fmax(mx, fabs(dlam[k]));
+  }
+  slot[0] = dd_to_double(sdd);
+  slot[1] = dd_to_double(sdg);
+  unsigned long long* addr = &ctrl->max_step_bits;
+  const unsigned long long bits = static_cast<unsigned long long>(__double_as_longlong(mx));
+  atomicMax(addr, bits);  // non-negative doubles order as their bit patterns
+}
+
 }  // namespace
+
+int launch_eq_eval(const Sizes& s, const Dev& d, cudaStream_t st) {
+  if (s.n_eq <= 0) return 0;
+  k_eq_eval<<<1, 32, 0, st>>>(s.n_eq, d.eq_pose, d.eq_fb, d.eq_radius, d.poses, d.eq_c, d.eq_jac, d.eq_lambda, d.bf,
+                              d.rb, d.ctrl);
+  return 1;
+}
+
+int launch_eq_post(const Sizes& s, const Dev& d, double* upd_slot, cudaStream_t st) {
+  if (s.n_eq <= 0) return 0;
+  k_eq_post<<<1, 32, 0, st>>>(s.n_eq, d.eq_dlam, d.eq_c, upd_slot, d.ctrl);
+  return 1;
+}
 
 int launch_edge_eval(const Sizes& s, const Dev& d, const double* poses, int lin, int gate, double* cost_sum,
                      cudaStream_t st) {

@@ -170,7 +170,7 @@ EXPORTED = [
     "sgba_optimizer_init", "sgba_optimizer_step", "sgba_optimize", "sgba_get_variables",
     "sgba_get_cost", "sgba_set_variables", "sgba_get_layout", "sgba_export_pattern",
     "sgba_debug_last_system", "sgba_debug_jacobians", "sgba_state_save", "sgba_state_load", "sgba_get_profile",
-    "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_batch_optimize", "sgba_batch_last_stats", "sgba_set_pose_priors",
+    "sgba_set_profiling", "sgba_bench_iterations", "sgba_bench_kernel", "sgba_batch_optimize", "sgba_batch_last_stats", "sgba_set_pose_priors", "sgba_set_eq_constraints",
     "sgba_set_linear_solver", "sgba_get_pcg_stats", "sgba_pcg_num_params", "sgba_pcg_model_create",
     "sgba_pcg_model_destroy", "sgba_pcg_model_set_params", "sgba_pcg_model_get_params",
     "sgba_pcg_trainset_create", "sgba_pcg_trainset_destroy", "sgba_pcg_trainset_size", "sgba_pcg_trainset_add",
@@ -243,6 +243,7 @@ def lib():
                                       C.POINTER(IterRecord), C.c_int32, C.POINTER(WindowResult)]
     L.sgba_batch_last_stats.argtypes = [C.POINTER(BatchStats)]
     L.sgba_set_pose_priors.argtypes = [C.c_void_p, C.c_int32, ip, dp, dp]
+    L.sgba_set_eq_constraints.argtypes = [C.c_void_p, C.c_int32, ip, dp]
     L.sgba_set_linear_solver.argtypes = [C.c_void_p, C.POINTER(LinearSolverC), C.c_void_p]
     L.sgba_get_pcg_stats.argtypes = [C.c_void_p, C.POINTER(PcgStats)]
     L.sgba_pcg_num_params.restype = C.c_int32
@@ -427,6 +428,14 @@ class Problem:
         precision = np.ascontiguousarray(precision, dtype=np.float64).reshape(n, 6, 6)
         check(lib().sgba_set_pose_priors(self._h, n, pose.ctypes.data_as(C.POINTER(C.c_int32)) if n else None,
                                          _dptr(mean) if n else None, _dptr(precision) if n else None))
+
+    def set_eq_constraints(self, pose, radius):
+        """sgba_set_eq_constraints: |t(pose[k])| = radius[k]; an empty set removes them."""
+        pose = np.ascontiguousarray(pose, dtype=np.int32).reshape(-1)
+        radius = np.ascontiguousarray(radius, dtype=np.float64).reshape(-1)
+        n = pose.shape[0]
+        check(lib().sgba_set_eq_constraints(self._h, n, pose.ctypes.data_as(C.POINTER(C.c_int32)) if n else None,
+                                            _dptr(radius) if n else None))
 
     def cost(self):
         c = C.c_double()
