@@ -249,6 +249,20 @@ impl Problem {
     /// `sgba_problem_create_ex`: the camera model, and whether its params
     /// are a Free family (kinds F, F, M) optimised with the poses.
     pub fn new_with_camera(p: &BaProblem<'_>, camera: Camera, intrinsics_free: bool, device: i32) -> Result<Self, Error> {
+        Self::new_with_graph(p, camera, intrinsics_free, &[], &[], device)
+    }
+
+    /// `sgba_problem_create_graph`: `new_with_camera` plus PoseGraph3 edges
+    /// (pose_graph3.rs): (m, n) pose pairs and the measured pose_m_from_pose_n
+    /// of each.
+    pub fn new_with_graph(
+        p: &BaProblem<'_>,
+        camera: Camera,
+        intrinsics_free: bool,
+        edges: &[[i32; 2]],
+        edges_m_from_n: &[[f64; 7]],
+        device: i32,
+    ) -> Result<Self, Error> {
         let n_obs = p.obs_cam.len();
         if p.obs_pt.len() != n_obs || p.obs_uv.len() != n_obs {
             return Err(Error::invalid_argument("observation arrays differ in length"));
@@ -283,12 +297,46 @@ impl Problem {
             eucm_alpha_beta,
             reserved: [0; 2],
         };
+        let graph = ffi::sgba_pose_graph {
+            n_edge: to_i32(edges.len(), "too many edges")?,
+            edge_pose: edges.as_ptr().cast::<i32>(),
+            edge_m_from_n: edges_m_from_n.as_ptr().cast::<f64>(),
+        };
+        if edges.len() != edges_m_from_n.len() {
+            return Err(Error::invalid_argument("edge pose pairs and measurements differ in length"));
+        }
         let mut raw = core::ptr::null_mut();
-        // SAFETY: every pointer in `desc` covers the length it states and
-        // outlives the call (the library copies the data); `opts` is a
-        // complete options struct.
-        check(unsafe { ffi::sgba_problem_create_ex(&desc, &opts, device, &mut raw) })?;
+        // SAFETY: every pointer in `desc` and `graph` covers the length it
+        // states and outlives the call (the library copies the data); `opts`
+        // is a complete options struct.
+        check(unsafe { ffi::sgba_problem_create_graph(&desc, &opts, &graph, device, &mut raw) })?;
         Ok(Self { raw, n_cam: p.poses.len(), n_pt: p.points.len(), n_cam_params })
+    }
+
+    /// Isometry3 pose priors (isometry3_prior.rs): pose indices, means
+    /// (qw qx qy qz tx ty tz) and 6x6 precisions (row-major); an empty set
+    /// removes them.
+    pub fn set_pose_priors(&mut self, pose: &[i32], mean: &[[f64; 7]], precision: &[[f64; 36]]) -> Result<(), Error> {
+        if mean.len() != pose.len() || precision.len() != pose.len() {
+            return Err(Error::invalid_argument("prior arrays differ in length"));
+        }
+        let n = to_i32(pose.len(), "too many priors")?;
+        // SAFETY: the slices hold n indices, n * 7 and n * 36 doubles.
+        check(unsafe {
+            ffi::sgba_set_pose_priors(self.raw, n, pose.as_ptr(), mean.as_ptr().cast::<f64>(),
+                                      precision.as_ptr().cast::<f64>())
+        })
+    }
+
+    /// Equality constraints |t(pose[k])| = radius[k] (TranslationNormConstraint);
+    /// an empty set removes them.
+    pub fn set_eq_constraints(&mut self, pose: &[i32], radius: &[f64]) -> Result<(), Error> {
+        if radius.len() != pose.len() {
+            return Err(Error::invalid_argument("constraint arrays differ in length"));
+        }
+        let n = to_i32(pose.len(), "too many constraints")?;
+        // SAFETY: the slices hold n indices and n doubles.
+        check(unsafe { ffi::sgba_set_eq_constraints(self.raw, n, pose.as_ptr(), radius.as_ptr()) })
     }
 
     /// `Optimizer::new`: validates the solver configuration, evaluates the
