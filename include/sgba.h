@@ -44,6 +44,7 @@ typedef enum {
   SGBA_ERR_OUT_OF_MEMORY = -6,
   SGBA_ERR_STATE = -7,                /* call out of order (e.g. step before init) */
   SGBA_ERR_DEVICE_TIMEOUT = -8,       /* a bounded device wait gave up */
+  SGBA_ERR_FACTORIZATION = -9,        /* covariance: H_mm or S could not be factored */
 } sgba_status;
 
 /* Problem description (host SoA; the caller keeps ownership, the library copies).
@@ -312,6 +313,65 @@ int sgba_debug_last_system(sgba_problem *p, double *s_dense, double *rhs, double
  * float-float).  j_pose: n*12 doubles, j_point: n*6.  Synchronous. */
 int sgba_debug_jacobians(sgba_problem *p, int64_t n, const int32_t *cam, const int32_t *pt, int32_t precision,
                          double *j_pose, double *j_point);
+
+/* ---- covariance and precision queries of the solution ---------------------
+ * Replaces OptimizationSolution::covariance_block / precision_block
+ * (crates/sophus_opt/src/nlls/optimizer_types.rs:277-370) over the final
+ * Hessian that Optimizer::build_solution evaluates with zero damping
+ * (crates/sophus_opt/src/nlls/optimizer.rs:609-646), answered through the
+ * Schur factor as SchurFactor::inverse_block does
+ * (crates/sophus_solver/src/ldlt/schur_ldlt.rs:815-957):
+ *   pose x pose    S^-1 block
+ *   pose x point   -(S^-1 H_fm H_mm^-1) block (and its transpose)
+ *   point x point  H_mm^-1 delta_ij + H_mm[i]^-1 H_mf_i S^-1 H_mf_j^T H_mm[j]^-1
+ * with S^-1 the min-norm pseudo-inverse when the LDL^T of S has zero pivots
+ * (min_norm_ldlt.rs:55-140).  All in f64 on the device.
+ *
+ * sgba_covariance_prepare evaluates H at the current variables (after
+ * sgba_optimize: the solution), forms S, factors and inverts it; the queries
+ * answer from that snapshot until the next prepare or release (like the
+ * reference's solution object, later changes of the variables do not reach
+ * it).  Problems with free intrinsics or equality constraints, and more than
+ * 4096 free poses, are SGBA_ERR_UNSUPPORTED; an H_mm block with a zero
+ * determinant or an S the factor rejects (a non-finite pivot, or an
+ * indefinite block in the Bunch-Kaufman case) is SGBA_ERR_FACTORIZATION.
+ * Memory: 2 (6 nf)^2 doubles for S and its inverse, 66 doubles per reduced
+ * term. */
+typedef struct {
+  int32_t n;          /* rows of S (6 per free pose) */
+  int32_t rank;       /* positive pivots of its LDL^T (n: S^-1; fewer: the min-norm pseudo-inverse) */
+  int32_t kernel_launches;
+  int32_t pad;
+  double ms_assemble; /* device time: H blocks and S */
+  double ms_factor;   /* LDL^T */
+  double ms_inverse;  /* S^-1 or S+ */
+} sgba_cov_info;
+int sgba_covariance_prepare(sgba_problem *p, sgba_cov_info *info);
+int sgba_covariance_release(sgba_problem *p);
+
+/* Variable kinds of a query: the reference's variable families. */
+enum {
+  SGBA_VAR_POSE = 1,  /* index: pose (camera) index */
+  SGBA_VAR_POINT = 2  /* index: point index */
+};
+typedef struct {
+  int32_t row_kind;  /* SGBA_VAR_* */
+  int32_t row_index;
+  int32_t col_kind;
+  int32_t col_index;
+} sgba_cov_query;
+enum {
+  SGBA_QUERY_COVARIANCE = 0, /* covariance_block */
+  SGBA_QUERY_PRECISION = 1   /* precision_block: the block of the undamped H */
+};
+/* n block queries in one launch.  out: 36 doubles per query (rows x cols,
+ * row-major, rows 6 for a pose and 3 for a point); dims: 2 per query
+ * (rows, cols), (0, 0) where the reference returns None (a constant pose or
+ * point, an index out of range).  Requires sgba_covariance_prepare (else
+ * SGBA_ERR_STATE); an unknown kind or mode is SGBA_ERR_INVALID_ARGUMENT.
+ * Synchronous. */
+int sgba_covariance_blocks(sgba_problem *p, int32_t mode, int32_t n, const sgba_cov_query *queries, double *out,
+                           int32_t *dims);
 
 /* Opaque optimizer state (variables, damping, reject count, step count) for
  * resume: *size receives the byte size when buf is NULL. */

@@ -21,6 +21,7 @@ pub const SGBA_ERR_CUDA: c_int = -5;
 pub const SGBA_ERR_OUT_OF_MEMORY: c_int = -6;
 pub const SGBA_ERR_STATE: c_int = -7;
 pub const SGBA_ERR_DEVICE_TIMEOUT: c_int = -8;
+pub const SGBA_ERR_FACTORIZATION: c_int = -9;
 
 // sgba_termination (TerminationReason, crates/sophus_opt/src/nlls/optimizer_types.rs:93-122)
 pub const SGBA_TERM_NONE: i32 = 0;
@@ -161,6 +162,35 @@ pub struct sgba_layout {
     pub intrinsics_rows: i32,
 }
 
+/// Result of `sgba_covariance_prepare`: the order of S, the positive pivots of
+/// its LDL^T (fewer than n: the min-norm pseudo-inverse) and device times.
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct sgba_cov_info {
+    pub n: i32,
+    pub rank: i32,
+    pub kernel_launches: i32,
+    pub pad: i32,
+    pub ms_assemble: f64,
+    pub ms_factor: f64,
+    pub ms_inverse: f64,
+}
+
+pub const SGBA_VAR_POSE: i32 = 1;
+pub const SGBA_VAR_POINT: i32 = 2;
+pub const SGBA_QUERY_COVARIANCE: i32 = 0;
+pub const SGBA_QUERY_PRECISION: i32 = 1;
+
+/// One block query: (row kind, row index) x (col kind, col index).
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct sgba_cov_query {
+    pub row_kind: i32,
+    pub row_index: i32,
+    pub col_kind: i32,
+    pub col_index: i32,
+}
+
 pub const SGBA_CAMERA_PINHOLE: i32 = 0;
 pub const SGBA_CAMERA_EUCM: i32 = 1;
 
@@ -298,6 +328,16 @@ extern "C" {
         precision: i32,
         j_pose: *mut f64,
         j_point: *mut f64,
+    ) -> c_int;
+    pub fn sgba_covariance_prepare(p: *mut sgba_problem, info: *mut sgba_cov_info) -> c_int;
+    pub fn sgba_covariance_release(p: *mut sgba_problem) -> c_int;
+    pub fn sgba_covariance_blocks(
+        p: *mut sgba_problem,
+        mode: i32,
+        n: i32,
+        queries: *const sgba_cov_query,
+        out: *mut f64,
+        dims: *mut i32,
     ) -> c_int;
     pub fn sgba_state_save(p: *mut sgba_problem, buf: *mut c_void, size: *mut usize) -> c_int;
     pub fn sgba_state_load(p: *mut sgba_problem, buf: *const c_void, size: usize) -> c_int;

@@ -40,6 +40,8 @@ pub enum ErrorKind {
     State,
     /// A bounded device wait gave up.
     DeviceTimeout,
+    /// Covariance: an H_mm block or S could not be factored.
+    Factorization,
     /// A status this binding does not know.
     Unknown,
 }
@@ -55,6 +57,7 @@ impl ErrorKind {
             ffi::SGBA_ERR_OUT_OF_MEMORY => Self::OutOfMemory,
             ffi::SGBA_ERR_STATE => Self::State,
             ffi::SGBA_ERR_DEVICE_TIMEOUT => Self::DeviceTimeout,
+            ffi::SGBA_ERR_FACTORIZATION => Self::Factorization,
             _ => Self::Unknown,
         }
     }
@@ -337,6 +340,46 @@ impl Problem {
         let n = to_i32(pose.len(), "too many constraints")?;
         // SAFETY: the slices hold n indices and n doubles.
         check(unsafe { ffi::sgba_set_eq_constraints(self.raw, n, pose.as_ptr(), radius.as_ptr()) })
+    }
+
+    /// `build_solution`'s final Hessian at the current variables, S, its
+    /// LDL^T and its inverse (the min-norm pseudo-inverse when S is
+    /// rank-deficient), on the device, for `covariance_block` /
+    /// `precision_block`.
+    pub fn covariance_prepare(&mut self) -> Result<ffi::sgba_cov_info, Error> {
+        let mut info = ffi::sgba_cov_info::default();
+        // SAFETY: `self.raw` is a live handle; `info` is writable.
+        check(unsafe { ffi::sgba_covariance_prepare(self.raw, &mut info) })?;
+        Ok(info)
+    }
+
+    /// Block queries (`OptimizationSolution::covariance_block` with
+    /// `mode` = SGBA_QUERY_COVARIANCE, `precision_block` with
+    /// SGBA_QUERY_PRECISION): per query the (rows, cols) block row-major, or
+    /// None where the reference returns None.
+    pub fn covariance_blocks(
+        &mut self,
+        mode: i32,
+        queries: &[ffi::sgba_cov_query],
+    ) -> Result<Vec<Option<(usize, usize, Vec<f64>)>>, Error> {
+        let n = to_i32(queries.len(), "too many queries")?;
+        let mut out = vec![0.0f64; 36 * queries.len().max(1)];
+        let mut dims = vec![0i32; 2 * queries.len().max(1)];
+        // SAFETY: `queries` holds n queries, `out` 36 n doubles, `dims` 2 n ints.
+        check(unsafe {
+            ffi::sgba_covariance_blocks(self.raw, mode, n, queries.as_ptr(), out.as_mut_ptr(), dims.as_mut_ptr())
+        })?;
+        Ok((0..queries.len())
+            .map(|k| {
+                let (r, c) = (dims[2 * k], dims[2 * k + 1]);
+                if r <= 0 {
+                    None
+                } else {
+                    let (r, c) = (r as usize, c as usize);
+                    Some((r, c, out[36 * k..36 * k + r * c].to_vec()))
+                }
+            })
+            .collect())
     }
 
     /// `Optimizer::new`: validates the solver configuration, evaluates the

@@ -144,6 +144,8 @@ struct sgba_problem {
   char* chunk_ptr = nullptr;
   size_t chunk_left = 0;
   size_t chunk_size = size_t(1) << 20;
+  // covariance of the solution (sgba_covariance_prepare)
+  sgba::CovBufs cov;
 };
 
 namespace {
@@ -1237,6 +1239,7 @@ int sgba_problem_destroy(sgba_problem* p) {
   if (p->stream) cudaStreamSynchronize(p->stream);
   if (p->graph_exec) cudaGraphExecDestroy(p->graph_exec);
   if (p->graph) cudaGraphDestroy(p->graph);
+  for (void* v : p->cov.allocs) cudaFreeAsync(v, p->stream);
   for (void* v : p->allocs) cudaFreeAsync(v, p->stream);  // back to the pool, in stream order
   if (p->flush_buf) cudaFree(p->flush_buf);
   if (p->d.records) cudaFree(p->d.records);
@@ -1707,6 +1710,171 @@ int sgba_debug_jacobians(sgba_problem* p, int64_t n, const int32_t* cam, const i
 }
 
 // State blob: magic, sizes, LM scalars, poses, points.
+// ---------------------------------------------------------------------------
+// Covariance and precision queries of the solution (sgba_cov.cu)
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+namespace {
+
+void cov_free(sgba_problem* p) {
+  for (void* v : p->cov.allocs) cudaFreeAsync(v, p->stream);
+  p->cov = sgba::CovBufs{};
+}
+
+template <class T>
+int cov_alloc(sgba_problem* p, T** ptr, size_t count) {
+  void* v = nullptr;
+  SGBA_CK(cudaMallocFromPoolAsync(&v, sizeof(T) * std::max<size_t>(count, 1), p->pool, p->stream));
+  p->cov.allocs.push_back(v);
+  *ptr = static_cast<T*>(v);
+  return SGBA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sgba_covariance_release(sgba_problem* p) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  SGBA_CK(cudaSetDevice(p->device));
+  cov_free(p);
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  return SGBA_OK;
+}
+
+int sgba_covariance_prepare(sgba_problem* p, sgba_cov_info* info) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  if (p->intr_free)
+    return set_error(SGBA_ERR_UNSUPPORTED, "covariance queries with free intrinsics are not on the GPU path");
+  if (p->sz.n_eq > 0)
+    return set_error(SGBA_ERR_UNSUPPORTED, "covariance queries with equality constraints are not on the GPU path");
+  if (p->plan.nf > kMaxDenseFree)
+    return set_error(SGBA_ERR_UNSUPPORTED, "covariance: %d free poses (at most %d)", p->plan.nf, kMaxDenseFree);
+  SGBA_CK(cudaSetDevice(p->device));
+  SGBA_CK(cudaStreamSynchronize(p->stream));
+  cov_free(p);
+  const sgba::Sizes& s = p->sz;
+  const sgba::Dev& d = p->d;
+  sgba::CovBufs& c = p->cov;
+  const int n = 6 * p->plan.nf;
+  const size_t nn = static_cast<size_t>(n) * n;
+  c.n = n;
+  int st;
+  if ((st = cov_alloc(p, &c.rec, static_cast<size_t>(sgba::kCovRec) * s.ng))) return st;
+  if ((st = cov_alloc(p, &c.y, 18 * static_cast<size_t>(s.ng)))) return st;
+  if ((st = cov_alloc(p, &c.vinv, 9 * static_cast<size_t>(s.nm)))) return st;
+  if ((st = cov_alloc(p, &c.hdiag, 36 * static_cast<size_t>(s.nf)))) return st;
+  if ((st = cov_alloc(p, &c.S, nn))) return st;
+  if ((st = cov_alloc(p, &c.Z, nn))) return st;
+  if ((st = cov_alloc(p, &c.ldiag, 6 * static_cast<size_t>(n)))) return st;
+  if ((st = cov_alloc(p, &c.dpiv, static_cast<size_t>(n)))) return st;
+  if ((st = cov_alloc(p, &c.status, 2))) return st;
+  cudaStream_t str = p->stream;
+  EventSet evs;
+  cudaEvent_t ev[4];
+  for (cudaEvent_t& e : ev) SGBA_CK(evs.create(&e));
+  SGBA_CK(cudaMemsetAsync(c.status, 0, 2 * sizeof(int), str));
+  SGBA_CK(cudaMemsetAsync(c.y, 0, sizeof(double) * 18 * std::max<int64_t>(s.ng, 1), str));
+  if (nn) SGBA_CK(cudaMemsetAsync(c.S, 0, sizeof(double) * nn, str));
+  SGBA_CK(cudaEventRecord(ev[0], str));
+  int launches = 0;
+  // the pose-only cost functions' blocks at the current poses
+  launches += sgba::launch_prior_eval(s, d, d.poses, 1, 0, nullptr, str);
+  launches += sgba::launch_edge_eval(s, d, d.poses, 1, 0, nullptr, str);
+  launches += sgba::launch_cov_assemble(s, d, c, str);
+  SGBA_CK(cudaGetLastError());
+  SGBA_CK(cudaEventRecord(ev[1], str));
+  if (n > 0) launches += sgba::launch_cov_factor(n, c.S, c.ldiag, c.dpiv, c.status, str);
+  SGBA_CK(cudaGetLastError());
+  SGBA_CK(cudaEventRecord(ev[2], str));
+  int hst[2] = {0, 0};
+  std::vector<double> piv(n);
+  SGBA_CK(cudaMemcpyAsync(hst, c.status, sizeof(hst), cudaMemcpyDeviceToHost, str));
+  if (n > 0) SGBA_CK(cudaMemcpyAsync(piv.data(), c.dpiv, sizeof(double) * n, cudaMemcpyDeviceToHost, str));
+  SGBA_CK(cudaStreamSynchronize(str));
+  if (hst[1]) {
+    cov_free(p);
+    return set_error(SGBA_ERR_FACTORIZATION, "covariance: a marginalized point's H block is singular");
+  }
+  if (hst[0]) {
+    cov_free(p);
+    return set_error(SGBA_ERR_FACTORIZATION, "covariance: S could not be factored (%s)",
+                     hst[0] == 1 ? "a non-finite pivot" : "an indefinite block");
+  }
+  std::vector<int32_t> J;
+  for (int j = 0; j < n; ++j)
+    if (piv[j] > 0.0) J.push_back(j);
+  c.rank = static_cast<int>(J.size());
+  if (n > 0) {
+    if (c.rank == n) {
+      launches += sgba::launch_cov_inverse(n, c.S, c.ldiag, c.dpiv, c.Z, str);
+    } else {
+      int g_ok = 1;
+      SGBA_CK(sgba::cov_pinv(n, c.S, c.ldiag, c.dpiv, J, c.Z, p->pool, str, &g_ok));
+      if (!g_ok) {
+        cov_free(p);
+        return set_error(SGBA_ERR_FACTORIZATION, "covariance: E^T E of the positive-pivot columns is singular");
+      }
+    }
+  }
+  SGBA_CK(cudaGetLastError());
+  SGBA_CK(cudaEventRecord(ev[3], str));
+  SGBA_CK(cudaStreamSynchronize(str));
+  c.ready = 1;
+  if (info) {
+    info->n = n;
+    info->rank = c.rank;
+    info->kernel_launches = launches;
+    info->pad = 0;
+    float ms = 0.f;
+    SGBA_CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    info->ms_assemble = ms;
+    SGBA_CK(cudaEventElapsedTime(&ms, ev[1], ev[2]));
+    info->ms_factor = ms;
+    SGBA_CK(cudaEventElapsedTime(&ms, ev[2], ev[3]));
+    info->ms_inverse = ms;
+  }
+  return SGBA_OK;
+}
+
+int sgba_covariance_blocks(sgba_problem* p, int32_t mode, int32_t n, const sgba_cov_query* queries, double* out,
+                           int32_t* dims) {
+  if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
+  if (mode != SGBA_QUERY_COVARIANCE && mode != SGBA_QUERY_PRECISION)
+    return set_error(SGBA_ERR_INVALID_ARGUMENT, "unknown query mode %d", mode);
+  if (n < 0) return set_error(SGBA_ERR_INVALID_ARGUMENT, "negative query count");
+  if (n > 0 && (!queries || !out || !dims)) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!p->cov.ready) return set_error(SGBA_ERR_STATE, "covariance queries need sgba_covariance_prepare first");
+  for (int32_t i = 0; i < n; ++i) {
+    const sgba_cov_query& q = queries[i];
+    for (int32_t kind : {q.row_kind, q.col_kind})
+      if (kind != SGBA_VAR_POSE && kind != SGBA_VAR_POINT)
+        return set_error(SGBA_ERR_INVALID_ARGUMENT, "query %d: unknown variable kind %d", i, kind);
+  }
+  if (n == 0) return SGBA_OK;
+  SGBA_CK(cudaSetDevice(p->device));
+  const size_t qbytes = (sizeof(int32_t) * 4 * static_cast<size_t>(n) + 255) & ~size_t(255);
+  const size_t obytes = sizeof(double) * 36 * static_cast<size_t>(n);
+  void* buf = nullptr;
+  SGBA_CK(cudaMallocFromPoolAsync(&buf, qbytes + obytes + sizeof(int32_t) * 2 * static_cast<size_t>(n), p->pool,
+                                  p->stream));
+  int32_t* dq = static_cast<int32_t*>(buf);
+  double* dout = reinterpret_cast<double*>(static_cast<char*>(buf) + qbytes);
+  int32_t* ddims = reinterpret_cast<int32_t*>(static_cast<char*>(buf) + qbytes + obytes);
+  static_assert(sizeof(sgba_cov_query) == 4 * sizeof(int32_t), "query layout");
+  cudaError_t e = cudaMemcpyAsync(dq, queries, sizeof(int32_t) * 4 * n, cudaMemcpyHostToDevice, p->stream);
+  if (e == cudaSuccess) e = sgba::launch_cov_query(p->sz, p->d, p->cov, mode, n, dq, dout, ddims, p->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, obytes, cudaMemcpyDeviceToHost, p->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dims, ddims, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, p->stream);
+  const cudaError_t ef = cudaFreeAsync(buf, p->stream);
+  if (e == cudaSuccess) e = ef;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->stream);
+  SGBA_CK(e);
+  return SGBA_OK;
+}
+
 int sgba_state_save(sgba_problem* p, void* buf, size_t* size) {
   if (!p || !size) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL argument");
   const size_t need = 64 + sizeof(double) * (7 * static_cast<size_t>(p->plan.nc) + 3 * static_cast<size_t>(p->plan.np) + kIntrMax);

@@ -568,6 +568,47 @@ int launch_dense_batch(const DenseBatch* b, cudaStream_t st);
 cudaError_t launch_debug_jacobians(const Sizes& s, const Dev& d, int64_t n, const int32_t* cam, const int32_t* pt,
                                    int precision, double* jp, double* jm, cudaStream_t st);
 
+// ---- covariance queries of the final Hessian (sgba_cov.cu) ---------------
+// Device buffers of one prepared covariance (all f64): per reduced term
+// J_pose^T J_pose (21 upper), W = J_pose^T J_point (18) and
+// J_point^T J_point (6 upper); per term with a free pose Y = W H_mm^-1 (18);
+// per marginalized point H_mm^-1 (9, NaN where H_mm is singular); per free
+// pose its undamped diagonal block of H (36); S (n x n, then its LDL^T factor
+// in the lower triangle), the diagonal blocks' unit-lower factors and the
+// pivots; Z = S^-1 or the min-norm pseudo-inverse S+ (n x n, both triangles).
+constexpr int kCovRec = 48;
+struct CovBufs {
+  int ready = 0;
+  int n = 0;      // rows of S: 6 per free pose
+  int rank = 0;   // pivots > 0
+  double* rec = nullptr;
+  double* y = nullptr;
+  double* vinv = nullptr;
+  double* hdiag = nullptr;
+  double* S = nullptr;
+  double* Z = nullptr;
+  double* ldiag = nullptr;
+  double* dpiv = nullptr;
+  int* status = nullptr;  // [0] factor: 1 non-finite pivot, 2 indefinite (Bunch-Kaufman case); [1] singular H_mm
+  std::vector<void*> allocs;
+};
+// H blocks of every reduced term and point, S assembled at the current
+// variables with zero damping (the priors' and edges' records must be current).
+int launch_cov_assemble(const Sizes& s, const Dev& d, const CovBufs& c, cudaStream_t st);
+// LDL^T of the n x n S in place (the reference's per-block pivot rule).
+int launch_cov_factor(int n, double* S, double* ldiag, double* dpiv, int* status, cudaStream_t st);
+// Z = S^-1 from the factor (full rank).
+int launch_cov_inverse(int n, const double* L, const double* ldiag, const double* dpiv, double* Z, cudaStream_t st);
+// Z = S+ = E G^-1 diag(d_J)^-1 G^-1 E^T (rank-deficient S; J the positive
+// pivots, host list); temporaries from `pool` on st.  *g_ok = 0 when G has a
+// pivot <= 0 (synchronises st).
+cudaError_t cov_pinv(int n, const double* L, const double* ldiag, const double* dpiv, const std::vector<int32_t>& J,
+                     double* Z, cudaMemPool_t pool, cudaStream_t st, int* g_ok);
+// Block queries: per query (row kind, row index, col kind, col index),
+// mode 0 covariance, 1 precision (H); out 36 doubles and dims 2 per query.
+cudaError_t launch_cov_query(const Sizes& s, const Dev& d, const CovBufs& c, int mode, int nq, const int32_t* q,
+                             double* out, int32_t* dims, cudaStream_t st);
+
 // Allocation-free total cost over caller-owned device arrays; the scratch is a
 // static __device__ array (sgba_kernels.cu).  Arguments are validated by the
 // caller except the observation indices, which the kernel checks.

@@ -22,6 +22,7 @@ ERR_CUDA = -5
 ERR_OUT_OF_MEMORY = -6
 ERR_STATE = -7
 ERR_DEVICE_TIMEOUT = -8
+ERR_FACTORIZATION = -9
 
 CAMERA_PINHOLE = 0
 CAMERA_EUCM = 1
@@ -175,7 +176,23 @@ EXPORTED = [
     "sgba_pcg_model_destroy", "sgba_pcg_model_set_params", "sgba_pcg_model_get_params",
     "sgba_pcg_trainset_create", "sgba_pcg_trainset_destroy", "sgba_pcg_trainset_size", "sgba_pcg_trainset_add",
     "sgba_pcg_collect", "sgba_pcg_loss_grad", "sgba_pcg_train", "sgba_pcg_evaluate",
+    "sgba_covariance_prepare", "sgba_covariance_release", "sgba_covariance_blocks",
 ]
+
+# covariance queries (sgba_covariance_blocks)
+VAR_POSE = 1
+VAR_POINT = 2
+QUERY_COVARIANCE = 0
+QUERY_PRECISION = 1
+
+
+class CovInfo(C.Structure):
+    _fields_ = [("n", C.c_int32), ("rank", C.c_int32), ("kernel_launches", C.c_int32), ("pad", C.c_int32),
+                ("ms_assemble", C.c_double), ("ms_factor", C.c_double), ("ms_inverse", C.c_double)]
+
+
+class CovQuery(C.Structure):
+    _fields_ = [("row_kind", C.c_int32), ("row_index", C.c_int32), ("col_kind", C.c_int32), ("col_index", C.c_int32)]
 
 
 class PcgTrainParams(C.Structure):
@@ -262,6 +279,9 @@ def lib():
     L.sgba_pcg_train.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(PcgTrainParams), dp]
     L.sgba_pcg_evaluate.argtypes = [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double,
                                     C.POINTER(C.c_int32), dp, C.POINTER(C.c_int32)]
+    L.sgba_covariance_prepare.argtypes = [C.c_void_p, C.POINTER(CovInfo)]
+    L.sgba_covariance_release.argtypes = [C.c_void_p]
+    L.sgba_covariance_blocks.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(CovQuery), dp, ip]
     _lib = L
     return L
 
@@ -436,6 +456,39 @@ class Problem:
         n = pose.shape[0]
         check(lib().sgba_set_eq_constraints(self._h, n, pose.ctypes.data_as(C.POINTER(C.c_int32)) if n else None,
                                             _dptr(radius) if n else None))
+
+    def covariance_prepare(self):
+        """sgba_covariance_prepare: the undamped H at the current variables, S,
+        its LDL^T and its inverse (or min-norm pseudo-inverse) on the device."""
+        info = CovInfo()
+        check(lib().sgba_covariance_prepare(self._h, C.byref(info)))
+        return info
+
+    def covariance_release(self):
+        check(lib().sgba_covariance_release(self._h))
+
+    def covariance_blocks(self, queries, mode=QUERY_COVARIANCE):
+        """Block queries ((row_kind, row_index), (col_kind, col_index)) in one
+        launch: a (rows, cols) array per query, None where the reference
+        returns None (constant variable, index out of range)."""
+        n = len(queries)
+        qs = (CovQuery * max(n, 1))()
+        for k, ((rk, ri), (ck, ci)) in enumerate(queries):
+            qs[k] = CovQuery(int(rk), int(ri), int(ck), int(ci))
+        out = np.zeros((max(n, 1), 36))
+        dims = np.zeros((max(n, 1), 2), dtype=np.int32)
+        check(lib().sgba_covariance_blocks(self._h, int(mode), n, qs, _dptr(out), _ipt(dims)))
+        res = []
+        for k in range(n):
+            r, c = int(dims[k, 0]), int(dims[k, 1])
+            res.append(None if r <= 0 else out[k, :r * c].reshape(r, c).copy())
+        return res
+
+    def covariance_block(self, row, col):
+        return self.covariance_blocks([(row, col)])[0]
+
+    def precision_block(self, row, col):
+        return self.covariance_blocks([(row, col)], QUERY_PRECISION)[0]
 
     def cost(self):
         c = C.c_double()

@@ -389,9 +389,52 @@ class StepInfo:
 
 @dataclass
 class OptimizationSolution:
+    """OptimizationSolution (crates/sophus_opt/src/nlls/optimizer_types.rs:242-370):
+    the variables, the final cost and the steps; covariance_block and
+    precision_block answer from the final Hessian on the GPU (built on the
+    first query, like the reference's lazily built Covariance)."""
     variables: VarFamilies
     final_cost: float
     steps: List[StepInfo]
+    _native: object = field(default=None, repr=False)
+    _names: list = field(default=None, repr=False)
+    _cov_ready: bool = field(default=False, repr=False)
+
+    def _ref(self, family, idx):
+        if self._native is None:
+            raise NllsError("this solution holds no final Hessian")
+        if family == self._names[1]:
+            return (native.VAR_POSE, int(idx))
+        if family == self._names[2]:
+            return (native.VAR_POINT, int(idx))
+        return None  # no such family on this path (or the Conditioned camera): None
+
+    def covariance_block(self, row_family, row_var_idx, col_family, col_var_idx):
+        """Sigma(i, j): H^-1, or the min-norm H+ for a gauge-deficient H; None
+        for a constant variable or an unknown family."""
+        row, col = self._ref(row_family, row_var_idx), self._ref(col_family, col_var_idx)
+        if row is None or col is None:
+            return None
+        if not self._cov_ready:
+            self._native.covariance_prepare()
+            self._cov_ready = True
+        return self._native.covariance_block(row, col)
+
+    def precision_block(self, row_family, row_var_idx, col_family, col_var_idx):
+        """The block H(i, j) of the undamped final Hessian, or None."""
+        row, col = self._ref(row_family, row_var_idx), self._ref(col_family, col_var_idx)
+        if row is None or col is None:
+            return None
+        if not self._cov_ready:
+            self._native.covariance_prepare()
+            self._cov_ready = True
+        return self._native.precision_block(row, col)
+
+    def close(self):
+        """Release the device copy of the problem held for the queries."""
+        if self._native is not None:
+            self._native.close()
+            self._native = None
 
 
 @dataclass
@@ -574,9 +617,10 @@ class Optimizer:
     def build_solution(self):
         poses, points = self._gpu.variables()
         cost = self._gpu.cost()
+        # the device problem moves to the solution (covariance / precision queries)
         sol = OptimizationSolution(_write_back(self._variables, self._names, poses, points, self._intrinsics()),
-                                   cost, self._steps)
-        self._gpu.close()
+                                   cost, self._steps, self._gpu, list(self._names))
+        self._gpu = None
         return sol
 
 
@@ -584,11 +628,16 @@ def optimize_nlls(variables, cost_fns, eq_fns, params, device=-1):
     """optimize_nlls on the GPU: steps until a termination reason, then build_solution."""
     _validate_solver_config(variables, cost_fns, eq_fns, params)
     prob, names = _extract_problem(variables, cost_fns)
-    with native.Problem(prob, device=device) as gp:
+    gp = native.Problem(prob, device=device)
+    try:
         _set_priors(gp, prob)
         recs, _ = gp.optimize(params)
         poses, points = gp.variables()
         intr = gp.intrinsics() if prob.intrinsics_free else None
         cost = gp.cost()
+    except BaseException:
+        gp.close()
+        raise
     steps = [_step_info(r, k) for k, r in enumerate(recs)]
-    return OptimizationSolution(_write_back(variables, names, poses, points, intr), cost, steps)
+    # the device problem stays with the solution for covariance / precision queries
+    return OptimizationSolution(_write_back(variables, names, poses, points, intr), cost, steps, gp, list(names))
