@@ -1769,6 +1769,7 @@ int sgba_covariance_prepare(sgba_problem* p, sgba_cov_info* info) {
   if ((st = cov_alloc(p, &c.Z, nn))) return st;
   if ((st = cov_alloc(p, &c.ldiag, 6 * static_cast<size_t>(n)))) return st;
   if ((st = cov_alloc(p, &c.dpiv, static_cast<size_t>(n)))) return st;
+  if ((st = cov_alloc(p, &c.work, sgba::cov_inverse_work(n)))) return st;
   if ((st = cov_alloc(p, &c.status, 2))) return st;
   cudaStream_t str = p->stream;
   EventSet evs;
@@ -1808,7 +1809,7 @@ int sgba_covariance_prepare(sgba_problem* p, sgba_cov_info* info) {
   c.rank = static_cast<int>(J.size());
   if (n > 0) {
     if (c.rank == n) {
-      launches += sgba::launch_cov_inverse(n, c.S, c.ldiag, c.dpiv, c.Z, str);
+      launches += sgba::launch_cov_inverse(n, c.S, c.ldiag, c.dpiv, c.Z, c.work, str);
     } else {
       int g_ok = 1;
       SGBA_CK(sgba::cov_pinv(n, c.S, c.ldiag, c.dpiv, J, c.Z, p->pool, str, &g_ok));

@@ -45,17 +45,20 @@
 //                    zeroed and zeroes its column of L), solves its rows of
 //                    the column below, then the trailing lower triangle is
 //                    updated in 32 x 32 tiles
-//   k_cov_inv_row /  Z = S^-1 by the Takahashi recurrence on the factor,
-//   k_cov_inv_diag   block rows last to first:
-//                      Z_rc = delta_rc / d_r - sum_{m > r} L_mr Z_mc  (c >= r),
-//                    the off-diagonal columns of the block row in one launch
-//                    (thread per column, reading rows of Z written by the
-//                    launches before), then the 6x6 diagonal block
+//   k_cov_inv_part / Z = S^-1 by the Takahashi recurrence on the factor,
+//   k_cov_inv_fin /  block rows last to first:
+//   k_cov_inv_diag     Z_rc = delta_rc / d_r - sum_{m > r} L_mr Z_mc  (c >= r);
+//                    the sums over m of the block row's columns beyond the
+//                    block (thread per column, rows m split over CTAs, reading
+//                    rows of Z written by the launches before), their finish
+//                    (the 6-row recurrence, the row and its mirror, the
+//                    diagonal block's sums), then the 6x6 diagonal block
 //   k_cov_gemm       tiled f64 products of the pseudo-inverse (rank-deficient S)
 //   k_cov_query      CTA per query: covariance or H blocks from Z, Y, H_mm^-1
 #include <cuda_runtime.h>
 
 #include <cfloat>
+#include <algorithm>
 #include <cstdint>
 #include <vector>
 
@@ -69,7 +72,8 @@ namespace {
 constexpr int kCovThreads = 256;
 constexpr double kCovTolRel = 1e-12;  // BlockSparseLdlt's tol_rel
 constexpr int kUT = 32;               // trailing-update tile
-constexpr int kInvRows = 256;         // rows of L staged per round of k_cov_inv_row
+constexpr int kInvRows = 256;         // rows of L staged per round of k_cov_inv_part
+constexpr int kInvSplitMax = 32;      // ranges of rows m of one block row at most
 constexpr int kGT = 64, kGK = 16;     // GEMM tile and depth
 
 // ---------------------------------------------------------------------------
@@ -412,69 +416,107 @@ __global__ void __launch_bounds__(kCovThreads) k_cov_update(int n, int k, double
 }
 
 // ---------------------------------------------------------------------------
-// Inverse from the factor (Takahashi): block row i, columns c >= 6i + 6.
+// Inverse from the factor (Takahashi), block row i (rows r0 = 6i .. r0 + 5),
+// three launches: the sums over the rows m >= 6i + 6 split over ranges of m
+// (enough CTAs to fill the GPU when few columns remain), the finish (sums in
+// range order, the 6-row recurrence, the row and its mirror, and per CTA the
+// diagonal block's sums over the new row), the diagonal block.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kCovThreads) k_cov_inv_row(int n, int i, const double* __restrict__ L,
-                                                            const double* __restrict__ ldiag, double* Z) {
-  const int r0 = 6 * i, cb = r0 + 6;
+__global__ void __launch_bounds__(kCovThreads) k_cov_inv_part(int n, int i, int kchunk, const double* __restrict__ L,
+                                                             const double* __restrict__ Z, double* __restrict__ part) {
+  const int r0 = 6 * i, cb = r0 + 6, ncols = n - cb;
   const int c = cb + blockIdx.x * blockDim.x + threadIdx.x;
+  const int mbeg = cb + blockIdx.y * kchunk, mend = min(n, mbeg + kchunk);
   __shared__ double Ls[kInvRows][6];
   double acc[6] = {0, 0, 0, 0, 0, 0};
-  for (int m0 = cb; m0 < n; m0 += kInvRows) {
+  for (int m0 = mbeg; m0 < mend; m0 += kInvRows) {
     __syncthreads();
     for (int e = threadIdx.x; e < kInvRows * 6; e += blockDim.x) {
       const int mm = e / 6, t = e % 6;
-      Ls[mm][t] = (m0 + mm < n) ? L[static_cast<int64_t>(m0 + mm) * n + r0 + t] : 0.0;
+      Ls[mm][t] = (m0 + mm < mend) ? L[static_cast<int64_t>(m0 + mm) * n + r0 + t] : 0.0;
     }
     __syncthreads();
     if (c < n) {
-      const int mend = min(kInvRows, n - m0);
+      const int cnt = min(kInvRows, mend - m0);
       const double* zc = Z + static_cast<int64_t>(m0) * n + c;
-      for (int mm = 0; mm < mend; ++mm) {
+      for (int mm = 0; mm < cnt; ++mm) {
         const double z = zc[static_cast<int64_t>(mm) * n];
 #pragma unroll
         for (int t = 0; t < 6; ++t) acc[t] += Ls[mm][t] * z;
       }
     }
   }
-  if (c >= n) return;
-  const double* Lb = ldiag + 36 * static_cast<int64_t>(i);
-  double z[6];
-  for (int t = 5; t >= 0; --t) {
-    double v = -acc[t];
-    for (int m = t + 1; m < 6; ++m) v -= Lb[6 * m + t] * z[m];
-    z[t] = v;
+  if (c < n)
+    for (int t = 0; t < 6; ++t) part[(static_cast<int64_t>(blockIdx.y) * 6 + t) * ncols + (c - cb)] = acc[t];
+}
+
+__global__ void __launch_bounds__(kCovThreads) k_cov_inv_fin(int n, int i, int nk, const double* __restrict__ L,
+                                                            const double* __restrict__ ldiag, double* Z,
+                                                            const double* __restrict__ part,
+                                                            double* __restrict__ dpart) {
+  const int r0 = 6 * i, cb = r0 + 6, ncols = n - cb;
+  const int c = cb + blockIdx.x * blockDim.x + threadIdx.x;
+  double prod[36];
+#pragma unroll
+  for (int k = 0; k < 36; ++k) prod[k] = 0.0;
+  if (c < n) {
+    double acc[6];
+    for (int t = 0; t < 6; ++t) {
+      double s = 0.0;
+      for (int ks = 0; ks < nk; ++ks) s += part[(static_cast<int64_t>(ks) * 6 + t) * ncols + (c - cb)];
+      acc[t] = s;
+    }
+    const double* Lb = ldiag + 36 * static_cast<int64_t>(i);
+    double z[6];
+    for (int t = 5; t >= 0; --t) {
+      double v = -acc[t];
+      for (int m = t + 1; m < 6; ++m) v -= Lb[6 * m + t] * z[m];
+      z[t] = v;
+    }
+    for (int t = 0; t < 6; ++t) {
+      Z[static_cast<int64_t>(r0 + t) * n + c] = z[t];
+      Z[static_cast<int64_t>(c) * n + r0 + t] = z[t];
+    }
+    // the diagonal block's sums over m >= cb: L_m,r0+t Z_m,r0+u with Z_m,r0+u = z_u of column m = c
+    const double* lc = L + static_cast<int64_t>(c) * n + r0;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      const double l = lc[t];
+#pragma unroll
+      for (int u = 0; u < 6; ++u) prod[6 * t + u] = l * z[u];
+    }
   }
-  for (int t = 0; t < 6; ++t) {
-    Z[static_cast<int64_t>(r0 + t) * n + c] = z[t];
-    Z[static_cast<int64_t>(c) * n + r0 + t] = z[t];
+  // CTA sums in a fixed order: a shuffle tree per warp, then the warps in order
+  __shared__ double ws[kCovThreads / 32][36];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < 36; ++k) {
+    double v = prod[k];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if (lane == 0) ws[warp][k] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 36) {
+    double s = 0.0;
+    for (int w = 0; w < kCovThreads / 32; ++w) s += ws[w][threadIdx.x];
+    dpart[36 * static_cast<int64_t>(blockIdx.x) + threadIdx.x] = s;
   }
 }
 
-// The 6x6 diagonal block of block row i: the sums over rows m >= 6i + 6 split
-// over 7 groups of 36 threads (fixed order), then the recurrence in one thread.
-__global__ void __launch_bounds__(kCovThreads) k_cov_inv_diag(int n, int i, const double* __restrict__ L,
-                                                             const double* __restrict__ ldiag,
-                                                             const double* __restrict__ dpiv, double* Z) {
-  const int r0 = 6 * i, cb = r0 + 6;
-  constexpr int kGroups = kCovThreads / 36;
-  __shared__ double part[kGroups][36];
-  const int tid = threadIdx.x;
-  if (tid < kGroups * 36) {
-    const int grp = tid / 36, pr = tid % 36, t = pr / 6, u = pr % 6;
+// The 6x6 diagonal block: the finish CTAs' sums in order, then the recurrence
+// (columns last to first within each row, rows last to first) in one thread.
+__global__ void __launch_bounds__(64) k_cov_inv_diag(int n, int i, int nfin, const double* __restrict__ ldiag,
+                                                    const double* __restrict__ dpiv, const double* __restrict__ dpart,
+                                                    double* Z) {
+  const int r0 = 6 * i;
+  __shared__ double acc[36];
+  if (threadIdx.x < 36) {
     double s = 0.0;
-    for (int m = cb + grp; m < n; m += kGroups)
-      s += L[static_cast<int64_t>(m) * n + r0 + t] * Z[static_cast<int64_t>(m) * n + r0 + u];
-    part[grp][pr] = s;
+    for (int b = 0; b < nfin; ++b) s += dpart[36 * static_cast<int64_t>(b) + threadIdx.x];
+    acc[threadIdx.x] = s;
   }
   __syncthreads();
-  if (tid != 0) return;
-  double acc[36];
-  for (int pr = 0; pr < 36; ++pr) {
-    double s = 0.0;
-    for (int g = 0; g < kGroups; ++g) s += part[g][pr];
-    acc[pr] = s;
-  }
+  if (threadIdx.x != 0) return;
   const double* Lb = ldiag + 36 * static_cast<int64_t>(i);
   double Zd[36];
   for (int t = 5; t >= 0; --t)
@@ -750,16 +792,33 @@ int launch_cov_factor(int n, double* S, double* ldiag, double* dpiv, int* status
   return nl;
 }
 
-int launch_cov_inverse(int n, const double* L, const double* ldiag, const double* dpiv, double* Z, cudaStream_t st) {
+size_t cov_inverse_work(int n) {
+  return static_cast<size_t>(kInvSplitMax) * 6 * n + static_cast<size_t>((n + kCovThreads - 1) / kCovThreads) * 36 + 64;
+}
+
+int launch_cov_inverse(int n, const double* L, const double* ldiag, const double* dpiv, double* Z, double* work,
+                       cudaStream_t st) {
   const int nb = n / 6;
   int nl = 0;
+  int num_sms = 152;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+  double* part = work;
+  double* dpart = work + static_cast<size_t>(kInvSplitMax) * 6 * n;
   for (int i = nb - 1; i >= 0; --i) {
     const int cols = n - 6 * i - 6;
+    int nfin = 0;
     if (cols > 0) {
-      k_cov_inv_row<<<blocks_for(cols, kCovThreads), kCovThreads, 0, st>>>(n, i, L, ldiag, Z);
-      ++nl;
+      nfin = static_cast<int>(blocks_for(cols, kCovThreads));
+      // split the rows m so that about two CTAs per SM run, each range at least kInvRows rows
+      int nk = (2 * num_sms + nfin - 1) / nfin;
+      nk = std::max(1, std::min({nk, kInvSplitMax, cols / kInvRows}));
+      const int kchunk = (cols + nk - 1) / nk;
+      k_cov_inv_part<<<dim3(nfin, nk), kCovThreads, 0, st>>>(n, i, kchunk, L, Z, part);
+      k_cov_inv_fin<<<nfin, kCovThreads, 0, st>>>(n, i, nk, L, ldiag, Z, part, dpart);
+      nl += 2;
     }
-    k_cov_inv_diag<<<1, kCovThreads, 0, st>>>(n, i, L, ldiag, dpiv, Z);
+    k_cov_inv_diag<<<1, 64, 0, st>>>(n, i, nfin, ldiag, dpiv, dpart, Z);
     ++nl;
   }
   return nl;
@@ -785,7 +844,8 @@ cudaError_t cov_pinv(int n, const double* L, const double* ldiag, const double* 
   const size_t rr = static_cast<size_t>(r) * r, rpp = static_cast<size_t>(rp) * rp;
   const size_t bytes = rnd(sizeof(int32_t) * r) + 2 * rnd(sizeof(double) * nr) + 2 * rnd(sizeof(double) * rpp) +
                        rnd(sizeof(double) * rr) + rnd(sizeof(double) * r) + rnd(sizeof(double) * rp) +
-                       rnd(sizeof(double) * (rp / 6) * 36) + rnd(sizeof(int) * 4);
+                       rnd(sizeof(double) * (rp / 6) * 36) + rnd(sizeof(int) * 4) +
+                       rnd(sizeof(double) * cov_inverse_work(rp));
   void* buf = nullptr;
   cudaError_t e = cudaMallocFromPoolAsync(&buf, bytes, pool, st);
   if (e != cudaSuccess) return e;
@@ -805,6 +865,7 @@ cudaError_t cov_pinv(int n, const double* L, const double* ldiag, const double* 
   double* gpiv = static_cast<double*>(take(sizeof(double) * rp));
   double* gdiag = static_cast<double*>(take(sizeof(double) * (rp / 6) * 36));
   int* gst = static_cast<int*>(take(sizeof(int) * 4));
+  double* gwork = static_cast<double*>(take(sizeof(double) * cov_inverse_work(rp)));
   std::vector<double> hpiv(rp);
   e = cudaMemcpyAsync(dJ, J.data(), sizeof(int32_t) * r, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(gst, 0, sizeof(int) * 4, st);
@@ -822,7 +883,7 @@ cudaError_t cov_pinv(int n, const double* L, const double* ldiag, const double* 
       if (!(hpiv[k] > 0.0)) *g_ok = 0;  // G is positive definite on the positive-pivot subspace
   }
   if (e == cudaSuccess && *g_ok) {
-    launch_cov_inverse(rp, G, gdiag, gpiv, Gi, st);
+    launch_cov_inverse(rp, G, gdiag, gpiv, Gi, gwork, st);
     k_cov_recip<<<blocks_for(r, 256), 256, 0, st>>>(r, dJ, dpiv, w);
     gemm(r, r, r, Gi, rp, 1, w, Gi, rp, 1, M, r, st);   // M = G^-1 diag(d_J)^-1 G^-1
     gemm(n, r, r, E, r, 1, nullptr, M, r, 1, F, r, st);  // F = E M

@@ -589,6 +589,7 @@ struct CovBufs {
   double* Z = nullptr;
   double* ldiag = nullptr;
   double* dpiv = nullptr;
+  double* work = nullptr;  // the inverse's partial sums
   int* status = nullptr;  // [0] factor: 1 non-finite pivot, 2 indefinite (Bunch-Kaufman case); [1] singular H_mm
   std::vector<void*> allocs;
 };
@@ -597,8 +598,10 @@ struct CovBufs {
 int launch_cov_assemble(const Sizes& s, const Dev& d, const CovBufs& c, cudaStream_t st);
 // LDL^T of the n x n S in place (the reference's per-block pivot rule).
 int launch_cov_factor(int n, double* S, double* ldiag, double* dpiv, int* status, cudaStream_t st);
-// Z = S^-1 from the factor (full rank).
-int launch_cov_inverse(int n, const double* L, const double* ldiag, const double* dpiv, double* Z, cudaStream_t st);
+// Z = S^-1 from the factor (full rank); work: cov_inverse_work(n) doubles.
+size_t cov_inverse_work(int n);
+int launch_cov_inverse(int n, const double* L, const double* ldiag, const double* dpiv, double* Z, double* work,
+                       cudaStream_t st);
 // Z = S+ = E G^-1 diag(d_J)^-1 G^-1 E^T (rank-deficient S; J the positive
 // pivots, host list); temporaries from `pool` on st.  *g_ok = 0 when G has a
 // pivot <= 0 (synchronises st).

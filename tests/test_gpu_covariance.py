@@ -258,7 +258,9 @@ def test_hessian_times_covariance_is_identity_loop(pkg, n_cam):
     identity: the row of pose i of the undamped H times the covariance's column
     of pose j is delta_ij I, i.e.
         H_ii Cov_ij + sum over the points q that pose i sees of W_iq Cov_qj,
-    every block from one batched query of each kind."""
+    every block from one batched query of each kind.  The deviation is
+    bounded by about cond(S) eps: 1e-6 at 300 cameras, 1e-5 at 1500 (S's
+    condition number ~6e10 there)."""
     prob = pkg.synth.generate(pkg.synth.LOOP, n_cam=n_cam, n_pt=200 * n_cam, seed=pkg.synth.BASE_SEED)
     prob.pose_const[:2] = 1
     params = fixed_iter_params(pkg, 2, prob.initial_lm_damping)
@@ -280,4 +282,4 @@ def test_hessian_times_covariance_is_identity_loop(pkg, n_cam):
     print("H Cov = I on the %d-camera loop (n=%d): max deviation %.2e over %d points; assemble %.1f ms, "
           "factor %.1f ms, inverse %.1f ms, %d launches"
           % (n_cam, info.n, worst, len(qs), info.ms_assemble, info.ms_factor, info.ms_inverse, info.kernel_launches))
-    assert worst < 1e-6
+    assert worst < (1e-6 if n_cam <= 300 else 1e-5)
