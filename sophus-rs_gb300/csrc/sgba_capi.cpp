@@ -222,7 +222,8 @@ int dev_upload(sgba_problem* p, T** ptr, const std::vector<T, A>& h) {
 // Persistent host worker pool (the set-up loops of sgba_problem_create run on
 // it; threads are created once per process).  run(n, f) calls f(k) for every
 // k in [0, n) on the workers and the calling thread and returns when all have
-// finished; parallel regions from different host threads are serialised.
+// finished; a region started while another host thread's region runs is
+// executed by its own caller, item by item.
 // The set-up runs about a dozen short regions back to back, so a worker that
 // finished a region watches for the next one for a while (kSpinNs) before it
 // sleeps on the condition variable, and regions are entered and retired
@@ -246,7 +247,15 @@ class HostPool {
       for (int k = 0; k < n; ++k) f(k);
       return;
     }
-    std::lock_guard<std::mutex> region_lock(region_mu_);
+    // Another host thread's region holds the workers (problems created
+    // concurrently, e.g. many local windows): run the items here, in order,
+    // instead of queueing behind it.  The items are the same either way, so
+    // the results are too.
+    std::unique_lock<std::mutex> region_lock(region_mu_, std::try_to_lock);
+    if (!region_lock.owns_lock()) {
+      for (int k = 0; k < n; ++k) f(k);
+      return;
+    }
     Region r;
     r.fn = &f;
     r.n = n;

@@ -1778,19 +1778,23 @@ __global__ void __launch_bounds__(256) k_schur_reduce(SchurArgs a, const Ctrl* c
 // ---------------------------------------------------------------------------
 // Dense reduced systems (local windows: every camera sees most points): S
 // formed by tiles of kSdB x kSdB pose blocks instead of observation pairs.
-// A CTA owns one tile of the lower triangle and streams every point once, in
-// rounds of kSdPts points: thread (point, slot) fetches the Z record of the
-// point's term with the slot's pose (the term table T; zeros where there is
-// none) into registers one round ahead, stores it into shared memory, and
-// every thread then accumulates a 3 x 3 piece of the tile (FP32 within a
-// round, float-float across rounds).  The entries are written as
+// A CTA (kSdThreads threads) owns one tile of the lower triangle and streams
+// every point once, in rounds of kSdPts points: thread (point, slot) fetches
+// the Z records of the point's terms with the slot's row pose and column pose
+// (the term table T; zeros where there is none) into registers one round
+// ahead and stores them into shared memory; every thread then accumulates a
+// 3 x 6 piece of the tile, rows (tid / 8) + 16 i and columns (tid % 8) + 8 j,
+// so that the rows a warp reads are consecutive (no bank conflicts) and each
+// shared-memory load feeds 18 or 9 FMAs (FP32 within a round, float-float
+// across rounds, every entry in point order).  The entries are written as
 // S = U + nu n I - sum Z Z^T (the formula of k_schur_reduce), in f64 and
 // float-float.  Loads per point and tile: 2 kSdB Z records, against two per
 // observation pair.
 // ---------------------------------------------------------------------------
 constexpr int kSdB = 8;          // pose blocks per tile side
 constexpr int kSdT = 6 * kSdB;   // 48 rows / columns
-constexpr int kSdPts = 16;       // points per round: 16 points x 16 slots = one per thread
+constexpr int kSdPts = 16;       // points per round: 16 points x 8 slots, one per thread
+constexpr int kSdThreads = 128;
 
 struct SchurDenseArgs {
   int np, nf, n6;
@@ -1814,6 +1818,16 @@ __device__ __forceinline__ void sd_fetch(const float* zmat, int g, float4* v) {
   }
 }
 
+// the six rows of a fetched record, padded to float4, into shared memory
+__device__ __forceinline__ void sd_store(float (*dst)[4], const float4* v) {
+  reinterpret_cast<float4*>(dst[0])[0] = make_float4(v[0].x, v[0].y, v[0].z, 0.f);
+  reinterpret_cast<float4*>(dst[1])[0] = make_float4(v[0].w, v[1].x, v[1].y, 0.f);
+  reinterpret_cast<float4*>(dst[2])[0] = make_float4(v[1].z, v[1].w, v[2].x, 0.f);
+  reinterpret_cast<float4*>(dst[3])[0] = make_float4(v[2].y, v[2].z, v[2].w, 0.f);
+  reinterpret_cast<float4*>(dst[4])[0] = make_float4(v[3].x, v[3].y, v[3].z, 0.f);
+  reinterpret_cast<float4*>(dst[5])[0] = make_float4(v[3].w, v[4].x, v[4].y, 0.f);
+}
+
 __device__ __forceinline__ void schur_dense_body(SchurDenseArgs a, const Ctrl* ctrl, int bid_, int nblk_) {
   (void)nblk_;
   if (skipping(ctrl)) return;
@@ -1826,63 +1840,65 @@ __device__ __forceinline__ void schur_dense_body(SchurDenseArgs a, const Ctrl* c
   const int tj = bid_ - ti * (ti + 1) / 2;
   const int I0 = ti * kSdB, J0 = tj * kSdB;
   const int tid = threadIdx.x;
-  const int r0 = 3 * (tid >> 4), c0 = 3 * (tid & 15);
-  // this thread's staging slot: point pp of each round, pose fb
-  const int pp = tid >> 4, slot = tid & 15;
-  const int fb = slot < kSdB ? I0 + slot : J0 + slot - kSdB;
-  float(*dst)[4] = slot < kSdB ? &zr[pp][6 * slot] : &zc[pp][6 * (slot - kSdB)];
-  auto term_of = [&](int p0) {
+  const int rq = tid >> 3, cq = tid & 7;  // rows rq + 16 i, columns cq + 8 j
+  // this thread's staging slot: point pp of each round, row pose I0 + slot and column pose J0 + slot
+  const int pp = tid >> 3, slot = tid & 7;
+  const int fr = I0 + slot, fc = J0 + slot;
+  auto term_of = [&](int p0, int f) {
     const int i = p0 + pp;
-    return (i < a.np && fb < a.nf) ? __ldg(a.zterm + static_cast<int64_t>(i) * a.nf + fb) : -1;
+    return (i < a.np && f < a.nf) ? __ldg(a.zterm + static_cast<int64_t>(i) * a.nf + f) : -1;
   };
-  float acc[3][3];
-  Acc accd[3][3];
+  float acc[3][6];
+  Acc accd[3][6];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
+    for (int j = 0; j < 6; ++j) {
       acc[i][j] = 0.0f;
       accd[i][j] = acc_zero();
     }
-  // the term index runs two rounds ahead, the Z record one round ahead
-  float4 v[5];
-  sd_fetch(a.zmat, term_of(0), v);
-  int g_next = term_of(kSdPts);
+  // the term indices run two rounds ahead, the Z records one round ahead
+  float4 vr[5], vc[5];
+  sd_fetch(a.zmat, term_of(0, fr), vr);
+  sd_fetch(a.zmat, term_of(0, fc), vc);
+  int gr_next = term_of(kSdPts, fr), gc_next = term_of(kSdPts, fc);
   for (int p0 = 0; p0 < a.np; p0 += kSdPts) {
     __syncthreads();  // the previous round's reads are done
-    reinterpret_cast<float4*>(dst[0])[0] = make_float4(v[0].x, v[0].y, v[0].z, 0.f);
-    reinterpret_cast<float4*>(dst[1])[0] = make_float4(v[0].w, v[1].x, v[1].y, 0.f);
-    reinterpret_cast<float4*>(dst[2])[0] = make_float4(v[1].z, v[1].w, v[2].x, 0.f);
-    reinterpret_cast<float4*>(dst[3])[0] = make_float4(v[2].y, v[2].z, v[2].w, 0.f);
-    reinterpret_cast<float4*>(dst[4])[0] = make_float4(v[3].x, v[3].y, v[3].z, 0.f);
-    reinterpret_cast<float4*>(dst[5])[0] = make_float4(v[3].w, v[4].x, v[4].y, 0.f);
+    sd_store(&zr[pp][6 * slot], vr);
+    sd_store(&zc[pp][6 * slot], vc);
     __syncthreads();
     if (p0 + kSdPts < a.np) {  // next round, in flight during the products
-      sd_fetch(a.zmat, g_next, v);
-      g_next = term_of(p0 + 2 * kSdPts);
+      sd_fetch(a.zmat, gr_next, vr);
+      sd_fetch(a.zmat, gc_next, vc);
+      gr_next = term_of(p0 + 2 * kSdPts, fr);
+      gc_next = term_of(p0 + 2 * kSdPts, fc);
     }
     const int npt = a.np - p0 < kSdPts ? a.np - p0 : kSdPts;
     for (int q = 0; q < npt; ++q) {
-      float4 ra[3], cb[3];
+      float4 ra[3];
 #pragma unroll
-      for (int i = 0; i < 3; ++i) ra[i] = reinterpret_cast<const float4*>(&zr[q][r0 + i][0])[0];
+      for (int i = 0; i < 3; ++i) ra[i] = reinterpret_cast<const float4*>(&zr[q][rq + 16 * i][0])[0];
 #pragma unroll
-      for (int j = 0; j < 3; ++j) cb[j] = reinterpret_cast<const float4*>(&zc[q][c0 + j][0])[0];
+      for (int h = 0; h < 2; ++h) {
+        float4 cb[3];
 #pragma unroll
-      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) cb[j] = reinterpret_cast<const float4*>(&zc[q][cq + 8 * (3 * h + j)][0])[0];
 #pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          float w = acc[i][j];
-          w = fmaf(ra[i].x, cb[j].x, w);
-          w = fmaf(ra[i].y, cb[j].y, w);
-          w = fmaf(ra[i].z, cb[j].z, w);
-          acc[i][j] = w;
-        }
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            float w = acc[i][3 * h + j];
+            w = fmaf(ra[i].x, cb[j].x, w);
+            w = fmaf(ra[i].y, cb[j].y, w);
+            w = fmaf(ra[i].z, cb[j].z, w);
+            acc[i][3 * h + j] = w;
+          }
+      }
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
+      for (int j = 0; j < 6; ++j) {
         acc_addf(accd[i][j], acc[i][j]);
         acc[i][j] = 0.0f;
       }
@@ -1891,8 +1907,8 @@ __device__ __forceinline__ void schur_dense_body(SchurDenseArgs a, const Ctrl* c
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      const int row = 6 * I0 + r0 + i, col = 6 * J0 + c0 + j;
+    for (int j = 0; j < 6; ++j) {
+      const int row = 6 * I0 + rq + 16 * i, col = 6 * J0 + cq + 8 * j;
       if (row >= a.n6 || col >= a.n6 || col > row) continue;
       const dd t = acc_get(accd[i][j]);
       const int bj = row / 6, bk = col / 6, r = row % 6, cc = col % 6;
@@ -1913,7 +1929,7 @@ __device__ __forceinline__ void schur_dense_body(SchurDenseArgs a, const Ctrl* c
       }
     }
 }
-__global__ void __launch_bounds__(256, 3) k_schur_dense(SchurDenseArgs a, const Ctrl* ctrl) {
+__global__ void __launch_bounds__(kSdThreads, 3) k_schur_dense(SchurDenseArgs a, const Ctrl* ctrl) {
   schur_dense_body(a, ctrl, blockIdx.x, gridDim.x);
 }
 
@@ -3245,7 +3261,7 @@ static int schur_dense_grid(const Sizes& s) {
 
 int launch_schur(const Sizes& s, const Dev& d, cudaStream_t st) {
   if (s.schur_dense) {
-    k_schur_dense<<<schur_dense_grid(s), 256, 0, st>>>(make_schur_dense_args(s, d), d.ctrl);
+    k_schur_dense<<<schur_dense_grid(s), kSdThreads, 0, st>>>(make_schur_dense_args(s, d), d.ctrl);
     return 1 + launch_intr_fill(s, d, st);
   }
   const SchurArgs a = make_schur_args(s, d);
@@ -3701,7 +3717,7 @@ __global__ void __launch_bounds__(64) k_camera_finalize_w(WinTab<FinArgs> t) {
   camera_finalize_body(a.nf, a.fb_tile_begin, a.tile_part, a.ufull, a.bf, a.rb, t.ctrl[q.w], a.with_schur, nullptr,
                        nullptr, nullptr, nullptr, nullptr, q.b, q.nb);
 }
-__global__ void __launch_bounds__(256, 3) k_schur_dense_w(WinTab<SchurDenseArgs> t) {
+__global__ void __launch_bounds__(kSdThreads, 3) k_schur_dense_w(WinTab<SchurDenseArgs> t) {
   const WinPos q = win_pos(t);
   schur_dense_body(t.args[q.w], t.ctrl[q.w], q.b, q.nb);
 }
@@ -3998,7 +4014,7 @@ int batch_launch_iteration(const BatchTables* t, cudaStream_t st) {
   if (go(t->schur)) k_schur_w<<<t->schur.blocks, 256, 0, st>>>(wtab<SchurArgs>(t, t->schur));
   if (go(t->schur_red)) k_schur_reduce_w<<<t->schur_red.blocks, 256, 0, st>>>(wtab<SchurArgs>(t, t->schur_red));
   if (go(t->schur_dense))
-    k_schur_dense_w<<<t->schur_dense.blocks, 256, 0, st>>>(wtab<SchurDenseArgs>(t, t->schur_dense));
+    k_schur_dense_w<<<t->schur_dense.blocks, kSdThreads, 0, st>>>(wtab<SchurDenseArgs>(t, t->schur_dense));
   n += launch_dense_batch(t->dense, st);
   if (go(t->bsub)) k_backsub_chunks_w<<<t->bsub.blocks, 256, t->bsub.smem, st>>>(wtab<BsubArgs>(t, t->bsub));
   if (go(t->gauge)) k_gauge_partials_w<<<t->gauge.blocks, 256, 0, st>>>(wtab<GaugeArgs>(t, t->gauge));

@@ -19,6 +19,7 @@
 #include <cmath>
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <optional>
 #include <set>
 #include <stdexcept>
@@ -204,10 +205,54 @@ struct StepInfo {
   bool accepted;
 };
 
+// A block of the covariance or of the precision matrix, row-major.
+struct Block {
+  int rows = 0, cols = 0;
+  std::vector<double> values;
+};
+
+// OptimizationSolution (crates/sophus_opt/src/nlls/optimizer_types.rs:242-370).
+// covariance_block / precision_block answer from the final Hessian on the
+// GPU; the device problem stays with the solution and the covariance is
+// prepared on the first query (the reference builds its Covariance lazily).
 struct OptimizationSolution {
   VarFamilies variables;
   double final_cost;
   std::vector<StepInfo> steps;
+  std::shared_ptr<sgba_problem> problem{};
+  std::array<std::string, 3> names{};  // camera, pose and point families
+  std::shared_ptr<bool> cov_ready = std::make_shared<bool>(false);
+
+  // Sigma(i, j), or nullopt for a constant variable or another family.
+  std::optional<Block> covariance_block(const std::string& row_family, size_t row_idx, const std::string& col_family,
+                                        size_t col_idx) const {
+    return query(SGBA_QUERY_COVARIANCE, row_family, row_idx, col_family, col_idx);
+  }
+  // H(i, j) of the undamped final Hessian, or nullopt.
+  std::optional<Block> precision_block(const std::string& row_family, size_t row_idx, const std::string& col_family,
+                                       size_t col_idx) const {
+    return query(SGBA_QUERY_PRECISION, row_family, row_idx, col_family, col_idx);
+  }
+  std::optional<Block> query(int mode, const std::string& rf, size_t ri, const std::string& cf, size_t ci) const {
+    if (!problem) throw NllsError("this solution holds no final Hessian");
+    auto kind = [this](const std::string& f) { return f == names[1] ? SGBA_VAR_POSE : f == names[2] ? SGBA_VAR_POINT : 0; };
+    const int rk = kind(rf), ck = kind(cf);
+    if (!rk || !ck) return std::nullopt;
+    if (!*cov_ready) {
+      check(sgba_covariance_prepare(problem.get(), nullptr));
+      *cov_ready = true;
+    }
+    sgba_cov_query q{rk, static_cast<int32_t>(ri), ck, static_cast<int32_t>(ci)};
+    Block b;
+    b.values.assign(36, 0.0);
+    int32_t dims[2] = {0, 0};
+    check(sgba_covariance_blocks(problem.get(), mode, 1, &q, b.values.data(), dims));
+    if (dims[0] <= 0) return std::nullopt;
+    b.rows = dims[0];
+    b.cols = dims[1];
+    b.values.resize(static_cast<size_t>(b.rows) * b.cols);
+    return b;
+  }
 };
 
 namespace detail {
@@ -336,39 +381,34 @@ class Optimizer {
       : vars_(std::move(variables)), params_(params) {
     detail::validate(vars_, costs, params_);
     flat_ = detail::flatten(vars_, costs);
-    p_ = detail::create(flat_, device);
+    p_ = std::shared_ptr<sgba_problem>(detail::create(flat_, device), sgba_problem_destroy);
     sgba_opt_params c = detail::cparams(params_);
-    int st = sgba_optimizer_init(p_, &c);
-    if (st != SGBA_OK) {
-      sgba_problem_destroy(p_);
-      p_ = nullptr;
-      check(st);
-    }
+    check(sgba_optimizer_init(p_.get(), &c));
   }
   Optimizer(const Optimizer&) = delete;
   Optimizer& operator=(const Optimizer&) = delete;
-  ~Optimizer() {
-    if (p_) sgba_problem_destroy(p_);
-  }
   StepInfo step() {
     sgba_iter_record r{};
-    check(sgba_optimizer_step(p_, &r));
+    check(sgba_optimizer_step(p_.get(), &r));
     steps_.push_back(detail::step_info(r, steps_.size()));
     return steps_.back();
   }
+  // The solution shares the device problem (its covariance is prepared at the
+  // variables of its first query; the reference's build_solution consumes
+  // the optimizer, so no step comes between).
   OptimizationSolution build_solution() {
     std::vector<double> poses(flat_.poses.size()), points(flat_.points.size());
-    check(sgba_get_variables(p_, poses.data(), points.data()));
+    check(sgba_get_variables(p_.get(), poses.data(), points.data()));
     double cost = 0.0;
-    check(sgba_get_cost(p_, &cost));
-    return OptimizationSolution{detail::write_back(vars_, flat_, poses, points), cost, steps_};
+    check(sgba_get_cost(p_.get(), &cost));
+    return OptimizationSolution{detail::write_back(vars_, flat_, poses, points), cost, steps_, p_, flat_.names};
   }
 
  private:
   VarFamilies vars_;
   OptParams params_;
   detail::Flat flat_;
-  sgba_problem* p_ = nullptr;
+  std::shared_ptr<sgba_problem> p_;
   std::vector<StepInfo> steps_;
 };
 
@@ -393,10 +433,11 @@ inline OptimizationSolution optimize_nlls(const VarFamilies& variables, const st
     sgba_problem_destroy(p);
     check(st);
   }
-  sgba_problem_destroy(p);
   std::vector<StepInfo> steps;
   for (int k = 0; k < n && k < cap; ++k) steps.push_back(detail::step_info(recs[k], k));
-  return OptimizationSolution{detail::write_back(variables, f, poses, points), cost, steps};
+  // the device problem stays with the solution (covariance / precision queries)
+  return OptimizationSolution{detail::write_back(variables, f, poses, points), cost, steps,
+                              std::shared_ptr<sgba_problem>(p, sgba_problem_destroy), f.names};
 }
 
 }  // namespace opt

@@ -78,6 +78,25 @@ static void simple_cam_marg_points() {
          "camera 2 translation " + std::to_string(t[0]) + "," + std::to_string(t[1]) + "," + std::to_string(t[2]));
   std::printf("OK simple_cam_marg_points (t2 = %.4f %.4f %.4f, cost %.4f, %zu steps)\n", t[0], t[1], t[2],
               sol.final_cost, sol.steps.size());
+  // covariance / precision queries by family name (OptimizationSolution::covariance_block)
+  auto c22 = sol.covariance_block("poses", 2, "poses", 2);
+  EXPECT(c22 && c22->rows == 6 && c22->cols == 6, "pose 2 covariance block");
+  if (c22) {
+    bool sym = true, pos = true;
+    for (int a = 0; a < 6; ++a) {
+      pos = pos && c22->values[a * 6 + a] > 0.0;
+      for (int b = 0; b < 6; ++b)
+        sym = sym && std::fabs(c22->values[a * 6 + b] - c22->values[b * 6 + a]) <= 1e-12 * std::fabs(c22->values[a * 6 + a]);
+    }
+    EXPECT(sym && pos, "pose 2 covariance is symmetric with a positive diagonal");
+  }
+  auto c2p = sol.covariance_block("poses", 2, "points", 0);
+  EXPECT(c2p && c2p->rows == 6 && c2p->cols == 3, "pose x point covariance block");
+  auto h22 = sol.precision_block("poses", 2, "poses", 2);
+  EXPECT(h22 && h22->rows == 6 && h22->values[0] > 0.0, "pose 2 precision block");
+  EXPECT(!sol.covariance_block("poses", 0, "poses", 2), "a constant pose has no block");
+  EXPECT(!sol.covariance_block("cams", 0, "poses", 2), "the Conditioned camera family has no block");
+  std::printf("OK covariance queries (var t2_x %.3e)\n", c22 ? c22->values[21] : 0.0);
 }
 
 // Circle scene; converge to the ground truth up to the scale gauge about
