@@ -30,13 +30,13 @@
 //                    (term order), its inverse (cofactors, singular iff the
 //                    determinant is 0, as nalgebra's try_inverse), and
 //                    Y = W H_mm^-1 for its terms with a free pose
-//   k_cov_s          thread per lower block (a, b) of S: the diagonal block
+//   k_cov_s          warp per lower block (a, b) of S: the diagonal block
 //                    U_a + priors + edges - sum Y W^T over pose a's terms;
 //                    off-diagonal blocks - sum Y_a W_b^T over the points both
-//                    poses see (a merge of the two poses' term lists, which
-//                    are in point order) + J_m^T J_n of edges; both triangles
-//                    written.  No atomics: every entry has one writer and a
-//                    fixed summation order.
+//                    poses see (the lanes merge slices of the two poses' term
+//                    lists, which are in point order) + J_m^T J_n of edges;
+//                    both triangles written.  No atomics: lane sums by a
+//                    fixed shuffle tree, one writer per entry.
 //   k_cov_panel /    right-looking scalar LDL^T in natural order, one 6-row
 //   k_cov_update     pose block per step: every CTA factors the 6x6 diagonal
 //                    block redundantly with the reference's pivot rule
@@ -255,37 +255,73 @@ __device__ __forceinline__ void sub_ywt(double* acc, const double* Y, const doub
       acc[6 * r + c] -= Y[3 * r] * W[3 * c] + Y[3 * r + 1] * W[3 * c + 1] + Y[3 * r + 2] * W[3 * c + 2];
 }
 
+// the 36 lane sums of a warp by a fixed shuffle tree (lane 0 holds the totals)
+__device__ __forceinline__ void warp_sum36(double* acc) {
+#pragma unroll
+  for (int k = 0; k < 36; ++k)
+    for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
+}
+
+// A warp per lower block (fa, fb) of S.  Diagonal blocks: the lanes take
+// pose fa's terms in turn.  Off-diagonal blocks: lane l merges its slice of
+// pose fa's term list (1/32 of it, in point order) with pose fb's list from
+// the first term at or after the slice's first point (one binary search).
 __global__ void __launch_bounds__(128) k_cov_s(CovSArgs a) {
-  const int64_t s = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  if (s >= a.nsb) return;
+  const int lane = threadIdx.x & 31;
+  const int64_t s = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5;
+  if (s >= a.nsb) return;  // the whole warp
   const int fa = a.sb_row[s], fb = a.sb_col[s];
   double acc[36];
+#pragma unroll
   for (int k = 0; k < 36; ++k) acc[k] = 0.0;
   int64_t ib, ie;
   cam_range(a, fa, &ib, &ie);
   if (fa == fb) {
-    for (int64_t i = ib; i < ie; ++i) {
+    for (int64_t i = ib + lane; i < ie; i += 32) {
       const double* h = a.rec + kCovRec * a.cam_g[i];
       for (int r = 0; r < 6; ++r)
         for (int c = 0; c < 6; ++c) acc[6 * r + c] += h[r <= c ? up_idx(6, r, c) : up_idx(6, c, r)];
     }
-    if (a.prior_beg)
-      for (int q = a.prior_beg[fa]; q < a.prior_beg[fa + 1]; ++q)
-        for (int k = 0; k < 36; ++k) acc[k] += a.prior_out[static_cast<int64_t>(kPriorOut) * q + k];
-    if (a.e_beg)
-      for (int q = a.e_beg[fa]; q < a.e_beg[fa + 1]; ++q)
-        for (int k = 0; k < 36; ++k) acc[k] += a.e_out[static_cast<int64_t>(kPriorOut) * a.e_slot[q] + k];
-    for (int k = 0; k < 36; ++k) a.hdiag[36 * static_cast<int64_t>(fa) + k] = acc[k];
-    for (int64_t i = ib; i < ie; ++i) {
+    warp_sum36(acc);
+    if (lane == 0) {
+      if (a.prior_beg)
+        for (int q = a.prior_beg[fa]; q < a.prior_beg[fa + 1]; ++q)
+          for (int k = 0; k < 36; ++k) acc[k] += a.prior_out[static_cast<int64_t>(kPriorOut) * q + k];
+      if (a.e_beg)
+        for (int q = a.e_beg[fa]; q < a.e_beg[fa + 1]; ++q)
+          for (int k = 0; k < 36; ++k) acc[k] += a.e_out[static_cast<int64_t>(kPriorOut) * a.e_slot[q] + k];
+      for (int k = 0; k < 36; ++k) a.hdiag[36 * static_cast<int64_t>(fa) + k] = acc[k];
+    }
+    // the Schur part, then lane 0 adds back the H block it stored
+#pragma unroll
+    for (int k = 0; k < 36; ++k) acc[k] = 0.0;
+    for (int64_t i = ib + lane; i < ie; i += 32) {
       const int64_t g = a.cam_g[i];
       if (a.pt_mb[a.g_pt[g]] < 0) continue;
       sub_ywt(acc, a.y + 18 * g, a.rec + kCovRec * g + 21);
     }
+    warp_sum36(acc);
+    if (lane == 0)
+      for (int k = 0; k < 36; ++k) acc[k] += a.hdiag[36 * static_cast<int64_t>(fa) + k];
   } else {
     int64_t jb, je;
     cam_range(a, fb, &jb, &je);
-    int64_t i = ib, j = jb;
-    while (i < ie && j < je) {
+    const int64_t len = ie - ib;
+    int64_t i = ib + len * lane / 32;
+    const int64_t iend = ib + len * (lane + 1) / 32;
+    int64_t j = je;
+    if (i < iend) {
+      // first term of pose fb whose point is >= this slice's first point
+      const int p0 = a.g_pt[a.cam_g[i]];
+      int64_t lo = jb, hi = je;
+      while (lo < hi) {
+        const int64_t mid = lo + (hi - lo) / 2;
+        if (a.g_pt[a.cam_g[mid]] < p0) lo = mid + 1;
+        else hi = mid;
+      }
+      j = lo;
+    }
+    while (i < iend && j < je) {
       const int64_t gi = a.cam_g[i], gj = a.cam_g[j];
       const int pi = a.g_pt[gi], pj = a.g_pt[gj];
       if (pi < pj) {
@@ -298,7 +334,8 @@ __global__ void __launch_bounds__(128) k_cov_s(CovSArgs a) {
         ++j;
       }
     }
-    if (a.eblk_begin)
+    warp_sum36(acc);
+    if (lane == 0 && a.eblk_begin)
       for (int q = a.eblk_begin[s]; q < a.eblk_begin[s + 1]; ++q) {
         const int32_t tt = a.eblk_term[q];
         const int64_t term = tt & 0x7fffffff;
@@ -307,6 +344,7 @@ __global__ void __launch_bounds__(128) k_cov_s(CovSArgs a) {
             acc[6 * r + c] += (tt < 0) ? a.e_hmn[36 * term + c * 6 + r] : a.e_hmn[36 * term + r * 6 + c];
       }
   }
+  if (lane != 0) return;
   const int64_t n = a.n;
   for (int r = 0; r < 6; ++r)
     for (int c = 0; c < 6; ++c) {
@@ -769,7 +807,7 @@ int launch_cov_assemble(const Sizes& s, const Dev& d, const CovBufs& c, cudaStre
     a.e_hmn = d.edge_hmn;
     a.S = c.S;
     a.hdiag = c.hdiag;
-    k_cov_s<<<blocks_for(s.nsb, 128), 128, 0, st>>>(a);
+    k_cov_s<<<blocks_for(32 * s.nsb, 128), 128, 0, st>>>(a);
     ++nl;
   }
   return nl;
