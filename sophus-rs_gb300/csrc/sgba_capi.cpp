@@ -77,10 +77,13 @@ int set_error(int status, const char* fmt, ...) {
   return status;
 }
 
+// (a failed call's error is also cleared from the thread's last-error slot, so
+// that a later launch check of another problem on this thread does not see it)
 #define SGBA_CK(expr)                                                                           \
   do {                                                                                          \
     cudaError_t e_ = (expr);                                                                    \
     if (e_ != cudaSuccess) {                                                                    \
+      (void)cudaGetLastError();                                                                 \
       return set_error(e_ == cudaErrorMemoryAllocation ? SGBA_ERR_OUT_OF_MEMORY : SGBA_ERR_CUDA, \
                        "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_), __FILE__, __LINE__);   \
     }                                                                                           \
