@@ -331,8 +331,10 @@ int sgba_debug_jacobians(sgba_problem *p, int64_t n, const int32_t *cam, const i
  * sgba_optimize: the solution), forms S, factors and inverts it; the queries
  * answer from that snapshot until the next prepare or release (like the
  * reference's solution object, later changes of the variables do not reach
- * it).  Problems with free intrinsics or equality constraints, and more than
- * 4096 free poses, are SGBA_ERR_UNSUPPORTED; an H_mm block with a zero
+ * it).  With Free camera params their block comes first (4 or 6 rows, the
+ * reference's family order) and couples to every pose and point.  Problems
+ * with equality constraints, and more than 4096 free poses, are
+ * SGBA_ERR_UNSUPPORTED; an H_mm block with a zero
  * determinant or an S the factor rejects (a non-finite pivot, or an
  * indefinite block in the Bunch-Kaufman case) is SGBA_ERR_FACTORIZATION.
  * Memory: 2 (6 nf)^2 doubles for S and its inverse, 66 doubles per reduced
@@ -351,8 +353,9 @@ int sgba_covariance_release(sgba_problem *p);
 
 /* Variable kinds of a query: the reference's variable families. */
 enum {
-  SGBA_VAR_POSE = 1,  /* index: pose (camera) index */
-  SGBA_VAR_POINT = 2  /* index: point index */
+  SGBA_VAR_INTRINSICS = 0, /* the camera params (index 0); a block only when they are Free */
+  SGBA_VAR_POSE = 1,       /* index: pose (camera) index */
+  SGBA_VAR_POINT = 2       /* index: point index */
 };
 typedef struct {
   int32_t row_kind;  /* SGBA_VAR_* */
@@ -365,9 +368,10 @@ enum {
   SGBA_QUERY_PRECISION = 1   /* precision_block: the block of the undamped H */
 };
 /* n block queries in one launch.  out: 36 doubles per query (rows x cols,
- * row-major, rows 6 for a pose and 3 for a point); dims: 2 per query
+ * row-major, rows 4 or 6 for the camera params, 6 for a pose and 3 for a
+ * point); dims: 2 per query
  * (rows, cols), (0, 0) where the reference returns None (a constant pose or
- * point, an index out of range).  Requires sgba_covariance_prepare (else
+ * point, Conditioned camera params, an index out of range).  Requires sgba_covariance_prepare (else
  * SGBA_ERR_STATE); an unknown kind or mode is SGBA_ERR_INVALID_ARGUMENT.
  * Synchronous. */
 int sgba_covariance_blocks(sgba_problem *p, int32_t mode, int32_t n, const sgba_cov_query *queries, double *out,

@@ -176,6 +176,7 @@ pub struct sgba_cov_info {
     pub ms_inverse: f64,
 }
 
+pub const SGBA_VAR_INTRINSICS: i32 = 0;
 pub const SGBA_VAR_POSE: i32 = 1;
 pub const SGBA_VAR_POINT: i32 = 2;
 pub const SGBA_QUERY_COVARIANCE: i32 = 0;

@@ -1757,8 +1757,6 @@ int sgba_covariance_release(sgba_problem* p) {
 
 int sgba_covariance_prepare(sgba_problem* p, sgba_cov_info* info) {
   if (!p) return set_error(SGBA_ERR_INVALID_ARGUMENT, "NULL problem");
-  if (p->intr_free)
-    return set_error(SGBA_ERR_UNSUPPORTED, "covariance queries with free intrinsics are not on the GPU path");
   if (p->sz.n_eq > 0)
     return set_error(SGBA_ERR_UNSUPPORTED, "covariance queries with equality constraints are not on the GPU path");
   if (p->plan.nf > kMaxDenseFree)
@@ -1769,10 +1767,19 @@ int sgba_covariance_prepare(sgba_problem* p, sgba_cov_info* info) {
   const sgba::Sizes& s = p->sz;
   const sgba::Dev& d = p->d;
   sgba::CovBufs& c = p->cov;
-  const int n = 6 * p->plan.nf;
+  c.nci = p->intr_free ? 6 : 0;
+  c.nk = p->intr_free ? s.intr_nk : 0;
+  const int n = c.nci + 6 * p->plan.nf;
   const size_t nn = static_cast<size_t>(n) * n;
   c.n = n;
   int st;
+  if (p->intr_free) {
+    if ((st = cov_alloc(p, &c.crec, static_cast<size_t>(sgba::kCovCamRec) * std::max<int64_t>(s.ng, 1)))) return st;
+    if ((st = cov_alloc(p, &c.wc, 18 * static_cast<size_t>(std::max(s.nm, 1))))) return st;
+    if ((st = cov_alloc(p, &c.yc, 18 * static_cast<size_t>(std::max(s.nm, 1))))) return st;
+    if ((st = cov_alloc(p, &c.hcc, 36))) return st;
+    if ((st = cov_alloc(p, &c.hcp, 36 * static_cast<size_t>(std::max(s.nf, 1))))) return st;
+  }
   if ((st = cov_alloc(p, &c.rec, static_cast<size_t>(sgba::kCovRec) * s.ng))) return st;
   if ((st = cov_alloc(p, &c.y, 18 * static_cast<size_t>(s.ng)))) return st;
   if ((st = cov_alloc(p, &c.vinv, 9 * static_cast<size_t>(s.nm)))) return st;
@@ -1862,7 +1869,7 @@ int sgba_covariance_blocks(sgba_problem* p, int32_t mode, int32_t n, const sgba_
   for (int32_t i = 0; i < n; ++i) {
     const sgba_cov_query& q = queries[i];
     for (int32_t kind : {q.row_kind, q.col_kind})
-      if (kind != SGBA_VAR_POSE && kind != SGBA_VAR_POINT)
+      if (kind != SGBA_VAR_INTRINSICS && kind != SGBA_VAR_POSE && kind != SGBA_VAR_POINT)
         return set_error(SGBA_ERR_INVALID_ARGUMENT, "query %d: unknown variable kind %d", i, kind);
   }
   if (n == 0) return SGBA_OK;

@@ -138,18 +138,61 @@ __device__ void cov_jacobians(const double* T, const double* p, const double* in
 // index of (a, b), a <= b, in the row-major upper triangle of a k x k matrix
 __device__ __forceinline__ int up_idx(int k, int a, int b) { return a * k - a * (a - 1) / 2 + (b - a); }
 
+// Jacobian of r with respect to the camera params (2 x 6 row-major, columns
+// beyond the model's 4 or 6 zero): J_cam = -d pi / d params
+// (pinhole_reprojection.rs:85, dx_distort_params of perspective.rs and
+// enhanced_unified.rs:158-215): fx fy cx cy, then for the EUCM camera
+// alpha beta with d(1/norm) / d alpha = -(rho - 1) / norm^2 and
+// d(1/norm) / d beta = -alpha r2 / (2 rho norm^2).
+template <bool E>
+__device__ void cov_cam_jacobian(const double* T, const double* p, const double* intr, double* jc) {
+  double Rwc[9];
+  lie::quat_matrix<double>(T, Rwc);
+  double R[9], t[3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[3 * i + j] = Rwc[3 * j + i];
+  for (int i = 0; i < 3; ++i) t[i] = -(R[3 * i] * T[4] + R[3 * i + 1] * T[5] + R[3 * i + 2] * T[6]);
+  const double xc = R[0] * p[0] + R[1] * p[1] + R[2] * p[2] + t[0];
+  const double yc = R[3] * p[0] + R[4] * p[1] + R[5] * p[2] + t[1];
+  const double zc = R[6] * p[0] + R[7] * p[1] + R[8] * p[2] + t[2];
+  const double x = xc / zc, y = yc / zc;
+  for (int k = 0; k < 12; ++k) jc[k] = 0.0;
+  jc[2] = -1.0;
+  jc[6 + 3] = -1.0;
+  if constexpr (E) {
+    const double al = intr[4], be = intr[5];
+    const double r2 = x * x + y * y;
+    const double rho = sqrt(be * r2 + 1.0);
+    const double nrm = al * rho + (1.0 - al);
+    const double in2 = 1.0 / (nrm * nrm);
+    const double da = (rho - 1.0) * in2;
+    const double db = al * r2 * in2 / (2.0 * rho);
+    jc[0] = -x / nrm;
+    jc[6 + 1] = -y / nrm;
+    jc[4] = intr[0] * x * da;
+    jc[5] = intr[0] * x * db;
+    jc[6 + 4] = intr[1] * y * da;
+    jc[6 + 5] = intr[1] * y * db;
+  } else {
+    jc[0] = -x;
+    jc[6 + 1] = -y;
+  }
+}
+
 template <bool E>
 __global__ void __launch_bounds__(kCovThreads) k_cov_groups(int64_t ng, const int64_t* __restrict__ g_begin,
                                                            const int32_t* __restrict__ g_pose,
                                                            const int32_t* __restrict__ g_pt,
                                                            const double* __restrict__ poses,
                                                            const double* __restrict__ points,
-                                                           const double* __restrict__ intr, double* __restrict__ rec) {
+                                                           const double* __restrict__ intr, double* __restrict__ rec,
+                                                           double* __restrict__ crec) {
   const int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (g >= ng) return;
   double jp[12], jm[6];
-  cov_jacobians<E>(poses + 7 * static_cast<int64_t>(g_pose[g]), points + 3 * static_cast<int64_t>(g_pt[g]), intr, jp,
-                   jm);
+  const double* T = poses + 7 * static_cast<int64_t>(g_pose[g]);
+  const double* P = points + 3 * static_cast<int64_t>(g_pt[g]);
+  cov_jacobians<E>(T, P, intr, jp, jm);
   const double cnt = static_cast<double>(g_begin[g + 1] - g_begin[g]);
   double* o = rec + kCovRec * g;
   int k = 0;
@@ -160,6 +203,18 @@ __global__ void __launch_bounds__(kCovThreads) k_cov_groups(int64_t ng, const in
   k = 39;
   for (int i = 0; i < 3; ++i)
     for (int j = i; j < 3; ++j) o[k++] = cnt * (jm[i] * jm[j] + jm[3 + i] * jm[3 + j]);
+  if (!crec) return;
+  // free camera params: J_cam^T J_cam (21 upper), J_cam^T J_pose (6 x 6), J_cam^T J_point (6 x 3)
+  double jc[12];
+  cov_cam_jacobian<E>(T, P, intr, jc);
+  double* oc = crec + kCovCamRec * g;
+  k = 0;
+  for (int a = 0; a < 6; ++a)
+    for (int b = a; b < 6; ++b) oc[k++] = cnt * (jc[a] * jc[b] + jc[6 + a] * jc[6 + b]);
+  for (int a = 0; a < 6; ++a)
+    for (int b = 0; b < 6; ++b) oc[21 + 6 * a + b] = cnt * (jc[a] * jp[b] + jc[6 + a] * jp[6 + b]);
+  for (int a = 0; a < 6; ++a)
+    for (int j = 0; j < 3; ++j) oc[57 + 3 * a + j] = cnt * (jc[a] * jm[j] + jc[6 + a] * jm[3 + j]);
 }
 
 // nalgebra's 3x3 try_inverse: adjugate / determinant, singular iff det == 0
@@ -189,7 +244,9 @@ __global__ void __launch_bounds__(kCovThreads) k_cov_points(int np, const int64_
                                                            const int32_t* __restrict__ pose_fb,
                                                            const int32_t* __restrict__ pt_mb,
                                                            const double* __restrict__ rec, double* __restrict__ vinv,
-                                                           double* __restrict__ y, int* status) {
+                                                           double* __restrict__ y, int* status,
+                                                           const double* __restrict__ crec, double* __restrict__ wc,
+                                                           double* __restrict__ yc) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= np) return;
   const int mb = pt_mb[q];
@@ -214,6 +271,63 @@ __global__ void __launch_bounds__(kCovThreads) k_cov_points(int np, const int64_
       for (int j = 0; j < 3; ++j)
         yo[3 * a + j] = W[3 * a] * Vi[j] + W[3 * a + 1] * Vi[3 + j] + W[3 * a + 2] * Vi[6 + j];
   }
+  if (!crec) return;
+  // free camera params: W_cq = sum of the point's J_cam^T J_point, Y_cq = W_cq H_mm^-1
+  double W[18];
+  for (int k = 0; k < 18; ++k) W[k] = 0.0;
+  for (int64_t g = pt_g_begin[q]; g < pt_g_begin[q + 1]; ++g)
+    for (int k = 0; k < 18; ++k) W[k] += crec[kCovCamRec * g + 57 + k];
+  double* wo = wc + 18 * static_cast<int64_t>(mb);
+  double* yo = yc + 18 * static_cast<int64_t>(mb);
+  for (int a = 0; a < 6; ++a)
+    for (int j = 0; j < 3; ++j) {
+      wo[3 * a + j] = W[3 * a + j];
+      yo[3 * a + j] = W[3 * a] * Vi[j] + W[3 * a + 1] * Vi[3 + j] + W[3 * a + 2] * Vi[6 + j];
+    }
+}
+
+// The camera block of S (free camera params, rows 0..5 of S; rows nk..5 are
+// padding: identity): H_cc = sum over every term of J_cam^T J_cam, minus
+// sum over the marginalized points of Y_cq W_cq^T.  One CTA; thread t sums
+// terms and points t, t + 256, ...; the threads' sums by a fixed tree.
+__global__ void __launch_bounds__(kCovThreads) k_cov_cam(int64_t ng, int nm, int nk, int n,
+                                                        const double* __restrict__ crec,
+                                                        const double* __restrict__ wc, const double* __restrict__ yc,
+                                                        double* __restrict__ S, double* __restrict__ hcc) {
+  __shared__ double red[kCovThreads];
+  double h[21], sc[21];
+  for (int k = 0; k < 21; ++k) h[k] = sc[k] = 0.0;
+  for (int64_t g = threadIdx.x; g < ng; g += blockDim.x)
+    for (int k = 0; k < 21; ++k) h[k] += crec[kCovCamRec * g + k];
+  for (int mb = threadIdx.x; mb < nm; mb += blockDim.x) {
+    const double* W = wc + 18 * static_cast<int64_t>(mb);
+    const double* Y = yc + 18 * static_cast<int64_t>(mb);
+    int k = 0;
+    for (int a = 0; a < 6; ++a)
+      for (int b = a; b < 6; ++b, ++k) sc[k] += Y[3 * a] * W[3 * b] + Y[3 * a + 1] * W[3 * b + 1] + Y[3 * a + 2] * W[3 * b + 2];
+  }
+  for (int part = 0; part < 2; ++part)
+    for (int k = 0; k < 21; ++k) {
+      red[threadIdx.x] = part == 0 ? h[k] : sc[k];
+      __syncthreads();
+      for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        if (part == 0) h[k] = red[0];
+        else sc[k] = red[0];
+      }
+      __syncthreads();
+    }
+  if (threadIdx.x != 0) return;
+  for (int a = 0; a < 6; ++a)
+    for (int b = 0; b < 6; ++b) {
+      const int k = a <= b ? up_idx(6, a, b) : up_idx(6, b, a);
+      const bool real = a < nk && b < nk;
+      hcc[6 * a + b] = real ? h[k] : 0.0;
+      S[static_cast<int64_t>(a) * n + b] = real ? h[k] - sc[k] : (a == b ? 1.0 : 0.0);
+    }
 }
 
 struct CovSArgs {
@@ -239,6 +353,10 @@ struct CovSArgs {
   const double* e_hmn;
   double* S;
   double* hdiag;
+  int nci;             // rows of the camera block before the poses (6 with free camera params, else 0)
+  const double* crec;  // free camera params: per-term camera records (null: conditioned)
+  const double* wc;    // per marginalized point W_cq (6 x 3)
+  double* hcp;         // per free pose H_ca (camera rows x pose columns, 6 x 6)
 };
 
 // the term-list range of free pose fb (its camera tiles are contiguous in cam_g)
@@ -344,15 +462,46 @@ __global__ void __launch_bounds__(128) k_cov_s(CovSArgs a) {
             acc[6 * r + c] += (tt < 0) ? a.e_hmn[36 * term + c * 6 + r] : a.e_hmn[36 * term + r * 6 + c];
       }
   }
-  if (lane != 0) return;
   const int64_t n = a.n;
+  if (lane == 0)
+    for (int r = 0; r < 6; ++r)
+      for (int c = 0; c < 6; ++c) {
+        // the diagonal block from its lower triangle (exactly symmetric)
+        const double v = (fa == fb && c > r) ? acc[6 * c + r] : acc[6 * r + c];
+        const int64_t row = a.nci + 6 * fa + r, col = a.nci + 6 * fb + c;
+        a.S[row * n + col] = v;
+        a.S[col * n + row] = v;
+      }
+  if (fa != fb || !a.crec) return;
+  // free camera params: the pose's camera columns S_ac = H_ac - sum over its
+  // terms with a marginalized point of Y_g W_cq^T (acc[6 r + k]: pose row r, camera column k)
+#pragma unroll
+  for (int k = 0; k < 36; ++k) acc[k] = 0.0;
+  for (int64_t i = ib + lane; i < ie; i += 32) {
+    const double* hc = a.crec + kCovCamRec * a.cam_g[i] + 21;
+    for (int k = 0; k < 6; ++k)
+      for (int r = 0; r < 6; ++r) acc[6 * r + k] += hc[6 * k + r];
+  }
+  warp_sum36(acc);
+  if (lane == 0)
+    for (int k = 0; k < 6; ++k)
+      for (int r = 0; r < 6; ++r) a.hcp[36 * static_cast<int64_t>(fa) + 6 * k + r] = acc[6 * r + k];
+#pragma unroll
+  for (int k = 0; k < 36; ++k) acc[k] = 0.0;
+  for (int64_t i = ib + lane; i < ie; i += 32) {
+    const int64_t g = a.cam_g[i];
+    const int mb = a.pt_mb[a.g_pt[g]];
+    if (mb < 0) continue;
+    sub_ywt(acc, a.y + 18 * g, a.wc + 18 * static_cast<int64_t>(mb));
+  }
+  warp_sum36(acc);
+  if (lane != 0) return;
   for (int r = 0; r < 6; ++r)
-    for (int c = 0; c < 6; ++c) {
-      // the diagonal block from its lower triangle (exactly symmetric)
-      const double v = (fa == fb && c > r) ? acc[6 * c + r] : acc[6 * r + c];
-      const int64_t row = 6 * fa + r, col = 6 * fb + c;
-      a.S[row * n + col] = v;
-      a.S[col * n + row] = v;
+    for (int k = 0; k < 6; ++k) {
+      const double v = a.hcp[36 * static_cast<int64_t>(fa) + 6 * k + r] + acc[6 * r + k];
+      const int64_t row = a.nci + 6 * fa + r;
+      a.S[row * n + k] = v;
+      a.S[static_cast<int64_t>(k) * n + row] = v;
     }
 }
 
@@ -650,6 +799,7 @@ __global__ void k_cov_recip(int r, const int32_t* __restrict__ J, const double* 
 // ---------------------------------------------------------------------------
 struct CovQArgs {
   int nq, mode, nc, np, n;
+  int nci, nk;  // free camera params: rows of their block in S (6) and their count (4 or 6); else 0, 0
   const int32_t* q;
   const int32_t* pose_fb;
   const int32_t* pt_mb;
@@ -660,6 +810,10 @@ struct CovQArgs {
   const double* vinv;
   const double* Z;
   const double* hdiag;
+  const double* wc;   // free camera params: W_cq, Y_cq per marginalized point, H_cc, H_ca per free pose
+  const double* yc;
+  const double* hcc;
+  const double* hcp;
   int n_eterm;
   const int32_t* eterm_fm;
   const int32_t* eterm_fn;
@@ -668,8 +822,13 @@ struct CovQArgs {
   int32_t* dims;
 };
 
-// (kind, index) -> block: pose 1 -> free block, point 2 -> marg block; -1: none
+// (kind, index) -> block: camera 0 (index 0, free params only) -> 0, pose 1
+// -> free block, point 2 -> marg block; -1: none
 __device__ __forceinline__ int cov_resolve(const CovQArgs& a, int kind, int idx, int* dim) {
+  if (kind == 0 && idx == 0 && a.nci > 0) {
+    *dim = a.nk;
+    return 0;
+  }
   if (kind == 1 && idx >= 0 && idx < a.nc) {
     *dim = 6;
     return a.pose_fb[idx];
@@ -680,6 +839,30 @@ __device__ __forceinline__ int cov_resolve(const CovQArgs& a, int kind, int idx,
   }
   *dim = 0;
   return -1;
+}
+
+// Z row / column of a free variable's block: the camera at 0, pose fb after it
+__device__ __forceinline__ int64_t cov_zoff(const CovQArgs& a, int kind, int blk) {
+  return kind == 0 ? 0 : a.nci + 6 * static_cast<int64_t>(blk);
+}
+
+// sum over the free blocks f of point pt (its terms with a free pose, then the
+// camera when its params are free) of Z[row, f] Y_f[:, col]
+__device__ double cov_row_times_y(const CovQArgs& a, int64_t row, int pt, int mb, int col) {
+  double v = 0.0;
+  const double* zr = a.Z + row * a.n;
+  for (int64_t g = a.pt_g_begin[pt]; g < a.pt_g_begin[pt + 1]; ++g) {
+    const int gb = a.pose_fb[a.g_pose[g]];
+    if (gb < 0) continue;
+    const double* Y = a.y + 18 * g;
+    const double* z = zr + a.nci + 6 * static_cast<int64_t>(gb);
+    for (int k = 0; k < 6; ++k) v += z[k] * Y[3 * k + col];
+  }
+  if (a.nci > 0) {
+    const double* Y = a.yc + 18 * static_cast<int64_t>(mb);
+    for (int k = 0; k < a.nk; ++k) v += zr[k] * Y[3 * k + col];
+  }
+  return v;
 }
 
 __global__ void __launch_bounds__(64) k_cov_query(CovQArgs a) {
@@ -694,7 +877,8 @@ __global__ void __launch_bounds__(64) k_cov_query(CovQArgs a) {
     if (e == 0) a.dims[2 * qi] = a.dims[2 * qi + 1] = 0;  // no block (the reference's None)
     return;
   }
-  const bool rf = q[0] == 1, cf = q[2] == 1;
+  const int rk = q[0], ck = q[2];
+  const bool rf = rk != 2, cf = ck != 2;  // free (camera or pose) or marginalized (point)
   const int64_t n = a.n;
   // a query on a point whose H_mm is singular has no covariance
   const bool bad = a.mode == 0 && ((!rf && isnan(a.vinv[9 * static_cast<int64_t>(rb)])) ||
@@ -709,7 +893,13 @@ __global__ void __launch_bounds__(64) k_cov_query(CovQArgs a) {
   double v = 0.0;
   if (a.mode == 1) {
     // precision: blocks of the undamped H
-    if (rf && cf) {
+    if (rk == 0 && ck == 0) {
+      v = a.hcc[6 * r + c];
+    } else if (rk == 0 || ck == 0) {
+      const int other = rk == 0 ? ck : rk, ob = rk == 0 ? cb : rb;
+      const int cr = rk == 0 ? r : c, oc = rk == 0 ? c : r;  // camera row, the other block's column
+      v = other == 1 ? a.hcp[36 * static_cast<int64_t>(ob) + 6 * cr + oc] : a.wc[18 * static_cast<int64_t>(ob) + 3 * cr + oc];
+    } else if (rf && cf) {
       if (rb == cb) {
         v = a.hdiag[36 * static_cast<int64_t>(rb) + 6 * r + c];
       } else {
@@ -728,35 +918,24 @@ __global__ void __launch_bounds__(64) k_cov_query(CovQArgs a) {
         v += a.rec[kCovRec * g + 39 + (r <= c ? up_idx(3, r, c) : up_idx(3, c, r))];
     }
   } else if (rf && cf) {
-    v = a.Z[(6 * static_cast<int64_t>(rb) + r) * n + 6 * cb + c];
+    v = a.Z[(cov_zoff(a, rk, rb) + r) * n + cov_zoff(a, ck, cb) + c];
   } else if (rf != cf) {
-    // -(S^-1[pose rows, :] H_fm) H_mm^-1 = -sum over the point's terms of Z[pose rows, term block] Y
-    const int fb = rf ? rb : cb, pt = rf ? cp : rp;
+    // -(S^-1[free rows, :] H_fm) H_mm^-1 = -sum over the point's free blocks of Z[rows, block] Y
+    const int fk = rf ? rk : ck, fbk = rf ? rb : cb, pt = rf ? cp : rp, mb = rf ? cb : rb;
     const int pr = rf ? r : c, pc = rf ? c : r;
-    for (int64_t g = a.pt_g_begin[pt]; g < a.pt_g_begin[pt + 1]; ++g) {
-      const int gb = a.pose_fb[a.g_pose[g]];
-      if (gb < 0) continue;
-      const double* zr = a.Z + (6 * static_cast<int64_t>(fb) + pr) * n + 6 * gb;
-      const double* Y = a.y + 18 * g;
-      for (int k = 0; k < 6; ++k) v -= zr[k] * Y[3 * k + pc];
-    }
+    v = -cov_row_times_y(a, cov_zoff(a, fk, fbk) + pr, pt, mb, pc);
   } else {
-    // H_mm[i]^-1 delta_ij + sum_g sum_h Y_g^T Z[g block, h block] Y_h
+    // H_mm[i]^-1 delta_ij + sum over the free blocks g of point i and h of point j of Y_g^T Z[g, h] Y_h
     for (int64_t g = a.pt_g_begin[rp]; g < a.pt_g_begin[rp + 1]; ++g) {
       const int gb = a.pose_fb[a.g_pose[g]];
       if (gb < 0) continue;
       const double* Yg = a.y + 18 * g;
-      for (int64_t h = a.pt_g_begin[cp]; h < a.pt_g_begin[cp + 1]; ++h) {
-        const int hb = a.pose_fb[a.g_pose[h]];
-        if (hb < 0) continue;
-        const double* Yh = a.y + 18 * h;
-        for (int k = 0; k < 6; ++k) {
-          const double* zr = a.Z + (6 * static_cast<int64_t>(gb) + k) * n + 6 * hb;
-          double t = 0.0;
-          for (int l = 0; l < 6; ++l) t += zr[l] * Yh[3 * l + c];
-          v += Yg[3 * k + r] * t;
-        }
-      }
+      for (int k = 0; k < 6; ++k)
+        v += Yg[3 * k + r] * cov_row_times_y(a, a.nci + 6 * static_cast<int64_t>(gb) + k, cp, cb, c);
+    }
+    if (a.nci > 0) {
+      const double* Yc = a.yc + 18 * static_cast<int64_t>(rb);
+      for (int k = 0; k < a.nk; ++k) v += Yc[3 * k + r] * cov_row_times_y(a, k, cp, cb, c);
     }
     if (rp == cp) v += a.vinv[9 * static_cast<int64_t>(rb) + 3 * r + c];
   }
@@ -772,15 +951,22 @@ int launch_cov_assemble(const Sizes& s, const Dev& d, const CovBufs& c, cudaStre
   if (s.ng > 0) {
     if (s.eucm)
       k_cov_groups<true><<<blocks_for(s.ng, kCovThreads), kCovThreads, 0, st>>>(s.ng, d.g_begin, d.g_pose, d.g_pt,
-                                                                               d.poses, d.points, d.intr, c.rec);
+                                                                               d.poses, d.points, d.intr, c.rec,
+                                                                               c.crec);
     else
       k_cov_groups<false><<<blocks_for(s.ng, kCovThreads), kCovThreads, 0, st>>>(s.ng, d.g_begin, d.g_pose, d.g_pt,
-                                                                                d.poses, d.points, d.intr, c.rec);
+                                                                                d.poses, d.points, d.intr, c.rec,
+                                                                                c.crec);
     ++nl;
   }
   if (s.np > 0) {
     k_cov_points<<<blocks_for(s.np, kCovThreads), kCovThreads, 0, st>>>(s.np, d.pt_g_begin, d.g_pose, d.pose_fb,
-                                                                       d.pt_mb, c.rec, c.vinv, c.y, c.status);
+                                                                       d.pt_mb, c.rec, c.vinv, c.y, c.status, c.crec,
+                                                                       c.wc, c.yc);
+    ++nl;
+  }
+  if (c.crec) {
+    k_cov_cam<<<1, kCovThreads, 0, st>>>(s.ng, s.nm, c.nk, c.n, c.crec, c.wc, c.yc, c.S, c.hcc);
     ++nl;
   }
   if (s.nsb > 0) {
@@ -807,6 +993,10 @@ int launch_cov_assemble(const Sizes& s, const Dev& d, const CovBufs& c, cudaStre
     a.e_hmn = d.edge_hmn;
     a.S = c.S;
     a.hdiag = c.hdiag;
+    a.nci = c.nci;
+    a.crec = c.crec;
+    a.wc = c.wc;
+    a.hcp = c.hcp;
     k_cov_s<<<blocks_for(32 * s.nsb, 128), 128, 0, st>>>(a);
     ++nl;
   }
@@ -951,6 +1141,12 @@ cudaError_t launch_cov_query(const Sizes& s, const Dev& d, const CovBufs& c, int
   a.vinv = c.vinv;
   a.Z = c.Z;
   a.hdiag = c.hdiag;
+  a.nci = c.nci;
+  a.nk = c.nk;
+  a.wc = c.wc;
+  a.yc = c.yc;
+  a.hcc = c.hcc;
+  a.hcp = c.hcp;
   a.n_eterm = s.n_edge > 0 ? s.n_eterm : 0;
   a.eterm_fm = d.eterm_fm;
   a.eterm_fn = d.eterm_fn;

@@ -569,7 +569,8 @@ cudaError_t launch_debug_jacobians(const Sizes& s, const Dev& d, int64_t n, cons
                                    int precision, double* jp, double* jm, cudaStream_t st);
 
 // ---- covariance queries of the final Hessian (sgba_cov.cu) ---------------
-// Device buffers of one prepared covariance (all f64): per reduced term
+// Device buffers of one prepared covariance (all f64; the camera block first
+// when the camera params are free, as in the reference's family order): per reduced term
 // J_pose^T J_pose (21 upper), W = J_pose^T J_point (18) and
 // J_point^T J_point (6 upper); per term with a free pose Y = W H_mm^-1 (18);
 // per marginalized point H_mm^-1 (9, NaN where H_mm is singular); per free
@@ -577,10 +578,22 @@ cudaError_t launch_debug_jacobians(const Sizes& s, const Dev& d, int64_t n, cons
 // in the lower triangle), the diagonal blocks' unit-lower factors and the
 // pivots; Z = S^-1 or the min-norm pseudo-inverse S+ (n x n, both triangles).
 constexpr int kCovRec = 48;
+// per term with free camera params: J_cam^T J_cam (21 upper), J_cam^T J_pose (6 x 6), J_cam^T J_point (6 x 3)
+constexpr int kCovCamRec = 80;
 struct CovBufs {
   int ready = 0;
-  int n = 0;      // rows of S: 6 per free pose
+  int n = 0;      // rows of S: the camera block (nci rows) and 6 per free pose
+  int nci = 0;    // free camera params: 6 rows (their nk params, then identity padding), else 0
+  int nk = 0;     // free camera params: 4 (pinhole) or 6 (EUCM)
   int rank = 0;   // pivots > 0
+  // free camera params: per term J_cam^T J_cam, J_cam^T J_pose, J_cam^T J_point
+  // (80 doubles); per marginalized point W_cq and Y_cq = W_cq H_mm^-1 (6 x 3
+  // each); H_cc (6 x 6) and per free pose H_ca (camera rows x pose columns)
+  double* crec = nullptr;
+  double* wc = nullptr;
+  double* yc = nullptr;
+  double* hcc = nullptr;
+  double* hcp = nullptr;
   double* rec = nullptr;
   double* y = nullptr;
   double* vinv = nullptr;

@@ -235,9 +235,11 @@ struct OptimizationSolution {
   }
   std::optional<Block> query(int mode, const std::string& rf, size_t ri, const std::string& cf, size_t ci) const {
     if (!problem) throw NllsError("this solution holds no final Hessian");
-    auto kind = [this](const std::string& f) { return f == names[1] ? SGBA_VAR_POSE : f == names[2] ? SGBA_VAR_POINT : 0; };
+    auto kind = [this](const std::string& f) {
+      return f == names[0] ? SGBA_VAR_INTRINSICS : f == names[1] ? SGBA_VAR_POSE : f == names[2] ? SGBA_VAR_POINT : -1;
+    };
     const int rk = kind(rf), ck = kind(cf);
-    if (!rk || !ck) return std::nullopt;
+    if (rk < 0 || ck < 0) return std::nullopt;
     if (!*cov_ready) {
       check(sgba_covariance_prepare(problem.get(), nullptr));
       *cov_ready = true;

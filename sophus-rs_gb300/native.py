@@ -180,6 +180,7 @@ EXPORTED = [
 ]
 
 # covariance queries (sgba_covariance_blocks)
+VAR_INTRINSICS = 0
 VAR_POSE = 1
 VAR_POINT = 2
 QUERY_COVARIANCE = 0

@@ -403,11 +403,13 @@ class OptimizationSolution:
     def _ref(self, family, idx):
         if self._native is None:
             raise NllsError("this solution holds no final Hessian")
+        if family == self._names[0]:
+            return (native.VAR_INTRINSICS, int(idx))  # a block only when the camera params are Free
         if family == self._names[1]:
             return (native.VAR_POSE, int(idx))
         if family == self._names[2]:
             return (native.VAR_POINT, int(idx))
-        return None  # no such family on this path (or the Conditioned camera): None
+        return None  # no such family: None
 
     def covariance_block(self, row_family, row_var_idx, col_family, col_var_idx):
         """Sigma(i, j): H^-1, or the min-norm H+ for a gauge-deficient H; None

@@ -56,6 +56,8 @@ class _FakeNative:
 
     def covariance_block(self, row, col):
         self.calls.append(("cov", row, col))
+        if row[0] == 0 or col[0] == 0:
+            return None  # the device answers None for Conditioned camera params
         return np.zeros((6 if row[0] == 1 else 3, 6 if col[0] == 1 else 3))
 
     def precision_block(self, row, col):
@@ -71,9 +73,9 @@ def test_solution_maps_family_names_to_query_kinds(pkg):
     sol = pkg.OptimizationSolution(None, 0.0, [], fake, ["cams", "poses", "points"])
     assert sol.covariance_block("poses", 3, "points", 11).shape == (6, 3)
     assert sol.precision_block("points", 2, "points", 2).shape == (3, 3)
-    assert sol.covariance_block("cams", 0, "poses", 1) is None  # the Conditioned camera family: None
+    assert sol.covariance_block("cams", 0, "poses", 1) is None  # the camera family goes to the device as kind 0
     assert sol.covariance_block("poses", 1, "no_such_family", 0) is None
     assert fake.prepared == 1  # prepared once, on the first query
-    assert fake.calls == [("cov", (1, 3), (2, 11)), ("prec", (2, 2), (2, 2))]
+    assert fake.calls == [("cov", (1, 3), (2, 11)), ("prec", (2, 2), (2, 2)), ("cov", (0, 0), (1, 1))]
     with pytest.raises(pkg.NllsError):
         pkg.OptimizationSolution(None, 0.0, []).covariance_block("poses", 1, "poses", 1)

@@ -17,15 +17,18 @@ oracle's dense undamped H.
   cost functions   pose priors and pose-graph edges in H and S (every pose free,
                    priors holding the gauge)
   precision        blocks of the undamped H against the oracle's dense H
+  free camera      the camera params Free (pinhole and EUCM): their block
+                   first, coupled to every pose and point; every kind of
+                   block with the camera against the oracle
   None / errors    constant poses, indices out of range, unknown kinds, a
-                   query before prepare, free intrinsics"""
+                   query before prepare, equality constraints"""
 import copy
 
 import numpy as np
 import pytest
 
 from conftest import fixed_iter_params
-from test_oracle_free_intrinsics import _eucm_problem
+from test_oracle_free_intrinsics import _eucm_problem, _problem
 
 pytestmark = pytest.mark.gpu
 
@@ -202,15 +205,17 @@ def test_none_and_errors(pkg):
         assert res[0] is None and res[1] is None and res[2] is None and res[3] is None
         assert res[4].shape == (6, 6) and np.allclose(res[4], res[4].T, rtol=0, atol=1e-12 * np.abs(res[4]).max())
         assert np.all(np.linalg.eigvalsh(res[4]) > 0)
+        assert gp.covariance_block((0, 0), (1, 2)) is None  # Conditioned camera params: no block
         with pytest.raises(pkg.native.SgbaError):
-            gp.covariance_blocks([((0, 0), (1, 2))])  # the Conditioned camera is no query kind
+            gp.covariance_blocks([((5, 0), (1, 2))])  # no such kind
         gp.covariance_release()
         with pytest.raises(pkg.native.SgbaError):
             gp.covariance_block((1, 2), (1, 2))
-    prob2, _, _ = __import__("test_oracle_free_intrinsics")._problem(pkg, seed=3, free=True)
+    prob2 = pkg.synth.generate(pkg.synth.CIRCLE, n_cam=6, n_pt=100, seed=pkg.synth.BASE_SEED + 42)
     with pkg.native.Problem(prob2, device=0) as gp:
+        gp.set_eq_constraints([2], [4.0])
         with pytest.raises(pkg.native.SgbaError) as e:
-            gp.covariance_prepare()
+            gp.covariance_prepare()  # the constraint-projected covariance is not on this path
         assert e.value.status == pkg.native.ERR_UNSUPPORTED
 
 
@@ -283,3 +288,43 @@ def test_hessian_times_covariance_is_identity_loop(pkg, n_cam):
           "factor %.1f ms, inverse %.1f ms, %d launches"
           % (n_cam, info.n, worst, len(qs), info.ms_assemble, info.ms_factor, info.ms_inverse, info.kernel_launches))
     assert worst < (1e-6 if n_cam <= 300 else 1e-5)
+
+
+@pytest.mark.parametrize("model", ["pinhole", "eucm"])
+def test_covariance_free_camera_params(pkg, oracle, model):
+    """Free camera params (the reference's optimize with free intrinsics):
+    camera x camera, camera x pose, camera x point, pose x point and
+    point x point blocks against the oracle, and the camera's precision
+    blocks against the oracle's dense H."""
+    prob = _problem(pkg, seed=3, free=True)[0] if model == "pinhole" else _eucm_problem(pkg, 3)[0]
+    params = fixed_iter_params(pkg, 4, 1.0)
+    with pkg.native.Problem(prob, device=0) as gp:
+        gp.optimize(params)
+        poses, points = gp.variables()
+        intr = gp.intrinsics()
+        at = copy.copy(prob)
+        at.poses, at.points = poses, points
+        at.intrinsics = intr[:4].copy()
+        if len(intr) == 6:
+            at.eucm_alpha_beta = intr[4:].copy()
+        info = gp.covariance_prepare()
+        nk = len(intr)
+        free = [j for j in range(prob.n_cam) if not prob.pose_const[j]]
+        assert info.n == 6 + 6 * len(free) and info.rank == info.n
+        p, q = _observed_points(prob, 2)
+        a = free[-1]
+        queries = [((0, 0), (0, 0)), ((0, 0), (1, a)), ((1, a), (0, 0)), ((0, 0), (2, p)), ((2, q), (0, 0)),
+                   ((1, a), (2, p)), ((2, p), (2, p)), ((2, p), (2, q))]
+        worst = _check(gp, oracle, at, queries)
+        assert gp.covariance_block((0, 0), (0, 0)).shape == (nk, nk)
+        H, _ = oracle.dense_system(at, 0.0)
+        fidx = {j: k for k, j in enumerate(free)}
+        prec = gp.covariance_blocks([((0, 0), (0, 0)), ((0, 0), (1, a)), ((0, 0), (2, p))], pkg.native.QUERY_PRECISION)
+        scale = np.abs(H).max()
+        np.testing.assert_allclose(prec[0], H[:nk, :nk], rtol=1e-10, atol=1e-12 * scale)
+        np.testing.assert_allclose(prec[1], H[:nk, nk + 6 * fidx[a]:nk + 6 * fidx[a] + 6], rtol=1e-10,
+                                   atol=1e-12 * scale)
+        nf = len(free)
+        np.testing.assert_allclose(prec[2], H[:nk, nk + 6 * nf + 3 * p:nk + 6 * nf + 3 * p + 3], rtol=1e-10,
+                                   atol=1e-12 * scale)
+    print("covariance with free camera params (%s): vs oracle %.2e" % (model, worst))
