@@ -28,11 +28,74 @@ pub struct BaFamilies<'a> {
     pub points: &'a str,
 }
 
-/// Optimised variables (in the families' member order) and the run's records.
+/// Optimised variables (in the families' member order) and the run's records;
+/// the device problem stays with them for `OptimizationSolution`'s
+/// covariance and precision queries.
 pub struct BaOutcome {
     pub world_from_cameras: Vec<Isometry3F64>,
     pub points: Vec<VecF64<3>>,
     pub solution: Solution,
+    problem: Problem,
+    families: [String; 3],
+    cov_ready: bool,
+}
+
+impl BaOutcome {
+    fn kind(&self, family: &str) -> Option<i32> {
+        if family == self.families[0] {
+            Some(crate::ffi::SGBA_VAR_INTRINSICS)
+        } else if family == self.families[1] {
+            Some(crate::ffi::SGBA_VAR_POSE)
+        } else if family == self.families[2] {
+            Some(crate::ffi::SGBA_VAR_POINT)
+        } else {
+            None
+        }
+    }
+
+    fn query(
+        &mut self,
+        mode: i32,
+        row_family: &str,
+        row_var_idx: usize,
+        col_family: &str,
+        col_var_idx: usize,
+    ) -> Result<Option<(usize, usize, Vec<f64>)>, Error> {
+        let (Some(rk), Some(ck)) = (self.kind(row_family), self.kind(col_family)) else {
+            return Ok(None);
+        };
+        if !self.cov_ready {
+            self.problem.covariance_prepare()?;
+            self.cov_ready = true;
+        }
+        let idx = |i: usize| i32::try_from(i).map_err(|_| Error::invalid_argument("variable index out of range"));
+        let q = crate::ffi::sgba_cov_query { row_kind: rk, row_index: idx(row_var_idx)?, col_kind: ck, col_index: idx(col_var_idx)? };
+        Ok(self.problem.covariance_blocks(mode, &[q])?.pop().flatten())
+    }
+
+    /// `OptimizationSolution::covariance_block` (optimizer_types.rs:319-370):
+    /// (rows, cols, row-major values), or None for a constant variable or a
+    /// Conditioned family.
+    pub fn covariance_block(
+        &mut self,
+        row_family: &str,
+        row_var_idx: usize,
+        col_family: &str,
+        col_var_idx: usize,
+    ) -> Result<Option<(usize, usize, Vec<f64>)>, Error> {
+        self.query(crate::ffi::SGBA_QUERY_COVARIANCE, row_family, row_var_idx, col_family, col_var_idx)
+    }
+
+    /// `OptimizationSolution::precision_block`: the block of the undamped H.
+    pub fn precision_block(
+        &mut self,
+        row_family: &str,
+        row_var_idx: usize,
+        col_family: &str,
+        col_var_idx: usize,
+    ) -> Result<Option<(usize, usize, Vec<f64>)>, Error> {
+        self.query(crate::ffi::SGBA_QUERY_PRECISION, row_family, row_var_idx, col_family, col_var_idx)
+    }
 }
 
 fn unsupported(message: String) -> Error {
@@ -120,5 +183,8 @@ pub fn optimize_ba(
         world_from_cameras: poses_out.iter().map(|p| Isometry3F64::from_params(VecF64::<7>::from_column_slice(p))).collect(),
         points: points_out.iter().map(|p| VecF64::<3>::new(p[0], p[1], p[2])).collect(),
         solution,
+        problem,
+        families: [families.cams.to_string(), families.poses.to_string(), families.points.to_string()],
+        cov_ready: false,
     })
 }
