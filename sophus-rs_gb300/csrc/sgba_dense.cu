@@ -42,6 +42,9 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "sgba_dd.cuh"
@@ -1131,11 +1134,42 @@ size_t dense_smem_bytes(int P, int C) {
 
 }  // namespace
 
+namespace {
+int dense_cluster_choose(int P, int* cluster, size_t* smem);
+}  // namespace
+
+// The choice depends on the padded order alone; it is made once per
+// (device, block count) and remembered (the occupancy query is a driver call
+// that every problem created on many host threads would otherwise repeat).
 int dense_cluster_setup(int n, int* cluster, size_t* smem) {
   *cluster = 0;
   *smem = 0;
   if (n <= 0) return 0;
   const int P = (n + kNB - 1) / kNB;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, std::pair<int, size_t>> chosen;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    const auto it = chosen.find(std::make_pair(dev, P));
+    if (it != chosen.end()) {
+      *cluster = it->second.first;
+      *smem = it->second.second;
+      return *cluster;
+    }
+  }
+  const int C = dense_cluster_choose(P, cluster, smem);
+  std::lock_guard<std::mutex> lk(mu);
+  chosen[std::make_pair(dev, P)] = std::make_pair(*cluster, *smem);
+  return C;
+}
+
+namespace {
+int dense_cluster_choose(int P, int* cluster, size_t* smem) {
   // one CTA per 24-row block up to 8; beyond, 16 (non-portable) or 8
   int sizes[2] = {16, 8};
   int ncand = 2;
@@ -1179,6 +1213,7 @@ int dense_cluster_setup(int n, int* cluster, size_t* smem) {
   }
   return 0;
 }
+}  // namespace
 
 int small_dense_setup_eq(int n, int n_eq) {
   if (n <= 0 || n > kSmallMax || n_eq < 0 || n_eq > kMaxEq) return 0;
