@@ -79,3 +79,26 @@ def test_solution_maps_family_names_to_query_kinds(pkg):
     assert fake.calls == [("cov", (1, 3), (2, 11)), ("prec", (2, 2), (2, 2)), ("cov", (0, 0), (1, 1))]
     with pytest.raises(pkg.NllsError):
         pkg.OptimizationSolution(None, 0.0, []).covariance_block("poses", 1, "poses", 1)
+
+
+def test_oracle_covariance_free_pinhole_params_vs_dense_inverse(pkg, oracle):
+    """Free pinhole params (4, the oracle's camera block padded to 6 rows in S):
+    camera, pose and point blocks against the dense H^-1, whose camera block
+    has the 4 real rows first."""
+    from test_oracle_free_intrinsics import _problem
+
+    prob, _, _ = _problem(pkg, seed=3, free=True)
+    H, _ = oracle.dense_system(prob, 0.0)
+    cov = np.linalg.inv(H)
+    c0 = 4
+    nf = int(np.sum(prob.pose_const == 0))
+    fidx = np.cumsum(prob.pose_const == 0) - 1
+    cam = slice(0, c0)
+    pose = lambda j: slice(c0 + 6 * fidx[j], c0 + 6 * fidx[j] + 6)
+    point = lambda q: slice(c0 + 6 * nf + 3 * q, c0 + 6 * nf + 3 * q + 3)
+    scale = np.abs(cov).max()
+    for row, col, rs, cs in (((0, 0), (0, 0), cam, cam), ((0, 0), (1, 3), cam, pose(3)),
+                             ((2, 4), (0, 0), point(4), cam), ((1, 2), (2, 4), pose(2), point(4)),
+                             ((2, 4), (2, 6), point(4), point(6))):
+        blk = oracle.covariance_block(prob, row, col)
+        np.testing.assert_allclose(blk, cov[rs, cs], rtol=1e-7, atol=1e-9 * scale, err_msg=str((row, col)))
