@@ -74,6 +74,7 @@ constexpr double kCovTolRel = 1e-12;  // BlockSparseLdlt's tol_rel
 constexpr int kUT = 32;               // trailing-update tile
 constexpr int kInvRows = 256;         // rows of L staged per round of k_cov_inv_part
 constexpr int kInvSplitMax = 32;      // ranges of rows m of one block row at most
+constexpr int kInvMinRows = 32;       // rows m per range at least
 constexpr int kGT = 64, kGK = 16;     // GEMM tile and depth
 
 // ---------------------------------------------------------------------------
@@ -1038,9 +1039,9 @@ int launch_cov_inverse(int n, const double* L, const double* ldiag, const double
     int nfin = 0;
     if (cols > 0) {
       nfin = static_cast<int>(blocks_for(cols, kCovThreads));
-      // split the rows m so that about two CTAs per SM run, each range at least kInvRows rows
+      // split the rows m so that about two CTAs per SM run, each range at least kInvMinRows rows
       int nk = (2 * num_sms + nfin - 1) / nfin;
-      nk = std::max(1, std::min({nk, kInvSplitMax, cols / kInvRows}));
+      nk = std::max(1, std::min({nk, kInvSplitMax, cols / kInvMinRows}));
       const int kchunk = (cols + nk - 1) / nk;
       k_cov_inv_part<<<dim3(nfin, nk), kCovThreads, 0, st>>>(n, i, kchunk, L, Z, part);
       k_cov_inv_fin<<<nfin, kCovThreads, 0, st>>>(n, i, nk, L, ldiag, Z, part, dpart);
