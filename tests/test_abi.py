@@ -143,3 +143,32 @@ def test_camera_options_validated_without_gpu(pkg):
     o.intrinsics_free = 2
     assert L.sgba_problem_create_ex(ctypes.byref(desc), ctypes.byref(o), 0, ctypes.byref(h)) == \
         pkg.native.ERR_INVALID_ARGUMENT
+
+
+def _c_enum_values(text):
+    """NAME = value pairs of the header's enums (comments removed)."""
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(SGBA_\w+)\s*=\s*(-?\d+)", text)}
+
+
+def test_enum_values_match_the_bindings(pkg):
+    """The status codes, variable kinds and query modes of include/sgba.h have
+    the same values in the Python and Rust bindings."""
+    header = _c_enum_values(open(os.path.join(ROOT, "include", "sgba.h")).read())
+    ffi = open(os.path.join(ROOT, "rust", "sgba-sys", "src", "ffi.rs")).read()
+    rust = {m.group(1): int(m.group(2)) for m in re.finditer(r"pub const (SGBA_\w+): \w+ = (-?\d+);", ffi)}
+    native = pkg.native
+    for name, value in header.items():
+        if name.startswith(("SGBA_ERR_", "SGBA_VAR_", "SGBA_QUERY_")):
+            assert rust.get(name) == value, (name, value, rust.get(name))
+            py = getattr(native, name[len("SGBA_"):], None)
+            assert py == value, (name, value, py)
+    assert header["SGBA_ERR_FACTORIZATION"] == -9 and header["SGBA_VAR_INTRINSICS"] == 0
+
+
+def test_covariance_arguments_checked_without_gpu(pkg):
+    """sgba_covariance_* reject a NULL problem on the host."""
+    L = pkg.native.lib()
+    assert L.sgba_covariance_prepare(None, None) == pkg.native.ERR_INVALID_ARGUMENT
+    assert L.sgba_covariance_release(None) == pkg.native.ERR_INVALID_ARGUMENT
+    assert L.sgba_covariance_blocks(None, 0, 0, None, None, None) == pkg.native.ERR_INVALID_ARGUMENT
