@@ -149,6 +149,7 @@ struct sgba_problem {
   size_t chunk_size = size_t(1) << 20;
   // covariance of the solution (sgba_covariance_prepare)
   sgba::CovBufs cov;
+  bool pairs_built = true;  // the Schur pair lists exist (not for the tiled pass of nearly dense systems)
 };
 
 namespace {
@@ -770,6 +771,15 @@ int build_schur_pattern(sgba_problem* p) {
   P.sb_pair_begin.assign(nb + 1, 0);
   for (int64_t b = 0; b < nb; ++b) P.sb_pair_begin[b + 1] = P.sb_pair_begin[b] + cnt[lid(P.sb_row[b], P.sb_col[b])];
   const int64_t npairs = P.sb_pair_begin[nb];
+  int st;
+  // Nearly dense systems of the pinhole camera with fixed params and no
+  // pose-graph edges take the tiled Schur pass (the selection in upload()),
+  // which reads the term table: their pair lists are not built (a window of
+  // 40 cameras and 4000 points has ~3M pairs).
+  const bool tiled = p->camera_model == SGBA_CAMERA_PINHOLE && !p->intr_free && P.eterm_fm.empty() &&
+                     10 * nb > 9 * nlow && 2 * P.ng >= static_cast<int64_t>(P.np) * nf;
+  p->pairs_built = !tiled;
+  if (tiled) return dev_alloc(p, &d.pairs, 0);
   if (npairs >= (int64_t(1) << 31))
     return set_error(SGBA_ERR_UNSUPPORTED, "%lld observation pairs exceed the 2^31 limit", (long long)npairs);
   // chunks of at most kSchurChunk pairs within one block (at least one per block)
@@ -784,7 +794,6 @@ int build_schur_pattern(sgba_problem* p) {
   }
   P.block_chunk_begin[nb] = static_cast<int32_t>(P.chunk_begin.size());
   P.chunk_begin.push_back(npairs);
-  int st;
   if ((st = dev_alloc(p, &d.pairs, static_cast<size_t>(npairs)))) return st;
   if (npairs == 0) return SGBA_OK;
   // point chunks: as many as keep the (chunk x block) table near 64 Mi entries
@@ -1078,6 +1087,8 @@ int upload(sgba_problem* p, const sgba_problem_desc* desc) {
                    2 * P.ng >= static_cast<int64_t>(P.np) * static_cast<int64_t>(P.nf))
                       ? 1
                       : 0;
+  if (!p->pairs_built && !s.schur_dense)
+    return set_error(SGBA_ERR_UNSUPPORTED, "internal: no Schur pair lists for a system that needs them");
   if (s.schur_dense) {
     if ((st = dev_alloc(p, &d.zterm, static_cast<size_t>(P.np) * static_cast<size_t>(P.nf)))) return st;
     SGBA_CK(sgba::zterm_fill(s, d, d.zterm, p->stream));
